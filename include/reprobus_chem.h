@@ -1,0 +1,167 @@
+/*
+ * reprobus_chem.h — C-ABI of the GB300 (sm_103a) REPROBUS chemistry step.
+ *
+ * The library libreprobus_gb300.so replaces the per-latitude chemistry loop of
+ * the REPROBUS time loop:
+ *
+ *     do ilat = 1,nlat
+ *        call chem3d(ilat, daynum, dt, alt, trajlon, trajlat, trajpre,
+ *                    trajtem, irapp, qj1, hc, vsed3d, parth2osed,
+ *                    parthno3sed, surfarea, sza3d)
+ *     end do                          ! src/reprobus_l137_20230723.f:398-415
+ *     call conserv(qj1, hc)           ! :427   (optional, REPROBUS_FUSE_CONSERV)
+ *     qj1(:,:,:,1:42) >= 1e-30        ! :431-440
+ *     qj1(:,:,nivbas+1:,43) = qj1(..,5) ! :444-450
+ *
+ * Conventions (all entry points):
+ *  - Arrays are FP64 in Fortran (column-major) layout, lon fastest, exactly
+ *    as the reference declares them: qj1(nlon,nlat,niv,43), hc(nlon,nlat,niv,15),
+ *    alt/surfarea(nlon,nlat,niv), traj*(nlon,nlat,niv,nrappmax),
+ *    vsed3d/parth2osed/parthno3sed/sza3d(nlon,nlat,nivbas).
+ *  - Indices that the Fortran caller passes (ilat, irapp) are 1-based.
+ *  - Plain pointers and sizes only; the caller owns every array.
+ *  - Return 0 on success, a REPROBUS_ERR_* code otherwise; the text of the
+ *    last error of the calling thread is in reprobus_last_error().
+ *  - A handle owns its device buffers and one CUDA stream. It is not
+ *    thread-safe: one host thread drives a handle at a time.
+ *  - No entry point falls back to the CPU: without a usable GPU the calls
+ *    return REPROBUS_ERR_NODEVICE / REPROBUS_ERR_CUDA.
+ */
+#ifndef REPROBUS_CHEM_H
+#define REPROBUS_CHEM_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+enum {
+    REPROBUS_OK = 0,
+    REPROBUS_ERR_ARG = 1,        /* null pointer, bad size, bad row/slice index   */
+    REPROBUS_ERR_CUDA = 2,       /* a CUDA runtime call failed                    */
+    REPROBUS_ERR_NONFINITE = 3,  /* NaN/Inf written by the step (see stats)       */
+    REPROBUS_ERR_NOCONV = 4,     /* solver: cells left unconverged (see stats)    */
+    REPROBUS_ERR_TIMEOUT = 5,    /* a bounded device-side wait gave up            */
+    REPROBUS_ERR_NODEVICE = 6    /* no CUDA device visible                        */
+};
+
+/* ---- handle flags --------------------------------------------------------- */
+#define REPROBUS_FUSE_CONSERV  0x1  /* also run conserv (:2526-2616), clamps and
+                                       the HNO3-gas copy (:431-450) in the call  */
+#define REPROBUS_CHECK_FINITE  0x2  /* count NaN/Inf in outputs, return
+                                       REPROBUS_ERR_NONFINITE when any           */
+
+/* ---- per-call statistics --------------------------------------------------- */
+typedef struct reprobus_stats {
+    long long ncells;          /* cells integrated by the call (rows x nlon x nivbas) */
+    long long nonfinite;       /* NaN/Inf values produced (REPROBUS_CHECK_FINITE)     */
+    int kernel_launches;       /* kernels this call launched                          */
+    int passes;                /* fixed-point passes per cell (niter)                  */
+    double device_ms;          /* device time of the call's kernels (CUDA events)      */
+} reprobus_stats;
+
+/* ---- diagnostics layout (reprobus_chem_rates_*) ----------------------------
+ * Per chemistry cell, REPROBUS_DIAG_COUNT doubles, stored structure-of-arrays:
+ * diag[d * ncell + cell], cell = ilon-1 + nlon*((ilat-ilat0) + nrows*(iniv-1)).
+ * The 99 rate constants follow the order of src/reprobus_l137_20230723.f:930-1303
+ * (a1 a1et a2 a5 a6 a6b a7 a17 a19 a26 a27 a30 a31 a36 | b3 b4 b6 b7 b9 b12 b22
+ *  b23 b24 b27 b28 b32 b38 b39 | c1a c1b c1c c2 c3 c4 c5 c7 c8 c9 c10 c12 c14
+ *  c15 c17a c17b c18 c19 | d2 d3 d4 d5 d6 d7 d8 d9 d10 d11 d31 d32 d33 d34 d35
+ *  d36 d37 d60 d61 d62 d90 d91 d92 d93 d94 d95 d96 d97 | e2 e3 e4 e5a e5b e5c e6
+ *  e7 e8 e9 e10 e11 e13 e15 e16 e50 e51 e52 e53 e54 | hk1 hk2 hk3 hk4 hk5). */
+enum {
+    REPROBUS_DIAG_HNM = 0,
+    REPROBUS_DIAG_SZA = 1,
+    REPROBUS_DIAG_O3T = 2,
+    REPROBUS_DIAG_TJ = 3,            /* 41 photolysis rates, :754-794 order     */
+    REPROBUS_DIAG_HET = 44,          /* het1..het9                              */
+    REPROBUS_DIAG_PARTHNO3 = 53,
+    REPROBUS_DIAG_PARTHNO3SL = 54,
+    REPROBUS_DIAG_PARTH2O = 55,
+    REPROBUS_DIAG_PARTHCL = 56,
+    REPROBUS_DIAG_VSED = 57,
+    REPROBUS_DIAG_SURFAREA = 58,     /* levels nivhau..nivbas, else 0            */
+    REPROBUS_DIAG_RATE = 59,         /* 99 thermal rate constants               */
+    REPROBUS_DIAG_COUNT = 158
+};
+#define REPROBUS_NRATE 99
+#define REPROBUS_NBCON 43           /* transported slots qj1(...,43)            */
+#define REPROBUS_NCM 15             /* steady-state slots hc(...,15)            */
+#define REPROBUS_NPHOT 41
+#define REPROBUS_NZ 101
+#define REPROBUS_NSZA 27
+#define REPROBUS_NOZO 7
+#define REPROBUS_NTROE 18
+
+/* Library version string. */
+const char* reprobus_version(void);
+
+/* Text of the last error raised on the calling thread ("" if none). */
+const char* reprobus_last_error(void);
+
+/* Fills troe[18] with the fall-off prefactors of COMMON /constant/ in COMMON
+ * order (a0hox a1hox a0nox1 a1nox1 a0nox2 a1nox2 a0nox3 a1nox3 a0clx1 a1clx1
+ * a0clx2 a1clx2 a0clx3 a1clx3 a0brx a1brx a0c1 a1c1).
+ * Replaces: subroutine const, src/reprobus_l137_20230723.f:5927-5948.
+ * Host-only arithmetic; needs no GPU. */
+int reprobus_chem_troe(double* troe);
+
+/* Creates a handle: uploads the photolysis table ajl(40,101,27,7) (Fortran
+ * order) and o3up(0:79) of COMMON /photodis/, and the 18 Troe prefactors of
+ * COMMON /constant/; sizes the device buffers for the grid.
+ * Replaces: call const(relief), :294, i.e. the COMMON blocks filled at
+ * :5927-5973 and declared at :46-52.
+ * nivbas: last chemistry level (reference: 94); nivhau: first PSC/aerosol
+ * level (reference: 14); niter: fixed-point passes (reference: 5, :630). */
+int reprobus_chem_init(const double* ajl, const double* o3up, const double* troe,
+                       int nlon, int nlat, int niv, int nivbas, int nivhau,
+                       int nrappmax, int niter, int flags, void** handle);
+
+/* Releases the handle and its device memory. */
+int reprobus_chem_free(void* handle);
+
+/* Makes the handle launch on the caller's CUDA stream (a cudaStream_t passed
+ * as void*; NULL restores the handle's own stream). */
+int reprobus_chem_set_stream(void* handle, void* cuda_stream);
+
+/* One 15-min chemistry step for latitude rows ilat0..ilat1 (1-based,
+ * inclusive), HOST arrays: copies the rows in, integrates, copies them back.
+ * Replaces: do ilat = ilat0,ilat1 / call chem3d(...) (:398-415, chem3d at
+ * :601-2412); with REPROBUS_FUSE_CONSERV also conserv (:427, :2526-2616) and
+ * the clamps (:431-450) on those rows. Writes qj1/hc (levels 1..nivbas; with
+ * the flag also the clamps on all levels), vsed3d, parth2osed, parthno3sed,
+ * sza3d (levels 1..nivbas) and surfarea (levels nivhau..nivbas). */
+int reprobus_chem_step(void* handle, int ilat0, int ilat1, double daynum, double dt,
+                       const double* alt, const double* trajlon, const double* trajlat,
+                       const double* trajpre, const double* trajtem, int irapp,
+                       double* qj1, double* hc, double* vsed3d, double* parth2osed,
+                       double* parthno3sed, double* surfarea, double* sza3d,
+                       reprobus_stats* stats);
+
+/* Same step on DEVICE arrays (full-grid Fortran layout, already resident in
+ * HBM): no host<->device copies. Same replacement as reprobus_chem_step. */
+int reprobus_chem_step_dev(void* handle, int ilat0, int ilat1, double daynum, double dt,
+                           const double* alt, const double* trajlon, const double* trajlat,
+                           const double* trajpre, const double* trajtem, int irapp,
+                           double* qj1, double* hc, double* vsed3d, double* parth2osed,
+                           double* parthno3sed, double* surfarea, double* sza3d,
+                           reprobus_stats* stats);
+
+/* Rate stage only (setup :800-833, total, zenith, phot+jno, analytic+hetero,
+ * rate constants :920-1306) on DEVICE arrays; writes the per-cell
+ * diagnostics (REPROBUS_DIAG_* layout) to diag. Does not modify the state.
+ * Replaces: the part of chem3d before its iteration loop (:800-1338). */
+int reprobus_chem_rates_dev(void* handle, int ilat0, int ilat1, double daynum,
+                            const double* alt, const double* trajlon, const double* trajlat,
+                            const double* trajpre, const double* trajtem, int irapp,
+                            const double* qj1, const double* hc, double* diag);
+
+/* Element conservation + clamps on DEVICE arrays, rows ilat0..ilat1.
+ * Replaces: call conserv(qj1, hc) (:427, :2526-2616) and the loops at
+ * :431-450. */
+int reprobus_conserv_dev(void* handle, int ilat0, int ilat1, double* qj1, double* hc);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* REPROBUS_CHEM_H */

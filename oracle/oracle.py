@@ -1,0 +1,116 @@
+"""ctypes front end of the CPU FP64 oracle (chem_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, always as the checker, never as the measured or
+shipped path. PARITY UNPINNED: see chem_oracle.c.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+SRC = os.path.join(HERE, "chem_oracle.c")
+
+CFLAGS = ["-O3", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared"]
+
+
+def build(force: bool = False) -> str:
+    """Compiles the oracle with gcc (IEEE, no FMA contraction, OpenMP)."""
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        cmd = ["gcc", *CFLAGS, "-o", LIB, SRC, "-lm"]
+        subprocess.run(cmd, check=True)
+    return LIB
+
+
+class OrcGrid(ctypes.Structure):
+    _fields_ = [
+        ("nlon", ctypes.c_int), ("nlat", ctypes.c_int), ("niv", ctypes.c_int),
+        ("nivbas", ctypes.c_int), ("nivhau", ctypes.c_int), ("nrappmax", ctypes.c_int),
+        ("niter", ctypes.c_int), ("tol", ctypes.c_double), ("maxiter", ctypes.c_int),
+        ("ajl", ctypes.POINTER(ctypes.c_double)), ("o3up", ctypes.POINTER(ctypes.c_double)),
+        ("troe", ctypes.c_double * 18),
+    ]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(LIB)
+        dp = ctypes.POINTER(ctypes.c_double)
+        _lib.orc_step.restype = ctypes.c_int
+        _lib.orc_step.argtypes = [ctypes.POINTER(OrcGrid), ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                  ctypes.c_double, dp, dp, dp, dp, dp, ctypes.c_int, dp, dp, dp, dp, dp, dp,
+                                  dp, ctypes.c_int, dp, ctypes.c_int]
+        _lib.orc_const.argtypes = [dp]
+        _lib.orc_conserv.argtypes = [ctypes.POINTER(OrcGrid), ctypes.c_int, ctypes.c_int, dp, dp]
+        _lib.orc_clamp.argtypes = [ctypes.POINTER(OrcGrid), ctypes.c_int, ctypes.c_int, dp]
+    return _lib
+
+
+def _p(a):
+    assert a.dtype == np.float64
+    assert a.flags.f_contiguous or a.ndim == 1
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def troe():
+    out = np.zeros(18)
+    lib().orc_const(_p(out))
+    return out
+
+
+def grid(case, niter=5, tol=0.0, maxiter=0, troe_vals=None):
+    g = OrcGrid()
+    g.nlon, g.nlat, g.niv = case.nlon, case.nlat, case.niv
+    g.nivbas, g.nivhau, g.nrappmax = case.nivbas, case.nivhau, case.nrappmax
+    g.niter, g.tol, g.maxiter = niter, tol, maxiter
+    g.ajl = _p(case.ajl)
+    g.o3up = _p(case.o3up)
+    tv = case.troe if troe_vals is None else troe_vals
+    for i in range(18):
+        g.troe[i] = float(tv[i])
+    return g
+
+
+def step(case, niter=5, fuse=True, diag=False, nthreads=0, ilat0=1, ilat1=None, tol=0.0, maxiter=0,
+         state=None):
+    """Runs the chemistry block of the time loop on copies of the case state
+    (or on `state`, a dict as returned by case.state_copy(), in place).
+    ilat0/ilat1 are 1-based inclusive rows. Returns (state, diag or None, passes)."""
+    L = lib()
+    g = grid(case, niter=niter, tol=tol, maxiter=maxiter)
+    st = case.state_copy() if state is None else state
+    ilat1 = case.nlat if ilat1 is None else ilat1
+    dg = None
+    if diag:
+        from reprobus_gb300.species import DIAG_COUNT
+        dg = np.zeros(DIAG_COUNT * case.nlon * case.nlat * case.nivbas)
+    passes = L.orc_step(ctypes.byref(g), ilat0 - 1, ilat1 - 1, case.daynum, case.dt, _p(case.alt),
+                        _p(case.trajlon), _p(case.trajlat), _p(case.trajpre), _p(case.trajtem),
+                        case.irapp - 1, _p(st["qj1"]), _p(st["hc"]), _p(st["vsed3d"]), _p(st["parth2osed"]),
+                        _p(st["parthno3sed"]), _p(st["surfarea"]), _p(st["sza3d"]), int(bool(fuse)),
+                        _p(dg) if dg is not None else None, nthreads)
+    if dg is not None:
+        dg = dg.reshape(DIAG_COUNT, case.nlon * case.nlat * case.nivbas)
+    return st, dg, passes
+
+
+def conserv(case, qj1, hc, ilat0=1, ilat1=None):
+    g = grid(case)
+    ilat1 = case.nlat if ilat1 is None else ilat1
+    lib().orc_conserv(ctypes.byref(g), ilat0 - 1, ilat1 - 1, _p(qj1), _p(hc))
+
+
+def clamp(case, qj1, ilat0=1, ilat1=None):
+    g = grid(case)
+    ilat1 = case.nlat if ilat1 is None else ilat1
+    lib().orc_clamp(ctypes.byref(g), ilat0 - 1, ilat1 - 1, _p(qj1))

@@ -1,0 +1,708 @@
+// chem_kernels.cu — GB300 (sm_103a) kernels and C-ABI of the REPROBUS
+// chemistry step (include/reprobus_chem.h).
+//
+// Launch structure of one step (rows ilat0..ilat1, levels 1..nivbas):
+//   k_columns  one thread per column: the vertical prefix sums of total
+//              (F:5153-5186) and jno (JNO:107-126) and the level-1 zenith
+//              angle (JNO:139) -> column scratch (3 doubles per cell + 1 per
+//              column)
+//   k_chem     one thread per cell: setup, zenith, phot+jno, analytic+hetero,
+//              rate constants, rainout, the niter fixed-point passes,
+//              write-back and (fused) conserv + clamps  (F:800-2410, 2526-2616)
+//   k_tail     (fused, nivbas < niv) clamps and HNO3-gas copy of the levels
+//              below the chemistry (F:431-450)
+// All arrays keep the reference's Fortran layout, lon fastest, so a warp's
+// loads of one species plane are coalesced.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "../../include/reprobus_chem.h"
+#include "chem_cell.cuh"
+
+using namespace rpb;
+
+// ----------------------------------------------------------------------------
+// error reporting
+// ----------------------------------------------------------------------------
+static thread_local char g_err[512] = "";
+
+static int set_err(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define CUDA_TRY(x)                                                                                          \
+    do {                                                                                                     \
+        cudaError_t e_ = (x);                                                                                \
+        if (e_ != cudaSuccess) return set_err(REPROBUS_ERR_CUDA, "%s: %s (%s:%d)", #x, cudaGetErrorString(e_), \
+                                              __FILE__, __LINE__);                                           \
+    } while (0)
+
+// ----------------------------------------------------------------------------
+// kernel parameters
+// ----------------------------------------------------------------------------
+struct Params {
+    int nlon, nlat, niv, nivbas, nivhau;
+    int ilat0, nrows;          // 0-based first row, number of rows
+    long long trajoff;         // element offset of the irapp slice in traj*
+    int niter, fuse, check;
+    int ncell, ncol;           // nlon*nrows*nivbas, nlon*nrows
+    const double* __restrict__ alt;
+    const double* __restrict__ trajlon;
+    const double* __restrict__ trajlat;
+    const double* __restrict__ trajpre;
+    const double* __restrict__ trajtem;
+    double* qj1;
+    double* hc;
+    double* vsed3d;
+    double* parth2osed;
+    double* parthno3sed;
+    double* surfarea;
+    double* sza3d;
+    const double* __restrict__ ajl;
+    const double* __restrict__ o3up;
+    double* col;               // scratch: o3t | colo2 | colno (ncell each) | sza_top (ncol)
+    unsigned long long* nonfinite;
+    double* diag;
+    StepConst sc;
+};
+
+__device__ __forceinline__ size_t plane3(const Params& P) { return (size_t)P.nlon * P.nlat * P.niv; }
+__device__ __forceinline__ size_t plane_b(const Params& P) { return (size_t)P.nlon * P.nlat * P.nivbas; }
+
+// ----------------------------------------------------------------------------
+// k_columns — vertical prefix sums, total F:5172-5184 and jno JNO:109-126
+// ----------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_columns(Params P) {
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= P.ncol) return;
+    const int i = col % P.nlon;
+    const int j = P.ilat0 + col / P.nlon;
+    const size_t pl = plane3(P);
+    const double zcmt = 2.120e20;                      // total
+    const double zcmt2 = 287.0 / (1.38e-23 * 9.81);    // jno
+    const double r_o2 = 0.2095;
+    double* o3t = P.col;
+    double* colo2 = P.col + P.ncell;
+    double* colno = P.col + 2 * (size_t)P.ncell;
+    double* sza_top = P.col + 3 * (size_t)P.ncell;
+    // level 1
+    size_t g = (size_t)i + (size_t)P.nlon * j;
+    double p_prev = P.trajpre[P.trajoff + g];
+    double hnm_prev = p_prev / (P.trajtem[P.trajoff + g] * 1.38e-19);
+    double o3_prev = P.hc[g + pl * 4];
+    double no_prev = P.hc[g + pl * 7] * hnm_prev;  // cc(:,:,8) = hc*hnm
+    double a_o3 = o3_prev * hnm_prev * 6.8e5;
+    double a_o2 = 6.8e+05 * r_o2 * hnm_prev;
+    double a_no = 6.8e+05 * no_prev;
+    o3t[col] = a_o3;
+    colo2[col] = a_o2;
+    colno[col] = a_no;
+    sza_top[col] = cell_zenith(P.sc, P.trajlon[P.trajoff + g], P.trajlat[P.trajoff + g]);
+    for (int k = 1; k < P.nivbas; k++) {
+        g += (size_t)P.nlon * P.nlat;
+        double p = P.trajpre[P.trajoff + g];
+        double hnm = p / (P.trajtem[P.trajoff + g] * 1.38e-19);
+        double o3 = P.hc[g + pl * 4];
+        double no = P.hc[g + pl * 7] * hnm;
+        double dp = (p - p_prev) * 100.;
+        dp = fmax(dp, 0.);
+        a_o3 = a_o3 + zcmt * (o3 + o3_prev) * .5 * dp;
+        a_o2 = a_o2 + zcmt2 * (r_o2 + r_o2) * 0.5 * dp * 1.e-4;
+        a_no = a_no + zcmt2 * (no_prev / hnm_prev + no / hnm) * 0.5 * dp * 1.e-4;
+        const size_t c = (size_t)col + (size_t)P.ncol * k;
+        o3t[c] = a_o3;
+        colo2[c] = a_o2;
+        colno[c] = a_no;
+        p_prev = p;
+        hnm_prev = hnm;
+        o3_prev = o3;
+        no_prev = no;
+    }
+}
+
+// ----------------------------------------------------------------------------
+// k_chem — one cell per thread. DIAG: rate stage only, diagnostics out.
+// ----------------------------------------------------------------------------
+template <bool DIAG>
+__global__ void __launch_bounds__(128) k_chem(Params P) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= P.ncell) return;
+    const int i = cell % P.nlon;
+    const int rest = cell / P.nlon;
+    const int col = cell % P.ncol;
+    const int k = rest / P.nrows;
+    const int j = P.ilat0 + rest % P.nrows;
+    const size_t g = (size_t)i + (size_t)P.nlon * ((size_t)j + (size_t)P.nlat * k);
+    const size_t gb = g;  // (nlon,nlat,nivbas) arrays share the index for k < nivbas
+    const size_t pl = plane3(P);
+
+    // ---- setup F:800-833 ----
+    CellFix F;
+    const double t = P.trajtem[P.trajoff + g];
+    const double pm = P.trajpre[P.trajoff + g];
+    F.hnm = P.trajpre[P.trajoff + g] / (P.trajtem[P.trajoff + g] * 1.38e-19);
+    F.n2 = 0.78 * F.hnm;
+    F.o2 = 0.21 * F.hnm;
+    F.co2 = 360.e-6 * F.hnm;
+    F.h2 = 5.e-7 * F.hnm;
+    double ck0[NBCON], ck[NBCON], cc[NCM];
+#pragma unroll
+    for (int n = 0; n < NBCON; n++) {
+        ck0[n] = P.qj1[g + pl * n] * F.hnm;
+        ck[n] = ck0[n];
+    }
+#pragma unroll
+    for (int n = 0; n < NCM; n++) cc[n] = P.hc[g + pl * n] * F.hnm;
+
+    // ---- zenith F:845-851 ----
+    F.sza = cell_zenith(P.sc, P.trajlon[P.trajoff + g], P.trajlat[P.trajoff + g]);
+    if (!DIAG) P.sza3d[gb] = F.sza;
+
+    // ---- phot + jno F:857, F:5043-5146 ----
+    double tj[NPHOT];
+#pragma unroll
+    for (int n = 0; n < NPHOT; n++) tj[n] = 0.;
+    const double o3t = P.col[cell];
+    if (F.sza <= 95.) cell_phot(P.ajl, P.o3up, P.alt[g], F.sza, o3t, tj);
+    const double sza_top = P.col[3 * (size_t)P.ncell + col];
+    if (sza_top <= 89.0)
+        tj[J_no] = cell_jno(sza_top, F.hnm, P.col[(size_t)P.ncell + cell], P.col[2 * (size_t)P.ncell + cell], o3t);
+
+    // ---- heterogeneous init + analytic F:864-912 ----
+    Aerosol A;
+#pragma unroll
+    for (int m = 0; m < 9; m++) A.het[m] = 0.;
+    A.parthno3 = 1.;
+    A.parthno3sl = 1.;
+    A.parth2o = 1.;
+    A.parthcl = 1.;
+    A.vsed = 0.;
+    A.surf = 0.;
+    if (k >= P.nivhau - 1) {
+        cell_aerosol(t, pm, F.hnm, ck, A);
+        if (!DIAG) P.surfarea[g] = A.surf;
+    }
+    F.parthno3 = A.parthno3;
+    F.parth2o = A.parth2o;
+    F.parthcl = A.parthcl;
+    F.parthbr = 1.;
+    if (!DIAG) {
+        P.vsed3d[gb] = A.vsed;
+        P.parth2osed[gb] = A.parth2o;
+        P.parthno3sed[gb] = A.parthno3sl;
+    }
+
+    // ---- rate constants F:920-1306 ----
+    double K[NRATE];
+    cell_rates(P.sc.troe, t, F.hnm, pm, K);
+
+    if (DIAG) {
+        const size_t nc = (size_t)P.ncell;
+        double* d = P.diag + cell;
+        d[REPROBUS_DIAG_HNM * nc] = F.hnm;
+        d[REPROBUS_DIAG_SZA * nc] = F.sza;
+        d[REPROBUS_DIAG_O3T * nc] = o3t;
+#pragma unroll
+        for (int n = 0; n < NPHOT; n++) d[(REPROBUS_DIAG_TJ + n) * nc] = tj[n];
+#pragma unroll
+        for (int m = 0; m < 9; m++) d[(REPROBUS_DIAG_HET + m) * nc] = A.het[m];
+        d[REPROBUS_DIAG_PARTHNO3 * nc] = A.parthno3;
+        d[REPROBUS_DIAG_PARTHNO3SL * nc] = A.parthno3sl;
+        d[REPROBUS_DIAG_PARTH2O * nc] = A.parth2o;
+        d[REPROBUS_DIAG_PARTHCL * nc] = A.parthcl;
+        d[REPROBUS_DIAG_VSED * nc] = A.vsed;
+        d[REPROBUS_DIAG_SURFAREA * nc] = A.surf;
+#pragma unroll
+        for (int n = 0; n < NRATE; n++) d[(REPROBUS_DIAG_RATE + n) * nc] = K[n];
+        return;
+    }
+
+    // ---- rainout F:1315-1338 ----
+    const double rain_rate = 1.e-6;
+    const bool rain = ck[2] / F.hnm >= 100.e-6;
+    F.rain_hno3 = rain ? rain_rate : 0.;
+    F.rain_hno4 = 0.;
+    F.rain_hcl = rain ? rain_rate : 0.;
+    F.rain_hbr = rain ? rain_rate : 0.;
+    F.rain_h2o2 = rain ? rain_rate : 0.;
+    F.rain_ch2o = 0.;
+    F.rain_ch3o2h = 0.;
+
+    // ---- fixed-point passes F:1348-2378 ----
+#pragma unroll 1
+    for (int it = 0; it < P.niter; it++) cell_pass(F, K, tj, A.het, ck0, P.sc.dt, ck, cc);
+
+    // ---- write-back F:2380-2410 ----
+    double q[NBCON], h[NCM];
+#pragma unroll
+    for (int n = 0; n < NBCON - 1; n++) q[n] = ck[n] / F.hnm;
+    q[NBCON - 1] = ck[4] * F.parthno3 / F.hnm;
+#pragma unroll
+    for (int n = 0; n < NCM; n++) h[n] = cc[n] / F.hnm;
+    if (P.fuse) {
+        // conserv F:2539-2613 reads the 43 written-back slots
+        cell_conserv(q, h);
+    }
+    if (P.check) {
+        unsigned int bad = 0;
+#pragma unroll
+        for (int n = 0; n < NBCON; n++) bad += !isfinite(q[n]);
+#pragma unroll
+        for (int n = 0; n < NCM; n++) bad += !isfinite(h[n]);
+        if (bad) atomicAdd(P.nonfinite, (unsigned long long)bad);
+    }
+    if (P.fuse) {
+        // clamps F:431-440
+#pragma unroll
+        for (int n = 0; n < NBCON - 1; n++) q[n] = fmax(q[n], 1.e-30);
+    }
+#pragma unroll
+    for (int n = 0; n < NBCON; n++) P.qj1[g + pl * n] = q[n];
+#pragma unroll
+    for (int n = 0; n < NCM; n++) P.hc[g + pl * n] = h[n];
+}
+
+// ----------------------------------------------------------------------------
+// k_tail — levels nivbas+1..niv of the rows: clamps F:431-440, HNO3 gas F:444-450
+// ----------------------------------------------------------------------------
+__global__ void k_tail(Params P) {
+    const long long n = (long long)P.nlon * P.nrows * (P.niv - P.nivbas);
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n) return;
+    const int i = (int)(idx % P.nlon);
+    const long long rest = idx / P.nlon;
+    const int j = P.ilat0 + (int)(rest % P.nrows);
+    const int k = P.nivbas + (int)(rest / P.nrows);
+    const size_t g = (size_t)i + (size_t)P.nlon * ((size_t)j + (size_t)P.nlat * k);
+    const size_t pl = plane3(P);
+#pragma unroll 6
+    for (int s = 0; s < NBCON - 1; s++) P.qj1[g + pl * s] = fmax(P.qj1[g + pl * s], 1.e-30);
+    P.qj1[g + pl * (NBCON - 1)] = P.qj1[g + pl * 4];
+}
+
+// ----------------------------------------------------------------------------
+// k_conserv — standalone conserv + clamps on rows, all levels
+// ----------------------------------------------------------------------------
+__global__ void k_conserv(Params P) {
+    const long long n = (long long)P.nlon * P.nrows * P.niv;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n) return;
+    const int i = (int)(idx % P.nlon);
+    const long long rest = idx / P.nlon;
+    const int j = P.ilat0 + (int)(rest % P.nrows);
+    const int k = (int)(rest / P.nrows);
+    const size_t g = (size_t)i + (size_t)P.nlon * ((size_t)j + (size_t)P.nlat * k);
+    const size_t pl = plane3(P);
+    double q[NBCON], h[NCM];
+#pragma unroll
+    for (int s = 0; s < NBCON; s++) q[s] = P.qj1[g + pl * s];
+    if (k < P.nivbas) {
+#pragma unroll
+        for (int s = 0; s < NCM; s++) h[s] = P.hc[g + pl * s];
+        cell_conserv(q, h);
+#pragma unroll
+        for (int s = 0; s < NCM; s++) P.hc[g + pl * s] = h[s];
+    }
+#pragma unroll
+    for (int s = 0; s < NBCON - 1; s++) q[s] = fmax(q[s], 1.e-30);
+    if (k >= P.nivbas) q[NBCON - 1] = q[4];
+#pragma unroll
+    for (int s = 0; s < NBCON; s++) P.qj1[g + pl * s] = q[s];
+}
+
+// ----------------------------------------------------------------------------
+// handle
+// ----------------------------------------------------------------------------
+struct Handle {
+    int nlon, nlat, niv, nivbas, nivhau, nrappmax, niter, flags;
+    int device;
+    double troe[18];
+    double* d_ajl = nullptr;
+    double* d_o3up = nullptr;
+    double* d_col = nullptr;
+    unsigned long long* d_count = nullptr;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // device mirrors for the host-pointer entry point (allocated on first use)
+    double* m_alt = nullptr;
+    double* m_traj[4] = {nullptr, nullptr, nullptr, nullptr};
+    double* m_qj1 = nullptr;
+    double* m_hc = nullptr;
+    double* m_out[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // vsed, parth2o, parthno3, sza3d, surfarea
+};
+
+static const char* kVersion = "reprobus_gb300 0.1 (sm_103a, FP64 reference scheme)";
+
+extern "C" const char* reprobus_version(void) { return kVersion; }
+extern "C" const char* reprobus_last_error(void) { return g_err; }
+
+extern "C" int reprobus_chem_troe(double* troe) {
+    if (!troe) return set_err(REPROBUS_ERR_ARG, "troe is NULL");
+    troe[0] = 4.4e-32 * pow(300., 1.3);
+    troe[1] = 7.5e-11 * pow(300., -0.2);
+    troe[2] = 2.0e-30 * pow(300., 4.4);
+    troe[3] = 1.4e-12 * pow(300., 0.7);
+    troe[4] = 1.8e-30 * pow(300., 3.0);
+    troe[5] = 2.8e-11 * pow(300., 0.0);
+    troe[6] = 2.0e-31 * pow(300., 3.4);
+    troe[7] = 2.9e-12 * pow(300., 1.1);
+    troe[8] = 1.8e-31 * pow(300., 3.4);
+    troe[9] = 1.5e-11 * pow(300., 1.9);
+    troe[10] = 1.8e-31 * pow(300., 2.0);
+    troe[11] = 1.0e-10 * pow(300., 1.0);
+    troe[12] = 1.6e-32 * pow(300., 4.5);
+    troe[13] = 3.0e-12 * pow(300., 2.0);
+    troe[14] = 5.2e-31 * pow(300., 3.2);
+    troe[15] = 6.9e-12 * pow(300., 2.9);
+    troe[16] = 4.0e-31 * pow(300., 3.6);
+    troe[17] = 1.2e-12 * pow(300., -1.1);
+    return REPROBUS_OK;
+}
+
+static void free_handle(Handle* h) {
+    if (!h) return;
+    cudaFree(h->d_ajl);
+    cudaFree(h->d_o3up);
+    cudaFree(h->d_col);
+    cudaFree(h->d_count);
+    cudaFree(h->m_alt);
+    for (auto& p : h->m_traj) cudaFree(p);
+    cudaFree(h->m_qj1);
+    cudaFree(h->m_hc);
+    for (auto& p : h->m_out) cudaFree(p);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->own) cudaStreamDestroy(h->own);
+    delete h;
+}
+
+extern "C" int reprobus_chem_init(const double* ajl, const double* o3up, const double* troe, int nlon, int nlat,
+                                  int niv, int nivbas, int nivhau, int nrappmax, int niter, int flags,
+                                  void** handle) {
+    if (!handle) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
+    *handle = nullptr;
+    if (!ajl || !o3up || !troe) return set_err(REPROBUS_ERR_ARG, "ajl, o3up and troe must be non-NULL");
+    if (nlon <= 0 || nlat <= 0 || niv <= 0 || nivbas <= 0 || nivbas > niv || nivhau < 1 || nivhau > nivbas ||
+        nrappmax <= 0 || niter < 0)
+        return set_err(REPROBUS_ERR_ARG, "bad sizes: nlon=%d nlat=%d niv=%d nivbas=%d nivhau=%d nrappmax=%d niter=%d",
+                       nlon, nlat, niv, nivbas, nivhau, nrappmax, niter);
+    if ((long long)nlon * nlat * nivbas >= (1LL << 30))
+        return set_err(REPROBUS_ERR_ARG, "grid too large for 32-bit cell indexing");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return set_err(REPROBUS_ERR_NODEVICE, "no CUDA device visible");
+    Handle* h = new (std::nothrow) Handle();
+    if (!h) return set_err(REPROBUS_ERR_ARG, "out of host memory");
+    h->nlon = nlon;
+    h->nlat = nlat;
+    h->niv = niv;
+    h->nivbas = nivbas;
+    h->nivhau = nivhau;
+    h->nrappmax = nrappmax;
+    h->niter = niter;
+    h->flags = flags;
+    memcpy(h->troe, troe, sizeof(h->troe));
+    int rc = REPROBUS_OK;
+    auto fail = [&](int code) {
+        free_handle(h);
+        return code;
+    };
+    cudaError_t e;
+    if ((e = cudaGetDevice(&h->device)) != cudaSuccess) return fail(set_err(REPROBUS_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e)));
+    const size_t najl = (size_t)(NPHOT - 1) * NZ * NSZA * NOZO;
+    const size_t ncell = (size_t)nlon * nlat * nivbas;
+    const size_t ncol = (size_t)nlon * nlat;
+    if ((e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreate(&h->ev0)) != cudaSuccess || (e = cudaEventCreate(&h->ev1)) != cudaSuccess ||
+        (e = cudaMalloc(&h->d_ajl, najl * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&h->d_o3up, 80 * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&h->d_col, (3 * ncell + ncol) * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&h->d_count, sizeof(unsigned long long))) != cudaSuccess ||
+        (e = cudaMemcpy(h->d_ajl, ajl, najl * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(h->d_o3up, o3up, 80 * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return fail(set_err(REPROBUS_ERR_CUDA, "init: %s", cudaGetErrorString(e)));
+    h->stream = h->own;
+    (void)rc;
+    *handle = h;
+    return REPROBUS_OK;
+}
+
+extern "C" int reprobus_chem_free(void* handle) {
+    free_handle((Handle*)handle);
+    return REPROBUS_OK;
+}
+
+extern "C" int reprobus_chem_set_stream(void* handle, void* stream) {
+    Handle* h = (Handle*)handle;
+    if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
+    h->stream = stream ? (cudaStream_t)stream : h->own;
+    return REPROBUS_OK;
+}
+
+// per-step zenith constants, zenith F:5338-5380 (host, once per call)
+static void step_const(const Handle* h, double day, double dt, StepConst& sc) {
+    const double pi = PI;
+    double ut = (day - trunc(day)) * 24.;
+    double tz = 2. * pi * day / 365.;
+    double sintz = sin(tz);
+    double costz = cos(tz);
+    double sin2tz = 2. * sintz * costz;
+    double cos2tz = costz * costz - sintz * sintz;
+    double sin3tz = sintz * cos2tz + costz * sin2tz;
+    double cos3tz = costz * cos2tz - sintz * sin2tz;
+    double rdecl = 0.006918 - 0.399912 * costz + 0.070257 * sintz - 0.006758 * cos2tz + 0.000907 * sin2tz -
+                   0.002697 * cos3tz + 0.001480 * sin3tz;
+    double eqr = 0.000075 + 0.001868 * costz - 0.032077 * sintz - 0.014615 * cos2tz - 0.040849 * sin2tz;
+    sc.ut = ut;
+    sc.eqh = eqr * 24. / (2. * pi);
+    sc.srd = sin(rdecl);
+    sc.crd = cos(rdecl);
+    sc.dt = dt;
+    memcpy(sc.troe, h->troe, sizeof(sc.troe));
+}
+
+static int check_rows(const Handle* h, int ilat0, int ilat1) {
+    if (ilat0 < 1 || ilat1 > h->nlat || ilat0 > ilat1)
+        return set_err(REPROBUS_ERR_ARG, "bad row range %d..%d (nlat=%d)", ilat0, ilat1, h->nlat);
+    return REPROBUS_OK;
+}
+
+static void fill_params(const Handle* h, Params& P, int ilat0, int ilat1) {
+    memset(&P, 0, sizeof(P));
+    P.nlon = h->nlon;
+    P.nlat = h->nlat;
+    P.niv = h->niv;
+    P.nivbas = h->nivbas;
+    P.nivhau = h->nivhau;
+    P.ilat0 = ilat0 - 1;
+    P.nrows = ilat1 - ilat0 + 1;
+    P.niter = h->niter;
+    P.ncol = h->nlon * P.nrows;
+    P.ncell = P.ncol * h->nivbas;
+    P.ajl = h->d_ajl;
+    P.o3up = h->d_o3up;
+    P.col = h->d_col;
+    P.nonfinite = h->d_count;
+}
+
+// enqueue the kernels of one step on h->stream (device arrays in P)
+static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
+    const int tb = 128;
+    int launches = 0;
+    P.fuse = (h->flags & REPROBUS_FUSE_CONSERV) ? 1 : 0;
+    P.check = (h->flags & REPROBUS_CHECK_FINITE) ? 1 : 0;
+    if (P.check) CUDA_TRY(cudaMemsetAsync(h->d_count, 0, sizeof(unsigned long long), h->stream));
+    if (st) CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+    k_columns<<<(P.ncol + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    launches++;
+    k_chem<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    launches++;
+    if (P.fuse && h->nivbas < h->niv) {
+        long long nt = (long long)P.nlon * P.nrows * (h->niv - h->nivbas);
+        k_tail<<<(unsigned)((nt + 255) / 256), 256, 0, h->stream>>>(P);
+        launches++;
+    }
+    CUDA_TRY(cudaGetLastError());
+    if (st) {
+        CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
+        CUDA_TRY(cudaEventSynchronize(h->ev1));
+        float ms = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+        st->device_ms = ms;
+        st->ncells = P.ncell;
+        st->kernel_launches = launches;
+        st->passes = h->niter;
+        st->nonfinite = 0;
+    }
+    if (P.check) {
+        unsigned long long bad = 0;
+        CUDA_TRY(cudaMemcpyAsync(&bad, h->d_count, sizeof(bad), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        if (st) st->nonfinite = (long long)bad;
+        if (bad) return set_err(REPROBUS_ERR_NONFINITE, "%llu non-finite values in the step output", bad);
+    }
+    return REPROBUS_OK;
+}
+
+extern "C" int reprobus_chem_step_dev(void* handle, int ilat0, int ilat1, double daynum, double dt, const double* alt,
+                                      const double* trajlon, const double* trajlat, const double* trajpre,
+                                      const double* trajtem, int irapp, double* qj1, double* hc, double* vsed3d,
+                                      double* parth2osed, double* parthno3sed, double* surfarea, double* sza3d,
+                                      reprobus_stats* stats) {
+    Handle* h = (Handle*)handle;
+    if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
+    int rc = check_rows(h, ilat0, ilat1);
+    if (rc) return rc;
+    if (irapp < 1 || irapp > h->nrappmax) return set_err(REPROBUS_ERR_ARG, "irapp %d outside 1..%d", irapp, h->nrappmax);
+    if (!alt || !trajlon || !trajlat || !trajpre || !trajtem || !qj1 || !hc || !vsed3d || !parth2osed ||
+        !parthno3sed || !surfarea || !sza3d)
+        return set_err(REPROBUS_ERR_ARG, "NULL array argument");
+    Params P;
+    fill_params(h, P, ilat0, ilat1);
+    P.trajoff = (long long)(irapp - 1) * h->nlon * h->nlat * h->niv;
+    P.alt = alt;
+    P.trajlon = trajlon;
+    P.trajlat = trajlat;
+    P.trajpre = trajpre;
+    P.trajtem = trajtem;
+    P.qj1 = qj1;
+    P.hc = hc;
+    P.vsed3d = vsed3d;
+    P.parth2osed = parth2osed;
+    P.parthno3sed = parthno3sed;
+    P.surfarea = surfarea;
+    P.sza3d = sza3d;
+    step_const(h, daynum, dt, P.sc);
+    return launch_step(h, P, stats);
+}
+
+// strided copy of rows [r0, r0+nr) of `planes` consecutive (nlon,nlat) planes
+static int copy_rows(double* dst, const double* src, const Handle* h, int r0, int nr, size_t plane0, size_t planes,
+                     cudaMemcpyKind kind, cudaStream_t s) {
+    const size_t pitch = (size_t)h->nlon * h->nlat * sizeof(double);
+    const size_t off = plane0 * h->nlon * h->nlat + (size_t)h->nlon * r0;
+    CUDA_TRY(cudaMemcpy2DAsync(dst + off, pitch, src + off, pitch, (size_t)h->nlon * nr * sizeof(double), planes,
+                               kind, s));
+    return REPROBUS_OK;
+}
+
+static int ensure_mirrors(Handle* h) {
+    if (h->m_qj1) return REPROBUS_OK;
+    const size_t pl = (size_t)h->nlon * h->nlat * h->niv;
+    const size_t pb = (size_t)h->nlon * h->nlat * h->nivbas;
+    CUDA_TRY(cudaMalloc(&h->m_alt, pl * sizeof(double)));
+    for (auto& p : h->m_traj) CUDA_TRY(cudaMalloc(&p, pl * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&h->m_qj1, pl * NBCON * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&h->m_hc, pl * NCM * sizeof(double)));
+    for (int q = 0; q < 4; q++) CUDA_TRY(cudaMalloc(&h->m_out[q], pb * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&h->m_out[4], pl * sizeof(double)));
+    return REPROBUS_OK;
+}
+
+extern "C" int reprobus_chem_step(void* handle, int ilat0, int ilat1, double daynum, double dt, const double* alt,
+                                  const double* trajlon, const double* trajlat, const double* trajpre,
+                                  const double* trajtem, int irapp, double* qj1, double* hc, double* vsed3d,
+                                  double* parth2osed, double* parthno3sed, double* surfarea, double* sza3d,
+                                  reprobus_stats* stats) {
+    Handle* h = (Handle*)handle;
+    if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
+    int rc = check_rows(h, ilat0, ilat1);
+    if (rc) return rc;
+    if (irapp < 1 || irapp > h->nrappmax) return set_err(REPROBUS_ERR_ARG, "irapp %d outside 1..%d", irapp, h->nrappmax);
+    if (!alt || !trajlon || !trajlat || !trajpre || !trajtem || !qj1 || !hc || !vsed3d || !parth2osed ||
+        !parthno3sed || !surfarea || !sza3d)
+        return set_err(REPROBUS_ERR_ARG, "NULL array argument");
+    if ((rc = ensure_mirrors(h))) return rc;
+    const int r0 = ilat0 - 1, nr = ilat1 - ilat0 + 1;
+    const size_t pl = (size_t)h->nlon * h->nlat * h->niv;
+    const size_t nb = h->nivbas, niv = h->niv;
+    const int fuse = (h->flags & REPROBUS_FUSE_CONSERV) ? 1 : 0;
+    cudaStream_t s = h->stream;
+    const cudaMemcpyKind H2D = cudaMemcpyHostToDevice, D2H = cudaMemcpyDeviceToHost;
+    // inputs: alt and the irapp slice of traj* (levels 1..nivbas), state
+    if ((rc = copy_rows(h->m_alt, alt, h, r0, nr, 0, nb, H2D, s))) return rc;
+    const double* tr[4] = {trajlon + (irapp - 1) * pl, trajlat + (irapp - 1) * pl, trajpre + (irapp - 1) * pl,
+                           trajtem + (irapp - 1) * pl};
+    for (int q = 0; q < 4; q++)
+        if ((rc = copy_rows(h->m_traj[q], tr[q], h, r0, nr, 0, nb, H2D, s))) return rc;
+    if (fuse || nb == niv) {
+        if ((rc = copy_rows(h->m_qj1, qj1, h, r0, nr, 0, niv * NBCON, H2D, s))) return rc;
+    } else {
+        for (int n = 0; n < NBCON; n++)
+            if ((rc = copy_rows(h->m_qj1, qj1, h, r0, nr, niv * n, nb, H2D, s))) return rc;
+    }
+    for (int n = 0; n < NCM; n++)
+        if ((rc = copy_rows(h->m_hc, hc, h, r0, nr, niv * n, nb, H2D, s))) return rc;
+    Params P;
+    fill_params(h, P, ilat0, ilat1);
+    P.trajoff = 0;
+    P.alt = h->m_alt;
+    P.trajlon = h->m_traj[0];
+    P.trajlat = h->m_traj[1];
+    P.trajpre = h->m_traj[2];
+    P.trajtem = h->m_traj[3];
+    P.qj1 = h->m_qj1;
+    P.hc = h->m_hc;
+    P.vsed3d = h->m_out[0];
+    P.parth2osed = h->m_out[1];
+    P.parthno3sed = h->m_out[2];
+    P.sza3d = h->m_out[3];
+    P.surfarea = h->m_out[4];
+    step_const(h, daynum, dt, P.sc);
+    if ((rc = launch_step(h, P, stats))) return rc;
+    // outputs
+    if (fuse || nb == niv) {
+        if ((rc = copy_rows(qj1, h->m_qj1, h, r0, nr, 0, niv * NBCON, D2H, s))) return rc;
+    } else {
+        for (int n = 0; n < NBCON; n++)
+            if ((rc = copy_rows(qj1, h->m_qj1, h, r0, nr, niv * n, nb, D2H, s))) return rc;
+    }
+    for (int n = 0; n < NCM; n++)
+        if ((rc = copy_rows(hc, h->m_hc, h, r0, nr, niv * n, nb, D2H, s))) return rc;
+    if ((rc = copy_rows(vsed3d, h->m_out[0], h, r0, nr, 0, nb, D2H, s))) return rc;
+    if ((rc = copy_rows(parth2osed, h->m_out[1], h, r0, nr, 0, nb, D2H, s))) return rc;
+    if ((rc = copy_rows(parthno3sed, h->m_out[2], h, r0, nr, 0, nb, D2H, s))) return rc;
+    if ((rc = copy_rows(sza3d, h->m_out[3], h, r0, nr, 0, nb, D2H, s))) return rc;
+    const size_t kh = h->nivhau - 1;
+    if ((rc = copy_rows(surfarea, h->m_out[4], h, r0, nr, kh, nb - kh, D2H, s))) return rc;
+    CUDA_TRY(cudaStreamSynchronize(s));
+    return REPROBUS_OK;
+}
+
+extern "C" int reprobus_chem_rates_dev(void* handle, int ilat0, int ilat1, double daynum, const double* alt,
+                                       const double* trajlon, const double* trajlat, const double* trajpre,
+                                       const double* trajtem, int irapp, const double* qj1, const double* hc,
+                                       double* diag) {
+    Handle* h = (Handle*)handle;
+    if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
+    int rc = check_rows(h, ilat0, ilat1);
+    if (rc) return rc;
+    if (irapp < 1 || irapp > h->nrappmax) return set_err(REPROBUS_ERR_ARG, "irapp %d outside 1..%d", irapp, h->nrappmax);
+    if (!alt || !trajlon || !trajlat || !trajpre || !trajtem || !qj1 || !hc || !diag)
+        return set_err(REPROBUS_ERR_ARG, "NULL array argument");
+    Params P;
+    fill_params(h, P, ilat0, ilat1);
+    P.trajoff = (long long)(irapp - 1) * h->nlon * h->nlat * h->niv;
+    P.alt = alt;
+    P.trajlon = trajlon;
+    P.trajlat = trajlat;
+    P.trajpre = trajpre;
+    P.trajtem = trajtem;
+    P.qj1 = const_cast<double*>(qj1);  // read only in the DIAG instantiation
+    P.hc = const_cast<double*>(hc);
+    P.diag = diag;
+    step_const(h, daynum, 0., P.sc);
+    const int tb = 128;
+    k_columns<<<(P.ncol + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    k_chem<true><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return REPROBUS_OK;
+}
+
+extern "C" int reprobus_conserv_dev(void* handle, int ilat0, int ilat1, double* qj1, double* hc) {
+    Handle* h = (Handle*)handle;
+    if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
+    int rc = check_rows(h, ilat0, ilat1);
+    if (rc) return rc;
+    if (!qj1 || !hc) return set_err(REPROBUS_ERR_ARG, "NULL array argument");
+    Params P;
+    fill_params(h, P, ilat0, ilat1);
+    P.qj1 = qj1;
+    P.hc = hc;
+    long long n = (long long)h->nlon * P.nrows * h->niv;
+    k_conserv<<<(unsigned)((n + 127) / 128), 128, 0, h->stream>>>(P);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return REPROBUS_OK;
+}

@@ -1,0 +1,390 @@
+"""Seeded synthetic inputs for the REPROBUS chemistry step.
+
+The reference runs on ECMWF analyses, a restart file and a photolysis table
+(jstrato.txt) that are not available here, so every workload is synthetic and
+generated by this module from a seed. What is generated, and from where:
+
+* pressure: L137 hybrid coefficients (data/l137_ab.txt), mid levels
+  aaa = (a_k + a_k+1)/2 * 0.01, bbb = (b_k + b_k+1)/2 (as the reference does at
+  src/reprobus_l137_20230723.f:88-91), surface pressure U(980, 1030) hPa;
+* temperature: a piecewise-linear standard-atmosphere lapse-rate profile in
+  pressure altitude plus U(-25, 25) K, clipped to [185, 290] K; "polar" columns
+  get U(183, 195) K above 10 km;
+* mixing ratios: log-normal (sigma = 0.5 in ln) around smooth altitude profiles:
+  O3 (= Ox) peaking near 8e-6 at 10 hPa, inorganic Cl ~3.5e-9, Br ~2e-11,
+  NOy ~2e-8, H2O ~5e-6 (rising below the tropopause), CH4 and the source gases
+  decreasing with altitude, H2SO4 ~1e-10; family members (Cl, Br, N) are drawn
+  as fractions of their family, so the element totals that conserv restores
+  are consistent on input;
+* geometric altitude: the reference's own hypsometric algorithm (src/altitude.f90)
+  restated below with zero relief and trajectories at the grid points;
+* photolysis table ajl(40,101,27,7) and o3up(0:79): a smooth synthetic table
+  (positive everywhere up to SZA 95, as chem3d divides by J_BrCl) and the
+  standard O3 column of this generator's own mean O3 profile.
+
+Arrays are returned in the reference's Fortran layout (lon fastest) as numpy
+views with order='F'.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+import os
+
+import numpy as np
+
+from .species import L, NBCON, NCM, NPHOT, S
+
+NZ, NSZA, NOZO = 101, 27, 7
+_HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def l137_levels():
+    """(aaa [hPa], bbb) mid-level coefficients, F:79-91."""
+    ab = np.loadtxt(os.path.join(_HERE, "data", "l137_ab.txt"), comments="#")
+    a, b = ab[:, 1], ab[:, 2]
+    aaa = (a[:-1] + a[1:]) * 0.5 * 0.01
+    bbb = (b[:-1] + b[1:]) * 0.5
+    return aaa, bbb
+
+
+def troe_constants():
+    """COMMON /constant/, const F:5927-5948 (same arithmetic as the C library)."""
+    return np.array([
+        4.4e-32 * 300.0 ** 1.3, 7.5e-11 * 300.0 ** (-0.2),
+        2.0e-30 * 300.0 ** 4.4, 1.4e-12 * 300.0 ** 0.7,
+        1.8e-30 * 300.0 ** 3.0, 2.8e-11 * 300.0 ** 0.0,
+        2.0e-31 * 300.0 ** 3.4, 2.9e-12 * 300.0 ** 1.1,
+        1.8e-31 * 300.0 ** 3.4, 1.5e-11 * 300.0 ** 1.9,
+        1.8e-31 * 300.0 ** 2.0, 1.0e-10 * 300.0 ** 1.0,
+        1.6e-32 * 300.0 ** 4.5, 3.0e-12 * 300.0 ** 2.0,
+        5.2e-31 * 300.0 ** 3.2, 6.9e-12 * 300.0 ** 2.9,
+        4.0e-31 * 300.0 ** 3.6, 1.2e-12 * 300.0 ** (-1.1),
+    ])
+
+
+# --------------------------------------------------------------------------- #
+# photolysis table
+# --------------------------------------------------------------------------- #
+DSZA = np.array([0., 5., 10., 15., 20., 25., 30., 35., 40., 45., 50., 55., 60., 65.,
+                 70., 75., 80., 82., 84., 86., 88., 90., 91., 92., 93., 94., 95.])
+XV3 = np.array([0.4, 0.6, 0.8, 1.0, 1.2, 1.4, 1.6])
+
+# top-of-atmosphere J (s-1) and absorber optical depth at the ground for an
+# overhead sun; "o3" marks rates whose attenuation scales with the O3 column
+_J0 = {
+    "o2": (1e-9, 60., 0.2), "no2": (1e-2, 0.4, 0.1), "o3_o1d": (1e-4, 4., 1.0),
+    "o3_o3p": (5e-4, 0.5, 0.3), "no3_no": (2e-2, 0.3, 0.1), "no3_no2": (1.8e-1, 0.3, 0.1),
+    "n2o5": (5e-5, 3., 0.8), "hno3": (1e-5, 6., 0.8), "hno4": (1e-5, 4., 0.8),
+    "h2o2": (1e-5, 3., 0.8), "h2o": (1e-8, 50., 0.2), "n2o": (1e-7, 25., 0.4),
+    "hocl": (3e-4, 1.0, 0.5), "clono2_cl": (1e-4, 2., 0.7), "clono2_clo": (3e-5, 2., 0.7),
+    "cl2o2": (1e-3, 1.0, 0.5), "hcl": (1e-7, 40., 0.3), "cl2": (3e-3, 0.5, 0.3),
+    "clno2": (3e-4, 1.0, 0.5), "bro": (5e-2, 0.4, 0.2), "brono2": (1e-3, 1.0, 0.5),
+    "hobr": (2e-3, 0.6, 0.3), "oclo": (5e-2, 0.4, 0.2), "brcl": (1e-2, 0.5, 0.2),
+    "ch3o2h": (1e-5, 3., 0.8), "ch2o_hco": (4e-5, 2., 0.7), "ch2o_co": (6e-5, 2., 0.7),
+    "cfc11": (1e-6, 30., 0.5), "cfc12": (2e-7, 35., 0.5), "cfc113": (2e-7, 35., 0.5),
+    "ccl4": (1e-6, 28., 0.5), "ch3ccl3": (2e-7, 30., 0.5), "ch3cl": (1e-7, 35., 0.5),
+    "hcfc22": (1e-8, 40., 0.5), "ch3br": (3e-7, 30., 0.5), "h1211": (1e-5, 15., 0.6),
+    "h1301": (5e-7, 30., 0.5), "co2": (1e-11, 60., 0.2), "ch2br2": (5e-7, 25., 0.5),
+    "hbr": (1e-6, 20., 0.5),
+}
+
+
+def _airmass(sza_deg):
+    """Relative air mass; Kasten & Young (1989) up to 90 deg, then growing
+    smoothly so J stays positive up to 95 deg."""
+    s = np.asarray(sza_deg, dtype=np.float64)
+    s90 = np.minimum(s, 90.0)
+    m = 1.0 / (np.cos(np.radians(s90)) + 0.50572 * (96.07995 - s90) ** (-1.6364))
+    return m * np.exp(np.maximum(s - 90.0, 0.0) / 1.2)
+
+
+def make_jtable(o3up: np.ndarray):
+    """Synthetic ajl(40,101,27,7) in Fortran order; J(z, sza, v3rat) =
+    J0 * exp(-tau0 * exp(-z/7) * v^q * m(sza)) + J0*1e-7 (kept > 0)."""
+    from .species import PHOT
+    z = np.arange(NZ, dtype=np.float64)  # node j at altitude j-1 km (1-based)
+    m = _airmass(DSZA)
+    ajl = np.empty((NPHOT - 1, NZ, NSZA, NOZO), dtype=np.float64, order="F")
+    for n, name in enumerate(PHOT[:-1]):
+        j0, tau0, q = _J0[name]
+        tau = tau0 * np.exp(-z / 7.0)
+        for l, v in enumerate(XV3):
+            att = np.exp(-np.outer(tau * v ** q, m))  # (NZ, NSZA)
+            ajl[n, :, :, l] = j0 * att + j0 * 1e-7
+    return ajl
+
+
+# --------------------------------------------------------------------------- #
+# profiles
+# --------------------------------------------------------------------------- #
+def _t_standard(z):
+    """Piecewise-linear standard-atmosphere temperature (K) vs altitude (km)."""
+    zk = [0, 11, 20, 32, 47, 51, 71, 85, 200]
+    tk = [288.15, 216.65, 216.65, 228.65, 270.65, 270.65, 214.65, 186.87, 186.87]
+    return np.interp(z, zk, tk)
+
+
+def _sig(z, z0, h):
+    return 1.0 / (1.0 + np.exp(-(z - z0) / h))
+
+
+def _decay(z, h, z0=15.0):
+    return np.exp(-np.maximum(z - z0, 0.0) / h)
+
+
+@dataclasses.dataclass
+class ChemCase:
+    """One chemistry-step workload in the reference's array layout."""
+    name: str
+    nlon: int
+    nlat: int
+    niv: int
+    nivbas: int
+    nivhau: int
+    nrappmax: int
+    irapp: int          # 1-based slice of traj* to use
+    daynum: float
+    dt: float
+    alt: np.ndarray
+    trajlon: np.ndarray
+    trajlat: np.ndarray
+    trajpre: np.ndarray
+    trajtem: np.ndarray
+    qj1: np.ndarray
+    hc: np.ndarray
+    surfarea: np.ndarray
+    vsed3d: np.ndarray
+    parth2osed: np.ndarray
+    parthno3sed: np.ndarray
+    sza3d: np.ndarray
+    ajl: np.ndarray
+    o3up: np.ndarray
+    troe: np.ndarray
+
+    @property
+    def ncells(self):
+        return self.nlon * self.nlat * self.nivbas
+
+    def state_copy(self):
+        """Fresh copies of every array the step writes."""
+        return dict(qj1=self.qj1.copy(order="F"), hc=self.hc.copy(order="F"),
+                    vsed3d=self.vsed3d.copy(order="F"), parth2osed=self.parth2osed.copy(order="F"),
+                    parthno3sed=self.parthno3sed.copy(order="F"),
+                    surfarea=self.surfarea.copy(order="F"), sza3d=self.sza3d.copy(order="F"))
+
+
+def _fview(a_c, nlon, nlat):
+    """C-ordered (..., niv, ncol) -> Fortran (nlon, nlat, niv, ...) view."""
+    lead = a_c.shape[:-2]
+    niv = a_c.shape[-2]
+    v = a_c.reshape(lead + (niv, nlat, nlon))
+    return v.transpose(tuple(range(v.ndim - 1, -1, -1)))
+
+
+def _altitude(p, ps, tv, lat_deg):
+    """Geometric altitude (km) of every level; restates src/altitude.f90:32-146
+    with relief = 0 and the trajectory of each cell at its own grid point
+    (the nearest regular point is the column itself)."""
+    niv = p.shape[0]
+    ctegas = 287.04 / 9.80665
+    georeg = np.empty_like(p)
+    georeg[niv - 1] = 0.0 + ctegas * tv[niv - 1] * np.log(ps / p[niv - 1]) * 1.e-3
+    for k in range(niv - 2, -1, -1):
+        georeg[k] = georeg[k + 1] + ctegas * ((tv[k + 1] + tv[k]) / 2.) * np.log(p[k + 1] / p[k]) * 1.e-3
+    # pirr = min(trajpre, p(niv)) with trajpre = p: pirr = p; the search over
+    # inivreg = niv..2 keeps the last (smallest) level with p >= pirr, i.e.
+    # max(k, 2) in 1-based numbering.
+    geo = np.empty_like(p)
+    for k in range(niv):
+        kr = max(k, 1)
+        dz = ctegas * (tv[kr] + tv[kr - 1]) / 2. * np.log(p[kr] / p[k]) * 1.e-3
+        geo[k] = georeg[kr] + dz
+    xlat = lat_deg * math.pi / 180.
+    return (1. + 0.002644 * np.cos(2. * xlat)) * geo + (1. + 0.0089 * np.cos(2. * xlat)) * geo ** 2 / 6245.
+
+
+def _o3_column(p_mean, o3_mean, hnm_top):
+    """O3 column above each level with the arithmetic of total (F:5170-5184)."""
+    col = np.empty_like(p_mean)
+    col[0] = o3_mean[0] * hnm_top * 6.8e5
+    for k in range(1, len(p_mean)):
+        dp = max((p_mean[k] - p_mean[k - 1]) * 100., 0.)
+        col[k] = col[k - 1] + 2.120e20 * (o3_mean[k] + o3_mean[k - 1]) * .5 * dp
+    return col
+
+
+def make_case(config: str = "cfg0", seed: int = 0, nivbas: int | None = None, nivhau: int = 14,
+              nlon: int | None = None, nlat: int | None = None, daynum: float | None = None,
+              polar_frac: float | None = None, nrappmax: int = 1, irapp: int = 1,
+              dt: float = 900.0) -> ChemCase:
+    """Builds a seeded workload.
+
+    config: "cfg0" 64 random columns x 137 levels (8,768 cells);
+            "cfg1" the 2x2 deg grid 180 x 91 x 137 (2,244,060 cells);
+            "cfg2" cfg1 with 30% of the columns in polar winter;
+            "cfg4" the 1x1 deg grid 360 x 181 x 137;
+            "grid" a regular grid of nlon x nlat columns.
+    nivbas: last chemistry level (default: all 137 levels, so that every cell
+            of the named grid is integrated; the reference uses 94).
+    """
+    rng = np.random.default_rng(seed)
+    aaa, bbb = l137_levels()
+    niv = len(aaa)
+    if nivbas is None:
+        nivbas = niv
+    if config == "cfg0":
+        nlon = 64 if nlon is None else nlon
+        nlat = 1 if nlat is None else nlat
+        ncol = nlon * nlat
+        lat = rng.uniform(-90., 90., ncol)
+        lon = rng.uniform(0., 360., ncol)
+        day = rng.uniform(0., 365.) if daynum is None else daynum
+        pf = 0.0 if polar_frac is None else polar_frac
+    else:
+        dims = {"cfg1": (180, 91), "cfg2": (180, 91), "cfg4": (360, 181)}
+        if config in dims:
+            nlon, nlat = dims[config]
+        elif config != "grid":
+            raise ValueError(f"unknown config {config!r}")
+        dlon, dlat = 360. / nlon, 180. / (nlat - 1)
+        lon2 = np.arange(nlon) * dlon            # F:6051-6054
+        lat2 = 90. - np.arange(nlat) * dlat      # F:6041-6044, north to south
+        lon = np.tile(lon2, nlat)
+        lat = np.repeat(lat2, nlon)
+        ncol = nlon * nlat
+        if daynum is None:
+            day = 355.5 if config == "cfg2" else 80.5
+        else:
+            day = daynum
+        pf = (0.3 if config == "cfg2" else 0.0) if polar_frac is None else polar_frac
+    polar = np.zeros(ncol, dtype=bool)
+    if pf > 0:
+        polar[rng.choice(ncol, int(round(pf * ncol)), replace=False)] = True
+        # polar winter: move the parcels into the polar night (north in
+        # December, south otherwise), as trajectories do
+        north = (day % 365.) > 250. or (day % 365.) < 80.
+        lat = lat.copy()
+        lat[polar] = rng.uniform(76., 89., polar.sum()) * (1. if north else -1.)
+
+    ps = rng.uniform(980., 1030., ncol)
+    p = aaa[:, None] + bbb[:, None] * ps[None, :]                  # (niv, ncol) hPa
+    z = 7.0 * np.log(1013.25 / p)
+    shape = (niv, ncol)
+    T = np.clip(_t_standard(z) + rng.uniform(-25., 25., shape), 185., 290.)
+    if polar.any():
+        strat = (z > 10.0) & polar[None, :]
+        T = np.where(strat, rng.uniform(183., 195., shape), T)
+
+    def ln():
+        return np.exp(0.5 * rng.standard_normal(shape))
+
+    q = np.zeros((NBCON,) + shape)
+    q[L["n2o"]] = 3.3e-7 * _decay(z, 12.) * ln()
+    q[L["ch4"]] = 1.9e-6 * _decay(z, 25.) * ln()
+    q[L["h2o"]] = (5e-6 + 1.2e-2 * np.exp(-z / 2.2)) * ln()
+    q[L["ox"]] = (8e-6 * np.exp(-((z - 32.) / 8.) ** 2) + 4e-8) * ln()
+    q[L["co"]] = (1.5e-8 + 8e-8 * np.exp(-z / 6.)) * ln()
+    q[L["h2so4"]] = 1e-10 * ln()
+    q[L["h2o2"]] = 1e-10 * ln()
+    q[L["ch2o"]] = 5e-11 * ln()
+    q[L["ch3o2"]] = 1e-12 * ln()
+    q[L["ch3o2h"]] = 5e-11 * ln()
+    for name, x0, h in (("cfc11", 2.2e-10, 4.), ("cfc12", 5.0e-10, 7.), ("cfc113", 7e-11, 6.),
+                        ("ccl4", 8e-11, 4.), ("ch3ccl3", 2.5e-11, 5.), ("ch3cl", 5.5e-10, 6.),
+                        ("hcfc22", 2.7e-10, 10.), ("ch3br", 6.6e-12, 5.), ("h1211", 3.2e-12, 5.),
+                        ("h1301", 3.7e-12, 9.), ("ch2br2", 5e-12, 4.)):
+        q[L[name]] = x0 * _decay(z, h) * ln()
+    # bromine family, F:2595-2609 members
+    bry = (2e-11 * _sig(z, 20., 4.) + 2e-12) * ln()
+    brm = ["hbr", "brono2", "brox", "hobr", "brcl"]
+    fr = np.array([0.05, 0.35, 0.35, 0.2, 0.05])[:, None, None] * np.stack([ln() for _ in brm])
+    fr /= fr.sum(axis=0)
+    for i, nm in enumerate(brm):
+        q[L[nm]] = fr[i] * bry
+    q[L["bry"]] = bry
+    # chlorine family, F:2546-2567 members (weights 2 for cl2, cl2o2)
+    cly = (3.5e-9 * _sig(z, 22., 4.) + 5e-11) * ln()
+    clm = ["oclo", "hcl", "clono2", "hocl", "cl2", "clno2", "clox", "cl2o2"]
+    stoich = np.array([1, 1, 1, 1, 2, 1, 1, 2], dtype=np.float64)[:, None, None]
+    base = np.array([5e-4, 0.65, 0.25, 0.02, 0.002, 0.001, 0.05, 0.002])[:, None, None]
+    pol = np.array([5e-4, 0.2, 0.2, 0.05, 0.02, 0.005, 0.35, 0.15])[:, None, None]
+    act = (polar[None, :] & (z > 12.))[None]
+    fr = np.where(act, pol, base) * np.stack([ln() for _ in clm])
+    fr = fr / (stoich * fr).sum(axis=0)
+    avail = cly - q[L["brcl"]]
+    for i, nm in enumerate(clm):
+        q[L[nm]] = fr[i] * avail
+    q[L["cly"]] = cly
+    # nitrogen family, F:2573-2589 members
+    noy = (2e-8 * np.exp(-((z - 30.) / 11.) ** 2) + 3e-10) * ln()
+    other = q[L["clono2"]] + q[L["clno2"]] + q[L["brono2"]]
+    noy = np.maximum(noy, 2.0 * other + 1e-10)
+    nm_ = ["hno3", "n2o5", "nox", "ho2no2"]
+    stn = np.array([1, 2, 1, 1], dtype=np.float64)[:, None, None]
+    fr = np.array([0.6, 0.03, 0.3, 0.02])[:, None, None] * np.stack([ln() for _ in nm_])
+    fr = fr / (stn * fr).sum(axis=0)
+    for i, nm in enumerate(nm_):
+        q[L[nm]] = fr[i] * (noy - other)
+    q[L["noy"]] = noy
+    q[L["ox_passive"]] = q[L["ox"]]
+    q[L["hno3_gas"]] = q[L["hno3"]]
+
+    h = np.zeros((NCM,) + shape)
+    h[S["o1d"]] = 1e-19 * ln()
+    h[S["oh"]] = 5e-12 * ln()
+    h[S["cl"]] = 2e-14 * ln()
+    h[S["o3p"]] = np.minimum(1e-4 * np.exp((z - 30.) / 6.), 0.1) * q[L["ox"]]
+    h[S["o3"]] = q[L["ox"]]
+    h[S["ho2"]] = 3e-11 * ln()
+    h[S["no2"]] = 0.6 * q[L["nox"]]
+    h[S["no"]] = 0.4 * q[L["nox"]]
+    h[S["br"]] = 0.05 * q[L["brox"]]
+    h[S["n"]] = 1e-17 * ln()
+    h[S["clo"]] = 0.9 * q[L["clox"]]
+    h[S["bro"]] = 0.9 * q[L["brox"]]
+    h[S["no3"]] = 1e-12 * ln()
+    h[S["h"]] = 1e-16 * ln()
+    h[S["ch3"]] = 1e-19 * ln()
+
+    tv = T * (1. + 0.608 * q[L["h2o"]] * 18. / 28.97)
+    alt = _altitude(p, ps, tv, lat)
+
+    # standard O3 column vs altitude from the mean column of this generator
+    pm_ = p.mean(axis=1)
+    o3m = np.exp(np.log(q[L["ox"]]).mean(axis=1))
+    hnm_top = pm_[0] / (T[0].mean() * 1.38e-19)
+    col = _o3_column(pm_, o3m, hnm_top)
+    altm = alt.mean(axis=1)
+    order = np.argsort(altm)
+    zgrid = np.arange(80, dtype=np.float64)
+    o3up = np.exp(np.interp(zgrid, altm[order], np.log(col[order])))
+    ajl = make_jtable(o3up)
+
+    # arrays in Fortran layout
+    alt_f = np.asfortranarray(_fview(alt, nlon, nlat))
+    tl = np.broadcast_to(lon[None, :], shape)
+    tb = np.broadcast_to(lat[None, :], shape)
+
+    def traj(x):
+        a = np.empty((nrappmax,) + shape)
+        a[:] = x[None]
+        if nrappmax > 1:  # other slices differ, so that a wrong slice shows
+            for r in range(nrappmax):
+                if r != irapp - 1:
+                    a[r] *= 1.0 + 0.01 * (r + 1)
+        return _fview(a, nlon, nlat)
+
+    qj1 = _fview(q, nlon, nlat)
+    hcv = _fview(h, nlon, nlat)
+    zeros3 = np.zeros((niv, ncol))
+    zeros_b = np.zeros((nivbas, ncol))
+    return ChemCase(
+        name=config, nlon=nlon, nlat=nlat, niv=niv, nivbas=nivbas, nivhau=nivhau,
+        nrappmax=nrappmax, irapp=irapp, daynum=float(day), dt=dt,
+        alt=alt_f, trajlon=traj(tl), trajlat=traj(tb), trajpre=traj(p), trajtem=traj(T),
+        qj1=qj1, hc=hcv, surfarea=_fview(zeros3, nlon, nlat),
+        vsed3d=_fview(zeros_b.copy(), nlon, nlat), parth2osed=_fview(zeros_b.copy(), nlon, nlat),
+        parthno3sed=_fview(zeros_b.copy(), nlon, nlat), sza3d=_fview(zeros_b.copy(), nlon, nlat),
+        ajl=ajl, o3up=o3up, troe=troe_constants(),
+    )
