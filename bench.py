@@ -181,7 +181,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="cfg1")
+    ap.add_argument("--config", default="cfg1", help="cfg1 (180x91x137), cfg2, cfg4, or grid (--nlon x --nlat)")
+    ap.add_argument("--nlon", type=int, default=180)
+    ap.add_argument("--nlat", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
@@ -198,7 +200,10 @@ def main():
     from reprobus_gb300.chem import FUSE_CONSERV
     from reprobus_gb300.resident import DeviceCase
 
-    case = inputs.make_case(args.config, seed=1234 + rank)
+    if args.config == "grid":
+        case = inputs.make_case("grid", seed=1234 + rank, nlon=args.nlon, nlat=args.nlat)
+    else:
+        case = inputs.make_case(args.config, seed=1234 + rank)
     h = ChemStep.for_case(case, niter=5, flags=FUSE_CONSERV)
     stream = torch.cuda.Stream()
     h.set_stream(stream)

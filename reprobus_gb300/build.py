@@ -19,6 +19,9 @@ SOURCES = ["chem_kernels.cu"]
 HEADERS = ["chem_cell.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-diag-suppress", "550"]
+if os.environ.get("REPROBUS_FMAD", "1") == "0":
+    # strict IEEE variant (no FMA contraction) for parity studies
+    NVFLAGS += ["--fmad=false"]
 
 
 def nvcc() -> str:
