@@ -294,7 +294,9 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; reference inputs unavailable)",
-                "config": {"workload": WORKLOAD, "solver": "reference scheme, 5 fixed passes (drop-in)",
+                "config": {"workload": WORKLOAD if args.config == "cfg1" else
+                           f"{args.config}: {case.nlon}x{case.nlat}x{case.niv} = {case.ncells} cells, one 15-min step",
+                           "solver": "reference scheme, 5 fixed passes (drop-in)",
                            "cells": ncell, "l2": "inputs larger than L2 (1.2 GB resident state)",
                            "parallelism": f"replicas x{world}"},
                 "gpu_launches": launches_per_step * args.steps,
