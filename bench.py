@@ -34,6 +34,10 @@ sys.path.insert(0, ROOT)
 METRIC = "cell-steps/s (55 sp, 15-min) 1 GB300: MLP+mixed vs plain FP64, same 1e-6 err"
 WORKLOAD = "2x2deg L137 global grid, 180x91x137 = 2,244,060 cells, one 15-min step, FP64 reference scheme (5 passes)"
 BYTES_PER_CELL = 1008  # compulsory FP64 SoA traffic per cell-step: 63 reads + 63 writes
+# Algorithmic FP64 work of the reference scheme per cell-step on the cfg1 grid:
+# 6612 +-*/ (612 of them divisions) + 181 transcendentals, each counted once
+# (python -m oracle.count_ops --config cfg1 --rows 12).
+OPS_PER_CELL = 6793.08
 
 
 def dist_env():
@@ -277,7 +281,7 @@ def main():
             hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
         except Exception:
             hbm_peak = 6800.0
-        flops_cell = float(os.environ.get("REPROBUS_FLOPS_PER_CELL", "0")) or None
+        flops_cell = OPS_PER_CELL
         ach_gbs = BYTES_PER_CELL * ncell / (kernel_ms * 1e-3) / 1e9
         roof = {"bound": "fp64", "unit": "TFLOP/s", "peak": round(peak64, 4),
                 "peak_source": "cuBLAS DGEMM 4096^3 measured live in this run",
@@ -287,7 +291,9 @@ def main():
                         "frac": round(ach_gbs / hbm_peak, 5), "bytes_per_cell": BYTES_PER_CELL}}
         if flops_cell:
             ach = flops_cell * ncell / (kernel_ms * 1e-3) / 1e12
-            roof.update(achieved=round(ach, 4), frac=round(ach / peak64, 4), flops_per_cell=flops_cell)
+            roof.update(achieved=round(ach, 4), frac=round(ach / peak64, 4), flops_per_cell=flops_cell,
+                        flops_note="algorithmic ops of the reference scheme per cell-step (+-*/ and "
+                                   "transcendentals counted once each; the peak counts an FMA as 2)")
         cb = None
         if not args.no_cpu_baseline:
             cb = cpu_baseline(case)

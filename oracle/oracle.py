@@ -114,3 +114,49 @@ def clamp(case, qj1, ilat0=1, ilat1=None):
     g = grid(case)
     ilat1 = case.nlat if ilat1 is None else ilat1
     lib().orc_clamp(ctypes.byref(g), ilat0 - 1, ilat1 - 1, _p(qj1))
+
+
+# --------------------------------------------------------------------------- #
+# operation counts (op_count.cpp: the same oracle source with a counting type)
+# --------------------------------------------------------------------------- #
+COUNT_LIB = os.path.join(HERE, "liboracle_count.so")
+COUNT_SRC = os.path.join(HERE, "op_count.cpp")
+COUNT_CATS = ["add", "mul", "div", "exp", "log", "log10", "pow", "sqrt", "trig", "tanh", "cmp"]
+
+
+def build_count(force: bool = False) -> str:
+    deps = [COUNT_SRC, SRC, os.path.join(HERE, "chem_oracle.h")]
+    if force or not os.path.exists(COUNT_LIB) or any(os.path.getmtime(d) > os.path.getmtime(COUNT_LIB)
+                                                      for d in deps):
+        subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o",
+                        COUNT_LIB, COUNT_SRC, "-lm"], check=True)
+    return COUNT_LIB
+
+
+def op_counts(case, rows, niter=5):
+    """Operations the reference scheme executes per cell-step, averaged over
+    the cells of the given 1-based latitude rows (all lon, levels 1..nivbas).
+    Returns a dict: the categories of COUNT_CATS, 'flops' (+-*/) and
+    'transcendentals', all per cell."""
+    build_count()
+    L = ctypes.CDLL(COUNT_LIB)
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.orc_step.restype = ctypes.c_int
+    L.orc_step.argtypes = lib().orc_step.argtypes
+    L.orc_count_read.argtypes = [ctypes.POINTER(ctypes.c_ulonglong)]
+    g = grid(case, niter=niter)
+    st = case.state_copy()
+    L.orc_count_reset()
+    for r in rows:
+        L.orc_step(ctypes.byref(g), r - 1, r - 1, case.daynum, case.dt, _p(case.alt), _p(case.trajlon),
+                   _p(case.trajlat), _p(case.trajpre), _p(case.trajtem), case.irapp - 1, _p(st["qj1"]),
+                   _p(st["hc"]), _p(st["vsed3d"]), _p(st["parth2osed"]), _p(st["parthno3sed"]), _p(st["surfarea"]),
+                   _p(st["sza3d"]), 1, None, 1)
+    out = (ctypes.c_ulonglong * len(COUNT_CATS))()
+    L.orc_count_read(out)
+    ncell = len(rows) * case.nlon * case.nivbas
+    res = {k: out[i] / ncell for i, k in enumerate(COUNT_CATS)}
+    res["flops"] = res["add"] + res["mul"] + res["div"]
+    res["transcendentals"] = sum(res[k] for k in ("exp", "log", "log10", "pow", "sqrt", "trig", "tanh"))
+    res["cells"] = ncell
+    return res
