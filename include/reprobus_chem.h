@@ -161,6 +161,41 @@ int reprobus_chem_rates_dev(void* handle, int ilat0, int ilat1, double daynum,
  * :431-450. */
 int reprobus_conserv_dev(void* handle, int ilat0, int ilat1, double* qj1, double* hc);
 
+/* Allocation-free variant of reprobus_chem_step_dev. No counterpart in the
+ * reference: REPROBUS allocates all of its arrays itself, on the host.
+ *
+ * For callers that may not allocate device memory while they run: models
+ * whose GPU memory is reserved once and handed out by their own runtime or
+ * pool (OpenACC/CUDA-Fortran data regions, a framework's caching allocator),
+ * or processes held to a fixed device-memory budget. The call needs no handle
+ * and calls no cudaMalloc/cudaFree: the caller passes every array as a DEVICE
+ * pointer -- the photolysis table ajl(40,101,27,7) and o3up(0:79) included --
+ * plus the 18 Troe prefactors as a HOST array, and the step's only scratch
+ * (3 doubles per chemistry cell + 1 per column + a counter) lives in one
+ * fixed device array of REPROBUS_NOALLOC_SCRATCH_DOUBLES doubles (8 MiB),
+ * which every GPU that loads the library holds until the process exits.
+ * Limit: 3*nlon*nrows*nivbas + nlon*nrows + 32 <= REPROBUS_NOALLOC_SCRATCH_DOUBLES
+ * (reference grid, nivbas 94: up to 20 latitude rows per call); larger
+ * requests return REPROBUS_ERR_ARG and do nothing.
+ * The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before capturing
+ * any stream. All calls share the one array and it keeps the last call's
+ * contents: calls whose kernels overlap on the GPU (other streams, other host
+ * threads) race on it; serialise them. Launches on `stream` (NULL: the
+ * default stream); asynchronous unless REPROBUS_CHECK_FINITE is set, in
+ * which case it synchronises to read the non-finite count.
+ * Same replacement of the reference as reprobus_chem_step (:398-450). */
+#define REPROBUS_NOALLOC_SCRATCH_DOUBLES (1 << 20)
+int reprobus_chem_step_noalloc(const double* ajl, const double* o3up, const double* troe,
+                               int nlon, int nlat, int niv, int nivbas, int nivhau,
+                               int nrappmax, int niter, int flags, int ilat0, int ilat1,
+                               double daynum, double dt, const double* alt,
+                               const double* trajlon, const double* trajlat,
+                               const double* trajpre, const double* trajtem, int irapp,
+                               double* qj1, double* hc, double* vsed3d, double* parth2osed,
+                               double* parthno3sed, double* surfarea, double* sza3d,
+                               void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -36,8 +36,9 @@ ERRORS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NONFINITE", 4: "ERR_NOCO
 EXPORTS = [
     "reprobus_version", "reprobus_last_error", "reprobus_chem_troe", "reprobus_chem_init",
     "reprobus_chem_free", "reprobus_chem_set_stream", "reprobus_chem_step", "reprobus_chem_step_dev",
-    "reprobus_chem_rates_dev", "reprobus_conserv_dev",
+    "reprobus_chem_rates_dev", "reprobus_conserv_dev", "reprobus_chem_step_noalloc",
 ]
+NOALLOC_SCRATCH_DOUBLES = 1 << 20
 
 
 class ReprobusError(RuntimeError):
@@ -79,6 +80,8 @@ def load_library(path: str = LIBPATH):
     lib.reprobus_chem_step_dev.argtypes = step_args
     lib.reprobus_chem_rates_dev.argtypes = [vp, i, i, d, vp, vp, vp, vp, vp, i, vp, vp, vp]
     lib.reprobus_conserv_dev.argtypes = [vp, i, i, vp, vp]
+    lib.reprobus_chem_step_noalloc.argtypes = [vp, vp, dp, i, i, i, i, i, i, i, i, i, i, d, d, vp, vp, vp, vp, vp,
+                                               i, vp, vp, vp, vp, vp, vp, vp, vp]
     for name in EXPORTS:
         if name not in ("reprobus_version", "reprobus_last_error"):
             getattr(lib, name).restype = ctypes.c_int
@@ -190,6 +193,23 @@ class ChemStep:
 
     def conserv_dev(self, ilat0, ilat1, qj1, hc):
         _check(self.lib.reprobus_conserv_dev(self._h, ilat0, ilat1, _dp(qj1), _dp(hc)))
+
+
+def step_noalloc(ajl, o3up, troe, nlon, nlat, niv, nivbas, nivhau, nrappmax, niter, flags, ilat0, ilat1,
+                 daynum, dt, alt, trajlon, trajlat, trajpre, trajtem, irapp, qj1, hc, vsed3d, parth2osed,
+                 parthno3sed, surfarea, sza3d, stream=None):
+    """reprobus_chem_step_noalloc: the step with no device allocation (no
+    handle). ajl/o3up and every array are DEVICE arrays (torch CUDA tensors or
+    pointers); troe is a host sequence of 18 values. For callers that may not
+    allocate device memory; see include/reprobus_chem.h for the scratch limit."""
+    lib = load_library()
+    tr = np.ascontiguousarray(troe, dtype=np.float64)
+    sp = None if stream is None else (stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream))
+    _check(lib.reprobus_chem_step_noalloc(
+        _dp(ajl), _dp(o3up), tr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), nlon, nlat, niv, nivbas, nivhau,
+        nrappmax, niter, flags, ilat0, ilat1, float(daynum), float(dt), _dp(alt), _dp(trajlon), _dp(trajlat),
+        _dp(trajpre), _dp(trajtem), irapp, _dp(qj1), _dp(hc), _dp(vsed3d), _dp(parth2osed), _dp(parthno3sed),
+        _dp(surfarea), _dp(sza3d), ctypes.c_void_p(sp)))
 
 
 # --------------------------------------------------------------------------- #

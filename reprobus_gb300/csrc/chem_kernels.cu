@@ -706,3 +706,110 @@ extern "C" int reprobus_conserv_dev(void* handle, int ilat0, int ilat1, double* 
     CUDA_TRY(cudaStreamSynchronize(h->stream));
     return REPROBUS_OK;
 }
+
+// ----------------------------------------------------------------------------
+// Allocation-free step (no counterpart in the reference).
+//
+// Some callers may not allocate device memory once they are running: a model
+// whose GPU memory is reserved up front and handed out by its own runtime or
+// pool (an OpenACC/CUDA-Fortran data region, a framework's caching
+// allocator), or a process held to a fixed device-memory budget. For them,
+// reprobus_chem_step_noalloc takes every array from the caller and keeps the
+// only scratch the step needs (the column sums written by k_columns and read
+// by k_chem, and the non-finite counter) in the fixed array below, which the
+// CUDA runtime places on each device when the library's module is loaded
+// there and keeps until the process exits. The kernels and their launch are
+// those of reprobus_chem_step_dev.
+// ----------------------------------------------------------------------------
+#include <mutex>
+
+static __device__ __align__(256) double g_noalloc_scratch[REPROBUS_NOALLOC_SCRATCH_DOUBLES];
+
+// In host code g_noalloc_scratch names a host-side stand-in, not device
+// memory: its device address is looked up once per device (with that device
+// current) and cached here.
+static std::mutex g_noalloc_mu;
+static double* g_noalloc_dev[256];
+
+static int noalloc_scratch(double** out) {
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 256) return set_err(REPROBUS_ERR_ARG, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_dev[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return set_err(REPROBUS_ERR_CUDA, "cudaGetSymbolAddress(scratch) on device %d: %s", dev,
+                           cudaGetErrorString(e));
+        g_noalloc_dev[dev] = (double*)p;
+    }
+    *out = g_noalloc_dev[dev];
+    return REPROBUS_OK;
+}
+
+extern "C" int reprobus_chem_step_noalloc(const double* ajl, const double* o3up, const double* troe, int nlon,
+                                          int nlat, int niv, int nivbas, int nivhau, int nrappmax, int niter,
+                                          int flags, int ilat0, int ilat1, double daynum, double dt,
+                                          const double* alt, const double* trajlon, const double* trajlat,
+                                          const double* trajpre, const double* trajtem, int irapp, double* qj1,
+                                          double* hc, double* vsed3d, double* parth2osed, double* parthno3sed,
+                                          double* surfarea, double* sza3d, void* stream) {
+    if (!ajl || !o3up || !troe) return set_err(REPROBUS_ERR_ARG, "ajl, o3up and troe must be non-NULL");
+    if (nlon <= 0 || nlat <= 0 || niv <= 0 || nivbas <= 0 || nivbas > niv || nivhau < 1 || nivhau > nivbas ||
+        nrappmax <= 0 || niter < 0)
+        return set_err(REPROBUS_ERR_ARG, "bad sizes: nlon=%d nlat=%d niv=%d nivbas=%d nivhau=%d nrappmax=%d niter=%d",
+                       nlon, nlat, niv, nivbas, nivhau, nrappmax, niter);
+    if (ilat0 < 1 || ilat1 > nlat || ilat0 > ilat1)
+        return set_err(REPROBUS_ERR_ARG, "bad row range %d..%d (nlat=%d)", ilat0, ilat1, nlat);
+    if (irapp < 1 || irapp > nrappmax) return set_err(REPROBUS_ERR_ARG, "irapp %d outside 1..%d", irapp, nrappmax);
+    if (!alt || !trajlon || !trajlat || !trajpre || !trajtem || !qj1 || !hc || !vsed3d || !parth2osed ||
+        !parthno3sed || !surfarea || !sza3d)
+        return set_err(REPROBUS_ERR_ARG, "NULL array argument");
+    // scratch layout: [counter, padded to 256 B][3 doubles per cell][1 double per column]
+    const long long nrows = ilat1 - ilat0 + 1;
+    const long long ncol = (long long)nlon * nrows;
+    const long long need = 32 + 3 * ncol * nivbas + ncol;
+    if (need > REPROBUS_NOALLOC_SCRATCH_DOUBLES)
+        return set_err(REPROBUS_ERR_ARG,
+                       "rows %d..%d need %lld scratch doubles; the allocation-free step holds at most %d "
+                       "(3*nlon*rows*nivbas + nlon*rows + 32): pass fewer rows per call",
+                       ilat0, ilat1, need, REPROBUS_NOALLOC_SCRATCH_DOUBLES);
+    double* scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    // a handle on the stack that owns nothing: the caller's table and the fixed scratch
+    Handle h;
+    h.nlon = nlon;
+    h.nlat = nlat;
+    h.niv = niv;
+    h.nivbas = nivbas;
+    h.nivhau = nivhau;
+    h.nrappmax = nrappmax;
+    h.niter = niter;
+    h.flags = flags;
+    CUDA_TRY(cudaGetDevice(&h.device));
+    memcpy(h.troe, troe, sizeof(h.troe));
+    h.d_ajl = const_cast<double*>(ajl);
+    h.d_o3up = const_cast<double*>(o3up);
+    h.d_count = reinterpret_cast<unsigned long long*>(scratch);
+    h.d_col = scratch + 32;
+    h.stream = (cudaStream_t)stream;
+    Params P;
+    fill_params(&h, P, ilat0, ilat1);
+    P.trajoff = (long long)(irapp - 1) * nlon * nlat * niv;
+    P.alt = alt;
+    P.trajlon = trajlon;
+    P.trajlat = trajlat;
+    P.trajpre = trajpre;
+    P.trajtem = trajtem;
+    P.qj1 = qj1;
+    P.hc = hc;
+    P.vsed3d = vsed3d;
+    P.parth2osed = parth2osed;
+    P.parthno3sed = parthno3sed;
+    P.surfarea = surfarea;
+    P.sza3d = sza3d;
+    step_const(&h, daynum, dt, P.sc);
+    return launch_step(&h, P, nullptr);
+}
