@@ -32,7 +32,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "cell-steps/s (55 sp, 15-min) 1 GB300: MLP+mixed vs plain FP64, same 1e-6 err"
-WORKLOAD = "2x2deg L137 global grid, 180x91x137 = 2,244,060 cells, one 15-min step, FP64 reference scheme (5 passes)"
+WORKLOAD = "2x2deg L137 global grid, 180x91x137 = 2,244,060 cells, one 15-min step, 55 species, FP64 state"
 BYTES_PER_CELL = 1008  # compulsory FP64 SoA traffic per cell-step: 63 reads + 63 writes
 # Algorithmic FP64 work of the reference scheme per cell-step on the cfg1 grid:
 # 6612 +-*/ (612 of them divisions) + 181 transcendentals, each counted once
@@ -190,6 +190,8 @@ def main():
     ap.add_argument("--nlat", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--solver", default="all", choices=["all", "ref5", "newton64", "mixed"],
+                    help="all: time the three solvers, headline = mixed")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -208,43 +210,67 @@ def main():
         case = inputs.make_case("grid", seed=1234 + rank, nlon=args.nlon, nlat=args.nlat)
     else:
         case = inputs.make_case(args.config, seed=1234 + rank)
+    from reprobus_gb300.chem import SOLVER_NEWTON64, SOLVER_NEWTON_MIXED, SOLVER_REF5
+    solver_ids = {"ref5": SOLVER_REF5, "newton64": SOLVER_NEWTON64, "mixed": SOLVER_NEWTON_MIXED}
+    run = list(solver_ids) if args.solver == "all" else [args.solver]
+    headline = "mixed" if args.solver == "all" else args.solver
     h = ChemStep.for_case(case, niter=5, flags=FUSE_CONSERV)
     stream = torch.cuda.Stream()
     h.set_stream(stream)
     dc = DeviceCase(case)
     a = dc.args()
+    state = ("qj1", "hc", "vsed3d", "parth2osed", "parthno3sed", "surfarea", "sza3d")
+    pristine = {f: dc[f].clone() for f in state}
 
-    def step():
-        h.step_dev(1, case.nlat, case.daynum, case.dt, *a)
+    def restore():
+        with torch.cuda.stream(stream):
+            for f in state:
+                dc[f].copy_(pristine[f])
 
-    with torch.cuda.stream(stream):
-        for _ in range(max(args.warmup, 3)):
-            step()
-    torch.cuda.synchronize()
-    st = h.step_dev(1, case.nlat, case.daynum, case.dt, *a, stats=True)  # launches per step, kernel time
-    launches_per_step = st["kernel_launches"]
-    kernel_ms = st["device_ms"]
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
+    def step(stats=False):
+        return h.step_dev(1, case.nlat, case.daynum, case.dt, *a, stats=stats)
+
+    results = {}
     clocks = Clocks(local)
     clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
+    for name in run:
+        h.set_solver(solver_ids[name], npass=1, maxit=12, tol=1e-10)
+        for _ in range(max(args.warmup, 3)):
+            restore()
+            step()
+        restore()
+        st = step(stats=True)  # launches per step, kernel time, solver statistics
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        for e0, e1 in evs:
+            restore()
+            e0.record(stream)
+            step()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            torch.distributed.barrier()
+            ms = float(t.item())
+        conv = case.ncells - st["fallbacks"]
+        results[name] = {"cells_per_s": case.ncells * world * args.steps / (ms * 1e-3),
+                         "ms_per_step": ms / args.steps, "kernel_ms": st["device_ms"],
+                         "launches_per_step": st["kernel_launches"], "fallbacks": st["fallbacks"],
+                         "mean_newton_iters": (st["newton_iters"] / conv) if name != "ref5" and conv else None,
+                         "max_newton_iters": st["max_newton_iters"] if name != "ref5" else None}
     clk = clocks.stop()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.barrier()
-        ms = float(t.item())
-    ms_step = ms / args.steps
+    h.set_solver(solver_ids[headline], npass=1, maxit=12, tol=1e-10)
+    R = results[headline]
+    ms_step = R["ms_per_step"]
+    kernel_ms = R["kernel_ms"]
+    launches_per_step = R["launches_per_step"]
     ncell = case.ncells
-    value = ncell * world * args.steps / (ms * 1e-3)
+    value = R["cells_per_s"]
 
     # end to end through the host entry point, pinned host arrays
     e2e = None
@@ -302,10 +328,17 @@ def main():
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; reference inputs unavailable)",
                 "config": {"workload": WORKLOAD if args.config == "cfg1" else
                            f"{args.config}: {case.nlon}x{case.nlat}x{case.niv} = {case.ncells} cells, one 15-min step",
-                           "solver": "reference scheme, 5 fixed passes (drop-in)",
+                           "solver": {"ref5": "reference scheme, 5 fixed passes (drop-in)",
+                                      "newton64": "Newton to the fixed point of the reference map, FP64 Jacobian",
+                                      "mixed": "Newton to the fixed point, FP32 Jacobian+LU, FP64 residual/update"}
+                           [headline],
+                           "timing": "each timed step starts from the same restored device state",
                            "cells": ncell, "l2": "inputs larger than L2 (1.2 GB resident state)",
                            "parallelism": f"replicas x{world}"},
                 "gpu_launches": launches_per_step * args.steps,
+                "solvers": results,
+                "mixed_vs_fp64_newton": (results["mixed"]["cells_per_s"] / results["newton64"]["cells_per_s"]
+                                         if "mixed" in results and "newton64" in results else None),
                 "roofline": roof, "e2e": e2e, "cpu_baseline": cb, "clocks": clk}
         print(json.dumps(line))
     h.close()

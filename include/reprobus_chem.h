@@ -51,13 +51,23 @@ enum {
 #define REPROBUS_CHECK_FINITE  0x2  /* count NaN/Inf in outputs, return
                                        REPROBUS_ERR_NONFINITE when any           */
 
+/* ---- solvers (reprobus_chem_set_solver) ----------------------------------- */
+#define REPROBUS_SOLVER_REF5          0  /* the reference scheme: niter fixed passes  */
+#define REPROBUS_SOLVER_NEWTON64      1  /* Newton to the fixed point, FP64 Jacobian   */
+#define REPROBUS_SOLVER_NEWTON_MIXED  2  /* Newton, FP32 Jacobian and LU, FP64 residual
+                                            and update                                 */
+
 /* ---- per-call statistics --------------------------------------------------- */
 typedef struct reprobus_stats {
     long long ncells;          /* cells integrated by the call (rows x nlon x nivbas) */
     long long nonfinite;       /* NaN/Inf values produced (REPROBUS_CHECK_FINITE)     */
     int kernel_launches;       /* kernels this call launched                          */
-    int passes;                /* fixed-point passes per cell (niter)                  */
+    int passes;                /* reference passes per cell (niter, or Newton's npass) */
     double device_ms;          /* device time of the call's kernels (CUDA events)      */
+    long long newton_iters;    /* Newton solvers: iterations summed over converged cells */
+    long long fallbacks;       /* Newton solvers: cells that fell back to the passes  */
+    int max_newton_iters;      /* Newton solvers: most iterations one cell needed     */
+    int solver;                /* REPROBUS_SOLVER_* used                              */
 } reprobus_stats;
 
 /* ---- diagnostics layout (reprobus_chem_rates_*) ----------------------------
@@ -123,6 +133,17 @@ int reprobus_chem_free(void* handle);
 /* Makes the handle launch on the caller's CUDA stream (a cudaStream_t passed
  * as void*; NULL restores the handle's own stream). */
 int reprobus_chem_set_stream(void* handle, void* cuda_stream);
+
+/* Selects how the cells are integrated (default REPROBUS_SOLVER_REF5).
+ * The Newton solvers return the fixed point of the reference's pass map
+ * (:1350-2372) -- the step the reference's iteration approximates with its
+ * 5 passes: npass reference passes from the start state, then Newton on the
+ * equations generated from the pass (reprobus_gb300/codegen/gen_newton.py)
+ * until the largest step relative to max(|x|, 1e-20 hnm) is below tol, at
+ * most maxit iterations; a cell that does not converge falls back to the
+ * reference's niter passes and is counted in stats.fallbacks.
+ * Defaults: npass 1, maxit 12, tol 1e-10. No counterpart in the reference. */
+int reprobus_chem_set_solver(void* handle, int solver, int npass, int maxit, double tol);
 
 /* One 15-min chemistry step for latitude rows ilat0..ilat1 (1-based,
  * inclusive), HOST arrays: copies the rows in, integrates, copies them back.

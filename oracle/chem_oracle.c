@@ -33,6 +33,7 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <stdio.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -1392,6 +1393,174 @@ static void orc_pass(const orc_grid* g, double dt, work* w) {
 }
 
 /* ============================================================================
+ * Oracle-C: the fixed point of one pass of the iteration (F:1350-2372),
+ * G(x) = x with x = (ck(1..42), cc(1..15)), by Newton's method on
+ * F(x) = G(x) - x. The Jacobian of G is taken by forward differences of the
+ * pass itself (all cells of the block perturbed at once: cells are
+ * independent within a pass), each cell's 57x57 system is solved by LU with
+ * partial pivoting, and a step that does not reduce max|F|/scale is halved
+ * (up to 8 times). Converged when |G(x) - x| is below tol relative to
+ * max(|x|, 1e-40*hnm) for every unknown (the night NO2 fixed point sits near
+ * 1e-30 molecules/cm3, inside the max(NO2, 1e-30) of F:1722, and NO3
+ * depends on which side of that clamp NO2 is).
+ * ========================================================================== */
+#define NX (NBCON - 1 + NCM)
+
+static void get_x(const work* w, size_t c, double* x) {
+    for (int m = 0; m < NBCON - 1; m++) x[m] = w->ck[c + w->n * m];
+    for (int m = 0; m < NCM; m++) x[NBCON - 1 + m] = w->cc[c + w->n * m];
+}
+static void put_x(work* w, size_t c, const double* x) {
+    for (int m = 0; m < NBCON - 1; m++) w->ck[c + w->n * m] = x[m];
+    for (int m = 0; m < NCM; m++) w->cc[c + w->n * m] = x[NBCON - 1 + m];
+}
+
+/* G for every cell of the block at the states X (n x NX), into GX */
+static void block_map(const orc_grid* g, double dt, work* w, const double* X, double* GX) {
+    for (size_t c = 0; c < w->n; c++) put_x(w, c, X + c * NX);
+    orc_pass(g, dt, w);
+    for (size_t c = 0; c < w->n; c++) get_x(w, c, GX + c * NX);
+}
+
+static int lu_solve(double* A, double* b, int n) {
+    /* A row-major n x n, overwritten; b overwritten with the solution */
+    for (int k = 0; k < n; k++) {
+        int p = k;
+        double best = fabs(A[k * n + k]);
+        for (int i = k + 1; i < n; i++)
+            if (fabs(A[i * n + k]) > best) best = fabs(A[i * n + k]), p = i;
+        if (!(best > 0.)) return -1;
+        if (p != k) {
+            for (int j = 0; j < n; j++) {
+                double t = A[k * n + j];
+                A[k * n + j] = A[p * n + j];
+                A[p * n + j] = t;
+            }
+            double t = b[k];
+            b[k] = b[p];
+            b[p] = t;
+        }
+        for (int i = k + 1; i < n; i++) {
+            double f = A[i * n + k] / A[k * n + k];
+            if (f == 0.) continue;
+            for (int j = k; j < n; j++) A[i * n + j] -= f * A[k * n + j];
+            b[i] -= f * b[k];
+        }
+    }
+    for (int k = n - 1; k >= 0; k--) {
+        double s = b[k];
+        for (int j = k + 1; j < n; j++) s -= A[k * n + j] * b[j];
+        b[k] = s / A[k * n + k];
+    }
+    return 0;
+}
+
+static int g_fnorm_arg = -1;
+static const double g_floor = 1e-40;
+static double fnorm(const double* x, const double* gx, const double* floorv) {
+    double m = 0.;
+    for (int i = 0; i < NX; i++) {
+        double s = fmax(fabs(x[i]), floorv[i]);
+        double r = fabs(gx[i] - x[i]) / s;
+        if (!(r <= m)) m = r, g_fnorm_arg = i; /* NaN propagates as failure */
+    }
+    return m;
+}
+
+static void orc_newton_block(const orc_grid* g, double dt, work* w, int* iters, double* res) {
+    const size_t n = w->n;
+    double* X = (double*)malloc(sizeof(double) * n * NX);
+    double* GX = (double*)malloc(sizeof(double) * n * NX);
+    double* XP = (double*)malloc(sizeof(double) * n * NX);
+    double* GP = (double*)malloc(sizeof(double) * n * NX);
+    double* J = (double*)malloc(sizeof(double) * n * NX * NX);
+    double* FL = (double*)malloc(sizeof(double) * n * NX);
+    double* H = (double*)malloc(sizeof(double) * n * NX);
+    int* done = (int*)calloc(n, sizeof(int));
+    for (size_t c = 0; c < n; c++) {
+        get_x(w, c, X + c * NX);
+        for (int i = 0; i < NX; i++) FL[c * NX + i] = g_floor * w->hnm[c];
+        iters[c] = 0;
+    }
+    const int maxit = g->maxiter > 0 ? g->maxiter : 60;
+    for (int it = 0; it < maxit; it++) {
+        block_map(g, dt, w, X, GX);
+        int active = 0;
+        for (size_t c = 0; c < n; c++) {
+            if (done[c]) continue;
+            if (fnorm(X + c * NX, GX + c * NX, FL + c * NX) < g->tol) {
+                done[c] = 1;
+                continue;
+            }
+            active++;
+        }
+        if (!active) break;
+        /* forward-difference Jacobian of G, column j for all cells at once */
+        for (int j = 0; j < NX; j++) {
+            memcpy(XP, X, sizeof(double) * n * NX);
+            for (size_t c = 0; c < n; c++) {
+                double xj = X[c * NX + j];
+                double h = 1e-7 * fmax(fabs(xj), FL[c * NX + j] * 1e5);
+                H[c * NX + j] = h;
+                XP[c * NX + j] = xj + h;
+            }
+            block_map(g, dt, w, XP, GP);
+            for (size_t c = 0; c < n; c++)
+                for (int i = 0; i < NX; i++)
+                    J[(c * NX + i) * NX + j] = (GP[c * NX + i] - GX[c * NX + i]) / H[c * NX + j];
+        }
+        /* Newton steps (J_G - I) d = -(G - x), with halving */
+        for (size_t c = 0; c < n; c++) {
+            if (done[c]) continue;
+            double* A = J + c * NX * NX;
+            double b[NX], x0[NX];
+            for (int i = 0; i < NX; i++) {
+                A[i * NX + i] -= 1.;
+                b[i] = -(GX[c * NX + i] - X[c * NX + i]);
+                x0[i] = X[c * NX + i];
+            }
+            if (lu_solve(A, b, NX) != 0) {
+                done[c] = -1;
+                continue;
+            }
+            for (int i = 0; i < NX; i++) X[c * NX + i] = x0[i] + b[i];
+            iters[c] = it + 1;
+            memcpy(XP + c * NX, x0, sizeof(double) * NX);  /* keep the previous iterate */
+        }
+        /* halve steps that increase the residual */
+        block_map(g, dt, w, X, GP);
+        for (int half = 0; half < 8; half++) {
+            int any = 0;
+            for (size_t c = 0; c < n; c++) {
+                if (done[c]) continue;
+                double fn_new = fnorm(X + c * NX, GP + c * NX, FL + c * NX);
+                double fn_old = fnorm(XP + c * NX, GX + c * NX, FL + c * NX);
+                if (!(fn_new <= fn_old) && fn_new > g->tol) {
+                    for (int i = 0; i < NX; i++)
+                        X[c * NX + i] = 0.5 * (X[c * NX + i] + XP[c * NX + i]);
+                    any = 1;
+                }
+            }
+            if (!any) break;
+            block_map(g, dt, w, X, GP);
+        }
+    }
+    block_map(g, dt, w, X, GX);
+    for (size_t c = 0; c < n; c++) {
+        res[c] = fnorm(X + c * NX, GX + c * NX, FL + c * NX);
+        if (done[c] != 1 && !(res[c] < g->tol)) {
+            iters[c] = -abs(iters[c]) - 1;
+            if (getenv("ORC_DEBUG")) {
+                int a = g_fnorm_arg;
+                fprintf(stderr, "cell %zu comp %d x %.3e gx %.3e hnm %.3e\n", c, a, X[c * NX + a], GX[c * NX + a], w->hnm[c]);
+            }
+        }
+        put_x(w, c, X + c * NX); /* the iterate itself, not one more pass */
+    }
+    free(X); free(GX); free(XP); free(GP); free(J); free(FL); free(H); free(done);
+}
+
+/* ============================================================================
  * chem3d, F:601-2412 — one block of nl longitudes of row ilat
  * ========================================================================== */
 static int orc_chem3d_block(const orc_grid* g, work* w, int ilat, int i0, double daynum, double dt,
@@ -1500,9 +1669,33 @@ static int orc_chem3d_block(const orc_grid* g, work* w, int ilat, int i0, double
 #undef DG
             }
     }
+    /* ---- map-residual mode: one pass from the given state x ---- */
+    if (g->x_qj1 && g->x_hc) {
+        for (int m = 0; m < NBCON - 1; m++)
+            for (int k = 0; k < nb; k++)
+                for (int i = 0; i < nl; i++) w->ck[R(i, k) + n * m] = G4(g->x_qj1, i0 + i, ilat, k, m) * w->hnm[R(i, k)];
+        for (int m = 0; m < NCM; m++)
+            for (int k = 0; k < nb; k++)
+                for (int i = 0; i < nl; i++) w->cc[R(i, k) + n * m] = G4(g->x_hc, i0 + i, ilat, k, m) * w->hnm[R(i, k)];
+        double* X0 = (double*)malloc(sizeof(double) * n * NX);
+        for (size_t c = 0; c < n; c++) get_x(w, c, X0 + c * NX);
+        orc_pass(g, dt, w);
+        for (size_t c = 0; c < n; c++) {
+            double gx[NX], fl[NX];
+            get_x(w, c, gx);
+            for (int q = 0; q < NX; q++) fl[q] = 1e-20 * w->hnm[c];
+            if (g->cellres) {
+                const size_t cell = (size_t)(i0 + c % nl) + (size_t)g->nlon * ((size_t)ilat + (size_t)g->nlat * (c / nl));
+                g->cellres[cell] = fnorm(X0 + c * NX, gx, fl);
+            }
+        }
+        free(X0);
+    }
     /* ---- iteration, F:1348-2378 ---- */
     int passes = 0;
-    if (g->niter > 0) {
+    if (g->x_qj1 && g->x_hc) {
+        passes = 1;
+    } else if (g->niter > 0) {
         for (int it = 0; it < g->niter; it++) orc_pass(g, dt, w);
         passes = g->niter;
     } else {
@@ -1525,6 +1718,20 @@ static int orc_chem3d_block(const orc_grid* g, work* w, int ilat, int i0, double
             }
             if (dmax < g->tol) break;
         }
+    }
+    if (g->newton) {
+        /* Oracle-C: from the passes' result, Newton to the fixed point */
+        int* it = (int*)malloc(sizeof(int) * n);
+        double* res = (double*)malloc(sizeof(double) * n);
+        orc_newton_block(g, dt, w, it, res);
+        for (int k = 0; k < nb; k++)
+            for (int i = 0; i < nl; i++) {
+                const size_t cell = (size_t)(i0 + i) + (size_t)g->nlon * ((size_t)ilat + (size_t)g->nlat * k);
+                if (g->cellstat) g->cellstat[cell] = it[R(i, k)];
+                if (g->cellres) g->cellres[cell] = res[R(i, k)];
+            }
+        free(it);
+        free(res);
     }
     /* ---- write-back, F:2380-2410 ---- */
     for (int m = 0; m < NBCON - 1; m++)

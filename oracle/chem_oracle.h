@@ -32,6 +32,14 @@ typedef struct orc_grid {
     const double* ajl;     /* ajl(40,101,27,7)                                   */
     const double* o3up;    /* o3up(0:79)                                         */
     double troe[18];       /* COMMON /constant/                                  */
+    int newton;            /* 1: after niter passes, Newton on the pass map to tol */
+    int* cellstat;         /* nullable, per chemistry cell (diag layout): Newton
+                              iterations, negative when not converged            */
+    double* cellres;       /* nullable, per chemistry cell: final max|G(x)-x|/scale */
+    const double* x_qj1;   /* nullable: evaluate one pass G at the state x =    */
+    const double* x_hc;    /* (x_qj1, x_hc) (mixing ratios, full arrays) instead
+                              of iterating; cellres gets max|G(x)-x|/scale and
+                              qj1/hc get G(x)                                     */
 } orc_grid;
 
 /* const, :5927-5948 — fills the 18 Troe prefactors. */

@@ -34,6 +34,9 @@ class OrcGrid(ctypes.Structure):
         ("niter", ctypes.c_int), ("tol", ctypes.c_double), ("maxiter", ctypes.c_int),
         ("ajl", ctypes.POINTER(ctypes.c_double)), ("o3up", ctypes.POINTER(ctypes.c_double)),
         ("troe", ctypes.c_double * 18),
+        ("newton", ctypes.c_int), ("cellstat", ctypes.POINTER(ctypes.c_int)),
+        ("cellres", ctypes.POINTER(ctypes.c_double)),
+        ("x_qj1", ctypes.POINTER(ctypes.c_double)), ("x_hc", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -68,8 +71,11 @@ def troe():
     return out
 
 
-def grid(case, niter=5, tol=0.0, maxiter=0, troe_vals=None):
+def grid(case, niter=5, tol=0.0, maxiter=0, troe_vals=None, newton=False, cellstat=None, cellres=None):
     g = OrcGrid()
+    g.cellres = cellres.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) if cellres is not None else None
+    g.newton = int(bool(newton))
+    g.cellstat = cellstat.ctypes.data_as(ctypes.POINTER(ctypes.c_int)) if cellstat is not None else None
     g.nlon, g.nlat, g.niv = case.nlon, case.nlat, case.niv
     g.nivbas, g.nivhau, g.nrappmax = case.nivbas, case.nivhau, case.nrappmax
     g.niter, g.tol, g.maxiter = niter, tol, maxiter
@@ -88,6 +94,39 @@ def step(case, niter=5, fuse=True, diag=False, nthreads=0, ilat0=1, ilat1=None, 
     ilat0/ilat1 are 1-based inclusive rows. Returns (state, diag or None, passes)."""
     L = lib()
     g = grid(case, niter=niter, tol=tol, maxiter=maxiter)
+    return _run(L, g, case, fuse, diag, nthreads, ilat0, ilat1, state)
+
+
+def step_fixed_point(case, tol=1e-13, maxiter=60, fuse=True, nthreads=0, ilat0=1, ilat1=None, state=None):
+    """Oracle-C: the fixed point of the reference's pass map (5 passes, then
+    Newton on G(x) - x). Returns (state, cellstat, cellres): per chemistry cell
+    (diag layout) the Newton iterations (negative: not converged to tol) and
+    the final max |G(x) - x| / max(|x|, 1e-25 hnm)."""
+    L = lib()
+    stat = np.zeros(case.nlon * case.nlat * case.nivbas, dtype=np.int32)
+    res = np.zeros(case.nlon * case.nlat * case.nivbas)
+    g = grid(case, niter=5, tol=tol, maxiter=maxiter, newton=True, cellstat=stat, cellres=res)
+    st, _, _ = _run(L, g, case, fuse, False, nthreads, ilat0, ilat1, state)
+    return st, stat, res
+
+
+def map_residual(case, qj1, hc, nthreads=0):
+    """One pass of the reference's map (F:1350-2372) evaluated at the state
+    x = (qj1, hc) (mixing ratios; the step's start state still defines ck0 and
+    the rates). Returns per chemistry cell (diag layout)
+    max_i |G(x)_i - x_i| / max(|x_i|, 1e-20 hnm): zero at a fixed point."""
+    L = lib()
+    res = np.full(case.nlon * case.nlat * case.nivbas, np.nan)
+    g = grid(case, niter=1, cellres=res)
+    qx = np.asfortranarray(qj1)
+    hx = np.asfortranarray(hc)
+    g.x_qj1 = _p(qx)
+    g.x_hc = _p(hx)
+    _run(L, g, case, False, False, nthreads, 1, None, None)
+    return res
+
+
+def _run(L, g, case, fuse, diag, nthreads, ilat0, ilat1, state):
     st = case.state_copy() if state is None else state
     ilat1 = case.nlat if ilat1 is None else ilat1
     dg = None

@@ -17,7 +17,7 @@ LIB = os.path.join(HERE, "libreprobus_gb300.so")
 PROBE = os.path.join(HERE, "pipe_probe")  # throughput probe behind the roofline notes
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["chem_kernels.cu"]
-HEADERS = ["chem_cell.cuh"]
+HEADERS = ["chem_cell.cuh", "chem_enums.h", "newton_gen.cuh", "newton_solve.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-diag-suppress", "550"]
 if os.environ.get("REPROBUS_FMAD", "1") == "0":

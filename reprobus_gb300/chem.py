@@ -28,6 +28,7 @@ LIBPATH = os.path.join(HERE, "libreprobus_gb300.so")
 
 FUSE_CONSERV = 0x1
 CHECK_FINITE = 0x2
+SOLVER_REF5, SOLVER_NEWTON64, SOLVER_NEWTON_MIXED = 0, 1, 2
 
 ERRORS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NONFINITE", 4: "ERR_NOCONV", 5: "ERR_TIMEOUT",
           6: "ERR_NODEVICE"}
@@ -36,7 +37,7 @@ ERRORS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NONFINITE", 4: "ERR_NOCO
 EXPORTS = [
     "reprobus_version", "reprobus_last_error", "reprobus_chem_troe", "reprobus_chem_init",
     "reprobus_chem_free", "reprobus_chem_set_stream", "reprobus_chem_step", "reprobus_chem_step_dev",
-    "reprobus_chem_rates_dev", "reprobus_conserv_dev", "reprobus_chem_step_noalloc",
+    "reprobus_chem_rates_dev", "reprobus_conserv_dev", "reprobus_chem_step_noalloc", "reprobus_chem_set_solver",
 ]
 NOALLOC_SCRATCH_DOUBLES = 1 << 20
 
@@ -49,7 +50,9 @@ class ReprobusError(RuntimeError):
 
 class Stats(ctypes.Structure):
     _fields_ = [("ncells", ctypes.c_longlong), ("nonfinite", ctypes.c_longlong),
-                ("kernel_launches", ctypes.c_int), ("passes", ctypes.c_int), ("device_ms", ctypes.c_double)]
+                ("kernel_launches", ctypes.c_int), ("passes", ctypes.c_int), ("device_ms", ctypes.c_double),
+                ("newton_iters", ctypes.c_longlong), ("fallbacks", ctypes.c_longlong),
+                ("max_newton_iters", ctypes.c_int), ("solver", ctypes.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -75,6 +78,7 @@ def load_library(path: str = LIBPATH):
     lib.reprobus_chem_init.argtypes = [dp, dp, dp, i, i, i, i, i, i, i, i, ctypes.POINTER(vp)]
     lib.reprobus_chem_free.argtypes = [vp]
     lib.reprobus_chem_set_stream.argtypes = [vp, vp]
+    lib.reprobus_chem_set_solver.argtypes = [vp, i, i, i, d]
     step_args = [vp, i, i, d, d, vp, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp, vp, ctypes.POINTER(Stats)]
     lib.reprobus_chem_step.argtypes = step_args
     lib.reprobus_chem_step_dev.argtypes = step_args
@@ -159,6 +163,12 @@ class ChemStep:
             self.close()
         except Exception:
             pass
+
+    def set_solver(self, solver, npass=1, maxit=12, tol=1e-10):
+        """SOLVER_REF5 (the reference's fixed passes), SOLVER_NEWTON64 or
+        SOLVER_NEWTON_MIXED (fixed point of the pass map by Newton)."""
+        _check(self.lib.reprobus_chem_set_solver(self._h, solver, npass, maxit, float(tol)))
+        self.solver = solver
 
     def set_stream(self, stream):
         """stream: a torch.cuda.Stream, a raw cudaStream_t int, or None."""

@@ -23,6 +23,7 @@
 
 #include "../../include/reprobus_chem.h"
 #include "chem_cell.cuh"
+#include "newton_solve.cuh"
 
 using namespace rpb;
 
@@ -70,8 +71,11 @@ struct Params {
     const double* __restrict__ ajl;
     const double* __restrict__ o3up;
     double* col;               // scratch: o3t | colo2 | colno (ncell each) | sza_top (ncol)
-    unsigned long long* nonfinite;
+    unsigned long long* nonfinite;  // [0] non-finite values, [1] Newton iterations,
+                                    // [2] fallbacks, [3] max iterations of a cell
     double* diag;
+    int npass, maxit;               // Newton: reference passes before, iteration cap
+    double tol;                     // Newton: scaled step tolerance
     StepConst sc;
 };
 
@@ -130,23 +134,34 @@ __global__ void __launch_bounds__(128) k_columns(Params P) {
 }
 
 // ----------------------------------------------------------------------------
-// k_chem — one cell per thread. DIAG: rate stage only, diagnostics out.
+// rate stage of one cell (F:800-1338): everything chem3d computes before its
+// iteration. Shared by the fixed-pass kernel and the Newton kernels.
 // ----------------------------------------------------------------------------
+struct CellPro {
+    CellFix F;
+    double ck0[NBCON];
+    double cc0[NCM];
+    double tj[NPHOT];
+    double K[NRATE];
+    Aerosol A;
+    double o3t;
+    size_t g;
+    int k;
+};
+
 template <bool DIAG>
-__global__ void __launch_bounds__(128) k_chem(Params P) {
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= P.ncell) return;
+__device__ __forceinline__ void cell_prologue(const Params& P, int cell, CellPro& C) {
     const int i = cell % P.nlon;
     const int rest = cell / P.nlon;
     const int col = cell % P.ncol;
     const int k = rest / P.nrows;
     const int j = P.ilat0 + rest % P.nrows;
     const size_t g = (size_t)i + (size_t)P.nlon * ((size_t)j + (size_t)P.nlat * k);
-    const size_t gb = g;  // (nlon,nlat,nivbas) arrays share the index for k < nivbas
     const size_t pl = plane3(P);
-
-    // ---- setup F:800-833 ----
-    CellFix F;
+    C.g = g;
+    C.k = k;
+    CellFix& F = C.F;
+    // setup F:800-833
     const double t = P.trajtem[P.trajoff + g];
     const double pm = P.trajpre[P.trajoff + g];
     F.hnm = P.trajpre[P.trajoff + g] / (P.trajtem[P.trajoff + g] * 1.38e-19);
@@ -154,31 +169,23 @@ __global__ void __launch_bounds__(128) k_chem(Params P) {
     F.o2 = 0.21 * F.hnm;
     F.co2 = 360.e-6 * F.hnm;
     F.h2 = 5.e-7 * F.hnm;
-    double ck0[NBCON], ck[NBCON], cc[NCM];
 #pragma unroll
-    for (int n = 0; n < NBCON; n++) {
-        ck0[n] = P.qj1[g + pl * n] * F.hnm;
-        ck[n] = ck0[n];
-    }
+    for (int n = 0; n < NBCON; n++) C.ck0[n] = P.qj1[g + pl * n] * F.hnm;
 #pragma unroll
-    for (int n = 0; n < NCM; n++) cc[n] = P.hc[g + pl * n] * F.hnm;
-
-    // ---- zenith F:845-851 ----
+    for (int n = 0; n < NCM; n++) C.cc0[n] = P.hc[g + pl * n] * F.hnm;
+    // zenith F:845-851
     F.sza = cell_zenith(P.sc, P.trajlon[P.trajoff + g], P.trajlat[P.trajoff + g]);
-    if (!DIAG) P.sza3d[gb] = F.sza;
-
-    // ---- phot + jno F:857, F:5043-5146 ----
-    double tj[NPHOT];
+    if (!DIAG) P.sza3d[g] = F.sza;
+    // phot + jno F:857, F:5043-5146
 #pragma unroll
-    for (int n = 0; n < NPHOT; n++) tj[n] = 0.;
-    const double o3t = P.col[cell];
-    if (F.sza <= 95.) cell_phot(P.ajl, P.o3up, P.alt[g], F.sza, o3t, tj);
+    for (int n = 0; n < NPHOT; n++) C.tj[n] = 0.;
+    C.o3t = P.col[cell];
+    if (F.sza <= 95.) cell_phot(P.ajl, P.o3up, P.alt[g], F.sza, C.o3t, C.tj);
     const double sza_top = P.col[3 * (size_t)P.ncell + col];
     if (sza_top <= 89.0)
-        tj[J_no] = cell_jno(sza_top, F.hnm, P.col[(size_t)P.ncell + cell], P.col[2 * (size_t)P.ncell + cell], o3t);
-
-    // ---- heterogeneous init + analytic F:864-912 ----
-    Aerosol A;
+        C.tj[J_no] = cell_jno(sza_top, F.hnm, P.col[(size_t)P.ncell + cell], P.col[2 * (size_t)P.ncell + cell], C.o3t);
+    // heterogeneous init + analytic F:864-912
+    Aerosol& A = C.A;
 #pragma unroll
     for (int m = 0; m < 9; m++) A.het[m] = 0.;
     A.parthno3 = 1.;
@@ -188,7 +195,7 @@ __global__ void __launch_bounds__(128) k_chem(Params P) {
     A.vsed = 0.;
     A.surf = 0.;
     if (k >= P.nivhau - 1) {
-        cell_aerosol(t, pm, F.hnm, ck, A);
+        cell_aerosol(t, pm, F.hnm, C.ck0, A);
         if (!DIAG) P.surfarea[g] = A.surf;
     }
     F.parthno3 = A.parthno3;
@@ -196,39 +203,15 @@ __global__ void __launch_bounds__(128) k_chem(Params P) {
     F.parthcl = A.parthcl;
     F.parthbr = 1.;
     if (!DIAG) {
-        P.vsed3d[gb] = A.vsed;
-        P.parth2osed[gb] = A.parth2o;
-        P.parthno3sed[gb] = A.parthno3sl;
+        P.vsed3d[g] = A.vsed;
+        P.parth2osed[g] = A.parth2o;
+        P.parthno3sed[g] = A.parthno3sl;
     }
-
-    // ---- rate constants F:920-1306 ----
-    double K[NRATE];
-    cell_rates(P.sc.troe, t, F.hnm, pm, K);
-
-    if (DIAG) {
-        const size_t nc = (size_t)P.ncell;
-        double* d = P.diag + cell;
-        d[REPROBUS_DIAG_HNM * nc] = F.hnm;
-        d[REPROBUS_DIAG_SZA * nc] = F.sza;
-        d[REPROBUS_DIAG_O3T * nc] = o3t;
-#pragma unroll
-        for (int n = 0; n < NPHOT; n++) d[(REPROBUS_DIAG_TJ + n) * nc] = tj[n];
-#pragma unroll
-        for (int m = 0; m < 9; m++) d[(REPROBUS_DIAG_HET + m) * nc] = A.het[m];
-        d[REPROBUS_DIAG_PARTHNO3 * nc] = A.parthno3;
-        d[REPROBUS_DIAG_PARTHNO3SL * nc] = A.parthno3sl;
-        d[REPROBUS_DIAG_PARTH2O * nc] = A.parth2o;
-        d[REPROBUS_DIAG_PARTHCL * nc] = A.parthcl;
-        d[REPROBUS_DIAG_VSED * nc] = A.vsed;
-        d[REPROBUS_DIAG_SURFAREA * nc] = A.surf;
-#pragma unroll
-        for (int n = 0; n < NRATE; n++) d[(REPROBUS_DIAG_RATE + n) * nc] = K[n];
-        return;
-    }
-
-    // ---- rainout F:1315-1338 ----
+    // rate constants F:920-1306
+    cell_rates(P.sc.troe, t, F.hnm, pm, C.K);
+    // rainout F:1315-1338
     const double rain_rate = 1.e-6;
-    const bool rain = ck[2] / F.hnm >= 100.e-6;
+    const bool rain = C.ck0[2] / F.hnm >= 100.e-6;
     F.rain_hno3 = rain ? rain_rate : 0.;
     F.rain_hno4 = 0.;
     F.rain_hcl = rain ? rain_rate : 0.;
@@ -236,22 +219,18 @@ __global__ void __launch_bounds__(128) k_chem(Params P) {
     F.rain_h2o2 = rain ? rain_rate : 0.;
     F.rain_ch2o = 0.;
     F.rain_ch3o2h = 0.;
+}
 
-    // ---- fixed-point passes F:1348-2378 ----
-#pragma unroll 1
-    for (int it = 0; it < P.niter; it++) cell_pass(F, K, tj, A.het, ck0, P.sc.dt, ck, cc);
-
-    // ---- write-back F:2380-2410 ----
+// write-back F:2380-2410, then (fused) conserv F:2539-2613 and clamps F:431-440
+__device__ __forceinline__ void cell_epilogue(const Params& P, const CellPro& C, const double* ck, const double* cc) {
+    const size_t pl = plane3(P);
     double q[NBCON], h[NCM];
 #pragma unroll
-    for (int n = 0; n < NBCON - 1; n++) q[n] = ck[n] / F.hnm;
-    q[NBCON - 1] = ck[4] * F.parthno3 / F.hnm;
+    for (int n = 0; n < NBCON - 1; n++) q[n] = ck[n] / C.F.hnm;
+    q[NBCON - 1] = ck[4] * C.F.parthno3 / C.F.hnm;
 #pragma unroll
-    for (int n = 0; n < NCM; n++) h[n] = cc[n] / F.hnm;
-    if (P.fuse) {
-        // conserv F:2539-2613 reads the 43 written-back slots
-        cell_conserv(q, h);
-    }
+    for (int n = 0; n < NCM; n++) h[n] = cc[n] / C.F.hnm;
+    if (P.fuse) cell_conserv(q, h);
     if (P.check) {
         unsigned int bad = 0;
 #pragma unroll
@@ -261,14 +240,122 @@ __global__ void __launch_bounds__(128) k_chem(Params P) {
         if (bad) atomicAdd(P.nonfinite, (unsigned long long)bad);
     }
     if (P.fuse) {
-        // clamps F:431-440
 #pragma unroll
         for (int n = 0; n < NBCON - 1; n++) q[n] = fmax(q[n], 1.e-30);
     }
 #pragma unroll
-    for (int n = 0; n < NBCON; n++) P.qj1[g + pl * n] = q[n];
+    for (int n = 0; n < NBCON; n++) P.qj1[C.g + pl * n] = q[n];
 #pragma unroll
-    for (int n = 0; n < NCM; n++) P.hc[g + pl * n] = h[n];
+    for (int n = 0; n < NCM; n++) P.hc[C.g + pl * n] = h[n];
+}
+
+// ----------------------------------------------------------------------------
+// k_chem — one cell per thread. DIAG: rate stage only, diagnostics out.
+// ----------------------------------------------------------------------------
+template <bool DIAG>
+__global__ void __launch_bounds__(128) k_chem(Params P) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= P.ncell) return;
+    CellPro C;
+    cell_prologue<DIAG>(P, cell, C);
+    const CellFix& F = C.F;
+    const Aerosol& A = C.A;
+    if (DIAG) {
+        const size_t nc = (size_t)P.ncell;
+        double* d = P.diag + cell;
+        d[REPROBUS_DIAG_HNM * nc] = F.hnm;
+        d[REPROBUS_DIAG_SZA * nc] = F.sza;
+        d[REPROBUS_DIAG_O3T * nc] = C.o3t;
+#pragma unroll
+        for (int n = 0; n < NPHOT; n++) d[(REPROBUS_DIAG_TJ + n) * nc] = C.tj[n];
+#pragma unroll
+        for (int m = 0; m < 9; m++) d[(REPROBUS_DIAG_HET + m) * nc] = A.het[m];
+        d[REPROBUS_DIAG_PARTHNO3 * nc] = A.parthno3;
+        d[REPROBUS_DIAG_PARTHNO3SL * nc] = A.parthno3sl;
+        d[REPROBUS_DIAG_PARTH2O * nc] = A.parth2o;
+        d[REPROBUS_DIAG_PARTHCL * nc] = A.parthcl;
+        d[REPROBUS_DIAG_VSED * nc] = A.vsed;
+        d[REPROBUS_DIAG_SURFAREA * nc] = A.surf;
+#pragma unroll
+        for (int n = 0; n < NRATE; n++) d[(REPROBUS_DIAG_RATE + n) * nc] = C.K[n];
+        return;
+    }
+    double ck[NBCON], cc[NCM];
+#pragma unroll
+    for (int n = 0; n < NBCON; n++) ck[n] = C.ck0[n];
+#pragma unroll
+    for (int n = 0; n < NCM; n++) cc[n] = C.cc0[n];
+    // fixed-point passes F:1348-2378
+#pragma unroll 1
+    for (int it = 0; it < P.niter; it++) cell_pass(F, C.K, C.tj, A.het, C.ck0, P.sc.dt, ck, cc);
+    cell_epilogue(P, C, ck, cc);
+}
+
+// ----------------------------------------------------------------------------
+// k_newton — one cell per thread: the fixed point of the reference's pass map
+// by Newton's method on the generated equations (newton_solve.cuh), Jacobian
+// and LU in TJ (double: plain FP64 solver; float: mixed precision), residual
+// and update in FP64. Start: P.npass reference passes from the step's start
+// state. A cell that does not converge within P.maxit iterations falls back
+// to the reference scheme (P.niter passes from the start state).
+// ----------------------------------------------------------------------------
+template <typename TJ>
+__global__ void __launch_bounds__(128) k_newton(Params P) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= P.ncell) return;
+    CellPro C;
+    cell_prologue<false>(P, cell, C);
+    const CellFix& F = C.F;
+    double ck[NBCON], cc[NCM];
+#pragma unroll
+    for (int n = 0; n < NBCON; n++) ck[n] = C.ck0[n];
+#pragma unroll
+    for (int n = 0; n < NCM; n++) cc[n] = C.cc0[n];
+#pragma unroll 1
+    for (int it = 0; it < P.npass; it++) cell_pass(F, C.K, C.tj, C.A.het, C.ck0, P.sc.dt, ck, cc);
+    NtIn in;
+    in.F.o2 = F.o2; in.F.n2 = F.n2; in.F.h2 = F.h2; in.F.co2 = F.co2; in.F.hnm = F.hnm;
+    in.F.parthno3 = F.parthno3; in.F.parth2o = F.parth2o; in.F.parthcl = F.parthcl; in.F.parthbr = F.parthbr;
+    in.F.rain_hno3 = F.rain_hno3; in.F.rain_hcl = F.rain_hcl; in.F.rain_hbr = F.rain_hbr;
+    in.F.rain_h2o2 = F.rain_h2o2; in.F.dt = P.sc.dt;
+    in.K = C.K; in.tj = C.tj; in.het = C.A.het; in.ck0 = C.ck0; in.day = F.sza <= 95.;
+    NtFixT<TJ> FT;
+    FT.o2 = (TJ)F.o2; FT.n2 = (TJ)F.n2; FT.h2 = (TJ)F.h2; FT.co2 = (TJ)F.co2; FT.hnm = (TJ)F.hnm;
+    FT.parthno3 = (TJ)F.parthno3; FT.parth2o = (TJ)F.parth2o; FT.parthcl = (TJ)F.parthcl;
+    FT.parthbr = (TJ)F.parthbr; FT.rain_hno3 = (TJ)F.rain_hno3; FT.rain_hcl = (TJ)F.rain_hcl;
+    FT.rain_hbr = (TJ)F.rain_hbr; FT.rain_h2o2 = (TJ)F.rain_h2o2; FT.dt = (TJ)P.sc.dt;
+    TJ KT[NRATE], tjT[NPHOT], hetT[9];
+#pragma unroll
+    for (int n = 0; n < NRATE; n++) KT[n] = (TJ)C.K[n];
+#pragma unroll
+    for (int n = 0; n < NPHOT; n++) tjT[n] = (TJ)C.tj[n];
+#pragma unroll
+    for (int n = 0; n < 9; n++) hetT[n] = (TJ)C.A.het[n];
+    double x[NT_NX];
+#pragma unroll
+    for (int n = 0; n < NBCON - 1; n++) x[n] = ck[n];
+#pragma unroll
+    for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = cc[n];
+    double last;
+    const int its = nt_newton<TJ>(in, KT, tjT, hetT, FT, x, P.maxit, P.tol, &last);
+    if (its > 0) {
+#pragma unroll
+        for (int n = 0; n < NBCON - 1; n++) ck[n] = x[n];
+#pragma unroll
+        for (int n = 0; n < NCM; n++) cc[n] = x[NBCON - 1 + n];
+        atomicAdd(P.nonfinite + 1, (unsigned long long)its);
+        atomicMax(P.nonfinite + 3, (unsigned long long)its);
+    } else {
+        // fallback: the reference scheme from the start state
+#pragma unroll
+        for (int n = 0; n < NBCON; n++) ck[n] = C.ck0[n];
+#pragma unroll
+        for (int n = 0; n < NCM; n++) cc[n] = C.cc0[n];
+#pragma unroll 1
+        for (int it = 0; it < P.niter; it++) cell_pass(F, C.K, C.tj, C.A.het, C.ck0, P.sc.dt, ck, cc);
+        atomicAdd(P.nonfinite + 2, 1ULL);
+    }
+    cell_epilogue(P, C, ck, cc);
 }
 
 // ----------------------------------------------------------------------------
@@ -325,6 +412,9 @@ __global__ void k_conserv(Params P) {
 struct Handle {
     int nlon, nlat, niv, nivbas, nivhau, nrappmax, niter, flags;
     int device;
+    int solver = REPROBUS_SOLVER_REF5;  // which kernel integrates the cells
+    int npass = 1, maxit = 12;          // Newton: reference passes before, iteration cap
+    double tol = 1e-10;                 // Newton: scaled step tolerance
     double troe[18];
     double* d_ajl = nullptr;
     double* d_o3up = nullptr;
@@ -427,7 +517,7 @@ extern "C" int reprobus_chem_init(const double* ajl, const double* o3up, const d
         (e = cudaMalloc(&h->d_ajl, najl * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&h->d_o3up, 80 * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&h->d_col, (3 * ncell + ncol) * sizeof(double))) != cudaSuccess ||
-        (e = cudaMalloc(&h->d_count, sizeof(unsigned long long))) != cudaSuccess ||
+        (e = cudaMalloc(&h->d_count, 4 * sizeof(unsigned long long))) != cudaSuccess ||
         (e = cudaMemcpy(h->d_ajl, ajl, najl * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(h->d_o3up, o3up, 80 * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
         return fail(set_err(REPROBUS_ERR_CUDA, "init: %s", cudaGetErrorString(e)));
@@ -493,6 +583,9 @@ static void fill_params(const Handle* h, Params& P, int ilat0, int ilat1) {
     P.o3up = h->d_o3up;
     P.col = h->d_col;
     P.nonfinite = h->d_count;
+    P.npass = h->npass;
+    P.maxit = h->maxit;
+    P.tol = h->tol;
 }
 
 // enqueue the kernels of one step on h->stream (device arrays in P)
@@ -501,11 +594,17 @@ static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
     int launches = 0;
     P.fuse = (h->flags & REPROBUS_FUSE_CONSERV) ? 1 : 0;
     P.check = (h->flags & REPROBUS_CHECK_FINITE) ? 1 : 0;
-    if (P.check) CUDA_TRY(cudaMemsetAsync(h->d_count, 0, sizeof(unsigned long long), h->stream));
+    const bool counters = P.check || h->solver != REPROBUS_SOLVER_REF5;
+    if (counters) CUDA_TRY(cudaMemsetAsync(h->d_count, 0, 4 * sizeof(unsigned long long), h->stream));
     if (st) CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
     k_columns<<<(P.ncol + tb - 1) / tb, tb, 0, h->stream>>>(P);
     launches++;
-    k_chem<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    if (h->solver == REPROBUS_SOLVER_NEWTON64)
+        k_newton<double><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    else if (h->solver == REPROBUS_SOLVER_NEWTON_MIXED)
+        k_newton<float><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    else
+        k_chem<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     launches++;
     if (P.fuse && h->nivbas < h->niv) {
         long long nt = (long long)P.nlon * P.nrows * (h->niv - h->nivbas);
@@ -521,16 +620,38 @@ static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
         st->device_ms = ms;
         st->ncells = P.ncell;
         st->kernel_launches = launches;
-        st->passes = h->niter;
+        st->passes = h->solver == REPROBUS_SOLVER_REF5 ? h->niter : h->npass;
         st->nonfinite = 0;
+        st->newton_iters = 0;
+        st->fallbacks = 0;
+        st->max_newton_iters = 0;
+        st->solver = h->solver;
     }
-    if (P.check) {
-        unsigned long long bad = 0;
-        CUDA_TRY(cudaMemcpyAsync(&bad, h->d_count, sizeof(bad), cudaMemcpyDeviceToHost, h->stream));
+    if (counters && (st || P.check)) {
+        unsigned long long c[4] = {0, 0, 0, 0};
+        CUDA_TRY(cudaMemcpyAsync(c, h->d_count, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
         CUDA_TRY(cudaStreamSynchronize(h->stream));
-        if (st) st->nonfinite = (long long)bad;
-        if (bad) return set_err(REPROBUS_ERR_NONFINITE, "%llu non-finite values in the step output", bad);
+        if (st) {
+            st->nonfinite = (long long)c[0];
+            st->newton_iters = (long long)c[1];
+            st->fallbacks = (long long)c[2];
+            st->max_newton_iters = (int)c[3];
+        }
+        if (P.check && c[0]) return set_err(REPROBUS_ERR_NONFINITE, "%llu non-finite values in the step output", c[0]);
     }
+    return REPROBUS_OK;
+}
+
+extern "C" int reprobus_chem_set_solver(void* handle, int solver, int npass, int maxit, double tol) {
+    Handle* h = (Handle*)handle;
+    if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
+    if (solver < REPROBUS_SOLVER_REF5 || solver > REPROBUS_SOLVER_NEWTON_MIXED)
+        return set_err(REPROBUS_ERR_ARG, "unknown solver %d", solver);
+    if (npass < 0 || maxit < 1 || !(tol > 0.)) return set_err(REPROBUS_ERR_ARG, "bad npass/maxit/tol");
+    h->solver = solver;
+    h->npass = npass;
+    h->maxit = maxit;
+    h->tol = tol;
     return REPROBUS_OK;
 }
 
