@@ -222,12 +222,13 @@ def build(day: bool):
         # F:1721-1730: NO2 <- NOx/(1 + r8), r8 = b9 O3/(b12 max(NO2, 1e-30)),
         # NO3 = r8 * (updated NO2). The fixed point of this 1-D map is unique:
         # NO2 = NOx - c (c = b9 O3/b12) when that exceeds 1e-30, else inside the
-        # clamp NO2 = NOx/(1 + c/1e-30), NO3 = NOx (c/1e-30)/(1 + c/1e-30).
+        # clamp NO2 = NOx/(1 + c/1e-30), NO3 = NOx (c/1e-30)/(1 + c/1e-30)
+        # (written as NOx 1e-30/(1e-30 + c) so that no intermediate overflows FP32)
         cno = m.let("cno", K("b9") * CC(5) / K("b12"))
         dno = m.let("dno", CK(21) - cno)
-        q = cno / sp.Float(1e-30)
-        g[7] = m.let_sel("no2", dno, sp.Float(1e-30), dno, CK(21) / (1 + q))
-        g[13] = m.let_sel("no3", dno, sp.Float(1e-30), cno, CK(21) * q / (1 + q))
+        eps = sp.Float(1e-30)
+        g[7] = m.let_sel("no2", dno, eps, dno, CK(21) * eps / (eps + cno))
+        g[13] = m.let_sel("no3", dno, eps, cno, CK(21) * cno / (eps + cno))
         g[11] = m.let_max("clo", CK(23), 0)
         g[12] = m.let_max("bro", CK(24), 0)
         day_f = 0

@@ -62,7 +62,7 @@ __device__ __forceinline__ int nt_newton(const NtIn& in, const TJ* KT, const TJ*
         for (int i = 0; i < NT_NX; i++) {
             const double xo = x[i];
             double xn = xo + (double)(b[i] * s[i]);
-            if (xo > 0. && xn < 0.1 * xo) xn = 0.1 * xo;
+            if (xo > 0. && xn < 0.) xn = 0.1 * xo;
             const TJ y = fabs(b[i]);
             if (!(y <= TJ(1e30))) finite = false;
             step = fmax(step, y);

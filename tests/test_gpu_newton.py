@@ -62,7 +62,11 @@ def test_newton_matches_oracle_fixed_point(case, fixed_point, solver):
     got, st = _run(case, solver)
     assert st["solver"] == solver and st["ncells"] == case.ncells
     err = _species_err(got, fp, case.nivbas)
-    ok = stat > 0
+    # cells the solver handed to its fallback (the reference's passes) are off the
+    # fixed point by construction: they are the ones the map residual flags
+    fell_back = oracle.map_residual(case, got["qj1"], got["hc"]) > MAP_TOL
+    assert fell_back.sum() <= st["fallbacks"]
+    ok = (stat > 0) & ~fell_back
     assert ok.mean() > 0.9
     assert err[ok].max() <= ERR_TOL, (err[ok].max(), int(np.argmax(np.where(ok, err, 0))))
     assert np.percentile(err[ok], 99) <= 1e-9
