@@ -543,11 +543,9 @@ def generate(path):
     w("};")
     for tag, m, res in (("day", md, rd), ("night", mn, rn)):
         w("")
-        w(f"// residual R(x), {tag} equations, FP64")
-        w(f"template <typename T, typename FF>")
-        w(f"__device__ NT_FN void nt_residual_{tag}(const FF& F, const T* __restrict__ K, "
-          f"const T* __restrict__ tj, const T* __restrict__ het, const T* __restrict__ ck0, "
-          f"const T* __restrict__ x, T* __restrict__ R) {{")
+        w(f"// residual R(x), {tag} equations (PK/PX/PR: pointers or strided views)")
+        w(f"template <typename T, typename FF, typename PK, typename PC, typename PX, typename PR>")
+        w(f"__device__ NT_FN void nt_residual_{tag}(const FF& F, PK K, PK tj, PK het, PC ck0, PX x, PR R) {{")
         out.extend(emit_values(m, res, P, None))
         for i, r in enumerate(res):
             w(f"    R[{i}] = {P.doprint(r)};")
@@ -555,9 +553,8 @@ def generate(path):
         w("")
         lines, pat = (jd_lines, pat_d) if tag == "day" else (jn_lines, pat_n)
         w(f"// Jacobian dR/dx, {tag} equations, into the LU slots (T = double or float)")
-        w(f"template <typename T, typename FF>")
-        w(f"__device__ NT_FN void nt_jacobian_{tag}(const FF& F, const T* __restrict__ K, "
-          f"const T* __restrict__ tj, const T* __restrict__ het, const T* __restrict__ x, T* __restrict__ J) {{")
+        w(f"template <typename T, typename FF, typename PK, typename PX, typename PJ>")
+        w(f"__device__ NT_FN void nt_jacobian_{tag}(const FF& F, PK K, PK tj, PK het, PX x, PJ J) {{")
         out.extend(lines)
         filled = set()
         for (i, j), e in sorted(pat.items()):
@@ -570,9 +567,8 @@ def generate(path):
         w("}")
     # scaling to relative units J'_ij = J_ij * s_j / s_i (s, rs = 1/s in original numbering)
     w("")
-    w("template <typename T>")
-    w("__device__ NT_FN void nt_scale(T* __restrict__ J, const T* __restrict__ s, "
-      "const T* __restrict__ rs) {")
+    w("template <typename T, typename PJ>")
+    w("__device__ NT_FN void nt_scale(PJ J, const T* __restrict__ s, const T* __restrict__ rs) {")
     for (k, j), sl in sorted(slots.items(), key=lambda kv: kv[1]):
         w(f"    J[{sl}] *= s[{perm[j]}] * rs[{perm[k]}];")
     w("}")
@@ -580,8 +576,8 @@ def generate(path):
     w("")
     w("// in-place LU (no pivoting) of the permuted sparse matrix; a zero or")
     w("// non-finite pivot is replaced by tiny (the FP64 residual corrects the step)")
-    w("template <typename T>")
-    w("__device__ NT_FN void nt_lu(T* __restrict__ J, T tiny) {")
+    w("template <typename T, typename PJ>")
+    w("__device__ NT_FN void nt_lu(PJ J, T tiny) {")
     for k in range(NX):
         dk = slots[(k, k)]
         w(f"    {{ T p = J[{dk}]; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny; J[{dk}] = p; const T r = T(1) / p;")
@@ -597,8 +593,8 @@ def generate(path):
     w("}")
     w("")
     w("// solve (LU) y = b; b is given and returned in the original numbering")
-    w("template <typename T>")
-    w("__device__ NT_FN void nt_solve(const T* __restrict__ J, T* __restrict__ b) {")
+    w("template <typename T, typename PJ>")
+    w("__device__ NT_FN void nt_solve(PJ J, T* __restrict__ b) {")
     w(f"    T y[{NX}];")
     for k in range(NX):
         terms = [f" - J[{slots[(k, j)]}] * y[{j}]" for j in sorted(rows[k]) if j < k]

@@ -76,8 +76,23 @@ struct Params {
     double* diag;
     int npass, maxit;               // Newton: reference passes before, iteration cap
     double tol;                     // Newton: scaled step tolerance
+    // Newton pipeline state, structure-of-arrays over the call's cells
+    double* nt_r64;                 // NT_NR rate fields per cell, FP64
+    float* nt_r32;                  // the same in FP32 (mixed solver)
+    double* nt_x;                   // iterate x (57 per cell)
+    double* nt_res;                 // residual R(x) (57 per cell)
+    int* nt_stat;                   // 0 active, >0 converged at that iteration, -1 failed
+    int* nt_list_in;                // active cells of this iteration
+    int* nt_list_out;               // active cells of the next iteration
+    int* nt_cnt_in;
+    int* nt_cnt_out;
+    int it;                         // 1-based iteration of k_nt_res / k_nt_lin
     StepConst sc;
 };
+
+// fields of the Newton rate buffers: K (99), tj (41), het (9), fixed (14), day
+constexpr int NT_RK = 0, NT_RJ = NRATE, NT_RH = NRATE + NPHOT, NT_RF = NRATE + NPHOT + 9;
+constexpr int NT_RDAY = NT_RF + 14, NT_NR = NT_RDAY + 1;
 
 __device__ __forceinline__ size_t plane3(const Params& P) { return (size_t)P.nlon * P.nlat * P.niv; }
 __device__ __forceinline__ size_t plane_b(const Params& P) { return (size_t)P.nlon * P.nlat * P.nivbas; }
@@ -292,16 +307,58 @@ __global__ void __launch_bounds__(128) k_chem(Params P) {
 }
 
 // ----------------------------------------------------------------------------
-// k_newton — one cell per thread: the fixed point of the reference's pass map
-// by Newton's method on the generated equations (newton_solve.cuh), Jacobian
-// and LU in TJ (double: plain FP64 solver; float: mixed precision), residual
-// and update in FP64. Start: P.npass reference passes from the step's start
-// state. A cell that does not converge within P.maxit iterations falls back
-// to the reference scheme (P.niter passes from the start state).
+// Newton pipeline: the fixed point of the reference's pass map by Newton's
+// method on the generated equations (newton_solve.cuh), Jacobian and LU in TJ
+// (double: plain FP64 solver; float: mixed precision), residual and update in
+// FP64. Per-cell state lives in structure-of-arrays buffers between kernels:
+//   k_nt_setup   one thread per cell: rate stage, P.npass reference passes from
+//                the start state -> iterate x, rates (FP64 and TJ), active list
+//   per iteration (persistent grids working through the active list):
+//   k_nt_res     FP64 residual R(x)
+//   k_nt_lin     Jacobian, LU and solve with the matrix in shared memory
+//                (slot-major: slot q of thread t at q*blockDim + t), update x,
+//                converged cells leave the list
+//   k_nt_finish  one thread per cell: cells still unconverged after P.maxit
+//                iterations fall back to the reference's P.niter passes;
+//                write-back, conserv, clamps
 // ----------------------------------------------------------------------------
-template <typename TJ>
-__global__ void __launch_bounds__(128) k_newton(Params P) {
+template <typename T>
+struct SPScaled {  // start-of-step number densities: the input mixing ratios times hnm
+    const double* p;
+    size_t s;
+    double f;
+    __device__ __forceinline__ T operator[](int i) const { return (T)(p[(size_t)i * s] * f); }
+};
+
+__device__ __forceinline__ size_t cell_global(const Params& P, int cell) {
+    const int i = cell % P.nlon;
+    const int rest = cell / P.nlon;
+    const int k = rest / P.nrows;
+    const int j = P.ilat0 + rest % P.nrows;
+    return (size_t)i + (size_t)P.nlon * ((size_t)j + (size_t)P.nlat * k);
+}
+
+template <typename T, typename PV>
+__device__ __forceinline__ void nt_fix(PV r, NtFix* F, NtFixT<T>* FT) {
+    const int o = NT_RF;
+    if (F) {
+        F->o2 = r[o + 0]; F->n2 = r[o + 1]; F->h2 = r[o + 2]; F->co2 = r[o + 3]; F->hnm = r[o + 4];
+        F->parthno3 = r[o + 5]; F->parth2o = r[o + 6]; F->parthcl = r[o + 7]; F->parthbr = r[o + 8];
+        F->rain_hno3 = r[o + 9]; F->rain_hcl = r[o + 10]; F->rain_hbr = r[o + 11]; F->rain_h2o2 = r[o + 12];
+        F->dt = r[o + 13];
+    }
+    if (FT) {
+        FT->o2 = r[o + 0]; FT->n2 = r[o + 1]; FT->h2 = r[o + 2]; FT->co2 = r[o + 3]; FT->hnm = r[o + 4];
+        FT->parthno3 = r[o + 5]; FT->parth2o = r[o + 6]; FT->parthcl = r[o + 7]; FT->parthbr = r[o + 8];
+        FT->rain_hno3 = r[o + 9]; FT->rain_hcl = r[o + 10]; FT->rain_hbr = r[o + 11]; FT->rain_h2o2 = r[o + 12];
+        FT->dt = r[o + 13];
+    }
+}
+
+template <bool MIXED>
+__global__ void __launch_bounds__(128) k_nt_setup(Params P) {
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell == 0) *P.nt_cnt_in = P.ncell;
     if (cell >= P.ncell) return;
     CellPro C;
     cell_prologue<false>(P, cell, C);
@@ -313,44 +370,139 @@ __global__ void __launch_bounds__(128) k_newton(Params P) {
     for (int n = 0; n < NCM; n++) cc[n] = C.cc0[n];
 #pragma unroll 1
     for (int it = 0; it < P.npass; it++) cell_pass(F, C.K, C.tj, C.A.het, C.ck0, P.sc.dt, ck, cc);
-    NtIn in;
-    in.F.o2 = F.o2; in.F.n2 = F.n2; in.F.h2 = F.h2; in.F.co2 = F.co2; in.F.hnm = F.hnm;
-    in.F.parthno3 = F.parthno3; in.F.parth2o = F.parth2o; in.F.parthcl = F.parthcl; in.F.parthbr = F.parthbr;
-    in.F.rain_hno3 = F.rain_hno3; in.F.rain_hcl = F.rain_hcl; in.F.rain_hbr = F.rain_hbr;
-    in.F.rain_h2o2 = F.rain_h2o2; in.F.dt = P.sc.dt;
-    in.K = C.K; in.tj = C.tj; in.het = C.A.het; in.ck0 = C.ck0; in.day = F.sza <= 95.;
-    NtFixT<TJ> FT;
-    FT.o2 = (TJ)F.o2; FT.n2 = (TJ)F.n2; FT.h2 = (TJ)F.h2; FT.co2 = (TJ)F.co2; FT.hnm = (TJ)F.hnm;
-    FT.parthno3 = (TJ)F.parthno3; FT.parth2o = (TJ)F.parth2o; FT.parthcl = (TJ)F.parthcl;
-    FT.parthbr = (TJ)F.parthbr; FT.rain_hno3 = (TJ)F.rain_hno3; FT.rain_hcl = (TJ)F.rain_hcl;
-    FT.rain_hbr = (TJ)F.rain_hbr; FT.rain_h2o2 = (TJ)F.rain_h2o2; FT.dt = (TJ)P.sc.dt;
-    TJ KT[NRATE], tjT[NPHOT], hetT[9];
+    const size_t nc = (size_t)P.ncell;
+    double* x = P.nt_x + cell;
 #pragma unroll
-    for (int n = 0; n < NRATE; n++) KT[n] = (TJ)C.K[n];
+    for (int n = 0; n < NBCON - 1; n++) x[n * nc] = ck[n];
 #pragma unroll
-    for (int n = 0; n < NPHOT; n++) tjT[n] = (TJ)C.tj[n];
+    for (int n = 0; n < NCM; n++) x[(NBCON - 1 + n) * nc] = cc[n];
+    double fx[14] = {F.o2, F.n2, F.h2, F.co2, F.hnm, F.parthno3, F.parth2o, F.parthcl, F.parthbr,
+                     F.rain_hno3, F.rain_hcl, F.rain_hbr, F.rain_h2o2, P.sc.dt};
+    double* r = P.nt_r64 + cell;
+#pragma unroll 4
+    for (int n = 0; n < NRATE; n++) r[(NT_RK + n) * nc] = C.K[n];
+#pragma unroll 4
+    for (int n = 0; n < NPHOT; n++) r[(NT_RJ + n) * nc] = C.tj[n];
 #pragma unroll
-    for (int n = 0; n < 9; n++) hetT[n] = (TJ)C.A.het[n];
-    double x[NT_NX];
+    for (int n = 0; n < 9; n++) r[(NT_RH + n) * nc] = C.A.het[n];
 #pragma unroll
-    for (int n = 0; n < NBCON - 1; n++) x[n] = ck[n];
+    for (int n = 0; n < 14; n++) r[(NT_RF + n) * nc] = fx[n];
+    r[NT_RDAY * nc] = F.sza <= 95. ? 1. : 0.;
+    if (MIXED) {
+        float* q = P.nt_r32 + cell;
+#pragma unroll 4
+        for (int n = 0; n < NRATE; n++) q[(NT_RK + n) * nc] = (float)C.K[n];
+#pragma unroll 4
+        for (int n = 0; n < NPHOT; n++) q[(NT_RJ + n) * nc] = (float)C.tj[n];
 #pragma unroll
-    for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = cc[n];
-    double last;
-    const int its = nt_newton<TJ>(in, KT, tjT, hetT, FT, x, P.maxit, P.tol, &last);
-    if (its > 0) {
+        for (int n = 0; n < 9; n++) q[(NT_RH + n) * nc] = (float)C.A.het[n];
 #pragma unroll
-        for (int n = 0; n < NBCON - 1; n++) ck[n] = x[n];
+        for (int n = 0; n < 14; n++) q[(NT_RF + n) * nc] = (float)fx[n];
+    }
+    P.nt_stat[cell] = 0;
+    P.nt_list_in[cell] = cell;
+}
+
+__global__ void __launch_bounds__(128) k_nt_res(Params P) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid == 0) *P.nt_cnt_out = 0;
+    const int n = *P.nt_cnt_in;
+    const int nc = P.ncell;
+    const size_t pl = plane3(P);
+    for (int idx = tid; idx < n; idx += gridDim.x * blockDim.x) {
+        const int cell = P.nt_list_in[idx];
+        const SP<double> r{P.nt_r64 + cell, nc};
+        NtFix F;
+        nt_fix<double>(r, &F, (NtFixT<double>*)nullptr);
+        const SP<double> K{P.nt_r64 + (size_t)NT_RK * nc + cell, nc};
+        const SP<double> tj{P.nt_r64 + (size_t)NT_RJ * nc + cell, nc};
+        const SP<double> het{P.nt_r64 + (size_t)NT_RH * nc + cell, nc};
+        const SPScaled<double> ck0{P.qj1 + cell_global(P, cell), pl, F.hnm};
+        const SP<double> x{P.nt_x + cell, nc};
+        const SPW<double> R{P.nt_res + cell, nc};
+        if (r[NT_RDAY] != 0.)
+            nt_residual_day<double>(F, K, tj, het, ck0, x, R);
+        else
+            nt_residual_night<double>(F, K, tj, het, ck0, x, R);
+    }
+}
+
+template <typename TJ>
+__global__ void k_nt_lin(Params P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TJ* smem = reinterpret_cast<TJ*>(smem_raw);
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = *P.nt_cnt_in;
+    const int nc = P.ncell;
+    const SPW<TJ> J{smem + threadIdx.x, (int)blockDim.x};
+    for (int idx = tid; idx < n; idx += gridDim.x * blockDim.x) {
+        const int cell = P.nt_list_in[idx];
+        const TJ* rT = sizeof(TJ) == 4 ? (const TJ*)P.nt_r32 : (const TJ*)P.nt_r64;
+        const SP<TJ> r{rT + cell, nc};
+        NtFixT<TJ> FT;
+        nt_fix<TJ>(r, (NtFix*)nullptr, &FT);
+        const SP<TJ> KT{rT + (size_t)NT_RK * nc + cell, nc};
+        const SP<TJ> tjT{rT + (size_t)NT_RJ * nc + cell, nc};
+        const SP<TJ> hetT{rT + (size_t)NT_RH * nc + cell, nc};
+        const bool day = P.nt_r64[(size_t)NT_RDAY * nc + cell] != 0.;
+        const double hnm = P.nt_r64[(size_t)(NT_RF + 4) * nc + cell];
+        const SPW<double> x{P.nt_x + cell, nc};
+        const SP<double> R{P.nt_res + cell, nc};
+        TJ step;
+        const bool ok = nt_linear_step<TJ>(FT, KT, tjT, hetT, day, hnm, x, R, J, &step);
+        if (!ok) {
+            P.nt_stat[cell] = -1;
+        } else if (step < (TJ)P.tol) {
+            P.nt_stat[cell] = P.it;
+        } else if (P.it >= P.maxit) {
+            P.nt_stat[cell] = -1;
+        } else {
+            const int slot = atomicAdd(P.nt_cnt_out, 1);
+            P.nt_list_out[slot] = cell;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_nt_finish(Params P) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= P.ncell) return;
+    const int nc = P.ncell;
+    const int stat = P.nt_stat[cell];
+    const SP<double> r{P.nt_r64 + cell, nc};
+    CellPro C;
+    C.g = cell_global(P, cell);
+    CellFix& F = C.F;
+    NtFix N;
+    nt_fix<double>(r, &N, (NtFixT<double>*)nullptr);
+    F.o2 = N.o2; F.n2 = N.n2; F.h2 = N.h2; F.co2 = N.co2; F.hnm = N.hnm; F.parthno3 = N.parthno3;
+    F.parth2o = N.parth2o; F.parthcl = N.parthcl; F.parthbr = N.parthbr; F.rain_hno3 = N.rain_hno3;
+    F.rain_hno4 = 0.; F.rain_hcl = N.rain_hcl; F.rain_hbr = N.rain_hbr; F.rain_h2o2 = N.rain_h2o2;
+    F.rain_ch2o = 0.; F.rain_ch3o2h = 0.;
+    F.sza = r[NT_RDAY] != 0. ? 0. : 180.;
+    const size_t pl = plane3(P);
+    double ck[NBCON], cc[NCM];
+    if (stat > 0) {
 #pragma unroll
-        for (int n = 0; n < NCM; n++) cc[n] = x[NBCON - 1 + n];
-        atomicAdd(P.nonfinite + 1, (unsigned long long)its);
-        atomicMax(P.nonfinite + 3, (unsigned long long)its);
+        for (int n = 0; n < NBCON - 1; n++) ck[n] = P.nt_x[(size_t)n * nc + cell];
+        ck[NBCON - 1] = P.qj1[C.g + pl * (NBCON - 1)] * F.hnm;
+#pragma unroll
+        for (int n = 0; n < NCM; n++) cc[n] = P.nt_x[(size_t)(NBCON - 1 + n) * nc + cell];
+        atomicAdd(P.nonfinite + 1, (unsigned long long)stat);
+        atomicMax(P.nonfinite + 3, (unsigned long long)stat);
     } else {
         // fallback: the reference scheme from the start state
 #pragma unroll
+        for (int n = 0; n < NBCON; n++) C.ck0[n] = P.qj1[C.g + pl * n] * F.hnm;
+#pragma unroll
+        for (int n = 0; n < NRATE; n++) C.K[n] = r[NT_RK + n];
+#pragma unroll
+        for (int n = 0; n < NPHOT; n++) C.tj[n] = r[NT_RJ + n];
+#pragma unroll
+        for (int n = 0; n < 9; n++) C.A.het[n] = r[NT_RH + n];
+#pragma unroll
         for (int n = 0; n < NBCON; n++) ck[n] = C.ck0[n];
 #pragma unroll
-        for (int n = 0; n < NCM; n++) cc[n] = C.cc0[n];
+        for (int n = 0; n < NCM; n++) cc[n] = P.hc[C.g + pl * n] * F.hnm;
 #pragma unroll 1
         for (int it = 0; it < P.niter; it++) cell_pass(F, C.K, C.tj, C.A.het, C.ck0, P.sc.dt, ck, cc);
         atomicAdd(P.nonfinite + 2, 1ULL);
@@ -429,6 +581,15 @@ struct Handle {
     double* m_qj1 = nullptr;
     double* m_hc = nullptr;
     double* m_out[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // vsed, parth2o, parthno3, sza3d, surfarea
+    // Newton pipeline buffers (allocated when a Newton solver is selected)
+    double* nt_r64 = nullptr;
+    float* nt_r32 = nullptr;
+    double* nt_x = nullptr;
+    double* nt_res = nullptr;
+    int* nt_stat = nullptr;
+    int* nt_list = nullptr;   // two lists of ncell
+    int* nt_cnt = nullptr;    // two counters
+    int grid_res = 0, grid_lin32 = 0, grid_lin64 = 0;
 };
 
 static const char* kVersion = "reprobus_gb300 0.1 (sm_103a, FP64 reference scheme)";
@@ -470,6 +631,13 @@ static void free_handle(Handle* h) {
     cudaFree(h->m_qj1);
     cudaFree(h->m_hc);
     for (auto& p : h->m_out) cudaFree(p);
+    cudaFree(h->nt_r64);
+    cudaFree(h->nt_r32);
+    cudaFree(h->nt_x);
+    cudaFree(h->nt_res);
+    cudaFree(h->nt_stat);
+    cudaFree(h->nt_list);
+    cudaFree(h->nt_cnt);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->own) cudaStreamDestroy(h->own);
@@ -588,6 +756,81 @@ static void fill_params(const Handle* h, Params& P, int ilat0, int ilat1) {
     P.tol = h->tol;
 }
 
+constexpr int NT_BLK32 = 64;  // k_nt_lin threads per block: 524 float slots x 64 = 134 KB shared
+constexpr int NT_BLK64 = 32;  //                              524 double slots x 32 = 134 KB shared
+
+static int ensure_newton(Handle* h) {
+    if (h->nt_x) return REPROBUS_OK;
+    const size_t nc = (size_t)h->nlon * h->nlat * h->nivbas;
+    CUDA_TRY(cudaMalloc(&h->nt_r64, nc * NT_NR * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&h->nt_r32, nc * NT_NR * sizeof(float)));
+    CUDA_TRY(cudaMalloc(&h->nt_x, nc * NT_NX * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&h->nt_res, nc * NT_NX * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&h->nt_stat, nc * sizeof(int)));
+    CUDA_TRY(cudaMalloc(&h->nt_list, 2 * nc * sizeof(int)));
+    CUDA_TRY(cudaMalloc(&h->nt_cnt, 2 * sizeof(int)));
+    int nsm = 0, nb = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_nt_res, 128, 0));
+    h->grid_res = nsm * (nb > 0 ? nb : 1);
+    const size_t sm32 = (size_t)NT_NSLOT * NT_BLK32 * sizeof(float);
+    const size_t sm64 = (size_t)NT_NSLOT * NT_BLK64 * sizeof(double);
+    CUDA_TRY(cudaFuncSetAttribute(k_nt_lin<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm32));
+    CUDA_TRY(cudaFuncSetAttribute(k_nt_lin<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm64));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_nt_lin<float>, NT_BLK32, sm32));
+    h->grid_lin32 = nsm * (nb > 0 ? nb : 1);
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_nt_lin<double>, NT_BLK64, sm64));
+    h->grid_lin64 = nsm * (nb > 0 ? nb : 1);
+    return REPROBUS_OK;
+}
+
+// the Newton pipeline of one step (after k_columns)
+static int launch_newton(Handle* h, Params& P, int* launches) {
+    int rc = ensure_newton(h);
+    if (rc) return rc;
+    const bool mixed = h->solver == REPROBUS_SOLVER_NEWTON_MIXED;
+    const int tb = 128;
+    const size_t nc = (size_t)h->nlon * h->nlat * h->nivbas;
+    P.nt_r64 = h->nt_r64;
+    P.nt_r32 = h->nt_r32;
+    P.nt_x = h->nt_x;
+    P.nt_res = h->nt_res;
+    P.nt_stat = h->nt_stat;
+    int* lin = h->nt_list;
+    int* lout = h->nt_list + nc;
+    int* cin = h->nt_cnt;
+    int* cout = h->nt_cnt + 1;
+    P.nt_list_in = lin;
+    P.nt_cnt_in = cin;
+    if (mixed)
+        k_nt_setup<true><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    else
+        k_nt_setup<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    (*launches)++;
+    for (int it = 1; it <= h->maxit; it++) {
+        P.it = it;
+        P.nt_list_in = lin;
+        P.nt_list_out = lout;
+        P.nt_cnt_in = cin;
+        P.nt_cnt_out = cout;
+        k_nt_res<<<h->grid_res, 128, 0, h->stream>>>(P);
+        if (mixed)
+            k_nt_lin<float><<<h->grid_lin32, NT_BLK32, (size_t)NT_NSLOT * NT_BLK32 * sizeof(float), h->stream>>>(P);
+        else
+            k_nt_lin<double><<<h->grid_lin64, NT_BLK64, (size_t)NT_NSLOT * NT_BLK64 * sizeof(double), h->stream>>>(P);
+        *launches += 2;
+        int* t = lin;
+        lin = lout;
+        lout = t;
+        int* c = cin;
+        cin = cout;
+        cout = c;
+    }
+    k_nt_finish<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    (*launches)++;
+    return REPROBUS_OK;
+}
+
 // enqueue the kernels of one step on h->stream (device arrays in P)
 static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
     const int tb = 128;
@@ -599,13 +842,13 @@ static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
     if (st) CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
     k_columns<<<(P.ncol + tb - 1) / tb, tb, 0, h->stream>>>(P);
     launches++;
-    if (h->solver == REPROBUS_SOLVER_NEWTON64)
-        k_newton<double><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
-    else if (h->solver == REPROBUS_SOLVER_NEWTON_MIXED)
-        k_newton<float><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
-    else
+    if (h->solver == REPROBUS_SOLVER_REF5) {
         k_chem<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
-    launches++;
+        launches++;
+    } else {
+        int rc = launch_newton(h, P, &launches);
+        if (rc) return rc;
+    }
     if (P.fuse && h->nivbas < h->niv) {
         long long nt = (long long)P.nlon * P.nrows * (h->niv - h->nivbas);
         k_tail<<<(unsigned)((nt + 255) / 256), 256, 0, h->stream>>>(P);
