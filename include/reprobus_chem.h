@@ -68,6 +68,11 @@ typedef struct reprobus_stats {
     long long fallbacks;       /* Newton solvers: cells that fell back to the passes  */
     int max_newton_iters;      /* Newton solvers: most iterations one cell needed     */
     int solver;                /* REPROBUS_SOLVER_* used                              */
+    int lanes_per_block;       /* Newton solvers: cells in flight per block of the
+                                  persistent solve kernel (autotuned or set)         */
+    int blocks_per_sm;         /* Newton solvers: resident blocks of it per SM        */
+    int z_shared;              /* Newton solvers: 1 when the kernel keeps the right-
+                                  hand side in shared memory, 0 in registers         */
 } reprobus_stats;
 
 /* ---- diagnostics layout (reprobus_chem_rates_*) ----------------------------
@@ -144,6 +149,16 @@ int reprobus_chem_set_stream(void* handle, void* cuda_stream);
  * reference's niter passes and is counted in stats.fallbacks.
  * Defaults: npass 1, maxit 12, tol 1e-10. No counterpart in the reference. */
 int reprobus_chem_set_solver(void* handle, int solver, int npass, int maxit, double tol);
+
+/* Shape of the persistent Newton solve kernel. lanes_per_block = 0 (default):
+ * the first Newton step of each matrix precision times every compiled shape
+ * (lanes per block x right-hand side in registers or shared memory x
+ * resident blocks per SM) on that step's own cells and keeps the fastest
+ * (synchronous, once per handle); > 0: use that many lanes per block (a
+ * compiled value: 64, 96, 128 for the mixed solver; 32, 64 for the FP64 one),
+ * zshared (0 or 1) and blocks_per_sm (0: as many as fit). No counterpart in
+ * the reference. */
+int reprobus_chem_set_tuning(void* handle, int lanes_per_block, int blocks_per_sm, int zshared);
 
 /* One 15-min chemistry step for latitude rows ilat0..ilat1 (1-based,
  * inclusive), HOST arrays: copies the rows in, integrates, copies them back.

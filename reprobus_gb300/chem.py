@@ -38,6 +38,7 @@ EXPORTS = [
     "reprobus_version", "reprobus_last_error", "reprobus_chem_troe", "reprobus_chem_init",
     "reprobus_chem_free", "reprobus_chem_set_stream", "reprobus_chem_step", "reprobus_chem_step_dev",
     "reprobus_chem_rates_dev", "reprobus_conserv_dev", "reprobus_chem_step_noalloc", "reprobus_chem_set_solver",
+    "reprobus_chem_set_tuning",
 ]
 NOALLOC_SCRATCH_DOUBLES = 1 << 20
 
@@ -52,7 +53,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("ncells", ctypes.c_longlong), ("nonfinite", ctypes.c_longlong),
                 ("kernel_launches", ctypes.c_int), ("passes", ctypes.c_int), ("device_ms", ctypes.c_double),
                 ("newton_iters", ctypes.c_longlong), ("fallbacks", ctypes.c_longlong),
-                ("max_newton_iters", ctypes.c_int), ("solver", ctypes.c_int)]
+                ("max_newton_iters", ctypes.c_int), ("solver", ctypes.c_int),
+                ("lanes_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int), ("z_shared", ctypes.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -79,6 +81,7 @@ def load_library(path: str = LIBPATH):
     lib.reprobus_chem_free.argtypes = [vp]
     lib.reprobus_chem_set_stream.argtypes = [vp, vp]
     lib.reprobus_chem_set_solver.argtypes = [vp, i, i, i, d]
+    lib.reprobus_chem_set_tuning.argtypes = [vp, i, i, i]
     step_args = [vp, i, i, d, d, vp, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp, vp, ctypes.POINTER(Stats)]
     lib.reprobus_chem_step.argtypes = step_args
     lib.reprobus_chem_step_dev.argtypes = step_args
@@ -169,6 +172,11 @@ class ChemStep:
         SOLVER_NEWTON_MIXED (fixed point of the pass map by Newton)."""
         _check(self.lib.reprobus_chem_set_solver(self._h, solver, npass, maxit, float(tol)))
         self.solver = solver
+
+    def set_tuning(self, lanes_per_block=0, blocks_per_sm=0, zshared=0):
+        """Shape of the persistent Newton solve kernel (lanes_per_block 0:
+        autotune on the first Newton step of each matrix precision)."""
+        _check(self.lib.reprobus_chem_set_tuning(self._h, int(lanes_per_block), int(blocks_per_sm), int(zshared)))
 
     def set_stream(self, stream):
         """stream: a torch.cuda.Stream, a raw cudaStream_t int, or None."""

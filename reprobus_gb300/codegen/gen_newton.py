@@ -410,70 +410,91 @@ class Printer(C99CodePrinter):
         return e.name
 
 
-def emit_values(m, res, P, cast_x):
-    lines = []
-    for kind, s, payload, g in m.stmts:
-        if kind == "let":
-            lines.append(f"    const T {s.name} = {P.doprint(payload)};")
-        elif kind == "sel":
-            lhs, rhs, a, b = payload
-            lines.append(f"    const T {s.name} = ({P.doprint(lhs)}) > ({P.doprint(rhs)}) ? T({P.doprint(a)}) : "
-                         f"T({P.doprint(b)});")
-        else:
-            a, b = payload
-            fn = "fmin" if kind == "min" else "fmax"
-            lines.append(f"    const T {s.name} = {fn}({P.doprint(a)}, {P.doprint(b)});")
-    return lines
+class XPrinter(Printer):
+    """Jacobian printer: the FP64 iterate x[j] is read where it is used and
+    rounded to T there (no long-lived copies of x in registers)."""
+
+    def _print_Symbol(self, e):
+        n = e.name
+        if n.startswith("x["):
+            return f"nt_cvt<T>({n})"
+        return n
 
 
-def emit_jacobian(m, res, P, slot):
-    lines = []
-    for kind, s, payload, g in m.stmts:
+def _cse(exprs, prefix, P, real="T"):
+    """sympy CSE of a list of expressions -> (definition lines, reduced list)."""
+    rep, red = sp.cse(exprs, symbols=sp.numbered_symbols(prefix))
+    return [f"    const {real} {s.name} = {P.doprint(e)};" for s, e in rep], red
+
+
+def emit_statements(m, P, derivs):
+    """The named intermediates (and, with derivs, their gradients), one chunk
+    of lines per statement, with common subexpressions (shared reciprocals
+    above all) evaluated once."""
+    chunks = []
+    for idx, (kind, s, payload, g) in enumerate(m.stmts):
+        lines = []
+        pre = f"{s.name}_c"
+        keys = sorted(g) if derivs else []
         if kind == "let":
-            lines.append(f"    const T {s.name} = {P.doprint(payload)};")
-            for j, e in sorted(g.items()):
+            defs, red = _cse([payload] + [g[j] for j in keys], pre, P)
+            lines += defs
+            lines.append(f"    const T {s.name} = {P.doprint(red[0])};")
+            for j, e in zip(keys, red[1:]):
                 lines.append(f"    const T d_{s.name}_{j} = {P.doprint(e)};")
-        elif kind == "sel":
+            chunks.append(lines)
+            continue
+        if kind == "sel":
             lhs, rhs, a, b = payload
-            lines.append(f"    const bool sel_{s.name} = ({P.doprint(lhs)}) > ({P.doprint(rhs)});")
-            lines.append(f"    const T {s.name} = sel_{s.name} ? T({P.doprint(a)}) : T({P.doprint(b)});")
-            for j, (ga, gb) in sorted(g.items()):
-                lines.append(f"    const T d_{s.name}_{j} = sel_{s.name} ? T({P.doprint(ga)}) : T({P.doprint(gb)});")
+            cond = (lhs, rhs, ">")
         else:
             a, b = payload
-            fn, cmp = ("fmin", "<=") if kind == "min" else ("fmax", ">=")
-            lines.append(f"    const T {s.name} = {fn}({P.doprint(a)}, {P.doprint(b)});")
-            lines.append(f"    const bool sel_{s.name} = ({P.doprint(a)}) {cmp} ({P.doprint(b)});")
-            for j, (ga, gb) in sorted(g.items()):
-                lines.append(f"    const T d_{s.name}_{j} = sel_{s.name} ? T({P.doprint(ga)}) : T({P.doprint(gb)});")
+            cond = (a, b, "<=" if kind == "min" else ">=")
+        exprs = [cond[0], cond[1], a, b] + [g[j][0] for j in keys] + [g[j][1] for j in keys]
+        defs, red = _cse(exprs, pre, P)
+        lines += defs
+        c0, c1, ra, rb = (P.doprint(e) for e in red[:4])
+        lines.append(f"    const bool sel_{s.name} = ({c0}) {cond[2]} ({c1});")
+        lines.append(f"    const T {s.name} = sel_{s.name} ? T({ra}) : T({rb});")
+        nk = len(keys)
+        for q, j in enumerate(keys):
+            ga, gb = P.doprint(red[4 + q]), P.doprint(red[4 + nk + q])
+            lines.append(f"    const T d_{s.name}_{j} = sel_{s.name} ? T({ga}) : T({gb});")
+        chunks.append(lines)
+    return chunks
+
+
+def ready_after(m, exprs):
+    """Index of the last statement whose value or gradient symbols the
+    expressions use (-1: none), so that each row is emitted as soon as it
+    can be and the intermediates it reads die early."""
+    names = {}
+    for idx, (_, s, _, g) in enumerate(m.stmts):
+        names[s.name] = idx
+        for j in g:
+            names[f"d_{s.name}_{j}"] = idx
+    last = -1
+    for e in exprs:
+        for u in sp.sympify(e).free_symbols:
+            if u.name in names:
+                last = max(last, names[u.name])
+    return last
+
+
+def jacobian_entries(m, res):
+    """(i, j) -> dR_i/dx_j in terms of the intermediates' gradient symbols."""
     pattern = {}
     for i, r in enumerate(res):
-        gr = m.gradient(r)
-        for j, e in sorted(gr.items()):
+        for j, e in sorted(m.gradient(r).items()):
             pattern[(i, j)] = e
-    return lines, pattern
+    return pattern
 
 
-def min_degree_order(nz, n):
-    """Minimum-degree ordering of the symmetrised pattern."""
-    adj = {i: set() for i in range(n)}
-    for (i, j) in nz:
-        if i != j:
-            adj[i].add(j)
-            adj[j].add(i)
-    order, left = [], set(range(n))
-    while left:
-        v = min(left, key=lambda u: (len(adj[u] & left), u))
-        order.append(v)
-        nb = adj[v] & left
-        for a in nb:
-            adj[a] |= nb - {a}
-        left.remove(v)
-    return order
-
-
-def lu_pattern(nz, perm, n):
-    """Fill pattern of LU without pivoting in the permuted order."""
+# --------------------------------------------------------------------------- #
+# elimination order and storage plan
+# --------------------------------------------------------------------------- #
+def filled_rows(nz, perm, n):
+    """Rows (in elimination positions) of the LU fill pattern without pivoting."""
     pos = {v: k for k, v in enumerate(perm)}
     rows = [set() for _ in range(n)]
     for (i, j) in nz:
@@ -481,56 +502,256 @@ def lu_pattern(nz, perm, n):
     for k in range(n):
         rows[k].add(k)
     for k in range(n):
+        rk = [j for j in rows[k] if j > k]
         for i in range(k + 1, n):
             if k in rows[i]:
-                rows[i] |= {j for j in rows[k] if j > k}
+                rows[i].update(rk)
     return rows
+
+
+def lu_updates(rows, n):
+    return sum(sum(1 for j in rows[k] if j > k) for i in range(n) for k in rows[i] if k < i)
+
+
+def markowitz_order(nz, n):
+    """Diagonal Markowitz ordering: eliminate next the unknown whose pivot has
+    the fewest (row count - 1)(column count - 1) in the active submatrix."""
+    R = {i: set() for i in range(n)}
+    C = {j: set() for j in range(n)}
+    for (i, j) in nz:
+        R[i].add(j)
+        C[j].add(i)
+    left, order = set(range(n)), []
+    while left:
+        def key(v):
+            r = len(R[v] & left) - 1
+            c = len(C[v] & left) - 1
+            return (r * c, r + c, v)
+        v = min(left, key=key)
+        order.append(v)
+        rs, cs = R[v] & left, C[v] & left
+        for i in cs - {v}:
+            for j in rs - {v}:
+                R[i].add(j)
+                C[j].add(i)
+        left.remove(v)
+    return order
+
+
+def refine_order(nz, n, perm, iters=4000, seed=1):
+    """Deterministic local search (move one unknown) that keeps any move which
+    does not increase the LU update count."""
+    import random
+    rnd = random.Random(seed)
+    cur = list(perm)
+    cost = lu_updates(filled_rows(nz, cur, n), n)
+    for _ in range(iters):
+        a, b = rnd.randrange(n), rnd.randrange(n)
+        if a == b:
+            continue
+        o = cur[:]
+        o.insert(b, o.pop(a))
+        c = lu_updates(filled_rows(nz, o, n), n)
+        if c <= cost:
+            cur, cost = o, c
+    return cur
+
+
+def storage_plan(nz, const, perm, rows, n):
+    """Shared-memory slots of one cell. The Jacobian writes every stored entry
+    of A (constant diagonal entries are not stored); row t of the row-by-row
+    (Crout) factorisation reads its A entries into registers and writes the
+    off-diagonal entries of the unit upper factor U~ into slots freed by rows
+    <= t (lowest free slot first), so the peak is what the plan needs."""
+    import heapq
+    pos = {v: k for k, v in enumerate(perm)}
+    arow = [[] for _ in range(n)]
+    for (i, j) in nz:
+        if (i, j) not in const:
+            arow[pos[i]].append(pos[j])
+    slot_a = {}
+    for t in range(n):
+        for c in sorted(arow[t]):
+            slot_a[(t, c)] = len(slot_a)
+    na = len(slot_a)
+    free, nxt, slot_u = [], na, {}
+    for t in range(n):
+        for c in arow[t]:
+            heapq.heappush(free, slot_a[(t, c)])
+        for j in sorted(c for c in rows[t] if c > t):
+            if free:
+                slot_u[(t, j)] = heapq.heappop(free)
+            else:
+                slot_u[(t, j)] = nxt
+                nxt += 1
+    return slot_a, slot_u, na, max(na, nxt)
+
+
+# --------------------------------------------------------------------------- #
+# emission
+# --------------------------------------------------------------------------- #
+def emit_residual(w, tag, m, res, P):
+    w("")
+    w(f"// residual R(x), {tag} equations (FP64; K/tj/het/ck0/x: pointers or views)")
+    w("template <typename T, typename FF, typename PK, typename PC, typename PX, typename PR>")
+    w(f"__device__ __forceinline__ void nt_residual_{tag}(const FF& F, PK K, PK tj, PK het, PC ck0, PX x, PR R) {{")
+    chunks = emit_statements(m, P, derivs=False)
+    at = {}
+    for i, r in enumerate(res):
+        at.setdefault(ready_after(m, [r]), []).append(i)
+    for idx in range(-1, len(chunks)):
+        if idx >= 0:
+            for line in chunks[idx]:
+                w(line)
+        for i in at.get(idx, []):
+            defs, red = _cse([res[i]], f"{tag[0]}r{i}_c", P)
+            for line in defs:
+                w(line)
+            w(f"    R[{i}] = {P.doprint(red[0])};")
+    w("}")
+
+
+def emit_jacobian(w, tag, m, pat, union, const, slot_a, pos, XP):
+    w("")
+    w(f"// scaled Jacobian J'_ij = dR_i/dx_j s_j / s_i, {tag} equations, into the")
+    w("// stored A slots (T = double or float; x: FP64 iterate; s: nt_exp_hi scales)")
+    w("template <typename T, typename FF, typename PK, typename PJ>")
+    w(f"__device__ __forceinline__ void nt_jacobian_{tag}(const FF& F, PK K, PK tj, PK het, "
+      "const double* __restrict__ x, double floor_, PJ J) {")
+    w("    const int fh = nt_exp_hi(floor_);")
+    chunks = emit_statements(m, XP, derivs=True)
+    by_row = {}
+    for (i, j) in sorted(union):
+        by_row.setdefault(i, []).append(j)
+    at = {}
+    for i in range(NX):
+        cols = by_row.get(i, [])
+        exprs = [pat.get((i, j), sp.Integer(0)) for j in cols]
+        at.setdefault(ready_after(m, exprs), []).append(i)
+        for j in cols:
+            if (i, j) in const:
+                v = pat.get((i, j), sp.Integer(0))
+                assert v == const[(i, j)], ((i, j), v)
+    for idx in range(-1, len(chunks)):
+        if idx >= 0:
+            for line in chunks[idx]:
+                w(line)
+        for i in at.get(idx, []):
+            stored = [j for j in by_row.get(i, []) if (i, j) not in const]
+            exprs = [pat.get((i, j), sp.Integer(0)) for j in stored]
+            defs, red = _cse(exprs, f"{tag[0]}j{i}_c", XP)
+            w(f"    {{  // row {i}")
+            w(f"    const T rs{i} = nt_rscale<T>(nt_exp_hi(x[{i}]), fh);")
+            for line in defs:
+                w("    " + line)
+            for j, e in zip(stored, red):
+                sl = slot_a[(pos[i], pos[j])]
+                if e == 0:
+                    w(f"        J[{sl}] = T(0);")
+                else:
+                    w(f"        J[{sl}] = ({XP.doprint(e)}) * (nt_scale<T>(nt_exp_hi(x[{j}]), fh) * rs{i});")
+            w("    }")
+    w("}")
+
+
+def emit_factor(w, perm, rows, slot_a, slot_u, const_pos, n):
+    Z = lambda i: f"z[{i}]"
+    w("")
+    w("// Crout factorisation, row by row in elimination order, of the stored scaled")
+    w("// matrix, with the forward substitution fused: row t is read into registers")
+    w("// w, reduced by the earlier unit-upper rows U~(k,:), its pivot p = w_t taken")
+    w("// (a zero or non-finite pivot replaced by +-tiny: the FP64 residual corrects")
+    w("// the step), z_t = (z_t - sum_k w_k z_k) / p and U~(t,j) = w_j / p stored;")
+    w("// then the back substitution. z (original numbering, registers or a view):")
+    w("// right-hand side in, solution out. L is never stored. NT_FENCE keeps each")
+    w("// row's shared-memory loads in that row (hoisted loads would hold registers).")
+    w("template <typename T, typename PJ, typename PZ>")
+    w("__device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {")
+    for t in range(n):
+        w("    NT_FENCE();")
+        w(f"    {{  // row {t}: unknown {perm[t]}")
+        for c in sorted(rows[t]):
+            if (t, c) in slot_a:
+                w(f"        T w{c} = J[{slot_a[(t, c)]}];")
+            elif c == t and t in const_pos:
+                w(f"        T w{c} = T({float(const_pos[t])!r});")
+            else:
+                w(f"        T w{c} = T(0);")
+        w(f"        T zt = {Z(perm[t])};")
+        for k in sorted(c for c in rows[t] if c < t):
+            w(f"        zt -= w{k} * {Z(perm[k])};")
+            for j in sorted(c for c in rows[k] if c > k):
+                w(f"        w{j} -= w{k} * J[{slot_u[(k, j)]}];")
+        w(f"        T p = w{t}; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;")
+        w("        const T d = T(1) / p;")
+        w(f"        {Z(perm[t])} = zt * d;")
+        for j in sorted(c for c in rows[t] if c > t):
+            w(f"        J[{slot_u[(t, j)]}] = w{j} * d;")
+        w("    }")
+    for t in range(n - 1, -1, -1):
+        terms = "".join(f" - J[{slot_u[(t, j)]}] * {Z(perm[j])}" for j in sorted(c for c in rows[t] if c > t))
+        if terms:
+            w("    NT_FENCE();")
+            w(f"    {Z(perm[t])} = {Z(perm[t])}{terms};")
+    w("}")
 
 
 def generate(path):
     md, rd = build(True)
     mn, rn = build(False)
     P = Printer("T")
-    jd_lines, pat_d = emit_jacobian(md, rd, P, None)
-    jn_lines, pat_n = emit_jacobian(mn, rn, P, None)
-    nz = set(pat_d) | set(pat_n) | {(i, i) for i in range(NX)}
-    perm = min_degree_order(nz, NX)
-    rows = lu_pattern(nz, perm, NX)
-    slots = {}
-    for k in range(NX):
-        for j in sorted(rows[k]):
-            slots[(k, j)] = len(slots)
-    nslot = len(slots)
+    XP = XPrinter("T")
+    pat_d = jacobian_entries(md, rd)
+    pat_n = jacobian_entries(mn, rn)
+    union = set(pat_d) | set(pat_n)
+    nz = union | {(i, i) for i in range(NX)}
+    # constant diagonal entries (the same number in the day and night equations)
+    const = {}
+    for (i, j) in nz:
+        a, b = pat_d.get((i, j), sp.Integer(0)), pat_n.get((i, j), sp.Integer(0))
+        if i == j and a.is_Number and b.is_Number and a == b and a != 0:
+            const[(i, j)] = a
+    perm = refine_order(nz, NX, markowitz_order(nz, NX))
+    rows = filled_rows(nz, perm, NX)
     pos = {v: k for k, v in enumerate(perm)}
-    nnz_orig = len(nz)
+    slot_a, slot_u, na, nslot = storage_plan(nz, const, perm, rows, NX)
+    const_pos = {pos[i]: v for (i, _), v in const.items()}
+    nupd = lu_updates(rows, NX)
+    nu = len(slot_u)
 
     out = []
     w = out.append
     w("// newton_gen.cuh — GENERATED by reprobus_gb300/codegen/gen_newton.py; do not edit.")
     w("//")
-    w("// Residual, analytic Jacobian and sparse LU of the chemistry step equations")
-    w("// (fixed point of one pass of src/reprobus_l137_20230723.f:1350-2372, in the")
-    w("// Jacobi form described in the generator). Unknowns x[0..41] = ck(1..42),")
+    w("// Residual, scaled analytic Jacobian and sparse Crout LU of the chemistry step")
+    w("// equations (fixed point of one pass of src/reprobus_l137_20230723.f:1350-2372,")
+    w("// in the Jacobi form described in the generator). Unknowns x[0..41] = ck(1..42),")
     w("// x[42..56] = cc(1..15).")
-    w(f"// Jacobian: {nnz_orig} structural non-zeros (day|night|diagonal); LU slots with fill: {nslot};")
-    w(f"// minimum-degree order: {perm}")
+    w(f"// Jacobian: {len(nz)} structural non-zeros (day|night|diagonal), {len(const)} of them constant")
+    w(f"// diagonal entries; stored A entries {na}; off-diagonal U~ entries {nu}; LU updates {nupd};")
+    w(f"// shared-memory slots per cell {nslot}.")
+    w(f"// elimination order (Markowitz, refined): {perm}")
     w("#pragma once")
     w("#ifndef __CUDACC__")
     w("#define __device__")
     w("#define __forceinline__ inline")
-    w("#define NT_FN inline")
-    w("#else")
-    w("#define NT_FN __noinline__  // each generated block gets its own register allocation")
     w("#endif")
+    w('#include "newton_num.cuh"')
     w("")
     w("namespace rpb {")
     w(f"constexpr int NT_NX = {NX};")
-    w(f"constexpr int NT_NSLOT = {nslot};")
-    w(f"constexpr int NT_NNZ = {nnz_orig};")
-    w(f"constexpr int NT_PERM[{NX}] = {{{', '.join(map(str, perm))}}};  // LU position k holds unknown NT_PERM[k]")
-    inv = {v: k for k, v in slots.items()}
-    w(f"constexpr int NT_SLOT_I[{nslot}] = {{{', '.join(str(perm[inv[s][0]]) for s in range(nslot))}}};")
-    w(f"constexpr int NT_SLOT_J[{nslot}] = {{{', '.join(str(perm[inv[s][1]]) for s in range(nslot))}}};")
+    w(f"constexpr int NT_NNZ = {len(nz)};")
+    w(f"constexpr int NT_NA = {na};        // stored entries of A (the Jacobian)")
+    w(f"constexpr int NT_NSLOT = {nslot};     // shared-memory matrix slots per cell")
+    w(f"constexpr int NT_NUPD = {nupd};     // multiply-adds of the factorisation")
+    w(f"constexpr int NT_PERM[{NX}] = {{{', '.join(map(str, perm))}}};  // elimination position k holds unknown NT_PERM[k]")
+    inv_a = {v: k for k, v in slot_a.items()}
+    w(f"constexpr int NT_A_I[{na}] = {{{', '.join(str(perm[inv_a[q][0]]) for q in range(na))}}};")
+    w(f"constexpr int NT_A_J[{na}] = {{{', '.join(str(perm[inv_a[q][1]]) for q in range(na))}}};")
+    ci = sorted(i for (i, _) in const)
+    w(f"constexpr int NT_NCONST = {len(ci)};")
+    w(f"constexpr int NT_CONST_I[{len(ci)}] = {{{', '.join(map(str, ci))}}};  // constant diagonal entries")
+    w(f"constexpr double NT_CONST_V[{len(ci)}] = {{{', '.join(repr(float(const[(i, i)])) for i in ci)}}};")
     w("")
     w("// per-cell constants of the equations")
     w("struct NtFix {")
@@ -541,77 +762,19 @@ def generate(path):
     w("    T o2, n2, h2, co2, hnm, parthno3, parth2o, parthcl, parthbr;")
     w("    T rain_hno3, rain_hcl, rain_hbr, rain_h2o2, dt;")
     w("};")
-    for tag, m, res in (("day", md, rd), ("night", mn, rn)):
-        w("")
-        w(f"// residual R(x), {tag} equations (PK/PX/PR: pointers or strided views)")
-        w(f"template <typename T, typename FF, typename PK, typename PC, typename PX, typename PR>")
-        w(f"__device__ NT_FN void nt_residual_{tag}(const FF& F, PK K, PK tj, PK het, PC ck0, PX x, PR R) {{")
-        out.extend(emit_values(m, res, P, None))
-        for i, r in enumerate(res):
-            w(f"    R[{i}] = {P.doprint(r)};")
-        w("}")
-        w("")
-        lines, pat = (jd_lines, pat_d) if tag == "day" else (jn_lines, pat_n)
-        w(f"// Jacobian dR/dx, {tag} equations, into the LU slots (T = double or float)")
-        w(f"template <typename T, typename FF, typename PK, typename PX, typename PJ>")
-        w(f"__device__ NT_FN void nt_jacobian_{tag}(const FF& F, PK K, PK tj, PK het, PX x, PJ J) {{")
-        out.extend(lines)
-        filled = set()
-        for (i, j), e in sorted(pat.items()):
-            sl = slots[(pos[i], pos[j])]
-            filled.add(sl)
-            w(f"    J[{sl}] = {P.doprint(e)};")
-        for sl in range(nslot):
-            if sl not in filled:
-                w(f"    J[{sl}] = T(0);")
-        w("}")
-    # scaling to relative units J'_ij = J_ij * s_j / s_i (s, rs = 1/s in original numbering)
     w("")
-    w("template <typename T, typename PJ>")
-    w("__device__ NT_FN void nt_scale(PJ J, const T* __restrict__ s, const T* __restrict__ rs) {")
-    for (k, j), sl in sorted(slots.items(), key=lambda kv: kv[1]):
-        w(f"    J[{sl}] *= s[{perm[j]}] * rs[{perm[k]}];")
-    w("}")
-    # LU factorisation and solve (permuted order; b in original numbering)
-    w("")
-    w("// in-place LU (no pivoting) of the permuted sparse matrix; a zero or")
-    w("// non-finite pivot is replaced by tiny (the FP64 residual corrects the step)")
-    w("template <typename T, typename PJ>")
-    w("__device__ NT_FN void nt_lu(PJ J, T tiny) {")
-    for k in range(NX):
-        dk = slots[(k, k)]
-        w(f"    {{ T p = J[{dk}]; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny; J[{dk}] = p; const T r = T(1) / p;")
-        for i in range(k + 1, NX):
-            if (i, k) in slots:
-                lik = slots[(i, k)]
-                w(f"      {{ const T l = J[{lik}] * r; J[{lik}] = l;")
-                for j in sorted(rows[k]):
-                    if j > k:
-                        w(f"        J[{slots[(i, j)]}] -= l * J[{slots[(k, j)]}];")
-                w("      }")
-        w("    }")
-    w("}")
-    w("")
-    w("// solve (LU) y = b; b is given and returned in the original numbering")
-    w("template <typename T, typename PJ>")
-    w("__device__ NT_FN void nt_solve(PJ J, T* __restrict__ b) {")
-    w(f"    T y[{NX}];")
-    for k in range(NX):
-        terms = [f" - J[{slots[(k, j)]}] * y[{j}]" for j in sorted(rows[k]) if j < k]
-        w(f"    y[{k}] = b[{perm[k]}]{''.join(terms)};")
-    for k in range(NX - 1, -1, -1):
-        terms = [f" - J[{slots[(k, j)]}] * y[{j}]" for j in sorted(rows[k]) if j > k]
-        w(f"    y[{k}] = (y[{k}]{''.join(terms)}) / J[{slots[(k, k)]}];")
-    for k in range(NX):
-        w(f"    b[{perm[k]}] = y[{k}];")
-    w("}")
+    for tag, m, res, pat in (("day", md, rd, pat_d), ("night", mn, rn, pat_n)):
+        emit_residual(w, tag, m, res, P)
+        emit_jacobian(w, tag, m, pat, union, const, slot_a, pos, XP)
+    emit_factor(w, perm, rows, slot_a, slot_u, const_pos, NX)
     w("}  // namespace rpb")
     with open(path, "w") as f:
         f.write("\n".join(out) + "\n")
-    return {"nnz": nnz_orig, "slots": nslot, "perm": perm}
+    return {"nnz": len(nz), "slots": nslot, "stored": na, "updates": nupd, "perm": perm}
 
 
 if __name__ == "__main__":
     target = os.path.join(os.path.dirname(HERE), "csrc", "newton_gen.cuh")
     info = generate(target)
-    print(f"wrote {target}: nnz {info['nnz']}, LU slots {info['slots']}")
+    print(f"wrote {target}: nnz {info['nnz']}, stored A {info['stored']}, slots {info['slots']}, "
+          f"LU updates {info['updates']}")

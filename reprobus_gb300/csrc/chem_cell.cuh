@@ -190,7 +190,7 @@ __constant__ double c_dens_x[23] = {0., 2.393284E-02, -4.359335E-05, 7.961181E-0
                                     -1.22336185E-06, 0.3455282, -2.2111E-03, 3.503768245E-06, -0.2315332,
                                     1.60074E-03, -2.5827835E-06};
 
-__device__ __noinline__ void cell_aerosol(double temp, double ptot, double hnm, const double* ck, Aerosol& A) {
+static __device__ __noinline__ void cell_aerosol(double temp, double ptot, double hnm, const double* ck, Aerosol& A) {
     const double r = 8.205e-5, sigma = 1.8;
     const double* qn = c_an_qn;
     const double* qs = c_an_qs;

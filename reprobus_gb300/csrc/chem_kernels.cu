@@ -19,11 +19,13 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <new>
 
 #include "../../include/reprobus_chem.h"
-#include "chem_cell.cuh"
-#include "newton_solve.cuh"
+#include "chem_params.cuh"
+#include "newton_gen.cuh"
+#include "newton_launch.h"
 
 using namespace rpb;
 
@@ -46,56 +48,6 @@ static int set_err(int code, const char* fmt, ...) {
         if (e_ != cudaSuccess) return set_err(REPROBUS_ERR_CUDA, "%s: %s (%s:%d)", #x, cudaGetErrorString(e_), \
                                               __FILE__, __LINE__);                                           \
     } while (0)
-
-// ----------------------------------------------------------------------------
-// kernel parameters
-// ----------------------------------------------------------------------------
-struct Params {
-    int nlon, nlat, niv, nivbas, nivhau;
-    int ilat0, nrows;          // 0-based first row, number of rows
-    long long trajoff;         // element offset of the irapp slice in traj*
-    int niter, fuse, check;
-    int ncell, ncol;           // nlon*nrows*nivbas, nlon*nrows
-    const double* __restrict__ alt;
-    const double* __restrict__ trajlon;
-    const double* __restrict__ trajlat;
-    const double* __restrict__ trajpre;
-    const double* __restrict__ trajtem;
-    double* qj1;
-    double* hc;
-    double* vsed3d;
-    double* parth2osed;
-    double* parthno3sed;
-    double* surfarea;
-    double* sza3d;
-    const double* __restrict__ ajl;
-    const double* __restrict__ o3up;
-    double* col;               // scratch: o3t | colo2 | colno (ncell each) | sza_top (ncol)
-    unsigned long long* nonfinite;  // [0] non-finite values, [1] Newton iterations,
-                                    // [2] fallbacks, [3] max iterations of a cell
-    double* diag;
-    int npass, maxit;               // Newton: reference passes before, iteration cap
-    double tol;                     // Newton: scaled step tolerance
-    // Newton pipeline state, structure-of-arrays over the call's cells
-    double* nt_r64;                 // NT_NR rate fields per cell, FP64
-    float* nt_r32;                  // the same in FP32 (mixed solver)
-    double* nt_x;                   // iterate x (57 per cell)
-    double* nt_res;                 // residual R(x) (57 per cell)
-    int* nt_stat;                   // 0 active, >0 converged at that iteration, -1 failed
-    int* nt_list_in;                // active cells of this iteration
-    int* nt_list_out;               // active cells of the next iteration
-    int* nt_cnt_in;
-    int* nt_cnt_out;
-    int it;                         // 1-based iteration of k_nt_res / k_nt_lin
-    StepConst sc;
-};
-
-// fields of the Newton rate buffers: K (99), tj (41), het (9), fixed (14), day
-constexpr int NT_RK = 0, NT_RJ = NRATE, NT_RH = NRATE + NPHOT, NT_RF = NRATE + NPHOT + 9;
-constexpr int NT_RDAY = NT_RF + 14, NT_NR = NT_RDAY + 1;
-
-__device__ __forceinline__ size_t plane3(const Params& P) { return (size_t)P.nlon * P.nlat * P.niv; }
-__device__ __forceinline__ size_t plane_b(const Params& P) { return (size_t)P.nlon * P.nlat * P.nivbas; }
 
 // ----------------------------------------------------------------------------
 // k_columns — vertical prefix sums, total F:5172-5184 and jno JNO:109-126
@@ -310,55 +262,21 @@ __global__ void __launch_bounds__(128) k_chem(Params P) {
 // Newton pipeline: the fixed point of the reference's pass map by Newton's
 // method on the generated equations (newton_solve.cuh), Jacobian and LU in TJ
 // (double: plain FP64 solver; float: mixed precision), residual and update in
-// FP64. Per-cell state lives in structure-of-arrays buffers between kernels:
+// FP64. One step:
 //   k_nt_setup   one thread per cell: rate stage, P.npass reference passes from
-//                the start state -> iterate x, rates (FP64 and TJ), active list
-//   per iteration (persistent grids working through the active list):
-//   k_nt_res     FP64 residual R(x)
-//   k_nt_lin     Jacobian, LU and solve with the matrix in shared memory
-//                (slot-major: slot q of thread t at q*blockDim + t), update x,
-//                converged cells leave the list
-//   k_nt_finish  one thread per cell: cells still unconverged after P.maxit
+//                the start state -> iterate x and the cell's record (rates,
+//                fixed constants, day flag, ck0; FP32 copies for the mixed
+//                solver); the cell enters the work queue (day cells from the
+//                front, night cells from the back)
+//   k_nt_solve   persistent kernel, one lane per cell, lanes refilled from the
+//                queue (newton_kernel.cuh)
+//   k_nt_finish  one thread per cell: cells unconverged after P.maxit
 //                iterations fall back to the reference's P.niter passes;
 //                write-back, conserv, clamps
 // ----------------------------------------------------------------------------
-template <typename T>
-struct SPScaled {  // start-of-step number densities: the input mixing ratios times hnm
-    const double* p;
-    size_t s;
-    double f;
-    __device__ __forceinline__ T operator[](int i) const { return (T)(p[(size_t)i * s] * f); }
-};
-
-__device__ __forceinline__ size_t cell_global(const Params& P, int cell) {
-    const int i = cell % P.nlon;
-    const int rest = cell / P.nlon;
-    const int k = rest / P.nrows;
-    const int j = P.ilat0 + rest % P.nrows;
-    return (size_t)i + (size_t)P.nlon * ((size_t)j + (size_t)P.nlat * k);
-}
-
-template <typename T, typename PV>
-__device__ __forceinline__ void nt_fix(PV r, NtFix* F, NtFixT<T>* FT) {
-    const int o = NT_RF;
-    if (F) {
-        F->o2 = r[o + 0]; F->n2 = r[o + 1]; F->h2 = r[o + 2]; F->co2 = r[o + 3]; F->hnm = r[o + 4];
-        F->parthno3 = r[o + 5]; F->parth2o = r[o + 6]; F->parthcl = r[o + 7]; F->parthbr = r[o + 8];
-        F->rain_hno3 = r[o + 9]; F->rain_hcl = r[o + 10]; F->rain_hbr = r[o + 11]; F->rain_h2o2 = r[o + 12];
-        F->dt = r[o + 13];
-    }
-    if (FT) {
-        FT->o2 = r[o + 0]; FT->n2 = r[o + 1]; FT->h2 = r[o + 2]; FT->co2 = r[o + 3]; FT->hnm = r[o + 4];
-        FT->parthno3 = r[o + 5]; FT->parth2o = r[o + 6]; FT->parthcl = r[o + 7]; FT->parthbr = r[o + 8];
-        FT->rain_hno3 = r[o + 9]; FT->rain_hcl = r[o + 10]; FT->rain_hbr = r[o + 11]; FT->rain_h2o2 = r[o + 12];
-        FT->dt = r[o + 13];
-    }
-}
-
 template <bool MIXED>
 __global__ void __launch_bounds__(128) k_nt_setup(Params P) {
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell == 0) *P.nt_cnt_in = P.ncell;
     if (cell >= P.ncell) return;
     CellPro C;
     cell_prologue<false>(P, cell, C);
@@ -370,129 +288,74 @@ __global__ void __launch_bounds__(128) k_nt_setup(Params P) {
     for (int n = 0; n < NCM; n++) cc[n] = C.cc0[n];
 #pragma unroll 1
     for (int it = 0; it < P.npass; it++) cell_pass(F, C.K, C.tj, C.A.het, C.ck0, P.sc.dt, ck, cc);
-    const size_t nc = (size_t)P.ncell;
-    double* x = P.nt_x + cell;
+    double* x = P.nt_x + (size_t)cell * NT_NX;
 #pragma unroll
-    for (int n = 0; n < NBCON - 1; n++) x[n * nc] = ck[n];
+    for (int n = 0; n < NBCON - 1; n++) x[n] = ck[n];
 #pragma unroll
-    for (int n = 0; n < NCM; n++) x[(NBCON - 1 + n) * nc] = cc[n];
-    double fx[14] = {F.o2, F.n2, F.h2, F.co2, F.hnm, F.parthno3, F.parth2o, F.parthcl, F.parthbr,
-                     F.rain_hno3, F.rain_hcl, F.rain_hbr, F.rain_h2o2, P.sc.dt};
-    double* r = P.nt_r64 + cell;
+    for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = cc[n];
+    const double fx[14] = {F.o2, F.n2, F.h2, F.co2, F.hnm, F.parthno3, F.parth2o, F.parthcl, F.parthbr,
+                           F.rain_hno3, F.rain_hcl, F.rain_hbr, F.rain_h2o2, P.sc.dt};
+    const bool day = F.sza <= 95.;
+    double* r = P.nt_rec + (size_t)cell * NT_REC;
 #pragma unroll 4
-    for (int n = 0; n < NRATE; n++) r[(NT_RK + n) * nc] = C.K[n];
+    for (int n = 0; n < NRATE; n++) r[NT_RK + n] = C.K[n];
 #pragma unroll 4
-    for (int n = 0; n < NPHOT; n++) r[(NT_RJ + n) * nc] = C.tj[n];
+    for (int n = 0; n < NPHOT; n++) r[NT_RJ + n] = C.tj[n];
 #pragma unroll
-    for (int n = 0; n < 9; n++) r[(NT_RH + n) * nc] = C.A.het[n];
+    for (int n = 0; n < 9; n++) r[NT_RH + n] = C.A.het[n];
 #pragma unroll
-    for (int n = 0; n < 14; n++) r[(NT_RF + n) * nc] = fx[n];
-    r[NT_RDAY * nc] = F.sza <= 95. ? 1. : 0.;
+    for (int n = 0; n < 14; n++) r[NT_RF + n] = fx[n];
+    r[NT_RDAY] = day ? 1. : 0.;
+#pragma unroll 4
+    for (int n = 0; n < NBCON; n++) r[NT_RCK0 + n] = C.ck0[n];
     if (MIXED) {
-        float* q = P.nt_r32 + cell;
+        float* q = P.nt_rec32 + (size_t)cell * NT_REC32;
 #pragma unroll 4
-        for (int n = 0; n < NRATE; n++) q[(NT_RK + n) * nc] = (float)C.K[n];
+        for (int n = 0; n < NRATE; n++) q[NT_RK + n] = (float)C.K[n];
 #pragma unroll 4
-        for (int n = 0; n < NPHOT; n++) q[(NT_RJ + n) * nc] = (float)C.tj[n];
+        for (int n = 0; n < NPHOT; n++) q[NT_RJ + n] = (float)C.tj[n];
 #pragma unroll
-        for (int n = 0; n < 9; n++) q[(NT_RH + n) * nc] = (float)C.A.het[n];
+        for (int n = 0; n < 9; n++) q[NT_RH + n] = (float)C.A.het[n];
 #pragma unroll
-        for (int n = 0; n < 14; n++) q[(NT_RF + n) * nc] = (float)fx[n];
+        for (int n = 0; n < 14; n++) q[NT_RF + n] = (float)fx[n];
+        q[NT_RDAY] = day ? 1.f : 0.f;
     }
     P.nt_stat[cell] = 0;
-    P.nt_list_in[cell] = cell;
-}
-
-__global__ void __launch_bounds__(128) k_nt_res(Params P) {
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (tid == 0) *P.nt_cnt_out = 0;
-    const int n = *P.nt_cnt_in;
-    const int nc = P.ncell;
-    const size_t pl = plane3(P);
-    for (int idx = tid; idx < n; idx += gridDim.x * blockDim.x) {
-        const int cell = P.nt_list_in[idx];
-        const SP<double> r{P.nt_r64 + cell, nc};
-        NtFix F;
-        nt_fix<double>(r, &F, (NtFixT<double>*)nullptr);
-        const SP<double> K{P.nt_r64 + (size_t)NT_RK * nc + cell, nc};
-        const SP<double> tj{P.nt_r64 + (size_t)NT_RJ * nc + cell, nc};
-        const SP<double> het{P.nt_r64 + (size_t)NT_RH * nc + cell, nc};
-        const SPScaled<double> ck0{P.qj1 + cell_global(P, cell), pl, F.hnm};
-        const SP<double> x{P.nt_x + cell, nc};
-        const SPW<double> R{P.nt_res + cell, nc};
-        if (r[NT_RDAY] != 0.)
-            nt_residual_day<double>(F, K, tj, het, ck0, x, R);
-        else
-            nt_residual_night<double>(F, K, tj, het, ck0, x, R);
-    }
-}
-
-template <typename TJ>
-__global__ void k_nt_lin(Params P) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TJ* smem = reinterpret_cast<TJ*>(smem_raw);
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int n = *P.nt_cnt_in;
-    const int nc = P.ncell;
-    const SPW<TJ> J{smem + threadIdx.x, (int)blockDim.x};
-    for (int idx = tid; idx < n; idx += gridDim.x * blockDim.x) {
-        const int cell = P.nt_list_in[idx];
-        const TJ* rT = sizeof(TJ) == 4 ? (const TJ*)P.nt_r32 : (const TJ*)P.nt_r64;
-        const SP<TJ> r{rT + cell, nc};
-        NtFixT<TJ> FT;
-        nt_fix<TJ>(r, (NtFix*)nullptr, &FT);
-        const SP<TJ> KT{rT + (size_t)NT_RK * nc + cell, nc};
-        const SP<TJ> tjT{rT + (size_t)NT_RJ * nc + cell, nc};
-        const SP<TJ> hetT{rT + (size_t)NT_RH * nc + cell, nc};
-        const bool day = P.nt_r64[(size_t)NT_RDAY * nc + cell] != 0.;
-        const double hnm = P.nt_r64[(size_t)(NT_RF + 4) * nc + cell];
-        const SPW<double> x{P.nt_x + cell, nc};
-        const SP<double> R{P.nt_res + cell, nc};
-        TJ step;
-        const bool ok = nt_linear_step<TJ>(FT, KT, tjT, hetT, day, hnm, x, R, J, &step);
-        if (!ok) {
-            P.nt_stat[cell] = -1;
-        } else if (step < (TJ)P.tol) {
-            P.nt_stat[cell] = P.it;
-        } else if (P.it >= P.maxit) {
-            P.nt_stat[cell] = -1;
-        } else {
-            const int slot = atomicAdd(P.nt_cnt_out, 1);
-            P.nt_list_out[slot] = cell;
-        }
-    }
+    if (day)
+        P.nt_list[atomicAdd(P.nt_head + 1, 1)] = cell;
+    else
+        P.nt_list[P.ncell - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
 }
 
 __global__ void __launch_bounds__(128) k_nt_finish(Params P) {
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= P.ncell) return;
-    const int nc = P.ncell;
     const int stat = P.nt_stat[cell];
-    const SP<double> r{P.nt_r64 + cell, nc};
+    const double* r = P.nt_rec + (size_t)cell * NT_REC;
+    const double* x = P.nt_x + (size_t)cell * NT_NX;
     CellPro C;
     C.g = cell_global(P, cell);
     CellFix& F = C.F;
-    NtFix N;
-    nt_fix<double>(r, &N, (NtFixT<double>*)nullptr);
-    F.o2 = N.o2; F.n2 = N.n2; F.h2 = N.h2; F.co2 = N.co2; F.hnm = N.hnm; F.parthno3 = N.parthno3;
-    F.parth2o = N.parth2o; F.parthcl = N.parthcl; F.parthbr = N.parthbr; F.rain_hno3 = N.rain_hno3;
-    F.rain_hno4 = 0.; F.rain_hcl = N.rain_hcl; F.rain_hbr = N.rain_hbr; F.rain_h2o2 = N.rain_h2o2;
+    const double* f = r + NT_RF;
+    F.o2 = f[0]; F.n2 = f[1]; F.h2 = f[2]; F.co2 = f[3]; F.hnm = f[4]; F.parthno3 = f[5];
+    F.parth2o = f[6]; F.parthcl = f[7]; F.parthbr = f[8]; F.rain_hno3 = f[9];
+    F.rain_hno4 = 0.; F.rain_hcl = f[10]; F.rain_hbr = f[11]; F.rain_h2o2 = f[12];
     F.rain_ch2o = 0.; F.rain_ch3o2h = 0.;
     F.sza = r[NT_RDAY] != 0. ? 0. : 180.;
     const size_t pl = plane3(P);
     double ck[NBCON], cc[NCM];
     if (stat > 0) {
 #pragma unroll
-        for (int n = 0; n < NBCON - 1; n++) ck[n] = P.nt_x[(size_t)n * nc + cell];
-        ck[NBCON - 1] = P.qj1[C.g + pl * (NBCON - 1)] * F.hnm;
+        for (int n = 0; n < NBCON - 1; n++) ck[n] = x[n];
+        ck[NBCON - 1] = r[NT_RCK0 + NBCON - 1];
 #pragma unroll
-        for (int n = 0; n < NCM; n++) cc[n] = P.nt_x[(size_t)(NBCON - 1 + n) * nc + cell];
+        for (int n = 0; n < NCM; n++) cc[n] = x[NBCON - 1 + n];
         atomicAdd(P.nonfinite + 1, (unsigned long long)stat);
         atomicMax(P.nonfinite + 3, (unsigned long long)stat);
     } else {
         // fallback: the reference scheme from the start state
 #pragma unroll
-        for (int n = 0; n < NBCON; n++) C.ck0[n] = P.qj1[C.g + pl * n] * F.hnm;
+        for (int n = 0; n < NBCON; n++) C.ck0[n] = r[NT_RCK0 + n];
 #pragma unroll
         for (int n = 0; n < NRATE; n++) C.K[n] = r[NT_RK + n];
 #pragma unroll
@@ -582,14 +445,17 @@ struct Handle {
     double* m_hc = nullptr;
     double* m_out[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // vsed, parth2o, parthno3, sza3d, surfarea
     // Newton pipeline buffers (allocated when a Newton solver is selected)
-    double* nt_r64 = nullptr;
-    float* nt_r32 = nullptr;
+    double* nt_rec = nullptr;
+    float* nt_rec32 = nullptr;
     double* nt_x = nullptr;
-    double* nt_res = nullptr;
     int* nt_stat = nullptr;
-    int* nt_list = nullptr;   // two lists of ncell
-    int* nt_cnt = nullptr;    // two counters
-    int grid_res = 0, grid_lin32 = 0, grid_lin64 = 0;
+    int* nt_list = nullptr;
+    int* nt_head = nullptr;
+    int nsm = 0;
+    // persistent solve kernel shape per matrix precision ([0] FP32, [1] FP64)
+    int want_lanes = 0, want_bps = 0, want_zs = 0;   // reprobus_chem_set_tuning; lanes 0: autotune
+    const NtVariant* nt_var[2] = {nullptr, nullptr};
+    int nt_bps[2] = {0, 0};
 };
 
 static const char* kVersion = "reprobus_gb300 0.1 (sm_103a, FP64 reference scheme)";
@@ -631,13 +497,12 @@ static void free_handle(Handle* h) {
     cudaFree(h->m_qj1);
     cudaFree(h->m_hc);
     for (auto& p : h->m_out) cudaFree(p);
-    cudaFree(h->nt_r64);
-    cudaFree(h->nt_r32);
+    cudaFree(h->nt_rec);
+    cudaFree(h->nt_rec32);
     cudaFree(h->nt_x);
-    cudaFree(h->nt_res);
     cudaFree(h->nt_stat);
     cudaFree(h->nt_list);
-    cudaFree(h->nt_cnt);
+    cudaFree(h->nt_head);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->own) cudaStreamDestroy(h->own);
@@ -756,31 +621,99 @@ static void fill_params(const Handle* h, Params& P, int ilat0, int ilat1) {
     P.tol = h->tol;
 }
 
-constexpr int NT_BLK32 = 64;  // k_nt_lin threads per block: 524 float slots x 64 = 134 KB shared
-constexpr int NT_BLK64 = 32;  //                              524 double slots x 32 = 134 KB shared
+// every compiled solve-kernel variant of one matrix precision
+static int nt_all_variants(bool mixed, const NtVariant** out, int cap) {
+    int n = 0, k = 0;
+    const NtVariant* lists[2];
+    int counts[2];
+    if (mixed) {
+        lists[0] = nt_variants_f32_zr(&counts[0]);
+        lists[1] = nt_variants_f32_zs(&counts[1]);
+    } else {
+        lists[0] = nt_variants_f64_zr(&counts[0]);
+        lists[1] = nt_variants_f64_zs(&counts[1]);
+    }
+    for (int l = 0; l < 2; l++)
+        for (k = 0; k < counts[l] && n < cap; k++) out[n++] = &lists[l][k];
+    return n;
+}
 
 static int ensure_newton(Handle* h) {
     if (h->nt_x) return REPROBUS_OK;
     const size_t nc = (size_t)h->nlon * h->nlat * h->nivbas;
-    CUDA_TRY(cudaMalloc(&h->nt_r64, nc * NT_NR * sizeof(double)));
-    CUDA_TRY(cudaMalloc(&h->nt_r32, nc * NT_NR * sizeof(float)));
+    CUDA_TRY(cudaMalloc(&h->nt_rec, nc * NT_REC * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&h->nt_rec32, nc * NT_REC32 * sizeof(float)));
     CUDA_TRY(cudaMalloc(&h->nt_x, nc * NT_NX * sizeof(double)));
-    CUDA_TRY(cudaMalloc(&h->nt_res, nc * NT_NX * sizeof(double)));
     CUDA_TRY(cudaMalloc(&h->nt_stat, nc * sizeof(int)));
-    CUDA_TRY(cudaMalloc(&h->nt_list, 2 * nc * sizeof(int)));
-    CUDA_TRY(cudaMalloc(&h->nt_cnt, 2 * sizeof(int)));
-    int nsm = 0, nb = 0;
-    CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device));
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_nt_res, 128, 0));
-    h->grid_res = nsm * (nb > 0 ? nb : 1);
-    const size_t sm32 = (size_t)NT_NSLOT * NT_BLK32 * sizeof(float);
-    const size_t sm64 = (size_t)NT_NSLOT * NT_BLK64 * sizeof(double);
-    CUDA_TRY(cudaFuncSetAttribute(k_nt_lin<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm32));
-    CUDA_TRY(cudaFuncSetAttribute(k_nt_lin<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm64));
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_nt_lin<float>, NT_BLK32, sm32));
-    h->grid_lin32 = nsm * (nb > 0 ? nb : 1);
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_nt_lin<double>, NT_BLK64, sm64));
-    h->grid_lin64 = nsm * (nb > 0 ? nb : 1);
+    CUDA_TRY(cudaMalloc(&h->nt_list, nc * sizeof(int)));
+    CUDA_TRY(cudaMalloc(&h->nt_head, 4 * sizeof(int)));
+    CUDA_TRY(cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device));
+    return REPROBUS_OK;
+}
+
+static int enqueue_setup(Handle* h, Params& P, bool mixed) {
+    const int tb = 128;
+    CUDA_TRY(cudaMemsetAsync(h->nt_head, 0, 4 * sizeof(int), h->stream));
+    if (mixed)
+        k_nt_setup<true><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    else
+        k_nt_setup<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    return REPROBUS_OK;
+}
+
+// Autotuner of the persistent solve kernel: every compiled shape (lanes per
+// block) at every resident block count per SM that fits is timed on this
+// step's cells (setup, then the timed solve; the setup restores the iterate
+// and the queue between candidates) and the fastest is kept for the handle.
+static int choose_shape(Handle* h, Params& P, bool mixed) {
+    const int ip = mixed ? 0 : 1;
+    if (h->nt_var[ip]) return REPROBUS_OK;
+    const NtVariant* vs[16];
+    const int nv = nt_all_variants(mixed, vs, 16);
+    struct Cand { const NtVariant* v; int bps; };
+    Cand cands[32];
+    int nc = 0;
+    for (int i = 0; i < nv; i++) {
+        int occ = 0;
+        CUDA_TRY(vs[i]->prepare(&occ));
+        if (occ < 1) continue;
+        if (h->want_lanes > 0) {
+            if (vs[i]->nth != h->want_lanes || vs[i]->zshared != h->want_zs) continue;
+            const int b = h->want_bps > 0 && h->want_bps < occ ? h->want_bps : occ;
+            cands[nc++] = {vs[i], b};
+            continue;
+        }
+        for (int b = 1; b <= occ && nc < 32; b++) cands[nc++] = {vs[i], b};
+    }
+    if (nc == 0)
+        return set_err(REPROBUS_ERR_ARG, "no compiled solve-kernel shape with %d lanes per block fits", h->want_lanes);
+    if (nc == 1) {
+        h->nt_var[ip] = cands[0].v;
+        h->nt_bps[ip] = cands[0].bps;
+        return REPROBUS_OK;
+    }
+    float best = 1e30f;
+    int bi = 0;
+    const char* verbose = getenv("REPROBUS_TUNE_VERBOSE");  // print every candidate's time to stderr
+    for (int c = 0; c < nc; c++) {
+        int rc = enqueue_setup(h, P, mixed);
+        if (rc) return rc;
+        CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+        CUDA_TRY(cands[c].v->launch(P, h->nsm * cands[c].bps, h->stream));
+        CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
+        CUDA_TRY(cudaEventSynchronize(h->ev1));
+        float ms = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+        if (verbose && verbose[0] == '1')
+            fprintf(stderr, "reprobus autotune: %s lanes %d zshared %d blocks/SM %d: %.3f ms\n",
+                    mixed ? "fp32" : "fp64", cands[c].v->nth, cands[c].v->zshared, cands[c].bps, ms);
+        if (ms < best) {
+            best = ms;
+            bi = c;
+        }
+    }
+    h->nt_var[ip] = cands[bi].v;
+    h->nt_bps[ip] = cands[bi].bps;
     return REPROBUS_OK;
 }
 
@@ -790,44 +723,18 @@ static int launch_newton(Handle* h, Params& P, int* launches) {
     if (rc) return rc;
     const bool mixed = h->solver == REPROBUS_SOLVER_NEWTON_MIXED;
     const int tb = 128;
-    const size_t nc = (size_t)h->nlon * h->nlat * h->nivbas;
-    P.nt_r64 = h->nt_r64;
-    P.nt_r32 = h->nt_r32;
+    P.nt_rec = h->nt_rec;
+    P.nt_rec32 = h->nt_rec32;
     P.nt_x = h->nt_x;
-    P.nt_res = h->nt_res;
     P.nt_stat = h->nt_stat;
-    int* lin = h->nt_list;
-    int* lout = h->nt_list + nc;
-    int* cin = h->nt_cnt;
-    int* cout = h->nt_cnt + 1;
-    P.nt_list_in = lin;
-    P.nt_cnt_in = cin;
-    if (mixed)
-        k_nt_setup<true><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
-    else
-        k_nt_setup<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
-    (*launches)++;
-    for (int it = 1; it <= h->maxit; it++) {
-        P.it = it;
-        P.nt_list_in = lin;
-        P.nt_list_out = lout;
-        P.nt_cnt_in = cin;
-        P.nt_cnt_out = cout;
-        k_nt_res<<<h->grid_res, 128, 0, h->stream>>>(P);
-        if (mixed)
-            k_nt_lin<float><<<h->grid_lin32, NT_BLK32, (size_t)NT_NSLOT * NT_BLK32 * sizeof(float), h->stream>>>(P);
-        else
-            k_nt_lin<double><<<h->grid_lin64, NT_BLK64, (size_t)NT_NSLOT * NT_BLK64 * sizeof(double), h->stream>>>(P);
-        *launches += 2;
-        int* t = lin;
-        lin = lout;
-        lout = t;
-        int* c = cin;
-        cin = cout;
-        cout = c;
-    }
+    P.nt_list = h->nt_list;
+    P.nt_head = h->nt_head;
+    if ((rc = choose_shape(h, P, mixed))) return rc;
+    const int ip = mixed ? 0 : 1;
+    if ((rc = enqueue_setup(h, P, mixed))) return rc;
+    CUDA_TRY(h->nt_var[ip]->launch(P, h->nsm * h->nt_bps[ip], h->stream));
     k_nt_finish<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
-    (*launches)++;
+    *launches += 3;
     return REPROBUS_OK;
 }
 
@@ -869,6 +776,10 @@ static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
         st->fallbacks = 0;
         st->max_newton_iters = 0;
         st->solver = h->solver;
+        const int ip = h->solver == REPROBUS_SOLVER_NEWTON_MIXED ? 0 : 1;
+        st->lanes_per_block = h->solver == REPROBUS_SOLVER_REF5 || !h->nt_var[ip] ? 0 : h->nt_var[ip]->nth;
+        st->blocks_per_sm = h->solver == REPROBUS_SOLVER_REF5 ? 0 : h->nt_bps[ip];
+        st->z_shared = h->solver == REPROBUS_SOLVER_REF5 || !h->nt_var[ip] ? 0 : h->nt_var[ip]->zshared;
     }
     if (counters && (st || P.check)) {
         unsigned long long c[4] = {0, 0, 0, 0};
@@ -882,6 +793,30 @@ static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
         }
         if (P.check && c[0]) return set_err(REPROBUS_ERR_NONFINITE, "%llu non-finite values in the step output", c[0]);
     }
+    return REPROBUS_OK;
+}
+
+extern "C" int reprobus_chem_set_tuning(void* handle, int lanes_per_block, int blocks_per_sm, int zshared) {
+    Handle* h = (Handle*)handle;
+    if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
+    if (lanes_per_block < 0 || blocks_per_sm < 0) return set_err(REPROBUS_ERR_ARG, "bad tuning values");
+    if (zshared < 0 || zshared > 1) return set_err(REPROBUS_ERR_ARG, "zshared must be 0 or 1");
+    if (lanes_per_block > 0) {
+        bool found = false;
+        const NtVariant* vs[16];
+        for (int m = 0; m < 2; m++) {
+            const int nv = nt_all_variants(m == 0, vs, 16);
+            for (int i = 0; i < nv; i++) found |= vs[i]->nth == lanes_per_block && vs[i]->zshared == zshared;
+        }
+        if (!found)
+            return set_err(REPROBUS_ERR_ARG, "no solve-kernel shape with %d lanes per block (zshared %d)",
+                           lanes_per_block, zshared);
+    }
+    h->want_lanes = lanes_per_block;
+    h->want_zs = zshared;
+    h->want_bps = blocks_per_sm;
+    h->nt_var[0] = h->nt_var[1] = nullptr;
+    h->nt_bps[0] = h->nt_bps[1] = 0;
     return REPROBUS_OK;
 }
 

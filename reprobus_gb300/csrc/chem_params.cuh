@@ -1,0 +1,70 @@
+// chem_params.cuh — launch parameters shared by the step kernels
+// (chem_kernels.cu) and the Newton solve kernels (nt_solve_*.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "chem_cell.cuh"
+
+namespace rpb {
+
+// ----------------------------------------------------------------------------
+// kernel parameters
+// ----------------------------------------------------------------------------
+struct Params {
+    int nlon, nlat, niv, nivbas, nivhau;
+    int ilat0, nrows;          // 0-based first row, number of rows
+    long long trajoff;         // element offset of the irapp slice in traj*
+    int niter, fuse, check;
+    int ncell, ncol;           // nlon*nrows*nivbas, nlon*nrows
+    const double* __restrict__ alt;
+    const double* __restrict__ trajlon;
+    const double* __restrict__ trajlat;
+    const double* __restrict__ trajpre;
+    const double* __restrict__ trajtem;
+    double* qj1;
+    double* hc;
+    double* vsed3d;
+    double* parth2osed;
+    double* parthno3sed;
+    double* surfarea;
+    double* sza3d;
+    const double* __restrict__ ajl;
+    const double* __restrict__ o3up;
+    double* col;               // scratch: o3t | colo2 | colno (ncell each) | sza_top (ncol)
+    unsigned long long* nonfinite;  // [0] non-finite values, [1] Newton iterations,
+                                    // [2] fallbacks, [3] max iterations of a cell
+    double* diag;
+    int npass, maxit;               // Newton: reference passes before, iteration cap
+    double tol;                     // Newton: scaled step tolerance
+    // Newton state, one record per cell of the call (cell-major)
+    double* nt_rec;                 // NT_REC FP64 fields: rates, fixed constants, day flag, ck0
+    float* nt_rec32;                // NT_REC32 FP32 copies of the rate fields (mixed solver)
+    double* nt_x;                   // iterate x (NT_NX per cell)
+    int* nt_stat;                   // 0 active, >0 converged at that iteration, -1 failed
+    int* nt_list;                   // work queue: day cells from the front, night cells from the back
+    int* nt_head;                   // [0] next queue entry, [1] day count, [2] night count
+    StepConst sc;
+};
+
+// fields of a Newton cell record: K (99), tj (41), het (9), fixed constants
+// (14: o2 n2 h2 co2 hnm parthno3 parth2o parthcl parthbr rain_hno3 rain_hcl
+// rain_hbr rain_h2o2 dt), day flag, start-of-step number densities ck0 (42)
+constexpr int NT_RK = 0, NT_RJ = NRATE, NT_RH = NRATE + NPHOT, NT_RF = NRATE + NPHOT + 9;
+constexpr int NT_RDAY = NT_RF + 14, NT_RCK0 = NT_RDAY + 1;
+constexpr int NT_REC = 208;    // FP64 record stride (206 used; 1664 B = 13 lines of 128 B)
+constexpr int NT_REC32 = 168;  // FP32 record stride (164 used)
+static_assert(NT_RCK0 + NBCON <= NT_REC, "record layout");
+
+__device__ __forceinline__ size_t plane3(const Params& P) { return (size_t)P.nlon * P.nlat * P.niv; }
+__device__ __forceinline__ size_t plane_b(const Params& P) { return (size_t)P.nlon * P.nlat * P.nivbas; }
+
+
+__device__ __forceinline__ size_t cell_global(const Params& P, int cell) {
+    const int i = cell % P.nlon;
+    const int rest = cell / P.nlon;
+    const int k = rest / P.nrows;
+    const int j = P.ilat0 + rest % P.nrows;
+    return (size_t)i + (size_t)P.nlon * ((size_t)j + (size_t)P.nlat * k);
+}
+
+}  // namespace rpb

@@ -1,0 +1,112 @@
+// newton_kernel.cuh — the persistent Newton solve kernel of one step.
+//
+// One lane integrates one cell at a time. The lanes of a warp take cells from
+// a global work queue (one atomic per warp and refill, lanes ranked by
+// ballot): a lane whose cell has converged, failed or hit the iteration cap
+// takes the next queue entry at the top of the loop, so cells needing 2 or 15
+// iterations share a warp without idling it. The queue holds the day cells
+// first and the night cells after them, so the lanes of a warp mostly run the
+// same (day or night) equations.
+//
+// Per iteration (newton_solve.cuh): scaled Jacobian in TJ into the lane's
+// NT_NSLOT shared-memory slots (slot-major, stride NTH: every slot access of
+// a warp is one conflict-free row of banks), FP64 residual, Crout
+// factorisation with fused forward substitution and back substitution in TJ,
+// FP64 update of the iterate in the cell's record. ZS: the right-hand side
+// and step z in NT_NX more shared-memory slots per lane (else registers).
+#pragma once
+#include "chem_params.cuh"
+#include "newton_launch.h"
+#include "newton_solve.cuh"
+
+namespace rpb {
+
+template <typename T>
+__device__ __forceinline__ void nt_load_fix(const T* r, NtFixT<T>& F) {
+    F.o2 = r[0]; F.n2 = r[1]; F.h2 = r[2]; F.co2 = r[3]; F.hnm = r[4];
+    F.parthno3 = r[5]; F.parth2o = r[6]; F.parthcl = r[7]; F.parthbr = r[8];
+    F.rain_hno3 = r[9]; F.rain_hcl = r[10]; F.rain_hbr = r[11]; F.rain_h2o2 = r[12]; F.dt = r[13];
+}
+
+template <typename TJ, int NTH, bool ZS>
+__global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
+    static_assert(NTH % 32 == 0, "whole warps");
+    extern __shared__ __align__(16) unsigned char nt_smem[];
+    const SJ<TJ, NTH> J{reinterpret_cast<TJ*>(nt_smem) + threadIdx.x};
+    const unsigned lane = threadIdx.x & 31u;
+    const int ncell = P.ncell;
+    int cell = -1;  // >= 0: cell in work; -1: wants a cell; -2: queue exhausted
+    int it = 0;
+    for (;;) {
+        const unsigned want = __ballot_sync(0xffffffffu, cell == -1);
+        if (want) {
+            const int leader = __ffs(want) - 1;
+            int base = 0;
+            if ((int)lane == leader) base = atomicAdd(P.nt_head, __popc(want));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (cell == -1) {
+                const int q = base + __popc(want & ((1u << lane) - 1u));
+                cell = q < ncell ? P.nt_list[q] : -2;
+                it = 0;
+            }
+        }
+        if (__all_sync(0xffffffffu, cell == -2)) break;
+        if (cell >= 0) {
+            const double* rec = P.nt_rec + (size_t)cell * NT_REC;
+            const TJ* recT;
+            if constexpr (sizeof(TJ) == 4)
+                recT = P.nt_rec32 + (size_t)cell * NT_REC32;
+            else
+                recT = rec;
+            NtFixT<double> F;
+            NtFixT<TJ> FT;
+            nt_load_fix<double>(rec + NT_RF, F);
+            nt_load_fix<TJ>(recT + NT_RF, FT);
+            const bool day = rec[NT_RDAY] != 0.;
+            double* x = P.nt_x + (size_t)cell * NT_NX;
+            TJ step;
+            const bool ok = nt_iterate<TJ, ZS>(F, rec + NT_RK, rec + NT_RJ, rec + NT_RH, rec + NT_RCK0, FT, recT + NT_RK,
+                                           recT + NT_RJ, recT + NT_RH, day, x, J, &step);
+            it++;
+            int done = 0;
+            if (!ok)
+                done = -1;
+            else if (step < (TJ)P.tol)
+                done = it;
+            else if (it >= P.maxit)
+                done = -1;
+            if (done) {
+                P.nt_stat[cell] = done;
+                cell = -1;
+            }
+        }
+    }
+}
+
+template <typename TJ, int NTH, bool ZS>
+constexpr size_t nt_smem_bytes() {
+    return (size_t)(NT_NSLOT + (ZS ? NT_NX : 0)) * NTH * sizeof(TJ);
+}
+
+template <typename TJ, int NTH, bool ZS>
+cudaError_t nt_prepare(int* blocks_per_sm) {
+    cudaError_t e = cudaFuncSetAttribute(k_nt_solve<TJ, NTH, ZS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)nt_smem_bytes<TJ, NTH, ZS>());
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_nt_solve<TJ, NTH, ZS>, NTH,
+                                                         nt_smem_bytes<TJ, NTH, ZS>());
+}
+
+template <typename TJ, int NTH, bool ZS>
+cudaError_t nt_launch(const Params& P, int grid, cudaStream_t stream) {
+    k_nt_solve<TJ, NTH, ZS><<<grid, NTH, nt_smem_bytes<TJ, NTH, ZS>(), stream>>>(P);
+    return cudaGetLastError();
+}
+
+template <typename TJ, int NTH, bool ZS>
+constexpr NtVariant nt_variant() {
+    return NtVariant{(int)sizeof(TJ), NTH, ZS ? 1 : 0, nt_smem_bytes<TJ, NTH, ZS>(), &nt_prepare<TJ, NTH, ZS>,
+                     &nt_launch<TJ, NTH, ZS>};
+}
+
+}  // namespace rpb

@@ -1,0 +1,12 @@
+// nt_solve_f32_zs.cu — FP32-matrix (mixed-precision) variants of the persistent
+// Newton solve kernel, right-hand side in shared memory; the autotuner picks among the
+// compiled lanes-per-block values.
+#include "newton_kernel.cuh"
+
+namespace rpb {
+static const NtVariant kV[] = {nt_variant<float, 64, true>(), nt_variant<float, 96, true>(), nt_variant<float, 128, true>()};
+const NtVariant* nt_variants_f32_zs(int* n) {
+    *n = (int)(sizeof(kV) / sizeof(kV[0]));
+    return kV;
+}
+}  // namespace rpb

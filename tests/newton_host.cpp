@@ -44,17 +44,20 @@ void nt_host_residual(const double* K, const double* tj, const double* het, cons
         nt_residual_night<double>(F, K, tj, het, ck0, x, R);
 }
 
-// dense Jacobian (row-major NX x NX, original numbering), FP64
+// dense scaled Jacobian J'_ij = dR_i/dx_j s_j / s_i (row-major NX x NX,
+// original numbering, power-of-two scales of nt_pow2_scale), FP64
 void nt_host_jacobian(const double* K, const double* tj, const double* het, const double* fix, int day,
                       const double* x, double* Jd) {
     NtFix F = fix_from(fix);
     double J[NT_NSLOT];
+    const double floor_ = 1e-20 * F.hnm;
     if (day)
-        nt_jacobian_day<double>(F, K, tj, het, x, J);
+        nt_jacobian_day<double>(F, K, tj, het, x, floor_, J);
     else
-        nt_jacobian_night<double>(F, K, tj, het, x, J);
+        nt_jacobian_night<double>(F, K, tj, het, x, floor_, J);
     memset(Jd, 0, sizeof(double) * NT_NX * NT_NX);
-    for (int q = 0; q < NT_NSLOT; q++) Jd[NT_SLOT_I[q] * NT_NX + NT_SLOT_J[q]] = J[q];
+    for (int q = 0; q < NT_NA; q++) Jd[NT_A_I[q] * NT_NX + NT_A_J[q]] = J[q];
+    for (int q = 0; q < NT_NCONST; q++) Jd[NT_CONST_I[q] * (NT_NX + 1)] = NT_CONST_V[q];
 }
 
 // Newton from x (in/out); mixed: float Jacobian. Returns iterations or -1.

@@ -66,6 +66,12 @@ def _x(c, st, dg, cell):
     return np.concatenate([st["qj1"][i, 0, k, :42] * hnm, st["hc"][i, 0, k, :] * hnm])
 
 
+def _pow2_scale(x, floor):
+    """2^floor(log2(max(|x|, floor))), the generated code's unknown scales."""
+    m, e = np.frexp(np.maximum(np.abs(x), floor))
+    return np.ldexp(1.0, e - 1)
+
+
 def test_generated_header_is_current(tmp_path):
     pytest.importorskip("sympy")
     from reprobus_gb300.codegen import gen_newton
@@ -94,7 +100,7 @@ def test_jacobian_matches_finite_differences(host, data):
         Jd = np.zeros(57 * 57)
         host.nt_host_jacobian(_P(K), _P(tj), _P(het), _P(fix), day, _P(x), _P(Jd))
         Jd = Jd.reshape(57, 57)
-        s = np.maximum(np.abs(x), 1e-20 * fix[4])
+        s = _pow2_scale(x, 1e-20 * fix[4])
         for j in range(57):
             h = 1e-6 * s[j]
             xp, xm = x.copy(), x.copy()
@@ -104,7 +110,7 @@ def test_jacobian_matches_finite_differences(host, data):
             host.nt_host_residual(_P(K), _P(tj), _P(het), _P(fix), _P(ck0), day, _P(xp), _P(Rp))
             host.nt_host_residual(_P(K), _P(tj), _P(het), _P(fix), _P(ck0), day, _P(xm), _P(Rm))
             fd = (Rp - Rm) / (2 * h) * s[j] / s
-            an = Jd[:, j] * s[j] / s
+            an = Jd[:, j]
             assert np.all(np.abs(an - fd) <= 1e-4 * np.abs(fd) + 1e-6), (cell, j)
 
 
