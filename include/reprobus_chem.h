@@ -73,6 +73,11 @@ typedef struct reprobus_stats {
     int blocks_per_sm;         /* Newton solvers: resident blocks of it per SM        */
     int z_shared;              /* Newton solvers: 1 when the kernel keeps the right-
                                   hand side in shared memory, 0 in registers         */
+    int warm_start;            /* Newton solvers: 1 when the learned warm start ran  */
+    long long warm_restarts;   /* warm start: cells whose predicted start missed the
+                                  convergence test and restarted from the plain start */
+    long long failed_iters;    /* Newton solvers: iterations of attempts that did not
+                                  converge (warm-start misses, fallbacks)            */
 } reprobus_stats;
 
 /* ---- diagnostics layout (reprobus_chem_rates_*) ----------------------------
@@ -159,6 +164,58 @@ int reprobus_chem_set_solver(void* handle, int solver, int npass, int maxit, dou
  * zshared (0 or 1) and blocks_per_sm (0: as many as fit). No counterpart in
  * the reference. */
 int reprobus_chem_set_tuning(void* handle, int lanes_per_block, int blocks_per_sm, int zshared);
+
+/* ---- learned warm start ----------------------------------------------------
+ * A 64-256-256-256-64 MLP (SiLU; BF16 weights and activations, FP32
+ * accumulation on the tensor cores) maps the 64 features of a cell at the
+ * Newton solvers' plain start (npass reference passes from the start state):
+ * log10 of its 42 transported and 15 short-lived mixing ratios floored at
+ * 1e-30, T [K], ln p [hPa], cos(sza), log10 of the aerosol surface area
+ * floored at 1e-12, latitude [deg], time of day [fraction], 0; to the log10
+ * ratios of the 57 end-of-step mixing ratios to those of the plain start.
+ * None of this has a counterpart in the reference. Device pointers
+ * throughout; B rows of 64 FP32 values, row-major. */
+#define REPROBUS_MLP_FEATURES 64
+#define REPROBUS_MLP_OUTPUTS 64   /* 57 used */
+#define REPROBUS_MLP_NNORM 320    /* in_mean[64] in_std[64] out_mean[64] out_std[64] out_min[64]:
+                                     predictions with |y| < out_min are replaced by 0 */
+
+/* Creates a network with He-uniform weights from seed and a training batch
+ * capacity (a multiple of 128). */
+int reprobus_mlp_create(int batch_cap, unsigned long long seed, void** net);
+int reprobus_mlp_free(void* net);
+/* Number of FP32 parameters, packed W0 b0 W1 b1 W2 b2 W3 b3 (W row-major,
+ * fan_out x fan_in). */
+int reprobus_mlp_nparams(void);
+/* Host copies of the parameters and of the normalisation (either may be NULL). */
+int reprobus_mlp_set_params(void* net, const float* params, const float* norm);
+int reprobus_mlp_get_params(void* net, float* params, float* norm);
+/* One Adam step (lr) on a batch (B a multiple of 128 up to batch_cap) of raw
+ * features X and raw targets Y; *loss (nullable, host): mean squared error of
+ * the normalised outputs before the step. */
+int reprobus_mlp_train_step(void* net, const float* X, const float* Y, int B, float lr, float* loss,
+                            void* cuda_stream);
+/* Gradients of that loss (host, packed like the parameters) without a step. */
+int reprobus_mlp_grads(void* net, const float* X, const float* Y, int B, float* grads, float* loss,
+                       void* cuda_stream);
+/* Inference on B rows (any B): Y = network(X), raw units. */
+int reprobus_mlp_forward(void* net, const float* X, float* Y, int B, void* cuda_stream);
+
+/* Attaches a network to a chemistry handle (NULL detaches): the Newton
+ * solvers then start every cell from the network's prediction instead of the
+ * plain start; a cell whose predicted start misses the convergence test is
+ * solved again from the plain start (stats.warm_restarts), and one that
+ * misses again falls back to the reference passes. */
+int reprobus_chem_set_mlp(void* handle, void* net);
+
+/* The 64 raw features of every chemistry cell of rows ilat0..ilat1 at the
+ * plain start of a step of length dt (the handle's npass reference passes;
+ * device arrays as for reprobus_chem_rates_dev; feat: ncell x 64 FP32,
+ * 16-byte aligned, cells in the diagnostics order). */
+int reprobus_chem_features_dev(void* handle, int ilat0, int ilat1, double daynum, double dt, const double* alt,
+                               const double* trajlon, const double* trajlat, const double* trajpre,
+                               const double* trajtem, int irapp, const double* qj1, const double* hc,
+                               float* feat);
 
 /* One 15-min chemistry step for latitude rows ilat0..ilat1 (1-based,
  * inclusive), HOST arrays: copies the rows in, integrates, copies them back.

@@ -38,7 +38,9 @@ EXPORTS = [
     "reprobus_version", "reprobus_last_error", "reprobus_chem_troe", "reprobus_chem_init",
     "reprobus_chem_free", "reprobus_chem_set_stream", "reprobus_chem_step", "reprobus_chem_step_dev",
     "reprobus_chem_rates_dev", "reprobus_conserv_dev", "reprobus_chem_step_noalloc", "reprobus_chem_set_solver",
-    "reprobus_chem_set_tuning",
+    "reprobus_chem_set_tuning", "reprobus_mlp_create", "reprobus_mlp_free", "reprobus_mlp_nparams",
+    "reprobus_mlp_set_params", "reprobus_mlp_get_params", "reprobus_mlp_train_step", "reprobus_mlp_grads",
+    "reprobus_mlp_forward", "reprobus_chem_set_mlp", "reprobus_chem_features_dev",
 ]
 NOALLOC_SCRATCH_DOUBLES = 1 << 20
 
@@ -54,7 +56,9 @@ class Stats(ctypes.Structure):
                 ("kernel_launches", ctypes.c_int), ("passes", ctypes.c_int), ("device_ms", ctypes.c_double),
                 ("newton_iters", ctypes.c_longlong), ("fallbacks", ctypes.c_longlong),
                 ("max_newton_iters", ctypes.c_int), ("solver", ctypes.c_int),
-                ("lanes_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int), ("z_shared", ctypes.c_int)]
+                ("lanes_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int), ("z_shared", ctypes.c_int),
+                ("warm_start", ctypes.c_int), ("warm_restarts", ctypes.c_longlong),
+                ("failed_iters", ctypes.c_longlong)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -89,6 +93,17 @@ def load_library(path: str = LIBPATH):
     lib.reprobus_conserv_dev.argtypes = [vp, i, i, vp, vp]
     lib.reprobus_chem_step_noalloc.argtypes = [vp, vp, dp, i, i, i, i, i, i, i, i, i, i, d, d, vp, vp, vp, vp, vp,
                                                i, vp, vp, vp, vp, vp, vp, vp, vp]
+    fp = ctypes.POINTER(ctypes.c_float)
+    lib.reprobus_mlp_create.argtypes = [i, ctypes.c_ulonglong, ctypes.POINTER(vp)]
+    lib.reprobus_mlp_free.argtypes = [vp]
+    lib.reprobus_mlp_nparams.argtypes = []
+    lib.reprobus_mlp_set_params.argtypes = [vp, fp, fp]
+    lib.reprobus_mlp_get_params.argtypes = [vp, fp, fp]
+    lib.reprobus_mlp_train_step.argtypes = [vp, vp, vp, i, ctypes.c_float, fp, vp]
+    lib.reprobus_mlp_grads.argtypes = [vp, vp, vp, i, fp, fp, vp]
+    lib.reprobus_mlp_forward.argtypes = [vp, vp, vp, i, vp]
+    lib.reprobus_chem_set_mlp.argtypes = [vp, vp]
+    lib.reprobus_chem_features_dev.argtypes = [vp, i, i, d, d, vp, vp, vp, vp, vp, i, vp, vp, vp]
     for name in EXPORTS:
         if name not in ("reprobus_version", "reprobus_last_error"):
             getattr(lib, name).restype = ctypes.c_int
@@ -177,6 +192,20 @@ class ChemStep:
         """Shape of the persistent Newton solve kernel (lanes_per_block 0:
         autotune on the first Newton step of each matrix precision)."""
         _check(self.lib.reprobus_chem_set_tuning(self._h, int(lanes_per_block), int(blocks_per_sm), int(zshared)))
+
+    def set_mlp(self, net):
+        """Attaches a reprobus_gb300.mlp.Mlp as the Newton solvers' warm start
+        (None detaches)."""
+        _check(self.lib.reprobus_chem_set_mlp(self._h, ctypes.c_void_p(net.handle if net is not None else None)))
+        self.mlp = net
+
+    def features_dev(self, ilat0, ilat1, daynum, dt, alt, trajlon, trajlat, trajpre, trajtem, irapp, qj1, hc,
+                     feat):
+        """The 64 raw warm-start features of every chemistry cell of the rows
+        at the plain start into feat (a CUDA float32 tensor of ncell x 64)."""
+        _check(self.lib.reprobus_chem_features_dev(self._h, ilat0, ilat1, daynum, dt, _dp(alt), _dp(trajlon),
+                                                   _dp(trajlat), _dp(trajpre), _dp(trajtem), irapp, _dp(qj1),
+                                                   _dp(hc), _dp(feat)))
 
     def set_stream(self, stream):
         """stream: a torch.cuda.Stream, a raw cudaStream_t int, or None."""

@@ -26,6 +26,7 @@
 #include "chem_params.cuh"
 #include "newton_gen.cuh"
 #include "newton_launch.h"
+#include "mlp_net.h"
 
 using namespace rpb;
 
@@ -35,6 +36,15 @@ using namespace rpb;
 static thread_local char g_err[512] = "";
 
 static int set_err(int code, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+// the same error channel for the other translation units (not exported)
+extern "C" __attribute__((visibility("hidden"))) int reprobus_set_error(int code, const char* fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
     vsnprintf(g_err, sizeof(g_err), fmt, ap);
@@ -274,6 +284,28 @@ __global__ void __launch_bounds__(128) k_chem(Params P) {
 //                iterations fall back to the reference's P.niter passes;
 //                write-back, conserv, clamps
 // ----------------------------------------------------------------------------
+// the 64 raw features of the warm-start network for one cell: log10 of the 42
+// transported and 15 short-lived mixing ratios of the plain start (ck, cc:
+// number densities after the plain start's reference passes; floored at
+// 1e-30), T, ln p, cos(sza), log10 of the aerosol surface area (floored at
+// 1e-12), latitude, time of day (fraction), 0
+__device__ __forceinline__ void cell_features(const Params& P, const CellPro& C, const double* ck, const double* cc,
+                                              float* f) {
+    const double hnm = C.F.hnm;
+#pragma unroll 6
+    for (int n = 0; n < NBCON - 1; n++) f[n] = (float)log10(fmax(ck[n] / hnm, 1e-30));
+#pragma unroll 5
+    for (int n = 0; n < NCM; n++) f[NBCON - 1 + n] = (float)log10(fmax(cc[n] / hnm, 1e-30));
+    const size_t gi = P.trajoff + C.g;
+    f[57] = (float)P.trajtem[gi];
+    f[58] = (float)log(P.trajpre[gi]);
+    f[59] = (float)cos(C.F.sza * (PI / 180.));
+    f[60] = (float)log10(fmax(C.A.surf, 1e-12));
+    f[61] = (float)P.trajlat[gi];
+    f[62] = (float)(P.sc.ut / 24.);
+    f[63] = 0.f;
+}
+
 template <bool MIXED>
 __global__ void __launch_bounds__(128) k_nt_setup(Params P) {
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
@@ -320,11 +352,69 @@ __global__ void __launch_bounds__(128) k_nt_setup(Params P) {
         for (int n = 0; n < 14; n++) q[NT_RF + n] = (float)fx[n];
         q[NT_RDAY] = day ? 1.f : 0.f;
     }
+    if (P.warm) {
+        float fe[64];
+        cell_features(P, C, ck, cc, fe);
+        float4* o = reinterpret_cast<float4*>(P.mlp_feat + (size_t)cell * 64);
+#pragma unroll
+        for (int i = 0; i < 16; i++) o[i] = make_float4(fe[4 * i], fe[4 * i + 1], fe[4 * i + 2], fe[4 * i + 3]);
+    }
+    if (cell == 0) P.nt_head[3] = P.ncell;
     P.nt_stat[cell] = 0;
     if (day)
         P.nt_list[atomicAdd(P.nt_head + 1, 1)] = cell;
     else
         P.nt_list[P.ncell - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
+}
+
+// warm start: x_i = max(x_i, 1e-30 hnm) 10^y_i from the network's prediction
+__global__ void __launch_bounds__(128) k_nt_warm(Params P) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= P.ncell) return;
+    const double hnm = P.nt_rec[(size_t)cell * NT_REC + NT_RF + 4];
+    double* x = P.nt_x + (size_t)cell * NT_NX;
+    const float* y = P.mlp_y + (size_t)cell * 64;
+#pragma unroll 4
+    for (int i = 0; i < NT_NX; i++) {
+        const float yi = fminf(fmaxf(y[i], -30.f), 30.f);
+        x[i] = fmax(x[i], 1e-30 * hnm) * (double)exp10f(yi);
+    }
+}
+
+// cells whose warm start missed the convergence test start again from the
+// plain start (P.npass_plain reference passes) and re-enter the queue
+__global__ void __launch_bounds__(128) k_nt_restart(Params P) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= P.ncell || P.nt_stat[cell] >= 0) return;
+    const double* r = P.nt_rec + (size_t)cell * NT_REC;
+    CellFix F;
+    F.o2 = r[NT_RF]; F.n2 = r[NT_RF + 1]; F.h2 = r[NT_RF + 2]; F.co2 = r[NT_RF + 3]; F.hnm = r[NT_RF + 4];
+    F.parthno3 = r[NT_RF + 5]; F.parth2o = r[NT_RF + 6]; F.parthcl = r[NT_RF + 7]; F.parthbr = r[NT_RF + 8];
+    F.rain_hno3 = r[NT_RF + 9]; F.rain_hno4 = 0.; F.rain_hcl = r[NT_RF + 10]; F.rain_hbr = r[NT_RF + 11];
+    F.rain_h2o2 = r[NT_RF + 12]; F.rain_ch2o = 0.; F.rain_ch3o2h = 0.;
+    F.sza = r[NT_RDAY] != 0. ? 0. : 180.;
+    const size_t g = cell_global(P, cell), pl = plane3(P);
+    double K[NRATE], tj[NPHOT], het[9], ck0[NBCON], ck[NBCON], cc[NCM];
+#pragma unroll
+    for (int n = 0; n < NRATE; n++) K[n] = r[NT_RK + n];
+#pragma unroll
+    for (int n = 0; n < NPHOT; n++) tj[n] = r[NT_RJ + n];
+#pragma unroll
+    for (int n = 0; n < 9; n++) het[n] = r[NT_RH + n];
+#pragma unroll
+    for (int n = 0; n < NBCON; n++) ck[n] = ck0[n] = r[NT_RCK0 + n];
+#pragma unroll
+    for (int n = 0; n < NCM; n++) cc[n] = P.hc[g + pl * n] * F.hnm;
+#pragma unroll 1
+    for (int it = 0; it < P.npass_plain; it++) cell_pass(F, K, tj, het, ck0, P.sc.dt, ck, cc);
+    double* x = P.nt_x + (size_t)cell * NT_NX;
+#pragma unroll
+    for (int n = 0; n < NBCON - 1; n++) x[n] = ck[n];
+#pragma unroll
+    for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = cc[n];
+    P.nt_stat[cell] = 0;
+    P.nt_list[atomicAdd(P.nt_head + 3, 1)] = cell;
+    atomicAdd(P.nonfinite + 4, 1ULL);
 }
 
 __global__ void __launch_bounds__(128) k_nt_finish(Params P) {
@@ -456,6 +546,10 @@ struct Handle {
     int want_lanes = 0, want_bps = 0, want_zs = 0;   // reprobus_chem_set_tuning; lanes 0: autotune
     const NtVariant* nt_var[2] = {nullptr, nullptr};
     int nt_bps[2] = {0, 0};
+    // learned warm start (reprobus_chem_set_mlp): the network and its buffers
+    void* mlp = nullptr;
+    float* mlp_feat = nullptr;
+    float* mlp_y = nullptr;
 };
 
 static const char* kVersion = "reprobus_gb300 0.1 (sm_103a, FP64 reference scheme)";
@@ -503,6 +597,8 @@ static void free_handle(Handle* h) {
     cudaFree(h->nt_stat);
     cudaFree(h->nt_list);
     cudaFree(h->nt_head);
+    cudaFree(h->mlp_feat);
+    cudaFree(h->mlp_y);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->own) cudaStreamDestroy(h->own);
@@ -550,7 +646,7 @@ extern "C" int reprobus_chem_init(const double* ajl, const double* o3up, const d
         (e = cudaMalloc(&h->d_ajl, najl * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&h->d_o3up, 80 * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&h->d_col, (3 * ncell + ncol) * sizeof(double))) != cudaSuccess ||
-        (e = cudaMalloc(&h->d_count, 4 * sizeof(unsigned long long))) != cudaSuccess ||
+        (e = cudaMalloc(&h->d_count, 8 * sizeof(unsigned long long))) != cudaSuccess ||
         (e = cudaMemcpy(h->d_ajl, ajl, najl * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(h->d_o3up, o3up, 80 * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
         return fail(set_err(REPROBUS_ERR_CUDA, "init: %s", cudaGetErrorString(e)));
@@ -729,12 +825,38 @@ static int launch_newton(Handle* h, Params& P, int* launches) {
     P.nt_stat = h->nt_stat;
     P.nt_list = h->nt_list;
     P.nt_head = h->nt_head;
+    const bool warm = h->mlp != nullptr;
+    P.npass_plain = h->npass;
+    if (warm) {
+        if (!h->mlp_feat) {
+            const size_t nc = (size_t)h->nlon * h->nlat * h->nivbas;
+            CUDA_TRY(cudaMalloc(&h->mlp_feat, nc * MLP_FEAT * sizeof(float)));
+            CUDA_TRY(cudaMalloc(&h->mlp_y, nc * MLP_YOUT * sizeof(float)));
+        }
+        P.warm = 1;
+        P.mlp_feat = h->mlp_feat;
+        P.mlp_y = h->mlp_y;
+    }
     if ((rc = choose_shape(h, P, mixed))) return rc;
     const int ip = mixed ? 0 : 1;
+    const int grid = h->nsm * h->nt_bps[ip];
     if ((rc = enqueue_setup(h, P, mixed))) return rc;
-    CUDA_TRY(h->nt_var[ip]->launch(P, h->nsm * h->nt_bps[ip], h->stream));
-    k_nt_finish<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    if (warm) {
+        CUDA_TRY(cudaMemsetAsync(mlp_err_flag(h->mlp), 0, sizeof(unsigned int), h->stream));
+        if ((rc = mlp_infer(h->mlp, h->mlp_feat, h->mlp_y, P.ncell, h->stream))) return rc;
+        k_nt_warm<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        *launches += 2;
+    }
+    CUDA_TRY(h->nt_var[ip]->launch(P, grid, h->stream));
     *launches += 3;
+    if (warm) {
+        // misses of the warm start: the plain start, a second pass of the solve kernel
+        CUDA_TRY(cudaMemsetAsync(h->nt_head, 0, 4 * sizeof(int), h->stream));
+        k_nt_restart<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        CUDA_TRY(h->nt_var[ip]->launch(P, grid, h->stream));
+        *launches += 2;
+    }
+    k_nt_finish<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     return REPROBUS_OK;
 }
 
@@ -745,7 +867,7 @@ static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
     P.fuse = (h->flags & REPROBUS_FUSE_CONSERV) ? 1 : 0;
     P.check = (h->flags & REPROBUS_CHECK_FINITE) ? 1 : 0;
     const bool counters = P.check || h->solver != REPROBUS_SOLVER_REF5;
-    if (counters) CUDA_TRY(cudaMemsetAsync(h->d_count, 0, 4 * sizeof(unsigned long long), h->stream));
+    if (counters) CUDA_TRY(cudaMemsetAsync(h->d_count, 0, 8 * sizeof(unsigned long long), h->stream));
     if (st) CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
     k_columns<<<(P.ncol + tb - 1) / tb, tb, 0, h->stream>>>(P);
     launches++;
@@ -780,9 +902,12 @@ static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
         st->lanes_per_block = h->solver == REPROBUS_SOLVER_REF5 || !h->nt_var[ip] ? 0 : h->nt_var[ip]->nth;
         st->blocks_per_sm = h->solver == REPROBUS_SOLVER_REF5 ? 0 : h->nt_bps[ip];
         st->z_shared = h->solver == REPROBUS_SOLVER_REF5 || !h->nt_var[ip] ? 0 : h->nt_var[ip]->zshared;
+        st->warm_start = h->solver != REPROBUS_SOLVER_REF5 && h->mlp ? 1 : 0;
+        st->warm_restarts = 0;
+        st->failed_iters = 0;
     }
     if (counters && (st || P.check)) {
-        unsigned long long c[4] = {0, 0, 0, 0};
+        unsigned long long c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         CUDA_TRY(cudaMemcpyAsync(c, h->d_count, sizeof(c), cudaMemcpyDeviceToHost, h->stream));
         CUDA_TRY(cudaStreamSynchronize(h->stream));
         if (st) {
@@ -790,6 +915,8 @@ static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
             st->newton_iters = (long long)c[1];
             st->fallbacks = (long long)c[2];
             st->max_newton_iters = (int)c[3];
+            st->warm_restarts = (long long)c[4];
+            st->failed_iters = (long long)c[5];
         }
         if (P.check && c[0]) return set_err(REPROBUS_ERR_NONFINITE, "%llu non-finite values in the step output", c[0]);
     }
@@ -817,6 +944,65 @@ extern "C" int reprobus_chem_set_tuning(void* handle, int lanes_per_block, int b
     h->want_bps = blocks_per_sm;
     h->nt_var[0] = h->nt_var[1] = nullptr;
     h->nt_bps[0] = h->nt_bps[1] = 0;
+    return REPROBUS_OK;
+}
+
+extern "C" int reprobus_chem_set_mlp(void* handle, void* net) {
+    Handle* h = (Handle*)handle;
+    if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
+    h->mlp = net;
+    return REPROBUS_OK;
+}
+
+__global__ void __launch_bounds__(128) k_features(Params P) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= P.ncell) return;
+    CellPro C;
+    cell_prologue<true>(P, cell, C);
+    double ck[NBCON], cc[NCM];
+#pragma unroll
+    for (int n = 0; n < NBCON; n++) ck[n] = C.ck0[n];
+#pragma unroll
+    for (int n = 0; n < NCM; n++) cc[n] = C.cc0[n];
+#pragma unroll 1
+    for (int it = 0; it < P.npass; it++) cell_pass(C.F, C.K, C.tj, C.A.het, C.ck0, P.sc.dt, ck, cc);
+    float fe[64];
+    cell_features(P, C, ck, cc, fe);
+    float4* o = reinterpret_cast<float4*>(P.mlp_feat + (size_t)cell * 64);
+#pragma unroll
+    for (int i = 0; i < 16; i++) o[i] = make_float4(fe[4 * i], fe[4 * i + 1], fe[4 * i + 2], fe[4 * i + 3]);
+}
+
+extern "C" int reprobus_chem_features_dev(void* handle, int ilat0, int ilat1, double daynum, double dt,
+                                          const double* alt,
+                                          const double* trajlon, const double* trajlat, const double* trajpre,
+                                          const double* trajtem, int irapp, const double* qj1, const double* hc,
+                                          float* feat) {
+    Handle* h = (Handle*)handle;
+    if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
+    int rc = check_rows(h, ilat0, ilat1);
+    if (rc) return rc;
+    if (irapp < 1 || irapp > h->nrappmax) return set_err(REPROBUS_ERR_ARG, "irapp %d outside 1..%d", irapp, h->nrappmax);
+    if (!alt || !trajlon || !trajlat || !trajpre || !trajtem || !qj1 || !hc || !feat)
+        return set_err(REPROBUS_ERR_ARG, "NULL array argument");
+    if (((uintptr_t)feat) & 15) return set_err(REPROBUS_ERR_ARG, "feat must be 16-byte aligned");
+    Params P;
+    fill_params(h, P, ilat0, ilat1);
+    P.trajoff = (long long)(irapp - 1) * h->nlon * h->nlat * h->niv;
+    P.alt = alt;
+    P.trajlon = trajlon;
+    P.trajlat = trajlat;
+    P.trajpre = trajpre;
+    P.trajtem = trajtem;
+    P.qj1 = const_cast<double*>(qj1);  // read only (DIAG prologue)
+    P.hc = const_cast<double*>(hc);
+    P.mlp_feat = feat;
+    step_const(h, daynum, dt, P.sc);
+    const int tb = 128;
+    k_columns<<<(P.ncol + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    k_features<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(h->stream));
     return REPROBUS_OK;
 }
 

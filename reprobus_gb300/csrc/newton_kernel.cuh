@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
     extern __shared__ __align__(16) unsigned char nt_smem[];
     const SJ<TJ, NTH> J{reinterpret_cast<TJ*>(nt_smem) + threadIdx.x};
     const unsigned lane = threadIdx.x & 31u;
-    const int ncell = P.ncell;
+    const int nq = P.nt_head[3];  // queue length (set by the kernel that filled the queue)
     int cell = -1;  // >= 0: cell in work; -1: wants a cell; -2: queue exhausted
     int it = 0;
     for (;;) {
@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
             base = __shfl_sync(0xffffffffu, base, leader);
             if (cell == -1) {
                 const int q = base + __popc(want & ((1u << lane) - 1u));
-                cell = q < ncell ? P.nt_list[q] : -2;
+                cell = q < nq ? P.nt_list[q] : -2;
                 it = 0;
             }
         }
@@ -76,6 +76,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
             else if (it >= P.maxit)
                 done = -1;
             if (done) {
+                if (done < 0) atomicAdd(P.nonfinite + 5, (unsigned long long)it);  // iterations spent in vain
                 P.nt_stat[cell] = done;
                 cell = -1;
             }

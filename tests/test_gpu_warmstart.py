@@ -1,0 +1,72 @@
+"""The learned warm start on the GPU: a network trained here (by the
+library's tensor-core kernels, on cells the plain FP64 Newton solver
+integrates) corrects the plain start of the mixed-precision Newton solver.
+The answer must be the same fixed point (checked against Oracle-C and the
+reference map, as for the plain start), and the ablation against the plain
+start is recorded: iterations spent per cell (including attempts that
+missed) and fallbacks, which must not get worse beyond noise."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from reprobus_gb300 import ChemStep, inputs
+from reprobus_gb300.chem import SOLVER_NEWTON_MIXED
+
+pytestmark = pytest.mark.gpu
+
+ERR_TOL = 1e-6
+MAP_TOL = 1e-8
+
+
+@pytest.fixture(scope="module")
+def net(lib_built):
+    from reprobus_gb300 import mlp, train_mlp
+    X, Y = train_mlp.make_training_set(12, 36, 12, seed0=500, log=lambda *a: None)
+    Xv, Yv = train_mlp.make_training_set(1, 36, 12, seed0=900, log=lambda *a: None)
+    n = mlp.Mlp(batch_cap=4096, seed=1)
+    n.set_params(None, mlp.normalisation(X, Y))
+    hist = mlp.train(n, X, Y, 3000, batch=4096, lr=1e-3)
+    assert np.mean(hist[-50:]) < 0.5 * np.mean(hist[:10])
+    tau = mlp.fit_thresholds(n, Xv, Yv)
+    print(f"loss {np.mean(hist[:10]):.3f} -> {np.mean(hist[-50:]):.4f}; outputs on: {int(np.isfinite(tau).sum())}")
+    yield n
+    n.close()
+
+
+@pytest.fixture(scope="module")
+def case():
+    return inputs.make_case("cfg0", seed=2, nlon=16, nivbas=94)
+
+
+def _run(case, net):
+    from reprobus_gb300.resident import DeviceCase
+    h = ChemStep.for_case(case, niter=5, flags=0)
+    h.set_solver(SOLVER_NEWTON_MIXED, npass=1, maxit=12, tol=1e-10)
+    if net is not None:
+        h.set_mlp(net)
+    dc = DeviceCase(case)
+    st = h.step_dev(1, case.nlat, case.daynum, case.dt, *dc.args(), stats=True)
+    out = dc.state_host()
+    h.close()
+    return out, st
+
+
+def test_warm_start_reaches_the_fixed_point_and_records_the_ablation(case, net):
+    from test_gpu_newton import _species_err
+    fp, stat, _ = oracle.step_fixed_point(case, tol=1e-12, maxiter=60, fuse=False)
+    cold, st0 = _run(case, None)
+    warm, st1 = _run(case, net)
+    assert st1["warm_start"] == 1 and st0["warm_start"] == 0
+    fell_back = oracle.map_residual(case, warm["qj1"], warm["hc"]) > MAP_TOL
+    assert fell_back.sum() <= st1["fallbacks"] <= 0.01 * case.ncells
+    ok = (stat > 0) & ~fell_back
+    err = _species_err(warm, fp, case.nivbas)
+    assert err[ok].max() <= ERR_TOL
+    # all iterations spent per cell, including attempts that missed
+    it0 = (st0["newton_iters"] + st0["failed_iters"]) / case.ncells
+    it1 = (st1["newton_iters"] + st1["failed_iters"]) / case.ncells
+    print(f"mean Newton iterations: plain start {it0:.2f}, learned start {it1:.2f}; "
+          f"restarts {st1['warm_restarts']}, fallbacks {st0['fallbacks']} -> {st1['fallbacks']}")
+    assert it1 <= 1.05 * it0
+    assert st1["fallbacks"] <= st0["fallbacks"] + 2
+    assert st1["warm_restarts"] <= 0.05 * case.ncells
