@@ -40,6 +40,25 @@ BYTES_PER_CELL = 1008  # compulsory FP64 SoA traffic per cell-step: 63 reads + 6
 OPS_PER_CELL = 6793.08
 
 
+def newton_ops():
+    """Arithmetic operators (+ - * /) of one Newton iteration, counted in the
+    generated source (reprobus_gb300/csrc/newton_gen.cuh; an FMA counts 2):
+    residual (day, night), Jacobian (day, night), factorisation + solve."""
+    path = os.path.join(ROOT, "reprobus_gb300", "csrc", "newton_gen.cuh")
+    src = open(path).read()
+
+    def body(name):
+        i = src.index(f"void {name}(")
+        j = src.index("\n}\n", i)
+        lines = [ln.split("//")[0] for ln in src[i:j].splitlines()[1:]]
+        text = "\n".join(lines)
+        return sum(text.count(op) for op in ("*", " + ", " - ", "/", "-=")) - text.count("J[") * 0
+
+    return {"res_day": body("nt_residual_day"), "res_night": body("nt_residual_night"),
+            "jac_day": body("nt_jacobian_day"), "jac_night": body("nt_jacobian_night"),
+            "factor": body("nt_factor_solve"), "update": 3 * 57, "rhs": 2 * 57}
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -194,7 +213,7 @@ def main():
                     help="Newton solve kernel lanes per block (0: autotune)")
     ap.add_argument("--bps", type=int, default=0, help="Newton solve kernel blocks per SM (0: all that fit)")
     ap.add_argument("--zshared", type=int, default=0, help="with --lanes: right-hand side in shared memory")
-    ap.add_argument("--solver", default="all", choices=["all", "ref5", "newton64", "mixed"],
+    ap.add_argument("--solver", default="all", choices=["all", "ref5", "newton64", "mixed", "mlp"],
                     help="all: time the three solvers, headline = mixed")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -215,9 +234,15 @@ def main():
     else:
         case = inputs.make_case(args.config, seed=1234 + rank)
     from reprobus_gb300.chem import SOLVER_NEWTON64, SOLVER_NEWTON_MIXED, SOLVER_REF5
-    solver_ids = {"ref5": SOLVER_REF5, "newton64": SOLVER_NEWTON64, "mixed": SOLVER_NEWTON_MIXED}
+    solver_ids = {"ref5": SOLVER_REF5, "newton64": SOLVER_NEWTON64, "mixed": SOLVER_NEWTON_MIXED,
+                  "mlp": SOLVER_NEWTON_MIXED}
     run = list(solver_ids) if args.solver == "all" else [args.solver]
-    headline = "mixed" if args.solver == "all" else args.solver
+    headline = "mlp" if args.solver == "all" else args.solver
+    net = None
+    if "mlp" in run:
+        from reprobus_gb300 import mlp as mlpmod
+        net = mlpmod.Mlp(batch_cap=128, seed=0)
+        net.load()  # reprobus_gb300/data/mlp_warmstart.npz, trained by reprobus_gb300.train_mlp
     h = ChemStep.for_case(case, niter=5, flags=FUSE_CONSERV)
     if args.lanes:
         h.set_tuning(args.lanes, args.bps, args.zshared)
@@ -241,6 +266,7 @@ def main():
     clocks.start()
     for name in run:
         h.set_solver(solver_ids[name], npass=1, maxit=12, tol=1e-10)
+        h.set_mlp(net if name == "mlp" else None)
         for _ in range(max(args.warmup, 3)):
             restore()
             step()
@@ -264,16 +290,23 @@ def main():
             torch.distributed.barrier()
             ms = float(t.item())
         conv = case.ncells - st["fallbacks"]
+        day_frac = float((dc["sza3d"][:case.ncells] <= 95.0).double().mean())
         results[name] = {"cells_per_s": case.ncells * world * args.steps / (ms * 1e-3),
                          "ms_per_step": ms / args.steps, "kernel_ms": st["device_ms"],
+                         "solve_ms": st["solve_ms"] if name != "ref5" else None,
                          "launches_per_step": st["kernel_launches"], "fallbacks": st["fallbacks"],
                          "mean_newton_iters": (st["newton_iters"] / conv) if name != "ref5" and conv else None,
+                         "iters_per_cell": ((st["newton_iters"] + st["failed_iters"]) / case.ncells
+                                            if name != "ref5" else None),
+                         "warm_restarts": st["warm_restarts"] if name == "mlp" else None,
+                         "day_frac": day_frac,
                          "max_newton_iters": st["max_newton_iters"] if name != "ref5" else None,
                          "solve_shape": None if name == "ref5" else
                          {"lanes_per_block": st["lanes_per_block"], "blocks_per_sm": st["blocks_per_sm"],
                           "z_shared": st["z_shared"]}}
     clk = clocks.stop()
     h.set_solver(solver_ids[headline], npass=1, maxit=12, tol=1e-10)
+    h.set_mlp(net if headline == "mlp" else None)
     R = results[headline]
     ms_step = R["ms_per_step"]
     kernel_ms = R["kernel_ms"]
@@ -333,11 +366,30 @@ def main():
                 "kernel_ms": round(kernel_ms, 4),
                 "hbm": {"achieved": round(ach_gbs, 2), "peak": hbm_peak, "unit": "GB/s",
                         "frac": round(ach_gbs / hbm_peak, 5), "bytes_per_cell": BYTES_PER_CELL}}
-        if flops_cell:
+        if headline == "ref5" and flops_cell:
             ach = flops_cell * ncell / (kernel_ms * 1e-3) / 1e12
             roof.update(achieved=round(ach, 4), frac=round(ach / peak64, 4), flops_per_cell=flops_cell,
                         flops_note="algorithmic ops of the reference scheme per cell-step (+-*/ and "
                                    "transcendentals counted once each; the peak counts an FMA as 2)")
+        elif headline != "ref5":
+            # dominant kernel: the persistent Newton solve kernel (k_nt_solve)
+            ops = newton_ops()
+            f = R["day_frac"]
+            res = f * ops["res_day"] + (1 - f) * ops["res_night"]
+            jac = f * ops["jac_day"] + (1 - f) * ops["jac_night"]
+            fp64_it = res + ops["update"] + (0 if headline in ("mixed", "mlp") else jac + ops["factor"] + ops["rhs"])
+            fp32_it = (jac + ops["factor"] + ops["rhs"]) if headline in ("mixed", "mlp") else 0
+            iters = R["iters_per_cell"] * ncell
+            sm = R["solve_ms"] * 1e-3
+            ach = fp64_it * iters / sm / 1e12
+            roof.update(kernel="k_nt_solve", kernel_ms=round(R["solve_ms"], 4), achieved=round(ach, 4),
+                        frac=round(ach / peak64, 4), fp64_ops_per_iteration=round(fp64_it, 1),
+                        fp32_ops_per_iteration=round(fp32_it, 1), iterations_per_cell=round(R["iters_per_cell"], 3),
+                        fp32_tflops=round(fp32_it * iters / sm / 1e12, 4),
+                        flops_note="arithmetic operators of one Newton iteration counted in the generated "
+                                   "source (an FMA counts 2), times the iterations the step ran, over the "
+                                   "solve kernel's CUDA-event time; FP64 part (residual, update) against the "
+                                   "live DGEMM peak")
         cb = None
         if not args.no_cpu_baseline:
             cb = cpu_baseline(case)
@@ -347,6 +399,8 @@ def main():
                 "config": {"workload": WORKLOAD if args.config == "cfg1" else
                            f"{args.config}: {case.nlon}x{case.nlat}x{case.niv} = {case.ncells} cells, one 15-min step",
                            "solver": {"ref5": "reference scheme, 5 fixed passes (drop-in)",
+                                      "mlp": "Newton to the fixed point, FP32 Jacobian+LU, FP64 residual/update, "
+                                             "learned warm start (BF16 MLP on tensor cores)",
                                       "newton64": "Newton to the fixed point of the reference map, FP64 Jacobian",
                                       "mixed": "Newton to the fixed point, FP32 Jacobian+LU, FP64 residual/update"}
                            [headline],
@@ -357,6 +411,8 @@ def main():
                 "solvers": results,
                 "mixed_vs_fp64_newton": (results["mixed"]["cells_per_s"] / results["newton64"]["cells_per_s"]
                                          if "mixed" in results and "newton64" in results else None),
+                "mlp_mixed_vs_fp64_newton": (results["mlp"]["cells_per_s"] / results["newton64"]["cells_per_s"]
+                                             if "mlp" in results and "newton64" in results else None),
                 "roofline": roof, "e2e": e2e, "cpu_baseline": cb, "clocks": clk}
         print(json.dumps(line))
     h.close()

@@ -78,6 +78,8 @@ typedef struct reprobus_stats {
                                   convergence test and restarted from the plain start */
     long long failed_iters;    /* Newton solvers: iterations of attempts that did not
                                   converge (warm-start misses, fallbacks)            */
+    double solve_ms;           /* Newton solvers: device time of the persistent solve
+                                  kernel (its first launch)                          */
 } reprobus_stats;
 
 /* ---- diagnostics layout (reprobus_chem_rates_*) ----------------------------
@@ -160,9 +162,9 @@ int reprobus_chem_set_solver(void* handle, int solver, int npass, int maxit, dou
  * (lanes per block x right-hand side in registers or shared memory x
  * resident blocks per SM) on that step's own cells and keeps the fastest
  * (synchronous, once per handle); > 0: use that many lanes per block (a
- * compiled value: 64, 96, 128 for the mixed solver; 32, 64 for the FP64 one),
- * zshared (0 or 1) and blocks_per_sm (0: as many as fit). No counterpart in
- * the reference. */
+ * compiled value: 64, 96, 128 for the mixed solver; 32, 64 for the FP64 one;
+ * a precision without that value is autotuned), zshared (0 or 1) and
+ * blocks_per_sm (0: as many as fit). No counterpart in the reference. */
 int reprobus_chem_set_tuning(void* handle, int lanes_per_block, int blocks_per_sm, int zshared);
 
 /* ---- learned warm start ----------------------------------------------------

@@ -291,11 +291,12 @@ __global__ void __launch_bounds__(128) k_chem(Params P) {
 // 1e-12), latitude, time of day (fraction), 0
 __device__ __forceinline__ void cell_features(const Params& P, const CellPro& C, const double* ck, const double* cc,
                                               float* f) {
-    const double hnm = C.F.hnm;
+    // log10 in FP32 (the features are FP32): ratio in FP64, then float
+    const double rh = 1. / C.F.hnm;
 #pragma unroll 6
-    for (int n = 0; n < NBCON - 1; n++) f[n] = (float)log10(fmax(ck[n] / hnm, 1e-30));
+    for (int n = 0; n < NBCON - 1; n++) f[n] = log10f((float)fmax(ck[n] * rh, 1e-30));
 #pragma unroll 5
-    for (int n = 0; n < NCM; n++) f[NBCON - 1 + n] = (float)log10(fmax(cc[n] / hnm, 1e-30));
+    for (int n = 0; n < NCM; n++) f[NBCON - 1 + n] = log10f((float)fmax(cc[n] * rh, 1e-30));
     const size_t gi = P.trajoff + C.g;
     f[57] = (float)P.trajtem[gi];
     f[58] = (float)log(P.trajpre[gi]);
@@ -528,6 +529,7 @@ struct Handle {
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev2 = nullptr, ev3 = nullptr;  // around the persistent solve kernel (stats.solve_ms)
     // device mirrors for the host-pointer entry point (allocated on first use)
     double* m_alt = nullptr;
     double* m_traj[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -601,6 +603,8 @@ static void free_handle(Handle* h) {
     cudaFree(h->mlp_y);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->ev2) cudaEventDestroy(h->ev2);
+    if (h->ev3) cudaEventDestroy(h->ev3);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
 }
@@ -643,6 +647,7 @@ extern "C" int reprobus_chem_init(const double* ajl, const double* o3up, const d
     const size_t ncol = (size_t)nlon * nlat;
     if ((e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreate(&h->ev0)) != cudaSuccess || (e = cudaEventCreate(&h->ev1)) != cudaSuccess ||
+        (e = cudaEventCreate(&h->ev2)) != cudaSuccess || (e = cudaEventCreate(&h->ev3)) != cudaSuccess ||
         (e = cudaMalloc(&h->d_ajl, najl * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&h->d_o3up, 80 * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&h->d_col, (3 * ncell + ncol) * sizeof(double))) != cudaSuccess ||
@@ -769,11 +774,18 @@ static int choose_shape(Handle* h, Params& P, bool mixed) {
     struct Cand { const NtVariant* v; int bps; };
     Cand cands[32];
     int nc = 0;
+    // a requested shape that this precision does not have: autotune it instead
+    bool want = h->want_lanes > 0;
+    if (want) {
+        bool any = false;
+        for (int i = 0; i < nv; i++) any |= vs[i]->nth == h->want_lanes && vs[i]->zshared == h->want_zs;
+        want = any;
+    }
     for (int i = 0; i < nv; i++) {
         int occ = 0;
         CUDA_TRY(vs[i]->prepare(&occ));
         if (occ < 1) continue;
-        if (h->want_lanes > 0) {
+        if (want) {
             if (vs[i]->nth != h->want_lanes || vs[i]->zshared != h->want_zs) continue;
             const int b = h->want_bps > 0 && h->want_bps < occ ? h->want_bps : occ;
             cands[nc++] = {vs[i], b};
@@ -814,7 +826,7 @@ static int choose_shape(Handle* h, Params& P, bool mixed) {
 }
 
 // the Newton pipeline of one step (after k_columns)
-static int launch_newton(Handle* h, Params& P, int* launches) {
+static int launch_newton(Handle* h, Params& P, int* launches, bool timed) {
     int rc = ensure_newton(h);
     if (rc) return rc;
     const bool mixed = h->solver == REPROBUS_SOLVER_NEWTON_MIXED;
@@ -847,7 +859,9 @@ static int launch_newton(Handle* h, Params& P, int* launches) {
         k_nt_warm<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
         *launches += 2;
     }
+    if (timed) CUDA_TRY(cudaEventRecord(h->ev2, h->stream));
     CUDA_TRY(h->nt_var[ip]->launch(P, grid, h->stream));
+    if (timed) CUDA_TRY(cudaEventRecord(h->ev3, h->stream));
     *launches += 3;
     if (warm) {
         // misses of the warm start: the plain start, a second pass of the solve kernel
@@ -875,7 +889,7 @@ static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
         k_chem<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
         launches++;
     } else {
-        int rc = launch_newton(h, P, &launches);
+        int rc = launch_newton(h, P, &launches, st != nullptr);
         if (rc) return rc;
     }
     if (P.fuse && h->nivbas < h->niv) {
@@ -890,6 +904,12 @@ static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
         float ms = 0.f;
         CUDA_TRY(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
         st->device_ms = ms;
+        st->solve_ms = 0.;
+        if (h->solver != REPROBUS_SOLVER_REF5) {
+            float sm = 0.f;
+            CUDA_TRY(cudaEventElapsedTime(&sm, h->ev2, h->ev3));
+            st->solve_ms = sm;
+        }
         st->ncells = P.ncell;
         st->kernel_launches = launches;
         st->passes = h->solver == REPROBUS_SOLVER_REF5 ? h->niter : h->npass;

@@ -147,40 +147,80 @@ constexpr int MLP_NNORM = 2 * MLP_IN + 3 * MLP_OUT;  // in_mean, in_std, out_mea
 // out_min: per output, the smallest |prediction| that is applied (smaller
 // predicted corrections are replaced by 0: the plain start is kept)
 
+// the weights of one inference tile as six shared-memory images in the
+// core-matrix layout, stored back to back in global memory so that each one
+// is a single bulk (TMA) copy: [W0 | W0] (256 x 128), W1 rows 0-127 and
+// 128-255, W2 rows 0-127 and 128-255 (128 x 256 each), W3 (64 x 256)
+constexpr int WIMG_N = 6;
+__host__ __device__ constexpr uint32_t wimg_bytes(int i) { return i == WIMG_N - 1 ? 32768u : 65536u; }
+__host__ __device__ constexpr uint32_t wimg_off(int i) { return (uint32_t)i * 65536u; }
+constexpr uint32_t WIMG_TOTAL = 5 * 65536 + 32768;
+
 struct InferArgs {
     const float* X;              // B x 64 raw features
-    float* Y;                    // B x 64 raw outputs (log10 ratios)
+    float* Y;                    // B x 64 raw outputs (log10 corrections)
     int B;
-    const __nv_bfloat16* W[MLP_NL];
+    const uint8_t* img;          // WIMG_TOTAL bytes of weight images
     const float* b[MLP_NL];
     const float* norm;
     unsigned int* err;
 };
 
-// rows x K BF16 weight rows [row0, row0 + rows) into the core-matrix layout
-__device__ __forceinline__ void stage_rows(uint8_t* dst, const __nv_bfloat16* W, int row0, int rows, int K) {
-    const int k8n = K >> 3;
-    for (int i = threadIdx.x; i < rows * k8n; i += blockDim.x) {
-        const int r = i / k8n, k8 = i - r * k8n;
-        *reinterpret_cast<uint4*>(dst + tc_off(r, k8 * 8, K)) =
-            *reinterpret_cast<const uint4*>(W + (size_t)(row0 + r) * K + k8 * 8);
+// build the weight images from the BF16 row-major weights
+__global__ void k_wimage(const __nv_bfloat16* W0c, const __nv_bfloat16* W1, const __nv_bfloat16* W2,
+                         const __nv_bfloat16* W3, uint8_t* img) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // one 16-byte chunk (8 elements)
+    // image 0: 256 x 128 (16 chunks per row)
+    if (i < 256 * 16) {
+        const int r = i / 16, k8 = i % 16;
+        *reinterpret_cast<uint4*>(img + wimg_off(0) + tc_off(r, k8 * 8, MLP_K0)) =
+            *reinterpret_cast<const uint4*>(W0c + (size_t)r * MLP_K0 + k8 * 8);
+        return;
+    }
+    int j = i - 256 * 16;
+    // images 1-4: 128 x 256 halves (32 chunks per row)
+    if (j < 4 * 128 * 32) {
+        const int im = j / (128 * 32), rem = j % (128 * 32), r = rem / 32, k8 = rem % 32;
+        const __nv_bfloat16* W = im < 2 ? W1 : W2;
+        const int row = (im & 1) * 128 + r;
+        *reinterpret_cast<uint4*>(img + wimg_off(1 + im) + tc_off(r, k8 * 8, MLP_H)) =
+            *reinterpret_cast<const uint4*>(W + (size_t)row * MLP_H + k8 * 8);
+        return;
+    }
+    j -= 4 * 128 * 32;
+    // image 5: 64 x 256
+    if (j < 64 * 32) {
+        const int r = j / 32, k8 = j % 32;
+        *reinterpret_cast<uint4*>(img + wimg_off(5) + tc_off(r, k8 * 8, MLP_H)) =
+            *reinterpret_cast<const uint4*>(W3 + (size_t)r * MLP_H + k8 * 8);
     }
 }
+constexpr int WIMG_CHUNKS = 256 * 16 + 4 * 128 * 32 + 64 * 32;
 
 // the whole network on 128 rows per tile (persistent over tiles): input
 // normalisation, 4 layers on the tensor cores with the activations kept in
-// shared memory, output de-normalisation
+// shared memory, output de-normalisation. The six weight images of a tile
+// stream through two 64 KB buffers by bulk copies: the copy of the next
+// image runs while the tensor cores work on the current one.
 __global__ void __launch_bounds__(128, 1) k_mlp_infer(InferArgs a) {
     extern __shared__ __align__(1024) uint8_t sm[];
-    uint8_t* act = sm;                   // 128 x 256 BF16 (64 KB)
-    uint8_t* wb = sm + 65536;            // 128 x 256 BF16 weight rows (64 KB)
-    float* bias = reinterpret_cast<float*>(sm + 131072);  // 832 floats
-    float* nrm = bias + 3 * MLP_H + MLP_OUT;              // 256 floats
-    __shared__ uint64_t bar;
+    uint8_t* act = sm;                                     // 128 x 256 BF16 (64 KB)
+    uint8_t* wbuf[2] = {sm + 65536, sm + 131072};          // weight images (64 KB each)
+    float* bias = reinterpret_cast<float*>(sm + 196608);   // 832 floats
+    float* nrm = bias + 3 * MLP_H + MLP_OUT;               // MLP_NNORM floats
+    __shared__ uint64_t bar, wbar[2];
     __shared__ uint32_t tslot;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ntiles = (a.B + 127) / 128;
+    const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int nimg = my_tiles * WIMG_N;  // weight images this CTA loads in all
     if (warp == 0) tmem_alloc(&tslot, 256);
-    if (threadIdx.x == 0) mbar_init(&bar, 1);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        mbar_init(&wbar[0], 1);
+        mbar_init(&wbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     for (int i = threadIdx.x; i < MLP_H; i += blockDim.x) {
         bias[i] = a.b[0][i];
         bias[MLP_H + i] = a.b[1][i];
@@ -193,26 +233,42 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(InferArgs a) {
     tc_fence_after();
     const uint32_t tbase = tslot;
     const uint32_t trow = tbase + ((uint32_t)(warp * 32) << 16);
-    uint32_t phase = 0;
+    uint32_t phase = 0, wph[2] = {0, 0};
     bool ok = true;
-    const int ntiles = (a.B + 127) / 128;
-    auto mma_run = [&](uint32_t dcol, int K, int N, uint32_t wrows_addr) {
-        // act (K wide) x weight rows (N x K) -> TMEM columns [dcol, dcol + N)
+    if (threadIdx.x == 0 && nimg > 0) {
+        mbar_expect_tx(&wbar[0], wimg_bytes(0));
+        bulk_g2s(wbuf[0], a.img + wimg_off(0), wimg_bytes(0), &wbar[0]);
+    }
+    int q = 0;  // weight images consumed so far
+    // MMAs of weight image q % WIMG_N (in wbuf[q & 1]) into TMEM columns
+    // [dcol, dcol + N); the copy of image q + 1 starts once they are issued
+    auto mma_img = [&](uint32_t dcol, int K, int N) {
+        const int buf = q & 1;
         fence_async_smem();
         __syncthreads();
+        if (ok) ok = mbar_wait(&wbar[buf], wph[buf], MB_POLLS);
+        ok = __syncthreads_and(ok);  // one verdict for the block
+        wph[buf] ^= 1;
         if (threadIdx.x == 0) {
             tc_fence_after();
             const uint32_t sbo = (uint32_t)(K / 8 * 128);
             const uint32_t idesc = tc_idesc_bf16(128, N);
-            for (int kk = 0; kk < K / 16; kk++)
-                tc_mma_bf16(tbase + dcol, tc_desc(smem_u32(act) + kk * 256, 128, sbo),
-                            tc_desc(wrows_addr + kk * 256, 128, sbo), idesc, kk > 0);
+            if (ok)
+                for (int kk = 0; kk < K / 16; kk++)
+                    tc_mma_bf16(tbase + dcol, tc_desc(smem_u32(act) + kk * 256, 128, sbo),
+                                tc_desc(smem_u32(wbuf[buf]) + kk * 256, 128, sbo), idesc, kk > 0);
             tc_commit(&bar);
+            if (ok && q + 1 < nimg) {  // the other buffer's last reader finished before this image began
+                const int nx = (q + 1) % WIMG_N;
+                mbar_expect_tx(&wbar[buf ^ 1], wimg_bytes(nx));
+                bulk_g2s(wbuf[buf ^ 1], a.img + wimg_off(nx), wimg_bytes(nx), &wbar[buf ^ 1]);
+            }
         }
-        ok = ok && mbar_wait(&bar, phase, MB_POLLS);
+        if (ok) ok = mbar_wait(&bar, phase, MB_POLLS);
+        ok = __syncthreads_and(ok);
         phase ^= 1;
+        q++;
         tc_fence_after();
-        __syncthreads();
     };
     auto hidden_epilogue = [&](int l) {
         // TMEM (256 columns) + bias, SiLU -> BF16 activations (K = 256 layout) in act
@@ -232,9 +288,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(InferArgs a) {
         }
         tc_fence_before();
     };
-    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int m0 = tile * 128;
-        {   // input: normalise, split into BF16 hi + lo, K = 128 layout (hi | lo)
+        if (ok) {   // input: normalise, split into BF16 hi + lo, K = 128 layout (hi | lo)
             const int r = threadIdx.x, row = m0 + r;
 #pragma unroll
             for (int k8 = 0; k8 < 8; k8++) {
@@ -251,19 +307,16 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(InferArgs a) {
                 *reinterpret_cast<uint4*>(act + tc_off(r, MLP_IN + k8 * 8, MLP_K0)) = *reinterpret_cast<uint4*>(lo);
             }
         }
-        stage_rows(wb, a.W[0], 0, MLP_H, MLP_K0);  // layer 0: [W0 | W0], 256 x 128 (64 KB)
-        mma_run(0, MLP_K0, MLP_H, smem_u32(wb));
-        hidden_epilogue(0);
-        for (int l = 1; l <= 2; l++) {
-            for (int h = 0; h < 2; h++) {
-                stage_rows(wb, a.W[l], h * 128, 128, MLP_H);
-                mma_run(h * 128, MLP_H, 128, smem_u32(wb));
-            }
-            hidden_epilogue(l);
-        }
-        stage_rows(wb, a.W[3], 0, MLP_OUT, MLP_H);
-        mma_run(0, MLP_H, MLP_OUT, smem_u32(wb));
-        {   // output: + bias, de-normalise
+        mma_img(0, MLP_K0, MLP_H);    // layer 0
+        if (ok) hidden_epilogue(0);
+        mma_img(0, MLP_H, 128);       // layer 1, outputs 0-127
+        mma_img(128, MLP_H, 128);     //          outputs 128-255
+        if (ok) hidden_epilogue(1);
+        mma_img(0, MLP_H, 128);       // layer 2
+        mma_img(128, MLP_H, 128);
+        if (ok) hidden_epilogue(2);
+        mma_img(0, MLP_H, MLP_OUT);   // layer 3
+        if (ok) {   // output: + bias, de-normalise, threshold
             const int r = warp * 32 + lane, row = m0 + r;
 #pragma unroll 1
             for (int c = 0; c < MLP_OUT; c += 16) {
@@ -283,7 +336,12 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(InferArgs a) {
             tc_fence_before();
         }
     }
-    if (!ok && threadIdx.x == 0) atomicAdd(a.err, 1u);
+    if (!ok) {
+        // a wait gave up: give a copy still in flight a last bounded chance to land
+        mbar_wait(&wbar[0], wph[0], MB_POLLS);
+        mbar_wait(&wbar[1], wph[1], MB_POLLS);
+        if (threadIdx.x == 0) atomicAdd(a.err, 1u);
+    }
     tc_fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tbase, 256);
@@ -459,6 +517,7 @@ struct MlpNet {
     __nv_bfloat16* Wb[MLP_NL] = {};
     __nv_bfloat16* WTb[MLP_NL] = {};
     __nv_bfloat16* W0c = nullptr;  // [W0 | W0] (256 x 128), the layer-0 operand for the hi/lo input pairs
+    uint8_t* img = nullptr;        // weight images of the inference kernel
     float* Gc = nullptr;           // gradient of [W0 | W0]
     float* norm = nullptr;    // in_mean, in_std, out_mean, out_std
     int step = 0;
@@ -497,6 +556,7 @@ static void free_net(MlpNet* n) {
         cudaFree(n->dZ[l]);
     }
     cudaFree(n->W0c);
+    cudaFree(n->img);
     cudaFree(n->Gc);
     cudaFree(n->norm);
     cudaFree(n->X);
@@ -513,6 +573,7 @@ static int refresh_bf16(MlpNet* n, cudaStream_t s) {
         k_wcast<<<(out * in + 255) / 256, 256, 0, s>>>(n->P + n->off(l), n->Wb[l], n->WTb[l], out, in);
     }
     k_w0_pair<<<(MLP_H * MLP_K0 + 255) / 256, 256, 0, s>>>(n->Wb[0], n->W0c);
+    k_wimage<<<(WIMG_CHUNKS + 255) / 256, 256, 0, s>>>(n->W0c, n->Wb[1], n->Wb[2], n->Wb[3], n->img);
     MLP_TRY(cudaGetLastError());
     return REPROBUS_OK;
 }
@@ -620,13 +681,11 @@ int mlp_infer(void* net, const float* X, float* Y, int B, cudaStream_t s) {
     a.X = X;
     a.Y = Y;
     a.B = B;
-    for (int l = 0; l < MLP_NL; l++) {
-        a.W[l] = l == 0 ? n->W0c : n->Wb[l];
-        a.b[l] = n->P + n->off(l) + wsize(l);
-    }
+    a.img = n->img;
+    for (int l = 0; l < MLP_NL; l++) a.b[l] = n->P + n->off(l) + wsize(l);
     a.norm = n->norm;
     a.err = n->err;
-    const size_t smem = 131072 + (3 * MLP_H + MLP_OUT + MLP_NNORM) * sizeof(float);
+    const size_t smem = 196608 + (3 * MLP_H + MLP_OUT + MLP_NNORM) * sizeof(float);
     MLP_TRY(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int dev = 0, nsm = 0;
     MLP_TRY(cudaGetDevice(&dev));
@@ -673,6 +732,7 @@ extern "C" int reprobus_mlp_create(int batch_cap, unsigned long long seed, void*
         al((void**)&n->dZ[l], (size_t)batch_cap * mlp_fan_out(l) * 2);
     }
     al((void**)&n->W0c, (size_t)MLP_H * MLP_K0 * 2);
+    al((void**)&n->img, WIMG_TOTAL);
     al((void**)&n->Gc, (size_t)MLP_H * MLP_K0 * 4);
     al((void**)&n->norm, MLP_NNORM * 4);
     al((void**)&n->X, (size_t)batch_cap * MLP_K0 * 2);
