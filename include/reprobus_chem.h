@@ -50,6 +50,10 @@ enum {
                                        the HNO3-gas copy (:431-450) in the call  */
 #define REPROBUS_CHECK_FINITE  0x2  /* count NaN/Inf in outputs, return
                                        REPROBUS_ERR_NONFINITE when any           */
+#define REPROBUS_USE_GRAPH     0x4  /* launch the step as one CUDA graph (each
+                                       solver configuration runs once directly
+                                       first; the graph is captured per call and
+                                       updated in place)                         */
 
 /* ---- solvers (reprobus_chem_set_solver) ----------------------------------- */
 #define REPROBUS_SOLVER_REF5          0  /* the reference scheme: niter fixed passes  */
@@ -80,6 +84,7 @@ typedef struct reprobus_stats {
                                   converge (warm-start misses, fallbacks)            */
     double solve_ms;           /* Newton solvers: device time of the persistent solve
                                   kernel (its first launch)                          */
+    int graph;                 /* 1 when the step ran as a CUDA graph               */
 } reprobus_stats;
 
 /* ---- diagnostics layout (reprobus_chem_rates_*) ----------------------------
@@ -145,6 +150,10 @@ int reprobus_chem_free(void* handle);
 /* Makes the handle launch on the caller's CUDA stream (a cudaStream_t passed
  * as void*; NULL restores the handle's own stream). */
 int reprobus_chem_set_stream(void* handle, void* cuda_stream);
+
+/* Switches REPROBUS_USE_GRAPH on or off for the handle. No counterpart in
+ * the reference. */
+int reprobus_chem_set_graph(void* handle, int on);
 
 /* Selects how the cells are integrated (default REPROBUS_SOLVER_REF5).
  * The Newton solvers return the fixed point of the reference's pass map

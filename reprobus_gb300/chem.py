@@ -28,6 +28,7 @@ LIBPATH = os.path.join(HERE, "libreprobus_gb300.so")
 
 FUSE_CONSERV = 0x1
 CHECK_FINITE = 0x2
+USE_GRAPH = 0x4
 SOLVER_REF5, SOLVER_NEWTON64, SOLVER_NEWTON_MIXED = 0, 1, 2
 
 ERRORS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NONFINITE", 4: "ERR_NOCONV", 5: "ERR_TIMEOUT",
@@ -40,7 +41,7 @@ EXPORTS = [
     "reprobus_chem_rates_dev", "reprobus_conserv_dev", "reprobus_chem_step_noalloc", "reprobus_chem_set_solver",
     "reprobus_chem_set_tuning", "reprobus_mlp_create", "reprobus_mlp_free", "reprobus_mlp_nparams",
     "reprobus_mlp_set_params", "reprobus_mlp_get_params", "reprobus_mlp_train_step", "reprobus_mlp_grads",
-    "reprobus_mlp_forward", "reprobus_chem_set_mlp", "reprobus_chem_features_dev",
+    "reprobus_mlp_forward", "reprobus_chem_set_mlp", "reprobus_chem_features_dev", "reprobus_chem_set_graph",
 ]
 NOALLOC_SCRATCH_DOUBLES = 1 << 20
 
@@ -58,7 +59,7 @@ class Stats(ctypes.Structure):
                 ("max_newton_iters", ctypes.c_int), ("solver", ctypes.c_int),
                 ("lanes_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int), ("z_shared", ctypes.c_int),
                 ("warm_start", ctypes.c_int), ("warm_restarts", ctypes.c_longlong),
-                ("failed_iters", ctypes.c_longlong), ("solve_ms", ctypes.c_double)]
+                ("failed_iters", ctypes.c_longlong), ("solve_ms", ctypes.c_double), ("graph", ctypes.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -103,6 +104,7 @@ def load_library(path: str = LIBPATH):
     lib.reprobus_mlp_grads.argtypes = [vp, vp, vp, i, fp, fp, vp]
     lib.reprobus_mlp_forward.argtypes = [vp, vp, vp, i, vp]
     lib.reprobus_chem_set_mlp.argtypes = [vp, vp]
+    lib.reprobus_chem_set_graph.argtypes = [vp, i]
     lib.reprobus_chem_features_dev.argtypes = [vp, i, i, d, d, vp, vp, vp, vp, vp, i, vp, vp, vp]
     for name in EXPORTS:
         if name not in ("reprobus_version", "reprobus_last_error"):
@@ -192,6 +194,10 @@ class ChemStep:
         """Shape of the persistent Newton solve kernel (lanes_per_block 0:
         autotune on the first Newton step of each matrix precision)."""
         _check(self.lib.reprobus_chem_set_tuning(self._h, int(lanes_per_block), int(blocks_per_sm), int(zshared)))
+
+    def set_graph(self, on=True):
+        """Launch each step as one CUDA graph (REPROBUS_USE_GRAPH)."""
+        _check(self.lib.reprobus_chem_set_graph(self._h, 1 if on else 0))
 
     def set_mlp(self, net):
         """Attaches a reprobus_gb300.mlp.Mlp as the Newton solvers' warm start

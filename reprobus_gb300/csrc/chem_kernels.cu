@@ -548,6 +548,10 @@ struct Handle {
     int want_lanes = 0, want_bps = 0, want_zs = 0;   // reprobus_chem_set_tuning; lanes 0: autotune
     const NtVariant* nt_var[2] = {nullptr, nullptr};
     int nt_bps[2] = {0, 0};
+    // CUDA graph of the step (REPROBUS_USE_GRAPH)
+    cudaGraphExec_t gexec = nullptr;
+    int gexec_sig = -1;
+    unsigned graph_ready = 0;  // configurations that have run once directly
     // learned warm start (reprobus_chem_set_mlp): the network and its buffers
     void* mlp = nullptr;
     float* mlp_feat = nullptr;
@@ -603,6 +607,7 @@ static void free_handle(Handle* h) {
     cudaFree(h->mlp_y);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
     if (h->ev2) cudaEventDestroy(h->ev2);
     if (h->ev3) cudaEventDestroy(h->ev3);
     if (h->own) cudaStreamDestroy(h->own);
@@ -826,7 +831,7 @@ static int choose_shape(Handle* h, Params& P, bool mixed) {
 }
 
 // the Newton pipeline of one step (after k_columns)
-static int launch_newton(Handle* h, Params& P, int* launches, bool timed) {
+static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool capturing) {
     int rc = ensure_newton(h);
     if (rc) return rc;
     const bool mixed = h->solver == REPROBUS_SOLVER_NEWTON_MIXED;
@@ -859,9 +864,11 @@ static int launch_newton(Handle* h, Params& P, int* launches, bool timed) {
         k_nt_warm<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
         *launches += 2;
     }
-    if (timed) CUDA_TRY(cudaEventRecord(h->ev2, h->stream));
+    if (timed) CUDA_TRY(capturing ? cudaEventRecordWithFlags(h->ev2, h->stream, cudaEventRecordExternal)
+                                  : cudaEventRecord(h->ev2, h->stream));
     CUDA_TRY(h->nt_var[ip]->launch(P, grid, h->stream));
-    if (timed) CUDA_TRY(cudaEventRecord(h->ev3, h->stream));
+    if (timed) CUDA_TRY(capturing ? cudaEventRecordWithFlags(h->ev3, h->stream, cudaEventRecordExternal)
+                                  : cudaEventRecord(h->ev3, h->stream));
     *launches += 3;
     if (warm) {
         // misses of the warm start: the plain start, a second pass of the solve kernel
@@ -875,29 +882,82 @@ static int launch_newton(Handle* h, Params& P, int* launches, bool timed) {
 }
 
 // enqueue the kernels of one step on h->stream (device arrays in P)
-static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
+// the work of one step on h->stream (device arrays in P); capturing: the
+// calls are being recorded into a CUDA graph (events become graph nodes)
+static int enqueue_step(Handle* h, Params& P, bool capturing, int* launches) {
     const int tb = 128;
-    int launches = 0;
-    P.fuse = (h->flags & REPROBUS_FUSE_CONSERV) ? 1 : 0;
-    P.check = (h->flags & REPROBUS_CHECK_FINITE) ? 1 : 0;
     const bool counters = P.check || h->solver != REPROBUS_SOLVER_REF5;
     if (counters) CUDA_TRY(cudaMemsetAsync(h->d_count, 0, 8 * sizeof(unsigned long long), h->stream));
-    if (st) CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
     k_columns<<<(P.ncol + tb - 1) / tb, tb, 0, h->stream>>>(P);
-    launches++;
+    (*launches)++;
     if (h->solver == REPROBUS_SOLVER_REF5) {
         k_chem<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
-        launches++;
+        (*launches)++;
     } else {
-        int rc = launch_newton(h, P, &launches, st != nullptr);
+        int rc = launch_newton(h, P, launches, true, capturing);
         if (rc) return rc;
     }
     if (P.fuse && h->nivbas < h->niv) {
         long long nt = (long long)P.nlon * P.nrows * (h->niv - h->nivbas);
         k_tail<<<(unsigned)((nt + 255) / 256), 256, 0, h->stream>>>(P);
-        launches++;
+        (*launches)++;
     }
     CUDA_TRY(cudaGetLastError());
+    return REPROBUS_OK;
+}
+
+// which solver configuration a step runs (graphs are reused per configuration)
+static int step_signature(const Handle* h) { return h->solver * 2 + (h->mlp ? 1 : 0); }
+
+// One step: directly, or (REPROBUS_USE_GRAPH, once this configuration has run
+// once directly, so that its buffers exist and its solve kernel is tuned) as
+// a CUDA graph: the step's calls are captured, the handle's executable graph
+// is updated in place (or instantiated), and launched as one unit.
+static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
+    int launches = 0;
+    P.fuse = (h->flags & REPROBUS_FUSE_CONSERV) ? 1 : 0;
+    P.check = (h->flags & REPROBUS_CHECK_FINITE) ? 1 : 0;
+    const bool counters = P.check || h->solver != REPROBUS_SOLVER_REF5;
+    const int sig = step_signature(h);
+    const bool graph = (h->flags & REPROBUS_USE_GRAPH) && (h->graph_ready & (1u << sig));
+    if (st) CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+    if (!graph) {
+        int rc = enqueue_step(h, P, false, &launches);
+        if (rc) return rc;
+        h->graph_ready |= 1u << sig;
+    } else {
+        cudaGraph_t g = nullptr;
+        CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_step(h, P, true, &launches);
+        const cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        CUDA_TRY(e);
+        if (h->gexec && h->gexec_sig == sig) {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(h->gexec, g, &info) != cudaSuccess) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(h->gexec);
+                h->gexec = nullptr;
+            }
+        } else if (h->gexec) {
+            cudaGraphExecDestroy(h->gexec);
+            h->gexec = nullptr;
+        }
+        if (!h->gexec) {
+            const cudaError_t ei = cudaGraphInstantiate(&h->gexec, g, 0);
+            if (ei != cudaSuccess) {
+                cudaGraphDestroy(g);
+                h->gexec = nullptr;
+                return set_err(REPROBUS_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(ei));
+            }
+            h->gexec_sig = sig;
+        }
+        cudaGraphDestroy(g);
+        CUDA_TRY(cudaGraphLaunch(h->gexec, h->stream));
+    }
     if (st) {
         CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
         CUDA_TRY(cudaEventSynchronize(h->ev1));
@@ -925,6 +985,7 @@ static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
         st->warm_start = h->solver != REPROBUS_SOLVER_REF5 && h->mlp ? 1 : 0;
         st->warm_restarts = 0;
         st->failed_iters = 0;
+        st->graph = graph ? 1 : 0;
     }
     if (counters && (st || P.check)) {
         unsigned long long c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -967,9 +1028,17 @@ extern "C" int reprobus_chem_set_tuning(void* handle, int lanes_per_block, int b
     return REPROBUS_OK;
 }
 
+extern "C" int reprobus_chem_set_graph(void* handle, int on) {
+    Handle* h = (Handle*)handle;
+    if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
+    h->flags = on ? (h->flags | REPROBUS_USE_GRAPH) : (h->flags & ~REPROBUS_USE_GRAPH);
+    return REPROBUS_OK;
+}
+
 extern "C" int reprobus_chem_set_mlp(void* handle, void* net) {
     Handle* h = (Handle*)handle;
     if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
+    if (h->mlp != net) h->graph_ready &= ~(1u << (h->solver * 2 + 1));  // a new network runs directly once
     h->mlp = net;
     return REPROBUS_OK;
 }

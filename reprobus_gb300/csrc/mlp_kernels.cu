@@ -521,6 +521,7 @@ struct MlpNet {
     float* Gc = nullptr;           // gradient of [W0 | W0]
     float* norm = nullptr;    // in_mean, in_std, out_mean, out_std
     int step = 0;
+    int nsm = 0;  // SM count (set on the first inference)
     // training activations
     __nv_bfloat16* X = nullptr;
     float* Z[MLP_NL] = {};
@@ -686,10 +687,13 @@ int mlp_infer(void* net, const float* X, float* Y, int B, cudaStream_t s) {
     a.norm = n->norm;
     a.err = n->err;
     const size_t smem = 196608 + (3 * MLP_H + MLP_OUT + MLP_NNORM) * sizeof(float);
-    MLP_TRY(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int dev = 0, nsm = 0;
-    MLP_TRY(cudaGetDevice(&dev));
-    MLP_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    if (!n->nsm) {  // once per network (not while a graph is being captured)
+        int dev = 0;
+        MLP_TRY(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        MLP_TRY(cudaGetDevice(&dev));
+        MLP_TRY(cudaDeviceGetAttribute(&n->nsm, cudaDevAttrMultiProcessorCount, dev));
+    }
+    const int nsm = n->nsm;
     const int tiles = (B + 127) / 128;
     k_mlp_infer<<<tiles < nsm ? tiles : nsm, 128, smem, s>>>(a);
     MLP_TRY(cudaGetLastError());
