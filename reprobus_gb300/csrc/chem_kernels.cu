@@ -360,7 +360,6 @@ __global__ void __launch_bounds__(128) k_nt_setup(Params P) {
 #pragma unroll
         for (int i = 0; i < 16; i++) o[i] = make_float4(fe[4 * i], fe[4 * i + 1], fe[4 * i + 2], fe[4 * i + 3]);
     }
-    if (cell == 0) P.nt_head[3] = P.ncell;
     P.nt_stat[cell] = 0;
     if (day)
         P.nt_list[atomicAdd(P.nt_head + 1, 1)] = cell;
@@ -414,7 +413,10 @@ __global__ void __launch_bounds__(128) k_nt_restart(Params P) {
 #pragma unroll
     for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = cc[n];
     P.nt_stat[cell] = 0;
-    P.nt_list[atomicAdd(P.nt_head + 3, 1)] = cell;
+    if (r[NT_RDAY] != 0.)
+        P.nt_list[atomicAdd(P.nt_head + 1, 1)] = cell;
+    else
+        P.nt_list[P.ncell - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
     atomicAdd(P.nonfinite + 4, 1ULL);
 }
 
@@ -731,7 +733,8 @@ static void fill_params(const Handle* h, Params& P, int ilat0, int ilat1) {
 static int nt_all_variants(bool mixed, const NtVariant** out, int cap) {
     int n = 0, k = 0;
     const NtVariant* lists[2];
-    int counts[2];
+    int counts[2] = {0, 0};
+    const int nl = 2;
     if (mixed) {
         lists[0] = nt_variants_f32_zr(&counts[0]);
         lists[1] = nt_variants_f32_zs(&counts[1]);
@@ -739,7 +742,7 @@ static int nt_all_variants(bool mixed, const NtVariant** out, int cap) {
         lists[0] = nt_variants_f64_zr(&counts[0]);
         lists[1] = nt_variants_f64_zs(&counts[1]);
     }
-    for (int l = 0; l < 2; l++)
+    for (int l = 0; l < nl; l++)
         for (k = 0; k < counts[l] && n < cap; k++) out[n++] = &lists[l][k];
     return n;
 }
@@ -752,14 +755,14 @@ static int ensure_newton(Handle* h) {
     CUDA_TRY(cudaMalloc(&h->nt_x, nc * NT_NX * sizeof(double)));
     CUDA_TRY(cudaMalloc(&h->nt_stat, nc * sizeof(int)));
     CUDA_TRY(cudaMalloc(&h->nt_list, nc * sizeof(int)));
-    CUDA_TRY(cudaMalloc(&h->nt_head, 4 * sizeof(int)));
+    CUDA_TRY(cudaMalloc(&h->nt_head, 8 * sizeof(int)));
     CUDA_TRY(cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->device));
     return REPROBUS_OK;
 }
 
 static int enqueue_setup(Handle* h, Params& P, bool mixed) {
     const int tb = 128;
-    CUDA_TRY(cudaMemsetAsync(h->nt_head, 0, 4 * sizeof(int), h->stream));
+    CUDA_TRY(cudaMemsetAsync(h->nt_head, 0, 8 * sizeof(int), h->stream));
     if (mixed)
         k_nt_setup<true><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     else
@@ -872,7 +875,7 @@ static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool c
     *launches += 3;
     if (warm) {
         // misses of the warm start: the plain start, a second pass of the solve kernel
-        CUDA_TRY(cudaMemsetAsync(h->nt_head, 0, 4 * sizeof(int), h->stream));
+        CUDA_TRY(cudaMemsetAsync(h->nt_head, 0, 8 * sizeof(int), h->stream));
         k_nt_restart<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
         CUDA_TRY(h->nt_var[ip]->launch(P, grid, h->stream));
         *launches += 2;

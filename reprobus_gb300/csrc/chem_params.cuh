@@ -42,7 +42,8 @@ struct Params {
     double* nt_x;                   // iterate x (NT_NX per cell)
     int* nt_stat;                   // 0 active, >0 converged at that iteration, -1 failed
     int* nt_list;                   // work queue: day cells from the front, night cells from the back
-    int* nt_head;                   // [0] next queue entry, [1] day count, [2] night count, [3] queue length
+    int* nt_head;                   // [0] next queue entry, [1] day count, [2] night count,
+                                    // [4] next day entry, [5] next night entry (per-mode queues)
     int npass_plain;                // reference passes of the plain start (restart after a warm-start miss)
     int warm;                       // 1: features for the warm-start network, start from its prediction
     float* mlp_feat;                // 64 raw features per cell (row-major)

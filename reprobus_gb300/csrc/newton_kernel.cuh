@@ -28,13 +28,19 @@ __device__ __forceinline__ void nt_load_fix(const T* r, NtFixT<T>& F) {
     F.rain_hno3 = r[9]; F.rain_hcl = r[10]; F.rain_hbr = r[11]; F.rain_h2o2 = r[12]; F.dt = r[13];
 }
 
+// entry q of the queue: day cells at list[0 .. nday), night cells from the back
+__device__ __forceinline__ int nt_queue_cell(const Params& P, int q, int nday) {
+    return q < nday ? P.nt_list[q] : P.nt_list[P.ncell - 1 - (q - nday)];
+}
+
 template <typename TJ, int NTH, bool ZS>
 __global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
     static_assert(NTH % 32 == 0, "whole warps");
     extern __shared__ __align__(16) unsigned char nt_smem[];
     const SJ<TJ, NTH> J{reinterpret_cast<TJ*>(nt_smem) + threadIdx.x};
     const unsigned lane = threadIdx.x & 31u;
-    const int nq = P.nt_head[3];  // queue length (set by the kernel that filled the queue)
+    const int nday = P.nt_head[1], nnight = P.nt_head[2];  // queue: day cells, then night cells
+    const int nq = nday + nnight;
     int cell = -1;  // >= 0: cell in work; -1: wants a cell; -2: queue exhausted
     int it = 0;
     for (;;) {
@@ -46,7 +52,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
             base = __shfl_sync(0xffffffffu, base, leader);
             if (cell == -1) {
                 const int q = base + __popc(want & ((1u << lane) - 1u));
-                cell = q < nq ? P.nt_list[q] : -2;
+                cell = q < nq ? nt_queue_cell(P, q, nday) : -2;
                 it = 0;
             }
         }

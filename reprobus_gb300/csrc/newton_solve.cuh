@@ -115,14 +115,14 @@ __device__ __forceinline__ void nt_jacobian_call(bool day, const FFT& FT, PKT KT
 // cell's NT_NSLOT matrix slots. Returns false when the step is not finite;
 // *step = max |z_i|.
 template <typename TJ, typename PZ>
-__device__ __forceinline__ bool nt_update(double* x, double floor_, PZ z, TJ* step);
+__device__ __forceinline__ bool nt_update(double* x, double floor_, PZ z, TJ* step, bool active);
 
 // ZSHARED (device only): z in NT_NX shared-memory slots after the matrix (the
 // residual as a call of its own) instead of registers (residual inlined).
 template <typename TJ, bool ZSHARED = false, typename FF, typename PK, typename PC, typename FFT, typename PKT,
           typename PJ>
 __device__ __forceinline__ bool nt_iterate(const FF& F, PK K, PK tj, PK het, PC ck0, const FFT& FT, PKT KT, PKT tjT,
-                                           PKT hetT, bool day, double* x, PJ J, TJ* step) {
+                                           PKT hetT, bool day, double* x, PJ J, TJ* step, bool active = true) {
     const double floor_ = 1e-20 * F.hnm;
     nt_jacobian_call<TJ>(day, FT, KT, tjT, hetT, x, floor_, J);
     NT_FENCE();
@@ -131,19 +131,20 @@ __device__ __forceinline__ bool nt_iterate(const FF& F, PK K, PK tj, PK het, PC 
         const SJZ<TJ, PJ::stride> z{J.p};
         nt_rhs_fn<TJ>(day, F, K, tj, het, ck0, x, floor_, z);
         nt_factor_solve<TJ>(J, z, TJ(NT_TINY));
-        return nt_update<TJ>(x, floor_, z, step);
+        return nt_update<TJ>(x, floor_, z, step, active);
     }
 #endif
     TJ z[NT_NX];
     nt_rhs<TJ>(day, F, K, tj, het, ck0, x, floor_, (TJ*)z);
     nt_factor_solve<TJ>(J, (TJ*)z, TJ(NT_TINY));
-    return nt_update<TJ>(x, floor_, (const TJ*)z, step);
+    return nt_update<TJ>(x, floor_, (const TJ*)z, step, active);
 }
 
 // FP64 update x_i += s_i z_i (negative results clipped to x_i / 10);
-// returns false when a step is not finite; *step = max |z_i|
+// returns false when a step is not finite; *step = max |z_i|. active false:
+// a lane that runs the iteration only to keep its warp converged writes nothing.
 template <typename TJ, typename PZ>
-__device__ __forceinline__ bool nt_update(double* x, double floor_, PZ z, TJ* step) {
+__device__ __forceinline__ bool nt_update(double* x, double floor_, PZ z, TJ* step, bool active) {
     const int fh = nt_exp_hi(floor_);
     TJ st = 0;
     bool finite = true;
@@ -156,7 +157,7 @@ __device__ __forceinline__ bool nt_update(double* x, double floor_, PZ z, TJ* st
         const TJ y = fabs(zi);
         if (!(y <= TJ(1e30))) finite = false;
         st = fmax(st, y);
-        x[i] = xn;
+        if (active) x[i] = xn;
     }
     *step = st;
     return finite;

@@ -102,3 +102,23 @@ def test_mixed_and_fp64_newton_agree(case):
     b, _ = _run(case, SOLVER_NEWTON_MIXED)
     e = _species_err(b, a, case.nivbas)
     assert np.percentile(e, 99.9) <= 1e-9
+
+
+@pytest.mark.parametrize("lanes", [128, 64])
+def test_mixed_solve_kernel_shapes_agree_with_the_oracle(case, fixed_point, lanes):
+    """Compiled shapes of the mixed solve kernel, forced (the autotuner's
+    candidates): 128 and 64 lanes per block."""
+    from reprobus_gb300.resident import DeviceCase
+    fp, stat, _ = fixed_point
+    h = ChemStep.for_case(case, niter=5, flags=0)
+    h.set_solver(SOLVER_NEWTON_MIXED, npass=1, maxit=12, tol=1e-10)
+    h.set_tuning(lanes, 0, 0)
+    dc = DeviceCase(case)
+    st = h.step_dev(1, case.nlat, case.daynum, case.dt, *dc.args(), stats=True)
+    got = dc.state_host()
+    h.close()
+    assert st["lanes_per_block"] == lanes
+    fell_back = oracle.map_residual(case, got["qj1"], got["hc"]) > MAP_TOL
+    assert fell_back.sum() <= st["fallbacks"] <= 0.01 * case.ncells
+    ok = (stat > 0) & ~fell_back
+    assert _species_err(got, fp, case.nivbas)[ok].max() <= ERR_TOL
