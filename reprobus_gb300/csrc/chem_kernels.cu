@@ -273,11 +273,15 @@ __global__ void __launch_bounds__(128) k_chem(Params P) {
 // method on the generated equations (newton_solve.cuh), Jacobian and LU in TJ
 // (double: plain FP64 solver; float: mixed precision), residual and update in
 // FP64. One step:
-//   k_nt_setup   one thread per cell: rate stage, P.npass reference passes from
-//                the start state -> iterate x and the cell's record (rates,
-//                fixed constants, day flag, ck0; FP32 copies for the mixed
-//                solver); the cell enters the work queue (day cells from the
-//                front, night cells from the back)
+//   k_nt_setup   one thread per cell: rate stage -> the cell's record (rates,
+//                fixed constants, zenith angle, ck0, aerosol area; FP32
+//                copies for the mixed solver)
+//   k_nt_start   one thread per cell: P.npass_plain reference passes from the
+//                record's start state -> iterate x; the cell enters the work
+//                queue (day cells from the front, night cells from the back);
+//                warm start: the network's features (then k_mlp_infer and
+//                k_nt_warm). Two kernels rather than one: the rate stage
+//                alone is a smaller program for the instruction cache.
 //   k_nt_solve   persistent kernel, one lane per cell, lanes refilled from the
 //                queue (newton_kernel.cuh)
 //   k_nt_finish  one thread per cell: cells unconverged after P.maxit
@@ -289,19 +293,19 @@ __global__ void __launch_bounds__(128) k_chem(Params P) {
 // number densities after the plain start's reference passes; floored at
 // 1e-30), T, ln p, cos(sza), log10 of the aerosol surface area (floored at
 // 1e-12), latitude, time of day (fraction), 0
-__device__ __forceinline__ void cell_features(const Params& P, const CellPro& C, const double* ck, const double* cc,
-                                              float* f) {
+__device__ __forceinline__ void cell_features(const Params& P, size_t g, double hnm, double sza, double surf,
+                                              const double* ck, const double* cc, float* f) {
     // log10 in FP32 (the features are FP32): ratio in FP64, then float
-    const double rh = 1. / C.F.hnm;
+    const double rh = 1. / hnm;
 #pragma unroll 6
     for (int n = 0; n < NBCON - 1; n++) f[n] = log10f((float)fmax(ck[n] * rh, 1e-30));
 #pragma unroll 5
     for (int n = 0; n < NCM; n++) f[NBCON - 1 + n] = log10f((float)fmax(cc[n] * rh, 1e-30));
-    const size_t gi = P.trajoff + C.g;
+    const size_t gi = P.trajoff + g;
     f[57] = (float)P.trajtem[gi];
-    f[58] = (float)log(P.trajpre[gi]);
-    f[59] = (float)cos(C.F.sza * (PI / 180.));
-    f[60] = (float)log10(fmax(C.A.surf, 1e-12));
+    f[58] = logf((float)P.trajpre[gi]);
+    f[59] = cosf((float)(sza * (PI / 180.)));
+    f[60] = log10f((float)fmax(surf, 1e-12));
     f[61] = (float)P.trajlat[gi];
     f[62] = (float)(P.sc.ut / 24.);
     f[63] = 0.f;
@@ -314,21 +318,8 @@ __global__ void __launch_bounds__(128) k_nt_setup(Params P) {
     CellPro C;
     cell_prologue<false>(P, cell, C);
     const CellFix& F = C.F;
-    double ck[NBCON], cc[NCM];
-#pragma unroll
-    for (int n = 0; n < NBCON; n++) ck[n] = C.ck0[n];
-#pragma unroll
-    for (int n = 0; n < NCM; n++) cc[n] = C.cc0[n];
-#pragma unroll 1
-    for (int it = 0; it < P.npass; it++) cell_pass(F, C.K, C.tj, C.A.het, C.ck0, P.sc.dt, ck, cc);
-    double* x = P.nt_x + (size_t)cell * NT_NX;
-#pragma unroll
-    for (int n = 0; n < NBCON - 1; n++) x[n] = ck[n];
-#pragma unroll
-    for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = cc[n];
     const double fx[14] = {F.o2, F.n2, F.h2, F.co2, F.hnm, F.parthno3, F.parth2o, F.parthcl, F.parthbr,
                            F.rain_hno3, F.rain_hcl, F.rain_hbr, F.rain_h2o2, P.sc.dt};
-    const bool day = F.sza <= 95.;
     double* r = P.nt_rec + (size_t)cell * NT_REC;
 #pragma unroll 4
     for (int n = 0; n < NRATE; n++) r[NT_RK + n] = C.K[n];
@@ -338,7 +329,8 @@ __global__ void __launch_bounds__(128) k_nt_setup(Params P) {
     for (int n = 0; n < 9; n++) r[NT_RH + n] = C.A.het[n];
 #pragma unroll
     for (int n = 0; n < 14; n++) r[NT_RF + n] = fx[n];
-    r[NT_RDAY] = day ? 1. : 0.;
+    r[NT_RSZA] = F.sza;
+    r[NT_RSURF] = C.A.surf;
 #pragma unroll 4
     for (int n = 0; n < NBCON; n++) r[NT_RCK0 + n] = C.ck0[n];
     if (MIXED) {
@@ -351,48 +343,27 @@ __global__ void __launch_bounds__(128) k_nt_setup(Params P) {
         for (int n = 0; n < 9; n++) q[NT_RH + n] = (float)C.A.het[n];
 #pragma unroll
         for (int n = 0; n < 14; n++) q[NT_RF + n] = (float)fx[n];
-        q[NT_RDAY] = day ? 1.f : 0.f;
+        q[NT_RSZA] = (float)F.sza;
     }
-    if (P.warm) {
-        float fe[64];
-        cell_features(P, C, ck, cc, fe);
-        float4* o = reinterpret_cast<float4*>(P.mlp_feat + (size_t)cell * 64);
-#pragma unroll
-        for (int i = 0; i < 16; i++) o[i] = make_float4(fe[4 * i], fe[4 * i + 1], fe[4 * i + 2], fe[4 * i + 3]);
-    }
-    P.nt_stat[cell] = 0;
-    if (day)
-        P.nt_list[atomicAdd(P.nt_head + 1, 1)] = cell;
-    else
-        P.nt_list[P.ncell - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
 }
 
-// warm start: x_i = max(x_i, 1e-30 hnm) 10^y_i from the network's prediction
-__global__ void __launch_bounds__(128) k_nt_warm(Params P) {
+// the plain start of a cell from its record: P.npass_plain reference passes
+// from the start state (ck0 from the record, cc from hc) -> x; the cell
+// enters the work queue (day cells from the front, night cells from the
+// back); with the warm start, the network's features of that plain start.
+// restart: only cells whose warm start missed (stat < 0).
+template <bool RESTART>
+__global__ void __launch_bounds__(128) k_nt_start(Params P) {
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= P.ncell) return;
-    const double hnm = P.nt_rec[(size_t)cell * NT_REC + NT_RF + 4];
-    double* x = P.nt_x + (size_t)cell * NT_NX;
-    const float* y = P.mlp_y + (size_t)cell * 64;
-#pragma unroll 4
-    for (int i = 0; i < NT_NX; i++) {
-        const float yi = fminf(fmaxf(y[i], -30.f), 30.f);
-        x[i] = fmax(x[i], 1e-30 * hnm) * (double)exp10f(yi);
-    }
-}
-
-// cells whose warm start missed the convergence test start again from the
-// plain start (P.npass_plain reference passes) and re-enter the queue
-__global__ void __launch_bounds__(128) k_nt_restart(Params P) {
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= P.ncell || P.nt_stat[cell] >= 0) return;
+    if (RESTART && P.nt_stat[cell] >= 0) return;
     const double* r = P.nt_rec + (size_t)cell * NT_REC;
     CellFix F;
     F.o2 = r[NT_RF]; F.n2 = r[NT_RF + 1]; F.h2 = r[NT_RF + 2]; F.co2 = r[NT_RF + 3]; F.hnm = r[NT_RF + 4];
     F.parthno3 = r[NT_RF + 5]; F.parth2o = r[NT_RF + 6]; F.parthcl = r[NT_RF + 7]; F.parthbr = r[NT_RF + 8];
     F.rain_hno3 = r[NT_RF + 9]; F.rain_hno4 = 0.; F.rain_hcl = r[NT_RF + 10]; F.rain_hbr = r[NT_RF + 11];
     F.rain_h2o2 = r[NT_RF + 12]; F.rain_ch2o = 0.; F.rain_ch3o2h = 0.;
-    F.sza = r[NT_RDAY] != 0. ? 0. : 180.;
+    F.sza = r[NT_RSZA];
     const size_t g = cell_global(P, cell), pl = plane3(P);
     double K[NRATE], tj[NPHOT], het[9], ck0[NBCON], ck[NBCON], cc[NCM];
 #pragma unroll
@@ -412,12 +383,33 @@ __global__ void __launch_bounds__(128) k_nt_restart(Params P) {
     for (int n = 0; n < NBCON - 1; n++) x[n] = ck[n];
 #pragma unroll
     for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = cc[n];
+    if (!RESTART && P.warm) {
+        float fe[64];
+        cell_features(P, g, F.hnm, F.sza, r[NT_RSURF], ck, cc, fe);
+        float4* o = reinterpret_cast<float4*>(P.mlp_feat + (size_t)cell * 64);
+#pragma unroll
+        for (int i = 0; i < 16; i++) o[i] = make_float4(fe[4 * i], fe[4 * i + 1], fe[4 * i + 2], fe[4 * i + 3]);
+    }
     P.nt_stat[cell] = 0;
-    if (r[NT_RDAY] != 0.)
+    if (F.sza <= 95.)
         P.nt_list[atomicAdd(P.nt_head + 1, 1)] = cell;
     else
         P.nt_list[P.ncell - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
-    atomicAdd(P.nonfinite + 4, 1ULL);
+    if (RESTART) atomicAdd(P.nonfinite + 4, 1ULL);
+}
+
+// warm start: x_i = max(x_i, 1e-30 hnm) 10^y_i from the network's prediction
+__global__ void __launch_bounds__(128) k_nt_warm(Params P) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= P.ncell) return;
+    const double hnm = P.nt_rec[(size_t)cell * NT_REC + NT_RF + 4];
+    double* x = P.nt_x + (size_t)cell * NT_NX;
+    const float* y = P.mlp_y + (size_t)cell * 64;
+#pragma unroll 4
+    for (int i = 0; i < NT_NX; i++) {
+        const float yi = fminf(fmaxf(y[i], -30.f), 30.f);
+        x[i] = fmax(x[i], 1e-30 * hnm) * (double)exp10f(yi);
+    }
 }
 
 __global__ void __launch_bounds__(128) k_nt_finish(Params P) {
@@ -434,7 +426,7 @@ __global__ void __launch_bounds__(128) k_nt_finish(Params P) {
     F.parth2o = f[6]; F.parthcl = f[7]; F.parthbr = f[8]; F.rain_hno3 = f[9];
     F.rain_hno4 = 0.; F.rain_hcl = f[10]; F.rain_hbr = f[11]; F.rain_h2o2 = f[12];
     F.rain_ch2o = 0.; F.rain_ch3o2h = 0.;
-    F.sza = r[NT_RDAY] != 0. ? 0. : 180.;
+    F.sza = r[NT_RSZA];
     const size_t pl = plane3(P);
     double ck[NBCON], cc[NCM];
     if (stat > 0) {
@@ -767,6 +759,7 @@ static int enqueue_setup(Handle* h, Params& P, bool mixed) {
         k_nt_setup<true><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     else
         k_nt_setup<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    k_nt_start<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     return REPROBUS_OK;
 }
 
@@ -872,11 +865,11 @@ static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool c
     CUDA_TRY(h->nt_var[ip]->launch(P, grid, h->stream));
     if (timed) CUDA_TRY(capturing ? cudaEventRecordWithFlags(h->ev3, h->stream, cudaEventRecordExternal)
                                   : cudaEventRecord(h->ev3, h->stream));
-    *launches += 3;
+    *launches += 4;
     if (warm) {
         // misses of the warm start: the plain start, a second pass of the solve kernel
         CUDA_TRY(cudaMemsetAsync(h->nt_head, 0, 8 * sizeof(int), h->stream));
-        k_nt_restart<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        k_nt_start<true><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
         CUDA_TRY(h->nt_var[ip]->launch(P, grid, h->stream));
         *launches += 2;
     }
@@ -1059,7 +1052,7 @@ __global__ void __launch_bounds__(128) k_features(Params P) {
 #pragma unroll 1
     for (int it = 0; it < P.npass; it++) cell_pass(C.F, C.K, C.tj, C.A.het, C.ck0, P.sc.dt, ck, cc);
     float fe[64];
-    cell_features(P, C, ck, cc, fe);
+    cell_features(P, C.g, C.F.hnm, C.F.sza, C.A.surf, ck, cc, fe);
     float4* o = reinterpret_cast<float4*>(P.mlp_feat + (size_t)cell * 64);
 #pragma unroll
     for (int i = 0; i < 16; i++) o[i] = make_float4(fe[4 * i], fe[4 * i + 1], fe[4 * i + 2], fe[4 * i + 3]);

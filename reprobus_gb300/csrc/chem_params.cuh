@@ -53,12 +53,13 @@ struct Params {
 
 // fields of a Newton cell record: K (99), tj (41), het (9), fixed constants
 // (14: o2 n2 h2 co2 hnm parthno3 parth2o parthcl parthbr rain_hno3 rain_hcl
-// rain_hbr rain_h2o2 dt), day flag, start-of-step number densities ck0 (42)
+// rain_hbr rain_h2o2 dt), solar zenith angle (a cell is a day cell when it is
+// <= 95 deg), start-of-step number densities ck0 (43), aerosol surface area
 constexpr int NT_RK = 0, NT_RJ = NRATE, NT_RH = NRATE + NPHOT, NT_RF = NRATE + NPHOT + 9;
-constexpr int NT_RDAY = NT_RF + 14, NT_RCK0 = NT_RDAY + 1;
-constexpr int NT_REC = 208;    // FP64 record stride (206 used; 1664 B = 13 lines of 128 B)
+constexpr int NT_RSZA = NT_RF + 14, NT_RCK0 = NT_RSZA + 1, NT_RSURF = NT_RCK0 + NBCON;
+constexpr int NT_REC = 208;    // FP64 record stride (1664 B = 13 lines of 128 B)
 constexpr int NT_REC32 = 168;  // FP32 record stride (164 used)
-static_assert(NT_RCK0 + NBCON <= NT_REC, "record layout");
+static_assert(NT_RSURF < NT_REC, "record layout");
 
 __device__ __forceinline__ size_t plane3(const Params& P) { return (size_t)P.nlon * P.nlat * P.niv; }
 __device__ __forceinline__ size_t plane_b(const Params& P) { return (size_t)P.nlon * P.nlat * P.nivbas; }

@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
             NtFixT<TJ> FT;
             nt_load_fix<double>(rec + NT_RF, F);
             nt_load_fix<TJ>(recT + NT_RF, FT);
-            const bool day = rec[NT_RDAY] != 0.;
+            const bool day = rec[NT_RSZA] <= 95.;
             double* x = P.nt_x + (size_t)cell * NT_NX;
             TJ step;
             const bool ok = nt_iterate<TJ, ZS>(F, rec + NT_RK, rec + NT_RJ, rec + NT_RH, rec + NT_RCK0, FT, recT + NT_RK,

@@ -1,7 +1,8 @@
 """The step launched as a CUDA graph (REPROBUS_USE_GRAPH) gives the same
 bits as the direct launches, for the reference scheme and the Newton
 solvers, over consecutive steps (the graph is captured per call and updated
-in place)."""
+in place). A given solve-kernel shape is deterministic per cell whichever
+lane takes the cell; different shapes agree to rounding only."""
 import numpy as np
 import pytest
 
@@ -19,6 +20,9 @@ def test_graph_steps_match_direct_steps(lib_built, solver):
     for graph in (False, True):
         h = ChemStep.for_case(case, niter=5, flags=FUSE_CONSERV)
         h.set_solver(solver)
+        # one solve-kernel shape for both runs: shapes differ in rounding (the
+        # autotuner may pick either), so only the same shape can match bitwise
+        h.set_tuning(64, 1, 0)
         h.set_graph(graph)
         dc = DeviceCase(case)
         seen = []
