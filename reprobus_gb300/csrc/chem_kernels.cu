@@ -412,6 +412,40 @@ __global__ void __launch_bounds__(128) k_nt_warm(Params P) {
     }
 }
 
+// REF5 in two kernels (k_nt_setup<false>, then this one): the reference's
+// P.niter passes from the cell's record (rates, fixed constants, zenith
+// angle, ck0) and hc, write-back and (fused) conserv + clamps -- the same
+// arithmetic as k_chem, split so that each program is smaller for the
+// instruction cache
+__global__ void __launch_bounds__(128) k_ref_passes(Params P) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= P.ncell) return;
+    const double* r = P.nt_rec + (size_t)cell * NT_REC;
+    CellPro C;
+    C.g = cell_global(P, cell);
+    CellFix& F = C.F;
+    F.o2 = r[NT_RF]; F.n2 = r[NT_RF + 1]; F.h2 = r[NT_RF + 2]; F.co2 = r[NT_RF + 3]; F.hnm = r[NT_RF + 4];
+    F.parthno3 = r[NT_RF + 5]; F.parth2o = r[NT_RF + 6]; F.parthcl = r[NT_RF + 7]; F.parthbr = r[NT_RF + 8];
+    F.rain_hno3 = r[NT_RF + 9]; F.rain_hno4 = 0.; F.rain_hcl = r[NT_RF + 10]; F.rain_hbr = r[NT_RF + 11];
+    F.rain_h2o2 = r[NT_RF + 12]; F.rain_ch2o = 0.; F.rain_ch3o2h = 0.;
+    F.sza = r[NT_RSZA];
+    const size_t pl = plane3(P);
+    double ck[NBCON], cc[NCM];
+#pragma unroll
+    for (int n = 0; n < NRATE; n++) C.K[n] = r[NT_RK + n];
+#pragma unroll
+    for (int n = 0; n < NPHOT; n++) C.tj[n] = r[NT_RJ + n];
+#pragma unroll
+    for (int n = 0; n < 9; n++) C.A.het[n] = r[NT_RH + n];
+#pragma unroll
+    for (int n = 0; n < NBCON; n++) ck[n] = C.ck0[n] = r[NT_RCK0 + n];
+#pragma unroll
+    for (int n = 0; n < NCM; n++) cc[n] = P.hc[C.g + pl * n] * F.hnm;
+#pragma unroll 1
+    for (int it = 0; it < P.niter; it++) cell_pass(F, C.K, C.tj, C.A.het, C.ck0, P.sc.dt, ck, cc);
+    cell_epilogue(P, C, ck, cc);
+}
+
 __global__ void __launch_bounds__(128) k_nt_finish(Params P) {
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= P.ncell) return;
@@ -542,6 +576,9 @@ struct Handle {
     int want_lanes = 0, want_bps = 0, want_zs = 0;   // reprobus_chem_set_tuning; lanes 0: autotune
     const NtVariant* nt_var[2] = {nullptr, nullptr};
     int nt_bps[2] = {0, 0};
+    // REF5 as the rate-stage kernel + the passes kernel through the cell
+    // records (false: the single kernel k_chem, no record buffers)
+    bool split_ref5 = true;
     // CUDA graph of the step (REPROBUS_USE_GRAPH)
     cudaGraphExec_t gexec = nullptr;
     int gexec_sig = -1;
@@ -886,9 +923,18 @@ static int enqueue_step(Handle* h, Params& P, bool capturing, int* launches) {
     if (counters) CUDA_TRY(cudaMemsetAsync(h->d_count, 0, 8 * sizeof(unsigned long long), h->stream));
     k_columns<<<(P.ncol + tb - 1) / tb, tb, 0, h->stream>>>(P);
     (*launches)++;
-    if (h->solver == REPROBUS_SOLVER_REF5) {
+    if (h->solver == REPROBUS_SOLVER_REF5 && !h->split_ref5) {
         k_chem<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
         (*launches)++;
+    } else if (h->solver == REPROBUS_SOLVER_REF5) {
+        if (!capturing) {
+            int rc = ensure_newton(h);
+            if (rc) return rc;
+        }
+        P.nt_rec = h->nt_rec;
+        k_nt_setup<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        k_ref_passes<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        *launches += 2;
     } else {
         int rc = launch_newton(h, P, launches, true, capturing);
         if (rc) return rc;
@@ -1365,6 +1411,7 @@ extern "C" int reprobus_chem_step_noalloc(const double* ajl, const double* o3up,
     h.d_count = reinterpret_cast<unsigned long long*>(scratch);
     h.d_col = scratch + 32;
     h.stream = (cudaStream_t)stream;
+    h.split_ref5 = false;  // no record buffers: the single-kernel REF5
     Params P;
     fill_params(&h, P, ilat0, ilat1);
     P.trajoff = (long long)(irapp - 1) * nlon * nlat * niv;

@@ -98,7 +98,7 @@ def test_step_unfused_matches_oracle(torch):
     ref, _, _ = oracle.step(case, niter=5, fuse=False)
     got, st = _run_gpu(case, flags=0)
     _compare(got, ref)
-    assert st["kernel_launches"] == 2
+    assert st["kernel_launches"] == 3  # columns, rate stage, passes
 
 
 def test_polar_winter_cells(torch):
