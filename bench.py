@@ -265,7 +265,7 @@ def main():
     clocks = Clocks(local)
     clocks.start()
     for name in run:
-        h.set_solver(solver_ids[name], npass=1, maxit=12, tol=1e-10)
+        h.set_solver(solver_ids[name], npass=1, maxit=12, tol=1e-8)
         h.set_mlp(net if name == "mlp" else None)
         for _ in range(max(args.warmup, 3)):
             restore()
@@ -305,7 +305,7 @@ def main():
                          {"lanes_per_block": st["lanes_per_block"], "blocks_per_sm": st["blocks_per_sm"],
                           "z_shared": st["z_shared"]}}
     clk = clocks.stop()
-    h.set_solver(solver_ids[headline], npass=1, maxit=12, tol=1e-10)
+    h.set_solver(solver_ids[headline], npass=1, maxit=12, tol=1e-8)
     h.set_mlp(net if headline == "mlp" else None)
     R = results[headline]
     ms_step = R["ms_per_step"]

@@ -163,7 +163,9 @@ int reprobus_chem_set_graph(void* handle, int on);
  * until the largest step relative to max(|x|, 1e-20 hnm) is below tol, at
  * most maxit iterations; a cell that does not converge falls back to the
  * reference's niter passes and is counted in stats.fallbacks.
- * Defaults: npass 1, maxit 12, tol 1e-10. No counterpart in the reference. */
+ * Defaults: npass 1, maxit 12, tol 1e-8 (the answer then lies within ~1e-13
+ * of the fixed point, far inside the 1e-6 accuracy target). No counterpart in
+ * the reference. */
 int reprobus_chem_set_solver(void* handle, int solver, int npass, int maxit, double tol);
 
 /* Shape of the persistent Newton solve kernel. lanes_per_block = 0 (default):

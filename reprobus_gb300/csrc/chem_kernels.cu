@@ -548,7 +548,7 @@ struct Handle {
     int device;
     int solver = REPROBUS_SOLVER_REF5;  // which kernel integrates the cells
     int npass = 1, maxit = 12;          // Newton: reference passes before, iteration cap
-    double tol = 1e-10;                 // Newton: scaled step tolerance
+    double tol = 1e-8;                  // Newton: scaled step tolerance
     double troe[18];
     double* d_ajl = nullptr;
     double* d_o3up = nullptr;
