@@ -76,7 +76,9 @@ typedef struct reprobus_stats {
                                   persistent solve kernel (autotuned or set)         */
     int blocks_per_sm;         /* Newton solvers: resident blocks of it per SM        */
     int z_shared;              /* Newton solvers: 1 when the kernel keeps the right-
-                                  hand side in shared memory, 0 in registers         */
+                                  hand side in shared memory, 0 in registers, 2 in
+                                  registers with two warp groups sharing the matrix
+                                  slots                                              */
     int warm_start;            /* Newton solvers: 1 when the learned warm start ran  */
     long long warm_restarts;   /* warm start: cells whose predicted start missed the
                                   convergence test and restarted from the plain start */
@@ -173,9 +175,13 @@ int reprobus_chem_set_solver(void* handle, int solver, int npass, int maxit, dou
  * (lanes per block x right-hand side in registers or shared memory x
  * resident blocks per SM) on that step's own cells and keeps the fastest
  * (synchronous, once per handle); > 0: use that many lanes per block (a
- * compiled value: 64, 96, 128 for the mixed solver; 32, 64 for the FP64 one;
- * a precision without that value is autotuned), zshared (0 or 1) and
- * blocks_per_sm (0: as many as fit). No counterpart in the reference. */
+ * compiled value: 64, 96, 128 (zshared 0, 1) or 128, 256 (zshared 2) for the
+ * mixed solver; 32, 64 (zshared 0, 1) or 64, 128 (zshared 2) for the FP64
+ * one; a precision without that value is autotuned), zshared (0: right-hand
+ * side in registers, 1: in shared memory, 2: in registers with two warp
+ * groups taking turns on one set of matrix slots, so that a block keeps
+ * twice the cells in flight) and blocks_per_sm (0: as many as fit). No
+ * counterpart in the reference. */
 int reprobus_chem_set_tuning(void* handle, int lanes_per_block, int blocks_per_sm, int zshared);
 
 /* ---- learned warm start ----------------------------------------------------

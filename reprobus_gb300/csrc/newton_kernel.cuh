@@ -90,6 +90,124 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
     }
 }
 
+// Two warp groups of NTH/2 lanes each take turns on one set of NTH/2 lanes'
+// matrix slots. An iteration of a cell splits into a matrix phase (scaled
+// Jacobian, factorisation and solve in the shared-memory slots) and an
+// update phase (FP64 update with the solved step, convergence test, refill
+// from the work queue, FP64 residual of the new iterate into the step
+// registers z): while one group runs its matrix phase, the other runs its
+// update phase, which needs no shared memory. So a block keeps NTH cells in
+// flight on the shared memory of NTH/2. Phases end at a block-wide
+// barrier-and-reduction that also decides, for all threads at once, when the
+// queue is exhausted: every thread passes the same number of barriers, and
+// none waits on another block. Phase t (t >= 1): group g runs the matrix
+// phase when t + g is odd; at t = 0 group 0 runs its first update phase alone.
+template <typename TJ, int NTH>
+__global__ void __launch_bounds__(NTH, 1) k_nt_solve_pp(Params P) {
+    constexpr int NS = NTH / 2;  // lanes of matrix slots
+    static_assert(NS % 32 == 0, "whole warps per group");
+    extern __shared__ __align__(16) unsigned char nt_smem[];
+    const int grp = (int)threadIdx.x / NS;
+    const SJ<TJ, NS> J{reinterpret_cast<TJ*>(nt_smem) + (threadIdx.x % NS)};
+    const unsigned lane = threadIdx.x & 31u;
+    const int nday = P.nt_head[1], nnight = P.nt_head[2];
+    const int nq = nday + nnight;
+    int cell = -1;  // >= 0: cell in work; -1: wants a cell; -2: queue exhausted
+    int it = 0;
+    bool has_z = false;  // z holds the (solved) step of the cell's current iterate
+    TJ z[NT_NX];
+    for (int t = 0;; t++) {
+        const bool matrix_phase = ((t + grp) & 1) != 0;
+        if (t == 0 && grp == 1) {
+            // group 1 starts with the second phase
+        } else if (!matrix_phase) {
+            if (cell >= 0 && has_z) {
+                const double* rec = P.nt_rec + (size_t)cell * NT_REC;
+                double* x = P.nt_x + (size_t)cell * NT_NX;
+                TJ step;
+                const bool ok = nt_update<TJ>(x, 1e-20 * rec[NT_RF + 4], (const TJ*)z, &step, true);
+                it++;
+                has_z = false;
+                int done = 0;
+                if (!ok)
+                    done = -1;
+                else if (step < (TJ)P.tol)
+                    done = it;
+                else if (it >= P.maxit)
+                    done = -1;
+                if (done) {
+                    if (done < 0) atomicAdd(P.nonfinite + 5, (unsigned long long)it);
+                    P.nt_stat[cell] = done;
+                    cell = -1;
+                }
+            }
+            const unsigned want = __ballot_sync(0xffffffffu, cell == -1);
+            if (want) {
+                const int leader = __ffs(want) - 1;
+                int base = 0;
+                if ((int)lane == leader) base = atomicAdd(P.nt_head, __popc(want));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (cell == -1) {
+                    const int q = base + __popc(want & ((1u << lane) - 1u));
+                    cell = q < nq ? nt_queue_cell(P, q, nday) : -2;
+                    it = 0;
+                }
+            }
+            if (cell >= 0) {
+                const double* rec = P.nt_rec + (size_t)cell * NT_REC;
+                NtFixT<double> F;
+                nt_load_fix<double>(rec + NT_RF, F);
+                const bool day = rec[NT_RSZA] <= 95.;
+                nt_rhs<TJ>(day, F, rec + NT_RK, rec + NT_RJ, rec + NT_RH, rec + NT_RCK0,
+                           (const double*)(P.nt_x + (size_t)cell * NT_NX), 1e-20 * F.hnm, (TJ*)z);
+                has_z = true;
+            }
+        } else if (cell >= 0) {
+            const double* rec = P.nt_rec + (size_t)cell * NT_REC;
+            const TJ* recT;
+            if constexpr (sizeof(TJ) == 4)
+                recT = P.nt_rec32 + (size_t)cell * NT_REC32;
+            else
+                recT = rec;
+            NtFixT<TJ> FT;
+            nt_load_fix<TJ>(recT + NT_RF, FT);
+            const bool day = rec[NT_RSZA] <= 95.;
+            const double* x = P.nt_x + (size_t)cell * NT_NX;
+            nt_jacobian_call<TJ>(day, FT, recT + NT_RK, recT + NT_RJ, recT + NT_RH, x, 1e-20 * rec[NT_RF + 4], J);
+            NT_FENCE();
+            nt_factor_solve<TJ>(J, (TJ*)z, TJ(NT_TINY));
+        }
+        if (__syncthreads_and(cell == -2)) break;
+    }
+}
+
+template <typename TJ, int NTH>
+constexpr size_t nt_pp_smem_bytes() {
+    return (size_t)NT_NSLOT * (NTH / 2) * sizeof(TJ);
+}
+
+template <typename TJ, int NTH>
+cudaError_t nt_pp_prepare(int* blocks_per_sm) {
+    cudaError_t e = cudaFuncSetAttribute(k_nt_solve_pp<TJ, NTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)nt_pp_smem_bytes<TJ, NTH>());
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_nt_solve_pp<TJ, NTH>, NTH,
+                                                         nt_pp_smem_bytes<TJ, NTH>());
+}
+
+template <typename TJ, int NTH>
+cudaError_t nt_pp_launch(const Params& P, int grid, cudaStream_t stream) {
+    k_nt_solve_pp<TJ, NTH><<<grid, NTH, nt_pp_smem_bytes<TJ, NTH>(), stream>>>(P);
+    return cudaGetLastError();
+}
+
+// form 2: two warp groups sharing the matrix slots, z in registers
+template <typename TJ, int NTH>
+constexpr NtVariant nt_pp_variant() {
+    return NtVariant{(int)sizeof(TJ), NTH, 2, nt_pp_smem_bytes<TJ, NTH>(), &nt_pp_prepare<TJ, NTH>,
+                     &nt_pp_launch<TJ, NTH>};
+}
+
 template <typename TJ, int NTH, bool ZS>
 constexpr size_t nt_smem_bytes() {
     return (size_t)(NT_NSLOT + (ZS ? NT_NX : 0)) * NTH * sizeof(TJ);

@@ -9,16 +9,20 @@ struct Params;
 struct NtVariant {
     int tj_bytes;  // matrix precision: 4 = FP32 (mixed solver), 8 = FP64 (plain solver)
     int nth;       // lanes per block = cells in flight per block
-    int zshared;   // 1: right-hand side / step in shared memory, 0: in registers
+    int zshared;   // 1: right-hand side / step in shared memory, 0: in registers,
+                   // 2: in registers, two warp groups taking turns on the matrix slots
     size_t smem;   // dynamic shared memory per block (the cells' matrix slots)
     cudaError_t (*prepare)(int* blocks_per_sm);  // shared-memory opt-in, occupancy
     cudaError_t (*launch)(const Params& P, int grid, cudaStream_t stream);
 };
 
-// variants compiled in nt_solve_{f32,f64}_{zr,zs}.cu, gathered in
-// chem_kernels.cu: the matrix precision's variants, z in registers first
+// variants compiled in nt_solve_{f32,f64}_{zr,zs}.cu and nt_solve_pp.cu,
+// gathered in chem_kernels.cu: the matrix precision's variants, z in
+// registers first
 const NtVariant* nt_variants_f32_zr(int* n);
 const NtVariant* nt_variants_f32_zs(int* n);
 const NtVariant* nt_variants_f64_zr(int* n);
 const NtVariant* nt_variants_f64_zs(int* n);
+const NtVariant* nt_variants_f32_pp(int* n);
+const NtVariant* nt_variants_f64_pp(int* n);
 }  // namespace rpb
