@@ -198,6 +198,71 @@ def cpu_baseline_one(case, nrows=12):
                       f"OpenMP {cores} threads"}
 
 
+def column_bench(torch, h, case, dc, stream, hbm_peak, reps=5):
+    """Times the column physics around the step on the benchmark grid
+    (device-resident arrays, CUDA events on the handle's stream): per entry
+    point the mean device time, the algorithmic bytes (each array element the
+    reference routine reads or writes, counted once) and the HBM fraction."""
+    from reprobus_gb300 import ChemStep
+    # the reference's level split: chemistry on levels 1..94, forcing below
+    nlon, nlat, niv, nb, nh = case.nlon, case.nlat, case.niv, min(94, case.niv), case.nivhau
+    ncol = nlon * nlat
+    h = ChemStep(case.ajl, case.o3up, nlon, nlat, niv, nivbas=nb, nivhau=nh, nrappmax=case.nrappmax, niter=5,
+                 flags=0, troe=case.troe)
+    h.set_stream(stream)
+    rng = np.random.default_rng(11)
+    f64 = dict(dtype=torch.float64, device="cuda")
+    vsed = torch.rand(ncol * nb, **f64) * 2e-3
+    ph2o = torch.rand(ncol * nb, **f64)
+    pno3 = torch.rand(ncol * nb, **f64)
+    co = torch.full((ncol,), 1e-7, **f64)
+    hj1 = torch.rand(ncol * niv, **f64) * 1e-3
+    aaa, bbb = inputs_l137()
+    aaa_d, bbb_d = torch.tensor(aaa, **f64), torch.tensor(bbb, **f64)
+    psol = torch.tensor(rng.uniform(980., 1030., ncol), **f64)
+    relief = torch.zeros(ncol, **f64)
+    alt = torch.empty(ncol * niv, **f64)
+    q0, h0 = dc["qj1"].clone(), dc["hc"].clone()
+    h2o = dc["qj1"][2 * ncol * niv:3 * ncol * niv]  # regular-grid H2O (slot 3)
+    nivh2o = min(59, nb + 1)
+    ksed = max(nivh2o - nh, 0)
+    calls = {
+        "sedimentation": (lambda: h.sedimentation_dev(dc["trajpre"], dc["trajtem"], 1, dc["qj1"], vsed, nivh2o, ph2o,
+                                                      pno3, 10800.),
+                          ncol * 8 * (5 * (nb - nh + 2) + 2 * (ksed + 1) + ksed + 3 * (nb - nh + 1))),
+        "forcing": (lambda: h.forcing_dev(2010, 3, 900., dc["trajpre"], 1, dc["qj1"], dc["hc"], co_month=co, hj1=hj1,
+                                          nivh2oecmwf=nivh2o),
+                    ncol * 8 * ((niv - nb) * 21 + 2 * (niv - nb + 1) + 1 + 2 * (niv - nivh2o + 1))),
+        "altitude": (lambda: h.altitude_dev(relief, psol, aaa_d, bbb_d, dc["trajtem"], h2o, dc["trajlon"],
+                                            dc["trajlat"], dc["trajpre"], alt),
+                     ncol * 8 * (5 * niv + 2) + ncol * niv * 8 * 9),
+    }
+    out = {}
+    for name, (fn, nbytes) in calls.items():
+        fn()
+        ms = 0.0
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ms += e0.elapsed_time(e1)
+        ms /= reps
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        out[name] = {"ms": round(ms, 4), "bytes": int(nbytes), "achieved_gbs": round(gbs, 1),
+                     "frac_hbm": round(gbs / hbm_peak, 4)}
+    dc["qj1"].copy_(q0)
+    dc["hc"].copy_(h0)
+    h.close()
+    return out
+
+
+def inputs_l137():
+    from reprobus_gb300 import inputs
+    return inputs.l137_levels()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -209,6 +274,7 @@ def main():
     ap.add_argument("--nlat", type=int, default=16)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-columns", action="store_true", help="skip timing the column physics kernels")
     ap.add_argument("--lanes", type=int, default=0,
                     help="Newton solve kernel lanes per block (0: autotune)")
     ap.add_argument("--bps", type=int, default=0, help="Newton solve kernel blocks per SM (0: all that fit)")
@@ -390,6 +456,9 @@ def main():
                                    "source (an FMA counts 2), times the iterations the step ran, over the "
                                    "solve kernel's CUDA-event time; FP64 part (residual, update) against the "
                                    "live DGEMM peak")
+        cols = None
+        if not args.no_columns:
+            cols = column_bench(torch, h, case, dc, stream, hbm_peak)
         cb = None
         if not args.no_cpu_baseline:
             cb = cpu_baseline(case)
@@ -413,7 +482,7 @@ def main():
                                          if "mixed" in results and "newton64" in results else None),
                 "mlp_mixed_vs_fp64_newton": (results["mlp"]["cells_per_s"] / results["newton64"]["cells_per_s"]
                                              if "mlp" in results and "newton64" in results else None),
-                "roofline": roof, "e2e": e2e, "cpu_baseline": cb, "clocks": clk}
+                "roofline": roof, "e2e": e2e, "cpu_baseline": cb, "clocks": clk, "columns": cols}
         print(json.dumps(line))
     h.close()
     if world > 1:

@@ -273,6 +273,83 @@ int reprobus_chem_rates_dev(void* handle, int ilat0, int ilat1, double daynum,
  * :431-450. */
 int reprobus_conserv_dev(void* handle, int ilat0, int ilat1, double* qj1, double* hc);
 
+/* ---- column physics around the chemistry step ------------------------------
+ * The other per-column work of the chemistry sub-step of the time loop
+ * (:370-450), on DEVICE arrays in the reference's layout. Each call
+ * synchronises the handle's stream before it returns. */
+
+/* Sedimentation of H2O (levels nivhau..nivh2oecmwf-1), NOy and HNO3 (levels
+ * nivhau..nivbas) for rows ilat0..ilat1, from the settling velocities and
+ * non-sedimenting fractions that the chemistry step wrote (vsed3d,
+ * parth2osed, parthno3sed), over the time step dtsedi. Needs nivhau >= 2 and
+ * nivhau <= nivh2oecmwf <= nivbas + 1.
+ * Replaces: call sedimentation(trajpre, trajtem, irapp, qj1, vsed3d,
+ * nivh2oecmwf, parth2osed, parthno3sed, dtsedi) (:420-422, routine
+ * :2416-2522), which the reference runs after the last chemistry sub-step of
+ * a transport step and before conserv. */
+int reprobus_sedimentation_dev(void* handle, int ilat0, int ilat1, const double* trajpre,
+                               const double* trajtem, int irapp, double* qj1, const double* vsed3d,
+                               int nivh2oecmwf, const double* parth2osed, const double* parthno3sed,
+                               double dtsedi);
+
+/* The 16 tropospheric forcing mixing ratios of tropo for year ian, month imois
+ * (June values of the years around the date, linear in time, lumped species
+ * added), in the order of the qj1 slots 1 2 4 7 31..42 they set. Dates before
+ * June 1988 or from June 2024 on are refused (the reference's tables end
+ * there). Host only. Replaces: the date interpolation of tropo (:4414-4495). */
+int reprobus_tropo_values(int ian, int imois, double* v);
+
+/* Tropospheric forcing of rows ilat0..ilat1 for the date (ian, imois) and
+ * step dt: tropo (levels nivbas+1..niv set to the forcing values, Ox relaxed
+ * with a 1-day time constant, O3 and passive Ox = Ox from level nivbas);
+ * co_tropo when co_month (nlon,nlat: the MOPITT CO field of the month) is
+ * non-NULL; ecmwfh2o (H2O = hj1 x 28.97/18 from level nivh2oecmwf) when hj1
+ * (nlon,nlat,niv: the ECMWF specific humidity at the step's time) is non-NULL.
+ * Replaces: call tropo(ian, imois, dt, trajpre, irapp, qj1, hc) (:373,
+ * routine :4077-4574), call co_tropo(imois, dt, qj1) (:377, :4577-4639) and
+ * call ecmwfh2o(daynum, qj1, nivh2oecmwf, ...) (:382, :8621-8658); the
+ * reference reads the CO and humidity fields from files (mopitt_corrected.txt,
+ * ECMWF analyses): here the caller passes them. */
+int reprobus_forcing_dev(void* handle, int ilat0, int ilat1, int ian, int imois, double dt,
+                         const double* trajpre, int irapp, const double* co_month, const double* hj1,
+                         int nivh2oecmwf, double* qj1, double* hc);
+
+/* Geometric altitude (km) of every trajectory point (slice irapp of traj*)
+ * from the regular grid's surface pressure psol(nlon,nlat), relief
+ * (nlon,nlat), hybrid coefficients aaa(niv) [hPa] and bbb(niv), temperature
+ * t(nlon,nlat,niv) and H2O mixing ratio h2o(nlon,nlat,niv); writes
+ * alt(nlon,nlat,niv). The nearest regular column of a point uses the grid
+ * spacing 360/nlon x 180/(nlat-1) (2 x 2 degrees on the reference grid, where
+ * the reference hard-codes 2). Uses device scratch of the handle (3 doubles
+ * per grid point).
+ * Replaces: call altitude(nlon, nlat, niv, relief, pj1, aaa, bbb, tj1,
+ * qj1(:,:,:,3), trajlon(:,:,:,irapp), trajlat(..), trajpre(..), alt) (:391-394,
+ * routine altitude.f90:1-148). */
+int reprobus_altitude_dev(void* handle, const double* relief, const double* psol, const double* aaa,
+                          const double* bbb, const double* t, const double* h2o, const double* trajlon,
+                          const double* trajlat, const double* trajpre, int irapp, double* alt);
+
+/* History / restart record of the model state in the reference's file
+ * format: one big-endian Fortran sequential unformatted record (4-byte length
+ * markers) holding namexp (6 characters, blank padded), ian, imois, ijour,
+ * iheure, imin (int32), pj1(nlon,nlat), uj1, vj1, alt, tj1 (nlon,nlat,niv),
+ * qj1(...,43), surfarea(nlon,nlat,niv), hc(...,15). Arrays are DEVICE arrays;
+ * the byte order is reversed on the GPU through mapped pinned buffers.
+ * Records of 2^31 bytes or more are refused.
+ * Replaces: write(78) namexp, ian, ..., hc (:587-588). */
+int reprobus_history_write_dev(void* handle, const char* path, const char* namexp, int ian, int imois,
+                               int ijour, int iheure, int imin, const double* pj1, const double* uj1,
+                               const double* vj1, const double* alt, const double* tj1, const double* qj1,
+                               const double* surfarea, const double* hc);
+
+/* Reads such a record into DEVICE arrays; namexp gets 7 bytes (6 characters
+ * and a NUL), date the 5 integers. A record whose length does not match the
+ * handle's grid is refused. Replaces: read(90) namexp, ian, ..., hc
+ * (:231-235). */
+int reprobus_history_read_dev(void* handle, const char* path, char* namexp, int* date, double* pj1,
+                              double* uj1, double* vj1, double* alt, double* tj1, double* qj1,
+                              double* surfarea, double* hc);
+
 /* Allocation-free variant of reprobus_chem_step_dev. No counterpart in the
  * reference: REPROBUS allocates all of its arrays itself, on the host.
  *

@@ -24,6 +24,8 @@ def build(force: bool = False) -> str:
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
         cmd = ["gcc", *CFLAGS, "-o", LIB, SRC, "-lm"]
         subprocess.run(cmd, check=True)
+    from . import column
+    column.build(force)
     return LIB
 
 

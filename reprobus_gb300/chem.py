@@ -42,6 +42,8 @@ EXPORTS = [
     "reprobus_chem_set_tuning", "reprobus_mlp_create", "reprobus_mlp_free", "reprobus_mlp_nparams",
     "reprobus_mlp_set_params", "reprobus_mlp_get_params", "reprobus_mlp_train_step", "reprobus_mlp_grads",
     "reprobus_mlp_forward", "reprobus_chem_set_mlp", "reprobus_chem_features_dev", "reprobus_chem_set_graph",
+    "reprobus_sedimentation_dev", "reprobus_tropo_values", "reprobus_forcing_dev", "reprobus_altitude_dev",
+    "reprobus_history_write_dev", "reprobus_history_read_dev",
 ]
 NOALLOC_SCRATCH_DOUBLES = 1 << 20
 
@@ -106,6 +108,13 @@ def load_library(path: str = LIBPATH):
     lib.reprobus_chem_set_mlp.argtypes = [vp, vp]
     lib.reprobus_chem_set_graph.argtypes = [vp, i]
     lib.reprobus_chem_features_dev.argtypes = [vp, i, i, d, d, vp, vp, vp, vp, vp, i, vp, vp, vp]
+    lib.reprobus_sedimentation_dev.argtypes = [vp, i, i, vp, vp, i, vp, vp, i, vp, vp, d]
+    lib.reprobus_tropo_values.argtypes = [i, i, dp]
+    lib.reprobus_forcing_dev.argtypes = [vp, i, i, i, i, d, vp, i, vp, vp, i, vp, vp]
+    lib.reprobus_altitude_dev.argtypes = [vp] + [vp] * 9 + [i, vp]
+    cp = ctypes.c_char_p
+    lib.reprobus_history_write_dev.argtypes = [vp, cp, cp, i, i, i, i, i] + [vp] * 8
+    lib.reprobus_history_read_dev.argtypes = [vp, cp, vp, ctypes.POINTER(ctypes.c_int)] + [vp] * 8
     for name in EXPORTS:
         if name not in ("reprobus_version", "reprobus_last_error"):
             getattr(lib, name).restype = ctypes.c_int
@@ -246,6 +255,56 @@ class ChemStep:
 
     def conserv_dev(self, ilat0, ilat1, qj1, hc):
         _check(self.lib.reprobus_conserv_dev(self._h, ilat0, ilat1, _dp(qj1), _dp(hc)))
+
+    # column physics around the step (device arrays, Fortran layout)
+    def sedimentation_dev(self, trajpre, trajtem, irapp, qj1, vsed3d, nivh2oecmwf, parth2osed, parthno3sed,
+                          dtsedi, ilat0=1, ilat1=None):
+        """subroutine sedimentation (:2416-2522), same arguments, rows ilat0..ilat1."""
+        ilat1 = self.nlat if ilat1 is None else ilat1
+        _check(self.lib.reprobus_sedimentation_dev(self._h, ilat0, ilat1, _dp(trajpre), _dp(trajtem), irapp,
+                                                   _dp(qj1), _dp(vsed3d), int(nivh2oecmwf), _dp(parth2osed),
+                                                   _dp(parthno3sed), float(dtsedi)))
+
+    def forcing_dev(self, ian, imois, dt, trajpre, irapp, qj1, hc, co_month=None, hj1=None, nivh2oecmwf=59,
+                    ilat0=1, ilat1=None):
+        """tropo (:4077-4574), then co_tropo (:4577-4639) when co_month (the
+        month's CO field, nlon x nlat) is given and ecmwfh2o (:8621-8658) when
+        hj1 (the humidity field) is given."""
+        ilat1 = self.nlat if ilat1 is None else ilat1
+        _check(self.lib.reprobus_forcing_dev(self._h, ilat0, ilat1, int(ian), int(imois), float(dt), _dp(trajpre),
+                                             irapp, _dp(co_month) if co_month is not None else None,
+                                             _dp(hj1) if hj1 is not None else None, int(nivh2oecmwf), _dp(qj1),
+                                             _dp(hc)))
+
+    def altitude_dev(self, relief, psol, aaa, bbb, t, h2o, trajlon, trajlat, trajpre, alt, irapp=1):
+        """subroutine altitude (altitude.f90:1-148) on slice irapp of the trajectories."""
+        _check(self.lib.reprobus_altitude_dev(self._h, _dp(relief), _dp(psol), _dp(aaa), _dp(bbb), _dp(t), _dp(h2o),
+                                              _dp(trajlon), _dp(trajlat), _dp(trajpre), irapp, _dp(alt)))
+
+    def history_write_dev(self, path, namexp, date, pj1, uj1, vj1, alt, tj1, qj1, surfarea, hc):
+        """write(78) of the history record (:587-588); date = (ian, imois, ijour, iheure, imin)."""
+        ian, imois, ijour, iheure, imin = (int(x) for x in date)
+        _check(self.lib.reprobus_history_write_dev(self._h, os.fsencode(path), namexp.encode()[:6], ian, imois, ijour,
+                                                   iheure, imin, _dp(pj1), _dp(uj1), _dp(vj1), _dp(alt), _dp(tj1),
+                                                   _dp(qj1), _dp(surfarea), _dp(hc)))
+
+    def history_read_dev(self, path, pj1, uj1, vj1, alt, tj1, qj1, surfarea, hc):
+        """read(90) of a history/restart record (:231-235) into device arrays;
+        returns (namexp, (ian, imois, ijour, iheure, imin))."""
+        name = ctypes.create_string_buffer(7)
+        date = (ctypes.c_int * 5)()
+        _check(self.lib.reprobus_history_read_dev(self._h, os.fsencode(path), name, date, _dp(pj1), _dp(uj1),
+                                                  _dp(vj1), _dp(alt), _dp(tj1), _dp(qj1), _dp(surfarea), _dp(hc)))
+        return name.value.decode(), tuple(date)
+
+
+def tropo_values(ian, imois):
+    """The 16 forcing mixing ratios tropo imposes below nivbas for the date
+    (:4414-4495), ordered as the qj1 slots 1 2 4 7 31..42."""
+    lib = load_library()
+    out = np.zeros(16)
+    _check(lib.reprobus_tropo_values(int(ian), int(imois), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+    return out
 
 
 def step_noalloc(ajl, o3up, troe, nlon, nlat, niv, nivbas, nivhau, nrappmax, niter, flags, ilat0, ilat1,

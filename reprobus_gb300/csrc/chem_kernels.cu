@@ -27,6 +27,7 @@
 #include "newton_gen.cuh"
 #include "newton_launch.h"
 #include "mlp_net.h"
+#include "handle_info.h"
 
 using namespace rpb;
 
@@ -587,6 +588,9 @@ struct Handle {
     void* mlp = nullptr;
     float* mlp_feat = nullptr;
     float* mlp_y = nullptr;
+    // scratch of the column-physics entry points (column_kernels.cu)
+    void* col_scratch = nullptr;
+    size_t col_scratch_bytes = 0;
 };
 
 static const char* kVersion = "reprobus_gb300 0.1 (sm_103a, FP64 reference scheme)";
@@ -636,6 +640,7 @@ static void free_handle(Handle* h) {
     cudaFree(h->nt_head);
     cudaFree(h->mlp_feat);
     cudaFree(h->mlp_y);
+    cudaFree(h->col_scratch);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
@@ -696,6 +701,37 @@ extern "C" int reprobus_chem_init(const double* ajl, const double* o3up, const d
     *handle = h;
     return REPROBUS_OK;
 }
+
+namespace rpb {
+__attribute__((visibility("hidden"))) int handle_info(void* handle, HandleInfo* out) {
+    const Handle* h = (const Handle*)handle;
+    if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
+    out->device = h->device;
+    out->nlon = h->nlon;
+    out->nlat = h->nlat;
+    out->niv = h->niv;
+    out->nivbas = h->nivbas;
+    out->nivhau = h->nivhau;
+    out->nrappmax = h->nrappmax;
+    out->stream = h->stream;
+    return REPROBUS_OK;
+}
+
+__attribute__((visibility("hidden"))) int handle_scratch(void* handle, size_t bytes, void** out) {
+    Handle* h = (Handle*)handle;
+    if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
+    if (h->col_scratch_bytes < bytes) {
+        CUDA_TRY(cudaStreamSynchronize(h->stream));
+        cudaFree(h->col_scratch);
+        h->col_scratch = nullptr;
+        h->col_scratch_bytes = 0;
+        CUDA_TRY(cudaMalloc(&h->col_scratch, bytes));
+        h->col_scratch_bytes = bytes;
+    }
+    *out = h->col_scratch;
+    return REPROBUS_OK;
+}
+}  // namespace rpb
 
 extern "C" int reprobus_chem_free(void* handle) {
     free_handle((Handle*)handle);
