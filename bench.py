@@ -275,6 +275,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-columns", action="store_true", help="skip timing the column physics kernels")
+    ap.add_argument("--npass", type=int, default=0,
+                    help="reference passes before Newton for the plain solvers (0: each solver's default)")
     ap.add_argument("--lanes", type=int, default=0,
                     help="Newton solve kernel lanes per block (0: autotune)")
     ap.add_argument("--bps", type=int, default=0, help="Newton solve kernel blocks per SM (0: all that fit)")
@@ -327,11 +329,17 @@ def main():
     def step(stats=False):
         return h.step_dev(1, case.nlat, case.daynum, case.dt, *a, stats=stats)
 
+    def npass_of(name):
+        # the warm start's network is trained on the default 5-pass start
+        if name == "mlp":
+            return 5
+        return args.npass if args.npass > 0 else 5
+
     results = {}
     clocks = Clocks(local)
     clocks.start()
     for name in run:
-        h.set_solver(solver_ids[name], npass=1, maxit=12, tol=1e-8)
+        h.set_solver(solver_ids[name], npass=npass_of(name), maxit=12, tol=1e-6)
         h.set_mlp(net if name == "mlp" else None)
         for _ in range(max(args.warmup, 3)):
             restore()
@@ -371,7 +379,7 @@ def main():
                          {"lanes_per_block": st["lanes_per_block"], "blocks_per_sm": st["blocks_per_sm"],
                           "z_shared": st["z_shared"]}}
     clk = clocks.stop()
-    h.set_solver(solver_ids[headline], npass=1, maxit=12, tol=1e-8)
+    h.set_solver(solver_ids[headline], npass=npass_of(headline), maxit=12, tol=1e-6)
     h.set_mlp(net if headline == "mlp" else None)
     R = results[headline]
     ms_step = R["ms_per_step"]

@@ -165,9 +165,11 @@ int reprobus_chem_set_graph(void* handle, int on);
  * until the largest step relative to max(|x|, 1e-20 hnm) is below tol, at
  * most maxit iterations; a cell that does not converge falls back to the
  * reference's niter passes and is counted in stats.fallbacks.
- * Defaults: npass 1, maxit 12, tol 1e-8 (the answer then lies within ~1e-13
- * of the fixed point, far inside the 1e-6 accuracy target). No counterpart in
- * the reference. */
+ * Defaults: npass 5, maxit 12, tol 1e-6 (the answer then lies within ~1e-12
+ * of the fixed point, far inside the 1e-6 accuracy target; 5 passes are the
+ * fastest start of both solvers on the 2 x 2 degree grid). A warm-start
+ * network (reprobus_chem_set_mlp) is trained for one npass and must be used
+ * with it. No counterpart in the reference. */
 int reprobus_chem_set_solver(void* handle, int solver, int npass, int maxit, double tol);
 
 /* Shape of the persistent Newton solve kernel. lanes_per_block = 0 (default):
@@ -281,8 +283,8 @@ int reprobus_conserv_dev(void* handle, int ilat0, int ilat1, double* qj1, double
 /* Sedimentation of H2O (levels nivhau..nivh2oecmwf-1), NOy and HNO3 (levels
  * nivhau..nivbas) for rows ilat0..ilat1, from the settling velocities and
  * non-sedimenting fractions that the chemistry step wrote (vsed3d,
- * parth2osed, parthno3sed), over the time step dtsedi. Needs nivhau >= 2 and
- * nivhau <= nivh2oecmwf <= nivbas + 1.
+ * parth2osed, parthno3sed), over the time step dtsedi. Needs nivhau >= 2,
+ * nivhau <= nivh2oecmwf <= nivbas + 1 and at most 128 levels nivhau..nivbas.
  * Replaces: call sedimentation(trajpre, trajtem, irapp, qj1, vsed3d,
  * nivh2oecmwf, parth2osed, parthno3sed, dtsedi) (:420-422, routine
  * :2416-2522), which the reference runs after the last chemistry sub-step of

@@ -548,8 +548,8 @@ struct Handle {
     int nlon, nlat, niv, nivbas, nivhau, nrappmax, niter, flags;
     int device;
     int solver = REPROBUS_SOLVER_REF5;  // which kernel integrates the cells
-    int npass = 1, maxit = 12;          // Newton: reference passes before, iteration cap
-    double tol = 1e-8;                  // Newton: scaled step tolerance
+    int npass = 5, maxit = 12;          // Newton: reference passes before, iteration cap
+    double tol = 1e-6;                  // Newton: scaled step tolerance
     double troe[18];
     double* d_ajl = nullptr;
     double* d_o3up = nullptr;

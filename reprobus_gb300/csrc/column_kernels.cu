@@ -5,7 +5,9 @@
 //   k_forcing     tropospheric relaxation tropo            F:4077-4574 (called :373)
 //                 CO relaxation co_tropo                   F:4577-4639 (called :377)
 //                 tropospheric H2O ecmwfh2o                F:8621-8658 (called :382)
-//   k_geo_columns geopotential of the regular grid          altitude.f90:32-57
+//   k_geo_levels  pressure, virtual temperature and geopotential
+//                 increments of the regular grid            altitude.f90:32-57
+//   k_geo_sum     the hypsometric sum up each regular column altitude.f90:51-57
 //   k_altitude    geometric altitude of every trajectory    altitude.f90:59-146
 //   k_swap64      big-endian FP64 of the history record    F:231-235, F:587-588
 //
@@ -66,14 +68,19 @@ __device__ __forceinline__ double sed_update(double q, double q_up, double part_
     return sub(add(q, gain), mul(mul(q_self, sub(1.0, part)), fracdown));
 }
 
-// One thread per column. Both of the reference's loops read only values from
-// before the loop (level iniv-1 is updated after level iniv), so the column is
-// walked downwards from the top with the level above's old values carried in
-// registers.
-__global__ void __launch_bounds__(128) k_sediment(SedArgs A) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= A.nlon * A.nrows) return;
-    const size_t col = (size_t)(t % A.nlon) + (size_t)A.nlon * (A.row0 + t / A.nlon);
+// Both of the reference's loops read only values from before the loop (level
+// iniv-1 is updated after level iniv), so every level of a column can be
+// updated at once from the old values. A block owns SED_COLS whole columns
+// (consecutive longitudes: each level plane is read coalesced) with
+// SED_LANES threads per column, each on every SED_LANES-th level: all threads
+// compute their new values from the old ones, meet at one block barrier (no
+// other block touches these columns), then store them.
+constexpr int SED_COLS = 32, SED_LANES = 16, SED_KMAX = 8;  // levels nivhau..nivbas <= SED_LANES * SED_KMAX
+
+__global__ void __launch_bounds__(SED_COLS * SED_LANES) k_sediment(SedArgs A) {
+    const int t = blockIdx.x * SED_COLS + threadIdx.x;
+    const bool live = t < A.nlon * A.nrows;
+    const size_t col = live ? (size_t)(t % A.nlon) + (size_t)A.nlon * (A.row0 + t / A.nlon) : 0;
     const size_t pl = (size_t)A.nlon * A.nlat;
     const size_t p3 = pl * A.niv;  // one species of qj1
     double* q3 = A.qj1 + 2 * p3;   // H2O
@@ -81,37 +88,38 @@ __global__ void __launch_bounds__(128) k_sediment(SedArgs A) {
     double* q5 = A.qj1 + 4 * p3;   // HNO3
     // hnm of F:2443-2446 (the constant cancels in hnm_up / hnm)
     auto hnm_at = [&](size_t i) { return dvd(A.pre[i], mul(A.tem[i], 1.38e-19)); };
-    // level k (1-based) of column col in a (nlon, nlat, levels) array
-    auto at = [&](int k) { return col + pl * (size_t)(k - 1); };
-    // H2O, levels nivh2o-1 .. nivhau (F:2456-2480)
-    {
-        size_t iu = at(A.nivhau - 1);
-        double p_up = A.pre[iu], h_up = hnm_at(iu), v_up = A.vsed[iu], s_up = A.ph2o[iu], q_up = q3[iu];
-        for (int k = A.nivhau; k <= A.nivh2o - 1; k++) {
-            const size_t i = at(k);
-            const double p = A.pre[i], h = hnm_at(i), v = A.vsed[i], s = A.ph2o[i], q = q3[i];
-            const double dz = mul(7000., log(dvd(p, p_up)));
-            const double fu = fmin(dvd(mul(v_up, A.dt), dz), 1.0);
-            const double fd = fmin(dvd(mul(v, A.dt), dz), 1.0);
-            q3[i] = sed_update(q, q_up, s_up, h_up, h, fu, q, s, fd);
-            p_up = p, h_up = h, v_up = v, s_up = s, q_up = q;
+    double n3[SED_KMAX], n4[SED_KMAX], n5[SED_KMAX];
+#pragma unroll
+    for (int j = 0; j < SED_KMAX; j++) {
+        const int k = A.nivhau + (int)threadIdx.y + j * SED_LANES;  // 1-based level
+        if (!live || k > A.nivbas) continue;
+        const size_t i = col + pl * (size_t)(k - 1), iu = i - pl;
+        const double p = A.pre[i], p_up = A.pre[iu];
+        const double h = hnm_at(i), h_up = hnm_at(iu);
+        const double v = A.vsed[i], v_up = A.vsed[iu];
+        const double dz = mul(7000., log(dvd(p, p_up)));
+        const double fu = fmin(dvd(mul(v_up, A.dt), dz), 1.0);
+        const double fd = fmin(dvd(mul(v, A.dt), dz), 1.0);
+        // H2O, levels nivh2o-1 .. nivhau (F:2456-2480)
+        if (k <= A.nivh2o - 1) {
+            const double q = q3[i];
+            n3[j] = sed_update(q, q3[iu], A.ph2o[iu], h_up, h, fu, q, A.ph2o[i], fd);
         }
+        // NOy and HNO3, levels nivbas .. nivhau (F:2482-2514; the NOy update
+        // moves the HNO3 flux, the 01/12/2012 fix at :2493)
+        const double q = q5[i], q_up = q5[iu], s = A.pno3[i], s_up = A.pno3[iu];
+        n4[j] = sed_update(q4[i], q_up, s_up, h_up, h, fu, q, s, fd);
+        n5[j] = sed_update(q, q_up, s_up, h_up, h, fu, q, s, fd);
     }
-    // NOy and HNO3, levels nivbas .. nivhau (F:2482-2514; the NOy update moves
-    // the HNO3 flux, the 01/12/2012 fix at :2493)
-    {
-        size_t iu = at(A.nivhau - 1);
-        double p_up = A.pre[iu], h_up = hnm_at(iu), v_up = A.vsed[iu], s_up = A.pno3[iu], q_up = q5[iu];
-        for (int k = A.nivhau; k <= A.nivbas; k++) {
-            const size_t i = at(k);
-            const double p = A.pre[i], h = hnm_at(i), v = A.vsed[i], s = A.pno3[i], q = q5[i];
-            const double dz = mul(7000., log(dvd(p, p_up)));
-            const double fu = fmin(dvd(mul(v_up, A.dt), dz), 1.0);
-            const double fd = fmin(dvd(mul(v, A.dt), dz), 1.0);
-            q4[i] = sed_update(q4[i], q_up, s_up, h_up, h, fu, q, s, fd);
-            q5[i] = sed_update(q, q_up, s_up, h_up, h, fu, q, s, fd);
-            p_up = p, h_up = h, v_up = v, s_up = s, q_up = q;
-        }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < SED_KMAX; j++) {
+        const int k = A.nivhau + (int)threadIdx.y + j * SED_LANES;
+        if (!live || k > A.nivbas) continue;
+        const size_t i = col + pl * (size_t)(k - 1);
+        if (k <= A.nivh2o - 1) q3[i] = n3[j];
+        q4[i] = n4[j];
+        q5[i] = n5[j];
     }
 }
 
@@ -226,6 +234,9 @@ extern "C" int reprobus_sedimentation_dev(void* handle, int ilat0, int ilat1, co
     if (!trajpre || !trajtem || !qj1 || !vsed3d || !parth2osed || !parthno3sed)
         return reprobus_set_error(REPROBUS_ERR_ARG, "NULL array argument");
     if (H.nivhau < 2) return reprobus_set_error(REPROBUS_ERR_ARG, "sedimentation needs nivhau >= 2 (got %d)", H.nivhau);
+    if (H.nivbas - H.nivhau + 1 > SED_LANES * SED_KMAX)
+        return reprobus_set_error(REPROBUS_ERR_ARG, "sedimentation covers at most %d levels (nivhau..nivbas)",
+                                  SED_LANES * SED_KMAX);
     if (nivh2oecmwf < H.nivhau || nivh2oecmwf > H.nivbas + 1)
         return reprobus_set_error(REPROBUS_ERR_ARG, "nivh2oecmwf %d outside %d..%d", nivh2oecmwf, H.nivhau,
                                   H.nivbas + 1);
@@ -243,7 +254,7 @@ extern "C" int reprobus_sedimentation_dev(void* handle, int ilat0, int ilat1, co
     A.nrows = ilat1 - ilat0 + 1;
     A.dt = dtsedi;
     const int n = A.nlon * A.nrows;
-    k_sediment<<<(n + 127) / 128, 128, 0, H.stream>>>(A);
+    k_sediment<<<(n + SED_COLS - 1) / SED_COLS, dim3(SED_COLS, SED_LANES), 0, H.stream>>>(A);
     COL_TRY(cudaGetLastError());
     COL_TRY(cudaStreamSynchronize(H.stream));
     return REPROBUS_OK;
@@ -308,35 +319,48 @@ struct GeoArgs {
     int nlon, nlat, niv;
 };
 
-// one thread per regular column: p, tv (altitude.f90:34-46) and the
-// hypsometric sum from the surface up (:48-57)
-__global__ void __launch_bounds__(128) k_geo_columns(GeoArgs A) {
+// one thread per regular grid point: p and tv (altitude.f90:34-46) and the
+// geopotential increment between the point and the one below it (:55-57; at
+// the lowest level the step from the surface, :51-52), into georeg
+__global__ void __launch_bounds__(128) k_geo_levels(GeoArgs A) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t pl = (size_t)A.nlon * A.nlat;
+    if (t >= (long long)pl * A.niv) return;
+    const size_t c = (size_t)(t % pl);
+    const int k = (int)(t / pl);  // 0-based level
+    const double ps = A.psol[c];
+    auto tv_at = [&](size_t i) { return mul(A.t[i], add(1., dvd(mul(mul(0.608, A.h2o[i]), 18.), 28.97))); };
+    const double p = add(A.aaa[k], mul(A.bbb[k], ps));
+    const double tv = tv_at(t);
+    double inc;
+    if (k == A.niv - 1) {
+        inc = add(A.relief[c], mul(mul(mul(kCtegas, tv), log(dvd(ps, p))), 1.e-3));
+    } else {
+        const double p1 = add(A.aaa[k + 1], mul(A.bbb[k + 1], ps));
+        inc = mul(mul(mul(kCtegas, dvd(add(tv_at(t + pl), tv), 2.)), log(dvd(p1, p))), 1.e-3);
+    }
+    A.p[t] = p;
+    A.tv[t] = tv;
+    A.georeg[t] = inc;
+}
+
+// one thread per regular column: the hypsometric sum from the surface up in
+// the reference's order (:51-57), in place over the increments, and whether
+// the pressure increases with the level
+__global__ void __launch_bounds__(128) k_geo_sum(GeoArgs A) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= A.nlon * A.nlat) return;
     const size_t pl = (size_t)A.nlon * A.nlat;
-    const double ps = A.psol[c];
-    auto tv_at = [&](int k) {  // 0-based level
-        const size_t i = c + pl * k;
-        return mul(A.t[i], add(1., dvd(mul(mul(0.608, A.h2o[i]), 18.), 28.97)));
-    };
-    int k = A.niv - 1;
-    double pk = add(A.aaa[k], mul(A.bbb[k], ps));
-    double tvk = tv_at(k);
-    double g = add(A.relief[c], mul(mul(mul(kCtegas, tvk), log(dvd(ps, pk))), 1.e-3));
-    A.p[c + pl * k] = pk;
-    A.tv[c + pl * k] = tvk;
-    A.georeg[c + pl * k] = g;
+    double g = A.georeg[c + pl * (A.niv - 1)];
+    double pk = A.p[c + pl * (A.niv - 1)];
     int mono = 1;
-    for (k = A.niv - 2; k >= 0; k--) {
-        const double p = add(A.aaa[k], mul(A.bbb[k], ps));
-        const double tv = tv_at(k);
-        g = add(g, mul(mul(mul(kCtegas, dvd(add(tvk, tv), 2.)), log(dvd(pk, p))), 1.e-3));
+    for (int k = A.niv - 2; k >= 0; k--) {
+        const size_t i = c + pl * k;
+        g = add(g, A.georeg[i]);
+        A.georeg[i] = g;
+        const double p = A.p[i];
         if (!(p <= pk)) mono = 0;
-        A.p[c + pl * k] = p;
-        A.tv[c + pl * k] = tv;
-        A.georeg[c + pl * k] = g;
         pk = p;
-        tvk = tv;
     }
     A.mono[c] = mono;
 }
@@ -425,7 +449,8 @@ extern "C" int reprobus_altitude_dev(void* handle, const double* relief, const d
     G.georeg = G.tv + n3;
     G.mono = (int*)(G.georeg + n3);
     G.nlon = H.nlon, G.nlat = H.nlat, G.niv = H.niv;
-    k_geo_columns<<<(unsigned)((pl + 127) / 128), 128, 0, H.stream>>>(G);
+    k_geo_levels<<<(unsigned)((n3 + 127) / 128), 128, 0, H.stream>>>(G);
+    k_geo_sum<<<(unsigned)((pl + 127) / 128), 128, 0, H.stream>>>(G);
     COL_TRY(cudaGetLastError());
     AltArgs A;
     const size_t off = (size_t)(irapp - 1) * n3;

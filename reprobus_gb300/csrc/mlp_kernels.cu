@@ -201,8 +201,11 @@ constexpr int WIMG_CHUNKS = 256 * 16 + 4 * 128 * 32 + 64 * 32;
 // normalisation, 4 layers on the tensor cores with the activations kept in
 // shared memory, output de-normalisation. The six weight images of a tile
 // stream through two 64 KB buffers by bulk copies: the copy of the next
-// image runs while the tensor cores work on the current one.
-__global__ void __launch_bounds__(128, 1) k_mlp_infer(InferArgs a) {
+// image runs while the tensor cores work on the current one. 8 warps: warps
+// w and w + 4 read the same TMEM lane quarter (rows 32 (w % 4) ..) and split
+// the accumulator columns between them in the epilogues.
+constexpr int MLP_INFER_THREADS = 256;
+__global__ void __launch_bounds__(MLP_INFER_THREADS, 1) k_mlp_infer(InferArgs a) {
     extern __shared__ __align__(1024) uint8_t sm[];
     uint8_t* act = sm;                                     // 128 x 256 BF16 (64 KB)
     uint8_t* wbuf[2] = {sm + 65536, sm + 131072};          // weight images (64 KB each)
@@ -232,7 +235,8 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(InferArgs a) {
     __syncthreads();
     tc_fence_after();
     const uint32_t tbase = tslot;
-    const uint32_t trow = tbase + ((uint32_t)(warp * 32) << 16);
+    const int quarter = warp & 3, chalf = warp >> 2;  // TMEM lane quarter, column half
+    const uint32_t trow = tbase + ((uint32_t)(quarter * 32) << 16);
     uint32_t phase = 0, wph[2] = {0, 0};
     bool ok = true;
     if (threadIdx.x == 0 && nimg > 0) {
@@ -273,9 +277,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(InferArgs a) {
     auto hidden_epilogue = [&](int l) {
         // TMEM (256 columns) + bias, SiLU -> BF16 activations (K = 256 layout) in act
         const float* bl = bias + l * MLP_H;
-        const int r = warp * 32 + lane;
+        const int r = quarter * 32 + lane;
 #pragma unroll 1
-        for (int c = 0; c < MLP_H; c += 16) {
+        for (int c = chalf * (MLP_H / 2); c < (chalf + 1) * (MLP_H / 2); c += 16) {
             float v[16];
             tmem_ld16(trow + c, v);
 #pragma unroll
@@ -291,9 +295,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(InferArgs a) {
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int m0 = tile * 128;
         if (ok) {   // input: normalise, split into BF16 hi + lo, K = 128 layout (hi | lo)
-            const int r = threadIdx.x, row = m0 + r;
+            const int r = threadIdx.x & 127, row = m0 + r, k8h = (threadIdx.x >> 7) * 4;
 #pragma unroll
-            for (int k8 = 0; k8 < 8; k8++) {
+            for (int k8 = k8h; k8 < k8h + 4; k8++) {
                 __align__(16) __nv_bfloat16 hi[8], lo[8];
 #pragma unroll
                 for (int j = 0; j < 8; j++) {
@@ -317,9 +321,9 @@ __global__ void __launch_bounds__(128, 1) k_mlp_infer(InferArgs a) {
         if (ok) hidden_epilogue(2);
         mma_img(0, MLP_H, MLP_OUT);   // layer 3
         if (ok) {   // output: + bias, de-normalise, threshold
-            const int r = warp * 32 + lane, row = m0 + r;
+            const int r = quarter * 32 + lane, row = m0 + r;
 #pragma unroll 1
-            for (int c = 0; c < MLP_OUT; c += 16) {
+            for (int c = chalf * (MLP_OUT / 2); c < (chalf + 1) * (MLP_OUT / 2); c += 16) {
                 float v[16];
                 tmem_ld16(trow + c, v);
                 if (row < a.B) {
@@ -695,7 +699,7 @@ int mlp_infer(void* net, const float* X, float* Y, int B, cudaStream_t s) {
     }
     const int nsm = n->nsm;
     const int tiles = (B + 127) / 128;
-    k_mlp_infer<<<tiles < nsm ? tiles : nsm, 128, smem, s>>>(a);
+    k_mlp_infer<<<tiles < nsm ? tiles : nsm, MLP_INFER_THREADS, smem, s>>>(a);
     MLP_TRY(cudaGetLastError());
     return REPROBUS_OK;
 }

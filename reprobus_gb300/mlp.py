@@ -125,17 +125,17 @@ def cell_states(dc, case):
     return torch.cat([q, h], 0).T
 
 
-def sample(case, solver=chem.SOLVER_NEWTON64):
+def sample(case, solver=chem.SOLVER_NEWTON64, npass=5):
     """(features, targets) of every chemistry cell of a case: the features of
-    the plain start, and the log10 ratios of the end-of-step mixing ratios the
-    plain solver returns (no conserv) to the plain-start ones. CUDA float32
-    tensors ncell x 64."""
+    the plain start (npass reference passes), and the log10 ratios of the
+    end-of-step mixing ratios the plain solver returns (no conserv) to the
+    plain-start ones. CUDA float32 tensors ncell x 64."""
     import torch
     from .resident import DeviceCase
     dc = DeviceCase(case)
     nc = case.nlon * case.nlat * case.nivbas
     h = chem.ChemStep.for_case(case, niter=5, flags=0)
-    h.set_solver(solver)
+    h.set_solver(solver, npass=npass)
     feat = torch.empty(nc, NFEAT, dtype=torch.float32, device="cuda")
     a = dc.args()
     h.features_dev(1, case.nlat, case.daynum, case.dt, a[0], a[1], a[2], a[3], a[4], case.irapp, a[6], a[7], feat)

@@ -19,7 +19,7 @@ import time
 import numpy as np
 
 
-def make_training_set(cases, nlon, nlat, seed0=100, log=print):
+def make_training_set(cases, nlon, nlat, seed0=100, log=print, npass=5):
     import torch
     from . import inputs, mlp
     rng = np.random.default_rng(seed0)
@@ -29,7 +29,7 @@ def make_training_set(cases, nlon, nlat, seed0=100, log=print):
         pf = 0.3 if c % 2 else 0.0
         t0 = time.time()
         case = inputs.make_case("grid", seed=seed0 + 1 + c, nlon=nlon, nlat=nlat, daynum=day, polar_frac=pf)
-        X, Y = mlp.sample(case)
+        X, Y = mlp.sample(case, npass=npass)
         Xs.append(X)
         Ys.append(Y)
         log(f"case {c}: day {day:.2f} polar {pf} cells {X.shape[0]} ({time.time() - t0:.1f} s)")
@@ -59,7 +59,7 @@ def main(argv=None):
     torch.cuda.synchronize()
     dt = time.time() - t0
     tau = mlp.fit_thresholds(net, Xv, Yv)
-    summary = {"cells": int(X.shape[0]), "steps": args.steps, "batch": args.batch, "train_s": round(dt, 2),
+    summary = {"cells": int(X.shape[0]), "npass": 5, "steps": args.steps, "batch": args.batch, "train_s": round(dt, 2),
                "loss_first": float(np.mean(hist[:10])), "loss_last": float(np.mean(hist[-100:])),
                "outputs_on": int(np.isfinite(tau).sum()),
                "thresholds": [None if not np.isfinite(t) else float(t) for t in tau[:mlp.NY]]}

@@ -36,7 +36,7 @@ def fixed_point(case):
 def _run(case, solver, net=None):
     from reprobus_gb300.resident import DeviceCase
     h = ChemStep.for_case(case, niter=5, flags=0)
-    h.set_solver(solver, npass=1, maxit=16, tol=1e-8)  # the default tolerance
+    h.set_solver(solver, maxit=16)  # the default start and tolerance
     if net is not None:
         h.set_mlp(net)
     dc = DeviceCase(case)
