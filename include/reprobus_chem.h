@@ -87,6 +87,8 @@ typedef struct reprobus_stats {
     double solve_ms;           /* Newton solvers: device time of the persistent solve
                                   kernel (its first launch)                          */
     int graph;                 /* 1 when the step ran as a CUDA graph               */
+    long long start64_cells;   /* mixed solver: cells whose FP32 start passes left
+                                  the FP32 range and were started in FP64        */
 } reprobus_stats;
 
 /* ---- diagnostics layout (reprobus_chem_rates_*) ----------------------------

@@ -61,7 +61,8 @@ class Stats(ctypes.Structure):
                 ("max_newton_iters", ctypes.c_int), ("solver", ctypes.c_int),
                 ("lanes_per_block", ctypes.c_int), ("blocks_per_sm", ctypes.c_int), ("z_shared", ctypes.c_int),
                 ("warm_start", ctypes.c_int), ("warm_restarts", ctypes.c_longlong),
-                ("failed_iters", ctypes.c_longlong), ("solve_ms", ctypes.c_double), ("graph", ctypes.c_int)]
+                ("failed_iters", ctypes.c_longlong), ("solve_ms", ctypes.c_double), ("graph", ctypes.c_int),
+                ("start64_cells", ctypes.c_longlong)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}

@@ -695,182 +695,187 @@ __device__ __forceinline__ void cell_rates(const double* troe, double t, double 
 }
 
 // fixed per-cell quantities of the iteration
-struct CellFix {
-    double o2, n2, h2, co2, hnm;
-    double parthno3, parth2o, parthcl, parthbr;
-    double rain_hno3, rain_hno4, rain_hcl, rain_hbr, rain_h2o2, rain_ch2o, rain_ch3o2h;
-    double sza;
+template <typename T>
+struct CellFixT {
+    T o2, n2, h2, co2, hnm;
+    T parthno3, parth2o, parthcl, parthbr;
+    T rain_hno3, rain_hno4, rain_hcl, rain_hbr, rain_h2o2, rain_ch2o, rain_ch3o2h;
+    T sza;
 };
+using CellFix = CellFixT<double>;
 
 // ----------------------------------------------------------------------------
 // one pass of the iteration, F:1350-2372; ck (43), cc (15), ck0 (42)
 // ----------------------------------------------------------------------------
-__device__ __forceinline__ void cell_pass(const CellFix& F, const double* __restrict__ K, const double* __restrict__ tj,
-                                          const double* __restrict__ het, const double* __restrict__ ck0, double dt,
-                                          double* ck, double* cc) {
-    const double a3et = 1.2e-10, a23a = 7.2e-11, a23b = 6.9e-12, a23c = 1.6e-12;
+// T = double: the reference's arithmetic (every call of the FP64 path);
+// T = float: the same statements in FP32, for the start of the mixed solver
+template <typename T>
+__device__ __forceinline__ void cell_pass(const CellFixT<T>& F, const T* __restrict__ K, const T* __restrict__ tj,
+                                          const T* __restrict__ het, const T* __restrict__ ck0, T dt, T* ck,
+                                          T* cc) {
+    const T a3et = T(1.2e-10), a23a = T(7.2e-11), a23b = T(6.9e-12), a23c = T(1.6e-12);
 #define KK(name) K[K_##name]
 #define CK(m) ck[(m)-1]
 #define CC(m) cc[(m)-1]
 #define TJ(name) tj[J_##name]
 #define HET(m) het[(m)-1]
-    const double o2 = F.o2, n2 = F.n2, h2 = F.h2, hnm = F.hnm, co2 = F.co2;
-    const double parthno3 = F.parthno3, parth2o = F.parth2o, parthcl = F.parthcl, parthbr = F.parthbr;
-    double a, b, day, ch3o, hco;
-    if (F.sza <= 95.) {
-        day = 1.;
+    const T o2 = F.o2, n2 = F.n2, h2 = F.h2, hnm = F.hnm, co2 = F.co2;
+    const T parthno3 = F.parthno3, parth2o = F.parth2o, parthcl = F.parthcl, parthbr = F.parthbr;
+    T a, b, day, ch3o, hco;
+    if (F.sza <= T(95.)) {
+        day = T(1.);
         CC(15) = ((KK(c2) * CC(2) + KK(c1a) * CC(1) + KK(d5) * CC(3)) * CK(2)) / (KK(c4) * o2 + KK(c3) * CC(4));
-        ch3o = (KK(c1b) * CC(1) * CK(2) + (KK(c5) * CC(8) + 2. * KK(c14) * CK(29) + KK(c18) * CC(11)) * CK(29) +
+        ch3o = (KK(c1b) * CC(1) * CK(2) + (KK(c5) * CC(8) + T(2.) * KK(c14) * CK(29) + KK(c18) * CC(11)) * CK(29) +
                 TJ(ch3o2h) * CK(30)) /
                (KK(c15) * o2);
         hco = (KK(c8) * CC(2) + KK(c9) * CC(4) + KK(c10) * CC(3) + KK(c19) * CC(9) + TJ(ch2o_hco)) * CK(28) /
               (KK(c12) * o2);
-        double r1 = (TJ(o3_o1d) + TJ(o3_o3p) + KK(a2) * CC(14) + KK(a6) * CC(2) + KK(a6b) * CC(6) + KK(b4) * CC(8) +
+        T r1 = (TJ(o3_o1d) + TJ(o3_o3p) + KK(a2) * CC(14) + KK(a6) * CC(2) + KK(a6b) * CC(6) + KK(b4) * CC(8) +
                      KK(d2) * CC(3)) /
                     (KK(hk2) * o2);
-        double r2 = 1. / (1. + r1);
+        T r2 = T(1.) / (T(1.) + r1);
         CC(5) = r2 * CK(8);
         CC(4) = r1 * CC(5);
-        double r3 = TJ(o3_o1d) / (KK(hk4) * n2 + KK(hk5) * o2);
+        T r3 = TJ(o3_o1d) / (KK(hk4) * n2 + KK(hk5) * o2);
         CC(1) = r3 * CC(5);
-        double r4 = (KK(a5) * CC(4) + KK(a36) * CK(9) + KK(a19) * h2) /
+        T r4 = (KK(a5) * CC(4) + KK(a36) * CK(9) + KK(a19) * h2) /
                     (KK(a1) * o2 + KK(a2) * CC(5) + (a23a + a23b + a23c) * CC(6));
         CC(14) = r4 * CC(2);
-        double r7 = TJ(no) / (KK(b7) * o2 + KK(b6) * CC(8));
-        double r8 = (KK(b9) * CC(5)) / (TJ(no3_no) + TJ(no3_no2) + KK(b12) * CC(7));
-        double r5 = (TJ(no2) + KK(b3) * CC(4) + TJ(no3_no) * r8) /
+        T r7 = TJ(no) / (KK(b7) * o2 + KK(b6) * CC(8));
+        T r8 = (KK(b9) * CC(5)) / (TJ(no3_no) + TJ(no3_no2) + KK(b12) * CC(7));
+        T r5 = (TJ(no2) + KK(b3) * CC(4) + TJ(no3_no) * r8) /
                     (KK(b4) * CC(5) + KK(a26) * CC(6) + KK(d4) * CC(11) + KK(e4) * CC(12) + KK(c5) * CK(29));
-        CC(7) = CK(21) / (1. + r5 + r7 * r5 + r8);
+        CC(7) = CK(21) / (T(1.) + r5 + r7 * r5 + r8);
         CC(8) = r5 * CC(7);
         CC(10) = r7 * CC(8);
         CC(13) = r8 * CC(7);
-        double r6 = (KK(a6) * CC(5) + KK(a30) * CK(17) + KK(c8) * CK(28) + KK(d8) * CC(11) + KK(e10) * CC(12) +
+        T r6 = (KK(a6) * CC(5) + KK(a30) * CK(17) + KK(c8) * CK(28) + KK(d8) * CC(11) + KK(e10) * CC(12) +
                      KK(a1) * o2 * r4) /
                     ((a23a + a23b + a23c) * CC(14) + KK(a6b) * CC(5) + KK(a7) * CC(4) + KK(a26) * CC(8) +
-                     2. * KK(a27) * CC(6) + KK(a17) * CC(2) + KK(d7) * CC(3) + KK(d10) * CC(3) + KK(d33) * CC(11) +
+                     T(2.) * KK(a27) * CC(6) + KK(a17) * CC(2) + KK(d7) * CC(3) + KK(d10) * CC(3) + KK(d33) * CC(11) +
                      KK(e7) * CC(9) + KK(e15) * CC(12));
-        a = .5;
-        b = 1. - a;
+        a = T(.5);
+        b = T(1.) - a;
         CC(6) = a * CC(6) + b * CC(2) * r6;
-        double r13 = KK(d31) * CC(7) /
+        T r13 = KK(d31) * CC(7) /
                      (TJ(clono2_cl) + TJ(clono2_clo) + KK(d32) * CC(4) + HET(1) * CK(3) + HET(2) * CK(13));
-        double r9 = (KK(d33) * CC(6) + HET(1) * CK(3) * r13) / (HET(5) * CK(13) + KK(d35) * CC(4) + TJ(hocl));
-        double r10 = (KK(d60) * CC(11)) / (KK(d61) * hnm + TJ(cl2o2));
-        double r12 = KK(e5c) * CC(12) / TJ(brcl);
-        double r11 = (KK(d3) * CC(4) + KK(d4) * CC(8) + KK(d8) * CC(2) + KK(c18) * CK(29) + KK(e5b) * CC(12) +
-                      TJ(clono2_cl) * r13 + TJ(hocl) * r9 + 2. * TJ(cl2o2) * r10 + TJ(brcl) * r12) /
+        T r9 = (KK(d33) * CC(6) + HET(1) * CK(3) * r13) / (HET(5) * CK(13) + KK(d35) * CC(4) + TJ(hocl));
+        T r10 = (KK(d60) * CC(11)) / (KK(d61) * hnm + TJ(cl2o2));
+        T r12 = KK(e5c) * CC(12) / TJ(brcl);
+        T r11 = (KK(d3) * CC(4) + KK(d4) * CC(8) + KK(d8) * CC(2) + KK(c18) * CK(29) + KK(e5b) * CC(12) +
+                      TJ(clono2_cl) * r13 + TJ(hocl) * r9 + T(2.) * TJ(cl2o2) * r10 + TJ(brcl) * r12) /
                      (KK(d2) * CC(5) + KK(d5) * CK(2) + KK(d7) * CC(6) + KK(d10) * CC(6) + KK(d37) * CK(15));
-        CC(11) = a * CC(11) + b * CK(23) / (1. + r11);
+        CC(11) = a * CC(11) + b * CK(23) / (T(1.) + r11);
         CC(3) = r11 * CC(11);
-        double r27 = KK(e13) * CC(7) / (TJ(brono2) + KK(e8) * CC(4));
-        double r28 = KK(e15) * CC(6) / (TJ(hobr) + KK(e16) * CC(4));
-        double r29 = KK(e5c) * CC(11) / TJ(brcl);
-        double r30 = (KK(e3) * CC(4) + KK(e4) * CC(8) + KK(e5a) * CC(11) + KK(e5b) * CC(11) + 2. * KK(e6) * CC(12) +
-                      KK(e10) * CC(2) + TJ(bro) + TJ(brono2) * 0.85 * r27 + TJ(hobr) * r28 + TJ(brcl) * r29) /
+        T r27 = KK(e13) * CC(7) / (TJ(brono2) + KK(e8) * CC(4));
+        T r28 = KK(e15) * CC(6) / (TJ(hobr) + KK(e16) * CC(4));
+        T r29 = KK(e5c) * CC(11) / TJ(brcl);
+        T r30 = (KK(e3) * CC(4) + KK(e4) * CC(8) + KK(e5a) * CC(11) + KK(e5b) * CC(11) + T(2.) * KK(e6) * CC(12) +
+                      KK(e10) * CC(2) + TJ(bro) + TJ(brono2) * T(0.85) * r27 + TJ(hobr) * r28 + TJ(brcl) * r29) /
                      (KK(e2) * CC(5) + KK(e7) * CC(6) + KK(c19) * CK(28));
-        CC(12) = a * CC(12) + b * CK(24) / (1. + r30);
+        CC(12) = a * CC(12) + b * CK(24) / (T(1.) + r30);
         CC(9) = r30 * CC(12);
-        double coea = 2. * KK(a31) + 2. * (KK(a17) + KK(a27) * r6 + (a23b + a23c) * r4) * r6;
-        double coeb = KK(b27) * CK(5) * parthno3 + KK(b22) * CC(7) + KK(b28) * CK(22) + KK(b23) * CC(7) * r6 +
+        T coea = T(2.) * KK(a31) + T(2.) * (KK(a17) + KK(a27) * r6 + (a23b + a23c) * r4) * r6;
+        T coeb = KK(b27) * CK(5) * parthno3 + KK(b22) * CC(7) + KK(b28) * CK(22) + KK(b23) * CC(7) * r6 +
                       KK(c2) * CK(2) + KK(c7) * CK(29) * r6 + KK(c8) * CK(28) + KK(c17a) * CK(30) +
                       KK(d7) * CC(3) * r6 + KK(d9) * CC(11) + KK(d11) * CK(13) * parthcl + KK(d33) * CC(11) * r6 +
                       KK(d34) * CK(15) + KK(e11) * CK(19) * parthbr + KK(e7) * CC(9) * r6 + KK(e15) * CC(12) * r6;
-        double t01 = 2. * (KK(a1et) * CC(1) + TJ(h2o)) * CK(3) * parth2o;
-        double t02 = ((KK(c1a) + KK(c1b)) * CK(2) + 2. * a3et * h2) * CC(1);
-        double t03 = KK(c3) * CC(15) * CC(4);
-        double t04 = TJ(ch3o2h) * CK(30);
-        double t05 = KK(c15) * ch3o * o2;
-        double t06 = (TJ(ch2o_hco) + KK(c9) * CC(4)) * CK(28);
-        double t07 = KK(c12) * hco * o2;
-        double t08 = TJ(hno3) * CK(5) * parthno3;
-        double t09 = (KK(b24) * hnm + TJ(hno4)) * CK(22);
-        double t10 = (KK(d35) * CC(4) + KK(d37) * CC(3) + TJ(hocl)) * CK(15);
-        double t11 = 2. * TJ(h2o2) * CK(17);
-        double t12 = KK(d6) * h2 * CC(3);
-        double t13 = TJ(hobr) * CK(26);
-        double t14 = KK(e16) * CC(4) * CK(26);
-        double t15 = TJ(hbr) * CK(19);
-        double coec = t01 + t02 + t03 + t04 + t05 + t06 + t07 + t08 + t09 + t10 + t11 + t12 + t13 + t14 + t15;
-        double argum = coeb * coeb + 4. * coea * coec;
-        argum = fmax(argum, 0.);
-        CC(2) = a * CC(2) + b * (sqrt(argum) - coeb) / (2. * coea);
+        T t01 = T(2.) * (KK(a1et) * CC(1) + TJ(h2o)) * CK(3) * parth2o;
+        T t02 = ((KK(c1a) + KK(c1b)) * CK(2) + T(2.) * a3et * h2) * CC(1);
+        T t03 = KK(c3) * CC(15) * CC(4);
+        T t04 = TJ(ch3o2h) * CK(30);
+        T t05 = KK(c15) * ch3o * o2;
+        T t06 = (TJ(ch2o_hco) + KK(c9) * CC(4)) * CK(28);
+        T t07 = KK(c12) * hco * o2;
+        T t08 = TJ(hno3) * CK(5) * parthno3;
+        T t09 = (KK(b24) * hnm + TJ(hno4)) * CK(22);
+        T t10 = (KK(d35) * CC(4) + KK(d37) * CC(3) + TJ(hocl)) * CK(15);
+        T t11 = T(2.) * TJ(h2o2) * CK(17);
+        T t12 = KK(d6) * h2 * CC(3);
+        T t13 = TJ(hobr) * CK(26);
+        T t14 = KK(e16) * CC(4) * CK(26);
+        T t15 = TJ(hbr) * CK(19);
+        T coec = t01 + t02 + t03 + t04 + t05 + t06 + t07 + t08 + t09 + t10 + t11 + t12 + t13 + t14 + t15;
+        T argum = coeb * coeb + T(4.) * coea * coec;
+        argum = fmax(argum, T(0.));
+        CC(2) = a * CC(2) + b * (sqrt(argum) - coeb) / (T(2.) * coea);
     } else {
-        day = 0.;
-        CC(14) = 0.;
-        CC(15) = 0.;
-        ch3o = 0.;
-        hco = 0.;
-        CC(1) = 0.;
-        CC(4) = 0.;
+        day = T(0.);
+        CC(14) = T(0.);
+        CC(15) = T(0.);
+        ch3o = T(0.);
+        hco = T(0.);
+        CC(1) = T(0.);
+        CC(4) = T(0.);
         CC(5) = CK(8);
-        CC(2) = 0.;
-        CC(3) = 0.;
-        CC(6) = 0.;
-        CC(8) = 0.;
-        double r8 = KK(b9) * CC(5) / (KK(b12) * fmax(CC(7), 1.e-30));
-        CC(7) = CK(21) / (1. + r8);
+        CC(2) = T(0.);
+        CC(3) = T(0.);
+        CC(6) = T(0.);
+        CC(8) = T(0.);
+        T r8 = KK(b9) * CC(5) / (KK(b12) * fmax(CC(7), T(1.e-30)));
+        CC(7) = CK(21) / (T(1.) + r8);
         CC(13) = r8 * CC(7);
-        CC(10) = 0.;
-        CC(11) = fmax(CK(23), 0.);
-        CC(9) = 0.;
-        CC(12) = fmax(CK(24), 0.);
+        CC(10) = T(0.);
+        CC(11) = fmax(CK(23), T(0.));
+        CC(9) = T(0.);
+        CC(12) = fmax(CK(24), T(0.));
     }
     // production / loss, F:1758-2358; update F:2364-2372 applied per species
-    const double rain_hno3 = F.rain_hno3, rain_hno4 = F.rain_hno4, rain_hcl = F.rain_hcl, rain_hbr = F.rain_hbr,
+    const T rain_hno3 = F.rain_hno3, rain_hno4 = F.rain_hno4, rain_hcl = F.rain_hcl, rain_hbr = F.rain_hbr,
                  rain_h2o2 = F.rain_h2o2, rain_ch2o = F.rain_ch2o, rain_ch3o2h = F.rain_ch3o2h;
-    double pr[NBCON - 1], pe[NBCON - 1];
+    T pr[NBCON - 1], pe[NBCON - 1];
 #define PR(m) pr[(m)-1]
 #define PE(m) pe[(m)-1]
-    double t01, t02, t03, t04, t05, t06, t07, t08, t09, t10, t11, t12, t13, t14;
-    PR(1) = 0.e0;
+    T t01, t02, t03, t04, t05, t06, t07, t08, t09, t10, t11, t12, t13, t14;
+    PR(1) = T(0.e0);
     PE(1) = TJ(n2o) + (KK(b38) + KK(b39)) * CC(1);
-    PR(2) = 0.e0;
+    PR(2) = T(0.e0);
     PE(2) = KK(c2) * CC(2) + KK(c1a) * CC(1) + KK(c1b) * CC(1) + KK(c1c) * CC(1) + KK(d5) * CC(3);
     PR(3) = KK(c2) * CC(2) * CK(2) + KK(c8) * CC(2) * CK(28) + KK(c17a) * CK(30) * CC(2) +
             KK(c17b) * CK(30) * CC(2) + (KK(a17) * CC(2) + a23c * CC(14)) * CC(6) + KK(a19) * CC(2) * h2 +
             KK(a30) * CC(2) * CK(17) + KK(a31) * CC(2) * CC(2) + KK(b27) * CC(2) * CK(5) * parthno3 +
             KK(d11) * CC(2) * CK(13) * parthcl;
     PE(3) = (TJ(h2o) + KK(a1et) * CC(1)) * parth2o;
-    PR(4) = 2. * KK(b39) * CC(1) * CK(1);
-    PE(4) = 2. * KK(b6) * CC(10) * CC(8) + rain_hno3 * CK(5) + rain_hno4 * CK(22);
+    PR(4) = T(2.) * KK(b39) * CC(1) * CK(1);
+    PE(4) = T(2.) * KK(b6) * CC(10) * CC(8) + rain_hno3 * CK(5) + rain_hno4 * CK(22);
     PE(4) = PE(4) / CK(4);
     PR(5) = KK(b22) * CC(2) * CC(7) + HET(1) * CK(14) * CK(3) + HET(2) * CK(14) * CK(13) +
-            2. * HET(3) * CK(6) * CK(3) + HET(4) * CK(6) * CK(13) + HET(6) * CK(20) * CK(3);
+            T(2.) * HET(3) * CK(6) * CK(3) + HET(4) * CK(6) * CK(13) + HET(6) * CK(20) * CK(3);
     PE(5) = (TJ(hno3) + KK(b27) * CC(2)) * parthno3 + rain_hno3;
     PR(6) = KK(b12) * CC(13) * CC(7);
     PE(6) = TJ(n2o5) + KK(b32) * hnm + HET(3) * CK(3) + HET(4) * CK(13);
-    PR(7) = 3. * (TJ(cfc11) + KK(d90) * CC(1)) * CK(31) + 2. * (TJ(cfc12) + KK(d91) * CC(1)) * CK(32) +
-            3. * (TJ(cfc113) + KK(d92) * CC(1)) * CK(33) + 4. * (TJ(ccl4) + KK(d93) * CC(1)) * CK(34) +
-            3. * (TJ(ch3ccl3) + KK(d94) * CC(2)) * CK(35) + 1. * (TJ(ch3cl) + KK(d95) * CC(2)) * CK(36) +
-            1. * (TJ(hcfc22) + KK(d96) * CC(1) + KK(d97) * CC(2)) * CK(37) +
-            1. * (TJ(h1211) + KK(e52) * CC(1)) * CK(39);
+    PR(7) = T(3.) * (TJ(cfc11) + KK(d90) * CC(1)) * CK(31) + T(2.) * (TJ(cfc12) + KK(d91) * CC(1)) * CK(32) +
+            T(3.) * (TJ(cfc113) + KK(d92) * CC(1)) * CK(33) + T(4.) * (TJ(ccl4) + KK(d93) * CC(1)) * CK(34) +
+            T(3.) * (TJ(ch3ccl3) + KK(d94) * CC(2)) * CK(35) + T(1.) * (TJ(ch3cl) + KK(d95) * CC(2)) * CK(36) +
+            T(1.) * (TJ(hcfc22) + KK(d96) * CC(1) + KK(d97) * CC(2)) * CK(37) +
+            T(1.) * (TJ(h1211) + KK(e52) * CC(1)) * CK(39);
     PE(7) = rain_hcl * CK(13);
     PE(7) = PE(7) / CK(7);
-    double ratio = TJ(cl2o2) / (TJ(cl2o2) + KK(d61) * hnm);
-    PR(8) = 2. * TJ(o2) * o2 + KK(a26) * CC(6) * CC(8) + KK(c5) * CC(8) * CK(29);
-    t01 = 2. * KK(hk1) * CC(4) * CC(4);
-    t02 = 2. * KK(hk3) * CC(5) * CC(4);
-    t03 = 2. * KK(b3) * CC(7) * CC(4);
-    t04 = 2. * KK(d3) * CC(11) * CC(4);
-    t05 = 2. * KK(d60) * ratio * CC(11) * CC(11);
+    T ratio = TJ(cl2o2) / (TJ(cl2o2) + KK(d61) * hnm);
+    PR(8) = T(2.) * TJ(o2) * o2 + KK(a26) * CC(6) * CC(8) + KK(c5) * CC(8) * CK(29);
+    t01 = T(2.) * KK(hk1) * CC(4) * CC(4);
+    t02 = T(2.) * KK(hk3) * CC(5) * CC(4);
+    t03 = T(2.) * KK(b3) * CC(7) * CC(4);
+    t04 = T(2.) * KK(d3) * CC(11) * CC(4);
+    t05 = T(2.) * KK(d60) * ratio * CC(11) * CC(11);
     t06 = fmin(TJ(hocl) * CK(15), KK(d33) * CC(6) * CC(11));
-    t07 = 2. * fmin(KK(e5c) * CC(12) * CC(11), TJ(brcl) * CK(27));
-    t08 = 2. * KK(e5b) * CC(12) * CC(11) * day;
+    t07 = T(2.) * fmin(KK(e5c) * CC(12) * CC(11), TJ(brcl) * CK(27));
+    t08 = T(2.) * KK(e5b) * CC(12) * CC(11) * day;
     t09 = fmin(KK(e15) * CC(12) * CC(6), TJ(hobr) * CK(26));
-    t10 = 2. * KK(e6) * CC(12) * CC(12) * day;
-    t11 = 2. * (TJ(no3_no) / fmax(TJ(no3_no) + TJ(no3_no2), 1.e-30)) * TJ(clono2_cl) * CK(14);
+    t10 = T(2.) * KK(e6) * CC(12) * CC(12) * day;
+    t11 = T(2.) * (TJ(no3_no) / fmax(TJ(no3_no) + TJ(no3_no2), T(1.e-30))) * TJ(clono2_cl) * CK(14);
     t12 = (KK(a2) * CC(14) + KK(a6) * CC(2) + KK(a6b) * CC(6)) * CC(5) + (KK(a5) * CC(2) + KK(a7) * CC(6)) * CC(4);
-    t13 = 2. * KK(b9) * CC(7) * CC(5) * TJ(no3_no) / fmax(TJ(no3_no) + TJ(no3_no2), 1.e-30);
+    t13 = T(2.) * KK(b9) * CC(7) * CC(5) * TJ(no3_no) / fmax(TJ(no3_no) + TJ(no3_no2), T(1.e-30));
     PE(8) = t01 + t02 + t03 + t04 + t05 + t06 + t07 + t08 + t09 + t10 + t11 + t12 + t13;
     PE(8) = PE(8) / CK(8);
     PR(9) = TJ(co2) * co2 + TJ(ch2o_co) * CK(28) + KK(c12) * hco * o2;
     PE(9) = KK(a36) * CC(2);
     PR(10) = KK(e5a) * CC(12) * CC(11);
     PE(10) = TJ(oclo);
-    PR(11) = 0.;
-    PE(11) = 0.;
-    PR(12) = 0.;
-    PE(12) = 0.;
+    PR(11) = T(0.);
+    PE(11) = T(0.);
+    PR(12) = T(0.);
+    PE(12) = T(0.);
     PR(13) = (KK(c10) * CK(28) + KK(d5) * CK(2) + KK(d7) * CC(6) + KK(d6) * h2) * CC(3) + KK(d9) * CC(2) * CC(11);
     PE(13) = (TJ(hcl) + KK(d11) * CC(2)) * parthcl + HET(2) * CK(14) + HET(4) * CK(6) + HET(5) * CK(15) +
              HET(7) * CK(26) + rain_hcl;
@@ -890,32 +895,32 @@ __device__ __forceinline__ void cell_pass(const CellFix& F, const double* __rest
     PR(20) = KK(e13) * CC(12) * CC(7);
     PE(20) = TJ(brono2) + KK(e8) * CC(4) + HET(6) * CK(3);
     PR(21) = (TJ(hno4) + KK(b28) * CC(2) + KK(b24) * hnm) * CK(22) + TJ(hno3) * CK(5) * parthno3 +
-             2. * (TJ(n2o5) + KK(b32) * hnm) * CK(6) + 2. * KK(b39) * CC(1) * CK(1) + TJ(clno2) * CK(18) +
+             T(2.) * (TJ(n2o5) + KK(b32) * hnm) * CK(6) + T(2.) * KK(b39) * CC(1) * CK(1) + TJ(clno2) * CK(18) +
              KK(b27) * CK(5) * parthno3 * CC(2) + KK(d32) * CK(14) * CC(4) +
              (TJ(clono2_cl) + TJ(clono2_clo)) * CK(14) + TJ(brono2) * CK(20) + KK(e8) * CK(20) * CC(4);
-    PE(21) = (KK(d31) * CC(11) + KK(b22) * CC(2) + KK(b23) * CC(6) + 2. * KK(b12) * CC(13) + KK(d36) * CC(3) +
+    PE(21) = (KK(d31) * CC(11) + KK(b22) * CC(2) + KK(b23) * CC(6) + T(2.) * KK(b12) * CC(13) + KK(d36) * CC(3) +
               KK(e13) * CC(12)) *
                  CC(7) +
-             2. * KK(b6) * CC(10) * CC(8);
+             T(2.) * KK(b6) * CC(10) * CC(8);
     PE(21) = PE(21) / CK(21);
     PR(22) = KK(b23) * CC(6) * CC(7);
     PE(22) = TJ(hno4) + KK(b28) * CC(2) + KK(b24) * hnm + rain_hno4;
-    t01 = 2. * (KK(d61) * hnm + TJ(cl2o2)) * CK(25);
+    t01 = T(2.) * (KK(d61) * hnm + TJ(cl2o2)) * CK(25);
     t02 = (TJ(clono2_cl) + TJ(clono2_clo) + KK(d32) * CC(4)) * CK(14);
     t03 = (TJ(hocl) + KK(d34) * CC(2) + KK(d35) * CC(4)) * CK(15);
     t04 = TJ(oclo) * CK(10) + (TJ(hcl) + KK(d11) * CC(2)) * CK(13) * parthcl;
-    t05 = 2. * TJ(cl2) * CK(16);
+    t05 = T(2.) * TJ(cl2) * CK(16);
     t06 = TJ(clno2) * CK(18);
     t07 = TJ(brcl) * CK(27);
-    t08 = 3. * (TJ(cfc11) + KK(d90) * CC(1)) * CK(31);
-    t09 = 2. * (TJ(cfc12) + KK(d91) * CC(1)) * CK(32);
-    t10 = 3. * (TJ(cfc113) + KK(d92) * CC(1)) * CK(33);
-    t11 = 4. * (TJ(ccl4) + KK(d93) * CC(1)) * CK(34);
-    t12 = 3. * (TJ(ch3ccl3) + KK(d94) * CC(2)) * CK(35);
-    t13 = 1. * (TJ(ch3cl) + KK(d95) * CC(2)) * CK(36);
-    t14 = 1. * (TJ(hcfc22) + KK(d96) * CC(1) + KK(d97) * CC(2)) * CK(37);
+    t08 = T(3.) * (TJ(cfc11) + KK(d90) * CC(1)) * CK(31);
+    t09 = T(2.) * (TJ(cfc12) + KK(d91) * CC(1)) * CK(32);
+    t10 = T(3.) * (TJ(cfc113) + KK(d92) * CC(1)) * CK(33);
+    t11 = T(4.) * (TJ(ccl4) + KK(d93) * CC(1)) * CK(34);
+    t12 = T(3.) * (TJ(ch3ccl3) + KK(d94) * CC(2)) * CK(35);
+    t13 = T(1.) * (TJ(ch3cl) + KK(d95) * CC(2)) * CK(36);
+    t14 = T(1.) * (TJ(hcfc22) + KK(d96) * CC(1) + KK(d97) * CC(2)) * CK(37);
     PR(23) = t01 + t02 + t03 + t04 + t05 + t06 + t07 + t08 + t09 + t10 + t11 + t12 + t13 + t14;
-    PE(23) = (KK(d31) * CC(7) + 2. * KK(d60) * CC(11) + 2. * KK(d62) * CC(11) + KK(e5a) * CC(12) +
+    PE(23) = (KK(d31) * CC(7) + T(2.) * KK(d60) * CC(11) + T(2.) * KK(d62) * CC(11) + KK(e5a) * CC(12) +
               KK(e5c) * CC(12) + KK(d9) * CC(2) + KK(d33) * CC(6)) *
                  CC(11) +
              (KK(c10) * CK(28) + KK(d5) * CK(2) + KK(d7) * CC(6) + KK(d6) * h2 + KK(d36) * CC(7) +
@@ -924,7 +929,7 @@ __device__ __forceinline__ void cell_pass(const CellFix& F, const double* __rest
     PE(23) = PE(23) / CK(23);
     PR(24) = TJ(hobr) * CK(26) + TJ(brono2) * CK(20) + KK(e8) * CK(20) * CC(4) + KK(e16) * CK(26) * CC(4) +
              TJ(brcl) * CK(27) + (KK(e11) * CC(2) + KK(e9) * CC(1) + TJ(hbr)) * CK(19) * parthbr +
-             2. * HET(8) * CK(19) * CK(26);
+             T(2.) * HET(8) * CK(19) * CK(26);
     PE(24) = (KK(e13) * CC(7) + KK(e5c) * CC(11) + KK(e15) * CC(6)) * CC(12) + KK(c19) * CC(9) * CK(28) +
              KK(e7) * CC(9) * CC(6);
     PE(24) = PE(24) / CK(24);
@@ -938,37 +943,37 @@ __device__ __forceinline__ void cell_pass(const CellFix& F, const double* __rest
     PE(28) = KK(c8) * CC(2) + KK(c9) * CC(4) + KK(c10) * CC(3) + KK(c19) * CC(9) + TJ(ch2o_hco) + TJ(ch2o_co) +
              rain_ch2o;
     PR(29) = KK(c4) * CC(15) * o2 + KK(c17a) * CC(2) * CK(30);
-    PE(29) = 2. * KK(c14) * CK(29) + KK(c7) * CC(6) + KK(c5) * CC(8) + KK(c18) * CC(11);
+    PE(29) = T(2.) * KK(c14) * CK(29) + KK(c7) * CC(6) + KK(c5) * CC(8) + KK(c18) * CC(11);
     PR(30) = KK(c7) * CK(29) * CC(6);
     PE(30) = KK(c17a) * CC(2) + KK(c17b) * CC(2) + TJ(ch3o2h) + rain_ch3o2h;
-    PR(31) = 0.;
+    PR(31) = T(0.);
     PE(31) = TJ(cfc11) + KK(d90) * CC(1);
-    PR(32) = 0.;
+    PR(32) = T(0.);
     PE(32) = TJ(cfc12) + KK(d91) * CC(1);
-    PR(33) = 0.;
+    PR(33) = T(0.);
     PE(33) = TJ(cfc113) + KK(d92) * CC(1);
-    PR(34) = 0.;
+    PR(34) = T(0.);
     PE(34) = TJ(ccl4) + KK(d93) * CC(1);
-    PR(35) = 0.;
+    PR(35) = T(0.);
     PE(35) = TJ(ch3ccl3) + KK(d94) * CC(2);
-    PR(36) = 0.;
+    PR(36) = T(0.);
     PE(36) = TJ(ch3cl) + KK(d95) * CC(2);
-    PR(37) = 0.;
+    PR(37) = T(0.);
     PE(37) = TJ(hcfc22) + KK(d96) * CC(1) + KK(d97) * CC(2);
-    PR(38) = 0.;
+    PR(38) = T(0.);
     PE(38) = TJ(ch3br) + KK(e50) * CC(1) + KK(e51) * CC(2);
-    PR(39) = 0.;
+    PR(39) = T(0.);
     PE(39) = TJ(h1211) + KK(e52) * CC(1);
-    PR(40) = 0.;
+    PR(40) = T(0.);
     PE(40) = TJ(h1301) + KK(e53) * CC(1);
     PR(41) = (TJ(ch3br) + KK(e50) * CC(1) + KK(e51) * CC(2)) * CK(38) + (TJ(h1211) + KK(e52) * CC(1)) * CK(39) +
-             (TJ(h1301) + KK(e53) * CC(1)) * CK(40) + 2. * (KK(e54) * CC(2) + TJ(ch2br2)) * CK(42);
+             (TJ(h1301) + KK(e53) * CC(1)) * CK(40) + T(2.) * (KK(e54) * CC(2) + TJ(ch2br2)) * CK(42);
     PE(41) = rain_hbr * CK(19);
     PE(41) = PE(41) / CK(41);
-    PR(42) = 0.;
+    PR(42) = T(0.);
     PE(42) = TJ(ch2br2) + KK(e54) * CC(2);
 #pragma unroll
-    for (int m = 0; m < NBCON - 1; m++) ck[m] = (ck0[m] + dt * pr[m]) / (1. + dt * pe[m]);
+    for (int m = 0; m < NBCON - 1; m++) ck[m] = (ck0[m] + dt * pr[m]) / (T(1.) + dt * pe[m]);
 #undef PR
 #undef PE
 #undef KK

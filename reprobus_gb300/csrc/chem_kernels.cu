@@ -352,12 +352,15 @@ __global__ void __launch_bounds__(128) k_nt_setup(Params P) {
 // from the start state (ck0 from the record, cc from hc) -> x; the cell
 // enters the work queue (day cells from the front, night cells from the
 // back); with the warm start, the network's features of that plain start.
-// restart: only cells whose warm start missed (stat < 0).
-template <bool RESTART>
+// MODE 0: every cell; MODE 1 (restart): only cells whose warm start missed
+// (stat < 0); MODE 2: only cells whose FP32 start (k_nt_start32) was not
+// finite (stat < 0), features included.
+template <int MODE>
 __global__ void __launch_bounds__(128) k_nt_start(Params P) {
+    constexpr bool RESTART = MODE == 1;
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= P.ncell) return;
-    if (RESTART && P.nt_stat[cell] >= 0) return;
+    if (MODE != 0 && P.nt_stat[cell] >= 0) return;
     const double* r = P.nt_rec + (size_t)cell * NT_REC;
     CellFix F;
     F.o2 = r[NT_RF]; F.n2 = r[NT_RF + 1]; F.h2 = r[NT_RF + 2]; F.co2 = r[NT_RF + 3]; F.hnm = r[NT_RF + 4];
@@ -397,6 +400,74 @@ __global__ void __launch_bounds__(128) k_nt_start(Params P) {
     else
         P.nt_list[P.ncell - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
     if (RESTART) atomicAdd(P.nonfinite + 4, 1ULL);
+    if (MODE == 2) atomicAdd(P.nonfinite + 6, 1ULL);
+}
+
+// the plain start of the mixed solver: the same P.npass_plain reference passes
+// in FP32 arithmetic, from the FP32 record (rates, fixed quantities) and the
+// start state rounded to FP32. The start only seeds Newton, whose FP64
+// residual and update decide the converged answer. The day/night branch
+// follows the FP64 zenith angle. A cell whose FP32 start is not finite (a
+// night-time NO2/NO3 ratio beyond the FP32 range) gets stat -1 and is started
+// again in FP64 by k_nt_start<2>; the others enter the work queue.
+__global__ void __launch_bounds__(128) k_nt_start32(Params P) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= P.ncell) return;
+    const double* r = P.nt_rec + (size_t)cell * NT_REC;
+    const float* q = P.nt_rec32 + (size_t)cell * NT_REC32;
+    const double hnm = r[NT_RF + 4];
+    const bool day = r[NT_RSZA] <= 95.;
+    CellFixT<float> F;
+    F.o2 = q[NT_RF]; F.n2 = q[NT_RF + 1]; F.h2 = q[NT_RF + 2]; F.co2 = q[NT_RF + 3]; F.hnm = q[NT_RF + 4];
+    F.parthno3 = q[NT_RF + 5]; F.parth2o = q[NT_RF + 6]; F.parthcl = q[NT_RF + 7]; F.parthbr = q[NT_RF + 8];
+    F.rain_hno3 = q[NT_RF + 9]; F.rain_hno4 = 0.f; F.rain_hcl = q[NT_RF + 10]; F.rain_hbr = q[NT_RF + 11];
+    F.rain_h2o2 = q[NT_RF + 12]; F.rain_ch2o = 0.f; F.rain_ch3o2h = 0.f;
+    F.sza = day ? 0.f : 180.f;
+    const size_t g = cell_global(P, cell), pl = plane3(P);
+    float K[NRATE], tj[NPHOT], het[9], ck0[NBCON], ck[NBCON], cc[NCM];
+#pragma unroll
+    for (int n = 0; n < NRATE; n++) K[n] = q[NT_RK + n];
+#pragma unroll
+    for (int n = 0; n < NPHOT; n++) tj[n] = q[NT_RJ + n];
+#pragma unroll
+    for (int n = 0; n < 9; n++) het[n] = q[NT_RH + n];
+#pragma unroll
+    for (int n = 0; n < NBCON; n++) ck[n] = ck0[n] = (float)r[NT_RCK0 + n];
+#pragma unroll
+    for (int n = 0; n < NCM; n++) cc[n] = (float)(P.hc[g + pl * n] * hnm);
+#pragma unroll 1
+    for (int it = 0; it < P.npass_plain; it++) cell_pass(F, K, tj, het, ck0, (float)P.sc.dt, ck, cc);
+    bool finite = true;
+#pragma unroll
+    for (int n = 0; n < NBCON - 1; n++) finite &= isfinite(ck[n]);
+#pragma unroll
+    for (int n = 0; n < NCM; n++) finite &= isfinite(cc[n]);
+    if (!finite) {
+        P.nt_stat[cell] = -1;
+        return;
+    }
+    double* x = P.nt_x + (size_t)cell * NT_NX;
+    double xd[NT_NX];
+#pragma unroll
+    for (int n = 0; n < NBCON - 1; n++) x[n] = xd[n] = (double)ck[n];
+#pragma unroll
+    for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = xd[NBCON - 1 + n] = (double)cc[n];
+    if (P.warm) {
+        double ckd[NBCON];
+#pragma unroll
+        for (int n = 0; n < NBCON - 1; n++) ckd[n] = xd[n];
+        ckd[NBCON - 1] = 0.;
+        float fe[64];
+        cell_features(P, g, hnm, r[NT_RSZA], r[NT_RSURF], ckd, xd + NBCON - 1, fe);
+        float4* o = reinterpret_cast<float4*>(P.mlp_feat + (size_t)cell * 64);
+#pragma unroll
+        for (int i = 0; i < 16; i++) o[i] = make_float4(fe[4 * i], fe[4 * i + 1], fe[4 * i + 2], fe[4 * i + 3]);
+    }
+    P.nt_stat[cell] = 0;
+    if (day)
+        P.nt_list[atomicAdd(P.nt_head + 1, 1)] = cell;
+    else
+        P.nt_list[P.ncell - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
 }
 
 // warm start: x_i = max(x_i, 1e-30 hnm) 10^y_i from the network's prediction
@@ -834,7 +905,12 @@ static int enqueue_setup(Handle* h, Params& P, bool mixed) {
         k_nt_setup<true><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     else
         k_nt_setup<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
-    k_nt_start<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    if (mixed) {
+        k_nt_start32<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        k_nt_start<2><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    } else {
+        k_nt_start<0><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    }
     return REPROBUS_OK;
 }
 
@@ -940,11 +1016,11 @@ static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool c
     CUDA_TRY(h->nt_var[ip]->launch(P, grid, h->stream));
     if (timed) CUDA_TRY(capturing ? cudaEventRecordWithFlags(h->ev3, h->stream, cudaEventRecordExternal)
                                   : cudaEventRecord(h->ev3, h->stream));
-    *launches += 4;
+    *launches += mixed ? 5 : 4;  // setup, start (FP32 + FP64 redo), solve, finish
     if (warm) {
         // misses of the warm start: the plain start, a second pass of the solve kernel
         CUDA_TRY(cudaMemsetAsync(h->nt_head, 0, 8 * sizeof(int), h->stream));
-        k_nt_start<true><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        k_nt_start<1><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
         CUDA_TRY(h->nt_var[ip]->launch(P, grid, h->stream));
         *launches += 2;
     }
@@ -1065,6 +1141,7 @@ static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
         st->warm_start = h->solver != REPROBUS_SOLVER_REF5 && h->mlp ? 1 : 0;
         st->warm_restarts = 0;
         st->failed_iters = 0;
+        st->start64_cells = 0;
         st->graph = graph ? 1 : 0;
     }
     if (counters && (st || P.check)) {
@@ -1078,6 +1155,7 @@ static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
             st->max_newton_iters = (int)c[3];
             st->warm_restarts = (long long)c[4];
             st->failed_iters = (long long)c[5];
+            st->start64_cells = (long long)c[6];
         }
         if (P.check && c[0]) return set_err(REPROBUS_ERR_NONFINITE, "%llu non-finite values in the step output", c[0]);
     }
