@@ -339,7 +339,7 @@ def main():
     clocks = Clocks(local)
     clocks.start()
     for name in run:
-        h.set_solver(solver_ids[name], npass=npass_of(name), maxit=12, tol=1e-6)
+        h.set_solver(solver_ids[name], npass=npass_of(name), maxit=12, tol=1e-5)
         h.set_mlp(net if name == "mlp" else None)
         for _ in range(max(args.warmup, 3)):
             restore()
@@ -379,7 +379,7 @@ def main():
                          {"lanes_per_block": st["lanes_per_block"], "blocks_per_sm": st["blocks_per_sm"],
                           "z_shared": st["z_shared"]}}
     clk = clocks.stop()
-    h.set_solver(solver_ids[headline], npass=npass_of(headline), maxit=12, tol=1e-6)
+    h.set_solver(solver_ids[headline], npass=npass_of(headline), maxit=12, tol=1e-5)
     h.set_mlp(net if headline == "mlp" else None)
     R = results[headline]
     ms_step = R["ms_per_step"]
