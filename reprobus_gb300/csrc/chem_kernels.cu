@@ -200,14 +200,28 @@ __device__ __forceinline__ void cell_prologue(const Params& P, int cell, CellPro
 }
 
 // write-back F:2380-2410, then (fused) conserv F:2539-2613 and clamps F:431-440
+// RECIP: number density -> mixing ratio by one reciprocal of hnm and
+// products (within an ulp of the reference's divisions, F:2380-2410), for the
+// Newton solvers, whose answer is accurate to their tolerance; the reference
+// scheme keeps the divisions.
+template <bool RECIP = false>
 __device__ __forceinline__ void cell_epilogue(const Params& P, const CellPro& C, const double* ck, const double* cc) {
     const size_t pl = plane3(P);
     double q[NBCON], h[NCM];
+    if (RECIP) {
+        const double rh = 1. / C.F.hnm;
 #pragma unroll
-    for (int n = 0; n < NBCON - 1; n++) q[n] = ck[n] / C.F.hnm;
-    q[NBCON - 1] = ck[4] * C.F.parthno3 / C.F.hnm;
+        for (int n = 0; n < NBCON - 1; n++) q[n] = ck[n] * rh;
+        q[NBCON - 1] = ck[4] * C.F.parthno3 * rh;
 #pragma unroll
-    for (int n = 0; n < NCM; n++) h[n] = cc[n] / C.F.hnm;
+        for (int n = 0; n < NCM; n++) h[n] = cc[n] * rh;
+    } else {
+#pragma unroll
+        for (int n = 0; n < NBCON - 1; n++) q[n] = ck[n] / C.F.hnm;
+        q[NBCON - 1] = ck[4] * C.F.parthno3 / C.F.hnm;
+#pragma unroll
+        for (int n = 0; n < NCM; n++) h[n] = cc[n] / C.F.hnm;
+    }
     if (P.fuse) cell_conserv(q, h);
     if (P.check) {
         unsigned int bad = 0;
@@ -561,7 +575,7 @@ __global__ void __launch_bounds__(128) k_nt_finish(Params P) {
         for (int it = 0; it < P.niter; it++) cell_pass(F, C.K, C.tj, C.A.het, C.ck0, P.sc.dt, ck, cc);
         atomicAdd(P.nonfinite + 2, 1ULL);
     }
-    cell_epilogue(P, C, ck, cc);
+    cell_epilogue<true>(P, C, ck, cc);
 }
 
 // ----------------------------------------------------------------------------
