@@ -38,6 +38,11 @@ BYTES_PER_CELL = 1008  # compulsory FP64 SoA traffic per cell-step: 63 reads + 6
 # 6612 +-*/ (612 of them divisions) + 181 transcendentals, each counted once
 # (python -m oracle.count_ops --config cfg1 --rows 12).
 OPS_PER_CELL = 6793.08
+# DRAM bytes per cell-iteration of the mixed solve kernel, from one ncu capture
+# of the 394,560-cell grid (profiles/k_nt_solve_mixed_grid180x16.md: 1.35 GB
+# per launch at 3.79 iterations per cell): the cell records re-read from DRAM,
+# proportional to the cell-iterations; scaled to the benchmark launch
+SOLVE_DRAM_BYTES_PER_CELL_ITER = 899.0
 
 
 def newton_ops():
@@ -456,7 +461,10 @@ def main():
             iters = R["iters_per_cell"] * ncell
             sm = R["solve_ms"] * 1e-3
             ach = fp64_it * iters / sm / 1e12
+            traffic = (SOLVE_DRAM_BYTES_PER_CELL_ITER * iters if headline in ("mixed", "mlp") else None)
             roof.update(kernel="k_nt_solve", kernel_ms=round(R["solve_ms"], 4), achieved=round(ach, 4),
+                        traffic=traffic, traffic_note="DRAM bytes per launch: 899 B per cell-iteration from an "
+                        "ncu capture of the 394,560-cell grid, times this launch's cell-iterations",
                         frac=round(ach / peak64, 4), fp64_ops_per_iteration=round(fp64_it, 1),
                         fp32_ops_per_iteration=round(fp32_it, 1), iterations_per_cell=round(R["iters_per_cell"], 3),
                         fp32_tflops=round(fp32_it * iters / sm / 1e12, 4),

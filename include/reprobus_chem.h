@@ -185,8 +185,11 @@ int reprobus_chem_set_solver(void* handle, int solver, int npass, int maxit, dou
  * one; a precision without that value is autotuned), zshared (0: right-hand
  * side in registers, 1: in shared memory, 2: in registers with two warp
  * groups taking turns on one set of matrix slots, so that a block keeps
- * twice the cells in flight) and blocks_per_sm (0: as many as fit). No
- * counterpart in the reference. */
+ * twice the cells in flight) and blocks_per_sm (0: as many as fit).
+ * When the environment variable REPROBUS_TUNE_CACHE names a file, the
+ * autotuner first looks there for a choice made for the same GPU model,
+ * matrix precision and cell count (skipping the timing runs), and appends
+ * each new choice to it. No counterpart in the reference. */
 int reprobus_chem_set_tuning(void* handle, int lanes_per_block, int blocks_per_sm, int zshared);
 
 /* ---- learned warm start ----------------------------------------------------

@@ -436,7 +436,7 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
     F.parthno3 = q[NT_RF + 5]; F.parth2o = q[NT_RF + 6]; F.parthcl = q[NT_RF + 7]; F.parthbr = q[NT_RF + 8];
     F.rain_hno3 = q[NT_RF + 9]; F.rain_hno4 = 0.f; F.rain_hcl = q[NT_RF + 10]; F.rain_hbr = q[NT_RF + 11];
     F.rain_h2o2 = q[NT_RF + 12]; F.rain_ch2o = 0.f; F.rain_ch3o2h = 0.f;
-    F.sza = day ? 0.f : 180.f;
+    F.sza = day ? 0.f : 180.f;  // only the day/night test reads it, decided in FP64
     const size_t g = cell_global(P, cell), pl = plane3(P);
     float K[NRATE], tj[NPHOT], het[9], ck0[NBCON], ck[NBCON], cc[NCM];
 #pragma unroll
@@ -445,10 +445,12 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
     for (int n = 0; n < NPHOT; n++) tj[n] = q[NT_RJ + n];
 #pragma unroll
     for (int n = 0; n < 9; n++) het[n] = q[NT_RH + n];
+    // double <-> float by integer operations (newton_num.cuh): a conversion
+    // instruction would issue on the FP64 pipe
 #pragma unroll
-    for (int n = 0; n < NBCON; n++) ck[n] = ck0[n] = (float)r[NT_RCK0 + n];
+    for (int n = 0; n < NBCON; n++) ck[n] = ck0[n] = nt_cvt<float>(r[NT_RCK0 + n]);
 #pragma unroll
-    for (int n = 0; n < NCM; n++) cc[n] = (float)(P.hc[g + pl * n] * hnm);
+    for (int n = 0; n < NCM; n++) cc[n] = nt_cvt<float>(P.hc[g + pl * n] * hnm);
 #pragma unroll 1
     for (int it = 0; it < P.npass_plain; it++) cell_pass(F, K, tj, het, ck0, (float)P.sc.dt, ck, cc);
     bool finite = true;
@@ -463,9 +465,9 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
     double* x = P.nt_x + (size_t)cell * NT_NX;
     double xd[NT_NX];
 #pragma unroll
-    for (int n = 0; n < NBCON - 1; n++) x[n] = xd[n] = (double)ck[n];
+    for (int n = 0; n < NBCON - 1; n++) x[n] = xd[n] = nt_widen(ck[n]);
 #pragma unroll
-    for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = xd[NBCON - 1 + n] = (double)cc[n];
+    for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = xd[NBCON - 1 + n] = nt_widen(cc[n]);
     if (P.warm) {
         double ckd[NBCON];
 #pragma unroll
@@ -932,9 +934,67 @@ static int enqueue_setup(Handle* h, Params& P, bool mixed) {
 // block) at every resident block count per SM that fits is timed on this
 // step's cells (setup, then the timed solve; the setup restores the iterate
 // and the queue between candidates) and the fastest is kept for the handle.
+// Persisted choices of the autotuner (REPROBUS_TUNE_CACHE names a text file):
+// one line per choice, "<key> <lanes per block> <zshared> <blocks per SM>
+// <ms>", the key naming the GPU model, its compute capability and SM count,
+// the matrix precision and the step's cell count. The last line of a key
+// wins; a line whose shape this build does not have is ignored.
+static void tune_key(const Handle* h, bool mixed, int ncell, char* key, size_t n) {
+    cudaDeviceProp pr;
+    if (cudaGetDeviceProperties(&pr, h->device) != cudaSuccess) memset(&pr, 0, sizeof(pr));
+    char name[128];
+    snprintf(name, sizeof(name), "%s", pr.name);
+    for (char* c = name; *c; c++)
+        if (*c == ' ' || *c == '\t') *c = '_';
+    snprintf(key, n, "%s_sm%d%d_%dsm_%s_%dcells", name, pr.major, pr.minor, pr.multiProcessorCount,
+             mixed ? "fp32" : "fp64", ncell);
+}
+
+static bool tune_cache_lookup(const char* path, const char* key, int* nth, int* zs, int* bps) {
+    FILE* f = fopen(path, "r");
+    if (!f) return false;
+    char line[512], k[256];
+    bool found = false;
+    while (fgets(line, sizeof(line), f)) {
+        int a, b, c;
+        if (sscanf(line, "%255s %d %d %d", k, &a, &b, &c) == 4 && strcmp(k, key) == 0) {
+            *nth = a, *zs = b, *bps = c;
+            found = true;
+        }
+    }
+    fclose(f);
+    return found;
+}
+
+static void tune_cache_store(const char* path, const char* key, int nth, int zs, int bps, float ms) {
+    FILE* f = fopen(path, "a");
+    if (!f) return;  // a cache that cannot be written only costs the next handle a tuning run
+    fprintf(f, "%s %d %d %d %.3f\n", key, nth, zs, bps, ms);
+    fclose(f);
+}
+
 static int choose_shape(Handle* h, Params& P, bool mixed) {
     const int ip = mixed ? 0 : 1;
     if (h->nt_var[ip]) return REPROBUS_OK;
+    const char* cache = h->want_lanes > 0 ? nullptr : getenv("REPROBUS_TUNE_CACHE");
+    char key[256] = "";
+    if (cache && cache[0]) {
+        tune_key(h, mixed, P.ncell, key, sizeof(key));
+        int nth = 0, zs = 0, bps = 0;
+        if (tune_cache_lookup(cache, key, &nth, &zs, &bps)) {
+            const NtVariant* vc[16];
+            const int n = nt_all_variants(mixed, vc, 16);
+            for (int i = 0; i < n; i++) {
+                if (vc[i]->nth != nth || vc[i]->zshared != zs) continue;
+                int occ = 0;
+                CUDA_TRY(vc[i]->prepare(&occ));
+                if (bps < 1 || bps > occ) break;
+                h->nt_var[ip] = vc[i];
+                h->nt_bps[ip] = bps;
+                return REPROBUS_OK;
+            }
+        }
+    }
     const NtVariant* vs[16];
     const int nv = nt_all_variants(mixed, vs, 16);
     struct Cand { const NtVariant* v; int bps; };
@@ -988,6 +1048,7 @@ static int choose_shape(Handle* h, Params& P, bool mixed) {
     }
     h->nt_var[ip] = cands[bi].v;
     h->nt_bps[ip] = cands[bi].bps;
+    if (key[0]) tune_cache_store(cache, key, cands[bi].v->nth, cands[bi].v->zshared, cands[bi].bps, best);
     return REPROBUS_OK;
 }
 
