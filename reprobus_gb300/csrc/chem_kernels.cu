@@ -296,12 +296,14 @@ __global__ void __launch_bounds__(128) k_chem(Params P) {
 //                queue (day cells from the front, night cells from the back);
 //                warm start: the network's features (then k_mlp_infer and
 //                k_nt_warm). Two kernels rather than one: the rate stage
-//                alone is a smaller program for the instruction cache.
+//                alone is a smaller program for the instruction cache. The
+//                mixed solver runs the passes in FP32 (k_nt_start32).
 //   k_nt_solve   persistent kernel, one lane per cell, lanes refilled from the
 //                queue (newton_kernel.cuh)
-//   k_nt_finish  one thread per cell: cells unconverged after P.maxit
-//                iterations fall back to the reference's P.niter passes;
-//                write-back, conserv, clamps
+//   k_nt_finish  one thread per converged cell: write-back, conserv, clamps
+//   k_nt_fallback one thread per cell the solver did not converge after
+//                P.maxit iterations: the reference's P.niter passes, then the
+//                same write-back
 // ----------------------------------------------------------------------------
 // the 64 raw features of the warm-start network for one cell: log10 of the 42
 // transported and 15 short-lived mixing ratios of the plain start (ck, cc:
@@ -486,17 +488,20 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
         P.nt_list[P.ncell - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
 }
 
-// warm start: x_i = max(x_i, 1e-30 hnm) 10^y_i from the network's prediction
+// warm start: x_i = max(x_i, 1e-30 hnm) 10^y_i from the network's prediction.
+// A block takes 128 cells and walks their iterates element by element, so
+// that consecutive threads touch consecutive words of x (cell-major, NT_NX
+// per cell) and of the predictions (64 per cell).
 __global__ void __launch_bounds__(128) k_nt_warm(Params P) {
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= P.ncell) return;
-    const double hnm = P.nt_rec[(size_t)cell * NT_REC + NT_RF + 4];
-    double* x = P.nt_x + (size_t)cell * NT_NX;
-    const float* y = P.mlp_y + (size_t)cell * 64;
-#pragma unroll 4
-    for (int i = 0; i < NT_NX; i++) {
-        const float yi = fminf(fmaxf(y[i], -30.f), 30.f);
-        x[i] = fmax(x[i], 1e-30 * hnm) * (double)exp10f(yi);
+    const int c0 = blockIdx.x * 128;
+    const int nc = P.ncell - c0 < 128 ? P.ncell - c0 : 128;
+    double* x = P.nt_x + (size_t)c0 * NT_NX;
+    for (int e = threadIdx.x; e < nc * NT_NX; e += blockDim.x) {
+        const int cl = e / NT_NX, i = e - cl * NT_NX;
+        const size_t cell = (size_t)c0 + cl;
+        const double hnm = P.nt_rec[cell * NT_REC + NT_RF + 4];
+        const float yi = fminf(fmaxf(P.mlp_y[cell * 64 + i], -30.f), 30.f);
+        x[e] = fmax(x[e], 1e-30 * hnm) * nt_widen(exp10f(yi));
     }
 }
 
@@ -534,49 +539,67 @@ __global__ void __launch_bounds__(128) k_ref_passes(Params P) {
     cell_epilogue(P, C, ck, cc);
 }
 
-__global__ void __launch_bounds__(128) k_nt_finish(Params P) {
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= P.ncell) return;
-    const int stat = P.nt_stat[cell];
-    const double* r = P.nt_rec + (size_t)cell * NT_REC;
-    const double* x = P.nt_x + (size_t)cell * NT_NX;
-    CellPro C;
-    C.g = cell_global(P, cell);
-    CellFix& F = C.F;
+// the write-back of one cell's Newton answer (mixing ratios, fused conserv
+// and clamps); cells the solver handed to its fallback (stat <= 0) are left
+// to k_nt_fallback, so that this common path stays small
+__device__ __forceinline__ void nt_cell_fix(const double* r, CellFix& F) {
     const double* f = r + NT_RF;
     F.o2 = f[0]; F.n2 = f[1]; F.h2 = f[2]; F.co2 = f[3]; F.hnm = f[4]; F.parthno3 = f[5];
     F.parth2o = f[6]; F.parthcl = f[7]; F.parthbr = f[8]; F.rain_hno3 = f[9];
     F.rain_hno4 = 0.; F.rain_hcl = f[10]; F.rain_hbr = f[11]; F.rain_h2o2 = f[12];
     F.rain_ch2o = 0.; F.rain_ch3o2h = 0.;
     F.sza = r[NT_RSZA];
+}
+
+__global__ void __launch_bounds__(128) k_nt_finish(Params P) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= P.ncell) return;
+    const int stat = P.nt_stat[cell];
+    if (stat <= 0) return;
+    const double* r = P.nt_rec + (size_t)cell * NT_REC;
+    const double* x = P.nt_x + (size_t)cell * NT_NX;
+    CellPro C;
+    C.g = cell_global(P, cell);
+    nt_cell_fix(r, C.F);
+    double ck[NBCON], cc[NCM];
+#pragma unroll
+    for (int n = 0; n < NBCON - 1; n++) ck[n] = x[n];
+    ck[NBCON - 1] = r[NT_RCK0 + NBCON - 1];
+#pragma unroll
+    for (int n = 0; n < NCM; n++) cc[n] = x[NBCON - 1 + n];
+    atomicAdd(P.nonfinite + 1, (unsigned long long)stat);
+    atomicMax(P.nonfinite + 3, (unsigned long long)stat);
+    cell_epilogue<true>(P, C, ck, cc);
+}
+
+// fallback of the cells the Newton solver did not converge (stat <= 0): the
+// reference scheme's niter passes from the start state, then the write-back
+__global__ void __launch_bounds__(128) k_nt_fallback(Params P) {
+    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    if (cell >= P.ncell) return;
+    if (P.nt_stat[cell] > 0) return;
+    const double* r = P.nt_rec + (size_t)cell * NT_REC;
+    CellPro C;
+    C.g = cell_global(P, cell);
+    CellFix& F = C.F;
+    nt_cell_fix(r, F);
     const size_t pl = plane3(P);
     double ck[NBCON], cc[NCM];
-    if (stat > 0) {
 #pragma unroll
-        for (int n = 0; n < NBCON - 1; n++) ck[n] = x[n];
-        ck[NBCON - 1] = r[NT_RCK0 + NBCON - 1];
+    for (int n = 0; n < NBCON; n++) C.ck0[n] = r[NT_RCK0 + n];
 #pragma unroll
-        for (int n = 0; n < NCM; n++) cc[n] = x[NBCON - 1 + n];
-        atomicAdd(P.nonfinite + 1, (unsigned long long)stat);
-        atomicMax(P.nonfinite + 3, (unsigned long long)stat);
-    } else {
-        // fallback: the reference scheme from the start state
+    for (int n = 0; n < NRATE; n++) C.K[n] = r[NT_RK + n];
 #pragma unroll
-        for (int n = 0; n < NBCON; n++) C.ck0[n] = r[NT_RCK0 + n];
+    for (int n = 0; n < NPHOT; n++) C.tj[n] = r[NT_RJ + n];
 #pragma unroll
-        for (int n = 0; n < NRATE; n++) C.K[n] = r[NT_RK + n];
+    for (int n = 0; n < 9; n++) C.A.het[n] = r[NT_RH + n];
 #pragma unroll
-        for (int n = 0; n < NPHOT; n++) C.tj[n] = r[NT_RJ + n];
+    for (int n = 0; n < NBCON; n++) ck[n] = C.ck0[n];
 #pragma unroll
-        for (int n = 0; n < 9; n++) C.A.het[n] = r[NT_RH + n];
-#pragma unroll
-        for (int n = 0; n < NBCON; n++) ck[n] = C.ck0[n];
-#pragma unroll
-        for (int n = 0; n < NCM; n++) cc[n] = P.hc[C.g + pl * n] * F.hnm;
+    for (int n = 0; n < NCM; n++) cc[n] = P.hc[C.g + pl * n] * F.hnm;
 #pragma unroll 1
-        for (int it = 0; it < P.niter; it++) cell_pass(F, C.K, C.tj, C.A.het, C.ck0, P.sc.dt, ck, cc);
-        atomicAdd(P.nonfinite + 2, 1ULL);
-    }
+    for (int it = 0; it < P.niter; it++) cell_pass(F, C.K, C.tj, C.A.het, C.ck0, P.sc.dt, ck, cc);
+    atomicAdd(P.nonfinite + 2, 1ULL);
     cell_epilogue<true>(P, C, ck, cc);
 }
 
@@ -1091,7 +1114,7 @@ static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool c
     CUDA_TRY(h->nt_var[ip]->launch(P, grid, h->stream));
     if (timed) CUDA_TRY(capturing ? cudaEventRecordWithFlags(h->ev3, h->stream, cudaEventRecordExternal)
                                   : cudaEventRecord(h->ev3, h->stream));
-    *launches += mixed ? 5 : 4;  // setup, start (FP32 + FP64 redo), solve, finish
+    *launches += mixed ? 6 : 5;  // setup, start (FP32 + FP64 redo), solve, finish, fallback
     if (warm) {
         // misses of the warm start: the plain start, a second pass of the solve kernel
         CUDA_TRY(cudaMemsetAsync(h->nt_head, 0, 8 * sizeof(int), h->stream));
@@ -1100,6 +1123,7 @@ static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool c
         *launches += 2;
     }
     k_nt_finish<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    k_nt_fallback<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     return REPROBUS_OK;
 }
 
