@@ -78,7 +78,8 @@ typedef struct reprobus_stats {
     int z_shared;              /* Newton solvers: 1 when the kernel keeps the right-
                                   hand side in shared memory, 0 in registers, 2 in
                                   registers with two warp groups sharing the matrix
-                                  slots                                              */
+                                  slots, 3 with a residual lane per cell, 4 in
+                                  registers with the block's warps in lock-step  */
     int warm_start;            /* Newton solvers: 1 when the learned warm start ran  */
     long long warm_restarts;   /* warm start: cells whose predicted start missed the
                                   convergence test and restarted from the plain start */
@@ -185,7 +186,12 @@ int reprobus_chem_set_solver(void* handle, int solver, int npass, int maxit, dou
  * one; a precision without that value is autotuned), zshared (0: right-hand
  * side in registers, 1: in shared memory, 2: in registers with two warp
  * groups taking turns on one set of matrix slots, so that a block keeps
- * twice the cells in flight) and blocks_per_sm (0: as many as fit).
+ * twice the cells in flight; 3: in shared memory, with a second lane per cell
+ * that evaluates the FP64 residual while the first evaluates the Jacobian;
+ * lanes_per_block then counts cells: 64, 128 mixed, 32, 64 FP64; 4: in
+ * registers, the warps of a block passing each phase of an iteration
+ * together, so that they fetch the same code: 64, 128 mixed, 32, 64 FP64)
+ * and blocks_per_sm (0: as many as fit).
  * When the environment variable REPROBUS_TUNE_CACHE names a file, the
  * autotuner first looks there for a choice made for the same GPU model,
  * matrix precision and cell count (skipping the timing runs), and appends

@@ -17,7 +17,8 @@ LIB = os.path.join(HERE, "libreprobus_gb300.so")
 PROBE = os.path.join(HERE, "pipe_probe")  # throughput probe behind the roofline notes
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["chem_kernels.cu", "nt_solve_f32_zr.cu", "nt_solve_f32_zs.cu", "nt_solve_f64_zr.cu",
-           "nt_solve_f64_zs.cu", "nt_solve_pp.cu", "mlp_kernels.cu", "column_kernels.cu"]
+           "nt_solve_f64_zs.cu", "nt_solve_pp.cu", "nt_solve_sp.cu", "nt_solve_ls.cu", "mlp_kernels.cu",
+           "column_kernels.cu"]
 HEADERS = ["chem_cell.cuh", "chem_enums.h", "chem_params.cuh", "newton_gen.cuh", "newton_solve.cuh",
            "newton_kernel.cuh", "newton_launch.h", "newton_num.cuh", "tc_sm100.cuh", "handle_info.h",
            "tropo_tables.h"]

@@ -127,8 +127,13 @@ struct CellPro {
     int k;
 };
 
-template <bool DIAG>
-__device__ __forceinline__ void cell_prologue(const Params& P, int cell, CellPro& C) {
+// LS: the block's threads pass each phase (loads, zenith, photolysis,
+// aerosol, rates) between the same barriers, so that the warps of an SM
+// fetch the same code at the same time; every thread of the block must call
+// it (store = false: a thread without a cell of its own, which recomputes a
+// valid cell and writes nothing).
+template <bool DIAG, bool LS = false>
+__device__ __forceinline__ void cell_prologue(const Params& P, int cell, CellPro& C, bool store = true) {
     const int i = cell % P.nlon;
     const int rest = cell / P.nlon;
     const int col = cell % P.ncol;
@@ -151,9 +156,11 @@ __device__ __forceinline__ void cell_prologue(const Params& P, int cell, CellPro
     for (int n = 0; n < NBCON; n++) C.ck0[n] = P.qj1[g + pl * n] * F.hnm;
 #pragma unroll
     for (int n = 0; n < NCM; n++) C.cc0[n] = P.hc[g + pl * n] * F.hnm;
+    if (LS) __syncthreads();
     // zenith F:845-851
     F.sza = cell_zenith(P.sc, P.trajlon[P.trajoff + g], P.trajlat[P.trajoff + g]);
-    if (!DIAG) P.sza3d[g] = F.sza;
+    if (!DIAG && store) P.sza3d[g] = F.sza;
+    if (LS) __syncthreads();
     // phot + jno F:857, F:5043-5146
 #pragma unroll
     for (int n = 0; n < NPHOT; n++) C.tj[n] = 0.;
@@ -162,6 +169,7 @@ __device__ __forceinline__ void cell_prologue(const Params& P, int cell, CellPro
     const double sza_top = P.col[3 * (size_t)P.ncell + col];
     if (sza_top <= 89.0)
         C.tj[J_no] = cell_jno(sza_top, F.hnm, P.col[(size_t)P.ncell + cell], P.col[2 * (size_t)P.ncell + cell], C.o3t);
+    if (LS) __syncthreads();
     // heterogeneous init + analytic F:864-912
     Aerosol& A = C.A;
 #pragma unroll
@@ -174,17 +182,18 @@ __device__ __forceinline__ void cell_prologue(const Params& P, int cell, CellPro
     A.surf = 0.;
     if (k >= P.nivhau - 1) {
         cell_aerosol(t, pm, F.hnm, C.ck0, A);
-        if (!DIAG) P.surfarea[g] = A.surf;
+        if (!DIAG && store) P.surfarea[g] = A.surf;
     }
     F.parthno3 = A.parthno3;
     F.parth2o = A.parth2o;
     F.parthcl = A.parthcl;
     F.parthbr = 1.;
-    if (!DIAG) {
+    if (!DIAG && store) {
         P.vsed3d[g] = A.vsed;
         P.parth2osed[g] = A.parth2o;
         P.parthno3sed[g] = A.parthno3sl;
     }
+    if (LS) __syncthreads();
     // rate constants F:920-1306
     cell_rates(P.sc.troe, t, F.hnm, pm, C.K);
     // rainout F:1315-1338
@@ -328,12 +337,15 @@ __device__ __forceinline__ void cell_features(const Params& P, size_t g, double 
     f[63] = 0.f;
 }
 
-template <bool MIXED>
-__global__ void __launch_bounds__(128) k_nt_setup(Params P) {
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= P.ncell) return;
+template <bool MIXED, int NTB = 128, bool LS = false>
+__global__ void __launch_bounds__(NTB) k_nt_setup(Params P) {
+    int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool own = cell < P.ncell;
+    if (!LS && !own) return;
+    if (!own) cell = P.ncell - 1;  // lock-step: recompute a valid cell, write nothing
     CellPro C;
-    cell_prologue<false>(P, cell, C);
+    cell_prologue<false, LS>(P, cell, C, own);
+    if (!own) return;
     const CellFix& F = C.F;
     const double fx[14] = {F.o2, F.n2, F.h2, F.co2, F.hnm, F.parthno3, F.parth2o, F.parthcl, F.parthbr,
                            F.rain_hno3, F.rain_hcl, F.rain_hbr, F.rain_h2o2, P.sc.dt};
@@ -907,17 +919,21 @@ static void fill_params(const Handle* h, Params& P, int ilat0, int ilat1) {
 // every compiled solve-kernel variant of one matrix precision
 static int nt_all_variants(bool mixed, const NtVariant** out, int cap) {
     int n = 0, k = 0;
-    const NtVariant* lists[3];
-    int counts[3] = {0, 0, 0};
-    const int nl = 3;
+    const NtVariant* lists[5];
+    int counts[5] = {0, 0, 0, 0, 0};
+    const int nl = 5;
     if (mixed) {
         lists[0] = nt_variants_f32_zr(&counts[0]);
         lists[1] = nt_variants_f32_zs(&counts[1]);
         lists[2] = nt_variants_f32_pp(&counts[2]);
+        lists[3] = nt_variants_f32_sp(&counts[3]);
+        lists[4] = nt_variants_f32_ls(&counts[4]);
     } else {
         lists[0] = nt_variants_f64_zr(&counts[0]);
         lists[1] = nt_variants_f64_zs(&counts[1]);
         lists[2] = nt_variants_f64_pp(&counts[2]);
+        lists[3] = nt_variants_f64_sp(&counts[3]);
+        lists[4] = nt_variants_f64_ls(&counts[4]);
     }
     for (int l = 0; l < nl; l++)
         for (k = 0; k < counts[l] && n < cap; k++) out[n++] = &lists[l][k];
@@ -937,13 +953,22 @@ static int ensure_newton(Handle* h) {
     return REPROBUS_OK;
 }
 
+// the rate-stage kernel of the Newton pipeline (and of REF5): blocks of 256
+// threads in lock-step (measured at cfg1: 36 -> 28 ms against 128-thread
+// blocks without barriers; 512 threads 30 ms)
+constexpr int SETUP_TB = 256;
+static void launch_setup(Handle* h, const Params& P, bool mixed) {
+    const unsigned nb = (unsigned)((P.ncell + SETUP_TB - 1) / SETUP_TB);
+    if (mixed)
+        k_nt_setup<true, SETUP_TB, true><<<nb, SETUP_TB, 0, h->stream>>>(P);
+    else
+        k_nt_setup<false, SETUP_TB, true><<<nb, SETUP_TB, 0, h->stream>>>(P);
+}
+
 static int enqueue_setup(Handle* h, Params& P, bool mixed) {
     const int tb = 128;
     CUDA_TRY(cudaMemsetAsync(h->nt_head, 0, 8 * sizeof(int), h->stream));
-    if (mixed)
-        k_nt_setup<true><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
-    else
-        k_nt_setup<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    launch_setup(h, P, mixed);
     if (mixed) {
         k_nt_start32<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
         k_nt_start<2><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
@@ -1145,7 +1170,7 @@ static int enqueue_step(Handle* h, Params& P, bool capturing, int* launches) {
             if (rc) return rc;
         }
         P.nt_rec = h->nt_rec;
-        k_nt_setup<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        launch_setup(h, P, false);
         k_ref_passes<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
         *launches += 2;
     } else {
@@ -1265,7 +1290,7 @@ extern "C" int reprobus_chem_set_tuning(void* handle, int lanes_per_block, int b
     Handle* h = (Handle*)handle;
     if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
     if (lanes_per_block < 0 || blocks_per_sm < 0) return set_err(REPROBUS_ERR_ARG, "bad tuning values");
-    if (zshared < 0 || zshared > 2) return set_err(REPROBUS_ERR_ARG, "zshared must be 0, 1 or 2");
+    if (zshared < 0 || zshared > 4) return set_err(REPROBUS_ERR_ARG, "zshared must be 0 .. 4");
     if (lanes_per_block > 0) {
         bool found = false;
         const NtVariant* vs[16];

@@ -181,6 +181,232 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_pp(Params P) {
     }
 }
 
+// Warp-specialised form: NS cells per block, each with a matrix lane (threads
+// 0..NS-1, the cell's NT_NSLOT shared-memory slots) and a residual lane
+// (threads NS..2NS-1). Per iteration, phase A: the matrix lane evaluates the
+// scaled Jacobian of the current iterate in TJ while the residual lane
+// evaluates the FP64 residual of the same iterate into the cell's NT_NX
+// right-hand-side slots (the FP32 and FP64 pipes work side by side, on the
+// same cell record); phase B: the matrix lane factorises, solves, updates
+// the iterate in FP64, tests convergence and refills from the work queue
+// (one atomic per matrix warp), publishing the cell of the next iteration in
+// shared memory. Phases end at block-wide barriers that every thread passes
+// the same number of times; the exit is decided by a barrier-and-reduction
+// over all threads.
+template <typename T, int STRIDE>
+struct SZ {
+    T* p;
+    __device__ __forceinline__ T& operator[](int i) const { return p[i * STRIDE]; }
+};
+
+template <typename TJ, int NS>
+constexpr size_t nt_sp_smem_bytes() {
+    return (size_t)(NT_NSLOT + NT_NX) * NS * sizeof(TJ) + (size_t)NS * sizeof(int);
+}
+
+template <typename TJ, int NS>
+__global__ void __launch_bounds__(2 * NS, 1) k_nt_solve_sp(Params P) {
+    static_assert(NS % 32 == 0, "whole warps per group");
+    extern __shared__ __align__(16) unsigned char nt_smem[];
+    TJ* slots = reinterpret_cast<TJ*>(nt_smem);
+    int* cellbuf = reinterpret_cast<int*>(nt_smem + (size_t)(NT_NSLOT + NT_NX) * NS * sizeof(TJ));
+    const bool matrix_lane = (int)threadIdx.x < NS;
+    const int t = (int)threadIdx.x % NS;
+    const SJ<TJ, NS> J{slots + t};
+    const SZ<TJ, NS> z{slots + (size_t)NT_NSLOT * NS + t};
+    const unsigned lane = threadIdx.x & 31u;
+    const int nday = P.nt_head[1], nnight = P.nt_head[2];
+    const int nq = nday + nnight;
+    int cell = -1;  // matrix lanes: >= 0 cell in work; -1 wants a cell; -2 queue exhausted
+    int it = 0;
+    // the matrix warps refill their lanes and publish the cells
+    auto refill = [&]() {
+        const unsigned want = __ballot_sync(0xffffffffu, cell == -1);
+        if (want) {
+            const int leader = __ffs(want) - 1;
+            int base = 0;
+            if ((int)lane == leader) base = atomicAdd(P.nt_head, __popc(want));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (cell == -1) {
+                const int q = base + __popc(want & ((1u << lane) - 1u));
+                cell = q < nq ? nt_queue_cell(P, q, nday) : -2;
+                it = 0;
+            }
+        }
+        cellbuf[t] = cell;
+    };
+    if (matrix_lane) refill();
+    for (;;) {
+        __syncthreads();  // the published cells
+        const int c = cellbuf[t];
+        if (__syncthreads_and(c == -2)) break;
+        // phase A
+        if (c >= 0) {
+            const double* rec = P.nt_rec + (size_t)c * NT_REC;
+            const bool day = rec[NT_RSZA] <= 95.;
+            const double* x = P.nt_x + (size_t)c * NT_NX;
+            if (matrix_lane) {
+                const TJ* recT;
+                if constexpr (sizeof(TJ) == 4)
+                    recT = P.nt_rec32 + (size_t)c * NT_REC32;
+                else
+                    recT = rec;
+                NtFixT<TJ> FT;
+                nt_load_fix<TJ>(recT + NT_RF, FT);
+                nt_jacobian_call<TJ>(day, FT, recT + NT_RK, recT + NT_RJ, recT + NT_RH, x, 1e-20 * rec[NT_RF + 4], J);
+            } else {
+                NtFixT<double> F;
+                nt_load_fix<double>(rec + NT_RF, F);
+                nt_rhs<TJ>(day, F, rec + NT_RK, rec + NT_RJ, rec + NT_RH, rec + NT_RCK0, x, 1e-20 * F.hnm, z);
+            }
+        }
+        __syncthreads();  // the Jacobian and the right-hand side of every cell
+        // phase B
+        if (matrix_lane) {
+            if (c >= 0) {
+                const double* rec = P.nt_rec + (size_t)c * NT_REC;
+                double* x = P.nt_x + (size_t)c * NT_NX;
+                NT_FENCE();
+                nt_factor_solve<TJ>(J, z, TJ(NT_TINY));
+                TJ step;
+                const bool ok = nt_update<TJ>(x, 1e-20 * rec[NT_RF + 4], z, &step, true);
+                it++;
+                int done = 0;
+                if (!ok)
+                    done = -1;
+                else if (step < (TJ)P.tol)
+                    done = it;
+                else if (it >= P.maxit)
+                    done = -1;
+                if (done) {
+                    if (done < 0) atomicAdd(P.nonfinite + 5, (unsigned long long)it);
+                    P.nt_stat[c] = done;
+                    cell = -1;
+                }
+            }
+            refill();
+        }
+    }
+}
+
+template <typename TJ, int NS>
+cudaError_t nt_sp_prepare(int* blocks_per_sm) {
+    cudaError_t e = cudaFuncSetAttribute(k_nt_solve_sp<TJ, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)nt_sp_smem_bytes<TJ, NS>());
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_nt_solve_sp<TJ, NS>, 2 * NS,
+                                                         nt_sp_smem_bytes<TJ, NS>());
+}
+
+template <typename TJ, int NS>
+cudaError_t nt_sp_launch(const Params& P, int grid, cudaStream_t stream) {
+    k_nt_solve_sp<TJ, NS><<<grid, 2 * NS, nt_sp_smem_bytes<TJ, NS>(), stream>>>(P);
+    return cudaGetLastError();
+}
+
+// form 3: matrix lanes and residual lanes (nth = NS cells per block)
+template <typename TJ, int NS>
+constexpr NtVariant nt_sp_variant() {
+    return NtVariant{(int)sizeof(TJ), NS, 3, nt_sp_smem_bytes<TJ, NS>(), &nt_sp_prepare<TJ, NS>, &nt_sp_launch<TJ, NS>};
+}
+
+// Lock-step form of the one-group kernel: every warp of the block runs each
+// phase of an iteration (Jacobian, residual, factorisation and solve, update
+// and refill) between the same two block barriers, so that the warps of an
+// SM fetch the same generated code at the same time (the solve code is far
+// larger than the instruction cache). Lanes without a cell pass the barriers
+// idle; the exit is a barrier-and-reduction over all threads.
+template <typename TJ, int NTH>
+__global__ void __launch_bounds__(NTH, 1) k_nt_solve_ls(Params P) {
+    static_assert(NTH % 32 == 0, "whole warps");
+    extern __shared__ __align__(16) unsigned char nt_smem[];
+    const SJ<TJ, NTH> J{reinterpret_cast<TJ*>(nt_smem) + threadIdx.x};
+    const unsigned lane = threadIdx.x & 31u;
+    const int nday = P.nt_head[1], nnight = P.nt_head[2];
+    const int nq = nday + nnight;
+    int cell = -1, it = 0;
+    for (;;) {
+        const unsigned want = __ballot_sync(0xffffffffu, cell == -1);
+        if (want) {
+            const int leader = __ffs(want) - 1;
+            int base = 0;
+            if ((int)lane == leader) base = atomicAdd(P.nt_head, __popc(want));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (cell == -1) {
+                const int q = base + __popc(want & ((1u << lane) - 1u));
+                cell = q < nq ? nt_queue_cell(P, q, nday) : -2;
+                it = 0;
+            }
+        }
+        if (__syncthreads_and(cell == -2)) break;
+        const double* rec = P.nt_rec + (size_t)(cell > 0 ? cell : 0) * NT_REC;
+        const TJ* recT;
+        if constexpr (sizeof(TJ) == 4)
+            recT = P.nt_rec32 + (size_t)(cell > 0 ? cell : 0) * NT_REC32;
+        else
+            recT = rec;
+        double* x = P.nt_x + (size_t)(cell > 0 ? cell : 0) * NT_NX;
+        const bool day = rec[NT_RSZA] <= 95.;
+        const double floor_ = 1e-20 * rec[NT_RF + 4];
+        if (cell >= 0) {
+            NtFixT<TJ> FT;
+            nt_load_fix<TJ>(recT + NT_RF, FT);
+            nt_jacobian_call<TJ>(day, FT, recT + NT_RK, recT + NT_RJ, recT + NT_RH, x, floor_, J);
+        }
+        __syncthreads();
+        TJ z[NT_NX];
+        if (cell >= 0) {
+            NtFixT<double> F;
+            nt_load_fix<double>(rec + NT_RF, F);
+            nt_rhs<TJ>(day, F, rec + NT_RK, rec + NT_RJ, rec + NT_RH, rec + NT_RCK0, x, floor_, (TJ*)z);
+        }
+        __syncthreads();
+        if (cell >= 0) {
+            NT_FENCE();
+            nt_factor_solve<TJ>(J, (TJ*)z, TJ(NT_TINY));
+        }
+        __syncthreads();
+        if (cell >= 0) {
+            TJ step;
+            const bool ok = nt_update<TJ>(x, floor_, (const TJ*)z, &step, true);
+            it++;
+            int done = 0;
+            if (!ok)
+                done = -1;
+            else if (step < (TJ)P.tol)
+                done = it;
+            else if (it >= P.maxit)
+                done = -1;
+            if (done) {
+                if (done < 0) atomicAdd(P.nonfinite + 5, (unsigned long long)it);
+                P.nt_stat[cell] = done;
+                cell = -1;
+            }
+        }
+    }
+}
+
+template <typename TJ, int NTH>
+cudaError_t nt_ls_prepare(int* blocks_per_sm) {
+    const size_t smem = (size_t)NT_NSLOT * NTH * sizeof(TJ);
+    cudaError_t e = cudaFuncSetAttribute(k_nt_solve_ls<TJ, NTH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_nt_solve_ls<TJ, NTH>, NTH, smem);
+}
+
+template <typename TJ, int NTH>
+cudaError_t nt_ls_launch(const Params& P, int grid, cudaStream_t stream) {
+    k_nt_solve_ls<TJ, NTH><<<grid, NTH, (size_t)NT_NSLOT * NTH * sizeof(TJ), stream>>>(P);
+    return cudaGetLastError();
+}
+
+// form 4: one group in lock-step, z in registers
+template <typename TJ, int NTH>
+constexpr NtVariant nt_ls_variant() {
+    return NtVariant{(int)sizeof(TJ), NTH, 4, (size_t)NT_NSLOT * NTH * sizeof(TJ), &nt_ls_prepare<TJ, NTH>,
+                     &nt_ls_launch<TJ, NTH>};
+}
+
 template <typename TJ, int NTH>
 constexpr size_t nt_pp_smem_bytes() {
     return (size_t)NT_NSLOT * (NTH / 2) * sizeof(TJ);

@@ -124,22 +124,28 @@ def test_mixed_solve_kernel_shapes_agree_with_the_oracle(case, fixed_point, lane
     assert _species_err(got, fp, case.nivbas)[ok].max() <= ERR_TOL
 
 
-@pytest.mark.parametrize("solver,lanes", [(SOLVER_NEWTON_MIXED, 256), (SOLVER_NEWTON_MIXED, 128),
-                                          (SOLVER_NEWTON64, 128), (SOLVER_NEWTON64, 64)])
-def test_two_group_solve_kernel_agrees_with_the_oracle(case, fixed_point, solver, lanes):
-    """The solve kernel whose two warp groups take turns on one set of matrix
-    slots (zshared 2), forced, for both matrix precisions: same accuracy bound
-    and fixed-point property as the one-group kernel."""
+@pytest.mark.parametrize("solver,lanes,form", [(SOLVER_NEWTON_MIXED, 256, 2), (SOLVER_NEWTON_MIXED, 128, 2),
+                                               (SOLVER_NEWTON64, 128, 2), (SOLVER_NEWTON64, 64, 2),
+                                               (SOLVER_NEWTON_MIXED, 128, 3), (SOLVER_NEWTON_MIXED, 64, 3),
+                                               (SOLVER_NEWTON64, 64, 3), (SOLVER_NEWTON64, 32, 3),
+                                               (SOLVER_NEWTON_MIXED, 128, 4), (SOLVER_NEWTON_MIXED, 64, 4),
+                                               (SOLVER_NEWTON64, 64, 4)])
+def test_two_group_solve_kernel_agrees_with_the_oracle(case, fixed_point, solver, lanes, form):
+    """The solve kernels with two kinds of warps, forced, for both matrix
+    precisions: two warp groups taking turns on one set of matrix slots
+    (zshared 2), a matrix lane plus a residual lane per cell (zshared 3), and
+    the one-group kernel with its warps in lock-step (zshared 4). Same
+    accuracy bound and fixed-point property as the one-group kernel."""
     from reprobus_gb300.resident import DeviceCase
     fp, stat, _ = fixed_point
     h = ChemStep.for_case(case, niter=5, flags=0)
     h.set_solver(solver, npass=1, maxit=12, tol=1e-10)
-    h.set_tuning(lanes, 0, 2)
+    h.set_tuning(lanes, 0, form)
     dc = DeviceCase(case)
     st = h.step_dev(1, case.nlat, case.daynum, case.dt, *dc.args(), stats=True)
     got = dc.state_host()
     h.close()
-    assert st["lanes_per_block"] == lanes and st["z_shared"] == 2
+    assert st["lanes_per_block"] == lanes and st["z_shared"] == form
     fell_back = oracle.map_residual(case, got["qj1"], got["hc"]) > MAP_TOL
     assert fell_back.sum() <= st["fallbacks"] <= 0.01 * case.ncells
     ok = (stat > 0) & ~fell_back
