@@ -253,12 +253,17 @@ __device__ __forceinline__ void cell_epilogue(const Params& P, const CellPro& C,
 // ----------------------------------------------------------------------------
 // k_chem — one cell per thread. DIAG: rate stage only, diagnostics out.
 // ----------------------------------------------------------------------------
-template <bool DIAG>
-__global__ void __launch_bounds__(128) k_chem(Params P) {
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= P.ncell) return;
+// LS (with NTB threads per block): the rate stage in lock-step, as
+// k_nt_setup (threads past the last cell recompute it and write nothing)
+template <bool DIAG, int NTB = 128, bool LS = false>
+__global__ void __launch_bounds__(NTB, 1) k_chem(Params P) {
+    int cell = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool own = cell < P.ncell;
+    if (!LS && !own) return;
+    if (!own) cell = P.ncell - 1;
     CellPro C;
-    cell_prologue<DIAG>(P, cell, C);
+    cell_prologue<DIAG, LS>(P, cell, C, own);
+    if (!own) return;
     const CellFix& F = C.F;
     const Aerosol& A = C.A;
     if (DIAG) {
@@ -710,6 +715,9 @@ struct Handle {
     void* mlp = nullptr;
     float* mlp_feat = nullptr;
     float* mlp_y = nullptr;
+    // host-array entry point: copy streams and events of its row chunks
+    cudaStream_t cin = nullptr, cout = nullptr;
+    cudaEvent_t ev_in[4] = {}, ev_comp[4] = {};
     // scratch of the column-physics entry points (column_kernels.cu)
     void* col_scratch = nullptr;
     size_t col_scratch_bytes = 0;
@@ -763,6 +771,12 @@ static void free_handle(Handle* h) {
     cudaFree(h->mlp_feat);
     cudaFree(h->mlp_y);
     cudaFree(h->col_scratch);
+    for (int c = 0; c < 4; c++) {
+        if (h->ev_in[c]) cudaEventDestroy(h->ev_in[c]);
+        if (h->ev_comp[c]) cudaEventDestroy(h->ev_comp[c]);
+    }
+    if (h->cin) cudaStreamDestroy(h->cin);
+    if (h->cout) cudaStreamDestroy(h->cout);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
@@ -1162,7 +1176,7 @@ static int enqueue_step(Handle* h, Params& P, bool capturing, int* launches) {
     k_columns<<<(P.ncol + tb - 1) / tb, tb, 0, h->stream>>>(P);
     (*launches)++;
     if (h->solver == REPROBUS_SOLVER_REF5 && !h->split_ref5) {
-        k_chem<false><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        k_chem<false, SETUP_TB, true><<<(unsigned)((P.ncell + SETUP_TB - 1) / SETUP_TB), SETUP_TB, 0, h->stream>>>(P);
         (*launches)++;
     } else if (h->solver == REPROBUS_SOLVER_REF5) {
         if (!capturing) {
@@ -1422,15 +1436,23 @@ extern "C" int reprobus_chem_step_dev(void* handle, int ilat0, int ilat1, double
     return launch_step(h, P, stats);
 }
 
-// strided copy of rows [r0, r0+nr) of `planes` consecutive (nlon,nlat) planes
+// strided copy of rows [r0, r0+nr) of `planes` consecutive (nlon,nlat) planes;
+// all rows of the planes are one contiguous range: one linear copy (the 2-D
+// copy path moves whole planes markedly slower)
 static int copy_rows(double* dst, const double* src, const Handle* h, int r0, int nr, size_t plane0, size_t planes,
                      cudaMemcpyKind kind, cudaStream_t s) {
     const size_t pitch = (size_t)h->nlon * h->nlat * sizeof(double);
     const size_t off = plane0 * h->nlon * h->nlat + (size_t)h->nlon * r0;
+    if (nr == h->nlat) {
+        CUDA_TRY(cudaMemcpyAsync(dst + off, src + off, pitch * planes, kind, s));
+        return REPROBUS_OK;
+    }
     CUDA_TRY(cudaMemcpy2DAsync(dst + off, pitch, src + off, pitch, (size_t)h->nlon * nr * sizeof(double), planes,
                                kind, s));
     return REPROBUS_OK;
 }
+
+constexpr int HOST_CHUNK_MIN_ROWS = 8;  // rows per chunk of the host-array entry point at least
 
 static int ensure_mirrors(Handle* h) {
     if (h->m_qj1) return REPROBUS_OK;
@@ -1443,6 +1465,74 @@ static int ensure_mirrors(Handle* h) {
     for (int q = 0; q < 4; q++) CUDA_TRY(cudaMalloc(&h->m_out[q], pb * sizeof(double)));
     CUDA_TRY(cudaMalloc(&h->m_out[4], pl * sizeof(double)));
     return REPROBUS_OK;
+}
+
+// the host arrays of rows [r0, r0 + nr) into the handle's device mirrors
+// (alt and the irapp slice of traj* on levels 1..nivbas, the state) or back
+// (state and diagnostics), on stream s
+struct HostArrays {
+    const double* alt;
+    const double* traj[4];
+    double *qj1, *hc, *vsed3d, *parth2osed, *parthno3sed, *surfarea, *sza3d;
+};
+
+static int host_rows_in(Handle* h, const HostArrays& A, int r0, int nr, cudaStream_t s) {
+    const size_t nb = h->nivbas, niv = h->niv;
+    const bool fuse = (h->flags & REPROBUS_FUSE_CONSERV) != 0;
+    const cudaMemcpyKind H2D = cudaMemcpyHostToDevice;
+    int rc;
+    if ((rc = copy_rows(h->m_alt, A.alt, h, r0, nr, 0, nb, H2D, s))) return rc;
+    for (int q = 0; q < 4; q++)
+        if ((rc = copy_rows(h->m_traj[q], A.traj[q], h, r0, nr, 0, nb, H2D, s))) return rc;
+    if (fuse || nb == niv) {
+        if ((rc = copy_rows(h->m_qj1, A.qj1, h, r0, nr, 0, niv * NBCON, H2D, s))) return rc;
+    } else {
+        for (int n = 0; n < NBCON; n++)
+            if ((rc = copy_rows(h->m_qj1, A.qj1, h, r0, nr, niv * n, nb, H2D, s))) return rc;
+    }
+    for (int n = 0; n < NCM; n++)
+        if ((rc = copy_rows(h->m_hc, A.hc, h, r0, nr, niv * n, nb, H2D, s))) return rc;
+    return REPROBUS_OK;
+}
+
+static int host_rows_out(Handle* h, const HostArrays& A, int r0, int nr, cudaStream_t s) {
+    const size_t nb = h->nivbas, niv = h->niv;
+    const bool fuse = (h->flags & REPROBUS_FUSE_CONSERV) != 0;
+    const cudaMemcpyKind D2H = cudaMemcpyDeviceToHost;
+    int rc;
+    if (fuse || nb == niv) {
+        if ((rc = copy_rows(A.qj1, h->m_qj1, h, r0, nr, 0, niv * NBCON, D2H, s))) return rc;
+    } else {
+        for (int n = 0; n < NBCON; n++)
+            if ((rc = copy_rows(A.qj1, h->m_qj1, h, r0, nr, niv * n, nb, D2H, s))) return rc;
+    }
+    for (int n = 0; n < NCM; n++)
+        if ((rc = copy_rows(A.hc, h->m_hc, h, r0, nr, niv * n, nb, D2H, s))) return rc;
+    if ((rc = copy_rows(A.vsed3d, h->m_out[0], h, r0, nr, 0, nb, D2H, s))) return rc;
+    if ((rc = copy_rows(A.parth2osed, h->m_out[1], h, r0, nr, 0, nb, D2H, s))) return rc;
+    if ((rc = copy_rows(A.parthno3sed, h->m_out[2], h, r0, nr, 0, nb, D2H, s))) return rc;
+    if ((rc = copy_rows(A.sza3d, h->m_out[3], h, r0, nr, 0, nb, D2H, s))) return rc;
+    const size_t kh = h->nivhau - 1;
+    if ((rc = copy_rows(A.surfarea, h->m_out[4], h, r0, nr, kh, nb - kh, D2H, s))) return rc;
+    return REPROBUS_OK;
+}
+
+static void add_stats(reprobus_stats* acc, const reprobus_stats& c, bool first) {
+    if (first) {
+        *acc = c;
+        return;
+    }
+    acc->ncells += c.ncells;
+    acc->nonfinite += c.nonfinite;
+    acc->kernel_launches += c.kernel_launches;
+    acc->device_ms += c.device_ms;
+    acc->newton_iters += c.newton_iters;
+    acc->fallbacks += c.fallbacks;
+    if (c.max_newton_iters > acc->max_newton_iters) acc->max_newton_iters = c.max_newton_iters;
+    acc->warm_restarts += c.warm_restarts;
+    acc->failed_iters += c.failed_iters;
+    acc->solve_ms += c.solve_ms;
+    acc->start64_cells += c.start64_cells;
 }
 
 extern "C" int reprobus_chem_step(void* handle, int ilat0, int ilat1, double daynum, double dt, const double* alt,
@@ -1459,59 +1549,72 @@ extern "C" int reprobus_chem_step(void* handle, int ilat0, int ilat1, double day
         !parthno3sed || !surfarea || !sza3d)
         return set_err(REPROBUS_ERR_ARG, "NULL array argument");
     if ((rc = ensure_mirrors(h))) return rc;
-    const int r0 = ilat0 - 1, nr = ilat1 - ilat0 + 1;
     const size_t pl = (size_t)h->nlon * h->nlat * h->niv;
-    const size_t nb = h->nivbas, niv = h->niv;
-    const int fuse = (h->flags & REPROBUS_FUSE_CONSERV) ? 1 : 0;
-    cudaStream_t s = h->stream;
-    const cudaMemcpyKind H2D = cudaMemcpyHostToDevice, D2H = cudaMemcpyDeviceToHost;
-    // inputs: alt and the irapp slice of traj* (levels 1..nivbas), state
-    if ((rc = copy_rows(h->m_alt, alt, h, r0, nr, 0, nb, H2D, s))) return rc;
-    const double* tr[4] = {trajlon + (irapp - 1) * pl, trajlat + (irapp - 1) * pl, trajpre + (irapp - 1) * pl,
-                           trajtem + (irapp - 1) * pl};
-    for (int q = 0; q < 4; q++)
-        if ((rc = copy_rows(h->m_traj[q], tr[q], h, r0, nr, 0, nb, H2D, s))) return rc;
-    if (fuse || nb == niv) {
-        if ((rc = copy_rows(h->m_qj1, qj1, h, r0, nr, 0, niv * NBCON, H2D, s))) return rc;
-    } else {
-        for (int n = 0; n < NBCON; n++)
-            if ((rc = copy_rows(h->m_qj1, qj1, h, r0, nr, niv * n, nb, H2D, s))) return rc;
+    const HostArrays A{alt,
+                       {trajlon + (irapp - 1) * pl, trajlat + (irapp - 1) * pl, trajpre + (irapp - 1) * pl,
+                        trajtem + (irapp - 1) * pl},
+                       qj1, hc, vsed3d, parth2osed, parthno3sed, surfarea, sza3d};
+    // Rows in chunks: the copy of chunk c+1 in (stream cin) and of chunk c-1
+    // out (stream cout) run while chunk c integrates on the handle's stream;
+    // chunks touch disjoint rows of the device mirrors, and the order is
+    // carried by events (no kernel waits on another). Statistics, CHECK_FINITE
+    // and the first Newton step (autotuning) synchronise per chunk.
+    const int nrows = ilat1 - ilat0 + 1;
+    const int nchunk = nrows >= 4 * HOST_CHUNK_MIN_ROWS ? 4 : 1;
+    if (nchunk > 1 && !h->cin) {
+        CUDA_TRY(cudaStreamCreateWithFlags(&h->cin, cudaStreamNonBlocking));
+        CUDA_TRY(cudaStreamCreateWithFlags(&h->cout, cudaStreamNonBlocking));
+        for (int c = 0; c < 4; c++) {
+            CUDA_TRY(cudaEventCreateWithFlags(&h->ev_in[c], cudaEventDisableTiming));
+            CUDA_TRY(cudaEventCreateWithFlags(&h->ev_comp[c], cudaEventDisableTiming));
+        }
     }
-    for (int n = 0; n < NCM; n++)
-        if ((rc = copy_rows(h->m_hc, hc, h, r0, nr, niv * n, nb, H2D, s))) return rc;
-    Params P;
-    fill_params(h, P, ilat0, ilat1);
-    P.trajoff = 0;
-    P.alt = h->m_alt;
-    P.trajlon = h->m_traj[0];
-    P.trajlat = h->m_traj[1];
-    P.trajpre = h->m_traj[2];
-    P.trajtem = h->m_traj[3];
-    P.qj1 = h->m_qj1;
-    P.hc = h->m_hc;
-    P.vsed3d = h->m_out[0];
-    P.parth2osed = h->m_out[1];
-    P.parthno3sed = h->m_out[2];
-    P.sza3d = h->m_out[3];
-    P.surfarea = h->m_out[4];
-    step_const(h, daynum, dt, P.sc);
-    if ((rc = launch_step(h, P, stats))) return rc;
-    // outputs
-    if (fuse || nb == niv) {
-        if ((rc = copy_rows(qj1, h->m_qj1, h, r0, nr, 0, niv * NBCON, D2H, s))) return rc;
-    } else {
-        for (int n = 0; n < NBCON; n++)
-            if ((rc = copy_rows(qj1, h->m_qj1, h, r0, nr, niv * n, nb, D2H, s))) return rc;
+    cudaStream_t cin = nchunk > 1 ? h->cin : h->stream, cout = nchunk > 1 ? h->cout : h->stream;
+    if (nchunk > 1) {  // the copies in must not overtake work still queued on the handle's stream
+        CUDA_TRY(cudaEventRecord(h->ev_comp[3], h->stream));
+        CUDA_TRY(cudaStreamWaitEvent(cin, h->ev_comp[3], 0));
     }
-    for (int n = 0; n < NCM; n++)
-        if ((rc = copy_rows(hc, h->m_hc, h, r0, nr, niv * n, nb, D2H, s))) return rc;
-    if ((rc = copy_rows(vsed3d, h->m_out[0], h, r0, nr, 0, nb, D2H, s))) return rc;
-    if ((rc = copy_rows(parth2osed, h->m_out[1], h, r0, nr, 0, nb, D2H, s))) return rc;
-    if ((rc = copy_rows(parthno3sed, h->m_out[2], h, r0, nr, 0, nb, D2H, s))) return rc;
-    if ((rc = copy_rows(sza3d, h->m_out[3], h, r0, nr, 0, nb, D2H, s))) return rc;
-    const size_t kh = h->nivhau - 1;
-    if ((rc = copy_rows(surfarea, h->m_out[4], h, r0, nr, kh, nb - kh, D2H, s))) return rc;
-    CUDA_TRY(cudaStreamSynchronize(s));
+    reprobus_stats acc, one;
+    // on an error, let the copies already queued finish before returning
+    auto fail = [&](int code) {
+        cudaStreamSynchronize(cin);
+        cudaStreamSynchronize(cout);
+        return code;
+    };
+    for (int c = 0; c < nchunk; c++) {
+        const int a = ilat0 + (int)((long long)nrows * c / nchunk);
+        const int b = ilat0 + (int)((long long)nrows * (c + 1) / nchunk) - 1;
+        if ((rc = host_rows_in(h, A, a - 1, b - a + 1, cin))) return fail(rc);
+        if (nchunk > 1) {
+            CUDA_TRY(cudaEventRecord(h->ev_in[c], cin));
+            CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_in[c], 0));
+        }
+        Params P;
+        fill_params(h, P, a, b);
+        P.trajoff = 0;
+        P.alt = h->m_alt;
+        P.trajlon = h->m_traj[0];
+        P.trajlat = h->m_traj[1];
+        P.trajpre = h->m_traj[2];
+        P.trajtem = h->m_traj[3];
+        P.qj1 = h->m_qj1;
+        P.hc = h->m_hc;
+        P.vsed3d = h->m_out[0];
+        P.parth2osed = h->m_out[1];
+        P.parthno3sed = h->m_out[2];
+        P.sza3d = h->m_out[3];
+        P.surfarea = h->m_out[4];
+        step_const(h, daynum, dt, P.sc);
+        if ((rc = launch_step(h, P, stats ? &one : nullptr))) return fail(rc);
+        if (stats) add_stats(&acc, one, c == 0);
+        if (nchunk > 1) {
+            CUDA_TRY(cudaEventRecord(h->ev_comp[c], h->stream));
+            CUDA_TRY(cudaStreamWaitEvent(cout, h->ev_comp[c], 0));
+        }
+        if ((rc = host_rows_out(h, A, a - 1, b - a + 1, cout))) return fail(rc);
+    }
+    CUDA_TRY(cudaStreamSynchronize(cout));
+    if (stats) *stats = acc;
     return REPROBUS_OK;
 }
 

@@ -203,3 +203,32 @@ def test_reference_shaped_interface(torch):
                  st["surfarea"], st["sza3d"])
     R.conserv(st["qj1"], st["hc"])
     _compare(st, ref)
+
+
+@pytest.mark.parametrize("solver", ["ref5", "mixed"])
+def test_host_entry_in_row_chunks_equals_device_entry(torch, solver):
+    """The host-array entry point pipelines calls of 32 rows or more in row
+    chunks (copies of one chunk overlapping the integration of another): the
+    result is bit for bit the device-array entry point's on the same grid."""
+    from reprobus_gb300.chem import SOLVER_NEWTON_MIXED, SOLVER_REF5
+    from reprobus_gb300.resident import DeviceCase
+    case = inputs.make_case("grid", seed=41, nlon=12, nlat=40, nivbas=94)
+    outs = []
+    for host in (True, False):
+        h = ChemStep.for_case(case, niter=5, flags=FUSE_CONSERV)
+        if solver == "mixed":
+            h.set_solver(SOLVER_NEWTON_MIXED)
+            h.set_tuning(64, 1, 0)
+        if host:
+            st = case.state_copy()
+            h.step(1, case.nlat, case.daynum, case.dt, case.alt, case.trajlon, case.trajlat, case.trajpre,
+                   case.trajtem, case.irapp, st["qj1"], st["hc"], st["vsed3d"], st["parth2osed"],
+                   st["parthno3sed"], st["surfarea"], st["sza3d"])
+        else:
+            dc = DeviceCase(case)
+            h.step_dev(1, case.nlat, case.daynum, case.dt, *dc.args(), stats=True)
+            st = dc.state_host()
+        h.close()
+        outs.append(st)
+    for f in FIELDS:
+        assert np.array_equal(outs[0][f], outs[1][f]), f
