@@ -385,12 +385,11 @@ __global__ void __launch_bounds__(NTB) k_nt_setup(Params P) {
 // from the start state (ck0 from the record, cc from hc) -> x; the cell
 // enters the work queue (day cells from the front, night cells from the
 // back); with the warm start, the network's features of that plain start.
-// MODE 0: every cell; MODE 1 (restart): only cells whose warm start missed
-// (stat < 0); MODE 2: only cells whose FP32 start (k_nt_start32) was not
-// finite (stat < 0), features included.
+// MODE 0: every cell; MODE 2: only cells whose FP32 start (k_nt_start32)
+// was not finite (stat < 0).
 template <int MODE>
 __global__ void __launch_bounds__(128) k_nt_start(Params P) {
-    constexpr bool RESTART = MODE == 1;
+    static_assert(MODE == 0 || MODE == 2, "start modes");
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= P.ncell) return;
     if (MODE != 0 && P.nt_stat[cell] >= 0) return;
@@ -420,7 +419,7 @@ __global__ void __launch_bounds__(128) k_nt_start(Params P) {
     for (int n = 0; n < NBCON - 1; n++) x[n] = ck[n];
 #pragma unroll
     for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = cc[n];
-    if (!RESTART && P.warm) {
+    if (P.warm) {
         float fe[64];
         cell_features(P, g, F.hnm, F.sza, r[NT_RSURF], ck, cc, fe);
         float4* o = reinterpret_cast<float4*>(P.mlp_feat + (size_t)cell * 64);
@@ -432,7 +431,6 @@ __global__ void __launch_bounds__(128) k_nt_start(Params P) {
         P.nt_list[atomicAdd(P.nt_head + 1, 1)] = cell;
     else
         P.nt_list[P.ncell - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
-    if (RESTART) atomicAdd(P.nonfinite + 4, 1ULL);
     if (MODE == 2) atomicAdd(P.nonfinite + 6, 1ULL);
 }
 
@@ -505,7 +503,8 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
         P.nt_list[P.ncell - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
 }
 
-// warm start: x_i = max(x_i, 1e-30 hnm) 10^y_i from the network's prediction.
+// warm start: x_i = max(x_i, 1e-30 hnm) 10^y_i from the network's prediction;
+// the plain start is kept in nt_xp for a cell whose warm start misses.
 // A block takes 128 cells and walks their iterates element by element, so
 // that consecutive threads touch consecutive words of x (cell-major, NT_NX
 // per cell) and of the predictions (64 per cell).
@@ -518,7 +517,9 @@ __global__ void __launch_bounds__(128) k_nt_warm(Params P) {
         const size_t cell = (size_t)c0 + cl;
         const double hnm = P.nt_rec[cell * NT_REC + NT_RF + 4];
         const float yi = fminf(fmaxf(P.mlp_y[cell * 64 + i], -30.f), 30.f);
-        x[e] = fmax(x[e], 1e-30 * hnm) * nt_widen(exp10f(yi));
+        const double xe = x[e];
+        P.nt_xp[(size_t)c0 * NT_NX + e] = xe;  // the plain start, for a retry
+        x[e] = fmax(xe, 1e-30 * hnm) * nt_widen(exp10f(yi));
     }
 }
 
@@ -715,6 +716,7 @@ struct Handle {
     void* mlp = nullptr;
     float* mlp_feat = nullptr;
     float* mlp_y = nullptr;
+    double* nt_xp = nullptr;  // the plain start saved by k_nt_warm
     // host-array entry point: copy streams and events of its row chunks
     cudaStream_t cin = nullptr, cout = nullptr;
     cudaEvent_t ev_in[4] = {}, ev_comp[4] = {};
@@ -770,6 +772,7 @@ static void free_handle(Handle* h) {
     cudaFree(h->nt_head);
     cudaFree(h->mlp_feat);
     cudaFree(h->mlp_y);
+    cudaFree(h->nt_xp);
     cudaFree(h->col_scratch);
     for (int c = 0; c < 4; c++) {
         if (h->ev_in[c]) cudaEventDestroy(h->ev_in[c]);
@@ -1133,10 +1136,12 @@ static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool c
             const size_t nc = (size_t)h->nlon * h->nlat * h->nivbas;
             CUDA_TRY(cudaMalloc(&h->mlp_feat, nc * MLP_FEAT * sizeof(float)));
             CUDA_TRY(cudaMalloc(&h->mlp_y, nc * MLP_YOUT * sizeof(float)));
+            CUDA_TRY(cudaMalloc(&h->nt_xp, nc * NT_NX * sizeof(double)));
         }
         P.warm = 1;
         P.mlp_feat = h->mlp_feat;
         P.mlp_y = h->mlp_y;
+        P.nt_xp = h->nt_xp;
     }
     if ((rc = choose_shape(h, P, mixed))) return rc;
     const int ip = mixed ? 0 : 1;
@@ -1154,13 +1159,8 @@ static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool c
     if (timed) CUDA_TRY(capturing ? cudaEventRecordWithFlags(h->ev3, h->stream, cudaEventRecordExternal)
                                   : cudaEventRecord(h->ev3, h->stream));
     *launches += mixed ? 6 : 5;  // setup, start (FP32 + FP64 redo), solve, finish, fallback
-    if (warm) {
-        // misses of the warm start: the plain start, a second pass of the solve kernel
-        CUDA_TRY(cudaMemsetAsync(h->nt_head, 0, 8 * sizeof(int), h->stream));
-        k_nt_start<1><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
-        CUDA_TRY(h->nt_var[ip]->launch(P, grid, h->stream));
-        *launches += 2;
-    }
+    // (a warm start that misses the convergence test is retried from the saved
+    // plain start by the solve kernel itself, nt_retry_warm)
     k_nt_finish<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     k_nt_fallback<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     return REPROBUS_OK;

@@ -48,6 +48,7 @@ struct Params {
     int warm;                       // 1: features for the warm-start network, start from its prediction
     float* mlp_feat;                // 64 raw features per cell (row-major)
     const float* mlp_y;             // 64 predicted log10 end-of-step ratios per cell (57 used)
+    double* nt_xp;                  // warm start: the plain start of every cell (NT_NX doubles)
     StepConst sc;
 };
 

@@ -33,6 +33,27 @@ __device__ __forceinline__ int nt_queue_cell(const Params& P, int q, int nday) {
     return q < nday ? P.nt_list[q] : P.nt_list[P.ncell - 1 - (q - nday)];
 }
 
+// The end of an attempt of a lane's cell (done: iterations when converged, -1
+// when not). With the warm start, a first attempt that failed starts again
+// from the plain start that k_nt_warm saved: the lane keeps the cell and
+// returns true. Otherwise the cell's status is written and the lane wants a
+// new cell (false).
+__device__ __forceinline__ bool nt_end_attempt(const Params& P, int cell, int done, int& it, int& attempt) {
+    if (done < 0) atomicAdd(P.nonfinite + 5, (unsigned long long)it);  // iterations spent in vain
+    if (done < 0 && P.warm && attempt == 0) {
+        const double* xp = P.nt_xp + (size_t)cell * NT_NX;
+        double* x = P.nt_x + (size_t)cell * NT_NX;
+#pragma unroll 4
+        for (int i = 0; i < NT_NX; i++) x[i] = xp[i];
+        atomicAdd(P.nonfinite + 4, 1ULL);  // warm restarts
+        attempt = 1;
+        it = 0;
+        return true;
+    }
+    P.nt_stat[cell] = done;
+    return false;
+}
+
 template <typename TJ, int NTH, bool ZS>
 __global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
     static_assert(NTH % 32 == 0, "whole warps");
@@ -42,7 +63,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
     const int nday = P.nt_head[1], nnight = P.nt_head[2];  // queue: day cells, then night cells
     const int nq = nday + nnight;
     int cell = -1;  // >= 0: cell in work; -1: wants a cell; -2: queue exhausted
-    int it = 0;
+    int it = 0, attempt = 0;  // attempt 1: the retry of a missed warm start
     for (;;) {
         const unsigned want = __ballot_sync(0xffffffffu, cell == -1);
         if (want) {
@@ -54,6 +75,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
                 const int q = base + __popc(want & ((1u << lane) - 1u));
                 cell = q < nq ? nt_queue_cell(P, q, nday) : -2;
                 it = 0;
+                attempt = 0;
             }
         }
         if (__all_sync(0xffffffffu, cell == -2)) break;
@@ -81,11 +103,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
                 done = it;
             else if (it >= P.maxit)
                 done = -1;
-            if (done) {
-                if (done < 0) atomicAdd(P.nonfinite + 5, (unsigned long long)it);  // iterations spent in vain
-                P.nt_stat[cell] = done;
-                cell = -1;
-            }
+            if (done && !nt_end_attempt(P, cell, done, it, attempt)) cell = -1;
         }
     }
 }
@@ -113,7 +131,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_pp(Params P) {
     const int nday = P.nt_head[1], nnight = P.nt_head[2];
     const int nq = nday + nnight;
     int cell = -1;  // >= 0: cell in work; -1: wants a cell; -2: queue exhausted
-    int it = 0;
+    int it = 0, attempt = 0;  // attempt 1: the retry of a missed warm start
     bool has_z = false;  // z holds the (solved) step of the cell's current iterate
     TJ z[NT_NX];
     for (int t = 0;; t++) {
@@ -135,11 +153,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_pp(Params P) {
                     done = it;
                 else if (it >= P.maxit)
                     done = -1;
-                if (done) {
-                    if (done < 0) atomicAdd(P.nonfinite + 5, (unsigned long long)it);
-                    P.nt_stat[cell] = done;
-                    cell = -1;
-                }
+                if (done && !nt_end_attempt(P, cell, done, it, attempt)) cell = -1;
             }
             const unsigned want = __ballot_sync(0xffffffffu, cell == -1);
             if (want) {
@@ -151,6 +165,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_pp(Params P) {
                     const int q = base + __popc(want & ((1u << lane) - 1u));
                     cell = q < nq ? nt_queue_cell(P, q, nday) : -2;
                     it = 0;
+                    attempt = 0;
                 }
             }
             if (cell >= 0) {
@@ -218,7 +233,7 @@ __global__ void __launch_bounds__(2 * NS, 1) k_nt_solve_sp(Params P) {
     const int nday = P.nt_head[1], nnight = P.nt_head[2];
     const int nq = nday + nnight;
     int cell = -1;  // matrix lanes: >= 0 cell in work; -1 wants a cell; -2 queue exhausted
-    int it = 0;
+    int it = 0, attempt = 0;  // attempt 1: the retry of a missed warm start
     // the matrix warps refill their lanes and publish the cells
     auto refill = [&]() {
         const unsigned want = __ballot_sync(0xffffffffu, cell == -1);
@@ -231,6 +246,7 @@ __global__ void __launch_bounds__(2 * NS, 1) k_nt_solve_sp(Params P) {
                 const int q = base + __popc(want & ((1u << lane) - 1u));
                 cell = q < nq ? nt_queue_cell(P, q, nday) : -2;
                 it = 0;
+                attempt = 0;
             }
         }
         cellbuf[t] = cell;
@@ -278,11 +294,7 @@ __global__ void __launch_bounds__(2 * NS, 1) k_nt_solve_sp(Params P) {
                     done = it;
                 else if (it >= P.maxit)
                     done = -1;
-                if (done) {
-                    if (done < 0) atomicAdd(P.nonfinite + 5, (unsigned long long)it);
-                    P.nt_stat[c] = done;
-                    cell = -1;
-                }
+                if (done && !nt_end_attempt(P, c, done, it, attempt)) cell = -1;
             }
             refill();
         }
@@ -324,7 +336,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_ls(Params P) {
     const unsigned lane = threadIdx.x & 31u;
     const int nday = P.nt_head[1], nnight = P.nt_head[2];
     const int nq = nday + nnight;
-    int cell = -1, it = 0;
+    int cell = -1, it = 0, attempt = 0;
     for (;;) {
         const unsigned want = __ballot_sync(0xffffffffu, cell == -1);
         if (want) {
@@ -336,6 +348,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_ls(Params P) {
                 const int q = base + __popc(want & ((1u << lane) - 1u));
                 cell = q < nq ? nt_queue_cell(P, q, nday) : -2;
                 it = 0;
+                attempt = 0;
             }
         }
         if (__syncthreads_and(cell == -2)) break;
@@ -377,11 +390,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_ls(Params P) {
                 done = it;
             else if (it >= P.maxit)
                 done = -1;
-            if (done) {
-                if (done < 0) atomicAdd(P.nonfinite + 5, (unsigned long long)it);
-                P.nt_stat[cell] = done;
-                cell = -1;
-            }
+            if (done && !nt_end_attempt(P, cell, done, it, attempt)) cell = -1;
         }
     }
 }
