@@ -302,10 +302,11 @@ def main():
     from reprobus_gb300.chem import FUSE_CONSERV
     from reprobus_gb300.resident import DeviceCase
 
+    from reprobus_gb300.replicas import max_over_ranks, replica_seed, whole_job_rate
     if args.config == "grid":
-        case = inputs.make_case("grid", seed=1234 + rank, nlon=args.nlon, nlat=args.nlat)
+        case = inputs.make_case("grid", seed=replica_seed(1234, rank), nlon=args.nlon, nlat=args.nlat)
     else:
-        case = inputs.make_case(args.config, seed=1234 + rank)
+        case = inputs.make_case(args.config, seed=replica_seed(1234, rank))
     from reprobus_gb300.chem import SOLVER_NEWTON64, SOLVER_NEWTON_MIXED, SOLVER_REF5
     solver_ids = {"ref5": SOLVER_REF5, "newton64": SOLVER_NEWTON64, "mixed": SOLVER_NEWTON_MIXED,
                   "mlp": SOLVER_NEWTON_MIXED}
@@ -362,15 +363,10 @@ def main():
             step()
             e1.record(stream)
         torch.cuda.synchronize()
-        ms = sum(e0.elapsed_time(e1) for e0, e1 in evs)
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            torch.distributed.barrier()
-            ms = float(t.item())
+        ms = max_over_ranks(sum(e0.elapsed_time(e1) for e0, e1 in evs))
         conv = case.ncells - st["fallbacks"]
         day_frac = float((dc["sza3d"][:case.ncells] <= 95.0).double().mean())
-        results[name] = {"cells_per_s": case.ncells * world * args.steps / (ms * 1e-3),
+        results[name] = {"cells_per_s": whole_job_rate(case.ncells, world, args.steps, ms * 1e-3),
                          "ms_per_step": ms / args.steps, "kernel_ms": st["device_ms"],
                          "solve_ms": st["solve_ms"] if name != "ref5" else None,
                          "launches_per_step": st["kernel_launches"], "fallbacks": st["fallbacks"],
@@ -421,12 +417,12 @@ def main():
             hstep()
             torch.cuda.synchronize()
             te += time.perf_counter() - t0
-        te /= n_e2e
+        te = max_over_ranks(te / n_e2e)
         pl = case.nlon * case.nlat * case.niv * 8
         pb = case.nlon * case.nlat * case.nivbas * 8
         h2d = pb * 5 + pl * 43 + pb * 15
         d2h = pl * 43 + pb * 15 + pb * 4 + (case.nivbas - case.nivhau + 1) * case.nlon * case.nlat * 8
-        e2e = {"value": ncell * world / te, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
+        e2e = {"value": whole_job_rate(ncell, world, 1, te), "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": te * 1e3}
 
     line = None
