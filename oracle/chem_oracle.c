@@ -1455,14 +1455,13 @@ static int lu_solve(double* A, double* b, int n) {
     return 0;
 }
 
-static int g_fnorm_arg = -1;
 static const double g_floor = 1e-40;
 static double fnorm(const double* x, const double* gx, const double* floorv) {
     double m = 0.;
     for (int i = 0; i < NX; i++) {
         double s = fmax(fabs(x[i]), floorv[i]);
         double r = fabs(gx[i] - x[i]) / s;
-        if (!(r <= m)) m = r, g_fnorm_arg = i; /* NaN propagates as failure */
+        if (!(r <= m)) m = r; /* NaN propagates as failure */
     }
     return m;
 }
@@ -1550,10 +1549,6 @@ static void orc_newton_block(const orc_grid* g, double dt, work* w, int* iters, 
         res[c] = fnorm(X + c * NX, GX + c * NX, FL + c * NX);
         if (done[c] != 1 && !(res[c] < g->tol)) {
             iters[c] = -abs(iters[c]) - 1;
-            if (getenv("ORC_DEBUG")) {
-                int a = g_fnorm_arg;
-                fprintf(stderr, "cell %zu comp %d x %.3e gx %.3e hnm %.3e\n", c, a, X[c * NX + a], GX[c * NX + a], w->hnm[c]);
-            }
         }
         put_x(w, c, X + c * NX); /* the iterate itself, not one more pass */
     }

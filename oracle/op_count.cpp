@@ -29,6 +29,10 @@ struct CD {
     friend CD operator*(CD a, CD b) { opc::cnt[opc::MUL]++; return CD(a.v * b.v); }
     friend CD operator/(CD a, CD b) { opc::cnt[opc::DIV]++; return CD(a.v / b.v); }
     friend CD operator-(CD a) { return CD(-a.v); }
+    CD& operator+=(CD b) { return *this = *this + b; }
+    CD& operator-=(CD b) { return *this = *this - b; }
+    CD& operator*=(CD b) { return *this = *this * b; }
+    CD& operator/=(CD b) { return *this = *this / b; }
     friend bool operator<(CD a, CD b) { opc::cnt[opc::CMP]++; return a.v < b.v; }
     friend bool operator<=(CD a, CD b) { opc::cnt[opc::CMP]++; return a.v <= b.v; }
     friend bool operator>(CD a, CD b) { opc::cnt[opc::CMP]++; return a.v > b.v; }

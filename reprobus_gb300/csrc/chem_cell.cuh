@@ -24,6 +24,7 @@ constexpr int NSZA = 27;
 constexpr int NOZO = 7;
 constexpr int NRATE = 99;
 constexpr double PI = 3.141592653589793;  // 2.*asin(1.0), F:2750
+constexpr double LN10 = 2.302585092994046;  // 10^y evaluated as exp(y ln 10)
 
 // per-step constants shared by all cells
 struct StepConst {
@@ -211,10 +212,11 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
     A.parth2o = 1.;
     A.parthcl = 1.;
     // F:2778-2787
-    double qh2o = ck[2] / hnm;
+    const double rhnm = 1. / hnm;
+    double qh2o = ck[2] * rhnm;
     double pw = qh2o * ptot / 1013.0;
     pw = fmin(pw, 2.e-3 / 1013.);
-    double qhno3 = ck[4] / hnm;
+    double qhno3 = ck[4] * rhnm;
     double pn0 = qhno3 * ptot / 1013.0;
     // NAT F:2795-2857
     {
@@ -222,20 +224,20 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double pn0t = pn0 * 1013. * 0.75;
         double zmt = -2.7836 - 0.00088 * t;
         double zbt = 38.9855 - 11397.0 / t + 0.009179 * t;
-        double zhno3eq = pow(10.0, zmt * log10(pw * 1013. * 0.75) + zbt);
+        double zhno3eq = exp(zmt * log(pw * 1013. * 0.75) + zbt * LN10);
         if (pn0t / zhno3eq >= 1.) {
             lnat = 1;
             double pn = zhno3eq / (0.75 * 1013.);
             double hno3s = (pn0 - pn) * 1013. * hnm / ptot;
             hno3s = fmax(hno3s, 0.);
             vnat = hno3s * amu * 117. / 1.35;
-            double vnat_small_max = nnat_small_max * (4. / 3. * PI * pow(rnats, 3.));
+            double vnat_small_max = nnat_small_max * (4. / 3. * PI * (rnats * rnats * rnats));
             if (vnat > vnat_small_max) {
                 nnats = nnat_small_max;
-                nnatl = (vnat - vnat_small_max) / (4. / 3. * PI * pow(rnatl, 3.));
+                nnatl = (vnat - vnat_small_max) / (4. / 3. * PI * (rnatl * rnatl * rnatl));
                 vnatl = vnat - vnat_small_max;
             } else {
-                nnats = vnat / (4. / 3. * PI * pow(rnats, 3.));
+                nnats = vnat / (4. / 3. * PI * (rnats * rnats * rnats));
                 nnatl = 0.;
                 vnatl = 0.;
             }
@@ -257,18 +259,18 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             lice = 1;
             lnat = 0;
             anat = 0.;
-            double zh2oeq = pow(10.0, -2668.7 / t + 10.4310);
+            double zh2oeq = exp((-2668.7 / t + 10.4310) * LN10);
             double ph2o = zh2oeq / 760.0;
             double h2os = fmax(pw - ph2o, 0.) * 1013. * hnm / ptot;
             double vice = h2os * amu * 18. / 0.928;
-            nice = vice / (4. / 3. * PI * pow(rice, 3.));
+            nice = vice / (4. / 3. * PI * (rice * rice * rice));
             aice = nice * 4 * PI * (rice * rice);
             A.parth2o = 1.0 - fmax(pw - ph2o, 0.) / pw;
             A.parth2o = fmax(A.parth2o, 0.);
             A.parth2o = fmin(A.parth2o, 1.);
             double zmt = -2.7836 - 0.00088 * t;
             double zbt = 38.9855 - 11397.0 / t + 0.009179 * t;
-            double zhno3eq = pow(10.0, zmt * log10(pw * A.parth2o * 1013. * 0.75) + zbt);
+            double zhno3eq = exp(zmt * log(pw * A.parth2o * 1013. * 0.75) + zbt * LN10);
             double pn = zhno3eq / (0.75 * 1013.);
             parthno3s = 1.0 - (pn0 - pn) / pn0;
             parthno3s = fmax(parthno3s, 0.);
@@ -282,17 +284,18 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
     {
         condliq = 1;
         double t = tl;
-        double qh2ol = ck[2] * A.parth2o / hnm;
+        const double rt = 1. / t;  // E / T as E * (1 / T) in the liquid-aerosol blocks
+        double qh2ol = ck[2] * A.parth2o * rhnm;
         pw = qh2ol * ptot / 1013.0;
         pw = fmin(pw, 2.e-3 / 1013.);
         pw = fmax(pw, 2.e-5 / 1013.);
-        double qh2so4 = fmax(ck[11] / hnm, 1.e-18);
-        ns = ptot * 100.0 * qh2so4 / 8.314 / t;
-        double qhno3l = ck[4] * parthno3s / hnm;
+        double qh2so4 = fmax(ck[11] * rhnm, 1.e-18);
+        ns = ptot * 100.0 * qh2so4 / 8.314 * rt;
+        double qhno3l = ck[4] * parthno3s * rhnm;
         pn0 = ptot / 1013.0 * qhno3l;
-        double a = ks[3] + ks[4] / t;
-        double b = ks[1] + ks[2] / t;
-        double cq = ks[5] + ks[6] / t + ks[7] * log(t) - log(pw);
+        double a = ks[3] + ks[4] * rt;
+        double b = ks[1] + ks[2] * rt;
+        double cq = ks[5] + ks[6] * rt + ks[7] * log(t) - log(pw);
         double det = b * b - 4. * a * cq;
         double msb;
         if (det > 0.) {
@@ -307,8 +310,8 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         wn = 0.0;
         double wts = fmax(41., ws * 100.);
         double wd = wts - 40.;
-        double muh2so4 = 4.184 * (1.514e4 - 286. * wd + 1.08 * (wd * wd) - 3941. / pow(wd, 0.1));
-        double ph2so4 = exp(-10156. / t + 16.2590 - muh2so4 / (8.314 * t));
+        double muh2so4 = 4.184 * (1.514e4 - 286. * wd + 1.08 * (wd * wd) - 3941. / exp(0.1 * log(wd)));
+        double ph2so4 = exp(-10156. * rt + 16.2590 - muh2so4 * (rt / 8.314));
         if (qh2so4 * ptot / 1013. <= ph2so4) {
             ms = 0.;
             ws = 0.;
@@ -317,17 +320,16 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         if (condliq == 1 && t < 215.) {
             double tf = t;
             double tt = r * tf * ns;
-            double tr = 1.0e4 / tf - 43.4782608;
+            double tr = 1.0e4 * rt - 43.4782608;
             double pr = log(pw) + 18.4;
             double tr2 = tr * tr, tr3 = tr2 * tr, pr2 = pr * pr, pr3 = pr2 * pr;
             double hsb = qs[1] + qs[2] * tr2 + (qs[3] + qs[4] * tr + qs[5] * tr2 + qs[6] * tr3) * pr +
                          (qs[7] + qs[8] * tr + qs[9] * tr2) * pr2 + qs[10] * tr * pr3;
             hsb = exp(hsb);
-            double kx = kn[1] + kn[2] / tf;
-            double xnb = 1.0 / (2.0 * (kn[3] + kn[4] / tf)) *
-                         (-kn[1] - kn[2] / tf -
-                          pow(kx * kx - 4.0 * (kn[3] + kn[4] / tf) * (kn[5] + kn[6] / tf + kn[7] * log(tf) - log(pw)),
-                              0.5));
+            double kx = kn[1] + kn[2] * rt;
+            double xnb = 1.0 / (2.0 * (kn[3] + kn[4] * rt)) *
+                         (-kn[1] - kn[2] * rt -
+                          sqrt(kx * kx - 4.0 * (kn[3] + kn[4] * rt) * (kn[5] + kn[6] * rt + kn[7] * log(tf) - log(pw))));
             double mnb = 55.51 * xnb / (1.0 - xnb);
             double hnb = qn[1] + qn[2] * tr2 + (qn[3] + qn[4] * tr + qn[5] * tr2 + qn[6] * tr3) * pr +
                          (qn[7] + qn[8] * tr + qn[9] * tr2) * pr2 + qn[10] * tr * pr3;
@@ -380,32 +382,33 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
     if (condliq == 1) {
         double vliq = ns * 98.076e-6 / ws / dens;
         double ls = log(sigma);
-        double rmode = pow(3.0 * vliq / (4. * PI * ndrop) * exp(-9.0 / 2.0 * (ls * ls)), 1. / 3.);
+        double rmode = cbrt(3.0 * vliq / (4. * PI * ndrop) * exp(-9.0 / 2.0 * (ls * ls)));
         rmean = rmode * exp(0.5 * (ls * ls));
         aliq = 4.0 * PI * (rmode * rmode) * ndrop * exp(2.0 * (ls * ls));
         double t = tl;
-        double t2 = t * t, t3 = t2 * t;
-        double ph2o0 = exp(18.452406985 - 3505.1578807 / t - 330918.55082 / t2 + 12725068.262 / t3);
+        const double rt = 1. / t, rt2 = rt * rt, rt3 = rt2 * rt;
+        double ph2o0 = exp(18.452406985 - 3505.1578807 * rt - 330918.55082 * rt2 + 12725068.262 * rt3);
         aw = pw * 1013. / ph2o0;
         aw = fmin(aw, 1.);
         int br = (aw <= 0.05) ? 0 : ((aw < 0.85) ? 1 : 2);
-        double y1 = c_an_a1[br] * pow(aw, c_an_b1[br]) + c_an_c1[br] * aw + c_an_d1[br];
-        double y2 = c_an_a2[br] * pow(aw, c_an_b2[br]) + c_an_c2[br] * aw + c_an_d2[br];
-        double m = y1 + (t - 190.) * (y2 - y1) / 70.;
+        const double law = log(aw);
+        double y1 = c_an_a1[br] * exp(c_an_b1[br] * law) + c_an_c1[br] * aw + c_an_d1[br];
+        double y2 = c_an_a2[br] * exp(c_an_b2[br] * law) + c_an_c2[br] * aw + c_an_d2[br];
+        double m = y1 + (t - 190.) * (y2 - y1) * (1. / 70.);
         wt = 9800. * m / (98. * m + 1000.);
         wt = fmax(wt, 0.5);
         double mh2so4 = dens * wt / 9.8;
         double bigx = wt / (wt + (100. - wt) * 98. / 18.);
-        hhcl = (0.094 - 0.61 * bigx + 1.2 * (bigx * bigx)) * exp(-8.68 + (8515. - 10718. * pow(bigx, 0.7)) / t);
-        double qhcl = ck[12] / hnm;
+        hhcl = (0.094 - 0.61 * bigx + 1.2 * (bigx * bigx)) * exp(-8.68 + (8515. - 10718. * exp(0.7 * log(bigx))) * rt);
+        double qhcl = ck[12] * rhnm;
         double phcl0 = qhcl * ptot / 1013.0;
         double phcl1 = (phcl0 / (r * t)) / (1. / (r * t) + hhcl * ns / ms);
         A.parthcl = 1.0 - (phcl0 - phcl1) / phcl0;
-        double sclono2 = 0.306 + 24. / t;
-        hclono2 = 1.6e-6 * exp(4710. / t) * exp(-sclono2 * mh2so4);
-        double shocl = 0.0776 + 59.18 / t;
-        hhocl = 1.91e-6 * exp(5862.4 / t) * exp(-shocl * mh2so4);
-        hhobr = 4.6e-4 * exp(4.5e3 / t);
+        double sclono2 = 0.306 + 24. * rt;
+        hclono2 = 1.6e-6 * exp(4710. * rt) * exp(-sclono2 * mh2so4);
+        double shocl = 0.0776 + 59.18 * rt;
+        hhocl = 1.91e-6 * exp(5862.4 * rt) * exp(-shocl * mh2so4);
+        hhobr = 4.6e-4 * exp(4.5e3 * rt);
         // hhbr (F:3222-3228) feeds only the disabled HOCl+HBr branch of hetero
     }
     // total PSC area F:3240-3246, HNO3 partition F:3252-3258
@@ -446,25 +449,29 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
     double kl[9] = {0., 0., 0., 0., 0., 0., 0., 0., 0.};
     double ksl[9] = {0., 0., 0., 0., 0., 0., 0., 0., 0.};  // K*S zero-initialised
     const double T = temp;
+    const double rT = 1. / T;
     if (condliq == 1) {
         double ZH2O = fmax(ck[2], 1.E-08 * hnm);
         double ZHCL = fmax(ck[12], 1.E-13 * hnm);
         double ZCLONO2 = fmax(ck[13], 1.E-13 * hnm);
         double ZHOBR = fmax(ck[25], 1.E-15 * hnm);
-        double phcl = (ZHCL / hnm) * ptot / 1013.;
-        double pclono2 = (ZCLONO2 / hnm) * ptot / 1013.;
-        double phobr = (ZHOBR / hnm) * ptot / 1013.;
+        const double rZH2O = 1. / ZH2O, rZHCL = 1. / ZHCL;
+        const double pfac = rhnm * ptot * (1. / 1013.);
+        double phcl = ZHCL * pfac;
+        double pclono2 = ZCLONO2 * pfac;
+        double phobr = ZHOBR * pfac;
         double wt2 = wt * wt, wt3 = wt2 * wt;
         double t0 = 144.11 + 0.166 * wt - 0.015 * wt2 + 2.18e-4 * wt3;
         double biga = 169.5 + 5.18 * wt - 0.0825 * wt2 + 3.27e-3 * wt3;
-        double eta = biga * pow(T, -1.43) * exp(448. / (T - t0));
+        double eta = biga * exp(-1.43 * log(T)) * exp(448. / (T - t0));
+        const double Teta = T / eta;
         double sqT = sqrt(T);
         double ah = exp(60.51 - 0.095 * wt + 0.0077 * wt2 - 1.61e-5 * wt3 - (1.76 + 2.52e-4 * wt2) * sqT +
-                        (-805.89 + 253.05 * pow(wt, 0.076)) / sqT);
-        double dclono2 = 5.e-8 * T / eta;
+                        (-805.89 + 253.05 * exp(0.076 * log(wt))) / sqT);
+        double dclono2 = 5.e-8 * Teta;
         double cclono2 = 1474. * sqT;
-        double kh2o = 1.95e10 * exp(-2800. / T);
-        double khh = 1.22e12 * exp(-6200. / T);
+        double kh2o = 1.95e10 * exp(-2800. * rT);
+        double khh = 1.22e12 * exp(-6200. * rT);
         double khydr = kh2o * aw + khh * ah * aw;
         double gbh2o = 4 * hclono2 * 0.082 * T * sqrt(dclono2 * khydr) / cclono2;
         double mhcl = hhcl * phcl;
@@ -473,7 +480,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double fclono2 = 1. / tanh(rmean / lclono2) - lclono2 / rmean;
         double grxn = fclono2 * gbh2o * sqrt(1. + khcl / khydr);
         double gbhcl = grxn * khcl / (khcl + khydr);
-        double gs = 66.12 * hclono2 * mhcl * exp(-1374. / T);
+        double gs = 66.12 * hclono2 * mhcl * exp(-1374. * rT);
         double fhcl = 1. / (1 + 0.612 * (gs + gbhcl) * pclono2 / phcl);
         double gps = fhcl * gs;
         double gbhclp = fhcl * gbhcl;
@@ -481,30 +488,30 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double gclono2 = 1. / (1. + 1. / (gps + gb));
         double gclono2hcl = gclono2 * (gps + gbhclp) / (gps + gb);
         double gclono2h2o = gclono2 - gclono2hcl;
-        kl[0] = 0.25 * gclono2h2o * cclono2 * aliq / ZH2O;
-        kl[1] = 0.25 * gclono2hcl * cclono2 * aliq / ZHCL;
+        kl[0] = 0.25 * gclono2h2o * cclono2 * aliq * rZH2O;
+        kl[1] = 0.25 * gclono2hcl * cclono2 * aliq * rZHCL;
         double chocl = 2009. * sqT;
-        double dhocl = 6.4e-8 * T / eta;
+        double dhocl = 6.4e-8 * Teta;
         double khoclhcl = 1.25e9 * ah * dhocl * mhcl;
         double lhocl = sqrt(dhocl / khoclhcl);
         double fhocl = 1. / tanh(rmean / lhocl) - lhocl / rmean;
         grxn = 4. * hhocl * 0.082 * T * sqrt(dhocl * khoclhcl) / chocl;
         double ghoclhcl = 1. / (1. + 1. / (fhocl * grxn * fhcl));
-        kl[4] = 0.25 * ghoclhcl * chocl * aliq / ZHCL;
+        kl[4] = 0.25 * ghoclhcl * chocl * aliq * rZHCL;
         double mhobr = hhobr * phobr;
-        double k2hobrhcl = exp(0.542 * wt - 6.44e3 / T + 10.3);
+        double k2hobrhcl = exp(0.542 * wt - 6.44e3 * rT + 10.3);
         double ratio = mhobr / mhcl;
         if (ratio < 1.) {
             double k1hobrhcl = k2hobrhcl * mhcl;
-            double dhobr = 6.2e-8 * T / eta;
+            double dhobr = 6.2e-8 * Teta;
             double lhobr = sqrt(dhobr / k1hobrhcl);
             double fhobr = 1. / tanh(rmean / lhobr) - lhobr / rmean;
             double chobr = 1477. * sqT;
             double ghobrhcl = 4. * hhobr * 0.082 * T * sqrt(dhobr * k1hobrhcl) * fhobr / chobr;
-            kl[6] = 0.25 * ghobrhcl * chobr * aliq / ZHCL;
+            kl[6] = 0.25 * ghobrhcl * chobr * aliq * rZHCL;
         } else {
             double k1hobrhcl = k2hobrhcl * mhobr;
-            double dhcl = 7.8e-8 * T / eta;
+            double dhcl = 7.8e-8 * Teta;
             double lhcl = sqrt(dhcl / k1hobrhcl);
             double fh = 1. / tanh(rmean / lhcl) - lhcl / rmean;
             double chcl = 2408. * sqT;
@@ -512,26 +519,28 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             kl[6] = 0.25 * ghobrhcl * chcl * aliq / ZHOBR;
         }
         double CBAR = 1400.1 * sqT;
-        kl[2] = 0.25 * 0.1 * CBAR * aliq / ZH2O;
+        kl[2] = 0.25 * 0.1 * CBAR * aliq * rZH2O;
         double gxrn = exp(29.24 - 0.396 * 100. * ws) + 0.114;
         double gbrno3h2o = 1. / (1. / 0.805 + 1. / gxrn);
         CBAR = 1221.4 * sqT;
-        kl[5] = 0.25 * gbrno3h2o * CBAR * aliq / ZH2O;
+        kl[5] = 0.25 * gbrno3h2o * CBAR * aliq * rZH2O;
     }
     if (lnat == 1) {
         double ZH2O = fmax(ck[2], 1.E-08 * hnm);
         double ZHCL = fmax(ck[12], 1.E-13 * hnm);
-        const double P = ptot, NS = nnats, NL = nnatl;
-#define NATR(G, M, Z)                                                                                   \
-    ((G) * 4.56E4 * sqrt(T / (M)) * (rnats * rnats) * NS / (1.0 + 3.3E4 * (G) * rnats * P / T) / (Z) + \
-     (G) * 4.56E4 * sqrt(T / (M)) * (rnatl * rnatl) * NL / (1.0 + 3.3E4 * (G) * rnatl * P / T) / (Z))
-        ksl[0] = NATR(0.004, 97.45, ZH2O);
-        ksl[1] = NATR(0.2, 97.45, ZHCL);
-        ksl[2] = NATR(4.0E-4, 108.0, ZH2O);
-        ksl[5] = NATR(0., 142.0, ZH2O);
-        ksl[3] = NATR(3.0E-3, 108.0, ZHCL);
-        ksl[4] = NATR(0.1, 52.5, ZHCL);
-        ksl[6] = NATR(0., 96.9, ZHCL);
+        const double PT = ptot * rT, NS = nnats, NL = nnatl;
+        const double rZH2O = 1. / ZH2O, rZHCL = 1. / ZHCL;
+#define NATR(G, M, RZ)                                                                                        \
+    (((G) * 4.56E4 * sqrt(T * (1. / (M))) * (rnats * rnats) * NS / (1.0 + 3.3E4 * (G) * rnats * PT) +     \
+      (G) * 4.56E4 * sqrt(T * (1. / (M))) * (rnatl * rnatl) * NL / (1.0 + 3.3E4 * (G) * rnatl * PT)) * \
+     (RZ))
+        ksl[0] = NATR(0.004, 97.45, rZH2O);
+        ksl[1] = NATR(0.2, 97.45, rZHCL);
+        ksl[2] = NATR(4.0E-4, 108.0, rZH2O);
+        ksl[5] = NATR(0., 142.0, rZH2O);
+        ksl[3] = NATR(3.0E-3, 108.0, rZHCL);
+        ksl[4] = NATR(0.1, 52.5, rZHCL);
+        ksl[6] = NATR(0., 96.9, rZHCL);
 #undef NATR
         ksl[7] = 0.;
     }
@@ -539,16 +548,18 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double ZH2O = fmax(ck[2], 1.E-08 * hnm);
         double ZHCL = fmax(ck[12], 1.E-13 * hnm);
         double ZHOBR = fmax(ck[25], 1.E-13 * hnm);
-        const double P = ptot, NI = nice;
-#define ICER(G, M, Z) ((G) * 4.56E4 * sqrt(T / (M)) * (rice * rice) * NI / (1.0 + 3.3E4 * (G) * rice * P / T) / (Z))
-        ksl[1] = ICER(0.3, 97.45, ZHCL);
-        ksl[0] = ICER(0.3, 97.45, ZH2O);
-        ksl[2] = ICER(0.02, 108.0, ZH2O);
-        ksl[3] = ICER(0.03, 108.0, ZHCL);
-        ksl[4] = ICER(0.2, 52.5, ZHCL);
-        ksl[5] = ICER(0.3, 142.0, ZH2O);
-        ksl[6] = ICER(0.3, 96.9, ZHCL);
-        ksl[7] = ICER(0.1, 96.9, ZHOBR);
+        const double PT = ptot * rT, NI = nice;
+        const double rZH2O = 1. / ZH2O, rZHCL = 1. / ZHCL, rZHOBR = 1. / ZHOBR;
+#define ICER(G, M, RZ) \
+    ((G) * 4.56E4 * sqrt(T * (1. / (M))) * (rice * rice) * NI / (1.0 + 3.3E4 * (G) * rice * PT) * (RZ))
+        ksl[1] = ICER(0.3, 97.45, rZHCL);
+        ksl[0] = ICER(0.3, 97.45, rZH2O);
+        ksl[2] = ICER(0.02, 108.0, rZH2O);
+        ksl[3] = ICER(0.03, 108.0, rZHCL);
+        ksl[4] = ICER(0.2, 52.5, rZHCL);
+        ksl[5] = ICER(0.3, 142.0, rZH2O);
+        ksl[6] = ICER(0.3, 96.9, rZHCL);
+        ksl[7] = ICER(0.1, 96.9, rZHOBR);
 #undef ICER
     }
     double f = (double)(lnat + lice);
@@ -563,6 +574,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
 __device__ __forceinline__ void cell_rates(const double* troe, double t, double hnm, double pm, double* K) {
     const double xln6 = log(0.6);
     double lntemp = log(t);
+    const double rt = 1. / t;  // Arrhenius exponents E / T as E * (1 / T)
     double ak0, ak1, rate, xpo, deq, l10;
 #define RK(name) K[K_##name]
 #define TROE(A0, E0, A1, E1, OUT)                \
@@ -573,123 +585,123 @@ __device__ __forceinline__ void cell_rates(const double* troe, double t, double 
     xpo = 1. / (1. + l10 * l10);                 \
     OUT = rate * exp(xln6 * xpo)
     TROE(troe[0], -1.3, troe[1], 0.2, RK(a1));
-    RK(a1et) = 1.63e-10 * exp(60. / t);
-    RK(a2) = 1.4e-10 * exp(-470. / t);
-    RK(a5) = 1.8e-11 * exp(180. / t);
-    RK(a6) = 1.7e-12 * exp(-940. / t);
-    RK(a6b) = 1.0e-14 * exp(-490. / t);
-    double e200 = exp(200. / t);
+    RK(a1et) = 1.63e-10 * exp(60. * rt);
+    RK(a2) = 1.4e-10 * exp(-470. * rt);
+    RK(a5) = 1.8e-11 * exp(180. * rt);
+    RK(a6) = 1.7e-12 * exp(-940. * rt);
+    RK(a6b) = 1.0e-14 * exp(-490. * rt);
+    double e200 = exp(200. * rt);
     RK(a7) = 3.0e-11 * e200;
-    double e250 = exp(250. / t);
+    double e250 = exp(250. * rt);
     RK(a17) = 4.8e-11 * e250;
-    RK(a19) = 2.8e-12 * exp(-1800. / t);
-    double e270 = exp(270. / t);
+    RK(a19) = 2.8e-12 * exp(-1800. * rt);
+    double e270 = exp(270. * rt);
     RK(a26) = 3.3e-12 * e270;
-    RK(a27) = 1.5e-12 * exp(19. / t) + 2.1e-33 * exp(920. / t) * hnm;
+    RK(a27) = 1.5e-12 * exp(19. * rt) + 2.1e-33 * exp(920. * rt) * hnm;
     RK(a30) = 1.8e-12;
     RK(a31) = 1.8e-12;
     RK(a36) = 1.5e-13 * (1. + .6 * pm / 1013.);
-    RK(b3) = 5.1e-12 * exp(210. / t);
-    RK(b4) = 3.0e-12 * exp((-1500. / t));
-    RK(b6) = 2.1e-11 * exp((100. / t));
-    RK(b7) = 1.5e-11 * exp((-3600. / t));
-    double em2450 = exp((-2450. / t));
+    RK(b3) = 5.1e-12 * exp(210. * rt);
+    RK(b4) = 3.0e-12 * exp((-1500. * rt));
+    RK(b6) = 2.1e-11 * exp((100. * rt));
+    RK(b7) = 1.5e-11 * exp((-3600. * rt));
+    double em2450 = exp((-2450. * rt));
     RK(b9) = 1.2e-13 * em2450;
     TROE(troe[2], -4.4, troe[3], -0.7, RK(b12));
     TROE(troe[4], -3.0, troe[5], 0.0, RK(b22));
     TROE(troe[6], -3.4, troe[7], -1.1, RK(b23));
-    deq = 2.1e-27 * exp(10900. / t);
+    deq = 2.1e-27 * exp(10900. * rt);
     RK(b24) = RK(b23) / (deq * hnm);
-    double e460 = exp(460. / t);
+    double e460 = exp(460. * rt);
     {
-        double aux1 = 2.7e-17 * exp(2199. / t);
-        double aux2 = 1. + aux1 / (6.5e-34 * exp(1335. / t) * hnm);
+        double aux1 = 2.7e-17 * exp(2199. * rt);
+        double aux2 = 1. + aux1 / (6.5e-34 * exp(1335. * rt) * hnm);
         RK(b27) = 2.4e-14 * e460 + aux1 / aux2;
     }
-    RK(b28) = 1.3e-12 * exp(380. / t);
-    deq = 2.7e-27 * exp(11000. / t);
+    RK(b28) = 1.3e-12 * exp(380. * rt);
+    deq = 2.7e-27 * exp(11000. * rt);
     RK(b32) = RK(b12) / (deq * hnm);
-    double e20 = exp(20. / t);
+    double e20 = exp(20. * rt);
     RK(b38) = 4.63e-11 * e20;
     RK(b39) = 7.25e-11 * e20;
     RK(c1a) = 1.31e-10;
     RK(c1b) = 0.35e-10;
     RK(c1c) = 0.09e-10;
-    RK(c2) = 2.45e-12 * exp((-1775. / t));
+    RK(c2) = 2.45e-12 * exp((-1775. * rt));
     RK(c3) = 1.1e-10;
     TROE(troe[16], -3.6, troe[17], 1.1, RK(c4));
-    RK(c5) = 2.8e-12 * exp((300. / t));
-    RK(c7) = 3.8e-13 * exp((800. / t));
-    RK(c8) = 5.5e-12 * exp(125. / t);
-    double em1600 = exp((-1600. / t));
+    RK(c5) = 2.8e-12 * exp((300. * rt));
+    RK(c7) = 3.8e-13 * exp((800. * rt));
+    RK(c8) = 5.5e-12 * exp(125. * rt);
+    double em1600 = exp((-1600. * rt));
     RK(c9) = 3.4e-11 * em1600;
-    RK(c10) = 8.1e-11 * exp((-30. / t));
+    RK(c10) = 8.1e-11 * exp((-30. * rt));
     RK(c12) = 5.2e-12;
-    RK(c14) = 9.5e-14 * exp((390. / t));
-    RK(c15) = 3.9e-14 * exp((-900. / t));
+    RK(c14) = 9.5e-14 * exp((390. * rt));
+    RK(c15) = 3.9e-14 * exp((-900. * rt));
     RK(c17a) = 3.8e-12 * e200 * 0.7;
     RK(c17b) = 3.8e-12 * e200 * 0.3;
-    RK(c18) = 3.3e-12 * exp((-115. / t));
-    double em800 = exp((-800. / t));
+    RK(c18) = 3.3e-12 * exp((-115. * rt));
+    double em800 = exp((-800. * rt));
     RK(c19) = 1.7e-11 * em800;
-    RK(d2) = 2.3e-11 * exp((-200. / t));
-    RK(d3) = 2.8e-11 * exp(85. / t);
-    double e290 = exp(290. / t);
+    RK(d2) = 2.3e-11 * exp((-200. * rt));
+    RK(d3) = 2.8e-11 * exp(85. * rt);
+    double e290 = exp(290. * rt);
     RK(d4) = 6.4e-12 * e290;
-    RK(d5) = 7.3e-12 * exp((-1280. / t));
-    RK(d6) = 3.05e-11 * exp((-2270. / t));
-    RK(d7) = 1.4e-11 * exp(269. / t);
+    RK(d5) = 7.3e-12 * exp((-1280. * rt));
+    RK(d6) = 3.05e-11 * exp((-2270. * rt));
+    RK(d7) = 1.4e-11 * exp(269. * rt);
     RK(d8) = 7.4e-12 * e270;
-    double e230 = exp(230. / t);
+    double e230 = exp(230. * rt);
     RK(d9) = 6.0e-13 * e230;
-    RK(d10) = 3.6e-11 * exp(-375. / t);
-    RK(d11) = 1.8e-12 * exp((-250. / t));
+    RK(d10) = 3.6e-11 * exp(-375. * rt);
+    RK(d11) = 1.8e-12 * exp((-250. * rt));
     TROE(troe[8], -3.4, troe[9], -1.9, RK(d31));
-    double em840 = exp((-840. / t));
+    double em840 = exp((-840. * rt));
     RK(d32) = 3.6e-12 * em840;
     RK(d33) = 2.6e-12 * e290;
-    RK(d34) = 3.0e-12 * exp((-500. / t));
+    RK(d34) = 3.0e-12 * exp((-500. * rt));
     RK(d35) = 1.7e-13;
     TROE(troe[10], -2., troe[11], -1., RK(d36));
-    RK(d37) = 3.4e-12 * exp((-130. / t));
+    RK(d37) = 3.4e-12 * exp((-130. * rt));
     TROE(troe[12], -4.5, troe[13], -2.0, RK(d60));
-    deq = 1.72e-27 * exp(8649. / t);
+    deq = 1.72e-27 * exp(8649. * rt);
     RK(d61) = RK(d60) / (deq * hnm);
-    RK(d62) = 1.0e-12 * exp(-1590. / t) + 3.0e-11 * em2450;
+    RK(d62) = 1.0e-12 * exp(-1590. * rt) + 3.0e-11 * em2450;
     RK(d90) = 2.3e-10;
     RK(d91) = 1.4e-10;
     RK(d92) = 2.0e-10;
     RK(d93) = 3.3e-10;
-    RK(d94) = 1.64e-12 * exp((-1520. / t));
-    RK(d95) = 2.4e-12 * exp((-1250. / t));
+    RK(d94) = 1.64e-12 * exp((-1520. * rt));
+    RK(d95) = 2.4e-12 * exp((-1250. * rt));
     RK(d96) = 1.0e-10;
     RK(d97) = 1.05e-12 * em1600;
-    RK(e2) = 1.6e-11 * exp((-780. / t));
+    RK(e2) = 1.6e-11 * exp((-780. * rt));
     RK(e3) = 1.9e-11 * e230;
-    double e260 = exp(260. / t);
+    double e260 = exp(260. * rt);
     RK(e4) = 8.8e-12 * e260;
-    RK(e5a) = 9.5e-13 * exp(550. / t);
+    RK(e5a) = 9.5e-13 * exp(550. * rt);
     RK(e5b) = 2.3e-12 * e260;
     RK(e5c) = 4.1e-13 * e290;
     RK(e6) = 1.5e-12 * e230;
-    RK(e7) = 4.8e-12 * exp(-310. / t);
-    RK(e8) = 1.9e-11 * exp(215. / t);
+    RK(e7) = 4.8e-12 * exp(-310. * rt);
+    RK(e8) = 1.9e-11 * exp(215. * rt);
     RK(e9) = 1.5e-10;
     RK(e10) = 1.7e-11 * e250;
     RK(e11) = 5.5e-12 * e200;
     TROE(troe[14], -3.2, troe[15], -2.9, RK(e13));
     RK(e15) = 4.5e-12 * e460;
-    RK(e16) = 1.2e-10 * exp((-430. / t));
+    RK(e16) = 1.2e-10 * exp((-430. * rt));
     RK(e50) = 1.8e-10;
-    RK(e51) = 2.35e-12 * exp((-1300. / t));
+    RK(e51) = 2.35e-12 * exp((-1300. * rt));
     RK(e52) = 1.5e-10;
     RK(e53) = 1.0e-10;
     RK(e54) = 2.0e-12 * em840;
-    RK(hk1) = 4.23e-28 * hnm / (t * t);
-    RK(hk2) = 6.0e-34 * pow(300. / t, 2.4) * hnm;
-    RK(hk3) = 8.e-12 * exp((-2060. / t));
-    RK(hk4) = 2.15e-11 * exp(110. / t);
-    RK(hk5) = 3.3e-11 * exp(55. / t);
+    RK(hk1) = 4.23e-28 * hnm * (rt * rt);
+    RK(hk2) = 6.0e-34 * exp(2.4 * log(300. * rt)) * hnm;
+    RK(hk3) = 8.e-12 * exp((-2060. * rt));
+    RK(hk4) = 2.15e-11 * exp(110. * rt);
+    RK(hk5) = 3.3e-11 * exp(55. * rt);
 #undef TROE
 #undef RK
 }

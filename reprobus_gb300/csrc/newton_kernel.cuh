@@ -301,13 +301,18 @@ __global__ void __launch_bounds__(2 * NS, 1) k_nt_solve_sp(Params P) {
     }
 }
 
+// Sets the dynamic shared memory of a solve kernel and returns how many of its
+// blocks an SM runs.
+template <typename K>
+cudaError_t nt_fit_smem(K* fn, int nthreads, size_t smem, int* blocks_per_sm) {
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, nthreads, smem);
+}
+
 template <typename TJ, int NS>
 cudaError_t nt_sp_prepare(int* blocks_per_sm) {
-    cudaError_t e = cudaFuncSetAttribute(k_nt_solve_sp<TJ, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)nt_sp_smem_bytes<TJ, NS>());
-    if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_nt_solve_sp<TJ, NS>, 2 * NS,
-                                                         nt_sp_smem_bytes<TJ, NS>());
+    return nt_fit_smem(k_nt_solve_sp<TJ, NS>, 2 * NS, nt_sp_smem_bytes<TJ, NS>(), blocks_per_sm);
 }
 
 template <typename TJ, int NS>
@@ -397,10 +402,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_ls(Params P) {
 
 template <typename TJ, int NTH>
 cudaError_t nt_ls_prepare(int* blocks_per_sm) {
-    const size_t smem = (size_t)NT_NSLOT * NTH * sizeof(TJ);
-    cudaError_t e = cudaFuncSetAttribute(k_nt_solve_ls<TJ, NTH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_nt_solve_ls<TJ, NTH>, NTH, smem);
+    return nt_fit_smem(k_nt_solve_ls<TJ, NTH>, NTH, (size_t)NT_NSLOT * NTH * sizeof(TJ), blocks_per_sm);
 }
 
 template <typename TJ, int NTH>
@@ -423,11 +425,7 @@ constexpr size_t nt_pp_smem_bytes() {
 
 template <typename TJ, int NTH>
 cudaError_t nt_pp_prepare(int* blocks_per_sm) {
-    cudaError_t e = cudaFuncSetAttribute(k_nt_solve_pp<TJ, NTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)nt_pp_smem_bytes<TJ, NTH>());
-    if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_nt_solve_pp<TJ, NTH>, NTH,
-                                                         nt_pp_smem_bytes<TJ, NTH>());
+    return nt_fit_smem(k_nt_solve_pp<TJ, NTH>, NTH, nt_pp_smem_bytes<TJ, NTH>(), blocks_per_sm);
 }
 
 template <typename TJ, int NTH>
@@ -450,11 +448,7 @@ constexpr size_t nt_smem_bytes() {
 
 template <typename TJ, int NTH, bool ZS>
 cudaError_t nt_prepare(int* blocks_per_sm) {
-    cudaError_t e = cudaFuncSetAttribute(k_nt_solve<TJ, NTH, ZS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)nt_smem_bytes<TJ, NTH, ZS>());
-    if (e != cudaSuccess) return e;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, k_nt_solve<TJ, NTH, ZS>, NTH,
-                                                         nt_smem_bytes<TJ, NTH, ZS>());
+    return nt_fit_smem(k_nt_solve<TJ, NTH, ZS>, NTH, nt_smem_bytes<TJ, NTH, ZS>(), blocks_per_sm);
 }
 
 template <typename TJ, int NTH, bool ZS>
