@@ -256,7 +256,10 @@ int reprobus_chem_features_dev(void* handle, int ilat0, int ilat1, double daynum
  * :601-2412); with REPROBUS_FUSE_CONSERV also conserv (:427, :2526-2616) and
  * the clamps (:431-450) on those rows. Writes qj1/hc (levels 1..nivbas; with
  * the flag also the clamps on all levels), vsed3d, parth2osed, parthno3sed,
- * sza3d (levels 1..nivbas) and surfarea (levels nivhau..nivbas). */
+ * sza3d (levels 1..nivbas) and surfarea (levels nivhau..nivbas).
+ * With 32 rows or more the rows go in 4 chunks, the copies of one chunk
+ * overlapping the integration of the next; the environment variable
+ * REPROBUS_HOST_CHUNKS (1..4) sets another number of chunks. */
 int reprobus_chem_step(void* handle, int ilat0, int ilat1, double daynum, double dt,
                        const double* alt, const double* trajlon, const double* trajlat,
                        const double* trajpre, const double* trajtem, int irapp,

@@ -25,6 +25,13 @@ constexpr int NOZO = 7;
 constexpr int NRATE = 99;
 constexpr double PI = 3.141592653589793;  // 2.*asin(1.0), F:2750
 constexpr double LN10 = 2.302585092994046;  // 10^y evaluated as exp(y ln 10)
+// transcendental constants of the aerosol and rate code, evaluated once here:
+// ln 760 (F:2866), ln 0.6 (Troe broadening, F:920), and for the log-normal
+// liquid aerosol of width sigma = 1.8 (F:2632, F:3091-3096)
+// exp(-4.5 ln^2 sigma), exp(0.5 ln^2 sigma), exp(2 ln^2 sigma)
+constexpr double LN760 = 6.633318433280377, LN06 = -0.5108256237659907;
+constexpr double AER_EXP_M45 = 0.21124868545437422, AER_EXP_05 = 1.18856486285036,
+                 AER_EXP_2 = 1.9956829585543872;
 
 // per-step constants shared by all cells
 struct StepConst {
@@ -192,7 +199,7 @@ __constant__ double c_dens_x[23] = {0., 2.393284E-02, -4.359335E-05, 7.961181E-0
                                     1.60074E-03, -2.5827835E-06};
 
 static __device__ __noinline__ void cell_aerosol(double temp, double ptot, double hnm, const double* ck, Aerosol& A) {
-    const double r = 8.205e-5, sigma = 1.8;
+    const double r = 8.205e-5;
     const double* qn = c_an_qn;
     const double* qs = c_an_qs;
     const double* kn = c_an_kn;
@@ -254,7 +261,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
     double tice;
     {
         double t = fmin(temp, 273.);
-        tice = 2668.70 / (10.4310 - (log(pw) + log(760.0)) / log(10.0));
+        tice = 2668.70 / (10.4310 - (log(pw) + LN760) * (1. / LN10));
         if (t <= tice) {
             lice = 1;
             lnat = 0;
@@ -381,10 +388,9 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
     double aw = 0., wt = 0., hhcl = 0., hhocl = 0., hhobr = 0., hclono2 = 0.;
     if (condliq == 1) {
         double vliq = ns * 98.076e-6 / ws / dens;
-        double ls = log(sigma);
-        double rmode = cbrt(3.0 * vliq / (4. * PI * ndrop) * exp(-9.0 / 2.0 * (ls * ls)));
-        rmean = rmode * exp(0.5 * (ls * ls));
-        aliq = 4.0 * PI * (rmode * rmode) * ndrop * exp(2.0 * (ls * ls));
+        double rmode = cbrt(3.0 * vliq / (4. * PI * ndrop) * AER_EXP_M45);
+        rmean = rmode * AER_EXP_05;
+        aliq = 4.0 * PI * (rmode * rmode) * ndrop * AER_EXP_2;
         double t = tl;
         const double rt = 1. / t, rt2 = rt * rt, rt3 = rt2 * rt;
         double ph2o0 = exp(18.452406985 - 3505.1578807 * rt - 330918.55082 * rt2 + 12725068.262 * rt3);
@@ -572,7 +578,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
 // rate constants, F:920-1306
 // ----------------------------------------------------------------------------
 __device__ __forceinline__ void cell_rates(const double* troe, double t, double hnm, double pm, double* K) {
-    const double xln6 = log(0.6);
+    const double xln6 = LN06;
     double lntemp = log(t);
     const double rt = 1. / t;  // Arrhenius exponents E / T as E * (1 / T)
     double ak0, ak1, rate, xpo, deq, l10;

@@ -60,12 +60,26 @@ extern "C" __attribute__((visibility("hidden"))) int reprobus_set_error(int code
                                               __FILE__, __LINE__);                                           \
     } while (0)
 
+// Cells are numbered i + nlon (r + nrows k) over the longitudes (i), the
+// step's rows (r) and the chemistry levels (k); columns i + nlon r. The
+// per-cell kernels of the rate stage, the start and the write-back take the
+// cells of a window of rows win_r0 .. win_r0 + win_nr - 1: thread t handles
+// the t-th cell (column) of the window, the identity when the window is the
+// whole range. The host-array entry point runs those phases row chunk by row
+// chunk while the copies of the other chunks are in flight.
+__device__ __forceinline__ int win_cell(const Params& P, int t) {
+    const int i = t % P.nlon, rest = t / P.nlon;
+    return i + P.nlon * (P.win_r0 + rest % P.win_nr + P.nrows * (rest / P.win_nr));
+}
+__device__ __forceinline__ int win_col(const Params& P, int t) { return t % P.nlon + P.nlon * (P.win_r0 + t / P.nlon); }
+
 // ----------------------------------------------------------------------------
 // k_columns — vertical prefix sums, total F:5172-5184 and jno JNO:109-126
 // ----------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_columns(Params P) {
-    const int col = blockIdx.x * blockDim.x + threadIdx.x;
-    if (col >= P.ncol) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.win_ncol) return;
+    const int col = win_col(P, t);
     const int i = col % P.nlon;
     const int j = P.ilat0 + col / P.nlon;
     const size_t pl = plane3(P);
@@ -344,10 +358,10 @@ __device__ __forceinline__ void cell_features(const Params& P, size_t g, double 
 
 template <bool MIXED, int NTB = 128, bool LS = false>
 __global__ void __launch_bounds__(NTB) k_nt_setup(Params P) {
-    int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool own = cell < P.ncell;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool own = t < P.win_ncell;
     if (!LS && !own) return;
-    if (!own) cell = P.ncell - 1;  // lock-step: recompute a valid cell, write nothing
+    const int cell = win_cell(P, own ? t : P.win_ncell - 1);  // lock-step: recompute a valid cell, write nothing
     CellPro C;
     cell_prologue<false, LS>(P, cell, C, own);
     if (!own) return;
@@ -390,8 +404,9 @@ __global__ void __launch_bounds__(NTB) k_nt_setup(Params P) {
 template <int MODE>
 __global__ void __launch_bounds__(128) k_nt_start(Params P) {
     static_assert(MODE == 0 || MODE == 2, "start modes");
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= P.ncell) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.win_ncell) return;
+    const int cell = win_cell(P, t);
     if (MODE != 0 && P.nt_stat[cell] >= 0) return;
     const double* r = P.nt_rec + (size_t)cell * NT_REC;
     CellFix F;
@@ -430,7 +445,7 @@ __global__ void __launch_bounds__(128) k_nt_start(Params P) {
     if (F.sza <= 95.)
         P.nt_list[atomicAdd(P.nt_head + 1, 1)] = cell;
     else
-        P.nt_list[P.ncell - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
+        P.nt_list[P.nt_qcap - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
     if (MODE == 2) atomicAdd(P.nonfinite + 6, 1ULL);
 }
 
@@ -442,8 +457,9 @@ __global__ void __launch_bounds__(128) k_nt_start(Params P) {
 // night-time NO2/NO3 ratio beyond the FP32 range) gets stat -1 and is started
 // again in FP64 by k_nt_start<2>; the others enter the work queue.
 __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= P.ncell) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.win_ncell) return;
+    const int cell = win_cell(P, t);
     const double* r = P.nt_rec + (size_t)cell * NT_REC;
     const float* q = P.nt_rec32 + (size_t)cell * NT_REC32;
     const double hnm = r[NT_RF + 4];
@@ -500,7 +516,7 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
     if (day)
         P.nt_list[atomicAdd(P.nt_head + 1, 1)] = cell;
     else
-        P.nt_list[P.ncell - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
+        P.nt_list[P.nt_qcap - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
 }
 
 // warm start: x_i = max(x_i, 1e-30 hnm) 10^y_i from the network's prediction;
@@ -570,8 +586,9 @@ __device__ __forceinline__ void nt_cell_fix(const double* r, CellFix& F) {
 }
 
 __global__ void __launch_bounds__(128) k_nt_finish(Params P) {
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= P.ncell) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.win_ncell) return;
+    const int cell = win_cell(P, t);
     const int stat = P.nt_stat[cell];
     if (stat <= 0) return;
     const double* r = P.nt_rec + (size_t)cell * NT_REC;
@@ -593,8 +610,9 @@ __global__ void __launch_bounds__(128) k_nt_finish(Params P) {
 // fallback of the cells the Newton solver did not converge (stat <= 0): the
 // reference scheme's niter passes from the start state, then the write-back
 __global__ void __launch_bounds__(128) k_nt_fallback(Params P) {
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= P.ncell) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.win_ncell) return;
+    const int cell = win_cell(P, t);
     if (P.nt_stat[cell] > 0) return;
     const double* r = P.nt_rec + (size_t)cell * NT_REC;
     CellPro C;
@@ -625,13 +643,13 @@ __global__ void __launch_bounds__(128) k_nt_fallback(Params P) {
 // k_tail — levels nivbas+1..niv of the rows: clamps F:431-440, HNO3 gas F:444-450
 // ----------------------------------------------------------------------------
 __global__ void k_tail(Params P) {
-    const long long n = (long long)P.nlon * P.nrows * (P.niv - P.nivbas);
+    const long long n = (long long)P.nlon * P.win_nr * (P.niv - P.nivbas);
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= n) return;
     const int i = (int)(idx % P.nlon);
     const long long rest = idx / P.nlon;
-    const int j = P.ilat0 + (int)(rest % P.nrows);
-    const int k = P.nivbas + (int)(rest / P.nrows);
+    const int j = P.ilat0 + P.win_r0 + (int)(rest % P.win_nr);
+    const int k = P.nivbas + (int)(rest / P.win_nr);
     const size_t g = (size_t)i + (size_t)P.nlon * ((size_t)j + (size_t)P.nlat * k);
     const size_t pl = plane3(P);
 #pragma unroll 6
@@ -687,6 +705,7 @@ struct Handle {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t ev2 = nullptr, ev3 = nullptr;  // around the persistent solve kernel (stats.solve_ms)
+    cudaEvent_t ev4 = nullptr, ev5 = nullptr;  // around a second solve (host-array entry point)
     // device mirrors for the host-pointer entry point (allocated on first use)
     double* m_alt = nullptr;
     double* m_traj[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -785,6 +804,8 @@ static void free_handle(Handle* h) {
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     if (h->ev2) cudaEventDestroy(h->ev2);
     if (h->ev3) cudaEventDestroy(h->ev3);
+    if (h->ev4) cudaEventDestroy(h->ev4);
+    if (h->ev5) cudaEventDestroy(h->ev5);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
 }
@@ -828,6 +849,7 @@ extern "C" int reprobus_chem_init(const double* ajl, const double* o3up, const d
     if ((e = cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreate(&h->ev0)) != cudaSuccess || (e = cudaEventCreate(&h->ev1)) != cudaSuccess ||
         (e = cudaEventCreate(&h->ev2)) != cudaSuccess || (e = cudaEventCreate(&h->ev3)) != cudaSuccess ||
+        (e = cudaEventCreate(&h->ev4)) != cudaSuccess || (e = cudaEventCreate(&h->ev5)) != cudaSuccess ||
         (e = cudaMalloc(&h->d_ajl, najl * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&h->d_o3up, 80 * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&h->d_col, (3 * ncell + ncol) * sizeof(double))) != cudaSuccess ||
@@ -924,6 +946,11 @@ static void fill_params(const Handle* h, Params& P, int ilat0, int ilat1) {
     P.niter = h->niter;
     P.ncol = h->nlon * P.nrows;
     P.ncell = P.ncol * h->nivbas;
+    P.win_r0 = 0;
+    P.win_nr = P.nrows;
+    P.win_ncol = P.ncol;
+    P.win_ncell = P.ncell;
+    P.nt_qcap = P.ncell;
     P.ajl = h->d_ajl;
     P.o3up = h->d_o3up;
     P.col = h->d_col;
@@ -975,23 +1002,29 @@ static int ensure_newton(Handle* h) {
 // blocks without barriers; 512 threads 30 ms)
 constexpr int SETUP_TB = 256;
 static void launch_setup(Handle* h, const Params& P, bool mixed) {
-    const unsigned nb = (unsigned)((P.ncell + SETUP_TB - 1) / SETUP_TB);
+    const unsigned nb = (unsigned)((P.win_ncell + SETUP_TB - 1) / SETUP_TB);
     if (mixed)
         k_nt_setup<true, SETUP_TB, true><<<nb, SETUP_TB, 0, h->stream>>>(P);
     else
         k_nt_setup<false, SETUP_TB, true><<<nb, SETUP_TB, 0, h->stream>>>(P);
 }
 
-static int enqueue_setup(Handle* h, Params& P, bool mixed) {
+// rate stage and plain start of the cells of P's row window; they join the
+// work queue, whose heads the caller has zeroed
+static void newton_front(Handle* h, const Params& P, bool mixed) {
     const int tb = 128;
-    CUDA_TRY(cudaMemsetAsync(h->nt_head, 0, 8 * sizeof(int), h->stream));
     launch_setup(h, P, mixed);
     if (mixed) {
-        k_nt_start32<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
-        k_nt_start<2><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        k_nt_start32<<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        k_nt_start<2><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     } else {
-        k_nt_start<0><<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        k_nt_start<0><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     }
+}
+
+static int enqueue_setup(Handle* h, Params& P, bool mixed) {
+    CUDA_TRY(cudaMemsetAsync(h->nt_head, 0, 8 * sizeof(int), h->stream));
+    newton_front(h, P, mixed);
     return REPROBUS_OK;
 }
 
@@ -1117,21 +1150,20 @@ static int choose_shape(Handle* h, Params& P, bool mixed) {
     return REPROBUS_OK;
 }
 
-// the Newton pipeline of one step (after k_columns)
-static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool capturing) {
+// the Newton solvers' buffers and fields of P, and the solve-kernel shape
+// (autotuned on P's cells the first time)
+static int newton_prepare(Handle* h, Params& P) {
     int rc = ensure_newton(h);
     if (rc) return rc;
     const bool mixed = h->solver == REPROBUS_SOLVER_NEWTON_MIXED;
-    const int tb = 128;
     P.nt_rec = h->nt_rec;
     P.nt_rec32 = h->nt_rec32;
     P.nt_x = h->nt_x;
     P.nt_stat = h->nt_stat;
     P.nt_list = h->nt_list;
     P.nt_head = h->nt_head;
-    const bool warm = h->mlp != nullptr;
     P.npass_plain = h->npass;
-    if (warm) {
+    if (h->mlp) {
         if (!h->mlp_feat) {
             const size_t nc = (size_t)h->nlon * h->nlat * h->nivbas;
             CUDA_TRY(cudaMalloc(&h->mlp_feat, nc * MLP_FEAT * sizeof(float)));
@@ -1143,26 +1175,54 @@ static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool c
         P.mlp_y = h->mlp_y;
         P.nt_xp = h->nt_xp;
     }
-    if ((rc = choose_shape(h, P, mixed))) return rc;
-    const int ip = mixed ? 0 : 1;
-    const int grid = h->nsm * h->nt_bps[ip];
+    return choose_shape(h, P, mixed);
+}
+
+// warm start of all cells of P's range (inference and the warm-start
+// kernel), after the fronts of all its rows
+static int newton_warm(Handle* h, const Params& P) {
+    const int tb = 128;
+    CUDA_TRY(cudaMemsetAsync(mlp_err_flag(h->mlp), 0, sizeof(unsigned int), h->stream));
+    int rc = mlp_infer(h->mlp, h->mlp_feat, h->mlp_y, P.ncell, h->stream);
+    if (rc) return rc;
+    k_nt_warm<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    return REPROBUS_OK;
+}
+
+// the persistent solve of the cells of P's work queue; e0/e1 recorded around
+// it unless null. (A warm start that misses the convergence test is retried
+// from the saved plain start by the solve kernel itself, nt_end_attempt.)
+static int newton_solve(Handle* h, const Params& P, cudaEvent_t e0, cudaEvent_t e1, bool capturing) {
+    const int ip = h->solver == REPROBUS_SOLVER_NEWTON_MIXED ? 0 : 1;
+    if (e0) CUDA_TRY(capturing ? cudaEventRecordWithFlags(e0, h->stream, cudaEventRecordExternal)
+                               : cudaEventRecord(e0, h->stream));
+    CUDA_TRY(h->nt_var[ip]->launch(P, h->nsm * h->nt_bps[ip], h->stream));
+    if (e1) CUDA_TRY(capturing ? cudaEventRecordWithFlags(e1, h->stream, cudaEventRecordExternal)
+                               : cudaEventRecord(e1, h->stream));
+    return REPROBUS_OK;
+}
+
+// write-back of the cells of P's row window: converged cells, then the
+// reference passes for the others
+static void newton_back(Handle* h, const Params& P) {
+    const int tb = 128;
+    k_nt_finish<<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    k_nt_fallback<<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+}
+
+// the Newton pipeline of one step (after k_columns)
+static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool capturing) {
+    int rc = newton_prepare(h, P);
+    if (rc) return rc;
+    const bool mixed = h->solver == REPROBUS_SOLVER_NEWTON_MIXED;
     if ((rc = enqueue_setup(h, P, mixed))) return rc;
-    if (warm) {
-        CUDA_TRY(cudaMemsetAsync(mlp_err_flag(h->mlp), 0, sizeof(unsigned int), h->stream));
-        if ((rc = mlp_infer(h->mlp, h->mlp_feat, h->mlp_y, P.ncell, h->stream))) return rc;
-        k_nt_warm<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    if (h->mlp) {
+        if ((rc = newton_warm(h, P))) return rc;
         *launches += 2;
     }
-    if (timed) CUDA_TRY(capturing ? cudaEventRecordWithFlags(h->ev2, h->stream, cudaEventRecordExternal)
-                                  : cudaEventRecord(h->ev2, h->stream));
-    CUDA_TRY(h->nt_var[ip]->launch(P, grid, h->stream));
-    if (timed) CUDA_TRY(capturing ? cudaEventRecordWithFlags(h->ev3, h->stream, cudaEventRecordExternal)
-                                  : cudaEventRecord(h->ev3, h->stream));
+    if ((rc = newton_solve(h, P, timed ? h->ev2 : nullptr, timed ? h->ev3 : nullptr, capturing))) return rc;
+    newton_back(h, P);
     *launches += mixed ? 6 : 5;  // setup, start (FP32 + FP64 redo), solve, finish, fallback
-    // (a warm start that misses the convergence test is retried from the saved
-    // plain start by the solve kernel itself, nt_retry_warm)
-    k_nt_finish<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
-    k_nt_fallback<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     return REPROBUS_OK;
 }
 
@@ -1200,58 +1260,10 @@ static int enqueue_step(Handle* h, Params& P, bool capturing, int* launches) {
     return REPROBUS_OK;
 }
 
-// which solver configuration a step runs (graphs are reused per configuration)
-static int step_signature(const Handle* h) { return h->solver * 2 + (h->mlp ? 1 : 0); }
-
-// One step: directly, or (REPROBUS_USE_GRAPH, once this configuration has run
-// once directly, so that its buffers exist and its solve kernel is tuned) as
-// a CUDA graph: the step's calls are captured, the handle's executable graph
-// is updated in place (or instantiated), and launched as one unit.
-static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
-    int launches = 0;
-    P.fuse = (h->flags & REPROBUS_FUSE_CONSERV) ? 1 : 0;
-    P.check = (h->flags & REPROBUS_CHECK_FINITE) ? 1 : 0;
+// Statistics of the step just enqueued on h->stream (ev0 recorded before it,
+// ev2/ev3 around the solve), and the CHECK_FINITE verdict.
+static int step_stats(Handle* h, const Params& P, reprobus_stats* st, int launches, bool graph) {
     const bool counters = P.check || h->solver != REPROBUS_SOLVER_REF5;
-    const int sig = step_signature(h);
-    const bool graph = (h->flags & REPROBUS_USE_GRAPH) && (h->graph_ready & (1u << sig));
-    if (st) CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
-    if (!graph) {
-        int rc = enqueue_step(h, P, false, &launches);
-        if (rc) return rc;
-        h->graph_ready |= 1u << sig;
-    } else {
-        cudaGraph_t g = nullptr;
-        CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        const int rc = enqueue_step(h, P, true, &launches);
-        const cudaError_t e = cudaStreamEndCapture(h->stream, &g);
-        if (rc) {
-            if (g) cudaGraphDestroy(g);
-            return rc;
-        }
-        CUDA_TRY(e);
-        if (h->gexec && h->gexec_sig == sig) {
-            cudaGraphExecUpdateResultInfo info;
-            if (cudaGraphExecUpdate(h->gexec, g, &info) != cudaSuccess) {
-                cudaGetLastError();
-                cudaGraphExecDestroy(h->gexec);
-                h->gexec = nullptr;
-            }
-        } else if (h->gexec) {
-            cudaGraphExecDestroy(h->gexec);
-            h->gexec = nullptr;
-        }
-        if (!h->gexec) {
-            const cudaError_t ei = cudaGraphInstantiate(&h->gexec, g, 0);
-            if (ei != cudaSuccess) {
-                cudaGraphDestroy(g);
-                h->gexec = nullptr;
-                return set_err(REPROBUS_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(ei));
-            }
-            h->gexec_sig = sig;
-        }
-        cudaGraphDestroy(g);
-        CUDA_TRY(cudaGraphLaunch(h->gexec, h->stream));
-    }
     if (st) {
         CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
         CUDA_TRY(cudaEventSynchronize(h->ev1));
@@ -1298,6 +1310,60 @@ static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
         if (P.check && c[0]) return set_err(REPROBUS_ERR_NONFINITE, "%llu non-finite values in the step output", c[0]);
     }
     return REPROBUS_OK;
+}
+
+// which solver configuration a step runs (graphs are reused per configuration)
+static int step_signature(const Handle* h) { return h->solver * 2 + (h->mlp ? 1 : 0); }
+
+// One step: directly, or (REPROBUS_USE_GRAPH, once this configuration has run
+// once directly, so that its buffers exist and its solve kernel is tuned) as
+// a CUDA graph: the step's calls are captured, the handle's executable graph
+// is updated in place (or instantiated), and launched as one unit.
+static int launch_step(Handle* h, Params& P, reprobus_stats* st) {
+    int launches = 0;
+    P.fuse = (h->flags & REPROBUS_FUSE_CONSERV) ? 1 : 0;
+    P.check = (h->flags & REPROBUS_CHECK_FINITE) ? 1 : 0;
+    const int sig = step_signature(h);
+    const bool graph = (h->flags & REPROBUS_USE_GRAPH) && (h->graph_ready & (1u << sig));
+    if (st) CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+    if (!graph) {
+        int rc = enqueue_step(h, P, false, &launches);
+        if (rc) return rc;
+        h->graph_ready |= 1u << sig;
+    } else {
+        cudaGraph_t g = nullptr;
+        CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_step(h, P, true, &launches);
+        const cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        CUDA_TRY(e);
+        if (h->gexec && h->gexec_sig == sig) {
+            cudaGraphExecUpdateResultInfo info;
+            if (cudaGraphExecUpdate(h->gexec, g, &info) != cudaSuccess) {
+                cudaGetLastError();
+                cudaGraphExecDestroy(h->gexec);
+                h->gexec = nullptr;
+            }
+        } else if (h->gexec) {
+            cudaGraphExecDestroy(h->gexec);
+            h->gexec = nullptr;
+        }
+        if (!h->gexec) {
+            const cudaError_t ei = cudaGraphInstantiate(&h->gexec, g, 0);
+            if (ei != cudaSuccess) {
+                cudaGraphDestroy(g);
+                h->gexec = nullptr;
+                return set_err(REPROBUS_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(ei));
+            }
+            h->gexec_sig = sig;
+        }
+        cudaGraphDestroy(g);
+        CUDA_TRY(cudaGraphLaunch(h->gexec, h->stream));
+    }
+    return step_stats(h, P, st, launches, graph);
 }
 
 extern "C" int reprobus_chem_set_tuning(void* handle, int lanes_per_block, int blocks_per_sm, int zshared) {
@@ -1535,6 +1601,110 @@ static void add_stats(reprobus_stats* acc, const reprobus_stats& c, bool first) 
     acc->start64_cells += c.start64_cells;
 }
 
+// P over rows a..b (1-based) of the handle's device mirrors of the host arrays
+static void mirror_params(Handle* h, Params& P, int a, int b, double daynum, double dt) {
+    fill_params(h, P, a, b);
+    P.trajoff = 0;
+    P.alt = h->m_alt;
+    P.trajlon = h->m_traj[0];
+    P.trajlat = h->m_traj[1];
+    P.trajpre = h->m_traj[2];
+    P.trajtem = h->m_traj[3];
+    P.qj1 = h->m_qj1;
+    P.hc = h->m_hc;
+    P.vsed3d = h->m_out[0];
+    P.parth2osed = h->m_out[1];
+    P.parthno3sed = h->m_out[2];
+    P.sza3d = h->m_out[3];
+    P.surfarea = h->m_out[4];
+    step_const(h, daynum, dt, P.sc);
+}
+
+// rows r0..r0+nr-1 of P's range as the window of the per-cell kernels
+static void set_window(Params& P, int r0, int nr) {
+    P.win_r0 = r0;
+    P.win_nr = nr;
+    P.win_ncol = P.nlon * nr;
+    P.win_ncell = P.win_ncol * P.nivbas;
+}
+
+// A Newton step through the host arrays in row chunks. The rate stage and
+// plain start of chunk c run as soon as its rows are in (stream cin). The
+// cells of chunks 0 .. nchunk-2 and those of the last chunk then form two
+// work queues, solved one after the other by the persistent kernel: the
+// write-back of the first chunks and their copies out (stream cout) run
+// while the last chunk is solved, so that only its write-back and copy out
+// follow the solve. Chunk c holds rows ilat0 + nrows c / nchunk ..
+// ilat0 + nrows (c + 1) / nchunk - 1.
+static int host_step_newton(Handle* h, const HostArrays& A, int ilat0, int ilat1, int nchunk, double daynum,
+                            double dt, reprobus_stats* st) {
+    const bool mixed = h->solver == REPROBUS_SOLVER_NEWTON_MIXED;
+    const int nrows = ilat1 - ilat0 + 1, tb = 128;
+    Params P;
+    mirror_params(h, P, ilat0, ilat1, daynum, dt);
+    P.fuse = (h->flags & REPROBUS_FUSE_CONSERV) ? 1 : 0;
+    P.check = (h->flags & REPROBUS_CHECK_FINITE) ? 1 : 0;
+    int rc = newton_prepare(h, P);
+    if (rc) return rc;
+    auto row0 = [&](int c) { return ilat0 + (int)((long long)nrows * c / nchunk); };
+    // queue of the first chunks (heads nt_head[0..2]) and of the last (nt_head[4..6])
+    Params PA = P, PB = P;
+    PA.nt_qcap = P.nlon * (row0(nchunk - 1) - ilat0) * P.nivbas;
+    PB.nt_qcap = P.ncell - PA.nt_qcap;
+    PB.nt_list = P.nt_list + PA.nt_qcap;
+    PB.nt_head = P.nt_head + 4;
+    const bool tail = P.fuse && h->nivbas < h->niv;
+    int launches = 0;
+    if (st) CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+    CUDA_TRY(cudaMemsetAsync(h->d_count, 0, 8 * sizeof(unsigned long long), h->stream));
+    CUDA_TRY(cudaMemsetAsync(h->nt_head, 0, 8 * sizeof(int), h->stream));
+    for (int c = 0; c < nchunk; c++) {
+        const int a = row0(c), b = row0(c + 1) - 1;
+        if ((rc = host_rows_in(h, A, a - 1, b - a + 1, h->cin))) return rc;
+        CUDA_TRY(cudaEventRecord(h->ev_in[c], h->cin));
+        CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_in[c], 0));
+        Params& Q = c < nchunk - 1 ? PA : PB;
+        set_window(Q, a - ilat0, b - a + 1);
+        k_columns<<<(Q.win_ncol + tb - 1) / tb, tb, 0, h->stream>>>(Q);
+        newton_front(h, Q, mixed);
+        launches += mixed ? 4 : 3;
+    }
+    set_window(P, 0, nrows);
+    if (h->mlp) {
+        if ((rc = newton_warm(h, P))) return rc;
+        launches += 2;
+    }
+    for (int part = 0; part < 2; part++) {
+        Params& Q = part == 0 ? PA : PB;
+        if ((rc = newton_solve(h, Q, st ? (part ? h->ev4 : h->ev2) : nullptr, st ? (part ? h->ev5 : h->ev3) : nullptr,
+                               false)))
+            return rc;
+        launches++;
+        for (int c = part == 0 ? 0 : nchunk - 1; c < (part == 0 ? nchunk - 1 : nchunk); c++) {
+            const int a = row0(c), b = row0(c + 1) - 1;
+            set_window(Q, a - ilat0, b - a + 1);
+            newton_back(h, Q);
+            launches += 2;
+            if (tail) {
+                const long long nt = (long long)Q.nlon * Q.win_nr * (h->niv - h->nivbas);
+                k_tail<<<(unsigned)((nt + 255) / 256), 256, 0, h->stream>>>(Q);
+                launches++;
+            }
+            CUDA_TRY(cudaGetLastError());
+            CUDA_TRY(cudaEventRecord(h->ev_comp[c], h->stream));
+            CUDA_TRY(cudaStreamWaitEvent(h->cout, h->ev_comp[c], 0));
+            if ((rc = host_rows_out(h, A, a - 1, b - a + 1, h->cout))) return rc;
+        }
+    }
+    rc = step_stats(h, P, st, launches, false);
+    if (!rc && st) {  // the two solves
+        float sb = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&sb, h->ev4, h->ev5));
+        st->solve_ms += sb;
+    }
+    return rc;
+}
+
 extern "C" int reprobus_chem_step(void* handle, int ilat0, int ilat1, double daynum, double dt, const double* alt,
                                   const double* trajlon, const double* trajlat, const double* trajpre,
                                   const double* trajtem, int irapp, double* qj1, double* hc, double* vsed3d,
@@ -1554,13 +1724,22 @@ extern "C" int reprobus_chem_step(void* handle, int ilat0, int ilat1, double day
                        {trajlon + (irapp - 1) * pl, trajlat + (irapp - 1) * pl, trajpre + (irapp - 1) * pl,
                         trajtem + (irapp - 1) * pl},
                        qj1, hc, vsed3d, parth2osed, parthno3sed, surfarea, sza3d};
-    // Rows in chunks: the copy of chunk c+1 in (stream cin) and of chunk c-1
-    // out (stream cout) run while chunk c integrates on the handle's stream;
-    // chunks touch disjoint rows of the device mirrors, and the order is
-    // carried by events (no kernel waits on another). Statistics, CHECK_FINITE
-    // and the first Newton step (autotuning) synchronise per chunk.
+    // Rows in chunks (4, or REPROBUS_HOST_CHUNKS): the copy of chunk c+1 in
+    // (stream cin) and of chunk c-1 out (stream cout) run while chunk c
+    // integrates on the handle's stream; chunks touch disjoint rows of the
+    // device mirrors, and the order is carried by events (no kernel waits on
+    // another). REF5, the first Newton step (its autotuning) and graph
+    // launches integrate chunk by chunk (statistics and CHECK_FINITE
+    // synchronise per chunk); a tuned Newton step runs in phases instead
+    // (host_step_newton).
     const int nrows = ilat1 - ilat0 + 1;
-    const int nchunk = nrows >= 4 * HOST_CHUNK_MIN_ROWS ? 4 : 1;
+    int want_chunks = 4;
+    if (const char* ev = getenv("REPROBUS_HOST_CHUNKS")) {
+        const int v = atoi(ev);
+        if (v >= 1 && v <= 4) want_chunks = v;
+    }
+    int nchunk = want_chunks;
+    while (nchunk > 1 && nrows < nchunk * HOST_CHUNK_MIN_ROWS) nchunk--;
     if (nchunk > 1 && !h->cin) {
         CUDA_TRY(cudaStreamCreateWithFlags(&h->cin, cudaStreamNonBlocking));
         CUDA_TRY(cudaStreamCreateWithFlags(&h->cout, cudaStreamNonBlocking));
@@ -1581,6 +1760,15 @@ extern "C" int reprobus_chem_step(void* handle, int ilat0, int ilat1, double day
         cudaStreamSynchronize(cout);
         return code;
     };
+    // Newton solvers, once their solve kernel is tuned (the tuning times
+    // candidates on cells already on the device) and without a graph: one
+    // solve over all chunks
+    const int ip = h->solver == REPROBUS_SOLVER_NEWTON_MIXED ? 0 : 1;
+    if (nchunk > 1 && h->solver != REPROBUS_SOLVER_REF5 && !(h->flags & REPROBUS_USE_GRAPH) && h->nt_var[ip]) {
+        if ((rc = host_step_newton(h, A, ilat0, ilat1, nchunk, daynum, dt, stats))) return fail(rc);
+        CUDA_TRY(cudaStreamSynchronize(cout));
+        return REPROBUS_OK;
+    }
     for (int c = 0; c < nchunk; c++) {
         const int a = ilat0 + (int)((long long)nrows * c / nchunk);
         const int b = ilat0 + (int)((long long)nrows * (c + 1) / nchunk) - 1;
@@ -1590,21 +1778,7 @@ extern "C" int reprobus_chem_step(void* handle, int ilat0, int ilat1, double day
             CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_in[c], 0));
         }
         Params P;
-        fill_params(h, P, a, b);
-        P.trajoff = 0;
-        P.alt = h->m_alt;
-        P.trajlon = h->m_traj[0];
-        P.trajlat = h->m_traj[1];
-        P.trajpre = h->m_traj[2];
-        P.trajtem = h->m_traj[3];
-        P.qj1 = h->m_qj1;
-        P.hc = h->m_hc;
-        P.vsed3d = h->m_out[0];
-        P.parth2osed = h->m_out[1];
-        P.parthno3sed = h->m_out[2];
-        P.sza3d = h->m_out[3];
-        P.surfarea = h->m_out[4];
-        step_const(h, daynum, dt, P.sc);
+        mirror_params(h, P, a, b, daynum, dt);
         if ((rc = launch_step(h, P, stats ? &one : nullptr))) return fail(rc);
         if (stats) add_stats(&acc, one, c == 0);
         if (nchunk > 1) {

@@ -16,6 +16,9 @@ struct Params {
     long long trajoff;         // element offset of the irapp slice in traj*
     int niter, fuse, check;
     int ncell, ncol;           // nlon*nrows*nivbas, nlon*nrows
+    int win_r0, win_nr;        // row window of the per-cell kernels (rows of the range)
+    int win_ncell, win_ncol;   // nlon*win_nr*nivbas, nlon*win_nr
+    int nt_qcap;               // entries of the work queue nt_list (day from the front, night from the back)
     const double* __restrict__ alt;
     const double* __restrict__ trajlon;
     const double* __restrict__ trajlat;

@@ -30,7 +30,7 @@ __device__ __forceinline__ void nt_load_fix(const T* r, NtFixT<T>& F) {
 
 // entry q of the queue: day cells at list[0 .. nday), night cells from the back
 __device__ __forceinline__ int nt_queue_cell(const Params& P, int q, int nday) {
-    return q < nday ? P.nt_list[q] : P.nt_list[P.ncell - 1 - (q - nday)];
+    return q < nday ? P.nt_list[q] : P.nt_list[P.nt_qcap - 1 - (q - nday)];
 }
 
 // The end of an attempt of a lane's cell (done: iterations when converged, -1

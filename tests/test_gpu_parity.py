@@ -205,30 +205,51 @@ def test_reference_shaped_interface(torch):
     _compare(st, ref)
 
 
-@pytest.mark.parametrize("solver", ["ref5", "mixed"])
-def test_host_entry_in_row_chunks_equals_device_entry(torch, solver):
+@pytest.mark.parametrize("solver", ["ref5", "mixed", "fp64", "mlp"])
+@pytest.mark.parametrize("chunks", ["4", "3"])
+def test_host_entry_in_row_chunks_equals_device_entry(torch, solver, chunks, monkeypatch):
     """The host-array entry point pipelines calls of 32 rows or more in row
-    chunks (copies of one chunk overlapping the integration of another): the
-    result is bit for bit the device-array entry point's on the same grid."""
-    from reprobus_gb300.chem import SOLVER_NEWTON_MIXED, SOLVER_REF5
+    chunks (copies of one chunk overlapping the integration of another); once
+    a Newton solver is tuned, its step runs in phases (rate stage and start
+    chunk by chunk, one solve over all rows, write-back chunk by chunk). Both
+    the first (chunk by chunk) and the second (phased) host step are bit for
+    bit the device-array entry point's on the same grid, and so are the
+    solver statistics."""
+    from reprobus_gb300 import mlp as mlpmod
+    from reprobus_gb300.chem import SOLVER_NEWTON64, SOLVER_NEWTON_MIXED
     from reprobus_gb300.resident import DeviceCase
+    monkeypatch.setenv("REPROBUS_HOST_CHUNKS", chunks)
     case = inputs.make_case("grid", seed=41, nlon=12, nlat=40, nivbas=94)
-    outs = []
+    net = None
+    if solver == "mlp":
+        net = mlpmod.Mlp(batch_cap=128, seed=0)
+        net.load()
+    outs, stats = [], []
     for host in (True, False):
         h = ChemStep.for_case(case, niter=5, flags=FUSE_CONSERV)
-        if solver == "mixed":
+        if solver in ("mixed", "mlp"):
             h.set_solver(SOLVER_NEWTON_MIXED)
             h.set_tuning(64, 1, 0)
+        elif solver == "fp64":
+            h.set_solver(SOLVER_NEWTON64)
+            h.set_tuning(32, 1, 0)
+        if net is not None:
+            h.set_mlp(net)
         if host:
-            st = case.state_copy()
-            h.step(1, case.nlat, case.daynum, case.dt, case.alt, case.trajlon, case.trajlat, case.trajpre,
-                   case.trajtem, case.irapp, st["qj1"], st["hc"], st["vsed3d"], st["parth2osed"],
-                   st["parthno3sed"], st["surfarea"], st["sza3d"])
+            for _ in range(2):  # the second step takes the phased path
+                st = case.state_copy()
+                sd = h.step(1, case.nlat, case.daynum, case.dt, case.alt, case.trajlon, case.trajlat, case.trajpre,
+                            case.trajtem, case.irapp, st["qj1"], st["hc"], st["vsed3d"], st["parth2osed"],
+                            st["parthno3sed"], st["surfarea"], st["sza3d"])
+                outs.append(st)
+                stats.append(sd)
         else:
             dc = DeviceCase(case)
-            h.step_dev(1, case.nlat, case.daynum, case.dt, *dc.args(), stats=True)
-            st = dc.state_host()
+            stats.append(h.step_dev(1, case.nlat, case.daynum, case.dt, *dc.args(), stats=True))
+            outs.append(dc.state_host())
         h.close()
-        outs.append(st)
-    for f in FIELDS:
-        assert np.array_equal(outs[0][f], outs[1][f]), f
+    for k in (0, 1):
+        for f in FIELDS:
+            assert np.array_equal(outs[k][f], outs[2][f]), (k, f)
+        for key in ("ncells", "newton_iters", "fallbacks", "max_newton_iters", "warm_restarts", "nonfinite"):
+            assert stats[k][key] == stats[2][key], (k, key)
