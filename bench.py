@@ -408,7 +408,7 @@ def main():
         hrestore()
         hstep()
         torch.cuda.synchronize()
-        n_e2e = max(2, args.steps // 2)
+        n_e2e = max(3, args.steps)
         te = 0.0
         for _ in range(n_e2e):
             hrestore()
