@@ -1631,10 +1631,10 @@ static void set_window(Params& P, int r0, int nr) {
 // A Newton step through the host arrays in row chunks. The rate stage and
 // plain start of chunk c run as soon as its rows are in (stream cin). The
 // cells of chunks 0 .. nchunk-2 and those of the last chunk then form two
-// work queues, solved one after the other by the persistent kernel: the
-// write-back of the first chunks and their copies out (stream cout) run
-// while the last chunk is solved, so that only its write-back and copy out
-// follow the solve. Chunk c holds rows ilat0 + nrows c / nchunk ..
+// work queues, solved one after the other by the persistent kernel; the
+// write-back of the first chunks runs between the two solves and their
+// copies out (stream cout) during the second, so that only the last chunk's
+// write-back and copy out follow it. Chunk c holds rows ilat0 + nrows c / nchunk ..
 // ilat0 + nrows (c + 1) / nchunk - 1.
 static int host_step_newton(Handle* h, const HostArrays& A, int ilat0, int ilat1, int nchunk, double daynum,
                             double dt, reprobus_stats* st) {
