@@ -38,6 +38,7 @@ struct StepConst {
     double ut, eqh, srd, crd;  // zenith: UT hour, equation of time (h), sin/cos(declination)
     double dt;
     double troe[18];           // COMMON /constant/
+    double ltroe[18];          // ln troe[i] (0 where troe[i] <= 0)
 };
 
 // ----------------------------------------------------------------------------
@@ -577,20 +578,27 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
 // ----------------------------------------------------------------------------
 // rate constants, F:920-1306
 // ----------------------------------------------------------------------------
-__device__ __forceinline__ void cell_rates(const double* troe, double t, double hnm, double pm, double* K) {
+// Troe falloff: k0 = A0 T^E0, kinf = A1 T^E1, x = k0 n, k = x / (1 + x / kinf)
+// 0.6^(1 / (1 + log10(x / kinf)^2)). Here k = x kinf / (kinf + x) (one
+// division) and log10(x / kinf) = (ln A0 - ln A1 + ln n + (E0 - E1) ln T) / ln 10
+// from the step's ln A (no logarithm per term).
+__device__ __forceinline__ void cell_rates(const double* troe, const double* ltroe, double t, double hnm, double pm,
+                                           double* K) {
     const double xln6 = LN06;
     double lntemp = log(t);
+    const double lnhnm = log(hnm);
     const double rt = 1. / t;  // Arrhenius exponents E / T as E * (1 / T)
-    double ak0, ak1, rate, xpo, deq, l10;
+    double ak0, ak1, rate, xpo, deq, l10, xk;
 #define RK(name) K[K_##name]
-#define TROE(A0, E0, A1, E1, OUT)                \
-    ak0 = (A0) * exp(lntemp * (E0));             \
-    ak1 = (A1) * exp(lntemp * (E1));             \
-    rate = (ak0 * hnm) / (1. + ak0 * hnm / ak1); \
-    l10 = log10((ak0 * hnm) / ak1);              \
-    xpo = 1. / (1. + l10 * l10);                 \
+#define TROE(I0, E0, I1, E1, OUT)                                                            \
+    ak0 = troe[I0] * exp(lntemp * (E0));                                                     \
+    ak1 = troe[I1] * exp(lntemp * (E1));                                                     \
+    xk = ak0 * hnm;                                                                          \
+    rate = xk * ak1 / (ak1 + xk);                                                            \
+    l10 = (ltroe[I0] - ltroe[I1] + lnhnm + lntemp * ((E0) - (E1))) * (1. / LN10);           \
+    xpo = 1. / (1. + l10 * l10);                                                             \
     OUT = rate * exp(xln6 * xpo)
-    TROE(troe[0], -1.3, troe[1], 0.2, RK(a1));
+    TROE(0, -1.3, 1, 0.2, RK(a1));
     RK(a1et) = 1.63e-10 * exp(60. * rt);
     RK(a2) = 1.4e-10 * exp(-470. * rt);
     RK(a5) = 1.8e-11 * exp(180. * rt);
@@ -613,9 +621,9 @@ __device__ __forceinline__ void cell_rates(const double* troe, double t, double 
     RK(b7) = 1.5e-11 * exp((-3600. * rt));
     double em2450 = exp((-2450. * rt));
     RK(b9) = 1.2e-13 * em2450;
-    TROE(troe[2], -4.4, troe[3], -0.7, RK(b12));
-    TROE(troe[4], -3.0, troe[5], 0.0, RK(b22));
-    TROE(troe[6], -3.4, troe[7], -1.1, RK(b23));
+    TROE(2, -4.4, 3, -0.7, RK(b12));
+    TROE(4, -3.0, 5, 0.0, RK(b22));
+    TROE(6, -3.4, 7, -1.1, RK(b23));
     deq = 2.1e-27 * exp(10900. * rt);
     RK(b24) = RK(b23) / (deq * hnm);
     double e460 = exp(460. * rt);
@@ -635,7 +643,7 @@ __device__ __forceinline__ void cell_rates(const double* troe, double t, double 
     RK(c1c) = 0.09e-10;
     RK(c2) = 2.45e-12 * exp((-1775. * rt));
     RK(c3) = 1.1e-10;
-    TROE(troe[16], -3.6, troe[17], 1.1, RK(c4));
+    TROE(16, -3.6, 17, 1.1, RK(c4));
     RK(c5) = 2.8e-12 * exp((300. * rt));
     RK(c7) = 3.8e-13 * exp((800. * rt));
     RK(c8) = 5.5e-12 * exp(125. * rt);
@@ -662,15 +670,15 @@ __device__ __forceinline__ void cell_rates(const double* troe, double t, double 
     RK(d9) = 6.0e-13 * e230;
     RK(d10) = 3.6e-11 * exp(-375. * rt);
     RK(d11) = 1.8e-12 * exp((-250. * rt));
-    TROE(troe[8], -3.4, troe[9], -1.9, RK(d31));
+    TROE(8, -3.4, 9, -1.9, RK(d31));
     double em840 = exp((-840. * rt));
     RK(d32) = 3.6e-12 * em840;
     RK(d33) = 2.6e-12 * e290;
     RK(d34) = 3.0e-12 * exp((-500. * rt));
     RK(d35) = 1.7e-13;
-    TROE(troe[10], -2., troe[11], -1., RK(d36));
+    TROE(10, -2., 11, -1., RK(d36));
     RK(d37) = 3.4e-12 * exp((-130. * rt));
-    TROE(troe[12], -4.5, troe[13], -2.0, RK(d60));
+    TROE(12, -4.5, 13, -2.0, RK(d60));
     deq = 1.72e-27 * exp(8649. * rt);
     RK(d61) = RK(d60) / (deq * hnm);
     RK(d62) = 1.0e-12 * exp(-1590. * rt) + 3.0e-11 * em2450;
@@ -695,7 +703,7 @@ __device__ __forceinline__ void cell_rates(const double* troe, double t, double 
     RK(e9) = 1.5e-10;
     RK(e10) = 1.7e-11 * e250;
     RK(e11) = 5.5e-12 * e200;
-    TROE(troe[14], -3.2, troe[15], -2.9, RK(e13));
+    TROE(14, -3.2, 15, -2.9, RK(e13));
     RK(e15) = 4.5e-12 * e460;
     RK(e16) = 1.2e-10 * exp((-430. * rt));
     RK(e50) = 1.8e-10;

@@ -209,7 +209,7 @@ __device__ __forceinline__ void cell_prologue(const Params& P, int cell, CellPro
     }
     if (LS) __syncthreads();
     // rate constants F:920-1306
-    cell_rates(P.sc.troe, t, F.hnm, pm, C.K);
+    cell_rates(P.sc.troe, P.sc.ltroe, t, F.hnm, pm, C.K);
     // rainout F:1315-1338
     const double rain_rate = 1.e-6;
     const bool rain = C.ck0[2] / F.hnm >= 100.e-6;
@@ -926,6 +926,7 @@ static void step_const(const Handle* h, double day, double dt, StepConst& sc) {
     sc.crd = cos(rdecl);
     sc.dt = dt;
     memcpy(sc.troe, h->troe, sizeof(sc.troe));
+    for (int i = 0; i < 18; i++) sc.ltroe[i] = sc.troe[i] > 0. ? log(sc.troe[i]) : 0.;
 }
 
 static int check_rows(const Handle* h, int ilat0, int ilat1) {
