@@ -86,6 +86,7 @@ enum {
 typedef struct work {
     int nl, nb;          /* lons in block, chemistry levels */
     size_t n;            /* nl*nb */
+    size_t nd;           /* n-sized double planes in base (4 int planes in ibase) */
     double* base;
     int* ibase;
     /* chem3d */
@@ -115,6 +116,7 @@ static work* work_alloc(int nl, int nb) {
     /* count of n-sized double arrays */
     size_t nd = 7 + NBCON + NBCON + NCM + 2 + NPHOT + 9 + 5 + 2 + NBCON + NBCON + K_COUNT + 7 + 3 + NCM +
                 NBCON + 27 + 18 + 3 + 1 + 3 + 3;
+    w->nd = nd;
     w->base = (double*)calloc(nd * n, sizeof(double));
     w->ibase = (int*)calloc(4 * n, sizeof(int));
     double* p = w->base;
@@ -150,6 +152,17 @@ static void work_free(work* w) {
     free(w->base);
     free(w->ibase);
     free(w);
+}
+
+/* A workspace of the m cells idx[0..m) of w: every per-cell plane is copied,
+ * so a pass (which works cell by cell) gives on it what it gives on w. */
+static work* work_subset(const work* w, const size_t* idx, size_t m) {
+    work* s = work_alloc((int)m, 1);
+    for (size_t p = 0; p < w->nd; p++)
+        for (size_t j = 0; j < m; j++) s->base[p * m + j] = w->base[p * w->n + idx[j]];
+    for (size_t p = 0; p < 4; p++)
+        for (size_t j = 0; j < m; j++) s->ibase[p * m + j] = w->ibase[p * w->n + idx[j]];
+    return s;
 }
 
 #define R(i, k) ((size_t)(i) + (size_t)nl * (size_t)(k))
@@ -1396,13 +1409,34 @@ static void orc_pass(const orc_grid* g, double dt, work* w) {
  * Oracle-C: the fixed point of one pass of the iteration (F:1350-2372),
  * G(x) = x with x = (ck(1..42), cc(1..15)), by Newton's method on
  * F(x) = G(x) - x. The Jacobian of G is taken by forward differences of the
- * pass itself (all cells of the block perturbed at once: cells are
- * independent within a pass), each cell's 57x57 system is solved by LU with
- * partial pivoting, and a step that does not reduce max|F|/scale is halved
- * (up to 8 times). Converged when |G(x) - x| is below tol relative to
+ * pass itself (cells are independent within a pass, so all cells of a
+ * workspace are perturbed at once), each cell's 57x57 system is solved by LU
+ * with partial pivoting. Converged when |G(x) - x| is below tol relative to
  * max(|x|, 1e-40*hnm) for every unknown (the night NO2 fixed point sits near
  * 1e-30 molecules/cm3, inside the max(NO2, 1e-30) of F:1722, and NO3
  * depends on which side of that clamp NO2 is).
+ *
+ * Newton from the reference's 5-pass state does not converge in every cell:
+ * where the pass map oscillates (warm cells at high pressure, some polar
+ * night cells) that state can lie outside Newton's basin. A cell that has not
+ * converged moves on to the next start of a fixed sequence, and the first
+ * start whose iteration converges gives its answer:
+ *   stage 1  Newton from the 5-pass state (the reference's own answer);
+ *   stage 2  Newton from the step's initial state (no pass);
+ *   stage 3-5  Newton from the 1-, 2- and 3-pass states;
+ *   stage 6  pseudo-transient continuation from the 5-pass state:
+ *            (I/d - F'(x)) dx = F(x), d grown by the ratio of successive
+ *            residuals (switched evolution relaxation), i.e. relaxed passes
+ *            that turn into Newton steps as the residual falls.
+ * Newton steps are halved while they raise the residual (up to 8 times);
+ * a continuation step is shortened as a whole so that no component falls
+ * below a tenth of its value (stepping component by component towards zero
+ * finds spurious roots with Br radicals near 1e-120); in every stage a
+ * component still driven negative is set to a tenth of its previous value.
+ * Some night cells have two fixed points (NO2 on either side of the clamp);
+ * the sequence takes the one reached from the state nearest the reference's
+ * passes first. Each stage works on a compacted copy of the cells still
+ * iterating, so converged cells cost nothing.
  * ========================================================================== */
 #define NX (NBCON - 1 + NCM)
 
@@ -1415,7 +1449,7 @@ static void put_x(work* w, size_t c, const double* x) {
     for (int m = 0; m < NCM; m++) w->cc[c + w->n * m] = x[NBCON - 1 + m];
 }
 
-/* G for every cell of the block at the states X (n x NX), into GX */
+/* G for every cell of the workspace at the states X (n x NX), into GX */
 static void block_map(const orc_grid* g, double dt, work* w, const double* X, double* GX) {
     for (size_t c = 0; c < w->n; c++) put_x(w, c, X + c * NX);
     orc_pass(g, dt, w);
@@ -1456,103 +1490,205 @@ static int lu_solve(double* A, double* b, int n) {
 }
 
 static const double g_floor = 1e-40;
-static double fnorm(const double* x, const double* gx, const double* floorv) {
+/* max_i |G(x)_i - x_i| / max(|x_i|, fl); NaN gives NaN (never converged) */
+static double fnorm(const double* x, const double* gx, double fl) {
     double m = 0.;
     for (int i = 0; i < NX; i++) {
-        double s = fmax(fabs(x[i]), floorv[i]);
+        double s = fmax(fabs(x[i]), fl);
         double r = fabs(gx[i] - x[i]) / s;
-        if (!(r <= m)) m = r; /* NaN propagates as failure */
+        if (!(r <= m)) m = r;
     }
     return m;
 }
 
-static void orc_newton_block(const orc_grid* g, double dt, work* w, int* iters, double* res) {
-    const size_t n = w->n;
-    double* X = (double*)malloc(sizeof(double) * n * NX);
-    double* GX = (double*)malloc(sizeof(double) * n * NX);
-    double* XP = (double*)malloc(sizeof(double) * n * NX);
-    double* GP = (double*)malloc(sizeof(double) * n * NX);
-    double* J = (double*)malloc(sizeof(double) * n * NX * NX);
-    double* FL = (double*)malloc(sizeof(double) * n * NX);
-    double* H = (double*)malloc(sizeof(double) * n * NX);
-    int* done = (int*)calloc(n, sizeof(int));
-    for (size_t c = 0; c < n; c++) {
-        get_x(w, c, X + c * NX);
-        for (int i = 0; i < NX; i++) FL[c * NX + i] = g_floor * w->hnm[c];
-        iters[c] = 0;
+enum { STAGE_NEWTON = 0, STAGE_PTC = 1 };
+
+/* One stage over the cells act[0..na) of the block workspace w, each
+ * starting from its row of Xb (n x NX, in/out). A converged cell gets
+ * conv = stage_id, its iterate in Xb, its Newton steps added to iters and its
+ * residual in res. Returns the cells still unconverged, left in act. */
+static size_t newton_stage(const orc_grid* g, double dt, const work* w, size_t* act, size_t na, double* Xb,
+                           int mode, int stage_id, int maxit, int* iters, double* res, int* conv) {
+    if (!na) return 0;
+    work* ws = work_subset(w, act, na);
+    size_t m = na;
+    size_t* loc = (size_t*)malloc(sizeof(size_t) * na);  /* block index of each workspace cell */
+    size_t* keep = (size_t*)malloc(sizeof(size_t) * na);
+    double* X = (double*)malloc(sizeof(double) * na * NX);
+    double* GX = (double*)malloc(sizeof(double) * na * NX);
+    double* XP = (double*)malloc(sizeof(double) * na * NX);
+    double* GP = (double*)malloc(sizeof(double) * na * NX);
+    double* J = (double*)malloc(sizeof(double) * na * NX * NX);
+    double* H = (double*)malloc(sizeof(double) * na);
+    double* D = (double*)malloc(sizeof(double) * na);  /* PTC pseudo time step */
+    double* F0 = (double*)malloc(sizeof(double) * na); /* residual at X */
+    int* dead = (int*)calloc(na, sizeof(int));
+    for (size_t c = 0; c < na; c++) {
+        loc[c] = act[c];
+        memcpy(X + c * NX, Xb + act[c] * NX, sizeof(double) * NX);
+        D[c] = 0.5;
     }
-    const int maxit = g->maxiter > 0 ? g->maxiter : 60;
-    for (int it = 0; it < maxit; it++) {
-        block_map(g, dt, w, X, GX);
-        int active = 0;
-        for (size_t c = 0; c < n; c++) {
-            if (done[c]) continue;
-            if (fnorm(X + c * NX, GX + c * NX, FL + c * NX) < g->tol) {
-                done[c] = 1;
+    block_map(g, dt, ws, X, GX);
+    size_t left = 0;
+    for (int it = 0;; it++) {
+        /* convergence test; keep the cells still iterating */
+        size_t k = 0;
+        for (size_t c = 0; c < m; c++) {
+            const double f = fnorm(X + c * NX, GX + c * NX, g_floor * ws->hnm[c]);
+            const size_t b = loc[c];
+            if (f < g->tol) {
+                conv[b] = stage_id;
+                iters[b] += it;
+                res[b] = f;
+                memcpy(Xb + b * NX, X + c * NX, sizeof(double) * NX);
                 continue;
             }
-            active++;
+            if (it == maxit || dead[c]) {
+                res[b] = f;
+                iters[b] += it;
+                act[left++] = b;
+                continue;
+            }
+            F0[k] = f;
+            keep[k] = c;
+            if (k != c) {
+                memcpy(X + k * NX, X + c * NX, sizeof(double) * NX);
+                memcpy(GX + k * NX, GX + c * NX, sizeof(double) * NX);
+                D[k] = D[c];
+                loc[k] = loc[c];
+                dead[k] = 0;
+            }
+            k++;
         }
-        if (!active) break;
+        if (k == 0) break;
+        if (k < m) {
+            work* w2 = work_subset(ws, keep, k);
+            work_free(ws);
+            ws = w2;
+            m = k;
+        }
         /* forward-difference Jacobian of G, column j for all cells at once */
         for (int j = 0; j < NX; j++) {
-            memcpy(XP, X, sizeof(double) * n * NX);
-            for (size_t c = 0; c < n; c++) {
-                double xj = X[c * NX + j];
-                double h = 1e-7 * fmax(fabs(xj), FL[c * NX + j] * 1e5);
-                H[c * NX + j] = h;
+            memcpy(XP, X, sizeof(double) * m * NX);
+            for (size_t c = 0; c < m; c++) {
+                const double xj = X[c * NX + j];
+                const double h = 1e-7 * fmax(fabs(xj), g_floor * 1e5 * ws->hnm[c]);
+                H[c] = h;
                 XP[c * NX + j] = xj + h;
             }
-            block_map(g, dt, w, XP, GP);
-            for (size_t c = 0; c < n; c++)
+            block_map(g, dt, ws, XP, GP);
+            for (size_t c = 0; c < m; c++)
                 for (int i = 0; i < NX; i++)
-                    J[(c * NX + i) * NX + j] = (GP[c * NX + i] - GX[c * NX + i]) / H[c * NX + j];
+                    J[(c * NX + i) * NX + j] = (GP[c * NX + i] - GX[c * NX + i]) / H[c];
         }
-        /* Newton steps (J_G - I) d = -(G - x), with halving */
-        for (size_t c = 0; c < n; c++) {
-            if (done[c]) continue;
+        /* the step: Newton (J_G - I) dx = -(G - x); PTC (I/d - (J_G - I)) dx = G - x */
+        for (size_t c = 0; c < m; c++) {
             double* A = J + c * NX * NX;
-            double b[NX], x0[NX];
+            double bb[NX];
             for (int i = 0; i < NX; i++) {
-                A[i * NX + i] -= 1.;
-                b[i] = -(GX[c * NX + i] - X[c * NX + i]);
-                x0[i] = X[c * NX + i];
-            }
-            if (lu_solve(A, b, NX) != 0) {
-                done[c] = -1;
-                continue;
-            }
-            for (int i = 0; i < NX; i++) X[c * NX + i] = x0[i] + b[i];
-            iters[c] = it + 1;
-            memcpy(XP + c * NX, x0, sizeof(double) * NX);  /* keep the previous iterate */
-        }
-        /* halve steps that increase the residual */
-        block_map(g, dt, w, X, GP);
-        for (int half = 0; half < 8; half++) {
-            int any = 0;
-            for (size_t c = 0; c < n; c++) {
-                if (done[c]) continue;
-                double fn_new = fnorm(X + c * NX, GP + c * NX, FL + c * NX);
-                double fn_old = fnorm(XP + c * NX, GX + c * NX, FL + c * NX);
-                if (!(fn_new <= fn_old) && fn_new > g->tol) {
-                    for (int i = 0; i < NX; i++)
-                        X[c * NX + i] = 0.5 * (X[c * NX + i] + XP[c * NX + i]);
-                    any = 1;
+                const double fi = GX[c * NX + i] - X[c * NX + i];
+                if (mode == STAGE_PTC) {
+                    for (int q = 0; q < NX; q++) A[i * NX + q] = -A[i * NX + q];
+                    A[i * NX + i] += 1. + 1. / D[c];
+                    bb[i] = fi;
+                } else {
+                    A[i * NX + i] -= 1.;
+                    bb[i] = -fi;
                 }
             }
-            if (!any) break;
-            block_map(g, dt, w, X, GP);
+            memcpy(XP + c * NX, X + c * NX, sizeof(double) * NX); /* the previous iterate */
+            if (lu_solve(A, bb, NX) != 0) {
+                dead[c] = 1;
+                continue;
+            }
+            double lam = 1.;
+            if (mode == STAGE_PTC) /* the whole step shortened: no component below a tenth */
+                for (int i = 0; i < NX; i++) {
+                    const double x0 = X[c * NX + i];
+                    if (x0 > 0. && x0 + bb[i] < 0.1 * x0) lam = fmin(lam, -0.9 * x0 / bb[i]);
+                }
+            for (int i = 0; i < NX; i++) {
+                const double x0 = X[c * NX + i];
+                const double xn = x0 + lam * bb[i];
+                X[c * NX + i] = xn < 0. ? x0 / 10. : xn;
+            }
         }
+        block_map(g, dt, ws, X, GP);
+        if (mode == STAGE_PTC) {
+            for (size_t c = 0; c < m; c++) {
+                const double fn_new = fnorm(X + c * NX, GP + c * NX, g_floor * ws->hnm[c]);
+                double r = fn_new > 0. ? F0[c] / fn_new : 1e10;
+                if (!(r <= 1e10)) r = 1e10;
+                D[c] = fmin(fmax(D[c] * r, 1e-3), 1e12);
+            }
+        } else {
+            /* halve steps that raise the residual */
+            for (int half = 0; half < 8; half++) {
+                int any = 0;
+                for (size_t c = 0; c < m; c++) {
+                    if (dead[c]) continue;
+                    const double fn_new = fnorm(X + c * NX, GP + c * NX, g_floor * ws->hnm[c]);
+                    if (!(fn_new <= F0[c]) && fn_new > g->tol) {
+                        for (int i = 0; i < NX; i++) X[c * NX + i] = 0.5 * (X[c * NX + i] + XP[c * NX + i]);
+                        any = 1;
+                    }
+                }
+                if (!any) break;
+                block_map(g, dt, ws, X, GP);
+            }
+        }
+        memcpy(GX, GP, sizeof(double) * m * NX);
     }
-    block_map(g, dt, w, X, GX);
+    work_free(ws);
+    free(loc); free(keep); free(X); free(GX); free(XP); free(GP); free(J); free(H); free(D); free(F0);
+    free(dead);
+    return left;
+}
+
+/* Oracle-C over one block: X0 holds every cell's state before the passes
+ * (n x NX); w holds the 5-pass state. With X0 NULL (a given start state in
+ * w) only stage 1 runs: Newton from that state, to the fixed point nearest
+ * it. On return w holds each converged cell's fixed point and each
+ * unconverged cell's start state. Per cell:
+ * iters = Newton steps over all stages (-steps-1 if not converged),
+ * res = the final residual, stage = the stage that converged (0: none). */
+static void orc_newton_block(const orc_grid* g, double dt, work* w, const double* X0, int* iters, double* res,
+                             int* stage) {
+    const size_t n = w->n;
+    double* X5 = (double*)malloc(sizeof(double) * n * NX);
+    double* Xb = (double*)malloc(sizeof(double) * n * NX);
+    size_t* act = (size_t*)malloc(sizeof(size_t) * n);
     for (size_t c = 0; c < n; c++) {
-        res[c] = fnorm(X + c * NX, GX + c * NX, FL + c * NX);
-        if (done[c] != 1 && !(res[c] < g->tol)) {
-            iters[c] = -abs(iters[c]) - 1;
-        }
-        put_x(w, c, X + c * NX); /* the iterate itself, not one more pass */
+        get_x(w, c, X5 + c * NX);
+        act[c] = c;
+        iters[c] = 0;
+        stage[c] = 0;
     }
-    free(X); free(GX); free(XP); free(GP); free(J); free(FL); free(H); free(done);
+    memcpy(Xb, X5, sizeof(double) * n * NX);
+    const int maxit = g->maxiter > 0 ? g->maxiter : 60;
+    size_t na = newton_stage(g, dt, w, act, n, Xb, STAGE_NEWTON, 1, maxit, iters, res, stage);
+    for (int np = 0; np <= 3 && na && X0; np++) {
+        /* restart from the np-pass state */
+        work* ws = work_subset(w, act, na);
+        for (size_t c = 0; c < na; c++) put_x(ws, c, X0 + act[c] * NX);
+        for (int p = 0; p < np; p++) orc_pass(g, dt, ws);
+        for (size_t c = 0; c < na; c++) get_x(ws, c, Xb + act[c] * NX);
+        work_free(ws);
+        na = newton_stage(g, dt, w, act, na, Xb, STAGE_NEWTON, 2 + np, 40, iters, res, stage);
+    }
+    if (na && X0) {
+        for (size_t c = 0; c < na; c++) memcpy(Xb + act[c] * NX, X5 + act[c] * NX, sizeof(double) * NX);
+        na = newton_stage(g, dt, w, act, na, Xb, STAGE_PTC, 6, 4 * maxit, iters, res, stage);
+    }
+    for (size_t c = 0; c < n; c++) {
+        if (stage[c] == 0) {
+            iters[c] = -iters[c] - 1;
+            put_x(w, c, X5 + c * NX);
+        } else {
+            put_x(w, c, Xb + c * NX);
+        }
+    }
+    free(X5); free(Xb); free(act);
 }
 
 /* ============================================================================
@@ -1664,32 +1800,39 @@ static int orc_chem3d_block(const orc_grid* g, work* w, int ilat, int i0, double
 #undef DG
             }
     }
-    /* ---- map-residual mode: one pass from the given state x ---- */
-    if (g->x_qj1 && g->x_hc) {
+    /* ---- given state x: one pass from it (map residual), or Newton from it ---- */
+    const int given = g->x_qj1 && g->x_hc;
+    if (given) {
         for (int m = 0; m < NBCON - 1; m++)
             for (int k = 0; k < nb; k++)
                 for (int i = 0; i < nl; i++) w->ck[R(i, k) + n * m] = G4(g->x_qj1, i0 + i, ilat, k, m) * w->hnm[R(i, k)];
         for (int m = 0; m < NCM; m++)
             for (int k = 0; k < nb; k++)
                 for (int i = 0; i < nl; i++) w->cc[R(i, k) + n * m] = G4(g->x_hc, i0 + i, ilat, k, m) * w->hnm[R(i, k)];
+    }
+    if (given && !g->newton) {
         double* X0 = (double*)malloc(sizeof(double) * n * NX);
         for (size_t c = 0; c < n; c++) get_x(w, c, X0 + c * NX);
         orc_pass(g, dt, w);
         for (size_t c = 0; c < n; c++) {
-            double gx[NX], fl[NX];
+            double gx[NX];
             get_x(w, c, gx);
-            for (int q = 0; q < NX; q++) fl[q] = 1e-20 * w->hnm[c];
             if (g->cellres) {
                 const size_t cell = (size_t)(i0 + c % nl) + (size_t)g->nlon * ((size_t)ilat + (size_t)g->nlat * (c / nl));
-                g->cellres[cell] = fnorm(X0 + c * NX, gx, fl);
+                g->cellres[cell] = fnorm(X0 + c * NX, gx, 1e-20 * w->hnm[c]);
             }
         }
         free(X0);
     }
     /* ---- iteration, F:1348-2378 ---- */
+    double* Xstart = NULL; /* Oracle-C restarts from the state before the passes */
+    if (g->newton && !given) {
+        Xstart = (double*)malloc(sizeof(double) * n * NX);
+        for (size_t c = 0; c < n; c++) get_x(w, c, Xstart + c * NX);
+    }
     int passes = 0;
-    if (g->x_qj1 && g->x_hc) {
-        passes = 1;
+    if (given) {
+        passes = g->newton ? 0 : 1;
     } else if (g->niter > 0) {
         for (int it = 0; it < g->niter; it++) orc_pass(g, dt, w);
         passes = g->niter;
@@ -1715,19 +1858,24 @@ static int orc_chem3d_block(const orc_grid* g, work* w, int ilat, int i0, double
         }
     }
     if (g->newton) {
-        /* Oracle-C: from the passes' result, Newton to the fixed point */
+        /* Oracle-C: from the passes' result (or from the given state),
+         * Newton to the fixed point */
         int* it = (int*)malloc(sizeof(int) * n);
+        int* stg = (int*)malloc(sizeof(int) * n);
         double* res = (double*)malloc(sizeof(double) * n);
-        orc_newton_block(g, dt, w, it, res);
+        orc_newton_block(g, dt, w, Xstart, it, res, stg);
         for (int k = 0; k < nb; k++)
             for (int i = 0; i < nl; i++) {
                 const size_t cell = (size_t)(i0 + i) + (size_t)g->nlon * ((size_t)ilat + (size_t)g->nlat * k);
                 if (g->cellstat) g->cellstat[cell] = it[R(i, k)];
                 if (g->cellres) g->cellres[cell] = res[R(i, k)];
+                if (g->cellstage) g->cellstage[cell] = stg[R(i, k)];
             }
         free(it);
+        free(stg);
         free(res);
     }
+    free(Xstart);
     /* ---- write-back, F:2380-2410 ---- */
     for (int m = 0; m < NBCON - 1; m++)
         for (int k = 0; k < nb; k++)

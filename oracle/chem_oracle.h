@@ -34,12 +34,17 @@ typedef struct orc_grid {
     double troe[18];       /* COMMON /constant/                                  */
     int newton;            /* 1: after niter passes, Newton on the pass map to tol */
     int* cellstat;         /* nullable, per chemistry cell (diag layout): Newton
-                              iterations, negative when not converged            */
+                              steps over all stages, >= 0 when converged,
+                              -steps-1 when not                                   */
     double* cellres;       /* nullable, per chemistry cell: final max|G(x)-x|/scale */
     const double* x_qj1;   /* nullable: evaluate one pass G at the state x =    */
     const double* x_hc;    /* (x_qj1, x_hc) (mixing ratios, full arrays) instead
                               of iterating; cellres gets max|G(x)-x|/scale and
-                              qj1/hc get G(x)                                     */
+                              qj1/hc get G(x). With newton set: Newton (stage 1
+                              alone) from x instead of from the 5-pass state     */
+    int* cellstage;        /* nullable, per chemistry cell: the Newton stage that
+                              converged (1: from the 5-pass state, 2-5: from the
+                              0/1/2/3-pass state, 6: continuation; 0: none)       */
 } orc_grid;
 
 /* const, :5927-5948 — fills the 18 Troe prefactors. */

@@ -39,6 +39,7 @@ class OrcGrid(ctypes.Structure):
         ("newton", ctypes.c_int), ("cellstat", ctypes.POINTER(ctypes.c_int)),
         ("cellres", ctypes.POINTER(ctypes.c_double)),
         ("x_qj1", ctypes.POINTER(ctypes.c_double)), ("x_hc", ctypes.POINTER(ctypes.c_double)),
+        ("cellstage", ctypes.POINTER(ctypes.c_int)),
     ]
 
 
@@ -99,16 +100,43 @@ def step(case, niter=5, fuse=True, diag=False, nthreads=0, ilat0=1, ilat1=None, 
     return _run(L, g, case, fuse, diag, nthreads, ilat0, ilat1, state)
 
 
-def step_fixed_point(case, tol=1e-13, maxiter=60, fuse=True, nthreads=0, ilat0=1, ilat1=None, state=None):
+def step_fixed_point(case, tol=1e-13, maxiter=60, fuse=True, nthreads=0, ilat0=1, ilat1=None, state=None,
+                     with_stage=False):
     """Oracle-C: the fixed point of the reference's pass map (5 passes, then
-    Newton on G(x) - x). Returns (state, cellstat, cellres): per chemistry cell
-    (diag layout) the Newton iterations (negative: not converged to tol) and
-    the final max |G(x) - x| / max(|x|, 1e-25 hnm)."""
+    Newton on G(x) - x, restarted from earlier pass states and finally by
+    pseudo-transient continuation where it does not converge). Returns
+    (state, cellstat, cellres[, cellstage]): per chemistry cell (diag layout)
+    the Newton steps over all stages (>= 0 when converged, -steps-1 when not),
+    the final max |G(x) - x| / max(|x|, 1e-40 hnm), and with with_stage the
+    stage that converged (1: from the 5-pass state, 2-5: from the 0/1/2/3-pass
+    state, 6: continuation, 0: none)."""
     L = lib()
-    stat = np.zeros(case.nlon * case.nlat * case.nivbas, dtype=np.int32)
-    res = np.zeros(case.nlon * case.nlat * case.nivbas)
+    nc = case.nlon * case.nlat * case.nivbas
+    stat = np.zeros(nc, dtype=np.int32)
+    res = np.zeros(nc)
+    stage = np.zeros(nc, dtype=np.int32)
     g = grid(case, niter=5, tol=tol, maxiter=maxiter, newton=True, cellstat=stat, cellres=res)
+    g.cellstage = stage.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
     st, _, _ = _run(L, g, case, fuse, False, nthreads, ilat0, ilat1, state)
+    return (st, stat, res, stage) if with_stage else (st, stat, res)
+
+
+def newton_from(case, qj1, hc, tol=1e-12, maxiter=60, nthreads=0):
+    """Oracle-C's Newton (stage 1 alone) started from the given state
+    x = (qj1, hc) instead of the 5-pass state: the FP64 fixed point of the
+    reference's pass map nearest x. Returns (state, cellstat, cellres) as
+    step_fixed_point does; a cell whose iteration converges with a state
+    within e of x shows that x lies within e of an exact fixed point."""
+    L = lib()
+    nc = case.nlon * case.nlat * case.nivbas
+    stat = np.zeros(nc, dtype=np.int32)
+    res = np.zeros(nc)
+    g = grid(case, niter=5, tol=tol, maxiter=maxiter, newton=True, cellstat=stat, cellres=res)
+    qx = np.asfortranarray(qj1)
+    hx = np.asfortranarray(hc)
+    g.x_qj1 = _p(qx)
+    g.x_hc = _p(hx)
+    st, _, _ = _run(L, g, case, False, False, nthreads, 1, None, None)
     return st, stat, res
 
 

@@ -173,6 +173,28 @@ class ChemCase:
                     parthno3sed=self.parthno3sed.copy(order="F"),
                     surfarea=self.surfarea.copy(order="F"), sza3d=self.sza3d.copy(order="F"))
 
+    GRID_ARRAYS = ("alt", "trajlon", "trajlat", "trajpre", "trajtem", "qj1", "hc", "surfarea", "vsed3d",
+                   "parth2osed", "parthno3sed", "sza3d")
+
+    def columns(self, ilon, ilat):
+        """The columns (ilon[c], ilat[c]) (0-based) as a case of their own:
+        nlon = number of columns, nlat = 1, every per-cell array gathered.
+        Columns are independent in the step (the only vertical coupling, the
+        column sums, stays inside a column), so a step over this case gives,
+        column for column, what a step over the whole grid gives."""
+        ilon = np.asarray(ilon, dtype=np.int64)
+        ilat = np.asarray(ilat, dtype=np.int64)
+        out = dataclasses.replace(self, name=f"{self.name}[{len(ilon)} columns]", nlon=len(ilon), nlat=1)
+        for f in self.GRID_ARRAYS:
+            setattr(out, f, self.gather_columns(getattr(self, f), ilon, ilat))
+        return out
+
+    @staticmethod
+    def gather_columns(arr, ilon, ilat):
+        """A Fortran-layout grid array (nlon, nlat, ...) at the columns, in the
+        layout of columns(ilon, ilat): (ncol, 1, ...)."""
+        return np.asfortranarray(np.asarray(arr)[np.asarray(ilon), np.asarray(ilat)][:, None])
+
 
 def _fview(a_c, nlon, nlat):
     """C-ordered (..., niv, ncol) -> Fortran (nlon, nlat, niv, ...) view."""

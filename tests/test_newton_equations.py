@@ -4,7 +4,9 @@ code (tests/newton_host.cpp):
   * the committed header is what the generator writes;
   * its residual vanishes at the oracle's fixed point of the reference map;
   * its Jacobian matches finite differences of its residual;
-  * the Newton iteration (FP64 and FP32 Jacobian) converges to that fixed point.
+  * the Newton iteration (FP64 and FP32 Jacobian) converges to that fixed point;
+  * on a polar-winter mix, Oracle-C converges on at least 99.9 % of the cells
+    and the Newton iteration at the production tolerance lands within 1e-6.
 """
 import ctypes
 import os
@@ -83,7 +85,7 @@ def test_generated_header_is_current(tmp_path):
 def test_residual_vanishes_at_the_reference_fixed_point(host, data):
     c, dg, fp, stat, _ = data
     worst = 0.0
-    for cell in np.where(stat > 0)[0]:
+    for cell in np.where(stat >= 0)[0]:
         K, tj, het, fix, ck0, day = _cell_inputs(c, dg, cell)
         x = _x(c, fp, dg, cell)
         R = np.zeros(57)
@@ -94,7 +96,7 @@ def test_residual_vanishes_at_the_reference_fixed_point(host, data):
 
 def test_jacobian_matches_finite_differences(host, data):
     c, dg, fp, stat, _ = data
-    for cell in np.where(stat > 0)[0][::97][:4]:
+    for cell in np.where(stat >= 0)[0][::97][:4]:
         K, tj, het, fix, ck0, day = _cell_inputs(c, dg, cell)
         x = _x(c, fp, dg, cell)
         Jd = np.zeros(57 * 57)
@@ -127,8 +129,76 @@ def test_newton_converges_to_the_fixed_point(host, data, mixed):
         if it < 0:
             fails += 1
             continue
-        if stat[cell] > 0:
+        if stat[cell] >= 0:
             xs = _x(c, fp, dg, cell)
             errs.append(np.max(np.abs(x - xs) / np.maximum(np.abs(xs), 1e-20 * fix[4])))
     assert fails <= 2
     assert max(errs) < 1e-8
+
+
+@pytest.fixture(scope="module")
+def polar():
+    """A polar-winter mix (30 % of the columns in polar night, T 183-195 K,
+    active ClOx) on all 137 levels."""
+    c = inputs.make_case("grid", seed=77, nlon=8, nlat=4, daynum=355.5, polar_frac=0.3)
+    _, dg, _ = oracle.step(c, niter=1, fuse=False, diag=True)
+    fp, stat, _, stage = oracle.step_fixed_point(c, tol=1e-12, maxiter=60, fuse=False, with_stage=True)
+    r5, _, _ = oracle.step(c, niter=5, fuse=False)
+    return c, dg, fp, stat, stage, r5
+
+
+def test_oracle_fixed_point_covers_the_polar_winter_mix(polar):
+    """Oracle-C converges on at least 99.9 % of the cells, and each cell's
+    answer is an exact fixed point of the reference pass map."""
+    c, dg, fp, stat, stage, _ = polar
+    assert (stat >= 0).mean() >= 0.999, np.bincount(stage, minlength=7)
+    mr = oracle.map_residual(c, fp["qj1"], fp["hc"])
+    assert mr[stat >= 0].max() < 1e-10
+
+
+def test_oracle_newton_from_a_fixed_point_stays_there(polar):
+    """Newton started from a state (here Oracle-C's own answer) returns the
+    fixed point nearest it: the check the GPU tests apply to the cells
+    Oracle-C does not converge on."""
+    c, dg, fp, stat, _, _ = polar
+    st, pstat, _ = oracle.newton_from(c, fp["qj1"], fp["hc"])
+    ok = stat >= 0
+    assert (pstat[ok] >= 0).all()
+    from oracle import accuracy
+    assert accuracy.cell_errors(st, fp, c.nivbas)[ok].max() < 1e-9
+
+
+@pytest.mark.parametrize("mixed", [0, 1])
+def test_generated_newton_at_production_settings_matches_the_oracle(host, polar, mixed):
+    """The generated equations' Newton iteration (host build) from the
+    5-pass state with the production step tolerance 1e-5: within 1e-6 of
+    Oracle-C for every species above 1e-20 mol/mol on every cell both
+    converge on, for the FP64 and the FP32 Jacobian."""
+    c, dg, fp, stat, _, r5 = polar
+    fails, worst = 0, 0.0
+    for cell in range(c.ncells):
+        i, j, k = cell % c.nlon, (cell // c.nlon) % c.nlat, cell // (c.nlon * c.nlat)
+        hnm = dg[DIAG_HNM, cell]
+        q0 = c.qj1[i, j, k, :]
+        rain = 1e-6 if q0[2] >= 100e-6 else 0.0
+        fix = np.array([0.21 * hnm, 0.78 * hnm, 5e-7 * hnm, 360e-6 * hnm, hnm,
+                        dg[DIAG_NAMES.index("parthno3"), cell], dg[DIAG_NAMES.index("parth2o"), cell],
+                        dg[DIAG_NAMES.index("parthcl"), cell], 1.0, rain, rain, rain, rain, c.dt])
+        K = np.ascontiguousarray(dg[DIAG_RATE:DIAG_RATE + 99, cell])
+        tj = np.ascontiguousarray(dg[DIAG_TJ:DIAG_TJ + 41, cell])
+        het = np.ascontiguousarray(dg[DIAG_HET:DIAG_HET + 9, cell])
+        ck0 = np.ascontiguousarray(q0[:42] * hnm)
+        x = np.concatenate([r5["qj1"][i, j, k, :42], r5["hc"][i, j, k, :]]) * hnm
+        last = ctypes.c_double()
+        it = host.nt_host_newton(_P(K), _P(tj), _P(het), _P(fix), _P(ck0), int(dg[DIAG_SZA, cell] <= 95.0), _P(x),
+                                 16, 1e-5, mixed, ctypes.byref(last))
+        if it < 0:
+            fails += 1
+            continue
+        if stat[cell] >= 0:
+            xs = np.concatenate([fp["qj1"][i, j, k, :42], fp["hc"][i, j, k, :]]) * hnm
+            big = np.abs(xs) > 1e-20 * hnm
+            e = np.where(big, np.abs(x - xs) / np.maximum(np.abs(xs), 1e-300), 0.0)
+            worst = max(worst, float(e.max()))
+    assert fails <= 0.001 * c.ncells
+    assert worst <= 1e-6
