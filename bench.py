@@ -39,10 +39,14 @@ BYTES_PER_CELL = 1008  # compulsory FP64 SoA traffic per cell-step: 63 reads + 6
 # (python -m oracle.count_ops --config cfg1 --rows 12).
 OPS_PER_CELL = 6793.08
 # DRAM bytes per cell-iteration of the mixed solve kernel, from one ncu capture
-# of the 394,560-cell grid (profiles/k_nt_solve_mixed_grid180x16.md: 1.35 GB
-# per launch at 3.79 iterations per cell): the cell records re-read from DRAM,
-# proportional to the cell-iterations; scaled to the benchmark launch
+# of the 394,560-cell grid (1.35 GB per launch at 3.79 iterations per cell):
+# the cell records re-read from DRAM, proportional to the cell-iterations;
+# scaled to the benchmark launch
 SOLVE_DRAM_BYTES_PER_CELL_ITER = 899.0
+# the accuracy leg: seeded columns of the grid (x 137 levels ~ 1.1e4 cells)
+# checked against the CPU FP64 oracle after the timed steps
+ACCURACY_COLUMNS = 80
+ACCURACY_SEED = 2024
 
 
 def newton_ops():
@@ -119,11 +123,9 @@ class Clocks:
         return out
 
 
-def fp64_peak_tflops(torch):
-    """cuBLAS DGEMM 4096^3, best of 5 (CUDA events): the FP64 denominator."""
-    n = 4096
-    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
-    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+def _gemm_peak_tflops(torch, dtype, n):
+    a = torch.randn(n, n, dtype=dtype, device="cuda")
+    b = torch.randn(n, n, dtype=dtype, device="cuda")
     torch.matmul(a, b)
     torch.cuda.synchronize()
     best = 1e30
@@ -138,9 +140,28 @@ def fp64_peak_tflops(torch):
     return 2 * n ** 3 / (best * 1e-3) / 1e12
 
 
+def fp64_peak_tflops(torch):
+    """cuBLAS DGEMM 4096^3, best of 5 (CUDA events): the FP64 denominator."""
+    return _gemm_peak_tflops(torch, torch.float64, 4096)
+
+
+def fp32_peak_tflops(torch):
+    """cuBLAS SGEMM 8192^3 with TF32 off (FP32 FMA on the CUDA cores), best
+    of 5: the FP32 denominator."""
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        return _gemm_peak_tflops(torch, torch.float32, 8192)
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = old
+
+
 def _rows(case, nrows):
     """nrows latitude rows (1-based) spread evenly from pole to pole."""
     return sorted({int(round(x)) for x in np.linspace(1, case.nlat, nrows)})
+
+
+CPU_ROWS = 12  # latitude rows of the CPU sample, the same in both CPU legs
 
 
 def _time_rows(case, rows, nthreads=0):
@@ -152,20 +173,37 @@ def _time_rows(case, rows, nthreads=0):
     return time.perf_counter() - t0
 
 
-def cpu_baseline(case, target_s=12.0, nthreads=0):
-    """Times the oracle (the reference scheme restated on the CPU, OpenMP over
-    longitude blocks) on latitude rows spread over the same grid, sized to
-    about target_s of CPU time."""
+def cpu_sample(case, nrows=CPU_ROWS, nthreads=0):
+    """One timing of the oracle (the reference scheme restated on the CPU,
+    OpenMP over longitude blocks of a row) on nrows latitude rows spread pole
+    to pole: cell-steps/s. The per-cell rate does not depend on which rows
+    are sampled beyond the day/night mix, which spreading them keeps."""
     import multiprocessing
-    dt = _time_rows(case, _rows(case, 2), nthreads)
-    n = int(min(case.nlat, max(2, 2 * target_s / max(dt, 1e-3))))
-    rows = _rows(case, n)
+    rows = _rows(case, nrows)
     dt = _time_rows(case, rows, nthreads)
     cells = len(rows) * case.nlon * case.nivbas
     cores = nthreads if nthreads > 0 else multiprocessing.cpu_count()
     return {"value": cells / dt, "unit": "cell-steps/s", "cores": cores, "kind": "port",
             "sample": f"{len(rows)} latitude rows spread pole to pole x {case.nlon} lon x {case.nivbas} levels "
-                      f"= {cells} cells, one step, oracle/chem_oracle.c (OpenMP, {cores} threads), {dt:.2f} s"}
+                      f"= {cells} cells per step, oracle/chem_oracle.c restating the reference scheme "
+                      f"(niter 5, conserv and clamps), OpenMP {cores} threads", "seconds": dt}
+
+
+def cpu_baseline(case, target_s=10.0):
+    """The oracle on the machine's host cores: all cores (median of repeats of the
+    sample the reference arm times, about target_s in all) and one thread
+    (the reference is serial: the same rows, one repeat)."""
+    runs = [cpu_sample(case)]
+    while sum(r["seconds"] for r in runs) < target_s and len(runs) < 20:
+        runs.append(cpu_sample(case))
+    out = dict(runs[0])
+    out["value"] = statistics.median(r["value"] for r in runs)
+    out["repeats"] = len(runs)
+    out.pop("seconds", None)
+    one = cpu_sample(case, nthreads=1)
+    out["one_thread"] = {"value": one["value"], "unit": "cell-steps/s", "cores": 1,
+                         "seconds": round(one["seconds"], 3), "sample": "the same rows, 1 thread"}
+    return out
 
 
 def run_reference(args):
@@ -175,13 +213,12 @@ def run_reference(args):
     from reprobus_gb300 import inputs
     case = inputs.make_case("cfg1", seed=1234)
     for _ in range(args.warmup):
-        cpu_baseline_one(case)
-    vals = []
-    for _ in range(args.steps):
-        vals.append(cpu_baseline_one(case))
+        cpu_sample(case)
+    vals = [cpu_sample(case) for _ in range(args.steps)]
     v = statistics.median([x["value"] for x in vals])
     cb = dict(vals[0])
     cb["value"] = v
+    cb.pop("seconds", None)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cell-steps/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; reference inputs unavailable)",
@@ -189,18 +226,6 @@ def run_reference(args):
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
-
-
-def cpu_baseline_one(case, nrows=12):
-    import multiprocessing
-    rows = _rows(case, nrows)
-    dt = _time_rows(case, rows)
-    cells = len(rows) * case.nlon * case.nivbas
-    cores = multiprocessing.cpu_count()
-    return {"value": cells / dt, "unit": "cell-steps/s", "cores": cores, "kind": "port",
-            "sample": f"{len(rows)} latitude rows spread pole to pole x {case.nlon} lon x {case.nivbas} levels "
-                      f"= {cells} cells per step, oracle/chem_oracle.c restating the reference scheme, "
-                      f"OpenMP {cores} threads"}
 
 
 def column_bench(torch, h, case, dc, stream, hbm_peak, reps=5):
@@ -268,6 +293,107 @@ def inputs_l137():
     return inputs.l137_levels()
 
 
+ARMS = {"ref5": "reference scheme, 5 fixed passes (drop-in)",
+        "newton64": "Newton to the fixed point of the reference map, FP64 Jacobian",
+        "mixed": "Newton to the fixed point, FP32 Jacobian+LU, FP64 residual/update",
+        "mlp": "Newton to the fixed point, FP32 Jacobian+LU, FP64 residual/update, learned warm start (BF16 MLP "
+               "on tensor cores)"}
+SOLVER_ID = {"ref5": 0, "newton64": 1, "mixed": 2, "mlp": 2}  # REPROBUS_SOLVER_*
+
+
+class Accuracy:
+    """The accuracy leg: a seeded sample of whole columns of the grid, their
+    answer from the CPU FP64 oracle (Oracle-C fixed point and the reference's
+    5-pass answer, with conserv and the clamps), and per arm the error of the
+    answer the GPU produced in its last timed step on those columns. Runs
+    outside every timed region."""
+
+    def __init__(self, case, ncol=ACCURACY_COLUMNS, seed=ACCURACY_SEED):
+        from oracle import accuracy
+        rng = np.random.default_rng(seed)
+        pick = rng.choice(case.nlon * case.nlat, size=min(ncol, case.nlon * case.nlat), replace=False)
+        self.ilon, self.ilat = pick % case.nlon, pick // case.nlon
+        self.case = case
+        self.sub = case.columns(self.ilon, self.ilat)
+        t0 = time.perf_counter()
+        self.ref = accuracy.Reference(self.sub, fuse=True)
+        self.oracle_s = time.perf_counter() - t0
+
+    def check(self, dc):
+        got = {f: self.case.gather_columns(dc[f].cpu().numpy().reshape(getattr(self.case, f).shape, order="F"),
+                                           self.ilon, self.ilat) for f in ("qj1", "hc")}
+        return self.ref.report(got)
+
+    def describe(self):
+        return {"columns": int(len(self.ilon)), "cells": int(self.sub.ncells), "seed": ACCURACY_SEED,
+                "oracle": "Oracle-C (FP64 fixed point of the reference pass map) + conserv + clamps",
+                "oracle_converged": int((self.ref.stat >= 0).sum()),
+                "oracle_stages": np.bincount(self.ref.stage, minlength=7).tolist(),
+                "oracle_s": round(self.oracle_s, 2)}
+
+
+def time_arms(torch, h, case, dc, stream, arms, steps, warmup, net, npass_of, world, acc=None):
+    """Times each solver arm on the device-resident state: warm-up steps, one
+    step with statistics, then `steps` timed steps (CUDA events on the
+    handle's stream, each from the same restored start state). With acc the
+    last timed step's answer is checked against the oracle afterwards."""
+    from reprobus_gb300.replicas import max_over_ranks, whole_job_rate
+    a = dc.args()
+    state = ("qj1", "hc", "vsed3d", "parth2osed", "parthno3sed", "surfarea", "sza3d")
+    pristine = {f: dc[f].clone() for f in state}
+
+    def restore():
+        with torch.cuda.stream(stream):
+            for f in state:
+                dc[f].copy_(pristine[f])
+
+    def step(stats=False):
+        return h.step_dev(1, case.nlat, case.daynum, case.dt, *a, stats=stats)
+
+    results = {}
+    for name in arms:
+        h.set_solver(SOLVER_ID[name], npass=npass_of(name), maxit=12, tol=1e-5)
+        h.set_mlp(net if name == "mlp" else None)
+        for _ in range(max(warmup, 3)):
+            restore()
+            step()
+        restore()
+        st = step(stats=True)  # launches per step, kernel time, solver statistics
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        for e0, e1 in evs:
+            restore()
+            e0.record(stream)
+            step()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = max_over_ranks(sum(e0.elapsed_time(e1) for e0, e1 in evs))
+        conv = case.ncells - st["fallbacks"]
+        day_frac = float((dc["sza3d"][:case.ncells] <= 95.0).double().mean())
+        newton = name != "ref5"
+        results[name] = {"cells_per_s": whole_job_rate(case.ncells, world, steps, ms * 1e-3),
+                         "ms_per_step": ms / steps, "kernel_ms": st["device_ms"],
+                         "solve_ms": st["solve_ms"] if newton else None,
+                         "launches_per_step": st["kernel_launches"], "fallbacks": st["fallbacks"],
+                         "mean_newton_iters": (st["newton_iters"] / conv) if newton and conv else None,
+                         "iters_per_cell": ((st["newton_iters"] + st["failed_iters"]) / case.ncells
+                                            if newton else None),
+                         "warm_restarts": st["warm_restarts"] if name == "mlp" else None,
+                         "day_frac": day_frac,
+                         "max_newton_iters": st["max_newton_iters"] if newton else None,
+                         "solve_shape": None if not newton else
+                         {"lanes_per_block": st["lanes_per_block"], "blocks_per_sm": st["blocks_per_sm"],
+                          "z_shared": st["z_shared"]}}
+        if acc is not None:
+            results[name]["accuracy"] = acc.check(dc)
+    restore()
+    torch.cuda.synchronize()
+    return results
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -280,6 +406,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-columns", action="store_true", help="skip timing the column physics kernels")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip checking the timed answers against the oracle")
+    ap.add_argument("--no-polar", action="store_true", help="skip the 30%%-polar-winter grid block")
+    ap.add_argument("--polar-steps", type=int, default=5, help="timed steps per arm on the polar-winter grid")
     ap.add_argument("--npass", type=int, default=0,
                     help="reference passes before Newton for the plain solvers (0: each solver's default)")
     ap.add_argument("--lanes", type=int, default=0,
@@ -287,7 +416,7 @@ def main():
     ap.add_argument("--bps", type=int, default=0, help="Newton solve kernel blocks per SM (0: all that fit)")
     ap.add_argument("--zshared", type=int, default=0, help="with --lanes: right-hand side in shared memory")
     ap.add_argument("--solver", default="all", choices=["all", "ref5", "newton64", "mixed", "mlp"],
-                    help="all: time the three solvers, headline = mixed")
+                    help="all: time the four arms, headline = mlp")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -307,10 +436,7 @@ def main():
         case = inputs.make_case("grid", seed=replica_seed(1234, rank), nlon=args.nlon, nlat=args.nlat)
     else:
         case = inputs.make_case(args.config, seed=replica_seed(1234, rank))
-    from reprobus_gb300.chem import SOLVER_NEWTON64, SOLVER_NEWTON_MIXED, SOLVER_REF5
-    solver_ids = {"ref5": SOLVER_REF5, "newton64": SOLVER_NEWTON64, "mixed": SOLVER_NEWTON_MIXED,
-                  "mlp": SOLVER_NEWTON_MIXED}
-    run = list(solver_ids) if args.solver == "all" else [args.solver]
+    run = list(ARMS) if args.solver == "all" else [args.solver]
     headline = "mlp" if args.solver == "all" else args.solver
     net = None
     if "mlp" in run:
@@ -323,17 +449,6 @@ def main():
     stream = torch.cuda.Stream()
     h.set_stream(stream)
     dc = DeviceCase(case)
-    a = dc.args()
-    state = ("qj1", "hc", "vsed3d", "parth2osed", "parthno3sed", "surfarea", "sza3d")
-    pristine = {f: dc[f].clone() for f in state}
-
-    def restore():
-        with torch.cuda.stream(stream):
-            for f in state:
-                dc[f].copy_(pristine[f])
-
-    def step(stats=False):
-        return h.step_dev(1, case.nlat, case.daynum, case.dt, *a, stats=stats)
 
     def npass_of(name):
         # the warm start's network is trained on the default 5-pass start
@@ -341,46 +456,14 @@ def main():
             return 5
         return args.npass if args.npass > 0 else 5
 
-    results = {}
+    # the oracle's answers for the accuracy leg (CPU, before any timing)
+    acc = Accuracy(case) if (rank == 0 and not args.no_accuracy) else None
+
     clocks = Clocks(local)
     clocks.start()
-    for name in run:
-        h.set_solver(solver_ids[name], npass=npass_of(name), maxit=12, tol=1e-5)
-        h.set_mlp(net if name == "mlp" else None)
-        for _ in range(max(args.warmup, 3)):
-            restore()
-            step()
-        restore()
-        st = step(stats=True)  # launches per step, kernel time, solver statistics
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-               for _ in range(args.steps)]
-        for e0, e1 in evs:
-            restore()
-            e0.record(stream)
-            step()
-            e1.record(stream)
-        torch.cuda.synchronize()
-        ms = max_over_ranks(sum(e0.elapsed_time(e1) for e0, e1 in evs))
-        conv = case.ncells - st["fallbacks"]
-        day_frac = float((dc["sza3d"][:case.ncells] <= 95.0).double().mean())
-        results[name] = {"cells_per_s": whole_job_rate(case.ncells, world, args.steps, ms * 1e-3),
-                         "ms_per_step": ms / args.steps, "kernel_ms": st["device_ms"],
-                         "solve_ms": st["solve_ms"] if name != "ref5" else None,
-                         "launches_per_step": st["kernel_launches"], "fallbacks": st["fallbacks"],
-                         "mean_newton_iters": (st["newton_iters"] / conv) if name != "ref5" and conv else None,
-                         "iters_per_cell": ((st["newton_iters"] + st["failed_iters"]) / case.ncells
-                                            if name != "ref5" else None),
-                         "warm_restarts": st["warm_restarts"] if name == "mlp" else None,
-                         "day_frac": day_frac,
-                         "max_newton_iters": st["max_newton_iters"] if name != "ref5" else None,
-                         "solve_shape": None if name == "ref5" else
-                         {"lanes_per_block": st["lanes_per_block"], "blocks_per_sm": st["blocks_per_sm"],
-                          "z_shared": st["z_shared"]}}
+    results = time_arms(torch, h, case, dc, stream, run, args.steps, args.warmup, net, npass_of, world, acc)
     clk = clocks.stop()
-    h.set_solver(solver_ids[headline], npass=npass_of(headline), maxit=12, tol=1e-5)
+    h.set_solver(SOLVER_ID[headline], npass=npass_of(headline), maxit=12, tol=1e-5)
     h.set_mlp(net if headline == "mlp" else None)
     R = results[headline]
     ms_step = R["ms_per_step"]
@@ -424,50 +507,88 @@ def main():
         d2h = pl * 43 + pb * 15 + pb * 4 + (case.nivbas - case.nivhau + 1) * case.nlon * case.nlat * 8
         e2e = {"value": whole_job_rate(ncell, world, 1, te), "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": te * 1e3}
+        del hp, hs, harr, sarr
+
+    # the 30 %-polar-winter grid at full size: the Newton arms, timed and checked
+    polar = None
+    parms = [x for x in ("newton64", "mixed", "mlp") if x in run]
+    if not args.no_polar and args.config == "cfg1" and parms:
+        pcase = inputs.make_case("cfg2", seed=replica_seed(4321, rank))
+        pacc = Accuracy(pcase) if (rank == 0 and not args.no_accuracy) else None
+        pdc = DeviceCase(pcase)
+        pres = time_arms(torch, h, pcase, pdc, stream, parms, args.polar_steps, args.warmup, net, npass_of, world,
+                         pacc)
+        polar = {"workload": f"cfg2: {pcase.nlon}x{pcase.nlat}x{pcase.niv} = {pcase.ncells} cells, 30% of the "
+                             f"columns in polar winter (T 183-195 K, SZA > 95, active ClOx), day {pcase.daynum}",
+                 "steps": args.polar_steps, "solvers": pres,
+                 "mixed_vs_fp64_newton": (pres["mixed"]["cells_per_s"] / pres["newton64"]["cells_per_s"]
+                                          if "mixed" in pres and "newton64" in pres else None),
+                 "mlp_mixed_vs_fp64_newton": (pres["mlp"]["cells_per_s"] / pres["newton64"]["cells_per_s"]
+                                              if "mlp" in pres and "newton64" in pres else None),
+                 "accuracy_sample": pacc.describe() if pacc else None}
+        del pdc
+        torch.cuda.empty_cache()
+        h.set_solver(SOLVER_ID[headline], npass=npass_of(headline), maxit=12, tol=1e-5)
+        h.set_mlp(net if headline == "mlp" else None)
 
     line = None
     if rank == 0:
         peak64 = fp64_peak_tflops(torch)
-        hbm_peak = None
+        peak32 = fp32_peak_tflops(torch)
         try:
             hbm_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+            hbm_src = "MEASURED_PEAKS.json hbm_gbs (measured copy)"
         except Exception:
             hbm_peak = 6800.0
-        flops_cell = OPS_PER_CELL
+            hbm_src = "fallback 6.8 TB/s"
         ach_gbs = BYTES_PER_CELL * ncell / (kernel_ms * 1e-3) / 1e9
+        # the work of a step: the reference scheme's FP64 operations per cell
+        # (fixed across solvers so that their figures compare)
+        step_tf = OPS_PER_CELL * ncell / (kernel_ms * 1e-3) / 1e12
         roof = {"bound": "fp64", "unit": "TFLOP/s", "peak": round(peak64, 4),
                 "peak_source": "cuBLAS DGEMM 4096^3 measured live in this run",
-                "achieved": None, "frac": None, "traffic": None,
-                "kernel_ms": round(kernel_ms, 4),
-                "hbm": {"achieved": round(ach_gbs, 2), "peak": hbm_peak, "unit": "GB/s",
+                "flops_per_cell": OPS_PER_CELL,
+                "flops_note": "algorithmic work = the reference scheme's FP64 operations per cell-step "
+                              "(+-*/ and transcendentals counted once each, oracle operation counter), the same "
+                              "for every solver; the peak counts an FMA as 2",
+                "step": {"ms": round(kernel_ms, 4), "achieved": round(step_tf, 4),
+                         "frac": round(step_tf / peak64, 4)},
+                "hbm": {"achieved": round(ach_gbs, 2), "peak": hbm_peak, "peak_source": hbm_src, "unit": "GB/s",
                         "frac": round(ach_gbs / hbm_peak, 5), "bytes_per_cell": BYTES_PER_CELL}}
-        if headline == "ref5" and flops_cell:
-            ach = flops_cell * ncell / (kernel_ms * 1e-3) / 1e12
-            roof.update(achieved=round(ach, 4), frac=round(ach / peak64, 4), flops_per_cell=flops_cell,
-                        flops_note="algorithmic ops of the reference scheme per cell-step (+-*/ and "
-                                   "transcendentals counted once each; the peak counts an FMA as 2)")
-        elif headline != "ref5":
+        if headline == "ref5":
+            roof.update(kernel="whole step", kernel_ms=round(kernel_ms, 4), achieved=round(step_tf, 4),
+                        frac=round(step_tf / peak64, 4), traffic=None)
+        else:
             # dominant kernel: the persistent Newton solve kernel (k_nt_solve)
             ops = newton_ops()
             f = R["day_frac"]
             res = f * ops["res_day"] + (1 - f) * ops["res_night"]
             jac = f * ops["jac_day"] + (1 - f) * ops["jac_night"]
-            fp64_it = res + ops["update"] + (0 if headline in ("mixed", "mlp") else jac + ops["factor"] + ops["rhs"])
-            fp32_it = (jac + ops["factor"] + ops["rhs"]) if headline in ("mixed", "mlp") else 0
+            mixed = headline in ("mixed", "mlp")
+            fp64_it = res + ops["update"] + (0 if mixed else jac + ops["factor"] + ops["rhs"])
+            fp32_it = (jac + ops["factor"] + ops["rhs"]) if mixed else 0
             iters = R["iters_per_cell"] * ncell
             sm = R["solve_ms"] * 1e-3
-            ach = fp64_it * iters / sm / 1e12
-            traffic = (SOLVE_DRAM_BYTES_PER_CELL_ITER * iters if headline in ("mixed", "mlp") else None)
+            ach = OPS_PER_CELL * ncell / sm / 1e12
+            traffic = SOLVE_DRAM_BYTES_PER_CELL_ITER * iters if mixed else None
+            fp32_tf = fp32_it * iters / sm / 1e12
             roof.update(kernel="k_nt_solve", kernel_ms=round(R["solve_ms"], 4), achieved=round(ach, 4),
-                        traffic=traffic, traffic_note="DRAM bytes per launch: 899 B per cell-iteration from an "
-                        "ncu capture of the 394,560-cell grid, times this launch's cell-iterations",
-                        frac=round(ach / peak64, 4), fp64_ops_per_iteration=round(fp64_it, 1),
-                        fp32_ops_per_iteration=round(fp32_it, 1), iterations_per_cell=round(R["iters_per_cell"], 3),
-                        fp32_tflops=round(fp32_it * iters / sm / 1e12, 4),
-                        flops_note="arithmetic operators of one Newton iteration counted in the generated "
-                                   "source (an FMA counts 2), times the iterations the step ran, over the "
-                                   "solve kernel's CUDA-event time; FP64 part (residual, update) against the "
-                                   "live DGEMM peak")
+                        frac=round(ach / peak64, 4), traffic=traffic,
+                        traffic_ratio=(round(traffic / (BYTES_PER_CELL * ncell), 3) if traffic else None),
+                        traffic_note="DRAM bytes per launch: 899 B per cell-iteration from an ncu capture of the "
+                                     "394,560-cell grid, times this launch's cell-iterations; ratio against the "
+                                     "step's algorithmic 1,008 B per cell",
+                        solver_ops={"fp64_ops_per_iteration": round(fp64_it, 1),
+                                    "fp32_ops_per_iteration": round(fp32_it, 1),
+                                    "iterations_per_cell": round(R["iters_per_cell"], 3),
+                                    "fp64_tflops": round(fp64_it * iters / sm / 1e12, 4),
+                                    "fp64_frac": round(fp64_it * iters / sm / 1e12 / peak64, 4),
+                                    "note": "operators the solver executes, counted in the generated source (an "
+                                            "FMA counts 2), times the step's iterations, over the solve kernel's "
+                                            "CUDA-event time"},
+                        fp32={"achieved": round(fp32_tf, 4), "peak": round(peak32, 3),
+                              "peak_source": "cuBLAS SGEMM 8192^3, TF32 off, measured live in this run",
+                              "frac": round(fp32_tf / peak32, 5) if mixed else None})
         cols = None
         if not args.no_columns:
             cols = column_bench(torch, h, case, dc, stream, hbm_peak)
@@ -479,12 +600,7 @@ def main():
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; reference inputs unavailable)",
                 "config": {"workload": WORKLOAD if args.config == "cfg1" else
                            f"{args.config}: {case.nlon}x{case.nlat}x{case.niv} = {case.ncells} cells, one 15-min step",
-                           "solver": {"ref5": "reference scheme, 5 fixed passes (drop-in)",
-                                      "mlp": "Newton to the fixed point, FP32 Jacobian+LU, FP64 residual/update, "
-                                             "learned warm start (BF16 MLP on tensor cores)",
-                                      "newton64": "Newton to the fixed point of the reference map, FP64 Jacobian",
-                                      "mixed": "Newton to the fixed point, FP32 Jacobian+LU, FP64 residual/update"}
-                           [headline],
+                           "solver": ARMS[headline],
                            "timing": "each timed step starts from the same restored device state",
                            "cells": ncell, "l2": "inputs larger than L2 (1.2 GB resident state)",
                            "parallelism": f"replicas x{world}"},
@@ -494,6 +610,8 @@ def main():
                                          if "mixed" in results and "newton64" in results else None),
                 "mlp_mixed_vs_fp64_newton": (results["mlp"]["cells_per_s"] / results["newton64"]["cells_per_s"]
                                              if "mlp" in results and "newton64" in results else None),
+                "accuracy_sample": acc.describe() if acc else None,
+                "polar_winter": polar,
                 "roofline": roof, "e2e": e2e, "cpu_baseline": cb, "clocks": clk, "columns": cols}
         print(json.dumps(line))
     h.close()

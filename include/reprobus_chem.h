@@ -144,7 +144,9 @@ int reprobus_chem_troe(double* troe);
  * Replaces: call const(relief), :294, i.e. the COMMON blocks filled at
  * :5927-5973 and declared at :46-52.
  * nivbas: last chemistry level (reference: 94); nivhau: first PSC/aerosol
- * level (reference: 14); niter: fixed-point passes (reference: 5, :630). */
+ * level (reference: 14); niter: fixed-point passes (reference: 5, :630).
+ * Troe prefactors that are not positive and finite are refused with
+ * REPROBUS_ERR_ARG (the rate stage works with their logarithms). */
 int reprobus_chem_init(const double* ajl, const double* o3up, const double* troe,
                        int nlon, int nlat, int niv, int nivbas, int nivhau,
                        int nrappmax, int niter, int flags, void** handle);
@@ -233,6 +235,14 @@ int reprobus_mlp_grads(void* net, const float* X, const float* Y, int B, float* 
                        void* cuda_stream);
 /* Inference on B rows (any B): Y = network(X), raw units. */
 int reprobus_mlp_forward(void* net, const float* X, float* Y, int B, void* cuda_stream);
+/* Fault handling hook: the number of polls after which the inference
+ * kernel's waits on its weight copies and tensor-core work give up (polls < 0:
+ * the default, 2^24; 0: the first wait gives up at once). A wait that gives
+ * up makes the kernel skip its remaining work, wait (with the default limit)
+ * for the copies and MMAs it has in flight, release its tensor memory and
+ * report REPROBUS_ERR_TIMEOUT; the network stays usable. No counterpart in
+ * the reference. */
+int reprobus_mlp_set_wait_limit(void* net, long long polls);
 
 /* Attaches a network to a chemistry handle (NULL detaches): the Newton
  * solvers then start every cell from the network's prediction instead of the
@@ -387,10 +397,15 @@ int reprobus_history_read_dev(void* handle, const char* path, char* namexp, int*
  * device, with that device current); make that first call before capturing
  * any stream. All calls share the one array and it keeps the last call's
  * contents: calls whose kernels overlap on the GPU (other streams, other host
- * threads) race on it; serialise them. Launches on `stream` (NULL: the
- * default stream); asynchronous unless REPROBUS_CHECK_FINITE is set, in
- * which case it synchronises to read the non-finite count.
- * Same replacement of the reference as reprobus_chem_step (:398-450). */
+ * threads) race on it; serialise them. A process that resets the device
+ * (cudaDeviceReset) gets the address looked up again at its next call.
+ * The call always integrates with the reference scheme (niter fixed passes,
+ * REPROBUS_SOLVER_REF5): it has no handle, so no solver selection, Newton
+ * state or warm start. Launches on `stream` (NULL: the default stream);
+ * asynchronous unless REPROBUS_CHECK_FINITE is set, in which case it
+ * synchronises to read the non-finite count. It runs the kernels of
+ * reprobus_chem_step_dev with the same flags. Troe prefactors that are not
+ * positive and finite are refused with REPROBUS_ERR_ARG. */
 #define REPROBUS_NOALLOC_SCRATCH_DOUBLES (1 << 20)
 int reprobus_chem_step_noalloc(const double* ajl, const double* o3up, const double* troe,
                                int nlon, int nlat, int niv, int nivbas, int nivhau,

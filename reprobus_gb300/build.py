@@ -14,7 +14,6 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libreprobus_gb300.so")
-PROBE = os.path.join(HERE, "pipe_probe")  # throughput probe behind the roofline notes
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["chem_kernels.cu", "nt_solve_f32_zr.cu", "nt_solve_f32_zs.cu", "nt_solve_f64_zr.cu",
            "nt_solve_f64_zs.cu", "nt_solve_pp.cu", "nt_solve_sp.cu", "nt_solve_ls.cu", "mlp_kernels.cu",
@@ -62,9 +61,6 @@ def build(force: bool = False, verbose: bool = False) -> str:
         if verbose:
             print(r.stdout + r.stderr)
 
-    probe_src = os.path.join(CSRC, "pipe_probe.cu")
-    if force or _stale(PROBE, [probe_src]):
-        jobs.append([nvcc(), *ARCH, "-O3", "-o", PROBE, probe_src])
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         list(ex.map(run, jobs))
     if force or jobs or _stale(LIB, objs):

@@ -43,7 +43,7 @@ EXPORTS = [
     "reprobus_mlp_set_params", "reprobus_mlp_get_params", "reprobus_mlp_train_step", "reprobus_mlp_grads",
     "reprobus_mlp_forward", "reprobus_chem_set_mlp", "reprobus_chem_features_dev", "reprobus_chem_set_graph",
     "reprobus_sedimentation_dev", "reprobus_tropo_values", "reprobus_forcing_dev", "reprobus_altitude_dev",
-    "reprobus_history_write_dev", "reprobus_history_read_dev",
+    "reprobus_history_write_dev", "reprobus_history_read_dev", "reprobus_mlp_set_wait_limit",
 ]
 NOALLOC_SCRATCH_DOUBLES = 1 << 20
 
@@ -106,6 +106,7 @@ def load_library(path: str = LIBPATH):
     lib.reprobus_mlp_train_step.argtypes = [vp, vp, vp, i, ctypes.c_float, fp, vp]
     lib.reprobus_mlp_grads.argtypes = [vp, vp, vp, i, fp, fp, vp]
     lib.reprobus_mlp_forward.argtypes = [vp, vp, vp, i, vp]
+    lib.reprobus_mlp_set_wait_limit.argtypes = [vp, ctypes.c_longlong]
     lib.reprobus_chem_set_mlp.argtypes = [vp, vp]
     lib.reprobus_chem_set_graph.argtypes = [vp, i]
     lib.reprobus_chem_features_dev.argtypes = [vp, i, i, d, d, vp, vp, vp, vp, vp, i, vp, vp, vp]

@@ -810,12 +810,23 @@ static void free_handle(Handle* h) {
     delete h;
 }
 
+// The rate stage takes ln of the 18 Troe prefactors (COMMON /constant/,
+// :5927-5948): each must be positive and finite, as the reference's are.
+static int check_troe(const double* troe) {
+    for (int i = 0; i < 18; i++)
+        if (!(troe[i] > 0.) || !(troe[i] < INFINITY))
+            return set_err(REPROBUS_ERR_ARG, "troe[%d] = %g: the Troe prefactors must be positive and finite", i,
+                           troe[i]);
+    return REPROBUS_OK;
+}
+
 extern "C" int reprobus_chem_init(const double* ajl, const double* o3up, const double* troe, int nlon, int nlat,
                                   int niv, int nivbas, int nivhau, int nrappmax, int niter, int flags,
                                   void** handle) {
     if (!handle) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
     *handle = nullptr;
     if (!ajl || !o3up || !troe) return set_err(REPROBUS_ERR_ARG, "ajl, o3up and troe must be non-NULL");
+    if (int rc = check_troe(troe)) return rc;
     if (nlon <= 0 || nlat <= 0 || niv <= 0 || nivbas <= 0 || nivbas > niv || nivhau < 1 || nivhau > nivbas ||
         nrappmax <= 0 || niter < 0)
         return set_err(REPROBUS_ERR_ARG, "bad sizes: nlon=%d nlat=%d niv=%d nivbas=%d nivhau=%d nrappmax=%d niter=%d",
@@ -1861,7 +1872,10 @@ static __device__ __align__(256) double g_noalloc_scratch[REPROBUS_NOALLOC_SCRAT
 
 // In host code g_noalloc_scratch names a host-side stand-in, not device
 // memory: its device address is looked up once per device (with that device
-// current) and cached here.
+// current) and cached here. A cached address is confirmed on each call by a
+// pointer-attribute query (host-side, no allocation); after cudaDeviceReset
+// the module is loaded again in a new context, the old address no longer
+// belongs to the device, and it is looked up again.
 static std::mutex g_noalloc_mu;
 static double* g_noalloc_dev[256];
 
@@ -1870,6 +1884,14 @@ static int noalloc_scratch(double** out) {
     CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 256) return set_err(REPROBUS_ERR_ARG, "device ordinal %d out of range", dev);
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_noalloc_dev[dev]) {
+        cudaPointerAttributes pa;
+        if (cudaPointerGetAttributes(&pa, g_noalloc_dev[dev]) != cudaSuccess || pa.type != cudaMemoryTypeDevice ||
+            pa.device != dev) {
+            cudaGetLastError();  // clear the error state the query may have left
+            g_noalloc_dev[dev] = nullptr;
+        }
+    }
     if (!g_noalloc_dev[dev]) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
@@ -1890,6 +1912,7 @@ extern "C" int reprobus_chem_step_noalloc(const double* ajl, const double* o3up,
                                           double* hc, double* vsed3d, double* parth2osed, double* parthno3sed,
                                           double* surfarea, double* sza3d, void* stream) {
     if (!ajl || !o3up || !troe) return set_err(REPROBUS_ERR_ARG, "ajl, o3up and troe must be non-NULL");
+    if (int rc = check_troe(troe)) return rc;
     if (nlon <= 0 || nlat <= 0 || niv <= 0 || nivbas <= 0 || nivbas > niv || nivhau < 1 || nivhau > nivbas ||
         nrappmax <= 0 || niter < 0)
         return set_err(REPROBUS_ERR_ARG, "bad sizes: nlon=%d nlat=%d niv=%d nivbas=%d nivhau=%d nrappmax=%d niter=%d",

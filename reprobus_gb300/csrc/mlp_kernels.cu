@@ -92,11 +92,14 @@ __global__ void __launch_bounds__(128) k_gemm_tn(GemmArgs g) {
             tc_commit(&bar);
         }
         ok = mbar_wait(&bar, phase, MB_POLLS);  // the MMAs are done: the chunk buffers may be rewritten
-        phase ^= 1;
-        __syncthreads();
+        ok = __syncthreads_and(ok);             // one verdict for the block (and the barrier before that)
+        if (ok) phase ^= 1;
     }
     tc_fence_after();
     if (!ok) {
+        // the wait gave up: the MMAs of the outstanding phase get a last
+        // bounded chance to finish before TMEM is released
+        mbar_wait(&bar, phase, MB_POLLS);
         if (threadIdx.x == 0) atomicAdd(g.err, 1u);
     } else {
         const int row = m0 + warp * 32 + lane;
@@ -164,6 +167,7 @@ struct InferArgs {
     const float* b[MLP_NL];
     const float* norm;
     unsigned int* err;
+    uint32_t polls;              // polls before a wait on a weight image or the MMAs gives up
 };
 
 // build the weight images from the BF16 row-major weights
@@ -237,7 +241,14 @@ __global__ void __launch_bounds__(MLP_INFER_THREADS, 1) k_mlp_infer(InferArgs a)
     const uint32_t tbase = tslot;
     const int quarter = warp & 3, chalf = warp >> 2;  // TMEM lane quarter, column half
     const uint32_t trow = tbase + ((uint32_t)(quarter * 32) << 16);
+    // Phases are consumed only by waits that succeed: after a wait gives up,
+    // wph/phase still name the phase that is outstanding, and pend/mpend say
+    // whether a copy (per buffer) or the MMAs are still in flight, so that
+    // the exit path waits for exactly those before it frees TMEM. ok is
+    // block-uniform (each verdict goes through __syncthreads_and), so every
+    // thread keeps the same bookkeeping.
     uint32_t phase = 0, wph[2] = {0, 0};
+    bool pend[2] = {nimg > 0, false}, mpend = false;
     bool ok = true;
     if (threadIdx.x == 0 && nimg > 0) {
         mbar_expect_tx(&wbar[0], wimg_bytes(0));
@@ -250,27 +261,33 @@ __global__ void __launch_bounds__(MLP_INFER_THREADS, 1) k_mlp_infer(InferArgs a)
         const int buf = q & 1;
         fence_async_smem();
         __syncthreads();
-        if (ok) ok = mbar_wait(&wbar[buf], wph[buf], MB_POLLS);
+        if (ok) ok = mbar_wait(&wbar[buf], wph[buf], a.polls);
         ok = __syncthreads_and(ok);  // one verdict for the block
-        wph[buf] ^= 1;
-        if (threadIdx.x == 0) {
-            tc_fence_after();
-            const uint32_t sbo = (uint32_t)(K / 8 * 128);
-            const uint32_t idesc = tc_idesc_bf16(128, N);
-            if (ok)
+        if (ok) {  // the image landed
+            wph[buf] ^= 1;
+            pend[buf] = false;
+            if (threadIdx.x == 0) {
+                tc_fence_after();
+                const uint32_t sbo = (uint32_t)(K / 8 * 128);
+                const uint32_t idesc = tc_idesc_bf16(128, N);
                 for (int kk = 0; kk < K / 16; kk++)
                     tc_mma_bf16(tbase + dcol, tc_desc(smem_u32(act) + kk * 256, 128, sbo),
                                 tc_desc(smem_u32(wbuf[buf]) + kk * 256, 128, sbo), idesc, kk > 0);
-            tc_commit(&bar);
-            if (ok && q + 1 < nimg) {  // the other buffer's last reader finished before this image began
-                const int nx = (q + 1) % WIMG_N;
-                mbar_expect_tx(&wbar[buf ^ 1], wimg_bytes(nx));
-                bulk_g2s(wbuf[buf ^ 1], a.img + wimg_off(nx), wimg_bytes(nx), &wbar[buf ^ 1]);
+                tc_commit(&bar);
+                if (q + 1 < nimg) {  // the other buffer's last reader finished before this image began
+                    const int nx = (q + 1) % WIMG_N;
+                    mbar_expect_tx(&wbar[buf ^ 1], wimg_bytes(nx));
+                    bulk_g2s(wbuf[buf ^ 1], a.img + wimg_off(nx), wimg_bytes(nx), &wbar[buf ^ 1]);
+                }
             }
+            if (q + 1 < nimg) pend[buf ^ 1] = true;
+            ok = mbar_wait(&bar, phase, a.polls);
+            ok = __syncthreads_and(ok);
+            if (ok)
+                phase ^= 1;
+            else
+                mpend = true;
         }
-        if (ok) ok = mbar_wait(&bar, phase, MB_POLLS);
-        ok = __syncthreads_and(ok);
-        phase ^= 1;
         q++;
         tc_fence_after();
     };
@@ -341,9 +358,11 @@ __global__ void __launch_bounds__(MLP_INFER_THREADS, 1) k_mlp_infer(InferArgs a)
         }
     }
     if (!ok) {
-        // a wait gave up: give a copy still in flight a last bounded chance to land
-        mbar_wait(&wbar[0], wph[0], MB_POLLS);
-        mbar_wait(&wbar[1], wph[1], MB_POLLS);
+        // a wait gave up: give the copies and MMAs still in flight a last
+        // bounded chance to finish before TMEM and shared memory are released
+        if (pend[0]) mbar_wait(&wbar[0], wph[0], MB_POLLS);
+        if (pend[1]) mbar_wait(&wbar[1], wph[1], MB_POLLS);
+        if (mpend) mbar_wait(&bar, phase, MB_POLLS);
         if (threadIdx.x == 0) atomicAdd(a.err, 1u);
     }
     tc_fence_before();
@@ -535,6 +554,7 @@ struct MlpNet {
     __nv_bfloat16* T2 = nullptr;
     float* loss = nullptr;
     unsigned int* err = nullptr;
+    uint32_t polls = MB_POLLS;  // inference wait limit (reprobus_mlp_set_wait_limit)
     float* W(int l) const {
         size_t o = 0;
         for (int i = 0; i < l; i++) o += wsize(i) + mlp_fan_out(i);
@@ -690,6 +710,7 @@ int mlp_infer(void* net, const float* X, float* Y, int B, cudaStream_t s) {
     for (int l = 0; l < MLP_NL; l++) a.b[l] = n->P + n->off(l) + wsize(l);
     a.norm = n->norm;
     a.err = n->err;
+    a.polls = n->polls;
     const size_t smem = 196608 + (3 * MLP_H + MLP_OUT + MLP_NNORM) * sizeof(float);
     if (!n->nsm) {  // once per network (not while a graph is being captured)
         int dev = 0;
@@ -859,7 +880,16 @@ extern "C" int reprobus_mlp_forward(void* net, const float* X, float* Y, int B, 
     if (!n) return reprobus_set_error(REPROBUS_ERR_ARG, "net is NULL");
     if (!X || !Y || B <= 0) return reprobus_set_error(REPROBUS_ERR_ARG, "bad forward arguments");
     cudaStream_t s = (cudaStream_t)stream;
+    MLP_TRY(cudaMemsetAsync(n->err, 0, sizeof(unsigned int), s));
     int rc = mlp_infer(n, X, Y, B, s);
     if (rc) return rc;
     return check_err(n, s);
+}
+
+extern "C" int reprobus_mlp_set_wait_limit(void* net, long long polls) {
+    MlpNet* n = (MlpNet*)net;
+    if (!n) return reprobus_set_error(REPROBUS_ERR_ARG, "net is NULL");
+    if (polls > 0xffffffffLL) return reprobus_set_error(REPROBUS_ERR_ARG, "polls above 2^32 - 1");
+    n->polls = polls < 0 ? MB_POLLS : (uint32_t)polls;
+    return REPROBUS_OK;
 }

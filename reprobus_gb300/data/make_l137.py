@@ -4,14 +4,21 @@ L137 hybrid vertical grid, as tabulated in the REPROBUS source tree
 
 The reference reads the same coefficients from ecmwf_137_levels.txt at run time
 (src/reprobus_l137_20230723.f:79-91). Run once, with the reference checkout at
-REPROBUS_SRC (default /root/reference/src); the output is committed because the
+REPROBUS_SRC (the directory holding the reference's src files; required); the output is committed because the
 reference tree is not available where the library runs.
 """
 import csv
 import os
 import sys
 
-src = os.environ.get("REPROBUS_SRC", "/root/reference/src")
+
+def _src_dir():
+    d = os.environ.get("REPROBUS_SRC")
+    if not d:
+        sys.exit("set REPROBUS_SRC to the reference checkout's src directory")
+    return d
+
+src = _src_dir()
 rows = []
 with open(os.path.join(src, "ecmwf_levels_table.csv")) as f:
     rd = csv.reader(f)

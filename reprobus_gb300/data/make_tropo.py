@@ -5,7 +5,7 @@ reference's tropospheric relaxation interpolates in time, as tabulated in the
 
 These are observed surface mixing ratios (NOAA/GML, CCMVal), i.e. physical
 data that the port must reproduce exactly. Run once with the reference
-checkout at REPROBUS_SRC (default /root/reference/src); the output is committed
+checkout at REPROBUS_SRC (the directory holding the reference's src files; required); the output is committed
 because the reference tree is not available where the library is built and
 runs.
 """
@@ -13,11 +13,18 @@ import os
 import re
 import sys
 
+
+def _src_dir():
+    d = os.environ.get("REPROBUS_SRC")
+    if not d:
+        sys.exit("set REPROBUS_SRC to the reference checkout's src directory")
+    return d
+
 NAMES = ["noy", "cly", "bry", "n2o", "ch4", "ch3cl", "cfc11", "cfc12", "cfc114", "cfc115", "cfc113", "ccl4",
          "ch3ccl3", "hcfc22", "hcfc141b", "hcfc142b", "ch3br", "h1211", "h1301", "h2402", "ch2br2"]
 NYEAR = 37
 
-src = os.path.join(os.environ.get("REPROBUS_SRC", "/root/reference/src"), "reprobus_l137_20230723.f")
+src = os.path.join(_src_dir(), "reprobus_l137_20230723.f")
 lines = open(src).read().splitlines()
 lo, hi = 4077, 4574  # subroutine tropo
 body = lines[lo - 1:hi]

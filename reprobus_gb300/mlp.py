@@ -106,6 +106,13 @@ class Mlp:
         chem._check(self.lib.reprobus_mlp_forward(ctypes.c_void_p(self.handle), chem._dp(X), chem._dp(Y),
                                                   int(X.shape[0]), None))
 
+    def set_wait_limit(self, polls=-1):
+        """Polls after which the inference kernel's waits give up (-1: the
+        default; 0: at once). A fault-handling hook: a wait that gives up
+        makes forward() and the warm-started step raise REPROBUS_ERR_TIMEOUT
+        and leaves the network usable."""
+        chem._check(self.lib.reprobus_mlp_set_wait_limit(ctypes.c_void_p(self.handle), int(polls)))
+
     def save(self, path):
         p, n = self.get_params()
         np.savez(path, params=p, norm=n)

@@ -54,11 +54,18 @@ def test_bad_arguments_are_rejected(lib_built):
     assert rc == 1 and b"non-NULL" in lib.reprobus_last_error()
     z = np.zeros(40 * 101 * 27 * 7)
     o = np.zeros(80)
-    t = np.zeros(18)
+    t = chem.const()
     dp = ctypes.POINTER(ctypes.c_double)
     rc = lib.reprobus_chem_init(z.ctypes.data_as(dp), o.ctypes.data_as(dp), t.ctypes.data_as(dp), 10, 5, 137,
                                 140, 14, 1, 5, 0, ctypes.byref(h))
     assert rc == 1 and b"nivbas" in lib.reprobus_last_error()
+    # Troe prefactors must be positive and finite (the rate stage takes their logarithms)
+    for bad in (0.0, -1e-30, np.nan, np.inf):
+        tb = t.copy()
+        tb[5] = bad
+        rc = lib.reprobus_chem_init(z.ctypes.data_as(dp), o.ctypes.data_as(dp), tb.ctypes.data_as(dp), 10, 5, 137,
+                                    94, 14, 1, 5, 0, ctypes.byref(h))
+        assert rc == 1 and b"troe[5]" in lib.reprobus_last_error(), bad
     assert lib.reprobus_chem_step(None, 1, 1, 0., 0., *([None] * 5), 1, *([None] * 7), None) == 1
 
 

@@ -84,6 +84,33 @@ def test_rate_stage_matches_oracle(torch, nivbas):
     assert not bad, bad
 
 
+TROE_RATES = ("a1", "b12", "b22", "b23", "c4", "d31", "d36", "d60", "e13")  # :930-1303, the 9 falloff terms
+
+
+def test_troe_rates_over_a_temperature_and_density_sweep(torch):
+    """The nine Troe falloff rate constants, which the rate stage evaluates as
+    k = x kinf / (kinf + x) with log10(x / kinf) from logarithms, against the
+    reference's direct formula (the oracle) over T = 150..330 K (one value per
+    column) and every level's air density from the top of the L137 grid to
+    the surface."""
+    from reprobus_gb300.resident import DeviceCase
+    from reprobus_gb300.species import DIAG_RATE
+    case = inputs.make_case("cfg0", seed=22, nlon=64, nivbas=137)
+    T = np.linspace(150.0, 330.0, case.nlon)
+    case.trajtem[:, :, :, :] = T[:, None, None, None]
+    _, dref, _ = oracle.step(case, niter=1, fuse=False, diag=True)
+    h = ChemStep.for_case(case)
+    dc = DeviceCase(case)
+    diag = torch.zeros(DIAG_COUNT * case.ncells, dtype=torch.float64, device="cuda")
+    h.rates_dev(1, case.nlat, case.daynum, dc["alt"], dc["trajlon"], dc["trajlat"], dc["trajpre"], dc["trajtem"],
+                case.irapp, dc["qj1"], dc["hc"], diag)
+    d = diag.cpu().numpy().reshape(DIAG_COUNT, case.ncells)
+    h.close()
+    worst = {k: float(relerr(d[DIAG_NAMES.index(k)], dref[DIAG_NAMES.index(k)]).max()) for k in TROE_RATES}
+    assert all(DIAG_NAMES.index(k) >= DIAG_RATE for k in TROE_RATES)
+    assert max(worst.values()) <= 1e-13, worst
+
+
 @pytest.mark.parametrize("nivbas,seed", [(94, 31), (137, 32)])
 def test_step_matches_oracle(torch, nivbas, seed):
     case = inputs.make_case("cfg0", seed=seed, nlon=64, nivbas=nivbas)

@@ -68,9 +68,54 @@ def test_noalloc_row_subset_after_a_larger_call():
     h.step_dev(2, 3, case.daynum, case.dt, *ref.args())
     torch.cuda.synchronize()
     a, b = sub.state_host(), ref.state_host()
-    for f in ("qj1", "hc"):
-        assert relerr(a[f], b[f]).max() <= STEP_TOL
+    for f in ("qj1", "hc", "sza3d", "vsed3d", "parth2osed", "parthno3sed", "surfarea"):
+        assert relerr(a[f], b[f]).max() <= STEP_TOL, (f, relerr(a[f], b[f]).max())
     h.close()
+
+
+def test_noalloc_on_a_caller_stream_back_to_back():
+    # two calls on the caller's stream with no synchronisation between them
+    # (calls on one stream run in order, so they do not race on the scratch)
+    torch = pytest.importorskip("torch")
+    from reprobus_gb300 import ChemStep, chem, inputs
+    from reprobus_gb300.resident import DeviceCase
+
+    case = inputs.make_case("grid", seed=54, nlon=20, nlat=4, nivbas=94)
+    flags = chem.FUSE_CONSERV
+    ajl, o3up = _dev(torch, case.ajl), _dev(torch, case.o3up)
+    s = torch.cuda.Stream()
+    new = DeviceCase(case)
+    torch.cuda.synchronize()
+    for _ in range(2):
+        chem.step_noalloc(ajl, o3up, case.troe, case.nlon, case.nlat, case.niv, case.nivbas, case.nivhau,
+                          case.nrappmax, 5, flags, 1, case.nlat, case.daynum, case.dt, *new.args(), stream=s)
+    s.synchronize()
+    h = ChemStep.for_case(case, niter=5, flags=flags)
+    h.set_stream(s)
+    ref = DeviceCase(case)
+    for _ in range(2):
+        h.step_dev(1, case.nlat, case.daynum, case.dt, *ref.args())
+    s.synchronize()
+    a, b = new.state_host(), ref.state_host()
+    for f in ("qj1", "hc", "sza3d", "vsed3d", "parth2osed", "parthno3sed", "surfarea"):
+        assert relerr(a[f], b[f]).max() <= STEP_TOL, (f, relerr(a[f], b[f]).max())
+    h.close()
+
+
+def test_noalloc_refuses_troe_prefactors_that_are_not_positive():
+    torch = pytest.importorskip("torch")
+    from reprobus_gb300 import chem, inputs
+    from reprobus_gb300.resident import DeviceCase
+
+    case = inputs.make_case("grid", seed=55, nlon=8, nlat=2, nivbas=94)
+    dc = DeviceCase(case)
+    ajl, o3up = _dev(torch, case.ajl), _dev(torch, case.o3up)
+    bad = np.array(case.troe, dtype=np.float64)
+    bad[4] = -bad[4]
+    with pytest.raises(chem.ReprobusError) as ei:
+        chem.step_noalloc(ajl, o3up, bad, case.nlon, case.nlat, case.niv, case.nivbas, case.nivhau,
+                          case.nrappmax, 5, chem.FUSE_CONSERV, 1, case.nlat, case.daynum, case.dt, *dc.args())
+    assert ei.value.code == 1 and "troe" in str(ei.value)
 
 
 def test_noalloc_rejects_requests_beyond_its_scratch():
