@@ -516,8 +516,13 @@ def main():
         pcase = inputs.make_case("cfg2", seed=replica_seed(4321, rank))
         pacc = Accuracy(pcase) if (rank == 0 and not args.no_accuracy) else None
         pdc = DeviceCase(pcase)
-        pres = time_arms(torch, h, pcase, pdc, stream, parms, args.polar_steps, args.warmup, net, npass_of, world,
+        ph = ChemStep.for_case(pcase, niter=5, flags=FUSE_CONSERV)  # the case's own tables (o3up is seeded)
+        if args.lanes:
+            ph.set_tuning(args.lanes, args.bps, args.zshared)
+        ph.set_stream(stream)
+        pres = time_arms(torch, ph, pcase, pdc, stream, parms, args.polar_steps, args.warmup, net, npass_of, world,
                          pacc)
+        ph.close()
         polar = {"workload": f"cfg2: {pcase.nlon}x{pcase.nlat}x{pcase.niv} = {pcase.ncells} cells, 30% of the "
                              f"columns in polar winter (T 183-195 K, SZA > 95, active ClOx), day {pcase.daynum}",
                  "steps": args.polar_steps, "solvers": pres,
@@ -528,8 +533,6 @@ def main():
                  "accuracy_sample": pacc.describe() if pacc else None}
         del pdc
         torch.cuda.empty_cache()
-        h.set_solver(SOLVER_ID[headline], npass=npass_of(headline), maxit=12, tol=1e-5)
-        h.set_mlp(net if headline == "mlp" else None)
 
     line = None
     if rank == 0:

@@ -192,8 +192,10 @@ int reprobus_chem_set_solver(void* handle, int solver, int npass, int maxit, dou
  * that evaluates the FP64 residual while the first evaluates the Jacobian;
  * lanes_per_block then counts cells: 64, 128 mixed, 32, 64 FP64; 4: in
  * registers, the warps of a block passing each phase of an iteration
- * together, so that they fetch the same code: 64, 128 mixed, 32, 64 FP64)
- * and blocks_per_sm (0: as many as fit).
+ * together, so that they fetch the same code: 64, 128 mixed, 32, 64 FP64;
+ * 5: as 4 with the FP32 matrix slots stored as BF16, half the shared memory
+ * per cell, so that an SM keeps up to twice the cells in flight: 64, 128,
+ * 256 mixed) and blocks_per_sm (0: as many as fit).
  * When the environment variable REPROBUS_TUNE_CACHE names a file, the
  * autotuner first looks there for a choice made for the same GPU model,
  * matrix precision and cell count (skipping the timing runs), and appends
@@ -248,7 +250,10 @@ int reprobus_mlp_set_wait_limit(void* net, long long polls);
  * solvers then start every cell from the network's prediction instead of the
  * plain start; a cell whose predicted start misses the convergence test is
  * solved again from the plain start (stats.warm_restarts), and one that
- * misses again falls back to the reference passes. */
+ * misses again falls back to the reference passes. If the inference kernel
+ * gives up waiting, every cell of the step starts from the plain start (the
+ * answer is unchanged) and a call that reads the step's counters (stats
+ * requested, or REPROBUS_CHECK_FINITE) returns REPROBUS_ERR_TIMEOUT. */
 int reprobus_chem_set_mlp(void* handle, void* net);
 
 /* The 64 raw features of every chemistry cell of rows ilat0..ilat1 at the

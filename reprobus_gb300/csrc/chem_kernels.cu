@@ -524,17 +524,22 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
 // A block takes 128 cells and walks their iterates element by element, so
 // that consecutive threads touch consecutive words of x (cell-major, NT_NX
 // per cell) and of the predictions (64 per cell).
+// An inference that gave up (its error flag set) left no predictions: every
+// cell keeps its plain start and counter 7 records the timeout for the host.
 __global__ void __launch_bounds__(128) k_nt_warm(Params P) {
     const int c0 = blockIdx.x * 128;
     const int nc = P.ncell - c0 < 128 ? P.ncell - c0 : 128;
+    const bool failed = P.mlp_err && *P.mlp_err != 0u;
+    if (failed && blockIdx.x == 0 && threadIdx.x == 0) P.nonfinite[7] = 1ULL;
     double* x = P.nt_x + (size_t)c0 * NT_NX;
     for (int e = threadIdx.x; e < nc * NT_NX; e += blockDim.x) {
         const int cl = e / NT_NX, i = e - cl * NT_NX;
         const size_t cell = (size_t)c0 + cl;
         const double hnm = P.nt_rec[cell * NT_REC + NT_RF + 4];
-        const float yi = fminf(fmaxf(P.mlp_y[cell * 64 + i], -30.f), 30.f);
         const double xe = x[e];
         P.nt_xp[(size_t)c0 * NT_NX + e] = xe;  // the plain start, for a retry
+        if (failed) continue;
+        const float yi = fminf(fmaxf(P.mlp_y[cell * 64 + i], -30.f), 30.f);
         x[e] = fmax(xe, 1e-30 * hnm) * nt_widen(exp10f(yi));
     }
 }
@@ -975,15 +980,16 @@ static void fill_params(const Handle* h, Params& P, int ilat0, int ilat1) {
 // every compiled solve-kernel variant of one matrix precision
 static int nt_all_variants(bool mixed, const NtVariant** out, int cap) {
     int n = 0, k = 0;
-    const NtVariant* lists[5];
-    int counts[5] = {0, 0, 0, 0, 0};
-    const int nl = 5;
+    const NtVariant* lists[6] = {};
+    int counts[6] = {0, 0, 0, 0, 0, 0};
+    const int nl = 6;
     if (mixed) {
         lists[0] = nt_variants_f32_zr(&counts[0]);
         lists[1] = nt_variants_f32_zs(&counts[1]);
         lists[2] = nt_variants_f32_pp(&counts[2]);
         lists[3] = nt_variants_f32_sp(&counts[3]);
         lists[4] = nt_variants_f32_ls(&counts[4]);
+        lists[5] = nt_variants_f32_lsb(&counts[5]);
     } else {
         lists[0] = nt_variants_f64_zr(&counts[0]);
         lists[1] = nt_variants_f64_zs(&counts[1]);
@@ -1092,8 +1098,8 @@ static int choose_shape(Handle* h, Params& P, bool mixed) {
         tune_key(h, mixed, P.ncell, key, sizeof(key));
         int nth = 0, zs = 0, bps = 0;
         if (tune_cache_lookup(cache, key, &nth, &zs, &bps)) {
-            const NtVariant* vc[16];
-            const int n = nt_all_variants(mixed, vc, 16);
+            const NtVariant* vc[32];
+            const int n = nt_all_variants(mixed, vc, 32);
             for (int i = 0; i < n; i++) {
                 if (vc[i]->nth != nth || vc[i]->zshared != zs) continue;
                 int occ = 0;
@@ -1105,10 +1111,10 @@ static int choose_shape(Handle* h, Params& P, bool mixed) {
             }
         }
     }
-    const NtVariant* vs[16];
-    const int nv = nt_all_variants(mixed, vs, 16);
+    const NtVariant* vs[32];
+    const int nv = nt_all_variants(mixed, vs, 32);
     struct Cand { const NtVariant* v; int bps; };
-    Cand cands[32];
+    Cand cands[64];
     int nc = 0;
     // a requested shape that this precision does not have: autotune it instead
     bool want = h->want_lanes > 0;
@@ -1127,7 +1133,7 @@ static int choose_shape(Handle* h, Params& P, bool mixed) {
             cands[nc++] = {vs[i], b};
             continue;
         }
-        for (int b = 1; b <= occ && nc < 32; b++) cands[nc++] = {vs[i], b};
+        for (int b = 1; b <= occ && nc < 64; b++) cands[nc++] = {vs[i], b};
     }
     if (nc == 0)
         return set_err(REPROBUS_ERR_ARG, "no compiled solve-kernel shape with %d lanes per block fits", h->want_lanes);
@@ -1185,6 +1191,7 @@ static int newton_prepare(Handle* h, Params& P) {
         P.warm = 1;
         P.mlp_feat = h->mlp_feat;
         P.mlp_y = h->mlp_y;
+        P.mlp_err = mlp_err_flag(h->mlp);
         P.nt_xp = h->nt_xp;
     }
     return choose_shape(h, P, mixed);
@@ -1319,6 +1326,9 @@ static int step_stats(Handle* h, const Params& P, reprobus_stats* st, int launch
             st->failed_iters = (long long)c[5];
             st->start64_cells = (long long)c[6];
         }
+        if (c[7])
+            return set_err(REPROBUS_ERR_TIMEOUT,
+                           "the warm-start inference gave up waiting (its cells started from the plain start)");
         if (P.check && c[0]) return set_err(REPROBUS_ERR_NONFINITE, "%llu non-finite values in the step output", c[0]);
     }
     return REPROBUS_OK;
@@ -1382,12 +1392,12 @@ extern "C" int reprobus_chem_set_tuning(void* handle, int lanes_per_block, int b
     Handle* h = (Handle*)handle;
     if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
     if (lanes_per_block < 0 || blocks_per_sm < 0) return set_err(REPROBUS_ERR_ARG, "bad tuning values");
-    if (zshared < 0 || zshared > 4) return set_err(REPROBUS_ERR_ARG, "zshared must be 0 .. 4");
+    if (zshared < 0 || zshared > 5) return set_err(REPROBUS_ERR_ARG, "zshared must be 0 .. 5");
     if (lanes_per_block > 0) {
         bool found = false;
-        const NtVariant* vs[16];
+        const NtVariant* vs[32];
         for (int m = 0; m < 2; m++) {
-            const int nv = nt_all_variants(m == 0, vs, 16);
+            const int nv = nt_all_variants(m == 0, vs, 32);
             for (int i = 0; i < nv; i++) found |= vs[i]->nth == lanes_per_block && vs[i]->zshared == zshared;
         }
         if (!found)

@@ -35,7 +35,10 @@ struct Params {
     const double* __restrict__ o3up;
     double* col;               // scratch: o3t | colo2 | colno (ncell each) | sza_top (ncol)
     unsigned long long* nonfinite;  // [0] non-finite values, [1] Newton iterations,
-                                    // [2] fallbacks, [3] max iterations of a cell
+                                    // [2] fallbacks, [3] max iterations of a cell,
+                                    // [4] warm restarts, [5] iterations of attempts
+                                    // that missed, [6] FP64 redos of the FP32 start,
+                                    // [7] warm-start inference timed out
     double* diag;
     int npass, maxit;               // Newton: reference passes before, iteration cap
     double tol;                     // Newton: scaled step tolerance
@@ -51,6 +54,7 @@ struct Params {
     int warm;                       // 1: features for the warm-start network, start from its prediction
     float* mlp_feat;                // 64 raw features per cell (row-major)
     const float* mlp_y;             // 64 predicted log10 end-of-step ratios per cell (57 used)
+    const unsigned int* mlp_err;    // the inference kernel's error flag: set, the predictions are not used
     double* nt_xp;                  // warm start: the plain start of every cell (NT_NX doubles)
     StepConst sc;
 };
