@@ -614,11 +614,10 @@ def emit_residual(w, tag, m, res, P):
 def emit_jacobian(w, tag, m, pat, union, const, slot_a, pos, XP):
     w("")
     w(f"// scaled Jacobian J'_ij = dR_i/dx_j s_j / s_i, {tag} equations, into the")
-    w("// stored A slots (T = double or float; x: FP64 iterate, a pointer or view;")
-    w("// s: nt_exp_hi scales)")
-    w("template <typename T, typename FF, typename PK, typename PX, typename PJ>")
+    w("// stored A slots (T = double or float; x: FP64 iterate; s: nt_exp_hi scales)")
+    w("template <typename T, typename FF, typename PK, typename PJ>")
     w(f"__device__ __forceinline__ void nt_jacobian_{tag}(const FF& F, PK K, PK tj, PK het, "
-      "PX x, double floor_, PJ J) {")
+      "const double* __restrict__ x, double floor_, PJ J) {")
     w("    const int fh = nt_exp_hi(floor_);")
     chunks = emit_statements(m, XP, derivs=True)
     by_row = {}

@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(NTB) k_nt_setup(Params P) {
     const CellFix& F = C.F;
     const double fx[14] = {F.o2, F.n2, F.h2, F.co2, F.hnm, F.parthno3, F.parth2o, F.parthcl, F.parthbr,
                            F.rain_hno3, F.rain_hcl, F.rain_hbr, F.rain_h2o2, P.sc.dt};
-    const NtT<double> r = nt_tile(P.nt_rec, cell, NT_REC);
+    double* r = P.nt_rec + (size_t)cell * NT_REC;
 #pragma unroll 4
     for (int n = 0; n < NRATE; n++) r[NT_RK + n] = C.K[n];
 #pragma unroll 4
@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(NTB) k_nt_setup(Params P) {
 #pragma unroll 4
     for (int n = 0; n < NBCON; n++) r[NT_RCK0 + n] = C.ck0[n];
     if (MIXED) {
-        const NtT<float> q = nt_tile(P.nt_rec32, cell, NT_REC32);
+        float* q = P.nt_rec32 + (size_t)cell * NT_REC32;
 #pragma unroll 4
         for (int n = 0; n < NRATE; n++) q[NT_RK + n] = (float)C.K[n];
 #pragma unroll 4
@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(128) k_nt_start(Params P) {
     if (t >= P.win_ncell) return;
     const int cell = win_cell(P, t);
     if (MODE != 0 && P.nt_stat[cell] >= 0) return;
-    const NtT<const double> r = nt_tile((const double*)P.nt_rec, cell, NT_REC);
+    const double* r = P.nt_rec + (size_t)cell * NT_REC;
     CellFix F;
     F.o2 = r[NT_RF]; F.n2 = r[NT_RF + 1]; F.h2 = r[NT_RF + 2]; F.co2 = r[NT_RF + 3]; F.hnm = r[NT_RF + 4];
     F.parthno3 = r[NT_RF + 5]; F.parth2o = r[NT_RF + 6]; F.parthcl = r[NT_RF + 7]; F.parthbr = r[NT_RF + 8];
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(128) k_nt_start(Params P) {
     for (int n = 0; n < NCM; n++) cc[n] = P.hc[g + pl * n] * F.hnm;
 #pragma unroll 1
     for (int it = 0; it < P.npass_plain; it++) cell_pass(F, K, tj, het, ck0, P.sc.dt, ck, cc);
-    const NtT<double> x = nt_tile(P.nt_x, cell, NT_NX);
+    double* x = P.nt_x + (size_t)cell * NT_NX;
 #pragma unroll
     for (int n = 0; n < NBCON - 1; n++) x[n] = ck[n];
 #pragma unroll
@@ -460,8 +460,8 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= P.win_ncell) return;
     const int cell = win_cell(P, t);
-    const NtT<const double> r = nt_tile((const double*)P.nt_rec, cell, NT_REC);
-    const NtT<const float> q = nt_tile((const float*)P.nt_rec32, cell, NT_REC32);
+    const double* r = P.nt_rec + (size_t)cell * NT_REC;
+    const float* q = P.nt_rec32 + (size_t)cell * NT_REC32;
     const double hnm = r[NT_RF + 4];
     const bool day = r[NT_RSZA] <= 95.;
     CellFixT<float> F;
@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
         P.nt_stat[cell] = -1;
         return;
     }
-    const NtT<double> x = nt_tile(P.nt_x, cell, NT_NX);
+    double* x = P.nt_x + (size_t)cell * NT_NX;
     double xd[NT_NX];
 #pragma unroll
     for (int n = 0; n < NBCON - 1; n++) x[n] = xd[n] = nt_widen(ck[n]);
@@ -521,27 +521,25 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
 
 // warm start: x_i = max(x_i, 1e-30 hnm) 10^y_i from the network's prediction;
 // the plain start is kept in nt_xp for a cell whose warm start misses.
-// A block takes 128 cells (four tiles, contiguous in the tiled iterate array)
-// and walks them element by element, consecutive threads on consecutive
-// words of x.
+// A block takes 128 cells and walks their iterates element by element, so
+// that consecutive threads touch consecutive words of x (cell-major, NT_NX
+// per cell) and of the predictions (64 per cell).
 // An inference that gave up (its error flag set) left no predictions: every
 // cell keeps its plain start and counter 7 records the timeout for the host.
 __global__ void __launch_bounds__(128) k_nt_warm(Params P) {
     const int c0 = blockIdx.x * 128;
+    const int nc = P.ncell - c0 < 128 ? P.ncell - c0 : 128;
     const bool failed = P.mlp_err && *P.mlp_err != 0u;
     if (failed && blockIdx.x == 0 && threadIdx.x == 0) P.nonfinite[7] = 1ULL;
-    double* x = P.nt_x + (size_t)c0 * NT_NX;     // tile c0 / NT_TILE onwards
-    double* xp = P.nt_xp + (size_t)c0 * NT_NX;
-    for (int e = threadIdx.x; e < 128 * NT_NX; e += blockDim.x) {
-        const int tl = e / (NT_NX * NT_TILE), rem = e - tl * (NT_NX * NT_TILE);
-        const int i = rem / NT_TILE;
-        const int cell = c0 + tl * NT_TILE + (rem - i * NT_TILE);
-        if (cell >= P.ncell) continue;
-        const double hnm = nt_tile((const double*)P.nt_rec, cell, NT_REC)[NT_RF + 4];
+    double* x = P.nt_x + (size_t)c0 * NT_NX;
+    for (int e = threadIdx.x; e < nc * NT_NX; e += blockDim.x) {
+        const int cl = e / NT_NX, i = e - cl * NT_NX;
+        const size_t cell = (size_t)c0 + cl;
+        const double hnm = P.nt_rec[cell * NT_REC + NT_RF + 4];
         const double xe = x[e];
-        xp[e] = xe;  // the plain start, for a retry
+        P.nt_xp[(size_t)c0 * NT_NX + e] = xe;  // the plain start, for a retry
         if (failed) continue;
-        const float yi = fminf(fmaxf(P.mlp_y[(size_t)cell * 64 + i], -30.f), 30.f);
+        const float yi = fminf(fmaxf(P.mlp_y[cell * 64 + i], -30.f), 30.f);
         x[e] = fmax(xe, 1e-30 * hnm) * nt_widen(exp10f(yi));
     }
 }
@@ -554,7 +552,7 @@ __global__ void __launch_bounds__(128) k_nt_warm(Params P) {
 __global__ void __launch_bounds__(128) k_ref_passes(Params P) {
     const int cell = blockIdx.x * blockDim.x + threadIdx.x;
     if (cell >= P.ncell) return;
-    const NtT<const double> r = nt_tile((const double*)P.nt_rec, cell, NT_REC);
+    const double* r = P.nt_rec + (size_t)cell * NT_REC;
     CellPro C;
     C.g = cell_global(P, cell);
     CellFix& F = C.F;
@@ -583,8 +581,8 @@ __global__ void __launch_bounds__(128) k_ref_passes(Params P) {
 // the write-back of one cell's Newton answer (mixing ratios, fused conserv
 // and clamps); cells the solver handed to its fallback (stat <= 0) are left
 // to k_nt_fallback, so that this common path stays small
-__device__ __forceinline__ void nt_cell_fix(NtT<const double> r, CellFix& F) {
-    const NtT<const double> f = r + NT_RF;
+__device__ __forceinline__ void nt_cell_fix(const double* r, CellFix& F) {
+    const double* f = r + NT_RF;
     F.o2 = f[0]; F.n2 = f[1]; F.h2 = f[2]; F.co2 = f[3]; F.hnm = f[4]; F.parthno3 = f[5];
     F.parth2o = f[6]; F.parthcl = f[7]; F.parthbr = f[8]; F.rain_hno3 = f[9];
     F.rain_hno4 = 0.; F.rain_hcl = f[10]; F.rain_hbr = f[11]; F.rain_h2o2 = f[12];
@@ -598,8 +596,8 @@ __global__ void __launch_bounds__(128) k_nt_finish(Params P) {
     const int cell = win_cell(P, t);
     const int stat = P.nt_stat[cell];
     if (stat <= 0) return;
-    const NtT<const double> r = nt_tile((const double*)P.nt_rec, cell, NT_REC);
-    const NtT<const double> x = nt_tile((const double*)P.nt_x, cell, NT_NX);
+    const double* r = P.nt_rec + (size_t)cell * NT_REC;
+    const double* x = P.nt_x + (size_t)cell * NT_NX;
     CellPro C;
     C.g = cell_global(P, cell);
     nt_cell_fix(r, C.F);
@@ -621,7 +619,7 @@ __global__ void __launch_bounds__(128) k_nt_fallback(Params P) {
     if (t >= P.win_ncell) return;
     const int cell = win_cell(P, t);
     if (P.nt_stat[cell] > 0) return;
-    const NtT<const double> r = nt_tile((const double*)P.nt_rec, cell, NT_REC);
+    const double* r = P.nt_rec + (size_t)cell * NT_REC;
     CellPro C;
     C.g = cell_global(P, cell);
     CellFix& F = C.F;
@@ -1007,10 +1005,9 @@ static int nt_all_variants(bool mixed, const NtVariant** out, int cap) {
 static int ensure_newton(Handle* h) {
     if (h->nt_x) return REPROBUS_OK;
     const size_t nc = (size_t)h->nlon * h->nlat * h->nivbas;
-    const size_t nt = nt_tiled_cells(nc);  // the tiled arrays hold whole tiles
-    CUDA_TRY(cudaMalloc(&h->nt_rec, nt * NT_REC * sizeof(double)));
-    CUDA_TRY(cudaMalloc(&h->nt_rec32, nt * NT_REC32 * sizeof(float)));
-    CUDA_TRY(cudaMalloc(&h->nt_x, nt * NT_NX * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&h->nt_rec, nc * NT_REC * sizeof(double)));
+    CUDA_TRY(cudaMalloc(&h->nt_rec32, nc * NT_REC32 * sizeof(float)));
+    CUDA_TRY(cudaMalloc(&h->nt_x, nc * NT_NX * sizeof(double)));
     CUDA_TRY(cudaMalloc(&h->nt_stat, nc * sizeof(int)));
     CUDA_TRY(cudaMalloc(&h->nt_list, nc * sizeof(int)));
     CUDA_TRY(cudaMalloc(&h->nt_head, 8 * sizeof(int)));
@@ -1189,7 +1186,7 @@ static int newton_prepare(Handle* h, Params& P) {
             const size_t nc = (size_t)h->nlon * h->nlat * h->nivbas;
             CUDA_TRY(cudaMalloc(&h->mlp_feat, nc * MLP_FEAT * sizeof(float)));
             CUDA_TRY(cudaMalloc(&h->mlp_y, nc * MLP_YOUT * sizeof(float)));
-            CUDA_TRY(cudaMalloc(&h->nt_xp, nt_tiled_cells(nc) * NT_NX * sizeof(double)));
+            CUDA_TRY(cudaMalloc(&h->nt_xp, nc * NT_NX * sizeof(double)));
         }
         P.warm = 1;
         P.mlp_feat = h->mlp_feat;

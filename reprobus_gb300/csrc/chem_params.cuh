@@ -65,29 +65,8 @@ struct Params {
 // <= 95 deg), start-of-step number densities ck0 (43), aerosol surface area
 constexpr int NT_RK = 0, NT_RJ = NRATE, NT_RH = NRATE + NPHOT, NT_RF = NRATE + NPHOT + 9;
 constexpr int NT_RSZA = NT_RF + 14, NT_RCK0 = NT_RSZA + 1, NT_RSURF = NT_RCK0 + NBCON;
-constexpr int NT_REC = 208;    // FP64 record fields
-constexpr int NT_REC32 = 168;  // FP32 record fields (164 used)
-
-// The Newton solvers' per-cell arrays (the FP64 and FP32 records, the iterate
-// and the saved plain start) are tiled: cells are grouped in tiles of NT_TILE
-// consecutive cells, and a tile stores its cells field by field (field f of
-// the tile's cell p at f * NT_TILE + p). The lanes of a warp that hold cells
-// of one tile then read a field in one coalesced access, where a cell-major
-// record would cost one sector per lane.
-constexpr int NT_TILE = 32;
-template <typename T>
-struct NtT {
-    T* p;
-    __host__ __device__ __forceinline__ T& operator[](int f) const { return p[(size_t)f * NT_TILE]; }
-    __host__ __device__ __forceinline__ NtT operator+(int f) const { return NtT{p + (size_t)f * NT_TILE}; }
-};
-// the fields of `cell` in a tiled array of nfield fields per cell
-template <typename T>
-__host__ __device__ __forceinline__ NtT<T> nt_tile(T* base, size_t cell, int nfield) {
-    return NtT<T>{base + (cell / NT_TILE) * (size_t)nfield * NT_TILE + cell % NT_TILE};
-}
-// cells a tiled array is allocated for (whole tiles)
-__host__ __device__ inline size_t nt_tiled_cells(size_t nc) { return (nc + NT_TILE - 1) / NT_TILE * NT_TILE; }
+constexpr int NT_REC = 208;    // FP64 record stride (1664 B = 13 lines of 128 B)
+constexpr int NT_REC32 = 168;  // FP32 record stride (164 used)
 static_assert(NT_RSURF < NT_REC, "record layout");
 
 __device__ __forceinline__ size_t plane3(const Params& P) { return (size_t)P.nlon * P.nlat * P.niv; }

@@ -21,21 +21,11 @@
 
 namespace rpb {
 
-template <typename T, typename PR>
-__device__ __forceinline__ void nt_load_fix(PR r, NtFixT<T>& F) {
+template <typename T>
+__device__ __forceinline__ void nt_load_fix(const T* r, NtFixT<T>& F) {
     F.o2 = r[0]; F.n2 = r[1]; F.h2 = r[2]; F.co2 = r[3]; F.hnm = r[4];
     F.parthno3 = r[5]; F.parth2o = r[6]; F.parthcl = r[7]; F.parthbr = r[8];
     F.rain_hno3 = r[9]; F.rain_hcl = r[10]; F.rain_hbr = r[11]; F.rain_h2o2 = r[12]; F.dt = r[13];
-}
-
-// the record the Jacobian reads: the FP32 copy for an FP32 matrix, the FP64
-// record itself for an FP64 one
-template <typename TJ>
-__device__ __forceinline__ NtT<const TJ> nt_rec_t(const Params& P, int cell) {
-    if constexpr (sizeof(TJ) == 4)
-        return nt_tile((const float*)P.nt_rec32, cell, NT_REC32);
-    else
-        return nt_tile((const double*)P.nt_rec, cell, NT_REC);
 }
 
 // entry q of the queue: day cells at list[0 .. nday), night cells from the back
@@ -51,8 +41,8 @@ __device__ __forceinline__ int nt_queue_cell(const Params& P, int q, int nday) {
 __device__ __forceinline__ bool nt_end_attempt(const Params& P, int cell, int done, int& it, int& attempt) {
     if (done < 0) atomicAdd(P.nonfinite + 5, (unsigned long long)it);  // iterations spent in vain
     if (done < 0 && P.warm && attempt == 0) {
-        const NtT<const double> xp = nt_tile((const double*)P.nt_xp, cell, NT_NX);
-        const NtT<double> x = nt_tile(P.nt_x, cell, NT_NX);
+        const double* xp = P.nt_xp + (size_t)cell * NT_NX;
+        double* x = P.nt_x + (size_t)cell * NT_NX;
 #pragma unroll 4
         for (int i = 0; i < NT_NX; i++) x[i] = xp[i];
         atomicAdd(P.nonfinite + 4, 1ULL);  // warm restarts
@@ -90,14 +80,18 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
         }
         if (__all_sync(0xffffffffu, cell == -2)) break;
         if (cell >= 0) {
-            const NtT<const double> rec = nt_tile((const double*)P.nt_rec, cell, NT_REC);
-            const NtT<const TJ> recT = nt_rec_t<TJ>(P, cell);
+            const double* rec = P.nt_rec + (size_t)cell * NT_REC;
+            const TJ* recT;
+            if constexpr (sizeof(TJ) == 4)
+                recT = P.nt_rec32 + (size_t)cell * NT_REC32;
+            else
+                recT = rec;
             NtFixT<double> F;
             NtFixT<TJ> FT;
             nt_load_fix<double>(rec + NT_RF, F);
             nt_load_fix<TJ>(recT + NT_RF, FT);
             const bool day = rec[NT_RSZA] <= 95.;
-            const NtT<double> x = nt_tile(P.nt_x, cell, NT_NX);
+            double* x = P.nt_x + (size_t)cell * NT_NX;
             TJ step;
             const bool ok = nt_iterate<TJ, ZS>(F, rec + NT_RK, rec + NT_RJ, rec + NT_RH, rec + NT_RCK0, FT, recT + NT_RK,
                                            recT + NT_RJ, recT + NT_RH, day, x, J, &step);
@@ -146,8 +140,8 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_pp(Params P) {
             // group 1 starts with the second phase
         } else if (!matrix_phase) {
             if (cell >= 0 && has_z) {
-                const NtT<const double> rec = nt_tile((const double*)P.nt_rec, cell, NT_REC);
-                const NtT<double> x = nt_tile(P.nt_x, cell, NT_NX);
+                const double* rec = P.nt_rec + (size_t)cell * NT_REC;
+                double* x = P.nt_x + (size_t)cell * NT_NX;
                 TJ step;
                 const bool ok = nt_update<TJ>(x, 1e-20 * rec[NT_RF + 4], (const TJ*)z, &step, true);
                 it++;
@@ -175,21 +169,25 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_pp(Params P) {
                 }
             }
             if (cell >= 0) {
-                const NtT<const double> rec = nt_tile((const double*)P.nt_rec, cell, NT_REC);
+                const double* rec = P.nt_rec + (size_t)cell * NT_REC;
                 NtFixT<double> F;
                 nt_load_fix<double>(rec + NT_RF, F);
                 const bool day = rec[NT_RSZA] <= 95.;
                 nt_rhs<TJ>(day, F, rec + NT_RK, rec + NT_RJ, rec + NT_RH, rec + NT_RCK0,
-                           nt_tile((const double*)P.nt_x, cell, NT_NX), 1e-20 * F.hnm, (TJ*)z);
+                           (const double*)(P.nt_x + (size_t)cell * NT_NX), 1e-20 * F.hnm, (TJ*)z);
                 has_z = true;
             }
         } else if (cell >= 0) {
-            const NtT<const double> rec = nt_tile((const double*)P.nt_rec, cell, NT_REC);
-            const NtT<const TJ> recT = nt_rec_t<TJ>(P, cell);
+            const double* rec = P.nt_rec + (size_t)cell * NT_REC;
+            const TJ* recT;
+            if constexpr (sizeof(TJ) == 4)
+                recT = P.nt_rec32 + (size_t)cell * NT_REC32;
+            else
+                recT = rec;
             NtFixT<TJ> FT;
             nt_load_fix<TJ>(recT + NT_RF, FT);
             const bool day = rec[NT_RSZA] <= 95.;
-            const NtT<const double> x = nt_tile((const double*)P.nt_x, cell, NT_NX);
+            const double* x = P.nt_x + (size_t)cell * NT_NX;
             nt_jacobian_call<TJ>(day, FT, recT + NT_RK, recT + NT_RJ, recT + NT_RH, x, 1e-20 * rec[NT_RF + 4], J);
             NT_FENCE();
             nt_factor_solve<TJ>(J, (TJ*)z, TJ(NT_TINY));
@@ -260,11 +258,15 @@ __global__ void __launch_bounds__(2 * NS, 1) k_nt_solve_sp(Params P) {
         if (__syncthreads_and(c == -2)) break;
         // phase A
         if (c >= 0) {
-            const NtT<const double> rec = nt_tile((const double*)P.nt_rec, c, NT_REC);
+            const double* rec = P.nt_rec + (size_t)c * NT_REC;
             const bool day = rec[NT_RSZA] <= 95.;
-            const NtT<const double> x = nt_tile((const double*)P.nt_x, c, NT_NX);
+            const double* x = P.nt_x + (size_t)c * NT_NX;
             if (matrix_lane) {
-                const NtT<const TJ> recT = nt_rec_t<TJ>(P, c);
+                const TJ* recT;
+                if constexpr (sizeof(TJ) == 4)
+                    recT = P.nt_rec32 + (size_t)c * NT_REC32;
+                else
+                    recT = rec;
                 NtFixT<TJ> FT;
                 nt_load_fix<TJ>(recT + NT_RF, FT);
                 nt_jacobian_call<TJ>(day, FT, recT + NT_RK, recT + NT_RJ, recT + NT_RH, x, 1e-20 * rec[NT_RF + 4], J);
@@ -278,8 +280,8 @@ __global__ void __launch_bounds__(2 * NS, 1) k_nt_solve_sp(Params P) {
         // phase B
         if (matrix_lane) {
             if (c >= 0) {
-                const NtT<const double> rec = nt_tile((const double*)P.nt_rec, c, NT_REC);
-                const NtT<double> x = nt_tile(P.nt_x, c, NT_NX);
+                const double* rec = P.nt_rec + (size_t)c * NT_REC;
+                double* x = P.nt_x + (size_t)c * NT_NX;
                 NT_FENCE();
                 nt_factor_solve<TJ>(J, z, TJ(NT_TINY));
                 TJ step;
@@ -373,10 +375,13 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_ls(Params P) {
             }
         }
         if (__syncthreads_and(cell == -2)) break;
-        const int cv = cell > 0 ? cell : 0;
-        const NtT<const double> rec = nt_tile((const double*)P.nt_rec, cv, NT_REC);
-        const NtT<const TJ> recT = nt_rec_t<TJ>(P, cv);
-        const NtT<double> x = nt_tile(P.nt_x, cv, NT_NX);
+        const double* rec = P.nt_rec + (size_t)(cell > 0 ? cell : 0) * NT_REC;
+        const TJ* recT;
+        if constexpr (sizeof(TJ) == 4)
+            recT = P.nt_rec32 + (size_t)(cell > 0 ? cell : 0) * NT_REC32;
+        else
+            recT = rec;
+        double* x = P.nt_x + (size_t)(cell > 0 ? cell : 0) * NT_NX;
         const bool day = rec[NT_RSZA] <= 95.;
         const double floor_ = 1e-20 * rec[NT_RF + 4];
         if (cell >= 0) {

@@ -81,26 +81,26 @@ struct NtRhsRef {
         z[i] = nt_cvt<TJ>(-r) * nt_rscale<TJ>(nt_exp_hi(xi), fh);
     }
 };
-template <typename TJ, typename PZ, typename PX>
+template <typename TJ, typename PZ>
 struct NtRhsOut {
     PZ z;
-    PX x;
+    const double* x;
     int fh;
     __device__ __forceinline__ NtRhsRef<TJ, PZ> operator[](int i) const { return NtRhsRef<TJ, PZ>{z, i, x[i], fh}; }
 };
-template <typename TJ, typename FF, typename PK, typename PC, typename PX, typename PZ>
-__device__ __forceinline__ void nt_rhs(bool day, const FF& F, PK K, PK tj, PK het, PC ck0, PX x, double floor_,
-                                       PZ z) {
-    const NtRhsOut<TJ, PZ, PX> R{z, x, nt_exp_hi(floor_)};
+template <typename TJ, typename FF, typename PK, typename PC, typename PZ>
+__device__ __forceinline__ void nt_rhs(bool day, const FF& F, PK K, PK tj, PK het, PC ck0,
+                                       const double* __restrict__ x, double floor_, PZ z) {
+    const NtRhsOut<TJ, PZ> R{z, x, nt_exp_hi(floor_)};
     if (day)
         nt_residual_day<double>(F, K, tj, het, ck0, x, R);
     else
         nt_residual_night<double>(F, K, tj, het, ck0, x, R);
 }
 // the same as a call of its own (z in shared memory)
-template <typename TJ, typename FF, typename PK, typename PC, typename PX, typename PZ>
-__device__ __noinline__ void nt_rhs_fn(bool day, const FF& F, PK K, PK tj, PK het, PC ck0, PX x, double floor_,
-                                       PZ z) {
+template <typename TJ, typename FF, typename PK, typename PC, typename PZ>
+__device__ __noinline__ void nt_rhs_fn(bool day, const FF& F, PK K, PK tj, PK het, PC ck0,
+                                       const double* __restrict__ x, double floor_, PZ z) {
     nt_rhs<TJ>(day, F, K, tj, het, ck0, x, floor_, z);
 }
 
@@ -113,16 +113,16 @@ struct SJZ {
 
 // the Jacobian of the day or night equations as a call of its own, so that
 // its register allocation does not meet the residual's and the solve's
-template <typename TJ, typename FFT, typename PKT, typename PX, typename PJ>
-__device__ __noinline__ void nt_jacobian_fn(bool day, const FFT& FT, PKT KT, PKT tjT, PKT hetT, PX x, double floor_,
-                                             PJ J) {
+template <typename TJ, typename FFT, typename PKT, typename PJ>
+__device__ __noinline__ void nt_jacobian_fn(bool day, const FFT& FT, PKT KT, PKT tjT, PKT hetT, const double* x,
+                                             double floor_, PJ J) {
     if (day)
         nt_jacobian_day<TJ>(FT, KT, tjT, hetT, x, floor_, J);
     else
         nt_jacobian_night<TJ>(FT, KT, tjT, hetT, x, floor_, J);
 }
-template <typename TJ, typename FFT, typename PKT, typename PX, typename PJ>
-__device__ __forceinline__ void nt_jacobian_call(bool day, const FFT& FT, PKT KT, PKT tjT, PKT hetT, PX x,
+template <typename TJ, typename FFT, typename PKT, typename PJ>
+__device__ __forceinline__ void nt_jacobian_call(bool day, const FFT& FT, PKT KT, PKT tjT, PKT hetT, const double* x,
                                                  double floor_, PJ J) {
 #ifdef __CUDA_ARCH__
     nt_jacobian_fn<TJ>(day, FT, KT, tjT, hetT, x, floor_, J);
@@ -138,15 +138,15 @@ __device__ __forceinline__ void nt_jacobian_call(bool day, const FFT& FT, PKT KT
 // of the residual; FT/KT/tjT/hetT: the same in TJ for the Jacobian. J: the
 // cell's NT_NSLOT matrix slots. Returns false when the step is not finite;
 // *step = max |z_i|.
-template <typename TJ, typename PZ, typename PXW>
-__device__ __forceinline__ bool nt_update(PXW x, double floor_, PZ z, TJ* step, bool active);
+template <typename TJ, typename PZ>
+__device__ __forceinline__ bool nt_update(double* x, double floor_, PZ z, TJ* step, bool active);
 
 // ZSHARED (device only): z in NT_NX shared-memory slots after the matrix (the
 // residual as a call of its own) instead of registers (residual inlined).
 template <typename TJ, bool ZSHARED = false, typename FF, typename PK, typename PC, typename FFT, typename PKT,
-          typename PXW, typename PJ>
+          typename PJ>
 __device__ __forceinline__ bool nt_iterate(const FF& F, PK K, PK tj, PK het, PC ck0, const FFT& FT, PKT KT, PKT tjT,
-                                           PKT hetT, bool day, PXW x, PJ J, TJ* step, bool active = true) {
+                                           PKT hetT, bool day, double* x, PJ J, TJ* step, bool active = true) {
     const double floor_ = 1e-20 * F.hnm;
     nt_jacobian_call<TJ>(day, FT, KT, tjT, hetT, x, floor_, J);
     NT_FENCE();
@@ -167,8 +167,8 @@ __device__ __forceinline__ bool nt_iterate(const FF& F, PK K, PK tj, PK het, PC 
 // FP64 update x_i += s_i z_i (negative results clipped to x_i / 10);
 // returns false when a step is not finite; *step = max |z_i|. active false:
 // a lane that runs the iteration only to keep its warp converged writes nothing.
-template <typename TJ, typename PZ, typename PXW>
-__device__ __forceinline__ bool nt_update(PXW x, double floor_, PZ z, TJ* step, bool active) {
+template <typename TJ, typename PZ>
+__device__ __forceinline__ bool nt_update(double* x, double floor_, PZ z, TJ* step, bool active) {
     const int fh = nt_exp_hi(floor_);
     TJ st = 0;
     bool finite = true;
