@@ -333,29 +333,11 @@ constexpr NtVariant nt_sp_variant() {
 // SM fetch the same generated code at the same time (the solve code is far
 // larger than the instruction cache). Lanes without a cell pass the barriers
 // idle; the exit is a barrier-and-reduction over all threads.
-// BF (FP32 matrices only): the matrix slots stored as BF16 (SJB), half the
-// shared memory per cell, so an SM keeps twice the cells in flight; the
-// arithmetic stays FP32 and the FP64 residual still decides the answer.
-template <typename TJ, int NTH, bool BF = false>
-struct NtSlots {
-    using type = SJ<TJ, NTH>;
-    static constexpr size_t bytes = sizeof(TJ);
-    static __device__ __forceinline__ type make(unsigned char* s) { return type{reinterpret_cast<TJ*>(s) + threadIdx.x}; }
-};
-template <int NTH>
-struct NtSlots<float, NTH, true> {
-    using type = SJB<NTH>;
-    static constexpr size_t bytes = 2;
-    static __device__ __forceinline__ type make(unsigned char* s) {
-        return type{reinterpret_cast<__nv_bfloat16*>(s) + threadIdx.x};
-    }
-};
-
-template <typename TJ, int NTH, bool BF = false>
+template <typename TJ, int NTH>
 __global__ void __launch_bounds__(NTH, 1) k_nt_solve_ls(Params P) {
     static_assert(NTH % 32 == 0, "whole warps");
     extern __shared__ __align__(16) unsigned char nt_smem[];
-    const typename NtSlots<TJ, NTH, BF>::type J = NtSlots<TJ, NTH, BF>::make(nt_smem);
+    const SJ<TJ, NTH> J{reinterpret_cast<TJ*>(nt_smem) + threadIdx.x};
     const unsigned lane = threadIdx.x & 31u;
     const int nday = P.nt_head[1], nnight = P.nt_head[2];
     const int nq = nday + nnight;
@@ -418,34 +400,22 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_ls(Params P) {
     }
 }
 
-template <typename TJ, int NTH, bool BF = false>
-constexpr size_t nt_ls_smem_bytes() {
-    return (size_t)NT_NSLOT * NTH * NtSlots<TJ, NTH, BF>::bytes;
-}
-
-template <typename TJ, int NTH, bool BF = false>
+template <typename TJ, int NTH>
 cudaError_t nt_ls_prepare(int* blocks_per_sm) {
-    return nt_fit_smem(k_nt_solve_ls<TJ, NTH, BF>, NTH, nt_ls_smem_bytes<TJ, NTH, BF>(), blocks_per_sm);
+    return nt_fit_smem(k_nt_solve_ls<TJ, NTH>, NTH, (size_t)NT_NSLOT * NTH * sizeof(TJ), blocks_per_sm);
 }
 
-template <typename TJ, int NTH, bool BF = false>
+template <typename TJ, int NTH>
 cudaError_t nt_ls_launch(const Params& P, int grid, cudaStream_t stream) {
-    k_nt_solve_ls<TJ, NTH, BF><<<grid, NTH, nt_ls_smem_bytes<TJ, NTH, BF>(), stream>>>(P);
+    k_nt_solve_ls<TJ, NTH><<<grid, NTH, (size_t)NT_NSLOT * NTH * sizeof(TJ), stream>>>(P);
     return cudaGetLastError();
 }
 
 // form 4: one group in lock-step, z in registers
 template <typename TJ, int NTH>
 constexpr NtVariant nt_ls_variant() {
-    return NtVariant{(int)sizeof(TJ), NTH, 4, nt_ls_smem_bytes<TJ, NTH>(), &nt_ls_prepare<TJ, NTH>,
+    return NtVariant{(int)sizeof(TJ), NTH, 4, (size_t)NT_NSLOT * NTH * sizeof(TJ), &nt_ls_prepare<TJ, NTH>,
                      &nt_ls_launch<TJ, NTH>};
-}
-
-// form 5 (FP32 matrices): form 4 with the matrix slots stored as BF16
-template <int NTH>
-constexpr NtVariant nt_lsb_variant() {
-    return NtVariant{4, NTH, 5, nt_ls_smem_bytes<float, NTH, true>(), &nt_ls_prepare<float, NTH, true>,
-                     &nt_ls_launch<float, NTH, true>};
 }
 
 template <typename TJ, int NTH>

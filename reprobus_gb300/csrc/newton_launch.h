@@ -12,14 +12,13 @@ struct NtVariant {
     int zshared;   // 1: right-hand side / step in shared memory, 0: in registers,
                    // 2: in registers, two warp groups taking turns on the matrix slots,
                    // 3: in shared memory, written by a residual lane per cell,
-                   // 4: in registers, the block's warps in lock-step,
-                   // 5: as 4 with the FP32 matrix slots stored as BF16
+                   // 4: in registers, the block's warps in lock-step
     size_t smem;   // dynamic shared memory per block (the cells' matrix slots)
     cudaError_t (*prepare)(int* blocks_per_sm);  // shared-memory opt-in, occupancy
     cudaError_t (*launch)(const Params& P, int grid, cudaStream_t stream);
 };
 
-// variants compiled in nt_solve_{f32,f64}_{zr,zs}.cu, nt_solve_{pp,sp,ls,lsb}.cu,
+// variants compiled in nt_solve_{f32,f64}_{zr,zs}.cu, nt_solve_{pp,sp,ls}.cu,
 // gathered in chem_kernels.cu: the matrix precision's variants, z in
 // registers first
 const NtVariant* nt_variants_f32_zr(int* n);
@@ -32,5 +31,4 @@ const NtVariant* nt_variants_f32_sp(int* n);
 const NtVariant* nt_variants_f64_sp(int* n);
 const NtVariant* nt_variants_f32_ls(int* n);
 const NtVariant* nt_variants_f64_ls(int* n);
-const NtVariant* nt_variants_f32_lsb(int* n);
 }  // namespace rpb

@@ -12,9 +12,6 @@
 // value (the fixed point is non-negative). The iteration has converged when
 // max_i |z_i| < tol.
 #pragma once
-#ifdef __CUDACC__
-#include <cuda_bf16.h>
-#endif
 #include "newton_gen.cuh"
 #ifndef __CUDACC__
 #define __noinline__
@@ -44,27 +41,6 @@ struct SJ {
     T* p;
     __device__ __forceinline__ T& operator[](int q) const { return p[q * STRIDE]; }
 };
-
-// the NT_NSLOT matrix slots of one cell stored as BF16 (shared memory,
-// slot-major with a compile-time stride): values are computed in FP32 and
-// rounded to the nearest BF16 when stored, widened exactly when read, so a
-// cell takes half the shared memory of the FP32 slots
-#ifdef __CUDACC__
-template <int STRIDE>
-struct SJB {
-    static constexpr int stride = STRIDE;
-    __nv_bfloat16* p;
-    struct Ref {
-        __nv_bfloat16* q;
-        __device__ __forceinline__ operator float() const { return __bfloat162float(*q); }
-        __device__ __forceinline__ const Ref& operator=(float v) const {
-            *q = __float2bfloat16_rn(v);
-            return *this;
-        }
-    };
-    __device__ __forceinline__ Ref operator[](int q) const { return Ref{p + q * STRIDE}; }
-};
-#endif
 
 constexpr double NT_TINY = 1e-30;   // pivot guard of the factorisation
 
