@@ -192,8 +192,11 @@ int reprobus_chem_set_solver(void* handle, int solver, int npass, int maxit, dou
  * that evaluates the FP64 residual while the first evaluates the Jacobian;
  * lanes_per_block then counts cells: 64, 128 mixed, 32, 64 FP64; 4: in
  * registers, the warps of a block passing each phase of an iteration
- * together, so that they fetch the same code: 64, 128 mixed, 32, 64 FP64)
- * and blocks_per_sm (0: as many as fit).
+ * together, so that they fetch the same code: 64, 128 mixed, 32, 64 FP64;
+ * 5, 6: in shared memory, 2 or 4 warps per cell: the warps working on the
+ * same 32 cells share out the rows of the Jacobian and of the residual, one
+ * of them factorises and updates; lanes_per_block then counts cells: 32, 64
+ * (5) and 32 (6) mixed, 32 FP64) and blocks_per_sm (0: as many as fit).
  * When the environment variable REPROBUS_TUNE_CACHE names a file, the
  * autotuner first looks there for a choice made for the same GPU model,
  * matrix precision and cell count (skipping the timing runs), and appends

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libreprobus_gb300.so")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["chem_kernels.cu", "nt_solve_f32_zr.cu", "nt_solve_f32_zs.cu", "nt_solve_f64_zr.cu",
-           "nt_solve_f64_zs.cu", "nt_solve_pp.cu", "nt_solve_sp.cu", "nt_solve_ls.cu", "mlp_kernels.cu",
+           "nt_solve_f64_zs.cu", "nt_solve_pp.cu", "nt_solve_sp.cu", "nt_solve_ls.cu", "nt_solve_wc.cu", "mlp_kernels.cu",
            "column_kernels.cu"]
 HEADERS = ["chem_cell.cuh", "chem_enums.h", "chem_params.cuh", "newton_gen.cuh", "newton_solve.cuh",
            "newton_kernel.cuh", "newton_launch.h", "newton_num.cuh", "tc_sm100.cuh", "handle_info.h",

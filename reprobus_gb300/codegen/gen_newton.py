@@ -654,6 +654,197 @@ def emit_jacobian(w, tag, m, pat, union, const, slot_a, pos, XP):
     w("}")
 
 
+# --------------------------------------------------------------------------- #
+# row groups: the residual and Jacobian rows split among W warps that work on
+# the same cells, each group with the intermediates its rows need
+# --------------------------------------------------------------------------- #
+def stmt_symbols(m):
+    """name -> statement index for every value and gradient symbol."""
+    names = {}
+    for idx, (_, s, _, g) in enumerate(m.stmts):
+        names[s.name] = idx
+        for j in g:
+            names[f"d_{s.name}_{j}"] = idx
+    return names
+
+
+def stmt_refs(m, derivs):
+    """Per statement, the statements its value (and, with derivs, its
+    gradient) reads."""
+    names = stmt_symbols(m)
+    out = []
+    for idx, (kind, s, payload, g) in enumerate(m.stmts):
+        exprs = list(payload) if isinstance(payload, tuple) else [payload]
+        if derivs:
+            for j, e in g.items():
+                if e is None:
+                    continue
+                exprs += list(e) if isinstance(e, tuple) else [e]
+        if derivs and kind != "let":
+            # min/max/sel gradients are emitted from the branches' gradients
+            for u in payload:
+                exprs += list(m.gradient(sp.sympify(u)).values())
+        refs = set()
+        for e in exprs:
+            for u in sp.sympify(e).free_symbols:
+                if u.name in names and names[u.name] != idx:
+                    refs.add(names[u.name])
+        out.append(refs)
+    return out
+
+
+def closure(m, exprs, refs):
+    """Indices of the statements the expressions need, transitively."""
+    names = stmt_symbols(m)
+    need, todo = set(), []
+    for e in exprs:
+        for u in sp.sympify(e).free_symbols:
+            if u.name in names:
+                todo.append(names[u.name])
+    while todo:
+        i = todo.pop()
+        if i in need:
+            continue
+        need.add(i)
+        todo.extend(refs[i])
+    return need
+
+
+def stmt_cost(m, derivs):
+    out = []
+    for kind, s, payload, g in m.stmts:
+        exprs = list(payload) if isinstance(payload, tuple) else [payload]
+        if derivs:
+            for e in g.values():
+                if e is not None:
+                    exprs += list(e) if isinstance(e, tuple) else [e]
+        out.append(sum(sp.count_ops(sp.sympify(e)) for e in exprs) + 1)
+    return out
+
+
+def partition_rows(m, row_exprs, W, derivs):
+    """Rows (index -> list of expressions) split into W groups of balanced
+    cost (operations of the rows plus those of the statements each group
+    evaluates, shared statements counted once per group that needs them)."""
+    refs = stmt_refs(m, derivs)
+    scost = stmt_cost(m, derivs)
+    info = {}
+    for i, exprs in row_exprs.items():
+        info[i] = (sum(sp.count_ops(sp.sympify(e)) for e in exprs) + 1, closure(m, exprs, refs))
+    groups = [[] for _ in range(W)]
+    have = [set() for _ in range(W)]
+    cost = [0] * W
+    for i in sorted(info, key=lambda r: -(info[r][0] + sum(scost[k] for k in info[r][1]))):
+        rc, need = info[i]
+        best = min(range(W), key=lambda g: (cost[g] + rc + sum(scost[k] for k in need - have[g]), g))
+        groups[best].append(i)
+        cost[best] += rc + sum(scost[k] for k in need - have[best])
+        have[best] |= need
+    return [sorted(g) for g in groups], cost, [sorted(h) for h in have]
+
+
+def emit_residual_group(w, tag, m, res, P, rows, name):
+    need = closure(m, [res[i] for i in rows], stmt_refs(m, False))
+    w("")
+    w(f"// residual rows {rows} ({tag} equations, FP64)")
+    w("template <typename T, typename FF, typename PK, typename PC, typename PX, typename PR>")
+    w(f"__device__ __forceinline__ void {name}(const FF& F, PK K, PK tj, PK het, PC ck0, PX x, PR R) {{")
+    chunks = emit_statements(m, P, derivs=False)
+    at = {}
+    for i in rows:
+        at.setdefault(ready_after(m, [res[i]]), []).append(i)
+    for idx in range(-1, len(chunks)):
+        if idx >= 0 and idx in need:
+            for line in chunks[idx]:
+                w(line)
+        for i in at.get(idx, []):
+            defs, red = _cse([res[i]], f"{tag[0]}r{i}_c", P)
+            for line in defs:
+                w(line)
+            w(f"    R[{i}] = {P.doprint(red[0])};")
+    w("}")
+
+
+def emit_jacobian_group(w, tag, m, pat, union, const, slot_a, pos, XP, rows, name):
+    by_row = {}
+    for (i, j) in sorted(union):
+        by_row.setdefault(i, []).append(j)
+    row_exprs = {i: [pat.get((i, j), sp.Integer(0)) for j in by_row.get(i, []) if (i, j) not in const] for i in rows}
+    need = closure(m, [e for es in row_exprs.values() for e in es], stmt_refs(m, True))
+    w("")
+    w(f"// scaled Jacobian rows {rows} ({tag} equations) into their stored A slots")
+    w("template <typename T, typename FF, typename PK, typename PJ>")
+    w(f"__device__ __forceinline__ void {name}(const FF& F, PK K, PK tj, PK het, "
+      "const double* __restrict__ x, double floor_, PJ J) {")
+    w("    const int fh = nt_exp_hi(floor_);")
+    chunks = emit_statements(m, XP, derivs=True)
+    at = {}
+    for i in rows:
+        at.setdefault(ready_after(m, row_exprs[i]), []).append(i)
+    for idx in range(-1, len(chunks)):
+        if idx >= 0 and idx in need:
+            for line in chunks[idx]:
+                w(line)
+        for i in at.get(idx, []):
+            stored = [j for j in by_row.get(i, []) if (i, j) not in const]
+            if not stored:
+                continue
+            defs, red = _cse([pat.get((i, j), sp.Integer(0)) for j in stored], f"{tag[0]}j{i}_c", XP)
+            w(f"    {{  // row {i}")
+            w(f"    const T rs{i} = nt_rscale<T>(nt_exp_hi(x[{i}]), fh);")
+            for line in defs:
+                w("    " + line)
+            for j, e in zip(stored, red):
+                sl = slot_a[(pos[i], pos[j])]
+                if e == 0:
+                    w(f"        J[{sl}] = T(0);")
+                else:
+                    w(f"        J[{sl}] = ({XP.doprint(e)}) * (nt_scale<T>(nt_exp_hi(x[{j}]), fh) * rs{i});")
+            w("    }")
+    w("}")
+
+
+def emit_groups(w, W, tag, m, res, pat, union, const, slot_a, pos, P, XP, stats):
+    """W residual and W Jacobian row groups of the day or night equations and
+    their dispatchers (g: the group, warp-uniform)."""
+    by_row = {}
+    for (i, j) in sorted(union):
+        by_row.setdefault(i, []).append(j)
+    rgroups, rcost, _ = partition_rows(m, {i: [res[i]] for i in range(NX)}, W, False)
+    jrows = {i: [pat.get((i, j), sp.Integer(0)) for j in by_row.get(i, []) if (i, j) not in const]
+             for i in range(NX)}
+    jrows = {i: e for i, e in jrows.items() if e}
+    jgroups, jcost, _ = partition_rows(m, jrows, W, True)
+    stats[(tag, W)] = (rcost, jcost)
+    for g in range(W):
+        emit_residual_group(w, tag, m, res, P, rgroups[g], f"nt_residual_{tag}_w{W}_{g}")
+        emit_jacobian_group(w, tag, m, pat, union, const, slot_a, pos, XP, jgroups[g], f"nt_jacobian_{tag}_w{W}_{g}")
+    w("")
+    w(f"// residual rows of group g of {W} ({tag} equations)")
+    w("template <typename T, typename FF, typename PK, typename PC, typename PX, typename PR>")
+    w(f"__device__ __forceinline__ void nt_residual_{tag}_w{W}(int g, const FF& F, PK K, PK tj, PK het, PC ck0, PX x, "
+      "PR R) {")
+    w("    switch (g) {")
+    for g in range(W):
+        w(f"        case {g}: nt_residual_{tag}_w{W}_{g}<T>(F, K, tj, het, ck0, x, R); break;")
+    w("        default: break;")
+    w("    }")
+    w("}")
+    w(f"// Jacobian rows of group g of {W} ({tag} equations)")
+    w("template <typename T, typename FF, typename PK, typename PJ>")
+    w(f"__device__ __forceinline__ void nt_jacobian_{tag}_w{W}(int g, const FF& F, PK K, PK tj, PK het, "
+      "const double* __restrict__ x, double floor_, PJ J) {")
+    w("    switch (g) {")
+    for g in range(W):
+        w(f"        case {g}: nt_jacobian_{tag}_w{W}_{g}<T>(F, K, tj, het, x, floor_, J); break;")
+    w("        default: break;")
+    w("    }")
+    w("}")
+
+
+WARPS_PER_CELL = (2, 4)  # row groups generated for the warps-per-cell solve kernel
+
+
 def emit_factor(w, perm, rows, slot_a, slot_u, const_pos, n):
     Z = lambda i: f"z[{i}]"
     w("")
@@ -763,14 +954,17 @@ def generate(path):
     w("    T rain_hno3, rain_hcl, rain_hbr, rain_h2o2, dt;")
     w("};")
     w("")
+    stats = {}
     for tag, m, res, pat in (("day", md, rd, pat_d), ("night", mn, rn, pat_n)):
         emit_residual(w, tag, m, res, P)
         emit_jacobian(w, tag, m, pat, union, const, slot_a, pos, XP)
+        for W in WARPS_PER_CELL:
+            emit_groups(w, W, tag, m, res, pat, union, const, slot_a, pos, P, XP, stats)
     emit_factor(w, perm, rows, slot_a, slot_u, const_pos, NX)
     w("}  // namespace rpb")
     with open(path, "w") as f:
         f.write("\n".join(out) + "\n")
-    return {"nnz": len(nz), "slots": nslot, "stored": na, "updates": nupd, "perm": perm}
+    return {"nnz": len(nz), "slots": nslot, "stored": na, "updates": nupd, "perm": perm, "groups": stats}
 
 
 if __name__ == "__main__":
@@ -778,3 +972,5 @@ if __name__ == "__main__":
     info = generate(target)
     print(f"wrote {target}: nnz {info['nnz']}, stored A {info['stored']}, slots {info['slots']}, "
           f"LU updates {info['updates']}")
+    for (tag, W), (rc, jc) in info["groups"].items():
+        print(f"  {tag} W={W}: residual group costs {rc}, Jacobian group costs {jc}")

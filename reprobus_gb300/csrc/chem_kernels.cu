@@ -980,21 +980,23 @@ static void fill_params(const Handle* h, Params& P, int ilat0, int ilat1) {
 // every compiled solve-kernel variant of one matrix precision
 static int nt_all_variants(bool mixed, const NtVariant** out, int cap) {
     int n = 0, k = 0;
-    const NtVariant* lists[5] = {};
-    int counts[5] = {0, 0, 0, 0, 0};
-    const int nl = 5;
+    const NtVariant* lists[6] = {};
+    int counts[6] = {0, 0, 0, 0, 0, 0};
+    const int nl = 6;
     if (mixed) {
         lists[0] = nt_variants_f32_zr(&counts[0]);
         lists[1] = nt_variants_f32_zs(&counts[1]);
         lists[2] = nt_variants_f32_pp(&counts[2]);
         lists[3] = nt_variants_f32_sp(&counts[3]);
         lists[4] = nt_variants_f32_ls(&counts[4]);
+        lists[5] = nt_variants_f32_wc(&counts[5]);
     } else {
         lists[0] = nt_variants_f64_zr(&counts[0]);
         lists[1] = nt_variants_f64_zs(&counts[1]);
         lists[2] = nt_variants_f64_pp(&counts[2]);
         lists[3] = nt_variants_f64_sp(&counts[3]);
         lists[4] = nt_variants_f64_ls(&counts[4]);
+        lists[5] = nt_variants_f64_wc(&counts[5]);
     }
     for (int l = 0; l < nl; l++)
         for (k = 0; k < counts[l] && n < cap; k++) out[n++] = &lists[l][k];
@@ -1391,7 +1393,7 @@ extern "C" int reprobus_chem_set_tuning(void* handle, int lanes_per_block, int b
     Handle* h = (Handle*)handle;
     if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
     if (lanes_per_block < 0 || blocks_per_sm < 0) return set_err(REPROBUS_ERR_ARG, "bad tuning values");
-    if (zshared < 0 || zshared > 4) return set_err(REPROBUS_ERR_ARG, "zshared must be 0 .. 4");
+    if (zshared < 0 || zshared > 6) return set_err(REPROBUS_ERR_ARG, "zshared must be 0 .. 6");
     if (lanes_per_block > 0) {
         bool found = false;
         const NtVariant* vs[32];

@@ -418,6 +418,153 @@ constexpr NtVariant nt_ls_variant() {
                      &nt_ls_launch<TJ, NTH>};
 }
 
+// Warps-per-cell form (form 5): W warps work on the same 32 cells. Per
+// iteration, phase A: warp g of a cell group evaluates its share of the
+// scaled Jacobian rows (into the cells' shared-memory matrix slots) and of the
+// FP64 residual rows (scaled, into the cells' right-hand-side slots); the
+// row groups are balanced by operation count at generation time and each
+// evaluates only the intermediates its rows need (newton_gen.cuh,
+// nt_{jacobian,residual}_{day,night}_wW). Phase B: warp 0 of the group
+// factorises, solves, updates the iterate in FP64, tests convergence and
+// refills its lanes from the work queue, publishing the cells of the next
+// iteration. A block holds C cell groups; phases end at block barriers that
+// every thread passes the same number of times, and the exit is decided by a
+// barrier-and-reduction over all threads. Each warp of phase A has a smaller
+// program and fewer live values than one warp evaluating every row, and an
+// SM keeps W warps busy per 32 cells in flight.
+template <typename TJ>
+__host__ __device__ constexpr size_t nt_wc_group_bytes() {
+    return (size_t)(NT_NSLOT + NT_NX) * 32 * sizeof(TJ) + 32 * sizeof(int);
+}
+
+template <int W, typename TJ, typename FFT, typename PKT, typename PJ>
+__device__ __noinline__ void nt_jacobian_wc_fn(int g, bool day, const FFT& FT, PKT KT, PKT tjT, PKT hetT,
+                                                const double* x, double floor_, PJ J) {
+    if constexpr (W == 2) {
+        if (day)
+            nt_jacobian_day_w2<TJ>(g, FT, KT, tjT, hetT, x, floor_, J);
+        else
+            nt_jacobian_night_w2<TJ>(g, FT, KT, tjT, hetT, x, floor_, J);
+    } else {
+        if (day)
+            nt_jacobian_day_w4<TJ>(g, FT, KT, tjT, hetT, x, floor_, J);
+        else
+            nt_jacobian_night_w4<TJ>(g, FT, KT, tjT, hetT, x, floor_, J);
+    }
+}
+
+template <int W, typename TJ, typename FF, typename PK, typename PC, typename PZ>
+__device__ __noinline__ void nt_rhs_wc_fn(int g, bool day, const FF& F, PK K, PK tj, PK het, PC ck0,
+                                           const double* x, double floor_, PZ z) {
+    const NtRhsOut<TJ, PZ> R{z, x, nt_exp_hi(floor_)};
+    if constexpr (W == 2) {
+        if (day)
+            nt_residual_day_w2<double>(g, F, K, tj, het, ck0, x, R);
+        else
+            nt_residual_night_w2<double>(g, F, K, tj, het, ck0, x, R);
+    } else {
+        if (day)
+            nt_residual_day_w4<double>(g, F, K, tj, het, ck0, x, R);
+        else
+            nt_residual_night_w4<double>(g, F, K, tj, het, ck0, x, R);
+    }
+}
+
+template <typename TJ, int W, int C>
+__global__ void __launch_bounds__(32 * W * C, 1) k_nt_solve_wc(Params P) {
+    static_assert(W == 2 || W == 4, "row groups are generated for 2 and 4 warps per cell");
+    extern __shared__ __align__(16) unsigned char nt_smem[];
+    const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31u);
+    const int grp = warp / W, g = warp % W;  // cell group of the block, row group of the warp
+    unsigned char* base = nt_smem + (size_t)grp * nt_wc_group_bytes<TJ>();
+    TJ* slots = reinterpret_cast<TJ*>(base);
+    const SJ<TJ, 32> J{slots + lane};
+    const SZ<TJ, 32> z{slots + (size_t)NT_NSLOT * 32 + lane};
+    int* cells = reinterpret_cast<int*>(base + (size_t)(NT_NSLOT + NT_NX) * 32 * sizeof(TJ));
+    const int nday = P.nt_head[1], nnight = P.nt_head[2];
+    const int nq = nday + nnight;
+    int cell = -1, it = 0, attempt = 0;  // warp 0 of the group: the lane's cell and its progress
+    auto refill = [&]() {
+        const unsigned want = __ballot_sync(0xffffffffu, cell == -1);
+        if (want) {
+            const int leader = __ffs(want) - 1;
+            int b = 0;
+            if (lane == leader) b = atomicAdd(P.nt_head, __popc(want));
+            b = __shfl_sync(0xffffffffu, b, leader);
+            if (cell == -1) {
+                const int q = b + __popc(want & ((1u << lane) - 1u));
+                cell = q < nq ? nt_queue_cell(P, q, nday) : -2;
+                it = 0;
+                attempt = 0;
+            }
+        }
+        cells[lane] = cell;
+    };
+    if (g == 0) refill();
+    for (;;) {
+        __syncthreads();  // the published cells
+        const int c = cells[lane];
+        if (__syncthreads_and(c == -2)) break;
+        const double* rec = P.nt_rec + (size_t)(c > 0 ? c : 0) * NT_REC;
+        const double floor_ = 1e-20 * rec[NT_RF + 4];
+        double* x = P.nt_x + (size_t)(c > 0 ? c : 0) * NT_NX;
+        // phase A: this warp's rows of the Jacobian and of the residual
+        if (c >= 0) {
+            const TJ* recT;
+            if constexpr (sizeof(TJ) == 4)
+                recT = P.nt_rec32 + (size_t)c * NT_REC32;
+            else
+                recT = rec;
+            const bool day = rec[NT_RSZA] <= 95.;
+            NtFixT<TJ> FT;
+            nt_load_fix<TJ>(recT + NT_RF, FT);
+            nt_jacobian_wc_fn<W, TJ>(g, day, FT, recT + NT_RK, recT + NT_RJ, recT + NT_RH, x, floor_, J);
+            NtFixT<double> F;
+            nt_load_fix<double>(rec + NT_RF, F);
+            nt_rhs_wc_fn<W, TJ>(g, day, F, rec + NT_RK, rec + NT_RJ, rec + NT_RH, rec + NT_RCK0, x, floor_, z);
+        }
+        __syncthreads();  // the Jacobian and right-hand side of every cell
+        // phase B: warp 0 of the group
+        if (g == 0) {
+            if (c >= 0) {
+                NT_FENCE();
+                nt_factor_solve<TJ>(J, z, TJ(NT_TINY));
+                TJ step;
+                const bool ok = nt_update<TJ>(x, floor_, z, &step, true);
+                it++;
+                int done = 0;
+                if (!ok)
+                    done = -1;
+                else if (step < (TJ)P.tol)
+                    done = it;
+                else if (it >= P.maxit)
+                    done = -1;
+                if (done && !nt_end_attempt(P, c, done, it, attempt)) cell = -1;
+            }
+            refill();
+        }
+    }
+}
+
+template <typename TJ, int W, int C>
+cudaError_t nt_wc_prepare(int* blocks_per_sm) {
+    return nt_fit_smem(k_nt_solve_wc<TJ, W, C>, 32 * W * C, C * nt_wc_group_bytes<TJ>(), blocks_per_sm);
+}
+
+template <typename TJ, int W, int C>
+cudaError_t nt_wc_launch(const Params& P, int grid, cudaStream_t stream) {
+    k_nt_solve_wc<TJ, W, C><<<grid, 32 * W * C, C * nt_wc_group_bytes<TJ>(), stream>>>(P);
+    return cudaGetLastError();
+}
+
+// forms 5 (2 warps per cell) and 6 (4 warps per cell); nth counts the cells
+// of a block (32 C)
+template <typename TJ, int W, int C>
+constexpr NtVariant nt_wc_variant() {
+    return NtVariant{(int)sizeof(TJ), 32 * C, W == 2 ? 5 : 6, C * nt_wc_group_bytes<TJ>(), &nt_wc_prepare<TJ, W, C>,
+                     &nt_wc_launch<TJ, W, C>};
+}
+
 template <typename TJ, int NTH>
 constexpr size_t nt_pp_smem_bytes() {
     return (size_t)NT_NSLOT * (NTH / 2) * sizeof(TJ);

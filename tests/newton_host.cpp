@@ -4,6 +4,7 @@
 // against the oracle's fixed point. Compiled by tests/test_newton_equations.py.
 #include <cmath>
 #include <cstring>
+#include <cstdlib>
 using std::fabs;
 using std::fmax;
 using std::fmin;
@@ -55,6 +56,44 @@ void nt_host_jacobian(const double* K, const double* tj, const double* het, cons
         nt_jacobian_day<double>(F, K, tj, het, x, floor_, J);
     else
         nt_jacobian_night<double>(F, K, tj, het, x, floor_, J);
+    memset(Jd, 0, sizeof(double) * NT_NX * NT_NX);
+    for (int q = 0; q < NT_NA; q++) Jd[NT_A_I[q] * NT_NX + NT_A_J[q]] = J[q];
+    for (int q = 0; q < NT_NCONST; q++) Jd[NT_CONST_I[q] * (NT_NX + 1)] = NT_CONST_V[q];
+}
+
+// the residual and the scaled Jacobian assembled from the W row groups of the
+// warps-per-cell kernel (each row written by exactly one group; rows a group
+// does not own keep the NaN they start with)
+void nt_host_residual_groups(int W, const double* K, const double* tj, const double* het, const double* fix,
+                             const double* ck0, int day, const double* x, double* R) {
+    NtFix F = fix_from(fix);
+    for (int i = 0; i < NT_NX; i++) R[i] = NAN;
+    for (int g = 0; g < W; g++) {
+        if (W == 2) {
+            if (day) nt_residual_day_w2<double>(g, F, K, tj, het, ck0, x, R);
+            else nt_residual_night_w2<double>(g, F, K, tj, het, ck0, x, R);
+        } else {
+            if (day) nt_residual_day_w4<double>(g, F, K, tj, het, ck0, x, R);
+            else nt_residual_night_w4<double>(g, F, K, tj, het, ck0, x, R);
+        }
+    }
+}
+
+void nt_host_jacobian_groups(int W, const double* K, const double* tj, const double* het, const double* fix, int day,
+                             const double* x, double* Jd) {
+    NtFix F = fix_from(fix);
+    double J[NT_NSLOT];
+    for (int q = 0; q < NT_NSLOT; q++) J[q] = NAN;
+    const double floor_ = 1e-20 * F.hnm;
+    for (int g = 0; g < W; g++) {
+        if (W == 2) {
+            if (day) nt_jacobian_day_w2<double>(g, F, K, tj, het, x, floor_, J);
+            else nt_jacobian_night_w2<double>(g, F, K, tj, het, x, floor_, J);
+        } else {
+            if (day) nt_jacobian_day_w4<double>(g, F, K, tj, het, x, floor_, J);
+            else nt_jacobian_night_w4<double>(g, F, K, tj, het, x, floor_, J);
+        }
+    }
     memset(Jd, 0, sizeof(double) * NT_NX * NT_NX);
     for (int q = 0; q < NT_NA; q++) Jd[NT_A_I[q] * NT_NX + NT_A_J[q]] = J[q];
     for (int q = 0; q < NT_NCONST; q++) Jd[NT_CONST_I[q] * (NT_NX + 1)] = NT_CONST_V[q];

@@ -129,13 +129,17 @@ def test_mixed_solve_kernel_shapes_agree_with_the_oracle(case, fixed_point, lane
                                                (SOLVER_NEWTON_MIXED, 128, 3), (SOLVER_NEWTON_MIXED, 64, 3),
                                                (SOLVER_NEWTON64, 64, 3), (SOLVER_NEWTON64, 32, 3),
                                                (SOLVER_NEWTON_MIXED, 128, 4), (SOLVER_NEWTON_MIXED, 64, 4),
-                                               (SOLVER_NEWTON64, 64, 4)])
+                                               (SOLVER_NEWTON64, 64, 4), (SOLVER_NEWTON_MIXED, 32, 5),
+                                               (SOLVER_NEWTON_MIXED, 64, 5), (SOLVER_NEWTON_MIXED, 32, 6),
+                                               (SOLVER_NEWTON64, 32, 5), (SOLVER_NEWTON64, 32, 6)])
 def test_two_group_solve_kernel_agrees_with_the_oracle(case, fixed_point, solver, lanes, form):
     """The solve kernels with two kinds of warps, forced, for both matrix
     precisions: two warp groups taking turns on one set of matrix slots
-    (zshared 2), a matrix lane plus a residual lane per cell (zshared 3), and
-    the one-group kernel with its warps in lock-step (zshared 4). Same
-    accuracy bound and fixed-point property as the one-group kernel."""
+    (zshared 2), a matrix lane plus a residual lane per cell (zshared 3), the
+    one-group kernel with its warps in lock-step (zshared 4), and 2 or 4
+    warps per cell sharing the rows of the Jacobian and the residual (zshared
+    5, 6; lanes = cells per block). Same accuracy bound and fixed-point
+    property as the one-group kernel."""
     from reprobus_gb300.resident import DeviceCase
     fp, stat, _ = fixed_point
     h = ChemStep.for_case(case, niter=5, flags=0)

@@ -33,6 +33,8 @@ def host(tmp_path_factory):
     L.nt_host_residual.argtypes = [dp] * 5 + [ctypes.c_int, dp, dp]
     L.nt_host_jacobian.argtypes = [dp] * 4 + [ctypes.c_int, dp, dp]
     L.nt_host_newton.argtypes = [dp] * 5 + [ctypes.c_int, dp, ctypes.c_int, ctypes.c_double, ctypes.c_int, dp]
+    L.nt_host_residual_groups.argtypes = [ctypes.c_int] + [dp] * 5 + [ctypes.c_int, dp, dp]
+    L.nt_host_jacobian_groups.argtypes = [ctypes.c_int] + [dp] * 4 + [ctypes.c_int, dp, dp]
     return L
 
 
@@ -114,6 +116,25 @@ def test_jacobian_matches_finite_differences(host, data):
             fd = (Rp - Rm) / (2 * h) * s[j] / s
             an = Jd[:, j]
             assert np.all(np.abs(an - fd) <= 1e-4 * np.abs(fd) + 1e-6), (cell, j)
+
+
+@pytest.mark.parametrize("W", [2, 4])
+def test_row_groups_reproduce_the_residual_and_jacobian(host, data, W):
+    """The row groups that the warps of the warps-per-cell solve kernel
+    evaluate cover every residual row and every stored Jacobian entry once,
+    with the values of the whole functions, for day and night cells."""
+    c, dg, fp, stat, r1 = data
+    for cell in range(0, c.ncells, 7):
+        K, tj, het, fix, ck0, day = _cell_inputs(c, dg, cell)
+        x = _x(c, r1, dg, cell)
+        R, Rg = np.zeros(57), np.zeros(57)
+        host.nt_host_residual(_P(K), _P(tj), _P(het), _P(fix), _P(ck0), day, _P(x), _P(R))
+        host.nt_host_residual_groups(W, _P(K), _P(tj), _P(het), _P(fix), _P(ck0), day, _P(x), _P(Rg))
+        assert np.array_equal(R, Rg), (cell, np.where(R != Rg))
+        Jd, Jg = np.zeros(57 * 57), np.zeros(57 * 57)
+        host.nt_host_jacobian(_P(K), _P(tj), _P(het), _P(fix), day, _P(x), _P(Jd))
+        host.nt_host_jacobian_groups(W, _P(K), _P(tj), _P(het), _P(fix), day, _P(x), _P(Jg))
+        assert np.array_equal(Jd, Jg), (cell, np.where(Jd != Jg))
 
 
 @pytest.mark.parametrize("mixed", [0, 1])
