@@ -411,13 +411,13 @@ class Printer(C99CodePrinter):
 
 
 class XPrinter(Printer):
-    """Jacobian printer: the FP64 iterate x[j] is read where it is used and
-    rounded to T there (no long-lived copies of x in registers)."""
+    """Jacobian printer: the FP64 iterate x[j] is read once per call, rounded
+    to T (xt{j}, defined at the top of the function)."""
 
     def _print_Symbol(self, e):
         n = e.name
         if n.startswith("x["):
-            return f"nt_cvt<T>({n})"
+            return f"xt{n[2:-1]}"
         return n
 
 
@@ -619,6 +619,11 @@ def emit_jacobian(w, tag, m, pat, union, const, slot_a, pos, XP):
     w(f"__device__ __forceinline__ void nt_jacobian_{tag}(const FF& F, PK K, PK tj, PK het, "
       "const double* __restrict__ x, double floor_, PJ J) {")
     w("    const int fh = nt_exp_hi(floor_);")
+    w("    // the iterate in T and the column scales, once per call")
+    for j in range(NX):
+        w(f"    const T xt{j} = nt_cvt<T>(x[{j}]);")
+    for j in range(NX):
+        w(f"    const T cs{j} = nt_scale<T>(nt_exp_hi(x[{j}]), fh);")
     chunks = emit_statements(m, XP, derivs=True)
     by_row = {}
     for (i, j) in sorted(union):
@@ -649,7 +654,7 @@ def emit_jacobian(w, tag, m, pat, union, const, slot_a, pos, XP):
                 if e == 0:
                     w(f"        J[{sl}] = T(0);")
                 else:
-                    w(f"        J[{sl}] = ({XP.doprint(e)}) * (nt_scale<T>(nt_exp_hi(x[{j}]), fh) * rs{i});")
+                    w(f"        J[{sl}] = ({XP.doprint(e)}) * (cs{j} * rs{i});")
             w("    }")
     w("}")
 
@@ -777,6 +782,10 @@ def emit_jacobian_group(w, tag, m, pat, union, const, slot_a, pos, XP, rows, nam
     w(f"__device__ __forceinline__ void {name}(const FF& F, PK K, PK tj, PK het, "
       "const double* __restrict__ x, double floor_, PJ J) {")
     w("    const int fh = nt_exp_hi(floor_);")
+    for j in range(NX):
+        w(f"    const T xt{j} = nt_cvt<T>(x[{j}]);")
+    for j in sorted({j for i in rows for j in by_row.get(i, []) if (i, j) not in const}):
+        w(f"    const T cs{j} = nt_scale<T>(nt_exp_hi(x[{j}]), fh);")
     chunks = emit_statements(m, XP, derivs=True)
     at = {}
     for i in rows:
@@ -799,7 +808,7 @@ def emit_jacobian_group(w, tag, m, pat, union, const, slot_a, pos, XP, rows, nam
                 if e == 0:
                     w(f"        J[{sl}] = T(0);")
                 else:
-                    w(f"        J[{sl}] = ({XP.doprint(e)}) * (nt_scale<T>(nt_exp_hi(x[{j}]), fh) * rs{i});")
+                    w(f"        J[{sl}] = ({XP.doprint(e)}) * (cs{j} * rs{i});")
             w("    }")
     w("}")
 

@@ -148,96 +148,211 @@ __device__ __forceinline__ void nt_residual_day(const FF& F, PK K, PK tj, PK het
 template <typename T, typename FF, typename PK, typename PJ>
 __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het, const double* __restrict__ x, double floor_, PJ J) {
     const int fh = nt_exp_hi(floor_);
+    // the iterate in T and the column scales, once per call
+    const T xt0 = nt_cvt<T>(x[0]);
+    const T xt1 = nt_cvt<T>(x[1]);
+    const T xt2 = nt_cvt<T>(x[2]);
+    const T xt3 = nt_cvt<T>(x[3]);
+    const T xt4 = nt_cvt<T>(x[4]);
+    const T xt5 = nt_cvt<T>(x[5]);
+    const T xt6 = nt_cvt<T>(x[6]);
+    const T xt7 = nt_cvt<T>(x[7]);
+    const T xt8 = nt_cvt<T>(x[8]);
+    const T xt9 = nt_cvt<T>(x[9]);
+    const T xt10 = nt_cvt<T>(x[10]);
+    const T xt11 = nt_cvt<T>(x[11]);
+    const T xt12 = nt_cvt<T>(x[12]);
+    const T xt13 = nt_cvt<T>(x[13]);
+    const T xt14 = nt_cvt<T>(x[14]);
+    const T xt15 = nt_cvt<T>(x[15]);
+    const T xt16 = nt_cvt<T>(x[16]);
+    const T xt17 = nt_cvt<T>(x[17]);
+    const T xt18 = nt_cvt<T>(x[18]);
+    const T xt19 = nt_cvt<T>(x[19]);
+    const T xt20 = nt_cvt<T>(x[20]);
+    const T xt21 = nt_cvt<T>(x[21]);
+    const T xt22 = nt_cvt<T>(x[22]);
+    const T xt23 = nt_cvt<T>(x[23]);
+    const T xt24 = nt_cvt<T>(x[24]);
+    const T xt25 = nt_cvt<T>(x[25]);
+    const T xt26 = nt_cvt<T>(x[26]);
+    const T xt27 = nt_cvt<T>(x[27]);
+    const T xt28 = nt_cvt<T>(x[28]);
+    const T xt29 = nt_cvt<T>(x[29]);
+    const T xt30 = nt_cvt<T>(x[30]);
+    const T xt31 = nt_cvt<T>(x[31]);
+    const T xt32 = nt_cvt<T>(x[32]);
+    const T xt33 = nt_cvt<T>(x[33]);
+    const T xt34 = nt_cvt<T>(x[34]);
+    const T xt35 = nt_cvt<T>(x[35]);
+    const T xt36 = nt_cvt<T>(x[36]);
+    const T xt37 = nt_cvt<T>(x[37]);
+    const T xt38 = nt_cvt<T>(x[38]);
+    const T xt39 = nt_cvt<T>(x[39]);
+    const T xt40 = nt_cvt<T>(x[40]);
+    const T xt41 = nt_cvt<T>(x[41]);
+    const T xt42 = nt_cvt<T>(x[42]);
+    const T xt43 = nt_cvt<T>(x[43]);
+    const T xt44 = nt_cvt<T>(x[44]);
+    const T xt45 = nt_cvt<T>(x[45]);
+    const T xt46 = nt_cvt<T>(x[46]);
+    const T xt47 = nt_cvt<T>(x[47]);
+    const T xt48 = nt_cvt<T>(x[48]);
+    const T xt49 = nt_cvt<T>(x[49]);
+    const T xt50 = nt_cvt<T>(x[50]);
+    const T xt51 = nt_cvt<T>(x[51]);
+    const T xt52 = nt_cvt<T>(x[52]);
+    const T xt53 = nt_cvt<T>(x[53]);
+    const T xt54 = nt_cvt<T>(x[54]);
+    const T xt55 = nt_cvt<T>(x[55]);
+    const T xt56 = nt_cvt<T>(x[56]);
+    const T cs0 = nt_scale<T>(nt_exp_hi(x[0]), fh);
+    const T cs1 = nt_scale<T>(nt_exp_hi(x[1]), fh);
+    const T cs2 = nt_scale<T>(nt_exp_hi(x[2]), fh);
+    const T cs3 = nt_scale<T>(nt_exp_hi(x[3]), fh);
+    const T cs4 = nt_scale<T>(nt_exp_hi(x[4]), fh);
+    const T cs5 = nt_scale<T>(nt_exp_hi(x[5]), fh);
+    const T cs6 = nt_scale<T>(nt_exp_hi(x[6]), fh);
+    const T cs7 = nt_scale<T>(nt_exp_hi(x[7]), fh);
+    const T cs8 = nt_scale<T>(nt_exp_hi(x[8]), fh);
+    const T cs9 = nt_scale<T>(nt_exp_hi(x[9]), fh);
+    const T cs10 = nt_scale<T>(nt_exp_hi(x[10]), fh);
+    const T cs11 = nt_scale<T>(nt_exp_hi(x[11]), fh);
+    const T cs12 = nt_scale<T>(nt_exp_hi(x[12]), fh);
+    const T cs13 = nt_scale<T>(nt_exp_hi(x[13]), fh);
+    const T cs14 = nt_scale<T>(nt_exp_hi(x[14]), fh);
+    const T cs15 = nt_scale<T>(nt_exp_hi(x[15]), fh);
+    const T cs16 = nt_scale<T>(nt_exp_hi(x[16]), fh);
+    const T cs17 = nt_scale<T>(nt_exp_hi(x[17]), fh);
+    const T cs18 = nt_scale<T>(nt_exp_hi(x[18]), fh);
+    const T cs19 = nt_scale<T>(nt_exp_hi(x[19]), fh);
+    const T cs20 = nt_scale<T>(nt_exp_hi(x[20]), fh);
+    const T cs21 = nt_scale<T>(nt_exp_hi(x[21]), fh);
+    const T cs22 = nt_scale<T>(nt_exp_hi(x[22]), fh);
+    const T cs23 = nt_scale<T>(nt_exp_hi(x[23]), fh);
+    const T cs24 = nt_scale<T>(nt_exp_hi(x[24]), fh);
+    const T cs25 = nt_scale<T>(nt_exp_hi(x[25]), fh);
+    const T cs26 = nt_scale<T>(nt_exp_hi(x[26]), fh);
+    const T cs27 = nt_scale<T>(nt_exp_hi(x[27]), fh);
+    const T cs28 = nt_scale<T>(nt_exp_hi(x[28]), fh);
+    const T cs29 = nt_scale<T>(nt_exp_hi(x[29]), fh);
+    const T cs30 = nt_scale<T>(nt_exp_hi(x[30]), fh);
+    const T cs31 = nt_scale<T>(nt_exp_hi(x[31]), fh);
+    const T cs32 = nt_scale<T>(nt_exp_hi(x[32]), fh);
+    const T cs33 = nt_scale<T>(nt_exp_hi(x[33]), fh);
+    const T cs34 = nt_scale<T>(nt_exp_hi(x[34]), fh);
+    const T cs35 = nt_scale<T>(nt_exp_hi(x[35]), fh);
+    const T cs36 = nt_scale<T>(nt_exp_hi(x[36]), fh);
+    const T cs37 = nt_scale<T>(nt_exp_hi(x[37]), fh);
+    const T cs38 = nt_scale<T>(nt_exp_hi(x[38]), fh);
+    const T cs39 = nt_scale<T>(nt_exp_hi(x[39]), fh);
+    const T cs40 = nt_scale<T>(nt_exp_hi(x[40]), fh);
+    const T cs41 = nt_scale<T>(nt_exp_hi(x[41]), fh);
+    const T cs42 = nt_scale<T>(nt_exp_hi(x[42]), fh);
+    const T cs43 = nt_scale<T>(nt_exp_hi(x[43]), fh);
+    const T cs44 = nt_scale<T>(nt_exp_hi(x[44]), fh);
+    const T cs45 = nt_scale<T>(nt_exp_hi(x[45]), fh);
+    const T cs46 = nt_scale<T>(nt_exp_hi(x[46]), fh);
+    const T cs47 = nt_scale<T>(nt_exp_hi(x[47]), fh);
+    const T cs48 = nt_scale<T>(nt_exp_hi(x[48]), fh);
+    const T cs49 = nt_scale<T>(nt_exp_hi(x[49]), fh);
+    const T cs50 = nt_scale<T>(nt_exp_hi(x[50]), fh);
+    const T cs51 = nt_scale<T>(nt_exp_hi(x[51]), fh);
+    const T cs52 = nt_scale<T>(nt_exp_hi(x[52]), fh);
+    const T cs53 = nt_scale<T>(nt_exp_hi(x[53]), fh);
+    const T cs54 = nt_scale<T>(nt_exp_hi(x[54]), fh);
+    const T cs55 = nt_scale<T>(nt_exp_hi(x[55]), fh);
+    const T cs56 = nt_scale<T>(nt_exp_hi(x[56]), fh);
     {  // row 0
     const T rs0 = nt_rscale<T>(nt_exp_hi(x[0]), fh);
         const T dj0_c0 = K[K_b38] + K[K_b39];
-        J[76] = (F.dt*(dj0_c0*nt_cvt<T>(x[42]) + tj[J_n2o]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs0);
-        J[77] = (F.dt*dj0_c0*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs0);
+        J[76] = (F.dt*(dj0_c0*xt42 + tj[J_n2o]) + T(1)) * (cs0 * rs0);
+        J[77] = (F.dt*dj0_c0*xt0) * (cs42 * rs0);
     }
     {  // row 1
     const T rs1 = nt_rscale<T>(nt_exp_hi(x[1]), fh);
-        const T dj1_c0 = F.dt*nt_cvt<T>(x[1]);
-        J[157] = (F.dt*(K[K_c1a]*nt_cvt<T>(x[42]) + K[K_c1b]*nt_cvt<T>(x[42]) + K[K_c1c]*nt_cvt<T>(x[42]) + K[K_c2]*nt_cvt<T>(x[43]) + K[K_d5]*nt_cvt<T>(x[44])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs1);
-        J[156] = (dj1_c0*(K[K_c1a] + K[K_c1b] + K[K_c1c])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs1);
-        J[159] = (K[K_c2]*dj1_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs1);
-        J[158] = (K[K_d5]*dj1_c0) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs1);
+        const T dj1_c0 = F.dt*xt1;
+        J[157] = (F.dt*(K[K_c1a]*xt42 + K[K_c1b]*xt42 + K[K_c1c]*xt42 + K[K_c2]*xt43 + K[K_d5]*xt44) + T(1)) * (cs1 * rs1);
+        J[156] = (dj1_c0*(K[K_c1a] + K[K_c1b] + K[K_c1c])) * (cs42 * rs1);
+        J[159] = (K[K_c2]*dj1_c0) * (cs43 * rs1);
+        J[158] = (K[K_d5]*dj1_c0) * (cs44 * rs1);
     }
     {  // row 2
     const T rs2 = nt_rscale<T>(nt_exp_hi(x[2]), fh);
-        const T dj2_c0 = F.dt*nt_cvt<T>(x[43]);
+        const T dj2_c0 = F.dt*xt43;
         const T dj2_c1 = F.dt*F.parth2o;
         const T dj2_c2 = F.parthno3*K[K_b27];
         const T dj2_c3 = F.parthcl*K[K_d11];
-        J[261] = (-K[K_c2]*dj2_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs2);
-        J[266] = (dj2_c1*(K[K_a1et]*nt_cvt<T>(x[42]) + tj[J_h2o]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs2);
-        J[260] = (-dj2_c0*dj2_c2) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs2);
-        J[265] = (-dj2_c0*dj2_c3) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs2);
-        J[262] = (-K[K_a30]*dj2_c0) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs2);
-        J[264] = (-K[K_c8]*dj2_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs2);
-        J[258] = (-F.dt*(K[K_c17a]*nt_cvt<T>(x[43]) + K[K_c17b]*nt_cvt<T>(x[43]))) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs2);
-        J[259] = (K[K_a1et]*dj2_c1*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs2);
-        J[267] = (-F.dt*(F.h2*K[K_a19] + K[K_a17]*nt_cvt<T>(x[47]) + K[K_a30]*nt_cvt<T>(x[16]) + T(2)*K[K_a31]*nt_cvt<T>(x[43]) + K[K_c17a]*nt_cvt<T>(x[29]) + K[K_c17b]*nt_cvt<T>(x[29]) + K[K_c2]*nt_cvt<T>(x[1]) + K[K_c8]*nt_cvt<T>(x[27]) + dj2_c2*nt_cvt<T>(x[4]) + dj2_c3*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs2);
-        J[268] = (-F.dt*(K[K_a17]*nt_cvt<T>(x[43]) + T(1.6e-12)*nt_cvt<T>(x[55]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs2);
-        J[263] = (-T(1.6e-12)*F.dt*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs2);
+        J[261] = (-K[K_c2]*dj2_c0) * (cs1 * rs2);
+        J[266] = (dj2_c1*(K[K_a1et]*xt42 + tj[J_h2o]) + T(1)) * (cs2 * rs2);
+        J[260] = (-dj2_c0*dj2_c2) * (cs4 * rs2);
+        J[265] = (-dj2_c0*dj2_c3) * (cs12 * rs2);
+        J[262] = (-K[K_a30]*dj2_c0) * (cs16 * rs2);
+        J[264] = (-K[K_c8]*dj2_c0) * (cs27 * rs2);
+        J[258] = (-F.dt*(K[K_c17a]*xt43 + K[K_c17b]*xt43)) * (cs29 * rs2);
+        J[259] = (K[K_a1et]*dj2_c1*xt2) * (cs42 * rs2);
+        J[267] = (-F.dt*(F.h2*K[K_a19] + K[K_a17]*xt47 + K[K_a30]*xt16 + T(2)*K[K_a31]*xt43 + K[K_c17a]*xt29 + K[K_c17b]*xt29 + K[K_c2]*xt1 + K[K_c8]*xt27 + dj2_c2*xt4 + dj2_c3*xt12)) * (cs43 * rs2);
+        J[268] = (-F.dt*(K[K_a17]*xt43 + T(1.6e-12)*xt55)) * (cs47 * rs2);
+        J[263] = (-T(1.6e-12)*F.dt*xt47) * (cs55 * rs2);
     }
     {  // row 3
     const T rs3 = nt_rscale<T>(nt_exp_hi(x[3]), fh);
         const T dj3_c0 = T(2)*F.dt;
         const T dj3_c1 = K[K_b39]*dj3_c0;
         const T dj3_c2 = K[K_b6]*dj3_c0;
-        J[20] = (-dj3_c1*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs3);
-        J[23] = (F.dt*F.rain_hno3) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs3);
-        J[22] = (-dj3_c1*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs3);
-        J[24] = (dj3_c2*nt_cvt<T>(x[51])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs3);
-        J[21] = (dj3_c2*nt_cvt<T>(x[49])) * (nt_scale<T>(nt_exp_hi(x[51]), fh) * rs3);
+        J[20] = (-dj3_c1*xt42) * (cs0 * rs3);
+        J[23] = (F.dt*F.rain_hno3) * (cs4 * rs3);
+        J[22] = (-dj3_c1*xt0) * (cs42 * rs3);
+        J[24] = (dj3_c2*xt51) * (cs49 * rs3);
+        J[21] = (dj3_c2*xt49) * (cs51 * rs3);
     }
     {  // row 4
     const T rs4 = nt_rscale<T>(nt_exp_hi(x[4]), fh);
         const T dj4_c0 = T(2)*het[2];
         const T dj4_c1 = F.dt*K[K_b22];
-        J[122] = (-F.dt*(dj4_c0*nt_cvt<T>(x[5]) + het[0]*nt_cvt<T>(x[13]) + het[5]*nt_cvt<T>(x[19]))) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs4);
-        J[120] = (F.dt*(F.parthno3*(K[K_b27]*nt_cvt<T>(x[43]) + tj[J_hno3]) + F.rain_hno3) + T(1)) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs4);
-        J[118] = (-F.dt*(dj4_c0*nt_cvt<T>(x[2]) + het[3]*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs4);
-        J[121] = (-F.dt*(het[1]*nt_cvt<T>(x[13]) + het[3]*nt_cvt<T>(x[5]))) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs4);
-        J[119] = (-F.dt*(het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs4);
-        J[117] = (-F.dt*het[5]*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs4);
-        J[124] = (F.dt*F.parthno3*K[K_b27]*nt_cvt<T>(x[4]) - dj4_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs4);
-        J[123] = (-dj4_c1*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs4);
+        J[122] = (-F.dt*(dj4_c0*xt5 + het[0]*xt13 + het[5]*xt19)) * (cs2 * rs4);
+        J[120] = (F.dt*(F.parthno3*(K[K_b27]*xt43 + tj[J_hno3]) + F.rain_hno3) + T(1)) * (cs4 * rs4);
+        J[118] = (-F.dt*(dj4_c0*xt2 + het[3]*xt12)) * (cs5 * rs4);
+        J[121] = (-F.dt*(het[1]*xt13 + het[3]*xt5)) * (cs12 * rs4);
+        J[119] = (-F.dt*(het[0]*xt2 + het[1]*xt12)) * (cs13 * rs4);
+        J[117] = (-F.dt*het[5]*xt2) * (cs19 * rs4);
+        J[124] = (F.dt*F.parthno3*K[K_b27]*xt4 - dj4_c1*xt48) * (cs43 * rs4);
+        J[123] = (-dj4_c1*xt43) * (cs48 * rs4);
     }
     {  // row 5
     const T rs5 = nt_rscale<T>(nt_exp_hi(x[5]), fh);
-        const T dj5_c0 = F.dt*nt_cvt<T>(x[5]);
+        const T dj5_c0 = F.dt*xt5;
         const T dj5_c1 = F.dt*K[K_b12];
-        J[74] = (dj5_c0*het[2]) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs5);
-        J[72] = (F.dt*(F.hnm*K[K_b32] + het[2]*nt_cvt<T>(x[2]) + het[3]*nt_cvt<T>(x[12]) + tj[J_n2o5]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs5);
-        J[73] = (dj5_c0*het[3]) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs5);
-        J[75] = (-dj5_c1*nt_cvt<T>(x[54])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs5);
-        J[71] = (-dj5_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[54]), fh) * rs5);
+        J[74] = (dj5_c0*het[2]) * (cs2 * rs5);
+        J[72] = (F.dt*(F.hnm*K[K_b32] + het[2]*xt2 + het[3]*xt12 + tj[J_n2o5]) + T(1)) * (cs5 * rs5);
+        J[73] = (dj5_c0*het[3]) * (cs12 * rs5);
+        J[75] = (-dj5_c1*xt54) * (cs48 * rs5);
+        J[71] = (-dj5_c1*xt48) * (cs54 * rs5);
     }
     {  // row 6
     const T rs6 = nt_rscale<T>(nt_exp_hi(x[6]), fh);
-        const T dj6_c0 = T(3)*nt_cvt<T>(x[42]);
+        const T dj6_c0 = T(3)*xt42;
         const T dj6_c1 = T(2)*K[K_d91];
         const T dj6_c2 = T(4)*K[K_d93];
         const T dj6_c3 = T(3)*K[K_d94];
-        J[9] = (F.dt*F.rain_hcl) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs6);
-        J[7] = (-F.dt*(K[K_d90]*dj6_c0 + T(3)*tj[J_cfc11])) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs6);
-        J[4] = (-F.dt*(dj6_c1*nt_cvt<T>(x[42]) + T(2)*tj[J_cfc12])) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs6);
-        J[0] = (-F.dt*(K[K_d92]*dj6_c0 + T(3)*tj[J_cfc113])) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs6);
-        J[2] = (-F.dt*(dj6_c2*nt_cvt<T>(x[42]) + T(4)*tj[J_ccl4])) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs6);
-        J[6] = (-F.dt*(dj6_c3*nt_cvt<T>(x[43]) + T(3)*tj[J_ch3ccl3])) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs6);
-        J[5] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl])) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs6);
-        J[3] = (-F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22])) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs6);
-        J[1] = (-F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211])) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs6);
-        J[8] = (-F.dt*(T(3)*K[K_d90]*nt_cvt<T>(x[30]) + T(3)*K[K_d92]*nt_cvt<T>(x[32]) + K[K_d96]*nt_cvt<T>(x[36]) + K[K_e52]*nt_cvt<T>(x[38]) + dj6_c1*nt_cvt<T>(x[31]) + dj6_c2*nt_cvt<T>(x[33]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs6);
-        J[10] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[35]) + K[K_d97]*nt_cvt<T>(x[36]) + dj6_c3*nt_cvt<T>(x[34]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs6);
+        J[9] = (F.dt*F.rain_hcl) * (cs12 * rs6);
+        J[7] = (-F.dt*(K[K_d90]*dj6_c0 + T(3)*tj[J_cfc11])) * (cs30 * rs6);
+        J[4] = (-F.dt*(dj6_c1*xt42 + T(2)*tj[J_cfc12])) * (cs31 * rs6);
+        J[0] = (-F.dt*(K[K_d92]*dj6_c0 + T(3)*tj[J_cfc113])) * (cs32 * rs6);
+        J[2] = (-F.dt*(dj6_c2*xt42 + T(4)*tj[J_ccl4])) * (cs33 * rs6);
+        J[6] = (-F.dt*(dj6_c3*xt43 + T(3)*tj[J_ch3ccl3])) * (cs34 * rs6);
+        J[5] = (-F.dt*(K[K_d95]*xt43 + tj[J_ch3cl])) * (cs35 * rs6);
+        J[3] = (-F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22])) * (cs36 * rs6);
+        J[1] = (-F.dt*(K[K_e52]*xt42 + tj[J_h1211])) * (cs38 * rs6);
+        J[8] = (-F.dt*(T(3)*K[K_d90]*xt30 + T(3)*K[K_d92]*xt32 + K[K_d96]*xt36 + K[K_e52]*xt38 + dj6_c1*xt31 + dj6_c2*xt33)) * (cs42 * rs6);
+        J[10] = (-F.dt*(K[K_d95]*xt35 + K[K_d97]*xt36 + dj6_c3*xt34)) * (cs43 * rs6);
     }
     {  // row 9
     const T rs9 = nt_rscale<T>(nt_exp_hi(x[9]), fh);
         const T dj9_c0 = F.dt*K[K_e5a];
-        J[100] = (F.dt*tj[J_oclo] + T(1)) * (nt_scale<T>(nt_exp_hi(x[9]), fh) * rs9);
-        J[102] = (-dj9_c0*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs9);
-        J[101] = (-dj9_c0*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs9);
+        J[100] = (F.dt*tj[J_oclo] + T(1)) * (cs9 * rs9);
+        J[102] = (-dj9_c0*xt53) * (cs52 * rs9);
+        J[101] = (-dj9_c0*xt52) * (cs53 * rs9);
     }
     {  // row 10
     const T rs10 = nt_rscale<T>(nt_exp_hi(x[10]), fh);
@@ -247,336 +362,336 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     }
     {  // row 12
     const T rs12 = nt_rscale<T>(nt_exp_hi(x[12]), fh);
-        const T dj12_c0 = F.dt*nt_cvt<T>(x[44]);
-        const T dj12_c1 = F.dt*nt_cvt<T>(x[12]);
+        const T dj12_c0 = F.dt*xt44;
+        const T dj12_c1 = F.dt*xt12;
         const T dj12_c2 = F.dt*K[K_d9];
-        J[250] = (-K[K_d5]*dj12_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs12);
-        J[247] = (dj12_c1*het[3]) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs12);
-        J[253] = (F.dt*(F.parthcl*(K[K_d11]*nt_cvt<T>(x[43]) + tj[J_hcl]) + F.rain_hcl + het[1]*nt_cvt<T>(x[13]) + het[3]*nt_cvt<T>(x[5]) + het[4]*nt_cvt<T>(x[14]) + het[6]*nt_cvt<T>(x[25])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs12);
-        J[249] = (dj12_c1*het[1]) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs12);
-        J[251] = (dj12_c1*het[4]) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs12);
-        J[248] = (dj12_c1*het[6]) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs12);
-        J[252] = (-K[K_c10]*dj12_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs12);
-        J[255] = (F.parthcl*K[K_d11]*dj12_c1 - dj12_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs12);
-        J[254] = (-F.dt*(F.h2*K[K_d6] + K[K_c10]*nt_cvt<T>(x[27]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs12);
-        J[256] = (-K[K_d7]*dj12_c0) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs12);
-        J[257] = (-dj12_c2*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs12);
+        J[250] = (-K[K_d5]*dj12_c0) * (cs1 * rs12);
+        J[247] = (dj12_c1*het[3]) * (cs5 * rs12);
+        J[253] = (F.dt*(F.parthcl*(K[K_d11]*xt43 + tj[J_hcl]) + F.rain_hcl + het[1]*xt13 + het[3]*xt5 + het[4]*xt14 + het[6]*xt25) + T(1)) * (cs12 * rs12);
+        J[249] = (dj12_c1*het[1]) * (cs13 * rs12);
+        J[251] = (dj12_c1*het[4]) * (cs14 * rs12);
+        J[248] = (dj12_c1*het[6]) * (cs25 * rs12);
+        J[252] = (-K[K_c10]*dj12_c0) * (cs27 * rs12);
+        J[255] = (F.parthcl*K[K_d11]*dj12_c1 - dj12_c2*xt52) * (cs43 * rs12);
+        J[254] = (-F.dt*(F.h2*K[K_d6] + K[K_c10]*xt27 + K[K_d5]*xt1 + K[K_d7]*xt47)) * (cs44 * rs12);
+        J[256] = (-K[K_d7]*dj12_c0) * (cs47 * rs12);
+        J[257] = (-dj12_c2*xt43) * (cs52 * rs12);
     }
     {  // row 13
     const T rs13 = nt_rscale<T>(nt_exp_hi(x[13]), fh);
-        const T dj13_c0 = F.dt*nt_cvt<T>(x[13]);
+        const T dj13_c0 = F.dt*xt13;
         const T dj13_c1 = F.dt*K[K_d31];
-        J[89] = (dj13_c0*het[0]) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs13);
-        J[88] = (dj13_c0*het[1]) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs13);
-        J[87] = (F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]) + tj[J_clono2_cl] + tj[J_clono2_clo]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs13);
-        J[91] = (K[K_d32]*dj13_c0) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs13);
-        J[90] = (-dj13_c1*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs13);
-        J[92] = (-dj13_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs13);
+        J[89] = (dj13_c0*het[0]) * (cs2 * rs13);
+        J[88] = (dj13_c0*het[1]) * (cs12 * rs13);
+        J[87] = (F.dt*(K[K_d32]*xt45 + het[0]*xt2 + het[1]*xt12 + tj[J_clono2_cl] + tj[J_clono2_clo]) + T(1)) * (cs13 * rs13);
+        J[91] = (K[K_d32]*dj13_c0) * (cs45 * rs13);
+        J[90] = (-dj13_c1*xt52) * (cs48 * rs13);
+        J[92] = (-dj13_c1*xt48) * (cs52 * rs13);
     }
     {  // row 14
     const T rs14 = nt_rscale<T>(nt_exp_hi(x[14]), fh);
         const T dj14_c0 = F.dt*het[0];
-        const T dj14_c1 = F.dt*nt_cvt<T>(x[14]);
+        const T dj14_c1 = F.dt*xt14;
         const T dj14_c2 = F.dt*K[K_d33];
-        J[170] = (-dj14_c0*nt_cvt<T>(x[13])) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs14);
-        J[169] = (dj14_c1*het[4]) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs14);
-        J[166] = (-dj14_c0*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs14);
-        J[167] = (F.dt*(K[K_d34]*nt_cvt<T>(x[43]) + K[K_d35]*nt_cvt<T>(x[45]) + K[K_d37]*nt_cvt<T>(x[44]) + het[4]*nt_cvt<T>(x[12]) + het[8]*nt_cvt<T>(x[18]) + tj[J_hocl]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs14);
-        J[168] = (dj14_c1*het[8]) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs14);
-        J[173] = (K[K_d34]*dj14_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs14);
-        J[172] = (K[K_d37]*dj14_c1) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs14);
-        J[171] = (K[K_d35]*dj14_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs14);
-        J[174] = (-dj14_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs14);
-        J[175] = (-dj14_c2*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs14);
+        J[170] = (-dj14_c0*xt13) * (cs2 * rs14);
+        J[169] = (dj14_c1*het[4]) * (cs12 * rs14);
+        J[166] = (-dj14_c0*xt2) * (cs13 * rs14);
+        J[167] = (F.dt*(K[K_d34]*xt43 + K[K_d35]*xt45 + K[K_d37]*xt44 + het[4]*xt12 + het[8]*xt18 + tj[J_hocl]) + T(1)) * (cs14 * rs14);
+        J[168] = (dj14_c1*het[8]) * (cs18 * rs14);
+        J[173] = (K[K_d34]*dj14_c1) * (cs43 * rs14);
+        J[172] = (K[K_d37]*dj14_c1) * (cs44 * rs14);
+        J[171] = (K[K_d35]*dj14_c1) * (cs45 * rs14);
+        J[174] = (-dj14_c2*xt52) * (cs47 * rs14);
+        J[175] = (-dj14_c2*xt47) * (cs52 * rs14);
     }
     {  // row 15
     const T rs15 = nt_rscale<T>(nt_exp_hi(x[15]), fh);
-        J[63] = (-F.dt*(het[1]*nt_cvt<T>(x[13]) + het[4]*nt_cvt<T>(x[14]))) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs15);
-        J[61] = (-F.dt*het[1]*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs15);
-        J[62] = (-F.dt*(K[K_d37]*nt_cvt<T>(x[44]) + het[4]*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs15);
-        J[60] = (F.dt*tj[J_cl2] + T(1)) * (nt_scale<T>(nt_exp_hi(x[15]), fh) * rs15);
-        J[64] = (-F.dt*K[K_d37]*nt_cvt<T>(x[14])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs15);
-        J[65] = (-T(2)*F.dt*K[K_d62]*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs15);
+        J[63] = (-F.dt*(het[1]*xt13 + het[4]*xt14)) * (cs12 * rs15);
+        J[61] = (-F.dt*het[1]*xt12) * (cs13 * rs15);
+        J[62] = (-F.dt*(K[K_d37]*xt44 + het[4]*xt12)) * (cs14 * rs15);
+        J[60] = (F.dt*tj[J_cl2] + T(1)) * (cs15 * rs15);
+        J[64] = (-F.dt*K[K_d37]*xt14) * (cs44 * rs15);
+        J[65] = (-T(2)*F.dt*K[K_d62]*xt52) * (cs52 * rs15);
     }
     {  // row 16
     const T rs16 = nt_rscale<T>(nt_exp_hi(x[16]), fh);
-        J[189] = (F.dt*(F.rain_h2o2 + K[K_a30]*nt_cvt<T>(x[43]) + tj[J_h2o2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs16);
-        J[190] = (F.dt*K[K_a30]*nt_cvt<T>(x[16])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs16);
-        J[191] = (-T(2)*F.dt*K[K_a27]*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs16);
+        J[189] = (F.dt*(F.rain_h2o2 + K[K_a30]*xt43 + tj[J_h2o2]) + T(1)) * (cs16 * rs16);
+        J[190] = (F.dt*K[K_a30]*xt16) * (cs43 * rs16);
+        J[191] = (-T(2)*F.dt*K[K_a27]*xt47) * (cs47 * rs16);
     }
     {  // row 17
     const T rs17 = nt_rscale<T>(nt_exp_hi(x[17]), fh);
         const T dj17_c0 = F.dt*het[3];
         const T dj17_c1 = F.dt*K[K_d36];
-        J[26] = (-dj17_c0*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs17);
-        J[27] = (-dj17_c0*nt_cvt<T>(x[5])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs17);
-        J[25] = (F.dt*tj[J_clno2] + T(1)) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs17);
-        J[29] = (-dj17_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs17);
-        J[28] = (-dj17_c1*nt_cvt<T>(x[44])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs17);
+        J[26] = (-dj17_c0*xt12) * (cs5 * rs17);
+        J[27] = (-dj17_c0*xt5) * (cs12 * rs17);
+        J[25] = (F.dt*tj[J_clno2] + T(1)) * (cs17 * rs17);
+        J[29] = (-dj17_c1*xt48) * (cs44 * rs17);
+        J[28] = (-dj17_c1*xt44) * (cs48 * rs17);
     }
     {  // row 18
     const T rs18 = nt_rscale<T>(nt_exp_hi(x[18]), fh);
-        const T dj18_c0 = F.dt*nt_cvt<T>(x[18]);
-        const T dj18_c1 = F.dt*nt_cvt<T>(x[50]);
+        const T dj18_c0 = F.dt*xt18;
+        const T dj18_c1 = F.dt*xt50;
         const T dj18_c2 = F.parthbr*dj18_c0;
-        J[183] = (dj18_c0*het[8]) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs18);
-        J[184] = (F.dt*(F.parthbr*(K[K_e11]*nt_cvt<T>(x[43]) + K[K_e9]*nt_cvt<T>(x[42]) + tj[J_hbr]) + F.rain_hbr + het[7]*nt_cvt<T>(x[25]) + het[8]*nt_cvt<T>(x[14])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs18);
-        J[181] = (dj18_c0*het[7]) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs18);
-        J[185] = (-K[K_c19]*dj18_c1) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs18);
-        J[182] = (K[K_e9]*dj18_c2) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs18);
-        J[187] = (K[K_e11]*dj18_c2) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs18);
-        J[188] = (-K[K_e7]*dj18_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs18);
-        J[186] = (-F.dt*(K[K_c19]*nt_cvt<T>(x[27]) + K[K_e7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs18);
+        J[183] = (dj18_c0*het[8]) * (cs14 * rs18);
+        J[184] = (F.dt*(F.parthbr*(K[K_e11]*xt43 + K[K_e9]*xt42 + tj[J_hbr]) + F.rain_hbr + het[7]*xt25 + het[8]*xt14) + T(1)) * (cs18 * rs18);
+        J[181] = (dj18_c0*het[7]) * (cs25 * rs18);
+        J[185] = (-K[K_c19]*dj18_c1) * (cs27 * rs18);
+        J[182] = (K[K_e9]*dj18_c2) * (cs42 * rs18);
+        J[187] = (K[K_e11]*dj18_c2) * (cs43 * rs18);
+        J[188] = (-K[K_e7]*dj18_c1) * (cs47 * rs18);
+        J[186] = (-F.dt*(K[K_c19]*xt27 + K[K_e7]*xt47)) * (cs50 * rs18);
     }
     {  // row 19
     const T rs19 = nt_rscale<T>(nt_exp_hi(x[19]), fh);
-        const T dj19_c0 = F.dt*nt_cvt<T>(x[19]);
+        const T dj19_c0 = F.dt*xt19;
         const T dj19_c1 = F.dt*K[K_e13];
-        J[56] = (dj19_c0*het[5]) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs19);
-        J[55] = (F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + het[5]*nt_cvt<T>(x[2]) + tj[J_brono2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs19);
-        J[58] = (K[K_e8]*dj19_c0) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs19);
-        J[57] = (-dj19_c1*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs19);
-        J[59] = (-dj19_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs19);
+        J[56] = (dj19_c0*het[5]) * (cs2 * rs19);
+        J[55] = (F.dt*(K[K_e8]*xt45 + het[5]*xt2 + tj[J_brono2]) + T(1)) * (cs19 * rs19);
+        J[58] = (K[K_e8]*dj19_c0) * (cs45 * rs19);
+        J[57] = (-dj19_c1*xt53) * (cs48 * rs19);
+        J[59] = (-dj19_c1*xt48) * (cs53 * rs19);
     }
     {  // row 20
     const T rs20 = nt_rscale<T>(nt_exp_hi(x[20]), fh);
         const T dj20_c0 = T(2)*F.dt;
         const T dj20_c1 = K[K_b39]*dj20_c0;
         const T dj20_c2 = F.parthno3*K[K_b27];
-        const T dj20_c3 = F.dt*nt_cvt<T>(x[48]);
+        const T dj20_c3 = F.dt*xt48;
         const T dj20_c4 = T(2)*K[K_b12];
         const T dj20_c5 = K[K_b6]*dj20_c0;
-        J[233] = (-dj20_c1*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs20);
-        J[237] = (-F.dt*(F.parthno3*tj[J_hno3] + dj20_c2*nt_cvt<T>(x[43]))) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs20);
-        J[232] = (-F.dt*(T(2)*F.hnm*K[K_b32] + T(2)*tj[J_n2o5])) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs20);
-        J[235] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + tj[J_clono2_cl] + tj[J_clono2_clo])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs20);
-        J[229] = (-F.dt*tj[J_clno2]) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs20);
-        J[230] = (-F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + tj[J_brono2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs20);
-        J[238] = (-F.dt*(F.hnm*K[K_b24] + K[K_b28]*nt_cvt<T>(x[43]) + tj[J_hno4])) * (nt_scale<T>(nt_exp_hi(x[21]), fh) * rs20);
-        J[236] = (-dj20_c1*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs20);
-        J[243] = (-F.dt*(K[K_b28]*nt_cvt<T>(x[21]) + dj20_c2*nt_cvt<T>(x[4])) + K[K_b22]*dj20_c3) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs20);
-        J[241] = (K[K_d36]*dj20_c3) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs20);
-        J[240] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[13]) + K[K_e8]*nt_cvt<T>(x[19]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs20);
-        J[244] = (K[K_b23]*dj20_c3) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs20);
-        J[239] = (F.dt*(K[K_b22]*nt_cvt<T>(x[43]) + K[K_b23]*nt_cvt<T>(x[47]) + K[K_d31]*nt_cvt<T>(x[52]) + K[K_d36]*nt_cvt<T>(x[44]) + K[K_e13]*nt_cvt<T>(x[53]) + dj20_c4*nt_cvt<T>(x[54]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs20);
-        J[245] = (dj20_c5*nt_cvt<T>(x[51])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs20);
-        J[234] = (dj20_c5*nt_cvt<T>(x[49])) * (nt_scale<T>(nt_exp_hi(x[51]), fh) * rs20);
-        J[246] = (K[K_d31]*dj20_c3) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs20);
-        J[242] = (K[K_e13]*dj20_c3) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs20);
-        J[231] = (dj20_c3*dj20_c4) * (nt_scale<T>(nt_exp_hi(x[54]), fh) * rs20);
+        J[233] = (-dj20_c1*xt42) * (cs0 * rs20);
+        J[237] = (-F.dt*(F.parthno3*tj[J_hno3] + dj20_c2*xt43)) * (cs4 * rs20);
+        J[232] = (-F.dt*(T(2)*F.hnm*K[K_b32] + T(2)*tj[J_n2o5])) * (cs5 * rs20);
+        J[235] = (-F.dt*(K[K_d32]*xt45 + tj[J_clono2_cl] + tj[J_clono2_clo])) * (cs13 * rs20);
+        J[229] = (-F.dt*tj[J_clno2]) * (cs17 * rs20);
+        J[230] = (-F.dt*(K[K_e8]*xt45 + tj[J_brono2])) * (cs19 * rs20);
+        J[238] = (-F.dt*(F.hnm*K[K_b24] + K[K_b28]*xt43 + tj[J_hno4])) * (cs21 * rs20);
+        J[236] = (-dj20_c1*xt0) * (cs42 * rs20);
+        J[243] = (-F.dt*(K[K_b28]*xt21 + dj20_c2*xt4) + K[K_b22]*dj20_c3) * (cs43 * rs20);
+        J[241] = (K[K_d36]*dj20_c3) * (cs44 * rs20);
+        J[240] = (-F.dt*(K[K_d32]*xt13 + K[K_e8]*xt19)) * (cs45 * rs20);
+        J[244] = (K[K_b23]*dj20_c3) * (cs47 * rs20);
+        J[239] = (F.dt*(K[K_b22]*xt43 + K[K_b23]*xt47 + K[K_d31]*xt52 + K[K_d36]*xt44 + K[K_e13]*xt53 + dj20_c4*xt54)) * (cs48 * rs20);
+        J[245] = (dj20_c5*xt51) * (cs49 * rs20);
+        J[234] = (dj20_c5*xt49) * (cs51 * rs20);
+        J[246] = (K[K_d31]*dj20_c3) * (cs52 * rs20);
+        J[242] = (K[K_e13]*dj20_c3) * (cs53 * rs20);
+        J[231] = (dj20_c3*dj20_c4) * (cs54 * rs20);
     }
     {  // row 21
     const T rs21 = nt_rscale<T>(nt_exp_hi(x[21]), fh);
         const T dj21_c0 = F.dt*K[K_b23];
-        J[152] = (F.dt*(F.hnm*K[K_b24] + K[K_b28]*nt_cvt<T>(x[43]) + tj[J_hno4]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[21]), fh) * rs21);
-        J[154] = (F.dt*K[K_b28]*nt_cvt<T>(x[21])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs21);
-        J[155] = (-dj21_c0*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs21);
-        J[153] = (-dj21_c0*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs21);
+        J[152] = (F.dt*(F.hnm*K[K_b24] + K[K_b28]*xt43 + tj[J_hno4]) + T(1)) * (cs21 * rs21);
+        J[154] = (F.dt*K[K_b28]*xt21) * (cs43 * rs21);
+        J[155] = (-dj21_c0*xt48) * (cs47 * rs21);
+        J[153] = (-dj21_c0*xt47) * (cs48 * rs21);
     }
     {  // row 22
     const T rs22 = nt_rscale<T>(nt_exp_hi(x[22]), fh);
-        const T dj22_c0 = F.dt*nt_cvt<T>(x[44]);
-        const T dj22_c1 = T(3)*nt_cvt<T>(x[42]);
+        const T dj22_c0 = F.dt*xt44;
+        const T dj22_c1 = T(3)*xt42;
         const T dj22_c2 = T(2)*K[K_d91];
         const T dj22_c3 = T(4)*K[K_d93];
         const T dj22_c4 = T(3)*K[K_d94];
-        const T dj22_c5 = F.dt*nt_cvt<T>(x[52]);
+        const T dj22_c5 = F.dt*xt52;
         const T dj22_c6 = T(2)*K[K_d60];
         const T dj22_c7 = T(2)*K[K_d62];
-        J[141] = (K[K_d5]*dj22_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs22);
-        J[140] = (-F.dt*tj[J_oclo]) * (nt_scale<T>(nt_exp_hi(x[9]), fh) * rs22);
-        J[144] = (-F.dt*F.parthcl*(K[K_d11]*nt_cvt<T>(x[43]) + tj[J_hcl])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs22);
-        J[135] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + tj[J_clono2_cl] + tj[J_clono2_clo])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs22);
-        J[142] = (-F.dt*(K[K_d34]*nt_cvt<T>(x[43]) + K[K_d35]*nt_cvt<T>(x[45]) + tj[J_hocl]) + K[K_d37]*dj22_c0) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs22);
-        J[133] = (-T(2)*F.dt*tj[J_cl2]) * (nt_scale<T>(nt_exp_hi(x[15]), fh) * rs22);
-        J[128] = (-F.dt*tj[J_clno2]) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs22);
-        J[138] = (-F.dt*(T(2)*F.hnm*K[K_d61] + T(2)*tj[J_cl2o2])) * (nt_scale<T>(nt_exp_hi(x[24]), fh) * rs22);
-        J[132] = (-F.dt*tj[J_brcl]) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs22);
-        J[143] = (K[K_c10]*dj22_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs22);
-        J[137] = (-F.dt*(K[K_d90]*dj22_c1 + T(3)*tj[J_cfc11])) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs22);
-        J[131] = (-F.dt*(dj22_c2*nt_cvt<T>(x[42]) + T(2)*tj[J_cfc12])) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs22);
-        J[127] = (-F.dt*(K[K_d92]*dj22_c1 + T(3)*tj[J_cfc113])) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs22);
-        J[129] = (-F.dt*(dj22_c3*nt_cvt<T>(x[42]) + T(4)*tj[J_ccl4])) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs22);
-        J[136] = (-F.dt*(dj22_c4*nt_cvt<T>(x[43]) + T(3)*tj[J_ch3ccl3])) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs22);
-        J[134] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl])) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs22);
-        J[130] = (-F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22])) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs22);
-        J[139] = (-F.dt*(T(3)*K[K_d90]*nt_cvt<T>(x[30]) + T(3)*K[K_d92]*nt_cvt<T>(x[32]) + K[K_d96]*nt_cvt<T>(x[36]) + dj22_c2*nt_cvt<T>(x[31]) + dj22_c3*nt_cvt<T>(x[33]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs22);
-        J[149] = (-F.dt*(F.parthcl*K[K_d11]*nt_cvt<T>(x[12]) + K[K_d34]*nt_cvt<T>(x[14]) + K[K_d95]*nt_cvt<T>(x[35]) + K[K_d97]*nt_cvt<T>(x[36]) + dj22_c4*nt_cvt<T>(x[34])) + K[K_d9]*dj22_c5) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs22);
-        J[147] = (F.dt*(F.h2*K[K_d6] + K[K_c10]*nt_cvt<T>(x[27]) + K[K_d36]*nt_cvt<T>(x[48]) + K[K_d37]*nt_cvt<T>(x[14]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs22);
-        J[146] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[13]) + K[K_d35]*nt_cvt<T>(x[14]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs22);
-        J[150] = (F.dt*(K[K_d33]*nt_cvt<T>(x[52]) + K[K_d7]*nt_cvt<T>(x[44]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs22);
-        J[145] = (F.dt*(K[K_d31]*nt_cvt<T>(x[52]) + K[K_d36]*nt_cvt<T>(x[44]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs22);
-        J[151] = (F.dt*(K[K_d31]*nt_cvt<T>(x[48]) + K[K_d33]*nt_cvt<T>(x[47]) + K[K_d9]*nt_cvt<T>(x[43]) + K[K_e5a]*nt_cvt<T>(x[53]) + K[K_e5c]*nt_cvt<T>(x[53]) + dj22_c6*nt_cvt<T>(x[52]) + dj22_c7*nt_cvt<T>(x[52]) + nt_cvt<T>(x[52])*(dj22_c6 + dj22_c7))) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs22);
-        J[148] = (dj22_c5*(K[K_e5a] + K[K_e5c])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs22);
+        J[141] = (K[K_d5]*dj22_c0) * (cs1 * rs22);
+        J[140] = (-F.dt*tj[J_oclo]) * (cs9 * rs22);
+        J[144] = (-F.dt*F.parthcl*(K[K_d11]*xt43 + tj[J_hcl])) * (cs12 * rs22);
+        J[135] = (-F.dt*(K[K_d32]*xt45 + tj[J_clono2_cl] + tj[J_clono2_clo])) * (cs13 * rs22);
+        J[142] = (-F.dt*(K[K_d34]*xt43 + K[K_d35]*xt45 + tj[J_hocl]) + K[K_d37]*dj22_c0) * (cs14 * rs22);
+        J[133] = (-T(2)*F.dt*tj[J_cl2]) * (cs15 * rs22);
+        J[128] = (-F.dt*tj[J_clno2]) * (cs17 * rs22);
+        J[138] = (-F.dt*(T(2)*F.hnm*K[K_d61] + T(2)*tj[J_cl2o2])) * (cs24 * rs22);
+        J[132] = (-F.dt*tj[J_brcl]) * (cs26 * rs22);
+        J[143] = (K[K_c10]*dj22_c0) * (cs27 * rs22);
+        J[137] = (-F.dt*(K[K_d90]*dj22_c1 + T(3)*tj[J_cfc11])) * (cs30 * rs22);
+        J[131] = (-F.dt*(dj22_c2*xt42 + T(2)*tj[J_cfc12])) * (cs31 * rs22);
+        J[127] = (-F.dt*(K[K_d92]*dj22_c1 + T(3)*tj[J_cfc113])) * (cs32 * rs22);
+        J[129] = (-F.dt*(dj22_c3*xt42 + T(4)*tj[J_ccl4])) * (cs33 * rs22);
+        J[136] = (-F.dt*(dj22_c4*xt43 + T(3)*tj[J_ch3ccl3])) * (cs34 * rs22);
+        J[134] = (-F.dt*(K[K_d95]*xt43 + tj[J_ch3cl])) * (cs35 * rs22);
+        J[130] = (-F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22])) * (cs36 * rs22);
+        J[139] = (-F.dt*(T(3)*K[K_d90]*xt30 + T(3)*K[K_d92]*xt32 + K[K_d96]*xt36 + dj22_c2*xt31 + dj22_c3*xt33)) * (cs42 * rs22);
+        J[149] = (-F.dt*(F.parthcl*K[K_d11]*xt12 + K[K_d34]*xt14 + K[K_d95]*xt35 + K[K_d97]*xt36 + dj22_c4*xt34) + K[K_d9]*dj22_c5) * (cs43 * rs22);
+        J[147] = (F.dt*(F.h2*K[K_d6] + K[K_c10]*xt27 + K[K_d36]*xt48 + K[K_d37]*xt14 + K[K_d5]*xt1 + K[K_d7]*xt47)) * (cs44 * rs22);
+        J[146] = (-F.dt*(K[K_d32]*xt13 + K[K_d35]*xt14)) * (cs45 * rs22);
+        J[150] = (F.dt*(K[K_d33]*xt52 + K[K_d7]*xt44)) * (cs47 * rs22);
+        J[145] = (F.dt*(K[K_d31]*xt52 + K[K_d36]*xt44)) * (cs48 * rs22);
+        J[151] = (F.dt*(K[K_d31]*xt48 + K[K_d33]*xt47 + K[K_d9]*xt43 + K[K_e5a]*xt53 + K[K_e5c]*xt53 + dj22_c6*xt52 + dj22_c7*xt52 + xt52*(dj22_c6 + dj22_c7))) * (cs52 * rs22);
+        J[148] = (dj22_c5*(K[K_e5a] + K[K_e5c])) * (cs53 * rs22);
     }
     {  // row 23
     const T rs23 = nt_rscale<T>(nt_exp_hi(x[23]), fh);
         const T dj23_c0 = T(2)*het[7];
-        const T dj23_c1 = F.dt*F.parthbr*nt_cvt<T>(x[18]);
-        const T dj23_c2 = F.dt*nt_cvt<T>(x[53]);
-        J[196] = (-F.dt*(F.parthbr*(K[K_e11]*nt_cvt<T>(x[43]) + K[K_e9]*nt_cvt<T>(x[42]) + tj[J_hbr]) + dj23_c0*nt_cvt<T>(x[25]))) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs23);
-        J[193] = (-F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + tj[J_brono2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs23);
-        J[194] = (-F.dt*(K[K_e16]*nt_cvt<T>(x[45]) + dj23_c0*nt_cvt<T>(x[18]) + tj[J_hobr])) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs23);
-        J[192] = (-F.dt*tj[J_brcl]) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs23);
-        J[197] = (F.dt*K[K_c19]*nt_cvt<T>(x[50])) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs23);
-        J[195] = (-K[K_e9]*dj23_c1) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs23);
-        J[202] = (-K[K_e11]*dj23_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs23);
-        J[199] = (-F.dt*(K[K_e16]*nt_cvt<T>(x[25]) + K[K_e8]*nt_cvt<T>(x[19]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs23);
-        J[203] = (F.dt*(K[K_e15]*nt_cvt<T>(x[53]) + K[K_e7]*nt_cvt<T>(x[50]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs23);
-        J[198] = (K[K_e13]*dj23_c2) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs23);
-        J[201] = (F.dt*(K[K_c19]*nt_cvt<T>(x[27]) + K[K_e7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs23);
-        J[204] = (K[K_e5c]*dj23_c2) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs23);
-        J[200] = (F.dt*(K[K_e13]*nt_cvt<T>(x[48]) + K[K_e15]*nt_cvt<T>(x[47]) + K[K_e5c]*nt_cvt<T>(x[52]))) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs23);
+        const T dj23_c1 = F.dt*F.parthbr*xt18;
+        const T dj23_c2 = F.dt*xt53;
+        J[196] = (-F.dt*(F.parthbr*(K[K_e11]*xt43 + K[K_e9]*xt42 + tj[J_hbr]) + dj23_c0*xt25)) * (cs18 * rs23);
+        J[193] = (-F.dt*(K[K_e8]*xt45 + tj[J_brono2])) * (cs19 * rs23);
+        J[194] = (-F.dt*(K[K_e16]*xt45 + dj23_c0*xt18 + tj[J_hobr])) * (cs25 * rs23);
+        J[192] = (-F.dt*tj[J_brcl]) * (cs26 * rs23);
+        J[197] = (F.dt*K[K_c19]*xt50) * (cs27 * rs23);
+        J[195] = (-K[K_e9]*dj23_c1) * (cs42 * rs23);
+        J[202] = (-K[K_e11]*dj23_c1) * (cs43 * rs23);
+        J[199] = (-F.dt*(K[K_e16]*xt25 + K[K_e8]*xt19)) * (cs45 * rs23);
+        J[203] = (F.dt*(K[K_e15]*xt53 + K[K_e7]*xt50)) * (cs47 * rs23);
+        J[198] = (K[K_e13]*dj23_c2) * (cs48 * rs23);
+        J[201] = (F.dt*(K[K_c19]*xt27 + K[K_e7]*xt47)) * (cs50 * rs23);
+        J[204] = (K[K_e5c]*dj23_c2) * (cs52 * rs23);
+        J[200] = (F.dt*(K[K_e13]*xt48 + K[K_e15]*xt47 + K[K_e5c]*xt52)) * (cs53 * rs23);
     }
     {  // row 24
     const T rs24 = nt_rscale<T>(nt_exp_hi(x[24]), fh);
-        J[97] = (F.dt*(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[24]), fh) * rs24);
-        J[98] = (-T(2)*F.dt*K[K_d60]*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs24);
+        J[97] = (F.dt*(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(1)) * (cs24 * rs24);
+        J[98] = (-T(2)*F.dt*K[K_d60]*xt52) * (cs52 * rs24);
     }
     {  // row 25
     const T rs25 = nt_rscale<T>(nt_exp_hi(x[25]), fh);
         const T dj25_c0 = F.dt*het[5];
-        const T dj25_c1 = F.dt*nt_cvt<T>(x[25]);
+        const T dj25_c1 = F.dt*xt25;
         const T dj25_c2 = F.dt*K[K_e15];
-        J[83] = (-dj25_c0*nt_cvt<T>(x[19])) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs25);
-        J[82] = (dj25_c1*het[6]) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs25);
-        J[81] = (dj25_c1*het[7]) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs25);
-        J[79] = (-dj25_c0*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs25);
-        J[80] = (F.dt*(K[K_e16]*nt_cvt<T>(x[45]) + het[6]*nt_cvt<T>(x[12]) + het[7]*nt_cvt<T>(x[18]) + tj[J_hobr]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs25);
-        J[84] = (K[K_e16]*dj25_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs25);
-        J[86] = (-dj25_c2*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs25);
-        J[85] = (-dj25_c2*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs25);
+        J[83] = (-dj25_c0*xt19) * (cs2 * rs25);
+        J[82] = (dj25_c1*het[6]) * (cs12 * rs25);
+        J[81] = (dj25_c1*het[7]) * (cs18 * rs25);
+        J[79] = (-dj25_c0*xt2) * (cs19 * rs25);
+        J[80] = (F.dt*(K[K_e16]*xt45 + het[6]*xt12 + het[7]*xt18 + tj[J_hobr]) + T(1)) * (cs25 * rs25);
+        J[84] = (K[K_e16]*dj25_c1) * (cs45 * rs25);
+        J[86] = (-dj25_c2*xt53) * (cs47 * rs25);
+        J[85] = (-dj25_c2*xt47) * (cs53 * rs25);
     }
     {  // row 26
     const T rs26 = nt_rscale<T>(nt_exp_hi(x[26]), fh);
         const T dj26_c0 = F.dt*het[6];
         const T dj26_c1 = F.dt*het[8];
         const T dj26_c2 = F.dt*K[K_e5c];
-        J[47] = (-dj26_c0*nt_cvt<T>(x[25])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs26);
-        J[45] = (-dj26_c1*nt_cvt<T>(x[18])) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs26);
-        J[46] = (-dj26_c1*nt_cvt<T>(x[14])) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs26);
-        J[44] = (-dj26_c0*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs26);
-        J[43] = (F.dt*tj[J_brcl] + T(1)) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs26);
-        J[49] = (-dj26_c2*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs26);
-        J[48] = (-dj26_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs26);
+        J[47] = (-dj26_c0*xt25) * (cs12 * rs26);
+        J[45] = (-dj26_c1*xt18) * (cs14 * rs26);
+        J[46] = (-dj26_c1*xt14) * (cs18 * rs26);
+        J[44] = (-dj26_c0*xt12) * (cs25 * rs26);
+        J[43] = (F.dt*tj[J_brcl] + T(1)) * (cs26 * rs26);
+        J[49] = (-dj26_c2*xt53) * (cs52 * rs26);
+        J[48] = (-dj26_c2*xt52) * (cs53 * rs26);
     }
     {  // row 28
     const T rs28 = nt_rscale<T>(nt_exp_hi(x[28]), fh);
-        const T dj28_c0 = T(2)*K[K_c14]*nt_cvt<T>(x[28]);
+        const T dj28_c0 = T(2)*K[K_c14]*xt28;
         const T dj28_c1 = F.dt*K[K_c17a];
-        const T dj28_c2 = F.dt*nt_cvt<T>(x[28]);
-        J[212] = (F.dt*dj28_c0 + F.dt*(K[K_c18]*nt_cvt<T>(x[52]) + K[K_c5]*nt_cvt<T>(x[49]) + K[K_c7]*nt_cvt<T>(x[47]) + dj28_c0) + T(1)) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs28);
-        J[210] = (-dj28_c1*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs28);
-        J[213] = (-dj28_c1*nt_cvt<T>(x[29])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs28);
-        J[214] = (K[K_c7]*dj28_c2) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs28);
-        J[215] = (K[K_c5]*dj28_c2) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs28);
-        J[216] = (K[K_c18]*dj28_c2) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs28);
-        J[211] = (-F.dt*F.o2*K[K_c4]) * (nt_scale<T>(nt_exp_hi(x[56]), fh) * rs28);
+        const T dj28_c2 = F.dt*xt28;
+        J[212] = (F.dt*dj28_c0 + F.dt*(K[K_c18]*xt52 + K[K_c5]*xt49 + K[K_c7]*xt47 + dj28_c0) + T(1)) * (cs28 * rs28);
+        J[210] = (-dj28_c1*xt43) * (cs29 * rs28);
+        J[213] = (-dj28_c1*xt29) * (cs43 * rs28);
+        J[214] = (K[K_c7]*dj28_c2) * (cs47 * rs28);
+        J[215] = (K[K_c5]*dj28_c2) * (cs49 * rs28);
+        J[216] = (K[K_c18]*dj28_c2) * (cs52 * rs28);
+        J[211] = (-F.dt*F.o2*K[K_c4]) * (cs56 * rs28);
     }
     {  // row 29
     const T rs29 = nt_rscale<T>(nt_exp_hi(x[29]), fh);
         const T dj29_c0 = F.dt*K[K_c7];
-        J[35] = (-dj29_c0*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs29);
-        J[34] = (F.dt*(K[K_c17a]*nt_cvt<T>(x[43]) + K[K_c17b]*nt_cvt<T>(x[43]) + tj[J_ch3o2h]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs29);
-        J[36] = (F.dt*nt_cvt<T>(x[29])*(K[K_c17a] + K[K_c17b])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs29);
-        J[37] = (-dj29_c0*nt_cvt<T>(x[28])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs29);
+        J[35] = (-dj29_c0*xt47) * (cs28 * rs29);
+        J[34] = (F.dt*(K[K_c17a]*xt43 + K[K_c17b]*xt43 + tj[J_ch3o2h]) + T(1)) * (cs29 * rs29);
+        J[36] = (F.dt*xt29*(K[K_c17a] + K[K_c17b])) * (cs43 * rs29);
+        J[37] = (-dj29_c0*xt28) * (cs47 * rs29);
     }
     {  // row 30
     const T rs30 = nt_rscale<T>(nt_exp_hi(x[30]), fh);
-        J[95] = (F.dt*(K[K_d90]*nt_cvt<T>(x[42]) + tj[J_cfc11]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs30);
-        J[96] = (F.dt*K[K_d90]*nt_cvt<T>(x[30])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs30);
+        J[95] = (F.dt*(K[K_d90]*xt42 + tj[J_cfc11]) + T(1)) * (cs30 * rs30);
+        J[96] = (F.dt*K[K_d90]*xt30) * (cs42 * rs30);
     }
     {  // row 31
     const T rs31 = nt_rscale<T>(nt_exp_hi(x[31]), fh);
-        J[41] = (F.dt*(K[K_d91]*nt_cvt<T>(x[42]) + tj[J_cfc12]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs31);
-        J[42] = (F.dt*K[K_d91]*nt_cvt<T>(x[31])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs31);
+        J[41] = (F.dt*(K[K_d91]*xt42 + tj[J_cfc12]) + T(1)) * (cs31 * rs31);
+        J[42] = (F.dt*K[K_d91]*xt31) * (cs42 * rs31);
     }
     {  // row 32
     const T rs32 = nt_rscale<T>(nt_exp_hi(x[32]), fh);
-        J[18] = (F.dt*(K[K_d92]*nt_cvt<T>(x[42]) + tj[J_cfc113]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs32);
-        J[19] = (F.dt*K[K_d92]*nt_cvt<T>(x[32])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs32);
+        J[18] = (F.dt*(K[K_d92]*xt42 + tj[J_cfc113]) + T(1)) * (cs32 * rs32);
+        J[19] = (F.dt*K[K_d92]*xt32) * (cs42 * rs32);
     }
     {  // row 33
     const T rs33 = nt_rscale<T>(nt_exp_hi(x[33]), fh);
-        J[32] = (F.dt*(K[K_d93]*nt_cvt<T>(x[42]) + tj[J_ccl4]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs33);
-        J[33] = (F.dt*K[K_d93]*nt_cvt<T>(x[33])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs33);
+        J[32] = (F.dt*(K[K_d93]*xt42 + tj[J_ccl4]) + T(1)) * (cs33 * rs33);
+        J[33] = (F.dt*K[K_d93]*xt33) * (cs42 * rs33);
     }
     {  // row 34
     const T rs34 = nt_rscale<T>(nt_exp_hi(x[34]), fh);
-        J[93] = (F.dt*(K[K_d94]*nt_cvt<T>(x[43]) + tj[J_ch3ccl3]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs34);
-        J[94] = (F.dt*K[K_d94]*nt_cvt<T>(x[34])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs34);
+        J[93] = (F.dt*(K[K_d94]*xt43 + tj[J_ch3ccl3]) + T(1)) * (cs34 * rs34);
+        J[94] = (F.dt*K[K_d94]*xt34) * (cs43 * rs34);
     }
     {  // row 35
     const T rs35 = nt_rscale<T>(nt_exp_hi(x[35]), fh);
-        J[66] = (F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs35);
-        J[67] = (F.dt*K[K_d95]*nt_cvt<T>(x[35])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs35);
+        J[66] = (F.dt*(K[K_d95]*xt43 + tj[J_ch3cl]) + T(1)) * (cs35 * rs35);
+        J[67] = (F.dt*K[K_d95]*xt35) * (cs43 * rs35);
     }
     {  // row 36
     const T rs36 = nt_rscale<T>(nt_exp_hi(x[36]), fh);
-        const T dj36_c0 = F.dt*nt_cvt<T>(x[36]);
-        J[38] = (F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs36);
-        J[39] = (K[K_d96]*dj36_c0) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs36);
-        J[40] = (K[K_d97]*dj36_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs36);
+        const T dj36_c0 = F.dt*xt36;
+        J[38] = (F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22]) + T(1)) * (cs36 * rs36);
+        J[39] = (K[K_d96]*dj36_c0) * (cs42 * rs36);
+        J[40] = (K[K_d97]*dj36_c0) * (cs43 * rs36);
     }
     {  // row 37
     const T rs37 = nt_rscale<T>(nt_exp_hi(x[37]), fh);
-        const T dj37_c0 = F.dt*nt_cvt<T>(x[37]);
-        J[52] = (F.dt*(K[K_e50]*nt_cvt<T>(x[42]) + K[K_e51]*nt_cvt<T>(x[43]) + tj[J_ch3br]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[37]), fh) * rs37);
-        J[53] = (K[K_e50]*dj37_c0) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs37);
-        J[54] = (K[K_e51]*dj37_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs37);
+        const T dj37_c0 = F.dt*xt37;
+        J[52] = (F.dt*(K[K_e50]*xt42 + K[K_e51]*xt43 + tj[J_ch3br]) + T(1)) * (cs37 * rs37);
+        J[53] = (K[K_e50]*dj37_c0) * (cs42 * rs37);
+        J[54] = (K[K_e51]*dj37_c0) * (cs43 * rs37);
     }
     {  // row 38
     const T rs38 = nt_rscale<T>(nt_exp_hi(x[38]), fh);
-        J[30] = (F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs38);
-        J[31] = (F.dt*K[K_e52]*nt_cvt<T>(x[38])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs38);
+        J[30] = (F.dt*(K[K_e52]*xt42 + tj[J_h1211]) + T(1)) * (cs38 * rs38);
+        J[31] = (F.dt*K[K_e52]*xt38) * (cs42 * rs38);
     }
     {  // row 39
     const T rs39 = nt_rscale<T>(nt_exp_hi(x[39]), fh);
-        J[50] = (F.dt*(K[K_e53]*nt_cvt<T>(x[42]) + tj[J_h1301]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[39]), fh) * rs39);
-        J[51] = (F.dt*K[K_e53]*nt_cvt<T>(x[39])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs39);
+        J[50] = (F.dt*(K[K_e53]*xt42 + tj[J_h1301]) + T(1)) * (cs39 * rs39);
+        J[51] = (F.dt*K[K_e53]*xt39) * (cs42 * rs39);
     }
     {  // row 40
     const T rs40 = nt_rscale<T>(nt_exp_hi(x[40]), fh);
         const T dj40_c0 = T(2)*K[K_e54];
-        J[16] = (F.dt*F.rain_hbr) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs40);
-        J[13] = (-F.dt*(K[K_e50]*nt_cvt<T>(x[42]) + K[K_e51]*nt_cvt<T>(x[43]) + tj[J_ch3br])) * (nt_scale<T>(nt_exp_hi(x[37]), fh) * rs40);
-        J[11] = (-F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211])) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs40);
-        J[12] = (-F.dt*(K[K_e53]*nt_cvt<T>(x[42]) + tj[J_h1301])) * (nt_scale<T>(nt_exp_hi(x[39]), fh) * rs40);
-        J[15] = (-F.dt*(dj40_c0*nt_cvt<T>(x[43]) + T(2)*tj[J_ch2br2])) * (nt_scale<T>(nt_exp_hi(x[41]), fh) * rs40);
-        J[14] = (-F.dt*(K[K_e50]*nt_cvt<T>(x[37]) + K[K_e52]*nt_cvt<T>(x[38]) + K[K_e53]*nt_cvt<T>(x[39]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs40);
-        J[17] = (-F.dt*(K[K_e51]*nt_cvt<T>(x[37]) + dj40_c0*nt_cvt<T>(x[41]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs40);
+        J[16] = (F.dt*F.rain_hbr) * (cs18 * rs40);
+        J[13] = (-F.dt*(K[K_e50]*xt42 + K[K_e51]*xt43 + tj[J_ch3br])) * (cs37 * rs40);
+        J[11] = (-F.dt*(K[K_e52]*xt42 + tj[J_h1211])) * (cs38 * rs40);
+        J[12] = (-F.dt*(K[K_e53]*xt42 + tj[J_h1301])) * (cs39 * rs40);
+        J[15] = (-F.dt*(dj40_c0*xt43 + T(2)*tj[J_ch2br2])) * (cs41 * rs40);
+        J[14] = (-F.dt*(K[K_e50]*xt37 + K[K_e52]*xt38 + K[K_e53]*xt39)) * (cs42 * rs40);
+        J[17] = (-F.dt*(K[K_e51]*xt37 + dj40_c0*xt41)) * (cs43 * rs40);
     }
     {  // row 41
     const T rs41 = nt_rscale<T>(nt_exp_hi(x[41]), fh);
-        J[125] = (F.dt*(K[K_e54]*nt_cvt<T>(x[43]) + tj[J_ch2br2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[41]), fh) * rs41);
-        J[126] = (F.dt*K[K_e54]*nt_cvt<T>(x[41])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs41);
+        J[125] = (F.dt*(K[K_e54]*xt43 + tj[J_ch2br2]) + T(1)) * (cs41 * rs41);
+        J[126] = (F.dt*K[K_e54]*xt41) * (cs43 * rs41);
     }
     {  // row 42
     const T rs42 = nt_rscale<T>(nt_exp_hi(x[42]), fh);
-        J[99] = (-tj[J_o3_o1d]/(F.n2*K[K_hk4] + F.o2*K[K_hk5])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs42);
+        J[99] = (-tj[J_o3_o1d]/(F.n2*K[K_hk4] + F.o2*K[K_hk5])) * (cs46 * rs42);
     }
     {  // row 56
     const T rs56 = nt_rscale<T>(nt_exp_hi(x[56]), fh);
-        const T dj56_c0 = F.o2*K[K_c4] + K[K_c3]*nt_cvt<T>(x[45]);
+        const T dj56_c0 = F.o2*K[K_c4] + K[K_c3]*xt45;
         const T dj56_c1 = (T(1)/(dj56_c0));
-        const T dj56_c2 = K[K_c1a]*nt_cvt<T>(x[42]) + K[K_c2]*nt_cvt<T>(x[43]) + K[K_d5]*nt_cvt<T>(x[44]);
-        const T dj56_c3 = dj56_c1*nt_cvt<T>(x[1]);
-        J[177] = (-dj56_c1*dj56_c2) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs56);
-        J[176] = (-K[K_c1a]*dj56_c3) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs56);
-        J[180] = (-K[K_c2]*dj56_c3) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs56);
-        J[179] = (-K[K_d5]*dj56_c3) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs56);
-        J[178] = (K[K_c3]*dj56_c2*nt_cvt<T>(x[1])/(dj56_c0*dj56_c0)) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs56);
+        const T dj56_c2 = K[K_c1a]*xt42 + K[K_c2]*xt43 + K[K_d5]*xt44;
+        const T dj56_c3 = dj56_c1*xt1;
+        J[177] = (-dj56_c1*dj56_c2) * (cs1 * rs56);
+        J[176] = (-K[K_c1a]*dj56_c3) * (cs42 * rs56);
+        J[180] = (-K[K_c2]*dj56_c3) * (cs43 * rs56);
+        J[179] = (-K[K_d5]*dj56_c3) * (cs44 * rs56);
+        J[178] = (K[K_c3]*dj56_c2*xt1/(dj56_c0*dj56_c0)) * (cs45 * rs56);
     }
-    const T D_ch3o_c0 = K[K_c1b]*nt_cvt<T>(x[42]);
-    const T D_ch3o_c1 = K[K_c14]*nt_cvt<T>(x[28]);
-    const T D_ch3o_c2 = K[K_c18]*nt_cvt<T>(x[52]) + K[K_c5]*nt_cvt<T>(x[49]);
+    const T D_ch3o_c0 = K[K_c1b]*xt42;
+    const T D_ch3o_c1 = K[K_c14]*xt28;
+    const T D_ch3o_c2 = K[K_c18]*xt52 + K[K_c5]*xt49;
     const T D_ch3o_c3 = T(1)/(F.o2*K[K_c15]);
-    const T D_ch3o_c4 = D_ch3o_c3*nt_cvt<T>(x[28]);
-    const T D_ch3o = D_ch3o_c3*(D_ch3o_c0*nt_cvt<T>(x[1]) + tj[J_ch3o2h]*nt_cvt<T>(x[29]) + nt_cvt<T>(x[28])*(T(2)*D_ch3o_c1 + D_ch3o_c2));
+    const T D_ch3o_c4 = D_ch3o_c3*xt28;
+    const T D_ch3o = D_ch3o_c3*(D_ch3o_c0*xt1 + tj[J_ch3o2h]*xt29 + xt28*(T(2)*D_ch3o_c1 + D_ch3o_c2));
     const T d_D_ch3o_1 = D_ch3o_c0*D_ch3o_c3;
     const T d_D_ch3o_28 = D_ch3o_c3*(T(4)*D_ch3o_c1 + D_ch3o_c2);
     const T d_D_ch3o_29 = D_ch3o_c3*tj[J_ch3o2h];
-    const T d_D_ch3o_42 = D_ch3o_c3*K[K_c1b]*nt_cvt<T>(x[1]);
+    const T d_D_ch3o_42 = D_ch3o_c3*K[K_c1b]*xt1;
     const T d_D_ch3o_49 = D_ch3o_c4*K[K_c5];
     const T d_D_ch3o_52 = D_ch3o_c4*K[K_c18];
     {  // row 27
@@ -584,25 +699,25 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
         const T dj27_c0 = F.dt*K[K_c1c];
         const T dj27_c1 = F.dt*F.o2*K[K_c15];
         const T dj27_c2 = F.dt*K[K_c17b];
-        const T dj27_c3 = F.dt*nt_cvt<T>(x[27]);
+        const T dj27_c3 = F.dt*xt27;
         const T dj27_c4 = F.dt*K[K_c3];
-        J[219] = (-d_D_ch3o_1*dj27_c1 - dj27_c0*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs27);
-        J[222] = (F.dt*(K[K_c10]*nt_cvt<T>(x[44]) + K[K_c19]*nt_cvt<T>(x[50]) + K[K_c8]*nt_cvt<T>(x[43]) + K[K_c9]*nt_cvt<T>(x[45]) + tj[J_ch2o_co] + tj[J_ch2o_hco]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs27);
-        J[221] = (-d_D_ch3o_28*dj27_c1) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs27);
-        J[217] = (-d_D_ch3o_29*dj27_c1 - dj27_c2*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs27);
-        J[218] = (-d_D_ch3o_42*dj27_c1 - dj27_c0*nt_cvt<T>(x[1])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs27);
-        J[226] = (F.dt*K[K_c8]*nt_cvt<T>(x[27]) - dj27_c2*nt_cvt<T>(x[29])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs27);
-        J[224] = (K[K_c10]*dj27_c3) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs27);
-        J[223] = (F.dt*K[K_c9]*nt_cvt<T>(x[27]) - dj27_c4*nt_cvt<T>(x[56])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs27);
-        J[227] = (-d_D_ch3o_49*dj27_c1) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs27);
-        J[225] = (K[K_c19]*dj27_c3) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs27);
-        J[228] = (-d_D_ch3o_52*dj27_c1) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs27);
-        J[220] = (-dj27_c4*nt_cvt<T>(x[45])) * (nt_scale<T>(nt_exp_hi(x[56]), fh) * rs27);
+        J[219] = (-d_D_ch3o_1*dj27_c1 - dj27_c0*xt42) * (cs1 * rs27);
+        J[222] = (F.dt*(K[K_c10]*xt44 + K[K_c19]*xt50 + K[K_c8]*xt43 + K[K_c9]*xt45 + tj[J_ch2o_co] + tj[J_ch2o_hco]) + T(1)) * (cs27 * rs27);
+        J[221] = (-d_D_ch3o_28*dj27_c1) * (cs28 * rs27);
+        J[217] = (-d_D_ch3o_29*dj27_c1 - dj27_c2*xt43) * (cs29 * rs27);
+        J[218] = (-d_D_ch3o_42*dj27_c1 - dj27_c0*xt1) * (cs42 * rs27);
+        J[226] = (F.dt*K[K_c8]*xt27 - dj27_c2*xt29) * (cs43 * rs27);
+        J[224] = (K[K_c10]*dj27_c3) * (cs44 * rs27);
+        J[223] = (F.dt*K[K_c9]*xt27 - dj27_c4*xt56) * (cs45 * rs27);
+        J[227] = (-d_D_ch3o_49*dj27_c1) * (cs49 * rs27);
+        J[225] = (K[K_c19]*dj27_c3) * (cs50 * rs27);
+        J[228] = (-d_D_ch3o_52*dj27_c1) * (cs52 * rs27);
+        J[220] = (-dj27_c4*xt45) * (cs56 * rs27);
     }
     const T D_hco_c0 = T(1)/(F.o2*K[K_c12]);
-    const T D_hco_c1 = D_hco_c0*(K[K_c10]*nt_cvt<T>(x[44]) + K[K_c19]*nt_cvt<T>(x[50]) + K[K_c8]*nt_cvt<T>(x[43]) + K[K_c9]*nt_cvt<T>(x[45]) + tj[J_ch2o_hco]);
-    const T D_hco_c2 = D_hco_c0*nt_cvt<T>(x[27]);
-    const T D_hco = D_hco_c1*nt_cvt<T>(x[27]);
+    const T D_hco_c1 = D_hco_c0*(K[K_c10]*xt44 + K[K_c19]*xt50 + K[K_c8]*xt43 + K[K_c9]*xt45 + tj[J_ch2o_hco]);
+    const T D_hco_c2 = D_hco_c0*xt27;
+    const T D_hco = D_hco_c1*xt27;
     const T d_D_hco_27 = D_hco_c1;
     const T d_D_hco_43 = D_hco_c2*K[K_c8];
     const T d_D_hco_44 = D_hco_c2*K[K_c10];
@@ -611,15 +726,15 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     {  // row 8
     const T rs8 = nt_rscale<T>(nt_exp_hi(x[8]), fh);
         const T dj8_c0 = F.dt*F.o2*K[K_c12];
-        J[160] = (F.dt*K[K_a36]*nt_cvt<T>(x[43]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[8]), fh) * rs8);
-        J[161] = (-F.dt*tj[J_ch2o_co] - d_D_hco_27*dj8_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs8);
-        J[165] = (F.dt*K[K_a36]*nt_cvt<T>(x[8]) - d_D_hco_43*dj8_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs8);
-        J[163] = (-d_D_hco_44*dj8_c0) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs8);
-        J[162] = (-d_D_hco_45*dj8_c0) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs8);
-        J[164] = (-d_D_hco_50*dj8_c0) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs8);
+        J[160] = (F.dt*K[K_a36]*xt43 + T(1)) * (cs8 * rs8);
+        J[161] = (-F.dt*tj[J_ch2o_co] - d_D_hco_27*dj8_c0) * (cs27 * rs8);
+        J[165] = (F.dt*K[K_a36]*xt8 - d_D_hco_43*dj8_c0) * (cs43 * rs8);
+        J[163] = (-d_D_hco_44*dj8_c0) * (cs44 * rs8);
+        J[162] = (-d_D_hco_45*dj8_c0) * (cs45 * rs8);
+        J[164] = (-d_D_hco_50*dj8_c0) * (cs50 * rs8);
     }
     const T D_r1_c0 = T(1)/(F.o2*K[K_hk2]);
-    const T D_r1 = D_r1_c0*(K[K_a2]*nt_cvt<T>(x[55]) + K[K_a6]*nt_cvt<T>(x[43]) + K[K_a6b]*nt_cvt<T>(x[47]) + K[K_b4]*nt_cvt<T>(x[49]) + K[K_d2]*nt_cvt<T>(x[44]) + tj[J_o3_o1d] + tj[J_o3_o3p]);
+    const T D_r1 = D_r1_c0*(K[K_a2]*xt55 + K[K_a6]*xt43 + K[K_a6b]*xt47 + K[K_b4]*xt49 + K[K_d2]*xt44 + tj[J_o3_o1d] + tj[J_o3_o3p]);
     const T d_D_r1_43 = D_r1_c0*K[K_a6];
     const T d_D_r1_44 = D_r1_c0*K[K_d2];
     const T d_D_r1_47 = D_r1_c0*K[K_a6b];
@@ -627,26 +742,26 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     const T d_D_r1_55 = D_r1_c0*K[K_a2];
     {  // row 45
     const T rs45 = nt_rscale<T>(nt_exp_hi(x[45]), fh);
-        J[280] = (-d_D_r1_43*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs45);
-        J[279] = (-d_D_r1_44*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs45);
-        J[282] = (-D_r1) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs45);
-        J[281] = (-d_D_r1_47*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs45);
-        J[283] = (-d_D_r1_49*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs45);
-        J[278] = (-d_D_r1_55*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs45);
+        J[280] = (-d_D_r1_43*xt46) * (cs43 * rs45);
+        J[279] = (-d_D_r1_44*xt46) * (cs44 * rs45);
+        J[282] = (-D_r1) * (cs46 * rs45);
+        J[281] = (-d_D_r1_47*xt46) * (cs47 * rs45);
+        J[283] = (-d_D_r1_49*xt46) * (cs49 * rs45);
+        J[278] = (-d_D_r1_55*xt46) * (cs55 * rs45);
     }
     {  // row 46
     const T rs46 = nt_rscale<T>(nt_exp_hi(x[46]), fh);
         const T dj46_c0 = D_r1 + T(1);
-        const T dj46_c1 = nt_cvt<T>(x[7])/(dj46_c0*dj46_c0);
-        J[355] = (-T(1)/dj46_c0) * (nt_scale<T>(nt_exp_hi(x[7]), fh) * rs46);
-        J[358] = (d_D_r1_43*dj46_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs46);
-        J[357] = (d_D_r1_44*dj46_c1) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs46);
-        J[359] = (d_D_r1_47*dj46_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs46);
-        J[360] = (d_D_r1_49*dj46_c1) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs46);
-        J[356] = (d_D_r1_55*dj46_c1) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs46);
+        const T dj46_c1 = xt7/(dj46_c0*dj46_c0);
+        J[355] = (-T(1)/dj46_c0) * (cs7 * rs46);
+        J[358] = (d_D_r1_43*dj46_c1) * (cs43 * rs46);
+        J[357] = (d_D_r1_44*dj46_c1) * (cs44 * rs46);
+        J[359] = (d_D_r1_47*dj46_c1) * (cs47 * rs46);
+        J[360] = (d_D_r1_49*dj46_c1) * (cs49 * rs46);
+        J[356] = (d_D_r1_55*dj46_c1) * (cs55 * rs46);
     }
-    const T D_r4_c0 = F.h2*K[K_a19] + K[K_a36]*nt_cvt<T>(x[8]) + K[K_a5]*nt_cvt<T>(x[45]);
-    const T D_r4_c1 = F.o2*K[K_a1] + K[K_a2]*nt_cvt<T>(x[46]) + T(8.049999999999999e-11)*nt_cvt<T>(x[47]);
+    const T D_r4_c0 = F.h2*K[K_a19] + K[K_a36]*xt8 + K[K_a5]*xt45;
+    const T D_r4_c1 = F.o2*K[K_a1] + K[K_a2]*xt46 + T(8.049999999999999e-11)*xt47;
     const T D_r4_c2 = (T(1)/(D_r4_c1));
     const T D_r4_c3 = D_r4_c0/(D_r4_c1*D_r4_c1);
     const T D_r4 = D_r4_c0*D_r4_c2;
@@ -656,32 +771,32 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     const T d_D_r4_47 = -T(8.049999999999999e-11)*D_r4_c3;
     {  // row 55
     const T rs55 = nt_rscale<T>(nt_exp_hi(x[55]), fh);
-        J[205] = (-d_D_r4_8*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[8]), fh) * rs55);
-        J[207] = (-D_r4) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs55);
-        J[206] = (-d_D_r4_45*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs55);
-        J[209] = (-d_D_r4_46*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs55);
-        J[208] = (-d_D_r4_47*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs55);
+        J[205] = (-d_D_r4_8*xt43) * (cs8 * rs55);
+        J[207] = (-D_r4) * (cs43 * rs55);
+        J[206] = (-d_D_r4_45*xt43) * (cs45 * rs55);
+        J[209] = (-d_D_r4_46*xt43) * (cs46 * rs55);
+        J[208] = (-d_D_r4_47*xt43) * (cs47 * rs55);
     }
-    const T D_r7_c0 = F.o2*K[K_b7] + K[K_b6]*nt_cvt<T>(x[49]);
+    const T D_r7_c0 = F.o2*K[K_b7] + K[K_b6]*xt49;
     const T D_r7 = tj[J_no]/D_r7_c0;
     const T d_D_r7_49 = -K[K_b6]*tj[J_no]/(D_r7_c0*D_r7_c0);
     {  // row 51
     const T rs51 = nt_rscale<T>(nt_exp_hi(x[51]), fh);
-        J[78] = (-D_r7 - d_D_r7_49*nt_cvt<T>(x[49])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs51);
+        J[78] = (-D_r7 - d_D_r7_49*xt49) * (cs49 * rs51);
     }
-    const T D_r8_c0 = K[K_b12]*nt_cvt<T>(x[48]) + tj[J_no3_no2] + tj[J_no3_no];
+    const T D_r8_c0 = K[K_b12]*xt48 + tj[J_no3_no2] + tj[J_no3_no];
     const T D_r8_c1 = K[K_b9]/D_r8_c0;
-    const T D_r8 = D_r8_c1*nt_cvt<T>(x[46]);
+    const T D_r8 = D_r8_c1*xt46;
     const T d_D_r8_46 = D_r8_c1;
-    const T d_D_r8_48 = -K[K_b12]*K[K_b9]*nt_cvt<T>(x[46])/(D_r8_c0*D_r8_c0);
+    const T d_D_r8_48 = -K[K_b12]*K[K_b9]*xt46/(D_r8_c0*D_r8_c0);
     {  // row 54
     const T rs54 = nt_rscale<T>(nt_exp_hi(x[54]), fh);
         J[68] = T(0);
-        J[70] = (-d_D_r8_46*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs54);
-        J[69] = (-D_r8 - d_D_r8_48*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs54);
+        J[70] = (-d_D_r8_46*xt48) * (cs46 * rs54);
+        J[69] = (-D_r8 - d_D_r8_48*xt48) * (cs48 * rs54);
     }
-    const T D_r5_c0 = D_r8*tj[J_no3_no] + K[K_b3]*nt_cvt<T>(x[45]) + tj[J_no2];
-    const T D_r5_c1 = K[K_a26]*nt_cvt<T>(x[47]) + K[K_b4]*nt_cvt<T>(x[46]) + K[K_c5]*nt_cvt<T>(x[28]) + K[K_d4]*nt_cvt<T>(x[52]) + K[K_e4]*nt_cvt<T>(x[53]);
+    const T D_r5_c0 = D_r8*tj[J_no3_no] + K[K_b3]*xt45 + tj[J_no2];
+    const T D_r5_c1 = K[K_a26]*xt47 + K[K_b4]*xt46 + K[K_c5]*xt28 + K[K_d4]*xt52 + K[K_e4]*xt53;
     const T D_r5_c2 = (T(1)/(D_r5_c1));
     const T D_r5_c3 = D_r5_c0/(D_r5_c1*D_r5_c1);
     const T D_r5 = D_r5_c0*D_r5_c2;
@@ -696,32 +811,32 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     const T rs48 = nt_rscale<T>(nt_exp_hi(x[48]), fh);
         const T dj48_c0 = D_r5*D_r7 + D_r5 + D_r8 + T(1);
         const T dj48_c1 = (T(1)/(dj48_c0*dj48_c0));
-        const T dj48_c2 = dj48_c1*nt_cvt<T>(x[20]);
+        const T dj48_c2 = dj48_c1*xt20;
         const T dj48_c3 = dj48_c2*(-D_r7 + T(-1));
-        J[270] = (-T(1)/dj48_c0) * (nt_scale<T>(nt_exp_hi(x[20]), fh) * rs48);
-        J[269] = (-d_D_r5_28*dj48_c3) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs48);
-        J[272] = (-d_D_r5_45*dj48_c3) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs48);
-        J[275] = (-d_D_r5_46*dj48_c3 + d_D_r8_46*dj48_c1*nt_cvt<T>(x[20])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs48);
-        J[274] = (-d_D_r5_47*dj48_c3) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs48);
-        J[271] = (-d_D_r5_48*dj48_c3 + d_D_r8_48*dj48_c2 + T(1)) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs48);
-        J[276] = (D_r5*d_D_r7_49*dj48_c2) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs48);
-        J[277] = (-d_D_r5_52*dj48_c3) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs48);
-        J[273] = (-d_D_r5_53*dj48_c3) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs48);
+        J[270] = (-T(1)/dj48_c0) * (cs20 * rs48);
+        J[269] = (-d_D_r5_28*dj48_c3) * (cs28 * rs48);
+        J[272] = (-d_D_r5_45*dj48_c3) * (cs45 * rs48);
+        J[275] = (-d_D_r5_46*dj48_c3 + d_D_r8_46*dj48_c1*xt20) * (cs46 * rs48);
+        J[274] = (-d_D_r5_47*dj48_c3) * (cs47 * rs48);
+        J[271] = (-d_D_r5_48*dj48_c3 + d_D_r8_48*dj48_c2 + T(1)) * (cs48 * rs48);
+        J[276] = (D_r5*d_D_r7_49*dj48_c2) * (cs49 * rs48);
+        J[277] = (-d_D_r5_52*dj48_c3) * (cs52 * rs48);
+        J[273] = (-d_D_r5_53*dj48_c3) * (cs53 * rs48);
     }
     {  // row 49
     const T rs49 = nt_rscale<T>(nt_exp_hi(x[49]), fh);
-        J[361] = (-d_D_r5_28*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs49);
-        J[363] = (-d_D_r5_45*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs49);
-        J[366] = (-d_D_r5_46*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs49);
-        J[365] = (-d_D_r5_47*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs49);
-        J[362] = (-D_r5 - d_D_r5_48*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs49);
-        J[367] = (-d_D_r5_52*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs49);
-        J[364] = (-d_D_r5_53*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs49);
+        J[361] = (-d_D_r5_28*xt48) * (cs28 * rs49);
+        J[363] = (-d_D_r5_45*xt48) * (cs45 * rs49);
+        J[366] = (-d_D_r5_46*xt48) * (cs46 * rs49);
+        J[365] = (-d_D_r5_47*xt48) * (cs47 * rs49);
+        J[362] = (-D_r5 - d_D_r5_48*xt48) * (cs48 * rs49);
+        J[367] = (-d_D_r5_52*xt48) * (cs52 * rs49);
+        J[364] = (-d_D_r5_53*xt48) * (cs53 * rs49);
     }
     const T D_r6_c0 = F.o2*K[K_a1];
-    const T D_r6_c1 = D_r4*D_r6_c0 + K[K_a30]*nt_cvt<T>(x[16]) + K[K_a6]*nt_cvt<T>(x[46]) + K[K_c8]*nt_cvt<T>(x[27]) + K[K_d8]*nt_cvt<T>(x[52]) + K[K_e10]*nt_cvt<T>(x[53]);
+    const T D_r6_c1 = D_r4*D_r6_c0 + K[K_a30]*xt16 + K[K_a6]*xt46 + K[K_c8]*xt27 + K[K_d8]*xt52 + K[K_e10]*xt53;
     const T D_r6_c2 = T(2)*K[K_a27];
-    const T D_r6_c3 = D_r6_c2*nt_cvt<T>(x[47]) + K[K_a17]*nt_cvt<T>(x[43]) + K[K_a26]*nt_cvt<T>(x[49]) + K[K_a6b]*nt_cvt<T>(x[46]) + K[K_a7]*nt_cvt<T>(x[45]) + K[K_d10]*nt_cvt<T>(x[44]) + K[K_d33]*nt_cvt<T>(x[52]) + K[K_d7]*nt_cvt<T>(x[44]) + K[K_e15]*nt_cvt<T>(x[53]) + K[K_e7]*nt_cvt<T>(x[50]) + T(8.049999999999999e-11)*nt_cvt<T>(x[55]);
+    const T D_r6_c3 = D_r6_c2*xt47 + K[K_a17]*xt43 + K[K_a26]*xt49 + K[K_a6b]*xt46 + K[K_a7]*xt45 + K[K_d10]*xt44 + K[K_d33]*xt52 + K[K_d7]*xt44 + K[K_e15]*xt53 + K[K_e7]*xt50 + T(8.049999999999999e-11)*xt55;
     const T D_r6_c4 = (T(1)/(D_r6_c3));
     const T D_r6_c5 = D_r6_c0*D_r6_c4;
     const T D_r6_c6 = D_r6_c1/(D_r6_c3*D_r6_c3);
@@ -741,50 +856,50 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     const T d_D_r6_55 = -T(8.049999999999999e-11)*D_r6_c6;
     {  // row 47
     const T rs47 = nt_rscale<T>(nt_exp_hi(x[47]), fh);
-        J[342] = (-d_D_r6_8*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[8]), fh) * rs47);
-        J[343] = (-d_D_r6_16*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs47);
-        J[345] = (-d_D_r6_27*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs47);
-        J[350] = (-D_r6 - d_D_r6_43*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs47);
-        J[347] = (-d_D_r6_44*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs47);
-        J[346] = (-d_D_r6_45*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs47);
-        J[352] = (-d_D_r6_46*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs47);
-        J[351] = (-d_D_r6_47*nt_cvt<T>(x[43]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs47);
-        J[353] = (-d_D_r6_49*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs47);
-        J[349] = (-d_D_r6_50*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs47);
-        J[354] = (-d_D_r6_52*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs47);
-        J[348] = (-d_D_r6_53*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs47);
-        J[344] = (-d_D_r6_55*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs47);
+        J[342] = (-d_D_r6_8*xt43) * (cs8 * rs47);
+        J[343] = (-d_D_r6_16*xt43) * (cs16 * rs47);
+        J[345] = (-d_D_r6_27*xt43) * (cs27 * rs47);
+        J[350] = (-D_r6 - d_D_r6_43*xt43) * (cs43 * rs47);
+        J[347] = (-d_D_r6_44*xt43) * (cs44 * rs47);
+        J[346] = (-d_D_r6_45*xt43) * (cs45 * rs47);
+        J[352] = (-d_D_r6_46*xt43) * (cs46 * rs47);
+        J[351] = (-d_D_r6_47*xt43 + T(1)) * (cs47 * rs47);
+        J[353] = (-d_D_r6_49*xt43) * (cs49 * rs47);
+        J[349] = (-d_D_r6_50*xt43) * (cs50 * rs47);
+        J[354] = (-d_D_r6_52*xt43) * (cs52 * rs47);
+        J[348] = (-d_D_r6_53*xt43) * (cs53 * rs47);
+        J[344] = (-d_D_r6_55*xt43) * (cs55 * rs47);
     }
-    const T D_r13_c0 = K[K_d32]*nt_cvt<T>(x[45]) + het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]) + tj[J_clono2_cl] + tj[J_clono2_clo];
+    const T D_r13_c0 = K[K_d32]*xt45 + het[0]*xt2 + het[1]*xt12 + tj[J_clono2_cl] + tj[J_clono2_clo];
     const T D_r13_c1 = K[K_d31]/D_r13_c0;
-    const T D_r13_c2 = K[K_d31]*nt_cvt<T>(x[48])/(D_r13_c0*D_r13_c0);
-    const T D_r13 = D_r13_c1*nt_cvt<T>(x[48]);
+    const T D_r13_c2 = K[K_d31]*xt48/(D_r13_c0*D_r13_c0);
+    const T D_r13 = D_r13_c1*xt48;
     const T d_D_r13_2 = -D_r13_c2*het[0];
     const T d_D_r13_12 = -D_r13_c2*het[1];
     const T d_D_r13_45 = -D_r13_c2*K[K_d32];
     const T d_D_r13_48 = D_r13_c1;
     const T D_r9_c0 = D_r13*het[0];
-    const T D_r9_c1 = D_r9_c0*nt_cvt<T>(x[2]) + K[K_d33]*nt_cvt<T>(x[47]);
-    const T D_r9_c2 = K[K_d35]*nt_cvt<T>(x[45]) + het[4]*nt_cvt<T>(x[12]) + tj[J_hocl];
+    const T D_r9_c1 = D_r9_c0*xt2 + K[K_d33]*xt47;
+    const T D_r9_c2 = K[K_d35]*xt45 + het[4]*xt12 + tj[J_hocl];
     const T D_r9_c3 = (T(1)/(D_r9_c2));
-    const T D_r9_c4 = D_r9_c3*het[0]*nt_cvt<T>(x[2]);
+    const T D_r9_c4 = D_r9_c3*het[0]*xt2;
     const T D_r9_c5 = D_r9_c1/(D_r9_c2*D_r9_c2);
     const T D_r9 = D_r9_c1*D_r9_c3;
     const T d_D_r9_2 = D_r9_c0*D_r9_c3 + D_r9_c4*d_D_r13_2;
     const T d_D_r9_12 = D_r9_c4*d_D_r13_12 - D_r9_c5*het[4];
-    const T d_D_r9_45 = D_r9_c3*d_D_r13_45*het[0]*nt_cvt<T>(x[2]) - D_r9_c5*K[K_d35];
+    const T d_D_r9_45 = D_r9_c3*d_D_r13_45*het[0]*xt2 - D_r9_c5*K[K_d35];
     const T d_D_r9_47 = D_r9_c3*K[K_d33];
     const T d_D_r9_48 = D_r9_c4*d_D_r13_48;
     const T D_r10_c0 = K[K_d60]/(F.hnm*K[K_d61] + tj[J_cl2o2]);
-    const T D_r10 = D_r10_c0*nt_cvt<T>(x[52]);
+    const T D_r10 = D_r10_c0*xt52;
     const T d_D_r10_52 = D_r10_c0;
     const T D_r12_c0 = K[K_e5c]/tj[J_brcl];
-    const T D_r12 = D_r12_c0*nt_cvt<T>(x[53]);
+    const T D_r12 = D_r12_c0*xt53;
     const T d_D_r12_53 = D_r12_c0;
-    const T D_r11_c0 = K[K_d10]*nt_cvt<T>(x[47]) + K[K_d2]*nt_cvt<T>(x[46]) + K[K_d37]*nt_cvt<T>(x[14]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]);
+    const T D_r11_c0 = K[K_d10]*xt47 + K[K_d2]*xt46 + K[K_d37]*xt14 + K[K_d5]*xt1 + K[K_d7]*xt47;
     const T D_r11_c1 = (T(1)/(D_r11_c0));
     const T D_r11_c2 = T(2)*tj[J_cl2o2];
-    const T D_r11_c3 = D_r10*D_r11_c2 + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*nt_cvt<T>(x[28]) + K[K_d3]*nt_cvt<T>(x[45]) + K[K_d4]*nt_cvt<T>(x[49]) + K[K_d8]*nt_cvt<T>(x[43]) + K[K_e5b]*nt_cvt<T>(x[53]);
+    const T D_r11_c3 = D_r10*D_r11_c2 + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*xt28 + K[K_d3]*xt45 + K[K_d4]*xt49 + K[K_d8]*xt43 + K[K_e5b]*xt53;
     const T D_r11_c4 = D_r11_c3/(D_r11_c0*D_r11_c0);
     const T D_r11_c5 = D_r11_c1*tj[J_clono2_cl];
     const T D_r11_c6 = D_r11_c1*tj[J_hocl];
@@ -804,57 +919,57 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     const T d_D_r11_53 = D_r11_c1*K[K_e5b] + D_r11_c1*d_D_r12_53*tj[J_brcl];
     {  // row 44
     const T rs44 = nt_rscale<T>(nt_exp_hi(x[44]), fh);
-        J[284] = (-d_D_r11_1*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs44);
-        J[288] = (-d_D_r11_2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs44);
-        J[287] = (-d_D_r11_12*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs44);
-        J[285] = (-d_D_r11_14*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs44);
-        J[286] = (-d_D_r11_28*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs44);
-        J[292] = (-d_D_r11_43*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs44);
-        J[290] = (-d_D_r11_45*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs44);
-        J[294] = (-d_D_r11_46*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs44);
-        J[293] = (-d_D_r11_47*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs44);
-        J[289] = (-d_D_r11_48*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs44);
-        J[295] = (-d_D_r11_49*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs44);
-        J[296] = (-D_r11 - d_D_r11_52*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs44);
-        J[291] = (-d_D_r11_53*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs44);
+        J[284] = (-d_D_r11_1*xt52) * (cs1 * rs44);
+        J[288] = (-d_D_r11_2*xt52) * (cs2 * rs44);
+        J[287] = (-d_D_r11_12*xt52) * (cs12 * rs44);
+        J[285] = (-d_D_r11_14*xt52) * (cs14 * rs44);
+        J[286] = (-d_D_r11_28*xt52) * (cs28 * rs44);
+        J[292] = (-d_D_r11_43*xt52) * (cs43 * rs44);
+        J[290] = (-d_D_r11_45*xt52) * (cs45 * rs44);
+        J[294] = (-d_D_r11_46*xt52) * (cs46 * rs44);
+        J[293] = (-d_D_r11_47*xt52) * (cs47 * rs44);
+        J[289] = (-d_D_r11_48*xt52) * (cs48 * rs44);
+        J[295] = (-d_D_r11_49*xt52) * (cs49 * rs44);
+        J[296] = (-D_r11 - d_D_r11_52*xt52) * (cs52 * rs44);
+        J[291] = (-d_D_r11_53*xt52) * (cs53 * rs44);
     }
     {  // row 52
     const T rs52 = nt_rscale<T>(nt_exp_hi(x[52]), fh);
         const T dj52_c0 = D_r11 + T(1);
-        const T dj52_c1 = nt_cvt<T>(x[22])/(dj52_c0*dj52_c0);
-        J[369] = (d_D_r11_1*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs52);
-        J[373] = (d_D_r11_2*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs52);
-        J[372] = (d_D_r11_12*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs52);
-        J[370] = (d_D_r11_14*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs52);
-        J[368] = (-T(1)/dj52_c0) * (nt_scale<T>(nt_exp_hi(x[22]), fh) * rs52);
-        J[371] = (d_D_r11_28*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs52);
-        J[377] = (d_D_r11_43*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs52);
-        J[375] = (d_D_r11_45*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs52);
-        J[379] = (d_D_r11_46*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs52);
-        J[378] = (d_D_r11_47*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs52);
-        J[374] = (d_D_r11_48*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs52);
-        J[380] = (d_D_r11_49*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs52);
-        J[381] = (d_D_r11_52*dj52_c1 + T(1)) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs52);
-        J[376] = (d_D_r11_53*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs52);
+        const T dj52_c1 = xt22/(dj52_c0*dj52_c0);
+        J[369] = (d_D_r11_1*dj52_c1) * (cs1 * rs52);
+        J[373] = (d_D_r11_2*dj52_c1) * (cs2 * rs52);
+        J[372] = (d_D_r11_12*dj52_c1) * (cs12 * rs52);
+        J[370] = (d_D_r11_14*dj52_c1) * (cs14 * rs52);
+        J[368] = (-T(1)/dj52_c0) * (cs22 * rs52);
+        J[371] = (d_D_r11_28*dj52_c1) * (cs28 * rs52);
+        J[377] = (d_D_r11_43*dj52_c1) * (cs43 * rs52);
+        J[375] = (d_D_r11_45*dj52_c1) * (cs45 * rs52);
+        J[379] = (d_D_r11_46*dj52_c1) * (cs46 * rs52);
+        J[378] = (d_D_r11_47*dj52_c1) * (cs47 * rs52);
+        J[374] = (d_D_r11_48*dj52_c1) * (cs48 * rs52);
+        J[380] = (d_D_r11_49*dj52_c1) * (cs49 * rs52);
+        J[381] = (d_D_r11_52*dj52_c1 + T(1)) * (cs52 * rs52);
+        J[376] = (d_D_r11_53*dj52_c1) * (cs53 * rs52);
     }
-    const T D_r27_c0 = K[K_e8]*nt_cvt<T>(x[45]) + tj[J_brono2];
+    const T D_r27_c0 = K[K_e8]*xt45 + tj[J_brono2];
     const T D_r27_c1 = K[K_e13]/D_r27_c0;
-    const T D_r27 = D_r27_c1*nt_cvt<T>(x[48]);
-    const T d_D_r27_45 = -K[K_e13]*K[K_e8]*nt_cvt<T>(x[48])/(D_r27_c0*D_r27_c0);
+    const T D_r27 = D_r27_c1*xt48;
+    const T d_D_r27_45 = -K[K_e13]*K[K_e8]*xt48/(D_r27_c0*D_r27_c0);
     const T d_D_r27_48 = D_r27_c1;
-    const T D_r28_c0 = K[K_e16]*nt_cvt<T>(x[45]) + tj[J_hobr];
+    const T D_r28_c0 = K[K_e16]*xt45 + tj[J_hobr];
     const T D_r28_c1 = K[K_e15]/D_r28_c0;
-    const T D_r28 = D_r28_c1*nt_cvt<T>(x[47]);
-    const T d_D_r28_45 = -K[K_e15]*K[K_e16]*nt_cvt<T>(x[47])/(D_r28_c0*D_r28_c0);
+    const T D_r28 = D_r28_c1*xt47;
+    const T d_D_r28_45 = -K[K_e15]*K[K_e16]*xt47/(D_r28_c0*D_r28_c0);
     const T d_D_r28_47 = D_r28_c1;
     const T D_r29_c0 = K[K_e5c]/tj[J_brcl];
-    const T D_r29 = D_r29_c0*nt_cvt<T>(x[52]);
+    const T D_r29 = D_r29_c0*xt52;
     const T d_D_r29_52 = D_r29_c0;
-    const T D_r30_c0 = K[K_c19]*nt_cvt<T>(x[27]) + K[K_e2]*nt_cvt<T>(x[46]) + K[K_e7]*nt_cvt<T>(x[47]);
+    const T D_r30_c0 = K[K_c19]*xt27 + K[K_e2]*xt46 + K[K_e7]*xt47;
     const T D_r30_c1 = (T(1)/(D_r30_c0));
     const T D_r30_c2 = T(0.85)*tj[J_brono2];
     const T D_r30_c3 = T(2)*K[K_e6];
-    const T D_r30_c4 = D_r27*D_r30_c2 + D_r28*tj[J_hobr] + D_r29*tj[J_brcl] + D_r30_c3*nt_cvt<T>(x[53]) + K[K_e10]*nt_cvt<T>(x[43]) + K[K_e3]*nt_cvt<T>(x[45]) + K[K_e4]*nt_cvt<T>(x[49]) + K[K_e5a]*nt_cvt<T>(x[52]) + K[K_e5b]*nt_cvt<T>(x[52]) + tj[J_bro];
+    const T D_r30_c4 = D_r27*D_r30_c2 + D_r28*tj[J_hobr] + D_r29*tj[J_brcl] + D_r30_c3*xt53 + K[K_e10]*xt43 + K[K_e3]*xt45 + K[K_e4]*xt49 + K[K_e5a]*xt52 + K[K_e5b]*xt52 + tj[J_bro];
     const T D_r30_c5 = D_r30_c4/(D_r30_c0*D_r30_c0);
     const T D_r30_c6 = D_r30_c1*D_r30_c2;
     const T D_r30 = D_r30_c1*D_r30_c4;
@@ -869,30 +984,30 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     const T d_D_r30_53 = D_r30_c1*D_r30_c3;
     {  // row 50
     const T rs50 = nt_rscale<T>(nt_exp_hi(x[50]), fh);
-        J[307] = (-d_D_r30_27*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs50);
-        J[311] = (-d_D_r30_43*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs50);
-        J[309] = (-d_D_r30_45*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs50);
-        J[313] = (-d_D_r30_46*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs50);
-        J[312] = (-d_D_r30_47*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs50);
-        J[308] = (-d_D_r30_48*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs50);
-        J[314] = (-d_D_r30_49*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs50);
-        J[315] = (-d_D_r30_52*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs50);
-        J[310] = (-D_r30 - d_D_r30_53*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs50);
+        J[307] = (-d_D_r30_27*xt53) * (cs27 * rs50);
+        J[311] = (-d_D_r30_43*xt53) * (cs43 * rs50);
+        J[309] = (-d_D_r30_45*xt53) * (cs45 * rs50);
+        J[313] = (-d_D_r30_46*xt53) * (cs46 * rs50);
+        J[312] = (-d_D_r30_47*xt53) * (cs47 * rs50);
+        J[308] = (-d_D_r30_48*xt53) * (cs48 * rs50);
+        J[314] = (-d_D_r30_49*xt53) * (cs49 * rs50);
+        J[315] = (-d_D_r30_52*xt53) * (cs52 * rs50);
+        J[310] = (-D_r30 - d_D_r30_53*xt53) * (cs53 * rs50);
     }
     {  // row 53
     const T rs53 = nt_rscale<T>(nt_exp_hi(x[53]), fh);
         const T dj53_c0 = D_r30 + T(1);
-        const T dj53_c1 = nt_cvt<T>(x[23])/(dj53_c0*dj53_c0);
-        J[297] = (-T(1)/dj53_c0) * (nt_scale<T>(nt_exp_hi(x[23]), fh) * rs53);
-        J[298] = (d_D_r30_27*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs53);
-        J[302] = (d_D_r30_43*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs53);
-        J[300] = (d_D_r30_45*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs53);
-        J[304] = (d_D_r30_46*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs53);
-        J[303] = (d_D_r30_47*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs53);
-        J[299] = (d_D_r30_48*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs53);
-        J[305] = (d_D_r30_49*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs53);
-        J[306] = (d_D_r30_52*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs53);
-        J[301] = (d_D_r30_53*dj53_c1 + T(1)) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs53);
+        const T dj53_c1 = xt23/(dj53_c0*dj53_c0);
+        J[297] = (-T(1)/dj53_c0) * (cs23 * rs53);
+        J[298] = (d_D_r30_27*dj53_c1) * (cs27 * rs53);
+        J[302] = (d_D_r30_43*dj53_c1) * (cs43 * rs53);
+        J[300] = (d_D_r30_45*dj53_c1) * (cs45 * rs53);
+        J[304] = (d_D_r30_46*dj53_c1) * (cs46 * rs53);
+        J[303] = (d_D_r30_47*dj53_c1) * (cs47 * rs53);
+        J[299] = (d_D_r30_48*dj53_c1) * (cs48 * rs53);
+        J[305] = (d_D_r30_49*dj53_c1) * (cs49 * rs53);
+        J[306] = (d_D_r30_52*dj53_c1) * (cs52 * rs53);
+        J[301] = (d_D_r30_53*dj53_c1 + T(1)) * (cs53 * rs53);
     }
     const T D_coea_c0 = D_r6*K[K_a27];
     const T D_coea_c1 = T(1.7e-11)*D_r4 + T(2)*K[K_a17];
@@ -912,17 +1027,17 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     const T d_D_coea_52 = D_coea_c3*d_D_r6_52;
     const T d_D_coea_53 = D_coea_c3*d_D_r6_53;
     const T d_D_coea_55 = D_coea_c3*d_D_r6_55;
-    const T D_coeb_c0 = K[K_b23]*nt_cvt<T>(x[48]);
-    const T D_coeb_c1 = K[K_c7]*nt_cvt<T>(x[28]);
-    const T D_coeb_c2 = K[K_d33]*nt_cvt<T>(x[52]);
-    const T D_coeb_c3 = K[K_d7]*nt_cvt<T>(x[44]);
-    const T D_coeb_c4 = K[K_e15]*nt_cvt<T>(x[53]);
-    const T D_coeb_c5 = K[K_e7]*nt_cvt<T>(x[50]);
+    const T D_coeb_c0 = K[K_b23]*xt48;
+    const T D_coeb_c1 = K[K_c7]*xt28;
+    const T D_coeb_c2 = K[K_d33]*xt52;
+    const T D_coeb_c3 = K[K_d7]*xt44;
+    const T D_coeb_c4 = K[K_e15]*xt53;
+    const T D_coeb_c5 = K[K_e7]*xt50;
     const T D_coeb_c6 = F.parthbr*K[K_e11];
     const T D_coeb_c7 = F.parthcl*K[K_d11];
     const T D_coeb_c8 = F.parthno3*K[K_b27];
     const T D_coeb_c9 = D_coeb_c0 + D_coeb_c1 + D_coeb_c2 + D_coeb_c3 + D_coeb_c4 + D_coeb_c5;
-    const T D_coeb = D_coeb_c0*D_r6 + D_coeb_c1*D_r6 + D_coeb_c2*D_r6 + D_coeb_c3*D_r6 + D_coeb_c4*D_r6 + D_coeb_c5*D_r6 + D_coeb_c6*nt_cvt<T>(x[18]) + D_coeb_c7*nt_cvt<T>(x[12]) + D_coeb_c8*nt_cvt<T>(x[4]) + K[K_b22]*nt_cvt<T>(x[48]) + K[K_b28]*nt_cvt<T>(x[21]) + K[K_c17a]*nt_cvt<T>(x[29]) + K[K_c2]*nt_cvt<T>(x[1]) + K[K_c8]*nt_cvt<T>(x[27]) + K[K_d34]*nt_cvt<T>(x[14]) + K[K_d9]*nt_cvt<T>(x[52]);
+    const T D_coeb = D_coeb_c0*D_r6 + D_coeb_c1*D_r6 + D_coeb_c2*D_r6 + D_coeb_c3*D_r6 + D_coeb_c4*D_r6 + D_coeb_c5*D_r6 + D_coeb_c6*xt18 + D_coeb_c7*xt12 + D_coeb_c8*xt4 + K[K_b22]*xt48 + K[K_b28]*xt21 + K[K_c17a]*xt29 + K[K_c2]*xt1 + K[K_c8]*xt27 + K[K_d34]*xt14 + K[K_d9]*xt52;
     const T d_D_coeb_1 = K[K_c2];
     const T d_D_coeb_4 = D_coeb_c8;
     const T d_D_coeb_8 = D_coeb_c9*d_D_r6_8;
@@ -950,17 +1065,17 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     const T D_coec_c2 = F.o2*K[K_c12];
     const T D_coec_c3 = F.h2*K[K_d6];
     const T D_coec_c4 = F.parthno3*tj[J_hno3];
-    const T D_coec_c5 = K[K_c3]*nt_cvt<T>(x[56]);
-    const T D_coec_c6 = K[K_e16]*nt_cvt<T>(x[45]);
+    const T D_coec_c5 = K[K_c3]*xt56;
+    const T D_coec_c6 = K[K_e16]*xt45;
     const T D_coec_c7 = F.hnm*K[K_b24] + tj[J_hno4];
-    const T D_coec_c8 = K[K_c9]*nt_cvt<T>(x[45]) + tj[J_ch2o_hco];
-    const T D_coec_c9 = K[K_d35]*nt_cvt<T>(x[45]) + K[K_d37]*nt_cvt<T>(x[44]) + tj[J_hocl];
+    const T D_coec_c8 = K[K_c9]*xt45 + tj[J_ch2o_hco];
+    const T D_coec_c9 = K[K_d35]*xt45 + K[K_d37]*xt44 + tj[J_hocl];
     const T D_coec_c10 = K[K_c1a] + K[K_c1b];
-    const T D_coec_c11 = D_coec_c10*nt_cvt<T>(x[1]) + T(2.4e-10)*F.h2;
+    const T D_coec_c11 = D_coec_c10*xt1 + T(2.4e-10)*F.h2;
     const T D_coec_c12 = T(2)*K[K_a1et];
-    const T D_coec_c13 = F.parth2o*(D_coec_c12*nt_cvt<T>(x[42]) + T(2)*tj[J_h2o]);
-    const T D_coec = D_ch3o*D_coec_c1 + D_coec_c0*nt_cvt<T>(x[16]) + D_coec_c11*nt_cvt<T>(x[42]) + D_coec_c13*nt_cvt<T>(x[2]) + D_coec_c2*D_hco + D_coec_c3*nt_cvt<T>(x[44]) + D_coec_c4*nt_cvt<T>(x[4]) + D_coec_c5*nt_cvt<T>(x[45]) + D_coec_c6*nt_cvt<T>(x[25]) + D_coec_c7*nt_cvt<T>(x[21]) + D_coec_c8*nt_cvt<T>(x[27]) + D_coec_c9*nt_cvt<T>(x[14]) + tj[J_ch3o2h]*nt_cvt<T>(x[29]) + tj[J_hbr]*nt_cvt<T>(x[18]) + tj[J_hobr]*nt_cvt<T>(x[25]);
-    const T d_D_coec_1 = D_coec_c1*d_D_ch3o_1 + D_coec_c10*nt_cvt<T>(x[42]);
+    const T D_coec_c13 = F.parth2o*(D_coec_c12*xt42 + T(2)*tj[J_h2o]);
+    const T D_coec = D_ch3o*D_coec_c1 + D_coec_c0*xt16 + D_coec_c11*xt42 + D_coec_c13*xt2 + D_coec_c2*D_hco + D_coec_c3*xt44 + D_coec_c4*xt4 + D_coec_c5*xt45 + D_coec_c6*xt25 + D_coec_c7*xt21 + D_coec_c8*xt27 + D_coec_c9*xt14 + tj[J_ch3o2h]*xt29 + tj[J_hbr]*xt18 + tj[J_hobr]*xt25;
+    const T d_D_coec_1 = D_coec_c1*d_D_ch3o_1 + D_coec_c10*xt42;
     const T d_D_coec_2 = D_coec_c13;
     const T d_D_coec_4 = D_coec_c4;
     const T d_D_coec_14 = D_coec_c9;
@@ -971,14 +1086,14 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     const T d_D_coec_27 = D_coec_c2*d_D_hco_27 + D_coec_c8;
     const T d_D_coec_28 = D_coec_c1*d_D_ch3o_28;
     const T d_D_coec_29 = D_coec_c1*d_D_ch3o_29 + tj[J_ch3o2h];
-    const T d_D_coec_42 = D_coec_c1*d_D_ch3o_42 + D_coec_c11 + D_coec_c12*F.parth2o*nt_cvt<T>(x[2]);
+    const T d_D_coec_42 = D_coec_c1*d_D_ch3o_42 + D_coec_c11 + D_coec_c12*F.parth2o*xt2;
     const T d_D_coec_43 = D_coec_c2*d_D_hco_43;
-    const T d_D_coec_44 = D_coec_c2*d_D_hco_44 + D_coec_c3 + K[K_d37]*nt_cvt<T>(x[14]);
-    const T d_D_coec_45 = D_coec_c2*d_D_hco_45 + D_coec_c5 + K[K_c9]*nt_cvt<T>(x[27]) + K[K_d35]*nt_cvt<T>(x[14]) + K[K_e16]*nt_cvt<T>(x[25]);
+    const T d_D_coec_44 = D_coec_c2*d_D_hco_44 + D_coec_c3 + K[K_d37]*xt14;
+    const T d_D_coec_45 = D_coec_c2*d_D_hco_45 + D_coec_c5 + K[K_c9]*xt27 + K[K_d35]*xt14 + K[K_e16]*xt25;
     const T d_D_coec_49 = D_coec_c1*d_D_ch3o_49;
     const T d_D_coec_50 = D_coec_c2*d_D_hco_50;
     const T d_D_coec_52 = D_coec_c1*d_D_ch3o_52;
-    const T d_D_coec_56 = K[K_c3]*nt_cvt<T>(x[45]);
+    const T d_D_coec_56 = K[K_c3]*xt45;
     const T D_argum_c0 = T(4)*D_coea;
     const T D_argum_c1 = D_argum_c0*D_coec + (D_coeb*D_coeb);
     const T D_argum_c2 = T(2)*D_coeb;
@@ -1018,81 +1133,81 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
         const T dj43_c2 = sqrt(D_argum);
         const T dj43_c3 = (T(0.25))*dj43_c0/dj43_c2;
         const T dj43_c4 = (T(0.5))*(-D_coeb + dj43_c2)/(D_coea*D_coea);
-        J[321] = (-d_D_argum_1*dj43_c3 + d_D_coeb_1*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs43);
-        J[331] = (-d_D_argum_2*dj43_c3) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs43);
-        J[319] = (-d_D_argum_4*dj43_c3 + d_D_coeb_4*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs43);
-        J[322] = (-d_D_argum_8*dj43_c3 + d_D_coea_8*dj43_c4 + d_D_coeb_8*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[8]), fh) * rs43);
-        J[330] = (-d_D_argum_12*dj43_c3 + d_D_coeb_12*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs43);
-        J[323] = (-d_D_argum_14*dj43_c3 + d_D_coeb_14*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs43);
-        J[326] = (-d_D_argum_16*dj43_c3 + d_D_coea_16*dj43_c4 + d_D_coeb_16*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs43);
-        J[325] = (-d_D_argum_18*dj43_c3 + d_D_coeb_18*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs43);
-        J[320] = (-d_D_argum_21*dj43_c3 + d_D_coeb_21*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[21]), fh) * rs43);
-        J[317] = (-d_D_argum_25*dj43_c3) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs43);
-        J[329] = (-d_D_argum_27*dj43_c3 + d_D_coea_27*dj43_c4 + d_D_coeb_27*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs43);
-        J[328] = (-d_D_argum_28*dj43_c3 + d_D_coeb_28*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs43);
-        J[316] = (-d_D_argum_29*dj43_c3 + d_D_coeb_29*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs43);
-        J[318] = (-d_D_argum_42*dj43_c3) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs43);
-        J[337] = (-d_D_argum_43*dj43_c3 + d_D_coea_43*dj43_c4 + d_D_coeb_43*dj43_c1 + T(1)) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs43);
-        J[334] = (-d_D_argum_44*dj43_c3 + d_D_coea_44*dj43_c4 + d_D_coeb_44*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs43);
-        J[333] = (-d_D_argum_45*dj43_c3 + d_D_coea_45*dj43_c4 + d_D_coeb_45*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs43);
-        J[339] = (-d_D_argum_46*dj43_c3 + d_D_coea_46*dj43_c4 + d_D_coeb_46*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs43);
-        J[338] = (-d_D_argum_47*dj43_c3 + d_D_coea_47*dj43_c4 + d_D_coeb_47*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs43);
-        J[332] = (-d_D_argum_48*dj43_c3 + d_D_coeb_48*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs43);
-        J[340] = (-d_D_argum_49*dj43_c3 + d_D_coea_49*dj43_c4 + d_D_coeb_49*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs43);
-        J[336] = (-d_D_argum_50*dj43_c3 + d_D_coea_50*dj43_c4 + d_D_coeb_50*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs43);
-        J[341] = (-d_D_argum_52*dj43_c3 + d_D_coea_52*dj43_c4 + d_D_coeb_52*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs43);
-        J[335] = (-d_D_argum_53*dj43_c3 + d_D_coea_53*dj43_c4 + d_D_coeb_53*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs43);
-        J[327] = (-d_D_argum_55*dj43_c3 + d_D_coea_55*dj43_c4 + d_D_coeb_55*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs43);
-        J[324] = (-d_D_argum_56*dj43_c3) * (nt_scale<T>(nt_exp_hi(x[56]), fh) * rs43);
+        J[321] = (-d_D_argum_1*dj43_c3 + d_D_coeb_1*dj43_c1) * (cs1 * rs43);
+        J[331] = (-d_D_argum_2*dj43_c3) * (cs2 * rs43);
+        J[319] = (-d_D_argum_4*dj43_c3 + d_D_coeb_4*dj43_c1) * (cs4 * rs43);
+        J[322] = (-d_D_argum_8*dj43_c3 + d_D_coea_8*dj43_c4 + d_D_coeb_8*dj43_c1) * (cs8 * rs43);
+        J[330] = (-d_D_argum_12*dj43_c3 + d_D_coeb_12*dj43_c1) * (cs12 * rs43);
+        J[323] = (-d_D_argum_14*dj43_c3 + d_D_coeb_14*dj43_c1) * (cs14 * rs43);
+        J[326] = (-d_D_argum_16*dj43_c3 + d_D_coea_16*dj43_c4 + d_D_coeb_16*dj43_c1) * (cs16 * rs43);
+        J[325] = (-d_D_argum_18*dj43_c3 + d_D_coeb_18*dj43_c1) * (cs18 * rs43);
+        J[320] = (-d_D_argum_21*dj43_c3 + d_D_coeb_21*dj43_c1) * (cs21 * rs43);
+        J[317] = (-d_D_argum_25*dj43_c3) * (cs25 * rs43);
+        J[329] = (-d_D_argum_27*dj43_c3 + d_D_coea_27*dj43_c4 + d_D_coeb_27*dj43_c1) * (cs27 * rs43);
+        J[328] = (-d_D_argum_28*dj43_c3 + d_D_coeb_28*dj43_c1) * (cs28 * rs43);
+        J[316] = (-d_D_argum_29*dj43_c3 + d_D_coeb_29*dj43_c1) * (cs29 * rs43);
+        J[318] = (-d_D_argum_42*dj43_c3) * (cs42 * rs43);
+        J[337] = (-d_D_argum_43*dj43_c3 + d_D_coea_43*dj43_c4 + d_D_coeb_43*dj43_c1 + T(1)) * (cs43 * rs43);
+        J[334] = (-d_D_argum_44*dj43_c3 + d_D_coea_44*dj43_c4 + d_D_coeb_44*dj43_c1) * (cs44 * rs43);
+        J[333] = (-d_D_argum_45*dj43_c3 + d_D_coea_45*dj43_c4 + d_D_coeb_45*dj43_c1) * (cs45 * rs43);
+        J[339] = (-d_D_argum_46*dj43_c3 + d_D_coea_46*dj43_c4 + d_D_coeb_46*dj43_c1) * (cs46 * rs43);
+        J[338] = (-d_D_argum_47*dj43_c3 + d_D_coea_47*dj43_c4 + d_D_coeb_47*dj43_c1) * (cs47 * rs43);
+        J[332] = (-d_D_argum_48*dj43_c3 + d_D_coeb_48*dj43_c1) * (cs48 * rs43);
+        J[340] = (-d_D_argum_49*dj43_c3 + d_D_coea_49*dj43_c4 + d_D_coeb_49*dj43_c1) * (cs49 * rs43);
+        J[336] = (-d_D_argum_50*dj43_c3 + d_D_coea_50*dj43_c4 + d_D_coeb_50*dj43_c1) * (cs50 * rs43);
+        J[341] = (-d_D_argum_52*dj43_c3 + d_D_coea_52*dj43_c4 + d_D_coeb_52*dj43_c1) * (cs52 * rs43);
+        J[335] = (-d_D_argum_53*dj43_c3 + d_D_coea_53*dj43_c4 + d_D_coeb_53*dj43_c1) * (cs53 * rs43);
+        J[327] = (-d_D_argum_55*dj43_c3 + d_D_coea_55*dj43_c4 + d_D_coeb_55*dj43_c1) * (cs55 * rs43);
+        J[324] = (-d_D_argum_56*dj43_c3) * (cs56 * rs43);
     }
-    const T D_t06_c0 = tj[J_hocl]*nt_cvt<T>(x[14]);
-    const T D_t06_c1 = K[K_d33]*nt_cvt<T>(x[52]);
-    const T D_t06_c2 = D_t06_c1*nt_cvt<T>(x[47]);
+    const T D_t06_c0 = tj[J_hocl]*xt14;
+    const T D_t06_c1 = K[K_d33]*xt52;
+    const T D_t06_c2 = D_t06_c1*xt47;
     const bool sel_D_t06 = (D_t06_c0) <= (D_t06_c2);
     const T D_t06 = sel_D_t06 ? T(D_t06_c0) : T(D_t06_c2);
     const T d_D_t06_14 = sel_D_t06 ? T(tj[J_hocl]) : T(T(0));
     const T d_D_t06_47 = sel_D_t06 ? T(T(0)) : T(D_t06_c1);
-    const T d_D_t06_52 = sel_D_t06 ? T(T(0)) : T(K[K_d33]*nt_cvt<T>(x[47]));
-    const T D_t07_c0 = K[K_e5c]*nt_cvt<T>(x[53]);
-    const T D_t07_c1 = D_t07_c0*nt_cvt<T>(x[52]);
-    const T D_t07_c2 = tj[J_brcl]*nt_cvt<T>(x[26]);
+    const T d_D_t06_52 = sel_D_t06 ? T(T(0)) : T(K[K_d33]*xt47);
+    const T D_t07_c0 = K[K_e5c]*xt53;
+    const T D_t07_c1 = D_t07_c0*xt52;
+    const T D_t07_c2 = tj[J_brcl]*xt26;
     const bool sel_D_t07 = (D_t07_c1) <= (D_t07_c2);
     const T D_t07 = sel_D_t07 ? T(D_t07_c1) : T(D_t07_c2);
     const T d_D_t07_26 = sel_D_t07 ? T(T(0)) : T(tj[J_brcl]);
     const T d_D_t07_52 = sel_D_t07 ? T(D_t07_c0) : T(T(0));
-    const T d_D_t07_53 = sel_D_t07 ? T(K[K_e5c]*nt_cvt<T>(x[52])) : T(T(0));
-    const T D_t09_c0 = K[K_e15]*nt_cvt<T>(x[53]);
-    const T D_t09_c1 = D_t09_c0*nt_cvt<T>(x[47]);
-    const T D_t09_c2 = tj[J_hobr]*nt_cvt<T>(x[25]);
+    const T d_D_t07_53 = sel_D_t07 ? T(K[K_e5c]*xt52) : T(T(0));
+    const T D_t09_c0 = K[K_e15]*xt53;
+    const T D_t09_c1 = D_t09_c0*xt47;
+    const T D_t09_c2 = tj[J_hobr]*xt25;
     const bool sel_D_t09 = (D_t09_c1) <= (D_t09_c2);
     const T D_t09 = sel_D_t09 ? T(D_t09_c1) : T(D_t09_c2);
     const T d_D_t09_25 = sel_D_t09 ? T(T(0)) : T(tj[J_hobr]);
     const T d_D_t09_47 = sel_D_t09 ? T(D_t09_c0) : T(T(0));
-    const T d_D_t09_53 = sel_D_t09 ? T(K[K_e15]*nt_cvt<T>(x[47])) : T(T(0));
+    const T d_D_t09_53 = sel_D_t09 ? T(K[K_e15]*xt47) : T(T(0));
     {  // row 7
     const T rs7 = nt_rscale<T>(nt_exp_hi(x[7]), fh);
         const T dj7_c0 = T(2)*F.dt;
         const T dj7_c1 = tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
-        const T dj7_c2 = F.dt*nt_cvt<T>(x[49]);
+        const T dj7_c2 = F.dt*xt49;
         const T dj7_c3 = T(2)*K[K_b3];
         const T dj7_c4 = T(2)*K[K_d3];
         const T dj7_c5 = T(2)*K[K_hk3];
         const T dj7_c6 = T(2)*K[K_b9]*dj7_c1;
         const T dj7_c7 = T(2)*K[K_e5b];
-        J[105] = (dj7_c0*dj7_c1*tj[J_clono2_cl]) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs7);
-        J[106] = (F.dt*d_D_t06_14) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs7);
-        J[104] = (F.dt*d_D_t09_25) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs7);
-        J[103] = (d_D_t07_26*dj7_c0) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs7);
-        J[108] = (-K[K_c5]*dj7_c2) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs7);
-        J[112] = (F.dt*(K[K_a5]*nt_cvt<T>(x[45]) + K[K_a6]*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs7);
-        J[110] = (F.dt*(K[K_a5]*nt_cvt<T>(x[43]) + K[K_a7]*nt_cvt<T>(x[47]) + T(4)*K[K_hk1]*nt_cvt<T>(x[45]) + dj7_c3*nt_cvt<T>(x[48]) + dj7_c4*nt_cvt<T>(x[52]) + dj7_c5*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs7);
-        J[114] = (F.dt*(K[K_a2]*nt_cvt<T>(x[55]) + K[K_a6]*nt_cvt<T>(x[43]) + K[K_a6b]*nt_cvt<T>(x[47]) + dj7_c5*nt_cvt<T>(x[45]) + dj7_c6*nt_cvt<T>(x[48]))) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs7);
-        J[113] = (F.dt*d_D_t06_47 + F.dt*d_D_t09_47 + F.dt*(K[K_a6b]*nt_cvt<T>(x[46]) + K[K_a7]*nt_cvt<T>(x[45])) - K[K_a26]*dj7_c2) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs7);
-        J[109] = (F.dt*(dj7_c3*nt_cvt<T>(x[45]) + dj7_c6*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs7);
-        J[115] = (-F.dt*(K[K_a26]*nt_cvt<T>(x[47]) + K[K_c5]*nt_cvt<T>(x[28]))) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs7);
-        J[116] = (F.dt*d_D_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*nt_cvt<T>(x[52])/(F.hnm*K[K_d61] + tj[J_cl2o2]) + dj7_c4*nt_cvt<T>(x[45]) + dj7_c7*nt_cvt<T>(x[53])) + d_D_t07_52*dj7_c0) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs7);
-        J[111] = (F.dt*d_D_t09_53 + F.dt*(T(4)*K[K_e6]*nt_cvt<T>(x[53]) + dj7_c7*nt_cvt<T>(x[52])) + d_D_t07_53*dj7_c0) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs7);
-        J[107] = (F.dt*K[K_a2]*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs7);
+        J[105] = (dj7_c0*dj7_c1*tj[J_clono2_cl]) * (cs13 * rs7);
+        J[106] = (F.dt*d_D_t06_14) * (cs14 * rs7);
+        J[104] = (F.dt*d_D_t09_25) * (cs25 * rs7);
+        J[103] = (d_D_t07_26*dj7_c0) * (cs26 * rs7);
+        J[108] = (-K[K_c5]*dj7_c2) * (cs28 * rs7);
+        J[112] = (F.dt*(K[K_a5]*xt45 + K[K_a6]*xt46)) * (cs43 * rs7);
+        J[110] = (F.dt*(K[K_a5]*xt43 + K[K_a7]*xt47 + T(4)*K[K_hk1]*xt45 + dj7_c3*xt48 + dj7_c4*xt52 + dj7_c5*xt46)) * (cs45 * rs7);
+        J[114] = (F.dt*(K[K_a2]*xt55 + K[K_a6]*xt43 + K[K_a6b]*xt47 + dj7_c5*xt45 + dj7_c6*xt48)) * (cs46 * rs7);
+        J[113] = (F.dt*d_D_t06_47 + F.dt*d_D_t09_47 + F.dt*(K[K_a6b]*xt46 + K[K_a7]*xt45) - K[K_a26]*dj7_c2) * (cs47 * rs7);
+        J[109] = (F.dt*(dj7_c3*xt45 + dj7_c6*xt46)) * (cs48 * rs7);
+        J[115] = (-F.dt*(K[K_a26]*xt47 + K[K_c5]*xt28)) * (cs49 * rs7);
+        J[116] = (F.dt*d_D_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*xt52/(F.hnm*K[K_d61] + tj[J_cl2o2]) + dj7_c4*xt45 + dj7_c7*xt53) + d_D_t07_52*dj7_c0) * (cs52 * rs7);
+        J[111] = (F.dt*d_D_t09_53 + F.dt*(T(4)*K[K_e6]*xt53 + dj7_c7*xt52) + d_D_t07_53*dj7_c0) * (cs53 * rs7);
+        J[107] = (F.dt*K[K_a2]*xt46) * (cs55 * rs7);
     }
 }
 
@@ -1157,239 +1272,341 @@ __device__ __forceinline__ void nt_residual_day_w2_0(const FF& F, PK K, PK tj, P
 template <typename T, typename FF, typename PK, typename PJ>
 __device__ __forceinline__ void nt_jacobian_day_w2_0(const FF& F, PK K, PK tj, PK het, const double* __restrict__ x, double floor_, PJ J) {
     const int fh = nt_exp_hi(floor_);
+    const T xt0 = nt_cvt<T>(x[0]);
+    const T xt1 = nt_cvt<T>(x[1]);
+    const T xt2 = nt_cvt<T>(x[2]);
+    const T xt3 = nt_cvt<T>(x[3]);
+    const T xt4 = nt_cvt<T>(x[4]);
+    const T xt5 = nt_cvt<T>(x[5]);
+    const T xt6 = nt_cvt<T>(x[6]);
+    const T xt7 = nt_cvt<T>(x[7]);
+    const T xt8 = nt_cvt<T>(x[8]);
+    const T xt9 = nt_cvt<T>(x[9]);
+    const T xt10 = nt_cvt<T>(x[10]);
+    const T xt11 = nt_cvt<T>(x[11]);
+    const T xt12 = nt_cvt<T>(x[12]);
+    const T xt13 = nt_cvt<T>(x[13]);
+    const T xt14 = nt_cvt<T>(x[14]);
+    const T xt15 = nt_cvt<T>(x[15]);
+    const T xt16 = nt_cvt<T>(x[16]);
+    const T xt17 = nt_cvt<T>(x[17]);
+    const T xt18 = nt_cvt<T>(x[18]);
+    const T xt19 = nt_cvt<T>(x[19]);
+    const T xt20 = nt_cvt<T>(x[20]);
+    const T xt21 = nt_cvt<T>(x[21]);
+    const T xt22 = nt_cvt<T>(x[22]);
+    const T xt23 = nt_cvt<T>(x[23]);
+    const T xt24 = nt_cvt<T>(x[24]);
+    const T xt25 = nt_cvt<T>(x[25]);
+    const T xt26 = nt_cvt<T>(x[26]);
+    const T xt27 = nt_cvt<T>(x[27]);
+    const T xt28 = nt_cvt<T>(x[28]);
+    const T xt29 = nt_cvt<T>(x[29]);
+    const T xt30 = nt_cvt<T>(x[30]);
+    const T xt31 = nt_cvt<T>(x[31]);
+    const T xt32 = nt_cvt<T>(x[32]);
+    const T xt33 = nt_cvt<T>(x[33]);
+    const T xt34 = nt_cvt<T>(x[34]);
+    const T xt35 = nt_cvt<T>(x[35]);
+    const T xt36 = nt_cvt<T>(x[36]);
+    const T xt37 = nt_cvt<T>(x[37]);
+    const T xt38 = nt_cvt<T>(x[38]);
+    const T xt39 = nt_cvt<T>(x[39]);
+    const T xt40 = nt_cvt<T>(x[40]);
+    const T xt41 = nt_cvt<T>(x[41]);
+    const T xt42 = nt_cvt<T>(x[42]);
+    const T xt43 = nt_cvt<T>(x[43]);
+    const T xt44 = nt_cvt<T>(x[44]);
+    const T xt45 = nt_cvt<T>(x[45]);
+    const T xt46 = nt_cvt<T>(x[46]);
+    const T xt47 = nt_cvt<T>(x[47]);
+    const T xt48 = nt_cvt<T>(x[48]);
+    const T xt49 = nt_cvt<T>(x[49]);
+    const T xt50 = nt_cvt<T>(x[50]);
+    const T xt51 = nt_cvt<T>(x[51]);
+    const T xt52 = nt_cvt<T>(x[52]);
+    const T xt53 = nt_cvt<T>(x[53]);
+    const T xt54 = nt_cvt<T>(x[54]);
+    const T xt55 = nt_cvt<T>(x[55]);
+    const T xt56 = nt_cvt<T>(x[56]);
+    const T cs1 = nt_scale<T>(nt_exp_hi(x[1]), fh);
+    const T cs2 = nt_scale<T>(nt_exp_hi(x[2]), fh);
+    const T cs4 = nt_scale<T>(nt_exp_hi(x[4]), fh);
+    const T cs5 = nt_scale<T>(nt_exp_hi(x[5]), fh);
+    const T cs8 = nt_scale<T>(nt_exp_hi(x[8]), fh);
+    const T cs9 = nt_scale<T>(nt_exp_hi(x[9]), fh);
+    const T cs12 = nt_scale<T>(nt_exp_hi(x[12]), fh);
+    const T cs13 = nt_scale<T>(nt_exp_hi(x[13]), fh);
+    const T cs14 = nt_scale<T>(nt_exp_hi(x[14]), fh);
+    const T cs15 = nt_scale<T>(nt_exp_hi(x[15]), fh);
+    const T cs16 = nt_scale<T>(nt_exp_hi(x[16]), fh);
+    const T cs17 = nt_scale<T>(nt_exp_hi(x[17]), fh);
+    const T cs18 = nt_scale<T>(nt_exp_hi(x[18]), fh);
+    const T cs19 = nt_scale<T>(nt_exp_hi(x[19]), fh);
+    const T cs21 = nt_scale<T>(nt_exp_hi(x[21]), fh);
+    const T cs24 = nt_scale<T>(nt_exp_hi(x[24]), fh);
+    const T cs25 = nt_scale<T>(nt_exp_hi(x[25]), fh);
+    const T cs26 = nt_scale<T>(nt_exp_hi(x[26]), fh);
+    const T cs27 = nt_scale<T>(nt_exp_hi(x[27]), fh);
+    const T cs28 = nt_scale<T>(nt_exp_hi(x[28]), fh);
+    const T cs29 = nt_scale<T>(nt_exp_hi(x[29]), fh);
+    const T cs30 = nt_scale<T>(nt_exp_hi(x[30]), fh);
+    const T cs31 = nt_scale<T>(nt_exp_hi(x[31]), fh);
+    const T cs32 = nt_scale<T>(nt_exp_hi(x[32]), fh);
+    const T cs33 = nt_scale<T>(nt_exp_hi(x[33]), fh);
+    const T cs34 = nt_scale<T>(nt_exp_hi(x[34]), fh);
+    const T cs35 = nt_scale<T>(nt_exp_hi(x[35]), fh);
+    const T cs36 = nt_scale<T>(nt_exp_hi(x[36]), fh);
+    const T cs37 = nt_scale<T>(nt_exp_hi(x[37]), fh);
+    const T cs38 = nt_scale<T>(nt_exp_hi(x[38]), fh);
+    const T cs41 = nt_scale<T>(nt_exp_hi(x[41]), fh);
+    const T cs42 = nt_scale<T>(nt_exp_hi(x[42]), fh);
+    const T cs43 = nt_scale<T>(nt_exp_hi(x[43]), fh);
+    const T cs44 = nt_scale<T>(nt_exp_hi(x[44]), fh);
+    const T cs45 = nt_scale<T>(nt_exp_hi(x[45]), fh);
+    const T cs46 = nt_scale<T>(nt_exp_hi(x[46]), fh);
+    const T cs47 = nt_scale<T>(nt_exp_hi(x[47]), fh);
+    const T cs48 = nt_scale<T>(nt_exp_hi(x[48]), fh);
+    const T cs49 = nt_scale<T>(nt_exp_hi(x[49]), fh);
+    const T cs50 = nt_scale<T>(nt_exp_hi(x[50]), fh);
+    const T cs52 = nt_scale<T>(nt_exp_hi(x[52]), fh);
+    const T cs53 = nt_scale<T>(nt_exp_hi(x[53]), fh);
+    const T cs54 = nt_scale<T>(nt_exp_hi(x[54]), fh);
+    const T cs55 = nt_scale<T>(nt_exp_hi(x[55]), fh);
+    const T cs56 = nt_scale<T>(nt_exp_hi(x[56]), fh);
     {  // row 2
     const T rs2 = nt_rscale<T>(nt_exp_hi(x[2]), fh);
-        const T dj2_c0 = F.dt*nt_cvt<T>(x[43]);
+        const T dj2_c0 = F.dt*xt43;
         const T dj2_c1 = F.dt*F.parth2o;
         const T dj2_c2 = F.parthno3*K[K_b27];
         const T dj2_c3 = F.parthcl*K[K_d11];
-        J[261] = (-K[K_c2]*dj2_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs2);
-        J[266] = (dj2_c1*(K[K_a1et]*nt_cvt<T>(x[42]) + tj[J_h2o]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs2);
-        J[260] = (-dj2_c0*dj2_c2) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs2);
-        J[265] = (-dj2_c0*dj2_c3) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs2);
-        J[262] = (-K[K_a30]*dj2_c0) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs2);
-        J[264] = (-K[K_c8]*dj2_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs2);
-        J[258] = (-F.dt*(K[K_c17a]*nt_cvt<T>(x[43]) + K[K_c17b]*nt_cvt<T>(x[43]))) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs2);
-        J[259] = (K[K_a1et]*dj2_c1*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs2);
-        J[267] = (-F.dt*(F.h2*K[K_a19] + K[K_a17]*nt_cvt<T>(x[47]) + K[K_a30]*nt_cvt<T>(x[16]) + T(2)*K[K_a31]*nt_cvt<T>(x[43]) + K[K_c17a]*nt_cvt<T>(x[29]) + K[K_c17b]*nt_cvt<T>(x[29]) + K[K_c2]*nt_cvt<T>(x[1]) + K[K_c8]*nt_cvt<T>(x[27]) + dj2_c2*nt_cvt<T>(x[4]) + dj2_c3*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs2);
-        J[268] = (-F.dt*(K[K_a17]*nt_cvt<T>(x[43]) + T(1.6e-12)*nt_cvt<T>(x[55]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs2);
-        J[263] = (-T(1.6e-12)*F.dt*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs2);
+        J[261] = (-K[K_c2]*dj2_c0) * (cs1 * rs2);
+        J[266] = (dj2_c1*(K[K_a1et]*xt42 + tj[J_h2o]) + T(1)) * (cs2 * rs2);
+        J[260] = (-dj2_c0*dj2_c2) * (cs4 * rs2);
+        J[265] = (-dj2_c0*dj2_c3) * (cs12 * rs2);
+        J[262] = (-K[K_a30]*dj2_c0) * (cs16 * rs2);
+        J[264] = (-K[K_c8]*dj2_c0) * (cs27 * rs2);
+        J[258] = (-F.dt*(K[K_c17a]*xt43 + K[K_c17b]*xt43)) * (cs29 * rs2);
+        J[259] = (K[K_a1et]*dj2_c1*xt2) * (cs42 * rs2);
+        J[267] = (-F.dt*(F.h2*K[K_a19] + K[K_a17]*xt47 + K[K_a30]*xt16 + T(2)*K[K_a31]*xt43 + K[K_c17a]*xt29 + K[K_c17b]*xt29 + K[K_c2]*xt1 + K[K_c8]*xt27 + dj2_c2*xt4 + dj2_c3*xt12)) * (cs43 * rs2);
+        J[268] = (-F.dt*(K[K_a17]*xt43 + T(1.6e-12)*xt55)) * (cs47 * rs2);
+        J[263] = (-T(1.6e-12)*F.dt*xt47) * (cs55 * rs2);
     }
     {  // row 4
     const T rs4 = nt_rscale<T>(nt_exp_hi(x[4]), fh);
         const T dj4_c0 = T(2)*het[2];
         const T dj4_c1 = F.dt*K[K_b22];
-        J[122] = (-F.dt*(dj4_c0*nt_cvt<T>(x[5]) + het[0]*nt_cvt<T>(x[13]) + het[5]*nt_cvt<T>(x[19]))) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs4);
-        J[120] = (F.dt*(F.parthno3*(K[K_b27]*nt_cvt<T>(x[43]) + tj[J_hno3]) + F.rain_hno3) + T(1)) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs4);
-        J[118] = (-F.dt*(dj4_c0*nt_cvt<T>(x[2]) + het[3]*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs4);
-        J[121] = (-F.dt*(het[1]*nt_cvt<T>(x[13]) + het[3]*nt_cvt<T>(x[5]))) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs4);
-        J[119] = (-F.dt*(het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs4);
-        J[117] = (-F.dt*het[5]*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs4);
-        J[124] = (F.dt*F.parthno3*K[K_b27]*nt_cvt<T>(x[4]) - dj4_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs4);
-        J[123] = (-dj4_c1*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs4);
+        J[122] = (-F.dt*(dj4_c0*xt5 + het[0]*xt13 + het[5]*xt19)) * (cs2 * rs4);
+        J[120] = (F.dt*(F.parthno3*(K[K_b27]*xt43 + tj[J_hno3]) + F.rain_hno3) + T(1)) * (cs4 * rs4);
+        J[118] = (-F.dt*(dj4_c0*xt2 + het[3]*xt12)) * (cs5 * rs4);
+        J[121] = (-F.dt*(het[1]*xt13 + het[3]*xt5)) * (cs12 * rs4);
+        J[119] = (-F.dt*(het[0]*xt2 + het[1]*xt12)) * (cs13 * rs4);
+        J[117] = (-F.dt*het[5]*xt2) * (cs19 * rs4);
+        J[124] = (F.dt*F.parthno3*K[K_b27]*xt4 - dj4_c1*xt48) * (cs43 * rs4);
+        J[123] = (-dj4_c1*xt43) * (cs48 * rs4);
     }
     {  // row 5
     const T rs5 = nt_rscale<T>(nt_exp_hi(x[5]), fh);
-        const T dj5_c0 = F.dt*nt_cvt<T>(x[5]);
+        const T dj5_c0 = F.dt*xt5;
         const T dj5_c1 = F.dt*K[K_b12];
-        J[74] = (dj5_c0*het[2]) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs5);
-        J[72] = (F.dt*(F.hnm*K[K_b32] + het[2]*nt_cvt<T>(x[2]) + het[3]*nt_cvt<T>(x[12]) + tj[J_n2o5]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs5);
-        J[73] = (dj5_c0*het[3]) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs5);
-        J[75] = (-dj5_c1*nt_cvt<T>(x[54])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs5);
-        J[71] = (-dj5_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[54]), fh) * rs5);
+        J[74] = (dj5_c0*het[2]) * (cs2 * rs5);
+        J[72] = (F.dt*(F.hnm*K[K_b32] + het[2]*xt2 + het[3]*xt12 + tj[J_n2o5]) + T(1)) * (cs5 * rs5);
+        J[73] = (dj5_c0*het[3]) * (cs12 * rs5);
+        J[75] = (-dj5_c1*xt54) * (cs48 * rs5);
+        J[71] = (-dj5_c1*xt48) * (cs54 * rs5);
     }
     {  // row 9
     const T rs9 = nt_rscale<T>(nt_exp_hi(x[9]), fh);
         const T dj9_c0 = F.dt*K[K_e5a];
-        J[100] = (F.dt*tj[J_oclo] + T(1)) * (nt_scale<T>(nt_exp_hi(x[9]), fh) * rs9);
-        J[102] = (-dj9_c0*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs9);
-        J[101] = (-dj9_c0*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs9);
+        J[100] = (F.dt*tj[J_oclo] + T(1)) * (cs9 * rs9);
+        J[102] = (-dj9_c0*xt53) * (cs52 * rs9);
+        J[101] = (-dj9_c0*xt52) * (cs53 * rs9);
     }
     {  // row 12
     const T rs12 = nt_rscale<T>(nt_exp_hi(x[12]), fh);
-        const T dj12_c0 = F.dt*nt_cvt<T>(x[44]);
-        const T dj12_c1 = F.dt*nt_cvt<T>(x[12]);
+        const T dj12_c0 = F.dt*xt44;
+        const T dj12_c1 = F.dt*xt12;
         const T dj12_c2 = F.dt*K[K_d9];
-        J[250] = (-K[K_d5]*dj12_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs12);
-        J[247] = (dj12_c1*het[3]) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs12);
-        J[253] = (F.dt*(F.parthcl*(K[K_d11]*nt_cvt<T>(x[43]) + tj[J_hcl]) + F.rain_hcl + het[1]*nt_cvt<T>(x[13]) + het[3]*nt_cvt<T>(x[5]) + het[4]*nt_cvt<T>(x[14]) + het[6]*nt_cvt<T>(x[25])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs12);
-        J[249] = (dj12_c1*het[1]) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs12);
-        J[251] = (dj12_c1*het[4]) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs12);
-        J[248] = (dj12_c1*het[6]) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs12);
-        J[252] = (-K[K_c10]*dj12_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs12);
-        J[255] = (F.parthcl*K[K_d11]*dj12_c1 - dj12_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs12);
-        J[254] = (-F.dt*(F.h2*K[K_d6] + K[K_c10]*nt_cvt<T>(x[27]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs12);
-        J[256] = (-K[K_d7]*dj12_c0) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs12);
-        J[257] = (-dj12_c2*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs12);
+        J[250] = (-K[K_d5]*dj12_c0) * (cs1 * rs12);
+        J[247] = (dj12_c1*het[3]) * (cs5 * rs12);
+        J[253] = (F.dt*(F.parthcl*(K[K_d11]*xt43 + tj[J_hcl]) + F.rain_hcl + het[1]*xt13 + het[3]*xt5 + het[4]*xt14 + het[6]*xt25) + T(1)) * (cs12 * rs12);
+        J[249] = (dj12_c1*het[1]) * (cs13 * rs12);
+        J[251] = (dj12_c1*het[4]) * (cs14 * rs12);
+        J[248] = (dj12_c1*het[6]) * (cs25 * rs12);
+        J[252] = (-K[K_c10]*dj12_c0) * (cs27 * rs12);
+        J[255] = (F.parthcl*K[K_d11]*dj12_c1 - dj12_c2*xt52) * (cs43 * rs12);
+        J[254] = (-F.dt*(F.h2*K[K_d6] + K[K_c10]*xt27 + K[K_d5]*xt1 + K[K_d7]*xt47)) * (cs44 * rs12);
+        J[256] = (-K[K_d7]*dj12_c0) * (cs47 * rs12);
+        J[257] = (-dj12_c2*xt43) * (cs52 * rs12);
     }
     {  // row 14
     const T rs14 = nt_rscale<T>(nt_exp_hi(x[14]), fh);
         const T dj14_c0 = F.dt*het[0];
-        const T dj14_c1 = F.dt*nt_cvt<T>(x[14]);
+        const T dj14_c1 = F.dt*xt14;
         const T dj14_c2 = F.dt*K[K_d33];
-        J[170] = (-dj14_c0*nt_cvt<T>(x[13])) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs14);
-        J[169] = (dj14_c1*het[4]) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs14);
-        J[166] = (-dj14_c0*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs14);
-        J[167] = (F.dt*(K[K_d34]*nt_cvt<T>(x[43]) + K[K_d35]*nt_cvt<T>(x[45]) + K[K_d37]*nt_cvt<T>(x[44]) + het[4]*nt_cvt<T>(x[12]) + het[8]*nt_cvt<T>(x[18]) + tj[J_hocl]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs14);
-        J[168] = (dj14_c1*het[8]) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs14);
-        J[173] = (K[K_d34]*dj14_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs14);
-        J[172] = (K[K_d37]*dj14_c1) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs14);
-        J[171] = (K[K_d35]*dj14_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs14);
-        J[174] = (-dj14_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs14);
-        J[175] = (-dj14_c2*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs14);
+        J[170] = (-dj14_c0*xt13) * (cs2 * rs14);
+        J[169] = (dj14_c1*het[4]) * (cs12 * rs14);
+        J[166] = (-dj14_c0*xt2) * (cs13 * rs14);
+        J[167] = (F.dt*(K[K_d34]*xt43 + K[K_d35]*xt45 + K[K_d37]*xt44 + het[4]*xt12 + het[8]*xt18 + tj[J_hocl]) + T(1)) * (cs14 * rs14);
+        J[168] = (dj14_c1*het[8]) * (cs18 * rs14);
+        J[173] = (K[K_d34]*dj14_c1) * (cs43 * rs14);
+        J[172] = (K[K_d37]*dj14_c1) * (cs44 * rs14);
+        J[171] = (K[K_d35]*dj14_c1) * (cs45 * rs14);
+        J[174] = (-dj14_c2*xt52) * (cs47 * rs14);
+        J[175] = (-dj14_c2*xt47) * (cs52 * rs14);
     }
     {  // row 15
     const T rs15 = nt_rscale<T>(nt_exp_hi(x[15]), fh);
-        J[63] = (-F.dt*(het[1]*nt_cvt<T>(x[13]) + het[4]*nt_cvt<T>(x[14]))) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs15);
-        J[61] = (-F.dt*het[1]*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs15);
-        J[62] = (-F.dt*(K[K_d37]*nt_cvt<T>(x[44]) + het[4]*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs15);
-        J[60] = (F.dt*tj[J_cl2] + T(1)) * (nt_scale<T>(nt_exp_hi(x[15]), fh) * rs15);
-        J[64] = (-F.dt*K[K_d37]*nt_cvt<T>(x[14])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs15);
-        J[65] = (-T(2)*F.dt*K[K_d62]*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs15);
+        J[63] = (-F.dt*(het[1]*xt13 + het[4]*xt14)) * (cs12 * rs15);
+        J[61] = (-F.dt*het[1]*xt12) * (cs13 * rs15);
+        J[62] = (-F.dt*(K[K_d37]*xt44 + het[4]*xt12)) * (cs14 * rs15);
+        J[60] = (F.dt*tj[J_cl2] + T(1)) * (cs15 * rs15);
+        J[64] = (-F.dt*K[K_d37]*xt14) * (cs44 * rs15);
+        J[65] = (-T(2)*F.dt*K[K_d62]*xt52) * (cs52 * rs15);
     }
     {  // row 16
     const T rs16 = nt_rscale<T>(nt_exp_hi(x[16]), fh);
-        J[189] = (F.dt*(F.rain_h2o2 + K[K_a30]*nt_cvt<T>(x[43]) + tj[J_h2o2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs16);
-        J[190] = (F.dt*K[K_a30]*nt_cvt<T>(x[16])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs16);
-        J[191] = (-T(2)*F.dt*K[K_a27]*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs16);
+        J[189] = (F.dt*(F.rain_h2o2 + K[K_a30]*xt43 + tj[J_h2o2]) + T(1)) * (cs16 * rs16);
+        J[190] = (F.dt*K[K_a30]*xt16) * (cs43 * rs16);
+        J[191] = (-T(2)*F.dt*K[K_a27]*xt47) * (cs47 * rs16);
     }
     {  // row 17
     const T rs17 = nt_rscale<T>(nt_exp_hi(x[17]), fh);
         const T dj17_c0 = F.dt*het[3];
         const T dj17_c1 = F.dt*K[K_d36];
-        J[26] = (-dj17_c0*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs17);
-        J[27] = (-dj17_c0*nt_cvt<T>(x[5])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs17);
-        J[25] = (F.dt*tj[J_clno2] + T(1)) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs17);
-        J[29] = (-dj17_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs17);
-        J[28] = (-dj17_c1*nt_cvt<T>(x[44])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs17);
+        J[26] = (-dj17_c0*xt12) * (cs5 * rs17);
+        J[27] = (-dj17_c0*xt5) * (cs12 * rs17);
+        J[25] = (F.dt*tj[J_clno2] + T(1)) * (cs17 * rs17);
+        J[29] = (-dj17_c1*xt48) * (cs44 * rs17);
+        J[28] = (-dj17_c1*xt44) * (cs48 * rs17);
     }
     {  // row 18
     const T rs18 = nt_rscale<T>(nt_exp_hi(x[18]), fh);
-        const T dj18_c0 = F.dt*nt_cvt<T>(x[18]);
-        const T dj18_c1 = F.dt*nt_cvt<T>(x[50]);
+        const T dj18_c0 = F.dt*xt18;
+        const T dj18_c1 = F.dt*xt50;
         const T dj18_c2 = F.parthbr*dj18_c0;
-        J[183] = (dj18_c0*het[8]) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs18);
-        J[184] = (F.dt*(F.parthbr*(K[K_e11]*nt_cvt<T>(x[43]) + K[K_e9]*nt_cvt<T>(x[42]) + tj[J_hbr]) + F.rain_hbr + het[7]*nt_cvt<T>(x[25]) + het[8]*nt_cvt<T>(x[14])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs18);
-        J[181] = (dj18_c0*het[7]) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs18);
-        J[185] = (-K[K_c19]*dj18_c1) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs18);
-        J[182] = (K[K_e9]*dj18_c2) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs18);
-        J[187] = (K[K_e11]*dj18_c2) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs18);
-        J[188] = (-K[K_e7]*dj18_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs18);
-        J[186] = (-F.dt*(K[K_c19]*nt_cvt<T>(x[27]) + K[K_e7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs18);
+        J[183] = (dj18_c0*het[8]) * (cs14 * rs18);
+        J[184] = (F.dt*(F.parthbr*(K[K_e11]*xt43 + K[K_e9]*xt42 + tj[J_hbr]) + F.rain_hbr + het[7]*xt25 + het[8]*xt14) + T(1)) * (cs18 * rs18);
+        J[181] = (dj18_c0*het[7]) * (cs25 * rs18);
+        J[185] = (-K[K_c19]*dj18_c1) * (cs27 * rs18);
+        J[182] = (K[K_e9]*dj18_c2) * (cs42 * rs18);
+        J[187] = (K[K_e11]*dj18_c2) * (cs43 * rs18);
+        J[188] = (-K[K_e7]*dj18_c1) * (cs47 * rs18);
+        J[186] = (-F.dt*(K[K_c19]*xt27 + K[K_e7]*xt47)) * (cs50 * rs18);
     }
     {  // row 22
     const T rs22 = nt_rscale<T>(nt_exp_hi(x[22]), fh);
-        const T dj22_c0 = F.dt*nt_cvt<T>(x[44]);
-        const T dj22_c1 = T(3)*nt_cvt<T>(x[42]);
+        const T dj22_c0 = F.dt*xt44;
+        const T dj22_c1 = T(3)*xt42;
         const T dj22_c2 = T(2)*K[K_d91];
         const T dj22_c3 = T(4)*K[K_d93];
         const T dj22_c4 = T(3)*K[K_d94];
-        const T dj22_c5 = F.dt*nt_cvt<T>(x[52]);
+        const T dj22_c5 = F.dt*xt52;
         const T dj22_c6 = T(2)*K[K_d60];
         const T dj22_c7 = T(2)*K[K_d62];
-        J[141] = (K[K_d5]*dj22_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs22);
-        J[140] = (-F.dt*tj[J_oclo]) * (nt_scale<T>(nt_exp_hi(x[9]), fh) * rs22);
-        J[144] = (-F.dt*F.parthcl*(K[K_d11]*nt_cvt<T>(x[43]) + tj[J_hcl])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs22);
-        J[135] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + tj[J_clono2_cl] + tj[J_clono2_clo])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs22);
-        J[142] = (-F.dt*(K[K_d34]*nt_cvt<T>(x[43]) + K[K_d35]*nt_cvt<T>(x[45]) + tj[J_hocl]) + K[K_d37]*dj22_c0) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs22);
-        J[133] = (-T(2)*F.dt*tj[J_cl2]) * (nt_scale<T>(nt_exp_hi(x[15]), fh) * rs22);
-        J[128] = (-F.dt*tj[J_clno2]) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs22);
-        J[138] = (-F.dt*(T(2)*F.hnm*K[K_d61] + T(2)*tj[J_cl2o2])) * (nt_scale<T>(nt_exp_hi(x[24]), fh) * rs22);
-        J[132] = (-F.dt*tj[J_brcl]) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs22);
-        J[143] = (K[K_c10]*dj22_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs22);
-        J[137] = (-F.dt*(K[K_d90]*dj22_c1 + T(3)*tj[J_cfc11])) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs22);
-        J[131] = (-F.dt*(dj22_c2*nt_cvt<T>(x[42]) + T(2)*tj[J_cfc12])) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs22);
-        J[127] = (-F.dt*(K[K_d92]*dj22_c1 + T(3)*tj[J_cfc113])) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs22);
-        J[129] = (-F.dt*(dj22_c3*nt_cvt<T>(x[42]) + T(4)*tj[J_ccl4])) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs22);
-        J[136] = (-F.dt*(dj22_c4*nt_cvt<T>(x[43]) + T(3)*tj[J_ch3ccl3])) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs22);
-        J[134] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl])) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs22);
-        J[130] = (-F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22])) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs22);
-        J[139] = (-F.dt*(T(3)*K[K_d90]*nt_cvt<T>(x[30]) + T(3)*K[K_d92]*nt_cvt<T>(x[32]) + K[K_d96]*nt_cvt<T>(x[36]) + dj22_c2*nt_cvt<T>(x[31]) + dj22_c3*nt_cvt<T>(x[33]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs22);
-        J[149] = (-F.dt*(F.parthcl*K[K_d11]*nt_cvt<T>(x[12]) + K[K_d34]*nt_cvt<T>(x[14]) + K[K_d95]*nt_cvt<T>(x[35]) + K[K_d97]*nt_cvt<T>(x[36]) + dj22_c4*nt_cvt<T>(x[34])) + K[K_d9]*dj22_c5) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs22);
-        J[147] = (F.dt*(F.h2*K[K_d6] + K[K_c10]*nt_cvt<T>(x[27]) + K[K_d36]*nt_cvt<T>(x[48]) + K[K_d37]*nt_cvt<T>(x[14]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs22);
-        J[146] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[13]) + K[K_d35]*nt_cvt<T>(x[14]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs22);
-        J[150] = (F.dt*(K[K_d33]*nt_cvt<T>(x[52]) + K[K_d7]*nt_cvt<T>(x[44]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs22);
-        J[145] = (F.dt*(K[K_d31]*nt_cvt<T>(x[52]) + K[K_d36]*nt_cvt<T>(x[44]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs22);
-        J[151] = (F.dt*(K[K_d31]*nt_cvt<T>(x[48]) + K[K_d33]*nt_cvt<T>(x[47]) + K[K_d9]*nt_cvt<T>(x[43]) + K[K_e5a]*nt_cvt<T>(x[53]) + K[K_e5c]*nt_cvt<T>(x[53]) + dj22_c6*nt_cvt<T>(x[52]) + dj22_c7*nt_cvt<T>(x[52]) + nt_cvt<T>(x[52])*(dj22_c6 + dj22_c7))) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs22);
-        J[148] = (dj22_c5*(K[K_e5a] + K[K_e5c])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs22);
+        J[141] = (K[K_d5]*dj22_c0) * (cs1 * rs22);
+        J[140] = (-F.dt*tj[J_oclo]) * (cs9 * rs22);
+        J[144] = (-F.dt*F.parthcl*(K[K_d11]*xt43 + tj[J_hcl])) * (cs12 * rs22);
+        J[135] = (-F.dt*(K[K_d32]*xt45 + tj[J_clono2_cl] + tj[J_clono2_clo])) * (cs13 * rs22);
+        J[142] = (-F.dt*(K[K_d34]*xt43 + K[K_d35]*xt45 + tj[J_hocl]) + K[K_d37]*dj22_c0) * (cs14 * rs22);
+        J[133] = (-T(2)*F.dt*tj[J_cl2]) * (cs15 * rs22);
+        J[128] = (-F.dt*tj[J_clno2]) * (cs17 * rs22);
+        J[138] = (-F.dt*(T(2)*F.hnm*K[K_d61] + T(2)*tj[J_cl2o2])) * (cs24 * rs22);
+        J[132] = (-F.dt*tj[J_brcl]) * (cs26 * rs22);
+        J[143] = (K[K_c10]*dj22_c0) * (cs27 * rs22);
+        J[137] = (-F.dt*(K[K_d90]*dj22_c1 + T(3)*tj[J_cfc11])) * (cs30 * rs22);
+        J[131] = (-F.dt*(dj22_c2*xt42 + T(2)*tj[J_cfc12])) * (cs31 * rs22);
+        J[127] = (-F.dt*(K[K_d92]*dj22_c1 + T(3)*tj[J_cfc113])) * (cs32 * rs22);
+        J[129] = (-F.dt*(dj22_c3*xt42 + T(4)*tj[J_ccl4])) * (cs33 * rs22);
+        J[136] = (-F.dt*(dj22_c4*xt43 + T(3)*tj[J_ch3ccl3])) * (cs34 * rs22);
+        J[134] = (-F.dt*(K[K_d95]*xt43 + tj[J_ch3cl])) * (cs35 * rs22);
+        J[130] = (-F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22])) * (cs36 * rs22);
+        J[139] = (-F.dt*(T(3)*K[K_d90]*xt30 + T(3)*K[K_d92]*xt32 + K[K_d96]*xt36 + dj22_c2*xt31 + dj22_c3*xt33)) * (cs42 * rs22);
+        J[149] = (-F.dt*(F.parthcl*K[K_d11]*xt12 + K[K_d34]*xt14 + K[K_d95]*xt35 + K[K_d97]*xt36 + dj22_c4*xt34) + K[K_d9]*dj22_c5) * (cs43 * rs22);
+        J[147] = (F.dt*(F.h2*K[K_d6] + K[K_c10]*xt27 + K[K_d36]*xt48 + K[K_d37]*xt14 + K[K_d5]*xt1 + K[K_d7]*xt47)) * (cs44 * rs22);
+        J[146] = (-F.dt*(K[K_d32]*xt13 + K[K_d35]*xt14)) * (cs45 * rs22);
+        J[150] = (F.dt*(K[K_d33]*xt52 + K[K_d7]*xt44)) * (cs47 * rs22);
+        J[145] = (F.dt*(K[K_d31]*xt52 + K[K_d36]*xt44)) * (cs48 * rs22);
+        J[151] = (F.dt*(K[K_d31]*xt48 + K[K_d33]*xt47 + K[K_d9]*xt43 + K[K_e5a]*xt53 + K[K_e5c]*xt53 + dj22_c6*xt52 + dj22_c7*xt52 + xt52*(dj22_c6 + dj22_c7))) * (cs52 * rs22);
+        J[148] = (dj22_c5*(K[K_e5a] + K[K_e5c])) * (cs53 * rs22);
     }
     {  // row 25
     const T rs25 = nt_rscale<T>(nt_exp_hi(x[25]), fh);
         const T dj25_c0 = F.dt*het[5];
-        const T dj25_c1 = F.dt*nt_cvt<T>(x[25]);
+        const T dj25_c1 = F.dt*xt25;
         const T dj25_c2 = F.dt*K[K_e15];
-        J[83] = (-dj25_c0*nt_cvt<T>(x[19])) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs25);
-        J[82] = (dj25_c1*het[6]) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs25);
-        J[81] = (dj25_c1*het[7]) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs25);
-        J[79] = (-dj25_c0*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs25);
-        J[80] = (F.dt*(K[K_e16]*nt_cvt<T>(x[45]) + het[6]*nt_cvt<T>(x[12]) + het[7]*nt_cvt<T>(x[18]) + tj[J_hobr]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs25);
-        J[84] = (K[K_e16]*dj25_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs25);
-        J[86] = (-dj25_c2*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs25);
-        J[85] = (-dj25_c2*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs25);
+        J[83] = (-dj25_c0*xt19) * (cs2 * rs25);
+        J[82] = (dj25_c1*het[6]) * (cs12 * rs25);
+        J[81] = (dj25_c1*het[7]) * (cs18 * rs25);
+        J[79] = (-dj25_c0*xt2) * (cs19 * rs25);
+        J[80] = (F.dt*(K[K_e16]*xt45 + het[6]*xt12 + het[7]*xt18 + tj[J_hobr]) + T(1)) * (cs25 * rs25);
+        J[84] = (K[K_e16]*dj25_c1) * (cs45 * rs25);
+        J[86] = (-dj25_c2*xt53) * (cs47 * rs25);
+        J[85] = (-dj25_c2*xt47) * (cs53 * rs25);
     }
     {  // row 26
     const T rs26 = nt_rscale<T>(nt_exp_hi(x[26]), fh);
         const T dj26_c0 = F.dt*het[6];
         const T dj26_c1 = F.dt*het[8];
         const T dj26_c2 = F.dt*K[K_e5c];
-        J[47] = (-dj26_c0*nt_cvt<T>(x[25])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs26);
-        J[45] = (-dj26_c1*nt_cvt<T>(x[18])) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs26);
-        J[46] = (-dj26_c1*nt_cvt<T>(x[14])) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs26);
-        J[44] = (-dj26_c0*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs26);
-        J[43] = (F.dt*tj[J_brcl] + T(1)) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs26);
-        J[49] = (-dj26_c2*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs26);
-        J[48] = (-dj26_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs26);
+        J[47] = (-dj26_c0*xt25) * (cs12 * rs26);
+        J[45] = (-dj26_c1*xt18) * (cs14 * rs26);
+        J[46] = (-dj26_c1*xt14) * (cs18 * rs26);
+        J[44] = (-dj26_c0*xt12) * (cs25 * rs26);
+        J[43] = (F.dt*tj[J_brcl] + T(1)) * (cs26 * rs26);
+        J[49] = (-dj26_c2*xt53) * (cs52 * rs26);
+        J[48] = (-dj26_c2*xt52) * (cs53 * rs26);
     }
     {  // row 29
     const T rs29 = nt_rscale<T>(nt_exp_hi(x[29]), fh);
         const T dj29_c0 = F.dt*K[K_c7];
-        J[35] = (-dj29_c0*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs29);
-        J[34] = (F.dt*(K[K_c17a]*nt_cvt<T>(x[43]) + K[K_c17b]*nt_cvt<T>(x[43]) + tj[J_ch3o2h]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs29);
-        J[36] = (F.dt*nt_cvt<T>(x[29])*(K[K_c17a] + K[K_c17b])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs29);
-        J[37] = (-dj29_c0*nt_cvt<T>(x[28])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs29);
+        J[35] = (-dj29_c0*xt47) * (cs28 * rs29);
+        J[34] = (F.dt*(K[K_c17a]*xt43 + K[K_c17b]*xt43 + tj[J_ch3o2h]) + T(1)) * (cs29 * rs29);
+        J[36] = (F.dt*xt29*(K[K_c17a] + K[K_c17b])) * (cs43 * rs29);
+        J[37] = (-dj29_c0*xt28) * (cs47 * rs29);
     }
     {  // row 30
     const T rs30 = nt_rscale<T>(nt_exp_hi(x[30]), fh);
-        J[95] = (F.dt*(K[K_d90]*nt_cvt<T>(x[42]) + tj[J_cfc11]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs30);
-        J[96] = (F.dt*K[K_d90]*nt_cvt<T>(x[30])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs30);
+        J[95] = (F.dt*(K[K_d90]*xt42 + tj[J_cfc11]) + T(1)) * (cs30 * rs30);
+        J[96] = (F.dt*K[K_d90]*xt30) * (cs42 * rs30);
     }
     {  // row 32
     const T rs32 = nt_rscale<T>(nt_exp_hi(x[32]), fh);
-        J[18] = (F.dt*(K[K_d92]*nt_cvt<T>(x[42]) + tj[J_cfc113]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs32);
-        J[19] = (F.dt*K[K_d92]*nt_cvt<T>(x[32])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs32);
+        J[18] = (F.dt*(K[K_d92]*xt42 + tj[J_cfc113]) + T(1)) * (cs32 * rs32);
+        J[19] = (F.dt*K[K_d92]*xt32) * (cs42 * rs32);
     }
     {  // row 34
     const T rs34 = nt_rscale<T>(nt_exp_hi(x[34]), fh);
-        J[93] = (F.dt*(K[K_d94]*nt_cvt<T>(x[43]) + tj[J_ch3ccl3]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs34);
-        J[94] = (F.dt*K[K_d94]*nt_cvt<T>(x[34])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs34);
+        J[93] = (F.dt*(K[K_d94]*xt43 + tj[J_ch3ccl3]) + T(1)) * (cs34 * rs34);
+        J[94] = (F.dt*K[K_d94]*xt34) * (cs43 * rs34);
     }
     {  // row 37
     const T rs37 = nt_rscale<T>(nt_exp_hi(x[37]), fh);
-        const T dj37_c0 = F.dt*nt_cvt<T>(x[37]);
-        J[52] = (F.dt*(K[K_e50]*nt_cvt<T>(x[42]) + K[K_e51]*nt_cvt<T>(x[43]) + tj[J_ch3br]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[37]), fh) * rs37);
-        J[53] = (K[K_e50]*dj37_c0) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs37);
-        J[54] = (K[K_e51]*dj37_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs37);
+        const T dj37_c0 = F.dt*xt37;
+        J[52] = (F.dt*(K[K_e50]*xt42 + K[K_e51]*xt43 + tj[J_ch3br]) + T(1)) * (cs37 * rs37);
+        J[53] = (K[K_e50]*dj37_c0) * (cs42 * rs37);
+        J[54] = (K[K_e51]*dj37_c0) * (cs43 * rs37);
     }
     {  // row 38
     const T rs38 = nt_rscale<T>(nt_exp_hi(x[38]), fh);
-        J[30] = (F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs38);
-        J[31] = (F.dt*K[K_e52]*nt_cvt<T>(x[38])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs38);
+        J[30] = (F.dt*(K[K_e52]*xt42 + tj[J_h1211]) + T(1)) * (cs38 * rs38);
+        J[31] = (F.dt*K[K_e52]*xt38) * (cs42 * rs38);
     }
     {  // row 41
     const T rs41 = nt_rscale<T>(nt_exp_hi(x[41]), fh);
-        J[125] = (F.dt*(K[K_e54]*nt_cvt<T>(x[43]) + tj[J_ch2br2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[41]), fh) * rs41);
-        J[126] = (F.dt*K[K_e54]*nt_cvt<T>(x[41])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs41);
+        J[125] = (F.dt*(K[K_e54]*xt43 + tj[J_ch2br2]) + T(1)) * (cs41 * rs41);
+        J[126] = (F.dt*K[K_e54]*xt41) * (cs43 * rs41);
     }
-    const T D_ch3o_c0 = K[K_c1b]*nt_cvt<T>(x[42]);
-    const T D_ch3o_c1 = K[K_c14]*nt_cvt<T>(x[28]);
-    const T D_ch3o_c2 = K[K_c18]*nt_cvt<T>(x[52]) + K[K_c5]*nt_cvt<T>(x[49]);
+    const T D_ch3o_c0 = K[K_c1b]*xt42;
+    const T D_ch3o_c1 = K[K_c14]*xt28;
+    const T D_ch3o_c2 = K[K_c18]*xt52 + K[K_c5]*xt49;
     const T D_ch3o_c3 = T(1)/(F.o2*K[K_c15]);
-    const T D_ch3o_c4 = D_ch3o_c3*nt_cvt<T>(x[28]);
-    const T D_ch3o = D_ch3o_c3*(D_ch3o_c0*nt_cvt<T>(x[1]) + tj[J_ch3o2h]*nt_cvt<T>(x[29]) + nt_cvt<T>(x[28])*(T(2)*D_ch3o_c1 + D_ch3o_c2));
+    const T D_ch3o_c4 = D_ch3o_c3*xt28;
+    const T D_ch3o = D_ch3o_c3*(D_ch3o_c0*xt1 + tj[J_ch3o2h]*xt29 + xt28*(T(2)*D_ch3o_c1 + D_ch3o_c2));
     const T d_D_ch3o_1 = D_ch3o_c0*D_ch3o_c3;
     const T d_D_ch3o_28 = D_ch3o_c3*(T(4)*D_ch3o_c1 + D_ch3o_c2);
     const T d_D_ch3o_29 = D_ch3o_c3*tj[J_ch3o2h];
-    const T d_D_ch3o_42 = D_ch3o_c3*K[K_c1b]*nt_cvt<T>(x[1]);
+    const T d_D_ch3o_42 = D_ch3o_c3*K[K_c1b]*xt1;
     const T d_D_ch3o_49 = D_ch3o_c4*K[K_c5];
     const T d_D_ch3o_52 = D_ch3o_c4*K[K_c18];
     {  // row 27
@@ -1397,25 +1614,25 @@ __device__ __forceinline__ void nt_jacobian_day_w2_0(const FF& F, PK K, PK tj, P
         const T dj27_c0 = F.dt*K[K_c1c];
         const T dj27_c1 = F.dt*F.o2*K[K_c15];
         const T dj27_c2 = F.dt*K[K_c17b];
-        const T dj27_c3 = F.dt*nt_cvt<T>(x[27]);
+        const T dj27_c3 = F.dt*xt27;
         const T dj27_c4 = F.dt*K[K_c3];
-        J[219] = (-d_D_ch3o_1*dj27_c1 - dj27_c0*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs27);
-        J[222] = (F.dt*(K[K_c10]*nt_cvt<T>(x[44]) + K[K_c19]*nt_cvt<T>(x[50]) + K[K_c8]*nt_cvt<T>(x[43]) + K[K_c9]*nt_cvt<T>(x[45]) + tj[J_ch2o_co] + tj[J_ch2o_hco]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs27);
-        J[221] = (-d_D_ch3o_28*dj27_c1) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs27);
-        J[217] = (-d_D_ch3o_29*dj27_c1 - dj27_c2*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs27);
-        J[218] = (-d_D_ch3o_42*dj27_c1 - dj27_c0*nt_cvt<T>(x[1])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs27);
-        J[226] = (F.dt*K[K_c8]*nt_cvt<T>(x[27]) - dj27_c2*nt_cvt<T>(x[29])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs27);
-        J[224] = (K[K_c10]*dj27_c3) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs27);
-        J[223] = (F.dt*K[K_c9]*nt_cvt<T>(x[27]) - dj27_c4*nt_cvt<T>(x[56])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs27);
-        J[227] = (-d_D_ch3o_49*dj27_c1) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs27);
-        J[225] = (K[K_c19]*dj27_c3) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs27);
-        J[228] = (-d_D_ch3o_52*dj27_c1) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs27);
-        J[220] = (-dj27_c4*nt_cvt<T>(x[45])) * (nt_scale<T>(nt_exp_hi(x[56]), fh) * rs27);
+        J[219] = (-d_D_ch3o_1*dj27_c1 - dj27_c0*xt42) * (cs1 * rs27);
+        J[222] = (F.dt*(K[K_c10]*xt44 + K[K_c19]*xt50 + K[K_c8]*xt43 + K[K_c9]*xt45 + tj[J_ch2o_co] + tj[J_ch2o_hco]) + T(1)) * (cs27 * rs27);
+        J[221] = (-d_D_ch3o_28*dj27_c1) * (cs28 * rs27);
+        J[217] = (-d_D_ch3o_29*dj27_c1 - dj27_c2*xt43) * (cs29 * rs27);
+        J[218] = (-d_D_ch3o_42*dj27_c1 - dj27_c0*xt1) * (cs42 * rs27);
+        J[226] = (F.dt*K[K_c8]*xt27 - dj27_c2*xt29) * (cs43 * rs27);
+        J[224] = (K[K_c10]*dj27_c3) * (cs44 * rs27);
+        J[223] = (F.dt*K[K_c9]*xt27 - dj27_c4*xt56) * (cs45 * rs27);
+        J[227] = (-d_D_ch3o_49*dj27_c1) * (cs49 * rs27);
+        J[225] = (K[K_c19]*dj27_c3) * (cs50 * rs27);
+        J[228] = (-d_D_ch3o_52*dj27_c1) * (cs52 * rs27);
+        J[220] = (-dj27_c4*xt45) * (cs56 * rs27);
     }
     const T D_hco_c0 = T(1)/(F.o2*K[K_c12]);
-    const T D_hco_c1 = D_hco_c0*(K[K_c10]*nt_cvt<T>(x[44]) + K[K_c19]*nt_cvt<T>(x[50]) + K[K_c8]*nt_cvt<T>(x[43]) + K[K_c9]*nt_cvt<T>(x[45]) + tj[J_ch2o_hco]);
-    const T D_hco_c2 = D_hco_c0*nt_cvt<T>(x[27]);
-    const T D_hco = D_hco_c1*nt_cvt<T>(x[27]);
+    const T D_hco_c1 = D_hco_c0*(K[K_c10]*xt44 + K[K_c19]*xt50 + K[K_c8]*xt43 + K[K_c9]*xt45 + tj[J_ch2o_hco]);
+    const T D_hco_c2 = D_hco_c0*xt27;
+    const T D_hco = D_hco_c1*xt27;
     const T d_D_hco_27 = D_hco_c1;
     const T d_D_hco_43 = D_hco_c2*K[K_c8];
     const T d_D_hco_44 = D_hco_c2*K[K_c10];
@@ -1424,15 +1641,15 @@ __device__ __forceinline__ void nt_jacobian_day_w2_0(const FF& F, PK K, PK tj, P
     {  // row 8
     const T rs8 = nt_rscale<T>(nt_exp_hi(x[8]), fh);
         const T dj8_c0 = F.dt*F.o2*K[K_c12];
-        J[160] = (F.dt*K[K_a36]*nt_cvt<T>(x[43]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[8]), fh) * rs8);
-        J[161] = (-F.dt*tj[J_ch2o_co] - d_D_hco_27*dj8_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs8);
-        J[165] = (F.dt*K[K_a36]*nt_cvt<T>(x[8]) - d_D_hco_43*dj8_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs8);
-        J[163] = (-d_D_hco_44*dj8_c0) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs8);
-        J[162] = (-d_D_hco_45*dj8_c0) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs8);
-        J[164] = (-d_D_hco_50*dj8_c0) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs8);
+        J[160] = (F.dt*K[K_a36]*xt43 + T(1)) * (cs8 * rs8);
+        J[161] = (-F.dt*tj[J_ch2o_co] - d_D_hco_27*dj8_c0) * (cs27 * rs8);
+        J[165] = (F.dt*K[K_a36]*xt8 - d_D_hco_43*dj8_c0) * (cs43 * rs8);
+        J[163] = (-d_D_hco_44*dj8_c0) * (cs44 * rs8);
+        J[162] = (-d_D_hco_45*dj8_c0) * (cs45 * rs8);
+        J[164] = (-d_D_hco_50*dj8_c0) * (cs50 * rs8);
     }
-    const T D_r4_c0 = F.h2*K[K_a19] + K[K_a36]*nt_cvt<T>(x[8]) + K[K_a5]*nt_cvt<T>(x[45]);
-    const T D_r4_c1 = F.o2*K[K_a1] + K[K_a2]*nt_cvt<T>(x[46]) + T(8.049999999999999e-11)*nt_cvt<T>(x[47]);
+    const T D_r4_c0 = F.h2*K[K_a19] + K[K_a36]*xt8 + K[K_a5]*xt45;
+    const T D_r4_c1 = F.o2*K[K_a1] + K[K_a2]*xt46 + T(8.049999999999999e-11)*xt47;
     const T D_r4_c2 = (T(1)/(D_r4_c1));
     const T D_r4_c3 = D_r4_c0/(D_r4_c1*D_r4_c1);
     const T D_r4 = D_r4_c0*D_r4_c2;
@@ -1442,19 +1659,19 @@ __device__ __forceinline__ void nt_jacobian_day_w2_0(const FF& F, PK K, PK tj, P
     const T d_D_r4_47 = -T(8.049999999999999e-11)*D_r4_c3;
     {  // row 55
     const T rs55 = nt_rscale<T>(nt_exp_hi(x[55]), fh);
-        J[205] = (-d_D_r4_8*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[8]), fh) * rs55);
-        J[207] = (-D_r4) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs55);
-        J[206] = (-d_D_r4_45*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs55);
-        J[209] = (-d_D_r4_46*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs55);
-        J[208] = (-d_D_r4_47*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs55);
+        J[205] = (-d_D_r4_8*xt43) * (cs8 * rs55);
+        J[207] = (-D_r4) * (cs43 * rs55);
+        J[206] = (-d_D_r4_45*xt43) * (cs45 * rs55);
+        J[209] = (-d_D_r4_46*xt43) * (cs46 * rs55);
+        J[208] = (-d_D_r4_47*xt43) * (cs47 * rs55);
     }
-    const T D_r8_c0 = K[K_b12]*nt_cvt<T>(x[48]) + tj[J_no3_no2] + tj[J_no3_no];
+    const T D_r8_c0 = K[K_b12]*xt48 + tj[J_no3_no2] + tj[J_no3_no];
     const T D_r8_c1 = K[K_b9]/D_r8_c0;
-    const T D_r8 = D_r8_c1*nt_cvt<T>(x[46]);
+    const T D_r8 = D_r8_c1*xt46;
     const T d_D_r8_46 = D_r8_c1;
-    const T d_D_r8_48 = -K[K_b12]*K[K_b9]*nt_cvt<T>(x[46])/(D_r8_c0*D_r8_c0);
-    const T D_r5_c0 = D_r8*tj[J_no3_no] + K[K_b3]*nt_cvt<T>(x[45]) + tj[J_no2];
-    const T D_r5_c1 = K[K_a26]*nt_cvt<T>(x[47]) + K[K_b4]*nt_cvt<T>(x[46]) + K[K_c5]*nt_cvt<T>(x[28]) + K[K_d4]*nt_cvt<T>(x[52]) + K[K_e4]*nt_cvt<T>(x[53]);
+    const T d_D_r8_48 = -K[K_b12]*K[K_b9]*xt46/(D_r8_c0*D_r8_c0);
+    const T D_r5_c0 = D_r8*tj[J_no3_no] + K[K_b3]*xt45 + tj[J_no2];
+    const T D_r5_c1 = K[K_a26]*xt47 + K[K_b4]*xt46 + K[K_c5]*xt28 + K[K_d4]*xt52 + K[K_e4]*xt53;
     const T D_r5_c2 = (T(1)/(D_r5_c1));
     const T D_r5_c3 = D_r5_c0/(D_r5_c1*D_r5_c1);
     const T D_r5 = D_r5_c0*D_r5_c2;
@@ -1467,18 +1684,18 @@ __device__ __forceinline__ void nt_jacobian_day_w2_0(const FF& F, PK K, PK tj, P
     const T d_D_r5_53 = -D_r5_c3*K[K_e4];
     {  // row 49
     const T rs49 = nt_rscale<T>(nt_exp_hi(x[49]), fh);
-        J[361] = (-d_D_r5_28*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs49);
-        J[363] = (-d_D_r5_45*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs49);
-        J[366] = (-d_D_r5_46*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs49);
-        J[365] = (-d_D_r5_47*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs49);
-        J[362] = (-D_r5 - d_D_r5_48*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs49);
-        J[367] = (-d_D_r5_52*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs49);
-        J[364] = (-d_D_r5_53*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs49);
+        J[361] = (-d_D_r5_28*xt48) * (cs28 * rs49);
+        J[363] = (-d_D_r5_45*xt48) * (cs45 * rs49);
+        J[366] = (-d_D_r5_46*xt48) * (cs46 * rs49);
+        J[365] = (-d_D_r5_47*xt48) * (cs47 * rs49);
+        J[362] = (-D_r5 - d_D_r5_48*xt48) * (cs48 * rs49);
+        J[367] = (-d_D_r5_52*xt48) * (cs52 * rs49);
+        J[364] = (-d_D_r5_53*xt48) * (cs53 * rs49);
     }
     const T D_r6_c0 = F.o2*K[K_a1];
-    const T D_r6_c1 = D_r4*D_r6_c0 + K[K_a30]*nt_cvt<T>(x[16]) + K[K_a6]*nt_cvt<T>(x[46]) + K[K_c8]*nt_cvt<T>(x[27]) + K[K_d8]*nt_cvt<T>(x[52]) + K[K_e10]*nt_cvt<T>(x[53]);
+    const T D_r6_c1 = D_r4*D_r6_c0 + K[K_a30]*xt16 + K[K_a6]*xt46 + K[K_c8]*xt27 + K[K_d8]*xt52 + K[K_e10]*xt53;
     const T D_r6_c2 = T(2)*K[K_a27];
-    const T D_r6_c3 = D_r6_c2*nt_cvt<T>(x[47]) + K[K_a17]*nt_cvt<T>(x[43]) + K[K_a26]*nt_cvt<T>(x[49]) + K[K_a6b]*nt_cvt<T>(x[46]) + K[K_a7]*nt_cvt<T>(x[45]) + K[K_d10]*nt_cvt<T>(x[44]) + K[K_d33]*nt_cvt<T>(x[52]) + K[K_d7]*nt_cvt<T>(x[44]) + K[K_e15]*nt_cvt<T>(x[53]) + K[K_e7]*nt_cvt<T>(x[50]) + T(8.049999999999999e-11)*nt_cvt<T>(x[55]);
+    const T D_r6_c3 = D_r6_c2*xt47 + K[K_a17]*xt43 + K[K_a26]*xt49 + K[K_a6b]*xt46 + K[K_a7]*xt45 + K[K_d10]*xt44 + K[K_d33]*xt52 + K[K_d7]*xt44 + K[K_e15]*xt53 + K[K_e7]*xt50 + T(8.049999999999999e-11)*xt55;
     const T D_r6_c4 = (T(1)/(D_r6_c3));
     const T D_r6_c5 = D_r6_c0*D_r6_c4;
     const T D_r6_c6 = D_r6_c1/(D_r6_c3*D_r6_c3);
@@ -1514,17 +1731,17 @@ __device__ __forceinline__ void nt_jacobian_day_w2_0(const FF& F, PK K, PK tj, P
     const T d_D_coea_52 = D_coea_c3*d_D_r6_52;
     const T d_D_coea_53 = D_coea_c3*d_D_r6_53;
     const T d_D_coea_55 = D_coea_c3*d_D_r6_55;
-    const T D_coeb_c0 = K[K_b23]*nt_cvt<T>(x[48]);
-    const T D_coeb_c1 = K[K_c7]*nt_cvt<T>(x[28]);
-    const T D_coeb_c2 = K[K_d33]*nt_cvt<T>(x[52]);
-    const T D_coeb_c3 = K[K_d7]*nt_cvt<T>(x[44]);
-    const T D_coeb_c4 = K[K_e15]*nt_cvt<T>(x[53]);
-    const T D_coeb_c5 = K[K_e7]*nt_cvt<T>(x[50]);
+    const T D_coeb_c0 = K[K_b23]*xt48;
+    const T D_coeb_c1 = K[K_c7]*xt28;
+    const T D_coeb_c2 = K[K_d33]*xt52;
+    const T D_coeb_c3 = K[K_d7]*xt44;
+    const T D_coeb_c4 = K[K_e15]*xt53;
+    const T D_coeb_c5 = K[K_e7]*xt50;
     const T D_coeb_c6 = F.parthbr*K[K_e11];
     const T D_coeb_c7 = F.parthcl*K[K_d11];
     const T D_coeb_c8 = F.parthno3*K[K_b27];
     const T D_coeb_c9 = D_coeb_c0 + D_coeb_c1 + D_coeb_c2 + D_coeb_c3 + D_coeb_c4 + D_coeb_c5;
-    const T D_coeb = D_coeb_c0*D_r6 + D_coeb_c1*D_r6 + D_coeb_c2*D_r6 + D_coeb_c3*D_r6 + D_coeb_c4*D_r6 + D_coeb_c5*D_r6 + D_coeb_c6*nt_cvt<T>(x[18]) + D_coeb_c7*nt_cvt<T>(x[12]) + D_coeb_c8*nt_cvt<T>(x[4]) + K[K_b22]*nt_cvt<T>(x[48]) + K[K_b28]*nt_cvt<T>(x[21]) + K[K_c17a]*nt_cvt<T>(x[29]) + K[K_c2]*nt_cvt<T>(x[1]) + K[K_c8]*nt_cvt<T>(x[27]) + K[K_d34]*nt_cvt<T>(x[14]) + K[K_d9]*nt_cvt<T>(x[52]);
+    const T D_coeb = D_coeb_c0*D_r6 + D_coeb_c1*D_r6 + D_coeb_c2*D_r6 + D_coeb_c3*D_r6 + D_coeb_c4*D_r6 + D_coeb_c5*D_r6 + D_coeb_c6*xt18 + D_coeb_c7*xt12 + D_coeb_c8*xt4 + K[K_b22]*xt48 + K[K_b28]*xt21 + K[K_c17a]*xt29 + K[K_c2]*xt1 + K[K_c8]*xt27 + K[K_d34]*xt14 + K[K_d9]*xt52;
     const T d_D_coeb_1 = K[K_c2];
     const T d_D_coeb_4 = D_coeb_c8;
     const T d_D_coeb_8 = D_coeb_c9*d_D_r6_8;
@@ -1552,17 +1769,17 @@ __device__ __forceinline__ void nt_jacobian_day_w2_0(const FF& F, PK K, PK tj, P
     const T D_coec_c2 = F.o2*K[K_c12];
     const T D_coec_c3 = F.h2*K[K_d6];
     const T D_coec_c4 = F.parthno3*tj[J_hno3];
-    const T D_coec_c5 = K[K_c3]*nt_cvt<T>(x[56]);
-    const T D_coec_c6 = K[K_e16]*nt_cvt<T>(x[45]);
+    const T D_coec_c5 = K[K_c3]*xt56;
+    const T D_coec_c6 = K[K_e16]*xt45;
     const T D_coec_c7 = F.hnm*K[K_b24] + tj[J_hno4];
-    const T D_coec_c8 = K[K_c9]*nt_cvt<T>(x[45]) + tj[J_ch2o_hco];
-    const T D_coec_c9 = K[K_d35]*nt_cvt<T>(x[45]) + K[K_d37]*nt_cvt<T>(x[44]) + tj[J_hocl];
+    const T D_coec_c8 = K[K_c9]*xt45 + tj[J_ch2o_hco];
+    const T D_coec_c9 = K[K_d35]*xt45 + K[K_d37]*xt44 + tj[J_hocl];
     const T D_coec_c10 = K[K_c1a] + K[K_c1b];
-    const T D_coec_c11 = D_coec_c10*nt_cvt<T>(x[1]) + T(2.4e-10)*F.h2;
+    const T D_coec_c11 = D_coec_c10*xt1 + T(2.4e-10)*F.h2;
     const T D_coec_c12 = T(2)*K[K_a1et];
-    const T D_coec_c13 = F.parth2o*(D_coec_c12*nt_cvt<T>(x[42]) + T(2)*tj[J_h2o]);
-    const T D_coec = D_ch3o*D_coec_c1 + D_coec_c0*nt_cvt<T>(x[16]) + D_coec_c11*nt_cvt<T>(x[42]) + D_coec_c13*nt_cvt<T>(x[2]) + D_coec_c2*D_hco + D_coec_c3*nt_cvt<T>(x[44]) + D_coec_c4*nt_cvt<T>(x[4]) + D_coec_c5*nt_cvt<T>(x[45]) + D_coec_c6*nt_cvt<T>(x[25]) + D_coec_c7*nt_cvt<T>(x[21]) + D_coec_c8*nt_cvt<T>(x[27]) + D_coec_c9*nt_cvt<T>(x[14]) + tj[J_ch3o2h]*nt_cvt<T>(x[29]) + tj[J_hbr]*nt_cvt<T>(x[18]) + tj[J_hobr]*nt_cvt<T>(x[25]);
-    const T d_D_coec_1 = D_coec_c1*d_D_ch3o_1 + D_coec_c10*nt_cvt<T>(x[42]);
+    const T D_coec_c13 = F.parth2o*(D_coec_c12*xt42 + T(2)*tj[J_h2o]);
+    const T D_coec = D_ch3o*D_coec_c1 + D_coec_c0*xt16 + D_coec_c11*xt42 + D_coec_c13*xt2 + D_coec_c2*D_hco + D_coec_c3*xt44 + D_coec_c4*xt4 + D_coec_c5*xt45 + D_coec_c6*xt25 + D_coec_c7*xt21 + D_coec_c8*xt27 + D_coec_c9*xt14 + tj[J_ch3o2h]*xt29 + tj[J_hbr]*xt18 + tj[J_hobr]*xt25;
+    const T d_D_coec_1 = D_coec_c1*d_D_ch3o_1 + D_coec_c10*xt42;
     const T d_D_coec_2 = D_coec_c13;
     const T d_D_coec_4 = D_coec_c4;
     const T d_D_coec_14 = D_coec_c9;
@@ -1573,14 +1790,14 @@ __device__ __forceinline__ void nt_jacobian_day_w2_0(const FF& F, PK K, PK tj, P
     const T d_D_coec_27 = D_coec_c2*d_D_hco_27 + D_coec_c8;
     const T d_D_coec_28 = D_coec_c1*d_D_ch3o_28;
     const T d_D_coec_29 = D_coec_c1*d_D_ch3o_29 + tj[J_ch3o2h];
-    const T d_D_coec_42 = D_coec_c1*d_D_ch3o_42 + D_coec_c11 + D_coec_c12*F.parth2o*nt_cvt<T>(x[2]);
+    const T d_D_coec_42 = D_coec_c1*d_D_ch3o_42 + D_coec_c11 + D_coec_c12*F.parth2o*xt2;
     const T d_D_coec_43 = D_coec_c2*d_D_hco_43;
-    const T d_D_coec_44 = D_coec_c2*d_D_hco_44 + D_coec_c3 + K[K_d37]*nt_cvt<T>(x[14]);
-    const T d_D_coec_45 = D_coec_c2*d_D_hco_45 + D_coec_c5 + K[K_c9]*nt_cvt<T>(x[27]) + K[K_d35]*nt_cvt<T>(x[14]) + K[K_e16]*nt_cvt<T>(x[25]);
+    const T d_D_coec_44 = D_coec_c2*d_D_hco_44 + D_coec_c3 + K[K_d37]*xt14;
+    const T d_D_coec_45 = D_coec_c2*d_D_hco_45 + D_coec_c5 + K[K_c9]*xt27 + K[K_d35]*xt14 + K[K_e16]*xt25;
     const T d_D_coec_49 = D_coec_c1*d_D_ch3o_49;
     const T d_D_coec_50 = D_coec_c2*d_D_hco_50;
     const T d_D_coec_52 = D_coec_c1*d_D_ch3o_52;
-    const T d_D_coec_56 = K[K_c3]*nt_cvt<T>(x[45]);
+    const T d_D_coec_56 = K[K_c3]*xt45;
     const T D_argum_c0 = T(4)*D_coea;
     const T D_argum_c1 = D_argum_c0*D_coec + (D_coeb*D_coeb);
     const T D_argum_c2 = T(2)*D_coeb;
@@ -1620,32 +1837,32 @@ __device__ __forceinline__ void nt_jacobian_day_w2_0(const FF& F, PK K, PK tj, P
         const T dj43_c2 = sqrt(D_argum);
         const T dj43_c3 = (T(0.25))*dj43_c0/dj43_c2;
         const T dj43_c4 = (T(0.5))*(-D_coeb + dj43_c2)/(D_coea*D_coea);
-        J[321] = (-d_D_argum_1*dj43_c3 + d_D_coeb_1*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs43);
-        J[331] = (-d_D_argum_2*dj43_c3) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs43);
-        J[319] = (-d_D_argum_4*dj43_c3 + d_D_coeb_4*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs43);
-        J[322] = (-d_D_argum_8*dj43_c3 + d_D_coea_8*dj43_c4 + d_D_coeb_8*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[8]), fh) * rs43);
-        J[330] = (-d_D_argum_12*dj43_c3 + d_D_coeb_12*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs43);
-        J[323] = (-d_D_argum_14*dj43_c3 + d_D_coeb_14*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs43);
-        J[326] = (-d_D_argum_16*dj43_c3 + d_D_coea_16*dj43_c4 + d_D_coeb_16*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs43);
-        J[325] = (-d_D_argum_18*dj43_c3 + d_D_coeb_18*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs43);
-        J[320] = (-d_D_argum_21*dj43_c3 + d_D_coeb_21*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[21]), fh) * rs43);
-        J[317] = (-d_D_argum_25*dj43_c3) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs43);
-        J[329] = (-d_D_argum_27*dj43_c3 + d_D_coea_27*dj43_c4 + d_D_coeb_27*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs43);
-        J[328] = (-d_D_argum_28*dj43_c3 + d_D_coeb_28*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs43);
-        J[316] = (-d_D_argum_29*dj43_c3 + d_D_coeb_29*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs43);
-        J[318] = (-d_D_argum_42*dj43_c3) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs43);
-        J[337] = (-d_D_argum_43*dj43_c3 + d_D_coea_43*dj43_c4 + d_D_coeb_43*dj43_c1 + T(1)) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs43);
-        J[334] = (-d_D_argum_44*dj43_c3 + d_D_coea_44*dj43_c4 + d_D_coeb_44*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs43);
-        J[333] = (-d_D_argum_45*dj43_c3 + d_D_coea_45*dj43_c4 + d_D_coeb_45*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs43);
-        J[339] = (-d_D_argum_46*dj43_c3 + d_D_coea_46*dj43_c4 + d_D_coeb_46*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs43);
-        J[338] = (-d_D_argum_47*dj43_c3 + d_D_coea_47*dj43_c4 + d_D_coeb_47*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs43);
-        J[332] = (-d_D_argum_48*dj43_c3 + d_D_coeb_48*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs43);
-        J[340] = (-d_D_argum_49*dj43_c3 + d_D_coea_49*dj43_c4 + d_D_coeb_49*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs43);
-        J[336] = (-d_D_argum_50*dj43_c3 + d_D_coea_50*dj43_c4 + d_D_coeb_50*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs43);
-        J[341] = (-d_D_argum_52*dj43_c3 + d_D_coea_52*dj43_c4 + d_D_coeb_52*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs43);
-        J[335] = (-d_D_argum_53*dj43_c3 + d_D_coea_53*dj43_c4 + d_D_coeb_53*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs43);
-        J[327] = (-d_D_argum_55*dj43_c3 + d_D_coea_55*dj43_c4 + d_D_coeb_55*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs43);
-        J[324] = (-d_D_argum_56*dj43_c3) * (nt_scale<T>(nt_exp_hi(x[56]), fh) * rs43);
+        J[321] = (-d_D_argum_1*dj43_c3 + d_D_coeb_1*dj43_c1) * (cs1 * rs43);
+        J[331] = (-d_D_argum_2*dj43_c3) * (cs2 * rs43);
+        J[319] = (-d_D_argum_4*dj43_c3 + d_D_coeb_4*dj43_c1) * (cs4 * rs43);
+        J[322] = (-d_D_argum_8*dj43_c3 + d_D_coea_8*dj43_c4 + d_D_coeb_8*dj43_c1) * (cs8 * rs43);
+        J[330] = (-d_D_argum_12*dj43_c3 + d_D_coeb_12*dj43_c1) * (cs12 * rs43);
+        J[323] = (-d_D_argum_14*dj43_c3 + d_D_coeb_14*dj43_c1) * (cs14 * rs43);
+        J[326] = (-d_D_argum_16*dj43_c3 + d_D_coea_16*dj43_c4 + d_D_coeb_16*dj43_c1) * (cs16 * rs43);
+        J[325] = (-d_D_argum_18*dj43_c3 + d_D_coeb_18*dj43_c1) * (cs18 * rs43);
+        J[320] = (-d_D_argum_21*dj43_c3 + d_D_coeb_21*dj43_c1) * (cs21 * rs43);
+        J[317] = (-d_D_argum_25*dj43_c3) * (cs25 * rs43);
+        J[329] = (-d_D_argum_27*dj43_c3 + d_D_coea_27*dj43_c4 + d_D_coeb_27*dj43_c1) * (cs27 * rs43);
+        J[328] = (-d_D_argum_28*dj43_c3 + d_D_coeb_28*dj43_c1) * (cs28 * rs43);
+        J[316] = (-d_D_argum_29*dj43_c3 + d_D_coeb_29*dj43_c1) * (cs29 * rs43);
+        J[318] = (-d_D_argum_42*dj43_c3) * (cs42 * rs43);
+        J[337] = (-d_D_argum_43*dj43_c3 + d_D_coea_43*dj43_c4 + d_D_coeb_43*dj43_c1 + T(1)) * (cs43 * rs43);
+        J[334] = (-d_D_argum_44*dj43_c3 + d_D_coea_44*dj43_c4 + d_D_coeb_44*dj43_c1) * (cs44 * rs43);
+        J[333] = (-d_D_argum_45*dj43_c3 + d_D_coea_45*dj43_c4 + d_D_coeb_45*dj43_c1) * (cs45 * rs43);
+        J[339] = (-d_D_argum_46*dj43_c3 + d_D_coea_46*dj43_c4 + d_D_coeb_46*dj43_c1) * (cs46 * rs43);
+        J[338] = (-d_D_argum_47*dj43_c3 + d_D_coea_47*dj43_c4 + d_D_coeb_47*dj43_c1) * (cs47 * rs43);
+        J[332] = (-d_D_argum_48*dj43_c3 + d_D_coeb_48*dj43_c1) * (cs48 * rs43);
+        J[340] = (-d_D_argum_49*dj43_c3 + d_D_coea_49*dj43_c4 + d_D_coeb_49*dj43_c1) * (cs49 * rs43);
+        J[336] = (-d_D_argum_50*dj43_c3 + d_D_coea_50*dj43_c4 + d_D_coeb_50*dj43_c1) * (cs50 * rs43);
+        J[341] = (-d_D_argum_52*dj43_c3 + d_D_coea_52*dj43_c4 + d_D_coeb_52*dj43_c1) * (cs52 * rs43);
+        J[335] = (-d_D_argum_53*dj43_c3 + d_D_coea_53*dj43_c4 + d_D_coeb_53*dj43_c1) * (cs53 * rs43);
+        J[327] = (-d_D_argum_55*dj43_c3 + d_D_coea_55*dj43_c4 + d_D_coeb_55*dj43_c1) * (cs55 * rs43);
+        J[324] = (-d_D_argum_56*dj43_c3) * (cs56 * rs43);
     }
 }
 
@@ -1715,198 +1932,305 @@ __device__ __forceinline__ void nt_residual_day_w2_1(const FF& F, PK K, PK tj, P
 template <typename T, typename FF, typename PK, typename PJ>
 __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, PK het, const double* __restrict__ x, double floor_, PJ J) {
     const int fh = nt_exp_hi(floor_);
+    const T xt0 = nt_cvt<T>(x[0]);
+    const T xt1 = nt_cvt<T>(x[1]);
+    const T xt2 = nt_cvt<T>(x[2]);
+    const T xt3 = nt_cvt<T>(x[3]);
+    const T xt4 = nt_cvt<T>(x[4]);
+    const T xt5 = nt_cvt<T>(x[5]);
+    const T xt6 = nt_cvt<T>(x[6]);
+    const T xt7 = nt_cvt<T>(x[7]);
+    const T xt8 = nt_cvt<T>(x[8]);
+    const T xt9 = nt_cvt<T>(x[9]);
+    const T xt10 = nt_cvt<T>(x[10]);
+    const T xt11 = nt_cvt<T>(x[11]);
+    const T xt12 = nt_cvt<T>(x[12]);
+    const T xt13 = nt_cvt<T>(x[13]);
+    const T xt14 = nt_cvt<T>(x[14]);
+    const T xt15 = nt_cvt<T>(x[15]);
+    const T xt16 = nt_cvt<T>(x[16]);
+    const T xt17 = nt_cvt<T>(x[17]);
+    const T xt18 = nt_cvt<T>(x[18]);
+    const T xt19 = nt_cvt<T>(x[19]);
+    const T xt20 = nt_cvt<T>(x[20]);
+    const T xt21 = nt_cvt<T>(x[21]);
+    const T xt22 = nt_cvt<T>(x[22]);
+    const T xt23 = nt_cvt<T>(x[23]);
+    const T xt24 = nt_cvt<T>(x[24]);
+    const T xt25 = nt_cvt<T>(x[25]);
+    const T xt26 = nt_cvt<T>(x[26]);
+    const T xt27 = nt_cvt<T>(x[27]);
+    const T xt28 = nt_cvt<T>(x[28]);
+    const T xt29 = nt_cvt<T>(x[29]);
+    const T xt30 = nt_cvt<T>(x[30]);
+    const T xt31 = nt_cvt<T>(x[31]);
+    const T xt32 = nt_cvt<T>(x[32]);
+    const T xt33 = nt_cvt<T>(x[33]);
+    const T xt34 = nt_cvt<T>(x[34]);
+    const T xt35 = nt_cvt<T>(x[35]);
+    const T xt36 = nt_cvt<T>(x[36]);
+    const T xt37 = nt_cvt<T>(x[37]);
+    const T xt38 = nt_cvt<T>(x[38]);
+    const T xt39 = nt_cvt<T>(x[39]);
+    const T xt40 = nt_cvt<T>(x[40]);
+    const T xt41 = nt_cvt<T>(x[41]);
+    const T xt42 = nt_cvt<T>(x[42]);
+    const T xt43 = nt_cvt<T>(x[43]);
+    const T xt44 = nt_cvt<T>(x[44]);
+    const T xt45 = nt_cvt<T>(x[45]);
+    const T xt46 = nt_cvt<T>(x[46]);
+    const T xt47 = nt_cvt<T>(x[47]);
+    const T xt48 = nt_cvt<T>(x[48]);
+    const T xt49 = nt_cvt<T>(x[49]);
+    const T xt50 = nt_cvt<T>(x[50]);
+    const T xt51 = nt_cvt<T>(x[51]);
+    const T xt52 = nt_cvt<T>(x[52]);
+    const T xt53 = nt_cvt<T>(x[53]);
+    const T xt54 = nt_cvt<T>(x[54]);
+    const T xt55 = nt_cvt<T>(x[55]);
+    const T xt56 = nt_cvt<T>(x[56]);
+    const T cs0 = nt_scale<T>(nt_exp_hi(x[0]), fh);
+    const T cs1 = nt_scale<T>(nt_exp_hi(x[1]), fh);
+    const T cs2 = nt_scale<T>(nt_exp_hi(x[2]), fh);
+    const T cs4 = nt_scale<T>(nt_exp_hi(x[4]), fh);
+    const T cs5 = nt_scale<T>(nt_exp_hi(x[5]), fh);
+    const T cs7 = nt_scale<T>(nt_exp_hi(x[7]), fh);
+    const T cs8 = nt_scale<T>(nt_exp_hi(x[8]), fh);
+    const T cs12 = nt_scale<T>(nt_exp_hi(x[12]), fh);
+    const T cs13 = nt_scale<T>(nt_exp_hi(x[13]), fh);
+    const T cs14 = nt_scale<T>(nt_exp_hi(x[14]), fh);
+    const T cs16 = nt_scale<T>(nt_exp_hi(x[16]), fh);
+    const T cs17 = nt_scale<T>(nt_exp_hi(x[17]), fh);
+    const T cs18 = nt_scale<T>(nt_exp_hi(x[18]), fh);
+    const T cs19 = nt_scale<T>(nt_exp_hi(x[19]), fh);
+    const T cs20 = nt_scale<T>(nt_exp_hi(x[20]), fh);
+    const T cs21 = nt_scale<T>(nt_exp_hi(x[21]), fh);
+    const T cs22 = nt_scale<T>(nt_exp_hi(x[22]), fh);
+    const T cs23 = nt_scale<T>(nt_exp_hi(x[23]), fh);
+    const T cs24 = nt_scale<T>(nt_exp_hi(x[24]), fh);
+    const T cs25 = nt_scale<T>(nt_exp_hi(x[25]), fh);
+    const T cs26 = nt_scale<T>(nt_exp_hi(x[26]), fh);
+    const T cs27 = nt_scale<T>(nt_exp_hi(x[27]), fh);
+    const T cs28 = nt_scale<T>(nt_exp_hi(x[28]), fh);
+    const T cs29 = nt_scale<T>(nt_exp_hi(x[29]), fh);
+    const T cs30 = nt_scale<T>(nt_exp_hi(x[30]), fh);
+    const T cs31 = nt_scale<T>(nt_exp_hi(x[31]), fh);
+    const T cs32 = nt_scale<T>(nt_exp_hi(x[32]), fh);
+    const T cs33 = nt_scale<T>(nt_exp_hi(x[33]), fh);
+    const T cs34 = nt_scale<T>(nt_exp_hi(x[34]), fh);
+    const T cs35 = nt_scale<T>(nt_exp_hi(x[35]), fh);
+    const T cs36 = nt_scale<T>(nt_exp_hi(x[36]), fh);
+    const T cs37 = nt_scale<T>(nt_exp_hi(x[37]), fh);
+    const T cs38 = nt_scale<T>(nt_exp_hi(x[38]), fh);
+    const T cs39 = nt_scale<T>(nt_exp_hi(x[39]), fh);
+    const T cs41 = nt_scale<T>(nt_exp_hi(x[41]), fh);
+    const T cs42 = nt_scale<T>(nt_exp_hi(x[42]), fh);
+    const T cs43 = nt_scale<T>(nt_exp_hi(x[43]), fh);
+    const T cs44 = nt_scale<T>(nt_exp_hi(x[44]), fh);
+    const T cs45 = nt_scale<T>(nt_exp_hi(x[45]), fh);
+    const T cs46 = nt_scale<T>(nt_exp_hi(x[46]), fh);
+    const T cs47 = nt_scale<T>(nt_exp_hi(x[47]), fh);
+    const T cs48 = nt_scale<T>(nt_exp_hi(x[48]), fh);
+    const T cs49 = nt_scale<T>(nt_exp_hi(x[49]), fh);
+    const T cs50 = nt_scale<T>(nt_exp_hi(x[50]), fh);
+    const T cs51 = nt_scale<T>(nt_exp_hi(x[51]), fh);
+    const T cs52 = nt_scale<T>(nt_exp_hi(x[52]), fh);
+    const T cs53 = nt_scale<T>(nt_exp_hi(x[53]), fh);
+    const T cs54 = nt_scale<T>(nt_exp_hi(x[54]), fh);
+    const T cs55 = nt_scale<T>(nt_exp_hi(x[55]), fh);
+    const T cs56 = nt_scale<T>(nt_exp_hi(x[56]), fh);
     {  // row 0
     const T rs0 = nt_rscale<T>(nt_exp_hi(x[0]), fh);
         const T dj0_c0 = K[K_b38] + K[K_b39];
-        J[76] = (F.dt*(dj0_c0*nt_cvt<T>(x[42]) + tj[J_n2o]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs0);
-        J[77] = (F.dt*dj0_c0*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs0);
+        J[76] = (F.dt*(dj0_c0*xt42 + tj[J_n2o]) + T(1)) * (cs0 * rs0);
+        J[77] = (F.dt*dj0_c0*xt0) * (cs42 * rs0);
     }
     {  // row 1
     const T rs1 = nt_rscale<T>(nt_exp_hi(x[1]), fh);
-        const T dj1_c0 = F.dt*nt_cvt<T>(x[1]);
-        J[157] = (F.dt*(K[K_c1a]*nt_cvt<T>(x[42]) + K[K_c1b]*nt_cvt<T>(x[42]) + K[K_c1c]*nt_cvt<T>(x[42]) + K[K_c2]*nt_cvt<T>(x[43]) + K[K_d5]*nt_cvt<T>(x[44])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs1);
-        J[156] = (dj1_c0*(K[K_c1a] + K[K_c1b] + K[K_c1c])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs1);
-        J[159] = (K[K_c2]*dj1_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs1);
-        J[158] = (K[K_d5]*dj1_c0) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs1);
+        const T dj1_c0 = F.dt*xt1;
+        J[157] = (F.dt*(K[K_c1a]*xt42 + K[K_c1b]*xt42 + K[K_c1c]*xt42 + K[K_c2]*xt43 + K[K_d5]*xt44) + T(1)) * (cs1 * rs1);
+        J[156] = (dj1_c0*(K[K_c1a] + K[K_c1b] + K[K_c1c])) * (cs42 * rs1);
+        J[159] = (K[K_c2]*dj1_c0) * (cs43 * rs1);
+        J[158] = (K[K_d5]*dj1_c0) * (cs44 * rs1);
     }
     {  // row 3
     const T rs3 = nt_rscale<T>(nt_exp_hi(x[3]), fh);
         const T dj3_c0 = T(2)*F.dt;
         const T dj3_c1 = K[K_b39]*dj3_c0;
         const T dj3_c2 = K[K_b6]*dj3_c0;
-        J[20] = (-dj3_c1*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs3);
-        J[23] = (F.dt*F.rain_hno3) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs3);
-        J[22] = (-dj3_c1*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs3);
-        J[24] = (dj3_c2*nt_cvt<T>(x[51])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs3);
-        J[21] = (dj3_c2*nt_cvt<T>(x[49])) * (nt_scale<T>(nt_exp_hi(x[51]), fh) * rs3);
+        J[20] = (-dj3_c1*xt42) * (cs0 * rs3);
+        J[23] = (F.dt*F.rain_hno3) * (cs4 * rs3);
+        J[22] = (-dj3_c1*xt0) * (cs42 * rs3);
+        J[24] = (dj3_c2*xt51) * (cs49 * rs3);
+        J[21] = (dj3_c2*xt49) * (cs51 * rs3);
     }
     {  // row 6
     const T rs6 = nt_rscale<T>(nt_exp_hi(x[6]), fh);
-        const T dj6_c0 = T(3)*nt_cvt<T>(x[42]);
+        const T dj6_c0 = T(3)*xt42;
         const T dj6_c1 = T(2)*K[K_d91];
         const T dj6_c2 = T(4)*K[K_d93];
         const T dj6_c3 = T(3)*K[K_d94];
-        J[9] = (F.dt*F.rain_hcl) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs6);
-        J[7] = (-F.dt*(K[K_d90]*dj6_c0 + T(3)*tj[J_cfc11])) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs6);
-        J[4] = (-F.dt*(dj6_c1*nt_cvt<T>(x[42]) + T(2)*tj[J_cfc12])) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs6);
-        J[0] = (-F.dt*(K[K_d92]*dj6_c0 + T(3)*tj[J_cfc113])) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs6);
-        J[2] = (-F.dt*(dj6_c2*nt_cvt<T>(x[42]) + T(4)*tj[J_ccl4])) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs6);
-        J[6] = (-F.dt*(dj6_c3*nt_cvt<T>(x[43]) + T(3)*tj[J_ch3ccl3])) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs6);
-        J[5] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl])) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs6);
-        J[3] = (-F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22])) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs6);
-        J[1] = (-F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211])) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs6);
-        J[8] = (-F.dt*(T(3)*K[K_d90]*nt_cvt<T>(x[30]) + T(3)*K[K_d92]*nt_cvt<T>(x[32]) + K[K_d96]*nt_cvt<T>(x[36]) + K[K_e52]*nt_cvt<T>(x[38]) + dj6_c1*nt_cvt<T>(x[31]) + dj6_c2*nt_cvt<T>(x[33]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs6);
-        J[10] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[35]) + K[K_d97]*nt_cvt<T>(x[36]) + dj6_c3*nt_cvt<T>(x[34]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs6);
+        J[9] = (F.dt*F.rain_hcl) * (cs12 * rs6);
+        J[7] = (-F.dt*(K[K_d90]*dj6_c0 + T(3)*tj[J_cfc11])) * (cs30 * rs6);
+        J[4] = (-F.dt*(dj6_c1*xt42 + T(2)*tj[J_cfc12])) * (cs31 * rs6);
+        J[0] = (-F.dt*(K[K_d92]*dj6_c0 + T(3)*tj[J_cfc113])) * (cs32 * rs6);
+        J[2] = (-F.dt*(dj6_c2*xt42 + T(4)*tj[J_ccl4])) * (cs33 * rs6);
+        J[6] = (-F.dt*(dj6_c3*xt43 + T(3)*tj[J_ch3ccl3])) * (cs34 * rs6);
+        J[5] = (-F.dt*(K[K_d95]*xt43 + tj[J_ch3cl])) * (cs35 * rs6);
+        J[3] = (-F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22])) * (cs36 * rs6);
+        J[1] = (-F.dt*(K[K_e52]*xt42 + tj[J_h1211])) * (cs38 * rs6);
+        J[8] = (-F.dt*(T(3)*K[K_d90]*xt30 + T(3)*K[K_d92]*xt32 + K[K_d96]*xt36 + K[K_e52]*xt38 + dj6_c1*xt31 + dj6_c2*xt33)) * (cs42 * rs6);
+        J[10] = (-F.dt*(K[K_d95]*xt35 + K[K_d97]*xt36 + dj6_c3*xt34)) * (cs43 * rs6);
     }
     {  // row 13
     const T rs13 = nt_rscale<T>(nt_exp_hi(x[13]), fh);
-        const T dj13_c0 = F.dt*nt_cvt<T>(x[13]);
+        const T dj13_c0 = F.dt*xt13;
         const T dj13_c1 = F.dt*K[K_d31];
-        J[89] = (dj13_c0*het[0]) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs13);
-        J[88] = (dj13_c0*het[1]) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs13);
-        J[87] = (F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]) + tj[J_clono2_cl] + tj[J_clono2_clo]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs13);
-        J[91] = (K[K_d32]*dj13_c0) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs13);
-        J[90] = (-dj13_c1*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs13);
-        J[92] = (-dj13_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs13);
+        J[89] = (dj13_c0*het[0]) * (cs2 * rs13);
+        J[88] = (dj13_c0*het[1]) * (cs12 * rs13);
+        J[87] = (F.dt*(K[K_d32]*xt45 + het[0]*xt2 + het[1]*xt12 + tj[J_clono2_cl] + tj[J_clono2_clo]) + T(1)) * (cs13 * rs13);
+        J[91] = (K[K_d32]*dj13_c0) * (cs45 * rs13);
+        J[90] = (-dj13_c1*xt52) * (cs48 * rs13);
+        J[92] = (-dj13_c1*xt48) * (cs52 * rs13);
     }
     {  // row 19
     const T rs19 = nt_rscale<T>(nt_exp_hi(x[19]), fh);
-        const T dj19_c0 = F.dt*nt_cvt<T>(x[19]);
+        const T dj19_c0 = F.dt*xt19;
         const T dj19_c1 = F.dt*K[K_e13];
-        J[56] = (dj19_c0*het[5]) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs19);
-        J[55] = (F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + het[5]*nt_cvt<T>(x[2]) + tj[J_brono2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs19);
-        J[58] = (K[K_e8]*dj19_c0) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs19);
-        J[57] = (-dj19_c1*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs19);
-        J[59] = (-dj19_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs19);
+        J[56] = (dj19_c0*het[5]) * (cs2 * rs19);
+        J[55] = (F.dt*(K[K_e8]*xt45 + het[5]*xt2 + tj[J_brono2]) + T(1)) * (cs19 * rs19);
+        J[58] = (K[K_e8]*dj19_c0) * (cs45 * rs19);
+        J[57] = (-dj19_c1*xt53) * (cs48 * rs19);
+        J[59] = (-dj19_c1*xt48) * (cs53 * rs19);
     }
     {  // row 20
     const T rs20 = nt_rscale<T>(nt_exp_hi(x[20]), fh);
         const T dj20_c0 = T(2)*F.dt;
         const T dj20_c1 = K[K_b39]*dj20_c0;
         const T dj20_c2 = F.parthno3*K[K_b27];
-        const T dj20_c3 = F.dt*nt_cvt<T>(x[48]);
+        const T dj20_c3 = F.dt*xt48;
         const T dj20_c4 = T(2)*K[K_b12];
         const T dj20_c5 = K[K_b6]*dj20_c0;
-        J[233] = (-dj20_c1*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs20);
-        J[237] = (-F.dt*(F.parthno3*tj[J_hno3] + dj20_c2*nt_cvt<T>(x[43]))) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs20);
-        J[232] = (-F.dt*(T(2)*F.hnm*K[K_b32] + T(2)*tj[J_n2o5])) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs20);
-        J[235] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + tj[J_clono2_cl] + tj[J_clono2_clo])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs20);
-        J[229] = (-F.dt*tj[J_clno2]) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs20);
-        J[230] = (-F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + tj[J_brono2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs20);
-        J[238] = (-F.dt*(F.hnm*K[K_b24] + K[K_b28]*nt_cvt<T>(x[43]) + tj[J_hno4])) * (nt_scale<T>(nt_exp_hi(x[21]), fh) * rs20);
-        J[236] = (-dj20_c1*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs20);
-        J[243] = (-F.dt*(K[K_b28]*nt_cvt<T>(x[21]) + dj20_c2*nt_cvt<T>(x[4])) + K[K_b22]*dj20_c3) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs20);
-        J[241] = (K[K_d36]*dj20_c3) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs20);
-        J[240] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[13]) + K[K_e8]*nt_cvt<T>(x[19]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs20);
-        J[244] = (K[K_b23]*dj20_c3) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs20);
-        J[239] = (F.dt*(K[K_b22]*nt_cvt<T>(x[43]) + K[K_b23]*nt_cvt<T>(x[47]) + K[K_d31]*nt_cvt<T>(x[52]) + K[K_d36]*nt_cvt<T>(x[44]) + K[K_e13]*nt_cvt<T>(x[53]) + dj20_c4*nt_cvt<T>(x[54]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs20);
-        J[245] = (dj20_c5*nt_cvt<T>(x[51])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs20);
-        J[234] = (dj20_c5*nt_cvt<T>(x[49])) * (nt_scale<T>(nt_exp_hi(x[51]), fh) * rs20);
-        J[246] = (K[K_d31]*dj20_c3) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs20);
-        J[242] = (K[K_e13]*dj20_c3) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs20);
-        J[231] = (dj20_c3*dj20_c4) * (nt_scale<T>(nt_exp_hi(x[54]), fh) * rs20);
+        J[233] = (-dj20_c1*xt42) * (cs0 * rs20);
+        J[237] = (-F.dt*(F.parthno3*tj[J_hno3] + dj20_c2*xt43)) * (cs4 * rs20);
+        J[232] = (-F.dt*(T(2)*F.hnm*K[K_b32] + T(2)*tj[J_n2o5])) * (cs5 * rs20);
+        J[235] = (-F.dt*(K[K_d32]*xt45 + tj[J_clono2_cl] + tj[J_clono2_clo])) * (cs13 * rs20);
+        J[229] = (-F.dt*tj[J_clno2]) * (cs17 * rs20);
+        J[230] = (-F.dt*(K[K_e8]*xt45 + tj[J_brono2])) * (cs19 * rs20);
+        J[238] = (-F.dt*(F.hnm*K[K_b24] + K[K_b28]*xt43 + tj[J_hno4])) * (cs21 * rs20);
+        J[236] = (-dj20_c1*xt0) * (cs42 * rs20);
+        J[243] = (-F.dt*(K[K_b28]*xt21 + dj20_c2*xt4) + K[K_b22]*dj20_c3) * (cs43 * rs20);
+        J[241] = (K[K_d36]*dj20_c3) * (cs44 * rs20);
+        J[240] = (-F.dt*(K[K_d32]*xt13 + K[K_e8]*xt19)) * (cs45 * rs20);
+        J[244] = (K[K_b23]*dj20_c3) * (cs47 * rs20);
+        J[239] = (F.dt*(K[K_b22]*xt43 + K[K_b23]*xt47 + K[K_d31]*xt52 + K[K_d36]*xt44 + K[K_e13]*xt53 + dj20_c4*xt54)) * (cs48 * rs20);
+        J[245] = (dj20_c5*xt51) * (cs49 * rs20);
+        J[234] = (dj20_c5*xt49) * (cs51 * rs20);
+        J[246] = (K[K_d31]*dj20_c3) * (cs52 * rs20);
+        J[242] = (K[K_e13]*dj20_c3) * (cs53 * rs20);
+        J[231] = (dj20_c3*dj20_c4) * (cs54 * rs20);
     }
     {  // row 21
     const T rs21 = nt_rscale<T>(nt_exp_hi(x[21]), fh);
         const T dj21_c0 = F.dt*K[K_b23];
-        J[152] = (F.dt*(F.hnm*K[K_b24] + K[K_b28]*nt_cvt<T>(x[43]) + tj[J_hno4]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[21]), fh) * rs21);
-        J[154] = (F.dt*K[K_b28]*nt_cvt<T>(x[21])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs21);
-        J[155] = (-dj21_c0*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs21);
-        J[153] = (-dj21_c0*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs21);
+        J[152] = (F.dt*(F.hnm*K[K_b24] + K[K_b28]*xt43 + tj[J_hno4]) + T(1)) * (cs21 * rs21);
+        J[154] = (F.dt*K[K_b28]*xt21) * (cs43 * rs21);
+        J[155] = (-dj21_c0*xt48) * (cs47 * rs21);
+        J[153] = (-dj21_c0*xt47) * (cs48 * rs21);
     }
     {  // row 23
     const T rs23 = nt_rscale<T>(nt_exp_hi(x[23]), fh);
         const T dj23_c0 = T(2)*het[7];
-        const T dj23_c1 = F.dt*F.parthbr*nt_cvt<T>(x[18]);
-        const T dj23_c2 = F.dt*nt_cvt<T>(x[53]);
-        J[196] = (-F.dt*(F.parthbr*(K[K_e11]*nt_cvt<T>(x[43]) + K[K_e9]*nt_cvt<T>(x[42]) + tj[J_hbr]) + dj23_c0*nt_cvt<T>(x[25]))) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs23);
-        J[193] = (-F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + tj[J_brono2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs23);
-        J[194] = (-F.dt*(K[K_e16]*nt_cvt<T>(x[45]) + dj23_c0*nt_cvt<T>(x[18]) + tj[J_hobr])) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs23);
-        J[192] = (-F.dt*tj[J_brcl]) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs23);
-        J[197] = (F.dt*K[K_c19]*nt_cvt<T>(x[50])) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs23);
-        J[195] = (-K[K_e9]*dj23_c1) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs23);
-        J[202] = (-K[K_e11]*dj23_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs23);
-        J[199] = (-F.dt*(K[K_e16]*nt_cvt<T>(x[25]) + K[K_e8]*nt_cvt<T>(x[19]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs23);
-        J[203] = (F.dt*(K[K_e15]*nt_cvt<T>(x[53]) + K[K_e7]*nt_cvt<T>(x[50]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs23);
-        J[198] = (K[K_e13]*dj23_c2) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs23);
-        J[201] = (F.dt*(K[K_c19]*nt_cvt<T>(x[27]) + K[K_e7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs23);
-        J[204] = (K[K_e5c]*dj23_c2) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs23);
-        J[200] = (F.dt*(K[K_e13]*nt_cvt<T>(x[48]) + K[K_e15]*nt_cvt<T>(x[47]) + K[K_e5c]*nt_cvt<T>(x[52]))) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs23);
+        const T dj23_c1 = F.dt*F.parthbr*xt18;
+        const T dj23_c2 = F.dt*xt53;
+        J[196] = (-F.dt*(F.parthbr*(K[K_e11]*xt43 + K[K_e9]*xt42 + tj[J_hbr]) + dj23_c0*xt25)) * (cs18 * rs23);
+        J[193] = (-F.dt*(K[K_e8]*xt45 + tj[J_brono2])) * (cs19 * rs23);
+        J[194] = (-F.dt*(K[K_e16]*xt45 + dj23_c0*xt18 + tj[J_hobr])) * (cs25 * rs23);
+        J[192] = (-F.dt*tj[J_brcl]) * (cs26 * rs23);
+        J[197] = (F.dt*K[K_c19]*xt50) * (cs27 * rs23);
+        J[195] = (-K[K_e9]*dj23_c1) * (cs42 * rs23);
+        J[202] = (-K[K_e11]*dj23_c1) * (cs43 * rs23);
+        J[199] = (-F.dt*(K[K_e16]*xt25 + K[K_e8]*xt19)) * (cs45 * rs23);
+        J[203] = (F.dt*(K[K_e15]*xt53 + K[K_e7]*xt50)) * (cs47 * rs23);
+        J[198] = (K[K_e13]*dj23_c2) * (cs48 * rs23);
+        J[201] = (F.dt*(K[K_c19]*xt27 + K[K_e7]*xt47)) * (cs50 * rs23);
+        J[204] = (K[K_e5c]*dj23_c2) * (cs52 * rs23);
+        J[200] = (F.dt*(K[K_e13]*xt48 + K[K_e15]*xt47 + K[K_e5c]*xt52)) * (cs53 * rs23);
     }
     {  // row 24
     const T rs24 = nt_rscale<T>(nt_exp_hi(x[24]), fh);
-        J[97] = (F.dt*(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[24]), fh) * rs24);
-        J[98] = (-T(2)*F.dt*K[K_d60]*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs24);
+        J[97] = (F.dt*(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(1)) * (cs24 * rs24);
+        J[98] = (-T(2)*F.dt*K[K_d60]*xt52) * (cs52 * rs24);
     }
     {  // row 28
     const T rs28 = nt_rscale<T>(nt_exp_hi(x[28]), fh);
-        const T dj28_c0 = T(2)*K[K_c14]*nt_cvt<T>(x[28]);
+        const T dj28_c0 = T(2)*K[K_c14]*xt28;
         const T dj28_c1 = F.dt*K[K_c17a];
-        const T dj28_c2 = F.dt*nt_cvt<T>(x[28]);
-        J[212] = (F.dt*dj28_c0 + F.dt*(K[K_c18]*nt_cvt<T>(x[52]) + K[K_c5]*nt_cvt<T>(x[49]) + K[K_c7]*nt_cvt<T>(x[47]) + dj28_c0) + T(1)) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs28);
-        J[210] = (-dj28_c1*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs28);
-        J[213] = (-dj28_c1*nt_cvt<T>(x[29])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs28);
-        J[214] = (K[K_c7]*dj28_c2) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs28);
-        J[215] = (K[K_c5]*dj28_c2) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs28);
-        J[216] = (K[K_c18]*dj28_c2) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs28);
-        J[211] = (-F.dt*F.o2*K[K_c4]) * (nt_scale<T>(nt_exp_hi(x[56]), fh) * rs28);
+        const T dj28_c2 = F.dt*xt28;
+        J[212] = (F.dt*dj28_c0 + F.dt*(K[K_c18]*xt52 + K[K_c5]*xt49 + K[K_c7]*xt47 + dj28_c0) + T(1)) * (cs28 * rs28);
+        J[210] = (-dj28_c1*xt43) * (cs29 * rs28);
+        J[213] = (-dj28_c1*xt29) * (cs43 * rs28);
+        J[214] = (K[K_c7]*dj28_c2) * (cs47 * rs28);
+        J[215] = (K[K_c5]*dj28_c2) * (cs49 * rs28);
+        J[216] = (K[K_c18]*dj28_c2) * (cs52 * rs28);
+        J[211] = (-F.dt*F.o2*K[K_c4]) * (cs56 * rs28);
     }
     {  // row 31
     const T rs31 = nt_rscale<T>(nt_exp_hi(x[31]), fh);
-        J[41] = (F.dt*(K[K_d91]*nt_cvt<T>(x[42]) + tj[J_cfc12]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs31);
-        J[42] = (F.dt*K[K_d91]*nt_cvt<T>(x[31])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs31);
+        J[41] = (F.dt*(K[K_d91]*xt42 + tj[J_cfc12]) + T(1)) * (cs31 * rs31);
+        J[42] = (F.dt*K[K_d91]*xt31) * (cs42 * rs31);
     }
     {  // row 33
     const T rs33 = nt_rscale<T>(nt_exp_hi(x[33]), fh);
-        J[32] = (F.dt*(K[K_d93]*nt_cvt<T>(x[42]) + tj[J_ccl4]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs33);
-        J[33] = (F.dt*K[K_d93]*nt_cvt<T>(x[33])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs33);
+        J[32] = (F.dt*(K[K_d93]*xt42 + tj[J_ccl4]) + T(1)) * (cs33 * rs33);
+        J[33] = (F.dt*K[K_d93]*xt33) * (cs42 * rs33);
     }
     {  // row 35
     const T rs35 = nt_rscale<T>(nt_exp_hi(x[35]), fh);
-        J[66] = (F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs35);
-        J[67] = (F.dt*K[K_d95]*nt_cvt<T>(x[35])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs35);
+        J[66] = (F.dt*(K[K_d95]*xt43 + tj[J_ch3cl]) + T(1)) * (cs35 * rs35);
+        J[67] = (F.dt*K[K_d95]*xt35) * (cs43 * rs35);
     }
     {  // row 36
     const T rs36 = nt_rscale<T>(nt_exp_hi(x[36]), fh);
-        const T dj36_c0 = F.dt*nt_cvt<T>(x[36]);
-        J[38] = (F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs36);
-        J[39] = (K[K_d96]*dj36_c0) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs36);
-        J[40] = (K[K_d97]*dj36_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs36);
+        const T dj36_c0 = F.dt*xt36;
+        J[38] = (F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22]) + T(1)) * (cs36 * rs36);
+        J[39] = (K[K_d96]*dj36_c0) * (cs42 * rs36);
+        J[40] = (K[K_d97]*dj36_c0) * (cs43 * rs36);
     }
     {  // row 39
     const T rs39 = nt_rscale<T>(nt_exp_hi(x[39]), fh);
-        J[50] = (F.dt*(K[K_e53]*nt_cvt<T>(x[42]) + tj[J_h1301]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[39]), fh) * rs39);
-        J[51] = (F.dt*K[K_e53]*nt_cvt<T>(x[39])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs39);
+        J[50] = (F.dt*(K[K_e53]*xt42 + tj[J_h1301]) + T(1)) * (cs39 * rs39);
+        J[51] = (F.dt*K[K_e53]*xt39) * (cs42 * rs39);
     }
     {  // row 40
     const T rs40 = nt_rscale<T>(nt_exp_hi(x[40]), fh);
         const T dj40_c0 = T(2)*K[K_e54];
-        J[16] = (F.dt*F.rain_hbr) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs40);
-        J[13] = (-F.dt*(K[K_e50]*nt_cvt<T>(x[42]) + K[K_e51]*nt_cvt<T>(x[43]) + tj[J_ch3br])) * (nt_scale<T>(nt_exp_hi(x[37]), fh) * rs40);
-        J[11] = (-F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211])) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs40);
-        J[12] = (-F.dt*(K[K_e53]*nt_cvt<T>(x[42]) + tj[J_h1301])) * (nt_scale<T>(nt_exp_hi(x[39]), fh) * rs40);
-        J[15] = (-F.dt*(dj40_c0*nt_cvt<T>(x[43]) + T(2)*tj[J_ch2br2])) * (nt_scale<T>(nt_exp_hi(x[41]), fh) * rs40);
-        J[14] = (-F.dt*(K[K_e50]*nt_cvt<T>(x[37]) + K[K_e52]*nt_cvt<T>(x[38]) + K[K_e53]*nt_cvt<T>(x[39]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs40);
-        J[17] = (-F.dt*(K[K_e51]*nt_cvt<T>(x[37]) + dj40_c0*nt_cvt<T>(x[41]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs40);
+        J[16] = (F.dt*F.rain_hbr) * (cs18 * rs40);
+        J[13] = (-F.dt*(K[K_e50]*xt42 + K[K_e51]*xt43 + tj[J_ch3br])) * (cs37 * rs40);
+        J[11] = (-F.dt*(K[K_e52]*xt42 + tj[J_h1211])) * (cs38 * rs40);
+        J[12] = (-F.dt*(K[K_e53]*xt42 + tj[J_h1301])) * (cs39 * rs40);
+        J[15] = (-F.dt*(dj40_c0*xt43 + T(2)*tj[J_ch2br2])) * (cs41 * rs40);
+        J[14] = (-F.dt*(K[K_e50]*xt37 + K[K_e52]*xt38 + K[K_e53]*xt39)) * (cs42 * rs40);
+        J[17] = (-F.dt*(K[K_e51]*xt37 + dj40_c0*xt41)) * (cs43 * rs40);
     }
     {  // row 42
     const T rs42 = nt_rscale<T>(nt_exp_hi(x[42]), fh);
-        J[99] = (-tj[J_o3_o1d]/(F.n2*K[K_hk4] + F.o2*K[K_hk5])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs42);
+        J[99] = (-tj[J_o3_o1d]/(F.n2*K[K_hk4] + F.o2*K[K_hk5])) * (cs46 * rs42);
     }
     {  // row 56
     const T rs56 = nt_rscale<T>(nt_exp_hi(x[56]), fh);
-        const T dj56_c0 = F.o2*K[K_c4] + K[K_c3]*nt_cvt<T>(x[45]);
+        const T dj56_c0 = F.o2*K[K_c4] + K[K_c3]*xt45;
         const T dj56_c1 = (T(1)/(dj56_c0));
-        const T dj56_c2 = K[K_c1a]*nt_cvt<T>(x[42]) + K[K_c2]*nt_cvt<T>(x[43]) + K[K_d5]*nt_cvt<T>(x[44]);
-        const T dj56_c3 = dj56_c1*nt_cvt<T>(x[1]);
-        J[177] = (-dj56_c1*dj56_c2) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs56);
-        J[176] = (-K[K_c1a]*dj56_c3) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs56);
-        J[180] = (-K[K_c2]*dj56_c3) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs56);
-        J[179] = (-K[K_d5]*dj56_c3) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs56);
-        J[178] = (K[K_c3]*dj56_c2*nt_cvt<T>(x[1])/(dj56_c0*dj56_c0)) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs56);
+        const T dj56_c2 = K[K_c1a]*xt42 + K[K_c2]*xt43 + K[K_d5]*xt44;
+        const T dj56_c3 = dj56_c1*xt1;
+        J[177] = (-dj56_c1*dj56_c2) * (cs1 * rs56);
+        J[176] = (-K[K_c1a]*dj56_c3) * (cs42 * rs56);
+        J[180] = (-K[K_c2]*dj56_c3) * (cs43 * rs56);
+        J[179] = (-K[K_d5]*dj56_c3) * (cs44 * rs56);
+        J[178] = (K[K_c3]*dj56_c2*xt1/(dj56_c0*dj56_c0)) * (cs45 * rs56);
     }
     const T D_r1_c0 = T(1)/(F.o2*K[K_hk2]);
-    const T D_r1 = D_r1_c0*(K[K_a2]*nt_cvt<T>(x[55]) + K[K_a6]*nt_cvt<T>(x[43]) + K[K_a6b]*nt_cvt<T>(x[47]) + K[K_b4]*nt_cvt<T>(x[49]) + K[K_d2]*nt_cvt<T>(x[44]) + tj[J_o3_o1d] + tj[J_o3_o3p]);
+    const T D_r1 = D_r1_c0*(K[K_a2]*xt55 + K[K_a6]*xt43 + K[K_a6b]*xt47 + K[K_b4]*xt49 + K[K_d2]*xt44 + tj[J_o3_o1d] + tj[J_o3_o3p]);
     const T d_D_r1_43 = D_r1_c0*K[K_a6];
     const T d_D_r1_44 = D_r1_c0*K[K_d2];
     const T d_D_r1_47 = D_r1_c0*K[K_a6b];
@@ -1914,26 +2238,26 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     const T d_D_r1_55 = D_r1_c0*K[K_a2];
     {  // row 45
     const T rs45 = nt_rscale<T>(nt_exp_hi(x[45]), fh);
-        J[280] = (-d_D_r1_43*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs45);
-        J[279] = (-d_D_r1_44*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs45);
-        J[282] = (-D_r1) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs45);
-        J[281] = (-d_D_r1_47*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs45);
-        J[283] = (-d_D_r1_49*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs45);
-        J[278] = (-d_D_r1_55*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs45);
+        J[280] = (-d_D_r1_43*xt46) * (cs43 * rs45);
+        J[279] = (-d_D_r1_44*xt46) * (cs44 * rs45);
+        J[282] = (-D_r1) * (cs46 * rs45);
+        J[281] = (-d_D_r1_47*xt46) * (cs47 * rs45);
+        J[283] = (-d_D_r1_49*xt46) * (cs49 * rs45);
+        J[278] = (-d_D_r1_55*xt46) * (cs55 * rs45);
     }
     {  // row 46
     const T rs46 = nt_rscale<T>(nt_exp_hi(x[46]), fh);
         const T dj46_c0 = D_r1 + T(1);
-        const T dj46_c1 = nt_cvt<T>(x[7])/(dj46_c0*dj46_c0);
-        J[355] = (-T(1)/dj46_c0) * (nt_scale<T>(nt_exp_hi(x[7]), fh) * rs46);
-        J[358] = (d_D_r1_43*dj46_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs46);
-        J[357] = (d_D_r1_44*dj46_c1) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs46);
-        J[359] = (d_D_r1_47*dj46_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs46);
-        J[360] = (d_D_r1_49*dj46_c1) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs46);
-        J[356] = (d_D_r1_55*dj46_c1) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs46);
+        const T dj46_c1 = xt7/(dj46_c0*dj46_c0);
+        J[355] = (-T(1)/dj46_c0) * (cs7 * rs46);
+        J[358] = (d_D_r1_43*dj46_c1) * (cs43 * rs46);
+        J[357] = (d_D_r1_44*dj46_c1) * (cs44 * rs46);
+        J[359] = (d_D_r1_47*dj46_c1) * (cs47 * rs46);
+        J[360] = (d_D_r1_49*dj46_c1) * (cs49 * rs46);
+        J[356] = (d_D_r1_55*dj46_c1) * (cs55 * rs46);
     }
-    const T D_r4_c0 = F.h2*K[K_a19] + K[K_a36]*nt_cvt<T>(x[8]) + K[K_a5]*nt_cvt<T>(x[45]);
-    const T D_r4_c1 = F.o2*K[K_a1] + K[K_a2]*nt_cvt<T>(x[46]) + T(8.049999999999999e-11)*nt_cvt<T>(x[47]);
+    const T D_r4_c0 = F.h2*K[K_a19] + K[K_a36]*xt8 + K[K_a5]*xt45;
+    const T D_r4_c1 = F.o2*K[K_a1] + K[K_a2]*xt46 + T(8.049999999999999e-11)*xt47;
     const T D_r4_c2 = (T(1)/(D_r4_c1));
     const T D_r4_c3 = D_r4_c0/(D_r4_c1*D_r4_c1);
     const T D_r4 = D_r4_c0*D_r4_c2;
@@ -1941,26 +2265,26 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     const T d_D_r4_45 = D_r4_c2*K[K_a5];
     const T d_D_r4_46 = -D_r4_c3*K[K_a2];
     const T d_D_r4_47 = -T(8.049999999999999e-11)*D_r4_c3;
-    const T D_r7_c0 = F.o2*K[K_b7] + K[K_b6]*nt_cvt<T>(x[49]);
+    const T D_r7_c0 = F.o2*K[K_b7] + K[K_b6]*xt49;
     const T D_r7 = tj[J_no]/D_r7_c0;
     const T d_D_r7_49 = -K[K_b6]*tj[J_no]/(D_r7_c0*D_r7_c0);
     {  // row 51
     const T rs51 = nt_rscale<T>(nt_exp_hi(x[51]), fh);
-        J[78] = (-D_r7 - d_D_r7_49*nt_cvt<T>(x[49])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs51);
+        J[78] = (-D_r7 - d_D_r7_49*xt49) * (cs49 * rs51);
     }
-    const T D_r8_c0 = K[K_b12]*nt_cvt<T>(x[48]) + tj[J_no3_no2] + tj[J_no3_no];
+    const T D_r8_c0 = K[K_b12]*xt48 + tj[J_no3_no2] + tj[J_no3_no];
     const T D_r8_c1 = K[K_b9]/D_r8_c0;
-    const T D_r8 = D_r8_c1*nt_cvt<T>(x[46]);
+    const T D_r8 = D_r8_c1*xt46;
     const T d_D_r8_46 = D_r8_c1;
-    const T d_D_r8_48 = -K[K_b12]*K[K_b9]*nt_cvt<T>(x[46])/(D_r8_c0*D_r8_c0);
+    const T d_D_r8_48 = -K[K_b12]*K[K_b9]*xt46/(D_r8_c0*D_r8_c0);
     {  // row 54
     const T rs54 = nt_rscale<T>(nt_exp_hi(x[54]), fh);
         J[68] = T(0);
-        J[70] = (-d_D_r8_46*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs54);
-        J[69] = (-D_r8 - d_D_r8_48*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs54);
+        J[70] = (-d_D_r8_46*xt48) * (cs46 * rs54);
+        J[69] = (-D_r8 - d_D_r8_48*xt48) * (cs48 * rs54);
     }
-    const T D_r5_c0 = D_r8*tj[J_no3_no] + K[K_b3]*nt_cvt<T>(x[45]) + tj[J_no2];
-    const T D_r5_c1 = K[K_a26]*nt_cvt<T>(x[47]) + K[K_b4]*nt_cvt<T>(x[46]) + K[K_c5]*nt_cvt<T>(x[28]) + K[K_d4]*nt_cvt<T>(x[52]) + K[K_e4]*nt_cvt<T>(x[53]);
+    const T D_r5_c0 = D_r8*tj[J_no3_no] + K[K_b3]*xt45 + tj[J_no2];
+    const T D_r5_c1 = K[K_a26]*xt47 + K[K_b4]*xt46 + K[K_c5]*xt28 + K[K_d4]*xt52 + K[K_e4]*xt53;
     const T D_r5_c2 = (T(1)/(D_r5_c1));
     const T D_r5_c3 = D_r5_c0/(D_r5_c1*D_r5_c1);
     const T D_r5 = D_r5_c0*D_r5_c2;
@@ -1975,22 +2299,22 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     const T rs48 = nt_rscale<T>(nt_exp_hi(x[48]), fh);
         const T dj48_c0 = D_r5*D_r7 + D_r5 + D_r8 + T(1);
         const T dj48_c1 = (T(1)/(dj48_c0*dj48_c0));
-        const T dj48_c2 = dj48_c1*nt_cvt<T>(x[20]);
+        const T dj48_c2 = dj48_c1*xt20;
         const T dj48_c3 = dj48_c2*(-D_r7 + T(-1));
-        J[270] = (-T(1)/dj48_c0) * (nt_scale<T>(nt_exp_hi(x[20]), fh) * rs48);
-        J[269] = (-d_D_r5_28*dj48_c3) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs48);
-        J[272] = (-d_D_r5_45*dj48_c3) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs48);
-        J[275] = (-d_D_r5_46*dj48_c3 + d_D_r8_46*dj48_c1*nt_cvt<T>(x[20])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs48);
-        J[274] = (-d_D_r5_47*dj48_c3) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs48);
-        J[271] = (-d_D_r5_48*dj48_c3 + d_D_r8_48*dj48_c2 + T(1)) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs48);
-        J[276] = (D_r5*d_D_r7_49*dj48_c2) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs48);
-        J[277] = (-d_D_r5_52*dj48_c3) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs48);
-        J[273] = (-d_D_r5_53*dj48_c3) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs48);
+        J[270] = (-T(1)/dj48_c0) * (cs20 * rs48);
+        J[269] = (-d_D_r5_28*dj48_c3) * (cs28 * rs48);
+        J[272] = (-d_D_r5_45*dj48_c3) * (cs45 * rs48);
+        J[275] = (-d_D_r5_46*dj48_c3 + d_D_r8_46*dj48_c1*xt20) * (cs46 * rs48);
+        J[274] = (-d_D_r5_47*dj48_c3) * (cs47 * rs48);
+        J[271] = (-d_D_r5_48*dj48_c3 + d_D_r8_48*dj48_c2 + T(1)) * (cs48 * rs48);
+        J[276] = (D_r5*d_D_r7_49*dj48_c2) * (cs49 * rs48);
+        J[277] = (-d_D_r5_52*dj48_c3) * (cs52 * rs48);
+        J[273] = (-d_D_r5_53*dj48_c3) * (cs53 * rs48);
     }
     const T D_r6_c0 = F.o2*K[K_a1];
-    const T D_r6_c1 = D_r4*D_r6_c0 + K[K_a30]*nt_cvt<T>(x[16]) + K[K_a6]*nt_cvt<T>(x[46]) + K[K_c8]*nt_cvt<T>(x[27]) + K[K_d8]*nt_cvt<T>(x[52]) + K[K_e10]*nt_cvt<T>(x[53]);
+    const T D_r6_c1 = D_r4*D_r6_c0 + K[K_a30]*xt16 + K[K_a6]*xt46 + K[K_c8]*xt27 + K[K_d8]*xt52 + K[K_e10]*xt53;
     const T D_r6_c2 = T(2)*K[K_a27];
-    const T D_r6_c3 = D_r6_c2*nt_cvt<T>(x[47]) + K[K_a17]*nt_cvt<T>(x[43]) + K[K_a26]*nt_cvt<T>(x[49]) + K[K_a6b]*nt_cvt<T>(x[46]) + K[K_a7]*nt_cvt<T>(x[45]) + K[K_d10]*nt_cvt<T>(x[44]) + K[K_d33]*nt_cvt<T>(x[52]) + K[K_d7]*nt_cvt<T>(x[44]) + K[K_e15]*nt_cvt<T>(x[53]) + K[K_e7]*nt_cvt<T>(x[50]) + T(8.049999999999999e-11)*nt_cvt<T>(x[55]);
+    const T D_r6_c3 = D_r6_c2*xt47 + K[K_a17]*xt43 + K[K_a26]*xt49 + K[K_a6b]*xt46 + K[K_a7]*xt45 + K[K_d10]*xt44 + K[K_d33]*xt52 + K[K_d7]*xt44 + K[K_e15]*xt53 + K[K_e7]*xt50 + T(8.049999999999999e-11)*xt55;
     const T D_r6_c4 = (T(1)/(D_r6_c3));
     const T D_r6_c5 = D_r6_c0*D_r6_c4;
     const T D_r6_c6 = D_r6_c1/(D_r6_c3*D_r6_c3);
@@ -2010,50 +2334,50 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     const T d_D_r6_55 = -T(8.049999999999999e-11)*D_r6_c6;
     {  // row 47
     const T rs47 = nt_rscale<T>(nt_exp_hi(x[47]), fh);
-        J[342] = (-d_D_r6_8*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[8]), fh) * rs47);
-        J[343] = (-d_D_r6_16*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs47);
-        J[345] = (-d_D_r6_27*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs47);
-        J[350] = (-D_r6 - d_D_r6_43*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs47);
-        J[347] = (-d_D_r6_44*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs47);
-        J[346] = (-d_D_r6_45*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs47);
-        J[352] = (-d_D_r6_46*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs47);
-        J[351] = (-d_D_r6_47*nt_cvt<T>(x[43]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs47);
-        J[353] = (-d_D_r6_49*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs47);
-        J[349] = (-d_D_r6_50*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs47);
-        J[354] = (-d_D_r6_52*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs47);
-        J[348] = (-d_D_r6_53*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs47);
-        J[344] = (-d_D_r6_55*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs47);
+        J[342] = (-d_D_r6_8*xt43) * (cs8 * rs47);
+        J[343] = (-d_D_r6_16*xt43) * (cs16 * rs47);
+        J[345] = (-d_D_r6_27*xt43) * (cs27 * rs47);
+        J[350] = (-D_r6 - d_D_r6_43*xt43) * (cs43 * rs47);
+        J[347] = (-d_D_r6_44*xt43) * (cs44 * rs47);
+        J[346] = (-d_D_r6_45*xt43) * (cs45 * rs47);
+        J[352] = (-d_D_r6_46*xt43) * (cs46 * rs47);
+        J[351] = (-d_D_r6_47*xt43 + T(1)) * (cs47 * rs47);
+        J[353] = (-d_D_r6_49*xt43) * (cs49 * rs47);
+        J[349] = (-d_D_r6_50*xt43) * (cs50 * rs47);
+        J[354] = (-d_D_r6_52*xt43) * (cs52 * rs47);
+        J[348] = (-d_D_r6_53*xt43) * (cs53 * rs47);
+        J[344] = (-d_D_r6_55*xt43) * (cs55 * rs47);
     }
-    const T D_r13_c0 = K[K_d32]*nt_cvt<T>(x[45]) + het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]) + tj[J_clono2_cl] + tj[J_clono2_clo];
+    const T D_r13_c0 = K[K_d32]*xt45 + het[0]*xt2 + het[1]*xt12 + tj[J_clono2_cl] + tj[J_clono2_clo];
     const T D_r13_c1 = K[K_d31]/D_r13_c0;
-    const T D_r13_c2 = K[K_d31]*nt_cvt<T>(x[48])/(D_r13_c0*D_r13_c0);
-    const T D_r13 = D_r13_c1*nt_cvt<T>(x[48]);
+    const T D_r13_c2 = K[K_d31]*xt48/(D_r13_c0*D_r13_c0);
+    const T D_r13 = D_r13_c1*xt48;
     const T d_D_r13_2 = -D_r13_c2*het[0];
     const T d_D_r13_12 = -D_r13_c2*het[1];
     const T d_D_r13_45 = -D_r13_c2*K[K_d32];
     const T d_D_r13_48 = D_r13_c1;
     const T D_r9_c0 = D_r13*het[0];
-    const T D_r9_c1 = D_r9_c0*nt_cvt<T>(x[2]) + K[K_d33]*nt_cvt<T>(x[47]);
-    const T D_r9_c2 = K[K_d35]*nt_cvt<T>(x[45]) + het[4]*nt_cvt<T>(x[12]) + tj[J_hocl];
+    const T D_r9_c1 = D_r9_c0*xt2 + K[K_d33]*xt47;
+    const T D_r9_c2 = K[K_d35]*xt45 + het[4]*xt12 + tj[J_hocl];
     const T D_r9_c3 = (T(1)/(D_r9_c2));
-    const T D_r9_c4 = D_r9_c3*het[0]*nt_cvt<T>(x[2]);
+    const T D_r9_c4 = D_r9_c3*het[0]*xt2;
     const T D_r9_c5 = D_r9_c1/(D_r9_c2*D_r9_c2);
     const T D_r9 = D_r9_c1*D_r9_c3;
     const T d_D_r9_2 = D_r9_c0*D_r9_c3 + D_r9_c4*d_D_r13_2;
     const T d_D_r9_12 = D_r9_c4*d_D_r13_12 - D_r9_c5*het[4];
-    const T d_D_r9_45 = D_r9_c3*d_D_r13_45*het[0]*nt_cvt<T>(x[2]) - D_r9_c5*K[K_d35];
+    const T d_D_r9_45 = D_r9_c3*d_D_r13_45*het[0]*xt2 - D_r9_c5*K[K_d35];
     const T d_D_r9_47 = D_r9_c3*K[K_d33];
     const T d_D_r9_48 = D_r9_c4*d_D_r13_48;
     const T D_r10_c0 = K[K_d60]/(F.hnm*K[K_d61] + tj[J_cl2o2]);
-    const T D_r10 = D_r10_c0*nt_cvt<T>(x[52]);
+    const T D_r10 = D_r10_c0*xt52;
     const T d_D_r10_52 = D_r10_c0;
     const T D_r12_c0 = K[K_e5c]/tj[J_brcl];
-    const T D_r12 = D_r12_c0*nt_cvt<T>(x[53]);
+    const T D_r12 = D_r12_c0*xt53;
     const T d_D_r12_53 = D_r12_c0;
-    const T D_r11_c0 = K[K_d10]*nt_cvt<T>(x[47]) + K[K_d2]*nt_cvt<T>(x[46]) + K[K_d37]*nt_cvt<T>(x[14]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]);
+    const T D_r11_c0 = K[K_d10]*xt47 + K[K_d2]*xt46 + K[K_d37]*xt14 + K[K_d5]*xt1 + K[K_d7]*xt47;
     const T D_r11_c1 = (T(1)/(D_r11_c0));
     const T D_r11_c2 = T(2)*tj[J_cl2o2];
-    const T D_r11_c3 = D_r10*D_r11_c2 + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*nt_cvt<T>(x[28]) + K[K_d3]*nt_cvt<T>(x[45]) + K[K_d4]*nt_cvt<T>(x[49]) + K[K_d8]*nt_cvt<T>(x[43]) + K[K_e5b]*nt_cvt<T>(x[53]);
+    const T D_r11_c3 = D_r10*D_r11_c2 + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*xt28 + K[K_d3]*xt45 + K[K_d4]*xt49 + K[K_d8]*xt43 + K[K_e5b]*xt53;
     const T D_r11_c4 = D_r11_c3/(D_r11_c0*D_r11_c0);
     const T D_r11_c5 = D_r11_c1*tj[J_clono2_cl];
     const T D_r11_c6 = D_r11_c1*tj[J_hocl];
@@ -2073,57 +2397,57 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     const T d_D_r11_53 = D_r11_c1*K[K_e5b] + D_r11_c1*d_D_r12_53*tj[J_brcl];
     {  // row 44
     const T rs44 = nt_rscale<T>(nt_exp_hi(x[44]), fh);
-        J[284] = (-d_D_r11_1*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs44);
-        J[288] = (-d_D_r11_2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs44);
-        J[287] = (-d_D_r11_12*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs44);
-        J[285] = (-d_D_r11_14*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs44);
-        J[286] = (-d_D_r11_28*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs44);
-        J[292] = (-d_D_r11_43*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs44);
-        J[290] = (-d_D_r11_45*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs44);
-        J[294] = (-d_D_r11_46*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs44);
-        J[293] = (-d_D_r11_47*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs44);
-        J[289] = (-d_D_r11_48*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs44);
-        J[295] = (-d_D_r11_49*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs44);
-        J[296] = (-D_r11 - d_D_r11_52*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs44);
-        J[291] = (-d_D_r11_53*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs44);
+        J[284] = (-d_D_r11_1*xt52) * (cs1 * rs44);
+        J[288] = (-d_D_r11_2*xt52) * (cs2 * rs44);
+        J[287] = (-d_D_r11_12*xt52) * (cs12 * rs44);
+        J[285] = (-d_D_r11_14*xt52) * (cs14 * rs44);
+        J[286] = (-d_D_r11_28*xt52) * (cs28 * rs44);
+        J[292] = (-d_D_r11_43*xt52) * (cs43 * rs44);
+        J[290] = (-d_D_r11_45*xt52) * (cs45 * rs44);
+        J[294] = (-d_D_r11_46*xt52) * (cs46 * rs44);
+        J[293] = (-d_D_r11_47*xt52) * (cs47 * rs44);
+        J[289] = (-d_D_r11_48*xt52) * (cs48 * rs44);
+        J[295] = (-d_D_r11_49*xt52) * (cs49 * rs44);
+        J[296] = (-D_r11 - d_D_r11_52*xt52) * (cs52 * rs44);
+        J[291] = (-d_D_r11_53*xt52) * (cs53 * rs44);
     }
     {  // row 52
     const T rs52 = nt_rscale<T>(nt_exp_hi(x[52]), fh);
         const T dj52_c0 = D_r11 + T(1);
-        const T dj52_c1 = nt_cvt<T>(x[22])/(dj52_c0*dj52_c0);
-        J[369] = (d_D_r11_1*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs52);
-        J[373] = (d_D_r11_2*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs52);
-        J[372] = (d_D_r11_12*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs52);
-        J[370] = (d_D_r11_14*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs52);
-        J[368] = (-T(1)/dj52_c0) * (nt_scale<T>(nt_exp_hi(x[22]), fh) * rs52);
-        J[371] = (d_D_r11_28*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs52);
-        J[377] = (d_D_r11_43*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs52);
-        J[375] = (d_D_r11_45*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs52);
-        J[379] = (d_D_r11_46*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs52);
-        J[378] = (d_D_r11_47*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs52);
-        J[374] = (d_D_r11_48*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs52);
-        J[380] = (d_D_r11_49*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs52);
-        J[381] = (d_D_r11_52*dj52_c1 + T(1)) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs52);
-        J[376] = (d_D_r11_53*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs52);
+        const T dj52_c1 = xt22/(dj52_c0*dj52_c0);
+        J[369] = (d_D_r11_1*dj52_c1) * (cs1 * rs52);
+        J[373] = (d_D_r11_2*dj52_c1) * (cs2 * rs52);
+        J[372] = (d_D_r11_12*dj52_c1) * (cs12 * rs52);
+        J[370] = (d_D_r11_14*dj52_c1) * (cs14 * rs52);
+        J[368] = (-T(1)/dj52_c0) * (cs22 * rs52);
+        J[371] = (d_D_r11_28*dj52_c1) * (cs28 * rs52);
+        J[377] = (d_D_r11_43*dj52_c1) * (cs43 * rs52);
+        J[375] = (d_D_r11_45*dj52_c1) * (cs45 * rs52);
+        J[379] = (d_D_r11_46*dj52_c1) * (cs46 * rs52);
+        J[378] = (d_D_r11_47*dj52_c1) * (cs47 * rs52);
+        J[374] = (d_D_r11_48*dj52_c1) * (cs48 * rs52);
+        J[380] = (d_D_r11_49*dj52_c1) * (cs49 * rs52);
+        J[381] = (d_D_r11_52*dj52_c1 + T(1)) * (cs52 * rs52);
+        J[376] = (d_D_r11_53*dj52_c1) * (cs53 * rs52);
     }
-    const T D_r27_c0 = K[K_e8]*nt_cvt<T>(x[45]) + tj[J_brono2];
+    const T D_r27_c0 = K[K_e8]*xt45 + tj[J_brono2];
     const T D_r27_c1 = K[K_e13]/D_r27_c0;
-    const T D_r27 = D_r27_c1*nt_cvt<T>(x[48]);
-    const T d_D_r27_45 = -K[K_e13]*K[K_e8]*nt_cvt<T>(x[48])/(D_r27_c0*D_r27_c0);
+    const T D_r27 = D_r27_c1*xt48;
+    const T d_D_r27_45 = -K[K_e13]*K[K_e8]*xt48/(D_r27_c0*D_r27_c0);
     const T d_D_r27_48 = D_r27_c1;
-    const T D_r28_c0 = K[K_e16]*nt_cvt<T>(x[45]) + tj[J_hobr];
+    const T D_r28_c0 = K[K_e16]*xt45 + tj[J_hobr];
     const T D_r28_c1 = K[K_e15]/D_r28_c0;
-    const T D_r28 = D_r28_c1*nt_cvt<T>(x[47]);
-    const T d_D_r28_45 = -K[K_e15]*K[K_e16]*nt_cvt<T>(x[47])/(D_r28_c0*D_r28_c0);
+    const T D_r28 = D_r28_c1*xt47;
+    const T d_D_r28_45 = -K[K_e15]*K[K_e16]*xt47/(D_r28_c0*D_r28_c0);
     const T d_D_r28_47 = D_r28_c1;
     const T D_r29_c0 = K[K_e5c]/tj[J_brcl];
-    const T D_r29 = D_r29_c0*nt_cvt<T>(x[52]);
+    const T D_r29 = D_r29_c0*xt52;
     const T d_D_r29_52 = D_r29_c0;
-    const T D_r30_c0 = K[K_c19]*nt_cvt<T>(x[27]) + K[K_e2]*nt_cvt<T>(x[46]) + K[K_e7]*nt_cvt<T>(x[47]);
+    const T D_r30_c0 = K[K_c19]*xt27 + K[K_e2]*xt46 + K[K_e7]*xt47;
     const T D_r30_c1 = (T(1)/(D_r30_c0));
     const T D_r30_c2 = T(0.85)*tj[J_brono2];
     const T D_r30_c3 = T(2)*K[K_e6];
-    const T D_r30_c4 = D_r27*D_r30_c2 + D_r28*tj[J_hobr] + D_r29*tj[J_brcl] + D_r30_c3*nt_cvt<T>(x[53]) + K[K_e10]*nt_cvt<T>(x[43]) + K[K_e3]*nt_cvt<T>(x[45]) + K[K_e4]*nt_cvt<T>(x[49]) + K[K_e5a]*nt_cvt<T>(x[52]) + K[K_e5b]*nt_cvt<T>(x[52]) + tj[J_bro];
+    const T D_r30_c4 = D_r27*D_r30_c2 + D_r28*tj[J_hobr] + D_r29*tj[J_brcl] + D_r30_c3*xt53 + K[K_e10]*xt43 + K[K_e3]*xt45 + K[K_e4]*xt49 + K[K_e5a]*xt52 + K[K_e5b]*xt52 + tj[J_bro];
     const T D_r30_c5 = D_r30_c4/(D_r30_c0*D_r30_c0);
     const T D_r30_c6 = D_r30_c1*D_r30_c2;
     const T D_r30 = D_r30_c1*D_r30_c4;
@@ -2138,79 +2462,79 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     const T d_D_r30_53 = D_r30_c1*D_r30_c3;
     {  // row 50
     const T rs50 = nt_rscale<T>(nt_exp_hi(x[50]), fh);
-        J[307] = (-d_D_r30_27*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs50);
-        J[311] = (-d_D_r30_43*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs50);
-        J[309] = (-d_D_r30_45*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs50);
-        J[313] = (-d_D_r30_46*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs50);
-        J[312] = (-d_D_r30_47*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs50);
-        J[308] = (-d_D_r30_48*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs50);
-        J[314] = (-d_D_r30_49*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs50);
-        J[315] = (-d_D_r30_52*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs50);
-        J[310] = (-D_r30 - d_D_r30_53*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs50);
+        J[307] = (-d_D_r30_27*xt53) * (cs27 * rs50);
+        J[311] = (-d_D_r30_43*xt53) * (cs43 * rs50);
+        J[309] = (-d_D_r30_45*xt53) * (cs45 * rs50);
+        J[313] = (-d_D_r30_46*xt53) * (cs46 * rs50);
+        J[312] = (-d_D_r30_47*xt53) * (cs47 * rs50);
+        J[308] = (-d_D_r30_48*xt53) * (cs48 * rs50);
+        J[314] = (-d_D_r30_49*xt53) * (cs49 * rs50);
+        J[315] = (-d_D_r30_52*xt53) * (cs52 * rs50);
+        J[310] = (-D_r30 - d_D_r30_53*xt53) * (cs53 * rs50);
     }
     {  // row 53
     const T rs53 = nt_rscale<T>(nt_exp_hi(x[53]), fh);
         const T dj53_c0 = D_r30 + T(1);
-        const T dj53_c1 = nt_cvt<T>(x[23])/(dj53_c0*dj53_c0);
-        J[297] = (-T(1)/dj53_c0) * (nt_scale<T>(nt_exp_hi(x[23]), fh) * rs53);
-        J[298] = (d_D_r30_27*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs53);
-        J[302] = (d_D_r30_43*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs53);
-        J[300] = (d_D_r30_45*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs53);
-        J[304] = (d_D_r30_46*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs53);
-        J[303] = (d_D_r30_47*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs53);
-        J[299] = (d_D_r30_48*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs53);
-        J[305] = (d_D_r30_49*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs53);
-        J[306] = (d_D_r30_52*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs53);
-        J[301] = (d_D_r30_53*dj53_c1 + T(1)) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs53);
+        const T dj53_c1 = xt23/(dj53_c0*dj53_c0);
+        J[297] = (-T(1)/dj53_c0) * (cs23 * rs53);
+        J[298] = (d_D_r30_27*dj53_c1) * (cs27 * rs53);
+        J[302] = (d_D_r30_43*dj53_c1) * (cs43 * rs53);
+        J[300] = (d_D_r30_45*dj53_c1) * (cs45 * rs53);
+        J[304] = (d_D_r30_46*dj53_c1) * (cs46 * rs53);
+        J[303] = (d_D_r30_47*dj53_c1) * (cs47 * rs53);
+        J[299] = (d_D_r30_48*dj53_c1) * (cs48 * rs53);
+        J[305] = (d_D_r30_49*dj53_c1) * (cs49 * rs53);
+        J[306] = (d_D_r30_52*dj53_c1) * (cs52 * rs53);
+        J[301] = (d_D_r30_53*dj53_c1 + T(1)) * (cs53 * rs53);
     }
-    const T D_t06_c0 = tj[J_hocl]*nt_cvt<T>(x[14]);
-    const T D_t06_c1 = K[K_d33]*nt_cvt<T>(x[52]);
-    const T D_t06_c2 = D_t06_c1*nt_cvt<T>(x[47]);
+    const T D_t06_c0 = tj[J_hocl]*xt14;
+    const T D_t06_c1 = K[K_d33]*xt52;
+    const T D_t06_c2 = D_t06_c1*xt47;
     const bool sel_D_t06 = (D_t06_c0) <= (D_t06_c2);
     const T D_t06 = sel_D_t06 ? T(D_t06_c0) : T(D_t06_c2);
     const T d_D_t06_14 = sel_D_t06 ? T(tj[J_hocl]) : T(T(0));
     const T d_D_t06_47 = sel_D_t06 ? T(T(0)) : T(D_t06_c1);
-    const T d_D_t06_52 = sel_D_t06 ? T(T(0)) : T(K[K_d33]*nt_cvt<T>(x[47]));
-    const T D_t07_c0 = K[K_e5c]*nt_cvt<T>(x[53]);
-    const T D_t07_c1 = D_t07_c0*nt_cvt<T>(x[52]);
-    const T D_t07_c2 = tj[J_brcl]*nt_cvt<T>(x[26]);
+    const T d_D_t06_52 = sel_D_t06 ? T(T(0)) : T(K[K_d33]*xt47);
+    const T D_t07_c0 = K[K_e5c]*xt53;
+    const T D_t07_c1 = D_t07_c0*xt52;
+    const T D_t07_c2 = tj[J_brcl]*xt26;
     const bool sel_D_t07 = (D_t07_c1) <= (D_t07_c2);
     const T D_t07 = sel_D_t07 ? T(D_t07_c1) : T(D_t07_c2);
     const T d_D_t07_26 = sel_D_t07 ? T(T(0)) : T(tj[J_brcl]);
     const T d_D_t07_52 = sel_D_t07 ? T(D_t07_c0) : T(T(0));
-    const T d_D_t07_53 = sel_D_t07 ? T(K[K_e5c]*nt_cvt<T>(x[52])) : T(T(0));
-    const T D_t09_c0 = K[K_e15]*nt_cvt<T>(x[53]);
-    const T D_t09_c1 = D_t09_c0*nt_cvt<T>(x[47]);
-    const T D_t09_c2 = tj[J_hobr]*nt_cvt<T>(x[25]);
+    const T d_D_t07_53 = sel_D_t07 ? T(K[K_e5c]*xt52) : T(T(0));
+    const T D_t09_c0 = K[K_e15]*xt53;
+    const T D_t09_c1 = D_t09_c0*xt47;
+    const T D_t09_c2 = tj[J_hobr]*xt25;
     const bool sel_D_t09 = (D_t09_c1) <= (D_t09_c2);
     const T D_t09 = sel_D_t09 ? T(D_t09_c1) : T(D_t09_c2);
     const T d_D_t09_25 = sel_D_t09 ? T(T(0)) : T(tj[J_hobr]);
     const T d_D_t09_47 = sel_D_t09 ? T(D_t09_c0) : T(T(0));
-    const T d_D_t09_53 = sel_D_t09 ? T(K[K_e15]*nt_cvt<T>(x[47])) : T(T(0));
+    const T d_D_t09_53 = sel_D_t09 ? T(K[K_e15]*xt47) : T(T(0));
     {  // row 7
     const T rs7 = nt_rscale<T>(nt_exp_hi(x[7]), fh);
         const T dj7_c0 = T(2)*F.dt;
         const T dj7_c1 = tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
-        const T dj7_c2 = F.dt*nt_cvt<T>(x[49]);
+        const T dj7_c2 = F.dt*xt49;
         const T dj7_c3 = T(2)*K[K_b3];
         const T dj7_c4 = T(2)*K[K_d3];
         const T dj7_c5 = T(2)*K[K_hk3];
         const T dj7_c6 = T(2)*K[K_b9]*dj7_c1;
         const T dj7_c7 = T(2)*K[K_e5b];
-        J[105] = (dj7_c0*dj7_c1*tj[J_clono2_cl]) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs7);
-        J[106] = (F.dt*d_D_t06_14) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs7);
-        J[104] = (F.dt*d_D_t09_25) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs7);
-        J[103] = (d_D_t07_26*dj7_c0) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs7);
-        J[108] = (-K[K_c5]*dj7_c2) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs7);
-        J[112] = (F.dt*(K[K_a5]*nt_cvt<T>(x[45]) + K[K_a6]*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs7);
-        J[110] = (F.dt*(K[K_a5]*nt_cvt<T>(x[43]) + K[K_a7]*nt_cvt<T>(x[47]) + T(4)*K[K_hk1]*nt_cvt<T>(x[45]) + dj7_c3*nt_cvt<T>(x[48]) + dj7_c4*nt_cvt<T>(x[52]) + dj7_c5*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs7);
-        J[114] = (F.dt*(K[K_a2]*nt_cvt<T>(x[55]) + K[K_a6]*nt_cvt<T>(x[43]) + K[K_a6b]*nt_cvt<T>(x[47]) + dj7_c5*nt_cvt<T>(x[45]) + dj7_c6*nt_cvt<T>(x[48]))) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs7);
-        J[113] = (F.dt*d_D_t06_47 + F.dt*d_D_t09_47 + F.dt*(K[K_a6b]*nt_cvt<T>(x[46]) + K[K_a7]*nt_cvt<T>(x[45])) - K[K_a26]*dj7_c2) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs7);
-        J[109] = (F.dt*(dj7_c3*nt_cvt<T>(x[45]) + dj7_c6*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs7);
-        J[115] = (-F.dt*(K[K_a26]*nt_cvt<T>(x[47]) + K[K_c5]*nt_cvt<T>(x[28]))) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs7);
-        J[116] = (F.dt*d_D_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*nt_cvt<T>(x[52])/(F.hnm*K[K_d61] + tj[J_cl2o2]) + dj7_c4*nt_cvt<T>(x[45]) + dj7_c7*nt_cvt<T>(x[53])) + d_D_t07_52*dj7_c0) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs7);
-        J[111] = (F.dt*d_D_t09_53 + F.dt*(T(4)*K[K_e6]*nt_cvt<T>(x[53]) + dj7_c7*nt_cvt<T>(x[52])) + d_D_t07_53*dj7_c0) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs7);
-        J[107] = (F.dt*K[K_a2]*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs7);
+        J[105] = (dj7_c0*dj7_c1*tj[J_clono2_cl]) * (cs13 * rs7);
+        J[106] = (F.dt*d_D_t06_14) * (cs14 * rs7);
+        J[104] = (F.dt*d_D_t09_25) * (cs25 * rs7);
+        J[103] = (d_D_t07_26*dj7_c0) * (cs26 * rs7);
+        J[108] = (-K[K_c5]*dj7_c2) * (cs28 * rs7);
+        J[112] = (F.dt*(K[K_a5]*xt45 + K[K_a6]*xt46)) * (cs43 * rs7);
+        J[110] = (F.dt*(K[K_a5]*xt43 + K[K_a7]*xt47 + T(4)*K[K_hk1]*xt45 + dj7_c3*xt48 + dj7_c4*xt52 + dj7_c5*xt46)) * (cs45 * rs7);
+        J[114] = (F.dt*(K[K_a2]*xt55 + K[K_a6]*xt43 + K[K_a6b]*xt47 + dj7_c5*xt45 + dj7_c6*xt48)) * (cs46 * rs7);
+        J[113] = (F.dt*d_D_t06_47 + F.dt*d_D_t09_47 + F.dt*(K[K_a6b]*xt46 + K[K_a7]*xt45) - K[K_a26]*dj7_c2) * (cs47 * rs7);
+        J[109] = (F.dt*(dj7_c3*xt45 + dj7_c6*xt46)) * (cs48 * rs7);
+        J[115] = (-F.dt*(K[K_a26]*xt47 + K[K_c5]*xt28)) * (cs49 * rs7);
+        J[116] = (F.dt*d_D_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*xt52/(F.hnm*K[K_d61] + tj[J_cl2o2]) + dj7_c4*xt45 + dj7_c7*xt53) + d_D_t07_52*dj7_c0) * (cs52 * rs7);
+        J[111] = (F.dt*d_D_t09_53 + F.dt*(T(4)*K[K_e6]*xt53 + dj7_c7*xt52) + d_D_t07_53*dj7_c0) * (cs53 * rs7);
+        J[107] = (F.dt*K[K_a2]*xt46) * (cs55 * rs7);
     }
 }
 
@@ -2264,29 +2588,112 @@ __device__ __forceinline__ void nt_residual_day_w4_0(const FF& F, PK K, PK tj, P
 template <typename T, typename FF, typename PK, typename PJ>
 __device__ __forceinline__ void nt_jacobian_day_w4_0(const FF& F, PK K, PK tj, PK het, const double* __restrict__ x, double floor_, PJ J) {
     const int fh = nt_exp_hi(floor_);
-    const T D_ch3o_c0 = K[K_c1b]*nt_cvt<T>(x[42]);
-    const T D_ch3o_c1 = K[K_c14]*nt_cvt<T>(x[28]);
-    const T D_ch3o_c2 = K[K_c18]*nt_cvt<T>(x[52]) + K[K_c5]*nt_cvt<T>(x[49]);
+    const T xt0 = nt_cvt<T>(x[0]);
+    const T xt1 = nt_cvt<T>(x[1]);
+    const T xt2 = nt_cvt<T>(x[2]);
+    const T xt3 = nt_cvt<T>(x[3]);
+    const T xt4 = nt_cvt<T>(x[4]);
+    const T xt5 = nt_cvt<T>(x[5]);
+    const T xt6 = nt_cvt<T>(x[6]);
+    const T xt7 = nt_cvt<T>(x[7]);
+    const T xt8 = nt_cvt<T>(x[8]);
+    const T xt9 = nt_cvt<T>(x[9]);
+    const T xt10 = nt_cvt<T>(x[10]);
+    const T xt11 = nt_cvt<T>(x[11]);
+    const T xt12 = nt_cvt<T>(x[12]);
+    const T xt13 = nt_cvt<T>(x[13]);
+    const T xt14 = nt_cvt<T>(x[14]);
+    const T xt15 = nt_cvt<T>(x[15]);
+    const T xt16 = nt_cvt<T>(x[16]);
+    const T xt17 = nt_cvt<T>(x[17]);
+    const T xt18 = nt_cvt<T>(x[18]);
+    const T xt19 = nt_cvt<T>(x[19]);
+    const T xt20 = nt_cvt<T>(x[20]);
+    const T xt21 = nt_cvt<T>(x[21]);
+    const T xt22 = nt_cvt<T>(x[22]);
+    const T xt23 = nt_cvt<T>(x[23]);
+    const T xt24 = nt_cvt<T>(x[24]);
+    const T xt25 = nt_cvt<T>(x[25]);
+    const T xt26 = nt_cvt<T>(x[26]);
+    const T xt27 = nt_cvt<T>(x[27]);
+    const T xt28 = nt_cvt<T>(x[28]);
+    const T xt29 = nt_cvt<T>(x[29]);
+    const T xt30 = nt_cvt<T>(x[30]);
+    const T xt31 = nt_cvt<T>(x[31]);
+    const T xt32 = nt_cvt<T>(x[32]);
+    const T xt33 = nt_cvt<T>(x[33]);
+    const T xt34 = nt_cvt<T>(x[34]);
+    const T xt35 = nt_cvt<T>(x[35]);
+    const T xt36 = nt_cvt<T>(x[36]);
+    const T xt37 = nt_cvt<T>(x[37]);
+    const T xt38 = nt_cvt<T>(x[38]);
+    const T xt39 = nt_cvt<T>(x[39]);
+    const T xt40 = nt_cvt<T>(x[40]);
+    const T xt41 = nt_cvt<T>(x[41]);
+    const T xt42 = nt_cvt<T>(x[42]);
+    const T xt43 = nt_cvt<T>(x[43]);
+    const T xt44 = nt_cvt<T>(x[44]);
+    const T xt45 = nt_cvt<T>(x[45]);
+    const T xt46 = nt_cvt<T>(x[46]);
+    const T xt47 = nt_cvt<T>(x[47]);
+    const T xt48 = nt_cvt<T>(x[48]);
+    const T xt49 = nt_cvt<T>(x[49]);
+    const T xt50 = nt_cvt<T>(x[50]);
+    const T xt51 = nt_cvt<T>(x[51]);
+    const T xt52 = nt_cvt<T>(x[52]);
+    const T xt53 = nt_cvt<T>(x[53]);
+    const T xt54 = nt_cvt<T>(x[54]);
+    const T xt55 = nt_cvt<T>(x[55]);
+    const T xt56 = nt_cvt<T>(x[56]);
+    const T cs1 = nt_scale<T>(nt_exp_hi(x[1]), fh);
+    const T cs2 = nt_scale<T>(nt_exp_hi(x[2]), fh);
+    const T cs4 = nt_scale<T>(nt_exp_hi(x[4]), fh);
+    const T cs8 = nt_scale<T>(nt_exp_hi(x[8]), fh);
+    const T cs12 = nt_scale<T>(nt_exp_hi(x[12]), fh);
+    const T cs14 = nt_scale<T>(nt_exp_hi(x[14]), fh);
+    const T cs16 = nt_scale<T>(nt_exp_hi(x[16]), fh);
+    const T cs18 = nt_scale<T>(nt_exp_hi(x[18]), fh);
+    const T cs21 = nt_scale<T>(nt_exp_hi(x[21]), fh);
+    const T cs25 = nt_scale<T>(nt_exp_hi(x[25]), fh);
+    const T cs27 = nt_scale<T>(nt_exp_hi(x[27]), fh);
+    const T cs28 = nt_scale<T>(nt_exp_hi(x[28]), fh);
+    const T cs29 = nt_scale<T>(nt_exp_hi(x[29]), fh);
+    const T cs42 = nt_scale<T>(nt_exp_hi(x[42]), fh);
+    const T cs43 = nt_scale<T>(nt_exp_hi(x[43]), fh);
+    const T cs44 = nt_scale<T>(nt_exp_hi(x[44]), fh);
+    const T cs45 = nt_scale<T>(nt_exp_hi(x[45]), fh);
+    const T cs46 = nt_scale<T>(nt_exp_hi(x[46]), fh);
+    const T cs47 = nt_scale<T>(nt_exp_hi(x[47]), fh);
+    const T cs48 = nt_scale<T>(nt_exp_hi(x[48]), fh);
+    const T cs49 = nt_scale<T>(nt_exp_hi(x[49]), fh);
+    const T cs50 = nt_scale<T>(nt_exp_hi(x[50]), fh);
+    const T cs52 = nt_scale<T>(nt_exp_hi(x[52]), fh);
+    const T cs53 = nt_scale<T>(nt_exp_hi(x[53]), fh);
+    const T cs55 = nt_scale<T>(nt_exp_hi(x[55]), fh);
+    const T cs56 = nt_scale<T>(nt_exp_hi(x[56]), fh);
+    const T D_ch3o_c0 = K[K_c1b]*xt42;
+    const T D_ch3o_c1 = K[K_c14]*xt28;
+    const T D_ch3o_c2 = K[K_c18]*xt52 + K[K_c5]*xt49;
     const T D_ch3o_c3 = T(1)/(F.o2*K[K_c15]);
-    const T D_ch3o_c4 = D_ch3o_c3*nt_cvt<T>(x[28]);
-    const T D_ch3o = D_ch3o_c3*(D_ch3o_c0*nt_cvt<T>(x[1]) + tj[J_ch3o2h]*nt_cvt<T>(x[29]) + nt_cvt<T>(x[28])*(T(2)*D_ch3o_c1 + D_ch3o_c2));
+    const T D_ch3o_c4 = D_ch3o_c3*xt28;
+    const T D_ch3o = D_ch3o_c3*(D_ch3o_c0*xt1 + tj[J_ch3o2h]*xt29 + xt28*(T(2)*D_ch3o_c1 + D_ch3o_c2));
     const T d_D_ch3o_1 = D_ch3o_c0*D_ch3o_c3;
     const T d_D_ch3o_28 = D_ch3o_c3*(T(4)*D_ch3o_c1 + D_ch3o_c2);
     const T d_D_ch3o_29 = D_ch3o_c3*tj[J_ch3o2h];
-    const T d_D_ch3o_42 = D_ch3o_c3*K[K_c1b]*nt_cvt<T>(x[1]);
+    const T d_D_ch3o_42 = D_ch3o_c3*K[K_c1b]*xt1;
     const T d_D_ch3o_49 = D_ch3o_c4*K[K_c5];
     const T d_D_ch3o_52 = D_ch3o_c4*K[K_c18];
     const T D_hco_c0 = T(1)/(F.o2*K[K_c12]);
-    const T D_hco_c1 = D_hco_c0*(K[K_c10]*nt_cvt<T>(x[44]) + K[K_c19]*nt_cvt<T>(x[50]) + K[K_c8]*nt_cvt<T>(x[43]) + K[K_c9]*nt_cvt<T>(x[45]) + tj[J_ch2o_hco]);
-    const T D_hco_c2 = D_hco_c0*nt_cvt<T>(x[27]);
-    const T D_hco = D_hco_c1*nt_cvt<T>(x[27]);
+    const T D_hco_c1 = D_hco_c0*(K[K_c10]*xt44 + K[K_c19]*xt50 + K[K_c8]*xt43 + K[K_c9]*xt45 + tj[J_ch2o_hco]);
+    const T D_hco_c2 = D_hco_c0*xt27;
+    const T D_hco = D_hco_c1*xt27;
     const T d_D_hco_27 = D_hco_c1;
     const T d_D_hco_43 = D_hco_c2*K[K_c8];
     const T d_D_hco_44 = D_hco_c2*K[K_c10];
     const T d_D_hco_45 = D_hco_c2*K[K_c9];
     const T d_D_hco_50 = D_hco_c2*K[K_c19];
-    const T D_r4_c0 = F.h2*K[K_a19] + K[K_a36]*nt_cvt<T>(x[8]) + K[K_a5]*nt_cvt<T>(x[45]);
-    const T D_r4_c1 = F.o2*K[K_a1] + K[K_a2]*nt_cvt<T>(x[46]) + T(8.049999999999999e-11)*nt_cvt<T>(x[47]);
+    const T D_r4_c0 = F.h2*K[K_a19] + K[K_a36]*xt8 + K[K_a5]*xt45;
+    const T D_r4_c1 = F.o2*K[K_a1] + K[K_a2]*xt46 + T(8.049999999999999e-11)*xt47;
     const T D_r4_c2 = (T(1)/(D_r4_c1));
     const T D_r4_c3 = D_r4_c0/(D_r4_c1*D_r4_c1);
     const T D_r4 = D_r4_c0*D_r4_c2;
@@ -2295,9 +2702,9 @@ __device__ __forceinline__ void nt_jacobian_day_w4_0(const FF& F, PK K, PK tj, P
     const T d_D_r4_46 = -D_r4_c3*K[K_a2];
     const T d_D_r4_47 = -T(8.049999999999999e-11)*D_r4_c3;
     const T D_r6_c0 = F.o2*K[K_a1];
-    const T D_r6_c1 = D_r4*D_r6_c0 + K[K_a30]*nt_cvt<T>(x[16]) + K[K_a6]*nt_cvt<T>(x[46]) + K[K_c8]*nt_cvt<T>(x[27]) + K[K_d8]*nt_cvt<T>(x[52]) + K[K_e10]*nt_cvt<T>(x[53]);
+    const T D_r6_c1 = D_r4*D_r6_c0 + K[K_a30]*xt16 + K[K_a6]*xt46 + K[K_c8]*xt27 + K[K_d8]*xt52 + K[K_e10]*xt53;
     const T D_r6_c2 = T(2)*K[K_a27];
-    const T D_r6_c3 = D_r6_c2*nt_cvt<T>(x[47]) + K[K_a17]*nt_cvt<T>(x[43]) + K[K_a26]*nt_cvt<T>(x[49]) + K[K_a6b]*nt_cvt<T>(x[46]) + K[K_a7]*nt_cvt<T>(x[45]) + K[K_d10]*nt_cvt<T>(x[44]) + K[K_d33]*nt_cvt<T>(x[52]) + K[K_d7]*nt_cvt<T>(x[44]) + K[K_e15]*nt_cvt<T>(x[53]) + K[K_e7]*nt_cvt<T>(x[50]) + T(8.049999999999999e-11)*nt_cvt<T>(x[55]);
+    const T D_r6_c3 = D_r6_c2*xt47 + K[K_a17]*xt43 + K[K_a26]*xt49 + K[K_a6b]*xt46 + K[K_a7]*xt45 + K[K_d10]*xt44 + K[K_d33]*xt52 + K[K_d7]*xt44 + K[K_e15]*xt53 + K[K_e7]*xt50 + T(8.049999999999999e-11)*xt55;
     const T D_r6_c4 = (T(1)/(D_r6_c3));
     const T D_r6_c5 = D_r6_c0*D_r6_c4;
     const T D_r6_c6 = D_r6_c1/(D_r6_c3*D_r6_c3);
@@ -2333,17 +2740,17 @@ __device__ __forceinline__ void nt_jacobian_day_w4_0(const FF& F, PK K, PK tj, P
     const T d_D_coea_52 = D_coea_c3*d_D_r6_52;
     const T d_D_coea_53 = D_coea_c3*d_D_r6_53;
     const T d_D_coea_55 = D_coea_c3*d_D_r6_55;
-    const T D_coeb_c0 = K[K_b23]*nt_cvt<T>(x[48]);
-    const T D_coeb_c1 = K[K_c7]*nt_cvt<T>(x[28]);
-    const T D_coeb_c2 = K[K_d33]*nt_cvt<T>(x[52]);
-    const T D_coeb_c3 = K[K_d7]*nt_cvt<T>(x[44]);
-    const T D_coeb_c4 = K[K_e15]*nt_cvt<T>(x[53]);
-    const T D_coeb_c5 = K[K_e7]*nt_cvt<T>(x[50]);
+    const T D_coeb_c0 = K[K_b23]*xt48;
+    const T D_coeb_c1 = K[K_c7]*xt28;
+    const T D_coeb_c2 = K[K_d33]*xt52;
+    const T D_coeb_c3 = K[K_d7]*xt44;
+    const T D_coeb_c4 = K[K_e15]*xt53;
+    const T D_coeb_c5 = K[K_e7]*xt50;
     const T D_coeb_c6 = F.parthbr*K[K_e11];
     const T D_coeb_c7 = F.parthcl*K[K_d11];
     const T D_coeb_c8 = F.parthno3*K[K_b27];
     const T D_coeb_c9 = D_coeb_c0 + D_coeb_c1 + D_coeb_c2 + D_coeb_c3 + D_coeb_c4 + D_coeb_c5;
-    const T D_coeb = D_coeb_c0*D_r6 + D_coeb_c1*D_r6 + D_coeb_c2*D_r6 + D_coeb_c3*D_r6 + D_coeb_c4*D_r6 + D_coeb_c5*D_r6 + D_coeb_c6*nt_cvt<T>(x[18]) + D_coeb_c7*nt_cvt<T>(x[12]) + D_coeb_c8*nt_cvt<T>(x[4]) + K[K_b22]*nt_cvt<T>(x[48]) + K[K_b28]*nt_cvt<T>(x[21]) + K[K_c17a]*nt_cvt<T>(x[29]) + K[K_c2]*nt_cvt<T>(x[1]) + K[K_c8]*nt_cvt<T>(x[27]) + K[K_d34]*nt_cvt<T>(x[14]) + K[K_d9]*nt_cvt<T>(x[52]);
+    const T D_coeb = D_coeb_c0*D_r6 + D_coeb_c1*D_r6 + D_coeb_c2*D_r6 + D_coeb_c3*D_r6 + D_coeb_c4*D_r6 + D_coeb_c5*D_r6 + D_coeb_c6*xt18 + D_coeb_c7*xt12 + D_coeb_c8*xt4 + K[K_b22]*xt48 + K[K_b28]*xt21 + K[K_c17a]*xt29 + K[K_c2]*xt1 + K[K_c8]*xt27 + K[K_d34]*xt14 + K[K_d9]*xt52;
     const T d_D_coeb_1 = K[K_c2];
     const T d_D_coeb_4 = D_coeb_c8;
     const T d_D_coeb_8 = D_coeb_c9*d_D_r6_8;
@@ -2371,17 +2778,17 @@ __device__ __forceinline__ void nt_jacobian_day_w4_0(const FF& F, PK K, PK tj, P
     const T D_coec_c2 = F.o2*K[K_c12];
     const T D_coec_c3 = F.h2*K[K_d6];
     const T D_coec_c4 = F.parthno3*tj[J_hno3];
-    const T D_coec_c5 = K[K_c3]*nt_cvt<T>(x[56]);
-    const T D_coec_c6 = K[K_e16]*nt_cvt<T>(x[45]);
+    const T D_coec_c5 = K[K_c3]*xt56;
+    const T D_coec_c6 = K[K_e16]*xt45;
     const T D_coec_c7 = F.hnm*K[K_b24] + tj[J_hno4];
-    const T D_coec_c8 = K[K_c9]*nt_cvt<T>(x[45]) + tj[J_ch2o_hco];
-    const T D_coec_c9 = K[K_d35]*nt_cvt<T>(x[45]) + K[K_d37]*nt_cvt<T>(x[44]) + tj[J_hocl];
+    const T D_coec_c8 = K[K_c9]*xt45 + tj[J_ch2o_hco];
+    const T D_coec_c9 = K[K_d35]*xt45 + K[K_d37]*xt44 + tj[J_hocl];
     const T D_coec_c10 = K[K_c1a] + K[K_c1b];
-    const T D_coec_c11 = D_coec_c10*nt_cvt<T>(x[1]) + T(2.4e-10)*F.h2;
+    const T D_coec_c11 = D_coec_c10*xt1 + T(2.4e-10)*F.h2;
     const T D_coec_c12 = T(2)*K[K_a1et];
-    const T D_coec_c13 = F.parth2o*(D_coec_c12*nt_cvt<T>(x[42]) + T(2)*tj[J_h2o]);
-    const T D_coec = D_ch3o*D_coec_c1 + D_coec_c0*nt_cvt<T>(x[16]) + D_coec_c11*nt_cvt<T>(x[42]) + D_coec_c13*nt_cvt<T>(x[2]) + D_coec_c2*D_hco + D_coec_c3*nt_cvt<T>(x[44]) + D_coec_c4*nt_cvt<T>(x[4]) + D_coec_c5*nt_cvt<T>(x[45]) + D_coec_c6*nt_cvt<T>(x[25]) + D_coec_c7*nt_cvt<T>(x[21]) + D_coec_c8*nt_cvt<T>(x[27]) + D_coec_c9*nt_cvt<T>(x[14]) + tj[J_ch3o2h]*nt_cvt<T>(x[29]) + tj[J_hbr]*nt_cvt<T>(x[18]) + tj[J_hobr]*nt_cvt<T>(x[25]);
-    const T d_D_coec_1 = D_coec_c1*d_D_ch3o_1 + D_coec_c10*nt_cvt<T>(x[42]);
+    const T D_coec_c13 = F.parth2o*(D_coec_c12*xt42 + T(2)*tj[J_h2o]);
+    const T D_coec = D_ch3o*D_coec_c1 + D_coec_c0*xt16 + D_coec_c11*xt42 + D_coec_c13*xt2 + D_coec_c2*D_hco + D_coec_c3*xt44 + D_coec_c4*xt4 + D_coec_c5*xt45 + D_coec_c6*xt25 + D_coec_c7*xt21 + D_coec_c8*xt27 + D_coec_c9*xt14 + tj[J_ch3o2h]*xt29 + tj[J_hbr]*xt18 + tj[J_hobr]*xt25;
+    const T d_D_coec_1 = D_coec_c1*d_D_ch3o_1 + D_coec_c10*xt42;
     const T d_D_coec_2 = D_coec_c13;
     const T d_D_coec_4 = D_coec_c4;
     const T d_D_coec_14 = D_coec_c9;
@@ -2392,14 +2799,14 @@ __device__ __forceinline__ void nt_jacobian_day_w4_0(const FF& F, PK K, PK tj, P
     const T d_D_coec_27 = D_coec_c2*d_D_hco_27 + D_coec_c8;
     const T d_D_coec_28 = D_coec_c1*d_D_ch3o_28;
     const T d_D_coec_29 = D_coec_c1*d_D_ch3o_29 + tj[J_ch3o2h];
-    const T d_D_coec_42 = D_coec_c1*d_D_ch3o_42 + D_coec_c11 + D_coec_c12*F.parth2o*nt_cvt<T>(x[2]);
+    const T d_D_coec_42 = D_coec_c1*d_D_ch3o_42 + D_coec_c11 + D_coec_c12*F.parth2o*xt2;
     const T d_D_coec_43 = D_coec_c2*d_D_hco_43;
-    const T d_D_coec_44 = D_coec_c2*d_D_hco_44 + D_coec_c3 + K[K_d37]*nt_cvt<T>(x[14]);
-    const T d_D_coec_45 = D_coec_c2*d_D_hco_45 + D_coec_c5 + K[K_c9]*nt_cvt<T>(x[27]) + K[K_d35]*nt_cvt<T>(x[14]) + K[K_e16]*nt_cvt<T>(x[25]);
+    const T d_D_coec_44 = D_coec_c2*d_D_hco_44 + D_coec_c3 + K[K_d37]*xt14;
+    const T d_D_coec_45 = D_coec_c2*d_D_hco_45 + D_coec_c5 + K[K_c9]*xt27 + K[K_d35]*xt14 + K[K_e16]*xt25;
     const T d_D_coec_49 = D_coec_c1*d_D_ch3o_49;
     const T d_D_coec_50 = D_coec_c2*d_D_hco_50;
     const T d_D_coec_52 = D_coec_c1*d_D_ch3o_52;
-    const T d_D_coec_56 = K[K_c3]*nt_cvt<T>(x[45]);
+    const T d_D_coec_56 = K[K_c3]*xt45;
     const T D_argum_c0 = T(4)*D_coea;
     const T D_argum_c1 = D_argum_c0*D_coec + (D_coeb*D_coeb);
     const T D_argum_c2 = T(2)*D_coeb;
@@ -2439,32 +2846,32 @@ __device__ __forceinline__ void nt_jacobian_day_w4_0(const FF& F, PK K, PK tj, P
         const T dj43_c2 = sqrt(D_argum);
         const T dj43_c3 = (T(0.25))*dj43_c0/dj43_c2;
         const T dj43_c4 = (T(0.5))*(-D_coeb + dj43_c2)/(D_coea*D_coea);
-        J[321] = (-d_D_argum_1*dj43_c3 + d_D_coeb_1*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs43);
-        J[331] = (-d_D_argum_2*dj43_c3) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs43);
-        J[319] = (-d_D_argum_4*dj43_c3 + d_D_coeb_4*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs43);
-        J[322] = (-d_D_argum_8*dj43_c3 + d_D_coea_8*dj43_c4 + d_D_coeb_8*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[8]), fh) * rs43);
-        J[330] = (-d_D_argum_12*dj43_c3 + d_D_coeb_12*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs43);
-        J[323] = (-d_D_argum_14*dj43_c3 + d_D_coeb_14*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs43);
-        J[326] = (-d_D_argum_16*dj43_c3 + d_D_coea_16*dj43_c4 + d_D_coeb_16*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs43);
-        J[325] = (-d_D_argum_18*dj43_c3 + d_D_coeb_18*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs43);
-        J[320] = (-d_D_argum_21*dj43_c3 + d_D_coeb_21*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[21]), fh) * rs43);
-        J[317] = (-d_D_argum_25*dj43_c3) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs43);
-        J[329] = (-d_D_argum_27*dj43_c3 + d_D_coea_27*dj43_c4 + d_D_coeb_27*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs43);
-        J[328] = (-d_D_argum_28*dj43_c3 + d_D_coeb_28*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs43);
-        J[316] = (-d_D_argum_29*dj43_c3 + d_D_coeb_29*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs43);
-        J[318] = (-d_D_argum_42*dj43_c3) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs43);
-        J[337] = (-d_D_argum_43*dj43_c3 + d_D_coea_43*dj43_c4 + d_D_coeb_43*dj43_c1 + T(1)) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs43);
-        J[334] = (-d_D_argum_44*dj43_c3 + d_D_coea_44*dj43_c4 + d_D_coeb_44*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs43);
-        J[333] = (-d_D_argum_45*dj43_c3 + d_D_coea_45*dj43_c4 + d_D_coeb_45*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs43);
-        J[339] = (-d_D_argum_46*dj43_c3 + d_D_coea_46*dj43_c4 + d_D_coeb_46*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs43);
-        J[338] = (-d_D_argum_47*dj43_c3 + d_D_coea_47*dj43_c4 + d_D_coeb_47*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs43);
-        J[332] = (-d_D_argum_48*dj43_c3 + d_D_coeb_48*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs43);
-        J[340] = (-d_D_argum_49*dj43_c3 + d_D_coea_49*dj43_c4 + d_D_coeb_49*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs43);
-        J[336] = (-d_D_argum_50*dj43_c3 + d_D_coea_50*dj43_c4 + d_D_coeb_50*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs43);
-        J[341] = (-d_D_argum_52*dj43_c3 + d_D_coea_52*dj43_c4 + d_D_coeb_52*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs43);
-        J[335] = (-d_D_argum_53*dj43_c3 + d_D_coea_53*dj43_c4 + d_D_coeb_53*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs43);
-        J[327] = (-d_D_argum_55*dj43_c3 + d_D_coea_55*dj43_c4 + d_D_coeb_55*dj43_c1) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs43);
-        J[324] = (-d_D_argum_56*dj43_c3) * (nt_scale<T>(nt_exp_hi(x[56]), fh) * rs43);
+        J[321] = (-d_D_argum_1*dj43_c3 + d_D_coeb_1*dj43_c1) * (cs1 * rs43);
+        J[331] = (-d_D_argum_2*dj43_c3) * (cs2 * rs43);
+        J[319] = (-d_D_argum_4*dj43_c3 + d_D_coeb_4*dj43_c1) * (cs4 * rs43);
+        J[322] = (-d_D_argum_8*dj43_c3 + d_D_coea_8*dj43_c4 + d_D_coeb_8*dj43_c1) * (cs8 * rs43);
+        J[330] = (-d_D_argum_12*dj43_c3 + d_D_coeb_12*dj43_c1) * (cs12 * rs43);
+        J[323] = (-d_D_argum_14*dj43_c3 + d_D_coeb_14*dj43_c1) * (cs14 * rs43);
+        J[326] = (-d_D_argum_16*dj43_c3 + d_D_coea_16*dj43_c4 + d_D_coeb_16*dj43_c1) * (cs16 * rs43);
+        J[325] = (-d_D_argum_18*dj43_c3 + d_D_coeb_18*dj43_c1) * (cs18 * rs43);
+        J[320] = (-d_D_argum_21*dj43_c3 + d_D_coeb_21*dj43_c1) * (cs21 * rs43);
+        J[317] = (-d_D_argum_25*dj43_c3) * (cs25 * rs43);
+        J[329] = (-d_D_argum_27*dj43_c3 + d_D_coea_27*dj43_c4 + d_D_coeb_27*dj43_c1) * (cs27 * rs43);
+        J[328] = (-d_D_argum_28*dj43_c3 + d_D_coeb_28*dj43_c1) * (cs28 * rs43);
+        J[316] = (-d_D_argum_29*dj43_c3 + d_D_coeb_29*dj43_c1) * (cs29 * rs43);
+        J[318] = (-d_D_argum_42*dj43_c3) * (cs42 * rs43);
+        J[337] = (-d_D_argum_43*dj43_c3 + d_D_coea_43*dj43_c4 + d_D_coeb_43*dj43_c1 + T(1)) * (cs43 * rs43);
+        J[334] = (-d_D_argum_44*dj43_c3 + d_D_coea_44*dj43_c4 + d_D_coeb_44*dj43_c1) * (cs44 * rs43);
+        J[333] = (-d_D_argum_45*dj43_c3 + d_D_coea_45*dj43_c4 + d_D_coeb_45*dj43_c1) * (cs45 * rs43);
+        J[339] = (-d_D_argum_46*dj43_c3 + d_D_coea_46*dj43_c4 + d_D_coeb_46*dj43_c1) * (cs46 * rs43);
+        J[338] = (-d_D_argum_47*dj43_c3 + d_D_coea_47*dj43_c4 + d_D_coeb_47*dj43_c1) * (cs47 * rs43);
+        J[332] = (-d_D_argum_48*dj43_c3 + d_D_coeb_48*dj43_c1) * (cs48 * rs43);
+        J[340] = (-d_D_argum_49*dj43_c3 + d_D_coea_49*dj43_c4 + d_D_coeb_49*dj43_c1) * (cs49 * rs43);
+        J[336] = (-d_D_argum_50*dj43_c3 + d_D_coea_50*dj43_c4 + d_D_coeb_50*dj43_c1) * (cs50 * rs43);
+        J[341] = (-d_D_argum_52*dj43_c3 + d_D_coea_52*dj43_c4 + d_D_coeb_52*dj43_c1) * (cs52 * rs43);
+        J[335] = (-d_D_argum_53*dj43_c3 + d_D_coea_53*dj43_c4 + d_D_coeb_53*dj43_c1) * (cs53 * rs43);
+        J[327] = (-d_D_argum_55*dj43_c3 + d_D_coea_55*dj43_c4 + d_D_coeb_55*dj43_c1) * (cs55 * rs43);
+        J[324] = (-d_D_argum_56*dj43_c3) * (cs56 * rs43);
     }
 }
 
@@ -2497,154 +2904,253 @@ __device__ __forceinline__ void nt_residual_day_w4_1(const FF& F, PK K, PK tj, P
 template <typename T, typename FF, typename PK, typename PJ>
 __device__ __forceinline__ void nt_jacobian_day_w4_1(const FF& F, PK K, PK tj, PK het, const double* __restrict__ x, double floor_, PJ J) {
     const int fh = nt_exp_hi(floor_);
+    const T xt0 = nt_cvt<T>(x[0]);
+    const T xt1 = nt_cvt<T>(x[1]);
+    const T xt2 = nt_cvt<T>(x[2]);
+    const T xt3 = nt_cvt<T>(x[3]);
+    const T xt4 = nt_cvt<T>(x[4]);
+    const T xt5 = nt_cvt<T>(x[5]);
+    const T xt6 = nt_cvt<T>(x[6]);
+    const T xt7 = nt_cvt<T>(x[7]);
+    const T xt8 = nt_cvt<T>(x[8]);
+    const T xt9 = nt_cvt<T>(x[9]);
+    const T xt10 = nt_cvt<T>(x[10]);
+    const T xt11 = nt_cvt<T>(x[11]);
+    const T xt12 = nt_cvt<T>(x[12]);
+    const T xt13 = nt_cvt<T>(x[13]);
+    const T xt14 = nt_cvt<T>(x[14]);
+    const T xt15 = nt_cvt<T>(x[15]);
+    const T xt16 = nt_cvt<T>(x[16]);
+    const T xt17 = nt_cvt<T>(x[17]);
+    const T xt18 = nt_cvt<T>(x[18]);
+    const T xt19 = nt_cvt<T>(x[19]);
+    const T xt20 = nt_cvt<T>(x[20]);
+    const T xt21 = nt_cvt<T>(x[21]);
+    const T xt22 = nt_cvt<T>(x[22]);
+    const T xt23 = nt_cvt<T>(x[23]);
+    const T xt24 = nt_cvt<T>(x[24]);
+    const T xt25 = nt_cvt<T>(x[25]);
+    const T xt26 = nt_cvt<T>(x[26]);
+    const T xt27 = nt_cvt<T>(x[27]);
+    const T xt28 = nt_cvt<T>(x[28]);
+    const T xt29 = nt_cvt<T>(x[29]);
+    const T xt30 = nt_cvt<T>(x[30]);
+    const T xt31 = nt_cvt<T>(x[31]);
+    const T xt32 = nt_cvt<T>(x[32]);
+    const T xt33 = nt_cvt<T>(x[33]);
+    const T xt34 = nt_cvt<T>(x[34]);
+    const T xt35 = nt_cvt<T>(x[35]);
+    const T xt36 = nt_cvt<T>(x[36]);
+    const T xt37 = nt_cvt<T>(x[37]);
+    const T xt38 = nt_cvt<T>(x[38]);
+    const T xt39 = nt_cvt<T>(x[39]);
+    const T xt40 = nt_cvt<T>(x[40]);
+    const T xt41 = nt_cvt<T>(x[41]);
+    const T xt42 = nt_cvt<T>(x[42]);
+    const T xt43 = nt_cvt<T>(x[43]);
+    const T xt44 = nt_cvt<T>(x[44]);
+    const T xt45 = nt_cvt<T>(x[45]);
+    const T xt46 = nt_cvt<T>(x[46]);
+    const T xt47 = nt_cvt<T>(x[47]);
+    const T xt48 = nt_cvt<T>(x[48]);
+    const T xt49 = nt_cvt<T>(x[49]);
+    const T xt50 = nt_cvt<T>(x[50]);
+    const T xt51 = nt_cvt<T>(x[51]);
+    const T xt52 = nt_cvt<T>(x[52]);
+    const T xt53 = nt_cvt<T>(x[53]);
+    const T xt54 = nt_cvt<T>(x[54]);
+    const T xt55 = nt_cvt<T>(x[55]);
+    const T xt56 = nt_cvt<T>(x[56]);
+    const T cs0 = nt_scale<T>(nt_exp_hi(x[0]), fh);
+    const T cs1 = nt_scale<T>(nt_exp_hi(x[1]), fh);
+    const T cs4 = nt_scale<T>(nt_exp_hi(x[4]), fh);
+    const T cs5 = nt_scale<T>(nt_exp_hi(x[5]), fh);
+    const T cs7 = nt_scale<T>(nt_exp_hi(x[7]), fh);
+    const T cs8 = nt_scale<T>(nt_exp_hi(x[8]), fh);
+    const T cs9 = nt_scale<T>(nt_exp_hi(x[9]), fh);
+    const T cs12 = nt_scale<T>(nt_exp_hi(x[12]), fh);
+    const T cs13 = nt_scale<T>(nt_exp_hi(x[13]), fh);
+    const T cs14 = nt_scale<T>(nt_exp_hi(x[14]), fh);
+    const T cs15 = nt_scale<T>(nt_exp_hi(x[15]), fh);
+    const T cs16 = nt_scale<T>(nt_exp_hi(x[16]), fh);
+    const T cs17 = nt_scale<T>(nt_exp_hi(x[17]), fh);
+    const T cs18 = nt_scale<T>(nt_exp_hi(x[18]), fh);
+    const T cs19 = nt_scale<T>(nt_exp_hi(x[19]), fh);
+    const T cs21 = nt_scale<T>(nt_exp_hi(x[21]), fh);
+    const T cs24 = nt_scale<T>(nt_exp_hi(x[24]), fh);
+    const T cs25 = nt_scale<T>(nt_exp_hi(x[25]), fh);
+    const T cs26 = nt_scale<T>(nt_exp_hi(x[26]), fh);
+    const T cs27 = nt_scale<T>(nt_exp_hi(x[27]), fh);
+    const T cs30 = nt_scale<T>(nt_exp_hi(x[30]), fh);
+    const T cs31 = nt_scale<T>(nt_exp_hi(x[31]), fh);
+    const T cs32 = nt_scale<T>(nt_exp_hi(x[32]), fh);
+    const T cs33 = nt_scale<T>(nt_exp_hi(x[33]), fh);
+    const T cs34 = nt_scale<T>(nt_exp_hi(x[34]), fh);
+    const T cs35 = nt_scale<T>(nt_exp_hi(x[35]), fh);
+    const T cs36 = nt_scale<T>(nt_exp_hi(x[36]), fh);
+    const T cs39 = nt_scale<T>(nt_exp_hi(x[39]), fh);
+    const T cs42 = nt_scale<T>(nt_exp_hi(x[42]), fh);
+    const T cs43 = nt_scale<T>(nt_exp_hi(x[43]), fh);
+    const T cs44 = nt_scale<T>(nt_exp_hi(x[44]), fh);
+    const T cs45 = nt_scale<T>(nt_exp_hi(x[45]), fh);
+    const T cs46 = nt_scale<T>(nt_exp_hi(x[46]), fh);
+    const T cs47 = nt_scale<T>(nt_exp_hi(x[47]), fh);
+    const T cs48 = nt_scale<T>(nt_exp_hi(x[48]), fh);
+    const T cs49 = nt_scale<T>(nt_exp_hi(x[49]), fh);
+    const T cs50 = nt_scale<T>(nt_exp_hi(x[50]), fh);
+    const T cs51 = nt_scale<T>(nt_exp_hi(x[51]), fh);
+    const T cs52 = nt_scale<T>(nt_exp_hi(x[52]), fh);
+    const T cs53 = nt_scale<T>(nt_exp_hi(x[53]), fh);
+    const T cs54 = nt_scale<T>(nt_exp_hi(x[54]), fh);
+    const T cs55 = nt_scale<T>(nt_exp_hi(x[55]), fh);
     {  // row 1
     const T rs1 = nt_rscale<T>(nt_exp_hi(x[1]), fh);
-        const T dj1_c0 = F.dt*nt_cvt<T>(x[1]);
-        J[157] = (F.dt*(K[K_c1a]*nt_cvt<T>(x[42]) + K[K_c1b]*nt_cvt<T>(x[42]) + K[K_c1c]*nt_cvt<T>(x[42]) + K[K_c2]*nt_cvt<T>(x[43]) + K[K_d5]*nt_cvt<T>(x[44])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs1);
-        J[156] = (dj1_c0*(K[K_c1a] + K[K_c1b] + K[K_c1c])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs1);
-        J[159] = (K[K_c2]*dj1_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs1);
-        J[158] = (K[K_d5]*dj1_c0) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs1);
+        const T dj1_c0 = F.dt*xt1;
+        J[157] = (F.dt*(K[K_c1a]*xt42 + K[K_c1b]*xt42 + K[K_c1c]*xt42 + K[K_c2]*xt43 + K[K_d5]*xt44) + T(1)) * (cs1 * rs1);
+        J[156] = (dj1_c0*(K[K_c1a] + K[K_c1b] + K[K_c1c])) * (cs42 * rs1);
+        J[159] = (K[K_c2]*dj1_c0) * (cs43 * rs1);
+        J[158] = (K[K_d5]*dj1_c0) * (cs44 * rs1);
     }
     {  // row 3
     const T rs3 = nt_rscale<T>(nt_exp_hi(x[3]), fh);
         const T dj3_c0 = T(2)*F.dt;
         const T dj3_c1 = K[K_b39]*dj3_c0;
         const T dj3_c2 = K[K_b6]*dj3_c0;
-        J[20] = (-dj3_c1*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs3);
-        J[23] = (F.dt*F.rain_hno3) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs3);
-        J[22] = (-dj3_c1*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs3);
-        J[24] = (dj3_c2*nt_cvt<T>(x[51])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs3);
-        J[21] = (dj3_c2*nt_cvt<T>(x[49])) * (nt_scale<T>(nt_exp_hi(x[51]), fh) * rs3);
+        J[20] = (-dj3_c1*xt42) * (cs0 * rs3);
+        J[23] = (F.dt*F.rain_hno3) * (cs4 * rs3);
+        J[22] = (-dj3_c1*xt0) * (cs42 * rs3);
+        J[24] = (dj3_c2*xt51) * (cs49 * rs3);
+        J[21] = (dj3_c2*xt49) * (cs51 * rs3);
     }
     {  // row 9
     const T rs9 = nt_rscale<T>(nt_exp_hi(x[9]), fh);
         const T dj9_c0 = F.dt*K[K_e5a];
-        J[100] = (F.dt*tj[J_oclo] + T(1)) * (nt_scale<T>(nt_exp_hi(x[9]), fh) * rs9);
-        J[102] = (-dj9_c0*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs9);
-        J[101] = (-dj9_c0*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs9);
+        J[100] = (F.dt*tj[J_oclo] + T(1)) * (cs9 * rs9);
+        J[102] = (-dj9_c0*xt53) * (cs52 * rs9);
+        J[101] = (-dj9_c0*xt52) * (cs53 * rs9);
     }
     {  // row 15
     const T rs15 = nt_rscale<T>(nt_exp_hi(x[15]), fh);
-        J[63] = (-F.dt*(het[1]*nt_cvt<T>(x[13]) + het[4]*nt_cvt<T>(x[14]))) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs15);
-        J[61] = (-F.dt*het[1]*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs15);
-        J[62] = (-F.dt*(K[K_d37]*nt_cvt<T>(x[44]) + het[4]*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs15);
-        J[60] = (F.dt*tj[J_cl2] + T(1)) * (nt_scale<T>(nt_exp_hi(x[15]), fh) * rs15);
-        J[64] = (-F.dt*K[K_d37]*nt_cvt<T>(x[14])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs15);
-        J[65] = (-T(2)*F.dt*K[K_d62]*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs15);
+        J[63] = (-F.dt*(het[1]*xt13 + het[4]*xt14)) * (cs12 * rs15);
+        J[61] = (-F.dt*het[1]*xt12) * (cs13 * rs15);
+        J[62] = (-F.dt*(K[K_d37]*xt44 + het[4]*xt12)) * (cs14 * rs15);
+        J[60] = (F.dt*tj[J_cl2] + T(1)) * (cs15 * rs15);
+        J[64] = (-F.dt*K[K_d37]*xt14) * (cs44 * rs15);
+        J[65] = (-T(2)*F.dt*K[K_d62]*xt52) * (cs52 * rs15);
     }
     {  // row 17
     const T rs17 = nt_rscale<T>(nt_exp_hi(x[17]), fh);
         const T dj17_c0 = F.dt*het[3];
         const T dj17_c1 = F.dt*K[K_d36];
-        J[26] = (-dj17_c0*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs17);
-        J[27] = (-dj17_c0*nt_cvt<T>(x[5])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs17);
-        J[25] = (F.dt*tj[J_clno2] + T(1)) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs17);
-        J[29] = (-dj17_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs17);
-        J[28] = (-dj17_c1*nt_cvt<T>(x[44])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs17);
+        J[26] = (-dj17_c0*xt12) * (cs5 * rs17);
+        J[27] = (-dj17_c0*xt5) * (cs12 * rs17);
+        J[25] = (F.dt*tj[J_clno2] + T(1)) * (cs17 * rs17);
+        J[29] = (-dj17_c1*xt48) * (cs44 * rs17);
+        J[28] = (-dj17_c1*xt44) * (cs48 * rs17);
     }
     {  // row 18
     const T rs18 = nt_rscale<T>(nt_exp_hi(x[18]), fh);
-        const T dj18_c0 = F.dt*nt_cvt<T>(x[18]);
-        const T dj18_c1 = F.dt*nt_cvt<T>(x[50]);
+        const T dj18_c0 = F.dt*xt18;
+        const T dj18_c1 = F.dt*xt50;
         const T dj18_c2 = F.parthbr*dj18_c0;
-        J[183] = (dj18_c0*het[8]) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs18);
-        J[184] = (F.dt*(F.parthbr*(K[K_e11]*nt_cvt<T>(x[43]) + K[K_e9]*nt_cvt<T>(x[42]) + tj[J_hbr]) + F.rain_hbr + het[7]*nt_cvt<T>(x[25]) + het[8]*nt_cvt<T>(x[14])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs18);
-        J[181] = (dj18_c0*het[7]) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs18);
-        J[185] = (-K[K_c19]*dj18_c1) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs18);
-        J[182] = (K[K_e9]*dj18_c2) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs18);
-        J[187] = (K[K_e11]*dj18_c2) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs18);
-        J[188] = (-K[K_e7]*dj18_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs18);
-        J[186] = (-F.dt*(K[K_c19]*nt_cvt<T>(x[27]) + K[K_e7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs18);
+        J[183] = (dj18_c0*het[8]) * (cs14 * rs18);
+        J[184] = (F.dt*(F.parthbr*(K[K_e11]*xt43 + K[K_e9]*xt42 + tj[J_hbr]) + F.rain_hbr + het[7]*xt25 + het[8]*xt14) + T(1)) * (cs18 * rs18);
+        J[181] = (dj18_c0*het[7]) * (cs25 * rs18);
+        J[185] = (-K[K_c19]*dj18_c1) * (cs27 * rs18);
+        J[182] = (K[K_e9]*dj18_c2) * (cs42 * rs18);
+        J[187] = (K[K_e11]*dj18_c2) * (cs43 * rs18);
+        J[188] = (-K[K_e7]*dj18_c1) * (cs47 * rs18);
+        J[186] = (-F.dt*(K[K_c19]*xt27 + K[K_e7]*xt47)) * (cs50 * rs18);
     }
     {  // row 20
     const T rs20 = nt_rscale<T>(nt_exp_hi(x[20]), fh);
         const T dj20_c0 = T(2)*F.dt;
         const T dj20_c1 = K[K_b39]*dj20_c0;
         const T dj20_c2 = F.parthno3*K[K_b27];
-        const T dj20_c3 = F.dt*nt_cvt<T>(x[48]);
+        const T dj20_c3 = F.dt*xt48;
         const T dj20_c4 = T(2)*K[K_b12];
         const T dj20_c5 = K[K_b6]*dj20_c0;
-        J[233] = (-dj20_c1*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs20);
-        J[237] = (-F.dt*(F.parthno3*tj[J_hno3] + dj20_c2*nt_cvt<T>(x[43]))) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs20);
-        J[232] = (-F.dt*(T(2)*F.hnm*K[K_b32] + T(2)*tj[J_n2o5])) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs20);
-        J[235] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + tj[J_clono2_cl] + tj[J_clono2_clo])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs20);
-        J[229] = (-F.dt*tj[J_clno2]) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs20);
-        J[230] = (-F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + tj[J_brono2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs20);
-        J[238] = (-F.dt*(F.hnm*K[K_b24] + K[K_b28]*nt_cvt<T>(x[43]) + tj[J_hno4])) * (nt_scale<T>(nt_exp_hi(x[21]), fh) * rs20);
-        J[236] = (-dj20_c1*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs20);
-        J[243] = (-F.dt*(K[K_b28]*nt_cvt<T>(x[21]) + dj20_c2*nt_cvt<T>(x[4])) + K[K_b22]*dj20_c3) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs20);
-        J[241] = (K[K_d36]*dj20_c3) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs20);
-        J[240] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[13]) + K[K_e8]*nt_cvt<T>(x[19]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs20);
-        J[244] = (K[K_b23]*dj20_c3) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs20);
-        J[239] = (F.dt*(K[K_b22]*nt_cvt<T>(x[43]) + K[K_b23]*nt_cvt<T>(x[47]) + K[K_d31]*nt_cvt<T>(x[52]) + K[K_d36]*nt_cvt<T>(x[44]) + K[K_e13]*nt_cvt<T>(x[53]) + dj20_c4*nt_cvt<T>(x[54]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs20);
-        J[245] = (dj20_c5*nt_cvt<T>(x[51])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs20);
-        J[234] = (dj20_c5*nt_cvt<T>(x[49])) * (nt_scale<T>(nt_exp_hi(x[51]), fh) * rs20);
-        J[246] = (K[K_d31]*dj20_c3) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs20);
-        J[242] = (K[K_e13]*dj20_c3) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs20);
-        J[231] = (dj20_c3*dj20_c4) * (nt_scale<T>(nt_exp_hi(x[54]), fh) * rs20);
+        J[233] = (-dj20_c1*xt42) * (cs0 * rs20);
+        J[237] = (-F.dt*(F.parthno3*tj[J_hno3] + dj20_c2*xt43)) * (cs4 * rs20);
+        J[232] = (-F.dt*(T(2)*F.hnm*K[K_b32] + T(2)*tj[J_n2o5])) * (cs5 * rs20);
+        J[235] = (-F.dt*(K[K_d32]*xt45 + tj[J_clono2_cl] + tj[J_clono2_clo])) * (cs13 * rs20);
+        J[229] = (-F.dt*tj[J_clno2]) * (cs17 * rs20);
+        J[230] = (-F.dt*(K[K_e8]*xt45 + tj[J_brono2])) * (cs19 * rs20);
+        J[238] = (-F.dt*(F.hnm*K[K_b24] + K[K_b28]*xt43 + tj[J_hno4])) * (cs21 * rs20);
+        J[236] = (-dj20_c1*xt0) * (cs42 * rs20);
+        J[243] = (-F.dt*(K[K_b28]*xt21 + dj20_c2*xt4) + K[K_b22]*dj20_c3) * (cs43 * rs20);
+        J[241] = (K[K_d36]*dj20_c3) * (cs44 * rs20);
+        J[240] = (-F.dt*(K[K_d32]*xt13 + K[K_e8]*xt19)) * (cs45 * rs20);
+        J[244] = (K[K_b23]*dj20_c3) * (cs47 * rs20);
+        J[239] = (F.dt*(K[K_b22]*xt43 + K[K_b23]*xt47 + K[K_d31]*xt52 + K[K_d36]*xt44 + K[K_e13]*xt53 + dj20_c4*xt54)) * (cs48 * rs20);
+        J[245] = (dj20_c5*xt51) * (cs49 * rs20);
+        J[234] = (dj20_c5*xt49) * (cs51 * rs20);
+        J[246] = (K[K_d31]*dj20_c3) * (cs52 * rs20);
+        J[242] = (K[K_e13]*dj20_c3) * (cs53 * rs20);
+        J[231] = (dj20_c3*dj20_c4) * (cs54 * rs20);
     }
     {  // row 22
     const T rs22 = nt_rscale<T>(nt_exp_hi(x[22]), fh);
-        const T dj22_c0 = F.dt*nt_cvt<T>(x[44]);
-        const T dj22_c1 = T(3)*nt_cvt<T>(x[42]);
+        const T dj22_c0 = F.dt*xt44;
+        const T dj22_c1 = T(3)*xt42;
         const T dj22_c2 = T(2)*K[K_d91];
         const T dj22_c3 = T(4)*K[K_d93];
         const T dj22_c4 = T(3)*K[K_d94];
-        const T dj22_c5 = F.dt*nt_cvt<T>(x[52]);
+        const T dj22_c5 = F.dt*xt52;
         const T dj22_c6 = T(2)*K[K_d60];
         const T dj22_c7 = T(2)*K[K_d62];
-        J[141] = (K[K_d5]*dj22_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs22);
-        J[140] = (-F.dt*tj[J_oclo]) * (nt_scale<T>(nt_exp_hi(x[9]), fh) * rs22);
-        J[144] = (-F.dt*F.parthcl*(K[K_d11]*nt_cvt<T>(x[43]) + tj[J_hcl])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs22);
-        J[135] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + tj[J_clono2_cl] + tj[J_clono2_clo])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs22);
-        J[142] = (-F.dt*(K[K_d34]*nt_cvt<T>(x[43]) + K[K_d35]*nt_cvt<T>(x[45]) + tj[J_hocl]) + K[K_d37]*dj22_c0) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs22);
-        J[133] = (-T(2)*F.dt*tj[J_cl2]) * (nt_scale<T>(nt_exp_hi(x[15]), fh) * rs22);
-        J[128] = (-F.dt*tj[J_clno2]) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs22);
-        J[138] = (-F.dt*(T(2)*F.hnm*K[K_d61] + T(2)*tj[J_cl2o2])) * (nt_scale<T>(nt_exp_hi(x[24]), fh) * rs22);
-        J[132] = (-F.dt*tj[J_brcl]) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs22);
-        J[143] = (K[K_c10]*dj22_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs22);
-        J[137] = (-F.dt*(K[K_d90]*dj22_c1 + T(3)*tj[J_cfc11])) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs22);
-        J[131] = (-F.dt*(dj22_c2*nt_cvt<T>(x[42]) + T(2)*tj[J_cfc12])) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs22);
-        J[127] = (-F.dt*(K[K_d92]*dj22_c1 + T(3)*tj[J_cfc113])) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs22);
-        J[129] = (-F.dt*(dj22_c3*nt_cvt<T>(x[42]) + T(4)*tj[J_ccl4])) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs22);
-        J[136] = (-F.dt*(dj22_c4*nt_cvt<T>(x[43]) + T(3)*tj[J_ch3ccl3])) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs22);
-        J[134] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl])) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs22);
-        J[130] = (-F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22])) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs22);
-        J[139] = (-F.dt*(T(3)*K[K_d90]*nt_cvt<T>(x[30]) + T(3)*K[K_d92]*nt_cvt<T>(x[32]) + K[K_d96]*nt_cvt<T>(x[36]) + dj22_c2*nt_cvt<T>(x[31]) + dj22_c3*nt_cvt<T>(x[33]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs22);
-        J[149] = (-F.dt*(F.parthcl*K[K_d11]*nt_cvt<T>(x[12]) + K[K_d34]*nt_cvt<T>(x[14]) + K[K_d95]*nt_cvt<T>(x[35]) + K[K_d97]*nt_cvt<T>(x[36]) + dj22_c4*nt_cvt<T>(x[34])) + K[K_d9]*dj22_c5) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs22);
-        J[147] = (F.dt*(F.h2*K[K_d6] + K[K_c10]*nt_cvt<T>(x[27]) + K[K_d36]*nt_cvt<T>(x[48]) + K[K_d37]*nt_cvt<T>(x[14]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs22);
-        J[146] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[13]) + K[K_d35]*nt_cvt<T>(x[14]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs22);
-        J[150] = (F.dt*(K[K_d33]*nt_cvt<T>(x[52]) + K[K_d7]*nt_cvt<T>(x[44]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs22);
-        J[145] = (F.dt*(K[K_d31]*nt_cvt<T>(x[52]) + K[K_d36]*nt_cvt<T>(x[44]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs22);
-        J[151] = (F.dt*(K[K_d31]*nt_cvt<T>(x[48]) + K[K_d33]*nt_cvt<T>(x[47]) + K[K_d9]*nt_cvt<T>(x[43]) + K[K_e5a]*nt_cvt<T>(x[53]) + K[K_e5c]*nt_cvt<T>(x[53]) + dj22_c6*nt_cvt<T>(x[52]) + dj22_c7*nt_cvt<T>(x[52]) + nt_cvt<T>(x[52])*(dj22_c6 + dj22_c7))) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs22);
-        J[148] = (dj22_c5*(K[K_e5a] + K[K_e5c])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs22);
+        J[141] = (K[K_d5]*dj22_c0) * (cs1 * rs22);
+        J[140] = (-F.dt*tj[J_oclo]) * (cs9 * rs22);
+        J[144] = (-F.dt*F.parthcl*(K[K_d11]*xt43 + tj[J_hcl])) * (cs12 * rs22);
+        J[135] = (-F.dt*(K[K_d32]*xt45 + tj[J_clono2_cl] + tj[J_clono2_clo])) * (cs13 * rs22);
+        J[142] = (-F.dt*(K[K_d34]*xt43 + K[K_d35]*xt45 + tj[J_hocl]) + K[K_d37]*dj22_c0) * (cs14 * rs22);
+        J[133] = (-T(2)*F.dt*tj[J_cl2]) * (cs15 * rs22);
+        J[128] = (-F.dt*tj[J_clno2]) * (cs17 * rs22);
+        J[138] = (-F.dt*(T(2)*F.hnm*K[K_d61] + T(2)*tj[J_cl2o2])) * (cs24 * rs22);
+        J[132] = (-F.dt*tj[J_brcl]) * (cs26 * rs22);
+        J[143] = (K[K_c10]*dj22_c0) * (cs27 * rs22);
+        J[137] = (-F.dt*(K[K_d90]*dj22_c1 + T(3)*tj[J_cfc11])) * (cs30 * rs22);
+        J[131] = (-F.dt*(dj22_c2*xt42 + T(2)*tj[J_cfc12])) * (cs31 * rs22);
+        J[127] = (-F.dt*(K[K_d92]*dj22_c1 + T(3)*tj[J_cfc113])) * (cs32 * rs22);
+        J[129] = (-F.dt*(dj22_c3*xt42 + T(4)*tj[J_ccl4])) * (cs33 * rs22);
+        J[136] = (-F.dt*(dj22_c4*xt43 + T(3)*tj[J_ch3ccl3])) * (cs34 * rs22);
+        J[134] = (-F.dt*(K[K_d95]*xt43 + tj[J_ch3cl])) * (cs35 * rs22);
+        J[130] = (-F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22])) * (cs36 * rs22);
+        J[139] = (-F.dt*(T(3)*K[K_d90]*xt30 + T(3)*K[K_d92]*xt32 + K[K_d96]*xt36 + dj22_c2*xt31 + dj22_c3*xt33)) * (cs42 * rs22);
+        J[149] = (-F.dt*(F.parthcl*K[K_d11]*xt12 + K[K_d34]*xt14 + K[K_d95]*xt35 + K[K_d97]*xt36 + dj22_c4*xt34) + K[K_d9]*dj22_c5) * (cs43 * rs22);
+        J[147] = (F.dt*(F.h2*K[K_d6] + K[K_c10]*xt27 + K[K_d36]*xt48 + K[K_d37]*xt14 + K[K_d5]*xt1 + K[K_d7]*xt47)) * (cs44 * rs22);
+        J[146] = (-F.dt*(K[K_d32]*xt13 + K[K_d35]*xt14)) * (cs45 * rs22);
+        J[150] = (F.dt*(K[K_d33]*xt52 + K[K_d7]*xt44)) * (cs47 * rs22);
+        J[145] = (F.dt*(K[K_d31]*xt52 + K[K_d36]*xt44)) * (cs48 * rs22);
+        J[151] = (F.dt*(K[K_d31]*xt48 + K[K_d33]*xt47 + K[K_d9]*xt43 + K[K_e5a]*xt53 + K[K_e5c]*xt53 + dj22_c6*xt52 + dj22_c7*xt52 + xt52*(dj22_c6 + dj22_c7))) * (cs52 * rs22);
+        J[148] = (dj22_c5*(K[K_e5a] + K[K_e5c])) * (cs53 * rs22);
     }
     {  // row 31
     const T rs31 = nt_rscale<T>(nt_exp_hi(x[31]), fh);
-        J[41] = (F.dt*(K[K_d91]*nt_cvt<T>(x[42]) + tj[J_cfc12]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs31);
-        J[42] = (F.dt*K[K_d91]*nt_cvt<T>(x[31])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs31);
+        J[41] = (F.dt*(K[K_d91]*xt42 + tj[J_cfc12]) + T(1)) * (cs31 * rs31);
+        J[42] = (F.dt*K[K_d91]*xt31) * (cs42 * rs31);
     }
     {  // row 34
     const T rs34 = nt_rscale<T>(nt_exp_hi(x[34]), fh);
-        J[93] = (F.dt*(K[K_d94]*nt_cvt<T>(x[43]) + tj[J_ch3ccl3]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs34);
-        J[94] = (F.dt*K[K_d94]*nt_cvt<T>(x[34])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs34);
+        J[93] = (F.dt*(K[K_d94]*xt43 + tj[J_ch3ccl3]) + T(1)) * (cs34 * rs34);
+        J[94] = (F.dt*K[K_d94]*xt34) * (cs43 * rs34);
     }
     {  // row 36
     const T rs36 = nt_rscale<T>(nt_exp_hi(x[36]), fh);
-        const T dj36_c0 = F.dt*nt_cvt<T>(x[36]);
-        J[38] = (F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs36);
-        J[39] = (K[K_d96]*dj36_c0) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs36);
-        J[40] = (K[K_d97]*dj36_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs36);
+        const T dj36_c0 = F.dt*xt36;
+        J[38] = (F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22]) + T(1)) * (cs36 * rs36);
+        J[39] = (K[K_d96]*dj36_c0) * (cs42 * rs36);
+        J[40] = (K[K_d97]*dj36_c0) * (cs43 * rs36);
     }
     {  // row 39
     const T rs39 = nt_rscale<T>(nt_exp_hi(x[39]), fh);
-        J[50] = (F.dt*(K[K_e53]*nt_cvt<T>(x[42]) + tj[J_h1301]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[39]), fh) * rs39);
-        J[51] = (F.dt*K[K_e53]*nt_cvt<T>(x[39])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs39);
+        J[50] = (F.dt*(K[K_e53]*xt42 + tj[J_h1301]) + T(1)) * (cs39 * rs39);
+        J[51] = (F.dt*K[K_e53]*xt39) * (cs42 * rs39);
     }
     const T D_hco_c0 = T(1)/(F.o2*K[K_c12]);
-    const T D_hco_c1 = D_hco_c0*(K[K_c10]*nt_cvt<T>(x[44]) + K[K_c19]*nt_cvt<T>(x[50]) + K[K_c8]*nt_cvt<T>(x[43]) + K[K_c9]*nt_cvt<T>(x[45]) + tj[J_ch2o_hco]);
-    const T D_hco_c2 = D_hco_c0*nt_cvt<T>(x[27]);
-    const T D_hco = D_hco_c1*nt_cvt<T>(x[27]);
+    const T D_hco_c1 = D_hco_c0*(K[K_c10]*xt44 + K[K_c19]*xt50 + K[K_c8]*xt43 + K[K_c9]*xt45 + tj[J_ch2o_hco]);
+    const T D_hco_c2 = D_hco_c0*xt27;
+    const T D_hco = D_hco_c1*xt27;
     const T d_D_hco_27 = D_hco_c1;
     const T d_D_hco_43 = D_hco_c2*K[K_c8];
     const T d_D_hco_44 = D_hco_c2*K[K_c10];
@@ -2653,15 +3159,15 @@ __device__ __forceinline__ void nt_jacobian_day_w4_1(const FF& F, PK K, PK tj, P
     {  // row 8
     const T rs8 = nt_rscale<T>(nt_exp_hi(x[8]), fh);
         const T dj8_c0 = F.dt*F.o2*K[K_c12];
-        J[160] = (F.dt*K[K_a36]*nt_cvt<T>(x[43]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[8]), fh) * rs8);
-        J[161] = (-F.dt*tj[J_ch2o_co] - d_D_hco_27*dj8_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs8);
-        J[165] = (F.dt*K[K_a36]*nt_cvt<T>(x[8]) - d_D_hco_43*dj8_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs8);
-        J[163] = (-d_D_hco_44*dj8_c0) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs8);
-        J[162] = (-d_D_hco_45*dj8_c0) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs8);
-        J[164] = (-d_D_hco_50*dj8_c0) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs8);
+        J[160] = (F.dt*K[K_a36]*xt43 + T(1)) * (cs8 * rs8);
+        J[161] = (-F.dt*tj[J_ch2o_co] - d_D_hco_27*dj8_c0) * (cs27 * rs8);
+        J[165] = (F.dt*K[K_a36]*xt8 - d_D_hco_43*dj8_c0) * (cs43 * rs8);
+        J[163] = (-d_D_hco_44*dj8_c0) * (cs44 * rs8);
+        J[162] = (-d_D_hco_45*dj8_c0) * (cs45 * rs8);
+        J[164] = (-d_D_hco_50*dj8_c0) * (cs50 * rs8);
     }
     const T D_r1_c0 = T(1)/(F.o2*K[K_hk2]);
-    const T D_r1 = D_r1_c0*(K[K_a2]*nt_cvt<T>(x[55]) + K[K_a6]*nt_cvt<T>(x[43]) + K[K_a6b]*nt_cvt<T>(x[47]) + K[K_b4]*nt_cvt<T>(x[49]) + K[K_d2]*nt_cvt<T>(x[44]) + tj[J_o3_o1d] + tj[J_o3_o3p]);
+    const T D_r1 = D_r1_c0*(K[K_a2]*xt55 + K[K_a6]*xt43 + K[K_a6b]*xt47 + K[K_b4]*xt49 + K[K_d2]*xt44 + tj[J_o3_o1d] + tj[J_o3_o3p]);
     const T d_D_r1_43 = D_r1_c0*K[K_a6];
     const T d_D_r1_44 = D_r1_c0*K[K_d2];
     const T d_D_r1_47 = D_r1_c0*K[K_a6b];
@@ -2669,26 +3175,26 @@ __device__ __forceinline__ void nt_jacobian_day_w4_1(const FF& F, PK K, PK tj, P
     const T d_D_r1_55 = D_r1_c0*K[K_a2];
     {  // row 45
     const T rs45 = nt_rscale<T>(nt_exp_hi(x[45]), fh);
-        J[280] = (-d_D_r1_43*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs45);
-        J[279] = (-d_D_r1_44*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs45);
-        J[282] = (-D_r1) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs45);
-        J[281] = (-d_D_r1_47*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs45);
-        J[283] = (-d_D_r1_49*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs45);
-        J[278] = (-d_D_r1_55*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs45);
+        J[280] = (-d_D_r1_43*xt46) * (cs43 * rs45);
+        J[279] = (-d_D_r1_44*xt46) * (cs44 * rs45);
+        J[282] = (-D_r1) * (cs46 * rs45);
+        J[281] = (-d_D_r1_47*xt46) * (cs47 * rs45);
+        J[283] = (-d_D_r1_49*xt46) * (cs49 * rs45);
+        J[278] = (-d_D_r1_55*xt46) * (cs55 * rs45);
     }
     {  // row 46
     const T rs46 = nt_rscale<T>(nt_exp_hi(x[46]), fh);
         const T dj46_c0 = D_r1 + T(1);
-        const T dj46_c1 = nt_cvt<T>(x[7])/(dj46_c0*dj46_c0);
-        J[355] = (-T(1)/dj46_c0) * (nt_scale<T>(nt_exp_hi(x[7]), fh) * rs46);
-        J[358] = (d_D_r1_43*dj46_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs46);
-        J[357] = (d_D_r1_44*dj46_c1) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs46);
-        J[359] = (d_D_r1_47*dj46_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs46);
-        J[360] = (d_D_r1_49*dj46_c1) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs46);
-        J[356] = (d_D_r1_55*dj46_c1) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs46);
+        const T dj46_c1 = xt7/(dj46_c0*dj46_c0);
+        J[355] = (-T(1)/dj46_c0) * (cs7 * rs46);
+        J[358] = (d_D_r1_43*dj46_c1) * (cs43 * rs46);
+        J[357] = (d_D_r1_44*dj46_c1) * (cs44 * rs46);
+        J[359] = (d_D_r1_47*dj46_c1) * (cs47 * rs46);
+        J[360] = (d_D_r1_49*dj46_c1) * (cs49 * rs46);
+        J[356] = (d_D_r1_55*dj46_c1) * (cs55 * rs46);
     }
-    const T D_r4_c0 = F.h2*K[K_a19] + K[K_a36]*nt_cvt<T>(x[8]) + K[K_a5]*nt_cvt<T>(x[45]);
-    const T D_r4_c1 = F.o2*K[K_a1] + K[K_a2]*nt_cvt<T>(x[46]) + T(8.049999999999999e-11)*nt_cvt<T>(x[47]);
+    const T D_r4_c0 = F.h2*K[K_a19] + K[K_a36]*xt8 + K[K_a5]*xt45;
+    const T D_r4_c1 = F.o2*K[K_a1] + K[K_a2]*xt46 + T(8.049999999999999e-11)*xt47;
     const T D_r4_c2 = (T(1)/(D_r4_c1));
     const T D_r4_c3 = D_r4_c0/(D_r4_c1*D_r4_c1);
     const T D_r4 = D_r4_c0*D_r4_c2;
@@ -2698,16 +3204,16 @@ __device__ __forceinline__ void nt_jacobian_day_w4_1(const FF& F, PK K, PK tj, P
     const T d_D_r4_47 = -T(8.049999999999999e-11)*D_r4_c3;
     {  // row 55
     const T rs55 = nt_rscale<T>(nt_exp_hi(x[55]), fh);
-        J[205] = (-d_D_r4_8*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[8]), fh) * rs55);
-        J[207] = (-D_r4) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs55);
-        J[206] = (-d_D_r4_45*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs55);
-        J[209] = (-d_D_r4_46*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs55);
-        J[208] = (-d_D_r4_47*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs55);
+        J[205] = (-d_D_r4_8*xt43) * (cs8 * rs55);
+        J[207] = (-D_r4) * (cs43 * rs55);
+        J[206] = (-d_D_r4_45*xt43) * (cs45 * rs55);
+        J[209] = (-d_D_r4_46*xt43) * (cs46 * rs55);
+        J[208] = (-d_D_r4_47*xt43) * (cs47 * rs55);
     }
     const T D_r6_c0 = F.o2*K[K_a1];
-    const T D_r6_c1 = D_r4*D_r6_c0 + K[K_a30]*nt_cvt<T>(x[16]) + K[K_a6]*nt_cvt<T>(x[46]) + K[K_c8]*nt_cvt<T>(x[27]) + K[K_d8]*nt_cvt<T>(x[52]) + K[K_e10]*nt_cvt<T>(x[53]);
+    const T D_r6_c1 = D_r4*D_r6_c0 + K[K_a30]*xt16 + K[K_a6]*xt46 + K[K_c8]*xt27 + K[K_d8]*xt52 + K[K_e10]*xt53;
     const T D_r6_c2 = T(2)*K[K_a27];
-    const T D_r6_c3 = D_r6_c2*nt_cvt<T>(x[47]) + K[K_a17]*nt_cvt<T>(x[43]) + K[K_a26]*nt_cvt<T>(x[49]) + K[K_a6b]*nt_cvt<T>(x[46]) + K[K_a7]*nt_cvt<T>(x[45]) + K[K_d10]*nt_cvt<T>(x[44]) + K[K_d33]*nt_cvt<T>(x[52]) + K[K_d7]*nt_cvt<T>(x[44]) + K[K_e15]*nt_cvt<T>(x[53]) + K[K_e7]*nt_cvt<T>(x[50]) + T(8.049999999999999e-11)*nt_cvt<T>(x[55]);
+    const T D_r6_c3 = D_r6_c2*xt47 + K[K_a17]*xt43 + K[K_a26]*xt49 + K[K_a6b]*xt46 + K[K_a7]*xt45 + K[K_d10]*xt44 + K[K_d33]*xt52 + K[K_d7]*xt44 + K[K_e15]*xt53 + K[K_e7]*xt50 + T(8.049999999999999e-11)*xt55;
     const T D_r6_c4 = (T(1)/(D_r6_c3));
     const T D_r6_c5 = D_r6_c0*D_r6_c4;
     const T D_r6_c6 = D_r6_c1/(D_r6_c3*D_r6_c3);
@@ -2727,19 +3233,19 @@ __device__ __forceinline__ void nt_jacobian_day_w4_1(const FF& F, PK K, PK tj, P
     const T d_D_r6_55 = -T(8.049999999999999e-11)*D_r6_c6;
     {  // row 47
     const T rs47 = nt_rscale<T>(nt_exp_hi(x[47]), fh);
-        J[342] = (-d_D_r6_8*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[8]), fh) * rs47);
-        J[343] = (-d_D_r6_16*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs47);
-        J[345] = (-d_D_r6_27*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs47);
-        J[350] = (-D_r6 - d_D_r6_43*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs47);
-        J[347] = (-d_D_r6_44*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs47);
-        J[346] = (-d_D_r6_45*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs47);
-        J[352] = (-d_D_r6_46*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs47);
-        J[351] = (-d_D_r6_47*nt_cvt<T>(x[43]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs47);
-        J[353] = (-d_D_r6_49*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs47);
-        J[349] = (-d_D_r6_50*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs47);
-        J[354] = (-d_D_r6_52*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs47);
-        J[348] = (-d_D_r6_53*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs47);
-        J[344] = (-d_D_r6_55*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs47);
+        J[342] = (-d_D_r6_8*xt43) * (cs8 * rs47);
+        J[343] = (-d_D_r6_16*xt43) * (cs16 * rs47);
+        J[345] = (-d_D_r6_27*xt43) * (cs27 * rs47);
+        J[350] = (-D_r6 - d_D_r6_43*xt43) * (cs43 * rs47);
+        J[347] = (-d_D_r6_44*xt43) * (cs44 * rs47);
+        J[346] = (-d_D_r6_45*xt43) * (cs45 * rs47);
+        J[352] = (-d_D_r6_46*xt43) * (cs46 * rs47);
+        J[351] = (-d_D_r6_47*xt43 + T(1)) * (cs47 * rs47);
+        J[353] = (-d_D_r6_49*xt43) * (cs49 * rs47);
+        J[349] = (-d_D_r6_50*xt43) * (cs50 * rs47);
+        J[354] = (-d_D_r6_52*xt43) * (cs52 * rs47);
+        J[348] = (-d_D_r6_53*xt43) * (cs53 * rs47);
+        J[344] = (-d_D_r6_55*xt43) * (cs55 * rs47);
     }
 }
 
@@ -2787,149 +3293,247 @@ __device__ __forceinline__ void nt_residual_day_w4_2(const FF& F, PK K, PK tj, P
 template <typename T, typename FF, typename PK, typename PJ>
 __device__ __forceinline__ void nt_jacobian_day_w4_2(const FF& F, PK K, PK tj, PK het, const double* __restrict__ x, double floor_, PJ J) {
     const int fh = nt_exp_hi(floor_);
+    const T xt0 = nt_cvt<T>(x[0]);
+    const T xt1 = nt_cvt<T>(x[1]);
+    const T xt2 = nt_cvt<T>(x[2]);
+    const T xt3 = nt_cvt<T>(x[3]);
+    const T xt4 = nt_cvt<T>(x[4]);
+    const T xt5 = nt_cvt<T>(x[5]);
+    const T xt6 = nt_cvt<T>(x[6]);
+    const T xt7 = nt_cvt<T>(x[7]);
+    const T xt8 = nt_cvt<T>(x[8]);
+    const T xt9 = nt_cvt<T>(x[9]);
+    const T xt10 = nt_cvt<T>(x[10]);
+    const T xt11 = nt_cvt<T>(x[11]);
+    const T xt12 = nt_cvt<T>(x[12]);
+    const T xt13 = nt_cvt<T>(x[13]);
+    const T xt14 = nt_cvt<T>(x[14]);
+    const T xt15 = nt_cvt<T>(x[15]);
+    const T xt16 = nt_cvt<T>(x[16]);
+    const T xt17 = nt_cvt<T>(x[17]);
+    const T xt18 = nt_cvt<T>(x[18]);
+    const T xt19 = nt_cvt<T>(x[19]);
+    const T xt20 = nt_cvt<T>(x[20]);
+    const T xt21 = nt_cvt<T>(x[21]);
+    const T xt22 = nt_cvt<T>(x[22]);
+    const T xt23 = nt_cvt<T>(x[23]);
+    const T xt24 = nt_cvt<T>(x[24]);
+    const T xt25 = nt_cvt<T>(x[25]);
+    const T xt26 = nt_cvt<T>(x[26]);
+    const T xt27 = nt_cvt<T>(x[27]);
+    const T xt28 = nt_cvt<T>(x[28]);
+    const T xt29 = nt_cvt<T>(x[29]);
+    const T xt30 = nt_cvt<T>(x[30]);
+    const T xt31 = nt_cvt<T>(x[31]);
+    const T xt32 = nt_cvt<T>(x[32]);
+    const T xt33 = nt_cvt<T>(x[33]);
+    const T xt34 = nt_cvt<T>(x[34]);
+    const T xt35 = nt_cvt<T>(x[35]);
+    const T xt36 = nt_cvt<T>(x[36]);
+    const T xt37 = nt_cvt<T>(x[37]);
+    const T xt38 = nt_cvt<T>(x[38]);
+    const T xt39 = nt_cvt<T>(x[39]);
+    const T xt40 = nt_cvt<T>(x[40]);
+    const T xt41 = nt_cvt<T>(x[41]);
+    const T xt42 = nt_cvt<T>(x[42]);
+    const T xt43 = nt_cvt<T>(x[43]);
+    const T xt44 = nt_cvt<T>(x[44]);
+    const T xt45 = nt_cvt<T>(x[45]);
+    const T xt46 = nt_cvt<T>(x[46]);
+    const T xt47 = nt_cvt<T>(x[47]);
+    const T xt48 = nt_cvt<T>(x[48]);
+    const T xt49 = nt_cvt<T>(x[49]);
+    const T xt50 = nt_cvt<T>(x[50]);
+    const T xt51 = nt_cvt<T>(x[51]);
+    const T xt52 = nt_cvt<T>(x[52]);
+    const T xt53 = nt_cvt<T>(x[53]);
+    const T xt54 = nt_cvt<T>(x[54]);
+    const T xt55 = nt_cvt<T>(x[55]);
+    const T xt56 = nt_cvt<T>(x[56]);
+    const T cs0 = nt_scale<T>(nt_exp_hi(x[0]), fh);
+    const T cs1 = nt_scale<T>(nt_exp_hi(x[1]), fh);
+    const T cs2 = nt_scale<T>(nt_exp_hi(x[2]), fh);
+    const T cs4 = nt_scale<T>(nt_exp_hi(x[4]), fh);
+    const T cs5 = nt_scale<T>(nt_exp_hi(x[5]), fh);
+    const T cs12 = nt_scale<T>(nt_exp_hi(x[12]), fh);
+    const T cs13 = nt_scale<T>(nt_exp_hi(x[13]), fh);
+    const T cs14 = nt_scale<T>(nt_exp_hi(x[14]), fh);
+    const T cs16 = nt_scale<T>(nt_exp_hi(x[16]), fh);
+    const T cs18 = nt_scale<T>(nt_exp_hi(x[18]), fh);
+    const T cs19 = nt_scale<T>(nt_exp_hi(x[19]), fh);
+    const T cs22 = nt_scale<T>(nt_exp_hi(x[22]), fh);
+    const T cs23 = nt_scale<T>(nt_exp_hi(x[23]), fh);
+    const T cs25 = nt_scale<T>(nt_exp_hi(x[25]), fh);
+    const T cs27 = nt_scale<T>(nt_exp_hi(x[27]), fh);
+    const T cs28 = nt_scale<T>(nt_exp_hi(x[28]), fh);
+    const T cs29 = nt_scale<T>(nt_exp_hi(x[29]), fh);
+    const T cs30 = nt_scale<T>(nt_exp_hi(x[30]), fh);
+    const T cs31 = nt_scale<T>(nt_exp_hi(x[31]), fh);
+    const T cs32 = nt_scale<T>(nt_exp_hi(x[32]), fh);
+    const T cs33 = nt_scale<T>(nt_exp_hi(x[33]), fh);
+    const T cs34 = nt_scale<T>(nt_exp_hi(x[34]), fh);
+    const T cs35 = nt_scale<T>(nt_exp_hi(x[35]), fh);
+    const T cs36 = nt_scale<T>(nt_exp_hi(x[36]), fh);
+    const T cs37 = nt_scale<T>(nt_exp_hi(x[37]), fh);
+    const T cs38 = nt_scale<T>(nt_exp_hi(x[38]), fh);
+    const T cs39 = nt_scale<T>(nt_exp_hi(x[39]), fh);
+    const T cs41 = nt_scale<T>(nt_exp_hi(x[41]), fh);
+    const T cs42 = nt_scale<T>(nt_exp_hi(x[42]), fh);
+    const T cs43 = nt_scale<T>(nt_exp_hi(x[43]), fh);
+    const T cs44 = nt_scale<T>(nt_exp_hi(x[44]), fh);
+    const T cs45 = nt_scale<T>(nt_exp_hi(x[45]), fh);
+    const T cs46 = nt_scale<T>(nt_exp_hi(x[46]), fh);
+    const T cs47 = nt_scale<T>(nt_exp_hi(x[47]), fh);
+    const T cs48 = nt_scale<T>(nt_exp_hi(x[48]), fh);
+    const T cs49 = nt_scale<T>(nt_exp_hi(x[49]), fh);
+    const T cs50 = nt_scale<T>(nt_exp_hi(x[50]), fh);
+    const T cs52 = nt_scale<T>(nt_exp_hi(x[52]), fh);
+    const T cs53 = nt_scale<T>(nt_exp_hi(x[53]), fh);
+    const T cs54 = nt_scale<T>(nt_exp_hi(x[54]), fh);
+    const T cs56 = nt_scale<T>(nt_exp_hi(x[56]), fh);
     {  // row 0
     const T rs0 = nt_rscale<T>(nt_exp_hi(x[0]), fh);
         const T dj0_c0 = K[K_b38] + K[K_b39];
-        J[76] = (F.dt*(dj0_c0*nt_cvt<T>(x[42]) + tj[J_n2o]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs0);
-        J[77] = (F.dt*dj0_c0*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs0);
+        J[76] = (F.dt*(dj0_c0*xt42 + tj[J_n2o]) + T(1)) * (cs0 * rs0);
+        J[77] = (F.dt*dj0_c0*xt0) * (cs42 * rs0);
     }
     {  // row 4
     const T rs4 = nt_rscale<T>(nt_exp_hi(x[4]), fh);
         const T dj4_c0 = T(2)*het[2];
         const T dj4_c1 = F.dt*K[K_b22];
-        J[122] = (-F.dt*(dj4_c0*nt_cvt<T>(x[5]) + het[0]*nt_cvt<T>(x[13]) + het[5]*nt_cvt<T>(x[19]))) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs4);
-        J[120] = (F.dt*(F.parthno3*(K[K_b27]*nt_cvt<T>(x[43]) + tj[J_hno3]) + F.rain_hno3) + T(1)) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs4);
-        J[118] = (-F.dt*(dj4_c0*nt_cvt<T>(x[2]) + het[3]*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs4);
-        J[121] = (-F.dt*(het[1]*nt_cvt<T>(x[13]) + het[3]*nt_cvt<T>(x[5]))) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs4);
-        J[119] = (-F.dt*(het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs4);
-        J[117] = (-F.dt*het[5]*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs4);
-        J[124] = (F.dt*F.parthno3*K[K_b27]*nt_cvt<T>(x[4]) - dj4_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs4);
-        J[123] = (-dj4_c1*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs4);
+        J[122] = (-F.dt*(dj4_c0*xt5 + het[0]*xt13 + het[5]*xt19)) * (cs2 * rs4);
+        J[120] = (F.dt*(F.parthno3*(K[K_b27]*xt43 + tj[J_hno3]) + F.rain_hno3) + T(1)) * (cs4 * rs4);
+        J[118] = (-F.dt*(dj4_c0*xt2 + het[3]*xt12)) * (cs5 * rs4);
+        J[121] = (-F.dt*(het[1]*xt13 + het[3]*xt5)) * (cs12 * rs4);
+        J[119] = (-F.dt*(het[0]*xt2 + het[1]*xt12)) * (cs13 * rs4);
+        J[117] = (-F.dt*het[5]*xt2) * (cs19 * rs4);
+        J[124] = (F.dt*F.parthno3*K[K_b27]*xt4 - dj4_c1*xt48) * (cs43 * rs4);
+        J[123] = (-dj4_c1*xt43) * (cs48 * rs4);
     }
     {  // row 5
     const T rs5 = nt_rscale<T>(nt_exp_hi(x[5]), fh);
-        const T dj5_c0 = F.dt*nt_cvt<T>(x[5]);
+        const T dj5_c0 = F.dt*xt5;
         const T dj5_c1 = F.dt*K[K_b12];
-        J[74] = (dj5_c0*het[2]) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs5);
-        J[72] = (F.dt*(F.hnm*K[K_b32] + het[2]*nt_cvt<T>(x[2]) + het[3]*nt_cvt<T>(x[12]) + tj[J_n2o5]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs5);
-        J[73] = (dj5_c0*het[3]) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs5);
-        J[75] = (-dj5_c1*nt_cvt<T>(x[54])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs5);
-        J[71] = (-dj5_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[54]), fh) * rs5);
+        J[74] = (dj5_c0*het[2]) * (cs2 * rs5);
+        J[72] = (F.dt*(F.hnm*K[K_b32] + het[2]*xt2 + het[3]*xt12 + tj[J_n2o5]) + T(1)) * (cs5 * rs5);
+        J[73] = (dj5_c0*het[3]) * (cs12 * rs5);
+        J[75] = (-dj5_c1*xt54) * (cs48 * rs5);
+        J[71] = (-dj5_c1*xt48) * (cs54 * rs5);
     }
     {  // row 6
     const T rs6 = nt_rscale<T>(nt_exp_hi(x[6]), fh);
-        const T dj6_c0 = T(3)*nt_cvt<T>(x[42]);
+        const T dj6_c0 = T(3)*xt42;
         const T dj6_c1 = T(2)*K[K_d91];
         const T dj6_c2 = T(4)*K[K_d93];
         const T dj6_c3 = T(3)*K[K_d94];
-        J[9] = (F.dt*F.rain_hcl) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs6);
-        J[7] = (-F.dt*(K[K_d90]*dj6_c0 + T(3)*tj[J_cfc11])) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs6);
-        J[4] = (-F.dt*(dj6_c1*nt_cvt<T>(x[42]) + T(2)*tj[J_cfc12])) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs6);
-        J[0] = (-F.dt*(K[K_d92]*dj6_c0 + T(3)*tj[J_cfc113])) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs6);
-        J[2] = (-F.dt*(dj6_c2*nt_cvt<T>(x[42]) + T(4)*tj[J_ccl4])) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs6);
-        J[6] = (-F.dt*(dj6_c3*nt_cvt<T>(x[43]) + T(3)*tj[J_ch3ccl3])) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs6);
-        J[5] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl])) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs6);
-        J[3] = (-F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22])) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs6);
-        J[1] = (-F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211])) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs6);
-        J[8] = (-F.dt*(T(3)*K[K_d90]*nt_cvt<T>(x[30]) + T(3)*K[K_d92]*nt_cvt<T>(x[32]) + K[K_d96]*nt_cvt<T>(x[36]) + K[K_e52]*nt_cvt<T>(x[38]) + dj6_c1*nt_cvt<T>(x[31]) + dj6_c2*nt_cvt<T>(x[33]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs6);
-        J[10] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[35]) + K[K_d97]*nt_cvt<T>(x[36]) + dj6_c3*nt_cvt<T>(x[34]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs6);
+        J[9] = (F.dt*F.rain_hcl) * (cs12 * rs6);
+        J[7] = (-F.dt*(K[K_d90]*dj6_c0 + T(3)*tj[J_cfc11])) * (cs30 * rs6);
+        J[4] = (-F.dt*(dj6_c1*xt42 + T(2)*tj[J_cfc12])) * (cs31 * rs6);
+        J[0] = (-F.dt*(K[K_d92]*dj6_c0 + T(3)*tj[J_cfc113])) * (cs32 * rs6);
+        J[2] = (-F.dt*(dj6_c2*xt42 + T(4)*tj[J_ccl4])) * (cs33 * rs6);
+        J[6] = (-F.dt*(dj6_c3*xt43 + T(3)*tj[J_ch3ccl3])) * (cs34 * rs6);
+        J[5] = (-F.dt*(K[K_d95]*xt43 + tj[J_ch3cl])) * (cs35 * rs6);
+        J[3] = (-F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22])) * (cs36 * rs6);
+        J[1] = (-F.dt*(K[K_e52]*xt42 + tj[J_h1211])) * (cs38 * rs6);
+        J[8] = (-F.dt*(T(3)*K[K_d90]*xt30 + T(3)*K[K_d92]*xt32 + K[K_d96]*xt36 + K[K_e52]*xt38 + dj6_c1*xt31 + dj6_c2*xt33)) * (cs42 * rs6);
+        J[10] = (-F.dt*(K[K_d95]*xt35 + K[K_d97]*xt36 + dj6_c3*xt34)) * (cs43 * rs6);
     }
     {  // row 12
     const T rs12 = nt_rscale<T>(nt_exp_hi(x[12]), fh);
-        const T dj12_c0 = F.dt*nt_cvt<T>(x[44]);
-        const T dj12_c1 = F.dt*nt_cvt<T>(x[12]);
+        const T dj12_c0 = F.dt*xt44;
+        const T dj12_c1 = F.dt*xt12;
         const T dj12_c2 = F.dt*K[K_d9];
-        J[250] = (-K[K_d5]*dj12_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs12);
-        J[247] = (dj12_c1*het[3]) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs12);
-        J[253] = (F.dt*(F.parthcl*(K[K_d11]*nt_cvt<T>(x[43]) + tj[J_hcl]) + F.rain_hcl + het[1]*nt_cvt<T>(x[13]) + het[3]*nt_cvt<T>(x[5]) + het[4]*nt_cvt<T>(x[14]) + het[6]*nt_cvt<T>(x[25])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs12);
-        J[249] = (dj12_c1*het[1]) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs12);
-        J[251] = (dj12_c1*het[4]) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs12);
-        J[248] = (dj12_c1*het[6]) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs12);
-        J[252] = (-K[K_c10]*dj12_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs12);
-        J[255] = (F.parthcl*K[K_d11]*dj12_c1 - dj12_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs12);
-        J[254] = (-F.dt*(F.h2*K[K_d6] + K[K_c10]*nt_cvt<T>(x[27]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs12);
-        J[256] = (-K[K_d7]*dj12_c0) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs12);
-        J[257] = (-dj12_c2*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs12);
+        J[250] = (-K[K_d5]*dj12_c0) * (cs1 * rs12);
+        J[247] = (dj12_c1*het[3]) * (cs5 * rs12);
+        J[253] = (F.dt*(F.parthcl*(K[K_d11]*xt43 + tj[J_hcl]) + F.rain_hcl + het[1]*xt13 + het[3]*xt5 + het[4]*xt14 + het[6]*xt25) + T(1)) * (cs12 * rs12);
+        J[249] = (dj12_c1*het[1]) * (cs13 * rs12);
+        J[251] = (dj12_c1*het[4]) * (cs14 * rs12);
+        J[248] = (dj12_c1*het[6]) * (cs25 * rs12);
+        J[252] = (-K[K_c10]*dj12_c0) * (cs27 * rs12);
+        J[255] = (F.parthcl*K[K_d11]*dj12_c1 - dj12_c2*xt52) * (cs43 * rs12);
+        J[254] = (-F.dt*(F.h2*K[K_d6] + K[K_c10]*xt27 + K[K_d5]*xt1 + K[K_d7]*xt47)) * (cs44 * rs12);
+        J[256] = (-K[K_d7]*dj12_c0) * (cs47 * rs12);
+        J[257] = (-dj12_c2*xt43) * (cs52 * rs12);
     }
     {  // row 13
     const T rs13 = nt_rscale<T>(nt_exp_hi(x[13]), fh);
-        const T dj13_c0 = F.dt*nt_cvt<T>(x[13]);
+        const T dj13_c0 = F.dt*xt13;
         const T dj13_c1 = F.dt*K[K_d31];
-        J[89] = (dj13_c0*het[0]) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs13);
-        J[88] = (dj13_c0*het[1]) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs13);
-        J[87] = (F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]) + tj[J_clono2_cl] + tj[J_clono2_clo]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs13);
-        J[91] = (K[K_d32]*dj13_c0) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs13);
-        J[90] = (-dj13_c1*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs13);
-        J[92] = (-dj13_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs13);
+        J[89] = (dj13_c0*het[0]) * (cs2 * rs13);
+        J[88] = (dj13_c0*het[1]) * (cs12 * rs13);
+        J[87] = (F.dt*(K[K_d32]*xt45 + het[0]*xt2 + het[1]*xt12 + tj[J_clono2_cl] + tj[J_clono2_clo]) + T(1)) * (cs13 * rs13);
+        J[91] = (K[K_d32]*dj13_c0) * (cs45 * rs13);
+        J[90] = (-dj13_c1*xt52) * (cs48 * rs13);
+        J[92] = (-dj13_c1*xt48) * (cs52 * rs13);
     }
     {  // row 16
     const T rs16 = nt_rscale<T>(nt_exp_hi(x[16]), fh);
-        J[189] = (F.dt*(F.rain_h2o2 + K[K_a30]*nt_cvt<T>(x[43]) + tj[J_h2o2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs16);
-        J[190] = (F.dt*K[K_a30]*nt_cvt<T>(x[16])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs16);
-        J[191] = (-T(2)*F.dt*K[K_a27]*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs16);
+        J[189] = (F.dt*(F.rain_h2o2 + K[K_a30]*xt43 + tj[J_h2o2]) + T(1)) * (cs16 * rs16);
+        J[190] = (F.dt*K[K_a30]*xt16) * (cs43 * rs16);
+        J[191] = (-T(2)*F.dt*K[K_a27]*xt47) * (cs47 * rs16);
     }
     {  // row 25
     const T rs25 = nt_rscale<T>(nt_exp_hi(x[25]), fh);
         const T dj25_c0 = F.dt*het[5];
-        const T dj25_c1 = F.dt*nt_cvt<T>(x[25]);
+        const T dj25_c1 = F.dt*xt25;
         const T dj25_c2 = F.dt*K[K_e15];
-        J[83] = (-dj25_c0*nt_cvt<T>(x[19])) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs25);
-        J[82] = (dj25_c1*het[6]) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs25);
-        J[81] = (dj25_c1*het[7]) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs25);
-        J[79] = (-dj25_c0*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs25);
-        J[80] = (F.dt*(K[K_e16]*nt_cvt<T>(x[45]) + het[6]*nt_cvt<T>(x[12]) + het[7]*nt_cvt<T>(x[18]) + tj[J_hobr]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs25);
-        J[84] = (K[K_e16]*dj25_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs25);
-        J[86] = (-dj25_c2*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs25);
-        J[85] = (-dj25_c2*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs25);
+        J[83] = (-dj25_c0*xt19) * (cs2 * rs25);
+        J[82] = (dj25_c1*het[6]) * (cs12 * rs25);
+        J[81] = (dj25_c1*het[7]) * (cs18 * rs25);
+        J[79] = (-dj25_c0*xt2) * (cs19 * rs25);
+        J[80] = (F.dt*(K[K_e16]*xt45 + het[6]*xt12 + het[7]*xt18 + tj[J_hobr]) + T(1)) * (cs25 * rs25);
+        J[84] = (K[K_e16]*dj25_c1) * (cs45 * rs25);
+        J[86] = (-dj25_c2*xt53) * (cs47 * rs25);
+        J[85] = (-dj25_c2*xt47) * (cs53 * rs25);
     }
     {  // row 29
     const T rs29 = nt_rscale<T>(nt_exp_hi(x[29]), fh);
         const T dj29_c0 = F.dt*K[K_c7];
-        J[35] = (-dj29_c0*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs29);
-        J[34] = (F.dt*(K[K_c17a]*nt_cvt<T>(x[43]) + K[K_c17b]*nt_cvt<T>(x[43]) + tj[J_ch3o2h]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs29);
-        J[36] = (F.dt*nt_cvt<T>(x[29])*(K[K_c17a] + K[K_c17b])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs29);
-        J[37] = (-dj29_c0*nt_cvt<T>(x[28])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs29);
+        J[35] = (-dj29_c0*xt47) * (cs28 * rs29);
+        J[34] = (F.dt*(K[K_c17a]*xt43 + K[K_c17b]*xt43 + tj[J_ch3o2h]) + T(1)) * (cs29 * rs29);
+        J[36] = (F.dt*xt29*(K[K_c17a] + K[K_c17b])) * (cs43 * rs29);
+        J[37] = (-dj29_c0*xt28) * (cs47 * rs29);
     }
     {  // row 30
     const T rs30 = nt_rscale<T>(nt_exp_hi(x[30]), fh);
-        J[95] = (F.dt*(K[K_d90]*nt_cvt<T>(x[42]) + tj[J_cfc11]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs30);
-        J[96] = (F.dt*K[K_d90]*nt_cvt<T>(x[30])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs30);
+        J[95] = (F.dt*(K[K_d90]*xt42 + tj[J_cfc11]) + T(1)) * (cs30 * rs30);
+        J[96] = (F.dt*K[K_d90]*xt30) * (cs42 * rs30);
     }
     {  // row 33
     const T rs33 = nt_rscale<T>(nt_exp_hi(x[33]), fh);
-        J[32] = (F.dt*(K[K_d93]*nt_cvt<T>(x[42]) + tj[J_ccl4]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs33);
-        J[33] = (F.dt*K[K_d93]*nt_cvt<T>(x[33])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs33);
+        J[32] = (F.dt*(K[K_d93]*xt42 + tj[J_ccl4]) + T(1)) * (cs33 * rs33);
+        J[33] = (F.dt*K[K_d93]*xt33) * (cs42 * rs33);
     }
     {  // row 38
     const T rs38 = nt_rscale<T>(nt_exp_hi(x[38]), fh);
-        J[30] = (F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs38);
-        J[31] = (F.dt*K[K_e52]*nt_cvt<T>(x[38])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs38);
+        J[30] = (F.dt*(K[K_e52]*xt42 + tj[J_h1211]) + T(1)) * (cs38 * rs38);
+        J[31] = (F.dt*K[K_e52]*xt38) * (cs42 * rs38);
     }
     {  // row 40
     const T rs40 = nt_rscale<T>(nt_exp_hi(x[40]), fh);
         const T dj40_c0 = T(2)*K[K_e54];
-        J[16] = (F.dt*F.rain_hbr) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs40);
-        J[13] = (-F.dt*(K[K_e50]*nt_cvt<T>(x[42]) + K[K_e51]*nt_cvt<T>(x[43]) + tj[J_ch3br])) * (nt_scale<T>(nt_exp_hi(x[37]), fh) * rs40);
-        J[11] = (-F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211])) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs40);
-        J[12] = (-F.dt*(K[K_e53]*nt_cvt<T>(x[42]) + tj[J_h1301])) * (nt_scale<T>(nt_exp_hi(x[39]), fh) * rs40);
-        J[15] = (-F.dt*(dj40_c0*nt_cvt<T>(x[43]) + T(2)*tj[J_ch2br2])) * (nt_scale<T>(nt_exp_hi(x[41]), fh) * rs40);
-        J[14] = (-F.dt*(K[K_e50]*nt_cvt<T>(x[37]) + K[K_e52]*nt_cvt<T>(x[38]) + K[K_e53]*nt_cvt<T>(x[39]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs40);
-        J[17] = (-F.dt*(K[K_e51]*nt_cvt<T>(x[37]) + dj40_c0*nt_cvt<T>(x[41]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs40);
+        J[16] = (F.dt*F.rain_hbr) * (cs18 * rs40);
+        J[13] = (-F.dt*(K[K_e50]*xt42 + K[K_e51]*xt43 + tj[J_ch3br])) * (cs37 * rs40);
+        J[11] = (-F.dt*(K[K_e52]*xt42 + tj[J_h1211])) * (cs38 * rs40);
+        J[12] = (-F.dt*(K[K_e53]*xt42 + tj[J_h1301])) * (cs39 * rs40);
+        J[15] = (-F.dt*(dj40_c0*xt43 + T(2)*tj[J_ch2br2])) * (cs41 * rs40);
+        J[14] = (-F.dt*(K[K_e50]*xt37 + K[K_e52]*xt38 + K[K_e53]*xt39)) * (cs42 * rs40);
+        J[17] = (-F.dt*(K[K_e51]*xt37 + dj40_c0*xt41)) * (cs43 * rs40);
     }
     {  // row 42
     const T rs42 = nt_rscale<T>(nt_exp_hi(x[42]), fh);
-        J[99] = (-tj[J_o3_o1d]/(F.n2*K[K_hk4] + F.o2*K[K_hk5])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs42);
+        J[99] = (-tj[J_o3_o1d]/(F.n2*K[K_hk4] + F.o2*K[K_hk5])) * (cs46 * rs42);
     }
-    const T D_ch3o_c0 = K[K_c1b]*nt_cvt<T>(x[42]);
-    const T D_ch3o_c1 = K[K_c14]*nt_cvt<T>(x[28]);
-    const T D_ch3o_c2 = K[K_c18]*nt_cvt<T>(x[52]) + K[K_c5]*nt_cvt<T>(x[49]);
+    const T D_ch3o_c0 = K[K_c1b]*xt42;
+    const T D_ch3o_c1 = K[K_c14]*xt28;
+    const T D_ch3o_c2 = K[K_c18]*xt52 + K[K_c5]*xt49;
     const T D_ch3o_c3 = T(1)/(F.o2*K[K_c15]);
-    const T D_ch3o_c4 = D_ch3o_c3*nt_cvt<T>(x[28]);
-    const T D_ch3o = D_ch3o_c3*(D_ch3o_c0*nt_cvt<T>(x[1]) + tj[J_ch3o2h]*nt_cvt<T>(x[29]) + nt_cvt<T>(x[28])*(T(2)*D_ch3o_c1 + D_ch3o_c2));
+    const T D_ch3o_c4 = D_ch3o_c3*xt28;
+    const T D_ch3o = D_ch3o_c3*(D_ch3o_c0*xt1 + tj[J_ch3o2h]*xt29 + xt28*(T(2)*D_ch3o_c1 + D_ch3o_c2));
     const T d_D_ch3o_1 = D_ch3o_c0*D_ch3o_c3;
     const T d_D_ch3o_28 = D_ch3o_c3*(T(4)*D_ch3o_c1 + D_ch3o_c2);
     const T d_D_ch3o_29 = D_ch3o_c3*tj[J_ch3o2h];
-    const T d_D_ch3o_42 = D_ch3o_c3*K[K_c1b]*nt_cvt<T>(x[1]);
+    const T d_D_ch3o_42 = D_ch3o_c3*K[K_c1b]*xt1;
     const T d_D_ch3o_49 = D_ch3o_c4*K[K_c5];
     const T d_D_ch3o_52 = D_ch3o_c4*K[K_c18];
     {  // row 27
@@ -2937,51 +3541,51 @@ __device__ __forceinline__ void nt_jacobian_day_w4_2(const FF& F, PK K, PK tj, P
         const T dj27_c0 = F.dt*K[K_c1c];
         const T dj27_c1 = F.dt*F.o2*K[K_c15];
         const T dj27_c2 = F.dt*K[K_c17b];
-        const T dj27_c3 = F.dt*nt_cvt<T>(x[27]);
+        const T dj27_c3 = F.dt*xt27;
         const T dj27_c4 = F.dt*K[K_c3];
-        J[219] = (-d_D_ch3o_1*dj27_c1 - dj27_c0*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs27);
-        J[222] = (F.dt*(K[K_c10]*nt_cvt<T>(x[44]) + K[K_c19]*nt_cvt<T>(x[50]) + K[K_c8]*nt_cvt<T>(x[43]) + K[K_c9]*nt_cvt<T>(x[45]) + tj[J_ch2o_co] + tj[J_ch2o_hco]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs27);
-        J[221] = (-d_D_ch3o_28*dj27_c1) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs27);
-        J[217] = (-d_D_ch3o_29*dj27_c1 - dj27_c2*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs27);
-        J[218] = (-d_D_ch3o_42*dj27_c1 - dj27_c0*nt_cvt<T>(x[1])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs27);
-        J[226] = (F.dt*K[K_c8]*nt_cvt<T>(x[27]) - dj27_c2*nt_cvt<T>(x[29])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs27);
-        J[224] = (K[K_c10]*dj27_c3) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs27);
-        J[223] = (F.dt*K[K_c9]*nt_cvt<T>(x[27]) - dj27_c4*nt_cvt<T>(x[56])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs27);
-        J[227] = (-d_D_ch3o_49*dj27_c1) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs27);
-        J[225] = (K[K_c19]*dj27_c3) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs27);
-        J[228] = (-d_D_ch3o_52*dj27_c1) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs27);
-        J[220] = (-dj27_c4*nt_cvt<T>(x[45])) * (nt_scale<T>(nt_exp_hi(x[56]), fh) * rs27);
+        J[219] = (-d_D_ch3o_1*dj27_c1 - dj27_c0*xt42) * (cs1 * rs27);
+        J[222] = (F.dt*(K[K_c10]*xt44 + K[K_c19]*xt50 + K[K_c8]*xt43 + K[K_c9]*xt45 + tj[J_ch2o_co] + tj[J_ch2o_hco]) + T(1)) * (cs27 * rs27);
+        J[221] = (-d_D_ch3o_28*dj27_c1) * (cs28 * rs27);
+        J[217] = (-d_D_ch3o_29*dj27_c1 - dj27_c2*xt43) * (cs29 * rs27);
+        J[218] = (-d_D_ch3o_42*dj27_c1 - dj27_c0*xt1) * (cs42 * rs27);
+        J[226] = (F.dt*K[K_c8]*xt27 - dj27_c2*xt29) * (cs43 * rs27);
+        J[224] = (K[K_c10]*dj27_c3) * (cs44 * rs27);
+        J[223] = (F.dt*K[K_c9]*xt27 - dj27_c4*xt56) * (cs45 * rs27);
+        J[227] = (-d_D_ch3o_49*dj27_c1) * (cs49 * rs27);
+        J[225] = (K[K_c19]*dj27_c3) * (cs50 * rs27);
+        J[228] = (-d_D_ch3o_52*dj27_c1) * (cs52 * rs27);
+        J[220] = (-dj27_c4*xt45) * (cs56 * rs27);
     }
-    const T D_r13_c0 = K[K_d32]*nt_cvt<T>(x[45]) + het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]) + tj[J_clono2_cl] + tj[J_clono2_clo];
+    const T D_r13_c0 = K[K_d32]*xt45 + het[0]*xt2 + het[1]*xt12 + tj[J_clono2_cl] + tj[J_clono2_clo];
     const T D_r13_c1 = K[K_d31]/D_r13_c0;
-    const T D_r13_c2 = K[K_d31]*nt_cvt<T>(x[48])/(D_r13_c0*D_r13_c0);
-    const T D_r13 = D_r13_c1*nt_cvt<T>(x[48]);
+    const T D_r13_c2 = K[K_d31]*xt48/(D_r13_c0*D_r13_c0);
+    const T D_r13 = D_r13_c1*xt48;
     const T d_D_r13_2 = -D_r13_c2*het[0];
     const T d_D_r13_12 = -D_r13_c2*het[1];
     const T d_D_r13_45 = -D_r13_c2*K[K_d32];
     const T d_D_r13_48 = D_r13_c1;
     const T D_r9_c0 = D_r13*het[0];
-    const T D_r9_c1 = D_r9_c0*nt_cvt<T>(x[2]) + K[K_d33]*nt_cvt<T>(x[47]);
-    const T D_r9_c2 = K[K_d35]*nt_cvt<T>(x[45]) + het[4]*nt_cvt<T>(x[12]) + tj[J_hocl];
+    const T D_r9_c1 = D_r9_c0*xt2 + K[K_d33]*xt47;
+    const T D_r9_c2 = K[K_d35]*xt45 + het[4]*xt12 + tj[J_hocl];
     const T D_r9_c3 = (T(1)/(D_r9_c2));
-    const T D_r9_c4 = D_r9_c3*het[0]*nt_cvt<T>(x[2]);
+    const T D_r9_c4 = D_r9_c3*het[0]*xt2;
     const T D_r9_c5 = D_r9_c1/(D_r9_c2*D_r9_c2);
     const T D_r9 = D_r9_c1*D_r9_c3;
     const T d_D_r9_2 = D_r9_c0*D_r9_c3 + D_r9_c4*d_D_r13_2;
     const T d_D_r9_12 = D_r9_c4*d_D_r13_12 - D_r9_c5*het[4];
-    const T d_D_r9_45 = D_r9_c3*d_D_r13_45*het[0]*nt_cvt<T>(x[2]) - D_r9_c5*K[K_d35];
+    const T d_D_r9_45 = D_r9_c3*d_D_r13_45*het[0]*xt2 - D_r9_c5*K[K_d35];
     const T d_D_r9_47 = D_r9_c3*K[K_d33];
     const T d_D_r9_48 = D_r9_c4*d_D_r13_48;
     const T D_r10_c0 = K[K_d60]/(F.hnm*K[K_d61] + tj[J_cl2o2]);
-    const T D_r10 = D_r10_c0*nt_cvt<T>(x[52]);
+    const T D_r10 = D_r10_c0*xt52;
     const T d_D_r10_52 = D_r10_c0;
     const T D_r12_c0 = K[K_e5c]/tj[J_brcl];
-    const T D_r12 = D_r12_c0*nt_cvt<T>(x[53]);
+    const T D_r12 = D_r12_c0*xt53;
     const T d_D_r12_53 = D_r12_c0;
-    const T D_r11_c0 = K[K_d10]*nt_cvt<T>(x[47]) + K[K_d2]*nt_cvt<T>(x[46]) + K[K_d37]*nt_cvt<T>(x[14]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]);
+    const T D_r11_c0 = K[K_d10]*xt47 + K[K_d2]*xt46 + K[K_d37]*xt14 + K[K_d5]*xt1 + K[K_d7]*xt47;
     const T D_r11_c1 = (T(1)/(D_r11_c0));
     const T D_r11_c2 = T(2)*tj[J_cl2o2];
-    const T D_r11_c3 = D_r10*D_r11_c2 + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*nt_cvt<T>(x[28]) + K[K_d3]*nt_cvt<T>(x[45]) + K[K_d4]*nt_cvt<T>(x[49]) + K[K_d8]*nt_cvt<T>(x[43]) + K[K_e5b]*nt_cvt<T>(x[53]);
+    const T D_r11_c3 = D_r10*D_r11_c2 + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*xt28 + K[K_d3]*xt45 + K[K_d4]*xt49 + K[K_d8]*xt43 + K[K_e5b]*xt53;
     const T D_r11_c4 = D_r11_c3/(D_r11_c0*D_r11_c0);
     const T D_r11_c5 = D_r11_c1*tj[J_clono2_cl];
     const T D_r11_c6 = D_r11_c1*tj[J_hocl];
@@ -3002,40 +3606,40 @@ __device__ __forceinline__ void nt_jacobian_day_w4_2(const FF& F, PK K, PK tj, P
     {  // row 52
     const T rs52 = nt_rscale<T>(nt_exp_hi(x[52]), fh);
         const T dj52_c0 = D_r11 + T(1);
-        const T dj52_c1 = nt_cvt<T>(x[22])/(dj52_c0*dj52_c0);
-        J[369] = (d_D_r11_1*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs52);
-        J[373] = (d_D_r11_2*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs52);
-        J[372] = (d_D_r11_12*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs52);
-        J[370] = (d_D_r11_14*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs52);
-        J[368] = (-T(1)/dj52_c0) * (nt_scale<T>(nt_exp_hi(x[22]), fh) * rs52);
-        J[371] = (d_D_r11_28*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs52);
-        J[377] = (d_D_r11_43*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs52);
-        J[375] = (d_D_r11_45*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs52);
-        J[379] = (d_D_r11_46*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs52);
-        J[378] = (d_D_r11_47*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs52);
-        J[374] = (d_D_r11_48*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs52);
-        J[380] = (d_D_r11_49*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs52);
-        J[381] = (d_D_r11_52*dj52_c1 + T(1)) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs52);
-        J[376] = (d_D_r11_53*dj52_c1) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs52);
+        const T dj52_c1 = xt22/(dj52_c0*dj52_c0);
+        J[369] = (d_D_r11_1*dj52_c1) * (cs1 * rs52);
+        J[373] = (d_D_r11_2*dj52_c1) * (cs2 * rs52);
+        J[372] = (d_D_r11_12*dj52_c1) * (cs12 * rs52);
+        J[370] = (d_D_r11_14*dj52_c1) * (cs14 * rs52);
+        J[368] = (-T(1)/dj52_c0) * (cs22 * rs52);
+        J[371] = (d_D_r11_28*dj52_c1) * (cs28 * rs52);
+        J[377] = (d_D_r11_43*dj52_c1) * (cs43 * rs52);
+        J[375] = (d_D_r11_45*dj52_c1) * (cs45 * rs52);
+        J[379] = (d_D_r11_46*dj52_c1) * (cs46 * rs52);
+        J[378] = (d_D_r11_47*dj52_c1) * (cs47 * rs52);
+        J[374] = (d_D_r11_48*dj52_c1) * (cs48 * rs52);
+        J[380] = (d_D_r11_49*dj52_c1) * (cs49 * rs52);
+        J[381] = (d_D_r11_52*dj52_c1 + T(1)) * (cs52 * rs52);
+        J[376] = (d_D_r11_53*dj52_c1) * (cs53 * rs52);
     }
-    const T D_r27_c0 = K[K_e8]*nt_cvt<T>(x[45]) + tj[J_brono2];
+    const T D_r27_c0 = K[K_e8]*xt45 + tj[J_brono2];
     const T D_r27_c1 = K[K_e13]/D_r27_c0;
-    const T D_r27 = D_r27_c1*nt_cvt<T>(x[48]);
-    const T d_D_r27_45 = -K[K_e13]*K[K_e8]*nt_cvt<T>(x[48])/(D_r27_c0*D_r27_c0);
+    const T D_r27 = D_r27_c1*xt48;
+    const T d_D_r27_45 = -K[K_e13]*K[K_e8]*xt48/(D_r27_c0*D_r27_c0);
     const T d_D_r27_48 = D_r27_c1;
-    const T D_r28_c0 = K[K_e16]*nt_cvt<T>(x[45]) + tj[J_hobr];
+    const T D_r28_c0 = K[K_e16]*xt45 + tj[J_hobr];
     const T D_r28_c1 = K[K_e15]/D_r28_c0;
-    const T D_r28 = D_r28_c1*nt_cvt<T>(x[47]);
-    const T d_D_r28_45 = -K[K_e15]*K[K_e16]*nt_cvt<T>(x[47])/(D_r28_c0*D_r28_c0);
+    const T D_r28 = D_r28_c1*xt47;
+    const T d_D_r28_45 = -K[K_e15]*K[K_e16]*xt47/(D_r28_c0*D_r28_c0);
     const T d_D_r28_47 = D_r28_c1;
     const T D_r29_c0 = K[K_e5c]/tj[J_brcl];
-    const T D_r29 = D_r29_c0*nt_cvt<T>(x[52]);
+    const T D_r29 = D_r29_c0*xt52;
     const T d_D_r29_52 = D_r29_c0;
-    const T D_r30_c0 = K[K_c19]*nt_cvt<T>(x[27]) + K[K_e2]*nt_cvt<T>(x[46]) + K[K_e7]*nt_cvt<T>(x[47]);
+    const T D_r30_c0 = K[K_c19]*xt27 + K[K_e2]*xt46 + K[K_e7]*xt47;
     const T D_r30_c1 = (T(1)/(D_r30_c0));
     const T D_r30_c2 = T(0.85)*tj[J_brono2];
     const T D_r30_c3 = T(2)*K[K_e6];
-    const T D_r30_c4 = D_r27*D_r30_c2 + D_r28*tj[J_hobr] + D_r29*tj[J_brcl] + D_r30_c3*nt_cvt<T>(x[53]) + K[K_e10]*nt_cvt<T>(x[43]) + K[K_e3]*nt_cvt<T>(x[45]) + K[K_e4]*nt_cvt<T>(x[49]) + K[K_e5a]*nt_cvt<T>(x[52]) + K[K_e5b]*nt_cvt<T>(x[52]) + tj[J_bro];
+    const T D_r30_c4 = D_r27*D_r30_c2 + D_r28*tj[J_hobr] + D_r29*tj[J_brcl] + D_r30_c3*xt53 + K[K_e10]*xt43 + K[K_e3]*xt45 + K[K_e4]*xt49 + K[K_e5a]*xt52 + K[K_e5b]*xt52 + tj[J_bro];
     const T D_r30_c5 = D_r30_c4/(D_r30_c0*D_r30_c0);
     const T D_r30_c6 = D_r30_c1*D_r30_c2;
     const T D_r30 = D_r30_c1*D_r30_c4;
@@ -3050,30 +3654,30 @@ __device__ __forceinline__ void nt_jacobian_day_w4_2(const FF& F, PK K, PK tj, P
     const T d_D_r30_53 = D_r30_c1*D_r30_c3;
     {  // row 50
     const T rs50 = nt_rscale<T>(nt_exp_hi(x[50]), fh);
-        J[307] = (-d_D_r30_27*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs50);
-        J[311] = (-d_D_r30_43*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs50);
-        J[309] = (-d_D_r30_45*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs50);
-        J[313] = (-d_D_r30_46*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs50);
-        J[312] = (-d_D_r30_47*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs50);
-        J[308] = (-d_D_r30_48*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs50);
-        J[314] = (-d_D_r30_49*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs50);
-        J[315] = (-d_D_r30_52*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs50);
-        J[310] = (-D_r30 - d_D_r30_53*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs50);
+        J[307] = (-d_D_r30_27*xt53) * (cs27 * rs50);
+        J[311] = (-d_D_r30_43*xt53) * (cs43 * rs50);
+        J[309] = (-d_D_r30_45*xt53) * (cs45 * rs50);
+        J[313] = (-d_D_r30_46*xt53) * (cs46 * rs50);
+        J[312] = (-d_D_r30_47*xt53) * (cs47 * rs50);
+        J[308] = (-d_D_r30_48*xt53) * (cs48 * rs50);
+        J[314] = (-d_D_r30_49*xt53) * (cs49 * rs50);
+        J[315] = (-d_D_r30_52*xt53) * (cs52 * rs50);
+        J[310] = (-D_r30 - d_D_r30_53*xt53) * (cs53 * rs50);
     }
     {  // row 53
     const T rs53 = nt_rscale<T>(nt_exp_hi(x[53]), fh);
         const T dj53_c0 = D_r30 + T(1);
-        const T dj53_c1 = nt_cvt<T>(x[23])/(dj53_c0*dj53_c0);
-        J[297] = (-T(1)/dj53_c0) * (nt_scale<T>(nt_exp_hi(x[23]), fh) * rs53);
-        J[298] = (d_D_r30_27*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs53);
-        J[302] = (d_D_r30_43*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs53);
-        J[300] = (d_D_r30_45*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs53);
-        J[304] = (d_D_r30_46*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs53);
-        J[303] = (d_D_r30_47*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs53);
-        J[299] = (d_D_r30_48*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs53);
-        J[305] = (d_D_r30_49*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs53);
-        J[306] = (d_D_r30_52*dj53_c1) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs53);
-        J[301] = (d_D_r30_53*dj53_c1 + T(1)) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs53);
+        const T dj53_c1 = xt23/(dj53_c0*dj53_c0);
+        J[297] = (-T(1)/dj53_c0) * (cs23 * rs53);
+        J[298] = (d_D_r30_27*dj53_c1) * (cs27 * rs53);
+        J[302] = (d_D_r30_43*dj53_c1) * (cs43 * rs53);
+        J[300] = (d_D_r30_45*dj53_c1) * (cs45 * rs53);
+        J[304] = (d_D_r30_46*dj53_c1) * (cs46 * rs53);
+        J[303] = (d_D_r30_47*dj53_c1) * (cs47 * rs53);
+        J[299] = (d_D_r30_48*dj53_c1) * (cs48 * rs53);
+        J[305] = (d_D_r30_49*dj53_c1) * (cs49 * rs53);
+        J[306] = (d_D_r30_52*dj53_c1) * (cs52 * rs53);
+        J[301] = (d_D_r30_53*dj53_c1 + T(1)) * (cs53 * rs53);
     }
 }
 
@@ -3113,162 +3717,253 @@ __device__ __forceinline__ void nt_residual_day_w4_3(const FF& F, PK K, PK tj, P
 template <typename T, typename FF, typename PK, typename PJ>
 __device__ __forceinline__ void nt_jacobian_day_w4_3(const FF& F, PK K, PK tj, PK het, const double* __restrict__ x, double floor_, PJ J) {
     const int fh = nt_exp_hi(floor_);
+    const T xt0 = nt_cvt<T>(x[0]);
+    const T xt1 = nt_cvt<T>(x[1]);
+    const T xt2 = nt_cvt<T>(x[2]);
+    const T xt3 = nt_cvt<T>(x[3]);
+    const T xt4 = nt_cvt<T>(x[4]);
+    const T xt5 = nt_cvt<T>(x[5]);
+    const T xt6 = nt_cvt<T>(x[6]);
+    const T xt7 = nt_cvt<T>(x[7]);
+    const T xt8 = nt_cvt<T>(x[8]);
+    const T xt9 = nt_cvt<T>(x[9]);
+    const T xt10 = nt_cvt<T>(x[10]);
+    const T xt11 = nt_cvt<T>(x[11]);
+    const T xt12 = nt_cvt<T>(x[12]);
+    const T xt13 = nt_cvt<T>(x[13]);
+    const T xt14 = nt_cvt<T>(x[14]);
+    const T xt15 = nt_cvt<T>(x[15]);
+    const T xt16 = nt_cvt<T>(x[16]);
+    const T xt17 = nt_cvt<T>(x[17]);
+    const T xt18 = nt_cvt<T>(x[18]);
+    const T xt19 = nt_cvt<T>(x[19]);
+    const T xt20 = nt_cvt<T>(x[20]);
+    const T xt21 = nt_cvt<T>(x[21]);
+    const T xt22 = nt_cvt<T>(x[22]);
+    const T xt23 = nt_cvt<T>(x[23]);
+    const T xt24 = nt_cvt<T>(x[24]);
+    const T xt25 = nt_cvt<T>(x[25]);
+    const T xt26 = nt_cvt<T>(x[26]);
+    const T xt27 = nt_cvt<T>(x[27]);
+    const T xt28 = nt_cvt<T>(x[28]);
+    const T xt29 = nt_cvt<T>(x[29]);
+    const T xt30 = nt_cvt<T>(x[30]);
+    const T xt31 = nt_cvt<T>(x[31]);
+    const T xt32 = nt_cvt<T>(x[32]);
+    const T xt33 = nt_cvt<T>(x[33]);
+    const T xt34 = nt_cvt<T>(x[34]);
+    const T xt35 = nt_cvt<T>(x[35]);
+    const T xt36 = nt_cvt<T>(x[36]);
+    const T xt37 = nt_cvt<T>(x[37]);
+    const T xt38 = nt_cvt<T>(x[38]);
+    const T xt39 = nt_cvt<T>(x[39]);
+    const T xt40 = nt_cvt<T>(x[40]);
+    const T xt41 = nt_cvt<T>(x[41]);
+    const T xt42 = nt_cvt<T>(x[42]);
+    const T xt43 = nt_cvt<T>(x[43]);
+    const T xt44 = nt_cvt<T>(x[44]);
+    const T xt45 = nt_cvt<T>(x[45]);
+    const T xt46 = nt_cvt<T>(x[46]);
+    const T xt47 = nt_cvt<T>(x[47]);
+    const T xt48 = nt_cvt<T>(x[48]);
+    const T xt49 = nt_cvt<T>(x[49]);
+    const T xt50 = nt_cvt<T>(x[50]);
+    const T xt51 = nt_cvt<T>(x[51]);
+    const T xt52 = nt_cvt<T>(x[52]);
+    const T xt53 = nt_cvt<T>(x[53]);
+    const T xt54 = nt_cvt<T>(x[54]);
+    const T xt55 = nt_cvt<T>(x[55]);
+    const T xt56 = nt_cvt<T>(x[56]);
+    const T cs1 = nt_scale<T>(nt_exp_hi(x[1]), fh);
+    const T cs2 = nt_scale<T>(nt_exp_hi(x[2]), fh);
+    const T cs4 = nt_scale<T>(nt_exp_hi(x[4]), fh);
+    const T cs12 = nt_scale<T>(nt_exp_hi(x[12]), fh);
+    const T cs13 = nt_scale<T>(nt_exp_hi(x[13]), fh);
+    const T cs14 = nt_scale<T>(nt_exp_hi(x[14]), fh);
+    const T cs16 = nt_scale<T>(nt_exp_hi(x[16]), fh);
+    const T cs18 = nt_scale<T>(nt_exp_hi(x[18]), fh);
+    const T cs19 = nt_scale<T>(nt_exp_hi(x[19]), fh);
+    const T cs20 = nt_scale<T>(nt_exp_hi(x[20]), fh);
+    const T cs21 = nt_scale<T>(nt_exp_hi(x[21]), fh);
+    const T cs24 = nt_scale<T>(nt_exp_hi(x[24]), fh);
+    const T cs25 = nt_scale<T>(nt_exp_hi(x[25]), fh);
+    const T cs26 = nt_scale<T>(nt_exp_hi(x[26]), fh);
+    const T cs27 = nt_scale<T>(nt_exp_hi(x[27]), fh);
+    const T cs28 = nt_scale<T>(nt_exp_hi(x[28]), fh);
+    const T cs29 = nt_scale<T>(nt_exp_hi(x[29]), fh);
+    const T cs32 = nt_scale<T>(nt_exp_hi(x[32]), fh);
+    const T cs35 = nt_scale<T>(nt_exp_hi(x[35]), fh);
+    const T cs37 = nt_scale<T>(nt_exp_hi(x[37]), fh);
+    const T cs41 = nt_scale<T>(nt_exp_hi(x[41]), fh);
+    const T cs42 = nt_scale<T>(nt_exp_hi(x[42]), fh);
+    const T cs43 = nt_scale<T>(nt_exp_hi(x[43]), fh);
+    const T cs44 = nt_scale<T>(nt_exp_hi(x[44]), fh);
+    const T cs45 = nt_scale<T>(nt_exp_hi(x[45]), fh);
+    const T cs46 = nt_scale<T>(nt_exp_hi(x[46]), fh);
+    const T cs47 = nt_scale<T>(nt_exp_hi(x[47]), fh);
+    const T cs48 = nt_scale<T>(nt_exp_hi(x[48]), fh);
+    const T cs49 = nt_scale<T>(nt_exp_hi(x[49]), fh);
+    const T cs50 = nt_scale<T>(nt_exp_hi(x[50]), fh);
+    const T cs52 = nt_scale<T>(nt_exp_hi(x[52]), fh);
+    const T cs53 = nt_scale<T>(nt_exp_hi(x[53]), fh);
+    const T cs55 = nt_scale<T>(nt_exp_hi(x[55]), fh);
+    const T cs56 = nt_scale<T>(nt_exp_hi(x[56]), fh);
     {  // row 2
     const T rs2 = nt_rscale<T>(nt_exp_hi(x[2]), fh);
-        const T dj2_c0 = F.dt*nt_cvt<T>(x[43]);
+        const T dj2_c0 = F.dt*xt43;
         const T dj2_c1 = F.dt*F.parth2o;
         const T dj2_c2 = F.parthno3*K[K_b27];
         const T dj2_c3 = F.parthcl*K[K_d11];
-        J[261] = (-K[K_c2]*dj2_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs2);
-        J[266] = (dj2_c1*(K[K_a1et]*nt_cvt<T>(x[42]) + tj[J_h2o]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs2);
-        J[260] = (-dj2_c0*dj2_c2) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs2);
-        J[265] = (-dj2_c0*dj2_c3) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs2);
-        J[262] = (-K[K_a30]*dj2_c0) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs2);
-        J[264] = (-K[K_c8]*dj2_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs2);
-        J[258] = (-F.dt*(K[K_c17a]*nt_cvt<T>(x[43]) + K[K_c17b]*nt_cvt<T>(x[43]))) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs2);
-        J[259] = (K[K_a1et]*dj2_c1*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs2);
-        J[267] = (-F.dt*(F.h2*K[K_a19] + K[K_a17]*nt_cvt<T>(x[47]) + K[K_a30]*nt_cvt<T>(x[16]) + T(2)*K[K_a31]*nt_cvt<T>(x[43]) + K[K_c17a]*nt_cvt<T>(x[29]) + K[K_c17b]*nt_cvt<T>(x[29]) + K[K_c2]*nt_cvt<T>(x[1]) + K[K_c8]*nt_cvt<T>(x[27]) + dj2_c2*nt_cvt<T>(x[4]) + dj2_c3*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs2);
-        J[268] = (-F.dt*(K[K_a17]*nt_cvt<T>(x[43]) + T(1.6e-12)*nt_cvt<T>(x[55]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs2);
-        J[263] = (-T(1.6e-12)*F.dt*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs2);
+        J[261] = (-K[K_c2]*dj2_c0) * (cs1 * rs2);
+        J[266] = (dj2_c1*(K[K_a1et]*xt42 + tj[J_h2o]) + T(1)) * (cs2 * rs2);
+        J[260] = (-dj2_c0*dj2_c2) * (cs4 * rs2);
+        J[265] = (-dj2_c0*dj2_c3) * (cs12 * rs2);
+        J[262] = (-K[K_a30]*dj2_c0) * (cs16 * rs2);
+        J[264] = (-K[K_c8]*dj2_c0) * (cs27 * rs2);
+        J[258] = (-F.dt*(K[K_c17a]*xt43 + K[K_c17b]*xt43)) * (cs29 * rs2);
+        J[259] = (K[K_a1et]*dj2_c1*xt2) * (cs42 * rs2);
+        J[267] = (-F.dt*(F.h2*K[K_a19] + K[K_a17]*xt47 + K[K_a30]*xt16 + T(2)*K[K_a31]*xt43 + K[K_c17a]*xt29 + K[K_c17b]*xt29 + K[K_c2]*xt1 + K[K_c8]*xt27 + dj2_c2*xt4 + dj2_c3*xt12)) * (cs43 * rs2);
+        J[268] = (-F.dt*(K[K_a17]*xt43 + T(1.6e-12)*xt55)) * (cs47 * rs2);
+        J[263] = (-T(1.6e-12)*F.dt*xt47) * (cs55 * rs2);
     }
     {  // row 14
     const T rs14 = nt_rscale<T>(nt_exp_hi(x[14]), fh);
         const T dj14_c0 = F.dt*het[0];
-        const T dj14_c1 = F.dt*nt_cvt<T>(x[14]);
+        const T dj14_c1 = F.dt*xt14;
         const T dj14_c2 = F.dt*K[K_d33];
-        J[170] = (-dj14_c0*nt_cvt<T>(x[13])) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs14);
-        J[169] = (dj14_c1*het[4]) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs14);
-        J[166] = (-dj14_c0*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs14);
-        J[167] = (F.dt*(K[K_d34]*nt_cvt<T>(x[43]) + K[K_d35]*nt_cvt<T>(x[45]) + K[K_d37]*nt_cvt<T>(x[44]) + het[4]*nt_cvt<T>(x[12]) + het[8]*nt_cvt<T>(x[18]) + tj[J_hocl]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs14);
-        J[168] = (dj14_c1*het[8]) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs14);
-        J[173] = (K[K_d34]*dj14_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs14);
-        J[172] = (K[K_d37]*dj14_c1) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs14);
-        J[171] = (K[K_d35]*dj14_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs14);
-        J[174] = (-dj14_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs14);
-        J[175] = (-dj14_c2*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs14);
+        J[170] = (-dj14_c0*xt13) * (cs2 * rs14);
+        J[169] = (dj14_c1*het[4]) * (cs12 * rs14);
+        J[166] = (-dj14_c0*xt2) * (cs13 * rs14);
+        J[167] = (F.dt*(K[K_d34]*xt43 + K[K_d35]*xt45 + K[K_d37]*xt44 + het[4]*xt12 + het[8]*xt18 + tj[J_hocl]) + T(1)) * (cs14 * rs14);
+        J[168] = (dj14_c1*het[8]) * (cs18 * rs14);
+        J[173] = (K[K_d34]*dj14_c1) * (cs43 * rs14);
+        J[172] = (K[K_d37]*dj14_c1) * (cs44 * rs14);
+        J[171] = (K[K_d35]*dj14_c1) * (cs45 * rs14);
+        J[174] = (-dj14_c2*xt52) * (cs47 * rs14);
+        J[175] = (-dj14_c2*xt47) * (cs52 * rs14);
     }
     {  // row 19
     const T rs19 = nt_rscale<T>(nt_exp_hi(x[19]), fh);
-        const T dj19_c0 = F.dt*nt_cvt<T>(x[19]);
+        const T dj19_c0 = F.dt*xt19;
         const T dj19_c1 = F.dt*K[K_e13];
-        J[56] = (dj19_c0*het[5]) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs19);
-        J[55] = (F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + het[5]*nt_cvt<T>(x[2]) + tj[J_brono2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs19);
-        J[58] = (K[K_e8]*dj19_c0) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs19);
-        J[57] = (-dj19_c1*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs19);
-        J[59] = (-dj19_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs19);
+        J[56] = (dj19_c0*het[5]) * (cs2 * rs19);
+        J[55] = (F.dt*(K[K_e8]*xt45 + het[5]*xt2 + tj[J_brono2]) + T(1)) * (cs19 * rs19);
+        J[58] = (K[K_e8]*dj19_c0) * (cs45 * rs19);
+        J[57] = (-dj19_c1*xt53) * (cs48 * rs19);
+        J[59] = (-dj19_c1*xt48) * (cs53 * rs19);
     }
     {  // row 21
     const T rs21 = nt_rscale<T>(nt_exp_hi(x[21]), fh);
         const T dj21_c0 = F.dt*K[K_b23];
-        J[152] = (F.dt*(F.hnm*K[K_b24] + K[K_b28]*nt_cvt<T>(x[43]) + tj[J_hno4]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[21]), fh) * rs21);
-        J[154] = (F.dt*K[K_b28]*nt_cvt<T>(x[21])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs21);
-        J[155] = (-dj21_c0*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs21);
-        J[153] = (-dj21_c0*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs21);
+        J[152] = (F.dt*(F.hnm*K[K_b24] + K[K_b28]*xt43 + tj[J_hno4]) + T(1)) * (cs21 * rs21);
+        J[154] = (F.dt*K[K_b28]*xt21) * (cs43 * rs21);
+        J[155] = (-dj21_c0*xt48) * (cs47 * rs21);
+        J[153] = (-dj21_c0*xt47) * (cs48 * rs21);
     }
     {  // row 23
     const T rs23 = nt_rscale<T>(nt_exp_hi(x[23]), fh);
         const T dj23_c0 = T(2)*het[7];
-        const T dj23_c1 = F.dt*F.parthbr*nt_cvt<T>(x[18]);
-        const T dj23_c2 = F.dt*nt_cvt<T>(x[53]);
-        J[196] = (-F.dt*(F.parthbr*(K[K_e11]*nt_cvt<T>(x[43]) + K[K_e9]*nt_cvt<T>(x[42]) + tj[J_hbr]) + dj23_c0*nt_cvt<T>(x[25]))) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs23);
-        J[193] = (-F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + tj[J_brono2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs23);
-        J[194] = (-F.dt*(K[K_e16]*nt_cvt<T>(x[45]) + dj23_c0*nt_cvt<T>(x[18]) + tj[J_hobr])) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs23);
-        J[192] = (-F.dt*tj[J_brcl]) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs23);
-        J[197] = (F.dt*K[K_c19]*nt_cvt<T>(x[50])) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs23);
-        J[195] = (-K[K_e9]*dj23_c1) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs23);
-        J[202] = (-K[K_e11]*dj23_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs23);
-        J[199] = (-F.dt*(K[K_e16]*nt_cvt<T>(x[25]) + K[K_e8]*nt_cvt<T>(x[19]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs23);
-        J[203] = (F.dt*(K[K_e15]*nt_cvt<T>(x[53]) + K[K_e7]*nt_cvt<T>(x[50]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs23);
-        J[198] = (K[K_e13]*dj23_c2) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs23);
-        J[201] = (F.dt*(K[K_c19]*nt_cvt<T>(x[27]) + K[K_e7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs23);
-        J[204] = (K[K_e5c]*dj23_c2) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs23);
-        J[200] = (F.dt*(K[K_e13]*nt_cvt<T>(x[48]) + K[K_e15]*nt_cvt<T>(x[47]) + K[K_e5c]*nt_cvt<T>(x[52]))) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs23);
+        const T dj23_c1 = F.dt*F.parthbr*xt18;
+        const T dj23_c2 = F.dt*xt53;
+        J[196] = (-F.dt*(F.parthbr*(K[K_e11]*xt43 + K[K_e9]*xt42 + tj[J_hbr]) + dj23_c0*xt25)) * (cs18 * rs23);
+        J[193] = (-F.dt*(K[K_e8]*xt45 + tj[J_brono2])) * (cs19 * rs23);
+        J[194] = (-F.dt*(K[K_e16]*xt45 + dj23_c0*xt18 + tj[J_hobr])) * (cs25 * rs23);
+        J[192] = (-F.dt*tj[J_brcl]) * (cs26 * rs23);
+        J[197] = (F.dt*K[K_c19]*xt50) * (cs27 * rs23);
+        J[195] = (-K[K_e9]*dj23_c1) * (cs42 * rs23);
+        J[202] = (-K[K_e11]*dj23_c1) * (cs43 * rs23);
+        J[199] = (-F.dt*(K[K_e16]*xt25 + K[K_e8]*xt19)) * (cs45 * rs23);
+        J[203] = (F.dt*(K[K_e15]*xt53 + K[K_e7]*xt50)) * (cs47 * rs23);
+        J[198] = (K[K_e13]*dj23_c2) * (cs48 * rs23);
+        J[201] = (F.dt*(K[K_c19]*xt27 + K[K_e7]*xt47)) * (cs50 * rs23);
+        J[204] = (K[K_e5c]*dj23_c2) * (cs52 * rs23);
+        J[200] = (F.dt*(K[K_e13]*xt48 + K[K_e15]*xt47 + K[K_e5c]*xt52)) * (cs53 * rs23);
     }
     {  // row 24
     const T rs24 = nt_rscale<T>(nt_exp_hi(x[24]), fh);
-        J[97] = (F.dt*(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[24]), fh) * rs24);
-        J[98] = (-T(2)*F.dt*K[K_d60]*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs24);
+        J[97] = (F.dt*(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(1)) * (cs24 * rs24);
+        J[98] = (-T(2)*F.dt*K[K_d60]*xt52) * (cs52 * rs24);
     }
     {  // row 26
     const T rs26 = nt_rscale<T>(nt_exp_hi(x[26]), fh);
         const T dj26_c0 = F.dt*het[6];
         const T dj26_c1 = F.dt*het[8];
         const T dj26_c2 = F.dt*K[K_e5c];
-        J[47] = (-dj26_c0*nt_cvt<T>(x[25])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs26);
-        J[45] = (-dj26_c1*nt_cvt<T>(x[18])) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs26);
-        J[46] = (-dj26_c1*nt_cvt<T>(x[14])) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs26);
-        J[44] = (-dj26_c0*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs26);
-        J[43] = (F.dt*tj[J_brcl] + T(1)) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs26);
-        J[49] = (-dj26_c2*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs26);
-        J[48] = (-dj26_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs26);
+        J[47] = (-dj26_c0*xt25) * (cs12 * rs26);
+        J[45] = (-dj26_c1*xt18) * (cs14 * rs26);
+        J[46] = (-dj26_c1*xt14) * (cs18 * rs26);
+        J[44] = (-dj26_c0*xt12) * (cs25 * rs26);
+        J[43] = (F.dt*tj[J_brcl] + T(1)) * (cs26 * rs26);
+        J[49] = (-dj26_c2*xt53) * (cs52 * rs26);
+        J[48] = (-dj26_c2*xt52) * (cs53 * rs26);
     }
     {  // row 28
     const T rs28 = nt_rscale<T>(nt_exp_hi(x[28]), fh);
-        const T dj28_c0 = T(2)*K[K_c14]*nt_cvt<T>(x[28]);
+        const T dj28_c0 = T(2)*K[K_c14]*xt28;
         const T dj28_c1 = F.dt*K[K_c17a];
-        const T dj28_c2 = F.dt*nt_cvt<T>(x[28]);
-        J[212] = (F.dt*dj28_c0 + F.dt*(K[K_c18]*nt_cvt<T>(x[52]) + K[K_c5]*nt_cvt<T>(x[49]) + K[K_c7]*nt_cvt<T>(x[47]) + dj28_c0) + T(1)) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs28);
-        J[210] = (-dj28_c1*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs28);
-        J[213] = (-dj28_c1*nt_cvt<T>(x[29])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs28);
-        J[214] = (K[K_c7]*dj28_c2) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs28);
-        J[215] = (K[K_c5]*dj28_c2) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs28);
-        J[216] = (K[K_c18]*dj28_c2) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs28);
-        J[211] = (-F.dt*F.o2*K[K_c4]) * (nt_scale<T>(nt_exp_hi(x[56]), fh) * rs28);
+        const T dj28_c2 = F.dt*xt28;
+        J[212] = (F.dt*dj28_c0 + F.dt*(K[K_c18]*xt52 + K[K_c5]*xt49 + K[K_c7]*xt47 + dj28_c0) + T(1)) * (cs28 * rs28);
+        J[210] = (-dj28_c1*xt43) * (cs29 * rs28);
+        J[213] = (-dj28_c1*xt29) * (cs43 * rs28);
+        J[214] = (K[K_c7]*dj28_c2) * (cs47 * rs28);
+        J[215] = (K[K_c5]*dj28_c2) * (cs49 * rs28);
+        J[216] = (K[K_c18]*dj28_c2) * (cs52 * rs28);
+        J[211] = (-F.dt*F.o2*K[K_c4]) * (cs56 * rs28);
     }
     {  // row 32
     const T rs32 = nt_rscale<T>(nt_exp_hi(x[32]), fh);
-        J[18] = (F.dt*(K[K_d92]*nt_cvt<T>(x[42]) + tj[J_cfc113]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs32);
-        J[19] = (F.dt*K[K_d92]*nt_cvt<T>(x[32])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs32);
+        J[18] = (F.dt*(K[K_d92]*xt42 + tj[J_cfc113]) + T(1)) * (cs32 * rs32);
+        J[19] = (F.dt*K[K_d92]*xt32) * (cs42 * rs32);
     }
     {  // row 35
     const T rs35 = nt_rscale<T>(nt_exp_hi(x[35]), fh);
-        J[66] = (F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs35);
-        J[67] = (F.dt*K[K_d95]*nt_cvt<T>(x[35])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs35);
+        J[66] = (F.dt*(K[K_d95]*xt43 + tj[J_ch3cl]) + T(1)) * (cs35 * rs35);
+        J[67] = (F.dt*K[K_d95]*xt35) * (cs43 * rs35);
     }
     {  // row 37
     const T rs37 = nt_rscale<T>(nt_exp_hi(x[37]), fh);
-        const T dj37_c0 = F.dt*nt_cvt<T>(x[37]);
-        J[52] = (F.dt*(K[K_e50]*nt_cvt<T>(x[42]) + K[K_e51]*nt_cvt<T>(x[43]) + tj[J_ch3br]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[37]), fh) * rs37);
-        J[53] = (K[K_e50]*dj37_c0) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs37);
-        J[54] = (K[K_e51]*dj37_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs37);
+        const T dj37_c0 = F.dt*xt37;
+        J[52] = (F.dt*(K[K_e50]*xt42 + K[K_e51]*xt43 + tj[J_ch3br]) + T(1)) * (cs37 * rs37);
+        J[53] = (K[K_e50]*dj37_c0) * (cs42 * rs37);
+        J[54] = (K[K_e51]*dj37_c0) * (cs43 * rs37);
     }
     {  // row 41
     const T rs41 = nt_rscale<T>(nt_exp_hi(x[41]), fh);
-        J[125] = (F.dt*(K[K_e54]*nt_cvt<T>(x[43]) + tj[J_ch2br2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[41]), fh) * rs41);
-        J[126] = (F.dt*K[K_e54]*nt_cvt<T>(x[41])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs41);
+        J[125] = (F.dt*(K[K_e54]*xt43 + tj[J_ch2br2]) + T(1)) * (cs41 * rs41);
+        J[126] = (F.dt*K[K_e54]*xt41) * (cs43 * rs41);
     }
     {  // row 56
     const T rs56 = nt_rscale<T>(nt_exp_hi(x[56]), fh);
-        const T dj56_c0 = F.o2*K[K_c4] + K[K_c3]*nt_cvt<T>(x[45]);
+        const T dj56_c0 = F.o2*K[K_c4] + K[K_c3]*xt45;
         const T dj56_c1 = (T(1)/(dj56_c0));
-        const T dj56_c2 = K[K_c1a]*nt_cvt<T>(x[42]) + K[K_c2]*nt_cvt<T>(x[43]) + K[K_d5]*nt_cvt<T>(x[44]);
-        const T dj56_c3 = dj56_c1*nt_cvt<T>(x[1]);
-        J[177] = (-dj56_c1*dj56_c2) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs56);
-        J[176] = (-K[K_c1a]*dj56_c3) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs56);
-        J[180] = (-K[K_c2]*dj56_c3) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs56);
-        J[179] = (-K[K_d5]*dj56_c3) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs56);
-        J[178] = (K[K_c3]*dj56_c2*nt_cvt<T>(x[1])/(dj56_c0*dj56_c0)) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs56);
+        const T dj56_c2 = K[K_c1a]*xt42 + K[K_c2]*xt43 + K[K_d5]*xt44;
+        const T dj56_c3 = dj56_c1*xt1;
+        J[177] = (-dj56_c1*dj56_c2) * (cs1 * rs56);
+        J[176] = (-K[K_c1a]*dj56_c3) * (cs42 * rs56);
+        J[180] = (-K[K_c2]*dj56_c3) * (cs43 * rs56);
+        J[179] = (-K[K_d5]*dj56_c3) * (cs44 * rs56);
+        J[178] = (K[K_c3]*dj56_c2*xt1/(dj56_c0*dj56_c0)) * (cs45 * rs56);
     }
-    const T D_r7_c0 = F.o2*K[K_b7] + K[K_b6]*nt_cvt<T>(x[49]);
+    const T D_r7_c0 = F.o2*K[K_b7] + K[K_b6]*xt49;
     const T D_r7 = tj[J_no]/D_r7_c0;
     const T d_D_r7_49 = -K[K_b6]*tj[J_no]/(D_r7_c0*D_r7_c0);
     {  // row 51
     const T rs51 = nt_rscale<T>(nt_exp_hi(x[51]), fh);
-        J[78] = (-D_r7 - d_D_r7_49*nt_cvt<T>(x[49])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs51);
+        J[78] = (-D_r7 - d_D_r7_49*xt49) * (cs49 * rs51);
     }
-    const T D_r8_c0 = K[K_b12]*nt_cvt<T>(x[48]) + tj[J_no3_no2] + tj[J_no3_no];
+    const T D_r8_c0 = K[K_b12]*xt48 + tj[J_no3_no2] + tj[J_no3_no];
     const T D_r8_c1 = K[K_b9]/D_r8_c0;
-    const T D_r8 = D_r8_c1*nt_cvt<T>(x[46]);
+    const T D_r8 = D_r8_c1*xt46;
     const T d_D_r8_46 = D_r8_c1;
-    const T d_D_r8_48 = -K[K_b12]*K[K_b9]*nt_cvt<T>(x[46])/(D_r8_c0*D_r8_c0);
+    const T d_D_r8_48 = -K[K_b12]*K[K_b9]*xt46/(D_r8_c0*D_r8_c0);
     {  // row 54
     const T rs54 = nt_rscale<T>(nt_exp_hi(x[54]), fh);
         J[68] = T(0);
-        J[70] = (-d_D_r8_46*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs54);
-        J[69] = (-D_r8 - d_D_r8_48*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs54);
+        J[70] = (-d_D_r8_46*xt48) * (cs46 * rs54);
+        J[69] = (-D_r8 - d_D_r8_48*xt48) * (cs48 * rs54);
     }
-    const T D_r5_c0 = D_r8*tj[J_no3_no] + K[K_b3]*nt_cvt<T>(x[45]) + tj[J_no2];
-    const T D_r5_c1 = K[K_a26]*nt_cvt<T>(x[47]) + K[K_b4]*nt_cvt<T>(x[46]) + K[K_c5]*nt_cvt<T>(x[28]) + K[K_d4]*nt_cvt<T>(x[52]) + K[K_e4]*nt_cvt<T>(x[53]);
+    const T D_r5_c0 = D_r8*tj[J_no3_no] + K[K_b3]*xt45 + tj[J_no2];
+    const T D_r5_c1 = K[K_a26]*xt47 + K[K_b4]*xt46 + K[K_c5]*xt28 + K[K_d4]*xt52 + K[K_e4]*xt53;
     const T D_r5_c2 = (T(1)/(D_r5_c1));
     const T D_r5_c3 = D_r5_c0/(D_r5_c1*D_r5_c1);
     const T D_r5 = D_r5_c0*D_r5_c2;
@@ -3283,58 +3978,58 @@ __device__ __forceinline__ void nt_jacobian_day_w4_3(const FF& F, PK K, PK tj, P
     const T rs48 = nt_rscale<T>(nt_exp_hi(x[48]), fh);
         const T dj48_c0 = D_r5*D_r7 + D_r5 + D_r8 + T(1);
         const T dj48_c1 = (T(1)/(dj48_c0*dj48_c0));
-        const T dj48_c2 = dj48_c1*nt_cvt<T>(x[20]);
+        const T dj48_c2 = dj48_c1*xt20;
         const T dj48_c3 = dj48_c2*(-D_r7 + T(-1));
-        J[270] = (-T(1)/dj48_c0) * (nt_scale<T>(nt_exp_hi(x[20]), fh) * rs48);
-        J[269] = (-d_D_r5_28*dj48_c3) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs48);
-        J[272] = (-d_D_r5_45*dj48_c3) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs48);
-        J[275] = (-d_D_r5_46*dj48_c3 + d_D_r8_46*dj48_c1*nt_cvt<T>(x[20])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs48);
-        J[274] = (-d_D_r5_47*dj48_c3) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs48);
-        J[271] = (-d_D_r5_48*dj48_c3 + d_D_r8_48*dj48_c2 + T(1)) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs48);
-        J[276] = (D_r5*d_D_r7_49*dj48_c2) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs48);
-        J[277] = (-d_D_r5_52*dj48_c3) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs48);
-        J[273] = (-d_D_r5_53*dj48_c3) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs48);
+        J[270] = (-T(1)/dj48_c0) * (cs20 * rs48);
+        J[269] = (-d_D_r5_28*dj48_c3) * (cs28 * rs48);
+        J[272] = (-d_D_r5_45*dj48_c3) * (cs45 * rs48);
+        J[275] = (-d_D_r5_46*dj48_c3 + d_D_r8_46*dj48_c1*xt20) * (cs46 * rs48);
+        J[274] = (-d_D_r5_47*dj48_c3) * (cs47 * rs48);
+        J[271] = (-d_D_r5_48*dj48_c3 + d_D_r8_48*dj48_c2 + T(1)) * (cs48 * rs48);
+        J[276] = (D_r5*d_D_r7_49*dj48_c2) * (cs49 * rs48);
+        J[277] = (-d_D_r5_52*dj48_c3) * (cs52 * rs48);
+        J[273] = (-d_D_r5_53*dj48_c3) * (cs53 * rs48);
     }
     {  // row 49
     const T rs49 = nt_rscale<T>(nt_exp_hi(x[49]), fh);
-        J[361] = (-d_D_r5_28*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs49);
-        J[363] = (-d_D_r5_45*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs49);
-        J[366] = (-d_D_r5_46*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs49);
-        J[365] = (-d_D_r5_47*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs49);
-        J[362] = (-D_r5 - d_D_r5_48*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs49);
-        J[367] = (-d_D_r5_52*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs49);
-        J[364] = (-d_D_r5_53*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs49);
+        J[361] = (-d_D_r5_28*xt48) * (cs28 * rs49);
+        J[363] = (-d_D_r5_45*xt48) * (cs45 * rs49);
+        J[366] = (-d_D_r5_46*xt48) * (cs46 * rs49);
+        J[365] = (-d_D_r5_47*xt48) * (cs47 * rs49);
+        J[362] = (-D_r5 - d_D_r5_48*xt48) * (cs48 * rs49);
+        J[367] = (-d_D_r5_52*xt48) * (cs52 * rs49);
+        J[364] = (-d_D_r5_53*xt48) * (cs53 * rs49);
     }
-    const T D_r13_c0 = K[K_d32]*nt_cvt<T>(x[45]) + het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]) + tj[J_clono2_cl] + tj[J_clono2_clo];
+    const T D_r13_c0 = K[K_d32]*xt45 + het[0]*xt2 + het[1]*xt12 + tj[J_clono2_cl] + tj[J_clono2_clo];
     const T D_r13_c1 = K[K_d31]/D_r13_c0;
-    const T D_r13_c2 = K[K_d31]*nt_cvt<T>(x[48])/(D_r13_c0*D_r13_c0);
-    const T D_r13 = D_r13_c1*nt_cvt<T>(x[48]);
+    const T D_r13_c2 = K[K_d31]*xt48/(D_r13_c0*D_r13_c0);
+    const T D_r13 = D_r13_c1*xt48;
     const T d_D_r13_2 = -D_r13_c2*het[0];
     const T d_D_r13_12 = -D_r13_c2*het[1];
     const T d_D_r13_45 = -D_r13_c2*K[K_d32];
     const T d_D_r13_48 = D_r13_c1;
     const T D_r9_c0 = D_r13*het[0];
-    const T D_r9_c1 = D_r9_c0*nt_cvt<T>(x[2]) + K[K_d33]*nt_cvt<T>(x[47]);
-    const T D_r9_c2 = K[K_d35]*nt_cvt<T>(x[45]) + het[4]*nt_cvt<T>(x[12]) + tj[J_hocl];
+    const T D_r9_c1 = D_r9_c0*xt2 + K[K_d33]*xt47;
+    const T D_r9_c2 = K[K_d35]*xt45 + het[4]*xt12 + tj[J_hocl];
     const T D_r9_c3 = (T(1)/(D_r9_c2));
-    const T D_r9_c4 = D_r9_c3*het[0]*nt_cvt<T>(x[2]);
+    const T D_r9_c4 = D_r9_c3*het[0]*xt2;
     const T D_r9_c5 = D_r9_c1/(D_r9_c2*D_r9_c2);
     const T D_r9 = D_r9_c1*D_r9_c3;
     const T d_D_r9_2 = D_r9_c0*D_r9_c3 + D_r9_c4*d_D_r13_2;
     const T d_D_r9_12 = D_r9_c4*d_D_r13_12 - D_r9_c5*het[4];
-    const T d_D_r9_45 = D_r9_c3*d_D_r13_45*het[0]*nt_cvt<T>(x[2]) - D_r9_c5*K[K_d35];
+    const T d_D_r9_45 = D_r9_c3*d_D_r13_45*het[0]*xt2 - D_r9_c5*K[K_d35];
     const T d_D_r9_47 = D_r9_c3*K[K_d33];
     const T d_D_r9_48 = D_r9_c4*d_D_r13_48;
     const T D_r10_c0 = K[K_d60]/(F.hnm*K[K_d61] + tj[J_cl2o2]);
-    const T D_r10 = D_r10_c0*nt_cvt<T>(x[52]);
+    const T D_r10 = D_r10_c0*xt52;
     const T d_D_r10_52 = D_r10_c0;
     const T D_r12_c0 = K[K_e5c]/tj[J_brcl];
-    const T D_r12 = D_r12_c0*nt_cvt<T>(x[53]);
+    const T D_r12 = D_r12_c0*xt53;
     const T d_D_r12_53 = D_r12_c0;
-    const T D_r11_c0 = K[K_d10]*nt_cvt<T>(x[47]) + K[K_d2]*nt_cvt<T>(x[46]) + K[K_d37]*nt_cvt<T>(x[14]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]);
+    const T D_r11_c0 = K[K_d10]*xt47 + K[K_d2]*xt46 + K[K_d37]*xt14 + K[K_d5]*xt1 + K[K_d7]*xt47;
     const T D_r11_c1 = (T(1)/(D_r11_c0));
     const T D_r11_c2 = T(2)*tj[J_cl2o2];
-    const T D_r11_c3 = D_r10*D_r11_c2 + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*nt_cvt<T>(x[28]) + K[K_d3]*nt_cvt<T>(x[45]) + K[K_d4]*nt_cvt<T>(x[49]) + K[K_d8]*nt_cvt<T>(x[43]) + K[K_e5b]*nt_cvt<T>(x[53]);
+    const T D_r11_c3 = D_r10*D_r11_c2 + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*xt28 + K[K_d3]*xt45 + K[K_d4]*xt49 + K[K_d8]*xt43 + K[K_e5b]*xt53;
     const T D_r11_c4 = D_r11_c3/(D_r11_c0*D_r11_c0);
     const T D_r11_c5 = D_r11_c1*tj[J_clono2_cl];
     const T D_r11_c6 = D_r11_c1*tj[J_hocl];
@@ -3354,68 +4049,68 @@ __device__ __forceinline__ void nt_jacobian_day_w4_3(const FF& F, PK K, PK tj, P
     const T d_D_r11_53 = D_r11_c1*K[K_e5b] + D_r11_c1*d_D_r12_53*tj[J_brcl];
     {  // row 44
     const T rs44 = nt_rscale<T>(nt_exp_hi(x[44]), fh);
-        J[284] = (-d_D_r11_1*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs44);
-        J[288] = (-d_D_r11_2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs44);
-        J[287] = (-d_D_r11_12*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs44);
-        J[285] = (-d_D_r11_14*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs44);
-        J[286] = (-d_D_r11_28*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs44);
-        J[292] = (-d_D_r11_43*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs44);
-        J[290] = (-d_D_r11_45*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs44);
-        J[294] = (-d_D_r11_46*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs44);
-        J[293] = (-d_D_r11_47*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs44);
-        J[289] = (-d_D_r11_48*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs44);
-        J[295] = (-d_D_r11_49*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs44);
-        J[296] = (-D_r11 - d_D_r11_52*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs44);
-        J[291] = (-d_D_r11_53*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs44);
+        J[284] = (-d_D_r11_1*xt52) * (cs1 * rs44);
+        J[288] = (-d_D_r11_2*xt52) * (cs2 * rs44);
+        J[287] = (-d_D_r11_12*xt52) * (cs12 * rs44);
+        J[285] = (-d_D_r11_14*xt52) * (cs14 * rs44);
+        J[286] = (-d_D_r11_28*xt52) * (cs28 * rs44);
+        J[292] = (-d_D_r11_43*xt52) * (cs43 * rs44);
+        J[290] = (-d_D_r11_45*xt52) * (cs45 * rs44);
+        J[294] = (-d_D_r11_46*xt52) * (cs46 * rs44);
+        J[293] = (-d_D_r11_47*xt52) * (cs47 * rs44);
+        J[289] = (-d_D_r11_48*xt52) * (cs48 * rs44);
+        J[295] = (-d_D_r11_49*xt52) * (cs49 * rs44);
+        J[296] = (-D_r11 - d_D_r11_52*xt52) * (cs52 * rs44);
+        J[291] = (-d_D_r11_53*xt52) * (cs53 * rs44);
     }
-    const T D_t06_c0 = tj[J_hocl]*nt_cvt<T>(x[14]);
-    const T D_t06_c1 = K[K_d33]*nt_cvt<T>(x[52]);
-    const T D_t06_c2 = D_t06_c1*nt_cvt<T>(x[47]);
+    const T D_t06_c0 = tj[J_hocl]*xt14;
+    const T D_t06_c1 = K[K_d33]*xt52;
+    const T D_t06_c2 = D_t06_c1*xt47;
     const bool sel_D_t06 = (D_t06_c0) <= (D_t06_c2);
     const T D_t06 = sel_D_t06 ? T(D_t06_c0) : T(D_t06_c2);
     const T d_D_t06_14 = sel_D_t06 ? T(tj[J_hocl]) : T(T(0));
     const T d_D_t06_47 = sel_D_t06 ? T(T(0)) : T(D_t06_c1);
-    const T d_D_t06_52 = sel_D_t06 ? T(T(0)) : T(K[K_d33]*nt_cvt<T>(x[47]));
-    const T D_t07_c0 = K[K_e5c]*nt_cvt<T>(x[53]);
-    const T D_t07_c1 = D_t07_c0*nt_cvt<T>(x[52]);
-    const T D_t07_c2 = tj[J_brcl]*nt_cvt<T>(x[26]);
+    const T d_D_t06_52 = sel_D_t06 ? T(T(0)) : T(K[K_d33]*xt47);
+    const T D_t07_c0 = K[K_e5c]*xt53;
+    const T D_t07_c1 = D_t07_c0*xt52;
+    const T D_t07_c2 = tj[J_brcl]*xt26;
     const bool sel_D_t07 = (D_t07_c1) <= (D_t07_c2);
     const T D_t07 = sel_D_t07 ? T(D_t07_c1) : T(D_t07_c2);
     const T d_D_t07_26 = sel_D_t07 ? T(T(0)) : T(tj[J_brcl]);
     const T d_D_t07_52 = sel_D_t07 ? T(D_t07_c0) : T(T(0));
-    const T d_D_t07_53 = sel_D_t07 ? T(K[K_e5c]*nt_cvt<T>(x[52])) : T(T(0));
-    const T D_t09_c0 = K[K_e15]*nt_cvt<T>(x[53]);
-    const T D_t09_c1 = D_t09_c0*nt_cvt<T>(x[47]);
-    const T D_t09_c2 = tj[J_hobr]*nt_cvt<T>(x[25]);
+    const T d_D_t07_53 = sel_D_t07 ? T(K[K_e5c]*xt52) : T(T(0));
+    const T D_t09_c0 = K[K_e15]*xt53;
+    const T D_t09_c1 = D_t09_c0*xt47;
+    const T D_t09_c2 = tj[J_hobr]*xt25;
     const bool sel_D_t09 = (D_t09_c1) <= (D_t09_c2);
     const T D_t09 = sel_D_t09 ? T(D_t09_c1) : T(D_t09_c2);
     const T d_D_t09_25 = sel_D_t09 ? T(T(0)) : T(tj[J_hobr]);
     const T d_D_t09_47 = sel_D_t09 ? T(D_t09_c0) : T(T(0));
-    const T d_D_t09_53 = sel_D_t09 ? T(K[K_e15]*nt_cvt<T>(x[47])) : T(T(0));
+    const T d_D_t09_53 = sel_D_t09 ? T(K[K_e15]*xt47) : T(T(0));
     {  // row 7
     const T rs7 = nt_rscale<T>(nt_exp_hi(x[7]), fh);
         const T dj7_c0 = T(2)*F.dt;
         const T dj7_c1 = tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
-        const T dj7_c2 = F.dt*nt_cvt<T>(x[49]);
+        const T dj7_c2 = F.dt*xt49;
         const T dj7_c3 = T(2)*K[K_b3];
         const T dj7_c4 = T(2)*K[K_d3];
         const T dj7_c5 = T(2)*K[K_hk3];
         const T dj7_c6 = T(2)*K[K_b9]*dj7_c1;
         const T dj7_c7 = T(2)*K[K_e5b];
-        J[105] = (dj7_c0*dj7_c1*tj[J_clono2_cl]) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs7);
-        J[106] = (F.dt*d_D_t06_14) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs7);
-        J[104] = (F.dt*d_D_t09_25) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs7);
-        J[103] = (d_D_t07_26*dj7_c0) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs7);
-        J[108] = (-K[K_c5]*dj7_c2) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs7);
-        J[112] = (F.dt*(K[K_a5]*nt_cvt<T>(x[45]) + K[K_a6]*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs7);
-        J[110] = (F.dt*(K[K_a5]*nt_cvt<T>(x[43]) + K[K_a7]*nt_cvt<T>(x[47]) + T(4)*K[K_hk1]*nt_cvt<T>(x[45]) + dj7_c3*nt_cvt<T>(x[48]) + dj7_c4*nt_cvt<T>(x[52]) + dj7_c5*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs7);
-        J[114] = (F.dt*(K[K_a2]*nt_cvt<T>(x[55]) + K[K_a6]*nt_cvt<T>(x[43]) + K[K_a6b]*nt_cvt<T>(x[47]) + dj7_c5*nt_cvt<T>(x[45]) + dj7_c6*nt_cvt<T>(x[48]))) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs7);
-        J[113] = (F.dt*d_D_t06_47 + F.dt*d_D_t09_47 + F.dt*(K[K_a6b]*nt_cvt<T>(x[46]) + K[K_a7]*nt_cvt<T>(x[45])) - K[K_a26]*dj7_c2) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs7);
-        J[109] = (F.dt*(dj7_c3*nt_cvt<T>(x[45]) + dj7_c6*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs7);
-        J[115] = (-F.dt*(K[K_a26]*nt_cvt<T>(x[47]) + K[K_c5]*nt_cvt<T>(x[28]))) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs7);
-        J[116] = (F.dt*d_D_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*nt_cvt<T>(x[52])/(F.hnm*K[K_d61] + tj[J_cl2o2]) + dj7_c4*nt_cvt<T>(x[45]) + dj7_c7*nt_cvt<T>(x[53])) + d_D_t07_52*dj7_c0) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs7);
-        J[111] = (F.dt*d_D_t09_53 + F.dt*(T(4)*K[K_e6]*nt_cvt<T>(x[53]) + dj7_c7*nt_cvt<T>(x[52])) + d_D_t07_53*dj7_c0) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs7);
-        J[107] = (F.dt*K[K_a2]*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs7);
+        J[105] = (dj7_c0*dj7_c1*tj[J_clono2_cl]) * (cs13 * rs7);
+        J[106] = (F.dt*d_D_t06_14) * (cs14 * rs7);
+        J[104] = (F.dt*d_D_t09_25) * (cs25 * rs7);
+        J[103] = (d_D_t07_26*dj7_c0) * (cs26 * rs7);
+        J[108] = (-K[K_c5]*dj7_c2) * (cs28 * rs7);
+        J[112] = (F.dt*(K[K_a5]*xt45 + K[K_a6]*xt46)) * (cs43 * rs7);
+        J[110] = (F.dt*(K[K_a5]*xt43 + K[K_a7]*xt47 + T(4)*K[K_hk1]*xt45 + dj7_c3*xt48 + dj7_c4*xt52 + dj7_c5*xt46)) * (cs45 * rs7);
+        J[114] = (F.dt*(K[K_a2]*xt55 + K[K_a6]*xt43 + K[K_a6b]*xt47 + dj7_c5*xt45 + dj7_c6*xt48)) * (cs46 * rs7);
+        J[113] = (F.dt*d_D_t06_47 + F.dt*d_D_t09_47 + F.dt*(K[K_a6b]*xt46 + K[K_a7]*xt45) - K[K_a26]*dj7_c2) * (cs47 * rs7);
+        J[109] = (F.dt*(dj7_c3*xt45 + dj7_c6*xt46)) * (cs48 * rs7);
+        J[115] = (-F.dt*(K[K_a26]*xt47 + K[K_c5]*xt28)) * (cs49 * rs7);
+        J[116] = (F.dt*d_D_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*xt52/(F.hnm*K[K_d61] + tj[J_cl2o2]) + dj7_c4*xt45 + dj7_c7*xt53) + d_D_t07_52*dj7_c0) * (cs52 * rs7);
+        J[111] = (F.dt*d_D_t09_53 + F.dt*(T(4)*K[K_e6]*xt53 + dj7_c7*xt52) + d_D_t07_53*dj7_c0) * (cs53 * rs7);
+        J[107] = (F.dt*K[K_a2]*xt46) * (cs55 * rs7);
     }
 }
 
@@ -3538,96 +4233,211 @@ __device__ __forceinline__ void nt_residual_night(const FF& F, PK K, PK tj, PK h
 template <typename T, typename FF, typename PK, typename PJ>
 __device__ __forceinline__ void nt_jacobian_night(const FF& F, PK K, PK tj, PK het, const double* __restrict__ x, double floor_, PJ J) {
     const int fh = nt_exp_hi(floor_);
+    // the iterate in T and the column scales, once per call
+    const T xt0 = nt_cvt<T>(x[0]);
+    const T xt1 = nt_cvt<T>(x[1]);
+    const T xt2 = nt_cvt<T>(x[2]);
+    const T xt3 = nt_cvt<T>(x[3]);
+    const T xt4 = nt_cvt<T>(x[4]);
+    const T xt5 = nt_cvt<T>(x[5]);
+    const T xt6 = nt_cvt<T>(x[6]);
+    const T xt7 = nt_cvt<T>(x[7]);
+    const T xt8 = nt_cvt<T>(x[8]);
+    const T xt9 = nt_cvt<T>(x[9]);
+    const T xt10 = nt_cvt<T>(x[10]);
+    const T xt11 = nt_cvt<T>(x[11]);
+    const T xt12 = nt_cvt<T>(x[12]);
+    const T xt13 = nt_cvt<T>(x[13]);
+    const T xt14 = nt_cvt<T>(x[14]);
+    const T xt15 = nt_cvt<T>(x[15]);
+    const T xt16 = nt_cvt<T>(x[16]);
+    const T xt17 = nt_cvt<T>(x[17]);
+    const T xt18 = nt_cvt<T>(x[18]);
+    const T xt19 = nt_cvt<T>(x[19]);
+    const T xt20 = nt_cvt<T>(x[20]);
+    const T xt21 = nt_cvt<T>(x[21]);
+    const T xt22 = nt_cvt<T>(x[22]);
+    const T xt23 = nt_cvt<T>(x[23]);
+    const T xt24 = nt_cvt<T>(x[24]);
+    const T xt25 = nt_cvt<T>(x[25]);
+    const T xt26 = nt_cvt<T>(x[26]);
+    const T xt27 = nt_cvt<T>(x[27]);
+    const T xt28 = nt_cvt<T>(x[28]);
+    const T xt29 = nt_cvt<T>(x[29]);
+    const T xt30 = nt_cvt<T>(x[30]);
+    const T xt31 = nt_cvt<T>(x[31]);
+    const T xt32 = nt_cvt<T>(x[32]);
+    const T xt33 = nt_cvt<T>(x[33]);
+    const T xt34 = nt_cvt<T>(x[34]);
+    const T xt35 = nt_cvt<T>(x[35]);
+    const T xt36 = nt_cvt<T>(x[36]);
+    const T xt37 = nt_cvt<T>(x[37]);
+    const T xt38 = nt_cvt<T>(x[38]);
+    const T xt39 = nt_cvt<T>(x[39]);
+    const T xt40 = nt_cvt<T>(x[40]);
+    const T xt41 = nt_cvt<T>(x[41]);
+    const T xt42 = nt_cvt<T>(x[42]);
+    const T xt43 = nt_cvt<T>(x[43]);
+    const T xt44 = nt_cvt<T>(x[44]);
+    const T xt45 = nt_cvt<T>(x[45]);
+    const T xt46 = nt_cvt<T>(x[46]);
+    const T xt47 = nt_cvt<T>(x[47]);
+    const T xt48 = nt_cvt<T>(x[48]);
+    const T xt49 = nt_cvt<T>(x[49]);
+    const T xt50 = nt_cvt<T>(x[50]);
+    const T xt51 = nt_cvt<T>(x[51]);
+    const T xt52 = nt_cvt<T>(x[52]);
+    const T xt53 = nt_cvt<T>(x[53]);
+    const T xt54 = nt_cvt<T>(x[54]);
+    const T xt55 = nt_cvt<T>(x[55]);
+    const T xt56 = nt_cvt<T>(x[56]);
+    const T cs0 = nt_scale<T>(nt_exp_hi(x[0]), fh);
+    const T cs1 = nt_scale<T>(nt_exp_hi(x[1]), fh);
+    const T cs2 = nt_scale<T>(nt_exp_hi(x[2]), fh);
+    const T cs3 = nt_scale<T>(nt_exp_hi(x[3]), fh);
+    const T cs4 = nt_scale<T>(nt_exp_hi(x[4]), fh);
+    const T cs5 = nt_scale<T>(nt_exp_hi(x[5]), fh);
+    const T cs6 = nt_scale<T>(nt_exp_hi(x[6]), fh);
+    const T cs7 = nt_scale<T>(nt_exp_hi(x[7]), fh);
+    const T cs8 = nt_scale<T>(nt_exp_hi(x[8]), fh);
+    const T cs9 = nt_scale<T>(nt_exp_hi(x[9]), fh);
+    const T cs10 = nt_scale<T>(nt_exp_hi(x[10]), fh);
+    const T cs11 = nt_scale<T>(nt_exp_hi(x[11]), fh);
+    const T cs12 = nt_scale<T>(nt_exp_hi(x[12]), fh);
+    const T cs13 = nt_scale<T>(nt_exp_hi(x[13]), fh);
+    const T cs14 = nt_scale<T>(nt_exp_hi(x[14]), fh);
+    const T cs15 = nt_scale<T>(nt_exp_hi(x[15]), fh);
+    const T cs16 = nt_scale<T>(nt_exp_hi(x[16]), fh);
+    const T cs17 = nt_scale<T>(nt_exp_hi(x[17]), fh);
+    const T cs18 = nt_scale<T>(nt_exp_hi(x[18]), fh);
+    const T cs19 = nt_scale<T>(nt_exp_hi(x[19]), fh);
+    const T cs20 = nt_scale<T>(nt_exp_hi(x[20]), fh);
+    const T cs21 = nt_scale<T>(nt_exp_hi(x[21]), fh);
+    const T cs22 = nt_scale<T>(nt_exp_hi(x[22]), fh);
+    const T cs23 = nt_scale<T>(nt_exp_hi(x[23]), fh);
+    const T cs24 = nt_scale<T>(nt_exp_hi(x[24]), fh);
+    const T cs25 = nt_scale<T>(nt_exp_hi(x[25]), fh);
+    const T cs26 = nt_scale<T>(nt_exp_hi(x[26]), fh);
+    const T cs27 = nt_scale<T>(nt_exp_hi(x[27]), fh);
+    const T cs28 = nt_scale<T>(nt_exp_hi(x[28]), fh);
+    const T cs29 = nt_scale<T>(nt_exp_hi(x[29]), fh);
+    const T cs30 = nt_scale<T>(nt_exp_hi(x[30]), fh);
+    const T cs31 = nt_scale<T>(nt_exp_hi(x[31]), fh);
+    const T cs32 = nt_scale<T>(nt_exp_hi(x[32]), fh);
+    const T cs33 = nt_scale<T>(nt_exp_hi(x[33]), fh);
+    const T cs34 = nt_scale<T>(nt_exp_hi(x[34]), fh);
+    const T cs35 = nt_scale<T>(nt_exp_hi(x[35]), fh);
+    const T cs36 = nt_scale<T>(nt_exp_hi(x[36]), fh);
+    const T cs37 = nt_scale<T>(nt_exp_hi(x[37]), fh);
+    const T cs38 = nt_scale<T>(nt_exp_hi(x[38]), fh);
+    const T cs39 = nt_scale<T>(nt_exp_hi(x[39]), fh);
+    const T cs40 = nt_scale<T>(nt_exp_hi(x[40]), fh);
+    const T cs41 = nt_scale<T>(nt_exp_hi(x[41]), fh);
+    const T cs42 = nt_scale<T>(nt_exp_hi(x[42]), fh);
+    const T cs43 = nt_scale<T>(nt_exp_hi(x[43]), fh);
+    const T cs44 = nt_scale<T>(nt_exp_hi(x[44]), fh);
+    const T cs45 = nt_scale<T>(nt_exp_hi(x[45]), fh);
+    const T cs46 = nt_scale<T>(nt_exp_hi(x[46]), fh);
+    const T cs47 = nt_scale<T>(nt_exp_hi(x[47]), fh);
+    const T cs48 = nt_scale<T>(nt_exp_hi(x[48]), fh);
+    const T cs49 = nt_scale<T>(nt_exp_hi(x[49]), fh);
+    const T cs50 = nt_scale<T>(nt_exp_hi(x[50]), fh);
+    const T cs51 = nt_scale<T>(nt_exp_hi(x[51]), fh);
+    const T cs52 = nt_scale<T>(nt_exp_hi(x[52]), fh);
+    const T cs53 = nt_scale<T>(nt_exp_hi(x[53]), fh);
+    const T cs54 = nt_scale<T>(nt_exp_hi(x[54]), fh);
+    const T cs55 = nt_scale<T>(nt_exp_hi(x[55]), fh);
+    const T cs56 = nt_scale<T>(nt_exp_hi(x[56]), fh);
     {  // row 0
     const T rs0 = nt_rscale<T>(nt_exp_hi(x[0]), fh);
         const T nj0_c0 = K[K_b38] + K[K_b39];
-        J[76] = (F.dt*(nj0_c0*nt_cvt<T>(x[42]) + tj[J_n2o]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs0);
-        J[77] = (F.dt*nj0_c0*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs0);
+        J[76] = (F.dt*(nj0_c0*xt42 + tj[J_n2o]) + T(1)) * (cs0 * rs0);
+        J[77] = (F.dt*nj0_c0*xt0) * (cs42 * rs0);
     }
     {  // row 1
     const T rs1 = nt_rscale<T>(nt_exp_hi(x[1]), fh);
-        const T nj1_c0 = F.dt*nt_cvt<T>(x[1]);
-        J[157] = (F.dt*(K[K_c1a]*nt_cvt<T>(x[42]) + K[K_c1b]*nt_cvt<T>(x[42]) + K[K_c1c]*nt_cvt<T>(x[42]) + K[K_c2]*nt_cvt<T>(x[43]) + K[K_d5]*nt_cvt<T>(x[44])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs1);
-        J[156] = (nj1_c0*(K[K_c1a] + K[K_c1b] + K[K_c1c])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs1);
-        J[159] = (K[K_c2]*nj1_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs1);
-        J[158] = (K[K_d5]*nj1_c0) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs1);
+        const T nj1_c0 = F.dt*xt1;
+        J[157] = (F.dt*(K[K_c1a]*xt42 + K[K_c1b]*xt42 + K[K_c1c]*xt42 + K[K_c2]*xt43 + K[K_d5]*xt44) + T(1)) * (cs1 * rs1);
+        J[156] = (nj1_c0*(K[K_c1a] + K[K_c1b] + K[K_c1c])) * (cs42 * rs1);
+        J[159] = (K[K_c2]*nj1_c0) * (cs43 * rs1);
+        J[158] = (K[K_d5]*nj1_c0) * (cs44 * rs1);
     }
     {  // row 2
     const T rs2 = nt_rscale<T>(nt_exp_hi(x[2]), fh);
-        const T nj2_c0 = F.dt*nt_cvt<T>(x[43]);
+        const T nj2_c0 = F.dt*xt43;
         const T nj2_c1 = F.dt*F.parth2o;
         const T nj2_c2 = F.parthno3*K[K_b27];
         const T nj2_c3 = F.parthcl*K[K_d11];
-        J[261] = (-K[K_c2]*nj2_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs2);
-        J[266] = (nj2_c1*(K[K_a1et]*nt_cvt<T>(x[42]) + tj[J_h2o]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs2);
-        J[260] = (-nj2_c0*nj2_c2) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs2);
-        J[265] = (-nj2_c0*nj2_c3) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs2);
-        J[262] = (-K[K_a30]*nj2_c0) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs2);
-        J[264] = (-K[K_c8]*nj2_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs2);
-        J[258] = (-F.dt*(K[K_c17a]*nt_cvt<T>(x[43]) + K[K_c17b]*nt_cvt<T>(x[43]))) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs2);
-        J[259] = (K[K_a1et]*nj2_c1*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs2);
-        J[267] = (-F.dt*(F.h2*K[K_a19] + K[K_a17]*nt_cvt<T>(x[47]) + K[K_a30]*nt_cvt<T>(x[16]) + T(2)*K[K_a31]*nt_cvt<T>(x[43]) + K[K_c17a]*nt_cvt<T>(x[29]) + K[K_c17b]*nt_cvt<T>(x[29]) + K[K_c2]*nt_cvt<T>(x[1]) + K[K_c8]*nt_cvt<T>(x[27]) + nj2_c2*nt_cvt<T>(x[4]) + nj2_c3*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs2);
-        J[268] = (-F.dt*(K[K_a17]*nt_cvt<T>(x[43]) + T(1.6e-12)*nt_cvt<T>(x[55]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs2);
-        J[263] = (-T(1.6e-12)*F.dt*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs2);
+        J[261] = (-K[K_c2]*nj2_c0) * (cs1 * rs2);
+        J[266] = (nj2_c1*(K[K_a1et]*xt42 + tj[J_h2o]) + T(1)) * (cs2 * rs2);
+        J[260] = (-nj2_c0*nj2_c2) * (cs4 * rs2);
+        J[265] = (-nj2_c0*nj2_c3) * (cs12 * rs2);
+        J[262] = (-K[K_a30]*nj2_c0) * (cs16 * rs2);
+        J[264] = (-K[K_c8]*nj2_c0) * (cs27 * rs2);
+        J[258] = (-F.dt*(K[K_c17a]*xt43 + K[K_c17b]*xt43)) * (cs29 * rs2);
+        J[259] = (K[K_a1et]*nj2_c1*xt2) * (cs42 * rs2);
+        J[267] = (-F.dt*(F.h2*K[K_a19] + K[K_a17]*xt47 + K[K_a30]*xt16 + T(2)*K[K_a31]*xt43 + K[K_c17a]*xt29 + K[K_c17b]*xt29 + K[K_c2]*xt1 + K[K_c8]*xt27 + nj2_c2*xt4 + nj2_c3*xt12)) * (cs43 * rs2);
+        J[268] = (-F.dt*(K[K_a17]*xt43 + T(1.6e-12)*xt55)) * (cs47 * rs2);
+        J[263] = (-T(1.6e-12)*F.dt*xt47) * (cs55 * rs2);
     }
     {  // row 3
     const T rs3 = nt_rscale<T>(nt_exp_hi(x[3]), fh);
         const T nj3_c0 = T(2)*F.dt;
         const T nj3_c1 = K[K_b39]*nj3_c0;
         const T nj3_c2 = K[K_b6]*nj3_c0;
-        J[20] = (-nj3_c1*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs3);
-        J[23] = (F.dt*F.rain_hno3) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs3);
-        J[22] = (-nj3_c1*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs3);
-        J[24] = (nj3_c2*nt_cvt<T>(x[51])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs3);
-        J[21] = (nj3_c2*nt_cvt<T>(x[49])) * (nt_scale<T>(nt_exp_hi(x[51]), fh) * rs3);
+        J[20] = (-nj3_c1*xt42) * (cs0 * rs3);
+        J[23] = (F.dt*F.rain_hno3) * (cs4 * rs3);
+        J[22] = (-nj3_c1*xt0) * (cs42 * rs3);
+        J[24] = (nj3_c2*xt51) * (cs49 * rs3);
+        J[21] = (nj3_c2*xt49) * (cs51 * rs3);
     }
     {  // row 4
     const T rs4 = nt_rscale<T>(nt_exp_hi(x[4]), fh);
         const T nj4_c0 = T(2)*het[2];
         const T nj4_c1 = F.dt*K[K_b22];
-        J[122] = (-F.dt*(het[0]*nt_cvt<T>(x[13]) + het[5]*nt_cvt<T>(x[19]) + nj4_c0*nt_cvt<T>(x[5]))) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs4);
-        J[120] = (F.dt*(F.parthno3*(K[K_b27]*nt_cvt<T>(x[43]) + tj[J_hno3]) + F.rain_hno3) + T(1)) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs4);
-        J[118] = (-F.dt*(het[3]*nt_cvt<T>(x[12]) + nj4_c0*nt_cvt<T>(x[2]))) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs4);
-        J[121] = (-F.dt*(het[1]*nt_cvt<T>(x[13]) + het[3]*nt_cvt<T>(x[5]))) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs4);
-        J[119] = (-F.dt*(het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs4);
-        J[117] = (-F.dt*het[5]*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs4);
-        J[124] = (F.dt*F.parthno3*K[K_b27]*nt_cvt<T>(x[4]) - nj4_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs4);
-        J[123] = (-nj4_c1*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs4);
+        J[122] = (-F.dt*(het[0]*xt13 + het[5]*xt19 + nj4_c0*xt5)) * (cs2 * rs4);
+        J[120] = (F.dt*(F.parthno3*(K[K_b27]*xt43 + tj[J_hno3]) + F.rain_hno3) + T(1)) * (cs4 * rs4);
+        J[118] = (-F.dt*(het[3]*xt12 + nj4_c0*xt2)) * (cs5 * rs4);
+        J[121] = (-F.dt*(het[1]*xt13 + het[3]*xt5)) * (cs12 * rs4);
+        J[119] = (-F.dt*(het[0]*xt2 + het[1]*xt12)) * (cs13 * rs4);
+        J[117] = (-F.dt*het[5]*xt2) * (cs19 * rs4);
+        J[124] = (F.dt*F.parthno3*K[K_b27]*xt4 - nj4_c1*xt48) * (cs43 * rs4);
+        J[123] = (-nj4_c1*xt43) * (cs48 * rs4);
     }
     {  // row 5
     const T rs5 = nt_rscale<T>(nt_exp_hi(x[5]), fh);
-        const T nj5_c0 = F.dt*nt_cvt<T>(x[5]);
+        const T nj5_c0 = F.dt*xt5;
         const T nj5_c1 = F.dt*K[K_b12];
-        J[74] = (het[2]*nj5_c0) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs5);
-        J[72] = (F.dt*(F.hnm*K[K_b32] + het[2]*nt_cvt<T>(x[2]) + het[3]*nt_cvt<T>(x[12]) + tj[J_n2o5]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs5);
-        J[73] = (het[3]*nj5_c0) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs5);
-        J[75] = (-nj5_c1*nt_cvt<T>(x[54])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs5);
-        J[71] = (-nj5_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[54]), fh) * rs5);
+        J[74] = (het[2]*nj5_c0) * (cs2 * rs5);
+        J[72] = (F.dt*(F.hnm*K[K_b32] + het[2]*xt2 + het[3]*xt12 + tj[J_n2o5]) + T(1)) * (cs5 * rs5);
+        J[73] = (het[3]*nj5_c0) * (cs12 * rs5);
+        J[75] = (-nj5_c1*xt54) * (cs48 * rs5);
+        J[71] = (-nj5_c1*xt48) * (cs54 * rs5);
     }
     {  // row 6
     const T rs6 = nt_rscale<T>(nt_exp_hi(x[6]), fh);
-        const T nj6_c0 = T(3)*nt_cvt<T>(x[42]);
+        const T nj6_c0 = T(3)*xt42;
         const T nj6_c1 = T(2)*K[K_d91];
         const T nj6_c2 = T(4)*K[K_d93];
         const T nj6_c3 = T(3)*K[K_d94];
-        J[9] = (F.dt*F.rain_hcl) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs6);
-        J[7] = (-F.dt*(K[K_d90]*nj6_c0 + T(3)*tj[J_cfc11])) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs6);
-        J[4] = (-F.dt*(nj6_c1*nt_cvt<T>(x[42]) + T(2)*tj[J_cfc12])) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs6);
-        J[0] = (-F.dt*(K[K_d92]*nj6_c0 + T(3)*tj[J_cfc113])) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs6);
-        J[2] = (-F.dt*(nj6_c2*nt_cvt<T>(x[42]) + T(4)*tj[J_ccl4])) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs6);
-        J[6] = (-F.dt*(nj6_c3*nt_cvt<T>(x[43]) + T(3)*tj[J_ch3ccl3])) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs6);
-        J[5] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl])) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs6);
-        J[3] = (-F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22])) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs6);
-        J[1] = (-F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211])) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs6);
-        J[8] = (-F.dt*(T(3)*K[K_d90]*nt_cvt<T>(x[30]) + T(3)*K[K_d92]*nt_cvt<T>(x[32]) + K[K_d96]*nt_cvt<T>(x[36]) + K[K_e52]*nt_cvt<T>(x[38]) + nj6_c1*nt_cvt<T>(x[31]) + nj6_c2*nt_cvt<T>(x[33]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs6);
-        J[10] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[35]) + K[K_d97]*nt_cvt<T>(x[36]) + nj6_c3*nt_cvt<T>(x[34]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs6);
+        J[9] = (F.dt*F.rain_hcl) * (cs12 * rs6);
+        J[7] = (-F.dt*(K[K_d90]*nj6_c0 + T(3)*tj[J_cfc11])) * (cs30 * rs6);
+        J[4] = (-F.dt*(nj6_c1*xt42 + T(2)*tj[J_cfc12])) * (cs31 * rs6);
+        J[0] = (-F.dt*(K[K_d92]*nj6_c0 + T(3)*tj[J_cfc113])) * (cs32 * rs6);
+        J[2] = (-F.dt*(nj6_c2*xt42 + T(4)*tj[J_ccl4])) * (cs33 * rs6);
+        J[6] = (-F.dt*(nj6_c3*xt43 + T(3)*tj[J_ch3ccl3])) * (cs34 * rs6);
+        J[5] = (-F.dt*(K[K_d95]*xt43 + tj[J_ch3cl])) * (cs35 * rs6);
+        J[3] = (-F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22])) * (cs36 * rs6);
+        J[1] = (-F.dt*(K[K_e52]*xt42 + tj[J_h1211])) * (cs38 * rs6);
+        J[8] = (-F.dt*(T(3)*K[K_d90]*xt30 + T(3)*K[K_d92]*xt32 + K[K_d96]*xt36 + K[K_e52]*xt38 + nj6_c1*xt31 + nj6_c2*xt33)) * (cs42 * rs6);
+        J[10] = (-F.dt*(K[K_d95]*xt35 + K[K_d97]*xt36 + nj6_c3*xt34)) * (cs43 * rs6);
     }
     {  // row 8
     const T rs8 = nt_rscale<T>(nt_exp_hi(x[8]), fh);
         const T nj8_c0 = F.dt*K[K_a36];
-        J[160] = (nj8_c0*nt_cvt<T>(x[43]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[8]), fh) * rs8);
-        J[161] = (-F.dt*tj[J_ch2o_co]) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs8);
-        J[165] = (nj8_c0*nt_cvt<T>(x[8])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs8);
+        J[160] = (nj8_c0*xt43 + T(1)) * (cs8 * rs8);
+        J[161] = (-F.dt*tj[J_ch2o_co]) * (cs27 * rs8);
+        J[165] = (nj8_c0*xt8) * (cs43 * rs8);
         J[163] = T(0);
         J[162] = T(0);
         J[164] = T(0);
@@ -3635,9 +4445,9 @@ __device__ __forceinline__ void nt_jacobian_night(const FF& F, PK K, PK tj, PK h
     {  // row 9
     const T rs9 = nt_rscale<T>(nt_exp_hi(x[9]), fh);
         const T nj9_c0 = F.dt*K[K_e5a];
-        J[100] = (F.dt*tj[J_oclo] + T(1)) * (nt_scale<T>(nt_exp_hi(x[9]), fh) * rs9);
-        J[102] = (-nj9_c0*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs9);
-        J[101] = (-nj9_c0*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs9);
+        J[100] = (F.dt*tj[J_oclo] + T(1)) * (cs9 * rs9);
+        J[102] = (-nj9_c0*xt53) * (cs52 * rs9);
+        J[101] = (-nj9_c0*xt52) * (cs53 * rs9);
     }
     {  // row 10
     const T rs10 = nt_rscale<T>(nt_exp_hi(x[10]), fh);
@@ -3647,328 +4457,328 @@ __device__ __forceinline__ void nt_jacobian_night(const FF& F, PK K, PK tj, PK h
     }
     {  // row 12
     const T rs12 = nt_rscale<T>(nt_exp_hi(x[12]), fh);
-        const T nj12_c0 = F.dt*nt_cvt<T>(x[44]);
-        const T nj12_c1 = F.dt*nt_cvt<T>(x[12]);
+        const T nj12_c0 = F.dt*xt44;
+        const T nj12_c1 = F.dt*xt12;
         const T nj12_c2 = F.dt*K[K_d9];
-        J[250] = (-K[K_d5]*nj12_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs12);
-        J[247] = (het[3]*nj12_c1) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs12);
-        J[253] = (F.dt*(F.parthcl*(K[K_d11]*nt_cvt<T>(x[43]) + tj[J_hcl]) + F.rain_hcl + het[1]*nt_cvt<T>(x[13]) + het[3]*nt_cvt<T>(x[5]) + het[4]*nt_cvt<T>(x[14]) + het[6]*nt_cvt<T>(x[25])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs12);
-        J[249] = (het[1]*nj12_c1) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs12);
-        J[251] = (het[4]*nj12_c1) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs12);
-        J[248] = (het[6]*nj12_c1) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs12);
-        J[252] = (-K[K_c10]*nj12_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs12);
-        J[255] = (F.parthcl*K[K_d11]*nj12_c1 - nj12_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs12);
-        J[254] = (-F.dt*(F.h2*K[K_d6] + K[K_c10]*nt_cvt<T>(x[27]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs12);
-        J[256] = (-K[K_d7]*nj12_c0) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs12);
-        J[257] = (-nj12_c2*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs12);
+        J[250] = (-K[K_d5]*nj12_c0) * (cs1 * rs12);
+        J[247] = (het[3]*nj12_c1) * (cs5 * rs12);
+        J[253] = (F.dt*(F.parthcl*(K[K_d11]*xt43 + tj[J_hcl]) + F.rain_hcl + het[1]*xt13 + het[3]*xt5 + het[4]*xt14 + het[6]*xt25) + T(1)) * (cs12 * rs12);
+        J[249] = (het[1]*nj12_c1) * (cs13 * rs12);
+        J[251] = (het[4]*nj12_c1) * (cs14 * rs12);
+        J[248] = (het[6]*nj12_c1) * (cs25 * rs12);
+        J[252] = (-K[K_c10]*nj12_c0) * (cs27 * rs12);
+        J[255] = (F.parthcl*K[K_d11]*nj12_c1 - nj12_c2*xt52) * (cs43 * rs12);
+        J[254] = (-F.dt*(F.h2*K[K_d6] + K[K_c10]*xt27 + K[K_d5]*xt1 + K[K_d7]*xt47)) * (cs44 * rs12);
+        J[256] = (-K[K_d7]*nj12_c0) * (cs47 * rs12);
+        J[257] = (-nj12_c2*xt43) * (cs52 * rs12);
     }
     {  // row 13
     const T rs13 = nt_rscale<T>(nt_exp_hi(x[13]), fh);
-        const T nj13_c0 = F.dt*nt_cvt<T>(x[13]);
+        const T nj13_c0 = F.dt*xt13;
         const T nj13_c1 = F.dt*K[K_d31];
-        J[89] = (het[0]*nj13_c0) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs13);
-        J[88] = (het[1]*nj13_c0) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs13);
-        J[87] = (F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]) + tj[J_clono2_cl] + tj[J_clono2_clo]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs13);
-        J[91] = (K[K_d32]*nj13_c0) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs13);
-        J[90] = (-nj13_c1*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs13);
-        J[92] = (-nj13_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs13);
+        J[89] = (het[0]*nj13_c0) * (cs2 * rs13);
+        J[88] = (het[1]*nj13_c0) * (cs12 * rs13);
+        J[87] = (F.dt*(K[K_d32]*xt45 + het[0]*xt2 + het[1]*xt12 + tj[J_clono2_cl] + tj[J_clono2_clo]) + T(1)) * (cs13 * rs13);
+        J[91] = (K[K_d32]*nj13_c0) * (cs45 * rs13);
+        J[90] = (-nj13_c1*xt52) * (cs48 * rs13);
+        J[92] = (-nj13_c1*xt48) * (cs52 * rs13);
     }
     {  // row 14
     const T rs14 = nt_rscale<T>(nt_exp_hi(x[14]), fh);
         const T nj14_c0 = F.dt*het[0];
-        const T nj14_c1 = F.dt*nt_cvt<T>(x[14]);
+        const T nj14_c1 = F.dt*xt14;
         const T nj14_c2 = F.dt*K[K_d33];
-        J[170] = (-nj14_c0*nt_cvt<T>(x[13])) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs14);
-        J[169] = (het[4]*nj14_c1) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs14);
-        J[166] = (-nj14_c0*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs14);
-        J[167] = (F.dt*(K[K_d34]*nt_cvt<T>(x[43]) + K[K_d35]*nt_cvt<T>(x[45]) + K[K_d37]*nt_cvt<T>(x[44]) + het[4]*nt_cvt<T>(x[12]) + het[8]*nt_cvt<T>(x[18]) + tj[J_hocl]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs14);
-        J[168] = (het[8]*nj14_c1) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs14);
-        J[173] = (K[K_d34]*nj14_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs14);
-        J[172] = (K[K_d37]*nj14_c1) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs14);
-        J[171] = (K[K_d35]*nj14_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs14);
-        J[174] = (-nj14_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs14);
-        J[175] = (-nj14_c2*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs14);
+        J[170] = (-nj14_c0*xt13) * (cs2 * rs14);
+        J[169] = (het[4]*nj14_c1) * (cs12 * rs14);
+        J[166] = (-nj14_c0*xt2) * (cs13 * rs14);
+        J[167] = (F.dt*(K[K_d34]*xt43 + K[K_d35]*xt45 + K[K_d37]*xt44 + het[4]*xt12 + het[8]*xt18 + tj[J_hocl]) + T(1)) * (cs14 * rs14);
+        J[168] = (het[8]*nj14_c1) * (cs18 * rs14);
+        J[173] = (K[K_d34]*nj14_c1) * (cs43 * rs14);
+        J[172] = (K[K_d37]*nj14_c1) * (cs44 * rs14);
+        J[171] = (K[K_d35]*nj14_c1) * (cs45 * rs14);
+        J[174] = (-nj14_c2*xt52) * (cs47 * rs14);
+        J[175] = (-nj14_c2*xt47) * (cs52 * rs14);
     }
     {  // row 15
     const T rs15 = nt_rscale<T>(nt_exp_hi(x[15]), fh);
-        J[63] = (-F.dt*(het[1]*nt_cvt<T>(x[13]) + het[4]*nt_cvt<T>(x[14]))) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs15);
-        J[61] = (-F.dt*het[1]*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs15);
-        J[62] = (-F.dt*(K[K_d37]*nt_cvt<T>(x[44]) + het[4]*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs15);
-        J[60] = (F.dt*tj[J_cl2] + T(1)) * (nt_scale<T>(nt_exp_hi(x[15]), fh) * rs15);
-        J[64] = (-F.dt*K[K_d37]*nt_cvt<T>(x[14])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs15);
-        J[65] = (-T(2)*F.dt*K[K_d62]*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs15);
+        J[63] = (-F.dt*(het[1]*xt13 + het[4]*xt14)) * (cs12 * rs15);
+        J[61] = (-F.dt*het[1]*xt12) * (cs13 * rs15);
+        J[62] = (-F.dt*(K[K_d37]*xt44 + het[4]*xt12)) * (cs14 * rs15);
+        J[60] = (F.dt*tj[J_cl2] + T(1)) * (cs15 * rs15);
+        J[64] = (-F.dt*K[K_d37]*xt14) * (cs44 * rs15);
+        J[65] = (-T(2)*F.dt*K[K_d62]*xt52) * (cs52 * rs15);
     }
     {  // row 16
     const T rs16 = nt_rscale<T>(nt_exp_hi(x[16]), fh);
-        J[189] = (F.dt*(F.rain_h2o2 + K[K_a30]*nt_cvt<T>(x[43]) + tj[J_h2o2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs16);
-        J[190] = (F.dt*K[K_a30]*nt_cvt<T>(x[16])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs16);
-        J[191] = (-T(2)*F.dt*K[K_a27]*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs16);
+        J[189] = (F.dt*(F.rain_h2o2 + K[K_a30]*xt43 + tj[J_h2o2]) + T(1)) * (cs16 * rs16);
+        J[190] = (F.dt*K[K_a30]*xt16) * (cs43 * rs16);
+        J[191] = (-T(2)*F.dt*K[K_a27]*xt47) * (cs47 * rs16);
     }
     {  // row 17
     const T rs17 = nt_rscale<T>(nt_exp_hi(x[17]), fh);
         const T nj17_c0 = F.dt*het[3];
         const T nj17_c1 = F.dt*K[K_d36];
-        J[26] = (-nj17_c0*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs17);
-        J[27] = (-nj17_c0*nt_cvt<T>(x[5])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs17);
-        J[25] = (F.dt*tj[J_clno2] + T(1)) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs17);
-        J[29] = (-nj17_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs17);
-        J[28] = (-nj17_c1*nt_cvt<T>(x[44])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs17);
+        J[26] = (-nj17_c0*xt12) * (cs5 * rs17);
+        J[27] = (-nj17_c0*xt5) * (cs12 * rs17);
+        J[25] = (F.dt*tj[J_clno2] + T(1)) * (cs17 * rs17);
+        J[29] = (-nj17_c1*xt48) * (cs44 * rs17);
+        J[28] = (-nj17_c1*xt44) * (cs48 * rs17);
     }
     {  // row 18
     const T rs18 = nt_rscale<T>(nt_exp_hi(x[18]), fh);
-        const T nj18_c0 = F.dt*nt_cvt<T>(x[18]);
-        const T nj18_c1 = F.dt*nt_cvt<T>(x[50]);
+        const T nj18_c0 = F.dt*xt18;
+        const T nj18_c1 = F.dt*xt50;
         const T nj18_c2 = F.parthbr*nj18_c0;
-        J[183] = (het[8]*nj18_c0) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs18);
-        J[184] = (F.dt*(F.parthbr*(K[K_e11]*nt_cvt<T>(x[43]) + K[K_e9]*nt_cvt<T>(x[42]) + tj[J_hbr]) + F.rain_hbr + het[7]*nt_cvt<T>(x[25]) + het[8]*nt_cvt<T>(x[14])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs18);
-        J[181] = (het[7]*nj18_c0) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs18);
-        J[185] = (-K[K_c19]*nj18_c1) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs18);
-        J[182] = (K[K_e9]*nj18_c2) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs18);
-        J[187] = (K[K_e11]*nj18_c2) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs18);
-        J[188] = (-K[K_e7]*nj18_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs18);
-        J[186] = (-F.dt*(K[K_c19]*nt_cvt<T>(x[27]) + K[K_e7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs18);
+        J[183] = (het[8]*nj18_c0) * (cs14 * rs18);
+        J[184] = (F.dt*(F.parthbr*(K[K_e11]*xt43 + K[K_e9]*xt42 + tj[J_hbr]) + F.rain_hbr + het[7]*xt25 + het[8]*xt14) + T(1)) * (cs18 * rs18);
+        J[181] = (het[7]*nj18_c0) * (cs25 * rs18);
+        J[185] = (-K[K_c19]*nj18_c1) * (cs27 * rs18);
+        J[182] = (K[K_e9]*nj18_c2) * (cs42 * rs18);
+        J[187] = (K[K_e11]*nj18_c2) * (cs43 * rs18);
+        J[188] = (-K[K_e7]*nj18_c1) * (cs47 * rs18);
+        J[186] = (-F.dt*(K[K_c19]*xt27 + K[K_e7]*xt47)) * (cs50 * rs18);
     }
     {  // row 19
     const T rs19 = nt_rscale<T>(nt_exp_hi(x[19]), fh);
-        const T nj19_c0 = F.dt*nt_cvt<T>(x[19]);
+        const T nj19_c0 = F.dt*xt19;
         const T nj19_c1 = F.dt*K[K_e13];
-        J[56] = (het[5]*nj19_c0) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs19);
-        J[55] = (F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + het[5]*nt_cvt<T>(x[2]) + tj[J_brono2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs19);
-        J[58] = (K[K_e8]*nj19_c0) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs19);
-        J[57] = (-nj19_c1*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs19);
-        J[59] = (-nj19_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs19);
+        J[56] = (het[5]*nj19_c0) * (cs2 * rs19);
+        J[55] = (F.dt*(K[K_e8]*xt45 + het[5]*xt2 + tj[J_brono2]) + T(1)) * (cs19 * rs19);
+        J[58] = (K[K_e8]*nj19_c0) * (cs45 * rs19);
+        J[57] = (-nj19_c1*xt53) * (cs48 * rs19);
+        J[59] = (-nj19_c1*xt48) * (cs53 * rs19);
     }
     {  // row 20
     const T rs20 = nt_rscale<T>(nt_exp_hi(x[20]), fh);
         const T nj20_c0 = T(2)*F.dt;
         const T nj20_c1 = K[K_b39]*nj20_c0;
         const T nj20_c2 = F.parthno3*K[K_b27];
-        const T nj20_c3 = F.dt*nt_cvt<T>(x[48]);
+        const T nj20_c3 = F.dt*xt48;
         const T nj20_c4 = T(2)*K[K_b12];
         const T nj20_c5 = K[K_b6]*nj20_c0;
-        J[233] = (-nj20_c1*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs20);
-        J[237] = (-F.dt*(F.parthno3*tj[J_hno3] + nj20_c2*nt_cvt<T>(x[43]))) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs20);
-        J[232] = (-F.dt*(T(2)*F.hnm*K[K_b32] + T(2)*tj[J_n2o5])) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs20);
-        J[235] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + tj[J_clono2_cl] + tj[J_clono2_clo])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs20);
-        J[229] = (-F.dt*tj[J_clno2]) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs20);
-        J[230] = (-F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + tj[J_brono2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs20);
-        J[238] = (-F.dt*(F.hnm*K[K_b24] + K[K_b28]*nt_cvt<T>(x[43]) + tj[J_hno4])) * (nt_scale<T>(nt_exp_hi(x[21]), fh) * rs20);
-        J[236] = (-nj20_c1*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs20);
-        J[243] = (-F.dt*(K[K_b28]*nt_cvt<T>(x[21]) + nj20_c2*nt_cvt<T>(x[4])) + K[K_b22]*nj20_c3) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs20);
-        J[241] = (K[K_d36]*nj20_c3) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs20);
-        J[240] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[13]) + K[K_e8]*nt_cvt<T>(x[19]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs20);
-        J[244] = (K[K_b23]*nj20_c3) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs20);
-        J[239] = (F.dt*(K[K_b22]*nt_cvt<T>(x[43]) + K[K_b23]*nt_cvt<T>(x[47]) + K[K_d31]*nt_cvt<T>(x[52]) + K[K_d36]*nt_cvt<T>(x[44]) + K[K_e13]*nt_cvt<T>(x[53]) + nj20_c4*nt_cvt<T>(x[54]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs20);
-        J[245] = (nj20_c5*nt_cvt<T>(x[51])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs20);
-        J[234] = (nj20_c5*nt_cvt<T>(x[49])) * (nt_scale<T>(nt_exp_hi(x[51]), fh) * rs20);
-        J[246] = (K[K_d31]*nj20_c3) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs20);
-        J[242] = (K[K_e13]*nj20_c3) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs20);
-        J[231] = (nj20_c3*nj20_c4) * (nt_scale<T>(nt_exp_hi(x[54]), fh) * rs20);
+        J[233] = (-nj20_c1*xt42) * (cs0 * rs20);
+        J[237] = (-F.dt*(F.parthno3*tj[J_hno3] + nj20_c2*xt43)) * (cs4 * rs20);
+        J[232] = (-F.dt*(T(2)*F.hnm*K[K_b32] + T(2)*tj[J_n2o5])) * (cs5 * rs20);
+        J[235] = (-F.dt*(K[K_d32]*xt45 + tj[J_clono2_cl] + tj[J_clono2_clo])) * (cs13 * rs20);
+        J[229] = (-F.dt*tj[J_clno2]) * (cs17 * rs20);
+        J[230] = (-F.dt*(K[K_e8]*xt45 + tj[J_brono2])) * (cs19 * rs20);
+        J[238] = (-F.dt*(F.hnm*K[K_b24] + K[K_b28]*xt43 + tj[J_hno4])) * (cs21 * rs20);
+        J[236] = (-nj20_c1*xt0) * (cs42 * rs20);
+        J[243] = (-F.dt*(K[K_b28]*xt21 + nj20_c2*xt4) + K[K_b22]*nj20_c3) * (cs43 * rs20);
+        J[241] = (K[K_d36]*nj20_c3) * (cs44 * rs20);
+        J[240] = (-F.dt*(K[K_d32]*xt13 + K[K_e8]*xt19)) * (cs45 * rs20);
+        J[244] = (K[K_b23]*nj20_c3) * (cs47 * rs20);
+        J[239] = (F.dt*(K[K_b22]*xt43 + K[K_b23]*xt47 + K[K_d31]*xt52 + K[K_d36]*xt44 + K[K_e13]*xt53 + nj20_c4*xt54)) * (cs48 * rs20);
+        J[245] = (nj20_c5*xt51) * (cs49 * rs20);
+        J[234] = (nj20_c5*xt49) * (cs51 * rs20);
+        J[246] = (K[K_d31]*nj20_c3) * (cs52 * rs20);
+        J[242] = (K[K_e13]*nj20_c3) * (cs53 * rs20);
+        J[231] = (nj20_c3*nj20_c4) * (cs54 * rs20);
     }
     {  // row 21
     const T rs21 = nt_rscale<T>(nt_exp_hi(x[21]), fh);
         const T nj21_c0 = F.dt*K[K_b23];
-        J[152] = (F.dt*(F.hnm*K[K_b24] + K[K_b28]*nt_cvt<T>(x[43]) + tj[J_hno4]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[21]), fh) * rs21);
-        J[154] = (F.dt*K[K_b28]*nt_cvt<T>(x[21])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs21);
-        J[155] = (-nj21_c0*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs21);
-        J[153] = (-nj21_c0*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs21);
+        J[152] = (F.dt*(F.hnm*K[K_b24] + K[K_b28]*xt43 + tj[J_hno4]) + T(1)) * (cs21 * rs21);
+        J[154] = (F.dt*K[K_b28]*xt21) * (cs43 * rs21);
+        J[155] = (-nj21_c0*xt48) * (cs47 * rs21);
+        J[153] = (-nj21_c0*xt47) * (cs48 * rs21);
     }
     {  // row 22
     const T rs22 = nt_rscale<T>(nt_exp_hi(x[22]), fh);
-        const T nj22_c0 = F.dt*nt_cvt<T>(x[44]);
-        const T nj22_c1 = T(3)*nt_cvt<T>(x[42]);
+        const T nj22_c0 = F.dt*xt44;
+        const T nj22_c1 = T(3)*xt42;
         const T nj22_c2 = T(2)*K[K_d91];
         const T nj22_c3 = T(4)*K[K_d93];
         const T nj22_c4 = T(3)*K[K_d94];
-        const T nj22_c5 = F.dt*nt_cvt<T>(x[52]);
+        const T nj22_c5 = F.dt*xt52;
         const T nj22_c6 = T(2)*K[K_d60];
         const T nj22_c7 = T(2)*K[K_d62];
-        J[141] = (K[K_d5]*nj22_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs22);
-        J[140] = (-F.dt*tj[J_oclo]) * (nt_scale<T>(nt_exp_hi(x[9]), fh) * rs22);
-        J[144] = (-F.dt*F.parthcl*(K[K_d11]*nt_cvt<T>(x[43]) + tj[J_hcl])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs22);
-        J[135] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + tj[J_clono2_cl] + tj[J_clono2_clo])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs22);
-        J[142] = (-F.dt*(K[K_d34]*nt_cvt<T>(x[43]) + K[K_d35]*nt_cvt<T>(x[45]) + tj[J_hocl]) + K[K_d37]*nj22_c0) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs22);
-        J[133] = (-T(2)*F.dt*tj[J_cl2]) * (nt_scale<T>(nt_exp_hi(x[15]), fh) * rs22);
-        J[128] = (-F.dt*tj[J_clno2]) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs22);
-        J[138] = (-F.dt*(T(2)*F.hnm*K[K_d61] + T(2)*tj[J_cl2o2])) * (nt_scale<T>(nt_exp_hi(x[24]), fh) * rs22);
-        J[132] = (-F.dt*tj[J_brcl]) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs22);
-        J[143] = (K[K_c10]*nj22_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs22);
-        J[137] = (-F.dt*(K[K_d90]*nj22_c1 + T(3)*tj[J_cfc11])) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs22);
-        J[131] = (-F.dt*(nj22_c2*nt_cvt<T>(x[42]) + T(2)*tj[J_cfc12])) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs22);
-        J[127] = (-F.dt*(K[K_d92]*nj22_c1 + T(3)*tj[J_cfc113])) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs22);
-        J[129] = (-F.dt*(nj22_c3*nt_cvt<T>(x[42]) + T(4)*tj[J_ccl4])) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs22);
-        J[136] = (-F.dt*(nj22_c4*nt_cvt<T>(x[43]) + T(3)*tj[J_ch3ccl3])) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs22);
-        J[134] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl])) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs22);
-        J[130] = (-F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22])) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs22);
-        J[139] = (-F.dt*(T(3)*K[K_d90]*nt_cvt<T>(x[30]) + T(3)*K[K_d92]*nt_cvt<T>(x[32]) + K[K_d96]*nt_cvt<T>(x[36]) + nj22_c2*nt_cvt<T>(x[31]) + nj22_c3*nt_cvt<T>(x[33]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs22);
-        J[149] = (-F.dt*(F.parthcl*K[K_d11]*nt_cvt<T>(x[12]) + K[K_d34]*nt_cvt<T>(x[14]) + K[K_d95]*nt_cvt<T>(x[35]) + K[K_d97]*nt_cvt<T>(x[36]) + nj22_c4*nt_cvt<T>(x[34])) + K[K_d9]*nj22_c5) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs22);
-        J[147] = (F.dt*(F.h2*K[K_d6] + K[K_c10]*nt_cvt<T>(x[27]) + K[K_d36]*nt_cvt<T>(x[48]) + K[K_d37]*nt_cvt<T>(x[14]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs22);
-        J[146] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[13]) + K[K_d35]*nt_cvt<T>(x[14]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs22);
-        J[150] = (F.dt*(K[K_d33]*nt_cvt<T>(x[52]) + K[K_d7]*nt_cvt<T>(x[44]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs22);
-        J[145] = (F.dt*(K[K_d31]*nt_cvt<T>(x[52]) + K[K_d36]*nt_cvt<T>(x[44]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs22);
-        J[151] = (F.dt*(K[K_d31]*nt_cvt<T>(x[48]) + K[K_d33]*nt_cvt<T>(x[47]) + K[K_d9]*nt_cvt<T>(x[43]) + K[K_e5a]*nt_cvt<T>(x[53]) + K[K_e5c]*nt_cvt<T>(x[53]) + nj22_c6*nt_cvt<T>(x[52]) + nj22_c7*nt_cvt<T>(x[52]) + nt_cvt<T>(x[52])*(nj22_c6 + nj22_c7))) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs22);
-        J[148] = (nj22_c5*(K[K_e5a] + K[K_e5c])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs22);
+        J[141] = (K[K_d5]*nj22_c0) * (cs1 * rs22);
+        J[140] = (-F.dt*tj[J_oclo]) * (cs9 * rs22);
+        J[144] = (-F.dt*F.parthcl*(K[K_d11]*xt43 + tj[J_hcl])) * (cs12 * rs22);
+        J[135] = (-F.dt*(K[K_d32]*xt45 + tj[J_clono2_cl] + tj[J_clono2_clo])) * (cs13 * rs22);
+        J[142] = (-F.dt*(K[K_d34]*xt43 + K[K_d35]*xt45 + tj[J_hocl]) + K[K_d37]*nj22_c0) * (cs14 * rs22);
+        J[133] = (-T(2)*F.dt*tj[J_cl2]) * (cs15 * rs22);
+        J[128] = (-F.dt*tj[J_clno2]) * (cs17 * rs22);
+        J[138] = (-F.dt*(T(2)*F.hnm*K[K_d61] + T(2)*tj[J_cl2o2])) * (cs24 * rs22);
+        J[132] = (-F.dt*tj[J_brcl]) * (cs26 * rs22);
+        J[143] = (K[K_c10]*nj22_c0) * (cs27 * rs22);
+        J[137] = (-F.dt*(K[K_d90]*nj22_c1 + T(3)*tj[J_cfc11])) * (cs30 * rs22);
+        J[131] = (-F.dt*(nj22_c2*xt42 + T(2)*tj[J_cfc12])) * (cs31 * rs22);
+        J[127] = (-F.dt*(K[K_d92]*nj22_c1 + T(3)*tj[J_cfc113])) * (cs32 * rs22);
+        J[129] = (-F.dt*(nj22_c3*xt42 + T(4)*tj[J_ccl4])) * (cs33 * rs22);
+        J[136] = (-F.dt*(nj22_c4*xt43 + T(3)*tj[J_ch3ccl3])) * (cs34 * rs22);
+        J[134] = (-F.dt*(K[K_d95]*xt43 + tj[J_ch3cl])) * (cs35 * rs22);
+        J[130] = (-F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22])) * (cs36 * rs22);
+        J[139] = (-F.dt*(T(3)*K[K_d90]*xt30 + T(3)*K[K_d92]*xt32 + K[K_d96]*xt36 + nj22_c2*xt31 + nj22_c3*xt33)) * (cs42 * rs22);
+        J[149] = (-F.dt*(F.parthcl*K[K_d11]*xt12 + K[K_d34]*xt14 + K[K_d95]*xt35 + K[K_d97]*xt36 + nj22_c4*xt34) + K[K_d9]*nj22_c5) * (cs43 * rs22);
+        J[147] = (F.dt*(F.h2*K[K_d6] + K[K_c10]*xt27 + K[K_d36]*xt48 + K[K_d37]*xt14 + K[K_d5]*xt1 + K[K_d7]*xt47)) * (cs44 * rs22);
+        J[146] = (-F.dt*(K[K_d32]*xt13 + K[K_d35]*xt14)) * (cs45 * rs22);
+        J[150] = (F.dt*(K[K_d33]*xt52 + K[K_d7]*xt44)) * (cs47 * rs22);
+        J[145] = (F.dt*(K[K_d31]*xt52 + K[K_d36]*xt44)) * (cs48 * rs22);
+        J[151] = (F.dt*(K[K_d31]*xt48 + K[K_d33]*xt47 + K[K_d9]*xt43 + K[K_e5a]*xt53 + K[K_e5c]*xt53 + nj22_c6*xt52 + nj22_c7*xt52 + xt52*(nj22_c6 + nj22_c7))) * (cs52 * rs22);
+        J[148] = (nj22_c5*(K[K_e5a] + K[K_e5c])) * (cs53 * rs22);
     }
     {  // row 23
     const T rs23 = nt_rscale<T>(nt_exp_hi(x[23]), fh);
         const T nj23_c0 = T(2)*het[7];
-        const T nj23_c1 = F.dt*F.parthbr*nt_cvt<T>(x[18]);
-        const T nj23_c2 = F.dt*nt_cvt<T>(x[53]);
-        J[196] = (-F.dt*(F.parthbr*(K[K_e11]*nt_cvt<T>(x[43]) + K[K_e9]*nt_cvt<T>(x[42]) + tj[J_hbr]) + nj23_c0*nt_cvt<T>(x[25]))) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs23);
-        J[193] = (-F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + tj[J_brono2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs23);
-        J[194] = (-F.dt*(K[K_e16]*nt_cvt<T>(x[45]) + nj23_c0*nt_cvt<T>(x[18]) + tj[J_hobr])) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs23);
-        J[192] = (-F.dt*tj[J_brcl]) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs23);
-        J[197] = (F.dt*K[K_c19]*nt_cvt<T>(x[50])) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs23);
-        J[195] = (-K[K_e9]*nj23_c1) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs23);
-        J[202] = (-K[K_e11]*nj23_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs23);
-        J[199] = (-F.dt*(K[K_e16]*nt_cvt<T>(x[25]) + K[K_e8]*nt_cvt<T>(x[19]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs23);
-        J[203] = (F.dt*(K[K_e15]*nt_cvt<T>(x[53]) + K[K_e7]*nt_cvt<T>(x[50]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs23);
-        J[198] = (K[K_e13]*nj23_c2) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs23);
-        J[201] = (F.dt*(K[K_c19]*nt_cvt<T>(x[27]) + K[K_e7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs23);
-        J[204] = (K[K_e5c]*nj23_c2) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs23);
-        J[200] = (F.dt*(K[K_e13]*nt_cvt<T>(x[48]) + K[K_e15]*nt_cvt<T>(x[47]) + K[K_e5c]*nt_cvt<T>(x[52]))) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs23);
+        const T nj23_c1 = F.dt*F.parthbr*xt18;
+        const T nj23_c2 = F.dt*xt53;
+        J[196] = (-F.dt*(F.parthbr*(K[K_e11]*xt43 + K[K_e9]*xt42 + tj[J_hbr]) + nj23_c0*xt25)) * (cs18 * rs23);
+        J[193] = (-F.dt*(K[K_e8]*xt45 + tj[J_brono2])) * (cs19 * rs23);
+        J[194] = (-F.dt*(K[K_e16]*xt45 + nj23_c0*xt18 + tj[J_hobr])) * (cs25 * rs23);
+        J[192] = (-F.dt*tj[J_brcl]) * (cs26 * rs23);
+        J[197] = (F.dt*K[K_c19]*xt50) * (cs27 * rs23);
+        J[195] = (-K[K_e9]*nj23_c1) * (cs42 * rs23);
+        J[202] = (-K[K_e11]*nj23_c1) * (cs43 * rs23);
+        J[199] = (-F.dt*(K[K_e16]*xt25 + K[K_e8]*xt19)) * (cs45 * rs23);
+        J[203] = (F.dt*(K[K_e15]*xt53 + K[K_e7]*xt50)) * (cs47 * rs23);
+        J[198] = (K[K_e13]*nj23_c2) * (cs48 * rs23);
+        J[201] = (F.dt*(K[K_c19]*xt27 + K[K_e7]*xt47)) * (cs50 * rs23);
+        J[204] = (K[K_e5c]*nj23_c2) * (cs52 * rs23);
+        J[200] = (F.dt*(K[K_e13]*xt48 + K[K_e15]*xt47 + K[K_e5c]*xt52)) * (cs53 * rs23);
     }
     {  // row 24
     const T rs24 = nt_rscale<T>(nt_exp_hi(x[24]), fh);
-        J[97] = (F.dt*(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[24]), fh) * rs24);
-        J[98] = (-T(2)*F.dt*K[K_d60]*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs24);
+        J[97] = (F.dt*(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(1)) * (cs24 * rs24);
+        J[98] = (-T(2)*F.dt*K[K_d60]*xt52) * (cs52 * rs24);
     }
     {  // row 25
     const T rs25 = nt_rscale<T>(nt_exp_hi(x[25]), fh);
         const T nj25_c0 = F.dt*het[5];
-        const T nj25_c1 = F.dt*nt_cvt<T>(x[25]);
+        const T nj25_c1 = F.dt*xt25;
         const T nj25_c2 = F.dt*K[K_e15];
-        J[83] = (-nj25_c0*nt_cvt<T>(x[19])) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs25);
-        J[82] = (het[6]*nj25_c1) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs25);
-        J[81] = (het[7]*nj25_c1) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs25);
-        J[79] = (-nj25_c0*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs25);
-        J[80] = (F.dt*(K[K_e16]*nt_cvt<T>(x[45]) + het[6]*nt_cvt<T>(x[12]) + het[7]*nt_cvt<T>(x[18]) + tj[J_hobr]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs25);
-        J[84] = (K[K_e16]*nj25_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs25);
-        J[86] = (-nj25_c2*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs25);
-        J[85] = (-nj25_c2*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs25);
+        J[83] = (-nj25_c0*xt19) * (cs2 * rs25);
+        J[82] = (het[6]*nj25_c1) * (cs12 * rs25);
+        J[81] = (het[7]*nj25_c1) * (cs18 * rs25);
+        J[79] = (-nj25_c0*xt2) * (cs19 * rs25);
+        J[80] = (F.dt*(K[K_e16]*xt45 + het[6]*xt12 + het[7]*xt18 + tj[J_hobr]) + T(1)) * (cs25 * rs25);
+        J[84] = (K[K_e16]*nj25_c1) * (cs45 * rs25);
+        J[86] = (-nj25_c2*xt53) * (cs47 * rs25);
+        J[85] = (-nj25_c2*xt47) * (cs53 * rs25);
     }
     {  // row 26
     const T rs26 = nt_rscale<T>(nt_exp_hi(x[26]), fh);
         const T nj26_c0 = F.dt*het[6];
         const T nj26_c1 = F.dt*het[8];
         const T nj26_c2 = F.dt*K[K_e5c];
-        J[47] = (-nj26_c0*nt_cvt<T>(x[25])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs26);
-        J[45] = (-nj26_c1*nt_cvt<T>(x[18])) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs26);
-        J[46] = (-nj26_c1*nt_cvt<T>(x[14])) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs26);
-        J[44] = (-nj26_c0*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs26);
-        J[43] = (F.dt*tj[J_brcl] + T(1)) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs26);
-        J[49] = (-nj26_c2*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs26);
-        J[48] = (-nj26_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs26);
+        J[47] = (-nj26_c0*xt25) * (cs12 * rs26);
+        J[45] = (-nj26_c1*xt18) * (cs14 * rs26);
+        J[46] = (-nj26_c1*xt14) * (cs18 * rs26);
+        J[44] = (-nj26_c0*xt12) * (cs25 * rs26);
+        J[43] = (F.dt*tj[J_brcl] + T(1)) * (cs26 * rs26);
+        J[49] = (-nj26_c2*xt53) * (cs52 * rs26);
+        J[48] = (-nj26_c2*xt52) * (cs53 * rs26);
     }
     {  // row 27
     const T rs27 = nt_rscale<T>(nt_exp_hi(x[27]), fh);
         const T nj27_c0 = F.dt*K[K_c1c];
         const T nj27_c1 = F.dt*K[K_c17b];
-        const T nj27_c2 = F.dt*nt_cvt<T>(x[27]);
+        const T nj27_c2 = F.dt*xt27;
         const T nj27_c3 = F.dt*K[K_c3];
-        J[219] = (-nj27_c0*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs27);
-        J[222] = (F.dt*(K[K_c10]*nt_cvt<T>(x[44]) + K[K_c19]*nt_cvt<T>(x[50]) + K[K_c8]*nt_cvt<T>(x[43]) + K[K_c9]*nt_cvt<T>(x[45]) + tj[J_ch2o_co] + tj[J_ch2o_hco]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs27);
+        J[219] = (-nj27_c0*xt42) * (cs1 * rs27);
+        J[222] = (F.dt*(K[K_c10]*xt44 + K[K_c19]*xt50 + K[K_c8]*xt43 + K[K_c9]*xt45 + tj[J_ch2o_co] + tj[J_ch2o_hco]) + T(1)) * (cs27 * rs27);
         J[221] = T(0);
-        J[217] = (-nj27_c1*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs27);
-        J[218] = (-nj27_c0*nt_cvt<T>(x[1])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs27);
-        J[226] = (F.dt*K[K_c8]*nt_cvt<T>(x[27]) - nj27_c1*nt_cvt<T>(x[29])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs27);
-        J[224] = (K[K_c10]*nj27_c2) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs27);
-        J[223] = (F.dt*K[K_c9]*nt_cvt<T>(x[27]) - nj27_c3*nt_cvt<T>(x[56])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs27);
+        J[217] = (-nj27_c1*xt43) * (cs29 * rs27);
+        J[218] = (-nj27_c0*xt1) * (cs42 * rs27);
+        J[226] = (F.dt*K[K_c8]*xt27 - nj27_c1*xt29) * (cs43 * rs27);
+        J[224] = (K[K_c10]*nj27_c2) * (cs44 * rs27);
+        J[223] = (F.dt*K[K_c9]*xt27 - nj27_c3*xt56) * (cs45 * rs27);
         J[227] = T(0);
-        J[225] = (K[K_c19]*nj27_c2) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs27);
+        J[225] = (K[K_c19]*nj27_c2) * (cs50 * rs27);
         J[228] = T(0);
-        J[220] = (-nj27_c3*nt_cvt<T>(x[45])) * (nt_scale<T>(nt_exp_hi(x[56]), fh) * rs27);
+        J[220] = (-nj27_c3*xt45) * (cs56 * rs27);
     }
     {  // row 28
     const T rs28 = nt_rscale<T>(nt_exp_hi(x[28]), fh);
-        const T nj28_c0 = T(2)*K[K_c14]*nt_cvt<T>(x[28]);
+        const T nj28_c0 = T(2)*K[K_c14]*xt28;
         const T nj28_c1 = F.dt*K[K_c17a];
-        const T nj28_c2 = F.dt*nt_cvt<T>(x[28]);
-        J[212] = (F.dt*nj28_c0 + F.dt*(K[K_c18]*nt_cvt<T>(x[52]) + K[K_c5]*nt_cvt<T>(x[49]) + K[K_c7]*nt_cvt<T>(x[47]) + nj28_c0) + T(1)) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs28);
-        J[210] = (-nj28_c1*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs28);
-        J[213] = (-nj28_c1*nt_cvt<T>(x[29])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs28);
-        J[214] = (K[K_c7]*nj28_c2) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs28);
-        J[215] = (K[K_c5]*nj28_c2) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs28);
-        J[216] = (K[K_c18]*nj28_c2) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs28);
-        J[211] = (-F.dt*F.o2*K[K_c4]) * (nt_scale<T>(nt_exp_hi(x[56]), fh) * rs28);
+        const T nj28_c2 = F.dt*xt28;
+        J[212] = (F.dt*nj28_c0 + F.dt*(K[K_c18]*xt52 + K[K_c5]*xt49 + K[K_c7]*xt47 + nj28_c0) + T(1)) * (cs28 * rs28);
+        J[210] = (-nj28_c1*xt43) * (cs29 * rs28);
+        J[213] = (-nj28_c1*xt29) * (cs43 * rs28);
+        J[214] = (K[K_c7]*nj28_c2) * (cs47 * rs28);
+        J[215] = (K[K_c5]*nj28_c2) * (cs49 * rs28);
+        J[216] = (K[K_c18]*nj28_c2) * (cs52 * rs28);
+        J[211] = (-F.dt*F.o2*K[K_c4]) * (cs56 * rs28);
     }
     {  // row 29
     const T rs29 = nt_rscale<T>(nt_exp_hi(x[29]), fh);
         const T nj29_c0 = F.dt*K[K_c7];
-        J[35] = (-nj29_c0*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs29);
-        J[34] = (F.dt*(K[K_c17a]*nt_cvt<T>(x[43]) + K[K_c17b]*nt_cvt<T>(x[43]) + tj[J_ch3o2h]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs29);
-        J[36] = (F.dt*nt_cvt<T>(x[29])*(K[K_c17a] + K[K_c17b])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs29);
-        J[37] = (-nj29_c0*nt_cvt<T>(x[28])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs29);
+        J[35] = (-nj29_c0*xt47) * (cs28 * rs29);
+        J[34] = (F.dt*(K[K_c17a]*xt43 + K[K_c17b]*xt43 + tj[J_ch3o2h]) + T(1)) * (cs29 * rs29);
+        J[36] = (F.dt*xt29*(K[K_c17a] + K[K_c17b])) * (cs43 * rs29);
+        J[37] = (-nj29_c0*xt28) * (cs47 * rs29);
     }
     {  // row 30
     const T rs30 = nt_rscale<T>(nt_exp_hi(x[30]), fh);
-        J[95] = (F.dt*(K[K_d90]*nt_cvt<T>(x[42]) + tj[J_cfc11]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs30);
-        J[96] = (F.dt*K[K_d90]*nt_cvt<T>(x[30])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs30);
+        J[95] = (F.dt*(K[K_d90]*xt42 + tj[J_cfc11]) + T(1)) * (cs30 * rs30);
+        J[96] = (F.dt*K[K_d90]*xt30) * (cs42 * rs30);
     }
     {  // row 31
     const T rs31 = nt_rscale<T>(nt_exp_hi(x[31]), fh);
-        J[41] = (F.dt*(K[K_d91]*nt_cvt<T>(x[42]) + tj[J_cfc12]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs31);
-        J[42] = (F.dt*K[K_d91]*nt_cvt<T>(x[31])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs31);
+        J[41] = (F.dt*(K[K_d91]*xt42 + tj[J_cfc12]) + T(1)) * (cs31 * rs31);
+        J[42] = (F.dt*K[K_d91]*xt31) * (cs42 * rs31);
     }
     {  // row 32
     const T rs32 = nt_rscale<T>(nt_exp_hi(x[32]), fh);
-        J[18] = (F.dt*(K[K_d92]*nt_cvt<T>(x[42]) + tj[J_cfc113]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs32);
-        J[19] = (F.dt*K[K_d92]*nt_cvt<T>(x[32])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs32);
+        J[18] = (F.dt*(K[K_d92]*xt42 + tj[J_cfc113]) + T(1)) * (cs32 * rs32);
+        J[19] = (F.dt*K[K_d92]*xt32) * (cs42 * rs32);
     }
     {  // row 33
     const T rs33 = nt_rscale<T>(nt_exp_hi(x[33]), fh);
-        J[32] = (F.dt*(K[K_d93]*nt_cvt<T>(x[42]) + tj[J_ccl4]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs33);
-        J[33] = (F.dt*K[K_d93]*nt_cvt<T>(x[33])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs33);
+        J[32] = (F.dt*(K[K_d93]*xt42 + tj[J_ccl4]) + T(1)) * (cs33 * rs33);
+        J[33] = (F.dt*K[K_d93]*xt33) * (cs42 * rs33);
     }
     {  // row 34
     const T rs34 = nt_rscale<T>(nt_exp_hi(x[34]), fh);
-        J[93] = (F.dt*(K[K_d94]*nt_cvt<T>(x[43]) + tj[J_ch3ccl3]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs34);
-        J[94] = (F.dt*K[K_d94]*nt_cvt<T>(x[34])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs34);
+        J[93] = (F.dt*(K[K_d94]*xt43 + tj[J_ch3ccl3]) + T(1)) * (cs34 * rs34);
+        J[94] = (F.dt*K[K_d94]*xt34) * (cs43 * rs34);
     }
     {  // row 35
     const T rs35 = nt_rscale<T>(nt_exp_hi(x[35]), fh);
-        J[66] = (F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs35);
-        J[67] = (F.dt*K[K_d95]*nt_cvt<T>(x[35])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs35);
+        J[66] = (F.dt*(K[K_d95]*xt43 + tj[J_ch3cl]) + T(1)) * (cs35 * rs35);
+        J[67] = (F.dt*K[K_d95]*xt35) * (cs43 * rs35);
     }
     {  // row 36
     const T rs36 = nt_rscale<T>(nt_exp_hi(x[36]), fh);
-        const T nj36_c0 = F.dt*nt_cvt<T>(x[36]);
-        J[38] = (F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs36);
-        J[39] = (K[K_d96]*nj36_c0) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs36);
-        J[40] = (K[K_d97]*nj36_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs36);
+        const T nj36_c0 = F.dt*xt36;
+        J[38] = (F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22]) + T(1)) * (cs36 * rs36);
+        J[39] = (K[K_d96]*nj36_c0) * (cs42 * rs36);
+        J[40] = (K[K_d97]*nj36_c0) * (cs43 * rs36);
     }
     {  // row 37
     const T rs37 = nt_rscale<T>(nt_exp_hi(x[37]), fh);
-        const T nj37_c0 = F.dt*nt_cvt<T>(x[37]);
-        J[52] = (F.dt*(K[K_e50]*nt_cvt<T>(x[42]) + K[K_e51]*nt_cvt<T>(x[43]) + tj[J_ch3br]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[37]), fh) * rs37);
-        J[53] = (K[K_e50]*nj37_c0) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs37);
-        J[54] = (K[K_e51]*nj37_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs37);
+        const T nj37_c0 = F.dt*xt37;
+        J[52] = (F.dt*(K[K_e50]*xt42 + K[K_e51]*xt43 + tj[J_ch3br]) + T(1)) * (cs37 * rs37);
+        J[53] = (K[K_e50]*nj37_c0) * (cs42 * rs37);
+        J[54] = (K[K_e51]*nj37_c0) * (cs43 * rs37);
     }
     {  // row 38
     const T rs38 = nt_rscale<T>(nt_exp_hi(x[38]), fh);
-        J[30] = (F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs38);
-        J[31] = (F.dt*K[K_e52]*nt_cvt<T>(x[38])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs38);
+        J[30] = (F.dt*(K[K_e52]*xt42 + tj[J_h1211]) + T(1)) * (cs38 * rs38);
+        J[31] = (F.dt*K[K_e52]*xt38) * (cs42 * rs38);
     }
     {  // row 39
     const T rs39 = nt_rscale<T>(nt_exp_hi(x[39]), fh);
-        J[50] = (F.dt*(K[K_e53]*nt_cvt<T>(x[42]) + tj[J_h1301]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[39]), fh) * rs39);
-        J[51] = (F.dt*K[K_e53]*nt_cvt<T>(x[39])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs39);
+        J[50] = (F.dt*(K[K_e53]*xt42 + tj[J_h1301]) + T(1)) * (cs39 * rs39);
+        J[51] = (F.dt*K[K_e53]*xt39) * (cs42 * rs39);
     }
     {  // row 40
     const T rs40 = nt_rscale<T>(nt_exp_hi(x[40]), fh);
         const T nj40_c0 = T(2)*K[K_e54];
-        J[16] = (F.dt*F.rain_hbr) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs40);
-        J[13] = (-F.dt*(K[K_e50]*nt_cvt<T>(x[42]) + K[K_e51]*nt_cvt<T>(x[43]) + tj[J_ch3br])) * (nt_scale<T>(nt_exp_hi(x[37]), fh) * rs40);
-        J[11] = (-F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211])) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs40);
-        J[12] = (-F.dt*(K[K_e53]*nt_cvt<T>(x[42]) + tj[J_h1301])) * (nt_scale<T>(nt_exp_hi(x[39]), fh) * rs40);
-        J[15] = (-F.dt*(nj40_c0*nt_cvt<T>(x[43]) + T(2)*tj[J_ch2br2])) * (nt_scale<T>(nt_exp_hi(x[41]), fh) * rs40);
-        J[14] = (-F.dt*(K[K_e50]*nt_cvt<T>(x[37]) + K[K_e52]*nt_cvt<T>(x[38]) + K[K_e53]*nt_cvt<T>(x[39]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs40);
-        J[17] = (-F.dt*(K[K_e51]*nt_cvt<T>(x[37]) + nj40_c0*nt_cvt<T>(x[41]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs40);
+        J[16] = (F.dt*F.rain_hbr) * (cs18 * rs40);
+        J[13] = (-F.dt*(K[K_e50]*xt42 + K[K_e51]*xt43 + tj[J_ch3br])) * (cs37 * rs40);
+        J[11] = (-F.dt*(K[K_e52]*xt42 + tj[J_h1211])) * (cs38 * rs40);
+        J[12] = (-F.dt*(K[K_e53]*xt42 + tj[J_h1301])) * (cs39 * rs40);
+        J[15] = (-F.dt*(nj40_c0*xt43 + T(2)*tj[J_ch2br2])) * (cs41 * rs40);
+        J[14] = (-F.dt*(K[K_e50]*xt37 + K[K_e52]*xt38 + K[K_e53]*xt39)) * (cs42 * rs40);
+        J[17] = (-F.dt*(K[K_e51]*xt37 + nj40_c0*xt41)) * (cs43 * rs40);
     }
     {  // row 41
     const T rs41 = nt_rscale<T>(nt_exp_hi(x[41]), fh);
-        J[125] = (F.dt*(K[K_e54]*nt_cvt<T>(x[43]) + tj[J_ch2br2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[41]), fh) * rs41);
-        J[126] = (F.dt*K[K_e54]*nt_cvt<T>(x[41])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs41);
+        J[125] = (F.dt*(K[K_e54]*xt43 + tj[J_ch2br2]) + T(1)) * (cs41 * rs41);
+        J[126] = (F.dt*K[K_e54]*xt41) * (cs43 * rs41);
     }
     {  // row 42
     const T rs42 = nt_rscale<T>(nt_exp_hi(x[42]), fh);
@@ -3990,7 +4800,7 @@ __device__ __forceinline__ void nt_jacobian_night(const FF& F, PK K, PK tj, PK h
         J[328] = T(0);
         J[316] = T(0);
         J[318] = T(0);
-        J[337] = (T(1)) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs43);
+        J[337] = (T(1)) * (cs43 * rs43);
         J[334] = T(0);
         J[333] = T(0);
         J[339] = T(0);
@@ -4030,7 +4840,7 @@ __device__ __forceinline__ void nt_jacobian_night(const FF& F, PK K, PK tj, PK h
     }
     {  // row 46
     const T rs46 = nt_rscale<T>(nt_exp_hi(x[46]), fh);
-        J[355] = (T(-1)) * (nt_scale<T>(nt_exp_hi(x[7]), fh) * rs46);
+        J[355] = (T(-1)) * (cs7 * rs46);
         J[358] = T(0);
         J[357] = T(0);
         J[359] = T(0);
@@ -4046,7 +4856,7 @@ __device__ __forceinline__ void nt_jacobian_night(const FF& F, PK K, PK tj, PK h
         J[347] = T(0);
         J[346] = T(0);
         J[352] = T(0);
-        J[351] = (T(1)) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs47);
+        J[351] = (T(1)) * (cs47 * rs47);
         J[353] = T(0);
         J[349] = T(0);
         J[354] = T(0);
@@ -4096,25 +4906,25 @@ __device__ __forceinline__ void nt_jacobian_night(const FF& F, PK K, PK tj, PK h
         J[178] = T(0);
     }
     const T N_cno_c0 = K[K_b9]/K[K_b12];
-    const T N_cno = N_cno_c0*nt_cvt<T>(x[46]);
+    const T N_cno = N_cno_c0*xt46;
     const T d_N_cno_46 = N_cno_c0;
-    const T N_dno = -N_cno + nt_cvt<T>(x[20]);
+    const T N_dno = -N_cno + xt20;
     const T d_N_dno_20 = T(1);
     const T d_N_dno_46 = -d_N_cno_46;
     const T N_no2_c0 = N_cno + T(1e-30);
     const T N_no2_c1 = T(1e-30)/N_no2_c0;
     const bool sel_N_no2 = (N_dno) > (T(1e-30));
-    const T N_no2 = sel_N_no2 ? T(N_dno) : T(N_no2_c1*nt_cvt<T>(x[20]));
+    const T N_no2 = sel_N_no2 ? T(N_dno) : T(N_no2_c1*xt20);
     const T d_N_no2_20 = sel_N_no2 ? T(d_N_dno_20) : T(N_no2_c1);
-    const T d_N_no2_46 = sel_N_no2 ? T(d_N_dno_46) : T(-T(1e-30)*d_N_cno_46*nt_cvt<T>(x[20])/(N_no2_c0*N_no2_c0));
+    const T d_N_no2_46 = sel_N_no2 ? T(d_N_dno_46) : T(-T(1e-30)*d_N_cno_46*xt20/(N_no2_c0*N_no2_c0));
     {  // row 48
     const T rs48 = nt_rscale<T>(nt_exp_hi(x[48]), fh);
-        J[270] = (-d_N_no2_20) * (nt_scale<T>(nt_exp_hi(x[20]), fh) * rs48);
+        J[270] = (-d_N_no2_20) * (cs20 * rs48);
         J[269] = T(0);
         J[272] = T(0);
-        J[275] = (-d_N_no2_46) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs48);
+        J[275] = (-d_N_no2_46) * (cs46 * rs48);
         J[274] = T(0);
-        J[271] = (T(1)) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs48);
+        J[271] = (T(1)) * (cs48 * rs48);
         J[276] = T(0);
         J[277] = T(0);
         J[273] = T(0);
@@ -4123,17 +4933,17 @@ __device__ __forceinline__ void nt_jacobian_night(const FF& F, PK K, PK tj, PK h
     const T N_no3_c1 = (T(1)/(N_no3_c0));
     const T N_no3_c2 = N_cno*N_no3_c1;
     const bool sel_N_no3 = (N_dno) > (T(1e-30));
-    const T N_no3 = sel_N_no3 ? T(N_cno) : T(N_no3_c2*nt_cvt<T>(x[20]));
+    const T N_no3 = sel_N_no3 ? T(N_cno) : T(N_no3_c2*xt20);
     const T d_N_no3_20 = sel_N_no3 ? T(T(0)) : T(N_no3_c2);
-    const T d_N_no3_46 = sel_N_no3 ? T(d_N_cno_46) : T(d_N_cno_46*(-N_cno*nt_cvt<T>(x[20])/(N_no3_c0*N_no3_c0) + N_no3_c1*nt_cvt<T>(x[20])));
+    const T d_N_no3_46 = sel_N_no3 ? T(d_N_cno_46) : T(d_N_cno_46*(-N_cno*xt20/(N_no3_c0*N_no3_c0) + N_no3_c1*xt20));
     {  // row 54
     const T rs54 = nt_rscale<T>(nt_exp_hi(x[54]), fh);
-        J[68] = (-d_N_no3_20) * (nt_scale<T>(nt_exp_hi(x[20]), fh) * rs54);
-        J[70] = (-d_N_no3_46) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs54);
+        J[68] = (-d_N_no3_20) * (cs20 * rs54);
+        J[70] = (-d_N_no3_46) * (cs46 * rs54);
         J[69] = T(0);
     }
-    const bool sel_N_clo = (nt_cvt<T>(x[22])) >= (T(0));
-    const T N_clo = sel_N_clo ? T(nt_cvt<T>(x[22])) : T(T(0));
+    const bool sel_N_clo = (xt22) >= (T(0));
+    const T N_clo = sel_N_clo ? T(xt22) : T(T(0));
     const T d_N_clo_22 = sel_N_clo ? T(T(1)) : T(T(0));
     {  // row 52
     const T rs52 = nt_rscale<T>(nt_exp_hi(x[52]), fh);
@@ -4141,7 +4951,7 @@ __device__ __forceinline__ void nt_jacobian_night(const FF& F, PK K, PK tj, PK h
         J[373] = T(0);
         J[372] = T(0);
         J[370] = T(0);
-        J[368] = (-d_N_clo_22) * (nt_scale<T>(nt_exp_hi(x[22]), fh) * rs52);
+        J[368] = (-d_N_clo_22) * (cs22 * rs52);
         J[371] = T(0);
         J[377] = T(0);
         J[375] = T(0);
@@ -4149,15 +4959,15 @@ __device__ __forceinline__ void nt_jacobian_night(const FF& F, PK K, PK tj, PK h
         J[378] = T(0);
         J[374] = T(0);
         J[380] = T(0);
-        J[381] = (T(1)) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs52);
+        J[381] = (T(1)) * (cs52 * rs52);
         J[376] = T(0);
     }
-    const bool sel_N_bro = (nt_cvt<T>(x[23])) >= (T(0));
-    const T N_bro = sel_N_bro ? T(nt_cvt<T>(x[23])) : T(T(0));
+    const bool sel_N_bro = (xt23) >= (T(0));
+    const T N_bro = sel_N_bro ? T(xt23) : T(T(0));
     const T d_N_bro_23 = sel_N_bro ? T(T(1)) : T(T(0));
     {  // row 53
     const T rs53 = nt_rscale<T>(nt_exp_hi(x[53]), fh);
-        J[297] = (-d_N_bro_23) * (nt_scale<T>(nt_exp_hi(x[23]), fh) * rs53);
+        J[297] = (-d_N_bro_23) * (cs23 * rs53);
         J[298] = T(0);
         J[302] = T(0);
         J[300] = T(0);
@@ -4166,55 +4976,55 @@ __device__ __forceinline__ void nt_jacobian_night(const FF& F, PK K, PK tj, PK h
         J[299] = T(0);
         J[305] = T(0);
         J[306] = T(0);
-        J[301] = (T(1)) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs53);
+        J[301] = (T(1)) * (cs53 * rs53);
     }
-    const T N_t06_c0 = tj[J_hocl]*nt_cvt<T>(x[14]);
-    const T N_t06_c1 = K[K_d33]*nt_cvt<T>(x[52]);
-    const T N_t06_c2 = N_t06_c1*nt_cvt<T>(x[47]);
+    const T N_t06_c0 = tj[J_hocl]*xt14;
+    const T N_t06_c1 = K[K_d33]*xt52;
+    const T N_t06_c2 = N_t06_c1*xt47;
     const bool sel_N_t06 = (N_t06_c0) <= (N_t06_c2);
     const T N_t06 = sel_N_t06 ? T(N_t06_c0) : T(N_t06_c2);
     const T d_N_t06_14 = sel_N_t06 ? T(tj[J_hocl]) : T(T(0));
     const T d_N_t06_47 = sel_N_t06 ? T(T(0)) : T(N_t06_c1);
-    const T d_N_t06_52 = sel_N_t06 ? T(T(0)) : T(K[K_d33]*nt_cvt<T>(x[47]));
-    const T N_t07_c0 = K[K_e5c]*nt_cvt<T>(x[53]);
-    const T N_t07_c1 = N_t07_c0*nt_cvt<T>(x[52]);
-    const T N_t07_c2 = tj[J_brcl]*nt_cvt<T>(x[26]);
+    const T d_N_t06_52 = sel_N_t06 ? T(T(0)) : T(K[K_d33]*xt47);
+    const T N_t07_c0 = K[K_e5c]*xt53;
+    const T N_t07_c1 = N_t07_c0*xt52;
+    const T N_t07_c2 = tj[J_brcl]*xt26;
     const bool sel_N_t07 = (N_t07_c1) <= (N_t07_c2);
     const T N_t07 = sel_N_t07 ? T(N_t07_c1) : T(N_t07_c2);
     const T d_N_t07_26 = sel_N_t07 ? T(T(0)) : T(tj[J_brcl]);
     const T d_N_t07_52 = sel_N_t07 ? T(N_t07_c0) : T(T(0));
-    const T d_N_t07_53 = sel_N_t07 ? T(K[K_e5c]*nt_cvt<T>(x[52])) : T(T(0));
-    const T N_t09_c0 = K[K_e15]*nt_cvt<T>(x[53]);
-    const T N_t09_c1 = N_t09_c0*nt_cvt<T>(x[47]);
-    const T N_t09_c2 = tj[J_hobr]*nt_cvt<T>(x[25]);
+    const T d_N_t07_53 = sel_N_t07 ? T(K[K_e5c]*xt52) : T(T(0));
+    const T N_t09_c0 = K[K_e15]*xt53;
+    const T N_t09_c1 = N_t09_c0*xt47;
+    const T N_t09_c2 = tj[J_hobr]*xt25;
     const bool sel_N_t09 = (N_t09_c1) <= (N_t09_c2);
     const T N_t09 = sel_N_t09 ? T(N_t09_c1) : T(N_t09_c2);
     const T d_N_t09_25 = sel_N_t09 ? T(T(0)) : T(tj[J_hobr]);
     const T d_N_t09_47 = sel_N_t09 ? T(N_t09_c0) : T(T(0));
-    const T d_N_t09_53 = sel_N_t09 ? T(K[K_e15]*nt_cvt<T>(x[47])) : T(T(0));
+    const T d_N_t09_53 = sel_N_t09 ? T(K[K_e15]*xt47) : T(T(0));
     {  // row 7
     const T rs7 = nt_rscale<T>(nt_exp_hi(x[7]), fh);
         const T nj7_c0 = T(2)*F.dt;
         const T nj7_c1 = tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
-        const T nj7_c2 = F.dt*nt_cvt<T>(x[49]);
+        const T nj7_c2 = F.dt*xt49;
         const T nj7_c3 = T(2)*K[K_b3];
         const T nj7_c4 = T(2)*K[K_d3];
         const T nj7_c5 = T(2)*K[K_hk3];
         const T nj7_c6 = T(2)*K[K_b9]*nj7_c1;
-        J[105] = (nj7_c0*nj7_c1*tj[J_clono2_cl]) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs7);
-        J[106] = (F.dt*d_N_t06_14) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs7);
-        J[104] = (F.dt*d_N_t09_25) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs7);
-        J[103] = (d_N_t07_26*nj7_c0) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs7);
-        J[108] = (-K[K_c5]*nj7_c2) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs7);
-        J[112] = (F.dt*(K[K_a5]*nt_cvt<T>(x[45]) + K[K_a6]*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs7);
-        J[110] = (F.dt*(K[K_a5]*nt_cvt<T>(x[43]) + K[K_a7]*nt_cvt<T>(x[47]) + T(4)*K[K_hk1]*nt_cvt<T>(x[45]) + nj7_c3*nt_cvt<T>(x[48]) + nj7_c4*nt_cvt<T>(x[52]) + nj7_c5*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs7);
-        J[114] = (F.dt*(K[K_a2]*nt_cvt<T>(x[55]) + K[K_a6]*nt_cvt<T>(x[43]) + K[K_a6b]*nt_cvt<T>(x[47]) + nj7_c5*nt_cvt<T>(x[45]) + nj7_c6*nt_cvt<T>(x[48]))) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs7);
-        J[113] = (F.dt*d_N_t06_47 + F.dt*d_N_t09_47 + F.dt*(K[K_a6b]*nt_cvt<T>(x[46]) + K[K_a7]*nt_cvt<T>(x[45])) - K[K_a26]*nj7_c2) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs7);
-        J[109] = (F.dt*(nj7_c3*nt_cvt<T>(x[45]) + nj7_c6*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs7);
-        J[115] = (-F.dt*(K[K_a26]*nt_cvt<T>(x[47]) + K[K_c5]*nt_cvt<T>(x[28]))) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs7);
-        J[116] = (F.dt*d_N_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*nt_cvt<T>(x[52])/(F.hnm*K[K_d61] + tj[J_cl2o2]) + nj7_c4*nt_cvt<T>(x[45])) + d_N_t07_52*nj7_c0) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs7);
-        J[111] = (F.dt*d_N_t09_53 + d_N_t07_53*nj7_c0) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs7);
-        J[107] = (F.dt*K[K_a2]*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs7);
+        J[105] = (nj7_c0*nj7_c1*tj[J_clono2_cl]) * (cs13 * rs7);
+        J[106] = (F.dt*d_N_t06_14) * (cs14 * rs7);
+        J[104] = (F.dt*d_N_t09_25) * (cs25 * rs7);
+        J[103] = (d_N_t07_26*nj7_c0) * (cs26 * rs7);
+        J[108] = (-K[K_c5]*nj7_c2) * (cs28 * rs7);
+        J[112] = (F.dt*(K[K_a5]*xt45 + K[K_a6]*xt46)) * (cs43 * rs7);
+        J[110] = (F.dt*(K[K_a5]*xt43 + K[K_a7]*xt47 + T(4)*K[K_hk1]*xt45 + nj7_c3*xt48 + nj7_c4*xt52 + nj7_c5*xt46)) * (cs45 * rs7);
+        J[114] = (F.dt*(K[K_a2]*xt55 + K[K_a6]*xt43 + K[K_a6b]*xt47 + nj7_c5*xt45 + nj7_c6*xt48)) * (cs46 * rs7);
+        J[113] = (F.dt*d_N_t06_47 + F.dt*d_N_t09_47 + F.dt*(K[K_a6b]*xt46 + K[K_a7]*xt45) - K[K_a26]*nj7_c2) * (cs47 * rs7);
+        J[109] = (F.dt*(nj7_c3*xt45 + nj7_c6*xt46)) * (cs48 * rs7);
+        J[115] = (-F.dt*(K[K_a26]*xt47 + K[K_c5]*xt28)) * (cs49 * rs7);
+        J[116] = (F.dt*d_N_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*xt52/(F.hnm*K[K_d61] + tj[J_cl2o2]) + nj7_c4*xt45) + d_N_t07_52*nj7_c0) * (cs52 * rs7);
+        J[111] = (F.dt*d_N_t09_53 + d_N_t07_53*nj7_c0) * (cs53 * rs7);
+        J[107] = (F.dt*K[K_a2]*xt46) * (cs55 * rs7);
     }
 }
 
@@ -4267,221 +5077,323 @@ __device__ __forceinline__ void nt_residual_night_w2_0(const FF& F, PK K, PK tj,
 template <typename T, typename FF, typename PK, typename PJ>
 __device__ __forceinline__ void nt_jacobian_night_w2_0(const FF& F, PK K, PK tj, PK het, const double* __restrict__ x, double floor_, PJ J) {
     const int fh = nt_exp_hi(floor_);
+    const T xt0 = nt_cvt<T>(x[0]);
+    const T xt1 = nt_cvt<T>(x[1]);
+    const T xt2 = nt_cvt<T>(x[2]);
+    const T xt3 = nt_cvt<T>(x[3]);
+    const T xt4 = nt_cvt<T>(x[4]);
+    const T xt5 = nt_cvt<T>(x[5]);
+    const T xt6 = nt_cvt<T>(x[6]);
+    const T xt7 = nt_cvt<T>(x[7]);
+    const T xt8 = nt_cvt<T>(x[8]);
+    const T xt9 = nt_cvt<T>(x[9]);
+    const T xt10 = nt_cvt<T>(x[10]);
+    const T xt11 = nt_cvt<T>(x[11]);
+    const T xt12 = nt_cvt<T>(x[12]);
+    const T xt13 = nt_cvt<T>(x[13]);
+    const T xt14 = nt_cvt<T>(x[14]);
+    const T xt15 = nt_cvt<T>(x[15]);
+    const T xt16 = nt_cvt<T>(x[16]);
+    const T xt17 = nt_cvt<T>(x[17]);
+    const T xt18 = nt_cvt<T>(x[18]);
+    const T xt19 = nt_cvt<T>(x[19]);
+    const T xt20 = nt_cvt<T>(x[20]);
+    const T xt21 = nt_cvt<T>(x[21]);
+    const T xt22 = nt_cvt<T>(x[22]);
+    const T xt23 = nt_cvt<T>(x[23]);
+    const T xt24 = nt_cvt<T>(x[24]);
+    const T xt25 = nt_cvt<T>(x[25]);
+    const T xt26 = nt_cvt<T>(x[26]);
+    const T xt27 = nt_cvt<T>(x[27]);
+    const T xt28 = nt_cvt<T>(x[28]);
+    const T xt29 = nt_cvt<T>(x[29]);
+    const T xt30 = nt_cvt<T>(x[30]);
+    const T xt31 = nt_cvt<T>(x[31]);
+    const T xt32 = nt_cvt<T>(x[32]);
+    const T xt33 = nt_cvt<T>(x[33]);
+    const T xt34 = nt_cvt<T>(x[34]);
+    const T xt35 = nt_cvt<T>(x[35]);
+    const T xt36 = nt_cvt<T>(x[36]);
+    const T xt37 = nt_cvt<T>(x[37]);
+    const T xt38 = nt_cvt<T>(x[38]);
+    const T xt39 = nt_cvt<T>(x[39]);
+    const T xt40 = nt_cvt<T>(x[40]);
+    const T xt41 = nt_cvt<T>(x[41]);
+    const T xt42 = nt_cvt<T>(x[42]);
+    const T xt43 = nt_cvt<T>(x[43]);
+    const T xt44 = nt_cvt<T>(x[44]);
+    const T xt45 = nt_cvt<T>(x[45]);
+    const T xt46 = nt_cvt<T>(x[46]);
+    const T xt47 = nt_cvt<T>(x[47]);
+    const T xt48 = nt_cvt<T>(x[48]);
+    const T xt49 = nt_cvt<T>(x[49]);
+    const T xt50 = nt_cvt<T>(x[50]);
+    const T xt51 = nt_cvt<T>(x[51]);
+    const T xt52 = nt_cvt<T>(x[52]);
+    const T xt53 = nt_cvt<T>(x[53]);
+    const T xt54 = nt_cvt<T>(x[54]);
+    const T xt55 = nt_cvt<T>(x[55]);
+    const T xt56 = nt_cvt<T>(x[56]);
+    const T cs0 = nt_scale<T>(nt_exp_hi(x[0]), fh);
+    const T cs1 = nt_scale<T>(nt_exp_hi(x[1]), fh);
+    const T cs2 = nt_scale<T>(nt_exp_hi(x[2]), fh);
+    const T cs4 = nt_scale<T>(nt_exp_hi(x[4]), fh);
+    const T cs5 = nt_scale<T>(nt_exp_hi(x[5]), fh);
+    const T cs7 = nt_scale<T>(nt_exp_hi(x[7]), fh);
+    const T cs8 = nt_scale<T>(nt_exp_hi(x[8]), fh);
+    const T cs9 = nt_scale<T>(nt_exp_hi(x[9]), fh);
+    const T cs12 = nt_scale<T>(nt_exp_hi(x[12]), fh);
+    const T cs13 = nt_scale<T>(nt_exp_hi(x[13]), fh);
+    const T cs14 = nt_scale<T>(nt_exp_hi(x[14]), fh);
+    const T cs15 = nt_scale<T>(nt_exp_hi(x[15]), fh);
+    const T cs16 = nt_scale<T>(nt_exp_hi(x[16]), fh);
+    const T cs17 = nt_scale<T>(nt_exp_hi(x[17]), fh);
+    const T cs18 = nt_scale<T>(nt_exp_hi(x[18]), fh);
+    const T cs19 = nt_scale<T>(nt_exp_hi(x[19]), fh);
+    const T cs20 = nt_scale<T>(nt_exp_hi(x[20]), fh);
+    const T cs21 = nt_scale<T>(nt_exp_hi(x[21]), fh);
+    const T cs24 = nt_scale<T>(nt_exp_hi(x[24]), fh);
+    const T cs25 = nt_scale<T>(nt_exp_hi(x[25]), fh);
+    const T cs26 = nt_scale<T>(nt_exp_hi(x[26]), fh);
+    const T cs27 = nt_scale<T>(nt_exp_hi(x[27]), fh);
+    const T cs28 = nt_scale<T>(nt_exp_hi(x[28]), fh);
+    const T cs29 = nt_scale<T>(nt_exp_hi(x[29]), fh);
+    const T cs30 = nt_scale<T>(nt_exp_hi(x[30]), fh);
+    const T cs31 = nt_scale<T>(nt_exp_hi(x[31]), fh);
+    const T cs32 = nt_scale<T>(nt_exp_hi(x[32]), fh);
+    const T cs33 = nt_scale<T>(nt_exp_hi(x[33]), fh);
+    const T cs34 = nt_scale<T>(nt_exp_hi(x[34]), fh);
+    const T cs35 = nt_scale<T>(nt_exp_hi(x[35]), fh);
+    const T cs36 = nt_scale<T>(nt_exp_hi(x[36]), fh);
+    const T cs38 = nt_scale<T>(nt_exp_hi(x[38]), fh);
+    const T cs41 = nt_scale<T>(nt_exp_hi(x[41]), fh);
+    const T cs42 = nt_scale<T>(nt_exp_hi(x[42]), fh);
+    const T cs43 = nt_scale<T>(nt_exp_hi(x[43]), fh);
+    const T cs44 = nt_scale<T>(nt_exp_hi(x[44]), fh);
+    const T cs45 = nt_scale<T>(nt_exp_hi(x[45]), fh);
+    const T cs46 = nt_scale<T>(nt_exp_hi(x[46]), fh);
+    const T cs47 = nt_scale<T>(nt_exp_hi(x[47]), fh);
+    const T cs48 = nt_scale<T>(nt_exp_hi(x[48]), fh);
+    const T cs49 = nt_scale<T>(nt_exp_hi(x[49]), fh);
+    const T cs50 = nt_scale<T>(nt_exp_hi(x[50]), fh);
+    const T cs52 = nt_scale<T>(nt_exp_hi(x[52]), fh);
+    const T cs53 = nt_scale<T>(nt_exp_hi(x[53]), fh);
+    const T cs55 = nt_scale<T>(nt_exp_hi(x[55]), fh);
     {  // row 0
     const T rs0 = nt_rscale<T>(nt_exp_hi(x[0]), fh);
         const T nj0_c0 = K[K_b38] + K[K_b39];
-        J[76] = (F.dt*(nj0_c0*nt_cvt<T>(x[42]) + tj[J_n2o]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs0);
-        J[77] = (F.dt*nj0_c0*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs0);
+        J[76] = (F.dt*(nj0_c0*xt42 + tj[J_n2o]) + T(1)) * (cs0 * rs0);
+        J[77] = (F.dt*nj0_c0*xt0) * (cs42 * rs0);
     }
     {  // row 1
     const T rs1 = nt_rscale<T>(nt_exp_hi(x[1]), fh);
-        const T nj1_c0 = F.dt*nt_cvt<T>(x[1]);
-        J[157] = (F.dt*(K[K_c1a]*nt_cvt<T>(x[42]) + K[K_c1b]*nt_cvt<T>(x[42]) + K[K_c1c]*nt_cvt<T>(x[42]) + K[K_c2]*nt_cvt<T>(x[43]) + K[K_d5]*nt_cvt<T>(x[44])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs1);
-        J[156] = (nj1_c0*(K[K_c1a] + K[K_c1b] + K[K_c1c])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs1);
-        J[159] = (K[K_c2]*nj1_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs1);
-        J[158] = (K[K_d5]*nj1_c0) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs1);
+        const T nj1_c0 = F.dt*xt1;
+        J[157] = (F.dt*(K[K_c1a]*xt42 + K[K_c1b]*xt42 + K[K_c1c]*xt42 + K[K_c2]*xt43 + K[K_d5]*xt44) + T(1)) * (cs1 * rs1);
+        J[156] = (nj1_c0*(K[K_c1a] + K[K_c1b] + K[K_c1c])) * (cs42 * rs1);
+        J[159] = (K[K_c2]*nj1_c0) * (cs43 * rs1);
+        J[158] = (K[K_d5]*nj1_c0) * (cs44 * rs1);
     }
     {  // row 4
     const T rs4 = nt_rscale<T>(nt_exp_hi(x[4]), fh);
         const T nj4_c0 = T(2)*het[2];
         const T nj4_c1 = F.dt*K[K_b22];
-        J[122] = (-F.dt*(het[0]*nt_cvt<T>(x[13]) + het[5]*nt_cvt<T>(x[19]) + nj4_c0*nt_cvt<T>(x[5]))) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs4);
-        J[120] = (F.dt*(F.parthno3*(K[K_b27]*nt_cvt<T>(x[43]) + tj[J_hno3]) + F.rain_hno3) + T(1)) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs4);
-        J[118] = (-F.dt*(het[3]*nt_cvt<T>(x[12]) + nj4_c0*nt_cvt<T>(x[2]))) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs4);
-        J[121] = (-F.dt*(het[1]*nt_cvt<T>(x[13]) + het[3]*nt_cvt<T>(x[5]))) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs4);
-        J[119] = (-F.dt*(het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs4);
-        J[117] = (-F.dt*het[5]*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs4);
-        J[124] = (F.dt*F.parthno3*K[K_b27]*nt_cvt<T>(x[4]) - nj4_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs4);
-        J[123] = (-nj4_c1*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs4);
+        J[122] = (-F.dt*(het[0]*xt13 + het[5]*xt19 + nj4_c0*xt5)) * (cs2 * rs4);
+        J[120] = (F.dt*(F.parthno3*(K[K_b27]*xt43 + tj[J_hno3]) + F.rain_hno3) + T(1)) * (cs4 * rs4);
+        J[118] = (-F.dt*(het[3]*xt12 + nj4_c0*xt2)) * (cs5 * rs4);
+        J[121] = (-F.dt*(het[1]*xt13 + het[3]*xt5)) * (cs12 * rs4);
+        J[119] = (-F.dt*(het[0]*xt2 + het[1]*xt12)) * (cs13 * rs4);
+        J[117] = (-F.dt*het[5]*xt2) * (cs19 * rs4);
+        J[124] = (F.dt*F.parthno3*K[K_b27]*xt4 - nj4_c1*xt48) * (cs43 * rs4);
+        J[123] = (-nj4_c1*xt43) * (cs48 * rs4);
     }
     {  // row 6
     const T rs6 = nt_rscale<T>(nt_exp_hi(x[6]), fh);
-        const T nj6_c0 = T(3)*nt_cvt<T>(x[42]);
+        const T nj6_c0 = T(3)*xt42;
         const T nj6_c1 = T(2)*K[K_d91];
         const T nj6_c2 = T(4)*K[K_d93];
         const T nj6_c3 = T(3)*K[K_d94];
-        J[9] = (F.dt*F.rain_hcl) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs6);
-        J[7] = (-F.dt*(K[K_d90]*nj6_c0 + T(3)*tj[J_cfc11])) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs6);
-        J[4] = (-F.dt*(nj6_c1*nt_cvt<T>(x[42]) + T(2)*tj[J_cfc12])) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs6);
-        J[0] = (-F.dt*(K[K_d92]*nj6_c0 + T(3)*tj[J_cfc113])) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs6);
-        J[2] = (-F.dt*(nj6_c2*nt_cvt<T>(x[42]) + T(4)*tj[J_ccl4])) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs6);
-        J[6] = (-F.dt*(nj6_c3*nt_cvt<T>(x[43]) + T(3)*tj[J_ch3ccl3])) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs6);
-        J[5] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl])) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs6);
-        J[3] = (-F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22])) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs6);
-        J[1] = (-F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211])) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs6);
-        J[8] = (-F.dt*(T(3)*K[K_d90]*nt_cvt<T>(x[30]) + T(3)*K[K_d92]*nt_cvt<T>(x[32]) + K[K_d96]*nt_cvt<T>(x[36]) + K[K_e52]*nt_cvt<T>(x[38]) + nj6_c1*nt_cvt<T>(x[31]) + nj6_c2*nt_cvt<T>(x[33]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs6);
-        J[10] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[35]) + K[K_d97]*nt_cvt<T>(x[36]) + nj6_c3*nt_cvt<T>(x[34]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs6);
+        J[9] = (F.dt*F.rain_hcl) * (cs12 * rs6);
+        J[7] = (-F.dt*(K[K_d90]*nj6_c0 + T(3)*tj[J_cfc11])) * (cs30 * rs6);
+        J[4] = (-F.dt*(nj6_c1*xt42 + T(2)*tj[J_cfc12])) * (cs31 * rs6);
+        J[0] = (-F.dt*(K[K_d92]*nj6_c0 + T(3)*tj[J_cfc113])) * (cs32 * rs6);
+        J[2] = (-F.dt*(nj6_c2*xt42 + T(4)*tj[J_ccl4])) * (cs33 * rs6);
+        J[6] = (-F.dt*(nj6_c3*xt43 + T(3)*tj[J_ch3ccl3])) * (cs34 * rs6);
+        J[5] = (-F.dt*(K[K_d95]*xt43 + tj[J_ch3cl])) * (cs35 * rs6);
+        J[3] = (-F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22])) * (cs36 * rs6);
+        J[1] = (-F.dt*(K[K_e52]*xt42 + tj[J_h1211])) * (cs38 * rs6);
+        J[8] = (-F.dt*(T(3)*K[K_d90]*xt30 + T(3)*K[K_d92]*xt32 + K[K_d96]*xt36 + K[K_e52]*xt38 + nj6_c1*xt31 + nj6_c2*xt33)) * (cs42 * rs6);
+        J[10] = (-F.dt*(K[K_d95]*xt35 + K[K_d97]*xt36 + nj6_c3*xt34)) * (cs43 * rs6);
     }
     {  // row 14
     const T rs14 = nt_rscale<T>(nt_exp_hi(x[14]), fh);
         const T nj14_c0 = F.dt*het[0];
-        const T nj14_c1 = F.dt*nt_cvt<T>(x[14]);
+        const T nj14_c1 = F.dt*xt14;
         const T nj14_c2 = F.dt*K[K_d33];
-        J[170] = (-nj14_c0*nt_cvt<T>(x[13])) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs14);
-        J[169] = (het[4]*nj14_c1) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs14);
-        J[166] = (-nj14_c0*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs14);
-        J[167] = (F.dt*(K[K_d34]*nt_cvt<T>(x[43]) + K[K_d35]*nt_cvt<T>(x[45]) + K[K_d37]*nt_cvt<T>(x[44]) + het[4]*nt_cvt<T>(x[12]) + het[8]*nt_cvt<T>(x[18]) + tj[J_hocl]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs14);
-        J[168] = (het[8]*nj14_c1) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs14);
-        J[173] = (K[K_d34]*nj14_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs14);
-        J[172] = (K[K_d37]*nj14_c1) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs14);
-        J[171] = (K[K_d35]*nj14_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs14);
-        J[174] = (-nj14_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs14);
-        J[175] = (-nj14_c2*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs14);
+        J[170] = (-nj14_c0*xt13) * (cs2 * rs14);
+        J[169] = (het[4]*nj14_c1) * (cs12 * rs14);
+        J[166] = (-nj14_c0*xt2) * (cs13 * rs14);
+        J[167] = (F.dt*(K[K_d34]*xt43 + K[K_d35]*xt45 + K[K_d37]*xt44 + het[4]*xt12 + het[8]*xt18 + tj[J_hocl]) + T(1)) * (cs14 * rs14);
+        J[168] = (het[8]*nj14_c1) * (cs18 * rs14);
+        J[173] = (K[K_d34]*nj14_c1) * (cs43 * rs14);
+        J[172] = (K[K_d37]*nj14_c1) * (cs44 * rs14);
+        J[171] = (K[K_d35]*nj14_c1) * (cs45 * rs14);
+        J[174] = (-nj14_c2*xt52) * (cs47 * rs14);
+        J[175] = (-nj14_c2*xt47) * (cs52 * rs14);
     }
     {  // row 15
     const T rs15 = nt_rscale<T>(nt_exp_hi(x[15]), fh);
-        J[63] = (-F.dt*(het[1]*nt_cvt<T>(x[13]) + het[4]*nt_cvt<T>(x[14]))) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs15);
-        J[61] = (-F.dt*het[1]*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs15);
-        J[62] = (-F.dt*(K[K_d37]*nt_cvt<T>(x[44]) + het[4]*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs15);
-        J[60] = (F.dt*tj[J_cl2] + T(1)) * (nt_scale<T>(nt_exp_hi(x[15]), fh) * rs15);
-        J[64] = (-F.dt*K[K_d37]*nt_cvt<T>(x[14])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs15);
-        J[65] = (-T(2)*F.dt*K[K_d62]*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs15);
+        J[63] = (-F.dt*(het[1]*xt13 + het[4]*xt14)) * (cs12 * rs15);
+        J[61] = (-F.dt*het[1]*xt12) * (cs13 * rs15);
+        J[62] = (-F.dt*(K[K_d37]*xt44 + het[4]*xt12)) * (cs14 * rs15);
+        J[60] = (F.dt*tj[J_cl2] + T(1)) * (cs15 * rs15);
+        J[64] = (-F.dt*K[K_d37]*xt14) * (cs44 * rs15);
+        J[65] = (-T(2)*F.dt*K[K_d62]*xt52) * (cs52 * rs15);
     }
     {  // row 18
     const T rs18 = nt_rscale<T>(nt_exp_hi(x[18]), fh);
-        const T nj18_c0 = F.dt*nt_cvt<T>(x[18]);
-        const T nj18_c1 = F.dt*nt_cvt<T>(x[50]);
+        const T nj18_c0 = F.dt*xt18;
+        const T nj18_c1 = F.dt*xt50;
         const T nj18_c2 = F.parthbr*nj18_c0;
-        J[183] = (het[8]*nj18_c0) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs18);
-        J[184] = (F.dt*(F.parthbr*(K[K_e11]*nt_cvt<T>(x[43]) + K[K_e9]*nt_cvt<T>(x[42]) + tj[J_hbr]) + F.rain_hbr + het[7]*nt_cvt<T>(x[25]) + het[8]*nt_cvt<T>(x[14])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs18);
-        J[181] = (het[7]*nj18_c0) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs18);
-        J[185] = (-K[K_c19]*nj18_c1) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs18);
-        J[182] = (K[K_e9]*nj18_c2) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs18);
-        J[187] = (K[K_e11]*nj18_c2) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs18);
-        J[188] = (-K[K_e7]*nj18_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs18);
-        J[186] = (-F.dt*(K[K_c19]*nt_cvt<T>(x[27]) + K[K_e7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs18);
+        J[183] = (het[8]*nj18_c0) * (cs14 * rs18);
+        J[184] = (F.dt*(F.parthbr*(K[K_e11]*xt43 + K[K_e9]*xt42 + tj[J_hbr]) + F.rain_hbr + het[7]*xt25 + het[8]*xt14) + T(1)) * (cs18 * rs18);
+        J[181] = (het[7]*nj18_c0) * (cs25 * rs18);
+        J[185] = (-K[K_c19]*nj18_c1) * (cs27 * rs18);
+        J[182] = (K[K_e9]*nj18_c2) * (cs42 * rs18);
+        J[187] = (K[K_e11]*nj18_c2) * (cs43 * rs18);
+        J[188] = (-K[K_e7]*nj18_c1) * (cs47 * rs18);
+        J[186] = (-F.dt*(K[K_c19]*xt27 + K[K_e7]*xt47)) * (cs50 * rs18);
     }
     {  // row 19
     const T rs19 = nt_rscale<T>(nt_exp_hi(x[19]), fh);
-        const T nj19_c0 = F.dt*nt_cvt<T>(x[19]);
+        const T nj19_c0 = F.dt*xt19;
         const T nj19_c1 = F.dt*K[K_e13];
-        J[56] = (het[5]*nj19_c0) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs19);
-        J[55] = (F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + het[5]*nt_cvt<T>(x[2]) + tj[J_brono2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs19);
-        J[58] = (K[K_e8]*nj19_c0) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs19);
-        J[57] = (-nj19_c1*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs19);
-        J[59] = (-nj19_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs19);
+        J[56] = (het[5]*nj19_c0) * (cs2 * rs19);
+        J[55] = (F.dt*(K[K_e8]*xt45 + het[5]*xt2 + tj[J_brono2]) + T(1)) * (cs19 * rs19);
+        J[58] = (K[K_e8]*nj19_c0) * (cs45 * rs19);
+        J[57] = (-nj19_c1*xt53) * (cs48 * rs19);
+        J[59] = (-nj19_c1*xt48) * (cs53 * rs19);
     }
     {  // row 21
     const T rs21 = nt_rscale<T>(nt_exp_hi(x[21]), fh);
         const T nj21_c0 = F.dt*K[K_b23];
-        J[152] = (F.dt*(F.hnm*K[K_b24] + K[K_b28]*nt_cvt<T>(x[43]) + tj[J_hno4]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[21]), fh) * rs21);
-        J[154] = (F.dt*K[K_b28]*nt_cvt<T>(x[21])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs21);
-        J[155] = (-nj21_c0*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs21);
-        J[153] = (-nj21_c0*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs21);
+        J[152] = (F.dt*(F.hnm*K[K_b24] + K[K_b28]*xt43 + tj[J_hno4]) + T(1)) * (cs21 * rs21);
+        J[154] = (F.dt*K[K_b28]*xt21) * (cs43 * rs21);
+        J[155] = (-nj21_c0*xt48) * (cs47 * rs21);
+        J[153] = (-nj21_c0*xt47) * (cs48 * rs21);
     }
     {  // row 22
     const T rs22 = nt_rscale<T>(nt_exp_hi(x[22]), fh);
-        const T nj22_c0 = F.dt*nt_cvt<T>(x[44]);
-        const T nj22_c1 = T(3)*nt_cvt<T>(x[42]);
+        const T nj22_c0 = F.dt*xt44;
+        const T nj22_c1 = T(3)*xt42;
         const T nj22_c2 = T(2)*K[K_d91];
         const T nj22_c3 = T(4)*K[K_d93];
         const T nj22_c4 = T(3)*K[K_d94];
-        const T nj22_c5 = F.dt*nt_cvt<T>(x[52]);
+        const T nj22_c5 = F.dt*xt52;
         const T nj22_c6 = T(2)*K[K_d60];
         const T nj22_c7 = T(2)*K[K_d62];
-        J[141] = (K[K_d5]*nj22_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs22);
-        J[140] = (-F.dt*tj[J_oclo]) * (nt_scale<T>(nt_exp_hi(x[9]), fh) * rs22);
-        J[144] = (-F.dt*F.parthcl*(K[K_d11]*nt_cvt<T>(x[43]) + tj[J_hcl])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs22);
-        J[135] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + tj[J_clono2_cl] + tj[J_clono2_clo])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs22);
-        J[142] = (-F.dt*(K[K_d34]*nt_cvt<T>(x[43]) + K[K_d35]*nt_cvt<T>(x[45]) + tj[J_hocl]) + K[K_d37]*nj22_c0) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs22);
-        J[133] = (-T(2)*F.dt*tj[J_cl2]) * (nt_scale<T>(nt_exp_hi(x[15]), fh) * rs22);
-        J[128] = (-F.dt*tj[J_clno2]) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs22);
-        J[138] = (-F.dt*(T(2)*F.hnm*K[K_d61] + T(2)*tj[J_cl2o2])) * (nt_scale<T>(nt_exp_hi(x[24]), fh) * rs22);
-        J[132] = (-F.dt*tj[J_brcl]) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs22);
-        J[143] = (K[K_c10]*nj22_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs22);
-        J[137] = (-F.dt*(K[K_d90]*nj22_c1 + T(3)*tj[J_cfc11])) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs22);
-        J[131] = (-F.dt*(nj22_c2*nt_cvt<T>(x[42]) + T(2)*tj[J_cfc12])) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs22);
-        J[127] = (-F.dt*(K[K_d92]*nj22_c1 + T(3)*tj[J_cfc113])) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs22);
-        J[129] = (-F.dt*(nj22_c3*nt_cvt<T>(x[42]) + T(4)*tj[J_ccl4])) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs22);
-        J[136] = (-F.dt*(nj22_c4*nt_cvt<T>(x[43]) + T(3)*tj[J_ch3ccl3])) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs22);
-        J[134] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl])) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs22);
-        J[130] = (-F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22])) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs22);
-        J[139] = (-F.dt*(T(3)*K[K_d90]*nt_cvt<T>(x[30]) + T(3)*K[K_d92]*nt_cvt<T>(x[32]) + K[K_d96]*nt_cvt<T>(x[36]) + nj22_c2*nt_cvt<T>(x[31]) + nj22_c3*nt_cvt<T>(x[33]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs22);
-        J[149] = (-F.dt*(F.parthcl*K[K_d11]*nt_cvt<T>(x[12]) + K[K_d34]*nt_cvt<T>(x[14]) + K[K_d95]*nt_cvt<T>(x[35]) + K[K_d97]*nt_cvt<T>(x[36]) + nj22_c4*nt_cvt<T>(x[34])) + K[K_d9]*nj22_c5) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs22);
-        J[147] = (F.dt*(F.h2*K[K_d6] + K[K_c10]*nt_cvt<T>(x[27]) + K[K_d36]*nt_cvt<T>(x[48]) + K[K_d37]*nt_cvt<T>(x[14]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs22);
-        J[146] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[13]) + K[K_d35]*nt_cvt<T>(x[14]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs22);
-        J[150] = (F.dt*(K[K_d33]*nt_cvt<T>(x[52]) + K[K_d7]*nt_cvt<T>(x[44]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs22);
-        J[145] = (F.dt*(K[K_d31]*nt_cvt<T>(x[52]) + K[K_d36]*nt_cvt<T>(x[44]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs22);
-        J[151] = (F.dt*(K[K_d31]*nt_cvt<T>(x[48]) + K[K_d33]*nt_cvt<T>(x[47]) + K[K_d9]*nt_cvt<T>(x[43]) + K[K_e5a]*nt_cvt<T>(x[53]) + K[K_e5c]*nt_cvt<T>(x[53]) + nj22_c6*nt_cvt<T>(x[52]) + nj22_c7*nt_cvt<T>(x[52]) + nt_cvt<T>(x[52])*(nj22_c6 + nj22_c7))) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs22);
-        J[148] = (nj22_c5*(K[K_e5a] + K[K_e5c])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs22);
+        J[141] = (K[K_d5]*nj22_c0) * (cs1 * rs22);
+        J[140] = (-F.dt*tj[J_oclo]) * (cs9 * rs22);
+        J[144] = (-F.dt*F.parthcl*(K[K_d11]*xt43 + tj[J_hcl])) * (cs12 * rs22);
+        J[135] = (-F.dt*(K[K_d32]*xt45 + tj[J_clono2_cl] + tj[J_clono2_clo])) * (cs13 * rs22);
+        J[142] = (-F.dt*(K[K_d34]*xt43 + K[K_d35]*xt45 + tj[J_hocl]) + K[K_d37]*nj22_c0) * (cs14 * rs22);
+        J[133] = (-T(2)*F.dt*tj[J_cl2]) * (cs15 * rs22);
+        J[128] = (-F.dt*tj[J_clno2]) * (cs17 * rs22);
+        J[138] = (-F.dt*(T(2)*F.hnm*K[K_d61] + T(2)*tj[J_cl2o2])) * (cs24 * rs22);
+        J[132] = (-F.dt*tj[J_brcl]) * (cs26 * rs22);
+        J[143] = (K[K_c10]*nj22_c0) * (cs27 * rs22);
+        J[137] = (-F.dt*(K[K_d90]*nj22_c1 + T(3)*tj[J_cfc11])) * (cs30 * rs22);
+        J[131] = (-F.dt*(nj22_c2*xt42 + T(2)*tj[J_cfc12])) * (cs31 * rs22);
+        J[127] = (-F.dt*(K[K_d92]*nj22_c1 + T(3)*tj[J_cfc113])) * (cs32 * rs22);
+        J[129] = (-F.dt*(nj22_c3*xt42 + T(4)*tj[J_ccl4])) * (cs33 * rs22);
+        J[136] = (-F.dt*(nj22_c4*xt43 + T(3)*tj[J_ch3ccl3])) * (cs34 * rs22);
+        J[134] = (-F.dt*(K[K_d95]*xt43 + tj[J_ch3cl])) * (cs35 * rs22);
+        J[130] = (-F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22])) * (cs36 * rs22);
+        J[139] = (-F.dt*(T(3)*K[K_d90]*xt30 + T(3)*K[K_d92]*xt32 + K[K_d96]*xt36 + nj22_c2*xt31 + nj22_c3*xt33)) * (cs42 * rs22);
+        J[149] = (-F.dt*(F.parthcl*K[K_d11]*xt12 + K[K_d34]*xt14 + K[K_d95]*xt35 + K[K_d97]*xt36 + nj22_c4*xt34) + K[K_d9]*nj22_c5) * (cs43 * rs22);
+        J[147] = (F.dt*(F.h2*K[K_d6] + K[K_c10]*xt27 + K[K_d36]*xt48 + K[K_d37]*xt14 + K[K_d5]*xt1 + K[K_d7]*xt47)) * (cs44 * rs22);
+        J[146] = (-F.dt*(K[K_d32]*xt13 + K[K_d35]*xt14)) * (cs45 * rs22);
+        J[150] = (F.dt*(K[K_d33]*xt52 + K[K_d7]*xt44)) * (cs47 * rs22);
+        J[145] = (F.dt*(K[K_d31]*xt52 + K[K_d36]*xt44)) * (cs48 * rs22);
+        J[151] = (F.dt*(K[K_d31]*xt48 + K[K_d33]*xt47 + K[K_d9]*xt43 + K[K_e5a]*xt53 + K[K_e5c]*xt53 + nj22_c6*xt52 + nj22_c7*xt52 + xt52*(nj22_c6 + nj22_c7))) * (cs52 * rs22);
+        J[148] = (nj22_c5*(K[K_e5a] + K[K_e5c])) * (cs53 * rs22);
     }
     {  // row 23
     const T rs23 = nt_rscale<T>(nt_exp_hi(x[23]), fh);
         const T nj23_c0 = T(2)*het[7];
-        const T nj23_c1 = F.dt*F.parthbr*nt_cvt<T>(x[18]);
-        const T nj23_c2 = F.dt*nt_cvt<T>(x[53]);
-        J[196] = (-F.dt*(F.parthbr*(K[K_e11]*nt_cvt<T>(x[43]) + K[K_e9]*nt_cvt<T>(x[42]) + tj[J_hbr]) + nj23_c0*nt_cvt<T>(x[25]))) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs23);
-        J[193] = (-F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + tj[J_brono2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs23);
-        J[194] = (-F.dt*(K[K_e16]*nt_cvt<T>(x[45]) + nj23_c0*nt_cvt<T>(x[18]) + tj[J_hobr])) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs23);
-        J[192] = (-F.dt*tj[J_brcl]) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs23);
-        J[197] = (F.dt*K[K_c19]*nt_cvt<T>(x[50])) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs23);
-        J[195] = (-K[K_e9]*nj23_c1) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs23);
-        J[202] = (-K[K_e11]*nj23_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs23);
-        J[199] = (-F.dt*(K[K_e16]*nt_cvt<T>(x[25]) + K[K_e8]*nt_cvt<T>(x[19]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs23);
-        J[203] = (F.dt*(K[K_e15]*nt_cvt<T>(x[53]) + K[K_e7]*nt_cvt<T>(x[50]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs23);
-        J[198] = (K[K_e13]*nj23_c2) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs23);
-        J[201] = (F.dt*(K[K_c19]*nt_cvt<T>(x[27]) + K[K_e7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs23);
-        J[204] = (K[K_e5c]*nj23_c2) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs23);
-        J[200] = (F.dt*(K[K_e13]*nt_cvt<T>(x[48]) + K[K_e15]*nt_cvt<T>(x[47]) + K[K_e5c]*nt_cvt<T>(x[52]))) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs23);
+        const T nj23_c1 = F.dt*F.parthbr*xt18;
+        const T nj23_c2 = F.dt*xt53;
+        J[196] = (-F.dt*(F.parthbr*(K[K_e11]*xt43 + K[K_e9]*xt42 + tj[J_hbr]) + nj23_c0*xt25)) * (cs18 * rs23);
+        J[193] = (-F.dt*(K[K_e8]*xt45 + tj[J_brono2])) * (cs19 * rs23);
+        J[194] = (-F.dt*(K[K_e16]*xt45 + nj23_c0*xt18 + tj[J_hobr])) * (cs25 * rs23);
+        J[192] = (-F.dt*tj[J_brcl]) * (cs26 * rs23);
+        J[197] = (F.dt*K[K_c19]*xt50) * (cs27 * rs23);
+        J[195] = (-K[K_e9]*nj23_c1) * (cs42 * rs23);
+        J[202] = (-K[K_e11]*nj23_c1) * (cs43 * rs23);
+        J[199] = (-F.dt*(K[K_e16]*xt25 + K[K_e8]*xt19)) * (cs45 * rs23);
+        J[203] = (F.dt*(K[K_e15]*xt53 + K[K_e7]*xt50)) * (cs47 * rs23);
+        J[198] = (K[K_e13]*nj23_c2) * (cs48 * rs23);
+        J[201] = (F.dt*(K[K_c19]*xt27 + K[K_e7]*xt47)) * (cs50 * rs23);
+        J[204] = (K[K_e5c]*nj23_c2) * (cs52 * rs23);
+        J[200] = (F.dt*(K[K_e13]*xt48 + K[K_e15]*xt47 + K[K_e5c]*xt52)) * (cs53 * rs23);
     }
     {  // row 24
     const T rs24 = nt_rscale<T>(nt_exp_hi(x[24]), fh);
-        J[97] = (F.dt*(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[24]), fh) * rs24);
-        J[98] = (-T(2)*F.dt*K[K_d60]*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs24);
+        J[97] = (F.dt*(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(1)) * (cs24 * rs24);
+        J[98] = (-T(2)*F.dt*K[K_d60]*xt52) * (cs52 * rs24);
     }
     {  // row 25
     const T rs25 = nt_rscale<T>(nt_exp_hi(x[25]), fh);
         const T nj25_c0 = F.dt*het[5];
-        const T nj25_c1 = F.dt*nt_cvt<T>(x[25]);
+        const T nj25_c1 = F.dt*xt25;
         const T nj25_c2 = F.dt*K[K_e15];
-        J[83] = (-nj25_c0*nt_cvt<T>(x[19])) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs25);
-        J[82] = (het[6]*nj25_c1) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs25);
-        J[81] = (het[7]*nj25_c1) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs25);
-        J[79] = (-nj25_c0*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs25);
-        J[80] = (F.dt*(K[K_e16]*nt_cvt<T>(x[45]) + het[6]*nt_cvt<T>(x[12]) + het[7]*nt_cvt<T>(x[18]) + tj[J_hobr]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs25);
-        J[84] = (K[K_e16]*nj25_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs25);
-        J[86] = (-nj25_c2*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs25);
-        J[85] = (-nj25_c2*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs25);
+        J[83] = (-nj25_c0*xt19) * (cs2 * rs25);
+        J[82] = (het[6]*nj25_c1) * (cs12 * rs25);
+        J[81] = (het[7]*nj25_c1) * (cs18 * rs25);
+        J[79] = (-nj25_c0*xt2) * (cs19 * rs25);
+        J[80] = (F.dt*(K[K_e16]*xt45 + het[6]*xt12 + het[7]*xt18 + tj[J_hobr]) + T(1)) * (cs25 * rs25);
+        J[84] = (K[K_e16]*nj25_c1) * (cs45 * rs25);
+        J[86] = (-nj25_c2*xt53) * (cs47 * rs25);
+        J[85] = (-nj25_c2*xt47) * (cs53 * rs25);
     }
     {  // row 29
     const T rs29 = nt_rscale<T>(nt_exp_hi(x[29]), fh);
         const T nj29_c0 = F.dt*K[K_c7];
-        J[35] = (-nj29_c0*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs29);
-        J[34] = (F.dt*(K[K_c17a]*nt_cvt<T>(x[43]) + K[K_c17b]*nt_cvt<T>(x[43]) + tj[J_ch3o2h]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs29);
-        J[36] = (F.dt*nt_cvt<T>(x[29])*(K[K_c17a] + K[K_c17b])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs29);
-        J[37] = (-nj29_c0*nt_cvt<T>(x[28])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs29);
+        J[35] = (-nj29_c0*xt47) * (cs28 * rs29);
+        J[34] = (F.dt*(K[K_c17a]*xt43 + K[K_c17b]*xt43 + tj[J_ch3o2h]) + T(1)) * (cs29 * rs29);
+        J[36] = (F.dt*xt29*(K[K_c17a] + K[K_c17b])) * (cs43 * rs29);
+        J[37] = (-nj29_c0*xt28) * (cs47 * rs29);
     }
     {  // row 30
     const T rs30 = nt_rscale<T>(nt_exp_hi(x[30]), fh);
-        J[95] = (F.dt*(K[K_d90]*nt_cvt<T>(x[42]) + tj[J_cfc11]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs30);
-        J[96] = (F.dt*K[K_d90]*nt_cvt<T>(x[30])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs30);
+        J[95] = (F.dt*(K[K_d90]*xt42 + tj[J_cfc11]) + T(1)) * (cs30 * rs30);
+        J[96] = (F.dt*K[K_d90]*xt30) * (cs42 * rs30);
     }
     {  // row 32
     const T rs32 = nt_rscale<T>(nt_exp_hi(x[32]), fh);
-        J[18] = (F.dt*(K[K_d92]*nt_cvt<T>(x[42]) + tj[J_cfc113]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs32);
-        J[19] = (F.dt*K[K_d92]*nt_cvt<T>(x[32])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs32);
+        J[18] = (F.dt*(K[K_d92]*xt42 + tj[J_cfc113]) + T(1)) * (cs32 * rs32);
+        J[19] = (F.dt*K[K_d92]*xt32) * (cs42 * rs32);
     }
     {  // row 34
     const T rs34 = nt_rscale<T>(nt_exp_hi(x[34]), fh);
-        J[93] = (F.dt*(K[K_d94]*nt_cvt<T>(x[43]) + tj[J_ch3ccl3]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs34);
-        J[94] = (F.dt*K[K_d94]*nt_cvt<T>(x[34])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs34);
+        J[93] = (F.dt*(K[K_d94]*xt43 + tj[J_ch3ccl3]) + T(1)) * (cs34 * rs34);
+        J[94] = (F.dt*K[K_d94]*xt34) * (cs43 * rs34);
     }
     {  // row 36
     const T rs36 = nt_rscale<T>(nt_exp_hi(x[36]), fh);
-        const T nj36_c0 = F.dt*nt_cvt<T>(x[36]);
-        J[38] = (F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs36);
-        J[39] = (K[K_d96]*nj36_c0) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs36);
-        J[40] = (K[K_d97]*nj36_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs36);
+        const T nj36_c0 = F.dt*xt36;
+        J[38] = (F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22]) + T(1)) * (cs36 * rs36);
+        J[39] = (K[K_d96]*nj36_c0) * (cs42 * rs36);
+        J[40] = (K[K_d97]*nj36_c0) * (cs43 * rs36);
     }
     {  // row 38
     const T rs38 = nt_rscale<T>(nt_exp_hi(x[38]), fh);
-        J[30] = (F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs38);
-        J[31] = (F.dt*K[K_e52]*nt_cvt<T>(x[38])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs38);
+        J[30] = (F.dt*(K[K_e52]*xt42 + tj[J_h1211]) + T(1)) * (cs38 * rs38);
+        J[31] = (F.dt*K[K_e52]*xt38) * (cs42 * rs38);
     }
     {  // row 41
     const T rs41 = nt_rscale<T>(nt_exp_hi(x[41]), fh);
-        J[125] = (F.dt*(K[K_e54]*nt_cvt<T>(x[43]) + tj[J_ch2br2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[41]), fh) * rs41);
-        J[126] = (F.dt*K[K_e54]*nt_cvt<T>(x[41])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs41);
+        J[125] = (F.dt*(K[K_e54]*xt43 + tj[J_ch2br2]) + T(1)) * (cs41 * rs41);
+        J[126] = (F.dt*K[K_e54]*xt41) * (cs43 * rs41);
     }
     {  // row 42
     const T rs42 = nt_rscale<T>(nt_exp_hi(x[42]), fh);
@@ -4505,7 +5417,7 @@ __device__ __forceinline__ void nt_jacobian_night_w2_0(const FF& F, PK K, PK tj,
     }
     {  // row 46
     const T rs46 = nt_rscale<T>(nt_exp_hi(x[46]), fh);
-        J[355] = (T(-1)) * (nt_scale<T>(nt_exp_hi(x[7]), fh) * rs46);
+        J[355] = (T(-1)) * (cs7 * rs46);
         J[358] = T(0);
         J[357] = T(0);
         J[359] = T(0);
@@ -4521,7 +5433,7 @@ __device__ __forceinline__ void nt_jacobian_night_w2_0(const FF& F, PK K, PK tj,
         J[347] = T(0);
         J[346] = T(0);
         J[352] = T(0);
-        J[351] = (T(1)) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs47);
+        J[351] = (T(1)) * (cs47 * rs47);
         J[353] = T(0);
         J[349] = T(0);
         J[354] = T(0);
@@ -4549,25 +5461,25 @@ __device__ __forceinline__ void nt_jacobian_night_w2_0(const FF& F, PK K, PK tj,
         J[208] = T(0);
     }
     const T N_cno_c0 = K[K_b9]/K[K_b12];
-    const T N_cno = N_cno_c0*nt_cvt<T>(x[46]);
+    const T N_cno = N_cno_c0*xt46;
     const T d_N_cno_46 = N_cno_c0;
-    const T N_dno = -N_cno + nt_cvt<T>(x[20]);
+    const T N_dno = -N_cno + xt20;
     const T d_N_dno_20 = T(1);
     const T d_N_dno_46 = -d_N_cno_46;
     const T N_no2_c0 = N_cno + T(1e-30);
     const T N_no2_c1 = T(1e-30)/N_no2_c0;
     const bool sel_N_no2 = (N_dno) > (T(1e-30));
-    const T N_no2 = sel_N_no2 ? T(N_dno) : T(N_no2_c1*nt_cvt<T>(x[20]));
+    const T N_no2 = sel_N_no2 ? T(N_dno) : T(N_no2_c1*xt20);
     const T d_N_no2_20 = sel_N_no2 ? T(d_N_dno_20) : T(N_no2_c1);
-    const T d_N_no2_46 = sel_N_no2 ? T(d_N_dno_46) : T(-T(1e-30)*d_N_cno_46*nt_cvt<T>(x[20])/(N_no2_c0*N_no2_c0));
+    const T d_N_no2_46 = sel_N_no2 ? T(d_N_dno_46) : T(-T(1e-30)*d_N_cno_46*xt20/(N_no2_c0*N_no2_c0));
     {  // row 48
     const T rs48 = nt_rscale<T>(nt_exp_hi(x[48]), fh);
-        J[270] = (-d_N_no2_20) * (nt_scale<T>(nt_exp_hi(x[20]), fh) * rs48);
+        J[270] = (-d_N_no2_20) * (cs20 * rs48);
         J[269] = T(0);
         J[272] = T(0);
-        J[275] = (-d_N_no2_46) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs48);
+        J[275] = (-d_N_no2_46) * (cs46 * rs48);
         J[274] = T(0);
-        J[271] = (T(1)) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs48);
+        J[271] = (T(1)) * (cs48 * rs48);
         J[276] = T(0);
         J[277] = T(0);
         J[273] = T(0);
@@ -4629,51 +5541,153 @@ __device__ __forceinline__ void nt_residual_night_w2_1(const FF& F, PK K, PK tj,
 template <typename T, typename FF, typename PK, typename PJ>
 __device__ __forceinline__ void nt_jacobian_night_w2_1(const FF& F, PK K, PK tj, PK het, const double* __restrict__ x, double floor_, PJ J) {
     const int fh = nt_exp_hi(floor_);
+    const T xt0 = nt_cvt<T>(x[0]);
+    const T xt1 = nt_cvt<T>(x[1]);
+    const T xt2 = nt_cvt<T>(x[2]);
+    const T xt3 = nt_cvt<T>(x[3]);
+    const T xt4 = nt_cvt<T>(x[4]);
+    const T xt5 = nt_cvt<T>(x[5]);
+    const T xt6 = nt_cvt<T>(x[6]);
+    const T xt7 = nt_cvt<T>(x[7]);
+    const T xt8 = nt_cvt<T>(x[8]);
+    const T xt9 = nt_cvt<T>(x[9]);
+    const T xt10 = nt_cvt<T>(x[10]);
+    const T xt11 = nt_cvt<T>(x[11]);
+    const T xt12 = nt_cvt<T>(x[12]);
+    const T xt13 = nt_cvt<T>(x[13]);
+    const T xt14 = nt_cvt<T>(x[14]);
+    const T xt15 = nt_cvt<T>(x[15]);
+    const T xt16 = nt_cvt<T>(x[16]);
+    const T xt17 = nt_cvt<T>(x[17]);
+    const T xt18 = nt_cvt<T>(x[18]);
+    const T xt19 = nt_cvt<T>(x[19]);
+    const T xt20 = nt_cvt<T>(x[20]);
+    const T xt21 = nt_cvt<T>(x[21]);
+    const T xt22 = nt_cvt<T>(x[22]);
+    const T xt23 = nt_cvt<T>(x[23]);
+    const T xt24 = nt_cvt<T>(x[24]);
+    const T xt25 = nt_cvt<T>(x[25]);
+    const T xt26 = nt_cvt<T>(x[26]);
+    const T xt27 = nt_cvt<T>(x[27]);
+    const T xt28 = nt_cvt<T>(x[28]);
+    const T xt29 = nt_cvt<T>(x[29]);
+    const T xt30 = nt_cvt<T>(x[30]);
+    const T xt31 = nt_cvt<T>(x[31]);
+    const T xt32 = nt_cvt<T>(x[32]);
+    const T xt33 = nt_cvt<T>(x[33]);
+    const T xt34 = nt_cvt<T>(x[34]);
+    const T xt35 = nt_cvt<T>(x[35]);
+    const T xt36 = nt_cvt<T>(x[36]);
+    const T xt37 = nt_cvt<T>(x[37]);
+    const T xt38 = nt_cvt<T>(x[38]);
+    const T xt39 = nt_cvt<T>(x[39]);
+    const T xt40 = nt_cvt<T>(x[40]);
+    const T xt41 = nt_cvt<T>(x[41]);
+    const T xt42 = nt_cvt<T>(x[42]);
+    const T xt43 = nt_cvt<T>(x[43]);
+    const T xt44 = nt_cvt<T>(x[44]);
+    const T xt45 = nt_cvt<T>(x[45]);
+    const T xt46 = nt_cvt<T>(x[46]);
+    const T xt47 = nt_cvt<T>(x[47]);
+    const T xt48 = nt_cvt<T>(x[48]);
+    const T xt49 = nt_cvt<T>(x[49]);
+    const T xt50 = nt_cvt<T>(x[50]);
+    const T xt51 = nt_cvt<T>(x[51]);
+    const T xt52 = nt_cvt<T>(x[52]);
+    const T xt53 = nt_cvt<T>(x[53]);
+    const T xt54 = nt_cvt<T>(x[54]);
+    const T xt55 = nt_cvt<T>(x[55]);
+    const T xt56 = nt_cvt<T>(x[56]);
+    const T cs0 = nt_scale<T>(nt_exp_hi(x[0]), fh);
+    const T cs1 = nt_scale<T>(nt_exp_hi(x[1]), fh);
+    const T cs2 = nt_scale<T>(nt_exp_hi(x[2]), fh);
+    const T cs4 = nt_scale<T>(nt_exp_hi(x[4]), fh);
+    const T cs5 = nt_scale<T>(nt_exp_hi(x[5]), fh);
+    const T cs8 = nt_scale<T>(nt_exp_hi(x[8]), fh);
+    const T cs9 = nt_scale<T>(nt_exp_hi(x[9]), fh);
+    const T cs12 = nt_scale<T>(nt_exp_hi(x[12]), fh);
+    const T cs13 = nt_scale<T>(nt_exp_hi(x[13]), fh);
+    const T cs14 = nt_scale<T>(nt_exp_hi(x[14]), fh);
+    const T cs16 = nt_scale<T>(nt_exp_hi(x[16]), fh);
+    const T cs17 = nt_scale<T>(nt_exp_hi(x[17]), fh);
+    const T cs18 = nt_scale<T>(nt_exp_hi(x[18]), fh);
+    const T cs19 = nt_scale<T>(nt_exp_hi(x[19]), fh);
+    const T cs20 = nt_scale<T>(nt_exp_hi(x[20]), fh);
+    const T cs21 = nt_scale<T>(nt_exp_hi(x[21]), fh);
+    const T cs22 = nt_scale<T>(nt_exp_hi(x[22]), fh);
+    const T cs23 = nt_scale<T>(nt_exp_hi(x[23]), fh);
+    const T cs25 = nt_scale<T>(nt_exp_hi(x[25]), fh);
+    const T cs26 = nt_scale<T>(nt_exp_hi(x[26]), fh);
+    const T cs27 = nt_scale<T>(nt_exp_hi(x[27]), fh);
+    const T cs28 = nt_scale<T>(nt_exp_hi(x[28]), fh);
+    const T cs29 = nt_scale<T>(nt_exp_hi(x[29]), fh);
+    const T cs31 = nt_scale<T>(nt_exp_hi(x[31]), fh);
+    const T cs33 = nt_scale<T>(nt_exp_hi(x[33]), fh);
+    const T cs35 = nt_scale<T>(nt_exp_hi(x[35]), fh);
+    const T cs37 = nt_scale<T>(nt_exp_hi(x[37]), fh);
+    const T cs38 = nt_scale<T>(nt_exp_hi(x[38]), fh);
+    const T cs39 = nt_scale<T>(nt_exp_hi(x[39]), fh);
+    const T cs41 = nt_scale<T>(nt_exp_hi(x[41]), fh);
+    const T cs42 = nt_scale<T>(nt_exp_hi(x[42]), fh);
+    const T cs43 = nt_scale<T>(nt_exp_hi(x[43]), fh);
+    const T cs44 = nt_scale<T>(nt_exp_hi(x[44]), fh);
+    const T cs45 = nt_scale<T>(nt_exp_hi(x[45]), fh);
+    const T cs46 = nt_scale<T>(nt_exp_hi(x[46]), fh);
+    const T cs47 = nt_scale<T>(nt_exp_hi(x[47]), fh);
+    const T cs48 = nt_scale<T>(nt_exp_hi(x[48]), fh);
+    const T cs49 = nt_scale<T>(nt_exp_hi(x[49]), fh);
+    const T cs50 = nt_scale<T>(nt_exp_hi(x[50]), fh);
+    const T cs51 = nt_scale<T>(nt_exp_hi(x[51]), fh);
+    const T cs52 = nt_scale<T>(nt_exp_hi(x[52]), fh);
+    const T cs53 = nt_scale<T>(nt_exp_hi(x[53]), fh);
+    const T cs54 = nt_scale<T>(nt_exp_hi(x[54]), fh);
+    const T cs55 = nt_scale<T>(nt_exp_hi(x[55]), fh);
+    const T cs56 = nt_scale<T>(nt_exp_hi(x[56]), fh);
     {  // row 2
     const T rs2 = nt_rscale<T>(nt_exp_hi(x[2]), fh);
-        const T nj2_c0 = F.dt*nt_cvt<T>(x[43]);
+        const T nj2_c0 = F.dt*xt43;
         const T nj2_c1 = F.dt*F.parth2o;
         const T nj2_c2 = F.parthno3*K[K_b27];
         const T nj2_c3 = F.parthcl*K[K_d11];
-        J[261] = (-K[K_c2]*nj2_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs2);
-        J[266] = (nj2_c1*(K[K_a1et]*nt_cvt<T>(x[42]) + tj[J_h2o]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs2);
-        J[260] = (-nj2_c0*nj2_c2) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs2);
-        J[265] = (-nj2_c0*nj2_c3) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs2);
-        J[262] = (-K[K_a30]*nj2_c0) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs2);
-        J[264] = (-K[K_c8]*nj2_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs2);
-        J[258] = (-F.dt*(K[K_c17a]*nt_cvt<T>(x[43]) + K[K_c17b]*nt_cvt<T>(x[43]))) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs2);
-        J[259] = (K[K_a1et]*nj2_c1*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs2);
-        J[267] = (-F.dt*(F.h2*K[K_a19] + K[K_a17]*nt_cvt<T>(x[47]) + K[K_a30]*nt_cvt<T>(x[16]) + T(2)*K[K_a31]*nt_cvt<T>(x[43]) + K[K_c17a]*nt_cvt<T>(x[29]) + K[K_c17b]*nt_cvt<T>(x[29]) + K[K_c2]*nt_cvt<T>(x[1]) + K[K_c8]*nt_cvt<T>(x[27]) + nj2_c2*nt_cvt<T>(x[4]) + nj2_c3*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs2);
-        J[268] = (-F.dt*(K[K_a17]*nt_cvt<T>(x[43]) + T(1.6e-12)*nt_cvt<T>(x[55]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs2);
-        J[263] = (-T(1.6e-12)*F.dt*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs2);
+        J[261] = (-K[K_c2]*nj2_c0) * (cs1 * rs2);
+        J[266] = (nj2_c1*(K[K_a1et]*xt42 + tj[J_h2o]) + T(1)) * (cs2 * rs2);
+        J[260] = (-nj2_c0*nj2_c2) * (cs4 * rs2);
+        J[265] = (-nj2_c0*nj2_c3) * (cs12 * rs2);
+        J[262] = (-K[K_a30]*nj2_c0) * (cs16 * rs2);
+        J[264] = (-K[K_c8]*nj2_c0) * (cs27 * rs2);
+        J[258] = (-F.dt*(K[K_c17a]*xt43 + K[K_c17b]*xt43)) * (cs29 * rs2);
+        J[259] = (K[K_a1et]*nj2_c1*xt2) * (cs42 * rs2);
+        J[267] = (-F.dt*(F.h2*K[K_a19] + K[K_a17]*xt47 + K[K_a30]*xt16 + T(2)*K[K_a31]*xt43 + K[K_c17a]*xt29 + K[K_c17b]*xt29 + K[K_c2]*xt1 + K[K_c8]*xt27 + nj2_c2*xt4 + nj2_c3*xt12)) * (cs43 * rs2);
+        J[268] = (-F.dt*(K[K_a17]*xt43 + T(1.6e-12)*xt55)) * (cs47 * rs2);
+        J[263] = (-T(1.6e-12)*F.dt*xt47) * (cs55 * rs2);
     }
     {  // row 3
     const T rs3 = nt_rscale<T>(nt_exp_hi(x[3]), fh);
         const T nj3_c0 = T(2)*F.dt;
         const T nj3_c1 = K[K_b39]*nj3_c0;
         const T nj3_c2 = K[K_b6]*nj3_c0;
-        J[20] = (-nj3_c1*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs3);
-        J[23] = (F.dt*F.rain_hno3) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs3);
-        J[22] = (-nj3_c1*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs3);
-        J[24] = (nj3_c2*nt_cvt<T>(x[51])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs3);
-        J[21] = (nj3_c2*nt_cvt<T>(x[49])) * (nt_scale<T>(nt_exp_hi(x[51]), fh) * rs3);
+        J[20] = (-nj3_c1*xt42) * (cs0 * rs3);
+        J[23] = (F.dt*F.rain_hno3) * (cs4 * rs3);
+        J[22] = (-nj3_c1*xt0) * (cs42 * rs3);
+        J[24] = (nj3_c2*xt51) * (cs49 * rs3);
+        J[21] = (nj3_c2*xt49) * (cs51 * rs3);
     }
     {  // row 5
     const T rs5 = nt_rscale<T>(nt_exp_hi(x[5]), fh);
-        const T nj5_c0 = F.dt*nt_cvt<T>(x[5]);
+        const T nj5_c0 = F.dt*xt5;
         const T nj5_c1 = F.dt*K[K_b12];
-        J[74] = (het[2]*nj5_c0) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs5);
-        J[72] = (F.dt*(F.hnm*K[K_b32] + het[2]*nt_cvt<T>(x[2]) + het[3]*nt_cvt<T>(x[12]) + tj[J_n2o5]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs5);
-        J[73] = (het[3]*nj5_c0) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs5);
-        J[75] = (-nj5_c1*nt_cvt<T>(x[54])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs5);
-        J[71] = (-nj5_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[54]), fh) * rs5);
+        J[74] = (het[2]*nj5_c0) * (cs2 * rs5);
+        J[72] = (F.dt*(F.hnm*K[K_b32] + het[2]*xt2 + het[3]*xt12 + tj[J_n2o5]) + T(1)) * (cs5 * rs5);
+        J[73] = (het[3]*nj5_c0) * (cs12 * rs5);
+        J[75] = (-nj5_c1*xt54) * (cs48 * rs5);
+        J[71] = (-nj5_c1*xt48) * (cs54 * rs5);
     }
     {  // row 8
     const T rs8 = nt_rscale<T>(nt_exp_hi(x[8]), fh);
         const T nj8_c0 = F.dt*K[K_a36];
-        J[160] = (nj8_c0*nt_cvt<T>(x[43]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[8]), fh) * rs8);
-        J[161] = (-F.dt*tj[J_ch2o_co]) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs8);
-        J[165] = (nj8_c0*nt_cvt<T>(x[8])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs8);
+        J[160] = (nj8_c0*xt43 + T(1)) * (cs8 * rs8);
+        J[161] = (-F.dt*tj[J_ch2o_co]) * (cs27 * rs8);
+        J[165] = (nj8_c0*xt8) * (cs43 * rs8);
         J[163] = T(0);
         J[162] = T(0);
         J[164] = T(0);
@@ -4681,163 +5695,163 @@ __device__ __forceinline__ void nt_jacobian_night_w2_1(const FF& F, PK K, PK tj,
     {  // row 9
     const T rs9 = nt_rscale<T>(nt_exp_hi(x[9]), fh);
         const T nj9_c0 = F.dt*K[K_e5a];
-        J[100] = (F.dt*tj[J_oclo] + T(1)) * (nt_scale<T>(nt_exp_hi(x[9]), fh) * rs9);
-        J[102] = (-nj9_c0*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs9);
-        J[101] = (-nj9_c0*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs9);
+        J[100] = (F.dt*tj[J_oclo] + T(1)) * (cs9 * rs9);
+        J[102] = (-nj9_c0*xt53) * (cs52 * rs9);
+        J[101] = (-nj9_c0*xt52) * (cs53 * rs9);
     }
     {  // row 12
     const T rs12 = nt_rscale<T>(nt_exp_hi(x[12]), fh);
-        const T nj12_c0 = F.dt*nt_cvt<T>(x[44]);
-        const T nj12_c1 = F.dt*nt_cvt<T>(x[12]);
+        const T nj12_c0 = F.dt*xt44;
+        const T nj12_c1 = F.dt*xt12;
         const T nj12_c2 = F.dt*K[K_d9];
-        J[250] = (-K[K_d5]*nj12_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs12);
-        J[247] = (het[3]*nj12_c1) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs12);
-        J[253] = (F.dt*(F.parthcl*(K[K_d11]*nt_cvt<T>(x[43]) + tj[J_hcl]) + F.rain_hcl + het[1]*nt_cvt<T>(x[13]) + het[3]*nt_cvt<T>(x[5]) + het[4]*nt_cvt<T>(x[14]) + het[6]*nt_cvt<T>(x[25])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs12);
-        J[249] = (het[1]*nj12_c1) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs12);
-        J[251] = (het[4]*nj12_c1) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs12);
-        J[248] = (het[6]*nj12_c1) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs12);
-        J[252] = (-K[K_c10]*nj12_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs12);
-        J[255] = (F.parthcl*K[K_d11]*nj12_c1 - nj12_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs12);
-        J[254] = (-F.dt*(F.h2*K[K_d6] + K[K_c10]*nt_cvt<T>(x[27]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs12);
-        J[256] = (-K[K_d7]*nj12_c0) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs12);
-        J[257] = (-nj12_c2*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs12);
+        J[250] = (-K[K_d5]*nj12_c0) * (cs1 * rs12);
+        J[247] = (het[3]*nj12_c1) * (cs5 * rs12);
+        J[253] = (F.dt*(F.parthcl*(K[K_d11]*xt43 + tj[J_hcl]) + F.rain_hcl + het[1]*xt13 + het[3]*xt5 + het[4]*xt14 + het[6]*xt25) + T(1)) * (cs12 * rs12);
+        J[249] = (het[1]*nj12_c1) * (cs13 * rs12);
+        J[251] = (het[4]*nj12_c1) * (cs14 * rs12);
+        J[248] = (het[6]*nj12_c1) * (cs25 * rs12);
+        J[252] = (-K[K_c10]*nj12_c0) * (cs27 * rs12);
+        J[255] = (F.parthcl*K[K_d11]*nj12_c1 - nj12_c2*xt52) * (cs43 * rs12);
+        J[254] = (-F.dt*(F.h2*K[K_d6] + K[K_c10]*xt27 + K[K_d5]*xt1 + K[K_d7]*xt47)) * (cs44 * rs12);
+        J[256] = (-K[K_d7]*nj12_c0) * (cs47 * rs12);
+        J[257] = (-nj12_c2*xt43) * (cs52 * rs12);
     }
     {  // row 13
     const T rs13 = nt_rscale<T>(nt_exp_hi(x[13]), fh);
-        const T nj13_c0 = F.dt*nt_cvt<T>(x[13]);
+        const T nj13_c0 = F.dt*xt13;
         const T nj13_c1 = F.dt*K[K_d31];
-        J[89] = (het[0]*nj13_c0) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs13);
-        J[88] = (het[1]*nj13_c0) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs13);
-        J[87] = (F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]) + tj[J_clono2_cl] + tj[J_clono2_clo]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs13);
-        J[91] = (K[K_d32]*nj13_c0) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs13);
-        J[90] = (-nj13_c1*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs13);
-        J[92] = (-nj13_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs13);
+        J[89] = (het[0]*nj13_c0) * (cs2 * rs13);
+        J[88] = (het[1]*nj13_c0) * (cs12 * rs13);
+        J[87] = (F.dt*(K[K_d32]*xt45 + het[0]*xt2 + het[1]*xt12 + tj[J_clono2_cl] + tj[J_clono2_clo]) + T(1)) * (cs13 * rs13);
+        J[91] = (K[K_d32]*nj13_c0) * (cs45 * rs13);
+        J[90] = (-nj13_c1*xt52) * (cs48 * rs13);
+        J[92] = (-nj13_c1*xt48) * (cs52 * rs13);
     }
     {  // row 16
     const T rs16 = nt_rscale<T>(nt_exp_hi(x[16]), fh);
-        J[189] = (F.dt*(F.rain_h2o2 + K[K_a30]*nt_cvt<T>(x[43]) + tj[J_h2o2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs16);
-        J[190] = (F.dt*K[K_a30]*nt_cvt<T>(x[16])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs16);
-        J[191] = (-T(2)*F.dt*K[K_a27]*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs16);
+        J[189] = (F.dt*(F.rain_h2o2 + K[K_a30]*xt43 + tj[J_h2o2]) + T(1)) * (cs16 * rs16);
+        J[190] = (F.dt*K[K_a30]*xt16) * (cs43 * rs16);
+        J[191] = (-T(2)*F.dt*K[K_a27]*xt47) * (cs47 * rs16);
     }
     {  // row 17
     const T rs17 = nt_rscale<T>(nt_exp_hi(x[17]), fh);
         const T nj17_c0 = F.dt*het[3];
         const T nj17_c1 = F.dt*K[K_d36];
-        J[26] = (-nj17_c0*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs17);
-        J[27] = (-nj17_c0*nt_cvt<T>(x[5])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs17);
-        J[25] = (F.dt*tj[J_clno2] + T(1)) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs17);
-        J[29] = (-nj17_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs17);
-        J[28] = (-nj17_c1*nt_cvt<T>(x[44])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs17);
+        J[26] = (-nj17_c0*xt12) * (cs5 * rs17);
+        J[27] = (-nj17_c0*xt5) * (cs12 * rs17);
+        J[25] = (F.dt*tj[J_clno2] + T(1)) * (cs17 * rs17);
+        J[29] = (-nj17_c1*xt48) * (cs44 * rs17);
+        J[28] = (-nj17_c1*xt44) * (cs48 * rs17);
     }
     {  // row 20
     const T rs20 = nt_rscale<T>(nt_exp_hi(x[20]), fh);
         const T nj20_c0 = T(2)*F.dt;
         const T nj20_c1 = K[K_b39]*nj20_c0;
         const T nj20_c2 = F.parthno3*K[K_b27];
-        const T nj20_c3 = F.dt*nt_cvt<T>(x[48]);
+        const T nj20_c3 = F.dt*xt48;
         const T nj20_c4 = T(2)*K[K_b12];
         const T nj20_c5 = K[K_b6]*nj20_c0;
-        J[233] = (-nj20_c1*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs20);
-        J[237] = (-F.dt*(F.parthno3*tj[J_hno3] + nj20_c2*nt_cvt<T>(x[43]))) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs20);
-        J[232] = (-F.dt*(T(2)*F.hnm*K[K_b32] + T(2)*tj[J_n2o5])) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs20);
-        J[235] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + tj[J_clono2_cl] + tj[J_clono2_clo])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs20);
-        J[229] = (-F.dt*tj[J_clno2]) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs20);
-        J[230] = (-F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + tj[J_brono2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs20);
-        J[238] = (-F.dt*(F.hnm*K[K_b24] + K[K_b28]*nt_cvt<T>(x[43]) + tj[J_hno4])) * (nt_scale<T>(nt_exp_hi(x[21]), fh) * rs20);
-        J[236] = (-nj20_c1*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs20);
-        J[243] = (-F.dt*(K[K_b28]*nt_cvt<T>(x[21]) + nj20_c2*nt_cvt<T>(x[4])) + K[K_b22]*nj20_c3) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs20);
-        J[241] = (K[K_d36]*nj20_c3) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs20);
-        J[240] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[13]) + K[K_e8]*nt_cvt<T>(x[19]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs20);
-        J[244] = (K[K_b23]*nj20_c3) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs20);
-        J[239] = (F.dt*(K[K_b22]*nt_cvt<T>(x[43]) + K[K_b23]*nt_cvt<T>(x[47]) + K[K_d31]*nt_cvt<T>(x[52]) + K[K_d36]*nt_cvt<T>(x[44]) + K[K_e13]*nt_cvt<T>(x[53]) + nj20_c4*nt_cvt<T>(x[54]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs20);
-        J[245] = (nj20_c5*nt_cvt<T>(x[51])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs20);
-        J[234] = (nj20_c5*nt_cvt<T>(x[49])) * (nt_scale<T>(nt_exp_hi(x[51]), fh) * rs20);
-        J[246] = (K[K_d31]*nj20_c3) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs20);
-        J[242] = (K[K_e13]*nj20_c3) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs20);
-        J[231] = (nj20_c3*nj20_c4) * (nt_scale<T>(nt_exp_hi(x[54]), fh) * rs20);
+        J[233] = (-nj20_c1*xt42) * (cs0 * rs20);
+        J[237] = (-F.dt*(F.parthno3*tj[J_hno3] + nj20_c2*xt43)) * (cs4 * rs20);
+        J[232] = (-F.dt*(T(2)*F.hnm*K[K_b32] + T(2)*tj[J_n2o5])) * (cs5 * rs20);
+        J[235] = (-F.dt*(K[K_d32]*xt45 + tj[J_clono2_cl] + tj[J_clono2_clo])) * (cs13 * rs20);
+        J[229] = (-F.dt*tj[J_clno2]) * (cs17 * rs20);
+        J[230] = (-F.dt*(K[K_e8]*xt45 + tj[J_brono2])) * (cs19 * rs20);
+        J[238] = (-F.dt*(F.hnm*K[K_b24] + K[K_b28]*xt43 + tj[J_hno4])) * (cs21 * rs20);
+        J[236] = (-nj20_c1*xt0) * (cs42 * rs20);
+        J[243] = (-F.dt*(K[K_b28]*xt21 + nj20_c2*xt4) + K[K_b22]*nj20_c3) * (cs43 * rs20);
+        J[241] = (K[K_d36]*nj20_c3) * (cs44 * rs20);
+        J[240] = (-F.dt*(K[K_d32]*xt13 + K[K_e8]*xt19)) * (cs45 * rs20);
+        J[244] = (K[K_b23]*nj20_c3) * (cs47 * rs20);
+        J[239] = (F.dt*(K[K_b22]*xt43 + K[K_b23]*xt47 + K[K_d31]*xt52 + K[K_d36]*xt44 + K[K_e13]*xt53 + nj20_c4*xt54)) * (cs48 * rs20);
+        J[245] = (nj20_c5*xt51) * (cs49 * rs20);
+        J[234] = (nj20_c5*xt49) * (cs51 * rs20);
+        J[246] = (K[K_d31]*nj20_c3) * (cs52 * rs20);
+        J[242] = (K[K_e13]*nj20_c3) * (cs53 * rs20);
+        J[231] = (nj20_c3*nj20_c4) * (cs54 * rs20);
     }
     {  // row 26
     const T rs26 = nt_rscale<T>(nt_exp_hi(x[26]), fh);
         const T nj26_c0 = F.dt*het[6];
         const T nj26_c1 = F.dt*het[8];
         const T nj26_c2 = F.dt*K[K_e5c];
-        J[47] = (-nj26_c0*nt_cvt<T>(x[25])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs26);
-        J[45] = (-nj26_c1*nt_cvt<T>(x[18])) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs26);
-        J[46] = (-nj26_c1*nt_cvt<T>(x[14])) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs26);
-        J[44] = (-nj26_c0*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs26);
-        J[43] = (F.dt*tj[J_brcl] + T(1)) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs26);
-        J[49] = (-nj26_c2*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs26);
-        J[48] = (-nj26_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs26);
+        J[47] = (-nj26_c0*xt25) * (cs12 * rs26);
+        J[45] = (-nj26_c1*xt18) * (cs14 * rs26);
+        J[46] = (-nj26_c1*xt14) * (cs18 * rs26);
+        J[44] = (-nj26_c0*xt12) * (cs25 * rs26);
+        J[43] = (F.dt*tj[J_brcl] + T(1)) * (cs26 * rs26);
+        J[49] = (-nj26_c2*xt53) * (cs52 * rs26);
+        J[48] = (-nj26_c2*xt52) * (cs53 * rs26);
     }
     {  // row 27
     const T rs27 = nt_rscale<T>(nt_exp_hi(x[27]), fh);
         const T nj27_c0 = F.dt*K[K_c1c];
         const T nj27_c1 = F.dt*K[K_c17b];
-        const T nj27_c2 = F.dt*nt_cvt<T>(x[27]);
+        const T nj27_c2 = F.dt*xt27;
         const T nj27_c3 = F.dt*K[K_c3];
-        J[219] = (-nj27_c0*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs27);
-        J[222] = (F.dt*(K[K_c10]*nt_cvt<T>(x[44]) + K[K_c19]*nt_cvt<T>(x[50]) + K[K_c8]*nt_cvt<T>(x[43]) + K[K_c9]*nt_cvt<T>(x[45]) + tj[J_ch2o_co] + tj[J_ch2o_hco]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs27);
+        J[219] = (-nj27_c0*xt42) * (cs1 * rs27);
+        J[222] = (F.dt*(K[K_c10]*xt44 + K[K_c19]*xt50 + K[K_c8]*xt43 + K[K_c9]*xt45 + tj[J_ch2o_co] + tj[J_ch2o_hco]) + T(1)) * (cs27 * rs27);
         J[221] = T(0);
-        J[217] = (-nj27_c1*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs27);
-        J[218] = (-nj27_c0*nt_cvt<T>(x[1])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs27);
-        J[226] = (F.dt*K[K_c8]*nt_cvt<T>(x[27]) - nj27_c1*nt_cvt<T>(x[29])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs27);
-        J[224] = (K[K_c10]*nj27_c2) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs27);
-        J[223] = (F.dt*K[K_c9]*nt_cvt<T>(x[27]) - nj27_c3*nt_cvt<T>(x[56])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs27);
+        J[217] = (-nj27_c1*xt43) * (cs29 * rs27);
+        J[218] = (-nj27_c0*xt1) * (cs42 * rs27);
+        J[226] = (F.dt*K[K_c8]*xt27 - nj27_c1*xt29) * (cs43 * rs27);
+        J[224] = (K[K_c10]*nj27_c2) * (cs44 * rs27);
+        J[223] = (F.dt*K[K_c9]*xt27 - nj27_c3*xt56) * (cs45 * rs27);
         J[227] = T(0);
-        J[225] = (K[K_c19]*nj27_c2) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs27);
+        J[225] = (K[K_c19]*nj27_c2) * (cs50 * rs27);
         J[228] = T(0);
-        J[220] = (-nj27_c3*nt_cvt<T>(x[45])) * (nt_scale<T>(nt_exp_hi(x[56]), fh) * rs27);
+        J[220] = (-nj27_c3*xt45) * (cs56 * rs27);
     }
     {  // row 28
     const T rs28 = nt_rscale<T>(nt_exp_hi(x[28]), fh);
-        const T nj28_c0 = T(2)*K[K_c14]*nt_cvt<T>(x[28]);
+        const T nj28_c0 = T(2)*K[K_c14]*xt28;
         const T nj28_c1 = F.dt*K[K_c17a];
-        const T nj28_c2 = F.dt*nt_cvt<T>(x[28]);
-        J[212] = (F.dt*nj28_c0 + F.dt*(K[K_c18]*nt_cvt<T>(x[52]) + K[K_c5]*nt_cvt<T>(x[49]) + K[K_c7]*nt_cvt<T>(x[47]) + nj28_c0) + T(1)) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs28);
-        J[210] = (-nj28_c1*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs28);
-        J[213] = (-nj28_c1*nt_cvt<T>(x[29])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs28);
-        J[214] = (K[K_c7]*nj28_c2) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs28);
-        J[215] = (K[K_c5]*nj28_c2) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs28);
-        J[216] = (K[K_c18]*nj28_c2) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs28);
-        J[211] = (-F.dt*F.o2*K[K_c4]) * (nt_scale<T>(nt_exp_hi(x[56]), fh) * rs28);
+        const T nj28_c2 = F.dt*xt28;
+        J[212] = (F.dt*nj28_c0 + F.dt*(K[K_c18]*xt52 + K[K_c5]*xt49 + K[K_c7]*xt47 + nj28_c0) + T(1)) * (cs28 * rs28);
+        J[210] = (-nj28_c1*xt43) * (cs29 * rs28);
+        J[213] = (-nj28_c1*xt29) * (cs43 * rs28);
+        J[214] = (K[K_c7]*nj28_c2) * (cs47 * rs28);
+        J[215] = (K[K_c5]*nj28_c2) * (cs49 * rs28);
+        J[216] = (K[K_c18]*nj28_c2) * (cs52 * rs28);
+        J[211] = (-F.dt*F.o2*K[K_c4]) * (cs56 * rs28);
     }
     {  // row 31
     const T rs31 = nt_rscale<T>(nt_exp_hi(x[31]), fh);
-        J[41] = (F.dt*(K[K_d91]*nt_cvt<T>(x[42]) + tj[J_cfc12]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs31);
-        J[42] = (F.dt*K[K_d91]*nt_cvt<T>(x[31])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs31);
+        J[41] = (F.dt*(K[K_d91]*xt42 + tj[J_cfc12]) + T(1)) * (cs31 * rs31);
+        J[42] = (F.dt*K[K_d91]*xt31) * (cs42 * rs31);
     }
     {  // row 33
     const T rs33 = nt_rscale<T>(nt_exp_hi(x[33]), fh);
-        J[32] = (F.dt*(K[K_d93]*nt_cvt<T>(x[42]) + tj[J_ccl4]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs33);
-        J[33] = (F.dt*K[K_d93]*nt_cvt<T>(x[33])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs33);
+        J[32] = (F.dt*(K[K_d93]*xt42 + tj[J_ccl4]) + T(1)) * (cs33 * rs33);
+        J[33] = (F.dt*K[K_d93]*xt33) * (cs42 * rs33);
     }
     {  // row 35
     const T rs35 = nt_rscale<T>(nt_exp_hi(x[35]), fh);
-        J[66] = (F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs35);
-        J[67] = (F.dt*K[K_d95]*nt_cvt<T>(x[35])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs35);
+        J[66] = (F.dt*(K[K_d95]*xt43 + tj[J_ch3cl]) + T(1)) * (cs35 * rs35);
+        J[67] = (F.dt*K[K_d95]*xt35) * (cs43 * rs35);
     }
     {  // row 37
     const T rs37 = nt_rscale<T>(nt_exp_hi(x[37]), fh);
-        const T nj37_c0 = F.dt*nt_cvt<T>(x[37]);
-        J[52] = (F.dt*(K[K_e50]*nt_cvt<T>(x[42]) + K[K_e51]*nt_cvt<T>(x[43]) + tj[J_ch3br]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[37]), fh) * rs37);
-        J[53] = (K[K_e50]*nj37_c0) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs37);
-        J[54] = (K[K_e51]*nj37_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs37);
+        const T nj37_c0 = F.dt*xt37;
+        J[52] = (F.dt*(K[K_e50]*xt42 + K[K_e51]*xt43 + tj[J_ch3br]) + T(1)) * (cs37 * rs37);
+        J[53] = (K[K_e50]*nj37_c0) * (cs42 * rs37);
+        J[54] = (K[K_e51]*nj37_c0) * (cs43 * rs37);
     }
     {  // row 39
     const T rs39 = nt_rscale<T>(nt_exp_hi(x[39]), fh);
-        J[50] = (F.dt*(K[K_e53]*nt_cvt<T>(x[42]) + tj[J_h1301]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[39]), fh) * rs39);
-        J[51] = (F.dt*K[K_e53]*nt_cvt<T>(x[39])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs39);
+        J[50] = (F.dt*(K[K_e53]*xt42 + tj[J_h1301]) + T(1)) * (cs39 * rs39);
+        J[51] = (F.dt*K[K_e53]*xt39) * (cs42 * rs39);
     }
     {  // row 40
     const T rs40 = nt_rscale<T>(nt_exp_hi(x[40]), fh);
         const T nj40_c0 = T(2)*K[K_e54];
-        J[16] = (F.dt*F.rain_hbr) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs40);
-        J[13] = (-F.dt*(K[K_e50]*nt_cvt<T>(x[42]) + K[K_e51]*nt_cvt<T>(x[43]) + tj[J_ch3br])) * (nt_scale<T>(nt_exp_hi(x[37]), fh) * rs40);
-        J[11] = (-F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211])) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs40);
-        J[12] = (-F.dt*(K[K_e53]*nt_cvt<T>(x[42]) + tj[J_h1301])) * (nt_scale<T>(nt_exp_hi(x[39]), fh) * rs40);
-        J[15] = (-F.dt*(nj40_c0*nt_cvt<T>(x[43]) + T(2)*tj[J_ch2br2])) * (nt_scale<T>(nt_exp_hi(x[41]), fh) * rs40);
-        J[14] = (-F.dt*(K[K_e50]*nt_cvt<T>(x[37]) + K[K_e52]*nt_cvt<T>(x[38]) + K[K_e53]*nt_cvt<T>(x[39]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs40);
-        J[17] = (-F.dt*(K[K_e51]*nt_cvt<T>(x[37]) + nj40_c0*nt_cvt<T>(x[41]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs40);
+        J[16] = (F.dt*F.rain_hbr) * (cs18 * rs40);
+        J[13] = (-F.dt*(K[K_e50]*xt42 + K[K_e51]*xt43 + tj[J_ch3br])) * (cs37 * rs40);
+        J[11] = (-F.dt*(K[K_e52]*xt42 + tj[J_h1211])) * (cs38 * rs40);
+        J[12] = (-F.dt*(K[K_e53]*xt42 + tj[J_h1301])) * (cs39 * rs40);
+        J[15] = (-F.dt*(nj40_c0*xt43 + T(2)*tj[J_ch2br2])) * (cs41 * rs40);
+        J[14] = (-F.dt*(K[K_e50]*xt37 + K[K_e52]*xt38 + K[K_e53]*xt39)) * (cs42 * rs40);
+        J[17] = (-F.dt*(K[K_e51]*xt37 + nj40_c0*xt41)) * (cs43 * rs40);
     }
     {  // row 43
     const T rs43 = nt_rscale<T>(nt_exp_hi(x[43]), fh);
@@ -4855,7 +5869,7 @@ __device__ __forceinline__ void nt_jacobian_night_w2_1(const FF& F, PK K, PK tj,
         J[328] = T(0);
         J[316] = T(0);
         J[318] = T(0);
-        J[337] = (T(1)) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs43);
+        J[337] = (T(1)) * (cs43 * rs43);
         J[334] = T(0);
         J[333] = T(0);
         J[339] = T(0);
@@ -4900,26 +5914,26 @@ __device__ __forceinline__ void nt_jacobian_night_w2_1(const FF& F, PK K, PK tj,
         J[178] = T(0);
     }
     const T N_cno_c0 = K[K_b9]/K[K_b12];
-    const T N_cno = N_cno_c0*nt_cvt<T>(x[46]);
+    const T N_cno = N_cno_c0*xt46;
     const T d_N_cno_46 = N_cno_c0;
-    const T N_dno = -N_cno + nt_cvt<T>(x[20]);
+    const T N_dno = -N_cno + xt20;
     const T d_N_dno_20 = T(1);
     const T d_N_dno_46 = -d_N_cno_46;
     const T N_no3_c0 = N_cno + T(1e-30);
     const T N_no3_c1 = (T(1)/(N_no3_c0));
     const T N_no3_c2 = N_cno*N_no3_c1;
     const bool sel_N_no3 = (N_dno) > (T(1e-30));
-    const T N_no3 = sel_N_no3 ? T(N_cno) : T(N_no3_c2*nt_cvt<T>(x[20]));
+    const T N_no3 = sel_N_no3 ? T(N_cno) : T(N_no3_c2*xt20);
     const T d_N_no3_20 = sel_N_no3 ? T(T(0)) : T(N_no3_c2);
-    const T d_N_no3_46 = sel_N_no3 ? T(d_N_cno_46) : T(d_N_cno_46*(-N_cno*nt_cvt<T>(x[20])/(N_no3_c0*N_no3_c0) + N_no3_c1*nt_cvt<T>(x[20])));
+    const T d_N_no3_46 = sel_N_no3 ? T(d_N_cno_46) : T(d_N_cno_46*(-N_cno*xt20/(N_no3_c0*N_no3_c0) + N_no3_c1*xt20));
     {  // row 54
     const T rs54 = nt_rscale<T>(nt_exp_hi(x[54]), fh);
-        J[68] = (-d_N_no3_20) * (nt_scale<T>(nt_exp_hi(x[20]), fh) * rs54);
-        J[70] = (-d_N_no3_46) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs54);
+        J[68] = (-d_N_no3_20) * (cs20 * rs54);
+        J[70] = (-d_N_no3_46) * (cs46 * rs54);
         J[69] = T(0);
     }
-    const bool sel_N_clo = (nt_cvt<T>(x[22])) >= (T(0));
-    const T N_clo = sel_N_clo ? T(nt_cvt<T>(x[22])) : T(T(0));
+    const bool sel_N_clo = (xt22) >= (T(0));
+    const T N_clo = sel_N_clo ? T(xt22) : T(T(0));
     const T d_N_clo_22 = sel_N_clo ? T(T(1)) : T(T(0));
     {  // row 52
     const T rs52 = nt_rscale<T>(nt_exp_hi(x[52]), fh);
@@ -4927,7 +5941,7 @@ __device__ __forceinline__ void nt_jacobian_night_w2_1(const FF& F, PK K, PK tj,
         J[373] = T(0);
         J[372] = T(0);
         J[370] = T(0);
-        J[368] = (-d_N_clo_22) * (nt_scale<T>(nt_exp_hi(x[22]), fh) * rs52);
+        J[368] = (-d_N_clo_22) * (cs22 * rs52);
         J[371] = T(0);
         J[377] = T(0);
         J[375] = T(0);
@@ -4935,15 +5949,15 @@ __device__ __forceinline__ void nt_jacobian_night_w2_1(const FF& F, PK K, PK tj,
         J[378] = T(0);
         J[374] = T(0);
         J[380] = T(0);
-        J[381] = (T(1)) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs52);
+        J[381] = (T(1)) * (cs52 * rs52);
         J[376] = T(0);
     }
-    const bool sel_N_bro = (nt_cvt<T>(x[23])) >= (T(0));
-    const T N_bro = sel_N_bro ? T(nt_cvt<T>(x[23])) : T(T(0));
+    const bool sel_N_bro = (xt23) >= (T(0));
+    const T N_bro = sel_N_bro ? T(xt23) : T(T(0));
     const T d_N_bro_23 = sel_N_bro ? T(T(1)) : T(T(0));
     {  // row 53
     const T rs53 = nt_rscale<T>(nt_exp_hi(x[53]), fh);
-        J[297] = (-d_N_bro_23) * (nt_scale<T>(nt_exp_hi(x[23]), fh) * rs53);
+        J[297] = (-d_N_bro_23) * (cs23 * rs53);
         J[298] = T(0);
         J[302] = T(0);
         J[300] = T(0);
@@ -4952,55 +5966,55 @@ __device__ __forceinline__ void nt_jacobian_night_w2_1(const FF& F, PK K, PK tj,
         J[299] = T(0);
         J[305] = T(0);
         J[306] = T(0);
-        J[301] = (T(1)) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs53);
+        J[301] = (T(1)) * (cs53 * rs53);
     }
-    const T N_t06_c0 = tj[J_hocl]*nt_cvt<T>(x[14]);
-    const T N_t06_c1 = K[K_d33]*nt_cvt<T>(x[52]);
-    const T N_t06_c2 = N_t06_c1*nt_cvt<T>(x[47]);
+    const T N_t06_c0 = tj[J_hocl]*xt14;
+    const T N_t06_c1 = K[K_d33]*xt52;
+    const T N_t06_c2 = N_t06_c1*xt47;
     const bool sel_N_t06 = (N_t06_c0) <= (N_t06_c2);
     const T N_t06 = sel_N_t06 ? T(N_t06_c0) : T(N_t06_c2);
     const T d_N_t06_14 = sel_N_t06 ? T(tj[J_hocl]) : T(T(0));
     const T d_N_t06_47 = sel_N_t06 ? T(T(0)) : T(N_t06_c1);
-    const T d_N_t06_52 = sel_N_t06 ? T(T(0)) : T(K[K_d33]*nt_cvt<T>(x[47]));
-    const T N_t07_c0 = K[K_e5c]*nt_cvt<T>(x[53]);
-    const T N_t07_c1 = N_t07_c0*nt_cvt<T>(x[52]);
-    const T N_t07_c2 = tj[J_brcl]*nt_cvt<T>(x[26]);
+    const T d_N_t06_52 = sel_N_t06 ? T(T(0)) : T(K[K_d33]*xt47);
+    const T N_t07_c0 = K[K_e5c]*xt53;
+    const T N_t07_c1 = N_t07_c0*xt52;
+    const T N_t07_c2 = tj[J_brcl]*xt26;
     const bool sel_N_t07 = (N_t07_c1) <= (N_t07_c2);
     const T N_t07 = sel_N_t07 ? T(N_t07_c1) : T(N_t07_c2);
     const T d_N_t07_26 = sel_N_t07 ? T(T(0)) : T(tj[J_brcl]);
     const T d_N_t07_52 = sel_N_t07 ? T(N_t07_c0) : T(T(0));
-    const T d_N_t07_53 = sel_N_t07 ? T(K[K_e5c]*nt_cvt<T>(x[52])) : T(T(0));
-    const T N_t09_c0 = K[K_e15]*nt_cvt<T>(x[53]);
-    const T N_t09_c1 = N_t09_c0*nt_cvt<T>(x[47]);
-    const T N_t09_c2 = tj[J_hobr]*nt_cvt<T>(x[25]);
+    const T d_N_t07_53 = sel_N_t07 ? T(K[K_e5c]*xt52) : T(T(0));
+    const T N_t09_c0 = K[K_e15]*xt53;
+    const T N_t09_c1 = N_t09_c0*xt47;
+    const T N_t09_c2 = tj[J_hobr]*xt25;
     const bool sel_N_t09 = (N_t09_c1) <= (N_t09_c2);
     const T N_t09 = sel_N_t09 ? T(N_t09_c1) : T(N_t09_c2);
     const T d_N_t09_25 = sel_N_t09 ? T(T(0)) : T(tj[J_hobr]);
     const T d_N_t09_47 = sel_N_t09 ? T(N_t09_c0) : T(T(0));
-    const T d_N_t09_53 = sel_N_t09 ? T(K[K_e15]*nt_cvt<T>(x[47])) : T(T(0));
+    const T d_N_t09_53 = sel_N_t09 ? T(K[K_e15]*xt47) : T(T(0));
     {  // row 7
     const T rs7 = nt_rscale<T>(nt_exp_hi(x[7]), fh);
         const T nj7_c0 = T(2)*F.dt;
         const T nj7_c1 = tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
-        const T nj7_c2 = F.dt*nt_cvt<T>(x[49]);
+        const T nj7_c2 = F.dt*xt49;
         const T nj7_c3 = T(2)*K[K_b3];
         const T nj7_c4 = T(2)*K[K_d3];
         const T nj7_c5 = T(2)*K[K_hk3];
         const T nj7_c6 = T(2)*K[K_b9]*nj7_c1;
-        J[105] = (nj7_c0*nj7_c1*tj[J_clono2_cl]) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs7);
-        J[106] = (F.dt*d_N_t06_14) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs7);
-        J[104] = (F.dt*d_N_t09_25) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs7);
-        J[103] = (d_N_t07_26*nj7_c0) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs7);
-        J[108] = (-K[K_c5]*nj7_c2) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs7);
-        J[112] = (F.dt*(K[K_a5]*nt_cvt<T>(x[45]) + K[K_a6]*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs7);
-        J[110] = (F.dt*(K[K_a5]*nt_cvt<T>(x[43]) + K[K_a7]*nt_cvt<T>(x[47]) + T(4)*K[K_hk1]*nt_cvt<T>(x[45]) + nj7_c3*nt_cvt<T>(x[48]) + nj7_c4*nt_cvt<T>(x[52]) + nj7_c5*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs7);
-        J[114] = (F.dt*(K[K_a2]*nt_cvt<T>(x[55]) + K[K_a6]*nt_cvt<T>(x[43]) + K[K_a6b]*nt_cvt<T>(x[47]) + nj7_c5*nt_cvt<T>(x[45]) + nj7_c6*nt_cvt<T>(x[48]))) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs7);
-        J[113] = (F.dt*d_N_t06_47 + F.dt*d_N_t09_47 + F.dt*(K[K_a6b]*nt_cvt<T>(x[46]) + K[K_a7]*nt_cvt<T>(x[45])) - K[K_a26]*nj7_c2) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs7);
-        J[109] = (F.dt*(nj7_c3*nt_cvt<T>(x[45]) + nj7_c6*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs7);
-        J[115] = (-F.dt*(K[K_a26]*nt_cvt<T>(x[47]) + K[K_c5]*nt_cvt<T>(x[28]))) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs7);
-        J[116] = (F.dt*d_N_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*nt_cvt<T>(x[52])/(F.hnm*K[K_d61] + tj[J_cl2o2]) + nj7_c4*nt_cvt<T>(x[45])) + d_N_t07_52*nj7_c0) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs7);
-        J[111] = (F.dt*d_N_t09_53 + d_N_t07_53*nj7_c0) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs7);
-        J[107] = (F.dt*K[K_a2]*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs7);
+        J[105] = (nj7_c0*nj7_c1*tj[J_clono2_cl]) * (cs13 * rs7);
+        J[106] = (F.dt*d_N_t06_14) * (cs14 * rs7);
+        J[104] = (F.dt*d_N_t09_25) * (cs25 * rs7);
+        J[103] = (d_N_t07_26*nj7_c0) * (cs26 * rs7);
+        J[108] = (-K[K_c5]*nj7_c2) * (cs28 * rs7);
+        J[112] = (F.dt*(K[K_a5]*xt45 + K[K_a6]*xt46)) * (cs43 * rs7);
+        J[110] = (F.dt*(K[K_a5]*xt43 + K[K_a7]*xt47 + T(4)*K[K_hk1]*xt45 + nj7_c3*xt48 + nj7_c4*xt52 + nj7_c5*xt46)) * (cs45 * rs7);
+        J[114] = (F.dt*(K[K_a2]*xt55 + K[K_a6]*xt43 + K[K_a6b]*xt47 + nj7_c5*xt45 + nj7_c6*xt48)) * (cs46 * rs7);
+        J[113] = (F.dt*d_N_t06_47 + F.dt*d_N_t09_47 + F.dt*(K[K_a6b]*xt46 + K[K_a7]*xt45) - K[K_a26]*nj7_c2) * (cs47 * rs7);
+        J[109] = (F.dt*(nj7_c3*xt45 + nj7_c6*xt46)) * (cs48 * rs7);
+        J[115] = (-F.dt*(K[K_a26]*xt47 + K[K_c5]*xt28)) * (cs49 * rs7);
+        J[116] = (F.dt*d_N_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*xt52/(F.hnm*K[K_d61] + tj[J_cl2o2]) + nj7_c4*xt45) + d_N_t07_52*nj7_c0) * (cs52 * rs7);
+        J[111] = (F.dt*d_N_t09_53 + d_N_t07_53*nj7_c0) * (cs53 * rs7);
+        J[107] = (F.dt*K[K_a2]*xt46) * (cs55 * rs7);
     }
 }
 
@@ -5047,120 +6061,221 @@ __device__ __forceinline__ void nt_residual_night_w4_0(const FF& F, PK K, PK tj,
 template <typename T, typename FF, typename PK, typename PJ>
 __device__ __forceinline__ void nt_jacobian_night_w4_0(const FF& F, PK K, PK tj, PK het, const double* __restrict__ x, double floor_, PJ J) {
     const int fh = nt_exp_hi(floor_);
+    const T xt0 = nt_cvt<T>(x[0]);
+    const T xt1 = nt_cvt<T>(x[1]);
+    const T xt2 = nt_cvt<T>(x[2]);
+    const T xt3 = nt_cvt<T>(x[3]);
+    const T xt4 = nt_cvt<T>(x[4]);
+    const T xt5 = nt_cvt<T>(x[5]);
+    const T xt6 = nt_cvt<T>(x[6]);
+    const T xt7 = nt_cvt<T>(x[7]);
+    const T xt8 = nt_cvt<T>(x[8]);
+    const T xt9 = nt_cvt<T>(x[9]);
+    const T xt10 = nt_cvt<T>(x[10]);
+    const T xt11 = nt_cvt<T>(x[11]);
+    const T xt12 = nt_cvt<T>(x[12]);
+    const T xt13 = nt_cvt<T>(x[13]);
+    const T xt14 = nt_cvt<T>(x[14]);
+    const T xt15 = nt_cvt<T>(x[15]);
+    const T xt16 = nt_cvt<T>(x[16]);
+    const T xt17 = nt_cvt<T>(x[17]);
+    const T xt18 = nt_cvt<T>(x[18]);
+    const T xt19 = nt_cvt<T>(x[19]);
+    const T xt20 = nt_cvt<T>(x[20]);
+    const T xt21 = nt_cvt<T>(x[21]);
+    const T xt22 = nt_cvt<T>(x[22]);
+    const T xt23 = nt_cvt<T>(x[23]);
+    const T xt24 = nt_cvt<T>(x[24]);
+    const T xt25 = nt_cvt<T>(x[25]);
+    const T xt26 = nt_cvt<T>(x[26]);
+    const T xt27 = nt_cvt<T>(x[27]);
+    const T xt28 = nt_cvt<T>(x[28]);
+    const T xt29 = nt_cvt<T>(x[29]);
+    const T xt30 = nt_cvt<T>(x[30]);
+    const T xt31 = nt_cvt<T>(x[31]);
+    const T xt32 = nt_cvt<T>(x[32]);
+    const T xt33 = nt_cvt<T>(x[33]);
+    const T xt34 = nt_cvt<T>(x[34]);
+    const T xt35 = nt_cvt<T>(x[35]);
+    const T xt36 = nt_cvt<T>(x[36]);
+    const T xt37 = nt_cvt<T>(x[37]);
+    const T xt38 = nt_cvt<T>(x[38]);
+    const T xt39 = nt_cvt<T>(x[39]);
+    const T xt40 = nt_cvt<T>(x[40]);
+    const T xt41 = nt_cvt<T>(x[41]);
+    const T xt42 = nt_cvt<T>(x[42]);
+    const T xt43 = nt_cvt<T>(x[43]);
+    const T xt44 = nt_cvt<T>(x[44]);
+    const T xt45 = nt_cvt<T>(x[45]);
+    const T xt46 = nt_cvt<T>(x[46]);
+    const T xt47 = nt_cvt<T>(x[47]);
+    const T xt48 = nt_cvt<T>(x[48]);
+    const T xt49 = nt_cvt<T>(x[49]);
+    const T xt50 = nt_cvt<T>(x[50]);
+    const T xt51 = nt_cvt<T>(x[51]);
+    const T xt52 = nt_cvt<T>(x[52]);
+    const T xt53 = nt_cvt<T>(x[53]);
+    const T xt54 = nt_cvt<T>(x[54]);
+    const T xt55 = nt_cvt<T>(x[55]);
+    const T xt56 = nt_cvt<T>(x[56]);
+    const T cs0 = nt_scale<T>(nt_exp_hi(x[0]), fh);
+    const T cs1 = nt_scale<T>(nt_exp_hi(x[1]), fh);
+    const T cs2 = nt_scale<T>(nt_exp_hi(x[2]), fh);
+    const T cs4 = nt_scale<T>(nt_exp_hi(x[4]), fh);
+    const T cs8 = nt_scale<T>(nt_exp_hi(x[8]), fh);
+    const T cs9 = nt_scale<T>(nt_exp_hi(x[9]), fh);
+    const T cs12 = nt_scale<T>(nt_exp_hi(x[12]), fh);
+    const T cs13 = nt_scale<T>(nt_exp_hi(x[13]), fh);
+    const T cs14 = nt_scale<T>(nt_exp_hi(x[14]), fh);
+    const T cs15 = nt_scale<T>(nt_exp_hi(x[15]), fh);
+    const T cs16 = nt_scale<T>(nt_exp_hi(x[16]), fh);
+    const T cs17 = nt_scale<T>(nt_exp_hi(x[17]), fh);
+    const T cs18 = nt_scale<T>(nt_exp_hi(x[18]), fh);
+    const T cs19 = nt_scale<T>(nt_exp_hi(x[19]), fh);
+    const T cs21 = nt_scale<T>(nt_exp_hi(x[21]), fh);
+    const T cs22 = nt_scale<T>(nt_exp_hi(x[22]), fh);
+    const T cs23 = nt_scale<T>(nt_exp_hi(x[23]), fh);
+    const T cs24 = nt_scale<T>(nt_exp_hi(x[24]), fh);
+    const T cs25 = nt_scale<T>(nt_exp_hi(x[25]), fh);
+    const T cs26 = nt_scale<T>(nt_exp_hi(x[26]), fh);
+    const T cs27 = nt_scale<T>(nt_exp_hi(x[27]), fh);
+    const T cs28 = nt_scale<T>(nt_exp_hi(x[28]), fh);
+    const T cs29 = nt_scale<T>(nt_exp_hi(x[29]), fh);
+    const T cs30 = nt_scale<T>(nt_exp_hi(x[30]), fh);
+    const T cs31 = nt_scale<T>(nt_exp_hi(x[31]), fh);
+    const T cs32 = nt_scale<T>(nt_exp_hi(x[32]), fh);
+    const T cs33 = nt_scale<T>(nt_exp_hi(x[33]), fh);
+    const T cs34 = nt_scale<T>(nt_exp_hi(x[34]), fh);
+    const T cs35 = nt_scale<T>(nt_exp_hi(x[35]), fh);
+    const T cs36 = nt_scale<T>(nt_exp_hi(x[36]), fh);
+    const T cs42 = nt_scale<T>(nt_exp_hi(x[42]), fh);
+    const T cs43 = nt_scale<T>(nt_exp_hi(x[43]), fh);
+    const T cs44 = nt_scale<T>(nt_exp_hi(x[44]), fh);
+    const T cs45 = nt_scale<T>(nt_exp_hi(x[45]), fh);
+    const T cs46 = nt_scale<T>(nt_exp_hi(x[46]), fh);
+    const T cs47 = nt_scale<T>(nt_exp_hi(x[47]), fh);
+    const T cs48 = nt_scale<T>(nt_exp_hi(x[48]), fh);
+    const T cs49 = nt_scale<T>(nt_exp_hi(x[49]), fh);
+    const T cs50 = nt_scale<T>(nt_exp_hi(x[50]), fh);
+    const T cs51 = nt_scale<T>(nt_exp_hi(x[51]), fh);
+    const T cs52 = nt_scale<T>(nt_exp_hi(x[52]), fh);
+    const T cs53 = nt_scale<T>(nt_exp_hi(x[53]), fh);
+    const T cs55 = nt_scale<T>(nt_exp_hi(x[55]), fh);
+    const T cs56 = nt_scale<T>(nt_exp_hi(x[56]), fh);
     {  // row 3
     const T rs3 = nt_rscale<T>(nt_exp_hi(x[3]), fh);
         const T nj3_c0 = T(2)*F.dt;
         const T nj3_c1 = K[K_b39]*nj3_c0;
         const T nj3_c2 = K[K_b6]*nj3_c0;
-        J[20] = (-nj3_c1*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs3);
-        J[23] = (F.dt*F.rain_hno3) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs3);
-        J[22] = (-nj3_c1*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs3);
-        J[24] = (nj3_c2*nt_cvt<T>(x[51])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs3);
-        J[21] = (nj3_c2*nt_cvt<T>(x[49])) * (nt_scale<T>(nt_exp_hi(x[51]), fh) * rs3);
+        J[20] = (-nj3_c1*xt42) * (cs0 * rs3);
+        J[23] = (F.dt*F.rain_hno3) * (cs4 * rs3);
+        J[22] = (-nj3_c1*xt0) * (cs42 * rs3);
+        J[24] = (nj3_c2*xt51) * (cs49 * rs3);
+        J[21] = (nj3_c2*xt49) * (cs51 * rs3);
     }
     {  // row 9
     const T rs9 = nt_rscale<T>(nt_exp_hi(x[9]), fh);
         const T nj9_c0 = F.dt*K[K_e5a];
-        J[100] = (F.dt*tj[J_oclo] + T(1)) * (nt_scale<T>(nt_exp_hi(x[9]), fh) * rs9);
-        J[102] = (-nj9_c0*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs9);
-        J[101] = (-nj9_c0*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs9);
+        J[100] = (F.dt*tj[J_oclo] + T(1)) * (cs9 * rs9);
+        J[102] = (-nj9_c0*xt53) * (cs52 * rs9);
+        J[101] = (-nj9_c0*xt52) * (cs53 * rs9);
     }
     {  // row 14
     const T rs14 = nt_rscale<T>(nt_exp_hi(x[14]), fh);
         const T nj14_c0 = F.dt*het[0];
-        const T nj14_c1 = F.dt*nt_cvt<T>(x[14]);
+        const T nj14_c1 = F.dt*xt14;
         const T nj14_c2 = F.dt*K[K_d33];
-        J[170] = (-nj14_c0*nt_cvt<T>(x[13])) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs14);
-        J[169] = (het[4]*nj14_c1) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs14);
-        J[166] = (-nj14_c0*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs14);
-        J[167] = (F.dt*(K[K_d34]*nt_cvt<T>(x[43]) + K[K_d35]*nt_cvt<T>(x[45]) + K[K_d37]*nt_cvt<T>(x[44]) + het[4]*nt_cvt<T>(x[12]) + het[8]*nt_cvt<T>(x[18]) + tj[J_hocl]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs14);
-        J[168] = (het[8]*nj14_c1) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs14);
-        J[173] = (K[K_d34]*nj14_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs14);
-        J[172] = (K[K_d37]*nj14_c1) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs14);
-        J[171] = (K[K_d35]*nj14_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs14);
-        J[174] = (-nj14_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs14);
-        J[175] = (-nj14_c2*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs14);
+        J[170] = (-nj14_c0*xt13) * (cs2 * rs14);
+        J[169] = (het[4]*nj14_c1) * (cs12 * rs14);
+        J[166] = (-nj14_c0*xt2) * (cs13 * rs14);
+        J[167] = (F.dt*(K[K_d34]*xt43 + K[K_d35]*xt45 + K[K_d37]*xt44 + het[4]*xt12 + het[8]*xt18 + tj[J_hocl]) + T(1)) * (cs14 * rs14);
+        J[168] = (het[8]*nj14_c1) * (cs18 * rs14);
+        J[173] = (K[K_d34]*nj14_c1) * (cs43 * rs14);
+        J[172] = (K[K_d37]*nj14_c1) * (cs44 * rs14);
+        J[171] = (K[K_d35]*nj14_c1) * (cs45 * rs14);
+        J[174] = (-nj14_c2*xt52) * (cs47 * rs14);
+        J[175] = (-nj14_c2*xt47) * (cs52 * rs14);
     }
     {  // row 21
     const T rs21 = nt_rscale<T>(nt_exp_hi(x[21]), fh);
         const T nj21_c0 = F.dt*K[K_b23];
-        J[152] = (F.dt*(F.hnm*K[K_b24] + K[K_b28]*nt_cvt<T>(x[43]) + tj[J_hno4]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[21]), fh) * rs21);
-        J[154] = (F.dt*K[K_b28]*nt_cvt<T>(x[21])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs21);
-        J[155] = (-nj21_c0*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs21);
-        J[153] = (-nj21_c0*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs21);
+        J[152] = (F.dt*(F.hnm*K[K_b24] + K[K_b28]*xt43 + tj[J_hno4]) + T(1)) * (cs21 * rs21);
+        J[154] = (F.dt*K[K_b28]*xt21) * (cs43 * rs21);
+        J[155] = (-nj21_c0*xt48) * (cs47 * rs21);
+        J[153] = (-nj21_c0*xt47) * (cs48 * rs21);
     }
     {  // row 22
     const T rs22 = nt_rscale<T>(nt_exp_hi(x[22]), fh);
-        const T nj22_c0 = F.dt*nt_cvt<T>(x[44]);
-        const T nj22_c1 = T(3)*nt_cvt<T>(x[42]);
+        const T nj22_c0 = F.dt*xt44;
+        const T nj22_c1 = T(3)*xt42;
         const T nj22_c2 = T(2)*K[K_d91];
         const T nj22_c3 = T(4)*K[K_d93];
         const T nj22_c4 = T(3)*K[K_d94];
-        const T nj22_c5 = F.dt*nt_cvt<T>(x[52]);
+        const T nj22_c5 = F.dt*xt52;
         const T nj22_c6 = T(2)*K[K_d60];
         const T nj22_c7 = T(2)*K[K_d62];
-        J[141] = (K[K_d5]*nj22_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs22);
-        J[140] = (-F.dt*tj[J_oclo]) * (nt_scale<T>(nt_exp_hi(x[9]), fh) * rs22);
-        J[144] = (-F.dt*F.parthcl*(K[K_d11]*nt_cvt<T>(x[43]) + tj[J_hcl])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs22);
-        J[135] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + tj[J_clono2_cl] + tj[J_clono2_clo])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs22);
-        J[142] = (-F.dt*(K[K_d34]*nt_cvt<T>(x[43]) + K[K_d35]*nt_cvt<T>(x[45]) + tj[J_hocl]) + K[K_d37]*nj22_c0) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs22);
-        J[133] = (-T(2)*F.dt*tj[J_cl2]) * (nt_scale<T>(nt_exp_hi(x[15]), fh) * rs22);
-        J[128] = (-F.dt*tj[J_clno2]) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs22);
-        J[138] = (-F.dt*(T(2)*F.hnm*K[K_d61] + T(2)*tj[J_cl2o2])) * (nt_scale<T>(nt_exp_hi(x[24]), fh) * rs22);
-        J[132] = (-F.dt*tj[J_brcl]) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs22);
-        J[143] = (K[K_c10]*nj22_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs22);
-        J[137] = (-F.dt*(K[K_d90]*nj22_c1 + T(3)*tj[J_cfc11])) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs22);
-        J[131] = (-F.dt*(nj22_c2*nt_cvt<T>(x[42]) + T(2)*tj[J_cfc12])) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs22);
-        J[127] = (-F.dt*(K[K_d92]*nj22_c1 + T(3)*tj[J_cfc113])) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs22);
-        J[129] = (-F.dt*(nj22_c3*nt_cvt<T>(x[42]) + T(4)*tj[J_ccl4])) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs22);
-        J[136] = (-F.dt*(nj22_c4*nt_cvt<T>(x[43]) + T(3)*tj[J_ch3ccl3])) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs22);
-        J[134] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl])) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs22);
-        J[130] = (-F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22])) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs22);
-        J[139] = (-F.dt*(T(3)*K[K_d90]*nt_cvt<T>(x[30]) + T(3)*K[K_d92]*nt_cvt<T>(x[32]) + K[K_d96]*nt_cvt<T>(x[36]) + nj22_c2*nt_cvt<T>(x[31]) + nj22_c3*nt_cvt<T>(x[33]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs22);
-        J[149] = (-F.dt*(F.parthcl*K[K_d11]*nt_cvt<T>(x[12]) + K[K_d34]*nt_cvt<T>(x[14]) + K[K_d95]*nt_cvt<T>(x[35]) + K[K_d97]*nt_cvt<T>(x[36]) + nj22_c4*nt_cvt<T>(x[34])) + K[K_d9]*nj22_c5) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs22);
-        J[147] = (F.dt*(F.h2*K[K_d6] + K[K_c10]*nt_cvt<T>(x[27]) + K[K_d36]*nt_cvt<T>(x[48]) + K[K_d37]*nt_cvt<T>(x[14]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs22);
-        J[146] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[13]) + K[K_d35]*nt_cvt<T>(x[14]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs22);
-        J[150] = (F.dt*(K[K_d33]*nt_cvt<T>(x[52]) + K[K_d7]*nt_cvt<T>(x[44]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs22);
-        J[145] = (F.dt*(K[K_d31]*nt_cvt<T>(x[52]) + K[K_d36]*nt_cvt<T>(x[44]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs22);
-        J[151] = (F.dt*(K[K_d31]*nt_cvt<T>(x[48]) + K[K_d33]*nt_cvt<T>(x[47]) + K[K_d9]*nt_cvt<T>(x[43]) + K[K_e5a]*nt_cvt<T>(x[53]) + K[K_e5c]*nt_cvt<T>(x[53]) + nj22_c6*nt_cvt<T>(x[52]) + nj22_c7*nt_cvt<T>(x[52]) + nt_cvt<T>(x[52])*(nj22_c6 + nj22_c7))) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs22);
-        J[148] = (nj22_c5*(K[K_e5a] + K[K_e5c])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs22);
+        J[141] = (K[K_d5]*nj22_c0) * (cs1 * rs22);
+        J[140] = (-F.dt*tj[J_oclo]) * (cs9 * rs22);
+        J[144] = (-F.dt*F.parthcl*(K[K_d11]*xt43 + tj[J_hcl])) * (cs12 * rs22);
+        J[135] = (-F.dt*(K[K_d32]*xt45 + tj[J_clono2_cl] + tj[J_clono2_clo])) * (cs13 * rs22);
+        J[142] = (-F.dt*(K[K_d34]*xt43 + K[K_d35]*xt45 + tj[J_hocl]) + K[K_d37]*nj22_c0) * (cs14 * rs22);
+        J[133] = (-T(2)*F.dt*tj[J_cl2]) * (cs15 * rs22);
+        J[128] = (-F.dt*tj[J_clno2]) * (cs17 * rs22);
+        J[138] = (-F.dt*(T(2)*F.hnm*K[K_d61] + T(2)*tj[J_cl2o2])) * (cs24 * rs22);
+        J[132] = (-F.dt*tj[J_brcl]) * (cs26 * rs22);
+        J[143] = (K[K_c10]*nj22_c0) * (cs27 * rs22);
+        J[137] = (-F.dt*(K[K_d90]*nj22_c1 + T(3)*tj[J_cfc11])) * (cs30 * rs22);
+        J[131] = (-F.dt*(nj22_c2*xt42 + T(2)*tj[J_cfc12])) * (cs31 * rs22);
+        J[127] = (-F.dt*(K[K_d92]*nj22_c1 + T(3)*tj[J_cfc113])) * (cs32 * rs22);
+        J[129] = (-F.dt*(nj22_c3*xt42 + T(4)*tj[J_ccl4])) * (cs33 * rs22);
+        J[136] = (-F.dt*(nj22_c4*xt43 + T(3)*tj[J_ch3ccl3])) * (cs34 * rs22);
+        J[134] = (-F.dt*(K[K_d95]*xt43 + tj[J_ch3cl])) * (cs35 * rs22);
+        J[130] = (-F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22])) * (cs36 * rs22);
+        J[139] = (-F.dt*(T(3)*K[K_d90]*xt30 + T(3)*K[K_d92]*xt32 + K[K_d96]*xt36 + nj22_c2*xt31 + nj22_c3*xt33)) * (cs42 * rs22);
+        J[149] = (-F.dt*(F.parthcl*K[K_d11]*xt12 + K[K_d34]*xt14 + K[K_d95]*xt35 + K[K_d97]*xt36 + nj22_c4*xt34) + K[K_d9]*nj22_c5) * (cs43 * rs22);
+        J[147] = (F.dt*(F.h2*K[K_d6] + K[K_c10]*xt27 + K[K_d36]*xt48 + K[K_d37]*xt14 + K[K_d5]*xt1 + K[K_d7]*xt47)) * (cs44 * rs22);
+        J[146] = (-F.dt*(K[K_d32]*xt13 + K[K_d35]*xt14)) * (cs45 * rs22);
+        J[150] = (F.dt*(K[K_d33]*xt52 + K[K_d7]*xt44)) * (cs47 * rs22);
+        J[145] = (F.dt*(K[K_d31]*xt52 + K[K_d36]*xt44)) * (cs48 * rs22);
+        J[151] = (F.dt*(K[K_d31]*xt48 + K[K_d33]*xt47 + K[K_d9]*xt43 + K[K_e5a]*xt53 + K[K_e5c]*xt53 + nj22_c6*xt52 + nj22_c7*xt52 + xt52*(nj22_c6 + nj22_c7))) * (cs52 * rs22);
+        J[148] = (nj22_c5*(K[K_e5a] + K[K_e5c])) * (cs53 * rs22);
     }
     {  // row 25
     const T rs25 = nt_rscale<T>(nt_exp_hi(x[25]), fh);
         const T nj25_c0 = F.dt*het[5];
-        const T nj25_c1 = F.dt*nt_cvt<T>(x[25]);
+        const T nj25_c1 = F.dt*xt25;
         const T nj25_c2 = F.dt*K[K_e15];
-        J[83] = (-nj25_c0*nt_cvt<T>(x[19])) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs25);
-        J[82] = (het[6]*nj25_c1) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs25);
-        J[81] = (het[7]*nj25_c1) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs25);
-        J[79] = (-nj25_c0*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs25);
-        J[80] = (F.dt*(K[K_e16]*nt_cvt<T>(x[45]) + het[6]*nt_cvt<T>(x[12]) + het[7]*nt_cvt<T>(x[18]) + tj[J_hobr]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs25);
-        J[84] = (K[K_e16]*nj25_c1) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs25);
-        J[86] = (-nj25_c2*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs25);
-        J[85] = (-nj25_c2*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs25);
+        J[83] = (-nj25_c0*xt19) * (cs2 * rs25);
+        J[82] = (het[6]*nj25_c1) * (cs12 * rs25);
+        J[81] = (het[7]*nj25_c1) * (cs18 * rs25);
+        J[79] = (-nj25_c0*xt2) * (cs19 * rs25);
+        J[80] = (F.dt*(K[K_e16]*xt45 + het[6]*xt12 + het[7]*xt18 + tj[J_hobr]) + T(1)) * (cs25 * rs25);
+        J[84] = (K[K_e16]*nj25_c1) * (cs45 * rs25);
+        J[86] = (-nj25_c2*xt53) * (cs47 * rs25);
+        J[85] = (-nj25_c2*xt47) * (cs53 * rs25);
     }
     {  // row 26
     const T rs26 = nt_rscale<T>(nt_exp_hi(x[26]), fh);
         const T nj26_c0 = F.dt*het[6];
         const T nj26_c1 = F.dt*het[8];
         const T nj26_c2 = F.dt*K[K_e5c];
-        J[47] = (-nj26_c0*nt_cvt<T>(x[25])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs26);
-        J[45] = (-nj26_c1*nt_cvt<T>(x[18])) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs26);
-        J[46] = (-nj26_c1*nt_cvt<T>(x[14])) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs26);
-        J[44] = (-nj26_c0*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs26);
-        J[43] = (F.dt*tj[J_brcl] + T(1)) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs26);
-        J[49] = (-nj26_c2*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs26);
-        J[48] = (-nj26_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs26);
+        J[47] = (-nj26_c0*xt25) * (cs12 * rs26);
+        J[45] = (-nj26_c1*xt18) * (cs14 * rs26);
+        J[46] = (-nj26_c1*xt14) * (cs18 * rs26);
+        J[44] = (-nj26_c0*xt12) * (cs25 * rs26);
+        J[43] = (F.dt*tj[J_brcl] + T(1)) * (cs26 * rs26);
+        J[49] = (-nj26_c2*xt53) * (cs52 * rs26);
+        J[48] = (-nj26_c2*xt52) * (cs53 * rs26);
     }
     {  // row 31
     const T rs31 = nt_rscale<T>(nt_exp_hi(x[31]), fh);
-        J[41] = (F.dt*(K[K_d91]*nt_cvt<T>(x[42]) + tj[J_cfc12]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs31);
-        J[42] = (F.dt*K[K_d91]*nt_cvt<T>(x[31])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs31);
+        J[41] = (F.dt*(K[K_d91]*xt42 + tj[J_cfc12]) + T(1)) * (cs31 * rs31);
+        J[42] = (F.dt*K[K_d91]*xt31) * (cs42 * rs31);
     }
     {  // row 35
     const T rs35 = nt_rscale<T>(nt_exp_hi(x[35]), fh);
-        J[66] = (F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs35);
-        J[67] = (F.dt*K[K_d95]*nt_cvt<T>(x[35])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs35);
+        J[66] = (F.dt*(K[K_d95]*xt43 + tj[J_ch3cl]) + T(1)) * (cs35 * rs35);
+        J[67] = (F.dt*K[K_d95]*xt35) * (cs43 * rs35);
     }
     {  // row 43
     const T rs43 = nt_rscale<T>(nt_exp_hi(x[43]), fh);
@@ -5178,7 +6293,7 @@ __device__ __forceinline__ void nt_jacobian_night_w4_0(const FF& F, PK K, PK tj,
         J[328] = T(0);
         J[316] = T(0);
         J[318] = T(0);
-        J[337] = (T(1)) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs43);
+        J[337] = (T(1)) * (cs43 * rs43);
         J[334] = T(0);
         J[333] = T(0);
         J[339] = T(0);
@@ -5209,8 +6324,8 @@ __device__ __forceinline__ void nt_jacobian_night_w4_0(const FF& F, PK K, PK tj,
         J[179] = T(0);
         J[178] = T(0);
     }
-    const bool sel_N_clo = (nt_cvt<T>(x[22])) >= (T(0));
-    const T N_clo = sel_N_clo ? T(nt_cvt<T>(x[22])) : T(T(0));
+    const bool sel_N_clo = (xt22) >= (T(0));
+    const T N_clo = sel_N_clo ? T(xt22) : T(T(0));
     const T d_N_clo_22 = sel_N_clo ? T(T(1)) : T(T(0));
     {  // row 52
     const T rs52 = nt_rscale<T>(nt_exp_hi(x[52]), fh);
@@ -5218,7 +6333,7 @@ __device__ __forceinline__ void nt_jacobian_night_w4_0(const FF& F, PK K, PK tj,
         J[373] = T(0);
         J[372] = T(0);
         J[370] = T(0);
-        J[368] = (-d_N_clo_22) * (nt_scale<T>(nt_exp_hi(x[22]), fh) * rs52);
+        J[368] = (-d_N_clo_22) * (cs22 * rs52);
         J[371] = T(0);
         J[377] = T(0);
         J[375] = T(0);
@@ -5226,15 +6341,15 @@ __device__ __forceinline__ void nt_jacobian_night_w4_0(const FF& F, PK K, PK tj,
         J[378] = T(0);
         J[374] = T(0);
         J[380] = T(0);
-        J[381] = (T(1)) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs52);
+        J[381] = (T(1)) * (cs52 * rs52);
         J[376] = T(0);
     }
-    const bool sel_N_bro = (nt_cvt<T>(x[23])) >= (T(0));
-    const T N_bro = sel_N_bro ? T(nt_cvt<T>(x[23])) : T(T(0));
+    const bool sel_N_bro = (xt23) >= (T(0));
+    const T N_bro = sel_N_bro ? T(xt23) : T(T(0));
     const T d_N_bro_23 = sel_N_bro ? T(T(1)) : T(T(0));
     {  // row 53
     const T rs53 = nt_rscale<T>(nt_exp_hi(x[53]), fh);
-        J[297] = (-d_N_bro_23) * (nt_scale<T>(nt_exp_hi(x[23]), fh) * rs53);
+        J[297] = (-d_N_bro_23) * (cs23 * rs53);
         J[298] = T(0);
         J[302] = T(0);
         J[300] = T(0);
@@ -5243,7 +6358,7 @@ __device__ __forceinline__ void nt_jacobian_night_w4_0(const FF& F, PK K, PK tj,
         J[299] = T(0);
         J[305] = T(0);
         J[306] = T(0);
-        J[301] = (T(1)) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs53);
+        J[301] = (T(1)) * (cs53 * rs53);
     }
 }
 
@@ -5285,70 +6400,159 @@ __device__ __forceinline__ void nt_residual_night_w4_1(const FF& F, PK K, PK tj,
 template <typename T, typename FF, typename PK, typename PJ>
 __device__ __forceinline__ void nt_jacobian_night_w4_1(const FF& F, PK K, PK tj, PK het, const double* __restrict__ x, double floor_, PJ J) {
     const int fh = nt_exp_hi(floor_);
+    const T xt0 = nt_cvt<T>(x[0]);
+    const T xt1 = nt_cvt<T>(x[1]);
+    const T xt2 = nt_cvt<T>(x[2]);
+    const T xt3 = nt_cvt<T>(x[3]);
+    const T xt4 = nt_cvt<T>(x[4]);
+    const T xt5 = nt_cvt<T>(x[5]);
+    const T xt6 = nt_cvt<T>(x[6]);
+    const T xt7 = nt_cvt<T>(x[7]);
+    const T xt8 = nt_cvt<T>(x[8]);
+    const T xt9 = nt_cvt<T>(x[9]);
+    const T xt10 = nt_cvt<T>(x[10]);
+    const T xt11 = nt_cvt<T>(x[11]);
+    const T xt12 = nt_cvt<T>(x[12]);
+    const T xt13 = nt_cvt<T>(x[13]);
+    const T xt14 = nt_cvt<T>(x[14]);
+    const T xt15 = nt_cvt<T>(x[15]);
+    const T xt16 = nt_cvt<T>(x[16]);
+    const T xt17 = nt_cvt<T>(x[17]);
+    const T xt18 = nt_cvt<T>(x[18]);
+    const T xt19 = nt_cvt<T>(x[19]);
+    const T xt20 = nt_cvt<T>(x[20]);
+    const T xt21 = nt_cvt<T>(x[21]);
+    const T xt22 = nt_cvt<T>(x[22]);
+    const T xt23 = nt_cvt<T>(x[23]);
+    const T xt24 = nt_cvt<T>(x[24]);
+    const T xt25 = nt_cvt<T>(x[25]);
+    const T xt26 = nt_cvt<T>(x[26]);
+    const T xt27 = nt_cvt<T>(x[27]);
+    const T xt28 = nt_cvt<T>(x[28]);
+    const T xt29 = nt_cvt<T>(x[29]);
+    const T xt30 = nt_cvt<T>(x[30]);
+    const T xt31 = nt_cvt<T>(x[31]);
+    const T xt32 = nt_cvt<T>(x[32]);
+    const T xt33 = nt_cvt<T>(x[33]);
+    const T xt34 = nt_cvt<T>(x[34]);
+    const T xt35 = nt_cvt<T>(x[35]);
+    const T xt36 = nt_cvt<T>(x[36]);
+    const T xt37 = nt_cvt<T>(x[37]);
+    const T xt38 = nt_cvt<T>(x[38]);
+    const T xt39 = nt_cvt<T>(x[39]);
+    const T xt40 = nt_cvt<T>(x[40]);
+    const T xt41 = nt_cvt<T>(x[41]);
+    const T xt42 = nt_cvt<T>(x[42]);
+    const T xt43 = nt_cvt<T>(x[43]);
+    const T xt44 = nt_cvt<T>(x[44]);
+    const T xt45 = nt_cvt<T>(x[45]);
+    const T xt46 = nt_cvt<T>(x[46]);
+    const T xt47 = nt_cvt<T>(x[47]);
+    const T xt48 = nt_cvt<T>(x[48]);
+    const T xt49 = nt_cvt<T>(x[49]);
+    const T xt50 = nt_cvt<T>(x[50]);
+    const T xt51 = nt_cvt<T>(x[51]);
+    const T xt52 = nt_cvt<T>(x[52]);
+    const T xt53 = nt_cvt<T>(x[53]);
+    const T xt54 = nt_cvt<T>(x[54]);
+    const T xt55 = nt_cvt<T>(x[55]);
+    const T xt56 = nt_cvt<T>(x[56]);
+    const T cs0 = nt_scale<T>(nt_exp_hi(x[0]), fh);
+    const T cs1 = nt_scale<T>(nt_exp_hi(x[1]), fh);
+    const T cs2 = nt_scale<T>(nt_exp_hi(x[2]), fh);
+    const T cs5 = nt_scale<T>(nt_exp_hi(x[5]), fh);
+    const T cs12 = nt_scale<T>(nt_exp_hi(x[12]), fh);
+    const T cs13 = nt_scale<T>(nt_exp_hi(x[13]), fh);
+    const T cs14 = nt_scale<T>(nt_exp_hi(x[14]), fh);
+    const T cs16 = nt_scale<T>(nt_exp_hi(x[16]), fh);
+    const T cs18 = nt_scale<T>(nt_exp_hi(x[18]), fh);
+    const T cs19 = nt_scale<T>(nt_exp_hi(x[19]), fh);
+    const T cs20 = nt_scale<T>(nt_exp_hi(x[20]), fh);
+    const T cs24 = nt_scale<T>(nt_exp_hi(x[24]), fh);
+    const T cs25 = nt_scale<T>(nt_exp_hi(x[25]), fh);
+    const T cs26 = nt_scale<T>(nt_exp_hi(x[26]), fh);
+    const T cs27 = nt_scale<T>(nt_exp_hi(x[27]), fh);
+    const T cs28 = nt_scale<T>(nt_exp_hi(x[28]), fh);
+    const T cs34 = nt_scale<T>(nt_exp_hi(x[34]), fh);
+    const T cs37 = nt_scale<T>(nt_exp_hi(x[37]), fh);
+    const T cs38 = nt_scale<T>(nt_exp_hi(x[38]), fh);
+    const T cs39 = nt_scale<T>(nt_exp_hi(x[39]), fh);
+    const T cs41 = nt_scale<T>(nt_exp_hi(x[41]), fh);
+    const T cs42 = nt_scale<T>(nt_exp_hi(x[42]), fh);
+    const T cs43 = nt_scale<T>(nt_exp_hi(x[43]), fh);
+    const T cs44 = nt_scale<T>(nt_exp_hi(x[44]), fh);
+    const T cs45 = nt_scale<T>(nt_exp_hi(x[45]), fh);
+    const T cs46 = nt_scale<T>(nt_exp_hi(x[46]), fh);
+    const T cs47 = nt_scale<T>(nt_exp_hi(x[47]), fh);
+    const T cs48 = nt_scale<T>(nt_exp_hi(x[48]), fh);
+    const T cs49 = nt_scale<T>(nt_exp_hi(x[49]), fh);
+    const T cs52 = nt_scale<T>(nt_exp_hi(x[52]), fh);
+    const T cs53 = nt_scale<T>(nt_exp_hi(x[53]), fh);
+    const T cs55 = nt_scale<T>(nt_exp_hi(x[55]), fh);
     {  // row 0
     const T rs0 = nt_rscale<T>(nt_exp_hi(x[0]), fh);
         const T nj0_c0 = K[K_b38] + K[K_b39];
-        J[76] = (F.dt*(nj0_c0*nt_cvt<T>(x[42]) + tj[J_n2o]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs0);
-        J[77] = (F.dt*nj0_c0*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs0);
+        J[76] = (F.dt*(nj0_c0*xt42 + tj[J_n2o]) + T(1)) * (cs0 * rs0);
+        J[77] = (F.dt*nj0_c0*xt0) * (cs42 * rs0);
     }
     {  // row 12
     const T rs12 = nt_rscale<T>(nt_exp_hi(x[12]), fh);
-        const T nj12_c0 = F.dt*nt_cvt<T>(x[44]);
-        const T nj12_c1 = F.dt*nt_cvt<T>(x[12]);
+        const T nj12_c0 = F.dt*xt44;
+        const T nj12_c1 = F.dt*xt12;
         const T nj12_c2 = F.dt*K[K_d9];
-        J[250] = (-K[K_d5]*nj12_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs12);
-        J[247] = (het[3]*nj12_c1) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs12);
-        J[253] = (F.dt*(F.parthcl*(K[K_d11]*nt_cvt<T>(x[43]) + tj[J_hcl]) + F.rain_hcl + het[1]*nt_cvt<T>(x[13]) + het[3]*nt_cvt<T>(x[5]) + het[4]*nt_cvt<T>(x[14]) + het[6]*nt_cvt<T>(x[25])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs12);
-        J[249] = (het[1]*nj12_c1) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs12);
-        J[251] = (het[4]*nj12_c1) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs12);
-        J[248] = (het[6]*nj12_c1) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs12);
-        J[252] = (-K[K_c10]*nj12_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs12);
-        J[255] = (F.parthcl*K[K_d11]*nj12_c1 - nj12_c2*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs12);
-        J[254] = (-F.dt*(F.h2*K[K_d6] + K[K_c10]*nt_cvt<T>(x[27]) + K[K_d5]*nt_cvt<T>(x[1]) + K[K_d7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs12);
-        J[256] = (-K[K_d7]*nj12_c0) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs12);
-        J[257] = (-nj12_c2*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs12);
+        J[250] = (-K[K_d5]*nj12_c0) * (cs1 * rs12);
+        J[247] = (het[3]*nj12_c1) * (cs5 * rs12);
+        J[253] = (F.dt*(F.parthcl*(K[K_d11]*xt43 + tj[J_hcl]) + F.rain_hcl + het[1]*xt13 + het[3]*xt5 + het[4]*xt14 + het[6]*xt25) + T(1)) * (cs12 * rs12);
+        J[249] = (het[1]*nj12_c1) * (cs13 * rs12);
+        J[251] = (het[4]*nj12_c1) * (cs14 * rs12);
+        J[248] = (het[6]*nj12_c1) * (cs25 * rs12);
+        J[252] = (-K[K_c10]*nj12_c0) * (cs27 * rs12);
+        J[255] = (F.parthcl*K[K_d11]*nj12_c1 - nj12_c2*xt52) * (cs43 * rs12);
+        J[254] = (-F.dt*(F.h2*K[K_d6] + K[K_c10]*xt27 + K[K_d5]*xt1 + K[K_d7]*xt47)) * (cs44 * rs12);
+        J[256] = (-K[K_d7]*nj12_c0) * (cs47 * rs12);
+        J[257] = (-nj12_c2*xt43) * (cs52 * rs12);
     }
     {  // row 16
     const T rs16 = nt_rscale<T>(nt_exp_hi(x[16]), fh);
-        J[189] = (F.dt*(F.rain_h2o2 + K[K_a30]*nt_cvt<T>(x[43]) + tj[J_h2o2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs16);
-        J[190] = (F.dt*K[K_a30]*nt_cvt<T>(x[16])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs16);
-        J[191] = (-T(2)*F.dt*K[K_a27]*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs16);
+        J[189] = (F.dt*(F.rain_h2o2 + K[K_a30]*xt43 + tj[J_h2o2]) + T(1)) * (cs16 * rs16);
+        J[190] = (F.dt*K[K_a30]*xt16) * (cs43 * rs16);
+        J[191] = (-T(2)*F.dt*K[K_a27]*xt47) * (cs47 * rs16);
     }
     {  // row 19
     const T rs19 = nt_rscale<T>(nt_exp_hi(x[19]), fh);
-        const T nj19_c0 = F.dt*nt_cvt<T>(x[19]);
+        const T nj19_c0 = F.dt*xt19;
         const T nj19_c1 = F.dt*K[K_e13];
-        J[56] = (het[5]*nj19_c0) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs19);
-        J[55] = (F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + het[5]*nt_cvt<T>(x[2]) + tj[J_brono2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs19);
-        J[58] = (K[K_e8]*nj19_c0) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs19);
-        J[57] = (-nj19_c1*nt_cvt<T>(x[53])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs19);
-        J[59] = (-nj19_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs19);
+        J[56] = (het[5]*nj19_c0) * (cs2 * rs19);
+        J[55] = (F.dt*(K[K_e8]*xt45 + het[5]*xt2 + tj[J_brono2]) + T(1)) * (cs19 * rs19);
+        J[58] = (K[K_e8]*nj19_c0) * (cs45 * rs19);
+        J[57] = (-nj19_c1*xt53) * (cs48 * rs19);
+        J[59] = (-nj19_c1*xt48) * (cs53 * rs19);
     }
     {  // row 24
     const T rs24 = nt_rscale<T>(nt_exp_hi(x[24]), fh);
-        J[97] = (F.dt*(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[24]), fh) * rs24);
-        J[98] = (-T(2)*F.dt*K[K_d60]*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs24);
+        J[97] = (F.dt*(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(1)) * (cs24 * rs24);
+        J[98] = (-T(2)*F.dt*K[K_d60]*xt52) * (cs52 * rs24);
     }
     {  // row 34
     const T rs34 = nt_rscale<T>(nt_exp_hi(x[34]), fh);
-        J[93] = (F.dt*(K[K_d94]*nt_cvt<T>(x[43]) + tj[J_ch3ccl3]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs34);
-        J[94] = (F.dt*K[K_d94]*nt_cvt<T>(x[34])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs34);
+        J[93] = (F.dt*(K[K_d94]*xt43 + tj[J_ch3ccl3]) + T(1)) * (cs34 * rs34);
+        J[94] = (F.dt*K[K_d94]*xt34) * (cs43 * rs34);
     }
     {  // row 40
     const T rs40 = nt_rscale<T>(nt_exp_hi(x[40]), fh);
         const T nj40_c0 = T(2)*K[K_e54];
-        J[16] = (F.dt*F.rain_hbr) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs40);
-        J[13] = (-F.dt*(K[K_e50]*nt_cvt<T>(x[42]) + K[K_e51]*nt_cvt<T>(x[43]) + tj[J_ch3br])) * (nt_scale<T>(nt_exp_hi(x[37]), fh) * rs40);
-        J[11] = (-F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211])) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs40);
-        J[12] = (-F.dt*(K[K_e53]*nt_cvt<T>(x[42]) + tj[J_h1301])) * (nt_scale<T>(nt_exp_hi(x[39]), fh) * rs40);
-        J[15] = (-F.dt*(nj40_c0*nt_cvt<T>(x[43]) + T(2)*tj[J_ch2br2])) * (nt_scale<T>(nt_exp_hi(x[41]), fh) * rs40);
-        J[14] = (-F.dt*(K[K_e50]*nt_cvt<T>(x[37]) + K[K_e52]*nt_cvt<T>(x[38]) + K[K_e53]*nt_cvt<T>(x[39]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs40);
-        J[17] = (-F.dt*(K[K_e51]*nt_cvt<T>(x[37]) + nj40_c0*nt_cvt<T>(x[41]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs40);
+        J[16] = (F.dt*F.rain_hbr) * (cs18 * rs40);
+        J[13] = (-F.dt*(K[K_e50]*xt42 + K[K_e51]*xt43 + tj[J_ch3br])) * (cs37 * rs40);
+        J[11] = (-F.dt*(K[K_e52]*xt42 + tj[J_h1211])) * (cs38 * rs40);
+        J[12] = (-F.dt*(K[K_e53]*xt42 + tj[J_h1301])) * (cs39 * rs40);
+        J[15] = (-F.dt*(nj40_c0*xt43 + T(2)*tj[J_ch2br2])) * (cs41 * rs40);
+        J[14] = (-F.dt*(K[K_e50]*xt37 + K[K_e52]*xt38 + K[K_e53]*xt39)) * (cs42 * rs40);
+        J[17] = (-F.dt*(K[K_e51]*xt37 + nj40_c0*xt41)) * (cs43 * rs40);
     }
     {  // row 41
     const T rs41 = nt_rscale<T>(nt_exp_hi(x[41]), fh);
-        J[125] = (F.dt*(K[K_e54]*nt_cvt<T>(x[43]) + tj[J_ch2br2]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[41]), fh) * rs41);
-        J[126] = (F.dt*K[K_e54]*nt_cvt<T>(x[41])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs41);
+        J[125] = (F.dt*(K[K_e54]*xt43 + tj[J_ch2br2]) + T(1)) * (cs41 * rs41);
+        J[126] = (F.dt*K[K_e54]*xt41) * (cs43 * rs41);
     }
     {  // row 44
     const T rs44 = nt_rscale<T>(nt_exp_hi(x[44]), fh);
@@ -5379,25 +6583,25 @@ __device__ __forceinline__ void nt_jacobian_night_w4_1(const FF& F, PK K, PK tj,
         J[310] = T(0);
     }
     const T N_cno_c0 = K[K_b9]/K[K_b12];
-    const T N_cno = N_cno_c0*nt_cvt<T>(x[46]);
+    const T N_cno = N_cno_c0*xt46;
     const T d_N_cno_46 = N_cno_c0;
-    const T N_dno = -N_cno + nt_cvt<T>(x[20]);
+    const T N_dno = -N_cno + xt20;
     const T d_N_dno_20 = T(1);
     const T d_N_dno_46 = -d_N_cno_46;
     const T N_no2_c0 = N_cno + T(1e-30);
     const T N_no2_c1 = T(1e-30)/N_no2_c0;
     const bool sel_N_no2 = (N_dno) > (T(1e-30));
-    const T N_no2 = sel_N_no2 ? T(N_dno) : T(N_no2_c1*nt_cvt<T>(x[20]));
+    const T N_no2 = sel_N_no2 ? T(N_dno) : T(N_no2_c1*xt20);
     const T d_N_no2_20 = sel_N_no2 ? T(d_N_dno_20) : T(N_no2_c1);
-    const T d_N_no2_46 = sel_N_no2 ? T(d_N_dno_46) : T(-T(1e-30)*d_N_cno_46*nt_cvt<T>(x[20])/(N_no2_c0*N_no2_c0));
+    const T d_N_no2_46 = sel_N_no2 ? T(d_N_dno_46) : T(-T(1e-30)*d_N_cno_46*xt20/(N_no2_c0*N_no2_c0));
     {  // row 48
     const T rs48 = nt_rscale<T>(nt_exp_hi(x[48]), fh);
-        J[270] = (-d_N_no2_20) * (nt_scale<T>(nt_exp_hi(x[20]), fh) * rs48);
+        J[270] = (-d_N_no2_20) * (cs20 * rs48);
         J[269] = T(0);
         J[272] = T(0);
-        J[275] = (-d_N_no2_46) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs48);
+        J[275] = (-d_N_no2_46) * (cs46 * rs48);
         J[274] = T(0);
-        J[271] = (T(1)) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs48);
+        J[271] = (T(1)) * (cs48 * rs48);
         J[276] = T(0);
         J[277] = T(0);
         J[273] = T(0);
@@ -5406,62 +6610,62 @@ __device__ __forceinline__ void nt_jacobian_night_w4_1(const FF& F, PK K, PK tj,
     const T N_no3_c1 = (T(1)/(N_no3_c0));
     const T N_no3_c2 = N_cno*N_no3_c1;
     const bool sel_N_no3 = (N_dno) > (T(1e-30));
-    const T N_no3 = sel_N_no3 ? T(N_cno) : T(N_no3_c2*nt_cvt<T>(x[20]));
+    const T N_no3 = sel_N_no3 ? T(N_cno) : T(N_no3_c2*xt20);
     const T d_N_no3_20 = sel_N_no3 ? T(T(0)) : T(N_no3_c2);
-    const T d_N_no3_46 = sel_N_no3 ? T(d_N_cno_46) : T(d_N_cno_46*(-N_cno*nt_cvt<T>(x[20])/(N_no3_c0*N_no3_c0) + N_no3_c1*nt_cvt<T>(x[20])));
+    const T d_N_no3_46 = sel_N_no3 ? T(d_N_cno_46) : T(d_N_cno_46*(-N_cno*xt20/(N_no3_c0*N_no3_c0) + N_no3_c1*xt20));
     {  // row 54
     const T rs54 = nt_rscale<T>(nt_exp_hi(x[54]), fh);
-        J[68] = (-d_N_no3_20) * (nt_scale<T>(nt_exp_hi(x[20]), fh) * rs54);
-        J[70] = (-d_N_no3_46) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs54);
+        J[68] = (-d_N_no3_20) * (cs20 * rs54);
+        J[70] = (-d_N_no3_46) * (cs46 * rs54);
         J[69] = T(0);
     }
-    const T N_t06_c0 = tj[J_hocl]*nt_cvt<T>(x[14]);
-    const T N_t06_c1 = K[K_d33]*nt_cvt<T>(x[52]);
-    const T N_t06_c2 = N_t06_c1*nt_cvt<T>(x[47]);
+    const T N_t06_c0 = tj[J_hocl]*xt14;
+    const T N_t06_c1 = K[K_d33]*xt52;
+    const T N_t06_c2 = N_t06_c1*xt47;
     const bool sel_N_t06 = (N_t06_c0) <= (N_t06_c2);
     const T N_t06 = sel_N_t06 ? T(N_t06_c0) : T(N_t06_c2);
     const T d_N_t06_14 = sel_N_t06 ? T(tj[J_hocl]) : T(T(0));
     const T d_N_t06_47 = sel_N_t06 ? T(T(0)) : T(N_t06_c1);
-    const T d_N_t06_52 = sel_N_t06 ? T(T(0)) : T(K[K_d33]*nt_cvt<T>(x[47]));
-    const T N_t07_c0 = K[K_e5c]*nt_cvt<T>(x[53]);
-    const T N_t07_c1 = N_t07_c0*nt_cvt<T>(x[52]);
-    const T N_t07_c2 = tj[J_brcl]*nt_cvt<T>(x[26]);
+    const T d_N_t06_52 = sel_N_t06 ? T(T(0)) : T(K[K_d33]*xt47);
+    const T N_t07_c0 = K[K_e5c]*xt53;
+    const T N_t07_c1 = N_t07_c0*xt52;
+    const T N_t07_c2 = tj[J_brcl]*xt26;
     const bool sel_N_t07 = (N_t07_c1) <= (N_t07_c2);
     const T N_t07 = sel_N_t07 ? T(N_t07_c1) : T(N_t07_c2);
     const T d_N_t07_26 = sel_N_t07 ? T(T(0)) : T(tj[J_brcl]);
     const T d_N_t07_52 = sel_N_t07 ? T(N_t07_c0) : T(T(0));
-    const T d_N_t07_53 = sel_N_t07 ? T(K[K_e5c]*nt_cvt<T>(x[52])) : T(T(0));
-    const T N_t09_c0 = K[K_e15]*nt_cvt<T>(x[53]);
-    const T N_t09_c1 = N_t09_c0*nt_cvt<T>(x[47]);
-    const T N_t09_c2 = tj[J_hobr]*nt_cvt<T>(x[25]);
+    const T d_N_t07_53 = sel_N_t07 ? T(K[K_e5c]*xt52) : T(T(0));
+    const T N_t09_c0 = K[K_e15]*xt53;
+    const T N_t09_c1 = N_t09_c0*xt47;
+    const T N_t09_c2 = tj[J_hobr]*xt25;
     const bool sel_N_t09 = (N_t09_c1) <= (N_t09_c2);
     const T N_t09 = sel_N_t09 ? T(N_t09_c1) : T(N_t09_c2);
     const T d_N_t09_25 = sel_N_t09 ? T(T(0)) : T(tj[J_hobr]);
     const T d_N_t09_47 = sel_N_t09 ? T(N_t09_c0) : T(T(0));
-    const T d_N_t09_53 = sel_N_t09 ? T(K[K_e15]*nt_cvt<T>(x[47])) : T(T(0));
+    const T d_N_t09_53 = sel_N_t09 ? T(K[K_e15]*xt47) : T(T(0));
     {  // row 7
     const T rs7 = nt_rscale<T>(nt_exp_hi(x[7]), fh);
         const T nj7_c0 = T(2)*F.dt;
         const T nj7_c1 = tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
-        const T nj7_c2 = F.dt*nt_cvt<T>(x[49]);
+        const T nj7_c2 = F.dt*xt49;
         const T nj7_c3 = T(2)*K[K_b3];
         const T nj7_c4 = T(2)*K[K_d3];
         const T nj7_c5 = T(2)*K[K_hk3];
         const T nj7_c6 = T(2)*K[K_b9]*nj7_c1;
-        J[105] = (nj7_c0*nj7_c1*tj[J_clono2_cl]) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs7);
-        J[106] = (F.dt*d_N_t06_14) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs7);
-        J[104] = (F.dt*d_N_t09_25) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs7);
-        J[103] = (d_N_t07_26*nj7_c0) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs7);
-        J[108] = (-K[K_c5]*nj7_c2) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs7);
-        J[112] = (F.dt*(K[K_a5]*nt_cvt<T>(x[45]) + K[K_a6]*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs7);
-        J[110] = (F.dt*(K[K_a5]*nt_cvt<T>(x[43]) + K[K_a7]*nt_cvt<T>(x[47]) + T(4)*K[K_hk1]*nt_cvt<T>(x[45]) + nj7_c3*nt_cvt<T>(x[48]) + nj7_c4*nt_cvt<T>(x[52]) + nj7_c5*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs7);
-        J[114] = (F.dt*(K[K_a2]*nt_cvt<T>(x[55]) + K[K_a6]*nt_cvt<T>(x[43]) + K[K_a6b]*nt_cvt<T>(x[47]) + nj7_c5*nt_cvt<T>(x[45]) + nj7_c6*nt_cvt<T>(x[48]))) * (nt_scale<T>(nt_exp_hi(x[46]), fh) * rs7);
-        J[113] = (F.dt*d_N_t06_47 + F.dt*d_N_t09_47 + F.dt*(K[K_a6b]*nt_cvt<T>(x[46]) + K[K_a7]*nt_cvt<T>(x[45])) - K[K_a26]*nj7_c2) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs7);
-        J[109] = (F.dt*(nj7_c3*nt_cvt<T>(x[45]) + nj7_c6*nt_cvt<T>(x[46]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs7);
-        J[115] = (-F.dt*(K[K_a26]*nt_cvt<T>(x[47]) + K[K_c5]*nt_cvt<T>(x[28]))) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs7);
-        J[116] = (F.dt*d_N_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*nt_cvt<T>(x[52])/(F.hnm*K[K_d61] + tj[J_cl2o2]) + nj7_c4*nt_cvt<T>(x[45])) + d_N_t07_52*nj7_c0) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs7);
-        J[111] = (F.dt*d_N_t09_53 + d_N_t07_53*nj7_c0) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs7);
-        J[107] = (F.dt*K[K_a2]*nt_cvt<T>(x[46])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs7);
+        J[105] = (nj7_c0*nj7_c1*tj[J_clono2_cl]) * (cs13 * rs7);
+        J[106] = (F.dt*d_N_t06_14) * (cs14 * rs7);
+        J[104] = (F.dt*d_N_t09_25) * (cs25 * rs7);
+        J[103] = (d_N_t07_26*nj7_c0) * (cs26 * rs7);
+        J[108] = (-K[K_c5]*nj7_c2) * (cs28 * rs7);
+        J[112] = (F.dt*(K[K_a5]*xt45 + K[K_a6]*xt46)) * (cs43 * rs7);
+        J[110] = (F.dt*(K[K_a5]*xt43 + K[K_a7]*xt47 + T(4)*K[K_hk1]*xt45 + nj7_c3*xt48 + nj7_c4*xt52 + nj7_c5*xt46)) * (cs45 * rs7);
+        J[114] = (F.dt*(K[K_a2]*xt55 + K[K_a6]*xt43 + K[K_a6b]*xt47 + nj7_c5*xt45 + nj7_c6*xt48)) * (cs46 * rs7);
+        J[113] = (F.dt*d_N_t06_47 + F.dt*d_N_t09_47 + F.dt*(K[K_a6b]*xt46 + K[K_a7]*xt45) - K[K_a26]*nj7_c2) * (cs47 * rs7);
+        J[109] = (F.dt*(nj7_c3*xt45 + nj7_c6*xt46)) * (cs48 * rs7);
+        J[115] = (-F.dt*(K[K_a26]*xt47 + K[K_c5]*xt28)) * (cs49 * rs7);
+        J[116] = (F.dt*d_N_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*xt52/(F.hnm*K[K_d61] + tj[J_cl2o2]) + nj7_c4*xt45) + d_N_t07_52*nj7_c0) * (cs52 * rs7);
+        J[111] = (F.dt*d_N_t09_53 + d_N_t07_53*nj7_c0) * (cs53 * rs7);
+        J[107] = (F.dt*K[K_a2]*xt46) * (cs55 * rs7);
     }
 }
 
@@ -5498,142 +6702,235 @@ __device__ __forceinline__ void nt_residual_night_w4_2(const FF& F, PK K, PK tj,
 template <typename T, typename FF, typename PK, typename PJ>
 __device__ __forceinline__ void nt_jacobian_night_w4_2(const FF& F, PK K, PK tj, PK het, const double* __restrict__ x, double floor_, PJ J) {
     const int fh = nt_exp_hi(floor_);
+    const T xt0 = nt_cvt<T>(x[0]);
+    const T xt1 = nt_cvt<T>(x[1]);
+    const T xt2 = nt_cvt<T>(x[2]);
+    const T xt3 = nt_cvt<T>(x[3]);
+    const T xt4 = nt_cvt<T>(x[4]);
+    const T xt5 = nt_cvt<T>(x[5]);
+    const T xt6 = nt_cvt<T>(x[6]);
+    const T xt7 = nt_cvt<T>(x[7]);
+    const T xt8 = nt_cvt<T>(x[8]);
+    const T xt9 = nt_cvt<T>(x[9]);
+    const T xt10 = nt_cvt<T>(x[10]);
+    const T xt11 = nt_cvt<T>(x[11]);
+    const T xt12 = nt_cvt<T>(x[12]);
+    const T xt13 = nt_cvt<T>(x[13]);
+    const T xt14 = nt_cvt<T>(x[14]);
+    const T xt15 = nt_cvt<T>(x[15]);
+    const T xt16 = nt_cvt<T>(x[16]);
+    const T xt17 = nt_cvt<T>(x[17]);
+    const T xt18 = nt_cvt<T>(x[18]);
+    const T xt19 = nt_cvt<T>(x[19]);
+    const T xt20 = nt_cvt<T>(x[20]);
+    const T xt21 = nt_cvt<T>(x[21]);
+    const T xt22 = nt_cvt<T>(x[22]);
+    const T xt23 = nt_cvt<T>(x[23]);
+    const T xt24 = nt_cvt<T>(x[24]);
+    const T xt25 = nt_cvt<T>(x[25]);
+    const T xt26 = nt_cvt<T>(x[26]);
+    const T xt27 = nt_cvt<T>(x[27]);
+    const T xt28 = nt_cvt<T>(x[28]);
+    const T xt29 = nt_cvt<T>(x[29]);
+    const T xt30 = nt_cvt<T>(x[30]);
+    const T xt31 = nt_cvt<T>(x[31]);
+    const T xt32 = nt_cvt<T>(x[32]);
+    const T xt33 = nt_cvt<T>(x[33]);
+    const T xt34 = nt_cvt<T>(x[34]);
+    const T xt35 = nt_cvt<T>(x[35]);
+    const T xt36 = nt_cvt<T>(x[36]);
+    const T xt37 = nt_cvt<T>(x[37]);
+    const T xt38 = nt_cvt<T>(x[38]);
+    const T xt39 = nt_cvt<T>(x[39]);
+    const T xt40 = nt_cvt<T>(x[40]);
+    const T xt41 = nt_cvt<T>(x[41]);
+    const T xt42 = nt_cvt<T>(x[42]);
+    const T xt43 = nt_cvt<T>(x[43]);
+    const T xt44 = nt_cvt<T>(x[44]);
+    const T xt45 = nt_cvt<T>(x[45]);
+    const T xt46 = nt_cvt<T>(x[46]);
+    const T xt47 = nt_cvt<T>(x[47]);
+    const T xt48 = nt_cvt<T>(x[48]);
+    const T xt49 = nt_cvt<T>(x[49]);
+    const T xt50 = nt_cvt<T>(x[50]);
+    const T xt51 = nt_cvt<T>(x[51]);
+    const T xt52 = nt_cvt<T>(x[52]);
+    const T xt53 = nt_cvt<T>(x[53]);
+    const T xt54 = nt_cvt<T>(x[54]);
+    const T xt55 = nt_cvt<T>(x[55]);
+    const T xt56 = nt_cvt<T>(x[56]);
+    const T cs0 = nt_scale<T>(nt_exp_hi(x[0]), fh);
+    const T cs1 = nt_scale<T>(nt_exp_hi(x[1]), fh);
+    const T cs2 = nt_scale<T>(nt_exp_hi(x[2]), fh);
+    const T cs4 = nt_scale<T>(nt_exp_hi(x[4]), fh);
+    const T cs5 = nt_scale<T>(nt_exp_hi(x[5]), fh);
+    const T cs8 = nt_scale<T>(nt_exp_hi(x[8]), fh);
+    const T cs12 = nt_scale<T>(nt_exp_hi(x[12]), fh);
+    const T cs13 = nt_scale<T>(nt_exp_hi(x[13]), fh);
+    const T cs14 = nt_scale<T>(nt_exp_hi(x[14]), fh);
+    const T cs17 = nt_scale<T>(nt_exp_hi(x[17]), fh);
+    const T cs18 = nt_scale<T>(nt_exp_hi(x[18]), fh);
+    const T cs19 = nt_scale<T>(nt_exp_hi(x[19]), fh);
+    const T cs21 = nt_scale<T>(nt_exp_hi(x[21]), fh);
+    const T cs25 = nt_scale<T>(nt_exp_hi(x[25]), fh);
+    const T cs26 = nt_scale<T>(nt_exp_hi(x[26]), fh);
+    const T cs27 = nt_scale<T>(nt_exp_hi(x[27]), fh);
+    const T cs28 = nt_scale<T>(nt_exp_hi(x[28]), fh);
+    const T cs29 = nt_scale<T>(nt_exp_hi(x[29]), fh);
+    const T cs33 = nt_scale<T>(nt_exp_hi(x[33]), fh);
+    const T cs36 = nt_scale<T>(nt_exp_hi(x[36]), fh);
+    const T cs39 = nt_scale<T>(nt_exp_hi(x[39]), fh);
+    const T cs42 = nt_scale<T>(nt_exp_hi(x[42]), fh);
+    const T cs43 = nt_scale<T>(nt_exp_hi(x[43]), fh);
+    const T cs44 = nt_scale<T>(nt_exp_hi(x[44]), fh);
+    const T cs45 = nt_scale<T>(nt_exp_hi(x[45]), fh);
+    const T cs46 = nt_scale<T>(nt_exp_hi(x[46]), fh);
+    const T cs47 = nt_scale<T>(nt_exp_hi(x[47]), fh);
+    const T cs48 = nt_scale<T>(nt_exp_hi(x[48]), fh);
+    const T cs49 = nt_scale<T>(nt_exp_hi(x[49]), fh);
+    const T cs50 = nt_scale<T>(nt_exp_hi(x[50]), fh);
+    const T cs51 = nt_scale<T>(nt_exp_hi(x[51]), fh);
+    const T cs52 = nt_scale<T>(nt_exp_hi(x[52]), fh);
+    const T cs53 = nt_scale<T>(nt_exp_hi(x[53]), fh);
+    const T cs54 = nt_scale<T>(nt_exp_hi(x[54]), fh);
+    const T cs55 = nt_scale<T>(nt_exp_hi(x[55]), fh);
+    const T cs56 = nt_scale<T>(nt_exp_hi(x[56]), fh);
     {  // row 5
     const T rs5 = nt_rscale<T>(nt_exp_hi(x[5]), fh);
-        const T nj5_c0 = F.dt*nt_cvt<T>(x[5]);
+        const T nj5_c0 = F.dt*xt5;
         const T nj5_c1 = F.dt*K[K_b12];
-        J[74] = (het[2]*nj5_c0) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs5);
-        J[72] = (F.dt*(F.hnm*K[K_b32] + het[2]*nt_cvt<T>(x[2]) + het[3]*nt_cvt<T>(x[12]) + tj[J_n2o5]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs5);
-        J[73] = (het[3]*nj5_c0) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs5);
-        J[75] = (-nj5_c1*nt_cvt<T>(x[54])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs5);
-        J[71] = (-nj5_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[54]), fh) * rs5);
+        J[74] = (het[2]*nj5_c0) * (cs2 * rs5);
+        J[72] = (F.dt*(F.hnm*K[K_b32] + het[2]*xt2 + het[3]*xt12 + tj[J_n2o5]) + T(1)) * (cs5 * rs5);
+        J[73] = (het[3]*nj5_c0) * (cs12 * rs5);
+        J[75] = (-nj5_c1*xt54) * (cs48 * rs5);
+        J[71] = (-nj5_c1*xt48) * (cs54 * rs5);
     }
     {  // row 8
     const T rs8 = nt_rscale<T>(nt_exp_hi(x[8]), fh);
         const T nj8_c0 = F.dt*K[K_a36];
-        J[160] = (nj8_c0*nt_cvt<T>(x[43]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[8]), fh) * rs8);
-        J[161] = (-F.dt*tj[J_ch2o_co]) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs8);
-        J[165] = (nj8_c0*nt_cvt<T>(x[8])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs8);
+        J[160] = (nj8_c0*xt43 + T(1)) * (cs8 * rs8);
+        J[161] = (-F.dt*tj[J_ch2o_co]) * (cs27 * rs8);
+        J[165] = (nj8_c0*xt8) * (cs43 * rs8);
         J[163] = T(0);
         J[162] = T(0);
         J[164] = T(0);
     }
     {  // row 13
     const T rs13 = nt_rscale<T>(nt_exp_hi(x[13]), fh);
-        const T nj13_c0 = F.dt*nt_cvt<T>(x[13]);
+        const T nj13_c0 = F.dt*xt13;
         const T nj13_c1 = F.dt*K[K_d31];
-        J[89] = (het[0]*nj13_c0) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs13);
-        J[88] = (het[1]*nj13_c0) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs13);
-        J[87] = (F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]) + tj[J_clono2_cl] + tj[J_clono2_clo]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs13);
-        J[91] = (K[K_d32]*nj13_c0) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs13);
-        J[90] = (-nj13_c1*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs13);
-        J[92] = (-nj13_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs13);
+        J[89] = (het[0]*nj13_c0) * (cs2 * rs13);
+        J[88] = (het[1]*nj13_c0) * (cs12 * rs13);
+        J[87] = (F.dt*(K[K_d32]*xt45 + het[0]*xt2 + het[1]*xt12 + tj[J_clono2_cl] + tj[J_clono2_clo]) + T(1)) * (cs13 * rs13);
+        J[91] = (K[K_d32]*nj13_c0) * (cs45 * rs13);
+        J[90] = (-nj13_c1*xt52) * (cs48 * rs13);
+        J[92] = (-nj13_c1*xt48) * (cs52 * rs13);
     }
     {  // row 17
     const T rs17 = nt_rscale<T>(nt_exp_hi(x[17]), fh);
         const T nj17_c0 = F.dt*het[3];
         const T nj17_c1 = F.dt*K[K_d36];
-        J[26] = (-nj17_c0*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs17);
-        J[27] = (-nj17_c0*nt_cvt<T>(x[5])) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs17);
-        J[25] = (F.dt*tj[J_clno2] + T(1)) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs17);
-        J[29] = (-nj17_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs17);
-        J[28] = (-nj17_c1*nt_cvt<T>(x[44])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs17);
+        J[26] = (-nj17_c0*xt12) * (cs5 * rs17);
+        J[27] = (-nj17_c0*xt5) * (cs12 * rs17);
+        J[25] = (F.dt*tj[J_clno2] + T(1)) * (cs17 * rs17);
+        J[29] = (-nj17_c1*xt48) * (cs44 * rs17);
+        J[28] = (-nj17_c1*xt44) * (cs48 * rs17);
     }
     {  // row 18
     const T rs18 = nt_rscale<T>(nt_exp_hi(x[18]), fh);
-        const T nj18_c0 = F.dt*nt_cvt<T>(x[18]);
-        const T nj18_c1 = F.dt*nt_cvt<T>(x[50]);
+        const T nj18_c0 = F.dt*xt18;
+        const T nj18_c1 = F.dt*xt50;
         const T nj18_c2 = F.parthbr*nj18_c0;
-        J[183] = (het[8]*nj18_c0) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs18);
-        J[184] = (F.dt*(F.parthbr*(K[K_e11]*nt_cvt<T>(x[43]) + K[K_e9]*nt_cvt<T>(x[42]) + tj[J_hbr]) + F.rain_hbr + het[7]*nt_cvt<T>(x[25]) + het[8]*nt_cvt<T>(x[14])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs18);
-        J[181] = (het[7]*nj18_c0) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs18);
-        J[185] = (-K[K_c19]*nj18_c1) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs18);
-        J[182] = (K[K_e9]*nj18_c2) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs18);
-        J[187] = (K[K_e11]*nj18_c2) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs18);
-        J[188] = (-K[K_e7]*nj18_c1) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs18);
-        J[186] = (-F.dt*(K[K_c19]*nt_cvt<T>(x[27]) + K[K_e7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs18);
+        J[183] = (het[8]*nj18_c0) * (cs14 * rs18);
+        J[184] = (F.dt*(F.parthbr*(K[K_e11]*xt43 + K[K_e9]*xt42 + tj[J_hbr]) + F.rain_hbr + het[7]*xt25 + het[8]*xt14) + T(1)) * (cs18 * rs18);
+        J[181] = (het[7]*nj18_c0) * (cs25 * rs18);
+        J[185] = (-K[K_c19]*nj18_c1) * (cs27 * rs18);
+        J[182] = (K[K_e9]*nj18_c2) * (cs42 * rs18);
+        J[187] = (K[K_e11]*nj18_c2) * (cs43 * rs18);
+        J[188] = (-K[K_e7]*nj18_c1) * (cs47 * rs18);
+        J[186] = (-F.dt*(K[K_c19]*xt27 + K[K_e7]*xt47)) * (cs50 * rs18);
     }
     {  // row 20
     const T rs20 = nt_rscale<T>(nt_exp_hi(x[20]), fh);
         const T nj20_c0 = T(2)*F.dt;
         const T nj20_c1 = K[K_b39]*nj20_c0;
         const T nj20_c2 = F.parthno3*K[K_b27];
-        const T nj20_c3 = F.dt*nt_cvt<T>(x[48]);
+        const T nj20_c3 = F.dt*xt48;
         const T nj20_c4 = T(2)*K[K_b12];
         const T nj20_c5 = K[K_b6]*nj20_c0;
-        J[233] = (-nj20_c1*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[0]), fh) * rs20);
-        J[237] = (-F.dt*(F.parthno3*tj[J_hno3] + nj20_c2*nt_cvt<T>(x[43]))) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs20);
-        J[232] = (-F.dt*(T(2)*F.hnm*K[K_b32] + T(2)*tj[J_n2o5])) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs20);
-        J[235] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[45]) + tj[J_clono2_cl] + tj[J_clono2_clo])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs20);
-        J[229] = (-F.dt*tj[J_clno2]) * (nt_scale<T>(nt_exp_hi(x[17]), fh) * rs20);
-        J[230] = (-F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + tj[J_brono2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs20);
-        J[238] = (-F.dt*(F.hnm*K[K_b24] + K[K_b28]*nt_cvt<T>(x[43]) + tj[J_hno4])) * (nt_scale<T>(nt_exp_hi(x[21]), fh) * rs20);
-        J[236] = (-nj20_c1*nt_cvt<T>(x[0])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs20);
-        J[243] = (-F.dt*(K[K_b28]*nt_cvt<T>(x[21]) + nj20_c2*nt_cvt<T>(x[4])) + K[K_b22]*nj20_c3) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs20);
-        J[241] = (K[K_d36]*nj20_c3) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs20);
-        J[240] = (-F.dt*(K[K_d32]*nt_cvt<T>(x[13]) + K[K_e8]*nt_cvt<T>(x[19]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs20);
-        J[244] = (K[K_b23]*nj20_c3) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs20);
-        J[239] = (F.dt*(K[K_b22]*nt_cvt<T>(x[43]) + K[K_b23]*nt_cvt<T>(x[47]) + K[K_d31]*nt_cvt<T>(x[52]) + K[K_d36]*nt_cvt<T>(x[44]) + K[K_e13]*nt_cvt<T>(x[53]) + nj20_c4*nt_cvt<T>(x[54]))) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs20);
-        J[245] = (nj20_c5*nt_cvt<T>(x[51])) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs20);
-        J[234] = (nj20_c5*nt_cvt<T>(x[49])) * (nt_scale<T>(nt_exp_hi(x[51]), fh) * rs20);
-        J[246] = (K[K_d31]*nj20_c3) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs20);
-        J[242] = (K[K_e13]*nj20_c3) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs20);
-        J[231] = (nj20_c3*nj20_c4) * (nt_scale<T>(nt_exp_hi(x[54]), fh) * rs20);
+        J[233] = (-nj20_c1*xt42) * (cs0 * rs20);
+        J[237] = (-F.dt*(F.parthno3*tj[J_hno3] + nj20_c2*xt43)) * (cs4 * rs20);
+        J[232] = (-F.dt*(T(2)*F.hnm*K[K_b32] + T(2)*tj[J_n2o5])) * (cs5 * rs20);
+        J[235] = (-F.dt*(K[K_d32]*xt45 + tj[J_clono2_cl] + tj[J_clono2_clo])) * (cs13 * rs20);
+        J[229] = (-F.dt*tj[J_clno2]) * (cs17 * rs20);
+        J[230] = (-F.dt*(K[K_e8]*xt45 + tj[J_brono2])) * (cs19 * rs20);
+        J[238] = (-F.dt*(F.hnm*K[K_b24] + K[K_b28]*xt43 + tj[J_hno4])) * (cs21 * rs20);
+        J[236] = (-nj20_c1*xt0) * (cs42 * rs20);
+        J[243] = (-F.dt*(K[K_b28]*xt21 + nj20_c2*xt4) + K[K_b22]*nj20_c3) * (cs43 * rs20);
+        J[241] = (K[K_d36]*nj20_c3) * (cs44 * rs20);
+        J[240] = (-F.dt*(K[K_d32]*xt13 + K[K_e8]*xt19)) * (cs45 * rs20);
+        J[244] = (K[K_b23]*nj20_c3) * (cs47 * rs20);
+        J[239] = (F.dt*(K[K_b22]*xt43 + K[K_b23]*xt47 + K[K_d31]*xt52 + K[K_d36]*xt44 + K[K_e13]*xt53 + nj20_c4*xt54)) * (cs48 * rs20);
+        J[245] = (nj20_c5*xt51) * (cs49 * rs20);
+        J[234] = (nj20_c5*xt49) * (cs51 * rs20);
+        J[246] = (K[K_d31]*nj20_c3) * (cs52 * rs20);
+        J[242] = (K[K_e13]*nj20_c3) * (cs53 * rs20);
+        J[231] = (nj20_c3*nj20_c4) * (cs54 * rs20);
     }
     {  // row 23
     const T rs23 = nt_rscale<T>(nt_exp_hi(x[23]), fh);
         const T nj23_c0 = T(2)*het[7];
-        const T nj23_c1 = F.dt*F.parthbr*nt_cvt<T>(x[18]);
-        const T nj23_c2 = F.dt*nt_cvt<T>(x[53]);
-        J[196] = (-F.dt*(F.parthbr*(K[K_e11]*nt_cvt<T>(x[43]) + K[K_e9]*nt_cvt<T>(x[42]) + tj[J_hbr]) + nj23_c0*nt_cvt<T>(x[25]))) * (nt_scale<T>(nt_exp_hi(x[18]), fh) * rs23);
-        J[193] = (-F.dt*(K[K_e8]*nt_cvt<T>(x[45]) + tj[J_brono2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs23);
-        J[194] = (-F.dt*(K[K_e16]*nt_cvt<T>(x[45]) + nj23_c0*nt_cvt<T>(x[18]) + tj[J_hobr])) * (nt_scale<T>(nt_exp_hi(x[25]), fh) * rs23);
-        J[192] = (-F.dt*tj[J_brcl]) * (nt_scale<T>(nt_exp_hi(x[26]), fh) * rs23);
-        J[197] = (F.dt*K[K_c19]*nt_cvt<T>(x[50])) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs23);
-        J[195] = (-K[K_e9]*nj23_c1) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs23);
-        J[202] = (-K[K_e11]*nj23_c1) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs23);
-        J[199] = (-F.dt*(K[K_e16]*nt_cvt<T>(x[25]) + K[K_e8]*nt_cvt<T>(x[19]))) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs23);
-        J[203] = (F.dt*(K[K_e15]*nt_cvt<T>(x[53]) + K[K_e7]*nt_cvt<T>(x[50]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs23);
-        J[198] = (K[K_e13]*nj23_c2) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs23);
-        J[201] = (F.dt*(K[K_c19]*nt_cvt<T>(x[27]) + K[K_e7]*nt_cvt<T>(x[47]))) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs23);
-        J[204] = (K[K_e5c]*nj23_c2) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs23);
-        J[200] = (F.dt*(K[K_e13]*nt_cvt<T>(x[48]) + K[K_e15]*nt_cvt<T>(x[47]) + K[K_e5c]*nt_cvt<T>(x[52]))) * (nt_scale<T>(nt_exp_hi(x[53]), fh) * rs23);
+        const T nj23_c1 = F.dt*F.parthbr*xt18;
+        const T nj23_c2 = F.dt*xt53;
+        J[196] = (-F.dt*(F.parthbr*(K[K_e11]*xt43 + K[K_e9]*xt42 + tj[J_hbr]) + nj23_c0*xt25)) * (cs18 * rs23);
+        J[193] = (-F.dt*(K[K_e8]*xt45 + tj[J_brono2])) * (cs19 * rs23);
+        J[194] = (-F.dt*(K[K_e16]*xt45 + nj23_c0*xt18 + tj[J_hobr])) * (cs25 * rs23);
+        J[192] = (-F.dt*tj[J_brcl]) * (cs26 * rs23);
+        J[197] = (F.dt*K[K_c19]*xt50) * (cs27 * rs23);
+        J[195] = (-K[K_e9]*nj23_c1) * (cs42 * rs23);
+        J[202] = (-K[K_e11]*nj23_c1) * (cs43 * rs23);
+        J[199] = (-F.dt*(K[K_e16]*xt25 + K[K_e8]*xt19)) * (cs45 * rs23);
+        J[203] = (F.dt*(K[K_e15]*xt53 + K[K_e7]*xt50)) * (cs47 * rs23);
+        J[198] = (K[K_e13]*nj23_c2) * (cs48 * rs23);
+        J[201] = (F.dt*(K[K_c19]*xt27 + K[K_e7]*xt47)) * (cs50 * rs23);
+        J[204] = (K[K_e5c]*nj23_c2) * (cs52 * rs23);
+        J[200] = (F.dt*(K[K_e13]*xt48 + K[K_e15]*xt47 + K[K_e5c]*xt52)) * (cs53 * rs23);
     }
     {  // row 27
     const T rs27 = nt_rscale<T>(nt_exp_hi(x[27]), fh);
         const T nj27_c0 = F.dt*K[K_c1c];
         const T nj27_c1 = F.dt*K[K_c17b];
-        const T nj27_c2 = F.dt*nt_cvt<T>(x[27]);
+        const T nj27_c2 = F.dt*xt27;
         const T nj27_c3 = F.dt*K[K_c3];
-        J[219] = (-nj27_c0*nt_cvt<T>(x[42])) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs27);
-        J[222] = (F.dt*(K[K_c10]*nt_cvt<T>(x[44]) + K[K_c19]*nt_cvt<T>(x[50]) + K[K_c8]*nt_cvt<T>(x[43]) + K[K_c9]*nt_cvt<T>(x[45]) + tj[J_ch2o_co] + tj[J_ch2o_hco]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs27);
+        J[219] = (-nj27_c0*xt42) * (cs1 * rs27);
+        J[222] = (F.dt*(K[K_c10]*xt44 + K[K_c19]*xt50 + K[K_c8]*xt43 + K[K_c9]*xt45 + tj[J_ch2o_co] + tj[J_ch2o_hco]) + T(1)) * (cs27 * rs27);
         J[221] = T(0);
-        J[217] = (-nj27_c1*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs27);
-        J[218] = (-nj27_c0*nt_cvt<T>(x[1])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs27);
-        J[226] = (F.dt*K[K_c8]*nt_cvt<T>(x[27]) - nj27_c1*nt_cvt<T>(x[29])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs27);
-        J[224] = (K[K_c10]*nj27_c2) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs27);
-        J[223] = (F.dt*K[K_c9]*nt_cvt<T>(x[27]) - nj27_c3*nt_cvt<T>(x[56])) * (nt_scale<T>(nt_exp_hi(x[45]), fh) * rs27);
+        J[217] = (-nj27_c1*xt43) * (cs29 * rs27);
+        J[218] = (-nj27_c0*xt1) * (cs42 * rs27);
+        J[226] = (F.dt*K[K_c8]*xt27 - nj27_c1*xt29) * (cs43 * rs27);
+        J[224] = (K[K_c10]*nj27_c2) * (cs44 * rs27);
+        J[223] = (F.dt*K[K_c9]*xt27 - nj27_c3*xt56) * (cs45 * rs27);
         J[227] = T(0);
-        J[225] = (K[K_c19]*nj27_c2) * (nt_scale<T>(nt_exp_hi(x[50]), fh) * rs27);
+        J[225] = (K[K_c19]*nj27_c2) * (cs50 * rs27);
         J[228] = T(0);
-        J[220] = (-nj27_c3*nt_cvt<T>(x[45])) * (nt_scale<T>(nt_exp_hi(x[56]), fh) * rs27);
+        J[220] = (-nj27_c3*xt45) * (cs56 * rs27);
     }
     {  // row 33
     const T rs33 = nt_rscale<T>(nt_exp_hi(x[33]), fh);
-        J[32] = (F.dt*(K[K_d93]*nt_cvt<T>(x[42]) + tj[J_ccl4]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs33);
-        J[33] = (F.dt*K[K_d93]*nt_cvt<T>(x[33])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs33);
+        J[32] = (F.dt*(K[K_d93]*xt42 + tj[J_ccl4]) + T(1)) * (cs33 * rs33);
+        J[33] = (F.dt*K[K_d93]*xt33) * (cs42 * rs33);
     }
     {  // row 36
     const T rs36 = nt_rscale<T>(nt_exp_hi(x[36]), fh);
-        const T nj36_c0 = F.dt*nt_cvt<T>(x[36]);
-        J[38] = (F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs36);
-        J[39] = (K[K_d96]*nj36_c0) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs36);
-        J[40] = (K[K_d97]*nj36_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs36);
+        const T nj36_c0 = F.dt*xt36;
+        J[38] = (F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22]) + T(1)) * (cs36 * rs36);
+        J[39] = (K[K_d96]*nj36_c0) * (cs42 * rs36);
+        J[40] = (K[K_d97]*nj36_c0) * (cs43 * rs36);
     }
     {  // row 39
     const T rs39 = nt_rscale<T>(nt_exp_hi(x[39]), fh);
-        J[50] = (F.dt*(K[K_e53]*nt_cvt<T>(x[42]) + tj[J_h1301]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[39]), fh) * rs39);
-        J[51] = (F.dt*K[K_e53]*nt_cvt<T>(x[39])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs39);
+        J[50] = (F.dt*(K[K_e53]*xt42 + tj[J_h1301]) + T(1)) * (cs39 * rs39);
+        J[51] = (F.dt*K[K_e53]*xt39) * (cs42 * rs39);
     }
     {  // row 42
     const T rs42 = nt_rscale<T>(nt_exp_hi(x[42]), fh);
@@ -5683,118 +6980,212 @@ __device__ __forceinline__ void nt_residual_night_w4_3(const FF& F, PK K, PK tj,
 template <typename T, typename FF, typename PK, typename PJ>
 __device__ __forceinline__ void nt_jacobian_night_w4_3(const FF& F, PK K, PK tj, PK het, const double* __restrict__ x, double floor_, PJ J) {
     const int fh = nt_exp_hi(floor_);
+    const T xt0 = nt_cvt<T>(x[0]);
+    const T xt1 = nt_cvt<T>(x[1]);
+    const T xt2 = nt_cvt<T>(x[2]);
+    const T xt3 = nt_cvt<T>(x[3]);
+    const T xt4 = nt_cvt<T>(x[4]);
+    const T xt5 = nt_cvt<T>(x[5]);
+    const T xt6 = nt_cvt<T>(x[6]);
+    const T xt7 = nt_cvt<T>(x[7]);
+    const T xt8 = nt_cvt<T>(x[8]);
+    const T xt9 = nt_cvt<T>(x[9]);
+    const T xt10 = nt_cvt<T>(x[10]);
+    const T xt11 = nt_cvt<T>(x[11]);
+    const T xt12 = nt_cvt<T>(x[12]);
+    const T xt13 = nt_cvt<T>(x[13]);
+    const T xt14 = nt_cvt<T>(x[14]);
+    const T xt15 = nt_cvt<T>(x[15]);
+    const T xt16 = nt_cvt<T>(x[16]);
+    const T xt17 = nt_cvt<T>(x[17]);
+    const T xt18 = nt_cvt<T>(x[18]);
+    const T xt19 = nt_cvt<T>(x[19]);
+    const T xt20 = nt_cvt<T>(x[20]);
+    const T xt21 = nt_cvt<T>(x[21]);
+    const T xt22 = nt_cvt<T>(x[22]);
+    const T xt23 = nt_cvt<T>(x[23]);
+    const T xt24 = nt_cvt<T>(x[24]);
+    const T xt25 = nt_cvt<T>(x[25]);
+    const T xt26 = nt_cvt<T>(x[26]);
+    const T xt27 = nt_cvt<T>(x[27]);
+    const T xt28 = nt_cvt<T>(x[28]);
+    const T xt29 = nt_cvt<T>(x[29]);
+    const T xt30 = nt_cvt<T>(x[30]);
+    const T xt31 = nt_cvt<T>(x[31]);
+    const T xt32 = nt_cvt<T>(x[32]);
+    const T xt33 = nt_cvt<T>(x[33]);
+    const T xt34 = nt_cvt<T>(x[34]);
+    const T xt35 = nt_cvt<T>(x[35]);
+    const T xt36 = nt_cvt<T>(x[36]);
+    const T xt37 = nt_cvt<T>(x[37]);
+    const T xt38 = nt_cvt<T>(x[38]);
+    const T xt39 = nt_cvt<T>(x[39]);
+    const T xt40 = nt_cvt<T>(x[40]);
+    const T xt41 = nt_cvt<T>(x[41]);
+    const T xt42 = nt_cvt<T>(x[42]);
+    const T xt43 = nt_cvt<T>(x[43]);
+    const T xt44 = nt_cvt<T>(x[44]);
+    const T xt45 = nt_cvt<T>(x[45]);
+    const T xt46 = nt_cvt<T>(x[46]);
+    const T xt47 = nt_cvt<T>(x[47]);
+    const T xt48 = nt_cvt<T>(x[48]);
+    const T xt49 = nt_cvt<T>(x[49]);
+    const T xt50 = nt_cvt<T>(x[50]);
+    const T xt51 = nt_cvt<T>(x[51]);
+    const T xt52 = nt_cvt<T>(x[52]);
+    const T xt53 = nt_cvt<T>(x[53]);
+    const T xt54 = nt_cvt<T>(x[54]);
+    const T xt55 = nt_cvt<T>(x[55]);
+    const T xt56 = nt_cvt<T>(x[56]);
+    const T cs1 = nt_scale<T>(nt_exp_hi(x[1]), fh);
+    const T cs2 = nt_scale<T>(nt_exp_hi(x[2]), fh);
+    const T cs4 = nt_scale<T>(nt_exp_hi(x[4]), fh);
+    const T cs5 = nt_scale<T>(nt_exp_hi(x[5]), fh);
+    const T cs7 = nt_scale<T>(nt_exp_hi(x[7]), fh);
+    const T cs8 = nt_scale<T>(nt_exp_hi(x[8]), fh);
+    const T cs12 = nt_scale<T>(nt_exp_hi(x[12]), fh);
+    const T cs13 = nt_scale<T>(nt_exp_hi(x[13]), fh);
+    const T cs14 = nt_scale<T>(nt_exp_hi(x[14]), fh);
+    const T cs15 = nt_scale<T>(nt_exp_hi(x[15]), fh);
+    const T cs16 = nt_scale<T>(nt_exp_hi(x[16]), fh);
+    const T cs19 = nt_scale<T>(nt_exp_hi(x[19]), fh);
+    const T cs27 = nt_scale<T>(nt_exp_hi(x[27]), fh);
+    const T cs28 = nt_scale<T>(nt_exp_hi(x[28]), fh);
+    const T cs29 = nt_scale<T>(nt_exp_hi(x[29]), fh);
+    const T cs30 = nt_scale<T>(nt_exp_hi(x[30]), fh);
+    const T cs31 = nt_scale<T>(nt_exp_hi(x[31]), fh);
+    const T cs32 = nt_scale<T>(nt_exp_hi(x[32]), fh);
+    const T cs33 = nt_scale<T>(nt_exp_hi(x[33]), fh);
+    const T cs34 = nt_scale<T>(nt_exp_hi(x[34]), fh);
+    const T cs35 = nt_scale<T>(nt_exp_hi(x[35]), fh);
+    const T cs36 = nt_scale<T>(nt_exp_hi(x[36]), fh);
+    const T cs37 = nt_scale<T>(nt_exp_hi(x[37]), fh);
+    const T cs38 = nt_scale<T>(nt_exp_hi(x[38]), fh);
+    const T cs42 = nt_scale<T>(nt_exp_hi(x[42]), fh);
+    const T cs43 = nt_scale<T>(nt_exp_hi(x[43]), fh);
+    const T cs44 = nt_scale<T>(nt_exp_hi(x[44]), fh);
+    const T cs45 = nt_scale<T>(nt_exp_hi(x[45]), fh);
+    const T cs46 = nt_scale<T>(nt_exp_hi(x[46]), fh);
+    const T cs47 = nt_scale<T>(nt_exp_hi(x[47]), fh);
+    const T cs48 = nt_scale<T>(nt_exp_hi(x[48]), fh);
+    const T cs49 = nt_scale<T>(nt_exp_hi(x[49]), fh);
+    const T cs50 = nt_scale<T>(nt_exp_hi(x[50]), fh);
+    const T cs52 = nt_scale<T>(nt_exp_hi(x[52]), fh);
+    const T cs53 = nt_scale<T>(nt_exp_hi(x[53]), fh);
+    const T cs55 = nt_scale<T>(nt_exp_hi(x[55]), fh);
+    const T cs56 = nt_scale<T>(nt_exp_hi(x[56]), fh);
     {  // row 1
     const T rs1 = nt_rscale<T>(nt_exp_hi(x[1]), fh);
-        const T nj1_c0 = F.dt*nt_cvt<T>(x[1]);
-        J[157] = (F.dt*(K[K_c1a]*nt_cvt<T>(x[42]) + K[K_c1b]*nt_cvt<T>(x[42]) + K[K_c1c]*nt_cvt<T>(x[42]) + K[K_c2]*nt_cvt<T>(x[43]) + K[K_d5]*nt_cvt<T>(x[44])) + T(1)) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs1);
-        J[156] = (nj1_c0*(K[K_c1a] + K[K_c1b] + K[K_c1c])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs1);
-        J[159] = (K[K_c2]*nj1_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs1);
-        J[158] = (K[K_d5]*nj1_c0) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs1);
+        const T nj1_c0 = F.dt*xt1;
+        J[157] = (F.dt*(K[K_c1a]*xt42 + K[K_c1b]*xt42 + K[K_c1c]*xt42 + K[K_c2]*xt43 + K[K_d5]*xt44) + T(1)) * (cs1 * rs1);
+        J[156] = (nj1_c0*(K[K_c1a] + K[K_c1b] + K[K_c1c])) * (cs42 * rs1);
+        J[159] = (K[K_c2]*nj1_c0) * (cs43 * rs1);
+        J[158] = (K[K_d5]*nj1_c0) * (cs44 * rs1);
     }
     {  // row 2
     const T rs2 = nt_rscale<T>(nt_exp_hi(x[2]), fh);
-        const T nj2_c0 = F.dt*nt_cvt<T>(x[43]);
+        const T nj2_c0 = F.dt*xt43;
         const T nj2_c1 = F.dt*F.parth2o;
         const T nj2_c2 = F.parthno3*K[K_b27];
         const T nj2_c3 = F.parthcl*K[K_d11];
-        J[261] = (-K[K_c2]*nj2_c0) * (nt_scale<T>(nt_exp_hi(x[1]), fh) * rs2);
-        J[266] = (nj2_c1*(K[K_a1et]*nt_cvt<T>(x[42]) + tj[J_h2o]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs2);
-        J[260] = (-nj2_c0*nj2_c2) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs2);
-        J[265] = (-nj2_c0*nj2_c3) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs2);
-        J[262] = (-K[K_a30]*nj2_c0) * (nt_scale<T>(nt_exp_hi(x[16]), fh) * rs2);
-        J[264] = (-K[K_c8]*nj2_c0) * (nt_scale<T>(nt_exp_hi(x[27]), fh) * rs2);
-        J[258] = (-F.dt*(K[K_c17a]*nt_cvt<T>(x[43]) + K[K_c17b]*nt_cvt<T>(x[43]))) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs2);
-        J[259] = (K[K_a1et]*nj2_c1*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs2);
-        J[267] = (-F.dt*(F.h2*K[K_a19] + K[K_a17]*nt_cvt<T>(x[47]) + K[K_a30]*nt_cvt<T>(x[16]) + T(2)*K[K_a31]*nt_cvt<T>(x[43]) + K[K_c17a]*nt_cvt<T>(x[29]) + K[K_c17b]*nt_cvt<T>(x[29]) + K[K_c2]*nt_cvt<T>(x[1]) + K[K_c8]*nt_cvt<T>(x[27]) + nj2_c2*nt_cvt<T>(x[4]) + nj2_c3*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs2);
-        J[268] = (-F.dt*(K[K_a17]*nt_cvt<T>(x[43]) + T(1.6e-12)*nt_cvt<T>(x[55]))) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs2);
-        J[263] = (-T(1.6e-12)*F.dt*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[55]), fh) * rs2);
+        J[261] = (-K[K_c2]*nj2_c0) * (cs1 * rs2);
+        J[266] = (nj2_c1*(K[K_a1et]*xt42 + tj[J_h2o]) + T(1)) * (cs2 * rs2);
+        J[260] = (-nj2_c0*nj2_c2) * (cs4 * rs2);
+        J[265] = (-nj2_c0*nj2_c3) * (cs12 * rs2);
+        J[262] = (-K[K_a30]*nj2_c0) * (cs16 * rs2);
+        J[264] = (-K[K_c8]*nj2_c0) * (cs27 * rs2);
+        J[258] = (-F.dt*(K[K_c17a]*xt43 + K[K_c17b]*xt43)) * (cs29 * rs2);
+        J[259] = (K[K_a1et]*nj2_c1*xt2) * (cs42 * rs2);
+        J[267] = (-F.dt*(F.h2*K[K_a19] + K[K_a17]*xt47 + K[K_a30]*xt16 + T(2)*K[K_a31]*xt43 + K[K_c17a]*xt29 + K[K_c17b]*xt29 + K[K_c2]*xt1 + K[K_c8]*xt27 + nj2_c2*xt4 + nj2_c3*xt12)) * (cs43 * rs2);
+        J[268] = (-F.dt*(K[K_a17]*xt43 + T(1.6e-12)*xt55)) * (cs47 * rs2);
+        J[263] = (-T(1.6e-12)*F.dt*xt47) * (cs55 * rs2);
     }
     {  // row 4
     const T rs4 = nt_rscale<T>(nt_exp_hi(x[4]), fh);
         const T nj4_c0 = T(2)*het[2];
         const T nj4_c1 = F.dt*K[K_b22];
-        J[122] = (-F.dt*(het[0]*nt_cvt<T>(x[13]) + het[5]*nt_cvt<T>(x[19]) + nj4_c0*nt_cvt<T>(x[5]))) * (nt_scale<T>(nt_exp_hi(x[2]), fh) * rs4);
-        J[120] = (F.dt*(F.parthno3*(K[K_b27]*nt_cvt<T>(x[43]) + tj[J_hno3]) + F.rain_hno3) + T(1)) * (nt_scale<T>(nt_exp_hi(x[4]), fh) * rs4);
-        J[118] = (-F.dt*(het[3]*nt_cvt<T>(x[12]) + nj4_c0*nt_cvt<T>(x[2]))) * (nt_scale<T>(nt_exp_hi(x[5]), fh) * rs4);
-        J[121] = (-F.dt*(het[1]*nt_cvt<T>(x[13]) + het[3]*nt_cvt<T>(x[5]))) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs4);
-        J[119] = (-F.dt*(het[0]*nt_cvt<T>(x[2]) + het[1]*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs4);
-        J[117] = (-F.dt*het[5]*nt_cvt<T>(x[2])) * (nt_scale<T>(nt_exp_hi(x[19]), fh) * rs4);
-        J[124] = (F.dt*F.parthno3*K[K_b27]*nt_cvt<T>(x[4]) - nj4_c1*nt_cvt<T>(x[48])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs4);
-        J[123] = (-nj4_c1*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[48]), fh) * rs4);
+        J[122] = (-F.dt*(het[0]*xt13 + het[5]*xt19 + nj4_c0*xt5)) * (cs2 * rs4);
+        J[120] = (F.dt*(F.parthno3*(K[K_b27]*xt43 + tj[J_hno3]) + F.rain_hno3) + T(1)) * (cs4 * rs4);
+        J[118] = (-F.dt*(het[3]*xt12 + nj4_c0*xt2)) * (cs5 * rs4);
+        J[121] = (-F.dt*(het[1]*xt13 + het[3]*xt5)) * (cs12 * rs4);
+        J[119] = (-F.dt*(het[0]*xt2 + het[1]*xt12)) * (cs13 * rs4);
+        J[117] = (-F.dt*het[5]*xt2) * (cs19 * rs4);
+        J[124] = (F.dt*F.parthno3*K[K_b27]*xt4 - nj4_c1*xt48) * (cs43 * rs4);
+        J[123] = (-nj4_c1*xt43) * (cs48 * rs4);
     }
     {  // row 6
     const T rs6 = nt_rscale<T>(nt_exp_hi(x[6]), fh);
-        const T nj6_c0 = T(3)*nt_cvt<T>(x[42]);
+        const T nj6_c0 = T(3)*xt42;
         const T nj6_c1 = T(2)*K[K_d91];
         const T nj6_c2 = T(4)*K[K_d93];
         const T nj6_c3 = T(3)*K[K_d94];
-        J[9] = (F.dt*F.rain_hcl) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs6);
-        J[7] = (-F.dt*(K[K_d90]*nj6_c0 + T(3)*tj[J_cfc11])) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs6);
-        J[4] = (-F.dt*(nj6_c1*nt_cvt<T>(x[42]) + T(2)*tj[J_cfc12])) * (nt_scale<T>(nt_exp_hi(x[31]), fh) * rs6);
-        J[0] = (-F.dt*(K[K_d92]*nj6_c0 + T(3)*tj[J_cfc113])) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs6);
-        J[2] = (-F.dt*(nj6_c2*nt_cvt<T>(x[42]) + T(4)*tj[J_ccl4])) * (nt_scale<T>(nt_exp_hi(x[33]), fh) * rs6);
-        J[6] = (-F.dt*(nj6_c3*nt_cvt<T>(x[43]) + T(3)*tj[J_ch3ccl3])) * (nt_scale<T>(nt_exp_hi(x[34]), fh) * rs6);
-        J[5] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[43]) + tj[J_ch3cl])) * (nt_scale<T>(nt_exp_hi(x[35]), fh) * rs6);
-        J[3] = (-F.dt*(K[K_d96]*nt_cvt<T>(x[42]) + K[K_d97]*nt_cvt<T>(x[43]) + tj[J_hcfc22])) * (nt_scale<T>(nt_exp_hi(x[36]), fh) * rs6);
-        J[1] = (-F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211])) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs6);
-        J[8] = (-F.dt*(T(3)*K[K_d90]*nt_cvt<T>(x[30]) + T(3)*K[K_d92]*nt_cvt<T>(x[32]) + K[K_d96]*nt_cvt<T>(x[36]) + K[K_e52]*nt_cvt<T>(x[38]) + nj6_c1*nt_cvt<T>(x[31]) + nj6_c2*nt_cvt<T>(x[33]))) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs6);
-        J[10] = (-F.dt*(K[K_d95]*nt_cvt<T>(x[35]) + K[K_d97]*nt_cvt<T>(x[36]) + nj6_c3*nt_cvt<T>(x[34]))) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs6);
+        J[9] = (F.dt*F.rain_hcl) * (cs12 * rs6);
+        J[7] = (-F.dt*(K[K_d90]*nj6_c0 + T(3)*tj[J_cfc11])) * (cs30 * rs6);
+        J[4] = (-F.dt*(nj6_c1*xt42 + T(2)*tj[J_cfc12])) * (cs31 * rs6);
+        J[0] = (-F.dt*(K[K_d92]*nj6_c0 + T(3)*tj[J_cfc113])) * (cs32 * rs6);
+        J[2] = (-F.dt*(nj6_c2*xt42 + T(4)*tj[J_ccl4])) * (cs33 * rs6);
+        J[6] = (-F.dt*(nj6_c3*xt43 + T(3)*tj[J_ch3ccl3])) * (cs34 * rs6);
+        J[5] = (-F.dt*(K[K_d95]*xt43 + tj[J_ch3cl])) * (cs35 * rs6);
+        J[3] = (-F.dt*(K[K_d96]*xt42 + K[K_d97]*xt43 + tj[J_hcfc22])) * (cs36 * rs6);
+        J[1] = (-F.dt*(K[K_e52]*xt42 + tj[J_h1211])) * (cs38 * rs6);
+        J[8] = (-F.dt*(T(3)*K[K_d90]*xt30 + T(3)*K[K_d92]*xt32 + K[K_d96]*xt36 + K[K_e52]*xt38 + nj6_c1*xt31 + nj6_c2*xt33)) * (cs42 * rs6);
+        J[10] = (-F.dt*(K[K_d95]*xt35 + K[K_d97]*xt36 + nj6_c3*xt34)) * (cs43 * rs6);
     }
     {  // row 15
     const T rs15 = nt_rscale<T>(nt_exp_hi(x[15]), fh);
-        J[63] = (-F.dt*(het[1]*nt_cvt<T>(x[13]) + het[4]*nt_cvt<T>(x[14]))) * (nt_scale<T>(nt_exp_hi(x[12]), fh) * rs15);
-        J[61] = (-F.dt*het[1]*nt_cvt<T>(x[12])) * (nt_scale<T>(nt_exp_hi(x[13]), fh) * rs15);
-        J[62] = (-F.dt*(K[K_d37]*nt_cvt<T>(x[44]) + het[4]*nt_cvt<T>(x[12]))) * (nt_scale<T>(nt_exp_hi(x[14]), fh) * rs15);
-        J[60] = (F.dt*tj[J_cl2] + T(1)) * (nt_scale<T>(nt_exp_hi(x[15]), fh) * rs15);
-        J[64] = (-F.dt*K[K_d37]*nt_cvt<T>(x[14])) * (nt_scale<T>(nt_exp_hi(x[44]), fh) * rs15);
-        J[65] = (-T(2)*F.dt*K[K_d62]*nt_cvt<T>(x[52])) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs15);
+        J[63] = (-F.dt*(het[1]*xt13 + het[4]*xt14)) * (cs12 * rs15);
+        J[61] = (-F.dt*het[1]*xt12) * (cs13 * rs15);
+        J[62] = (-F.dt*(K[K_d37]*xt44 + het[4]*xt12)) * (cs14 * rs15);
+        J[60] = (F.dt*tj[J_cl2] + T(1)) * (cs15 * rs15);
+        J[64] = (-F.dt*K[K_d37]*xt14) * (cs44 * rs15);
+        J[65] = (-T(2)*F.dt*K[K_d62]*xt52) * (cs52 * rs15);
     }
     {  // row 28
     const T rs28 = nt_rscale<T>(nt_exp_hi(x[28]), fh);
-        const T nj28_c0 = T(2)*K[K_c14]*nt_cvt<T>(x[28]);
+        const T nj28_c0 = T(2)*K[K_c14]*xt28;
         const T nj28_c1 = F.dt*K[K_c17a];
-        const T nj28_c2 = F.dt*nt_cvt<T>(x[28]);
-        J[212] = (F.dt*nj28_c0 + F.dt*(K[K_c18]*nt_cvt<T>(x[52]) + K[K_c5]*nt_cvt<T>(x[49]) + K[K_c7]*nt_cvt<T>(x[47]) + nj28_c0) + T(1)) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs28);
-        J[210] = (-nj28_c1*nt_cvt<T>(x[43])) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs28);
-        J[213] = (-nj28_c1*nt_cvt<T>(x[29])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs28);
-        J[214] = (K[K_c7]*nj28_c2) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs28);
-        J[215] = (K[K_c5]*nj28_c2) * (nt_scale<T>(nt_exp_hi(x[49]), fh) * rs28);
-        J[216] = (K[K_c18]*nj28_c2) * (nt_scale<T>(nt_exp_hi(x[52]), fh) * rs28);
-        J[211] = (-F.dt*F.o2*K[K_c4]) * (nt_scale<T>(nt_exp_hi(x[56]), fh) * rs28);
+        const T nj28_c2 = F.dt*xt28;
+        J[212] = (F.dt*nj28_c0 + F.dt*(K[K_c18]*xt52 + K[K_c5]*xt49 + K[K_c7]*xt47 + nj28_c0) + T(1)) * (cs28 * rs28);
+        J[210] = (-nj28_c1*xt43) * (cs29 * rs28);
+        J[213] = (-nj28_c1*xt29) * (cs43 * rs28);
+        J[214] = (K[K_c7]*nj28_c2) * (cs47 * rs28);
+        J[215] = (K[K_c5]*nj28_c2) * (cs49 * rs28);
+        J[216] = (K[K_c18]*nj28_c2) * (cs52 * rs28);
+        J[211] = (-F.dt*F.o2*K[K_c4]) * (cs56 * rs28);
     }
     {  // row 29
     const T rs29 = nt_rscale<T>(nt_exp_hi(x[29]), fh);
         const T nj29_c0 = F.dt*K[K_c7];
-        J[35] = (-nj29_c0*nt_cvt<T>(x[47])) * (nt_scale<T>(nt_exp_hi(x[28]), fh) * rs29);
-        J[34] = (F.dt*(K[K_c17a]*nt_cvt<T>(x[43]) + K[K_c17b]*nt_cvt<T>(x[43]) + tj[J_ch3o2h]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[29]), fh) * rs29);
-        J[36] = (F.dt*nt_cvt<T>(x[29])*(K[K_c17a] + K[K_c17b])) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs29);
-        J[37] = (-nj29_c0*nt_cvt<T>(x[28])) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs29);
+        J[35] = (-nj29_c0*xt47) * (cs28 * rs29);
+        J[34] = (F.dt*(K[K_c17a]*xt43 + K[K_c17b]*xt43 + tj[J_ch3o2h]) + T(1)) * (cs29 * rs29);
+        J[36] = (F.dt*xt29*(K[K_c17a] + K[K_c17b])) * (cs43 * rs29);
+        J[37] = (-nj29_c0*xt28) * (cs47 * rs29);
     }
     {  // row 30
     const T rs30 = nt_rscale<T>(nt_exp_hi(x[30]), fh);
-        J[95] = (F.dt*(K[K_d90]*nt_cvt<T>(x[42]) + tj[J_cfc11]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[30]), fh) * rs30);
-        J[96] = (F.dt*K[K_d90]*nt_cvt<T>(x[30])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs30);
+        J[95] = (F.dt*(K[K_d90]*xt42 + tj[J_cfc11]) + T(1)) * (cs30 * rs30);
+        J[96] = (F.dt*K[K_d90]*xt30) * (cs42 * rs30);
     }
     {  // row 32
     const T rs32 = nt_rscale<T>(nt_exp_hi(x[32]), fh);
-        J[18] = (F.dt*(K[K_d92]*nt_cvt<T>(x[42]) + tj[J_cfc113]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[32]), fh) * rs32);
-        J[19] = (F.dt*K[K_d92]*nt_cvt<T>(x[32])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs32);
+        J[18] = (F.dt*(K[K_d92]*xt42 + tj[J_cfc113]) + T(1)) * (cs32 * rs32);
+        J[19] = (F.dt*K[K_d92]*xt32) * (cs42 * rs32);
     }
     {  // row 37
     const T rs37 = nt_rscale<T>(nt_exp_hi(x[37]), fh);
-        const T nj37_c0 = F.dt*nt_cvt<T>(x[37]);
-        J[52] = (F.dt*(K[K_e50]*nt_cvt<T>(x[42]) + K[K_e51]*nt_cvt<T>(x[43]) + tj[J_ch3br]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[37]), fh) * rs37);
-        J[53] = (K[K_e50]*nj37_c0) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs37);
-        J[54] = (K[K_e51]*nj37_c0) * (nt_scale<T>(nt_exp_hi(x[43]), fh) * rs37);
+        const T nj37_c0 = F.dt*xt37;
+        J[52] = (F.dt*(K[K_e50]*xt42 + K[K_e51]*xt43 + tj[J_ch3br]) + T(1)) * (cs37 * rs37);
+        J[53] = (K[K_e50]*nj37_c0) * (cs42 * rs37);
+        J[54] = (K[K_e51]*nj37_c0) * (cs43 * rs37);
     }
     {  // row 38
     const T rs38 = nt_rscale<T>(nt_exp_hi(x[38]), fh);
-        J[30] = (F.dt*(K[K_e52]*nt_cvt<T>(x[42]) + tj[J_h1211]) + T(1)) * (nt_scale<T>(nt_exp_hi(x[38]), fh) * rs38);
-        J[31] = (F.dt*K[K_e52]*nt_cvt<T>(x[38])) * (nt_scale<T>(nt_exp_hi(x[42]), fh) * rs38);
+        J[30] = (F.dt*(K[K_e52]*xt42 + tj[J_h1211]) + T(1)) * (cs38 * rs38);
+        J[31] = (F.dt*K[K_e52]*xt38) * (cs42 * rs38);
     }
     {  // row 46
     const T rs46 = nt_rscale<T>(nt_exp_hi(x[46]), fh);
-        J[355] = (T(-1)) * (nt_scale<T>(nt_exp_hi(x[7]), fh) * rs46);
+        J[355] = (T(-1)) * (cs7 * rs46);
         J[358] = T(0);
         J[357] = T(0);
         J[359] = T(0);
@@ -5810,7 +7201,7 @@ __device__ __forceinline__ void nt_jacobian_night_w4_3(const FF& F, PK K, PK tj,
         J[347] = T(0);
         J[346] = T(0);
         J[352] = T(0);
-        J[351] = (T(1)) * (nt_scale<T>(nt_exp_hi(x[47]), fh) * rs47);
+        J[351] = (T(1)) * (cs47 * rs47);
         J[353] = T(0);
         J[349] = T(0);
         J[354] = T(0);

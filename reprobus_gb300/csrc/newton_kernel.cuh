@@ -21,8 +21,8 @@
 
 namespace rpb {
 
-template <typename T>
-__device__ __forceinline__ void nt_load_fix(const T* r, NtFixT<T>& F) {
+template <typename T, typename PR>
+__device__ __forceinline__ void nt_load_fix(PR r, NtFixT<T>& F) {
     F.o2 = r[0]; F.n2 = r[1]; F.h2 = r[2]; F.co2 = r[3]; F.hnm = r[4];
     F.parthno3 = r[5]; F.parth2o = r[6]; F.parthcl = r[7]; F.parthbr = r[8];
     F.rain_hno3 = r[9]; F.rain_hcl = r[10]; F.rain_hbr = r[11]; F.rain_h2o2 = r[12]; F.dt = r[13];
@@ -524,13 +524,17 @@ __global__ void __launch_bounds__(32 * W * C, 1) k_nt_solve_wc(Params P) {
             nt_rhs_wc_fn<W, TJ>(g, day, F, rec + NT_RK, rec + NT_RJ, rec + NT_RH, rec + NT_RCK0, x, floor_, z);
         }
         __syncthreads();  // the Jacobian and right-hand side of every cell
-        // phase B: warp 0 of the group
+        // phase B: warp 0 of the group, the right-hand side in registers (the
+        // factorisation's fused forward substitution reads it row by row)
         if (g == 0) {
             if (c >= 0) {
+                TJ zr[NT_NX];
+#pragma unroll
+                for (int i = 0; i < NT_NX; i++) zr[i] = z[i];
                 NT_FENCE();
-                nt_factor_solve<TJ>(J, z, TJ(NT_TINY));
+                nt_factor_solve<TJ>(J, (TJ*)zr, TJ(NT_TINY));
                 TJ step;
-                const bool ok = nt_update<TJ>(x, floor_, z, &step, true);
+                const bool ok = nt_update<TJ>(x, floor_, (const TJ*)zr, &step, true);
                 it++;
                 int done = 0;
                 if (!ok)
