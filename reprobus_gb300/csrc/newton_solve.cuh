@@ -12,6 +12,7 @@
 // value (the fixed point is non-negative). The iteration has converged when
 // max_i |z_i| < tol.
 #pragma once
+#include <cstdint>
 #include "newton_gen.cuh"
 #ifndef __CUDACC__
 #define __noinline__
@@ -41,6 +42,31 @@ struct SJ {
     T* p;
     __device__ __forceinline__ T& operator[](int q) const { return p[q * STRIDE]; }
 };
+
+// write-only view of the same slots for the Jacobian: each store is an
+// explicit shared-memory store, so the compiler knows that storing the
+// Jacobian never changes global memory and may keep the record values and
+// the iterate it has read in registers across the stores
+#ifdef __CUDA_ARCH__
+template <typename T, int STRIDE>
+struct SJW {
+    uint32_t a;  // shared-window address of slot 0 of this lane
+    struct Ref {
+        uint32_t q;
+        __device__ __forceinline__ void operator=(float v) const {
+            asm volatile("st.shared.f32 [%0], %1;" ::"r"(q), "f"(v));
+        }
+        __device__ __forceinline__ void operator=(double v) const {
+            asm volatile("st.shared.f64 [%0], %1;" ::"r"(q), "d"(v));
+        }
+    };
+    __device__ __forceinline__ Ref operator[](int s) const { return Ref{a + (uint32_t)(s * STRIDE * sizeof(T))}; }
+};
+template <typename T, int STRIDE>
+__device__ __forceinline__ SJW<T, STRIDE> nt_store_view(SJ<T, STRIDE> J) {
+    return SJW<T, STRIDE>{(uint32_t)__cvta_generic_to_shared(J.p)};
+}
+#endif
 
 constexpr double NT_TINY = 1e-30;   // pivot guard of the factorisation
 
@@ -87,6 +113,15 @@ struct SJZ {
     __device__ __forceinline__ T& operator[](int i) const { return p[(NT_NSLOT + i) * STRIDE]; }
 };
 
+template <typename PJ>
+struct nt_is_sj {
+    static constexpr bool value = false;
+};
+template <typename T, int STRIDE>
+struct nt_is_sj<SJ<T, STRIDE>> {
+    static constexpr bool value = true;
+};
+
 // the Jacobian of the day or night equations as a call of its own, so that
 // its register allocation does not meet the residual's and the solve's
 template <typename TJ, typename FFT, typename PKT, typename PJ>
@@ -101,7 +136,10 @@ template <typename TJ, typename FFT, typename PKT, typename PJ>
 __device__ __forceinline__ void nt_jacobian_call(bool day, const FFT& FT, PKT KT, PKT tjT, PKT hetT, const double* x,
                                                  double floor_, PJ J) {
 #ifdef __CUDA_ARCH__
-    nt_jacobian_fn<TJ>(day, FT, KT, tjT, hetT, x, floor_, J);
+    if constexpr (nt_is_sj<PJ>::value && sizeof(TJ) == 4)  // (FP64: the freedom costs spills)
+        nt_jacobian_fn<TJ>(day, FT, KT, tjT, hetT, x, floor_, nt_store_view(J));
+    else
+        nt_jacobian_fn<TJ>(day, FT, KT, tjT, hetT, x, floor_, J);
 #else
     if (day)
         nt_jacobian_day<TJ>(FT, KT, tjT, hetT, x, floor_, J);
