@@ -319,10 +319,10 @@ class Accuracy:
         self.ref = accuracy.Reference(self.sub, fuse=True)
         self.oracle_s = time.perf_counter() - t0
 
-    def check(self, dc):
+    def check(self, dc, against="fixed_point"):
         got = {f: self.case.gather_columns(dc[f].cpu().numpy().reshape(getattr(self.case, f).shape, order="F"),
                                            self.ilon, self.ilat) for f in ("qj1", "hc")}
-        return self.ref.report(got)
+        return self.ref.report(got, against=against)
 
     def describe(self):
         return {"columns": int(len(self.ilon)), "cells": int(self.sub.ncells), "seed": ACCURACY_SEED,
@@ -388,7 +388,7 @@ def time_arms(torch, h, case, dc, stream, arms, steps, warmup, net, npass_of, wo
                          {"lanes_per_block": st["lanes_per_block"], "blocks_per_sm": st["blocks_per_sm"],
                           "z_shared": st["z_shared"]}}
         if acc is not None:
-            results[name]["accuracy"] = acc.check(dc)
+            results[name]["accuracy"] = acc.check(dc, "ref5" if name == "ref5" else "fixed_point")
     restore()
     torch.cuda.synchronize()
     return results

@@ -47,7 +47,7 @@ struct SJ {
 // explicit shared-memory store, so the compiler knows that storing the
 // Jacobian never changes global memory and may keep the record values and
 // the iterate it has read in registers across the stores
-#ifdef __CUDA_ARCH__
+#ifdef __CUDACC__
 template <typename T, int STRIDE>
 struct SJW {
     uint32_t a;  // shared-window address of slot 0 of this lane
@@ -167,7 +167,11 @@ __device__ __forceinline__ bool nt_iterate(const FF& F, PK K, PK tj, PK het, PC 
 #ifdef __CUDA_ARCH__
     if constexpr (ZSHARED) {
         const SJZ<TJ, PJ::stride> z{J.p};
-        nt_rhs_fn<TJ>(day, F, K, tj, het, ck0, x, floor_, z);
+        // the residual stores z through explicit shared-memory stores (as the
+        // Jacobian does its slots), so the record values it reads stay in registers
+        const SJW<TJ, PJ::stride> zw{(uint32_t)__cvta_generic_to_shared(J.p) +
+                                     (uint32_t)(NT_NSLOT * PJ::stride * sizeof(TJ))};
+        nt_rhs_fn<TJ>(day, F, K, tj, het, ck0, x, floor_, zw);
         nt_factor_solve<TJ>(J, z, TJ(NT_TINY));
         return nt_update<TJ>(x, floor_, z, step, active);
     }
