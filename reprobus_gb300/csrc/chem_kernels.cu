@@ -1393,7 +1393,7 @@ extern "C" int reprobus_chem_set_tuning(void* handle, int lanes_per_block, int b
     Handle* h = (Handle*)handle;
     if (!h) return set_err(REPROBUS_ERR_ARG, "handle is NULL");
     if (lanes_per_block < 0 || blocks_per_sm < 0) return set_err(REPROBUS_ERR_ARG, "bad tuning values");
-    if (zshared < 0 || zshared > 7) return set_err(REPROBUS_ERR_ARG, "zshared must be 0 .. 7");
+    if (zshared < 0 || zshared > 6) return set_err(REPROBUS_ERR_ARG, "zshared must be 0 .. 6");
     if (lanes_per_block > 0) {
         bool found = false;
         const NtVariant* vs[32];

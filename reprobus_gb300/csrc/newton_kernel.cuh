@@ -15,7 +15,6 @@
 // FP64 update of the iterate in the cell's record. ZS: the right-hand side
 // and step z in NT_NX more shared-memory slots per lane (else registers).
 #pragma once
-#include <type_traits>
 #include "chem_params.cuh"
 #include "newton_launch.h"
 #include "newton_solve.cuh"
@@ -334,10 +333,7 @@ constexpr NtVariant nt_sp_variant() {
 // SM fetch the same generated code at the same time (the solve code is far
 // larger than the instruction cache). Lanes without a cell pass the barriers
 // idle; the exit is a barrier-and-reduction over all threads.
-// ZS: the right-hand side in NT_NX more shared-memory slots per lane (after
-// the matrix), written by the residual as a call of its own through explicit
-// shared-memory stores; the kernel then keeps no right-hand side in registers.
-template <typename TJ, int NTH, bool ZS = false>
+template <typename TJ, int NTH>
 __global__ void __launch_bounds__(NTH, 1) k_nt_solve_ls(Params P) {
     static_assert(NTH % 32 == 0, "whole warps");
     extern __shared__ __align__(16) unsigned char nt_smem[];
@@ -376,33 +372,21 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_ls(Params P) {
             nt_jacobian_call<TJ>(day, FT, recT + NT_RK, recT + NT_RJ, recT + NT_RH, x, floor_, J);
         }
         __syncthreads();
-        using ZV = std::conditional_t<ZS, SJZ<TJ, NTH>, TJ*>;
-        TJ zr[ZS ? 1 : NT_NX];
-        ZV z;
-        if constexpr (ZS)
-            z = SJZ<TJ, NTH>{J.p};
-        else
-            z = zr;
+        TJ z[NT_NX];
         if (cell >= 0) {
             NtFixT<double> F;
             nt_load_fix<double>(rec + NT_RF, F);
-            if constexpr (ZS) {
-                const SJW<TJ, NTH> zw{(uint32_t)__cvta_generic_to_shared(J.p) +
-                                      (uint32_t)(NT_NSLOT * NTH * sizeof(TJ))};
-                nt_rhs_fn<TJ>(day, F, rec + NT_RK, rec + NT_RJ, rec + NT_RH, rec + NT_RCK0, x, floor_, zw);
-            } else {
-                nt_rhs<TJ>(day, F, rec + NT_RK, rec + NT_RJ, rec + NT_RH, rec + NT_RCK0, x, floor_, z);
-            }
+            nt_rhs<TJ>(day, F, rec + NT_RK, rec + NT_RJ, rec + NT_RH, rec + NT_RCK0, x, floor_, (TJ*)z);
         }
         __syncthreads();
         if (cell >= 0) {
             NT_FENCE();
-            nt_factor_solve<TJ>(J, z, TJ(NT_TINY));
+            nt_factor_solve<TJ>(J, (TJ*)z, TJ(NT_TINY));
         }
         __syncthreads();
         if (cell >= 0) {
             TJ step;
-            const bool ok = nt_update<TJ>(x, floor_, z, &step, true);
+            const bool ok = nt_update<TJ>(x, floor_, (const TJ*)z, &step, true);
             it++;
             int done = 0;
             if (!ok)
@@ -416,34 +400,22 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_ls(Params P) {
     }
 }
 
-template <typename TJ, int NTH, bool ZS = false>
-constexpr size_t nt_ls_smem_bytes() {
-    return (size_t)(NT_NSLOT + (ZS ? NT_NX : 0)) * NTH * sizeof(TJ);
-}
-
-template <typename TJ, int NTH, bool ZS = false>
+template <typename TJ, int NTH>
 cudaError_t nt_ls_prepare(int* blocks_per_sm) {
-    return nt_fit_smem(k_nt_solve_ls<TJ, NTH, ZS>, NTH, nt_ls_smem_bytes<TJ, NTH, ZS>(), blocks_per_sm);
+    return nt_fit_smem(k_nt_solve_ls<TJ, NTH>, NTH, (size_t)NT_NSLOT * NTH * sizeof(TJ), blocks_per_sm);
 }
 
-template <typename TJ, int NTH, bool ZS = false>
+template <typename TJ, int NTH>
 cudaError_t nt_ls_launch(const Params& P, int grid, cudaStream_t stream) {
-    k_nt_solve_ls<TJ, NTH, ZS><<<grid, NTH, nt_ls_smem_bytes<TJ, NTH, ZS>(), stream>>>(P);
+    k_nt_solve_ls<TJ, NTH><<<grid, NTH, (size_t)NT_NSLOT * NTH * sizeof(TJ), stream>>>(P);
     return cudaGetLastError();
 }
 
 // form 4: one group in lock-step, z in registers
 template <typename TJ, int NTH>
 constexpr NtVariant nt_ls_variant() {
-    return NtVariant{(int)sizeof(TJ), NTH, 4, nt_ls_smem_bytes<TJ, NTH>(), &nt_ls_prepare<TJ, NTH>,
+    return NtVariant{(int)sizeof(TJ), NTH, 4, (size_t)NT_NSLOT * NTH * sizeof(TJ), &nt_ls_prepare<TJ, NTH>,
                      &nt_ls_launch<TJ, NTH>};
-}
-
-// form 7: form 4 with z in shared memory
-template <typename TJ, int NTH>
-constexpr NtVariant nt_lsz_variant() {
-    return NtVariant{(int)sizeof(TJ), NTH, 7, nt_ls_smem_bytes<TJ, NTH, true>(), &nt_ls_prepare<TJ, NTH, true>,
-                     &nt_ls_launch<TJ, NTH, true>};
 }
 
 // Warps-per-cell form (form 5): W warps work on the same 32 cells. Per
