@@ -72,3 +72,38 @@ def test_mixed_newton_full_grid_is_a_fixed_point_and_conserves(torch, case):
     oracle.clamp(case, q)
     assert relerr(fused["qj1"], q).max() < 1e-12
     assert relerr(fused["hc"], hc).max() < 1e-12
+
+
+def test_learned_warm_start_halves_the_fallbacks(torch, case):
+    """What the committed network gains over the plain start on the full
+    grid: cells whose Newton iteration from the plain start fails within the
+    iteration cap fall back to the reference's 5 passes (their answer is then
+    the reference scheme's, not the fixed point); from the network's start
+    fewer do. Its cost (a few ms per step and ~2 % more iterations at the
+    5-pass start) is reported by bench.py. Both answers are the same fixed
+    point on every cell neither solver handed to its fallback."""
+    from reprobus_gb300 import mlp
+    from reprobus_gb300.resident import DeviceCase
+    net = mlp.Mlp(batch_cap=128)
+    net.load()
+    out = {}
+    for name, n in (("plain", None), ("learned", net)):
+        h = ChemStep.for_case(case, niter=5, flags=0)
+        h.set_solver(SOLVER_NEWTON_MIXED)  # production settings: 5 passes, tol 1e-5, maxit 12
+        h.set_mlp(n)
+        dc = DeviceCase(case)
+        st = h.step_dev(1, case.nlat, case.daynum, case.dt, *dc.args(), stats=True)
+        out[name] = (dc.state_host(), st)
+        h.close()
+    net.close()
+    (a, sa), (b, sb) = out["plain"], out["learned"]
+    print(f"fallbacks: plain start {sa['fallbacks']}, learned start {sb['fallbacks']}; iterations per cell "
+          f"{(sa['newton_iters'] + sa['failed_iters']) / case.ncells:.3f} -> "
+          f"{(sb['newton_iters'] + sb['failed_iters']) / case.ncells:.3f}; restarts {sb['warm_restarts']}")
+    assert sa["fallbacks"] >= 100  # enough cells for the comparison to mean something
+    assert sb["fallbacks"] <= 0.75 * sa["fallbacks"]
+    from oracle import accuracy
+    both = (oracle.map_residual(case, a["qj1"], a["hc"]) <= MAP_TOL) & (
+        oracle.map_residual(case, b["qj1"], b["hc"]) <= MAP_TOL)
+    assert both.mean() > 0.999
+    assert accuracy.cell_errors(b, a, case.nivbas)[both].max() <= 1e-6
