@@ -47,6 +47,7 @@ SOLVE_DRAM_BYTES_PER_CELL_ITER = 899.0
 # checked against the CPU FP64 oracle after the timed steps
 ACCURACY_COLUMNS = 80
 ACCURACY_SEED = 2024
+STEP_TOL = 1e-4  # the Newton solvers' default step tolerance (both solvers alike)
 
 
 def newton_ops():
@@ -352,7 +353,7 @@ def time_arms(torch, h, case, dc, stream, arms, steps, warmup, net, npass_of, wo
 
     results = {}
     for name in arms:
-        h.set_solver(SOLVER_ID[name], npass=npass_of(name), maxit=12, tol=1e-5)
+        h.set_solver(SOLVER_ID[name], npass=npass_of(name), maxit=12, tol=STEP_TOL)
         h.set_mlp(net if name == "mlp" else None)
         for _ in range(max(warmup, 3)):
             restore()
@@ -463,7 +464,7 @@ def main():
     clocks.start()
     results = time_arms(torch, h, case, dc, stream, run, args.steps, args.warmup, net, npass_of, world, acc)
     clk = clocks.stop()
-    h.set_solver(SOLVER_ID[headline], npass=npass_of(headline), maxit=12, tol=1e-5)
+    h.set_solver(SOLVER_ID[headline], npass=npass_of(headline), maxit=12, tol=STEP_TOL)
     h.set_mlp(net if headline == "mlp" else None)
     R = results[headline]
     ms_step = R["ms_per_step"]

@@ -170,10 +170,10 @@ int reprobus_chem_set_graph(void* handle, int on);
  * until the largest step relative to max(|x|, 1e-20 hnm) is below tol, at
  * most maxit iterations; a cell that does not converge falls back to the
  * reference's niter passes and is counted in stats.fallbacks.
- * Defaults: npass 5, maxit 12, tol 1e-5 (Newton converges superlinearly: the
- * answer then lies within ~1e-10 of the fixed point, far inside the 1e-6
- * accuracy target; 5 passes are the
- * fastest start of both solvers on the 2 x 2 degree grid). A warm-start
+ * Defaults: npass 5, maxit 12, tol 1e-4 (Newton converges superlinearly: the
+ * step that passes the test is followed by none, and the answer lies within
+ * ~1e-8 of the fixed point, far inside the 1e-6 accuracy target; 5 passes are
+ * the fastest start of both solvers on the 2 x 2 degree grid). A warm-start
  * network (reprobus_chem_set_mlp) is trained for one npass and must be used
  * with it. No counterpart in the reference. */
 int reprobus_chem_set_solver(void* handle, int solver, int npass, int maxit, double tol);

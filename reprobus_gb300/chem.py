@@ -195,7 +195,7 @@ class ChemStep:
         except Exception:
             pass
 
-    def set_solver(self, solver, npass=5, maxit=12, tol=1e-5):
+    def set_solver(self, solver, npass=5, maxit=12, tol=1e-4):
         """SOLVER_REF5 (the reference's fixed passes), SOLVER_NEWTON64 or
         SOLVER_NEWTON_MIXED (fixed point of the pass map by Newton)."""
         _check(self.lib.reprobus_chem_set_solver(self._h, solver, npass, maxit, float(tol)))

@@ -700,7 +700,7 @@ struct Handle {
     int device;
     int solver = REPROBUS_SOLVER_REF5;  // which kernel integrates the cells
     int npass = 5, maxit = 12;          // Newton: reference passes before, iteration cap
-    double tol = 1e-5;                  // Newton: scaled step tolerance
+    double tol = 1e-4;                  // Newton: scaled step tolerance
     double troe[18];
     double* d_ajl = nullptr;
     double* d_o3up = nullptr;

@@ -192,7 +192,7 @@ def test_oracle_newton_from_a_fixed_point_stays_there(polar):
 @pytest.mark.parametrize("mixed", [0, 1])
 def test_generated_newton_at_production_settings_matches_the_oracle(host, polar, mixed):
     """The generated equations' Newton iteration (host build) from the
-    5-pass state with the production step tolerance 1e-5: within 1e-6 of
+    5-pass state with the production step tolerance 1e-4: within 1e-6 of
     Oracle-C for every species above 1e-20 mol/mol on every cell both
     converge on, for the FP64 and the FP32 Jacobian."""
     c, dg, fp, stat, _, r5 = polar
@@ -212,7 +212,7 @@ def test_generated_newton_at_production_settings_matches_the_oracle(host, polar,
         x = np.concatenate([r5["qj1"][i, j, k, :42], r5["hc"][i, j, k, :]]) * hnm
         last = ctypes.c_double()
         it = host.nt_host_newton(_P(K), _P(tj), _P(het), _P(fix), _P(ck0), int(dg[DIAG_SZA, cell] <= 95.0), _P(x),
-                                 16, 1e-5, mixed, ctypes.byref(last))
+                                 16, 1e-4, mixed, ctypes.byref(last))
         if it < 0:
             fails += 1
             continue
