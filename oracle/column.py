@@ -16,6 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "libcolumn_oracle.so")
 SRC = os.path.join(HERE, "column_oracle.cpp")
+LIB_OVERRIDE = "REPROBUS_COLUMN_ORACLE_LIB"  # a prebuilt copy to load instead
 DEPS = [SRC, os.path.join(HERE, "..", "reprobus_gb300", "csrc", "tropo_tables.h")]
 
 
@@ -33,8 +34,10 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        build()
-        L = ctypes.CDLL(LIB)
+        path = os.environ.get(LIB_OVERRIDE)
+        if not path:
+            path = build()
+        L = ctypes.CDLL(path)
         dp = ctypes.POINTER(ctypes.c_double)
         i, d = ctypes.c_int, ctypes.c_double
         L.orc_sedimentation.argtypes = [i, i, i, i, i, i, i, dp, dp, dp, dp, i, dp, dp, d]

@@ -15,6 +15,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 SRC = os.path.join(HERE, "chem_oracle.c")
+# a prebuilt copy to load instead (the sanitizer runs of tests/ build one)
+LIB_OVERRIDE = "REPROBUS_ORACLE_LIB"
 
 CFLAGS = ["-O3", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared"]
 
@@ -49,8 +51,10 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        build()
-        _lib = ctypes.CDLL(LIB)
+        path = os.environ.get(LIB_OVERRIDE)
+        if not path:
+            path = build()
+        _lib = ctypes.CDLL(path)
         dp = ctypes.POINTER(ctypes.c_double)
         _lib.orc_step.restype = ctypes.c_int
         _lib.orc_step.argtypes = [ctypes.POINTER(OrcGrid), ctypes.c_int, ctypes.c_int, ctypes.c_double,

@@ -26,7 +26,8 @@ GEN = os.path.join(ROOT, "reprobus_gb300", "csrc", "newton_gen.cuh")
 @pytest.fixture(scope="module")
 def host(tmp_path_factory):
     out = str(tmp_path_factory.mktemp("nt") / "libnthost.so")
-    subprocess.run(["g++", "-O1", "-std=c++17", "-fPIC", "-shared", "-o", out,
+    extra = os.environ.get("REPROBUS_SANITIZE_FLAGS", "").split()  # set by test_sanitizers.py
+    subprocess.run(["g++", "-O1", "-std=c++17", "-fPIC", "-shared", *extra, "-o", out,
                     os.path.join(ROOT, "tests", "newton_host.cpp")], check=True)
     L = ctypes.CDLL(out)
     dp = ctypes.POINTER(ctypes.c_double)
