@@ -297,8 +297,8 @@ def inputs_l137():
 ARMS = {"ref5": "reference scheme, 5 fixed passes (drop-in)",
         "newton64": "Newton to the fixed point of the reference map, FP64 Jacobian",
         "mixed": "Newton to the fixed point, FP32 Jacobian+LU, FP64 residual/update",
-        "mlp": "Newton to the fixed point, FP32 Jacobian+LU, FP64 residual/update, learned warm start (BF16 MLP "
-               "on tensor cores)"}
+        "mlp": "Newton to the fixed point, FP32 Jacobian+LU, FP64 residual/update, learned restart of the cells "
+               "whose plain start misses (BF16 MLP on tensor cores)"}
 SOLVER_ID = {"ref5": 0, "newton64": 1, "mixed": 2, "mlp": 2}  # REPROBUS_SOLVER_*
 
 
@@ -452,7 +452,7 @@ def main():
     dc = DeviceCase(case)
 
     def npass_of(name):
-        # the warm start's network is trained on the default 5-pass start
+        # the network is trained on the default 5-pass start
         if name == "mlp":
             return 5
         return args.npass if args.npass > 0 else 5

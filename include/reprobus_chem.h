@@ -80,11 +80,13 @@ typedef struct reprobus_stats {
                                   registers with two warp groups sharing the matrix
                                   slots, 3 with a residual lane per cell, 4 in
                                   registers with the block's warps in lock-step  */
-    int warm_start;            /* Newton solvers: 1 when the learned warm start ran  */
-    long long warm_restarts;   /* warm start: cells whose predicted start missed the
-                                  convergence test and restarted from the plain start */
+    int warm_start;            /* Newton solvers: 1 when a network for the learned
+                                  restart is attached                                */
+    long long warm_restarts;   /* learned restart: cells whose plain start missed the
+                                  convergence test and that were solved again from
+                                  the network's prediction                           */
     long long failed_iters;    /* Newton solvers: iterations of attempts that did not
-                                  converge (warm-start misses, fallbacks)            */
+                                  converge (plain starts that missed, fallbacks)     */
     double solve_ms;           /* Newton solvers: device time of the persistent solve
                                   kernel (its first launch)                          */
     int graph;                 /* 1 when the step ran as a CUDA graph               */
@@ -173,9 +175,9 @@ int reprobus_chem_set_graph(void* handle, int on);
  * Defaults: npass 5, maxit 12, tol 1e-4 (Newton converges superlinearly: the
  * step that passes the test is followed by none, and the answer lies within
  * ~1e-8 of the fixed point, far inside the 1e-6 accuracy target; 5 passes are
- * the fastest start of both solvers on the 2 x 2 degree grid). A warm-start
- * network (reprobus_chem_set_mlp) is trained for one npass and must be used
- * with it. No counterpart in the reference. */
+ * the fastest start of both solvers on the 2 x 2 degree grid). The network
+ * of the learned restart (reprobus_chem_set_mlp) is trained for one npass
+ * and must be used with it. No counterpart in the reference. */
 int reprobus_chem_set_solver(void* handle, int solver, int npass, int maxit, double tol);
 
 /* Shape of the persistent Newton solve kernel. lanes_per_block = 0 (default):
@@ -203,7 +205,7 @@ int reprobus_chem_set_solver(void* handle, int solver, int npass, int maxit, dou
  * each new choice to it. No counterpart in the reference. */
 int reprobus_chem_set_tuning(void* handle, int lanes_per_block, int blocks_per_sm, int zshared);
 
-/* ---- learned warm start ----------------------------------------------------
+/* ---- learned restart -------------------------------------------------------
  * A 64-256-256-256-64 MLP (SiLU; BF16 weights and activations, FP32
  * accumulation on the tensor cores) maps the 64 features of a cell at the
  * Newton solvers' plain start (npass reference passes from the start state):
@@ -247,14 +249,15 @@ int reprobus_mlp_forward(void* net, const float* X, float* Y, int B, void* cuda_
  * the reference. */
 int reprobus_mlp_set_wait_limit(void* net, long long polls);
 
-/* Attaches a network to a chemistry handle (NULL detaches): the Newton
- * solvers then start every cell from the network's prediction instead of the
- * plain start; a cell whose predicted start misses the convergence test is
- * solved again from the plain start (stats.warm_restarts), and one that
- * misses again falls back to the reference passes. If the inference kernel
- * gives up waiting, every cell of the step starts from the plain start (the
- * answer is unchanged) and a call that reads the step's counters (stats
- * requested, or REPROBUS_CHECK_FINITE) returns REPROBUS_ERR_TIMEOUT. */
+/* Attaches a network to a chemistry handle (NULL detaches). The Newton
+ * solvers then give a cell whose plain start misses the convergence test a
+ * second attempt from the network's prediction for that plain start
+ * (stats.warm_restarts; at most 65,536 cells per step), and only a cell that
+ * misses again falls back to the reference passes. Every other cell's answer
+ * is the same with and without the network. If the inference kernel gives up
+ * waiting, those cells are solved again from the plain start (the answer
+ * stands) and a call that reads the step's counters (stats requested, or
+ * REPROBUS_CHECK_FINITE) returns REPROBUS_ERR_TIMEOUT. */
 int reprobus_chem_set_mlp(void* handle, void* net);
 
 /* The 64 raw features of every chemistry cell of rows ilat0..ilat1 at the
@@ -407,7 +410,7 @@ int reprobus_history_read_dev(void* handle, const char* path, char* namexp, int*
  * (cudaDeviceReset) gets the address looked up again at its next call.
  * The call always integrates with the reference scheme (niter fixed passes,
  * REPROBUS_SOLVER_REF5): it has no handle, so no solver selection, Newton
- * state or warm start. Launches on `stream` (NULL: the default stream);
+ * state or network. Launches on `stream` (NULL: the default stream);
  * asynchronous unless REPROBUS_CHECK_FINITE is set, in which case it
  * synchronises to read the non-finite count. It runs the kernels of
  * reprobus_chem_step_dev with the same flags. Troe prefactors that are not

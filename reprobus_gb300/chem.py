@@ -211,14 +211,15 @@ class ChemStep:
         _check(self.lib.reprobus_chem_set_graph(self._h, 1 if on else 0))
 
     def set_mlp(self, net):
-        """Attaches a reprobus_gb300.mlp.Mlp as the Newton solvers' warm start
-        (None detaches)."""
+        """Attaches a reprobus_gb300.mlp.Mlp to the Newton solvers (None
+        detaches): a cell whose plain start misses the convergence test is
+        solved again from the network's prediction before it falls back."""
         _check(self.lib.reprobus_chem_set_mlp(self._h, ctypes.c_void_p(net.handle if net is not None else None)))
         self.mlp = net
 
     def features_dev(self, ilat0, ilat1, daynum, dt, alt, trajlon, trajlat, trajpre, trajtem, irapp, qj1, hc,
                      feat):
-        """The 64 raw warm-start features of every chemistry cell of the rows
+        """The network's 64 raw features of every chemistry cell of the rows
         at the plain start into feat (a CUDA float32 tensor of ncell x 64)."""
         _check(self.lib.reprobus_chem_features_dev(self._h, ilat0, ilat1, daynum, dt, _dp(alt), _dp(trajlon),
                                                    _dp(trajlat), _dp(trajpre), _dp(trajtem), irapp, _dp(qj1),

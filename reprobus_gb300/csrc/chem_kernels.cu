@@ -321,13 +321,16 @@ __global__ void __launch_bounds__(NTB, 1) k_chem(Params P) {
 //                copies for the mixed solver)
 //   k_nt_start   one thread per cell: P.npass_plain reference passes from the
 //                record's start state -> iterate x; the cell enters the work
-//                queue (day cells from the front, night cells from the back);
-//                warm start: the network's features (then k_mlp_infer and
-//                k_nt_warm). Two kernels rather than one: the rate stage
-//                alone is a smaller program for the instruction cache. The
-//                mixed solver runs the passes in FP32 (k_nt_start32).
+//                queue (day cells from the front, night cells from the back).
+//                Two kernels rather than one: the rate stage alone is a
+//                smaller program for the instruction cache. The mixed solver
+//                runs the passes in FP32 (k_nt_start32).
 //   k_nt_solve   persistent kernel, one lane per cell, lanes refilled from the
 //                queue (newton_kernel.cuh)
+//   learned restart (with a network): the cells that missed get the plain
+//                start again with the network's features (k_nt_start<3>),
+//                the network's prediction (k_mlp_infer), a start from it
+//                (k_nt_warm) and a second solve over a queue of their own
 //   k_nt_finish  one thread per converged cell: write-back, conserv, clamps
 //   k_nt_fallback one thread per cell the solver did not converge after
 //                P.maxit iterations: the reference's P.niter passes, then the
@@ -398,16 +401,23 @@ __global__ void __launch_bounds__(NTB) k_nt_setup(Params P) {
 // the plain start of a cell from its record: P.npass_plain reference passes
 // from the start state (ck0 from the record, cc from hc) -> x; the cell
 // enters the work queue (day cells from the front, night cells from the
-// back); with the warm start, the network's features of that plain start.
-// MODE 0: every cell; MODE 2: only cells whose FP32 start (k_nt_start32)
-// was not finite (stat < 0).
+// back). MODE 0: every cell; MODE 2: only cells whose FP32 start
+// (k_nt_start32) was not finite (stat < 0); MODE 3 (learned restart): only
+// cells whose Newton iteration missed (stat < 0), each in its own slot k <
+// P.mlp_cap (cells beyond the last slot keep stat < 0 and fall back), with
+// the network's features of the plain start at slot k.
 template <int MODE>
 __global__ void __launch_bounds__(128) k_nt_start(Params P) {
-    static_assert(MODE == 0 || MODE == 2, "start modes");
+    static_assert(MODE == 0 || MODE == 2 || MODE == 3, "start modes");
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= P.win_ncell) return;
     const int cell = win_cell(P, t);
     if (MODE != 0 && P.nt_stat[cell] >= 0) return;
+    int slot = 0;
+    if (MODE == 3) {
+        slot = atomicAdd(P.nt_head + 3, 1);
+        if (slot >= P.mlp_cap) return;
+    }
     const double* r = P.nt_rec + (size_t)cell * NT_REC;
     CellFix F;
     F.o2 = r[NT_RF]; F.n2 = r[NT_RF + 1]; F.h2 = r[NT_RF + 2]; F.co2 = r[NT_RF + 3]; F.hnm = r[NT_RF + 4];
@@ -434,12 +444,14 @@ __global__ void __launch_bounds__(128) k_nt_start(Params P) {
     for (int n = 0; n < NBCON - 1; n++) x[n] = ck[n];
 #pragma unroll
     for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = cc[n];
-    if (P.warm) {
+    if (MODE == 3) {
         float fe[64];
         cell_features(P, g, F.hnm, F.sza, r[NT_RSURF], ck, cc, fe);
-        float4* o = reinterpret_cast<float4*>(P.mlp_feat + (size_t)cell * 64);
+        float4* o = reinterpret_cast<float4*>(P.mlp_feat + (size_t)slot * 64);
 #pragma unroll
         for (int i = 0; i < 16; i++) o[i] = make_float4(fe[4 * i], fe[4 * i + 1], fe[4 * i + 2], fe[4 * i + 3]);
+        P.mlp_cells[slot] = cell;
+        atomicAdd(P.nonfinite + 4, 1ULL);
     }
     P.nt_stat[cell] = 0;
     if (F.sza <= 95.)
@@ -496,22 +508,10 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
         return;
     }
     double* x = P.nt_x + (size_t)cell * NT_NX;
-    double xd[NT_NX];
 #pragma unroll
-    for (int n = 0; n < NBCON - 1; n++) x[n] = xd[n] = nt_widen(ck[n]);
+    for (int n = 0; n < NBCON - 1; n++) x[n] = nt_widen(ck[n]);
 #pragma unroll
-    for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = xd[NBCON - 1 + n] = nt_widen(cc[n]);
-    if (P.warm) {
-        double ckd[NBCON];
-#pragma unroll
-        for (int n = 0; n < NBCON - 1; n++) ckd[n] = xd[n];
-        ckd[NBCON - 1] = 0.;
-        float fe[64];
-        cell_features(P, g, hnm, r[NT_RSZA], r[NT_RSURF], ckd, xd + NBCON - 1, fe);
-        float4* o = reinterpret_cast<float4*>(P.mlp_feat + (size_t)cell * 64);
-#pragma unroll
-        for (int i = 0; i < 16; i++) o[i] = make_float4(fe[4 * i], fe[4 * i + 1], fe[4 * i + 2], fe[4 * i + 3]);
-    }
+    for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = nt_widen(cc[n]);
     P.nt_stat[cell] = 0;
     if (day)
         P.nt_list[atomicAdd(P.nt_head + 1, 1)] = cell;
@@ -519,28 +519,25 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
         P.nt_list[P.nt_qcap - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
 }
 
-// warm start: x_i = max(x_i, 1e-30 hnm) 10^y_i from the network's prediction;
-// the plain start is kept in nt_xp for a cell whose warm start misses.
-// A block takes 128 cells and walks their iterates element by element, so
-// that consecutive threads touch consecutive words of x (cell-major, NT_NX
-// per cell) and of the predictions (64 per cell).
+// learned restart: x_i = max(x_i, 1e-30 hnm) 10^y_i for the cell of each
+// slot, y from the network's prediction for that slot. Consecutive threads
+// touch consecutive words of a slot's prediction and of its cell's iterate.
 // An inference that gave up (its error flag set) left no predictions: every
 // cell keeps its plain start and counter 7 records the timeout for the host.
 __global__ void __launch_bounds__(128) k_nt_warm(Params P) {
-    const int c0 = blockIdx.x * 128;
-    const int nc = P.ncell - c0 < 128 ? P.ncell - c0 : 128;
     const bool failed = P.mlp_err && *P.mlp_err != 0u;
-    if (failed && blockIdx.x == 0 && threadIdx.x == 0) P.nonfinite[7] = 1ULL;
-    double* x = P.nt_x + (size_t)c0 * NT_NX;
-    for (int e = threadIdx.x; e < nc * NT_NX; e += blockDim.x) {
-        const int cl = e / NT_NX, i = e - cl * NT_NX;
-        const size_t cell = (size_t)c0 + cl;
+    if (failed) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) P.nonfinite[7] = 1ULL;
+        return;
+    }
+    const int ns = min(P.nt_head[3], P.mlp_cap);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ns * NT_NX; e += gridDim.x * blockDim.x) {
+        const int k = e / NT_NX, i = e - k * NT_NX;
+        const size_t cell = (size_t)P.mlp_cells[k];
         const double hnm = P.nt_rec[cell * NT_REC + NT_RF + 4];
-        const double xe = x[e];
-        P.nt_xp[(size_t)c0 * NT_NX + e] = xe;  // the plain start, for a retry
-        if (failed) continue;
-        const float yi = fminf(fmaxf(P.mlp_y[cell * 64 + i], -30.f), 30.f);
-        x[e] = fmax(xe, 1e-30 * hnm) * nt_widen(exp10f(yi));
+        double* x = P.nt_x + cell * NT_NX + i;
+        const float yi = fminf(fmaxf(P.mlp_y[(size_t)k * 64 + i], -30.f), 30.f);
+        *x = fmax(*x, 1e-30 * hnm) * nt_widen(exp10f(yi));
     }
 }
 
@@ -736,11 +733,13 @@ struct Handle {
     cudaGraphExec_t gexec = nullptr;
     int gexec_sig = -1;
     unsigned graph_ready = 0;  // configurations that have run once directly
-    // learned warm start (reprobus_chem_set_mlp): the network and its buffers
+    // learned restart (reprobus_chem_set_mlp): the network and the buffers of
+    // its mlp_cap slots (features, predictions, cells)
     void* mlp = nullptr;
+    int mlp_cap = 0;
     float* mlp_feat = nullptr;
     float* mlp_y = nullptr;
-    double* nt_xp = nullptr;  // the plain start saved by k_nt_warm
+    int* mlp_cells = nullptr;
     // host-array entry point: copy streams and events of its row chunks
     cudaStream_t cin = nullptr, cout = nullptr;
     cudaEvent_t ev_in[4] = {}, ev_comp[4] = {};
@@ -796,7 +795,7 @@ static void free_handle(Handle* h) {
     cudaFree(h->nt_head);
     cudaFree(h->mlp_feat);
     cudaFree(h->mlp_y);
-    cudaFree(h->nt_xp);
+    cudaFree(h->mlp_cells);
     cudaFree(h->col_scratch);
     for (int c = 0; c < 4; c++) {
         if (h->ev_in[c]) cudaEventDestroy(h->ev_in[c]);
@@ -1184,34 +1183,23 @@ static int newton_prepare(Handle* h, Params& P) {
     P.npass_plain = h->npass;
     if (h->mlp) {
         if (!h->mlp_feat) {
-            const size_t nc = (size_t)h->nlon * h->nlat * h->nivbas;
-            CUDA_TRY(cudaMalloc(&h->mlp_feat, nc * MLP_FEAT * sizeof(float)));
-            CUDA_TRY(cudaMalloc(&h->mlp_y, nc * MLP_YOUT * sizeof(float)));
-            CUDA_TRY(cudaMalloc(&h->nt_xp, nc * NT_NX * sizeof(double)));
+            const long long nc = (long long)h->nlon * h->nlat * h->nivbas;
+            h->mlp_cap = (int)(nc < MLP_RESTART_CAP ? nc : MLP_RESTART_CAP);
+            CUDA_TRY(cudaMalloc(&h->mlp_feat, (size_t)h->mlp_cap * MLP_FEAT * sizeof(float)));
+            CUDA_TRY(cudaMalloc(&h->mlp_y, (size_t)h->mlp_cap * MLP_YOUT * sizeof(float)));
+            CUDA_TRY(cudaMalloc(&h->mlp_cells, (size_t)h->mlp_cap * sizeof(int)));
         }
-        P.warm = 1;
+        P.mlp_cap = h->mlp_cap;
         P.mlp_feat = h->mlp_feat;
         P.mlp_y = h->mlp_y;
+        P.mlp_cells = h->mlp_cells;
         P.mlp_err = mlp_err_flag(h->mlp);
-        P.nt_xp = h->nt_xp;
     }
     return choose_shape(h, P, mixed);
 }
 
-// warm start of all cells of P's range (inference and the warm-start
-// kernel), after the fronts of all its rows
-static int newton_warm(Handle* h, const Params& P) {
-    const int tb = 128;
-    CUDA_TRY(cudaMemsetAsync(mlp_err_flag(h->mlp), 0, sizeof(unsigned int), h->stream));
-    int rc = mlp_infer(h->mlp, h->mlp_feat, h->mlp_y, P.ncell, h->stream);
-    if (rc) return rc;
-    k_nt_warm<<<(P.ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
-    return REPROBUS_OK;
-}
-
 // the persistent solve of the cells of P's work queue; e0/e1 recorded around
-// it unless null. (A warm start that misses the convergence test is retried
-// from the saved plain start by the solve kernel itself, nt_end_attempt.)
+// it unless null
 static int newton_solve(Handle* h, const Params& P, cudaEvent_t e0, cudaEvent_t e1, bool capturing) {
     const int ip = h->solver == REPROBUS_SOLVER_NEWTON_MIXED ? 0 : 1;
     if (e0) CUDA_TRY(capturing ? cudaEventRecordWithFlags(e0, h->stream, cudaEventRecordExternal)
@@ -1219,6 +1207,27 @@ static int newton_solve(Handle* h, const Params& P, cudaEvent_t e0, cudaEvent_t 
     CUDA_TRY(h->nt_var[ip]->launch(P, h->nsm * h->nt_bps[ip], h->stream));
     if (e1) CUDA_TRY(capturing ? cudaEventRecordWithFlags(e1, h->stream, cudaEventRecordExternal)
                                : cudaEventRecord(e1, h->stream));
+    return REPROBUS_OK;
+}
+
+// The learned restart of the cells of P's window whose Newton iteration
+// missed (after newton_solve on P's queue): P's queue is emptied and refilled
+// with those cells (at most mlp_cap), each started from the network's
+// prediction for its plain start, and solved again. The cell counts stay on
+// the device: the inference and the warm-start kernel read them there.
+// Returns the kernels launched.
+static int newton_restart(Handle* h, const Params& P, int* launches) {
+    const int tb = 128;
+    if (P.win_ncell <= 0) return REPROBUS_OK;
+    CUDA_TRY(cudaMemsetAsync(P.nt_head, 0, 4 * sizeof(int), h->stream));
+    CUDA_TRY(cudaMemsetAsync(mlp_err_flag(h->mlp), 0, sizeof(unsigned int), h->stream));
+    k_nt_start<3><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    int rc = mlp_infer(h->mlp, h->mlp_feat, h->mlp_y, h->mlp_cap, h->stream, P.nt_head + 3);
+    if (rc) return rc;
+    const int nb = (h->mlp_cap * NT_NX + tb - 1) / tb;
+    k_nt_warm<<<nb < 2 * h->nsm ? nb : 2 * h->nsm, tb, 0, h->stream>>>(P);
+    if ((rc = newton_solve(h, P, nullptr, nullptr, false))) return rc;
+    *launches += 4;
     return REPROBUS_OK;
 }
 
@@ -1236,11 +1245,8 @@ static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool c
     if (rc) return rc;
     const bool mixed = h->solver == REPROBUS_SOLVER_NEWTON_MIXED;
     if ((rc = enqueue_setup(h, P, mixed))) return rc;
-    if (h->mlp) {
-        if ((rc = newton_warm(h, P))) return rc;
-        *launches += 2;
-    }
     if ((rc = newton_solve(h, P, timed ? h->ev2 : nullptr, timed ? h->ev3 : nullptr, capturing))) return rc;
+    if (h->mlp && (rc = newton_restart(h, P, launches))) return rc;
     newton_back(h, P);
     *launches += mixed ? 6 : 5;  // setup, start (FP32 + FP64 redo), solve, finish, fallback
     return REPROBUS_OK;
@@ -1329,7 +1335,8 @@ static int step_stats(Handle* h, const Params& P, reprobus_stats* st, int launch
         }
         if (c[7])
             return set_err(REPROBUS_ERR_TIMEOUT,
-                           "the warm-start inference gave up waiting (its cells started from the plain start)");
+                           "the learned restart's inference gave up waiting (its cells started again from the plain "
+                           "start)");
         if (P.check && c[0]) return set_err(REPROBUS_ERR_NONFINITE, "%llu non-finite values in the step output", c[0]);
     }
     return REPROBUS_OK;
@@ -1693,16 +1700,17 @@ static int host_step_newton(Handle* h, const HostArrays& A, int ilat0, int ilat1
         launches += mixed ? 4 : 3;
     }
     set_window(P, 0, nrows);
-    if (h->mlp) {
-        if ((rc = newton_warm(h, P))) return rc;
-        launches += 2;
-    }
     for (int part = 0; part < 2; part++) {
         Params& Q = part == 0 ? PA : PB;
         if ((rc = newton_solve(h, Q, st ? (part ? h->ev4 : h->ev2) : nullptr, st ? (part ? h->ev5 : h->ev3) : nullptr,
                                false)))
             return rc;
         launches++;
+        if (h->mlp) {  // over the rows of this queue
+            const int a = part == 0 ? row0(0) : row0(nchunk - 1), b = part == 0 ? row0(nchunk - 1) : ilat1 + 1;
+            set_window(Q, a - ilat0, b - a);
+            if ((rc = newton_restart(h, Q, &launches))) return rc;
+        }
         for (int c = part == 0 ? 0 : nchunk - 1; c < (part == 0 ? nchunk - 1 : nchunk); c++) {
             const int a = row0(c), b = row0(c + 1) - 1;
             set_window(Q, a - ilat0, b - a + 1);

@@ -36,9 +36,10 @@ struct Params {
     double* col;               // scratch: o3t | colo2 | colno (ncell each) | sza_top (ncol)
     unsigned long long* nonfinite;  // [0] non-finite values, [1] Newton iterations,
                                     // [2] fallbacks, [3] max iterations of a cell,
-                                    // [4] warm restarts, [5] iterations of attempts
-                                    // that missed, [6] FP64 redos of the FP32 start,
-                                    // [7] warm-start inference timed out
+                                    // [4] cells restarted from the network's start,
+                                    // [5] iterations of attempts that missed,
+                                    // [6] FP64 redos of the FP32 start,
+                                    // [7] the learned restart's inference timed out
     double* diag;
     int npass, maxit;               // Newton: reference passes before, iteration cap
     double tol;                     // Newton: scaled step tolerance
@@ -49,13 +50,16 @@ struct Params {
     int* nt_stat;                   // 0 active, >0 converged at that iteration, -1 failed
     int* nt_list;                   // work queue: day cells from the front, night cells from the back
     int* nt_head;                   // [0] next queue entry, [1] day count, [2] night count,
-                                    // [4] next day entry, [5] next night entry (per-mode queues)
-    int npass_plain;                // reference passes of the plain start (restart after a warm-start miss)
-    int warm;                       // 1: features for the warm-start network, start from its prediction
-    float* mlp_feat;                // 64 raw features per cell (row-major)
-    const float* mlp_y;             // 64 predicted log10 end-of-step ratios per cell (57 used)
+                                    // [3] cells taken for the learned restart
+    int npass_plain;                // reference passes of the plain start
+    // learned restart: a cell whose plain start misses the convergence test
+    // gets slot k < mlp_cap; its features, the network's prediction and its
+    // cell index are stored at slot k
+    int mlp_cap;
+    float* mlp_feat;                // 64 raw features per slot (row-major)
+    const float* mlp_y;             // 64 predicted log10 end-of-step ratios per slot (57 used)
+    int* mlp_cells;                 // the cell of each slot
     const unsigned int* mlp_err;    // the inference kernel's error flag: set, the predictions are not used
-    double* nt_xp;                  // warm start: the plain start of every cell (NT_NX doubles)
     StepConst sc;
 };
 

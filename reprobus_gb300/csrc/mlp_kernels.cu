@@ -1,6 +1,7 @@
-// mlp_kernels.cu — the learned warm start of the Newton solvers: a 64-256-256-
-// 256-64 MLP (SiLU) with BF16 weights and activations and FP32 accumulation
-// on the tcgen05 tensor cores, trained on the GPU by these kernels.
+// mlp_kernels.cu — the network of the Newton solvers' learned restart (the
+// start of the cells whose plain start misses): a 64-256-256-256-64 MLP
+// (SiLU) with BF16 weights and activations and FP32 accumulation on the
+// tcgen05 tensor cores, trained on the GPU by these kernels.
 //
 //   k_gemm_tn<EPI>   C[M x N] = A[M x K] B[N x K]^T, one 128 x BN tile per CTA,
 //                    K in chunks of 64 staged in shared memory (tc_sm100.cuh
@@ -171,6 +172,7 @@ struct InferArgs {
     const float* X;              // B x 64 raw features
     float* Y;                    // B x 64 raw outputs (log10 corrections)
     int B;
+    const int* Bdev;             // set: rows = min(B, *Bdev), a count written on the device
     const uint8_t* img;          // WIMG_TOTAL bytes of weight images
     const float* b[MLP_NL];
     const float* norm;
@@ -226,6 +228,7 @@ __global__ void __launch_bounds__(MLP_INFER_THREADS, 1) k_mlp_infer(InferArgs a)
     __shared__ uint64_t bar, wbar[2];
     __shared__ uint32_t tslot;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (a.Bdev) a.B = min(a.B, max(*a.Bdev, 0));
     const int ntiles = (a.B + 127) / 128;
     const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
     const int nimg = my_tiles * WIMG_N;  // weight images this CTA loads in all
@@ -712,12 +715,13 @@ static int check_err(MlpNet* n, cudaStream_t s) {
     return REPROBUS_OK;
 }
 
-int mlp_infer(void* net, const float* X, float* Y, int B, cudaStream_t s) {
+int mlp_infer(void* net, const float* X, float* Y, int B, cudaStream_t s, const int* rows_dev) {
     MlpNet* n = (MlpNet*)net;
     InferArgs a{};
     a.X = X;
     a.Y = Y;
     a.B = B;
+    a.Bdev = rows_dev;
     a.img = n->img;
     for (int l = 0; l < MLP_NL; l++) a.b[l] = n->P + n->off(l) + wsize(l);
     a.norm = n->norm;

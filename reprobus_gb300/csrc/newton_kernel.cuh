@@ -33,25 +33,11 @@ __device__ __forceinline__ int nt_queue_cell(const Params& P, int q, int nday) {
     return q < nday ? P.nt_list[q] : P.nt_list[P.nt_qcap - 1 - (q - nday)];
 }
 
-// The end of an attempt of a lane's cell (done: iterations when converged, -1
-// when not). With the warm start, a first attempt that failed starts again
-// from the plain start that k_nt_warm saved: the lane keeps the cell and
-// returns true. Otherwise the cell's status is written and the lane wants a
-// new cell (false).
-__device__ __forceinline__ bool nt_end_attempt(const Params& P, int cell, int done, int& it, int& attempt) {
+// The end of a lane's cell (done: iterations when converged, -1 when not):
+// its status is written; the iterations of a cell that missed are counted.
+__device__ __forceinline__ void nt_end_cell(const Params& P, int cell, int done, int it) {
     if (done < 0) atomicAdd(P.nonfinite + 5, (unsigned long long)it);  // iterations spent in vain
-    if (done < 0 && P.warm && attempt == 0) {
-        const double* xp = P.nt_xp + (size_t)cell * NT_NX;
-        double* x = P.nt_x + (size_t)cell * NT_NX;
-#pragma unroll 4
-        for (int i = 0; i < NT_NX; i++) x[i] = xp[i];
-        atomicAdd(P.nonfinite + 4, 1ULL);  // warm restarts
-        attempt = 1;
-        it = 0;
-        return true;
-    }
     P.nt_stat[cell] = done;
-    return false;
 }
 
 template <typename TJ, int NTH, bool ZS>
@@ -63,7 +49,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
     const int nday = P.nt_head[1], nnight = P.nt_head[2];  // queue: day cells, then night cells
     const int nq = nday + nnight;
     int cell = -1;  // >= 0: cell in work; -1: wants a cell; -2: queue exhausted
-    int it = 0, attempt = 0;  // attempt 1: the retry of a missed warm start
+    int it = 0;
     for (;;) {
         const unsigned want = __ballot_sync(0xffffffffu, cell == -1);
         if (want) {
@@ -75,7 +61,6 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
                 const int q = base + __popc(want & ((1u << lane) - 1u));
                 cell = q < nq ? nt_queue_cell(P, q, nday) : -2;
                 it = 0;
-                attempt = 0;
             }
         }
         if (__all_sync(0xffffffffu, cell == -2)) break;
@@ -103,7 +88,10 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve(Params P) {
                 done = it;
             else if (it >= P.maxit)
                 done = -1;
-            if (done && !nt_end_attempt(P, cell, done, it, attempt)) cell = -1;
+            if (done) {
+                nt_end_cell(P, cell, done, it);
+                cell = -1;
+            }
         }
     }
 }
@@ -131,7 +119,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_pp(Params P) {
     const int nday = P.nt_head[1], nnight = P.nt_head[2];
     const int nq = nday + nnight;
     int cell = -1;  // >= 0: cell in work; -1: wants a cell; -2: queue exhausted
-    int it = 0, attempt = 0;  // attempt 1: the retry of a missed warm start
+    int it = 0;
     bool has_z = false;  // z holds the (solved) step of the cell's current iterate
     TJ z[NT_NX];
     for (int t = 0;; t++) {
@@ -153,7 +141,10 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_pp(Params P) {
                     done = it;
                 else if (it >= P.maxit)
                     done = -1;
-                if (done && !nt_end_attempt(P, cell, done, it, attempt)) cell = -1;
+                if (done) {
+                    nt_end_cell(P, cell, done, it);
+                    cell = -1;
+                }
             }
             const unsigned want = __ballot_sync(0xffffffffu, cell == -1);
             if (want) {
@@ -165,7 +156,6 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_pp(Params P) {
                     const int q = base + __popc(want & ((1u << lane) - 1u));
                     cell = q < nq ? nt_queue_cell(P, q, nday) : -2;
                     it = 0;
-                    attempt = 0;
                 }
             }
             if (cell >= 0) {
@@ -233,7 +223,7 @@ __global__ void __launch_bounds__(2 * NS, 1) k_nt_solve_sp(Params P) {
     const int nday = P.nt_head[1], nnight = P.nt_head[2];
     const int nq = nday + nnight;
     int cell = -1;  // matrix lanes: >= 0 cell in work; -1 wants a cell; -2 queue exhausted
-    int it = 0, attempt = 0;  // attempt 1: the retry of a missed warm start
+    int it = 0;
     // the matrix warps refill their lanes and publish the cells
     auto refill = [&]() {
         const unsigned want = __ballot_sync(0xffffffffu, cell == -1);
@@ -246,7 +236,6 @@ __global__ void __launch_bounds__(2 * NS, 1) k_nt_solve_sp(Params P) {
                 const int q = base + __popc(want & ((1u << lane) - 1u));
                 cell = q < nq ? nt_queue_cell(P, q, nday) : -2;
                 it = 0;
-                attempt = 0;
             }
         }
         cellbuf[t] = cell;
@@ -294,7 +283,10 @@ __global__ void __launch_bounds__(2 * NS, 1) k_nt_solve_sp(Params P) {
                     done = it;
                 else if (it >= P.maxit)
                     done = -1;
-                if (done && !nt_end_attempt(P, c, done, it, attempt)) cell = -1;
+                if (done) {
+                    nt_end_cell(P, c, done, it);
+                    cell = -1;
+                }
             }
             refill();
         }
@@ -341,7 +333,7 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_ls(Params P) {
     const unsigned lane = threadIdx.x & 31u;
     const int nday = P.nt_head[1], nnight = P.nt_head[2];
     const int nq = nday + nnight;
-    int cell = -1, it = 0, attempt = 0;
+    int cell = -1, it = 0;
     for (;;) {
         const unsigned want = __ballot_sync(0xffffffffu, cell == -1);
         if (want) {
@@ -353,7 +345,6 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_ls(Params P) {
                 const int q = base + __popc(want & ((1u << lane) - 1u));
                 cell = q < nq ? nt_queue_cell(P, q, nday) : -2;
                 it = 0;
-                attempt = 0;
             }
         }
         if (__syncthreads_and(cell == -2)) break;
@@ -395,7 +386,10 @@ __global__ void __launch_bounds__(NTH, 1) k_nt_solve_ls(Params P) {
                 done = it;
             else if (it >= P.maxit)
                 done = -1;
-            if (done && !nt_end_attempt(P, cell, done, it, attempt)) cell = -1;
+            if (done) {
+                nt_end_cell(P, cell, done, it);
+                cell = -1;
+            }
         }
     }
 }
@@ -483,7 +477,7 @@ __global__ void __launch_bounds__(32 * W * C, 1) k_nt_solve_wc(Params P) {
     int* cells = reinterpret_cast<int*>(base + (size_t)(NT_NSLOT + NT_NX) * 32 * sizeof(TJ));
     const int nday = P.nt_head[1], nnight = P.nt_head[2];
     const int nq = nday + nnight;
-    int cell = -1, it = 0, attempt = 0;  // warp 0 of the group: the lane's cell and its progress
+    int cell = -1, it = 0;  // warp 0 of the group: the lane's cell and its progress
     auto refill = [&]() {
         const unsigned want = __ballot_sync(0xffffffffu, cell == -1);
         if (want) {
@@ -495,7 +489,6 @@ __global__ void __launch_bounds__(32 * W * C, 1) k_nt_solve_wc(Params P) {
                 const int q = b + __popc(want & ((1u << lane) - 1u));
                 cell = q < nq ? nt_queue_cell(P, q, nday) : -2;
                 it = 0;
-                attempt = 0;
             }
         }
         cells[lane] = cell;
@@ -548,7 +541,10 @@ __global__ void __launch_bounds__(32 * W * C, 1) k_nt_solve_wc(Params P) {
                     done = it;
                 else if (it >= P.maxit)
                     done = -1;
-                if (done && !nt_end_attempt(P, c, done, it, attempt)) cell = -1;
+                if (done) {
+                    nt_end_cell(P, c, done, it);
+                    cell = -1;
+                }
             }
             refill();
         }

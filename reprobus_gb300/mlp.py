@@ -1,11 +1,12 @@
-"""The learned warm start of the Newton solvers (libreprobus_gb300.so,
+"""The network of the Newton solvers' learned restart (libreprobus_gb300.so,
 mlp_kernels.cu): a 64-256-256-256-64 MLP with SiLU, BF16 weights and
 activations and FP32 accumulation on the tcgen05 tensor cores, trained on
 the GPU by the library's own forward/backward kernels on cells that the plain
 FP64 Newton solver integrates.
 
-The network corrects the solvers' plain start (one reference pass from the
-start state). Features of a cell (64, raw): log10 of the 42 transported and
+The network corrects the solvers' plain start (npass reference passes from
+the start state); a solver uses the corrected start for the cells whose
+plain start misses the convergence test. Features of a cell (64, raw): log10 of the 42 transported and
 15 short-lived mixing ratios of the plain start (floored at 1e-30), T, ln p,
 cos(sza), log10 aerosol surface area (floored at 1e-12), latitude, time of
 day, 0. Targets (64, raw): log10 of the ratio of each of the 57 end-of-step
@@ -109,7 +110,7 @@ class Mlp:
     def set_wait_limit(self, polls=-1):
         """Polls after which the inference kernel's waits give up (-1: the
         default; 0: at once). A fault-handling hook: a wait that gives up
-        makes forward() and the warm-started step raise REPROBUS_ERR_TIMEOUT
+        makes forward() and a step with the learned restart raise REPROBUS_ERR_TIMEOUT
         and leaves the network usable."""
         chem._check(self.lib.reprobus_mlp_set_wait_limit(ctypes.c_void_p(self.handle), int(polls)))
 

@@ -1,4 +1,4 @@
-"""Trains the Newton solvers' warm-start network on the GPU.
+"""Trains the network of the Newton solvers' learned restart on the GPU.
 
 Training cells come from the plain FP64 Newton solver itself: seeded
 synthetic grids (the reference's own initial/ECMWF files are not available)

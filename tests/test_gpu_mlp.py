@@ -1,4 +1,4 @@
-"""GPU checks of the tensor-core (tcgen05) kernels of the learned warm start:
+"""GPU checks of the tensor-core (tcgen05) kernels of the learned restart:
 the BF16 GEMM against an FP32 product of the same BF16 operands."""
 import ctypes
 

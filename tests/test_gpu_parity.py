@@ -255,7 +255,8 @@ def test_host_entry_in_row_chunks_equals_device_entry(torch, solver, chunks, mon
     for host in (True, False):
         h = ChemStep.for_case(case, niter=5, flags=FUSE_CONSERV)
         if solver in ("mixed", "mlp"):
-            h.set_solver(SOLVER_NEWTON_MIXED)
+            # mlp: a cap of 4 iterations, so that cells of both work queues take the learned restart
+            h.set_solver(SOLVER_NEWTON_MIXED, maxit=4 if solver == "mlp" else 12)
             h.set_tuning(64, 1, 0)
         elif solver == "fp64":
             h.set_solver(SOLVER_NEWTON64)
@@ -280,3 +281,5 @@ def test_host_entry_in_row_chunks_equals_device_entry(torch, solver, chunks, mon
             assert np.array_equal(outs[k][f], outs[2][f]), (k, f)
         for key in ("ncells", "newton_iters", "fallbacks", "max_newton_iters", "warm_restarts", "nonfinite"):
             assert stats[k][key] == stats[2][key], (k, key)
+    if solver == "mlp":
+        assert stats[2]["warm_restarts"] > 0

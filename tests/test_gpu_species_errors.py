@@ -3,7 +3,7 @@ polar-winter mix (the distributions of the 30 %-polar-winter workload: 30 % of
 the columns in polar night, T 183-195 K, active ClOx), at the solvers'
 production settings (5 start passes, step tolerance 1e-4, maxit 16), for the
 FP64 solver, the mixed-precision solver and the mixed solver with the
-committed learned warm start. Written as a table when
+committed network's learned restart. Written as a table when
 REPROBUS_SPECIES_REPORT names a file.
 
 The oracle is Oracle-C: the reference pass map's fixed point by the oracle's

@@ -1,4 +1,4 @@
-"""CPU checks of the warm-start network's oracle and packing (no GPU)."""
+"""CPU checks of the learned-restart network's oracle and packing (no GPU)."""
 import numpy as np
 import pytest
 
