@@ -398,6 +398,27 @@ __global__ void __launch_bounds__(NTB) k_nt_setup(Params P) {
     }
 }
 
+// a cell into the work queue: day cells from the front of the list, night
+// cells from the back; one atomic per warp and class for the threads that
+// arrive together
+__device__ __forceinline__ void nt_enqueue(const Params& P, int cell, bool day) {
+    const unsigned act = __activemask();
+    const unsigned lane = threadIdx.x & 31u, below = (1u << lane) - 1u;
+    const unsigned dm = __ballot_sync(act, day), nm = act & ~dm;
+    const int leader = __ffs(act) - 1;
+    int dbase = 0, nbase = 0;
+    if ((int)lane == leader) {
+        if (dm) dbase = atomicAdd(P.nt_head + 1, __popc(dm));
+        if (nm) nbase = atomicAdd(P.nt_head + 2, __popc(nm));
+    }
+    dbase = __shfl_sync(act, dbase, leader);
+    nbase = __shfl_sync(act, nbase, leader);
+    if (day)
+        P.nt_list[dbase + __popc(dm & below)] = cell;
+    else
+        P.nt_list[P.nt_qcap - 1 - (nbase + __popc(nm & below))] = cell;
+}
+
 // the plain start of a cell from its record: P.npass_plain reference passes
 // from the start state (ck0 from the record, cc from hc) -> x; the cell
 // enters the work queue (day cells from the front, night cells from the
@@ -454,10 +475,7 @@ __global__ void __launch_bounds__(128) k_nt_start(Params P) {
         atomicAdd(P.nonfinite + 4, 1ULL);
     }
     P.nt_stat[cell] = 0;
-    if (F.sza <= 95.)
-        P.nt_list[atomicAdd(P.nt_head + 1, 1)] = cell;
-    else
-        P.nt_list[P.nt_qcap - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
+    nt_enqueue(P, cell, F.sza <= 95.);
     if (MODE == 2) atomicAdd(P.nonfinite + 6, 1ULL);
 }
 
@@ -513,10 +531,7 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
 #pragma unroll
     for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = nt_widen(cc[n]);
     P.nt_stat[cell] = 0;
-    if (day)
-        P.nt_list[atomicAdd(P.nt_head + 1, 1)] = cell;
-    else
-        P.nt_list[P.nt_qcap - 1 - atomicAdd(P.nt_head + 2, 1)] = cell;
+    nt_enqueue(P, cell, day);
 }
 
 // learned restart: x_i = max(x_i, 1e-30 hnm) 10^y_i for the cell of each
@@ -589,9 +604,16 @@ __device__ __forceinline__ void nt_cell_fix(const double* r, CellFix& F) {
 
 __global__ void __launch_bounds__(128) k_nt_finish(Params P) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.win_ncell) return;
-    const int cell = win_cell(P, t);
-    const int stat = P.nt_stat[cell];
+    const bool own = t < P.win_ncell;
+    const int cell = own ? win_cell(P, t) : 0;
+    const int stat = own ? P.nt_stat[cell] : 0;
+    // iteration statistics, one atomic per warp (blocks are whole warps)
+    const unsigned it = stat > 0 ? (unsigned)stat : 0u;
+    const unsigned sum = __reduce_add_sync(0xffffffffu, it), most = __reduce_max_sync(0xffffffffu, it);
+    if ((threadIdx.x & 31u) == 0 && sum) {
+        atomicAdd(P.nonfinite + 1, (unsigned long long)sum);
+        atomicMax(P.nonfinite + 3, (unsigned long long)most);
+    }
     if (stat <= 0) return;
     const double* r = P.nt_rec + (size_t)cell * NT_REC;
     const double* x = P.nt_x + (size_t)cell * NT_NX;
@@ -604,8 +626,6 @@ __global__ void __launch_bounds__(128) k_nt_finish(Params P) {
     ck[NBCON - 1] = r[NT_RCK0 + NBCON - 1];
 #pragma unroll
     for (int n = 0; n < NCM; n++) cc[n] = x[NBCON - 1 + n];
-    atomicAdd(P.nonfinite + 1, (unsigned long long)stat);
-    atomicMax(P.nonfinite + 3, (unsigned long long)stat);
     cell_epilogue<true>(P, C, ck, cc);
 }
 
@@ -1145,15 +1165,16 @@ static int choose_shape(Handle* h, Params& P, bool mixed) {
     float best = 1e30f;
     int bi = 0;
     const char* verbose = getenv("REPROBUS_TUNE_VERBOSE");  // print every candidate's time to stderr
+    // (events ev4/ev5: ev0 marks the start of the step being prepared)
     for (int c = 0; c < nc; c++) {
         int rc = enqueue_setup(h, P, mixed);
         if (rc) return rc;
-        CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+        CUDA_TRY(cudaEventRecord(h->ev4, h->stream));
         CUDA_TRY(cands[c].v->launch(P, h->nsm * cands[c].bps, h->stream));
-        CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
-        CUDA_TRY(cudaEventSynchronize(h->ev1));
+        CUDA_TRY(cudaEventRecord(h->ev5, h->stream));
+        CUDA_TRY(cudaEventSynchronize(h->ev5));
         float ms = 0.f;
-        CUDA_TRY(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+        CUDA_TRY(cudaEventElapsedTime(&ms, h->ev4, h->ev5));
         if (verbose && verbose[0] == '1')
             fprintf(stderr, "reprobus autotune: %s lanes %d zshared %d blocks/SM %d: %.3f ms\n",
                     mixed ? "fp32" : "fp64", cands[c].v->nth, cands[c].v->zshared, cands[c].bps, ms);
@@ -1165,6 +1186,8 @@ static int choose_shape(Handle* h, Params& P, bool mixed) {
     h->nt_var[ip] = cands[bi].v;
     h->nt_bps[ip] = cands[bi].bps;
     if (key[0]) tune_cache_store(cache, key, cands[bi].v->nth, cands[bi].v->zshared, cands[bi].bps, best);
+    // the trial solves counted iterations and FP64 redos: the step counts afresh
+    CUDA_TRY(cudaMemsetAsync(h->d_count, 0, 8 * sizeof(unsigned long long), h->stream));
     return REPROBUS_OK;
 }
 
