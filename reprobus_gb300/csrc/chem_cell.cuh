@@ -13,6 +13,7 @@
 #include <math.h>
 
 #include "chem_enums.h"
+#include "exp64.cuh"
 
 namespace rpb {
 
@@ -152,13 +153,13 @@ __device__ __forceinline__ double cell_jno(double sza_top, double hnm, double co
     double bd[3];
 #pragma unroll
     for (int b = 0; b < 3; b++) {
-        double to3 = exp(-c_jno_so3[b] * colo3);
+        double to3 = exp64(-c_jno_so3[b] * colo3);
         double sum = 0.;
 #pragma unroll
         for (int s = 0; s < 6; s++) {
-            double term = exp(-c_jno_so2[b][s] * colo2) *
-                          (c_jno_w1[b][s] * c_jno_sno1[b][s] * exp(-c_jno_sno1[b][s] * colno) +
-                           c_jno_w2[b][s] * c_jno_sno2[b][s] * exp(-c_jno_sno2[b][s] * colno));
+            double term = exp64(-c_jno_so2[b][s] * colo2) *
+                          (c_jno_w1[b][s] * c_jno_sno1[b][s] * exp64(-c_jno_sno1[b][s] * colno) +
+                           c_jno_w2[b][s] * c_jno_sno2[b][s] * exp64(-c_jno_sno2[b][s] * colno));
             sum = (s == 0) ? term : sum + term;
         }
         bd[b] = c_jno_dl[b] * c_jno_i0[b] * to3 * p * sum;
@@ -232,7 +233,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double pn0t = pn0 * 1013. * 0.75;
         double zmt = -2.7836 - 0.00088 * t;
         double zbt = 38.9855 - 11397.0 / t + 0.009179 * t;
-        double zhno3eq = exp(zmt * log(pw * 1013. * 0.75) + zbt * LN10);
+        double zhno3eq = exp64(zmt * log(pw * 1013. * 0.75) + zbt * LN10);
         if (pn0t / zhno3eq >= 1.) {
             lnat = 1;
             double pn = zhno3eq / (0.75 * 1013.);
@@ -267,7 +268,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             lice = 1;
             lnat = 0;
             anat = 0.;
-            double zh2oeq = exp((-2668.7 / t + 10.4310) * LN10);
+            double zh2oeq = exp64((-2668.7 / t + 10.4310) * LN10);
             double ph2o = zh2oeq / 760.0;
             double h2os = fmax(pw - ph2o, 0.) * 1013. * hnm / ptot;
             double vice = h2os * amu * 18. / 0.928;
@@ -278,7 +279,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             A.parth2o = fmin(A.parth2o, 1.);
             double zmt = -2.7836 - 0.00088 * t;
             double zbt = 38.9855 - 11397.0 / t + 0.009179 * t;
-            double zhno3eq = exp(zmt * log(pw * A.parth2o * 1013. * 0.75) + zbt * LN10);
+            double zhno3eq = exp64(zmt * log(pw * A.parth2o * 1013. * 0.75) + zbt * LN10);
             double pn = zhno3eq / (0.75 * 1013.);
             parthno3s = 1.0 - (pn0 - pn) / pn0;
             parthno3s = fmax(parthno3s, 0.);
@@ -318,8 +319,8 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         wn = 0.0;
         double wts = fmax(41., ws * 100.);
         double wd = wts - 40.;
-        double muh2so4 = 4.184 * (1.514e4 - 286. * wd + 1.08 * (wd * wd) - 3941. / exp(0.1 * log(wd)));
-        double ph2so4 = exp(-10156. * rt + 16.2590 - muh2so4 * (rt / 8.314));
+        double muh2so4 = 4.184 * (1.514e4 - 286. * wd + 1.08 * (wd * wd) - 3941. / exp64(0.1 * log(wd)));
+        double ph2so4 = exp64(-10156. * rt + 16.2590 - muh2so4 * (rt / 8.314));
         if (qh2so4 * ptot / 1013. <= ph2so4) {
             ms = 0.;
             ws = 0.;
@@ -333,7 +334,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             double tr2 = tr * tr, tr3 = tr2 * tr, pr2 = pr * pr, pr3 = pr2 * pr;
             double hsb = qs[1] + qs[2] * tr2 + (qs[3] + qs[4] * tr + qs[5] * tr2 + qs[6] * tr3) * pr +
                          (qs[7] + qs[8] * tr + qs[9] * tr2) * pr2 + qs[10] * tr * pr3;
-            hsb = exp(hsb);
+            hsb = exp64(hsb);
             double kx = kn[1] + kn[2] * rt;
             double xnb = 1.0 / (2.0 * (kn[3] + kn[4] * rt)) *
                          (-kn[1] - kn[2] * rt -
@@ -341,7 +342,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             double mnb = 55.51 * xnb / (1.0 - xnb);
             double hnb = qn[1] + qn[2] * tr2 + (qn[3] + qn[4] * tr + qn[5] * tr2 + qn[6] * tr3) * pr +
                          (qn[7] + qn[8] * tr + qn[9] * tr2) * pr2 + qn[10] * tr * pr3;
-            hnb = exp(hnb);
+            hnb = exp64(hnb);
             double mnb2 = mnb * mnb, msb2 = msb * msb;
             a = (tt * hnb * mnb2 - tt * hsb * mnb * msb - 2.0 * mnb2 * msb + mnb * msb2 + hnb * mnb * msb * pn0 -
                  hsb * msb2 * pn0) /
@@ -394,28 +395,28 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         aliq = 4.0 * PI * (rmode * rmode) * ndrop * AER_EXP_2;
         double t = tl;
         const double rt = 1. / t, rt2 = rt * rt, rt3 = rt2 * rt;
-        double ph2o0 = exp(18.452406985 - 3505.1578807 * rt - 330918.55082 * rt2 + 12725068.262 * rt3);
+        double ph2o0 = exp64(18.452406985 - 3505.1578807 * rt - 330918.55082 * rt2 + 12725068.262 * rt3);
         aw = pw * 1013. / ph2o0;
         aw = fmin(aw, 1.);
         int br = (aw <= 0.05) ? 0 : ((aw < 0.85) ? 1 : 2);
         const double law = log(aw);
-        double y1 = c_an_a1[br] * exp(c_an_b1[br] * law) + c_an_c1[br] * aw + c_an_d1[br];
-        double y2 = c_an_a2[br] * exp(c_an_b2[br] * law) + c_an_c2[br] * aw + c_an_d2[br];
+        double y1 = c_an_a1[br] * exp64(c_an_b1[br] * law) + c_an_c1[br] * aw + c_an_d1[br];
+        double y2 = c_an_a2[br] * exp64(c_an_b2[br] * law) + c_an_c2[br] * aw + c_an_d2[br];
         double m = y1 + (t - 190.) * (y2 - y1) * (1. / 70.);
         wt = 9800. * m / (98. * m + 1000.);
         wt = fmax(wt, 0.5);
         double mh2so4 = dens * wt / 9.8;
         double bigx = wt / (wt + (100. - wt) * 98. / 18.);
-        hhcl = (0.094 - 0.61 * bigx + 1.2 * (bigx * bigx)) * exp(-8.68 + (8515. - 10718. * exp(0.7 * log(bigx))) * rt);
+        hhcl = (0.094 - 0.61 * bigx + 1.2 * (bigx * bigx)) * exp64(-8.68 + (8515. - 10718. * exp64(0.7 * log(bigx))) * rt);
         double qhcl = ck[12] * rhnm;
         double phcl0 = qhcl * ptot / 1013.0;
         double phcl1 = (phcl0 / (r * t)) / (1. / (r * t) + hhcl * ns / ms);
         A.parthcl = 1.0 - (phcl0 - phcl1) / phcl0;
         double sclono2 = 0.306 + 24. * rt;
-        hclono2 = 1.6e-6 * exp(4710. * rt) * exp(-sclono2 * mh2so4);
+        hclono2 = 1.6e-6 * exp64(4710. * rt) * exp64(-sclono2 * mh2so4);
         double shocl = 0.0776 + 59.18 * rt;
-        hhocl = 1.91e-6 * exp(5862.4 * rt) * exp(-shocl * mh2so4);
-        hhobr = 4.6e-4 * exp(4.5e3 * rt);
+        hhocl = 1.91e-6 * exp64(5862.4 * rt) * exp64(-shocl * mh2so4);
+        hhobr = 4.6e-4 * exp64(4.5e3 * rt);
         // hhbr (F:3222-3228) feeds only the disabled HOCl+HBr branch of hetero
     }
     // total PSC area F:3240-3246, HNO3 partition F:3252-3258
@@ -439,7 +440,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             double L2 = L * L, L3 = L2 * L, L4 = L2 * L2, L5 = L3 * L2, L6 = L3 * L3;
             double ynre = c_an_bnre[0] + c_an_bnre[1] * L + c_an_bnre[2] * L2 + c_an_bnre[3] * L3 +
                           c_an_bnre[4] * L4 + c_an_bnre[5] * L5 + c_an_bnre[6] * L6;
-            double nre = exp(ynre);
+            double nre = exp64(ynre);
             if (nre >= 1.e-2) {
                 A.vsed = netha * nre / (2 * rhoair * rpart);
             } else {
@@ -448,7 +449,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
                 double us = 2.0 * (rpart * rpart) * 9.80665 * (rhopart - rhoair) / (9.0 * netha);
                 double shapek = 1.2;
                 A.vsed = us / shapek *
-                         (1.0 + 1.246 * lambda / rpart + 0.42 * lambda / rpart * exp(-(0.87 * rpart / lambda)));
+                         (1.0 + 1.246 * lambda / rpart + 0.42 * lambda / rpart * exp64(-(0.87 * rpart / lambda)));
             }
         }
     }
@@ -470,15 +471,15 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double wt2 = wt * wt, wt3 = wt2 * wt;
         double t0 = 144.11 + 0.166 * wt - 0.015 * wt2 + 2.18e-4 * wt3;
         double biga = 169.5 + 5.18 * wt - 0.0825 * wt2 + 3.27e-3 * wt3;
-        double eta = biga * exp(-1.43 * log(T)) * exp(448. / (T - t0));
+        double eta = biga * exp64(-1.43 * log(T)) * exp64(448. / (T - t0));
         const double Teta = T / eta;
         double sqT = sqrt(T);
-        double ah = exp(60.51 - 0.095 * wt + 0.0077 * wt2 - 1.61e-5 * wt3 - (1.76 + 2.52e-4 * wt2) * sqT +
-                        (-805.89 + 253.05 * exp(0.076 * log(wt))) / sqT);
+        double ah = exp64(60.51 - 0.095 * wt + 0.0077 * wt2 - 1.61e-5 * wt3 - (1.76 + 2.52e-4 * wt2) * sqT +
+                        (-805.89 + 253.05 * exp64(0.076 * log(wt))) / sqT);
         double dclono2 = 5.e-8 * Teta;
         double cclono2 = 1474. * sqT;
-        double kh2o = 1.95e10 * exp(-2800. * rT);
-        double khh = 1.22e12 * exp(-6200. * rT);
+        double kh2o = 1.95e10 * exp64(-2800. * rT);
+        double khh = 1.22e12 * exp64(-6200. * rT);
         double khydr = kh2o * aw + khh * ah * aw;
         double gbh2o = 4 * hclono2 * 0.082 * T * sqrt(dclono2 * khydr) / cclono2;
         double mhcl = hhcl * phcl;
@@ -487,7 +488,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double fclono2 = 1. / tanh(rmean / lclono2) - lclono2 / rmean;
         double grxn = fclono2 * gbh2o * sqrt(1. + khcl / khydr);
         double gbhcl = grxn * khcl / (khcl + khydr);
-        double gs = 66.12 * hclono2 * mhcl * exp(-1374. * rT);
+        double gs = 66.12 * hclono2 * mhcl * exp64(-1374. * rT);
         double fhcl = 1. / (1 + 0.612 * (gs + gbhcl) * pclono2 / phcl);
         double gps = fhcl * gs;
         double gbhclp = fhcl * gbhcl;
@@ -506,7 +507,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double ghoclhcl = 1. / (1. + 1. / (fhocl * grxn * fhcl));
         kl[4] = 0.25 * ghoclhcl * chocl * aliq * rZHCL;
         double mhobr = hhobr * phobr;
-        double k2hobrhcl = exp(0.542 * wt - 6.44e3 * rT + 10.3);
+        double k2hobrhcl = exp64(0.542 * wt - 6.44e3 * rT + 10.3);
         double ratio = mhobr / mhcl;
         if (ratio < 1.) {
             double k1hobrhcl = k2hobrhcl * mhcl;
@@ -527,7 +528,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         }
         double CBAR = 1400.1 * sqT;
         kl[2] = 0.25 * 0.1 * CBAR * aliq * rZH2O;
-        double gxrn = exp(29.24 - 0.396 * 100. * ws) + 0.114;
+        double gxrn = exp64(29.24 - 0.396 * 100. * ws) + 0.114;
         double gbrno3h2o = 1. / (1. / 0.805 + 1. / gxrn);
         CBAR = 1221.4 * sqT;
         kl[5] = 0.25 * gbrno3h2o * CBAR * aliq * rZH2O;
@@ -591,131 +592,131 @@ __device__ __forceinline__ void cell_rates(const double* troe, const double* ltr
     double ak0, ak1, rate, xpo, deq, l10, xk;
 #define RK(name) K[K_##name]
 #define TROE(I0, E0, I1, E1, OUT)                                                            \
-    ak0 = troe[I0] * exp(lntemp * (E0));                                                     \
-    ak1 = troe[I1] * exp(lntemp * (E1));                                                     \
+    ak0 = troe[I0] * exp64(lntemp * (E0));                                                     \
+    ak1 = troe[I1] * exp64(lntemp * (E1));                                                     \
     xk = ak0 * hnm;                                                                          \
     rate = xk * ak1 / (ak1 + xk);                                                            \
     l10 = (ltroe[I0] - ltroe[I1] + lnhnm + lntemp * ((E0) - (E1))) * (1. / LN10);           \
     xpo = 1. / (1. + l10 * l10);                                                             \
-    OUT = rate * exp(xln6 * xpo)
+    OUT = rate * exp64(xln6 * xpo)
     TROE(0, -1.3, 1, 0.2, RK(a1));
-    RK(a1et) = 1.63e-10 * exp(60. * rt);
-    RK(a2) = 1.4e-10 * exp(-470. * rt);
-    RK(a5) = 1.8e-11 * exp(180. * rt);
-    RK(a6) = 1.7e-12 * exp(-940. * rt);
-    RK(a6b) = 1.0e-14 * exp(-490. * rt);
-    double e200 = exp(200. * rt);
+    RK(a1et) = 1.63e-10 * exp64(60. * rt);
+    RK(a2) = 1.4e-10 * exp64(-470. * rt);
+    RK(a5) = 1.8e-11 * exp64(180. * rt);
+    RK(a6) = 1.7e-12 * exp64(-940. * rt);
+    RK(a6b) = 1.0e-14 * exp64(-490. * rt);
+    double e200 = exp64(200. * rt);
     RK(a7) = 3.0e-11 * e200;
-    double e250 = exp(250. * rt);
+    double e250 = exp64(250. * rt);
     RK(a17) = 4.8e-11 * e250;
-    RK(a19) = 2.8e-12 * exp(-1800. * rt);
-    double e270 = exp(270. * rt);
+    RK(a19) = 2.8e-12 * exp64(-1800. * rt);
+    double e270 = exp64(270. * rt);
     RK(a26) = 3.3e-12 * e270;
-    RK(a27) = 1.5e-12 * exp(19. * rt) + 2.1e-33 * exp(920. * rt) * hnm;
+    RK(a27) = 1.5e-12 * exp64(19. * rt) + 2.1e-33 * exp64(920. * rt) * hnm;
     RK(a30) = 1.8e-12;
     RK(a31) = 1.8e-12;
     RK(a36) = 1.5e-13 * (1. + .6 * pm / 1013.);
-    RK(b3) = 5.1e-12 * exp(210. * rt);
-    RK(b4) = 3.0e-12 * exp((-1500. * rt));
-    RK(b6) = 2.1e-11 * exp((100. * rt));
-    RK(b7) = 1.5e-11 * exp((-3600. * rt));
-    double em2450 = exp((-2450. * rt));
+    RK(b3) = 5.1e-12 * exp64(210. * rt);
+    RK(b4) = 3.0e-12 * exp64((-1500. * rt));
+    RK(b6) = 2.1e-11 * exp64((100. * rt));
+    RK(b7) = 1.5e-11 * exp64((-3600. * rt));
+    double em2450 = exp64((-2450. * rt));
     RK(b9) = 1.2e-13 * em2450;
     TROE(2, -4.4, 3, -0.7, RK(b12));
     TROE(4, -3.0, 5, 0.0, RK(b22));
     TROE(6, -3.4, 7, -1.1, RK(b23));
-    deq = 2.1e-27 * exp(10900. * rt);
+    deq = 2.1e-27 * exp64(10900. * rt);
     RK(b24) = RK(b23) / (deq * hnm);
-    double e460 = exp(460. * rt);
+    double e460 = exp64(460. * rt);
     {
-        double aux1 = 2.7e-17 * exp(2199. * rt);
-        double aux2 = 1. + aux1 / (6.5e-34 * exp(1335. * rt) * hnm);
+        double aux1 = 2.7e-17 * exp64(2199. * rt);
+        double aux2 = 1. + aux1 / (6.5e-34 * exp64(1335. * rt) * hnm);
         RK(b27) = 2.4e-14 * e460 + aux1 / aux2;
     }
-    RK(b28) = 1.3e-12 * exp(380. * rt);
-    deq = 2.7e-27 * exp(11000. * rt);
+    RK(b28) = 1.3e-12 * exp64(380. * rt);
+    deq = 2.7e-27 * exp64(11000. * rt);
     RK(b32) = RK(b12) / (deq * hnm);
-    double e20 = exp(20. * rt);
+    double e20 = exp64(20. * rt);
     RK(b38) = 4.63e-11 * e20;
     RK(b39) = 7.25e-11 * e20;
     RK(c1a) = 1.31e-10;
     RK(c1b) = 0.35e-10;
     RK(c1c) = 0.09e-10;
-    RK(c2) = 2.45e-12 * exp((-1775. * rt));
+    RK(c2) = 2.45e-12 * exp64((-1775. * rt));
     RK(c3) = 1.1e-10;
     TROE(16, -3.6, 17, 1.1, RK(c4));
-    RK(c5) = 2.8e-12 * exp((300. * rt));
-    RK(c7) = 3.8e-13 * exp((800. * rt));
-    RK(c8) = 5.5e-12 * exp(125. * rt);
-    double em1600 = exp((-1600. * rt));
+    RK(c5) = 2.8e-12 * exp64((300. * rt));
+    RK(c7) = 3.8e-13 * exp64((800. * rt));
+    RK(c8) = 5.5e-12 * exp64(125. * rt);
+    double em1600 = exp64((-1600. * rt));
     RK(c9) = 3.4e-11 * em1600;
-    RK(c10) = 8.1e-11 * exp((-30. * rt));
+    RK(c10) = 8.1e-11 * exp64((-30. * rt));
     RK(c12) = 5.2e-12;
-    RK(c14) = 9.5e-14 * exp((390. * rt));
-    RK(c15) = 3.9e-14 * exp((-900. * rt));
+    RK(c14) = 9.5e-14 * exp64((390. * rt));
+    RK(c15) = 3.9e-14 * exp64((-900. * rt));
     RK(c17a) = 3.8e-12 * e200 * 0.7;
     RK(c17b) = 3.8e-12 * e200 * 0.3;
-    RK(c18) = 3.3e-12 * exp((-115. * rt));
-    double em800 = exp((-800. * rt));
+    RK(c18) = 3.3e-12 * exp64((-115. * rt));
+    double em800 = exp64((-800. * rt));
     RK(c19) = 1.7e-11 * em800;
-    RK(d2) = 2.3e-11 * exp((-200. * rt));
-    RK(d3) = 2.8e-11 * exp(85. * rt);
-    double e290 = exp(290. * rt);
+    RK(d2) = 2.3e-11 * exp64((-200. * rt));
+    RK(d3) = 2.8e-11 * exp64(85. * rt);
+    double e290 = exp64(290. * rt);
     RK(d4) = 6.4e-12 * e290;
-    RK(d5) = 7.3e-12 * exp((-1280. * rt));
-    RK(d6) = 3.05e-11 * exp((-2270. * rt));
-    RK(d7) = 1.4e-11 * exp(269. * rt);
+    RK(d5) = 7.3e-12 * exp64((-1280. * rt));
+    RK(d6) = 3.05e-11 * exp64((-2270. * rt));
+    RK(d7) = 1.4e-11 * exp64(269. * rt);
     RK(d8) = 7.4e-12 * e270;
-    double e230 = exp(230. * rt);
+    double e230 = exp64(230. * rt);
     RK(d9) = 6.0e-13 * e230;
-    RK(d10) = 3.6e-11 * exp(-375. * rt);
-    RK(d11) = 1.8e-12 * exp((-250. * rt));
+    RK(d10) = 3.6e-11 * exp64(-375. * rt);
+    RK(d11) = 1.8e-12 * exp64((-250. * rt));
     TROE(8, -3.4, 9, -1.9, RK(d31));
-    double em840 = exp((-840. * rt));
+    double em840 = exp64((-840. * rt));
     RK(d32) = 3.6e-12 * em840;
     RK(d33) = 2.6e-12 * e290;
-    RK(d34) = 3.0e-12 * exp((-500. * rt));
+    RK(d34) = 3.0e-12 * exp64((-500. * rt));
     RK(d35) = 1.7e-13;
     TROE(10, -2., 11, -1., RK(d36));
-    RK(d37) = 3.4e-12 * exp((-130. * rt));
+    RK(d37) = 3.4e-12 * exp64((-130. * rt));
     TROE(12, -4.5, 13, -2.0, RK(d60));
-    deq = 1.72e-27 * exp(8649. * rt);
+    deq = 1.72e-27 * exp64(8649. * rt);
     RK(d61) = RK(d60) / (deq * hnm);
-    RK(d62) = 1.0e-12 * exp(-1590. * rt) + 3.0e-11 * em2450;
+    RK(d62) = 1.0e-12 * exp64(-1590. * rt) + 3.0e-11 * em2450;
     RK(d90) = 2.3e-10;
     RK(d91) = 1.4e-10;
     RK(d92) = 2.0e-10;
     RK(d93) = 3.3e-10;
-    RK(d94) = 1.64e-12 * exp((-1520. * rt));
-    RK(d95) = 2.4e-12 * exp((-1250. * rt));
+    RK(d94) = 1.64e-12 * exp64((-1520. * rt));
+    RK(d95) = 2.4e-12 * exp64((-1250. * rt));
     RK(d96) = 1.0e-10;
     RK(d97) = 1.05e-12 * em1600;
-    RK(e2) = 1.6e-11 * exp((-780. * rt));
+    RK(e2) = 1.6e-11 * exp64((-780. * rt));
     RK(e3) = 1.9e-11 * e230;
-    double e260 = exp(260. * rt);
+    double e260 = exp64(260. * rt);
     RK(e4) = 8.8e-12 * e260;
-    RK(e5a) = 9.5e-13 * exp(550. * rt);
+    RK(e5a) = 9.5e-13 * exp64(550. * rt);
     RK(e5b) = 2.3e-12 * e260;
     RK(e5c) = 4.1e-13 * e290;
     RK(e6) = 1.5e-12 * e230;
-    RK(e7) = 4.8e-12 * exp(-310. * rt);
-    RK(e8) = 1.9e-11 * exp(215. * rt);
+    RK(e7) = 4.8e-12 * exp64(-310. * rt);
+    RK(e8) = 1.9e-11 * exp64(215. * rt);
     RK(e9) = 1.5e-10;
     RK(e10) = 1.7e-11 * e250;
     RK(e11) = 5.5e-12 * e200;
     TROE(14, -3.2, 15, -2.9, RK(e13));
     RK(e15) = 4.5e-12 * e460;
-    RK(e16) = 1.2e-10 * exp((-430. * rt));
+    RK(e16) = 1.2e-10 * exp64((-430. * rt));
     RK(e50) = 1.8e-10;
-    RK(e51) = 2.35e-12 * exp((-1300. * rt));
+    RK(e51) = 2.35e-12 * exp64((-1300. * rt));
     RK(e52) = 1.5e-10;
     RK(e53) = 1.0e-10;
     RK(e54) = 2.0e-12 * em840;
     RK(hk1) = 4.23e-28 * hnm * (rt * rt);
-    RK(hk2) = 6.0e-34 * exp(2.4 * log(300. * rt)) * hnm;
-    RK(hk3) = 8.e-12 * exp((-2060. * rt));
-    RK(hk4) = 2.15e-11 * exp(110. * rt);
-    RK(hk5) = 3.3e-11 * exp(55. * rt);
+    RK(hk2) = 6.0e-34 * exp64(2.4 * log(300. * rt)) * hnm;
+    RK(hk3) = 8.e-12 * exp64((-2060. * rt));
+    RK(hk4) = 2.15e-11 * exp64(110. * rt);
+    RK(hk5) = 3.3e-11 * exp64(55. * rt);
 #undef TROE
 #undef RK
 }

@@ -15,6 +15,7 @@
 // loads of one species plane are coalesced.
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -423,22 +424,23 @@ __device__ __forceinline__ void nt_enqueue(const Params& P, int cell, bool day) 
 // from the start state (ck0 from the record, cc from hc) -> x; the cell
 // enters the work queue (day cells from the front, night cells from the
 // back). MODE 0: every cell; MODE 2: only cells whose FP32 start
-// (k_nt_start32) was not finite (stat < 0); MODE 3 (learned restart): only
-// cells whose Newton iteration missed (stat < 0), each in its own slot k <
-// P.mlp_cap (cells beyond the last slot keep stat < 0 and fall back), with
-// the network's features of the plain start at slot k.
+// (k_nt_start32) was not finite (stat < 0); MODE 3 (learned restart): the
+// cells of the slots that k_nt_collect filled, with the network's features
+// of the plain start at the cell's slot.
 template <int MODE>
 __global__ void __launch_bounds__(128) k_nt_start(Params P) {
     static_assert(MODE == 0 || MODE == 2 || MODE == 3, "start modes");
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.win_ncell) return;
-    const int cell = win_cell(P, t);
-    if (MODE != 0 && P.nt_stat[cell] >= 0) return;
-    int slot = 0;
-    if (MODE == 3) {
-        slot = atomicAdd(P.nt_head + 3, 1);
-        if (slot >= P.mlp_cap) return;
+    int cell;
+    if (MODE == 3) {  // thread t: slot t (k_nt_collect)
+        if (t >= min(P.nt_head[3], P.mlp_cap)) return;
+        cell = P.mlp_cells[t];
+    } else {
+        if (t >= P.win_ncell) return;
+        cell = win_cell(P, t);
+        if (MODE == 2 && P.nt_stat[cell] >= 0) return;
     }
+    const int slot = t;
     const double* r = P.nt_rec + (size_t)cell * NT_REC;
     CellFix F;
     F.o2 = r[NT_RF]; F.n2 = r[NT_RF + 1]; F.h2 = r[NT_RF + 2]; F.co2 = r[NT_RF + 3]; F.hnm = r[NT_RF + 4];
@@ -471,7 +473,6 @@ __global__ void __launch_bounds__(128) k_nt_start(Params P) {
         float4* o = reinterpret_cast<float4*>(P.mlp_feat + (size_t)slot * 64);
 #pragma unroll
         for (int i = 0; i < 16; i++) o[i] = make_float4(fe[4 * i], fe[4 * i + 1], fe[4 * i + 2], fe[4 * i + 3]);
-        P.mlp_cells[slot] = cell;
         atomicAdd(P.nonfinite + 4, 1ULL);
     }
     P.nt_stat[cell] = 0;
@@ -532,6 +533,18 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
     for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = nt_widen(cc[n]);
     P.nt_stat[cell] = 0;
     nt_enqueue(P, cell, day);
+}
+
+// learned restart: each cell of the window whose Newton iteration missed
+// (stat < 0) takes a slot k < P.mlp_cap (cells beyond the last slot keep
+// stat < 0 and fall back); P.nt_head[3] counts the cells that asked
+__global__ void __launch_bounds__(128) k_nt_collect(Params P) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= P.win_ncell) return;
+    const int cell = win_cell(P, t);
+    if (P.nt_stat[cell] >= 0) return;
+    const int slot = atomicAdd(P.nt_head + 3, 1);
+    if (slot < P.mlp_cap) P.mlp_cells[slot] = cell;
 }
 
 // learned restart: x_i = max(x_i, 1e-30 hnm) 10^y_i for the cell of each
@@ -602,19 +615,34 @@ __device__ __forceinline__ void nt_cell_fix(const double* r, CellFix& F) {
     F.sza = r[NT_RSZA];
 }
 
+// MODE 0: the cells of the window that converged from the plain start
+// (0 < stat < NT_RESTART_BIAS); MODE 1: the cells of the learned restart's
+// slots that converged in its solve (stat >= NT_RESTART_BIAS). The two touch
+// disjoint cells, and neither reads a status that the other's solve may still
+// change, so MODE 0 may run while the restart is in flight.
+template <int MODE>
 __global__ void __launch_bounds__(128) k_nt_finish(Params P) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool own = t < P.win_ncell;
-    const int cell = own ? win_cell(P, t) : 0;
+    bool own;
+    int cell = 0;
+    if (MODE == 0) {
+        own = t < P.win_ncell;
+        if (own) cell = win_cell(P, t);
+    } else {
+        own = t < min(P.nt_head[3], P.mlp_cap);
+        if (own) cell = P.mlp_cells[t];
+    }
     const int stat = own ? P.nt_stat[cell] : 0;
+    const int lo = MODE == 0 ? 0 : NT_RESTART_BIAS, hi = MODE == 0 ? NT_RESTART_BIAS : INT_MAX;
+    const bool mine = stat > lo && stat < hi;
     // iteration statistics, one atomic per warp (blocks are whole warps)
-    const unsigned it = stat > 0 ? (unsigned)stat : 0u;
+    const unsigned it = mine ? (unsigned)(stat - lo) : 0u;
     const unsigned sum = __reduce_add_sync(0xffffffffu, it), most = __reduce_max_sync(0xffffffffu, it);
     if ((threadIdx.x & 31u) == 0 && sum) {
         atomicAdd(P.nonfinite + 1, (unsigned long long)sum);
         atomicMax(P.nonfinite + 3, (unsigned long long)most);
     }
-    if (stat <= 0) return;
+    if (!mine) return;
     const double* r = P.nt_rec + (size_t)cell * NT_REC;
     const double* x = P.nt_x + (size_t)cell * NT_NX;
     CellPro C;
@@ -728,6 +756,10 @@ struct Handle {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t ev2 = nullptr, ev3 = nullptr;  // around the persistent solve kernel (stats.solve_ms)
     cudaEvent_t ev4 = nullptr, ev5 = nullptr;  // around a second solve (host-array entry point)
+    // the learned restart runs on its own stream of the highest priority
+    // while the handle's stream writes back the converged cells
+    cudaStream_t rstream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // device mirrors for the host-pointer entry point (allocated on first use)
     double* m_alt = nullptr;
     double* m_traj[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -830,6 +862,9 @@ static void free_handle(Handle* h) {
     if (h->ev3) cudaEventDestroy(h->ev3);
     if (h->ev4) cudaEventDestroy(h->ev4);
     if (h->ev5) cudaEventDestroy(h->ev5);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->rstream) cudaStreamDestroy(h->rstream);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
 }
@@ -885,6 +920,8 @@ extern "C" int reprobus_chem_init(const double* ajl, const double* o3up, const d
         (e = cudaEventCreate(&h->ev0)) != cudaSuccess || (e = cudaEventCreate(&h->ev1)) != cudaSuccess ||
         (e = cudaEventCreate(&h->ev2)) != cudaSuccess || (e = cudaEventCreate(&h->ev3)) != cudaSuccess ||
         (e = cudaEventCreate(&h->ev4)) != cudaSuccess || (e = cudaEventCreate(&h->ev5)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaMalloc(&h->d_ajl, najl * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&h->d_o3up, 80 * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&h->d_col, (3 * ncell + ncol) * sizeof(double))) != cudaSuccess ||
@@ -1234,23 +1271,29 @@ static int newton_solve(Handle* h, const Params& P, cudaEvent_t e0, cudaEvent_t 
 }
 
 // The learned restart of the cells of P's window whose Newton iteration
-// missed (after newton_solve on P's queue): P's queue is emptied and refilled
-// with those cells (at most mlp_cap), each started from the network's
-// prediction for its plain start, and solved again. The cell counts stay on
-// the device: the inference and the warm-start kernel read them there.
-// Returns the kernels launched.
-static int newton_restart(Handle* h, const Params& P, int* launches) {
+// missed (after newton_solve on P's queue), on stream st: P's queue is emptied
+// and refilled with those cells (at most mlp_cap), each started from the
+// network's prediction for its plain start and solved again; the cells that
+// converge are written back. The cell counts stay on the device: the kernels
+// over slots read them there.
+static int newton_restart(Handle* h, const Params& P0, cudaStream_t st, int* launches) {
     const int tb = 128;
-    if (P.win_ncell <= 0) return REPROBUS_OK;
-    CUDA_TRY(cudaMemsetAsync(P.nt_head, 0, 4 * sizeof(int), h->stream));
-    CUDA_TRY(cudaMemsetAsync(mlp_err_flag(h->mlp), 0, sizeof(unsigned int), h->stream));
-    k_nt_start<3><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
-    int rc = mlp_infer(h->mlp, h->mlp_feat, h->mlp_y, h->mlp_cap, h->stream, P.nt_head + 3);
+    if (P0.win_ncell <= 0) return REPROBUS_OK;
+    Params P = P0;
+    P.stat_bias = NT_RESTART_BIAS;
+    const int ip = h->solver == REPROBUS_SOLVER_NEWTON_MIXED ? 0 : 1;
+    const unsigned nslot = (unsigned)((h->mlp_cap + tb - 1) / tb);
+    CUDA_TRY(cudaMemsetAsync(P.nt_head, 0, 4 * sizeof(int), st));
+    CUDA_TRY(cudaMemsetAsync(mlp_err_flag(h->mlp), 0, sizeof(unsigned int), st));
+    k_nt_collect<<<(P.win_ncell + tb - 1) / tb, tb, 0, st>>>(P);
+    k_nt_start<3><<<nslot, tb, 0, st>>>(P);
+    int rc = mlp_infer(h->mlp, h->mlp_feat, h->mlp_y, h->mlp_cap, st, P.nt_head + 3);
     if (rc) return rc;
-    const int nb = (h->mlp_cap * NT_NX + tb - 1) / tb;
-    k_nt_warm<<<nb < 2 * h->nsm ? nb : 2 * h->nsm, tb, 0, h->stream>>>(P);
-    if ((rc = newton_solve(h, P, nullptr, nullptr, false))) return rc;
-    *launches += 4;
+    const unsigned nb = (unsigned)((h->mlp_cap * NT_NX + tb - 1) / tb);
+    k_nt_warm<<<nb < 2u * h->nsm ? nb : 2u * h->nsm, tb, 0, st>>>(P);
+    CUDA_TRY(h->nt_var[ip]->launch(P, h->nsm * h->nt_bps[ip], st));
+    k_nt_finish<1><<<nslot, tb, 0, st>>>(P);
+    *launches += 6;
     return REPROBUS_OK;
 }
 
@@ -1258,7 +1301,7 @@ static int newton_restart(Handle* h, const Params& P, int* launches) {
 // reference passes for the others
 static void newton_back(Handle* h, const Params& P) {
     const int tb = 128;
-    k_nt_finish<<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    k_nt_finish<0><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     k_nt_fallback<<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
 }
 
@@ -1269,8 +1312,25 @@ static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool c
     const bool mixed = h->solver == REPROBUS_SOLVER_NEWTON_MIXED;
     if ((rc = enqueue_setup(h, P, mixed))) return rc;
     if ((rc = newton_solve(h, P, timed ? h->ev2 : nullptr, timed ? h->ev3 : nullptr, capturing))) return rc;
-    if (h->mlp && (rc = newton_restart(h, P, launches))) return rc;
-    newton_back(h, P);
+    if (h->mlp) {
+        // the restart on its own stream while this one writes back the cells
+        // that converged; the fallback waits for both
+        const int tb = 128;
+        if (!h->rstream) {
+            int lo = 0, hi = 0;
+            CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+            CUDA_TRY(cudaStreamCreateWithPriority(&h->rstream, cudaStreamNonBlocking, hi));
+        }
+        CUDA_TRY(cudaEventRecord(h->ev_fork, h->stream));
+        CUDA_TRY(cudaStreamWaitEvent(h->rstream, h->ev_fork, 0));
+        if ((rc = newton_restart(h, P, h->rstream, launches))) return rc;
+        k_nt_finish<0><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        CUDA_TRY(cudaEventRecord(h->ev_join, h->rstream));
+        CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
+        k_nt_fallback<<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    } else {
+        newton_back(h, P);
+    }
     *launches += mixed ? 6 : 5;  // setup, start (FP32 + FP64 redo), solve, finish, fallback
     return REPROBUS_OK;
 }
@@ -1732,7 +1792,7 @@ static int host_step_newton(Handle* h, const HostArrays& A, int ilat0, int ilat1
         if (h->mlp) {  // over the rows of this queue
             const int a = part == 0 ? row0(0) : row0(nchunk - 1), b = part == 0 ? row0(nchunk - 1) : ilat1 + 1;
             set_window(Q, a - ilat0, b - a);
-            if ((rc = newton_restart(h, Q, &launches))) return rc;
+            if ((rc = newton_restart(h, Q, h->stream, &launches))) return rc;
         }
         for (int c = part == 0 ? 0 : nchunk - 1; c < (part == 0 ? nchunk - 1 : nchunk); c++) {
             const int a = row0(c), b = row0(c + 1) - 1;

@@ -47,7 +47,9 @@ struct Params {
     double* nt_rec;                 // NT_REC FP64 fields: rates, fixed constants, day flag, ck0
     float* nt_rec32;                // NT_REC32 FP32 copies of the rate fields (mixed solver)
     double* nt_x;                   // iterate x (NT_NX per cell)
-    int* nt_stat;                   // 0 active, >0 converged at that iteration, -1 failed
+    int* nt_stat;                   // 0 active, >0 converged at that iteration (plus stat_bias), -1 failed
+    int stat_bias;                  // added to the iterations of a converged cell: 0 for the solve from the
+                                    // plain start, NT_RESTART_BIAS for the learned restart's solve
     int* nt_list;                   // work queue: day cells from the front, night cells from the back
     int* nt_head;                   // [0] next queue entry, [1] day count, [2] night count,
                                     // [3] cells taken for the learned restart
@@ -71,6 +73,7 @@ constexpr int NT_RK = 0, NT_RJ = NRATE, NT_RH = NRATE + NPHOT, NT_RF = NRATE + N
 constexpr int NT_RSZA = NT_RF + 14, NT_RCK0 = NT_RSZA + 1, NT_RSURF = NT_RCK0 + NBCON;
 constexpr int NT_REC = 208;    // FP64 record stride (1664 B = 13 lines of 128 B)
 constexpr int NT_REC32 = 168;  // FP32 record stride (164 used)
+constexpr int NT_RESTART_BIAS = 1 << 16;  // Params::stat_bias of the learned restart's solve
 static_assert(NT_RSURF < NT_REC, "record layout");
 
 __device__ __forceinline__ size_t plane3(const Params& P) { return (size_t)P.nlon * P.nlat * P.niv; }

@@ -34,10 +34,13 @@ __device__ __forceinline__ int nt_queue_cell(const Params& P, int q, int nday) {
 }
 
 // The end of a lane's cell (done: iterations when converged, -1 when not):
-// its status is written; the iterations of a cell that missed are counted.
+// its status is written (a converged cell's iterations plus P.stat_bias, so
+// that the write-back of the cells converged from the plain start and the
+// learned restart's solve may run at the same time); the iterations of a
+// cell that missed are counted.
 __device__ __forceinline__ void nt_end_cell(const Params& P, int cell, int done, int it) {
     if (done < 0) atomicAdd(P.nonfinite + 5, (unsigned long long)it);  // iterations spent in vain
-    P.nt_stat[cell] = done;
+    P.nt_stat[cell] = done > 0 ? done + P.stat_bias : done;
 }
 
 template <typename TJ, int NTH, bool ZS>

@@ -1,9 +1,10 @@
 """AddressSanitizer + UndefinedBehaviorSanitizer runs of the host C/C++ code
 that the CPU tests exercise: the chemistry oracle (oracle/chem_oracle.c, the
 reference scheme, Oracle-C's Newton with its staged restarts, conserv), the
-column oracle (oracle/column_oracle.cpp) and the host build of the generated
+column oracle (oracle/column_oracle.cpp), the host build of the generated
 Newton equations (tests/newton_host.cpp, which includes the same
-newton_gen.cuh and newton_solve.cuh as the CUDA kernels).
+newton_gen.cuh and newton_solve.cuh as the CUDA kernels) and that of the
+rate stage's exponential (tests/exp64_host.cpp, exp64.cuh).
 
 Each library is compiled again with -fsanitize=address,undefined (UBSan
 errors fatal) into a temporary folder, and the CPU test files that drive it
@@ -17,7 +18,8 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SAN = ["-fsanitize=address,undefined", "-fno-sanitize-recover=undefined", "-fno-omit-frame-pointer", "-g1"]
-FILES = ["tests/test_oracle_kat.py", "tests/test_column_oracle.py", "tests/test_newton_equations.py"]
+FILES = ["tests/test_oracle_kat.py", "tests/test_column_oracle.py", "tests/test_newton_equations.py",
+         "tests/test_exp64.py"]
 
 
 def _runtime(name):
