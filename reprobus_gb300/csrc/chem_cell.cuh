@@ -8,6 +8,10 @@
 // which is the same arithmetic because every block is elementwise in
 // (lon, level)). The vertical prefix sums of total (F:5153-5186) and jno
 // (JNO:107-126) are computed per column by k_columns before the cell kernel.
+// On GB300 every FP64 operation is scarce (2 per clock per SM), so the rate
+// stage divides by a constant as a product with its reciprocal (within an
+// ulp of the quotient) and takes its exponentials from exp64 (exp64.cuh,
+// within 1.5 ulp).
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -46,10 +50,10 @@ struct StepConst {
 // zenith, F:5382-5403 (per cell; the per-step part F:5340-5380 is in StepConst)
 // ----------------------------------------------------------------------------
 __device__ __forceinline__ double cell_zenith(const StepConst& sc, double lon, double lat) {
-    double rlt = lat * PI / 180.;
-    double lbut = 12. - sc.eqh - lon * 24. / 360.;
+    double rlt = lat * PI * (1. / 180.);
+    double lbut = 12. - sc.eqh - lon * 24. * (1. / 360.);
     double lzut = 15. * (sc.ut - lbut);
-    double zpt = lzut * PI / 180.;
+    double zpt = lzut * PI * (1. / 180.);
     double csz = sin(rlt) * sc.srd + cos(rlt) * sc.crd * cos(zpt);
     double zr = acos(csz);
     double s = zr * 180. / PI;
@@ -223,10 +227,10 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
     // F:2778-2787
     const double rhnm = 1. / hnm;
     double qh2o = ck[2] * rhnm;
-    double pw = qh2o * ptot / 1013.0;
+    double pw = qh2o * ptot * (1. / 1013.0);
     pw = fmin(pw, 2.e-3 / 1013.);
     double qhno3 = ck[4] * rhnm;
-    double pn0 = qhno3 * ptot / 1013.0;
+    double pn0 = qhno3 * ptot * (1. / 1013.0);
     // NAT F:2795-2857
     {
         double t = fmin(temp, 273.);
@@ -236,17 +240,17 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double zhno3eq = exp64(zmt * log(pw * 1013. * 0.75) + zbt * LN10);
         if (pn0t / zhno3eq >= 1.) {
             lnat = 1;
-            double pn = zhno3eq / (0.75 * 1013.);
+            double pn = zhno3eq * (1. / (0.75 * 1013.));
             double hno3s = (pn0 - pn) * 1013. * hnm / ptot;
             hno3s = fmax(hno3s, 0.);
-            vnat = hno3s * amu * 117. / 1.35;
+            vnat = hno3s * amu * 117. * (1. / 1.35);
             double vnat_small_max = nnat_small_max * (4. / 3. * PI * (rnats * rnats * rnats));
             if (vnat > vnat_small_max) {
                 nnats = nnat_small_max;
-                nnatl = (vnat - vnat_small_max) / (4. / 3. * PI * (rnatl * rnatl * rnatl));
+                nnatl = (vnat - vnat_small_max) * (1. / (4. / 3. * PI * (rnatl * rnatl * rnatl)));
                 vnatl = vnat - vnat_small_max;
             } else {
-                nnats = vnat / (4. / 3. * PI * (rnats * rnats * rnats));
+                nnats = vnat * (1. / (4. / 3. * PI * (rnats * rnats * rnats)));
                 nnatl = 0.;
                 vnatl = 0.;
             }
@@ -269,10 +273,10 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             lnat = 0;
             anat = 0.;
             double zh2oeq = exp64((-2668.7 / t + 10.4310) * LN10);
-            double ph2o = zh2oeq / 760.0;
+            double ph2o = zh2oeq * (1. / 760.0);
             double h2os = fmax(pw - ph2o, 0.) * 1013. * hnm / ptot;
-            double vice = h2os * amu * 18. / 0.928;
-            nice = vice / (4. / 3. * PI * (rice * rice * rice));
+            double vice = h2os * amu * 18. * (1. / 0.928);
+            nice = vice * (1. / (4. / 3. * PI * (rice * rice * rice)));
             aice = nice * 4 * PI * (rice * rice);
             A.parth2o = 1.0 - fmax(pw - ph2o, 0.) / pw;
             A.parth2o = fmax(A.parth2o, 0.);
@@ -280,7 +284,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             double zmt = -2.7836 - 0.00088 * t;
             double zbt = 38.9855 - 11397.0 / t + 0.009179 * t;
             double zhno3eq = exp64(zmt * log(pw * A.parth2o * 1013. * 0.75) + zbt * LN10);
-            double pn = zhno3eq / (0.75 * 1013.);
+            double pn = zhno3eq * (1. / (0.75 * 1013.));
             parthno3s = 1.0 - (pn0 - pn) / pn0;
             parthno3s = fmax(parthno3s, 0.);
             parthno3s = fmin(parthno3s, 1.);
@@ -295,13 +299,13 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double t = tl;
         const double rt = 1. / t;  // E / T as E * (1 / T) in the liquid-aerosol blocks
         double qh2ol = ck[2] * A.parth2o * rhnm;
-        pw = qh2ol * ptot / 1013.0;
+        pw = qh2ol * ptot * (1. / 1013.0);
         pw = fmin(pw, 2.e-3 / 1013.);
         pw = fmax(pw, 2.e-5 / 1013.);
         double qh2so4 = fmax(ck[11] * rhnm, 1.e-18);
-        ns = ptot * 100.0 * qh2so4 / 8.314 * rt;
+        ns = ptot * 100.0 * qh2so4 * (1. / 8.314) * rt;
         double qhno3l = ck[4] * parthno3s * rhnm;
-        pn0 = ptot / 1013.0 * qhno3l;
+        pn0 = ptot * (1. / 1013.0) * qhno3l;
         double a = ks[3] + ks[4] * rt;
         double b = ks[1] + ks[2] * rt;
         double cq = ks[5] + ks[6] * rt + ks[7] * log(t) - log(pw);
@@ -320,8 +324,8 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double wts = fmax(41., ws * 100.);
         double wd = wts - 40.;
         double muh2so4 = 4.184 * (1.514e4 - 286. * wd + 1.08 * (wd * wd) - 3941. / exp64(0.1 * log(wd)));
-        double ph2so4 = exp64(-10156. * rt + 16.2590 - muh2so4 * (rt / 8.314));
-        if (qh2so4 * ptot / 1013. <= ph2so4) {
+        double ph2so4 = exp64(-10156. * rt + 16.2590 - muh2so4 * (rt * (1. / 8.314)));
+        if (qh2so4 * ptot * (1. / 1013.) <= ph2so4) {
             ms = 0.;
             ws = 0.;
             condliq = 0;
@@ -383,14 +387,14 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
                     (X[11] + X[12] * T + X[13] * T2) * W * W;
         double VN = X[14] + X[15] * T + X[16] * T2 + (X[17] + X[18] * T + X[19] * T2) * W +
                     (X[20] + X[21] * T + X[22] * T2) * W * W;
-        double VMCAL = WH / 18.0160 * V1 + VS * ws / 98.080 + VN * wn / 63.0160;
+        double VMCAL = WH * (1. / 18.0160) * V1 + VS * ws * (1. / 98.080) + VN * wn * (1. / 63.0160);
         dens = 1.0 / VMCAL * 0.001;
     }
     // volume, radius, area, solubilities F:3068-3232
     double aw = 0., wt = 0., hhcl = 0., hhocl = 0., hhobr = 0., hclono2 = 0.;
     if (condliq == 1) {
         double vliq = ns * 98.076e-6 / ws / dens;
-        double rmode = cbrt(3.0 * vliq / (4. * PI * ndrop) * AER_EXP_M45);
+        double rmode = cbrt(3.0 * vliq * (1. / (4. * PI * ndrop)) * AER_EXP_M45);
         rmean = rmode * AER_EXP_05;
         aliq = 4.0 * PI * (rmode * rmode) * ndrop * AER_EXP_2;
         double t = tl;
@@ -405,11 +409,11 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double m = y1 + (t - 190.) * (y2 - y1) * (1. / 70.);
         wt = 9800. * m / (98. * m + 1000.);
         wt = fmax(wt, 0.5);
-        double mh2so4 = dens * wt / 9.8;
-        double bigx = wt / (wt + (100. - wt) * 98. / 18.);
+        double mh2so4 = dens * wt * (1. / 9.8);
+        double bigx = wt / (wt + (100. - wt) * 98. * (1. / 18.));
         hhcl = (0.094 - 0.61 * bigx + 1.2 * (bigx * bigx)) * exp64(-8.68 + (8515. - 10718. * exp64(0.7 * log(bigx))) * rt);
         double qhcl = ck[12] * rhnm;
-        double phcl0 = qhcl * ptot / 1013.0;
+        double phcl0 = qhcl * ptot * (1. / 1013.0);
         double phcl1 = (phcl0 / (r * t)) / (1. / (r * t) + hhcl * ns / ms);
         A.parthcl = 1.0 - (phcl0 - phcl1) / phcl0;
         double sclono2 = 0.306 + 24. * rt;
@@ -431,7 +435,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         rpart = fmin(rpart, 535.e-6);
         if (rpart >= 0.5e-6) {
             double rhopart = lice * rhoice + lnat * rhonat;
-            double rhoair = (hnm * 28.97 / 6.022e23) * 1000.0;
+            double rhoair = (hnm * 28.97 * (1. / 6.022e23)) * 1000.0;
             double tcel = t - 273.15;
             double netha = (1.718 + 0.0049 * tcel - 1.2e-5 * tcel * tcel) * 1.e-5;
             double rp3 = rpart * rpart * rpart;
@@ -445,7 +449,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
                 A.vsed = netha * nre / (2 * rhoair * rpart);
             } else {
                 double lambda0 = 6.6e-8;
-                double lambda = lambda0 * (1013.25 / ptot) * (t / 293.15);
+                double lambda = lambda0 * (1013.25 / ptot) * (t * (1. / 293.15));
                 double us = 2.0 * (rpart * rpart) * 9.80665 * (rhopart - rhoair) / (9.0 * netha);
                 double shapek = 1.2;
                 A.vsed = us / shapek *
@@ -615,7 +619,7 @@ __device__ __forceinline__ void cell_rates(const double* troe, const double* ltr
     RK(a27) = 1.5e-12 * exp64(19. * rt) + 2.1e-33 * exp64(920. * rt) * hnm;
     RK(a30) = 1.8e-12;
     RK(a31) = 1.8e-12;
-    RK(a36) = 1.5e-13 * (1. + .6 * pm / 1013.);
+    RK(a36) = 1.5e-13 * (1. + .6 * pm * (1. / 1013.));
     RK(b3) = 5.1e-12 * exp64(210. * rt);
     RK(b4) = 3.0e-12 * exp64((-1500. * rt));
     RK(b6) = 2.1e-11 * exp64((100. * rt));

@@ -487,10 +487,22 @@ __global__ void __launch_bounds__(128) k_nt_start(Params P) {
 // follows the FP64 zenith angle. A cell whose FP32 start is not finite (a
 // night-time NO2/NO3 ratio beyond the FP32 range) gets stat -1 and is started
 // again in FP64 by k_nt_start<2>; the others enter the work queue.
+// MODE 0: every cell of the window; MODE 3 (learned restart): the cells of
+// the slots that k_nt_collect filled, with the network's features of the
+// plain start at the cell's slot (a cell whose FP32 start is not finite keeps
+// stat -1 and falls back).
+template <int MODE>
 __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
+    static_assert(MODE == 0 || MODE == 3, "start modes");
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.win_ncell) return;
-    const int cell = win_cell(P, t);
+    int cell;
+    if (MODE == 3) {
+        if (t >= min(P.nt_head[3], P.mlp_cap)) return;
+        cell = P.mlp_cells[t];
+    } else {
+        if (t >= P.win_ncell) return;
+        cell = win_cell(P, t);
+    }
     const double* r = P.nt_rec + (size_t)cell * NT_REC;
     const float* q = P.nt_rec32 + (size_t)cell * NT_REC32;
     const double hnm = r[NT_RF + 4];
@@ -515,8 +527,9 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
     for (int n = 0; n < NBCON; n++) ck[n] = ck0[n] = nt_cvt<float>(r[NT_RCK0 + n]);
 #pragma unroll
     for (int n = 0; n < NCM; n++) cc[n] = nt_cvt<float>(P.hc[g + pl * n] * hnm);
+    const float dt = nt_cvt<float>(P.sc.dt);
 #pragma unroll 1
-    for (int it = 0; it < P.npass_plain; it++) cell_pass(F, K, tj, het, ck0, (float)P.sc.dt, ck, cc);
+    for (int it = 0; it < P.npass_plain; it++) cell_pass(F, K, tj, het, ck0, dt, ck, cc);
     bool finite = true;
 #pragma unroll
     for (int n = 0; n < NBCON - 1; n++) finite &= isfinite(ck[n]);
@@ -527,10 +540,23 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
         return;
     }
     double* x = P.nt_x + (size_t)cell * NT_NX;
+    double xd[NT_NX];
 #pragma unroll
-    for (int n = 0; n < NBCON - 1; n++) x[n] = nt_widen(ck[n]);
+    for (int n = 0; n < NBCON - 1; n++) x[n] = xd[n] = nt_widen(ck[n]);
 #pragma unroll
-    for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = nt_widen(cc[n]);
+    for (int n = 0; n < NCM; n++) x[NBCON - 1 + n] = xd[NBCON - 1 + n] = nt_widen(cc[n]);
+    if (MODE == 3) {
+        double ckd[NBCON];
+#pragma unroll
+        for (int n = 0; n < NBCON - 1; n++) ckd[n] = xd[n];
+        ckd[NBCON - 1] = 0.;
+        float fe[64];
+        cell_features(P, g, hnm, r[NT_RSZA], r[NT_RSURF], ckd, xd + NBCON - 1, fe);
+        float4* o = reinterpret_cast<float4*>(P.mlp_feat + (size_t)t * 64);
+#pragma unroll
+        for (int i = 0; i < 16; i++) o[i] = make_float4(fe[4 * i], fe[4 * i + 1], fe[4 * i + 2], fe[4 * i + 3]);
+        atomicAdd(P.nonfinite + 4, 1ULL);
+    }
     P.nt_stat[cell] = 0;
     nt_enqueue(P, cell, day);
 }
@@ -1090,7 +1116,7 @@ static void newton_front(Handle* h, const Params& P, bool mixed) {
     const int tb = 128;
     launch_setup(h, P, mixed);
     if (mixed) {
-        k_nt_start32<<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        k_nt_start32<0><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
         k_nt_start<2><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     } else {
         k_nt_start<0><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
@@ -1286,7 +1312,10 @@ static int newton_restart(Handle* h, const Params& P0, cudaStream_t st, int* lau
     CUDA_TRY(cudaMemsetAsync(P.nt_head, 0, 4 * sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(mlp_err_flag(h->mlp), 0, sizeof(unsigned int), st));
     k_nt_collect<<<(P.win_ncell + tb - 1) / tb, tb, 0, st>>>(P);
-    k_nt_start<3><<<nslot, tb, 0, st>>>(P);
+    if (h->solver == REPROBUS_SOLVER_NEWTON_MIXED)  // the plain start as the first attempt had it
+        k_nt_start32<3><<<nslot, tb, 0, st>>>(P);
+    else
+        k_nt_start<3><<<nslot, tb, 0, st>>>(P);
     int rc = mlp_infer(h->mlp, h->mlp_feat, h->mlp_y, h->mlp_cap, st, P.nt_head + 3);
     if (rc) return rc;
     const unsigned nb = (unsigned)((h->mlp_cap * NT_NX + tb - 1) / tb);
