@@ -804,6 +804,9 @@ struct Handle {
     int want_lanes = 0, want_bps = 0, want_zs = 0;   // reprobus_chem_set_tuning; lanes 0: autotune
     const NtVariant* nt_var[2] = {nullptr, nullptr};
     int nt_bps[2] = {0, 0};
+    // the learned restart's solve: a few hundred cells, so the form with the
+    // shortest iteration (4 warps per cell) rather than the autotuned one
+    const NtVariant* rs_var[2] = {nullptr, nullptr};
     // REF5 as the rate-stage kernel + the passes kernel through the cell
     // records (false: the single kernel k_chem, no record buffers)
     bool split_ref5 = true;
@@ -1275,6 +1278,15 @@ static int newton_prepare(Handle* h, Params& P) {
             CUDA_TRY(cudaMalloc(&h->mlp_y, (size_t)h->mlp_cap * MLP_YOUT * sizeof(float)));
             CUDA_TRY(cudaMalloc(&h->mlp_cells, (size_t)h->mlp_cap * sizeof(int)));
         }
+        const int ip = mixed ? 0 : 1;
+        if (!h->rs_var[ip]) {
+            int n = 0, occ = 0;
+            const NtVariant* v = mixed ? nt_variants_f32_wc(&n) : nt_variants_f64_wc(&n);
+            for (int i = 0; i < n; i++)
+                if (v[i].zshared == 6) h->rs_var[ip] = &v[i];
+            if (!h->rs_var[ip]) return set_err(REPROBUS_ERR_CUDA, "no 4-warps-per-cell solve form compiled");
+            CUDA_TRY(h->rs_var[ip]->prepare(&occ));
+        }
         P.mlp_cap = h->mlp_cap;
         P.mlp_feat = h->mlp_feat;
         P.mlp_y = h->mlp_y;
@@ -1320,7 +1332,7 @@ static int newton_restart(Handle* h, const Params& P0, cudaStream_t st, int* lau
     if (rc) return rc;
     const unsigned nb = (unsigned)((h->mlp_cap * NT_NX + tb - 1) / tb);
     k_nt_warm<<<nb < 2u * h->nsm ? nb : 2u * h->nsm, tb, 0, st>>>(P);
-    CUDA_TRY(h->nt_var[ip]->launch(P, h->nsm * h->nt_bps[ip], st));
+    CUDA_TRY(h->rs_var[ip]->launch(P, h->nsm, st));
     k_nt_finish<1><<<nslot, tb, 0, st>>>(P);
     *launches += 6;
     return REPROBUS_OK;
