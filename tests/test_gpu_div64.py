@@ -1,0 +1,35 @@
+"""div64 (reprobus_gb300/csrc/div64.cuh) on the GPU, from the hardware's
+reciprocal estimate: within one ulp of the IEEE quotient and equal to it
+but for rare operands, over the chemistry's magnitudes."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_device_quotients_match_ieee(tmp_path):
+    so = str(tmp_path / "libdiv64_dev.so")
+    subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-shared",
+                    "-Xcompiler", "-fPIC", "-o", so, os.path.join(ROOT, "tests", "div64_dev.cu")], check=True)
+    L = ctypes.CDLL(so)
+    L.div64_dev.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_long]
+    rng = np.random.default_rng(5)
+    n = 4_000_000
+    a = rng.choice([-1.0, 1.0], n) * 10.0 ** rng.uniform(-40, 30, n)
+    b = rng.choice([-1.0, 1.0], n) * 10.0 ** rng.uniform(-40, 30, n)
+    a = np.concatenate([a, rng.uniform(0.5, 2.0, n), [0.0, 1.0, 1.0, np.inf, np.nan]])
+    b = np.concatenate([b, rng.uniform(0.5, 2.0, n), [2.0, 0.0, 1e-310, 2.0, 2.0]])
+    q, ieee = np.empty_like(a), np.empty_like(a)
+    assert L.div64_dev(a.ctypes.data, b.ctypes.data, q.ctypes.data, ieee.ctypes.data, a.size) == 0
+    fin = np.isfinite(ieee) & (ieee != 0)
+    ulp = np.abs(q[fin] - ieee[fin]) / np.spacing(np.abs(ieee[fin]))
+    print(f"max {ulp.max():.2f} ulp; {np.mean(q[fin] != ieee[fin]):.2e} differ")
+    assert ulp.max() <= 1.0 and np.mean(q[fin] != ieee[fin]) < 1e-4
+    assert np.array_equal(np.isnan(q), np.isnan(ieee))
+    assert np.array_equal(q[~fin & ~np.isnan(q)], ieee[~fin & ~np.isnan(ieee)])
