@@ -10,13 +10,15 @@
 // (JNO:107-126) are computed per column by k_columns before the cell kernel.
 // On GB300 every FP64 operation is scarce (2 per clock per SM), so the rate
 // stage divides by a constant as a product with its reciprocal (within an
-// ulp of the quotient) and takes its exponentials from exp64 (exp64.cuh,
-// within 1.5 ulp).
+// ulp of the quotient), takes its exponentials from exp64 (exp64.cuh, within
+// 1.5 ulp) and the quotients of the rate constants and of the liquid aerosol
+// from div64 (div64.cuh, within an ulp).
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
 
 #include "chem_enums.h"
+#include "div64.cuh"
 #include "exp64.cuh"
 
 namespace rpb {
@@ -312,18 +314,18 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double det = b * b - 4. * a * cq;
         double msb;
         if (det > 0.) {
-            double xsb = (-b - sqrt(det)) / (2. * a);
-            msb = 55.51 * xsb / (1.0 - xsb);
+            double xsb = div64(-b - sqrt(det), 2. * a);
+            msb = div64(55.51 * xsb, 1.0 - xsb);
         } else {
             msb = 0.;
             condliq = 0;
         }
         ms = msb;
-        ws = msb * 0.098076 / (1.0 + msb * 0.098076);
+        ws = div64(msb * 0.098076, 1.0 + msb * 0.098076);
         wn = 0.0;
         double wts = fmax(41., ws * 100.);
         double wd = wts - 40.;
-        double muh2so4 = 4.184 * (1.514e4 - 286. * wd + 1.08 * (wd * wd) - 3941. / exp64(0.1 * log(wd)));
+        double muh2so4 = 4.184 * (1.514e4 - 286. * wd + 1.08 * (wd * wd) - div64(3941., exp64(0.1 * log(wd))));
         double ph2so4 = exp64(-10156. * rt + 16.2590 - muh2so4 * (rt * (1. / 8.314)));
         if (qh2so4 * ptot * (1. / 1013.) <= ph2so4) {
             ms = 0.;
@@ -388,34 +390,34 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double VN = X[14] + X[15] * T + X[16] * T2 + (X[17] + X[18] * T + X[19] * T2) * W +
                     (X[20] + X[21] * T + X[22] * T2) * W * W;
         double VMCAL = WH * (1. / 18.0160) * V1 + VS * ws * (1. / 98.080) + VN * wn * (1. / 63.0160);
-        dens = 1.0 / VMCAL * 0.001;
+        dens = div64(1.0, VMCAL) * 0.001;
     }
     // volume, radius, area, solubilities F:3068-3232
     double aw = 0., wt = 0., hhcl = 0., hhocl = 0., hhobr = 0., hclono2 = 0.;
     if (condliq == 1) {
-        double vliq = ns * 98.076e-6 / ws / dens;
+        double vliq = div64(div64(ns * 98.076e-6, ws), dens);
         double rmode = cbrt(3.0 * vliq * (1. / (4. * PI * ndrop)) * AER_EXP_M45);
         rmean = rmode * AER_EXP_05;
         aliq = 4.0 * PI * (rmode * rmode) * ndrop * AER_EXP_2;
         double t = tl;
         const double rt = 1. / t, rt2 = rt * rt, rt3 = rt2 * rt;
         double ph2o0 = exp64(18.452406985 - 3505.1578807 * rt - 330918.55082 * rt2 + 12725068.262 * rt3);
-        aw = pw * 1013. / ph2o0;
+        aw = div64(pw * 1013., ph2o0);
         aw = fmin(aw, 1.);
         int br = (aw <= 0.05) ? 0 : ((aw < 0.85) ? 1 : 2);
         const double law = log(aw);
         double y1 = c_an_a1[br] * exp64(c_an_b1[br] * law) + c_an_c1[br] * aw + c_an_d1[br];
         double y2 = c_an_a2[br] * exp64(c_an_b2[br] * law) + c_an_c2[br] * aw + c_an_d2[br];
         double m = y1 + (t - 190.) * (y2 - y1) * (1. / 70.);
-        wt = 9800. * m / (98. * m + 1000.);
+        wt = div64(9800. * m, 98. * m + 1000.);
         wt = fmax(wt, 0.5);
         double mh2so4 = dens * wt * (1. / 9.8);
-        double bigx = wt / (wt + (100. - wt) * 98. * (1. / 18.));
+        double bigx = div64(wt, wt + (100. - wt) * 98. * (1. / 18.));
         hhcl = (0.094 - 0.61 * bigx + 1.2 * (bigx * bigx)) * exp64(-8.68 + (8515. - 10718. * exp64(0.7 * log(bigx))) * rt);
         double qhcl = ck[12] * rhnm;
         double phcl0 = qhcl * ptot * (1. / 1013.0);
-        double phcl1 = (phcl0 / (r * t)) / (1. / (r * t) + hhcl * ns / ms);
-        A.parthcl = 1.0 - (phcl0 - phcl1) / phcl0;
+        double phcl1 = div64(div64(phcl0, r * t), div64(1., r * t) + div64(hhcl * ns, ms));
+        A.parthcl = 1.0 - div64(phcl0 - phcl1, phcl0);
         double sclono2 = 0.306 + 24. * rt;
         hclono2 = 1.6e-6 * exp64(4710. * rt) * exp64(-sclono2 * mh2so4);
         double shocl = 0.0776 + 59.18 * rt;
@@ -461,13 +463,13 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
     double kl[9] = {0., 0., 0., 0., 0., 0., 0., 0., 0.};
     double ksl[9] = {0., 0., 0., 0., 0., 0., 0., 0., 0.};  // K*S zero-initialised
     const double T = temp;
-    const double rT = 1. / T;
+    const double rT = div64(1., T);
     if (condliq == 1) {
         double ZH2O = fmax(ck[2], 1.E-08 * hnm);
         double ZHCL = fmax(ck[12], 1.E-13 * hnm);
         double ZCLONO2 = fmax(ck[13], 1.E-13 * hnm);
         double ZHOBR = fmax(ck[25], 1.E-15 * hnm);
-        const double rZH2O = 1. / ZH2O, rZHCL = 1. / ZHCL;
+        const double rZH2O = div64(1., ZH2O), rZHCL = div64(1., ZHCL);
         const double pfac = rhnm * ptot * (1. / 1013.);
         double phcl = ZHCL * pfac;
         double pclono2 = ZCLONO2 * pfac;
@@ -475,65 +477,65 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double wt2 = wt * wt, wt3 = wt2 * wt;
         double t0 = 144.11 + 0.166 * wt - 0.015 * wt2 + 2.18e-4 * wt3;
         double biga = 169.5 + 5.18 * wt - 0.0825 * wt2 + 3.27e-3 * wt3;
-        double eta = biga * exp64(-1.43 * log(T)) * exp64(448. / (T - t0));
-        const double Teta = T / eta;
+        double eta = biga * exp64(-1.43 * log(T)) * exp64(div64(448., T - t0));
+        const double Teta = div64(T, eta);
         double sqT = sqrt(T);
         double ah = exp64(60.51 - 0.095 * wt + 0.0077 * wt2 - 1.61e-5 * wt3 - (1.76 + 2.52e-4 * wt2) * sqT +
-                        (-805.89 + 253.05 * exp64(0.076 * log(wt))) / sqT);
+                        div64(-805.89 + 253.05 * exp64(0.076 * log(wt)), sqT));
         double dclono2 = 5.e-8 * Teta;
         double cclono2 = 1474. * sqT;
         double kh2o = 1.95e10 * exp64(-2800. * rT);
         double khh = 1.22e12 * exp64(-6200. * rT);
         double khydr = kh2o * aw + khh * ah * aw;
-        double gbh2o = 4 * hclono2 * 0.082 * T * sqrt(dclono2 * khydr) / cclono2;
+        double gbh2o = div64(4 * hclono2 * 0.082 * T * sqrt(dclono2 * khydr), cclono2);
         double mhcl = hhcl * phcl;
         double khcl = 7.9e11 * ah * dclono2 * mhcl;
-        double lclono2 = sqrt(dclono2 / (khydr + khcl));
-        double fclono2 = 1. / tanh(rmean / lclono2) - lclono2 / rmean;
-        double grxn = fclono2 * gbh2o * sqrt(1. + khcl / khydr);
-        double gbhcl = grxn * khcl / (khcl + khydr);
+        double lclono2 = sqrt(div64(dclono2, khydr + khcl));
+        double fclono2 = div64(1., tanh(div64(rmean, lclono2))) - div64(lclono2, rmean);
+        double grxn = fclono2 * gbh2o * sqrt(1. + div64(khcl, khydr));
+        double gbhcl = div64(grxn * khcl, khcl + khydr);
         double gs = 66.12 * hclono2 * mhcl * exp64(-1374. * rT);
-        double fhcl = 1. / (1 + 0.612 * (gs + gbhcl) * pclono2 / phcl);
+        double fhcl = div64(1., 1 + div64(0.612 * (gs + gbhcl) * pclono2, phcl));
         double gps = fhcl * gs;
         double gbhclp = fhcl * gbhcl;
-        double gb = gbhclp + grxn * khydr / (khcl + khydr);
-        double gclono2 = 1. / (1. + 1. / (gps + gb));
-        double gclono2hcl = gclono2 * (gps + gbhclp) / (gps + gb);
+        double gb = gbhclp + div64(grxn * khydr, khcl + khydr);
+        double gclono2 = div64(1., 1. + div64(1., gps + gb));
+        double gclono2hcl = div64(gclono2 * (gps + gbhclp), gps + gb);
         double gclono2h2o = gclono2 - gclono2hcl;
         kl[0] = 0.25 * gclono2h2o * cclono2 * aliq * rZH2O;
         kl[1] = 0.25 * gclono2hcl * cclono2 * aliq * rZHCL;
         double chocl = 2009. * sqT;
         double dhocl = 6.4e-8 * Teta;
         double khoclhcl = 1.25e9 * ah * dhocl * mhcl;
-        double lhocl = sqrt(dhocl / khoclhcl);
-        double fhocl = 1. / tanh(rmean / lhocl) - lhocl / rmean;
-        grxn = 4. * hhocl * 0.082 * T * sqrt(dhocl * khoclhcl) / chocl;
-        double ghoclhcl = 1. / (1. + 1. / (fhocl * grxn * fhcl));
+        double lhocl = sqrt(div64(dhocl, khoclhcl));
+        double fhocl = div64(1., tanh(div64(rmean, lhocl))) - div64(lhocl, rmean);
+        grxn = div64(4. * hhocl * 0.082 * T * sqrt(dhocl * khoclhcl), chocl);
+        double ghoclhcl = div64(1., 1. + div64(1., fhocl * grxn * fhcl));
         kl[4] = 0.25 * ghoclhcl * chocl * aliq * rZHCL;
         double mhobr = hhobr * phobr;
         double k2hobrhcl = exp64(0.542 * wt - 6.44e3 * rT + 10.3);
-        double ratio = mhobr / mhcl;
+        double ratio = div64(mhobr, mhcl);
         if (ratio < 1.) {
             double k1hobrhcl = k2hobrhcl * mhcl;
             double dhobr = 6.2e-8 * Teta;
-            double lhobr = sqrt(dhobr / k1hobrhcl);
-            double fhobr = 1. / tanh(rmean / lhobr) - lhobr / rmean;
+            double lhobr = sqrt(div64(dhobr, k1hobrhcl));
+            double fhobr = div64(1., tanh(div64(rmean, lhobr))) - div64(lhobr, rmean);
             double chobr = 1477. * sqT;
-            double ghobrhcl = 4. * hhobr * 0.082 * T * sqrt(dhobr * k1hobrhcl) * fhobr / chobr;
+            double ghobrhcl = div64(4. * hhobr * 0.082 * T * sqrt(dhobr * k1hobrhcl) * fhobr, chobr);
             kl[6] = 0.25 * ghobrhcl * chobr * aliq * rZHCL;
         } else {
             double k1hobrhcl = k2hobrhcl * mhobr;
             double dhcl = 7.8e-8 * Teta;
-            double lhcl = sqrt(dhcl / k1hobrhcl);
-            double fh = 1. / tanh(rmean / lhcl) - lhcl / rmean;
+            double lhcl = sqrt(div64(dhcl, k1hobrhcl));
+            double fh = div64(1., tanh(div64(rmean, lhcl))) - div64(lhcl, rmean);
             double chcl = 2408. * sqT;
-            double ghobrhcl = 4. * hhcl * 0.082 * T * sqrt(dhcl * k1hobrhcl) * fh / chcl;
-            kl[6] = 0.25 * ghobrhcl * chcl * aliq / ZHOBR;
+            double ghobrhcl = div64(4. * hhcl * 0.082 * T * sqrt(dhcl * k1hobrhcl) * fh, chcl);
+            kl[6] = div64(0.25 * ghobrhcl * chcl * aliq, ZHOBR);
         }
         double CBAR = 1400.1 * sqT;
         kl[2] = 0.25 * 0.1 * CBAR * aliq * rZH2O;
         double gxrn = exp64(29.24 - 0.396 * 100. * ws) + 0.114;
-        double gbrno3h2o = 1. / (1. / 0.805 + 1. / gxrn);
+        double gbrno3h2o = div64(1., 1. / 0.805 + div64(1., gxrn));
         CBAR = 1221.4 * sqT;
         kl[5] = 0.25 * gbrno3h2o * CBAR * aliq * rZH2O;
     }
@@ -592,16 +594,16 @@ __device__ __forceinline__ void cell_rates(const double* troe, const double* ltr
     const double xln6 = LN06;
     double lntemp = log(t);
     const double lnhnm = log(hnm);
-    const double rt = 1. / t;  // Arrhenius exponents E / T as E * (1 / T)
+    const double rt = div64(1., t);  // Arrhenius exponents E / T as E * (1 / T)
     double ak0, ak1, rate, xpo, deq, l10, xk;
 #define RK(name) K[K_##name]
 #define TROE(I0, E0, I1, E1, OUT)                                                            \
     ak0 = troe[I0] * exp64(lntemp * (E0));                                                     \
     ak1 = troe[I1] * exp64(lntemp * (E1));                                                     \
     xk = ak0 * hnm;                                                                          \
-    rate = xk * ak1 / (ak1 + xk);                                                            \
+    rate = div64(xk * ak1, ak1 + xk);                                                        \
     l10 = (ltroe[I0] - ltroe[I1] + lnhnm + lntemp * ((E0) - (E1))) * (1. / LN10);           \
-    xpo = 1. / (1. + l10 * l10);                                                             \
+    xpo = div64(1., 1. + l10 * l10);                                                         \
     OUT = rate * exp64(xln6 * xpo)
     TROE(0, -1.3, 1, 0.2, RK(a1));
     RK(a1et) = 1.63e-10 * exp64(60. * rt);
@@ -630,16 +632,16 @@ __device__ __forceinline__ void cell_rates(const double* troe, const double* ltr
     TROE(4, -3.0, 5, 0.0, RK(b22));
     TROE(6, -3.4, 7, -1.1, RK(b23));
     deq = 2.1e-27 * exp64(10900. * rt);
-    RK(b24) = RK(b23) / (deq * hnm);
+    RK(b24) = div64(RK(b23), deq * hnm);
     double e460 = exp64(460. * rt);
     {
         double aux1 = 2.7e-17 * exp64(2199. * rt);
-        double aux2 = 1. + aux1 / (6.5e-34 * exp64(1335. * rt) * hnm);
-        RK(b27) = 2.4e-14 * e460 + aux1 / aux2;
+        double aux2 = 1. + div64(aux1, 6.5e-34 * exp64(1335. * rt) * hnm);
+        RK(b27) = 2.4e-14 * e460 + div64(aux1, aux2);
     }
     RK(b28) = 1.3e-12 * exp64(380. * rt);
     deq = 2.7e-27 * exp64(11000. * rt);
-    RK(b32) = RK(b12) / (deq * hnm);
+    RK(b32) = div64(RK(b12), deq * hnm);
     double e20 = exp64(20. * rt);
     RK(b38) = 4.63e-11 * e20;
     RK(b39) = 7.25e-11 * e20;
@@ -685,7 +687,7 @@ __device__ __forceinline__ void cell_rates(const double* troe, const double* ltr
     RK(d37) = 3.4e-12 * exp64((-130. * rt));
     TROE(12, -4.5, 13, -2.0, RK(d60));
     deq = 1.72e-27 * exp64(8649. * rt);
-    RK(d61) = RK(d60) / (deq * hnm);
+    RK(d61) = div64(RK(d60), deq * hnm);
     RK(d62) = 1.0e-12 * exp64(-1590. * rt) + 3.0e-11 * em2450;
     RK(d90) = 2.3e-10;
     RK(d91) = 1.4e-10;

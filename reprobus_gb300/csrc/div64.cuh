@@ -1,6 +1,8 @@
 // div64.cuh — a / b in FP64 with five FP64-pipe instructions after an
 // approximate reciprocal: on GB300 the FP64 pipe issues 2 operations per
-// clock per SM, and the IEEE division sequence takes about 9.
+// clock per SM, and the IEEE division sequence takes about 9. For FP64-bound
+// code (the rate stage); in the latency-bound solve kernels the extra range
+// checks cost more than the FP64 instructions they save.
 //
 // Method: Newton-Raphson refinement of a reciprocal estimate r0 of b
 // (r1 = r0 + r0 (1 - b r0): the relative error squares), the quotient
@@ -22,9 +24,17 @@
 
 namespace rpb {
 
+// the IEEE division, out of line on the device: one call site per use of
+// div64 instead of an inline copy of its sequence
+#ifdef __CUDA_ARCH__
+static __device__ __noinline__ double div64_ieee(double a, double b) { return a / b; }
+#else
+inline double div64_ieee(double a, double b) { return a / b; }
+#endif
+
 __device__ __forceinline__ double div64(double a, double b) {
     const int ea = (int)((e64_hi(a) >> 20) & 0x7ffu), eb = (int)((e64_hi(b) >> 20) & 0x7ffu);
-    if (eb < 23 || eb > 2023 || ea < 23 || ea > 2023 || ea - eb > 1000 || eb - ea > 1000) return a / b;
+    if (eb < 23 || eb > 2023 || ea < 23 || ea > 2023 || ea - eb > 1000 || eb - ea > 1000) return div64_ieee(a, b);
 #ifdef __CUDA_ARCH__
     double r;
     asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(b));

@@ -15,8 +15,6 @@
 #include <cstdint>
 #include <cstring>
 
-#include "div64.cuh"
-
 // compiler-level memory fence: no load or store is moved across it, so the
 // generated factorisation keeps each row's loads in that row
 #ifdef __CUDA_ARCH__
@@ -97,17 +95,6 @@ __device__ __forceinline__ float nt_cvt<float>(double v) {
     else
         f = sign | ((uint32_t)(E - 896) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
     return nt_f32_from_bits(f);
-}
-
-// the quotients of the generated equations: div64 in FP64, the IEEE division
-// in FP32 (nt_div<T> in newton_gen.cuh)
-template <typename T>
-__device__ __forceinline__ T nt_div(T a, T b) {
-    return a / b;
-}
-template <>
-__device__ __forceinline__ double nt_div<double>(double a, double b) {
-    return div64(a, b);
 }
 
 __device__ __forceinline__ double nt_widen(double z) { return z; }
