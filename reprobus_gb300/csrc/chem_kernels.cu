@@ -786,11 +786,6 @@ struct Handle {
     // while the handle's stream writes back the converged cells
     cudaStream_t rstream = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    // the rate stage and start of the second half of the rows run on fstream
-    // while the first half is solved (events ev_front0: the first half's
-    // front done; ev_front1: the second's)
-    cudaStream_t fstream = nullptr;
-    cudaEvent_t ev_front0 = nullptr, ev_front1 = nullptr;
     // device mirrors for the host-pointer entry point (allocated on first use)
     double* m_alt = nullptr;
     double* m_traj[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -897,9 +892,6 @@ static void free_handle(Handle* h) {
     if (h->ev4) cudaEventDestroy(h->ev4);
     if (h->ev5) cudaEventDestroy(h->ev5);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
-    if (h->ev_front0) cudaEventDestroy(h->ev_front0);
-    if (h->ev_front1) cudaEventDestroy(h->ev_front1);
-    if (h->fstream) cudaStreamDestroy(h->fstream);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     if (h->rstream) cudaStreamDestroy(h->rstream);
     if (h->own) cudaStreamDestroy(h->own);
@@ -959,8 +951,6 @@ extern "C" int reprobus_chem_init(const double* ajl, const double* o3up, const d
         (e = cudaEventCreate(&h->ev4)) != cudaSuccess || (e = cudaEventCreate(&h->ev5)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming)) != cudaSuccess ||
-        (e = cudaEventCreateWithFlags(&h->ev_front0, cudaEventDisableTiming)) != cudaSuccess ||
-        (e = cudaEventCreateWithFlags(&h->ev_front1, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaMalloc(&h->d_ajl, najl * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&h->d_o3up, 80 * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&h->d_col, (3 * ncell + ncol) * sizeof(double))) != cudaSuccess ||
@@ -1115,27 +1105,24 @@ static int ensure_newton(Handle* h) {
 // threads in lock-step (measured at cfg1: 36 -> 28 ms against 128-thread
 // blocks without barriers; 512 threads 30 ms)
 constexpr int SETUP_TB = 256;
-static void launch_setup(Handle* h, const Params& P, bool mixed, cudaStream_t st = nullptr) {
+static void launch_setup(Handle* h, const Params& P, bool mixed) {
     const unsigned nb = (unsigned)((P.win_ncell + SETUP_TB - 1) / SETUP_TB);
-    if (!st) st = h->stream;
     if (mixed)
-        k_nt_setup<true, SETUP_TB, true><<<nb, SETUP_TB, 0, st>>>(P);
+        k_nt_setup<true, SETUP_TB, true><<<nb, SETUP_TB, 0, h->stream>>>(P);
     else
-        k_nt_setup<false, SETUP_TB, true><<<nb, SETUP_TB, 0, st>>>(P);
+        k_nt_setup<false, SETUP_TB, true><<<nb, SETUP_TB, 0, h->stream>>>(P);
 }
 
-// rate stage and plain start of the cells of P's row window (on stream st,
-// default the handle's); they join the work queue, whose heads the caller
-// has zeroed
-static void newton_front(Handle* h, const Params& P, bool mixed, cudaStream_t st = nullptr) {
+// rate stage and plain start of the cells of P's row window; they join the
+// work queue, whose heads the caller has zeroed
+static void newton_front(Handle* h, const Params& P, bool mixed) {
     const int tb = 128;
-    if (!st) st = h->stream;
-    launch_setup(h, P, mixed, st);
+    launch_setup(h, P, mixed);
     if (mixed) {
-        k_nt_start32<0><<<(P.win_ncell + tb - 1) / tb, tb, 0, st>>>(P);
-        k_nt_start<2><<<(P.win_ncell + tb - 1) / tb, tb, 0, st>>>(P);
+        k_nt_start32<0><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        k_nt_start<2><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     } else {
-        k_nt_start<0><<<(P.win_ncell + tb - 1) / tb, tb, 0, st>>>(P);
+        k_nt_start<0><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     }
 }
 
@@ -1359,50 +1346,13 @@ static void newton_back(Handle* h, const Params& P) {
     k_nt_fallback<<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
 }
 
-// rows r0..r0+nr-1 of P's range as the window of the per-cell kernels
-static void set_window(Params& P, int r0, int nr) {
-    P.win_r0 = r0;
-    P.win_nr = nr;
-    P.win_ncol = P.nlon * nr;
-    P.win_ncell = P.win_ncol * P.nivbas;
-}
-
-// Cells of a step from which its rows are solved in two halves: the rate
-// stage and start of the second half (FP64-pipe and FP32 work) run on a
-// second stream while the persistent solve kernel (latency bound, a few warps
-// per SM) works on the first half, on the same SMs.
-constexpr long long NT_SPLIT_MIN_CELLS = 1 << 18;
-
 // the Newton pipeline of one step (after k_columns)
 static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool capturing) {
     int rc = newton_prepare(h, P);
     if (rc) return rc;
     const bool mixed = h->solver == REPROBUS_SOLVER_NEWTON_MIXED;
-    if (P.nrows >= 2 && (long long)P.ncell >= NT_SPLIT_MIN_CELLS) {
-        if (!h->fstream) CUDA_TRY(cudaStreamCreateWithFlags(&h->fstream, cudaStreamNonBlocking));
-        // two work queues (heads nt_head[0..2] and [4..6]) over the two halves of the rows
-        const int r1 = P.nrows / 2;
-        Params PA = P, PB = P;
-        PA.nt_qcap = P.nlon * r1 * P.nivbas;
-        PB.nt_qcap = P.ncell - PA.nt_qcap;
-        PB.nt_list = P.nt_list + PA.nt_qcap;
-        PB.nt_head = P.nt_head + 4;
-        set_window(PA, 0, r1);
-        set_window(PB, r1, P.nrows - r1);
-        CUDA_TRY(cudaMemsetAsync(h->nt_head, 0, 8 * sizeof(int), h->stream));
-        newton_front(h, PA, mixed);
-        CUDA_TRY(cudaEventRecord(h->ev_front0, h->stream));
-        CUDA_TRY(cudaStreamWaitEvent(h->fstream, h->ev_front0, 0));
-        newton_front(h, PB, mixed, h->fstream);
-        CUDA_TRY(cudaEventRecord(h->ev_front1, h->fstream));
-        if ((rc = newton_solve(h, PA, timed ? h->ev2 : nullptr, nullptr, capturing))) return rc;
-        CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_front1, 0));
-        if ((rc = newton_solve(h, PB, nullptr, timed ? h->ev3 : nullptr, capturing))) return rc;
-        *launches += mixed ? 3 : 1;  // the second solve and the second half's front
-    } else {
-        if ((rc = enqueue_setup(h, P, mixed))) return rc;
-        if ((rc = newton_solve(h, P, timed ? h->ev2 : nullptr, timed ? h->ev3 : nullptr, capturing))) return rc;
-    }
+    if ((rc = enqueue_setup(h, P, mixed))) return rc;
+    if ((rc = newton_solve(h, P, timed ? h->ev2 : nullptr, timed ? h->ev3 : nullptr, capturing))) return rc;
     if (h->mlp) {
         // the restart on its own stream while this one writes back the cells
         // that converged; the fallback waits for both
@@ -1822,6 +1772,14 @@ static void mirror_params(Handle* h, Params& P, int a, int b, double daynum, dou
     P.sza3d = h->m_out[3];
     P.surfarea = h->m_out[4];
     step_const(h, daynum, dt, P.sc);
+}
+
+// rows r0..r0+nr-1 of P's range as the window of the per-cell kernels
+static void set_window(Params& P, int r0, int nr) {
+    P.win_r0 = r0;
+    P.win_nr = nr;
+    P.win_ncol = P.nlon * nr;
+    P.win_ncell = P.win_ncol * P.nivbas;
 }
 
 // A Newton step through the host arrays in row chunks. The rate stage and
