@@ -741,13 +741,26 @@ using CellFix = CellFixT<double>;
 // one pass of the iteration, F:1350-2372; ck (43), cc (15), ck0 (42)
 // ----------------------------------------------------------------------------
 // T = double: the reference's arithmetic (every call of the FP64 path);
-// T = float: the same statements in FP32, for the start of the mixed solver
+// T = float: the same statements in FP32, for the start of the mixed solver.
+// Its quotients (pass_div): the IEEE division in FP64 (the reference's
+// arithmetic); in FP32 (the start only seeds Newton) the fast division,
+// within 2 ulp for divisors below 2^126
+template <typename T>
+__device__ __forceinline__ T pass_div(T a, T b) {
+    return a / b;
+}
+template <>
+__device__ __forceinline__ float pass_div<float>(float a, float b) {
+    return __fdividef(a, b);
+}
+
 template <typename T>
 __device__ __forceinline__ void cell_pass(const CellFixT<T>& F, const T* __restrict__ K, const T* __restrict__ tj,
                                           const T* __restrict__ het, const T* __restrict__ ck0, T dt, T* ck,
                                           T* cc) {
     const T a3et = T(1.2e-10), a23a = T(7.2e-11), a23b = T(6.9e-12), a23c = T(1.6e-12);
 #define KK(name) K[K_##name]
+#define PDIV(a, b) pass_div<T>(a, b)
 #define CK(m) ck[(m)-1]
 #define CC(m) cc[(m)-1]
 #define TJ(name) tj[J_##name]
@@ -757,56 +770,56 @@ __device__ __forceinline__ void cell_pass(const CellFixT<T>& F, const T* __restr
     T a, b, day, ch3o, hco;
     if (F.sza <= T(95.)) {
         day = T(1.);
-        CC(15) = ((KK(c2) * CC(2) + KK(c1a) * CC(1) + KK(d5) * CC(3)) * CK(2)) / (KK(c4) * o2 + KK(c3) * CC(4));
-        ch3o = (KK(c1b) * CC(1) * CK(2) + (KK(c5) * CC(8) + T(2.) * KK(c14) * CK(29) + KK(c18) * CC(11)) * CK(29) +
-                TJ(ch3o2h) * CK(30)) /
-               (KK(c15) * o2);
-        hco = (KK(c8) * CC(2) + KK(c9) * CC(4) + KK(c10) * CC(3) + KK(c19) * CC(9) + TJ(ch2o_hco)) * CK(28) /
-              (KK(c12) * o2);
-        T r1 = (TJ(o3_o1d) + TJ(o3_o3p) + KK(a2) * CC(14) + KK(a6) * CC(2) + KK(a6b) * CC(6) + KK(b4) * CC(8) +
-                     KK(d2) * CC(3)) /
-                    (KK(hk2) * o2);
-        T r2 = T(1.) / (T(1.) + r1);
+        CC(15) = PDIV(((KK(c2) * CC(2) + KK(c1a) * CC(1) + KK(d5) * CC(3)) * CK(2)), (KK(c4) * o2 + KK(c3) * CC(4)));
+        ch3o = PDIV((KK(c1b) * CC(1) * CK(2) + (KK(c5) * CC(8) + T(2.) * KK(c14) * CK(29) + KK(c18) * CC(11)) * CK(29) +
+                     TJ(ch3o2h) * CK(30)),
+                    (KK(c15) * o2));
+        hco = PDIV((KK(c8) * CC(2) + KK(c9) * CC(4) + KK(c10) * CC(3) + KK(c19) * CC(9) + TJ(ch2o_hco)) * CK(28),
+                   (KK(c12) * o2));
+        T r1 = PDIV((TJ(o3_o1d) + TJ(o3_o3p) + KK(a2) * CC(14) + KK(a6) * CC(2) + KK(a6b) * CC(6) + KK(b4) * CC(8) +
+                      KK(d2) * CC(3)),
+                     (KK(hk2) * o2));
+        T r2 = PDIV(T(1.), (T(1.) + r1));
         CC(5) = r2 * CK(8);
         CC(4) = r1 * CC(5);
-        T r3 = TJ(o3_o1d) / (KK(hk4) * n2 + KK(hk5) * o2);
+        T r3 = PDIV(TJ(o3_o1d), (KK(hk4) * n2 + KK(hk5) * o2));
         CC(1) = r3 * CC(5);
-        T r4 = (KK(a5) * CC(4) + KK(a36) * CK(9) + KK(a19) * h2) /
-                    (KK(a1) * o2 + KK(a2) * CC(5) + (a23a + a23b + a23c) * CC(6));
+        T r4 = PDIV((KK(a5) * CC(4) + KK(a36) * CK(9) + KK(a19) * h2),
+                    (KK(a1) * o2 + KK(a2) * CC(5) + (a23a + a23b + a23c) * CC(6)));
         CC(14) = r4 * CC(2);
-        T r7 = TJ(no) / (KK(b7) * o2 + KK(b6) * CC(8));
-        T r8 = (KK(b9) * CC(5)) / (TJ(no3_no) + TJ(no3_no2) + KK(b12) * CC(7));
-        T r5 = (TJ(no2) + KK(b3) * CC(4) + TJ(no3_no) * r8) /
-                    (KK(b4) * CC(5) + KK(a26) * CC(6) + KK(d4) * CC(11) + KK(e4) * CC(12) + KK(c5) * CK(29));
-        CC(7) = CK(21) / (T(1.) + r5 + r7 * r5 + r8);
+        T r7 = PDIV(TJ(no), (KK(b7) * o2 + KK(b6) * CC(8)));
+        T r8 = PDIV((KK(b9) * CC(5)), (TJ(no3_no) + TJ(no3_no2) + KK(b12) * CC(7)));
+        T r5 = PDIV((TJ(no2) + KK(b3) * CC(4) + TJ(no3_no) * r8),
+                    (KK(b4) * CC(5) + KK(a26) * CC(6) + KK(d4) * CC(11) + KK(e4) * CC(12) + KK(c5) * CK(29)));
+        CC(7) = PDIV(CK(21), (T(1.) + r5 + r7 * r5 + r8));
         CC(8) = r5 * CC(7);
         CC(10) = r7 * CC(8);
         CC(13) = r8 * CC(7);
-        T r6 = (KK(a6) * CC(5) + KK(a30) * CK(17) + KK(c8) * CK(28) + KK(d8) * CC(11) + KK(e10) * CC(12) +
-                     KK(a1) * o2 * r4) /
-                    ((a23a + a23b + a23c) * CC(14) + KK(a6b) * CC(5) + KK(a7) * CC(4) + KK(a26) * CC(8) +
-                     T(2.) * KK(a27) * CC(6) + KK(a17) * CC(2) + KK(d7) * CC(3) + KK(d10) * CC(3) + KK(d33) * CC(11) +
-                     KK(e7) * CC(9) + KK(e15) * CC(12));
+        T r6 = PDIV((KK(a6) * CC(5) + KK(a30) * CK(17) + KK(c8) * CK(28) + KK(d8) * CC(11) + KK(e10) * CC(12) +
+                      KK(a1) * o2 * r4),
+                     ((a23a + a23b + a23c) * CC(14) + KK(a6b) * CC(5) + KK(a7) * CC(4) + KK(a26) * CC(8) +
+                      T(2.) * KK(a27) * CC(6) + KK(a17) * CC(2) + KK(d7) * CC(3) + KK(d10) * CC(3) + KK(d33) * CC(11) +
+                      KK(e7) * CC(9) + KK(e15) * CC(12)));
         a = T(.5);
         b = T(1.) - a;
         CC(6) = a * CC(6) + b * CC(2) * r6;
-        T r13 = KK(d31) * CC(7) /
-                     (TJ(clono2_cl) + TJ(clono2_clo) + KK(d32) * CC(4) + HET(1) * CK(3) + HET(2) * CK(13));
-        T r9 = (KK(d33) * CC(6) + HET(1) * CK(3) * r13) / (HET(5) * CK(13) + KK(d35) * CC(4) + TJ(hocl));
-        T r10 = (KK(d60) * CC(11)) / (KK(d61) * hnm + TJ(cl2o2));
-        T r12 = KK(e5c) * CC(12) / TJ(brcl);
-        T r11 = (KK(d3) * CC(4) + KK(d4) * CC(8) + KK(d8) * CC(2) + KK(c18) * CK(29) + KK(e5b) * CC(12) +
-                      TJ(clono2_cl) * r13 + TJ(hocl) * r9 + T(2.) * TJ(cl2o2) * r10 + TJ(brcl) * r12) /
-                     (KK(d2) * CC(5) + KK(d5) * CK(2) + KK(d7) * CC(6) + KK(d10) * CC(6) + KK(d37) * CK(15));
-        CC(11) = a * CC(11) + b * CK(23) / (T(1.) + r11);
+        T r13 = PDIV(KK(d31) * CC(7),
+                     (TJ(clono2_cl) + TJ(clono2_clo) + KK(d32) * CC(4) + HET(1) * CK(3) + HET(2) * CK(13)));
+        T r9 = PDIV((KK(d33) * CC(6) + HET(1) * CK(3) * r13), (HET(5) * CK(13) + KK(d35) * CC(4) + TJ(hocl)));
+        T r10 = PDIV((KK(d60) * CC(11)), (KK(d61) * hnm + TJ(cl2o2)));
+        T r12 = PDIV(KK(e5c) * CC(12), TJ(brcl));
+        T r11 = PDIV((KK(d3) * CC(4) + KK(d4) * CC(8) + KK(d8) * CC(2) + KK(c18) * CK(29) + KK(e5b) * CC(12) +
+                       TJ(clono2_cl) * r13 + TJ(hocl) * r9 + T(2.) * TJ(cl2o2) * r10 + TJ(brcl) * r12),
+                      (KK(d2) * CC(5) + KK(d5) * CK(2) + KK(d7) * CC(6) + KK(d10) * CC(6) + KK(d37) * CK(15)));
+        CC(11) = a * CC(11) + PDIV(b * CK(23), (T(1.) + r11));
         CC(3) = r11 * CC(11);
-        T r27 = KK(e13) * CC(7) / (TJ(brono2) + KK(e8) * CC(4));
-        T r28 = KK(e15) * CC(6) / (TJ(hobr) + KK(e16) * CC(4));
-        T r29 = KK(e5c) * CC(11) / TJ(brcl);
-        T r30 = (KK(e3) * CC(4) + KK(e4) * CC(8) + KK(e5a) * CC(11) + KK(e5b) * CC(11) + T(2.) * KK(e6) * CC(12) +
-                      KK(e10) * CC(2) + TJ(bro) + TJ(brono2) * T(0.85) * r27 + TJ(hobr) * r28 + TJ(brcl) * r29) /
-                     (KK(e2) * CC(5) + KK(e7) * CC(6) + KK(c19) * CK(28));
-        CC(12) = a * CC(12) + b * CK(24) / (T(1.) + r30);
+        T r27 = PDIV(KK(e13) * CC(7), (TJ(brono2) + KK(e8) * CC(4)));
+        T r28 = PDIV(KK(e15) * CC(6), (TJ(hobr) + KK(e16) * CC(4)));
+        T r29 = PDIV(KK(e5c) * CC(11), TJ(brcl));
+        T r30 = PDIV((KK(e3) * CC(4) + KK(e4) * CC(8) + KK(e5a) * CC(11) + KK(e5b) * CC(11) + T(2.) * KK(e6) * CC(12) +
+                       KK(e10) * CC(2) + TJ(bro) + TJ(brono2) * T(0.85) * r27 + TJ(hobr) * r28 + TJ(brcl) * r29),
+                      (KK(e2) * CC(5) + KK(e7) * CC(6) + KK(c19) * CK(28)));
+        CC(12) = a * CC(12) + PDIV(b * CK(24), (T(1.) + r30));
         CC(9) = r30 * CC(12);
         T coea = T(2.) * KK(a31) + T(2.) * (KK(a17) + KK(a27) * r6 + (a23b + a23c) * r4) * r6;
         T coeb = KK(b27) * CK(5) * parthno3 + KK(b22) * CC(7) + KK(b28) * CK(22) + KK(b23) * CC(7) * r6 +
@@ -831,7 +844,7 @@ __device__ __forceinline__ void cell_pass(const CellFixT<T>& F, const T* __restr
         T coec = t01 + t02 + t03 + t04 + t05 + t06 + t07 + t08 + t09 + t10 + t11 + t12 + t13 + t14 + t15;
         T argum = coeb * coeb + T(4.) * coea * coec;
         argum = fmax(argum, T(0.));
-        CC(2) = a * CC(2) + b * (sqrt(argum) - coeb) / (T(2.) * coea);
+        CC(2) = a * CC(2) + PDIV(b * (sqrt(argum) - coeb), (T(2.) * coea));
     } else {
         day = T(0.);
         CC(14) = T(0.);
@@ -845,8 +858,8 @@ __device__ __forceinline__ void cell_pass(const CellFixT<T>& F, const T* __restr
         CC(3) = T(0.);
         CC(6) = T(0.);
         CC(8) = T(0.);
-        T r8 = KK(b9) * CC(5) / (KK(b12) * fmax(CC(7), T(1.e-30)));
-        CC(7) = CK(21) / (T(1.) + r8);
+        T r8 = PDIV(KK(b9) * CC(5), (KK(b12) * fmax(CC(7), T(1.e-30))));
+        CC(7) = PDIV(CK(21), (T(1.) + r8));
         CC(13) = r8 * CC(7);
         CC(10) = T(0.);
         CC(11) = fmax(CK(23), T(0.));
@@ -871,7 +884,7 @@ __device__ __forceinline__ void cell_pass(const CellFixT<T>& F, const T* __restr
     PE(3) = (TJ(h2o) + KK(a1et) * CC(1)) * parth2o;
     PR(4) = T(2.) * KK(b39) * CC(1) * CK(1);
     PE(4) = T(2.) * KK(b6) * CC(10) * CC(8) + rain_hno3 * CK(5) + rain_hno4 * CK(22);
-    PE(4) = PE(4) / CK(4);
+    PE(4) = PDIV(PE(4), CK(4));
     PR(5) = KK(b22) * CC(2) * CC(7) + HET(1) * CK(14) * CK(3) + HET(2) * CK(14) * CK(13) +
             T(2.) * HET(3) * CK(6) * CK(3) + HET(4) * CK(6) * CK(13) + HET(6) * CK(20) * CK(3);
     PE(5) = (TJ(hno3) + KK(b27) * CC(2)) * parthno3 + rain_hno3;
@@ -883,8 +896,8 @@ __device__ __forceinline__ void cell_pass(const CellFixT<T>& F, const T* __restr
             T(1.) * (TJ(hcfc22) + KK(d96) * CC(1) + KK(d97) * CC(2)) * CK(37) +
             T(1.) * (TJ(h1211) + KK(e52) * CC(1)) * CK(39);
     PE(7) = rain_hcl * CK(13);
-    PE(7) = PE(7) / CK(7);
-    T ratio = TJ(cl2o2) / (TJ(cl2o2) + KK(d61) * hnm);
+    PE(7) = PDIV(PE(7), CK(7));
+    T ratio = PDIV(TJ(cl2o2), (TJ(cl2o2) + KK(d61) * hnm));
     PR(8) = T(2.) * TJ(o2) * o2 + KK(a26) * CC(6) * CC(8) + KK(c5) * CC(8) * CK(29);
     t01 = T(2.) * KK(hk1) * CC(4) * CC(4);
     t02 = T(2.) * KK(hk3) * CC(5) * CC(4);
@@ -896,11 +909,11 @@ __device__ __forceinline__ void cell_pass(const CellFixT<T>& F, const T* __restr
     t08 = T(2.) * KK(e5b) * CC(12) * CC(11) * day;
     t09 = fmin(KK(e15) * CC(12) * CC(6), TJ(hobr) * CK(26));
     t10 = T(2.) * KK(e6) * CC(12) * CC(12) * day;
-    t11 = T(2.) * (TJ(no3_no) / fmax(TJ(no3_no) + TJ(no3_no2), T(1.e-30))) * TJ(clono2_cl) * CK(14);
+    t11 = T(2.) * PDIV(TJ(no3_no), fmax(TJ(no3_no) + TJ(no3_no2), T(1.e-30))) * TJ(clono2_cl) * CK(14);
     t12 = (KK(a2) * CC(14) + KK(a6) * CC(2) + KK(a6b) * CC(6)) * CC(5) + (KK(a5) * CC(2) + KK(a7) * CC(6)) * CC(4);
-    t13 = T(2.) * KK(b9) * CC(7) * CC(5) * TJ(no3_no) / fmax(TJ(no3_no) + TJ(no3_no2), T(1.e-30));
+    t13 = PDIV(T(2.) * KK(b9) * CC(7) * CC(5) * TJ(no3_no), fmax(TJ(no3_no) + TJ(no3_no2), T(1.e-30)));
     PE(8) = t01 + t02 + t03 + t04 + t05 + t06 + t07 + t08 + t09 + t10 + t11 + t12 + t13;
-    PE(8) = PE(8) / CK(8);
+    PE(8) = PDIV(PE(8), CK(8));
     PR(9) = TJ(co2) * co2 + TJ(ch2o_co) * CK(28) + KK(c12) * hco * o2;
     PE(9) = KK(a36) * CC(2);
     PR(10) = KK(e5a) * CC(12) * CC(11);
@@ -935,7 +948,7 @@ __device__ __forceinline__ void cell_pass(const CellFixT<T>& F, const T* __restr
               KK(e13) * CC(12)) *
                  CC(7) +
              T(2.) * KK(b6) * CC(10) * CC(8);
-    PE(21) = PE(21) / CK(21);
+    PE(21) = PDIV(PE(21), CK(21));
     PR(22) = KK(b23) * CC(6) * CC(7);
     PE(22) = TJ(hno4) + KK(b28) * CC(2) + KK(b24) * hnm + rain_hno4;
     t01 = T(2.) * (KK(d61) * hnm + TJ(cl2o2)) * CK(25);
@@ -959,13 +972,13 @@ __device__ __forceinline__ void cell_pass(const CellFixT<T>& F, const T* __restr
              (KK(c10) * CK(28) + KK(d5) * CK(2) + KK(d7) * CC(6) + KK(d6) * h2 + KK(d36) * CC(7) +
               KK(d37) * CK(15)) *
                  CC(3);
-    PE(23) = PE(23) / CK(23);
+    PE(23) = PDIV(PE(23), CK(23));
     PR(24) = TJ(hobr) * CK(26) + TJ(brono2) * CK(20) + KK(e8) * CK(20) * CC(4) + KK(e16) * CK(26) * CC(4) +
              TJ(brcl) * CK(27) + (KK(e11) * CC(2) + KK(e9) * CC(1) + TJ(hbr)) * CK(19) * parthbr +
              T(2.) * HET(8) * CK(19) * CK(26);
     PE(24) = (KK(e13) * CC(7) + KK(e5c) * CC(11) + KK(e15) * CC(6)) * CC(12) + KK(c19) * CC(9) * CK(28) +
              KK(e7) * CC(9) * CC(6);
-    PE(24) = PE(24) / CK(24);
+    PE(24) = PDIV(PE(24), CK(24));
     PR(25) = KK(d60) * CC(11) * CC(11);
     PE(25) = TJ(cl2o2) + KK(d61) * hnm;
     PR(26) = KK(e15) * CC(12) * CC(6) + HET(6) * CK(20) * CK(3);
@@ -1002,14 +1015,15 @@ __device__ __forceinline__ void cell_pass(const CellFixT<T>& F, const T* __restr
     PR(41) = (TJ(ch3br) + KK(e50) * CC(1) + KK(e51) * CC(2)) * CK(38) + (TJ(h1211) + KK(e52) * CC(1)) * CK(39) +
              (TJ(h1301) + KK(e53) * CC(1)) * CK(40) + T(2.) * (KK(e54) * CC(2) + TJ(ch2br2)) * CK(42);
     PE(41) = rain_hbr * CK(19);
-    PE(41) = PE(41) / CK(41);
+    PE(41) = PDIV(PE(41), CK(41));
     PR(42) = T(0.);
     PE(42) = TJ(ch2br2) + KK(e54) * CC(2);
 #pragma unroll
-    for (int m = 0; m < NBCON - 1; m++) ck[m] = (ck0[m] + dt * pr[m]) / (T(1.) + dt * pe[m]);
+    for (int m = 0; m < NBCON - 1; m++) ck[m] = PDIV((ck0[m] + dt * pr[m]), (T(1.) + dt * pe[m]));
 #undef PR
 #undef PE
 #undef KK
+#undef PDIV
 #undef CK
 #undef CC
 #undef TJ
