@@ -80,25 +80,21 @@ template <>
 __device__ __forceinline__ double nt_cvt<double>(double v) {
     return v;
 }
-// The top 32 bits of |v| << 3 hold the exponent's low 9 bits and the first
-// 23 mantissa bits (one funnel shift); subtracting 384 << 23 there (mod 2^32)
-// rebiases exponents 897..1150 to 1..254. Beyond that range: +-0 below, a
-// non-finite value above (inf for inf and nan alike: the solver only tests
-// finiteness).
 template <>
 __device__ __forceinline__ float nt_cvt<float>(double v) {
     uint64_t b;
     memcpy(&b, &v, 8);
     const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
-    const uint32_t a = hi & 0x7fffffffu;
-#ifdef __CUDA_ARCH__
-    uint32_t f = __funnelshift_l(lo, a, 3) - (384u << 23);
-#else
-    uint32_t f = ((a << 3) | (lo >> 29)) - (384u << 23);
-#endif
-    f = a < (897u << 20) ? 0u : f;
-    f = a >= (1151u << 20) ? 0x7f800000u : f;
-    return nt_f32_from_bits(f | (hi & 0x80000000u));
+    const uint32_t sign = hi & 0x80000000u;
+    const int E = (int)((hi >> 20) & 0x7ffu);
+    uint32_t f;
+    if (E <= 896)
+        f = sign;  // below the float normal range: +-0
+    else if (E >= 1151)
+        f = sign | 0x7f800000u | ((E == 2047 && ((hi & 0xfffffu) | lo)) ? 0x400000u : 0u);  // inf / nan
+    else
+        f = sign | ((uint32_t)(E - 896) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    return nt_f32_from_bits(f);
 }
 
 __device__ __forceinline__ double nt_widen(double z) { return z; }

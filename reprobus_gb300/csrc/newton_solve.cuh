@@ -185,8 +185,6 @@ __device__ __forceinline__ bool nt_iterate(const FF& F, PK K, PK tj, PK het, PC 
 // FP64 update x_i += s_i z_i (negative results clipped to x_i / 10);
 // returns false when a step is not finite; *step = max |z_i|. active false:
 // a lane that runs the iteration only to keep its warp converged writes nothing.
-// The clip's sign tests read the bits (xo > 0: positive and not zero; xn < 0:
-// negative and not -0), on the integer pipe.
 template <typename TJ, typename PZ>
 __device__ __forceinline__ bool nt_update(double* x, double floor_, PZ z, TJ* step, bool active) {
     const int fh = nt_exp_hi(floor_);
@@ -197,10 +195,7 @@ __device__ __forceinline__ bool nt_update(double* x, double floor_, PZ z, TJ* st
         const TJ zi = z[i];
         const double xo = x[i];
         double xn = xo + nt_widen(zi) * nt_scale<double>(nt_exp_hi(xo), fh);
-        int64_t bo, bn;
-        memcpy(&bo, &xo, 8);
-        memcpy(&bn, &xn, 8);
-        if (bo > 0 && bn < 0 && (uint64_t)bn != 0x8000000000000000ull) xn = 0.1 * xo;
+        if (xo > 0. && xn < 0.) xn = 0.1 * xo;
         const TJ y = fabs(zi);
         if (!(y <= TJ(1e30))) finite = false;
         st = fmax(st, y);
