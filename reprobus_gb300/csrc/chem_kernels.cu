@@ -386,16 +386,18 @@ __global__ void __launch_bounds__(NTB) k_nt_setup(Params P) {
 #pragma unroll 4
     for (int n = 0; n < NBCON; n++) r[NT_RCK0 + n] = C.ck0[n];
     if (MIXED) {
+        // FP32 copies by integer operations (nt_cvt: truncated, below 2^-126
+        // zero), not conversion instructions, which issue on the FP64 pipe
         float* q = P.nt_rec32 + (size_t)cell * NT_REC32;
 #pragma unroll 4
-        for (int n = 0; n < NRATE; n++) q[NT_RK + n] = (float)C.K[n];
+        for (int n = 0; n < NRATE; n++) q[NT_RK + n] = nt_cvt<float>(C.K[n]);
 #pragma unroll 4
-        for (int n = 0; n < NPHOT; n++) q[NT_RJ + n] = (float)C.tj[n];
+        for (int n = 0; n < NPHOT; n++) q[NT_RJ + n] = nt_cvt<float>(C.tj[n]);
 #pragma unroll
-        for (int n = 0; n < 9; n++) q[NT_RH + n] = (float)C.A.het[n];
+        for (int n = 0; n < 9; n++) q[NT_RH + n] = nt_cvt<float>(C.A.het[n]);
 #pragma unroll
-        for (int n = 0; n < 14; n++) q[NT_RF + n] = (float)fx[n];
-        q[NT_RSZA] = (float)F.sza;
+        for (int n = 0; n < 14; n++) q[NT_RF + n] = nt_cvt<float>(fx[n]);
+        q[NT_RSZA] = nt_cvt<float>(F.sza);
     }
 }
 
@@ -1363,9 +1365,9 @@ static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool c
             CUDA_TRY(cudaStreamCreateWithPriority(&h->rstream, cudaStreamNonBlocking, hi));
         }
         CUDA_TRY(cudaEventRecord(h->ev_fork, h->stream));
+        k_nt_finish<0><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
         CUDA_TRY(cudaStreamWaitEvent(h->rstream, h->ev_fork, 0));
         if ((rc = newton_restart(h, P, h->rstream, launches))) return rc;
-        k_nt_finish<0><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
         CUDA_TRY(cudaEventRecord(h->ev_join, h->rstream));
         CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
         k_nt_fallback<<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
