@@ -1038,7 +1038,7 @@ __device__ __forceinline__ void cell_conserv(double* q, double* h) {
 #define Q(m) q[(m)-1]
 #define H(m) h[(m)-1]
     double totmas = Q(10) + Q(13) + Q(14) + Q(15) + 2. * Q(16) + Q(18) + Q(23) + 2. * Q(25);
-    double rapcly = (Q(7) - Q(27)) / totmas;
+    double rapcly = div64(Q(7) - Q(27), totmas);
     H(3) = H(3) * rapcly;
     H(11) = H(11) * rapcly;
     Q(10) = Q(10) * rapcly;
@@ -1050,7 +1050,7 @@ __device__ __forceinline__ void cell_conserv(double* q, double* h) {
     Q(23) = Q(23) * rapcly;
     Q(25) = Q(25) * rapcly;
     totmas = Q(5) + 2. * Q(6) + Q(21) + Q(22);
-    double rapnoy = fmax((Q(4) - Q(14) - Q(18) - Q(20)), 0.) / totmas;
+    double rapnoy = div64(fmax((Q(4) - Q(14) - Q(18) - Q(20)), 0.), totmas);
     H(7) = H(7) * rapnoy;
     H(8) = H(8) * rapnoy;
     H(10) = H(10) * rapnoy;
@@ -1060,7 +1060,7 @@ __device__ __forceinline__ void cell_conserv(double* q, double* h) {
     Q(21) = Q(21) * rapnoy;
     Q(22) = Q(22) * rapnoy;
     totmas = Q(19) + Q(20) + Q(24) + Q(26) + Q(27);
-    double rapbry = Q(41) / totmas;
+    double rapbry = div64(Q(41), totmas);
     H(9) = H(9) * rapbry;
     H(12) = H(12) * rapbry;
     Q(19) = Q(19) * rapbry;

@@ -223,6 +223,17 @@ __device__ __forceinline__ void cell_prologue(const Params& P, int cell, CellPro
     F.rain_ch3o2h = 0.;
 }
 
+// fmax(v, 1e-30) on the integer pipe: below 1e-30 (negative, zero or
+// smaller), the signed integer of a double's bits is below that of 1e-30;
+// NaN gives 1e-30, as fmax does
+__device__ __forceinline__ double clamp_1e30(double v) {
+    long long b;
+    memcpy(&b, &v, 8);
+    const long long lo = 0x39b4484bfeebc2a0LL;  // the bits of 1e-30
+    const bool nan = (b & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+    return (b < lo || nan) ? 1.e-30 : v;
+}
+
 // write-back F:2380-2410, then (fused) conserv F:2539-2613 and clamps F:431-440
 // RECIP: number density -> mixing ratio by one reciprocal of hnm and
 // products (within an ulp of the reference's divisions, F:2380-2410), for the
@@ -233,7 +244,7 @@ __device__ __forceinline__ void cell_epilogue(const Params& P, const CellPro& C,
     const size_t pl = plane3(P);
     double q[NBCON], h[NCM];
     if (RECIP) {
-        const double rh = 1. / C.F.hnm;
+        const double rh = div64(1., C.F.hnm);
 #pragma unroll
         for (int n = 0; n < NBCON - 1; n++) q[n] = ck[n] * rh;
         q[NBCON - 1] = ck[4] * C.F.parthno3 * rh;
@@ -257,7 +268,7 @@ __device__ __forceinline__ void cell_epilogue(const Params& P, const CellPro& C,
     }
     if (P.fuse) {
 #pragma unroll
-        for (int n = 0; n < NBCON - 1; n++) q[n] = fmax(q[n], 1.e-30);
+        for (int n = 0; n < NBCON - 1; n++) q[n] = clamp_1e30(q[n]);
     }
 #pragma unroll
     for (int n = 0; n < NBCON; n++) P.qj1[C.g + pl * n] = q[n];
@@ -564,15 +575,18 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
 }
 
 // learned restart: each cell of the window whose Newton iteration missed
-// (stat < 0) takes a slot k < P.mlp_cap (cells beyond the last slot keep
-// stat < 0 and fall back); P.nt_head[3] counts the cells that asked
+// (stat < 0) takes a slot k < P.mlp_cap (cells beyond the last slot get stat
+// NT_STAT_NOSLOT and fall back); P.nt_head[3] counts the cells that asked
 __global__ void __launch_bounds__(128) k_nt_collect(Params P) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= P.win_ncell) return;
     const int cell = win_cell(P, t);
     if (P.nt_stat[cell] >= 0) return;
     const int slot = atomicAdd(P.nt_head + 3, 1);
-    if (slot < P.mlp_cap) P.mlp_cells[slot] = cell;
+    if (slot < P.mlp_cap)
+        P.mlp_cells[slot] = cell;
+    else
+        P.nt_stat[cell] = NT_STAT_NOSLOT;
 }
 
 // learned restart: x_i = max(x_i, 1e-30 hnm) 10^y_i for the cell of each
@@ -645,9 +659,10 @@ __device__ __forceinline__ void nt_cell_fix(const double* r, CellFix& F) {
 
 // MODE 0: the cells of the window that converged from the plain start
 // (0 < stat < NT_RESTART_BIAS); MODE 1: the cells of the learned restart's
-// slots that converged in its solve (stat >= NT_RESTART_BIAS). The two touch
-// disjoint cells, and neither reads a status that the other's solve may still
-// change, so MODE 0 may run while the restart is in flight.
+// slots that converged in its solve (stat >= NT_RESTART_BIAS), after
+// k_nt_fallback<2> wrote the fallback answer of every slot. MODE 0 touches
+// none of the restart's cells and reads no status its solve may still
+// change, so it may run while the restart is in flight.
 template <int MODE>
 __global__ void __launch_bounds__(128) k_nt_finish(Params P) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -663,6 +678,18 @@ __global__ void __launch_bounds__(128) k_nt_finish(Params P) {
     const int stat = own ? P.nt_stat[cell] : 0;
     const int lo = MODE == 0 ? 0 : NT_RESTART_BIAS, hi = MODE == 0 ? NT_RESTART_BIAS : INT_MAX;
     const bool mine = stat > lo && stat < hi;
+    // a restarted cell that missed again keeps the fallback answer written for
+    // it (whose non-finite values, if any, are counted here)
+    if (MODE == 1 && own && !mine) {
+        atomicAdd(P.nonfinite + 2, 1ULL);
+        if (P.check) {
+            const size_t g = cell_global(P, cell), pl = plane3(P);
+            unsigned int bad = 0;
+            for (int n = 0; n < NBCON; n++) bad += !isfinite(P.qj1[g + pl * n]);
+            for (int n = 0; n < NCM; n++) bad += !isfinite(P.hc[g + pl * n]);
+            if (bad) atomicAdd(P.nonfinite, (unsigned long long)bad);
+        }
+    }
     // iteration statistics, one atomic per warp (blocks are whole warps)
     const unsigned it = mine ? (unsigned)(stat - lo) : 0u;
     const unsigned sum = __reduce_add_sync(0xffffffffu, it), most = __reduce_max_sync(0xffffffffu, it);
@@ -685,13 +712,26 @@ __global__ void __launch_bounds__(128) k_nt_finish(Params P) {
     cell_epilogue<true>(P, C, ck, cc);
 }
 
-// fallback of the cells the Newton solver did not converge (stat <= 0): the
-// reference scheme's niter passes from the start state, then the write-back
+// fallback of the cells the Newton solver did not converge: the reference
+// scheme's niter passes from the start state, then the write-back.
+// MODE 0: the cells of the window with stat <= 0 (no learned restart);
+// MODE 1: those with stat NT_STAT_NOSLOT (the restart had no slot for them);
+// MODE 2: every cell of the restart's slots, ahead of their second solve and
+// beside it: k_nt_finish<1> then writes back the ones it converged over
+// these answers and counts the others as fallbacks.
+template <int MODE>
 __global__ void __launch_bounds__(128) k_nt_fallback(Params P) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.win_ncell) return;
-    const int cell = win_cell(P, t);
-    if (P.nt_stat[cell] > 0) return;
+    int cell;
+    if (MODE == 2) {
+        if (t >= min(P.nt_head[3], P.mlp_cap)) return;
+        cell = P.mlp_cells[t];
+    } else {
+        if (t >= P.win_ncell) return;
+        cell = win_cell(P, t);
+        const int stat = P.nt_stat[cell];
+        if (MODE == 0 ? stat > 0 : stat != NT_STAT_NOSLOT) return;
+    }
     const double* r = P.nt_rec + (size_t)cell * NT_REC;
     CellPro C;
     C.g = cell_global(P, cell);
@@ -713,7 +753,7 @@ __global__ void __launch_bounds__(128) k_nt_fallback(Params P) {
     for (int n = 0; n < NCM; n++) cc[n] = P.hc[C.g + pl * n] * F.hnm;
 #pragma unroll 1
     for (int it = 0; it < P.niter; it++) cell_pass(F, C.K, C.tj, C.A.het, C.ck0, P.sc.dt, ck, cc);
-    atomicAdd(P.nonfinite + 2, 1ULL);
+    if (MODE != 2) atomicAdd(P.nonfinite + 2, 1ULL);
     cell_epilogue<true>(P, C, ck, cc);
 }
 
@@ -731,7 +771,7 @@ __global__ void k_tail(Params P) {
     const size_t g = (size_t)i + (size_t)P.nlon * ((size_t)j + (size_t)P.nlat * k);
     const size_t pl = plane3(P);
 #pragma unroll 6
-    for (int s = 0; s < NBCON - 1; s++) P.qj1[g + pl * s] = fmax(P.qj1[g + pl * s], 1.e-30);
+    for (int s = 0; s < NBCON - 1; s++) P.qj1[g + pl * s] = clamp_1e30(P.qj1[g + pl * s]);
     P.qj1[g + pl * (NBCON - 1)] = P.qj1[g + pl * 4];
 }
 
@@ -759,7 +799,7 @@ __global__ void k_conserv(Params P) {
         for (int s = 0; s < NCM; s++) P.hc[g + pl * s] = h[s];
     }
 #pragma unroll
-    for (int s = 0; s < NBCON - 1; s++) q[s] = fmax(q[s], 1.e-30);
+    for (int s = 0; s < NBCON - 1; s++) q[s] = clamp_1e30(q[s]);
     if (k >= P.nivbas) q[NBCON - 1] = q[4];
 #pragma unroll
     for (int s = 0; s < NBCON; s++) P.qj1[g + pl * s] = q[s];
@@ -787,7 +827,7 @@ struct Handle {
     // the learned restart runs on its own stream of the highest priority
     // while the handle's stream writes back the converged cells
     cudaStream_t rstream = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_collect = nullptr, ev_spec = nullptr;
     // device mirrors for the host-pointer entry point (allocated on first use)
     double* m_alt = nullptr;
     double* m_traj[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -894,6 +934,8 @@ static void free_handle(Handle* h) {
     if (h->ev4) cudaEventDestroy(h->ev4);
     if (h->ev5) cudaEventDestroy(h->ev5);
     if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_collect) cudaEventDestroy(h->ev_collect);
+    if (h->ev_spec) cudaEventDestroy(h->ev_spec);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     if (h->rstream) cudaStreamDestroy(h->rstream);
     if (h->own) cudaStreamDestroy(h->own);
@@ -953,6 +995,8 @@ extern "C" int reprobus_chem_init(const double* ajl, const double* o3up, const d
         (e = cudaEventCreate(&h->ev4)) != cudaSuccess || (e = cudaEventCreate(&h->ev5)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&h->ev_collect, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&h->ev_spec, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaMalloc(&h->d_ajl, najl * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&h->d_o3up, 80 * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&h->d_col, (3 * ncell + ncol) * sizeof(double))) != cudaSuccess ||
@@ -1311,12 +1355,15 @@ static int newton_solve(Handle* h, const Params& P, cudaEvent_t e0, cudaEvent_t 
 }
 
 // The learned restart of the cells of P's window whose Newton iteration
-// missed (after newton_solve on P's queue), on stream st: P's queue is emptied
-// and refilled with those cells (at most mlp_cap), each started from the
-// network's prediction for its plain start and solved again; the cells that
-// converge are written back. The cell counts stay on the device: the kernels
-// over slots read them there.
-static int newton_restart(Handle* h, const Params& P0, cudaStream_t st, int* launches) {
+// missed (after newton_solve on P's queue): P's queue is emptied and refilled
+// with those cells (at most mlp_cap slots), each started from the network's
+// prediction for its plain start and solved again; k_nt_fallback<2> writes
+// the fallback answer of every slot, then k_nt_finish<1> the answer of those
+// that converged. The cell counts stay on the device. st: the restart's
+// stream; sf: the stream of the slots' fallback (st too: one after the
+// other; else the fallback runs on sf beside the second solve, after sf's
+// work so far, and h->ev_collect / h->ev_spec order the two streams).
+static int newton_restart(Handle* h, const Params& P0, cudaStream_t st, cudaStream_t sf, int* launches) {
     const int tb = 128;
     if (P0.win_ncell <= 0) return REPROBUS_OK;
     Params P = P0;
@@ -1326,6 +1373,16 @@ static int newton_restart(Handle* h, const Params& P0, cudaStream_t st, int* lau
     CUDA_TRY(cudaMemsetAsync(P.nt_head, 0, 4 * sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(mlp_err_flag(h->mlp), 0, sizeof(unsigned int), st));
     k_nt_collect<<<(P.win_ncell + tb - 1) / tb, tb, 0, st>>>(P);
+    if (sf != st) {
+        CUDA_TRY(cudaEventRecord(h->ev_collect, st));
+        CUDA_TRY(cudaStreamWaitEvent(sf, h->ev_collect, 0));
+    }
+    {
+        Params PF = P;
+        PF.check = 0;  // k_nt_finish<1> counts the non-finite values of the answers that stay
+        k_nt_fallback<2><<<nslot, tb, 0, sf>>>(PF);
+    }
+    if (sf != st) CUDA_TRY(cudaEventRecord(h->ev_spec, sf));
     if (h->solver == REPROBUS_SOLVER_NEWTON_MIXED)  // the plain start as the first attempt had it
         k_nt_start32<3><<<nslot, tb, 0, st>>>(P);
     else
@@ -1335,8 +1392,9 @@ static int newton_restart(Handle* h, const Params& P0, cudaStream_t st, int* lau
     const unsigned nb = (unsigned)((h->mlp_cap * NT_NX + tb - 1) / tb);
     k_nt_warm<<<nb < 2u * h->nsm ? nb : 2u * h->nsm, tb, 0, st>>>(P);
     CUDA_TRY(h->rs_var[ip]->launch(P, h->nsm, st));
+    if (sf != st) CUDA_TRY(cudaStreamWaitEvent(st, h->ev_spec, 0));
     k_nt_finish<1><<<nslot, tb, 0, st>>>(P);
-    *launches += 6;
+    *launches += 7;
     return REPROBUS_OK;
 }
 
@@ -1345,7 +1403,10 @@ static int newton_restart(Handle* h, const Params& P0, cudaStream_t st, int* lau
 static void newton_back(Handle* h, const Params& P) {
     const int tb = 128;
     k_nt_finish<0><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
-    k_nt_fallback<<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    if (h->mlp)  // the restart wrote back its slots' cells
+        k_nt_fallback<1><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+    else
+        k_nt_fallback<0><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
 }
 
 // the Newton pipeline of one step (after k_columns)
@@ -1357,7 +1418,7 @@ static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool c
     if ((rc = newton_solve(h, P, timed ? h->ev2 : nullptr, timed ? h->ev3 : nullptr, capturing))) return rc;
     if (h->mlp) {
         // the restart on its own stream while this one writes back the cells
-        // that converged; the fallback waits for both
+        // that converged and then the fallback answers of the restart's cells
         const int tb = 128;
         if (!h->rstream) {
             int lo = 0, hi = 0;
@@ -1367,10 +1428,10 @@ static int launch_newton(Handle* h, Params& P, int* launches, bool timed, bool c
         CUDA_TRY(cudaEventRecord(h->ev_fork, h->stream));
         k_nt_finish<0><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
         CUDA_TRY(cudaStreamWaitEvent(h->rstream, h->ev_fork, 0));
-        if ((rc = newton_restart(h, P, h->rstream, launches))) return rc;
+        if ((rc = newton_restart(h, P, h->rstream, h->stream, launches))) return rc;
         CUDA_TRY(cudaEventRecord(h->ev_join, h->rstream));
         CUDA_TRY(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
-        k_nt_fallback<<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
+        k_nt_fallback<1><<<(P.win_ncell + tb - 1) / tb, tb, 0, h->stream>>>(P);
     } else {
         newton_back(h, P);
     }
@@ -1835,7 +1896,7 @@ static int host_step_newton(Handle* h, const HostArrays& A, int ilat0, int ilat1
         if (h->mlp) {  // over the rows of this queue
             const int a = part == 0 ? row0(0) : row0(nchunk - 1), b = part == 0 ? row0(nchunk - 1) : ilat1 + 1;
             set_window(Q, a - ilat0, b - a);
-            if ((rc = newton_restart(h, Q, h->stream, &launches))) return rc;
+            if ((rc = newton_restart(h, Q, h->stream, h->stream, &launches))) return rc;
         }
         for (int c = part == 0 ? 0 : nchunk - 1; c < (part == 0 ? nchunk - 1 : nchunk); c++) {
             const int a = row0(c), b = row0(c + 1) - 1;

@@ -74,6 +74,7 @@ constexpr int NT_RSZA = NT_RF + 14, NT_RCK0 = NT_RSZA + 1, NT_RSURF = NT_RCK0 + 
 constexpr int NT_REC = 208;    // FP64 record stride (1664 B = 13 lines of 128 B)
 constexpr int NT_REC32 = 168;  // FP32 record stride (164 used)
 constexpr int NT_RESTART_BIAS = 1 << 16;  // Params::stat_bias of the learned restart's solve
+constexpr int NT_STAT_NOSLOT = -4;         // a cell that missed and found no slot of the restart
 static_assert(NT_RSURF < NT_REC, "record layout");
 
 __device__ __forceinline__ size_t plane3(const Params& P) { return (size_t)P.nlon * P.nlat * P.niv; }
