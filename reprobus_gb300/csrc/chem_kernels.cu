@@ -1373,6 +1373,12 @@ static int newton_restart(Handle* h, const Params& P0, cudaStream_t st, cudaStre
     CUDA_TRY(cudaMemsetAsync(P.nt_head, 0, 4 * sizeof(int), st));
     CUDA_TRY(cudaMemsetAsync(mlp_err_flag(h->mlp), 0, sizeof(unsigned int), st));
     k_nt_collect<<<(P.win_ncell + tb - 1) / tb, tb, 0, st>>>(P);
+    if (h->solver == REPROBUS_SOLVER_NEWTON_MIXED)  // the plain start as the first attempt had it
+        k_nt_start32<3><<<nslot, tb, 0, st>>>(P);
+    else
+        k_nt_start<3><<<nslot, tb, 0, st>>>(P);
+    // the fallback answers go to the output arrays, whose hc the starts just
+    // read as the start state: the fallback only once they are done
     if (sf != st) {
         CUDA_TRY(cudaEventRecord(h->ev_collect, st));
         CUDA_TRY(cudaStreamWaitEvent(sf, h->ev_collect, 0));
@@ -1383,10 +1389,6 @@ static int newton_restart(Handle* h, const Params& P0, cudaStream_t st, cudaStre
         k_nt_fallback<2><<<nslot, tb, 0, sf>>>(PF);
     }
     if (sf != st) CUDA_TRY(cudaEventRecord(h->ev_spec, sf));
-    if (h->solver == REPROBUS_SOLVER_NEWTON_MIXED)  // the plain start as the first attempt had it
-        k_nt_start32<3><<<nslot, tb, 0, st>>>(P);
-    else
-        k_nt_start<3><<<nslot, tb, 0, st>>>(P);
     int rc = mlp_infer(h->mlp, h->mlp_feat, h->mlp_y, h->mlp_cap, st, P.nt_head + 3);
     if (rc) return rc;
     const unsigned nb = (unsigned)((h->mlp_cap * NT_NX + tb - 1) / tb);
