@@ -1368,8 +1368,6 @@ static int newton_restart(Handle* h, const Params& P0, cudaStream_t st, cudaStre
     if (P0.win_ncell <= 0) return REPROBUS_OK;
     Params P = P0;
     P.stat_bias = NT_RESTART_BIAS;
-    static const int xmi = getenv("XRMAXIT") ? atoi(getenv("XRMAXIT")) : 0;  // EXPERIMENT
-    if (xmi > 0) P.maxit = xmi;
     const int ip = h->solver == REPROBUS_SOLVER_NEWTON_MIXED ? 0 : 1;
     const unsigned nslot = (unsigned)((h->mlp_cap + tb - 1) / tb);
     CUDA_TRY(cudaMemsetAsync(P.nt_head, 0, 4 * sizeof(int), st));
