@@ -20,7 +20,7 @@ SOURCES = ["chem_kernels.cu", "nt_solve_f32_zr.cu", "nt_solve_f32_zs.cu", "nt_so
            "column_kernels.cu"]
 HEADERS = ["chem_cell.cuh", "chem_enums.h", "chem_params.cuh", "newton_gen.cuh", "newton_solve.cuh",
            "newton_kernel.cuh", "newton_launch.h", "newton_num.cuh", "tc_sm100.cuh", "handle_info.h",
-           "tropo_tables.h", "exp64.cuh", "exp_table.h", "div64.cuh", "mlp_net.h"]
+           "tropo_tables.h", "exp64.cuh", "exp_table.h", "div64.cuh", "log64.cuh", "log_table.h", "mlp_net.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-diag-suppress", "550"]
 if os.environ.get("REPROBUS_FMAD", "1") == "0":

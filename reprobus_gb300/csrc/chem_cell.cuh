@@ -11,8 +11,9 @@
 // On GB300 every FP64 operation is scarce (2 per clock per SM), so the rate
 // stage divides by a constant as a product with its reciprocal (within an
 // ulp of the quotient), takes its exponentials from exp64 (exp64.cuh, within
-// 1.5 ulp) and the quotients of the rate constants and of the liquid aerosol
-// from div64 (div64.cuh, within an ulp).
+// 1.5 ulp), its logarithms from log64 (log64.cuh, within 1.6 ulp) and the
+// quotients of the rate constants and of the liquid aerosol from div64
+// (div64.cuh, within an ulp).
 #pragma once
 #include <cuda_runtime.h>
 #include <math.h>
@@ -20,6 +21,7 @@
 #include "chem_enums.h"
 #include "div64.cuh"
 #include "exp64.cuh"
+#include "log64.cuh"
 
 namespace rpb {
 
@@ -239,7 +241,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double pn0t = pn0 * 1013. * 0.75;
         double zmt = -2.7836 - 0.00088 * t;
         double zbt = 38.9855 - 11397.0 / t + 0.009179 * t;
-        double zhno3eq = exp64(zmt * log(pw * 1013. * 0.75) + zbt * LN10);
+        double zhno3eq = exp64(zmt * log64(pw * 1013. * 0.75) + zbt * LN10);
         if (pn0t / zhno3eq >= 1.) {
             lnat = 1;
             double pn = zhno3eq * (1. / (0.75 * 1013.));
@@ -269,7 +271,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
     double tice;
     {
         double t = fmin(temp, 273.);
-        tice = 2668.70 / (10.4310 - (log(pw) + LN760) * (1. / LN10));
+        tice = 2668.70 / (10.4310 - (log64(pw) + LN760) * (1. / LN10));
         if (t <= tice) {
             lice = 1;
             lnat = 0;
@@ -285,7 +287,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             A.parth2o = fmin(A.parth2o, 1.);
             double zmt = -2.7836 - 0.00088 * t;
             double zbt = 38.9855 - 11397.0 / t + 0.009179 * t;
-            double zhno3eq = exp64(zmt * log(pw * A.parth2o * 1013. * 0.75) + zbt * LN10);
+            double zhno3eq = exp64(zmt * log64(pw * A.parth2o * 1013. * 0.75) + zbt * LN10);
             double pn = zhno3eq * (1. / (0.75 * 1013.));
             parthno3s = 1.0 - (pn0 - pn) / pn0;
             parthno3s = fmax(parthno3s, 0.);
@@ -310,7 +312,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         pn0 = ptot * (1. / 1013.0) * qhno3l;
         double a = ks[3] + ks[4] * rt;
         double b = ks[1] + ks[2] * rt;
-        double cq = ks[5] + ks[6] * rt + ks[7] * log(t) - log(pw);
+        double cq = ks[5] + ks[6] * rt + ks[7] * log64(t) - log64(pw);
         double det = b * b - 4. * a * cq;
         double msb;
         if (det > 0.) {
@@ -325,7 +327,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         wn = 0.0;
         double wts = fmax(41., ws * 100.);
         double wd = wts - 40.;
-        double muh2so4 = 4.184 * (1.514e4 - 286. * wd + 1.08 * (wd * wd) - div64(3941., exp64(0.1 * log(wd))));
+        double muh2so4 = 4.184 * (1.514e4 - 286. * wd + 1.08 * (wd * wd) - div64(3941., exp64(0.1 * log64(wd))));
         double ph2so4 = exp64(-10156. * rt + 16.2590 - muh2so4 * (rt * (1. / 8.314)));
         if (qh2so4 * ptot * (1. / 1013.) <= ph2so4) {
             ms = 0.;
@@ -336,7 +338,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             double tf = t;
             double tt = r * tf * ns;
             double tr = 1.0e4 * rt - 43.4782608;
-            double pr = log(pw) + 18.4;
+            double pr = log64(pw) + 18.4;
             double tr2 = tr * tr, tr3 = tr2 * tr, pr2 = pr * pr, pr3 = pr2 * pr;
             double hsb = qs[1] + qs[2] * tr2 + (qs[3] + qs[4] * tr + qs[5] * tr2 + qs[6] * tr3) * pr +
                          (qs[7] + qs[8] * tr + qs[9] * tr2) * pr2 + qs[10] * tr * pr3;
@@ -344,7 +346,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             double kx = kn[1] + kn[2] * rt;
             double xnb = 1.0 / (2.0 * (kn[3] + kn[4] * rt)) *
                          (-kn[1] - kn[2] * rt -
-                          sqrt(kx * kx - 4.0 * (kn[3] + kn[4] * rt) * (kn[5] + kn[6] * rt + kn[7] * log(tf) - log(pw))));
+                          sqrt(kx * kx - 4.0 * (kn[3] + kn[4] * rt) * (kn[5] + kn[6] * rt + kn[7] * log64(tf) - log64(pw))));
             double mnb = 55.51 * xnb / (1.0 - xnb);
             double hnb = qn[1] + qn[2] * tr2 + (qn[3] + qn[4] * tr + qn[5] * tr2 + qn[6] * tr3) * pr +
                          (qn[7] + qn[8] * tr + qn[9] * tr2) * pr2 + qn[10] * tr * pr3;
@@ -405,7 +407,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         aw = div64(pw * 1013., ph2o0);
         aw = fmin(aw, 1.);
         int br = (aw <= 0.05) ? 0 : ((aw < 0.85) ? 1 : 2);
-        const double law = log(aw);
+        const double law = log64(aw);
         double y1 = c_an_a1[br] * exp64(c_an_b1[br] * law) + c_an_c1[br] * aw + c_an_d1[br];
         double y2 = c_an_a2[br] * exp64(c_an_b2[br] * law) + c_an_c2[br] * aw + c_an_d2[br];
         double m = y1 + (t - 190.) * (y2 - y1) * (1. / 70.);
@@ -413,7 +415,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         wt = fmax(wt, 0.5);
         double mh2so4 = dens * wt * (1. / 9.8);
         double bigx = div64(wt, wt + (100. - wt) * 98. * (1. / 18.));
-        hhcl = (0.094 - 0.61 * bigx + 1.2 * (bigx * bigx)) * exp64(-8.68 + (8515. - 10718. * exp64(0.7 * log(bigx))) * rt);
+        hhcl = (0.094 - 0.61 * bigx + 1.2 * (bigx * bigx)) * exp64(-8.68 + (8515. - 10718. * exp64(0.7 * log64(bigx))) * rt);
         double qhcl = ck[12] * rhnm;
         double phcl0 = qhcl * ptot * (1. / 1013.0);
         double phcl1 = div64(div64(phcl0, r * t), div64(1., r * t) + div64(hhcl * ns, ms));
@@ -442,7 +444,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             double netha = (1.718 + 0.0049 * tcel - 1.2e-5 * tcel * tcel) * 1.e-5;
             double rp3 = rpart * rpart * rpart;
             double cdnre2 = 32.0 * rp3 * (rhopart - rhoair) * rhoair * 9.80665 / (3.0 * (netha * netha));
-            double L = log(cdnre2);
+            double L = log64(cdnre2);
             double L2 = L * L, L3 = L2 * L, L4 = L2 * L2, L5 = L3 * L2, L6 = L3 * L3;
             double ynre = c_an_bnre[0] + c_an_bnre[1] * L + c_an_bnre[2] * L2 + c_an_bnre[3] * L3 +
                           c_an_bnre[4] * L4 + c_an_bnre[5] * L5 + c_an_bnre[6] * L6;
@@ -477,11 +479,11 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double wt2 = wt * wt, wt3 = wt2 * wt;
         double t0 = 144.11 + 0.166 * wt - 0.015 * wt2 + 2.18e-4 * wt3;
         double biga = 169.5 + 5.18 * wt - 0.0825 * wt2 + 3.27e-3 * wt3;
-        double eta = biga * exp64(-1.43 * log(T)) * exp64(div64(448., T - t0));
+        double eta = biga * exp64(-1.43 * log64(T)) * exp64(div64(448., T - t0));
         const double Teta = div64(T, eta);
         double sqT = sqrt(T);
         double ah = exp64(60.51 - 0.095 * wt + 0.0077 * wt2 - 1.61e-5 * wt3 - (1.76 + 2.52e-4 * wt2) * sqT +
-                        div64(-805.89 + 253.05 * exp64(0.076 * log(wt)), sqT));
+                        div64(-805.89 + 253.05 * exp64(0.076 * log64(wt)), sqT));
         double dclono2 = 5.e-8 * Teta;
         double cclono2 = 1474. * sqT;
         double kh2o = 1.95e10 * exp64(-2800. * rT);
@@ -592,8 +594,8 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
 __device__ __forceinline__ void cell_rates(const double* troe, const double* ltroe, double t, double hnm, double pm,
                                            double* K) {
     const double xln6 = LN06;
-    double lntemp = log(t);
-    const double lnhnm = log(hnm);
+    double lntemp = log64(t);
+    const double lnhnm = log64(hnm);
     const double rt = div64(1., t);  // Arrhenius exponents E / T as E * (1 / T)
     double ak0, ak1, rate, xpo, deq, l10, xk;
 #define RK(name) K[K_##name]
@@ -719,7 +721,7 @@ __device__ __forceinline__ void cell_rates(const double* troe, const double* ltr
     RK(e53) = 1.0e-10;
     RK(e54) = 2.0e-12 * em840;
     RK(hk1) = 4.23e-28 * hnm * (rt * rt);
-    RK(hk2) = 6.0e-34 * exp64(2.4 * log(300. * rt)) * hnm;
+    RK(hk2) = 6.0e-34 * exp64(2.4 * log64(300. * rt)) * hnm;
     RK(hk3) = 8.e-12 * exp64((-2060. * rt));
     RK(hk4) = 2.15e-11 * exp64(110. * rt);
     RK(hk5) = 3.3e-11 * exp64(55. * rt);

@@ -1,0 +1,40 @@
+"""log64 (reprobus_gb300/csrc/log64.cuh) on the GPU: the device code gives
+bit for bit the host build's results (whose error tests/test_log64.py bounds
+against long double), and stays within 2 ulp of CUDA's log."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_device_equals_host_build_and_cuda_log(tmp_path):
+    dev, host = str(tmp_path / "liblog64_dev.so"), str(tmp_path / "liblog64_host.so")
+    subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-shared",
+                    "-Xcompiler", "-fPIC", "-o", dev, os.path.join(ROOT, "tests", "log64_dev.cu")], check=True)
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-o", host,
+                    os.path.join(ROOT, "tests", "log64_host.cpp")], check=True)
+    D, H = ctypes.CDLL(dev), ctypes.CDLL(host)
+    D.log64_dev.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_long]
+    H.log64_many.argtypes = [ctypes.c_void_p] * 2 + [ctypes.c_long]
+    rng = np.random.default_rng(13)
+    x = np.concatenate([10.0 ** rng.uniform(-307, 307, 3_000_000), rng.uniform(0.5, 2.0, 1_000_000),
+                        1.0 + rng.uniform(-1e-3, 1e-3, 300_000), np.linspace(150.0, 330.0, 100_000),
+                        np.array([1.0, 2.0, 0.0, -1.0, 1e-310, np.inf, np.nan])])
+    a, b, h = np.empty_like(x), np.empty_like(x), np.empty_like(x)
+    assert D.log64_dev(x.ctypes.data, a.ctypes.data, b.ctypes.data, x.size) == 0
+    H.log64_many(x.ctypes.data, h.ctypes.data, x.size)
+    fast = (x >= 2.2250738585072014e-308) & np.isfinite(x)
+    assert np.array_equal(a[fast], h[fast])  # bitwise
+    ok = fast & (b != 0)
+    ulp = np.abs(a[ok] - b[ok]) / np.spacing(np.abs(b[ok]))
+    print(f"log64 vs CUDA log: max {ulp.max():.2f} ulp, mean {ulp.mean():.3f} ulp")
+    assert ulp.max() <= 2.0
+    assert np.array_equal(np.isnan(a), np.isnan(b))
+    rest = ~fast & ~np.isnan(a)
+    assert np.array_equal(a[rest], b[rest])

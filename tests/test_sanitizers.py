@@ -19,7 +19,7 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SAN = ["-fsanitize=address,undefined", "-fno-sanitize-recover=undefined", "-fno-omit-frame-pointer", "-g1"]
 FILES = ["tests/test_oracle_kat.py", "tests/test_column_oracle.py", "tests/test_newton_equations.py",
-         "tests/test_exp64.py", "tests/test_div64.py"]
+         "tests/test_exp64.py", "tests/test_div64.py", "tests/test_log64.py"]
 
 
 def _runtime(name):
