@@ -58,9 +58,11 @@ __device__ __forceinline__ double cell_zenith(const StepConst& sc, double lon, d
     double lbut = 12. - sc.eqh - lon * 24. * (1. / 360.);
     double lzut = 15. * (sc.ut - lbut);
     double zpt = lzut * PI * (1. / 180.);
-    double csz = sin(rlt) * sc.srd + cos(rlt) * sc.crd * cos(zpt);
+    double srlt, crlt;
+    sincos(rlt, &srlt, &crlt);
+    double csz = srlt * sc.srd + crlt * sc.crd * cos(zpt);
     double zr = acos(csz);
-    double s = zr * 180. / PI;
+    double s = zr * (180. / PI);
     return fmax(s, 0.);
 }
 
@@ -316,7 +318,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double det = b * b - 4. * a * cq;
         double msb;
         if (det > 0.) {
-            double xsb = div64(-b - sqrt(det), 2. * a);
+            double xsb = div64(-b - sqrt64(det), 2. * a);
             msb = div64(55.51 * xsb, 1.0 - xsb);
         } else {
             msb = 0.;
@@ -346,7 +348,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             double kx = kn[1] + kn[2] * rt;
             double xnb = 1.0 / (2.0 * (kn[3] + kn[4] * rt)) *
                          (-kn[1] - kn[2] * rt -
-                          sqrt(kx * kx - 4.0 * (kn[3] + kn[4] * rt) * (kn[5] + kn[6] * rt + kn[7] * log64(tf) - log64(pw))));
+                          sqrt64(kx * kx - 4.0 * (kn[3] + kn[4] * rt) * (kn[5] + kn[6] * rt + kn[7] * log64(tf) - log64(pw))));
             double mnb = 55.51 * xnb / (1.0 - xnb);
             double hnb = qn[1] + qn[2] * tr2 + (qn[3] + qn[4] * tr + qn[5] * tr2 + qn[6] * tr3) * pr +
                          (qn[7] + qn[8] * tr + qn[9] * tr2) * pr2 + qn[10] * tr * pr3;
@@ -361,9 +363,9 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             double q = a2 - 3.0 * b;
             double q3 = q * q * q;
             double rr = -(2.0 * a3) + 9.0 * a * b - 27.0 * cq;
-            double phi = atan(sqrt(fmax(4.0 * q3 - rr * rr, 0.)) / rr);
+            double phi = atan(sqrt64(fmax(4.0 * q3 - rr * rr, 0.)) / rr);
             if (phi < 0.) phi = phi + PI;
-            double msf = -(1.0 / 3.0 * (a + 2.0 * sqrt(a2 - 3.0 * b) * cos((PI + phi) / 3.0)));
+            double msf = -(1.0 / 3.0 * (a + 2.0 * sqrt64(a2 - 3.0 * b) * cos((PI + phi) / 3.0)));
             msf = fmax(msf, 0.);
             double mnf = mnb * (1.0 - msf / msb);
             mnf = fmax(mnf, 0.);
@@ -481,7 +483,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double biga = 169.5 + 5.18 * wt - 0.0825 * wt2 + 3.27e-3 * wt3;
         double eta = biga * exp64(-1.43 * log64(T)) * exp64(div64(448., T - t0));
         const double Teta = div64(T, eta);
-        double sqT = sqrt(T);
+        double sqT = sqrt64(T);
         double ah = exp64(60.51 - 0.095 * wt + 0.0077 * wt2 - 1.61e-5 * wt3 - (1.76 + 2.52e-4 * wt2) * sqT +
                         div64(-805.89 + 253.05 * exp64(0.076 * log64(wt)), sqT));
         double dclono2 = 5.e-8 * Teta;
@@ -489,12 +491,12 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double kh2o = 1.95e10 * exp64(-2800. * rT);
         double khh = 1.22e12 * exp64(-6200. * rT);
         double khydr = kh2o * aw + khh * ah * aw;
-        double gbh2o = div64(4 * hclono2 * 0.082 * T * sqrt(dclono2 * khydr), cclono2);
+        double gbh2o = div64(4 * hclono2 * 0.082 * T * sqrt64(dclono2 * khydr), cclono2);
         double mhcl = hhcl * phcl;
         double khcl = 7.9e11 * ah * dclono2 * mhcl;
-        double lclono2 = sqrt(div64(dclono2, khydr + khcl));
+        double lclono2 = sqrt64(div64(dclono2, khydr + khcl));
         double fclono2 = div64(1., tanh(div64(rmean, lclono2))) - div64(lclono2, rmean);
-        double grxn = fclono2 * gbh2o * sqrt(1. + div64(khcl, khydr));
+        double grxn = fclono2 * gbh2o * sqrt64(1. + div64(khcl, khydr));
         double gbhcl = div64(grxn * khcl, khcl + khydr);
         double gs = 66.12 * hclono2 * mhcl * exp64(-1374. * rT);
         double fhcl = div64(1., 1 + div64(0.612 * (gs + gbhcl) * pclono2, phcl));
@@ -509,9 +511,9 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double chocl = 2009. * sqT;
         double dhocl = 6.4e-8 * Teta;
         double khoclhcl = 1.25e9 * ah * dhocl * mhcl;
-        double lhocl = sqrt(div64(dhocl, khoclhcl));
+        double lhocl = sqrt64(div64(dhocl, khoclhcl));
         double fhocl = div64(1., tanh(div64(rmean, lhocl))) - div64(lhocl, rmean);
-        grxn = div64(4. * hhocl * 0.082 * T * sqrt(dhocl * khoclhcl), chocl);
+        grxn = div64(4. * hhocl * 0.082 * T * sqrt64(dhocl * khoclhcl), chocl);
         double ghoclhcl = div64(1., 1. + div64(1., fhocl * grxn * fhcl));
         kl[4] = 0.25 * ghoclhcl * chocl * aliq * rZHCL;
         double mhobr = hhobr * phobr;
@@ -520,18 +522,18 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         if (ratio < 1.) {
             double k1hobrhcl = k2hobrhcl * mhcl;
             double dhobr = 6.2e-8 * Teta;
-            double lhobr = sqrt(div64(dhobr, k1hobrhcl));
+            double lhobr = sqrt64(div64(dhobr, k1hobrhcl));
             double fhobr = div64(1., tanh(div64(rmean, lhobr))) - div64(lhobr, rmean);
             double chobr = 1477. * sqT;
-            double ghobrhcl = div64(4. * hhobr * 0.082 * T * sqrt(dhobr * k1hobrhcl) * fhobr, chobr);
+            double ghobrhcl = div64(4. * hhobr * 0.082 * T * sqrt64(dhobr * k1hobrhcl) * fhobr, chobr);
             kl[6] = 0.25 * ghobrhcl * chobr * aliq * rZHCL;
         } else {
             double k1hobrhcl = k2hobrhcl * mhobr;
             double dhcl = 7.8e-8 * Teta;
-            double lhcl = sqrt(div64(dhcl, k1hobrhcl));
+            double lhcl = sqrt64(div64(dhcl, k1hobrhcl));
             double fh = div64(1., tanh(div64(rmean, lhcl))) - div64(lhcl, rmean);
             double chcl = 2408. * sqT;
-            double ghobrhcl = div64(4. * hhcl * 0.082 * T * sqrt(dhcl * k1hobrhcl) * fh, chcl);
+            double ghobrhcl = div64(4. * hhcl * 0.082 * T * sqrt64(dhcl * k1hobrhcl) * fh, chcl);
             kl[6] = div64(0.25 * ghobrhcl * chcl * aliq, ZHOBR);
         }
         double CBAR = 1400.1 * sqT;
@@ -547,8 +549,8 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         const double PT = ptot * rT, NS = nnats, NL = nnatl;
         const double rZH2O = 1. / ZH2O, rZHCL = 1. / ZHCL;
 #define NATR(G, M, RZ)                                                                                        \
-    (((G) * 4.56E4 * sqrt(T * (1. / (M))) * (rnats * rnats) * NS / (1.0 + 3.3E4 * (G) * rnats * PT) +     \
-      (G) * 4.56E4 * sqrt(T * (1. / (M))) * (rnatl * rnatl) * NL / (1.0 + 3.3E4 * (G) * rnatl * PT)) * \
+    (((G) * 4.56E4 * sqrt64(T * (1. / (M))) * (rnats * rnats) * NS / (1.0 + 3.3E4 * (G) * rnats * PT) +     \
+      (G) * 4.56E4 * sqrt64(T * (1. / (M))) * (rnatl * rnatl) * NL / (1.0 + 3.3E4 * (G) * rnatl * PT)) * \
      (RZ))
         ksl[0] = NATR(0.004, 97.45, rZH2O);
         ksl[1] = NATR(0.2, 97.45, rZHCL);
@@ -567,7 +569,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         const double PT = ptot * rT, NI = nice;
         const double rZH2O = 1. / ZH2O, rZHCL = 1. / ZHCL, rZHOBR = 1. / ZHOBR;
 #define ICER(G, M, RZ) \
-    ((G) * 4.56E4 * sqrt(T * (1. / (M))) * (rice * rice) * NI / (1.0 + 3.3E4 * (G) * rice * PT) * (RZ))
+    ((G) * 4.56E4 * sqrt64(T * (1. / (M))) * (rice * rice) * NI / (1.0 + 3.3E4 * (G) * rice * PT) * (RZ))
         ksl[1] = ICER(0.3, 97.45, rZHCL);
         ksl[0] = ICER(0.3, 97.45, rZH2O);
         ksl[2] = ICER(0.02, 108.0, rZH2O);

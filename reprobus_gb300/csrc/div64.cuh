@@ -50,4 +50,32 @@ __device__ __forceinline__ double div64(double a, double b) {
     return fma(r, fma(-b, q, a), q);
 }
 
+// sqrt(x) for positive normal x with six FP64-pipe instructions after the
+// hardware's reciprocal square root estimate (rsqrt.approx.ftz.f64; the host
+// build rounds 1 / sqrt(x) down to 20 bits): one Goldschmidt step refines
+// s ~ sqrt(x) and h ~ 1 / (2 sqrt(x)) together, and the remainder x - s^2
+// (exact in one FMA) corrects s (the same correction as div64's). Other
+// arguments take the IEEE square root.
+static __device__ __forceinline__ double sqrt64_ieee(double x) { return sqrt(x); }
+
+__device__ __forceinline__ double sqrt64(double x) {
+    if (e64_hi(x) - 0x00100000u >= 0x7fe00000u) return sqrt64_ieee(x);  // not a positive normal
+#ifdef __CUDA_ARCH__
+    double r;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+#else
+    double r = 1.0 / sqrt(x);
+    uint64_t br;
+    memcpy(&br, &r, 8);
+    br &= ~((1ull << 32) - 1);
+    memcpy(&r, &br, 8);
+#endif
+    double s = x * r;
+    double h = 0.5 * r;
+    const double e = fma(-s, h, 0.5);
+    s = fma(s, e, s);
+    h = fma(h, e, h);
+    return fma(fma(-s, s, x), h, s);
+}
+
 }  // namespace rpb

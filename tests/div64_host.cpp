@@ -7,3 +7,7 @@
 extern "C" void div64_many(const double* a, const double* b, double* out, long n) {
     for (long i = 0; i < n; i++) out[i] = rpb::div64(a[i], b[i]);
 }
+
+extern "C" void sqrt64_many(const double* x, double* out, long n) {
+    for (long i = 0; i < n; i++) out[i] = rpb::sqrt64(x[i]);
+}

@@ -1,5 +1,5 @@
-"""CPU checks of div64 (reprobus_gb300/csrc/div64.cuh), the FP64 division of
-the generated Newton equations, through its host build
+"""CPU checks of div64 and sqrt64 (reprobus_gb300/csrc/div64.cuh), the rate
+stage's FP64 quotients and square roots, through their host build
 (tests/div64_host.cpp): against the IEEE quotient over random operands of
 the chemistry's magnitudes (1e-40 .. 1e30), unit-range operands, and the
 operands that take the IEEE division (zero, subnormal, huge, inf, nan)."""
@@ -21,6 +21,7 @@ def lib(tmp_path_factory):
                     os.path.join(ROOT, "tests", "div64_host.cpp")], check=True)
     L = ctypes.CDLL(out)
     L.div64_many.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_long]
+    L.sqrt64_many.argtypes = [ctypes.c_void_p] * 2 + [ctypes.c_long]
     return L
 
 
@@ -54,3 +55,21 @@ def test_operands_outside_the_range_take_the_ieee_division(lib):
     assert np.array_equal(np.isnan(got), np.isnan(want))
     ok = ~np.isnan(want)
     assert np.array_equal(got[ok], want[ok])
+
+
+def test_square_roots_are_the_ieee_ones_within_an_ulp(lib):
+    rng = np.random.default_rng(4)
+    x = np.concatenate([10.0 ** rng.uniform(-300, 300, 1_000_000), rng.uniform(0.25, 4.0, 1_000_000),
+                        np.array([0.0, -0.0, -1.0, 5e-324, 1e-310, np.inf, np.nan, 1.0, 4.0, 2.0])])
+    x = np.ascontiguousarray(x)
+    got = np.empty_like(x)
+    lib.sqrt64_many(x.ctypes.data, got.ctypes.data, x.size)
+    with np.errstate(invalid="ignore"):
+        want = np.sqrt(x)
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    fin = np.isfinite(want) & (want > 0)
+    ulp = np.abs(got[fin] - want[fin]) / np.spacing(want[fin])
+    print(f"sqrt64: max {ulp.max():.2f} ulp; {np.mean(got[fin] != want[fin]):.2e} differ from IEEE")
+    assert ulp.max() <= 1.0 and np.mean(got[fin] != want[fin]) < 1e-4
+    rest = ~fin & ~np.isnan(want)
+    assert np.array_equal(got[rest], want[rest])

@@ -1,6 +1,7 @@
-"""div64 (reprobus_gb300/csrc/div64.cuh) on the GPU, from the hardware's
-reciprocal estimate: within one ulp of the IEEE quotient and equal to it
-but for rare operands, over the chemistry's magnitudes."""
+"""div64 and sqrt64 (reprobus_gb300/csrc/div64.cuh) on the GPU, from the
+hardware's reciprocal (square root) estimates: within one ulp of the IEEE
+quotient (square root) and equal to it but for rare operands, over the
+chemistry's magnitudes."""
 import ctypes
 import os
 import subprocess
@@ -33,3 +34,21 @@ def test_device_quotients_match_ieee(tmp_path):
     assert ulp.max() <= 1.0 and np.mean(q[fin] != ieee[fin]) < 1e-4
     assert np.array_equal(np.isnan(q), np.isnan(ieee))
     assert np.array_equal(q[~fin & ~np.isnan(q)], ieee[~fin & ~np.isnan(ieee)])
+
+
+def test_device_square_roots_match_ieee(tmp_path):
+    so = str(tmp_path / "libdiv64_dev.so")
+    subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-shared",
+                    "-Xcompiler", "-fPIC", "-o", so, os.path.join(ROOT, "tests", "div64_dev.cu")], check=True)
+    L = ctypes.CDLL(so)
+    L.sqrt64_dev.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_long]
+    rng = np.random.default_rng(6)
+    x = np.concatenate([10.0 ** rng.uniform(-300, 300, 3_000_000), rng.uniform(0.25, 4.0, 1_000_000),
+                        np.array([0.0, -1.0, 1e-310, np.inf, np.nan, 1.0, 4.0])])
+    q, ieee = np.empty_like(x), np.empty_like(x)
+    assert L.sqrt64_dev(x.ctypes.data, q.ctypes.data, ieee.ctypes.data, x.size) == 0
+    fin = np.isfinite(ieee) & (ieee > 0)
+    ulp = np.abs(q[fin] - ieee[fin]) / np.spacing(ieee[fin])
+    print(f"sqrt64: max {ulp.max():.2f} ulp; {np.mean(q[fin] != ieee[fin]):.2e} differ")
+    assert ulp.max() <= 1.0 and np.mean(q[fin] != ieee[fin]) < 1e-4
+    assert np.array_equal(np.isnan(q), np.isnan(ieee))
