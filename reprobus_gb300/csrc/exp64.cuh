@@ -21,7 +21,8 @@
 // FMA. The error is that of the final rounding, the table entry and the
 // tail: at most about 1.5 ulp (tests/test_exp64.py checks the host build
 // against long double, tests/test_gpu_exp64.py the device code against
-// CUDA's exp). Outside |y| < 64 (and for NaN, inf) it returns exp(y).
+// CUDA's exp). Below -745.2 it returns 0 (as exp does); elsewhere outside
+// |y| < 64 (and for NaN, inf) it returns exp(y).
 #pragma once
 #include <cmath>
 #include <cstdint>
@@ -99,7 +100,12 @@ __device__ __forceinline__ double e64_int(int k) {
 
 __device__ __forceinline__ double exp64(double y) {
     const uint32_t hy = e64_hi(y);
-    if ((hy & 0x7ff00000u) >= 0x40500000u) return exp(y);  // |y| >= 64, inf, nan
+    if ((hy & 0x7ff00000u) >= 0x40500000u) {  // |y| >= 64, inf, nan
+        // exp(y) rounds to 0 below -745.2 (the column absorption terms of
+        // J(NO) deep in the atmosphere): no library call for those
+        if (y < -745.2) return 0.;
+        return exp(y);
+    }
     // k = rint(y / L) in FP32 (|y / L| < 2^22: the 1.5 2^23 shift rounds it)
     const float kf = fmaf(e64_to_f32(y), EXP64_INVF, 12582912.f);
     const int k = (int)e64_bits(kf) - (int)e64_bits(12582912.f);

@@ -69,7 +69,8 @@ def test_rate_stage_arguments(lib):
 
 
 def test_outside_the_fast_range_it_is_exp(lib):
-    y = np.array([64.0, -64.0, 100.0, -700.0, 709.0, 710.0, -745.0, -746.0, -1e4, np.inf, -np.inf, np.nan])
+    y = np.array([64.0, -64.0, 100.0, -700.0, 709.0, 710.0, -745.0, -745.13, -745.14, -745.2, -745.21, -746.0,
+                  -1e4, -2.7e6, np.inf, -np.inf, np.nan])
     got = _exp64(lib, y)
     with np.errstate(over="ignore"):
         want = np.exp(y)
