@@ -83,22 +83,22 @@ __device__ __forceinline__ void cell_phot(const double* __restrict__ ajl, const 
         if (c_dsza[i - 1] >= sza) { is = i - 1; break; }
     }
     const double dz = 1.;
-    const double stepo3 = (c_xv3[NOZO - 1] - c_xv3[0]) / (NOZO - 1);
+    const double stepo3 = div64(c_xv3[NOZO - 1] - c_xv3[0], (double)(NOZO - 1));
     double zin = fmin(alt, 78.9);
     int iz = (int)(zin / dz) + 1;
     int ii = (int)zin;
     double v3std = o3up[ii] - (zin - (double)ii) * (o3up[ii] - o3up[ii + 1]);
-    double v3rat = o3t / v3std;
+    double v3rat = div64(o3t, v3std);
     v3rat = fmax(v3rat, c_xv3[0]);
     v3rat = fmin(v3rat, c_xv3[NOZO - 1]);
-    int iv = (int)trunc((v3rat - c_xv3[0]) / stepo3) + 1;
+    int iv = (int)trunc(div64(v3rat - c_xv3[0], stepo3)) + 1;
     iv = min(iv, NOZO - 1);
     int j = max(iz, 1);
     int k = max(is, 1);
     int l = max(iv, 1);
     double cizin = (zin - (double)(j - 1) * dz) / dz;
-    double cisza = (sza - c_dsza[k - 1]) / (c_dsza[k] - c_dsza[k - 1]);
-    double cio3t = (v3rat - c_xv3[l - 1]) / (c_xv3[l] - c_xv3[l - 1]);
+    double cisza = div64(sza - c_dsza[k - 1], c_dsza[k] - c_dsza[k - 1]);
+    double cio3t = div64(v3rat - c_xv3[l - 1], c_xv3[l] - c_xv3[l - 1]);
     double w111 = (1. - cizin) * (1. - cisza) * (1. - cio3t);
     double w112 = (1. - cizin) * (1. - cisza) * cio3t;
     double w121 = (1. - cizin) * cisza * (1. - cio3t);
@@ -154,12 +154,12 @@ __constant__ double c_jno_so3[3] = {4.6e-19, 6.7e-19, 7.1e-19};
 __device__ __forceinline__ double cell_jno(double sza_top, double hnm, double colo2, double colno, double colo3) {
     const double factor = 3.141592 / 180.;
     const double d = 1.65e+09, a = 5.1e+07, kq = 1.5e-09;
-    double sec = 1. / cos(sza_top * factor);
+    double sec = div64(1., cos(sza_top * factor));
     colo2 = colo2 * sec;
     colno = colno * sec;
     colo3 = colo3 * sec;
     double n2 = hnm * 0.78;
-    double p = d / (a + d + kq * n2);
+    double p = div64(d, a + d + kq * n2);
     double bd[3];
 #pragma unroll
     for (int b = 0; b < 3; b++) {
@@ -231,7 +231,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
     A.parth2o = 1.;
     A.parthcl = 1.;
     // F:2778-2787
-    const double rhnm = 1. / hnm;
+    const double rhnm = div64(1., hnm);
     double qh2o = ck[2] * rhnm;
     double pw = qh2o * ptot * (1. / 1013.0);
     pw = fmin(pw, 2.e-3 / 1013.);
@@ -242,12 +242,12 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double t = fmin(temp, 273.);
         double pn0t = pn0 * 1013. * 0.75;
         double zmt = -2.7836 - 0.00088 * t;
-        double zbt = 38.9855 - 11397.0 / t + 0.009179 * t;
+        double zbt = 38.9855 - div64(11397.0, t) + 0.009179 * t;
         double zhno3eq = exp64(zmt * log64(pw * 1013. * 0.75) + zbt * LN10);
-        if (pn0t / zhno3eq >= 1.) {
+        if (div64(pn0t, zhno3eq) >= 1.) {
             lnat = 1;
             double pn = zhno3eq * (1. / (0.75 * 1013.));
-            double hno3s = (pn0 - pn) * 1013. * hnm / ptot;
+            double hno3s = div64((pn0 - pn) * 1013. * hnm, ptot);
             hno3s = fmax(hno3s, 0.);
             vnat = hno3s * amu * 117. * (1. / 1.35);
             double vnat_small_max = nnat_small_max * (4. / 3. * PI * (rnats * rnats * rnats));
@@ -261,10 +261,10 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
                 vnatl = 0.;
             }
             anat = nnats * 4 * PI * (rnats * rnats) + nnatl * 4 * PI * (rnatl * rnatl);
-            parthno3s = 1.0 - (pn0 - pn) / pn0;
+            parthno3s = 1.0 - div64(pn0 - pn, pn0);
             parthno3s = fmax(parthno3s, 0.);
             parthno3s = fmin(parthno3s, 1.);
-            A.parthno3sl = 1.0 - (pn0 - pn) * vnatl / vnat / pn0;
+            A.parthno3sl = 1.0 - div64(div64((pn0 - pn) * vnatl, vnat), pn0);
             A.parthno3sl = fmax(A.parthno3sl, 0.);
             A.parthno3sl = fmin(A.parthno3sl, 1.);
         }
@@ -273,25 +273,25 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
     double tice;
     {
         double t = fmin(temp, 273.);
-        tice = 2668.70 / (10.4310 - (log64(pw) + LN760) * (1. / LN10));
+        tice = div64(2668.70, 10.4310 - (log64(pw) + LN760) * (1. / LN10));
         if (t <= tice) {
             lice = 1;
             lnat = 0;
             anat = 0.;
-            double zh2oeq = exp64((-2668.7 / t + 10.4310) * LN10);
+            double zh2oeq = exp64((div64(-2668.7, t) + 10.4310) * LN10);
             double ph2o = zh2oeq * (1. / 760.0);
-            double h2os = fmax(pw - ph2o, 0.) * 1013. * hnm / ptot;
+            double h2os = div64(fmax(pw - ph2o, 0.) * 1013. * hnm, ptot);
             double vice = h2os * amu * 18. * (1. / 0.928);
             nice = vice * (1. / (4. / 3. * PI * (rice * rice * rice)));
             aice = nice * 4 * PI * (rice * rice);
-            A.parth2o = 1.0 - fmax(pw - ph2o, 0.) / pw;
+            A.parth2o = 1.0 - div64(fmax(pw - ph2o, 0.), pw);
             A.parth2o = fmax(A.parth2o, 0.);
             A.parth2o = fmin(A.parth2o, 1.);
             double zmt = -2.7836 - 0.00088 * t;
-            double zbt = 38.9855 - 11397.0 / t + 0.009179 * t;
+            double zbt = 38.9855 - div64(11397.0, t) + 0.009179 * t;
             double zhno3eq = exp64(zmt * log64(pw * A.parth2o * 1013. * 0.75) + zbt * LN10);
             double pn = zhno3eq * (1. / (0.75 * 1013.));
-            parthno3s = 1.0 - (pn0 - pn) / pn0;
+            parthno3s = 1.0 - div64(pn0 - pn, pn0);
             parthno3s = fmax(parthno3s, 0.);
             parthno3s = fmin(parthno3s, 1.);
             A.parthno3sl = parthno3s;
@@ -303,7 +303,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
     {
         condliq = 1;
         double t = tl;
-        const double rt = 1. / t;  // E / T as E * (1 / T) in the liquid-aerosol blocks
+        const double rt = div64(1., t);  // E / T as E * (1 / T) in the liquid-aerosol blocks
         double qh2ol = ck[2] * A.parth2o * rhnm;
         pw = qh2ol * ptot * (1. / 1013.0);
         pw = fmin(pw, 2.e-3 / 1013.);
@@ -346,36 +346,36 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
                          (qs[7] + qs[8] * tr + qs[9] * tr2) * pr2 + qs[10] * tr * pr3;
             hsb = exp64(hsb);
             double kx = kn[1] + kn[2] * rt;
-            double xnb = 1.0 / (2.0 * (kn[3] + kn[4] * rt)) *
+            double xnb = div64(1.0, 2.0 * (kn[3] + kn[4] * rt)) *
                          (-kn[1] - kn[2] * rt -
                           sqrt64(kx * kx - 4.0 * (kn[3] + kn[4] * rt) * (kn[5] + kn[6] * rt + kn[7] * log64(tf) - log64(pw))));
-            double mnb = 55.51 * xnb / (1.0 - xnb);
+            double mnb = div64(55.51 * xnb, 1.0 - xnb);
             double hnb = qn[1] + qn[2] * tr2 + (qn[3] + qn[4] * tr + qn[5] * tr2 + qn[6] * tr3) * pr +
                          (qn[7] + qn[8] * tr + qn[9] * tr2) * pr2 + qn[10] * tr * pr3;
             hnb = exp64(hnb);
             double mnb2 = mnb * mnb, msb2 = msb * msb;
-            a = (tt * hnb * mnb2 - tt * hsb * mnb * msb - 2.0 * mnb2 * msb + mnb * msb2 + hnb * mnb * msb * pn0 -
-                 hsb * msb2 * pn0) /
-                (mnb2 - mnb * msb);
-            b = msb * (-(2.0 * tt * hnb * mnb) + tt * hsb * msb + mnb * msb - hnb * msb * pn0) / (mnb - msb);
-            cq = (tt * hnb * mnb * msb2) / (mnb - msb);
+            a = div64(tt * hnb * mnb2 - tt * hsb * mnb * msb - 2.0 * mnb2 * msb + mnb * msb2 + hnb * mnb * msb * pn0 -
+                          hsb * msb2 * pn0,
+                      mnb2 - mnb * msb);
+            b = div64(msb * (-(2.0 * tt * hnb * mnb) + tt * hsb * msb + mnb * msb - hnb * msb * pn0), mnb - msb);
+            cq = div64(tt * hnb * mnb * msb2, mnb - msb);
             double a2 = a * a, a3 = a2 * a;
             double q = a2 - 3.0 * b;
             double q3 = q * q * q;
             double rr = -(2.0 * a3) + 9.0 * a * b - 27.0 * cq;
-            double phi = atan(sqrt64(fmax(4.0 * q3 - rr * rr, 0.)) / rr);
+            double phi = atan(div64(sqrt64(fmax(4.0 * q3 - rr * rr, 0.)), rr));
             if (phi < 0.) phi = phi + PI;
-            double msf = -(1.0 / 3.0 * (a + 2.0 * sqrt64(a2 - 3.0 * b) * cos((PI + phi) / 3.0)));
+            double msf = -(1.0 / 3.0 * (a + 2.0 * sqrt64(a2 - 3.0 * b) * cos(div64(PI + phi, 3.0))));
             msf = fmax(msf, 0.);
-            double mnf = mnb * (1.0 - msf / msb);
+            double mnf = mnb * (1.0 - div64(msf, msb));
             mnf = fmax(mnf, 0.);
-            double pn = mnf / (hnb * mnf / (mnf + msf) + hsb * msf / (mnf + msf));
-            double wsf = msf * 0.098076 / (1.0 + msf * 0.098076 + mnf * 0.063012);
-            double wnf = mnf * 0.063012 / (1.0 + msf * 0.098076 + mnf * 0.063012);
+            double pn = div64(mnf, div64(hnb * mnf, mnf + msf) + div64(hsb * msf, mnf + msf));
+            double wsf = div64(msf * 0.098076, 1.0 + msf * 0.098076 + mnf * 0.063012);
+            double wnf = div64(mnf * 0.063012, 1.0 + msf * 0.098076 + mnf * 0.063012);
             ms = msf;
             ws = wsf;
             wn = wnf;
-            parthno3l = 1.0 - (pn0 - pn) / pn0;
+            parthno3l = 1.0 - div64(pn0 - pn, pn0);
             parthno3l = fmin(parthno3l, 1.);
         }
         ws = fmax(ws, 0.005);
@@ -404,7 +404,7 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         rmean = rmode * AER_EXP_05;
         aliq = 4.0 * PI * (rmode * rmode) * ndrop * AER_EXP_2;
         double t = tl;
-        const double rt = 1. / t, rt2 = rt * rt, rt3 = rt2 * rt;
+        const double rt = div64(1., t), rt2 = rt * rt, rt3 = rt2 * rt;
         double ph2o0 = exp64(18.452406985 - 3505.1578807 * rt - 330918.55082 * rt2 + 12725068.262 * rt3);
         aw = div64(pw * 1013., ph2o0);
         aw = fmin(aw, 1.);
@@ -445,21 +445,21 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
             double tcel = t - 273.15;
             double netha = (1.718 + 0.0049 * tcel - 1.2e-5 * tcel * tcel) * 1.e-5;
             double rp3 = rpart * rpart * rpart;
-            double cdnre2 = 32.0 * rp3 * (rhopart - rhoair) * rhoair * 9.80665 / (3.0 * (netha * netha));
+            double cdnre2 = div64(32.0 * rp3 * (rhopart - rhoair) * rhoair * 9.80665, 3.0 * (netha * netha));
             double L = log64(cdnre2);
             double L2 = L * L, L3 = L2 * L, L4 = L2 * L2, L5 = L3 * L2, L6 = L3 * L3;
             double ynre = c_an_bnre[0] + c_an_bnre[1] * L + c_an_bnre[2] * L2 + c_an_bnre[3] * L3 +
                           c_an_bnre[4] * L4 + c_an_bnre[5] * L5 + c_an_bnre[6] * L6;
             double nre = exp64(ynre);
             if (nre >= 1.e-2) {
-                A.vsed = netha * nre / (2 * rhoair * rpart);
+                A.vsed = div64(netha * nre, 2 * rhoair * rpart);
             } else {
                 double lambda0 = 6.6e-8;
-                double lambda = lambda0 * (1013.25 / ptot) * (t * (1. / 293.15));
-                double us = 2.0 * (rpart * rpart) * 9.80665 * (rhopart - rhoair) / (9.0 * netha);
+                double lambda = lambda0 * div64(1013.25, ptot) * (t * (1. / 293.15));
+                double us = div64(2.0 * (rpart * rpart) * 9.80665 * (rhopart - rhoair), 9.0 * netha);
                 double shapek = 1.2;
-                A.vsed = us / shapek *
-                         (1.0 + 1.246 * lambda / rpart + 0.42 * lambda / rpart * exp64(-(0.87 * rpart / lambda)));
+                A.vsed = div64(us, shapek) * (1.0 + div64(1.246 * lambda, rpart) +
+                                              div64(0.42 * lambda, rpart) * exp64(-div64(0.87 * rpart, lambda)));
             }
         }
     }
@@ -547,10 +547,10 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double ZH2O = fmax(ck[2], 1.E-08 * hnm);
         double ZHCL = fmax(ck[12], 1.E-13 * hnm);
         const double PT = ptot * rT, NS = nnats, NL = nnatl;
-        const double rZH2O = 1. / ZH2O, rZHCL = 1. / ZHCL;
+        const double rZH2O = div64(1., ZH2O), rZHCL = div64(1., ZHCL);
 #define NATR(G, M, RZ)                                                                                        \
-    (((G) * 4.56E4 * sqrt64(T * (1. / (M))) * (rnats * rnats) * NS / (1.0 + 3.3E4 * (G) * rnats * PT) +     \
-      (G) * 4.56E4 * sqrt64(T * (1. / (M))) * (rnatl * rnatl) * NL / (1.0 + 3.3E4 * (G) * rnatl * PT)) * \
+    ((div64((G) * 4.56E4 * sqrt64(T * (1. / (M))) * (rnats * rnats) * NS, 1.0 + 3.3E4 * (G) * rnats * PT) +   \
+      div64((G) * 4.56E4 * sqrt64(T * (1. / (M))) * (rnatl * rnatl) * NL, 1.0 + 3.3E4 * (G) * rnatl * PT)) * \
      (RZ))
         ksl[0] = NATR(0.004, 97.45, rZH2O);
         ksl[1] = NATR(0.2, 97.45, rZHCL);
@@ -567,9 +567,9 @@ static __device__ __noinline__ void cell_aerosol(double temp, double ptot, doubl
         double ZHCL = fmax(ck[12], 1.E-13 * hnm);
         double ZHOBR = fmax(ck[25], 1.E-13 * hnm);
         const double PT = ptot * rT, NI = nice;
-        const double rZH2O = 1. / ZH2O, rZHCL = 1. / ZHCL, rZHOBR = 1. / ZHOBR;
+        const double rZH2O = div64(1., ZH2O), rZHCL = div64(1., ZHCL), rZHOBR = div64(1., ZHOBR);
 #define ICER(G, M, RZ) \
-    ((G) * 4.56E4 * sqrt64(T * (1. / (M))) * (rice * rice) * NI / (1.0 + 3.3E4 * (G) * rice * PT) * (RZ))
+    (div64((G) * 4.56E4 * sqrt64(T * (1. / (M))) * (rice * rice) * NI, 1.0 + 3.3E4 * (G) * rice * PT) * (RZ))
         ksl[1] = ICER(0.3, 97.45, rZHCL);
         ksl[0] = ICER(0.3, 97.45, rZH2O);
         ksl[2] = ICER(0.02, 108.0, rZH2O);

@@ -162,7 +162,7 @@ __device__ __forceinline__ void cell_prologue(const Params& P, int cell, CellPro
     // setup F:800-833
     const double t = P.trajtem[P.trajoff + g];
     const double pm = P.trajpre[P.trajoff + g];
-    F.hnm = P.trajpre[P.trajoff + g] / (P.trajtem[P.trajoff + g] * 1.38e-19);
+    F.hnm = div64(P.trajpre[P.trajoff + g], P.trajtem[P.trajoff + g] * 1.38e-19);
     F.n2 = 0.78 * F.hnm;
     F.o2 = 0.21 * F.hnm;
     F.co2 = 360.e-6 * F.hnm;
@@ -213,7 +213,7 @@ __device__ __forceinline__ void cell_prologue(const Params& P, int cell, CellPro
     cell_rates(P.sc.troe, P.sc.ltroe, t, F.hnm, pm, C.K);
     // rainout F:1315-1338
     const double rain_rate = 1.e-6;
-    const bool rain = C.ck0[2] / F.hnm >= 100.e-6;
+    const bool rain = div64(C.ck0[2], F.hnm) >= 100.e-6;
     F.rain_hno3 = rain ? rain_rate : 0.;
     F.rain_hno4 = 0.;
     F.rain_hcl = rain ? rain_rate : 0.;
