@@ -369,7 +369,8 @@ def build(day: bool):
 # --------------------------------------------------------------------------- #
 class Printer(C99CodePrinter):
     """Numbers as T(...) so that the float instantiation stays in FP32;
-    integer powers as products."""
+    integer powers as products; every quotient as nt_div<T>(numerator,
+    denominator) (newton_num.cuh)."""
 
     def __init__(self, real="T"):
         super().__init__()
@@ -384,22 +385,31 @@ class Printer(C99CodePrinter):
     def _print_Rational(self, e):
         return f"{self.real}({float(e)!r})"
 
+    def _div(self, num, den):
+        return f"nt_div<{self.real}>({num}, {den})"
+
+    def _print_Mul(self, e):
+        num, den = sp.fraction(e, exact=True)
+        if den == 1:
+            return super()._print_Mul(e)
+        return self._div(self._print(num), self._print(den))
+
     def _print_Pow(self, e):
         b, ex = e.args
         if ex == sp.Rational(1, 2):
             return f"sqrt({self._print(b)})"
         if ex == -1:
-            return f"({self.real}(1)/({self._print(b)}))"
+            return self._div(f"{self.real}(1)", self._print(b))
         if ex.is_Integer and 0 < ex <= 4:
             s = self.parenthesize(b, 100)
             return "(" + "*".join([s] * int(ex)) + ")"
         if ex.is_Integer and -4 <= ex < 0:
             s = self.parenthesize(b, 100)
-            return f"({self.real}(1)/({'*'.join([s] * int(-ex))}))"
+            return self._div(f"{self.real}(1)", "*".join([s] * int(-ex)))
         if ex == sp.Rational(-1, 2):
-            return f"({self.real}(1)/sqrt({self._print(b)}))"
+            return self._div(f"{self.real}(1)", f"sqrt({self._print(b)})")
         if ex == sp.Rational(-3, 2):
-            return f"({self.real}(1)/(({self._print(b)})*sqrt({self._print(b)})))"
+            return self._div(f"{self.real}(1)", f"({self._print(b)})*sqrt({self._print(b)})")
         raise ValueError(f"unexpected power {e}")
 
     def _print_Max(self, e):

@@ -86,46 +86,46 @@ __device__ __forceinline__ void nt_residual_day(const FF& F, PK K, PK tj, PK het
     R[39] = -ck0[39] + x[39]*(F.dt*(K[K_e53]*x[42] + tj[J_h1301]) + T(1));
     R[40] = F.dt*F.rain_hbr*x[18] - F.dt*(x[37]*(K[K_e50]*x[42] + K[K_e51]*x[43] + tj[J_ch3br]) + x[38]*(K[K_e52]*x[42] + tj[J_h1211]) + x[39]*(K[K_e53]*x[42] + tj[J_h1301]) + x[41]*(T(2)*K[K_e54]*x[43] + T(2)*tj[J_ch2br2])) - ck0[40] + x[40];
     R[41] = -ck0[41] + x[41]*(F.dt*(K[K_e54]*x[43] + tj[J_ch2br2]) + T(1));
-    R[42] = -tj[J_o3_o1d]*x[46]/(F.n2*K[K_hk4] + F.o2*K[K_hk5]) + x[42];
-    R[56] = -x[1]*(K[K_c1a]*x[42] + K[K_c2]*x[43] + K[K_d5]*x[44])/(F.o2*K[K_c4] + K[K_c3]*x[45]) + x[56];
-    const T D_ch3o = (K[K_c1b]*x[1]*x[42] + tj[J_ch3o2h]*x[29] + x[28]*(T(2)*K[K_c14]*x[28] + K[K_c18]*x[52] + K[K_c5]*x[49]))/(F.o2*K[K_c15]);
+    R[42] = nt_div<T>(-tj[J_o3_o1d]*x[46], F.n2*K[K_hk4] + F.o2*K[K_hk5]) + x[42];
+    R[56] = nt_div<T>(-x[1]*(K[K_c1a]*x[42] + K[K_c2]*x[43] + K[K_d5]*x[44]), F.o2*K[K_c4] + K[K_c3]*x[45]) + x[56];
+    const T D_ch3o = nt_div<T>(K[K_c1b]*x[1]*x[42] + tj[J_ch3o2h]*x[29] + x[28]*(T(2)*K[K_c14]*x[28] + K[K_c18]*x[52] + K[K_c5]*x[49]), F.o2*K[K_c15]);
     R[27] = -F.dt*(D_ch3o*F.o2*K[K_c15] + K[K_c17b]*x[29]*x[43] + K[K_c1c]*x[1]*x[42] + K[K_c3]*x[45]*x[56]) - ck0[27] + x[27]*(F.dt*(K[K_c10]*x[44] + K[K_c19]*x[50] + K[K_c8]*x[43] + K[K_c9]*x[45] + tj[J_ch2o_co] + tj[J_ch2o_hco]) + T(1));
-    const T D_hco = x[27]*(K[K_c10]*x[44] + K[K_c19]*x[50] + K[K_c8]*x[43] + K[K_c9]*x[45] + tj[J_ch2o_hco])/(F.o2*K[K_c12]);
+    const T D_hco = nt_div<T>(x[27]*(K[K_c10]*x[44] + K[K_c19]*x[50] + K[K_c8]*x[43] + K[K_c9]*x[45] + tj[J_ch2o_hco]), F.o2*K[K_c12]);
     R[8] = -F.dt*(D_hco*F.o2*K[K_c12] + F.co2*tj[J_co2] + tj[J_ch2o_co]*x[27]) - ck0[8] + x[8]*(F.dt*K[K_a36]*x[43] + T(1));
-    const T D_r1 = (K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47] + K[K_b4]*x[49] + K[K_d2]*x[44] + tj[J_o3_o1d] + tj[J_o3_o3p])/(F.o2*K[K_hk2]);
+    const T D_r1 = nt_div<T>(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47] + K[K_b4]*x[49] + K[K_d2]*x[44] + tj[J_o3_o1d] + tj[J_o3_o3p], F.o2*K[K_hk2]);
     R[45] = -D_r1*x[46] + x[45];
-    R[46] = x[46] - x[7]/(D_r1 + T(1));
-    const T D_r4 = (F.h2*K[K_a19] + K[K_a36]*x[8] + K[K_a5]*x[45])/(F.o2*K[K_a1] + K[K_a2]*x[46] + T(8.049999999999999e-11)*x[47]);
+    R[46] = x[46] + nt_div<T>(-x[7], D_r1 + T(1));
+    const T D_r4 = nt_div<T>(F.h2*K[K_a19] + K[K_a36]*x[8] + K[K_a5]*x[45], F.o2*K[K_a1] + K[K_a2]*x[46] + T(8.049999999999999e-11)*x[47]);
     R[55] = -D_r4*x[43] + x[55];
-    const T D_r7 = tj[J_no]/(F.o2*K[K_b7] + K[K_b6]*x[49]);
+    const T D_r7 = nt_div<T>(tj[J_no], F.o2*K[K_b7] + K[K_b6]*x[49]);
     R[51] = -D_r7*x[49] + x[51];
-    const T D_r8 = K[K_b9]*x[46]/(K[K_b12]*x[48] + tj[J_no3_no2] + tj[J_no3_no]);
+    const T D_r8 = nt_div<T>(K[K_b9]*x[46], K[K_b12]*x[48] + tj[J_no3_no2] + tj[J_no3_no]);
     R[54] = -D_r8*x[48] + x[54];
-    const T D_r5 = (D_r8*tj[J_no3_no] + K[K_b3]*x[45] + tj[J_no2])/(K[K_a26]*x[47] + K[K_b4]*x[46] + K[K_c5]*x[28] + K[K_d4]*x[52] + K[K_e4]*x[53]);
-    R[48] = -x[20]/(D_r5*D_r7 + D_r5 + D_r8 + T(1)) + x[48];
+    const T D_r5 = nt_div<T>(D_r8*tj[J_no3_no] + K[K_b3]*x[45] + tj[J_no2], K[K_a26]*x[47] + K[K_b4]*x[46] + K[K_c5]*x[28] + K[K_d4]*x[52] + K[K_e4]*x[53]);
+    R[48] = nt_div<T>(-x[20], D_r5*D_r7 + D_r5 + D_r8 + T(1)) + x[48];
     R[49] = -D_r5*x[48] + x[49];
-    const T D_r6 = (D_r4*F.o2*K[K_a1] + K[K_a30]*x[16] + K[K_a6]*x[46] + K[K_c8]*x[27] + K[K_d8]*x[52] + K[K_e10]*x[53])/(K[K_a17]*x[43] + K[K_a26]*x[49] + T(2)*K[K_a27]*x[47] + K[K_a6b]*x[46] + K[K_a7]*x[45] + K[K_d10]*x[44] + K[K_d33]*x[52] + K[K_d7]*x[44] + K[K_e15]*x[53] + K[K_e7]*x[50] + T(8.049999999999999e-11)*x[55]);
+    const T D_r6 = nt_div<T>(D_r4*F.o2*K[K_a1] + K[K_a30]*x[16] + K[K_a6]*x[46] + K[K_c8]*x[27] + K[K_d8]*x[52] + K[K_e10]*x[53], K[K_a17]*x[43] + K[K_a26]*x[49] + T(2)*K[K_a27]*x[47] + K[K_a6b]*x[46] + K[K_a7]*x[45] + K[K_d10]*x[44] + K[K_d33]*x[52] + K[K_d7]*x[44] + K[K_e15]*x[53] + K[K_e7]*x[50] + T(8.049999999999999e-11)*x[55]);
     R[47] = -D_r6*x[43] + x[47];
-    const T D_r13 = K[K_d31]*x[48]/(K[K_d32]*x[45] + het[0]*x[2] + het[1]*x[12] + tj[J_clono2_cl] + tj[J_clono2_clo]);
-    const T D_r9 = (D_r13*het[0]*x[2] + K[K_d33]*x[47])/(K[K_d35]*x[45] + het[4]*x[12] + tj[J_hocl]);
-    const T D_r10 = K[K_d60]*x[52]/(F.hnm*K[K_d61] + tj[J_cl2o2]);
-    const T D_r12 = K[K_e5c]*x[53]/tj[J_brcl];
-    const T D_r11 = (T(2)*D_r10*tj[J_cl2o2] + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*x[28] + K[K_d3]*x[45] + K[K_d4]*x[49] + K[K_d8]*x[43] + K[K_e5b]*x[53])/(K[K_d10]*x[47] + K[K_d2]*x[46] + K[K_d37]*x[14] + K[K_d5]*x[1] + K[K_d7]*x[47]);
+    const T D_r13 = nt_div<T>(K[K_d31]*x[48], K[K_d32]*x[45] + het[0]*x[2] + het[1]*x[12] + tj[J_clono2_cl] + tj[J_clono2_clo]);
+    const T D_r9 = nt_div<T>(D_r13*het[0]*x[2] + K[K_d33]*x[47], K[K_d35]*x[45] + het[4]*x[12] + tj[J_hocl]);
+    const T D_r10 = nt_div<T>(K[K_d60]*x[52], F.hnm*K[K_d61] + tj[J_cl2o2]);
+    const T D_r12 = nt_div<T>(K[K_e5c]*x[53], tj[J_brcl]);
+    const T D_r11 = nt_div<T>(T(2)*D_r10*tj[J_cl2o2] + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*x[28] + K[K_d3]*x[45] + K[K_d4]*x[49] + K[K_d8]*x[43] + K[K_e5b]*x[53], K[K_d10]*x[47] + K[K_d2]*x[46] + K[K_d37]*x[14] + K[K_d5]*x[1] + K[K_d7]*x[47]);
     R[44] = -D_r11*x[52] + x[44];
-    R[52] = -x[22]/(D_r11 + T(1)) + x[52];
-    const T D_r27 = K[K_e13]*x[48]/(K[K_e8]*x[45] + tj[J_brono2]);
-    const T D_r28 = K[K_e15]*x[47]/(K[K_e16]*x[45] + tj[J_hobr]);
-    const T D_r29 = K[K_e5c]*x[52]/tj[J_brcl];
-    const T D_r30 = (T(0.85)*D_r27*tj[J_brono2] + D_r28*tj[J_hobr] + D_r29*tj[J_brcl] + K[K_e10]*x[43] + K[K_e3]*x[45] + K[K_e4]*x[49] + K[K_e5a]*x[52] + K[K_e5b]*x[52] + T(2)*K[K_e6]*x[53] + tj[J_bro])/(K[K_c19]*x[27] + K[K_e2]*x[46] + K[K_e7]*x[47]);
+    R[52] = nt_div<T>(-x[22], D_r11 + T(1)) + x[52];
+    const T D_r27 = nt_div<T>(K[K_e13]*x[48], K[K_e8]*x[45] + tj[J_brono2]);
+    const T D_r28 = nt_div<T>(K[K_e15]*x[47], K[K_e16]*x[45] + tj[J_hobr]);
+    const T D_r29 = nt_div<T>(K[K_e5c]*x[52], tj[J_brcl]);
+    const T D_r30 = nt_div<T>(T(0.85)*D_r27*tj[J_brono2] + D_r28*tj[J_hobr] + D_r29*tj[J_brcl] + K[K_e10]*x[43] + K[K_e3]*x[45] + K[K_e4]*x[49] + K[K_e5a]*x[52] + K[K_e5b]*x[52] + T(2)*K[K_e6]*x[53] + tj[J_bro], K[K_c19]*x[27] + K[K_e2]*x[46] + K[K_e7]*x[47]);
     R[50] = -D_r30*x[53] + x[50];
-    R[53] = -x[23]/(D_r30 + T(1)) + x[53];
+    R[53] = nt_div<T>(-x[23], D_r30 + T(1)) + x[53];
     const T D_coea = D_r6*(T(1.7e-11)*D_r4 + T(2)*D_r6*K[K_a27] + T(2)*K[K_a17]) + T(2)*K[K_a31];
     const T D_coeb = D_r6*K[K_b23]*x[48] + D_r6*K[K_c7]*x[28] + D_r6*K[K_d33]*x[52] + D_r6*K[K_d7]*x[44] + D_r6*K[K_e15]*x[53] + D_r6*K[K_e7]*x[50] + F.parthbr*K[K_e11]*x[18] + F.parthcl*K[K_d11]*x[12] + F.parthno3*K[K_b27]*x[4] + K[K_b22]*x[48] + K[K_b28]*x[21] + K[K_c17a]*x[29] + K[K_c2]*x[1] + K[K_c8]*x[27] + K[K_d34]*x[14] + K[K_d9]*x[52];
     const T D_coec = D_ch3o*F.o2*K[K_c15] + D_hco*F.o2*K[K_c12] + F.h2*K[K_d6]*x[44] + F.parth2o*x[2]*(T(2)*K[K_a1et]*x[42] + T(2)*tj[J_h2o]) + F.parthno3*tj[J_hno3]*x[4] + K[K_c3]*x[45]*x[56] + K[K_e16]*x[25]*x[45] + tj[J_ch3o2h]*x[29] + T(2)*tj[J_h2o2]*x[16] + tj[J_hbr]*x[18] + tj[J_hobr]*x[25] + x[14]*(K[K_d35]*x[45] + K[K_d37]*x[44] + tj[J_hocl]) + x[21]*(F.hnm*K[K_b24] + tj[J_hno4]) + x[27]*(K[K_c9]*x[45] + tj[J_ch2o_hco]) + x[42]*(T(2.4e-10)*F.h2 + x[1]*(K[K_c1a] + K[K_c1b]));
     const T D_argum_c0 = T(4)*D_coea*D_coec + (D_coeb*D_coeb);
     const bool sel_D_argum = (D_argum_c0) >= (T(0));
     const T D_argum = sel_D_argum ? T(D_argum_c0) : T(T(0));
-    R[43] = x[43] - T(0.5)*(sqrt(D_argum) - D_coeb)/D_coea;
+    R[43] = x[43] + nt_div<T>(-(sqrt(D_argum) - D_coeb), T(2)*D_coea);
     const T D_t06_c0 = tj[J_hocl]*x[14];
     const T D_t06_c1 = K[K_d33]*x[47]*x[52];
     const bool sel_D_t06 = (D_t06_c0) <= (D_t06_c1);
@@ -139,8 +139,8 @@ __device__ __forceinline__ void nt_residual_day(const FF& F, PK K, PK tj, PK het
     const bool sel_D_t09 = (D_t09_c0) <= (D_t09_c1);
     const T D_t09 = sel_D_t09 ? T(D_t09_c0) : T(D_t09_c1);
     const T dr7_c0 = T(2)*x[45];
-    const T dr7_c1 = T(2)*tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
-    R[7] = -F.dt*(T(2)*F.o2*tj[J_o2] + K[K_a26]*x[47]*x[49] + K[K_c5]*x[28]*x[49]) + F.dt*(D_t06 + T(2)*D_t07 + D_t09 + K[K_b3]*dr7_c0*x[48] + K[K_b9]*dr7_c1*x[46]*x[48] + K[K_d3]*dr7_c0*x[52] + T(2)*K[K_d60]*tj[J_cl2o2]*(x[52]*x[52])/(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(2)*K[K_e5b]*x[52]*x[53] + T(2)*K[K_e6]*(x[53]*x[53]) + T(2)*K[K_hk1]*(x[45]*x[45]) + K[K_hk3]*dr7_c0*x[46] + dr7_c1*tj[J_clono2_cl]*x[13] + x[45]*(K[K_a5]*x[43] + K[K_a7]*x[47]) + x[46]*(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47])) - ck0[7] + x[7];
+    const T dr7_c1 = nt_div<T>(T(2)*tj[J_no3_no], fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]));
+    R[7] = -F.dt*(T(2)*F.o2*tj[J_o2] + K[K_a26]*x[47]*x[49] + K[K_c5]*x[28]*x[49]) + F.dt*(D_t06 + T(2)*D_t07 + D_t09 + K[K_b3]*dr7_c0*x[48] + K[K_b9]*dr7_c1*x[46]*x[48] + K[K_d3]*dr7_c0*x[52] + nt_div<T>(T(2)*K[K_d60]*tj[J_cl2o2]*(x[52]*x[52]), F.hnm*K[K_d61] + tj[J_cl2o2]) + T(2)*K[K_e5b]*x[52]*x[53] + T(2)*K[K_e6]*(x[53]*x[53]) + T(2)*K[K_hk1]*(x[45]*x[45]) + K[K_hk3]*dr7_c0*x[46] + dr7_c1*tj[J_clono2_cl]*x[13] + x[45]*(K[K_a5]*x[43] + K[K_a7]*x[47]) + x[46]*(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47])) - ck0[7] + x[7];
 }
 
 // scaled Jacobian J'_ij = dR_i/dx_j s_j / s_i, day equations, into the
@@ -668,24 +668,24 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     }
     {  // row 42
     const T rs42 = nt_rscale<T>(nt_exp_hi(x[42]), fh);
-        J[99] = (-tj[J_o3_o1d]/(F.n2*K[K_hk4] + F.o2*K[K_hk5])) * (cs46 * rs42);
+        J[99] = (nt_div<T>(-tj[J_o3_o1d], F.n2*K[K_hk4] + F.o2*K[K_hk5])) * (cs46 * rs42);
     }
     {  // row 56
     const T rs56 = nt_rscale<T>(nt_exp_hi(x[56]), fh);
         const T dj56_c0 = F.o2*K[K_c4] + K[K_c3]*xt45;
-        const T dj56_c1 = (T(1)/(dj56_c0));
+        const T dj56_c1 = nt_div<T>(T(1), dj56_c0);
         const T dj56_c2 = K[K_c1a]*xt42 + K[K_c2]*xt43 + K[K_d5]*xt44;
         const T dj56_c3 = dj56_c1*xt1;
         J[177] = (-dj56_c1*dj56_c2) * (cs1 * rs56);
         J[176] = (-K[K_c1a]*dj56_c3) * (cs42 * rs56);
         J[180] = (-K[K_c2]*dj56_c3) * (cs43 * rs56);
         J[179] = (-K[K_d5]*dj56_c3) * (cs44 * rs56);
-        J[178] = (K[K_c3]*dj56_c2*xt1/(dj56_c0*dj56_c0)) * (cs45 * rs56);
+        J[178] = (nt_div<T>(K[K_c3]*dj56_c2*xt1, (dj56_c0*dj56_c0))) * (cs45 * rs56);
     }
     const T D_ch3o_c0 = K[K_c1b]*xt42;
     const T D_ch3o_c1 = K[K_c14]*xt28;
     const T D_ch3o_c2 = K[K_c18]*xt52 + K[K_c5]*xt49;
-    const T D_ch3o_c3 = T(1)/(F.o2*K[K_c15]);
+    const T D_ch3o_c3 = nt_div<T>(T(1), F.o2*K[K_c15]);
     const T D_ch3o_c4 = D_ch3o_c3*xt28;
     const T D_ch3o = D_ch3o_c3*(D_ch3o_c0*xt1 + tj[J_ch3o2h]*xt29 + xt28*(T(2)*D_ch3o_c1 + D_ch3o_c2));
     const T d_D_ch3o_1 = D_ch3o_c0*D_ch3o_c3;
@@ -714,7 +714,7 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
         J[228] = (-d_D_ch3o_52*dj27_c1) * (cs52 * rs27);
         J[220] = (-dj27_c4*xt45) * (cs56 * rs27);
     }
-    const T D_hco_c0 = T(1)/(F.o2*K[K_c12]);
+    const T D_hco_c0 = nt_div<T>(T(1), F.o2*K[K_c12]);
     const T D_hco_c1 = D_hco_c0*(K[K_c10]*xt44 + K[K_c19]*xt50 + K[K_c8]*xt43 + K[K_c9]*xt45 + tj[J_ch2o_hco]);
     const T D_hco_c2 = D_hco_c0*xt27;
     const T D_hco = D_hco_c1*xt27;
@@ -733,7 +733,7 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
         J[162] = (-d_D_hco_45*dj8_c0) * (cs45 * rs8);
         J[164] = (-d_D_hco_50*dj8_c0) * (cs50 * rs8);
     }
-    const T D_r1_c0 = T(1)/(F.o2*K[K_hk2]);
+    const T D_r1_c0 = nt_div<T>(T(1), F.o2*K[K_hk2]);
     const T D_r1 = D_r1_c0*(K[K_a2]*xt55 + K[K_a6]*xt43 + K[K_a6b]*xt47 + K[K_b4]*xt49 + K[K_d2]*xt44 + tj[J_o3_o1d] + tj[J_o3_o3p]);
     const T d_D_r1_43 = D_r1_c0*K[K_a6];
     const T d_D_r1_44 = D_r1_c0*K[K_d2];
@@ -752,8 +752,8 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     {  // row 46
     const T rs46 = nt_rscale<T>(nt_exp_hi(x[46]), fh);
         const T dj46_c0 = D_r1 + T(1);
-        const T dj46_c1 = xt7/(dj46_c0*dj46_c0);
-        J[355] = (-T(1)/dj46_c0) * (cs7 * rs46);
+        const T dj46_c1 = nt_div<T>(xt7, (dj46_c0*dj46_c0));
+        J[355] = (nt_div<T>(T(-1), dj46_c0)) * (cs7 * rs46);
         J[358] = (d_D_r1_43*dj46_c1) * (cs43 * rs46);
         J[357] = (d_D_r1_44*dj46_c1) * (cs44 * rs46);
         J[359] = (d_D_r1_47*dj46_c1) * (cs47 * rs46);
@@ -762,8 +762,8 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     }
     const T D_r4_c0 = F.h2*K[K_a19] + K[K_a36]*xt8 + K[K_a5]*xt45;
     const T D_r4_c1 = F.o2*K[K_a1] + K[K_a2]*xt46 + T(8.049999999999999e-11)*xt47;
-    const T D_r4_c2 = (T(1)/(D_r4_c1));
-    const T D_r4_c3 = D_r4_c0/(D_r4_c1*D_r4_c1);
+    const T D_r4_c2 = nt_div<T>(T(1), D_r4_c1);
+    const T D_r4_c3 = nt_div<T>(D_r4_c0, (D_r4_c1*D_r4_c1));
     const T D_r4 = D_r4_c0*D_r4_c2;
     const T d_D_r4_8 = D_r4_c2*K[K_a36];
     const T d_D_r4_45 = D_r4_c2*K[K_a5];
@@ -778,17 +778,17 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
         J[208] = (-d_D_r4_47*xt43) * (cs47 * rs55);
     }
     const T D_r7_c0 = F.o2*K[K_b7] + K[K_b6]*xt49;
-    const T D_r7 = tj[J_no]/D_r7_c0;
-    const T d_D_r7_49 = -K[K_b6]*tj[J_no]/(D_r7_c0*D_r7_c0);
+    const T D_r7 = nt_div<T>(tj[J_no], D_r7_c0);
+    const T d_D_r7_49 = nt_div<T>(-K[K_b6]*tj[J_no], (D_r7_c0*D_r7_c0));
     {  // row 51
     const T rs51 = nt_rscale<T>(nt_exp_hi(x[51]), fh);
         J[78] = (-D_r7 - d_D_r7_49*xt49) * (cs49 * rs51);
     }
     const T D_r8_c0 = K[K_b12]*xt48 + tj[J_no3_no2] + tj[J_no3_no];
-    const T D_r8_c1 = K[K_b9]/D_r8_c0;
+    const T D_r8_c1 = nt_div<T>(K[K_b9], D_r8_c0);
     const T D_r8 = D_r8_c1*xt46;
     const T d_D_r8_46 = D_r8_c1;
-    const T d_D_r8_48 = -K[K_b12]*K[K_b9]*xt46/(D_r8_c0*D_r8_c0);
+    const T d_D_r8_48 = nt_div<T>(-K[K_b12]*K[K_b9]*xt46, (D_r8_c0*D_r8_c0));
     {  // row 54
     const T rs54 = nt_rscale<T>(nt_exp_hi(x[54]), fh);
         J[68] = T(0);
@@ -797,8 +797,8 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     }
     const T D_r5_c0 = D_r8*tj[J_no3_no] + K[K_b3]*xt45 + tj[J_no2];
     const T D_r5_c1 = K[K_a26]*xt47 + K[K_b4]*xt46 + K[K_c5]*xt28 + K[K_d4]*xt52 + K[K_e4]*xt53;
-    const T D_r5_c2 = (T(1)/(D_r5_c1));
-    const T D_r5_c3 = D_r5_c0/(D_r5_c1*D_r5_c1);
+    const T D_r5_c2 = nt_div<T>(T(1), D_r5_c1);
+    const T D_r5_c3 = nt_div<T>(D_r5_c0, (D_r5_c1*D_r5_c1));
     const T D_r5 = D_r5_c0*D_r5_c2;
     const T d_D_r5_28 = -D_r5_c3*K[K_c5];
     const T d_D_r5_45 = D_r5_c2*K[K_b3];
@@ -810,10 +810,10 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     {  // row 48
     const T rs48 = nt_rscale<T>(nt_exp_hi(x[48]), fh);
         const T dj48_c0 = D_r5*D_r7 + D_r5 + D_r8 + T(1);
-        const T dj48_c1 = (T(1)/(dj48_c0*dj48_c0));
+        const T dj48_c1 = nt_div<T>(T(1), dj48_c0*dj48_c0);
         const T dj48_c2 = dj48_c1*xt20;
         const T dj48_c3 = dj48_c2*(-D_r7 + T(-1));
-        J[270] = (-T(1)/dj48_c0) * (cs20 * rs48);
+        J[270] = (nt_div<T>(T(-1), dj48_c0)) * (cs20 * rs48);
         J[269] = (-d_D_r5_28*dj48_c3) * (cs28 * rs48);
         J[272] = (-d_D_r5_45*dj48_c3) * (cs45 * rs48);
         J[275] = (-d_D_r5_46*dj48_c3 + d_D_r8_46*dj48_c1*xt20) * (cs46 * rs48);
@@ -837,9 +837,9 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     const T D_r6_c1 = D_r4*D_r6_c0 + K[K_a30]*xt16 + K[K_a6]*xt46 + K[K_c8]*xt27 + K[K_d8]*xt52 + K[K_e10]*xt53;
     const T D_r6_c2 = T(2)*K[K_a27];
     const T D_r6_c3 = D_r6_c2*xt47 + K[K_a17]*xt43 + K[K_a26]*xt49 + K[K_a6b]*xt46 + K[K_a7]*xt45 + K[K_d10]*xt44 + K[K_d33]*xt52 + K[K_d7]*xt44 + K[K_e15]*xt53 + K[K_e7]*xt50 + T(8.049999999999999e-11)*xt55;
-    const T D_r6_c4 = (T(1)/(D_r6_c3));
+    const T D_r6_c4 = nt_div<T>(T(1), D_r6_c3);
     const T D_r6_c5 = D_r6_c0*D_r6_c4;
-    const T D_r6_c6 = D_r6_c1/(D_r6_c3*D_r6_c3);
+    const T D_r6_c6 = nt_div<T>(D_r6_c1, (D_r6_c3*D_r6_c3));
     const T D_r6 = D_r6_c1*D_r6_c4;
     const T d_D_r6_8 = D_r6_c5*d_D_r4_8;
     const T d_D_r6_16 = D_r6_c4*K[K_a30];
@@ -871,8 +871,8 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
         J[344] = (-d_D_r6_55*xt43) * (cs55 * rs47);
     }
     const T D_r13_c0 = K[K_d32]*xt45 + het[0]*xt2 + het[1]*xt12 + tj[J_clono2_cl] + tj[J_clono2_clo];
-    const T D_r13_c1 = K[K_d31]/D_r13_c0;
-    const T D_r13_c2 = K[K_d31]*xt48/(D_r13_c0*D_r13_c0);
+    const T D_r13_c1 = nt_div<T>(K[K_d31], D_r13_c0);
+    const T D_r13_c2 = nt_div<T>(K[K_d31]*xt48, (D_r13_c0*D_r13_c0));
     const T D_r13 = D_r13_c1*xt48;
     const T d_D_r13_2 = -D_r13_c2*het[0];
     const T d_D_r13_12 = -D_r13_c2*het[1];
@@ -881,26 +881,26 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     const T D_r9_c0 = D_r13*het[0];
     const T D_r9_c1 = D_r9_c0*xt2 + K[K_d33]*xt47;
     const T D_r9_c2 = K[K_d35]*xt45 + het[4]*xt12 + tj[J_hocl];
-    const T D_r9_c3 = (T(1)/(D_r9_c2));
+    const T D_r9_c3 = nt_div<T>(T(1), D_r9_c2);
     const T D_r9_c4 = D_r9_c3*het[0]*xt2;
-    const T D_r9_c5 = D_r9_c1/(D_r9_c2*D_r9_c2);
+    const T D_r9_c5 = nt_div<T>(D_r9_c1, (D_r9_c2*D_r9_c2));
     const T D_r9 = D_r9_c1*D_r9_c3;
     const T d_D_r9_2 = D_r9_c0*D_r9_c3 + D_r9_c4*d_D_r13_2;
     const T d_D_r9_12 = D_r9_c4*d_D_r13_12 - D_r9_c5*het[4];
     const T d_D_r9_45 = D_r9_c3*d_D_r13_45*het[0]*xt2 - D_r9_c5*K[K_d35];
     const T d_D_r9_47 = D_r9_c3*K[K_d33];
     const T d_D_r9_48 = D_r9_c4*d_D_r13_48;
-    const T D_r10_c0 = K[K_d60]/(F.hnm*K[K_d61] + tj[J_cl2o2]);
+    const T D_r10_c0 = nt_div<T>(K[K_d60], F.hnm*K[K_d61] + tj[J_cl2o2]);
     const T D_r10 = D_r10_c0*xt52;
     const T d_D_r10_52 = D_r10_c0;
-    const T D_r12_c0 = K[K_e5c]/tj[J_brcl];
+    const T D_r12_c0 = nt_div<T>(K[K_e5c], tj[J_brcl]);
     const T D_r12 = D_r12_c0*xt53;
     const T d_D_r12_53 = D_r12_c0;
     const T D_r11_c0 = K[K_d10]*xt47 + K[K_d2]*xt46 + K[K_d37]*xt14 + K[K_d5]*xt1 + K[K_d7]*xt47;
-    const T D_r11_c1 = (T(1)/(D_r11_c0));
+    const T D_r11_c1 = nt_div<T>(T(1), D_r11_c0);
     const T D_r11_c2 = T(2)*tj[J_cl2o2];
     const T D_r11_c3 = D_r10*D_r11_c2 + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*xt28 + K[K_d3]*xt45 + K[K_d4]*xt49 + K[K_d8]*xt43 + K[K_e5b]*xt53;
-    const T D_r11_c4 = D_r11_c3/(D_r11_c0*D_r11_c0);
+    const T D_r11_c4 = nt_div<T>(D_r11_c3, (D_r11_c0*D_r11_c0));
     const T D_r11_c5 = D_r11_c1*tj[J_clono2_cl];
     const T D_r11_c6 = D_r11_c1*tj[J_hocl];
     const T D_r11 = D_r11_c1*D_r11_c3;
@@ -936,12 +936,12 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     {  // row 52
     const T rs52 = nt_rscale<T>(nt_exp_hi(x[52]), fh);
         const T dj52_c0 = D_r11 + T(1);
-        const T dj52_c1 = xt22/(dj52_c0*dj52_c0);
+        const T dj52_c1 = nt_div<T>(xt22, (dj52_c0*dj52_c0));
         J[369] = (d_D_r11_1*dj52_c1) * (cs1 * rs52);
         J[373] = (d_D_r11_2*dj52_c1) * (cs2 * rs52);
         J[372] = (d_D_r11_12*dj52_c1) * (cs12 * rs52);
         J[370] = (d_D_r11_14*dj52_c1) * (cs14 * rs52);
-        J[368] = (-T(1)/dj52_c0) * (cs22 * rs52);
+        J[368] = (nt_div<T>(T(-1), dj52_c0)) * (cs22 * rs52);
         J[371] = (d_D_r11_28*dj52_c1) * (cs28 * rs52);
         J[377] = (d_D_r11_43*dj52_c1) * (cs43 * rs52);
         J[375] = (d_D_r11_45*dj52_c1) * (cs45 * rs52);
@@ -953,24 +953,24 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
         J[376] = (d_D_r11_53*dj52_c1) * (cs53 * rs52);
     }
     const T D_r27_c0 = K[K_e8]*xt45 + tj[J_brono2];
-    const T D_r27_c1 = K[K_e13]/D_r27_c0;
+    const T D_r27_c1 = nt_div<T>(K[K_e13], D_r27_c0);
     const T D_r27 = D_r27_c1*xt48;
-    const T d_D_r27_45 = -K[K_e13]*K[K_e8]*xt48/(D_r27_c0*D_r27_c0);
+    const T d_D_r27_45 = nt_div<T>(-K[K_e13]*K[K_e8]*xt48, (D_r27_c0*D_r27_c0));
     const T d_D_r27_48 = D_r27_c1;
     const T D_r28_c0 = K[K_e16]*xt45 + tj[J_hobr];
-    const T D_r28_c1 = K[K_e15]/D_r28_c0;
+    const T D_r28_c1 = nt_div<T>(K[K_e15], D_r28_c0);
     const T D_r28 = D_r28_c1*xt47;
-    const T d_D_r28_45 = -K[K_e15]*K[K_e16]*xt47/(D_r28_c0*D_r28_c0);
+    const T d_D_r28_45 = nt_div<T>(-K[K_e15]*K[K_e16]*xt47, (D_r28_c0*D_r28_c0));
     const T d_D_r28_47 = D_r28_c1;
-    const T D_r29_c0 = K[K_e5c]/tj[J_brcl];
+    const T D_r29_c0 = nt_div<T>(K[K_e5c], tj[J_brcl]);
     const T D_r29 = D_r29_c0*xt52;
     const T d_D_r29_52 = D_r29_c0;
     const T D_r30_c0 = K[K_c19]*xt27 + K[K_e2]*xt46 + K[K_e7]*xt47;
-    const T D_r30_c1 = (T(1)/(D_r30_c0));
+    const T D_r30_c1 = nt_div<T>(T(1), D_r30_c0);
     const T D_r30_c2 = T(0.85)*tj[J_brono2];
     const T D_r30_c3 = T(2)*K[K_e6];
     const T D_r30_c4 = D_r27*D_r30_c2 + D_r28*tj[J_hobr] + D_r29*tj[J_brcl] + D_r30_c3*xt53 + K[K_e10]*xt43 + K[K_e3]*xt45 + K[K_e4]*xt49 + K[K_e5a]*xt52 + K[K_e5b]*xt52 + tj[J_bro];
-    const T D_r30_c5 = D_r30_c4/(D_r30_c0*D_r30_c0);
+    const T D_r30_c5 = nt_div<T>(D_r30_c4, (D_r30_c0*D_r30_c0));
     const T D_r30_c6 = D_r30_c1*D_r30_c2;
     const T D_r30 = D_r30_c1*D_r30_c4;
     const T d_D_r30_27 = -D_r30_c5*K[K_c19];
@@ -997,8 +997,8 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     {  // row 53
     const T rs53 = nt_rscale<T>(nt_exp_hi(x[53]), fh);
         const T dj53_c0 = D_r30 + T(1);
-        const T dj53_c1 = xt23/(dj53_c0*dj53_c0);
-        J[297] = (-T(1)/dj53_c0) * (cs23 * rs53);
+        const T dj53_c1 = nt_div<T>(xt23, (dj53_c0*dj53_c0));
+        J[297] = (nt_div<T>(T(-1), dj53_c0)) * (cs23 * rs53);
         J[298] = (d_D_r30_27*dj53_c1) * (cs27 * rs53);
         J[302] = (d_D_r30_43*dj53_c1) * (cs43 * rs53);
         J[300] = (d_D_r30_45*dj53_c1) * (cs45 * rs53);
@@ -1128,11 +1128,11 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     const T d_D_argum_56 = sel_D_argum ? T(D_argum_c0*d_D_coec_56) : T(T(0));
     {  // row 43
     const T rs43 = nt_rscale<T>(nt_exp_hi(x[43]), fh);
-        const T dj43_c0 = (T(1)/(D_coea));
-        const T dj43_c1 = (T(0.5))*dj43_c0;
+        const T dj43_c0 = nt_div<T>(T(1), D_coea);
+        const T dj43_c1 = nt_div<T>(dj43_c0, T(2));
         const T dj43_c2 = sqrt(D_argum);
-        const T dj43_c3 = (T(0.25))*dj43_c0/dj43_c2;
-        const T dj43_c4 = (T(0.5))*(-D_coeb + dj43_c2)/(D_coea*D_coea);
+        const T dj43_c3 = nt_div<T>(dj43_c0, T(4)*dj43_c2);
+        const T dj43_c4 = nt_div<T>(-D_coeb + dj43_c2, T(2)*(D_coea*D_coea));
         J[321] = (-d_D_argum_1*dj43_c3 + d_D_coeb_1*dj43_c1) * (cs1 * rs43);
         J[331] = (-d_D_argum_2*dj43_c3) * (cs2 * rs43);
         J[319] = (-d_D_argum_4*dj43_c3 + d_D_coeb_4*dj43_c1) * (cs4 * rs43);
@@ -1187,7 +1187,7 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
     {  // row 7
     const T rs7 = nt_rscale<T>(nt_exp_hi(x[7]), fh);
         const T dj7_c0 = T(2)*F.dt;
-        const T dj7_c1 = tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
+        const T dj7_c1 = nt_div<T>(tj[J_no3_no], fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]));
         const T dj7_c2 = F.dt*xt49;
         const T dj7_c3 = T(2)*K[K_b3];
         const T dj7_c4 = T(2)*K[K_d3];
@@ -1205,7 +1205,7 @@ __device__ __forceinline__ void nt_jacobian_day(const FF& F, PK K, PK tj, PK het
         J[113] = (F.dt*d_D_t06_47 + F.dt*d_D_t09_47 + F.dt*(K[K_a6b]*xt46 + K[K_a7]*xt45) - K[K_a26]*dj7_c2) * (cs47 * rs7);
         J[109] = (F.dt*(dj7_c3*xt45 + dj7_c6*xt46)) * (cs48 * rs7);
         J[115] = (-F.dt*(K[K_a26]*xt47 + K[K_c5]*xt28)) * (cs49 * rs7);
-        J[116] = (F.dt*d_D_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*xt52/(F.hnm*K[K_d61] + tj[J_cl2o2]) + dj7_c4*xt45 + dj7_c7*xt53) + d_D_t07_52*dj7_c0) * (cs52 * rs7);
+        J[116] = (F.dt*d_D_t06_52 + F.dt*(nt_div<T>(T(4)*K[K_d60]*tj[J_cl2o2]*xt52, F.hnm*K[K_d61] + tj[J_cl2o2]) + dj7_c4*xt45 + dj7_c7*xt53) + d_D_t07_52*dj7_c0) * (cs52 * rs7);
         J[111] = (F.dt*d_D_t09_53 + F.dt*(T(4)*K[K_e6]*xt53 + dj7_c7*xt52) + d_D_t07_53*dj7_c0) * (cs53 * rs7);
         J[107] = (F.dt*K[K_a2]*xt46) * (cs55 * rs7);
     }
@@ -1233,39 +1233,39 @@ __device__ __forceinline__ void nt_residual_day_w2_0(const FF& F, PK K, PK tj, P
     R[35] = -ck0[35] + x[35]*(F.dt*(K[K_d95]*x[43] + tj[J_ch3cl]) + T(1));
     R[36] = -ck0[36] + x[36]*(F.dt*(K[K_d96]*x[42] + K[K_d97]*x[43] + tj[J_hcfc22]) + T(1));
     R[39] = -ck0[39] + x[39]*(F.dt*(K[K_e53]*x[42] + tj[J_h1301]) + T(1));
-    R[42] = -tj[J_o3_o1d]*x[46]/(F.n2*K[K_hk4] + F.o2*K[K_hk5]) + x[42];
-    const T D_ch3o = (K[K_c1b]*x[1]*x[42] + tj[J_ch3o2h]*x[29] + x[28]*(T(2)*K[K_c14]*x[28] + K[K_c18]*x[52] + K[K_c5]*x[49]))/(F.o2*K[K_c15]);
+    R[42] = nt_div<T>(-tj[J_o3_o1d]*x[46], F.n2*K[K_hk4] + F.o2*K[K_hk5]) + x[42];
+    const T D_ch3o = nt_div<T>(K[K_c1b]*x[1]*x[42] + tj[J_ch3o2h]*x[29] + x[28]*(T(2)*K[K_c14]*x[28] + K[K_c18]*x[52] + K[K_c5]*x[49]), F.o2*K[K_c15]);
     R[27] = -F.dt*(D_ch3o*F.o2*K[K_c15] + K[K_c17b]*x[29]*x[43] + K[K_c1c]*x[1]*x[42] + K[K_c3]*x[45]*x[56]) - ck0[27] + x[27]*(F.dt*(K[K_c10]*x[44] + K[K_c19]*x[50] + K[K_c8]*x[43] + K[K_c9]*x[45] + tj[J_ch2o_co] + tj[J_ch2o_hco]) + T(1));
-    const T D_hco = x[27]*(K[K_c10]*x[44] + K[K_c19]*x[50] + K[K_c8]*x[43] + K[K_c9]*x[45] + tj[J_ch2o_hco])/(F.o2*K[K_c12]);
+    const T D_hco = nt_div<T>(x[27]*(K[K_c10]*x[44] + K[K_c19]*x[50] + K[K_c8]*x[43] + K[K_c9]*x[45] + tj[J_ch2o_hco]), F.o2*K[K_c12]);
     R[8] = -F.dt*(D_hco*F.o2*K[K_c12] + F.co2*tj[J_co2] + tj[J_ch2o_co]*x[27]) - ck0[8] + x[8]*(F.dt*K[K_a36]*x[43] + T(1));
-    const T D_r1 = (K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47] + K[K_b4]*x[49] + K[K_d2]*x[44] + tj[J_o3_o1d] + tj[J_o3_o3p])/(F.o2*K[K_hk2]);
+    const T D_r1 = nt_div<T>(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47] + K[K_b4]*x[49] + K[K_d2]*x[44] + tj[J_o3_o1d] + tj[J_o3_o3p], F.o2*K[K_hk2]);
     R[45] = -D_r1*x[46] + x[45];
-    const T D_r4 = (F.h2*K[K_a19] + K[K_a36]*x[8] + K[K_a5]*x[45])/(F.o2*K[K_a1] + K[K_a2]*x[46] + T(8.049999999999999e-11)*x[47]);
+    const T D_r4 = nt_div<T>(F.h2*K[K_a19] + K[K_a36]*x[8] + K[K_a5]*x[45], F.o2*K[K_a1] + K[K_a2]*x[46] + T(8.049999999999999e-11)*x[47]);
     R[55] = -D_r4*x[43] + x[55];
-    const T D_r7 = tj[J_no]/(F.o2*K[K_b7] + K[K_b6]*x[49]);
+    const T D_r7 = nt_div<T>(tj[J_no], F.o2*K[K_b7] + K[K_b6]*x[49]);
     R[51] = -D_r7*x[49] + x[51];
-    const T D_r8 = K[K_b9]*x[46]/(K[K_b12]*x[48] + tj[J_no3_no2] + tj[J_no3_no]);
+    const T D_r8 = nt_div<T>(K[K_b9]*x[46], K[K_b12]*x[48] + tj[J_no3_no2] + tj[J_no3_no]);
     R[54] = -D_r8*x[48] + x[54];
-    const T D_r6 = (D_r4*F.o2*K[K_a1] + K[K_a30]*x[16] + K[K_a6]*x[46] + K[K_c8]*x[27] + K[K_d8]*x[52] + K[K_e10]*x[53])/(K[K_a17]*x[43] + K[K_a26]*x[49] + T(2)*K[K_a27]*x[47] + K[K_a6b]*x[46] + K[K_a7]*x[45] + K[K_d10]*x[44] + K[K_d33]*x[52] + K[K_d7]*x[44] + K[K_e15]*x[53] + K[K_e7]*x[50] + T(8.049999999999999e-11)*x[55]);
-    const T D_r13 = K[K_d31]*x[48]/(K[K_d32]*x[45] + het[0]*x[2] + het[1]*x[12] + tj[J_clono2_cl] + tj[J_clono2_clo]);
-    const T D_r9 = (D_r13*het[0]*x[2] + K[K_d33]*x[47])/(K[K_d35]*x[45] + het[4]*x[12] + tj[J_hocl]);
-    const T D_r10 = K[K_d60]*x[52]/(F.hnm*K[K_d61] + tj[J_cl2o2]);
-    const T D_r12 = K[K_e5c]*x[53]/tj[J_brcl];
-    const T D_r11 = (T(2)*D_r10*tj[J_cl2o2] + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*x[28] + K[K_d3]*x[45] + K[K_d4]*x[49] + K[K_d8]*x[43] + K[K_e5b]*x[53])/(K[K_d10]*x[47] + K[K_d2]*x[46] + K[K_d37]*x[14] + K[K_d5]*x[1] + K[K_d7]*x[47]);
-    R[52] = -x[22]/(D_r11 + T(1)) + x[52];
-    const T D_r27 = K[K_e13]*x[48]/(K[K_e8]*x[45] + tj[J_brono2]);
-    const T D_r28 = K[K_e15]*x[47]/(K[K_e16]*x[45] + tj[J_hobr]);
-    const T D_r29 = K[K_e5c]*x[52]/tj[J_brcl];
-    const T D_r30 = (T(0.85)*D_r27*tj[J_brono2] + D_r28*tj[J_hobr] + D_r29*tj[J_brcl] + K[K_e10]*x[43] + K[K_e3]*x[45] + K[K_e4]*x[49] + K[K_e5a]*x[52] + K[K_e5b]*x[52] + T(2)*K[K_e6]*x[53] + tj[J_bro])/(K[K_c19]*x[27] + K[K_e2]*x[46] + K[K_e7]*x[47]);
+    const T D_r6 = nt_div<T>(D_r4*F.o2*K[K_a1] + K[K_a30]*x[16] + K[K_a6]*x[46] + K[K_c8]*x[27] + K[K_d8]*x[52] + K[K_e10]*x[53], K[K_a17]*x[43] + K[K_a26]*x[49] + T(2)*K[K_a27]*x[47] + K[K_a6b]*x[46] + K[K_a7]*x[45] + K[K_d10]*x[44] + K[K_d33]*x[52] + K[K_d7]*x[44] + K[K_e15]*x[53] + K[K_e7]*x[50] + T(8.049999999999999e-11)*x[55]);
+    const T D_r13 = nt_div<T>(K[K_d31]*x[48], K[K_d32]*x[45] + het[0]*x[2] + het[1]*x[12] + tj[J_clono2_cl] + tj[J_clono2_clo]);
+    const T D_r9 = nt_div<T>(D_r13*het[0]*x[2] + K[K_d33]*x[47], K[K_d35]*x[45] + het[4]*x[12] + tj[J_hocl]);
+    const T D_r10 = nt_div<T>(K[K_d60]*x[52], F.hnm*K[K_d61] + tj[J_cl2o2]);
+    const T D_r12 = nt_div<T>(K[K_e5c]*x[53], tj[J_brcl]);
+    const T D_r11 = nt_div<T>(T(2)*D_r10*tj[J_cl2o2] + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*x[28] + K[K_d3]*x[45] + K[K_d4]*x[49] + K[K_d8]*x[43] + K[K_e5b]*x[53], K[K_d10]*x[47] + K[K_d2]*x[46] + K[K_d37]*x[14] + K[K_d5]*x[1] + K[K_d7]*x[47]);
+    R[52] = nt_div<T>(-x[22], D_r11 + T(1)) + x[52];
+    const T D_r27 = nt_div<T>(K[K_e13]*x[48], K[K_e8]*x[45] + tj[J_brono2]);
+    const T D_r28 = nt_div<T>(K[K_e15]*x[47], K[K_e16]*x[45] + tj[J_hobr]);
+    const T D_r29 = nt_div<T>(K[K_e5c]*x[52], tj[J_brcl]);
+    const T D_r30 = nt_div<T>(T(0.85)*D_r27*tj[J_brono2] + D_r28*tj[J_hobr] + D_r29*tj[J_brcl] + K[K_e10]*x[43] + K[K_e3]*x[45] + K[K_e4]*x[49] + K[K_e5a]*x[52] + K[K_e5b]*x[52] + T(2)*K[K_e6]*x[53] + tj[J_bro], K[K_c19]*x[27] + K[K_e2]*x[46] + K[K_e7]*x[47]);
     R[50] = -D_r30*x[53] + x[50];
-    R[53] = -x[23]/(D_r30 + T(1)) + x[53];
+    R[53] = nt_div<T>(-x[23], D_r30 + T(1)) + x[53];
     const T D_coea = D_r6*(T(1.7e-11)*D_r4 + T(2)*D_r6*K[K_a27] + T(2)*K[K_a17]) + T(2)*K[K_a31];
     const T D_coeb = D_r6*K[K_b23]*x[48] + D_r6*K[K_c7]*x[28] + D_r6*K[K_d33]*x[52] + D_r6*K[K_d7]*x[44] + D_r6*K[K_e15]*x[53] + D_r6*K[K_e7]*x[50] + F.parthbr*K[K_e11]*x[18] + F.parthcl*K[K_d11]*x[12] + F.parthno3*K[K_b27]*x[4] + K[K_b22]*x[48] + K[K_b28]*x[21] + K[K_c17a]*x[29] + K[K_c2]*x[1] + K[K_c8]*x[27] + K[K_d34]*x[14] + K[K_d9]*x[52];
     const T D_coec = D_ch3o*F.o2*K[K_c15] + D_hco*F.o2*K[K_c12] + F.h2*K[K_d6]*x[44] + F.parth2o*x[2]*(T(2)*K[K_a1et]*x[42] + T(2)*tj[J_h2o]) + F.parthno3*tj[J_hno3]*x[4] + K[K_c3]*x[45]*x[56] + K[K_e16]*x[25]*x[45] + tj[J_ch3o2h]*x[29] + T(2)*tj[J_h2o2]*x[16] + tj[J_hbr]*x[18] + tj[J_hobr]*x[25] + x[14]*(K[K_d35]*x[45] + K[K_d37]*x[44] + tj[J_hocl]) + x[21]*(F.hnm*K[K_b24] + tj[J_hno4]) + x[27]*(K[K_c9]*x[45] + tj[J_ch2o_hco]) + x[42]*(T(2.4e-10)*F.h2 + x[1]*(K[K_c1a] + K[K_c1b]));
     const T D_argum_c0 = T(4)*D_coea*D_coec + (D_coeb*D_coeb);
     const bool sel_D_argum = (D_argum_c0) >= (T(0));
     const T D_argum = sel_D_argum ? T(D_argum_c0) : T(T(0));
-    R[43] = x[43] - T(0.5)*(sqrt(D_argum) - D_coeb)/D_coea;
+    R[43] = x[43] + nt_div<T>(-(sqrt(D_argum) - D_coeb), T(2)*D_coea);
 }
 
 // scaled Jacobian rows [2, 4, 5, 8, 9, 12, 14, 15, 16, 17, 18, 22, 25, 26, 27, 29, 30, 32, 34, 37, 38, 41, 43, 49, 55] (day equations) into their stored A slots
@@ -1600,7 +1600,7 @@ __device__ __forceinline__ void nt_jacobian_day_w2_0(const FF& F, PK K, PK tj, P
     const T D_ch3o_c0 = K[K_c1b]*xt42;
     const T D_ch3o_c1 = K[K_c14]*xt28;
     const T D_ch3o_c2 = K[K_c18]*xt52 + K[K_c5]*xt49;
-    const T D_ch3o_c3 = T(1)/(F.o2*K[K_c15]);
+    const T D_ch3o_c3 = nt_div<T>(T(1), F.o2*K[K_c15]);
     const T D_ch3o_c4 = D_ch3o_c3*xt28;
     const T D_ch3o = D_ch3o_c3*(D_ch3o_c0*xt1 + tj[J_ch3o2h]*xt29 + xt28*(T(2)*D_ch3o_c1 + D_ch3o_c2));
     const T d_D_ch3o_1 = D_ch3o_c0*D_ch3o_c3;
@@ -1629,7 +1629,7 @@ __device__ __forceinline__ void nt_jacobian_day_w2_0(const FF& F, PK K, PK tj, P
         J[228] = (-d_D_ch3o_52*dj27_c1) * (cs52 * rs27);
         J[220] = (-dj27_c4*xt45) * (cs56 * rs27);
     }
-    const T D_hco_c0 = T(1)/(F.o2*K[K_c12]);
+    const T D_hco_c0 = nt_div<T>(T(1), F.o2*K[K_c12]);
     const T D_hco_c1 = D_hco_c0*(K[K_c10]*xt44 + K[K_c19]*xt50 + K[K_c8]*xt43 + K[K_c9]*xt45 + tj[J_ch2o_hco]);
     const T D_hco_c2 = D_hco_c0*xt27;
     const T D_hco = D_hco_c1*xt27;
@@ -1650,8 +1650,8 @@ __device__ __forceinline__ void nt_jacobian_day_w2_0(const FF& F, PK K, PK tj, P
     }
     const T D_r4_c0 = F.h2*K[K_a19] + K[K_a36]*xt8 + K[K_a5]*xt45;
     const T D_r4_c1 = F.o2*K[K_a1] + K[K_a2]*xt46 + T(8.049999999999999e-11)*xt47;
-    const T D_r4_c2 = (T(1)/(D_r4_c1));
-    const T D_r4_c3 = D_r4_c0/(D_r4_c1*D_r4_c1);
+    const T D_r4_c2 = nt_div<T>(T(1), D_r4_c1);
+    const T D_r4_c3 = nt_div<T>(D_r4_c0, (D_r4_c1*D_r4_c1));
     const T D_r4 = D_r4_c0*D_r4_c2;
     const T d_D_r4_8 = D_r4_c2*K[K_a36];
     const T d_D_r4_45 = D_r4_c2*K[K_a5];
@@ -1666,14 +1666,14 @@ __device__ __forceinline__ void nt_jacobian_day_w2_0(const FF& F, PK K, PK tj, P
         J[208] = (-d_D_r4_47*xt43) * (cs47 * rs55);
     }
     const T D_r8_c0 = K[K_b12]*xt48 + tj[J_no3_no2] + tj[J_no3_no];
-    const T D_r8_c1 = K[K_b9]/D_r8_c0;
+    const T D_r8_c1 = nt_div<T>(K[K_b9], D_r8_c0);
     const T D_r8 = D_r8_c1*xt46;
     const T d_D_r8_46 = D_r8_c1;
-    const T d_D_r8_48 = -K[K_b12]*K[K_b9]*xt46/(D_r8_c0*D_r8_c0);
+    const T d_D_r8_48 = nt_div<T>(-K[K_b12]*K[K_b9]*xt46, (D_r8_c0*D_r8_c0));
     const T D_r5_c0 = D_r8*tj[J_no3_no] + K[K_b3]*xt45 + tj[J_no2];
     const T D_r5_c1 = K[K_a26]*xt47 + K[K_b4]*xt46 + K[K_c5]*xt28 + K[K_d4]*xt52 + K[K_e4]*xt53;
-    const T D_r5_c2 = (T(1)/(D_r5_c1));
-    const T D_r5_c3 = D_r5_c0/(D_r5_c1*D_r5_c1);
+    const T D_r5_c2 = nt_div<T>(T(1), D_r5_c1);
+    const T D_r5_c3 = nt_div<T>(D_r5_c0, (D_r5_c1*D_r5_c1));
     const T D_r5 = D_r5_c0*D_r5_c2;
     const T d_D_r5_28 = -D_r5_c3*K[K_c5];
     const T d_D_r5_45 = D_r5_c2*K[K_b3];
@@ -1696,9 +1696,9 @@ __device__ __forceinline__ void nt_jacobian_day_w2_0(const FF& F, PK K, PK tj, P
     const T D_r6_c1 = D_r4*D_r6_c0 + K[K_a30]*xt16 + K[K_a6]*xt46 + K[K_c8]*xt27 + K[K_d8]*xt52 + K[K_e10]*xt53;
     const T D_r6_c2 = T(2)*K[K_a27];
     const T D_r6_c3 = D_r6_c2*xt47 + K[K_a17]*xt43 + K[K_a26]*xt49 + K[K_a6b]*xt46 + K[K_a7]*xt45 + K[K_d10]*xt44 + K[K_d33]*xt52 + K[K_d7]*xt44 + K[K_e15]*xt53 + K[K_e7]*xt50 + T(8.049999999999999e-11)*xt55;
-    const T D_r6_c4 = (T(1)/(D_r6_c3));
+    const T D_r6_c4 = nt_div<T>(T(1), D_r6_c3);
     const T D_r6_c5 = D_r6_c0*D_r6_c4;
-    const T D_r6_c6 = D_r6_c1/(D_r6_c3*D_r6_c3);
+    const T D_r6_c6 = nt_div<T>(D_r6_c1, (D_r6_c3*D_r6_c3));
     const T D_r6 = D_r6_c1*D_r6_c4;
     const T d_D_r6_8 = D_r6_c5*d_D_r4_8;
     const T d_D_r6_16 = D_r6_c4*K[K_a30];
@@ -1832,11 +1832,11 @@ __device__ __forceinline__ void nt_jacobian_day_w2_0(const FF& F, PK K, PK tj, P
     const T d_D_argum_56 = sel_D_argum ? T(D_argum_c0*d_D_coec_56) : T(T(0));
     {  // row 43
     const T rs43 = nt_rscale<T>(nt_exp_hi(x[43]), fh);
-        const T dj43_c0 = (T(1)/(D_coea));
-        const T dj43_c1 = (T(0.5))*dj43_c0;
+        const T dj43_c0 = nt_div<T>(T(1), D_coea);
+        const T dj43_c1 = nt_div<T>(dj43_c0, T(2));
         const T dj43_c2 = sqrt(D_argum);
-        const T dj43_c3 = (T(0.25))*dj43_c0/dj43_c2;
-        const T dj43_c4 = (T(0.5))*(-D_coeb + dj43_c2)/(D_coea*D_coea);
+        const T dj43_c3 = nt_div<T>(dj43_c0, T(4)*dj43_c2);
+        const T dj43_c4 = nt_div<T>(-D_coeb + dj43_c2, T(2)*(D_coea*D_coea));
         J[321] = (-d_D_argum_1*dj43_c3 + d_D_coeb_1*dj43_c1) * (cs1 * rs43);
         J[331] = (-d_D_argum_2*dj43_c3) * (cs2 * rs43);
         J[319] = (-d_D_argum_4*dj43_c3 + d_D_coeb_4*dj43_c1) * (cs4 * rs43);
@@ -1894,22 +1894,22 @@ __device__ __forceinline__ void nt_residual_day_w2_1(const FF& F, PK K, PK tj, P
     R[38] = -ck0[38] + x[38]*(F.dt*(K[K_e52]*x[42] + tj[J_h1211]) + T(1));
     R[40] = F.dt*F.rain_hbr*x[18] - F.dt*(x[37]*(K[K_e50]*x[42] + K[K_e51]*x[43] + tj[J_ch3br]) + x[38]*(K[K_e52]*x[42] + tj[J_h1211]) + x[39]*(K[K_e53]*x[42] + tj[J_h1301]) + x[41]*(T(2)*K[K_e54]*x[43] + T(2)*tj[J_ch2br2])) - ck0[40] + x[40];
     R[41] = -ck0[41] + x[41]*(F.dt*(K[K_e54]*x[43] + tj[J_ch2br2]) + T(1));
-    R[56] = -x[1]*(K[K_c1a]*x[42] + K[K_c2]*x[43] + K[K_d5]*x[44])/(F.o2*K[K_c4] + K[K_c3]*x[45]) + x[56];
-    const T D_r1 = (K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47] + K[K_b4]*x[49] + K[K_d2]*x[44] + tj[J_o3_o1d] + tj[J_o3_o3p])/(F.o2*K[K_hk2]);
-    R[46] = x[46] - x[7]/(D_r1 + T(1));
-    const T D_r4 = (F.h2*K[K_a19] + K[K_a36]*x[8] + K[K_a5]*x[45])/(F.o2*K[K_a1] + K[K_a2]*x[46] + T(8.049999999999999e-11)*x[47]);
-    const T D_r7 = tj[J_no]/(F.o2*K[K_b7] + K[K_b6]*x[49]);
-    const T D_r8 = K[K_b9]*x[46]/(K[K_b12]*x[48] + tj[J_no3_no2] + tj[J_no3_no]);
-    const T D_r5 = (D_r8*tj[J_no3_no] + K[K_b3]*x[45] + tj[J_no2])/(K[K_a26]*x[47] + K[K_b4]*x[46] + K[K_c5]*x[28] + K[K_d4]*x[52] + K[K_e4]*x[53]);
-    R[48] = -x[20]/(D_r5*D_r7 + D_r5 + D_r8 + T(1)) + x[48];
+    R[56] = nt_div<T>(-x[1]*(K[K_c1a]*x[42] + K[K_c2]*x[43] + K[K_d5]*x[44]), F.o2*K[K_c4] + K[K_c3]*x[45]) + x[56];
+    const T D_r1 = nt_div<T>(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47] + K[K_b4]*x[49] + K[K_d2]*x[44] + tj[J_o3_o1d] + tj[J_o3_o3p], F.o2*K[K_hk2]);
+    R[46] = x[46] + nt_div<T>(-x[7], D_r1 + T(1));
+    const T D_r4 = nt_div<T>(F.h2*K[K_a19] + K[K_a36]*x[8] + K[K_a5]*x[45], F.o2*K[K_a1] + K[K_a2]*x[46] + T(8.049999999999999e-11)*x[47]);
+    const T D_r7 = nt_div<T>(tj[J_no], F.o2*K[K_b7] + K[K_b6]*x[49]);
+    const T D_r8 = nt_div<T>(K[K_b9]*x[46], K[K_b12]*x[48] + tj[J_no3_no2] + tj[J_no3_no]);
+    const T D_r5 = nt_div<T>(D_r8*tj[J_no3_no] + K[K_b3]*x[45] + tj[J_no2], K[K_a26]*x[47] + K[K_b4]*x[46] + K[K_c5]*x[28] + K[K_d4]*x[52] + K[K_e4]*x[53]);
+    R[48] = nt_div<T>(-x[20], D_r5*D_r7 + D_r5 + D_r8 + T(1)) + x[48];
     R[49] = -D_r5*x[48] + x[49];
-    const T D_r6 = (D_r4*F.o2*K[K_a1] + K[K_a30]*x[16] + K[K_a6]*x[46] + K[K_c8]*x[27] + K[K_d8]*x[52] + K[K_e10]*x[53])/(K[K_a17]*x[43] + K[K_a26]*x[49] + T(2)*K[K_a27]*x[47] + K[K_a6b]*x[46] + K[K_a7]*x[45] + K[K_d10]*x[44] + K[K_d33]*x[52] + K[K_d7]*x[44] + K[K_e15]*x[53] + K[K_e7]*x[50] + T(8.049999999999999e-11)*x[55]);
+    const T D_r6 = nt_div<T>(D_r4*F.o2*K[K_a1] + K[K_a30]*x[16] + K[K_a6]*x[46] + K[K_c8]*x[27] + K[K_d8]*x[52] + K[K_e10]*x[53], K[K_a17]*x[43] + K[K_a26]*x[49] + T(2)*K[K_a27]*x[47] + K[K_a6b]*x[46] + K[K_a7]*x[45] + K[K_d10]*x[44] + K[K_d33]*x[52] + K[K_d7]*x[44] + K[K_e15]*x[53] + K[K_e7]*x[50] + T(8.049999999999999e-11)*x[55]);
     R[47] = -D_r6*x[43] + x[47];
-    const T D_r13 = K[K_d31]*x[48]/(K[K_d32]*x[45] + het[0]*x[2] + het[1]*x[12] + tj[J_clono2_cl] + tj[J_clono2_clo]);
-    const T D_r9 = (D_r13*het[0]*x[2] + K[K_d33]*x[47])/(K[K_d35]*x[45] + het[4]*x[12] + tj[J_hocl]);
-    const T D_r10 = K[K_d60]*x[52]/(F.hnm*K[K_d61] + tj[J_cl2o2]);
-    const T D_r12 = K[K_e5c]*x[53]/tj[J_brcl];
-    const T D_r11 = (T(2)*D_r10*tj[J_cl2o2] + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*x[28] + K[K_d3]*x[45] + K[K_d4]*x[49] + K[K_d8]*x[43] + K[K_e5b]*x[53])/(K[K_d10]*x[47] + K[K_d2]*x[46] + K[K_d37]*x[14] + K[K_d5]*x[1] + K[K_d7]*x[47]);
+    const T D_r13 = nt_div<T>(K[K_d31]*x[48], K[K_d32]*x[45] + het[0]*x[2] + het[1]*x[12] + tj[J_clono2_cl] + tj[J_clono2_clo]);
+    const T D_r9 = nt_div<T>(D_r13*het[0]*x[2] + K[K_d33]*x[47], K[K_d35]*x[45] + het[4]*x[12] + tj[J_hocl]);
+    const T D_r10 = nt_div<T>(K[K_d60]*x[52], F.hnm*K[K_d61] + tj[J_cl2o2]);
+    const T D_r12 = nt_div<T>(K[K_e5c]*x[53], tj[J_brcl]);
+    const T D_r11 = nt_div<T>(T(2)*D_r10*tj[J_cl2o2] + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*x[28] + K[K_d3]*x[45] + K[K_d4]*x[49] + K[K_d8]*x[43] + K[K_e5b]*x[53], K[K_d10]*x[47] + K[K_d2]*x[46] + K[K_d37]*x[14] + K[K_d5]*x[1] + K[K_d7]*x[47]);
     R[44] = -D_r11*x[52] + x[44];
     const T D_t06_c0 = tj[J_hocl]*x[14];
     const T D_t06_c1 = K[K_d33]*x[47]*x[52];
@@ -1924,8 +1924,8 @@ __device__ __forceinline__ void nt_residual_day_w2_1(const FF& F, PK K, PK tj, P
     const bool sel_D_t09 = (D_t09_c0) <= (D_t09_c1);
     const T D_t09 = sel_D_t09 ? T(D_t09_c0) : T(D_t09_c1);
     const T dr7_c0 = T(2)*x[45];
-    const T dr7_c1 = T(2)*tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
-    R[7] = -F.dt*(T(2)*F.o2*tj[J_o2] + K[K_a26]*x[47]*x[49] + K[K_c5]*x[28]*x[49]) + F.dt*(D_t06 + T(2)*D_t07 + D_t09 + K[K_b3]*dr7_c0*x[48] + K[K_b9]*dr7_c1*x[46]*x[48] + K[K_d3]*dr7_c0*x[52] + T(2)*K[K_d60]*tj[J_cl2o2]*(x[52]*x[52])/(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(2)*K[K_e5b]*x[52]*x[53] + T(2)*K[K_e6]*(x[53]*x[53]) + T(2)*K[K_hk1]*(x[45]*x[45]) + K[K_hk3]*dr7_c0*x[46] + dr7_c1*tj[J_clono2_cl]*x[13] + x[45]*(K[K_a5]*x[43] + K[K_a7]*x[47]) + x[46]*(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47])) - ck0[7] + x[7];
+    const T dr7_c1 = nt_div<T>(T(2)*tj[J_no3_no], fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]));
+    R[7] = -F.dt*(T(2)*F.o2*tj[J_o2] + K[K_a26]*x[47]*x[49] + K[K_c5]*x[28]*x[49]) + F.dt*(D_t06 + T(2)*D_t07 + D_t09 + K[K_b3]*dr7_c0*x[48] + K[K_b9]*dr7_c1*x[46]*x[48] + K[K_d3]*dr7_c0*x[52] + nt_div<T>(T(2)*K[K_d60]*tj[J_cl2o2]*(x[52]*x[52]), F.hnm*K[K_d61] + tj[J_cl2o2]) + T(2)*K[K_e5b]*x[52]*x[53] + T(2)*K[K_e6]*(x[53]*x[53]) + T(2)*K[K_hk1]*(x[45]*x[45]) + K[K_hk3]*dr7_c0*x[46] + dr7_c1*tj[J_clono2_cl]*x[13] + x[45]*(K[K_a5]*x[43] + K[K_a7]*x[47]) + x[46]*(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47])) - ck0[7] + x[7];
 }
 
 // scaled Jacobian rows [0, 1, 3, 6, 7, 13, 19, 20, 21, 23, 24, 28, 31, 33, 35, 36, 39, 40, 42, 44, 45, 46, 47, 48, 50, 51, 52, 53, 54, 56] (day equations) into their stored A slots
@@ -2215,21 +2215,21 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     }
     {  // row 42
     const T rs42 = nt_rscale<T>(nt_exp_hi(x[42]), fh);
-        J[99] = (-tj[J_o3_o1d]/(F.n2*K[K_hk4] + F.o2*K[K_hk5])) * (cs46 * rs42);
+        J[99] = (nt_div<T>(-tj[J_o3_o1d], F.n2*K[K_hk4] + F.o2*K[K_hk5])) * (cs46 * rs42);
     }
     {  // row 56
     const T rs56 = nt_rscale<T>(nt_exp_hi(x[56]), fh);
         const T dj56_c0 = F.o2*K[K_c4] + K[K_c3]*xt45;
-        const T dj56_c1 = (T(1)/(dj56_c0));
+        const T dj56_c1 = nt_div<T>(T(1), dj56_c0);
         const T dj56_c2 = K[K_c1a]*xt42 + K[K_c2]*xt43 + K[K_d5]*xt44;
         const T dj56_c3 = dj56_c1*xt1;
         J[177] = (-dj56_c1*dj56_c2) * (cs1 * rs56);
         J[176] = (-K[K_c1a]*dj56_c3) * (cs42 * rs56);
         J[180] = (-K[K_c2]*dj56_c3) * (cs43 * rs56);
         J[179] = (-K[K_d5]*dj56_c3) * (cs44 * rs56);
-        J[178] = (K[K_c3]*dj56_c2*xt1/(dj56_c0*dj56_c0)) * (cs45 * rs56);
+        J[178] = (nt_div<T>(K[K_c3]*dj56_c2*xt1, (dj56_c0*dj56_c0))) * (cs45 * rs56);
     }
-    const T D_r1_c0 = T(1)/(F.o2*K[K_hk2]);
+    const T D_r1_c0 = nt_div<T>(T(1), F.o2*K[K_hk2]);
     const T D_r1 = D_r1_c0*(K[K_a2]*xt55 + K[K_a6]*xt43 + K[K_a6b]*xt47 + K[K_b4]*xt49 + K[K_d2]*xt44 + tj[J_o3_o1d] + tj[J_o3_o3p]);
     const T d_D_r1_43 = D_r1_c0*K[K_a6];
     const T d_D_r1_44 = D_r1_c0*K[K_d2];
@@ -2248,8 +2248,8 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     {  // row 46
     const T rs46 = nt_rscale<T>(nt_exp_hi(x[46]), fh);
         const T dj46_c0 = D_r1 + T(1);
-        const T dj46_c1 = xt7/(dj46_c0*dj46_c0);
-        J[355] = (-T(1)/dj46_c0) * (cs7 * rs46);
+        const T dj46_c1 = nt_div<T>(xt7, (dj46_c0*dj46_c0));
+        J[355] = (nt_div<T>(T(-1), dj46_c0)) * (cs7 * rs46);
         J[358] = (d_D_r1_43*dj46_c1) * (cs43 * rs46);
         J[357] = (d_D_r1_44*dj46_c1) * (cs44 * rs46);
         J[359] = (d_D_r1_47*dj46_c1) * (cs47 * rs46);
@@ -2258,25 +2258,25 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     }
     const T D_r4_c0 = F.h2*K[K_a19] + K[K_a36]*xt8 + K[K_a5]*xt45;
     const T D_r4_c1 = F.o2*K[K_a1] + K[K_a2]*xt46 + T(8.049999999999999e-11)*xt47;
-    const T D_r4_c2 = (T(1)/(D_r4_c1));
-    const T D_r4_c3 = D_r4_c0/(D_r4_c1*D_r4_c1);
+    const T D_r4_c2 = nt_div<T>(T(1), D_r4_c1);
+    const T D_r4_c3 = nt_div<T>(D_r4_c0, (D_r4_c1*D_r4_c1));
     const T D_r4 = D_r4_c0*D_r4_c2;
     const T d_D_r4_8 = D_r4_c2*K[K_a36];
     const T d_D_r4_45 = D_r4_c2*K[K_a5];
     const T d_D_r4_46 = -D_r4_c3*K[K_a2];
     const T d_D_r4_47 = -T(8.049999999999999e-11)*D_r4_c3;
     const T D_r7_c0 = F.o2*K[K_b7] + K[K_b6]*xt49;
-    const T D_r7 = tj[J_no]/D_r7_c0;
-    const T d_D_r7_49 = -K[K_b6]*tj[J_no]/(D_r7_c0*D_r7_c0);
+    const T D_r7 = nt_div<T>(tj[J_no], D_r7_c0);
+    const T d_D_r7_49 = nt_div<T>(-K[K_b6]*tj[J_no], (D_r7_c0*D_r7_c0));
     {  // row 51
     const T rs51 = nt_rscale<T>(nt_exp_hi(x[51]), fh);
         J[78] = (-D_r7 - d_D_r7_49*xt49) * (cs49 * rs51);
     }
     const T D_r8_c0 = K[K_b12]*xt48 + tj[J_no3_no2] + tj[J_no3_no];
-    const T D_r8_c1 = K[K_b9]/D_r8_c0;
+    const T D_r8_c1 = nt_div<T>(K[K_b9], D_r8_c0);
     const T D_r8 = D_r8_c1*xt46;
     const T d_D_r8_46 = D_r8_c1;
-    const T d_D_r8_48 = -K[K_b12]*K[K_b9]*xt46/(D_r8_c0*D_r8_c0);
+    const T d_D_r8_48 = nt_div<T>(-K[K_b12]*K[K_b9]*xt46, (D_r8_c0*D_r8_c0));
     {  // row 54
     const T rs54 = nt_rscale<T>(nt_exp_hi(x[54]), fh);
         J[68] = T(0);
@@ -2285,8 +2285,8 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     }
     const T D_r5_c0 = D_r8*tj[J_no3_no] + K[K_b3]*xt45 + tj[J_no2];
     const T D_r5_c1 = K[K_a26]*xt47 + K[K_b4]*xt46 + K[K_c5]*xt28 + K[K_d4]*xt52 + K[K_e4]*xt53;
-    const T D_r5_c2 = (T(1)/(D_r5_c1));
-    const T D_r5_c3 = D_r5_c0/(D_r5_c1*D_r5_c1);
+    const T D_r5_c2 = nt_div<T>(T(1), D_r5_c1);
+    const T D_r5_c3 = nt_div<T>(D_r5_c0, (D_r5_c1*D_r5_c1));
     const T D_r5 = D_r5_c0*D_r5_c2;
     const T d_D_r5_28 = -D_r5_c3*K[K_c5];
     const T d_D_r5_45 = D_r5_c2*K[K_b3];
@@ -2298,10 +2298,10 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     {  // row 48
     const T rs48 = nt_rscale<T>(nt_exp_hi(x[48]), fh);
         const T dj48_c0 = D_r5*D_r7 + D_r5 + D_r8 + T(1);
-        const T dj48_c1 = (T(1)/(dj48_c0*dj48_c0));
+        const T dj48_c1 = nt_div<T>(T(1), dj48_c0*dj48_c0);
         const T dj48_c2 = dj48_c1*xt20;
         const T dj48_c3 = dj48_c2*(-D_r7 + T(-1));
-        J[270] = (-T(1)/dj48_c0) * (cs20 * rs48);
+        J[270] = (nt_div<T>(T(-1), dj48_c0)) * (cs20 * rs48);
         J[269] = (-d_D_r5_28*dj48_c3) * (cs28 * rs48);
         J[272] = (-d_D_r5_45*dj48_c3) * (cs45 * rs48);
         J[275] = (-d_D_r5_46*dj48_c3 + d_D_r8_46*dj48_c1*xt20) * (cs46 * rs48);
@@ -2315,9 +2315,9 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     const T D_r6_c1 = D_r4*D_r6_c0 + K[K_a30]*xt16 + K[K_a6]*xt46 + K[K_c8]*xt27 + K[K_d8]*xt52 + K[K_e10]*xt53;
     const T D_r6_c2 = T(2)*K[K_a27];
     const T D_r6_c3 = D_r6_c2*xt47 + K[K_a17]*xt43 + K[K_a26]*xt49 + K[K_a6b]*xt46 + K[K_a7]*xt45 + K[K_d10]*xt44 + K[K_d33]*xt52 + K[K_d7]*xt44 + K[K_e15]*xt53 + K[K_e7]*xt50 + T(8.049999999999999e-11)*xt55;
-    const T D_r6_c4 = (T(1)/(D_r6_c3));
+    const T D_r6_c4 = nt_div<T>(T(1), D_r6_c3);
     const T D_r6_c5 = D_r6_c0*D_r6_c4;
-    const T D_r6_c6 = D_r6_c1/(D_r6_c3*D_r6_c3);
+    const T D_r6_c6 = nt_div<T>(D_r6_c1, (D_r6_c3*D_r6_c3));
     const T D_r6 = D_r6_c1*D_r6_c4;
     const T d_D_r6_8 = D_r6_c5*d_D_r4_8;
     const T d_D_r6_16 = D_r6_c4*K[K_a30];
@@ -2349,8 +2349,8 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
         J[344] = (-d_D_r6_55*xt43) * (cs55 * rs47);
     }
     const T D_r13_c0 = K[K_d32]*xt45 + het[0]*xt2 + het[1]*xt12 + tj[J_clono2_cl] + tj[J_clono2_clo];
-    const T D_r13_c1 = K[K_d31]/D_r13_c0;
-    const T D_r13_c2 = K[K_d31]*xt48/(D_r13_c0*D_r13_c0);
+    const T D_r13_c1 = nt_div<T>(K[K_d31], D_r13_c0);
+    const T D_r13_c2 = nt_div<T>(K[K_d31]*xt48, (D_r13_c0*D_r13_c0));
     const T D_r13 = D_r13_c1*xt48;
     const T d_D_r13_2 = -D_r13_c2*het[0];
     const T d_D_r13_12 = -D_r13_c2*het[1];
@@ -2359,26 +2359,26 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     const T D_r9_c0 = D_r13*het[0];
     const T D_r9_c1 = D_r9_c0*xt2 + K[K_d33]*xt47;
     const T D_r9_c2 = K[K_d35]*xt45 + het[4]*xt12 + tj[J_hocl];
-    const T D_r9_c3 = (T(1)/(D_r9_c2));
+    const T D_r9_c3 = nt_div<T>(T(1), D_r9_c2);
     const T D_r9_c4 = D_r9_c3*het[0]*xt2;
-    const T D_r9_c5 = D_r9_c1/(D_r9_c2*D_r9_c2);
+    const T D_r9_c5 = nt_div<T>(D_r9_c1, (D_r9_c2*D_r9_c2));
     const T D_r9 = D_r9_c1*D_r9_c3;
     const T d_D_r9_2 = D_r9_c0*D_r9_c3 + D_r9_c4*d_D_r13_2;
     const T d_D_r9_12 = D_r9_c4*d_D_r13_12 - D_r9_c5*het[4];
     const T d_D_r9_45 = D_r9_c3*d_D_r13_45*het[0]*xt2 - D_r9_c5*K[K_d35];
     const T d_D_r9_47 = D_r9_c3*K[K_d33];
     const T d_D_r9_48 = D_r9_c4*d_D_r13_48;
-    const T D_r10_c0 = K[K_d60]/(F.hnm*K[K_d61] + tj[J_cl2o2]);
+    const T D_r10_c0 = nt_div<T>(K[K_d60], F.hnm*K[K_d61] + tj[J_cl2o2]);
     const T D_r10 = D_r10_c0*xt52;
     const T d_D_r10_52 = D_r10_c0;
-    const T D_r12_c0 = K[K_e5c]/tj[J_brcl];
+    const T D_r12_c0 = nt_div<T>(K[K_e5c], tj[J_brcl]);
     const T D_r12 = D_r12_c0*xt53;
     const T d_D_r12_53 = D_r12_c0;
     const T D_r11_c0 = K[K_d10]*xt47 + K[K_d2]*xt46 + K[K_d37]*xt14 + K[K_d5]*xt1 + K[K_d7]*xt47;
-    const T D_r11_c1 = (T(1)/(D_r11_c0));
+    const T D_r11_c1 = nt_div<T>(T(1), D_r11_c0);
     const T D_r11_c2 = T(2)*tj[J_cl2o2];
     const T D_r11_c3 = D_r10*D_r11_c2 + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*xt28 + K[K_d3]*xt45 + K[K_d4]*xt49 + K[K_d8]*xt43 + K[K_e5b]*xt53;
-    const T D_r11_c4 = D_r11_c3/(D_r11_c0*D_r11_c0);
+    const T D_r11_c4 = nt_div<T>(D_r11_c3, (D_r11_c0*D_r11_c0));
     const T D_r11_c5 = D_r11_c1*tj[J_clono2_cl];
     const T D_r11_c6 = D_r11_c1*tj[J_hocl];
     const T D_r11 = D_r11_c1*D_r11_c3;
@@ -2414,12 +2414,12 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     {  // row 52
     const T rs52 = nt_rscale<T>(nt_exp_hi(x[52]), fh);
         const T dj52_c0 = D_r11 + T(1);
-        const T dj52_c1 = xt22/(dj52_c0*dj52_c0);
+        const T dj52_c1 = nt_div<T>(xt22, (dj52_c0*dj52_c0));
         J[369] = (d_D_r11_1*dj52_c1) * (cs1 * rs52);
         J[373] = (d_D_r11_2*dj52_c1) * (cs2 * rs52);
         J[372] = (d_D_r11_12*dj52_c1) * (cs12 * rs52);
         J[370] = (d_D_r11_14*dj52_c1) * (cs14 * rs52);
-        J[368] = (-T(1)/dj52_c0) * (cs22 * rs52);
+        J[368] = (nt_div<T>(T(-1), dj52_c0)) * (cs22 * rs52);
         J[371] = (d_D_r11_28*dj52_c1) * (cs28 * rs52);
         J[377] = (d_D_r11_43*dj52_c1) * (cs43 * rs52);
         J[375] = (d_D_r11_45*dj52_c1) * (cs45 * rs52);
@@ -2431,24 +2431,24 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
         J[376] = (d_D_r11_53*dj52_c1) * (cs53 * rs52);
     }
     const T D_r27_c0 = K[K_e8]*xt45 + tj[J_brono2];
-    const T D_r27_c1 = K[K_e13]/D_r27_c0;
+    const T D_r27_c1 = nt_div<T>(K[K_e13], D_r27_c0);
     const T D_r27 = D_r27_c1*xt48;
-    const T d_D_r27_45 = -K[K_e13]*K[K_e8]*xt48/(D_r27_c0*D_r27_c0);
+    const T d_D_r27_45 = nt_div<T>(-K[K_e13]*K[K_e8]*xt48, (D_r27_c0*D_r27_c0));
     const T d_D_r27_48 = D_r27_c1;
     const T D_r28_c0 = K[K_e16]*xt45 + tj[J_hobr];
-    const T D_r28_c1 = K[K_e15]/D_r28_c0;
+    const T D_r28_c1 = nt_div<T>(K[K_e15], D_r28_c0);
     const T D_r28 = D_r28_c1*xt47;
-    const T d_D_r28_45 = -K[K_e15]*K[K_e16]*xt47/(D_r28_c0*D_r28_c0);
+    const T d_D_r28_45 = nt_div<T>(-K[K_e15]*K[K_e16]*xt47, (D_r28_c0*D_r28_c0));
     const T d_D_r28_47 = D_r28_c1;
-    const T D_r29_c0 = K[K_e5c]/tj[J_brcl];
+    const T D_r29_c0 = nt_div<T>(K[K_e5c], tj[J_brcl]);
     const T D_r29 = D_r29_c0*xt52;
     const T d_D_r29_52 = D_r29_c0;
     const T D_r30_c0 = K[K_c19]*xt27 + K[K_e2]*xt46 + K[K_e7]*xt47;
-    const T D_r30_c1 = (T(1)/(D_r30_c0));
+    const T D_r30_c1 = nt_div<T>(T(1), D_r30_c0);
     const T D_r30_c2 = T(0.85)*tj[J_brono2];
     const T D_r30_c3 = T(2)*K[K_e6];
     const T D_r30_c4 = D_r27*D_r30_c2 + D_r28*tj[J_hobr] + D_r29*tj[J_brcl] + D_r30_c3*xt53 + K[K_e10]*xt43 + K[K_e3]*xt45 + K[K_e4]*xt49 + K[K_e5a]*xt52 + K[K_e5b]*xt52 + tj[J_bro];
-    const T D_r30_c5 = D_r30_c4/(D_r30_c0*D_r30_c0);
+    const T D_r30_c5 = nt_div<T>(D_r30_c4, (D_r30_c0*D_r30_c0));
     const T D_r30_c6 = D_r30_c1*D_r30_c2;
     const T D_r30 = D_r30_c1*D_r30_c4;
     const T d_D_r30_27 = -D_r30_c5*K[K_c19];
@@ -2475,8 +2475,8 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     {  // row 53
     const T rs53 = nt_rscale<T>(nt_exp_hi(x[53]), fh);
         const T dj53_c0 = D_r30 + T(1);
-        const T dj53_c1 = xt23/(dj53_c0*dj53_c0);
-        J[297] = (-T(1)/dj53_c0) * (cs23 * rs53);
+        const T dj53_c1 = nt_div<T>(xt23, (dj53_c0*dj53_c0));
+        J[297] = (nt_div<T>(T(-1), dj53_c0)) * (cs23 * rs53);
         J[298] = (d_D_r30_27*dj53_c1) * (cs27 * rs53);
         J[302] = (d_D_r30_43*dj53_c1) * (cs43 * rs53);
         J[300] = (d_D_r30_45*dj53_c1) * (cs45 * rs53);
@@ -2514,7 +2514,7 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
     {  // row 7
     const T rs7 = nt_rscale<T>(nt_exp_hi(x[7]), fh);
         const T dj7_c0 = T(2)*F.dt;
-        const T dj7_c1 = tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
+        const T dj7_c1 = nt_div<T>(tj[J_no3_no], fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]));
         const T dj7_c2 = F.dt*xt49;
         const T dj7_c3 = T(2)*K[K_b3];
         const T dj7_c4 = T(2)*K[K_d3];
@@ -2532,7 +2532,7 @@ __device__ __forceinline__ void nt_jacobian_day_w2_1(const FF& F, PK K, PK tj, P
         J[113] = (F.dt*d_D_t06_47 + F.dt*d_D_t09_47 + F.dt*(K[K_a6b]*xt46 + K[K_a7]*xt45) - K[K_a26]*dj7_c2) * (cs47 * rs7);
         J[109] = (F.dt*(dj7_c3*xt45 + dj7_c6*xt46)) * (cs48 * rs7);
         J[115] = (-F.dt*(K[K_a26]*xt47 + K[K_c5]*xt28)) * (cs49 * rs7);
-        J[116] = (F.dt*d_D_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*xt52/(F.hnm*K[K_d61] + tj[J_cl2o2]) + dj7_c4*xt45 + dj7_c7*xt53) + d_D_t07_52*dj7_c0) * (cs52 * rs7);
+        J[116] = (F.dt*d_D_t06_52 + F.dt*(nt_div<T>(T(4)*K[K_d60]*tj[J_cl2o2]*xt52, F.hnm*K[K_d61] + tj[J_cl2o2]) + dj7_c4*xt45 + dj7_c7*xt53) + d_D_t07_52*dj7_c0) * (cs52 * rs7);
         J[111] = (F.dt*d_D_t09_53 + F.dt*(T(4)*K[K_e6]*xt53 + dj7_c7*xt52) + d_D_t07_53*dj7_c0) * (cs53 * rs7);
         J[107] = (F.dt*K[K_a2]*xt46) * (cs55 * rs7);
     }
@@ -2569,19 +2569,19 @@ __device__ __forceinline__ void nt_residual_day_w4_0(const FF& F, PK K, PK tj, P
     R[34] = -ck0[34] + x[34]*(F.dt*(K[K_d94]*x[43] + tj[J_ch3ccl3]) + T(1));
     R[37] = -ck0[37] + x[37]*(F.dt*(K[K_e50]*x[42] + K[K_e51]*x[43] + tj[J_ch3br]) + T(1));
     R[41] = -ck0[41] + x[41]*(F.dt*(K[K_e54]*x[43] + tj[J_ch2br2]) + T(1));
-    R[56] = -x[1]*(K[K_c1a]*x[42] + K[K_c2]*x[43] + K[K_d5]*x[44])/(F.o2*K[K_c4] + K[K_c3]*x[45]) + x[56];
-    const T D_ch3o = (K[K_c1b]*x[1]*x[42] + tj[J_ch3o2h]*x[29] + x[28]*(T(2)*K[K_c14]*x[28] + K[K_c18]*x[52] + K[K_c5]*x[49]))/(F.o2*K[K_c15]);
-    const T D_hco = x[27]*(K[K_c10]*x[44] + K[K_c19]*x[50] + K[K_c8]*x[43] + K[K_c9]*x[45] + tj[J_ch2o_hco])/(F.o2*K[K_c12]);
-    const T D_r4 = (F.h2*K[K_a19] + K[K_a36]*x[8] + K[K_a5]*x[45])/(F.o2*K[K_a1] + K[K_a2]*x[46] + T(8.049999999999999e-11)*x[47]);
+    R[56] = nt_div<T>(-x[1]*(K[K_c1a]*x[42] + K[K_c2]*x[43] + K[K_d5]*x[44]), F.o2*K[K_c4] + K[K_c3]*x[45]) + x[56];
+    const T D_ch3o = nt_div<T>(K[K_c1b]*x[1]*x[42] + tj[J_ch3o2h]*x[29] + x[28]*(T(2)*K[K_c14]*x[28] + K[K_c18]*x[52] + K[K_c5]*x[49]), F.o2*K[K_c15]);
+    const T D_hco = nt_div<T>(x[27]*(K[K_c10]*x[44] + K[K_c19]*x[50] + K[K_c8]*x[43] + K[K_c9]*x[45] + tj[J_ch2o_hco]), F.o2*K[K_c12]);
+    const T D_r4 = nt_div<T>(F.h2*K[K_a19] + K[K_a36]*x[8] + K[K_a5]*x[45], F.o2*K[K_a1] + K[K_a2]*x[46] + T(8.049999999999999e-11)*x[47]);
     R[55] = -D_r4*x[43] + x[55];
-    const T D_r6 = (D_r4*F.o2*K[K_a1] + K[K_a30]*x[16] + K[K_a6]*x[46] + K[K_c8]*x[27] + K[K_d8]*x[52] + K[K_e10]*x[53])/(K[K_a17]*x[43] + K[K_a26]*x[49] + T(2)*K[K_a27]*x[47] + K[K_a6b]*x[46] + K[K_a7]*x[45] + K[K_d10]*x[44] + K[K_d33]*x[52] + K[K_d7]*x[44] + K[K_e15]*x[53] + K[K_e7]*x[50] + T(8.049999999999999e-11)*x[55]);
+    const T D_r6 = nt_div<T>(D_r4*F.o2*K[K_a1] + K[K_a30]*x[16] + K[K_a6]*x[46] + K[K_c8]*x[27] + K[K_d8]*x[52] + K[K_e10]*x[53], K[K_a17]*x[43] + K[K_a26]*x[49] + T(2)*K[K_a27]*x[47] + K[K_a6b]*x[46] + K[K_a7]*x[45] + K[K_d10]*x[44] + K[K_d33]*x[52] + K[K_d7]*x[44] + K[K_e15]*x[53] + K[K_e7]*x[50] + T(8.049999999999999e-11)*x[55]);
     const T D_coea = D_r6*(T(1.7e-11)*D_r4 + T(2)*D_r6*K[K_a27] + T(2)*K[K_a17]) + T(2)*K[K_a31];
     const T D_coeb = D_r6*K[K_b23]*x[48] + D_r6*K[K_c7]*x[28] + D_r6*K[K_d33]*x[52] + D_r6*K[K_d7]*x[44] + D_r6*K[K_e15]*x[53] + D_r6*K[K_e7]*x[50] + F.parthbr*K[K_e11]*x[18] + F.parthcl*K[K_d11]*x[12] + F.parthno3*K[K_b27]*x[4] + K[K_b22]*x[48] + K[K_b28]*x[21] + K[K_c17a]*x[29] + K[K_c2]*x[1] + K[K_c8]*x[27] + K[K_d34]*x[14] + K[K_d9]*x[52];
     const T D_coec = D_ch3o*F.o2*K[K_c15] + D_hco*F.o2*K[K_c12] + F.h2*K[K_d6]*x[44] + F.parth2o*x[2]*(T(2)*K[K_a1et]*x[42] + T(2)*tj[J_h2o]) + F.parthno3*tj[J_hno3]*x[4] + K[K_c3]*x[45]*x[56] + K[K_e16]*x[25]*x[45] + tj[J_ch3o2h]*x[29] + T(2)*tj[J_h2o2]*x[16] + tj[J_hbr]*x[18] + tj[J_hobr]*x[25] + x[14]*(K[K_d35]*x[45] + K[K_d37]*x[44] + tj[J_hocl]) + x[21]*(F.hnm*K[K_b24] + tj[J_hno4]) + x[27]*(K[K_c9]*x[45] + tj[J_ch2o_hco]) + x[42]*(T(2.4e-10)*F.h2 + x[1]*(K[K_c1a] + K[K_c1b]));
     const T D_argum_c0 = T(4)*D_coea*D_coec + (D_coeb*D_coeb);
     const bool sel_D_argum = (D_argum_c0) >= (T(0));
     const T D_argum = sel_D_argum ? T(D_argum_c0) : T(T(0));
-    R[43] = x[43] - T(0.5)*(sqrt(D_argum) - D_coeb)/D_coea;
+    R[43] = x[43] + nt_div<T>(-(sqrt(D_argum) - D_coeb), T(2)*D_coea);
 }
 
 // scaled Jacobian rows [43] (day equations) into their stored A slots
@@ -2674,7 +2674,7 @@ __device__ __forceinline__ void nt_jacobian_day_w4_0(const FF& F, PK K, PK tj, P
     const T D_ch3o_c0 = K[K_c1b]*xt42;
     const T D_ch3o_c1 = K[K_c14]*xt28;
     const T D_ch3o_c2 = K[K_c18]*xt52 + K[K_c5]*xt49;
-    const T D_ch3o_c3 = T(1)/(F.o2*K[K_c15]);
+    const T D_ch3o_c3 = nt_div<T>(T(1), F.o2*K[K_c15]);
     const T D_ch3o_c4 = D_ch3o_c3*xt28;
     const T D_ch3o = D_ch3o_c3*(D_ch3o_c0*xt1 + tj[J_ch3o2h]*xt29 + xt28*(T(2)*D_ch3o_c1 + D_ch3o_c2));
     const T d_D_ch3o_1 = D_ch3o_c0*D_ch3o_c3;
@@ -2683,7 +2683,7 @@ __device__ __forceinline__ void nt_jacobian_day_w4_0(const FF& F, PK K, PK tj, P
     const T d_D_ch3o_42 = D_ch3o_c3*K[K_c1b]*xt1;
     const T d_D_ch3o_49 = D_ch3o_c4*K[K_c5];
     const T d_D_ch3o_52 = D_ch3o_c4*K[K_c18];
-    const T D_hco_c0 = T(1)/(F.o2*K[K_c12]);
+    const T D_hco_c0 = nt_div<T>(T(1), F.o2*K[K_c12]);
     const T D_hco_c1 = D_hco_c0*(K[K_c10]*xt44 + K[K_c19]*xt50 + K[K_c8]*xt43 + K[K_c9]*xt45 + tj[J_ch2o_hco]);
     const T D_hco_c2 = D_hco_c0*xt27;
     const T D_hco = D_hco_c1*xt27;
@@ -2694,8 +2694,8 @@ __device__ __forceinline__ void nt_jacobian_day_w4_0(const FF& F, PK K, PK tj, P
     const T d_D_hco_50 = D_hco_c2*K[K_c19];
     const T D_r4_c0 = F.h2*K[K_a19] + K[K_a36]*xt8 + K[K_a5]*xt45;
     const T D_r4_c1 = F.o2*K[K_a1] + K[K_a2]*xt46 + T(8.049999999999999e-11)*xt47;
-    const T D_r4_c2 = (T(1)/(D_r4_c1));
-    const T D_r4_c3 = D_r4_c0/(D_r4_c1*D_r4_c1);
+    const T D_r4_c2 = nt_div<T>(T(1), D_r4_c1);
+    const T D_r4_c3 = nt_div<T>(D_r4_c0, (D_r4_c1*D_r4_c1));
     const T D_r4 = D_r4_c0*D_r4_c2;
     const T d_D_r4_8 = D_r4_c2*K[K_a36];
     const T d_D_r4_45 = D_r4_c2*K[K_a5];
@@ -2705,9 +2705,9 @@ __device__ __forceinline__ void nt_jacobian_day_w4_0(const FF& F, PK K, PK tj, P
     const T D_r6_c1 = D_r4*D_r6_c0 + K[K_a30]*xt16 + K[K_a6]*xt46 + K[K_c8]*xt27 + K[K_d8]*xt52 + K[K_e10]*xt53;
     const T D_r6_c2 = T(2)*K[K_a27];
     const T D_r6_c3 = D_r6_c2*xt47 + K[K_a17]*xt43 + K[K_a26]*xt49 + K[K_a6b]*xt46 + K[K_a7]*xt45 + K[K_d10]*xt44 + K[K_d33]*xt52 + K[K_d7]*xt44 + K[K_e15]*xt53 + K[K_e7]*xt50 + T(8.049999999999999e-11)*xt55;
-    const T D_r6_c4 = (T(1)/(D_r6_c3));
+    const T D_r6_c4 = nt_div<T>(T(1), D_r6_c3);
     const T D_r6_c5 = D_r6_c0*D_r6_c4;
-    const T D_r6_c6 = D_r6_c1/(D_r6_c3*D_r6_c3);
+    const T D_r6_c6 = nt_div<T>(D_r6_c1, (D_r6_c3*D_r6_c3));
     const T D_r6 = D_r6_c1*D_r6_c4;
     const T d_D_r6_8 = D_r6_c5*d_D_r4_8;
     const T d_D_r6_16 = D_r6_c4*K[K_a30];
@@ -2841,11 +2841,11 @@ __device__ __forceinline__ void nt_jacobian_day_w4_0(const FF& F, PK K, PK tj, P
     const T d_D_argum_56 = sel_D_argum ? T(D_argum_c0*d_D_coec_56) : T(T(0));
     {  // row 43
     const T rs43 = nt_rscale<T>(nt_exp_hi(x[43]), fh);
-        const T dj43_c0 = (T(1)/(D_coea));
-        const T dj43_c1 = (T(0.5))*dj43_c0;
+        const T dj43_c0 = nt_div<T>(T(1), D_coea);
+        const T dj43_c1 = nt_div<T>(dj43_c0, T(2));
         const T dj43_c2 = sqrt(D_argum);
-        const T dj43_c3 = (T(0.25))*dj43_c0/dj43_c2;
-        const T dj43_c4 = (T(0.5))*(-D_coeb + dj43_c2)/(D_coea*D_coea);
+        const T dj43_c3 = nt_div<T>(dj43_c0, T(4)*dj43_c2);
+        const T dj43_c4 = nt_div<T>(-D_coeb + dj43_c2, T(2)*(D_coea*D_coea));
         J[321] = (-d_D_argum_1*dj43_c3 + d_D_coeb_1*dj43_c1) * (cs1 * rs43);
         J[331] = (-d_D_argum_2*dj43_c3) * (cs2 * rs43);
         J[319] = (-d_D_argum_4*dj43_c3 + d_D_coeb_4*dj43_c1) * (cs4 * rs43);
@@ -2891,12 +2891,12 @@ __device__ __forceinline__ void nt_residual_day_w4_1(const FF& F, PK K, PK tj, P
     R[29] = -F.dt*K[K_c7]*x[28]*x[47] - ck0[29] + x[29]*(F.dt*(K[K_c17a]*x[43] + K[K_c17b]*x[43] + tj[J_ch3o2h]) + T(1));
     R[33] = -ck0[33] + x[33]*(F.dt*(K[K_d93]*x[42] + tj[J_ccl4]) + T(1));
     R[39] = -ck0[39] + x[39]*(F.dt*(K[K_e53]*x[42] + tj[J_h1301]) + T(1));
-    const T D_ch3o = (K[K_c1b]*x[1]*x[42] + tj[J_ch3o2h]*x[29] + x[28]*(T(2)*K[K_c14]*x[28] + K[K_c18]*x[52] + K[K_c5]*x[49]))/(F.o2*K[K_c15]);
+    const T D_ch3o = nt_div<T>(K[K_c1b]*x[1]*x[42] + tj[J_ch3o2h]*x[29] + x[28]*(T(2)*K[K_c14]*x[28] + K[K_c18]*x[52] + K[K_c5]*x[49]), F.o2*K[K_c15]);
     R[27] = -F.dt*(D_ch3o*F.o2*K[K_c15] + K[K_c17b]*x[29]*x[43] + K[K_c1c]*x[1]*x[42] + K[K_c3]*x[45]*x[56]) - ck0[27] + x[27]*(F.dt*(K[K_c10]*x[44] + K[K_c19]*x[50] + K[K_c8]*x[43] + K[K_c9]*x[45] + tj[J_ch2o_co] + tj[J_ch2o_hco]) + T(1));
-    const T D_r1 = (K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47] + K[K_b4]*x[49] + K[K_d2]*x[44] + tj[J_o3_o1d] + tj[J_o3_o3p])/(F.o2*K[K_hk2]);
+    const T D_r1 = nt_div<T>(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47] + K[K_b4]*x[49] + K[K_d2]*x[44] + tj[J_o3_o1d] + tj[J_o3_o3p], F.o2*K[K_hk2]);
     R[45] = -D_r1*x[46] + x[45];
-    R[46] = x[46] - x[7]/(D_r1 + T(1));
-    const T D_r7 = tj[J_no]/(F.o2*K[K_b7] + K[K_b6]*x[49]);
+    R[46] = x[46] + nt_div<T>(-x[7], D_r1 + T(1));
+    const T D_r7 = nt_div<T>(tj[J_no], F.o2*K[K_b7] + K[K_b6]*x[49]);
     R[51] = -D_r7*x[49] + x[51];
 }
 
@@ -3147,7 +3147,7 @@ __device__ __forceinline__ void nt_jacobian_day_w4_1(const FF& F, PK K, PK tj, P
         J[50] = (F.dt*(K[K_e53]*xt42 + tj[J_h1301]) + T(1)) * (cs39 * rs39);
         J[51] = (F.dt*K[K_e53]*xt39) * (cs42 * rs39);
     }
-    const T D_hco_c0 = T(1)/(F.o2*K[K_c12]);
+    const T D_hco_c0 = nt_div<T>(T(1), F.o2*K[K_c12]);
     const T D_hco_c1 = D_hco_c0*(K[K_c10]*xt44 + K[K_c19]*xt50 + K[K_c8]*xt43 + K[K_c9]*xt45 + tj[J_ch2o_hco]);
     const T D_hco_c2 = D_hco_c0*xt27;
     const T D_hco = D_hco_c1*xt27;
@@ -3166,7 +3166,7 @@ __device__ __forceinline__ void nt_jacobian_day_w4_1(const FF& F, PK K, PK tj, P
         J[162] = (-d_D_hco_45*dj8_c0) * (cs45 * rs8);
         J[164] = (-d_D_hco_50*dj8_c0) * (cs50 * rs8);
     }
-    const T D_r1_c0 = T(1)/(F.o2*K[K_hk2]);
+    const T D_r1_c0 = nt_div<T>(T(1), F.o2*K[K_hk2]);
     const T D_r1 = D_r1_c0*(K[K_a2]*xt55 + K[K_a6]*xt43 + K[K_a6b]*xt47 + K[K_b4]*xt49 + K[K_d2]*xt44 + tj[J_o3_o1d] + tj[J_o3_o3p]);
     const T d_D_r1_43 = D_r1_c0*K[K_a6];
     const T d_D_r1_44 = D_r1_c0*K[K_d2];
@@ -3185,8 +3185,8 @@ __device__ __forceinline__ void nt_jacobian_day_w4_1(const FF& F, PK K, PK tj, P
     {  // row 46
     const T rs46 = nt_rscale<T>(nt_exp_hi(x[46]), fh);
         const T dj46_c0 = D_r1 + T(1);
-        const T dj46_c1 = xt7/(dj46_c0*dj46_c0);
-        J[355] = (-T(1)/dj46_c0) * (cs7 * rs46);
+        const T dj46_c1 = nt_div<T>(xt7, (dj46_c0*dj46_c0));
+        J[355] = (nt_div<T>(T(-1), dj46_c0)) * (cs7 * rs46);
         J[358] = (d_D_r1_43*dj46_c1) * (cs43 * rs46);
         J[357] = (d_D_r1_44*dj46_c1) * (cs44 * rs46);
         J[359] = (d_D_r1_47*dj46_c1) * (cs47 * rs46);
@@ -3195,8 +3195,8 @@ __device__ __forceinline__ void nt_jacobian_day_w4_1(const FF& F, PK K, PK tj, P
     }
     const T D_r4_c0 = F.h2*K[K_a19] + K[K_a36]*xt8 + K[K_a5]*xt45;
     const T D_r4_c1 = F.o2*K[K_a1] + K[K_a2]*xt46 + T(8.049999999999999e-11)*xt47;
-    const T D_r4_c2 = (T(1)/(D_r4_c1));
-    const T D_r4_c3 = D_r4_c0/(D_r4_c1*D_r4_c1);
+    const T D_r4_c2 = nt_div<T>(T(1), D_r4_c1);
+    const T D_r4_c3 = nt_div<T>(D_r4_c0, (D_r4_c1*D_r4_c1));
     const T D_r4 = D_r4_c0*D_r4_c2;
     const T d_D_r4_8 = D_r4_c2*K[K_a36];
     const T d_D_r4_45 = D_r4_c2*K[K_a5];
@@ -3214,9 +3214,9 @@ __device__ __forceinline__ void nt_jacobian_day_w4_1(const FF& F, PK K, PK tj, P
     const T D_r6_c1 = D_r4*D_r6_c0 + K[K_a30]*xt16 + K[K_a6]*xt46 + K[K_c8]*xt27 + K[K_d8]*xt52 + K[K_e10]*xt53;
     const T D_r6_c2 = T(2)*K[K_a27];
     const T D_r6_c3 = D_r6_c2*xt47 + K[K_a17]*xt43 + K[K_a26]*xt49 + K[K_a6b]*xt46 + K[K_a7]*xt45 + K[K_d10]*xt44 + K[K_d33]*xt52 + K[K_d7]*xt44 + K[K_e15]*xt53 + K[K_e7]*xt50 + T(8.049999999999999e-11)*xt55;
-    const T D_r6_c4 = (T(1)/(D_r6_c3));
+    const T D_r6_c4 = nt_div<T>(T(1), D_r6_c3);
     const T D_r6_c5 = D_r6_c0*D_r6_c4;
-    const T D_r6_c6 = D_r6_c1/(D_r6_c3*D_r6_c3);
+    const T D_r6_c6 = nt_div<T>(D_r6_c1, (D_r6_c3*D_r6_c3));
     const T D_r6 = D_r6_c1*D_r6_c4;
     const T d_D_r6_8 = D_r6_c5*d_D_r4_8;
     const T d_D_r6_16 = D_r6_c4*K[K_a30];
@@ -3262,15 +3262,15 @@ __device__ __forceinline__ void nt_residual_day_w4_2(const FF& F, PK K, PK tj, P
     R[35] = -ck0[35] + x[35]*(F.dt*(K[K_d95]*x[43] + tj[J_ch3cl]) + T(1));
     R[36] = -ck0[36] + x[36]*(F.dt*(K[K_d96]*x[42] + K[K_d97]*x[43] + tj[J_hcfc22]) + T(1));
     R[40] = F.dt*F.rain_hbr*x[18] - F.dt*(x[37]*(K[K_e50]*x[42] + K[K_e51]*x[43] + tj[J_ch3br]) + x[38]*(K[K_e52]*x[42] + tj[J_h1211]) + x[39]*(K[K_e53]*x[42] + tj[J_h1301]) + x[41]*(T(2)*K[K_e54]*x[43] + T(2)*tj[J_ch2br2])) - ck0[40] + x[40];
-    R[42] = -tj[J_o3_o1d]*x[46]/(F.n2*K[K_hk4] + F.o2*K[K_hk5]) + x[42];
-    const T D_r4 = (F.h2*K[K_a19] + K[K_a36]*x[8] + K[K_a5]*x[45])/(F.o2*K[K_a1] + K[K_a2]*x[46] + T(8.049999999999999e-11)*x[47]);
-    const T D_r7 = tj[J_no]/(F.o2*K[K_b7] + K[K_b6]*x[49]);
-    const T D_r8 = K[K_b9]*x[46]/(K[K_b12]*x[48] + tj[J_no3_no2] + tj[J_no3_no]);
+    R[42] = nt_div<T>(-tj[J_o3_o1d]*x[46], F.n2*K[K_hk4] + F.o2*K[K_hk5]) + x[42];
+    const T D_r4 = nt_div<T>(F.h2*K[K_a19] + K[K_a36]*x[8] + K[K_a5]*x[45], F.o2*K[K_a1] + K[K_a2]*x[46] + T(8.049999999999999e-11)*x[47]);
+    const T D_r7 = nt_div<T>(tj[J_no], F.o2*K[K_b7] + K[K_b6]*x[49]);
+    const T D_r8 = nt_div<T>(K[K_b9]*x[46], K[K_b12]*x[48] + tj[J_no3_no2] + tj[J_no3_no]);
     R[54] = -D_r8*x[48] + x[54];
-    const T D_r5 = (D_r8*tj[J_no3_no] + K[K_b3]*x[45] + tj[J_no2])/(K[K_a26]*x[47] + K[K_b4]*x[46] + K[K_c5]*x[28] + K[K_d4]*x[52] + K[K_e4]*x[53]);
-    R[48] = -x[20]/(D_r5*D_r7 + D_r5 + D_r8 + T(1)) + x[48];
+    const T D_r5 = nt_div<T>(D_r8*tj[J_no3_no] + K[K_b3]*x[45] + tj[J_no2], K[K_a26]*x[47] + K[K_b4]*x[46] + K[K_c5]*x[28] + K[K_d4]*x[52] + K[K_e4]*x[53]);
+    R[48] = nt_div<T>(-x[20], D_r5*D_r7 + D_r5 + D_r8 + T(1)) + x[48];
     R[49] = -D_r5*x[48] + x[49];
-    const T D_r6 = (D_r4*F.o2*K[K_a1] + K[K_a30]*x[16] + K[K_a6]*x[46] + K[K_c8]*x[27] + K[K_d8]*x[52] + K[K_e10]*x[53])/(K[K_a17]*x[43] + K[K_a26]*x[49] + T(2)*K[K_a27]*x[47] + K[K_a6b]*x[46] + K[K_a7]*x[45] + K[K_d10]*x[44] + K[K_d33]*x[52] + K[K_d7]*x[44] + K[K_e15]*x[53] + K[K_e7]*x[50] + T(8.049999999999999e-11)*x[55]);
+    const T D_r6 = nt_div<T>(D_r4*F.o2*K[K_a1] + K[K_a30]*x[16] + K[K_a6]*x[46] + K[K_c8]*x[27] + K[K_d8]*x[52] + K[K_e10]*x[53], K[K_a17]*x[43] + K[K_a26]*x[49] + T(2)*K[K_a27]*x[47] + K[K_a6b]*x[46] + K[K_a7]*x[45] + K[K_d10]*x[44] + K[K_d33]*x[52] + K[K_d7]*x[44] + K[K_e15]*x[53] + K[K_e7]*x[50] + T(8.049999999999999e-11)*x[55]);
     R[47] = -D_r6*x[43] + x[47];
     const T D_t06_c0 = tj[J_hocl]*x[14];
     const T D_t06_c1 = K[K_d33]*x[47]*x[52];
@@ -3285,8 +3285,8 @@ __device__ __forceinline__ void nt_residual_day_w4_2(const FF& F, PK K, PK tj, P
     const bool sel_D_t09 = (D_t09_c0) <= (D_t09_c1);
     const T D_t09 = sel_D_t09 ? T(D_t09_c0) : T(D_t09_c1);
     const T dr7_c0 = T(2)*x[45];
-    const T dr7_c1 = T(2)*tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
-    R[7] = -F.dt*(T(2)*F.o2*tj[J_o2] + K[K_a26]*x[47]*x[49] + K[K_c5]*x[28]*x[49]) + F.dt*(D_t06 + T(2)*D_t07 + D_t09 + K[K_b3]*dr7_c0*x[48] + K[K_b9]*dr7_c1*x[46]*x[48] + K[K_d3]*dr7_c0*x[52] + T(2)*K[K_d60]*tj[J_cl2o2]*(x[52]*x[52])/(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(2)*K[K_e5b]*x[52]*x[53] + T(2)*K[K_e6]*(x[53]*x[53]) + T(2)*K[K_hk1]*(x[45]*x[45]) + K[K_hk3]*dr7_c0*x[46] + dr7_c1*tj[J_clono2_cl]*x[13] + x[45]*(K[K_a5]*x[43] + K[K_a7]*x[47]) + x[46]*(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47])) - ck0[7] + x[7];
+    const T dr7_c1 = nt_div<T>(T(2)*tj[J_no3_no], fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]));
+    R[7] = -F.dt*(T(2)*F.o2*tj[J_o2] + K[K_a26]*x[47]*x[49] + K[K_c5]*x[28]*x[49]) + F.dt*(D_t06 + T(2)*D_t07 + D_t09 + K[K_b3]*dr7_c0*x[48] + K[K_b9]*dr7_c1*x[46]*x[48] + K[K_d3]*dr7_c0*x[52] + nt_div<T>(T(2)*K[K_d60]*tj[J_cl2o2]*(x[52]*x[52]), F.hnm*K[K_d61] + tj[J_cl2o2]) + T(2)*K[K_e5b]*x[52]*x[53] + T(2)*K[K_e6]*(x[53]*x[53]) + T(2)*K[K_hk1]*(x[45]*x[45]) + K[K_hk3]*dr7_c0*x[46] + dr7_c1*tj[J_clono2_cl]*x[13] + x[45]*(K[K_a5]*x[43] + K[K_a7]*x[47]) + x[46]*(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47])) - ck0[7] + x[7];
 }
 
 // scaled Jacobian rows [0, 4, 5, 6, 12, 13, 16, 25, 27, 29, 30, 33, 38, 40, 42, 50, 52, 53] (day equations) into their stored A slots
@@ -3522,12 +3522,12 @@ __device__ __forceinline__ void nt_jacobian_day_w4_2(const FF& F, PK K, PK tj, P
     }
     {  // row 42
     const T rs42 = nt_rscale<T>(nt_exp_hi(x[42]), fh);
-        J[99] = (-tj[J_o3_o1d]/(F.n2*K[K_hk4] + F.o2*K[K_hk5])) * (cs46 * rs42);
+        J[99] = (nt_div<T>(-tj[J_o3_o1d], F.n2*K[K_hk4] + F.o2*K[K_hk5])) * (cs46 * rs42);
     }
     const T D_ch3o_c0 = K[K_c1b]*xt42;
     const T D_ch3o_c1 = K[K_c14]*xt28;
     const T D_ch3o_c2 = K[K_c18]*xt52 + K[K_c5]*xt49;
-    const T D_ch3o_c3 = T(1)/(F.o2*K[K_c15]);
+    const T D_ch3o_c3 = nt_div<T>(T(1), F.o2*K[K_c15]);
     const T D_ch3o_c4 = D_ch3o_c3*xt28;
     const T D_ch3o = D_ch3o_c3*(D_ch3o_c0*xt1 + tj[J_ch3o2h]*xt29 + xt28*(T(2)*D_ch3o_c1 + D_ch3o_c2));
     const T d_D_ch3o_1 = D_ch3o_c0*D_ch3o_c3;
@@ -3557,8 +3557,8 @@ __device__ __forceinline__ void nt_jacobian_day_w4_2(const FF& F, PK K, PK tj, P
         J[220] = (-dj27_c4*xt45) * (cs56 * rs27);
     }
     const T D_r13_c0 = K[K_d32]*xt45 + het[0]*xt2 + het[1]*xt12 + tj[J_clono2_cl] + tj[J_clono2_clo];
-    const T D_r13_c1 = K[K_d31]/D_r13_c0;
-    const T D_r13_c2 = K[K_d31]*xt48/(D_r13_c0*D_r13_c0);
+    const T D_r13_c1 = nt_div<T>(K[K_d31], D_r13_c0);
+    const T D_r13_c2 = nt_div<T>(K[K_d31]*xt48, (D_r13_c0*D_r13_c0));
     const T D_r13 = D_r13_c1*xt48;
     const T d_D_r13_2 = -D_r13_c2*het[0];
     const T d_D_r13_12 = -D_r13_c2*het[1];
@@ -3567,26 +3567,26 @@ __device__ __forceinline__ void nt_jacobian_day_w4_2(const FF& F, PK K, PK tj, P
     const T D_r9_c0 = D_r13*het[0];
     const T D_r9_c1 = D_r9_c0*xt2 + K[K_d33]*xt47;
     const T D_r9_c2 = K[K_d35]*xt45 + het[4]*xt12 + tj[J_hocl];
-    const T D_r9_c3 = (T(1)/(D_r9_c2));
+    const T D_r9_c3 = nt_div<T>(T(1), D_r9_c2);
     const T D_r9_c4 = D_r9_c3*het[0]*xt2;
-    const T D_r9_c5 = D_r9_c1/(D_r9_c2*D_r9_c2);
+    const T D_r9_c5 = nt_div<T>(D_r9_c1, (D_r9_c2*D_r9_c2));
     const T D_r9 = D_r9_c1*D_r9_c3;
     const T d_D_r9_2 = D_r9_c0*D_r9_c3 + D_r9_c4*d_D_r13_2;
     const T d_D_r9_12 = D_r9_c4*d_D_r13_12 - D_r9_c5*het[4];
     const T d_D_r9_45 = D_r9_c3*d_D_r13_45*het[0]*xt2 - D_r9_c5*K[K_d35];
     const T d_D_r9_47 = D_r9_c3*K[K_d33];
     const T d_D_r9_48 = D_r9_c4*d_D_r13_48;
-    const T D_r10_c0 = K[K_d60]/(F.hnm*K[K_d61] + tj[J_cl2o2]);
+    const T D_r10_c0 = nt_div<T>(K[K_d60], F.hnm*K[K_d61] + tj[J_cl2o2]);
     const T D_r10 = D_r10_c0*xt52;
     const T d_D_r10_52 = D_r10_c0;
-    const T D_r12_c0 = K[K_e5c]/tj[J_brcl];
+    const T D_r12_c0 = nt_div<T>(K[K_e5c], tj[J_brcl]);
     const T D_r12 = D_r12_c0*xt53;
     const T d_D_r12_53 = D_r12_c0;
     const T D_r11_c0 = K[K_d10]*xt47 + K[K_d2]*xt46 + K[K_d37]*xt14 + K[K_d5]*xt1 + K[K_d7]*xt47;
-    const T D_r11_c1 = (T(1)/(D_r11_c0));
+    const T D_r11_c1 = nt_div<T>(T(1), D_r11_c0);
     const T D_r11_c2 = T(2)*tj[J_cl2o2];
     const T D_r11_c3 = D_r10*D_r11_c2 + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*xt28 + K[K_d3]*xt45 + K[K_d4]*xt49 + K[K_d8]*xt43 + K[K_e5b]*xt53;
-    const T D_r11_c4 = D_r11_c3/(D_r11_c0*D_r11_c0);
+    const T D_r11_c4 = nt_div<T>(D_r11_c3, (D_r11_c0*D_r11_c0));
     const T D_r11_c5 = D_r11_c1*tj[J_clono2_cl];
     const T D_r11_c6 = D_r11_c1*tj[J_hocl];
     const T D_r11 = D_r11_c1*D_r11_c3;
@@ -3606,12 +3606,12 @@ __device__ __forceinline__ void nt_jacobian_day_w4_2(const FF& F, PK K, PK tj, P
     {  // row 52
     const T rs52 = nt_rscale<T>(nt_exp_hi(x[52]), fh);
         const T dj52_c0 = D_r11 + T(1);
-        const T dj52_c1 = xt22/(dj52_c0*dj52_c0);
+        const T dj52_c1 = nt_div<T>(xt22, (dj52_c0*dj52_c0));
         J[369] = (d_D_r11_1*dj52_c1) * (cs1 * rs52);
         J[373] = (d_D_r11_2*dj52_c1) * (cs2 * rs52);
         J[372] = (d_D_r11_12*dj52_c1) * (cs12 * rs52);
         J[370] = (d_D_r11_14*dj52_c1) * (cs14 * rs52);
-        J[368] = (-T(1)/dj52_c0) * (cs22 * rs52);
+        J[368] = (nt_div<T>(T(-1), dj52_c0)) * (cs22 * rs52);
         J[371] = (d_D_r11_28*dj52_c1) * (cs28 * rs52);
         J[377] = (d_D_r11_43*dj52_c1) * (cs43 * rs52);
         J[375] = (d_D_r11_45*dj52_c1) * (cs45 * rs52);
@@ -3623,24 +3623,24 @@ __device__ __forceinline__ void nt_jacobian_day_w4_2(const FF& F, PK K, PK tj, P
         J[376] = (d_D_r11_53*dj52_c1) * (cs53 * rs52);
     }
     const T D_r27_c0 = K[K_e8]*xt45 + tj[J_brono2];
-    const T D_r27_c1 = K[K_e13]/D_r27_c0;
+    const T D_r27_c1 = nt_div<T>(K[K_e13], D_r27_c0);
     const T D_r27 = D_r27_c1*xt48;
-    const T d_D_r27_45 = -K[K_e13]*K[K_e8]*xt48/(D_r27_c0*D_r27_c0);
+    const T d_D_r27_45 = nt_div<T>(-K[K_e13]*K[K_e8]*xt48, (D_r27_c0*D_r27_c0));
     const T d_D_r27_48 = D_r27_c1;
     const T D_r28_c0 = K[K_e16]*xt45 + tj[J_hobr];
-    const T D_r28_c1 = K[K_e15]/D_r28_c0;
+    const T D_r28_c1 = nt_div<T>(K[K_e15], D_r28_c0);
     const T D_r28 = D_r28_c1*xt47;
-    const T d_D_r28_45 = -K[K_e15]*K[K_e16]*xt47/(D_r28_c0*D_r28_c0);
+    const T d_D_r28_45 = nt_div<T>(-K[K_e15]*K[K_e16]*xt47, (D_r28_c0*D_r28_c0));
     const T d_D_r28_47 = D_r28_c1;
-    const T D_r29_c0 = K[K_e5c]/tj[J_brcl];
+    const T D_r29_c0 = nt_div<T>(K[K_e5c], tj[J_brcl]);
     const T D_r29 = D_r29_c0*xt52;
     const T d_D_r29_52 = D_r29_c0;
     const T D_r30_c0 = K[K_c19]*xt27 + K[K_e2]*xt46 + K[K_e7]*xt47;
-    const T D_r30_c1 = (T(1)/(D_r30_c0));
+    const T D_r30_c1 = nt_div<T>(T(1), D_r30_c0);
     const T D_r30_c2 = T(0.85)*tj[J_brono2];
     const T D_r30_c3 = T(2)*K[K_e6];
     const T D_r30_c4 = D_r27*D_r30_c2 + D_r28*tj[J_hobr] + D_r29*tj[J_brcl] + D_r30_c3*xt53 + K[K_e10]*xt43 + K[K_e3]*xt45 + K[K_e4]*xt49 + K[K_e5a]*xt52 + K[K_e5b]*xt52 + tj[J_bro];
-    const T D_r30_c5 = D_r30_c4/(D_r30_c0*D_r30_c0);
+    const T D_r30_c5 = nt_div<T>(D_r30_c4, (D_r30_c0*D_r30_c0));
     const T D_r30_c6 = D_r30_c1*D_r30_c2;
     const T D_r30 = D_r30_c1*D_r30_c4;
     const T d_D_r30_27 = -D_r30_c5*K[K_c19];
@@ -3667,8 +3667,8 @@ __device__ __forceinline__ void nt_jacobian_day_w4_2(const FF& F, PK K, PK tj, P
     {  // row 53
     const T rs53 = nt_rscale<T>(nt_exp_hi(x[53]), fh);
         const T dj53_c0 = D_r30 + T(1);
-        const T dj53_c1 = xt23/(dj53_c0*dj53_c0);
-        J[297] = (-T(1)/dj53_c0) * (cs23 * rs53);
+        const T dj53_c1 = nt_div<T>(xt23, (dj53_c0*dj53_c0));
+        J[297] = (nt_div<T>(T(-1), dj53_c0)) * (cs23 * rs53);
         J[298] = (d_D_r30_27*dj53_c1) * (cs27 * rs53);
         J[302] = (d_D_r30_43*dj53_c1) * (cs43 * rs53);
         J[300] = (d_D_r30_45*dj53_c1) * (cs45 * rs53);
@@ -3696,21 +3696,21 @@ __device__ __forceinline__ void nt_residual_day_w4_3(const FF& F, PK K, PK tj, P
     R[28] = -F.dt*(F.o2*K[K_c4]*x[56] + K[K_c17a]*x[29]*x[43]) - ck0[28] + x[28]*(F.dt*(T(2)*K[K_c14]*x[28] + K[K_c18]*x[52] + K[K_c5]*x[49] + K[K_c7]*x[47]) + T(1));
     R[32] = -ck0[32] + x[32]*(F.dt*(K[K_d92]*x[42] + tj[J_cfc113]) + T(1));
     R[38] = -ck0[38] + x[38]*(F.dt*(K[K_e52]*x[42] + tj[J_h1211]) + T(1));
-    const T D_hco = x[27]*(K[K_c10]*x[44] + K[K_c19]*x[50] + K[K_c8]*x[43] + K[K_c9]*x[45] + tj[J_ch2o_hco])/(F.o2*K[K_c12]);
+    const T D_hco = nt_div<T>(x[27]*(K[K_c10]*x[44] + K[K_c19]*x[50] + K[K_c8]*x[43] + K[K_c9]*x[45] + tj[J_ch2o_hco]), F.o2*K[K_c12]);
     R[8] = -F.dt*(D_hco*F.o2*K[K_c12] + F.co2*tj[J_co2] + tj[J_ch2o_co]*x[27]) - ck0[8] + x[8]*(F.dt*K[K_a36]*x[43] + T(1));
-    const T D_r13 = K[K_d31]*x[48]/(K[K_d32]*x[45] + het[0]*x[2] + het[1]*x[12] + tj[J_clono2_cl] + tj[J_clono2_clo]);
-    const T D_r9 = (D_r13*het[0]*x[2] + K[K_d33]*x[47])/(K[K_d35]*x[45] + het[4]*x[12] + tj[J_hocl]);
-    const T D_r10 = K[K_d60]*x[52]/(F.hnm*K[K_d61] + tj[J_cl2o2]);
-    const T D_r12 = K[K_e5c]*x[53]/tj[J_brcl];
-    const T D_r11 = (T(2)*D_r10*tj[J_cl2o2] + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*x[28] + K[K_d3]*x[45] + K[K_d4]*x[49] + K[K_d8]*x[43] + K[K_e5b]*x[53])/(K[K_d10]*x[47] + K[K_d2]*x[46] + K[K_d37]*x[14] + K[K_d5]*x[1] + K[K_d7]*x[47]);
+    const T D_r13 = nt_div<T>(K[K_d31]*x[48], K[K_d32]*x[45] + het[0]*x[2] + het[1]*x[12] + tj[J_clono2_cl] + tj[J_clono2_clo]);
+    const T D_r9 = nt_div<T>(D_r13*het[0]*x[2] + K[K_d33]*x[47], K[K_d35]*x[45] + het[4]*x[12] + tj[J_hocl]);
+    const T D_r10 = nt_div<T>(K[K_d60]*x[52], F.hnm*K[K_d61] + tj[J_cl2o2]);
+    const T D_r12 = nt_div<T>(K[K_e5c]*x[53], tj[J_brcl]);
+    const T D_r11 = nt_div<T>(T(2)*D_r10*tj[J_cl2o2] + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*x[28] + K[K_d3]*x[45] + K[K_d4]*x[49] + K[K_d8]*x[43] + K[K_e5b]*x[53], K[K_d10]*x[47] + K[K_d2]*x[46] + K[K_d37]*x[14] + K[K_d5]*x[1] + K[K_d7]*x[47]);
     R[44] = -D_r11*x[52] + x[44];
-    R[52] = -x[22]/(D_r11 + T(1)) + x[52];
-    const T D_r27 = K[K_e13]*x[48]/(K[K_e8]*x[45] + tj[J_brono2]);
-    const T D_r28 = K[K_e15]*x[47]/(K[K_e16]*x[45] + tj[J_hobr]);
-    const T D_r29 = K[K_e5c]*x[52]/tj[J_brcl];
-    const T D_r30 = (T(0.85)*D_r27*tj[J_brono2] + D_r28*tj[J_hobr] + D_r29*tj[J_brcl] + K[K_e10]*x[43] + K[K_e3]*x[45] + K[K_e4]*x[49] + K[K_e5a]*x[52] + K[K_e5b]*x[52] + T(2)*K[K_e6]*x[53] + tj[J_bro])/(K[K_c19]*x[27] + K[K_e2]*x[46] + K[K_e7]*x[47]);
+    R[52] = nt_div<T>(-x[22], D_r11 + T(1)) + x[52];
+    const T D_r27 = nt_div<T>(K[K_e13]*x[48], K[K_e8]*x[45] + tj[J_brono2]);
+    const T D_r28 = nt_div<T>(K[K_e15]*x[47], K[K_e16]*x[45] + tj[J_hobr]);
+    const T D_r29 = nt_div<T>(K[K_e5c]*x[52], tj[J_brcl]);
+    const T D_r30 = nt_div<T>(T(0.85)*D_r27*tj[J_brono2] + D_r28*tj[J_hobr] + D_r29*tj[J_brcl] + K[K_e10]*x[43] + K[K_e3]*x[45] + K[K_e4]*x[49] + K[K_e5a]*x[52] + K[K_e5b]*x[52] + T(2)*K[K_e6]*x[53] + tj[J_bro], K[K_c19]*x[27] + K[K_e2]*x[46] + K[K_e7]*x[47]);
     R[50] = -D_r30*x[53] + x[50];
-    R[53] = -x[23]/(D_r30 + T(1)) + x[53];
+    R[53] = nt_div<T>(-x[23], D_r30 + T(1)) + x[53];
 }
 
 // scaled Jacobian rows [2, 7, 14, 19, 21, 23, 24, 26, 28, 32, 35, 37, 41, 44, 48, 49, 51, 54, 56] (day equations) into their stored A slots
@@ -3935,27 +3935,27 @@ __device__ __forceinline__ void nt_jacobian_day_w4_3(const FF& F, PK K, PK tj, P
     {  // row 56
     const T rs56 = nt_rscale<T>(nt_exp_hi(x[56]), fh);
         const T dj56_c0 = F.o2*K[K_c4] + K[K_c3]*xt45;
-        const T dj56_c1 = (T(1)/(dj56_c0));
+        const T dj56_c1 = nt_div<T>(T(1), dj56_c0);
         const T dj56_c2 = K[K_c1a]*xt42 + K[K_c2]*xt43 + K[K_d5]*xt44;
         const T dj56_c3 = dj56_c1*xt1;
         J[177] = (-dj56_c1*dj56_c2) * (cs1 * rs56);
         J[176] = (-K[K_c1a]*dj56_c3) * (cs42 * rs56);
         J[180] = (-K[K_c2]*dj56_c3) * (cs43 * rs56);
         J[179] = (-K[K_d5]*dj56_c3) * (cs44 * rs56);
-        J[178] = (K[K_c3]*dj56_c2*xt1/(dj56_c0*dj56_c0)) * (cs45 * rs56);
+        J[178] = (nt_div<T>(K[K_c3]*dj56_c2*xt1, (dj56_c0*dj56_c0))) * (cs45 * rs56);
     }
     const T D_r7_c0 = F.o2*K[K_b7] + K[K_b6]*xt49;
-    const T D_r7 = tj[J_no]/D_r7_c0;
-    const T d_D_r7_49 = -K[K_b6]*tj[J_no]/(D_r7_c0*D_r7_c0);
+    const T D_r7 = nt_div<T>(tj[J_no], D_r7_c0);
+    const T d_D_r7_49 = nt_div<T>(-K[K_b6]*tj[J_no], (D_r7_c0*D_r7_c0));
     {  // row 51
     const T rs51 = nt_rscale<T>(nt_exp_hi(x[51]), fh);
         J[78] = (-D_r7 - d_D_r7_49*xt49) * (cs49 * rs51);
     }
     const T D_r8_c0 = K[K_b12]*xt48 + tj[J_no3_no2] + tj[J_no3_no];
-    const T D_r8_c1 = K[K_b9]/D_r8_c0;
+    const T D_r8_c1 = nt_div<T>(K[K_b9], D_r8_c0);
     const T D_r8 = D_r8_c1*xt46;
     const T d_D_r8_46 = D_r8_c1;
-    const T d_D_r8_48 = -K[K_b12]*K[K_b9]*xt46/(D_r8_c0*D_r8_c0);
+    const T d_D_r8_48 = nt_div<T>(-K[K_b12]*K[K_b9]*xt46, (D_r8_c0*D_r8_c0));
     {  // row 54
     const T rs54 = nt_rscale<T>(nt_exp_hi(x[54]), fh);
         J[68] = T(0);
@@ -3964,8 +3964,8 @@ __device__ __forceinline__ void nt_jacobian_day_w4_3(const FF& F, PK K, PK tj, P
     }
     const T D_r5_c0 = D_r8*tj[J_no3_no] + K[K_b3]*xt45 + tj[J_no2];
     const T D_r5_c1 = K[K_a26]*xt47 + K[K_b4]*xt46 + K[K_c5]*xt28 + K[K_d4]*xt52 + K[K_e4]*xt53;
-    const T D_r5_c2 = (T(1)/(D_r5_c1));
-    const T D_r5_c3 = D_r5_c0/(D_r5_c1*D_r5_c1);
+    const T D_r5_c2 = nt_div<T>(T(1), D_r5_c1);
+    const T D_r5_c3 = nt_div<T>(D_r5_c0, (D_r5_c1*D_r5_c1));
     const T D_r5 = D_r5_c0*D_r5_c2;
     const T d_D_r5_28 = -D_r5_c3*K[K_c5];
     const T d_D_r5_45 = D_r5_c2*K[K_b3];
@@ -3977,10 +3977,10 @@ __device__ __forceinline__ void nt_jacobian_day_w4_3(const FF& F, PK K, PK tj, P
     {  // row 48
     const T rs48 = nt_rscale<T>(nt_exp_hi(x[48]), fh);
         const T dj48_c0 = D_r5*D_r7 + D_r5 + D_r8 + T(1);
-        const T dj48_c1 = (T(1)/(dj48_c0*dj48_c0));
+        const T dj48_c1 = nt_div<T>(T(1), dj48_c0*dj48_c0);
         const T dj48_c2 = dj48_c1*xt20;
         const T dj48_c3 = dj48_c2*(-D_r7 + T(-1));
-        J[270] = (-T(1)/dj48_c0) * (cs20 * rs48);
+        J[270] = (nt_div<T>(T(-1), dj48_c0)) * (cs20 * rs48);
         J[269] = (-d_D_r5_28*dj48_c3) * (cs28 * rs48);
         J[272] = (-d_D_r5_45*dj48_c3) * (cs45 * rs48);
         J[275] = (-d_D_r5_46*dj48_c3 + d_D_r8_46*dj48_c1*xt20) * (cs46 * rs48);
@@ -4001,8 +4001,8 @@ __device__ __forceinline__ void nt_jacobian_day_w4_3(const FF& F, PK K, PK tj, P
         J[364] = (-d_D_r5_53*xt48) * (cs53 * rs49);
     }
     const T D_r13_c0 = K[K_d32]*xt45 + het[0]*xt2 + het[1]*xt12 + tj[J_clono2_cl] + tj[J_clono2_clo];
-    const T D_r13_c1 = K[K_d31]/D_r13_c0;
-    const T D_r13_c2 = K[K_d31]*xt48/(D_r13_c0*D_r13_c0);
+    const T D_r13_c1 = nt_div<T>(K[K_d31], D_r13_c0);
+    const T D_r13_c2 = nt_div<T>(K[K_d31]*xt48, (D_r13_c0*D_r13_c0));
     const T D_r13 = D_r13_c1*xt48;
     const T d_D_r13_2 = -D_r13_c2*het[0];
     const T d_D_r13_12 = -D_r13_c2*het[1];
@@ -4011,26 +4011,26 @@ __device__ __forceinline__ void nt_jacobian_day_w4_3(const FF& F, PK K, PK tj, P
     const T D_r9_c0 = D_r13*het[0];
     const T D_r9_c1 = D_r9_c0*xt2 + K[K_d33]*xt47;
     const T D_r9_c2 = K[K_d35]*xt45 + het[4]*xt12 + tj[J_hocl];
-    const T D_r9_c3 = (T(1)/(D_r9_c2));
+    const T D_r9_c3 = nt_div<T>(T(1), D_r9_c2);
     const T D_r9_c4 = D_r9_c3*het[0]*xt2;
-    const T D_r9_c5 = D_r9_c1/(D_r9_c2*D_r9_c2);
+    const T D_r9_c5 = nt_div<T>(D_r9_c1, (D_r9_c2*D_r9_c2));
     const T D_r9 = D_r9_c1*D_r9_c3;
     const T d_D_r9_2 = D_r9_c0*D_r9_c3 + D_r9_c4*d_D_r13_2;
     const T d_D_r9_12 = D_r9_c4*d_D_r13_12 - D_r9_c5*het[4];
     const T d_D_r9_45 = D_r9_c3*d_D_r13_45*het[0]*xt2 - D_r9_c5*K[K_d35];
     const T d_D_r9_47 = D_r9_c3*K[K_d33];
     const T d_D_r9_48 = D_r9_c4*d_D_r13_48;
-    const T D_r10_c0 = K[K_d60]/(F.hnm*K[K_d61] + tj[J_cl2o2]);
+    const T D_r10_c0 = nt_div<T>(K[K_d60], F.hnm*K[K_d61] + tj[J_cl2o2]);
     const T D_r10 = D_r10_c0*xt52;
     const T d_D_r10_52 = D_r10_c0;
-    const T D_r12_c0 = K[K_e5c]/tj[J_brcl];
+    const T D_r12_c0 = nt_div<T>(K[K_e5c], tj[J_brcl]);
     const T D_r12 = D_r12_c0*xt53;
     const T d_D_r12_53 = D_r12_c0;
     const T D_r11_c0 = K[K_d10]*xt47 + K[K_d2]*xt46 + K[K_d37]*xt14 + K[K_d5]*xt1 + K[K_d7]*xt47;
-    const T D_r11_c1 = (T(1)/(D_r11_c0));
+    const T D_r11_c1 = nt_div<T>(T(1), D_r11_c0);
     const T D_r11_c2 = T(2)*tj[J_cl2o2];
     const T D_r11_c3 = D_r10*D_r11_c2 + D_r12*tj[J_brcl] + D_r13*tj[J_clono2_cl] + D_r9*tj[J_hocl] + K[K_c18]*xt28 + K[K_d3]*xt45 + K[K_d4]*xt49 + K[K_d8]*xt43 + K[K_e5b]*xt53;
-    const T D_r11_c4 = D_r11_c3/(D_r11_c0*D_r11_c0);
+    const T D_r11_c4 = nt_div<T>(D_r11_c3, (D_r11_c0*D_r11_c0));
     const T D_r11_c5 = D_r11_c1*tj[J_clono2_cl];
     const T D_r11_c6 = D_r11_c1*tj[J_hocl];
     const T D_r11 = D_r11_c1*D_r11_c3;
@@ -4090,7 +4090,7 @@ __device__ __forceinline__ void nt_jacobian_day_w4_3(const FF& F, PK K, PK tj, P
     {  // row 7
     const T rs7 = nt_rscale<T>(nt_exp_hi(x[7]), fh);
         const T dj7_c0 = T(2)*F.dt;
-        const T dj7_c1 = tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
+        const T dj7_c1 = nt_div<T>(tj[J_no3_no], fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]));
         const T dj7_c2 = F.dt*xt49;
         const T dj7_c3 = T(2)*K[K_b3];
         const T dj7_c4 = T(2)*K[K_d3];
@@ -4108,7 +4108,7 @@ __device__ __forceinline__ void nt_jacobian_day_w4_3(const FF& F, PK K, PK tj, P
         J[113] = (F.dt*d_D_t06_47 + F.dt*d_D_t09_47 + F.dt*(K[K_a6b]*xt46 + K[K_a7]*xt45) - K[K_a26]*dj7_c2) * (cs47 * rs7);
         J[109] = (F.dt*(dj7_c3*xt45 + dj7_c6*xt46)) * (cs48 * rs7);
         J[115] = (-F.dt*(K[K_a26]*xt47 + K[K_c5]*xt28)) * (cs49 * rs7);
-        J[116] = (F.dt*d_D_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*xt52/(F.hnm*K[K_d61] + tj[J_cl2o2]) + dj7_c4*xt45 + dj7_c7*xt53) + d_D_t07_52*dj7_c0) * (cs52 * rs7);
+        J[116] = (F.dt*d_D_t06_52 + F.dt*(nt_div<T>(T(4)*K[K_d60]*tj[J_cl2o2]*xt52, F.hnm*K[K_d61] + tj[J_cl2o2]) + dj7_c4*xt45 + dj7_c7*xt53) + d_D_t07_52*dj7_c0) * (cs52 * rs7);
         J[111] = (F.dt*d_D_t09_53 + F.dt*(T(4)*K[K_e6]*xt53 + dj7_c7*xt52) + d_D_t07_53*dj7_c0) * (cs53 * rs7);
         J[107] = (F.dt*K[K_a2]*xt46) * (cs55 * rs7);
     }
@@ -4197,13 +4197,13 @@ __device__ __forceinline__ void nt_residual_night(const FF& F, PK K, PK tj, PK h
     R[51] = x[51];
     R[55] = x[55];
     R[56] = x[56];
-    const T N_cno = K[K_b9]*x[46]/K[K_b12];
+    const T N_cno = nt_div<T>(K[K_b9]*x[46], K[K_b12]);
     const T N_dno = -N_cno + x[20];
     const bool sel_N_no2 = (N_dno) > (T(1e-30));
-    const T N_no2 = sel_N_no2 ? T(N_dno) : T(T(1e-30)*x[20]/(N_cno + T(1e-30)));
+    const T N_no2 = sel_N_no2 ? T(N_dno) : T(nt_div<T>(T(1e-30)*x[20], N_cno + T(1e-30)));
     R[48] = -N_no2 + x[48];
     const bool sel_N_no3 = (N_dno) > (T(1e-30));
-    const T N_no3 = sel_N_no3 ? T(N_cno) : T(N_cno*x[20]/(N_cno + T(1e-30)));
+    const T N_no3 = sel_N_no3 ? T(N_cno) : T(nt_div<T>(N_cno*x[20], N_cno + T(1e-30)));
     R[54] = -N_no3 + x[54];
     const bool sel_N_clo = (x[22]) >= (T(0));
     const T N_clo = sel_N_clo ? T(x[22]) : T(T(0));
@@ -4224,8 +4224,8 @@ __device__ __forceinline__ void nt_residual_night(const FF& F, PK K, PK tj, PK h
     const bool sel_N_t09 = (N_t09_c0) <= (N_t09_c1);
     const T N_t09 = sel_N_t09 ? T(N_t09_c0) : T(N_t09_c1);
     const T nr7_c0 = T(2)*x[45];
-    const T nr7_c1 = T(2)*tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
-    R[7] = -F.dt*(T(2)*F.o2*tj[J_o2] + K[K_a26]*x[47]*x[49] + K[K_c5]*x[28]*x[49]) + F.dt*(K[K_b3]*nr7_c0*x[48] + K[K_b9]*nr7_c1*x[46]*x[48] + K[K_d3]*nr7_c0*x[52] + T(2)*K[K_d60]*tj[J_cl2o2]*(x[52]*x[52])/(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(2)*K[K_hk1]*(x[45]*x[45]) + K[K_hk3]*nr7_c0*x[46] + N_t06 + T(2)*N_t07 + N_t09 + nr7_c1*tj[J_clono2_cl]*x[13] + x[45]*(K[K_a5]*x[43] + K[K_a7]*x[47]) + x[46]*(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47])) - ck0[7] + x[7];
+    const T nr7_c1 = nt_div<T>(T(2)*tj[J_no3_no], fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]));
+    R[7] = -F.dt*(T(2)*F.o2*tj[J_o2] + K[K_a26]*x[47]*x[49] + K[K_c5]*x[28]*x[49]) + F.dt*(K[K_b3]*nr7_c0*x[48] + K[K_b9]*nr7_c1*x[46]*x[48] + K[K_d3]*nr7_c0*x[52] + nt_div<T>(T(2)*K[K_d60]*tj[J_cl2o2]*(x[52]*x[52]), F.hnm*K[K_d61] + tj[J_cl2o2]) + T(2)*K[K_hk1]*(x[45]*x[45]) + K[K_hk3]*nr7_c0*x[46] + N_t06 + T(2)*N_t07 + N_t09 + nr7_c1*tj[J_clono2_cl]*x[13] + x[45]*(K[K_a5]*x[43] + K[K_a7]*x[47]) + x[46]*(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47])) - ck0[7] + x[7];
 }
 
 // scaled Jacobian J'_ij = dR_i/dx_j s_j / s_i, night equations, into the
@@ -4905,18 +4905,18 @@ __device__ __forceinline__ void nt_jacobian_night(const FF& F, PK K, PK tj, PK h
         J[179] = T(0);
         J[178] = T(0);
     }
-    const T N_cno_c0 = K[K_b9]/K[K_b12];
+    const T N_cno_c0 = nt_div<T>(K[K_b9], K[K_b12]);
     const T N_cno = N_cno_c0*xt46;
     const T d_N_cno_46 = N_cno_c0;
     const T N_dno = -N_cno + xt20;
     const T d_N_dno_20 = T(1);
     const T d_N_dno_46 = -d_N_cno_46;
     const T N_no2_c0 = N_cno + T(1e-30);
-    const T N_no2_c1 = T(1e-30)/N_no2_c0;
+    const T N_no2_c1 = nt_div<T>(T(1e-30), N_no2_c0);
     const bool sel_N_no2 = (N_dno) > (T(1e-30));
     const T N_no2 = sel_N_no2 ? T(N_dno) : T(N_no2_c1*xt20);
     const T d_N_no2_20 = sel_N_no2 ? T(d_N_dno_20) : T(N_no2_c1);
-    const T d_N_no2_46 = sel_N_no2 ? T(d_N_dno_46) : T(-T(1e-30)*d_N_cno_46*xt20/(N_no2_c0*N_no2_c0));
+    const T d_N_no2_46 = sel_N_no2 ? T(d_N_dno_46) : T(nt_div<T>(-T(1e-30)*d_N_cno_46*xt20, (N_no2_c0*N_no2_c0)));
     {  // row 48
     const T rs48 = nt_rscale<T>(nt_exp_hi(x[48]), fh);
         J[270] = (-d_N_no2_20) * (cs20 * rs48);
@@ -4930,12 +4930,12 @@ __device__ __forceinline__ void nt_jacobian_night(const FF& F, PK K, PK tj, PK h
         J[273] = T(0);
     }
     const T N_no3_c0 = N_cno + T(1e-30);
-    const T N_no3_c1 = (T(1)/(N_no3_c0));
+    const T N_no3_c1 = nt_div<T>(T(1), N_no3_c0);
     const T N_no3_c2 = N_cno*N_no3_c1;
     const bool sel_N_no3 = (N_dno) > (T(1e-30));
     const T N_no3 = sel_N_no3 ? T(N_cno) : T(N_no3_c2*xt20);
     const T d_N_no3_20 = sel_N_no3 ? T(T(0)) : T(N_no3_c2);
-    const T d_N_no3_46 = sel_N_no3 ? T(d_N_cno_46) : T(d_N_cno_46*(-N_cno*xt20/(N_no3_c0*N_no3_c0) + N_no3_c1*xt20));
+    const T d_N_no3_46 = sel_N_no3 ? T(d_N_cno_46) : T(d_N_cno_46*(nt_div<T>(-N_cno*xt20, (N_no3_c0*N_no3_c0)) + N_no3_c1*xt20));
     {  // row 54
     const T rs54 = nt_rscale<T>(nt_exp_hi(x[54]), fh);
         J[68] = (-d_N_no3_20) * (cs20 * rs54);
@@ -5005,7 +5005,7 @@ __device__ __forceinline__ void nt_jacobian_night(const FF& F, PK K, PK tj, PK h
     {  // row 7
     const T rs7 = nt_rscale<T>(nt_exp_hi(x[7]), fh);
         const T nj7_c0 = T(2)*F.dt;
-        const T nj7_c1 = tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
+        const T nj7_c1 = nt_div<T>(tj[J_no3_no], fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]));
         const T nj7_c2 = F.dt*xt49;
         const T nj7_c3 = T(2)*K[K_b3];
         const T nj7_c4 = T(2)*K[K_d3];
@@ -5022,7 +5022,7 @@ __device__ __forceinline__ void nt_jacobian_night(const FF& F, PK K, PK tj, PK h
         J[113] = (F.dt*d_N_t06_47 + F.dt*d_N_t09_47 + F.dt*(K[K_a6b]*xt46 + K[K_a7]*xt45) - K[K_a26]*nj7_c2) * (cs47 * rs7);
         J[109] = (F.dt*(nj7_c3*xt45 + nj7_c6*xt46)) * (cs48 * rs7);
         J[115] = (-F.dt*(K[K_a26]*xt47 + K[K_c5]*xt28)) * (cs49 * rs7);
-        J[116] = (F.dt*d_N_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*xt52/(F.hnm*K[K_d61] + tj[J_cl2o2]) + nj7_c4*xt45) + d_N_t07_52*nj7_c0) * (cs52 * rs7);
+        J[116] = (F.dt*d_N_t06_52 + F.dt*(nt_div<T>(T(4)*K[K_d60]*tj[J_cl2o2]*xt52, F.hnm*K[K_d61] + tj[J_cl2o2]) + nj7_c4*xt45) + d_N_t07_52*nj7_c0) * (cs52 * rs7);
         J[111] = (F.dt*d_N_t09_53 + d_N_t07_53*nj7_c0) * (cs53 * rs7);
         J[107] = (F.dt*K[K_a2]*xt46) * (cs55 * rs7);
     }
@@ -5060,13 +5060,13 @@ __device__ __forceinline__ void nt_residual_night_w2_0(const FF& F, PK K, PK tj,
     R[49] = x[49];
     R[51] = x[51];
     R[56] = x[56];
-    const T N_cno = K[K_b9]*x[46]/K[K_b12];
+    const T N_cno = nt_div<T>(K[K_b9]*x[46], K[K_b12]);
     const T N_dno = -N_cno + x[20];
     const bool sel_N_no2 = (N_dno) > (T(1e-30));
-    const T N_no2 = sel_N_no2 ? T(N_dno) : T(T(1e-30)*x[20]/(N_cno + T(1e-30)));
+    const T N_no2 = sel_N_no2 ? T(N_dno) : T(nt_div<T>(T(1e-30)*x[20], N_cno + T(1e-30)));
     R[48] = -N_no2 + x[48];
     const bool sel_N_no3 = (N_dno) > (T(1e-30));
-    const T N_no3 = sel_N_no3 ? T(N_cno) : T(N_cno*x[20]/(N_cno + T(1e-30)));
+    const T N_no3 = sel_N_no3 ? T(N_cno) : T(nt_div<T>(N_cno*x[20], N_cno + T(1e-30)));
     R[54] = -N_no3 + x[54];
     const bool sel_N_bro = (x[23]) >= (T(0));
     const T N_bro = sel_N_bro ? T(x[23]) : T(T(0));
@@ -5460,18 +5460,18 @@ __device__ __forceinline__ void nt_jacobian_night_w2_0(const FF& F, PK K, PK tj,
         J[209] = T(0);
         J[208] = T(0);
     }
-    const T N_cno_c0 = K[K_b9]/K[K_b12];
+    const T N_cno_c0 = nt_div<T>(K[K_b9], K[K_b12]);
     const T N_cno = N_cno_c0*xt46;
     const T d_N_cno_46 = N_cno_c0;
     const T N_dno = -N_cno + xt20;
     const T d_N_dno_20 = T(1);
     const T d_N_dno_46 = -d_N_cno_46;
     const T N_no2_c0 = N_cno + T(1e-30);
-    const T N_no2_c1 = T(1e-30)/N_no2_c0;
+    const T N_no2_c1 = nt_div<T>(T(1e-30), N_no2_c0);
     const bool sel_N_no2 = (N_dno) > (T(1e-30));
     const T N_no2 = sel_N_no2 ? T(N_dno) : T(N_no2_c1*xt20);
     const T d_N_no2_20 = sel_N_no2 ? T(d_N_dno_20) : T(N_no2_c1);
-    const T d_N_no2_46 = sel_N_no2 ? T(d_N_dno_46) : T(-T(1e-30)*d_N_cno_46*xt20/(N_no2_c0*N_no2_c0));
+    const T d_N_no2_46 = sel_N_no2 ? T(d_N_dno_46) : T(nt_div<T>(-T(1e-30)*d_N_cno_46*xt20, (N_no2_c0*N_no2_c0)));
     {  // row 48
     const T rs48 = nt_rscale<T>(nt_exp_hi(x[48]), fh);
         J[270] = (-d_N_no2_20) * (cs20 * rs48);
@@ -5533,8 +5533,8 @@ __device__ __forceinline__ void nt_residual_night_w2_1(const FF& F, PK K, PK tj,
     const bool sel_N_t09 = (N_t09_c0) <= (N_t09_c1);
     const T N_t09 = sel_N_t09 ? T(N_t09_c0) : T(N_t09_c1);
     const T nr7_c0 = T(2)*x[45];
-    const T nr7_c1 = T(2)*tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
-    R[7] = -F.dt*(T(2)*F.o2*tj[J_o2] + K[K_a26]*x[47]*x[49] + K[K_c5]*x[28]*x[49]) + F.dt*(K[K_b3]*nr7_c0*x[48] + K[K_b9]*nr7_c1*x[46]*x[48] + K[K_d3]*nr7_c0*x[52] + T(2)*K[K_d60]*tj[J_cl2o2]*(x[52]*x[52])/(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(2)*K[K_hk1]*(x[45]*x[45]) + K[K_hk3]*nr7_c0*x[46] + N_t06 + T(2)*N_t07 + N_t09 + nr7_c1*tj[J_clono2_cl]*x[13] + x[45]*(K[K_a5]*x[43] + K[K_a7]*x[47]) + x[46]*(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47])) - ck0[7] + x[7];
+    const T nr7_c1 = nt_div<T>(T(2)*tj[J_no3_no], fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]));
+    R[7] = -F.dt*(T(2)*F.o2*tj[J_o2] + K[K_a26]*x[47]*x[49] + K[K_c5]*x[28]*x[49]) + F.dt*(K[K_b3]*nr7_c0*x[48] + K[K_b9]*nr7_c1*x[46]*x[48] + K[K_d3]*nr7_c0*x[52] + nt_div<T>(T(2)*K[K_d60]*tj[J_cl2o2]*(x[52]*x[52]), F.hnm*K[K_d61] + tj[J_cl2o2]) + T(2)*K[K_hk1]*(x[45]*x[45]) + K[K_hk3]*nr7_c0*x[46] + N_t06 + T(2)*N_t07 + N_t09 + nr7_c1*tj[J_clono2_cl]*x[13] + x[45]*(K[K_a5]*x[43] + K[K_a7]*x[47]) + x[46]*(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47])) - ck0[7] + x[7];
 }
 
 // scaled Jacobian rows [2, 3, 5, 7, 8, 9, 12, 13, 16, 17, 20, 26, 27, 28, 31, 33, 35, 37, 39, 40, 43, 45, 49, 51, 52, 53, 54, 56] (night equations) into their stored A slots
@@ -5913,19 +5913,19 @@ __device__ __forceinline__ void nt_jacobian_night_w2_1(const FF& F, PK K, PK tj,
         J[179] = T(0);
         J[178] = T(0);
     }
-    const T N_cno_c0 = K[K_b9]/K[K_b12];
+    const T N_cno_c0 = nt_div<T>(K[K_b9], K[K_b12]);
     const T N_cno = N_cno_c0*xt46;
     const T d_N_cno_46 = N_cno_c0;
     const T N_dno = -N_cno + xt20;
     const T d_N_dno_20 = T(1);
     const T d_N_dno_46 = -d_N_cno_46;
     const T N_no3_c0 = N_cno + T(1e-30);
-    const T N_no3_c1 = (T(1)/(N_no3_c0));
+    const T N_no3_c1 = nt_div<T>(T(1), N_no3_c0);
     const T N_no3_c2 = N_cno*N_no3_c1;
     const bool sel_N_no3 = (N_dno) > (T(1e-30));
     const T N_no3 = sel_N_no3 ? T(N_cno) : T(N_no3_c2*xt20);
     const T d_N_no3_20 = sel_N_no3 ? T(T(0)) : T(N_no3_c2);
-    const T d_N_no3_46 = sel_N_no3 ? T(d_N_cno_46) : T(d_N_cno_46*(-N_cno*xt20/(N_no3_c0*N_no3_c0) + N_no3_c1*xt20));
+    const T d_N_no3_46 = sel_N_no3 ? T(d_N_cno_46) : T(d_N_cno_46*(nt_div<T>(-N_cno*xt20, (N_no3_c0*N_no3_c0)) + N_no3_c1*xt20));
     {  // row 54
     const T rs54 = nt_rscale<T>(nt_exp_hi(x[54]), fh);
         J[68] = (-d_N_no3_20) * (cs20 * rs54);
@@ -5995,7 +5995,7 @@ __device__ __forceinline__ void nt_jacobian_night_w2_1(const FF& F, PK K, PK tj,
     {  // row 7
     const T rs7 = nt_rscale<T>(nt_exp_hi(x[7]), fh);
         const T nj7_c0 = T(2)*F.dt;
-        const T nj7_c1 = tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
+        const T nj7_c1 = nt_div<T>(tj[J_no3_no], fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]));
         const T nj7_c2 = F.dt*xt49;
         const T nj7_c3 = T(2)*K[K_b3];
         const T nj7_c4 = T(2)*K[K_d3];
@@ -6012,7 +6012,7 @@ __device__ __forceinline__ void nt_jacobian_night_w2_1(const FF& F, PK K, PK tj,
         J[113] = (F.dt*d_N_t06_47 + F.dt*d_N_t09_47 + F.dt*(K[K_a6b]*xt46 + K[K_a7]*xt45) - K[K_a26]*nj7_c2) * (cs47 * rs7);
         J[109] = (F.dt*(nj7_c3*xt45 + nj7_c6*xt46)) * (cs48 * rs7);
         J[115] = (-F.dt*(K[K_a26]*xt47 + K[K_c5]*xt28)) * (cs49 * rs7);
-        J[116] = (F.dt*d_N_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*xt52/(F.hnm*K[K_d61] + tj[J_cl2o2]) + nj7_c4*xt45) + d_N_t07_52*nj7_c0) * (cs52 * rs7);
+        J[116] = (F.dt*d_N_t06_52 + F.dt*(nt_div<T>(T(4)*K[K_d60]*tj[J_cl2o2]*xt52, F.hnm*K[K_d61] + tj[J_cl2o2]) + nj7_c4*xt45) + d_N_t07_52*nj7_c0) * (cs52 * rs7);
         J[111] = (F.dt*d_N_t09_53 + d_N_t07_53*nj7_c0) * (cs53 * rs7);
         J[107] = (F.dt*K[K_a2]*xt46) * (cs55 * rs7);
     }
@@ -6392,8 +6392,8 @@ __device__ __forceinline__ void nt_residual_night_w4_1(const FF& F, PK K, PK tj,
     const bool sel_N_t09 = (N_t09_c0) <= (N_t09_c1);
     const T N_t09 = sel_N_t09 ? T(N_t09_c0) : T(N_t09_c1);
     const T nr7_c0 = T(2)*x[45];
-    const T nr7_c1 = T(2)*tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
-    R[7] = -F.dt*(T(2)*F.o2*tj[J_o2] + K[K_a26]*x[47]*x[49] + K[K_c5]*x[28]*x[49]) + F.dt*(K[K_b3]*nr7_c0*x[48] + K[K_b9]*nr7_c1*x[46]*x[48] + K[K_d3]*nr7_c0*x[52] + T(2)*K[K_d60]*tj[J_cl2o2]*(x[52]*x[52])/(F.hnm*K[K_d61] + tj[J_cl2o2]) + T(2)*K[K_hk1]*(x[45]*x[45]) + K[K_hk3]*nr7_c0*x[46] + N_t06 + T(2)*N_t07 + N_t09 + nr7_c1*tj[J_clono2_cl]*x[13] + x[45]*(K[K_a5]*x[43] + K[K_a7]*x[47]) + x[46]*(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47])) - ck0[7] + x[7];
+    const T nr7_c1 = nt_div<T>(T(2)*tj[J_no3_no], fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]));
+    R[7] = -F.dt*(T(2)*F.o2*tj[J_o2] + K[K_a26]*x[47]*x[49] + K[K_c5]*x[28]*x[49]) + F.dt*(K[K_b3]*nr7_c0*x[48] + K[K_b9]*nr7_c1*x[46]*x[48] + K[K_d3]*nr7_c0*x[52] + nt_div<T>(T(2)*K[K_d60]*tj[J_cl2o2]*(x[52]*x[52]), F.hnm*K[K_d61] + tj[J_cl2o2]) + T(2)*K[K_hk1]*(x[45]*x[45]) + K[K_hk3]*nr7_c0*x[46] + N_t06 + T(2)*N_t07 + N_t09 + nr7_c1*tj[J_clono2_cl]*x[13] + x[45]*(K[K_a5]*x[43] + K[K_a7]*x[47]) + x[46]*(K[K_a2]*x[55] + K[K_a6]*x[43] + K[K_a6b]*x[47])) - ck0[7] + x[7];
 }
 
 // scaled Jacobian rows [0, 7, 12, 16, 19, 24, 34, 40, 41, 44, 48, 50, 54] (night equations) into their stored A slots
@@ -6582,18 +6582,18 @@ __device__ __forceinline__ void nt_jacobian_night_w4_1(const FF& F, PK K, PK tj,
         J[315] = T(0);
         J[310] = T(0);
     }
-    const T N_cno_c0 = K[K_b9]/K[K_b12];
+    const T N_cno_c0 = nt_div<T>(K[K_b9], K[K_b12]);
     const T N_cno = N_cno_c0*xt46;
     const T d_N_cno_46 = N_cno_c0;
     const T N_dno = -N_cno + xt20;
     const T d_N_dno_20 = T(1);
     const T d_N_dno_46 = -d_N_cno_46;
     const T N_no2_c0 = N_cno + T(1e-30);
-    const T N_no2_c1 = T(1e-30)/N_no2_c0;
+    const T N_no2_c1 = nt_div<T>(T(1e-30), N_no2_c0);
     const bool sel_N_no2 = (N_dno) > (T(1e-30));
     const T N_no2 = sel_N_no2 ? T(N_dno) : T(N_no2_c1*xt20);
     const T d_N_no2_20 = sel_N_no2 ? T(d_N_dno_20) : T(N_no2_c1);
-    const T d_N_no2_46 = sel_N_no2 ? T(d_N_dno_46) : T(-T(1e-30)*d_N_cno_46*xt20/(N_no2_c0*N_no2_c0));
+    const T d_N_no2_46 = sel_N_no2 ? T(d_N_dno_46) : T(nt_div<T>(-T(1e-30)*d_N_cno_46*xt20, (N_no2_c0*N_no2_c0)));
     {  // row 48
     const T rs48 = nt_rscale<T>(nt_exp_hi(x[48]), fh);
         J[270] = (-d_N_no2_20) * (cs20 * rs48);
@@ -6607,12 +6607,12 @@ __device__ __forceinline__ void nt_jacobian_night_w4_1(const FF& F, PK K, PK tj,
         J[273] = T(0);
     }
     const T N_no3_c0 = N_cno + T(1e-30);
-    const T N_no3_c1 = (T(1)/(N_no3_c0));
+    const T N_no3_c1 = nt_div<T>(T(1), N_no3_c0);
     const T N_no3_c2 = N_cno*N_no3_c1;
     const bool sel_N_no3 = (N_dno) > (T(1e-30));
     const T N_no3 = sel_N_no3 ? T(N_cno) : T(N_no3_c2*xt20);
     const T d_N_no3_20 = sel_N_no3 ? T(T(0)) : T(N_no3_c2);
-    const T d_N_no3_46 = sel_N_no3 ? T(d_N_cno_46) : T(d_N_cno_46*(-N_cno*xt20/(N_no3_c0*N_no3_c0) + N_no3_c1*xt20));
+    const T d_N_no3_46 = sel_N_no3 ? T(d_N_cno_46) : T(d_N_cno_46*(nt_div<T>(-N_cno*xt20, (N_no3_c0*N_no3_c0)) + N_no3_c1*xt20));
     {  // row 54
     const T rs54 = nt_rscale<T>(nt_exp_hi(x[54]), fh);
         J[68] = (-d_N_no3_20) * (cs20 * rs54);
@@ -6646,7 +6646,7 @@ __device__ __forceinline__ void nt_jacobian_night_w4_1(const FF& F, PK K, PK tj,
     {  // row 7
     const T rs7 = nt_rscale<T>(nt_exp_hi(x[7]), fh);
         const T nj7_c0 = T(2)*F.dt;
-        const T nj7_c1 = tj[J_no3_no]/fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]);
+        const T nj7_c1 = nt_div<T>(tj[J_no3_no], fmax(T(1e-30), tj[J_no3_no2] + tj[J_no3_no]));
         const T nj7_c2 = F.dt*xt49;
         const T nj7_c3 = T(2)*K[K_b3];
         const T nj7_c4 = T(2)*K[K_d3];
@@ -6663,7 +6663,7 @@ __device__ __forceinline__ void nt_jacobian_night_w4_1(const FF& F, PK K, PK tj,
         J[113] = (F.dt*d_N_t06_47 + F.dt*d_N_t09_47 + F.dt*(K[K_a6b]*xt46 + K[K_a7]*xt45) - K[K_a26]*nj7_c2) * (cs47 * rs7);
         J[109] = (F.dt*(nj7_c3*xt45 + nj7_c6*xt46)) * (cs48 * rs7);
         J[115] = (-F.dt*(K[K_a26]*xt47 + K[K_c5]*xt28)) * (cs49 * rs7);
-        J[116] = (F.dt*d_N_t06_52 + F.dt*(T(4)*K[K_d60]*tj[J_cl2o2]*xt52/(F.hnm*K[K_d61] + tj[J_cl2o2]) + nj7_c4*xt45) + d_N_t07_52*nj7_c0) * (cs52 * rs7);
+        J[116] = (F.dt*d_N_t06_52 + F.dt*(nt_div<T>(T(4)*K[K_d60]*tj[J_cl2o2]*xt52, F.hnm*K[K_d61] + tj[J_cl2o2]) + nj7_c4*xt45) + d_N_t07_52*nj7_c0) * (cs52 * rs7);
         J[111] = (F.dt*d_N_t09_53 + d_N_t07_53*nj7_c0) * (cs53 * rs7);
         J[107] = (F.dt*K[K_a2]*xt46) * (cs55 * rs7);
     }
@@ -6685,10 +6685,10 @@ __device__ __forceinline__ void nt_residual_night_w4_2(const FF& F, PK K, PK tj,
     R[40] = F.dt*F.rain_hbr*x[18] - F.dt*(x[37]*(K[K_e50]*x[42] + K[K_e51]*x[43] + tj[J_ch3br]) + x[38]*(K[K_e52]*x[42] + tj[J_h1211]) + x[39]*(K[K_e53]*x[42] + tj[J_h1301]) + x[41]*(T(2)*K[K_e54]*x[43] + T(2)*tj[J_ch2br2])) - ck0[40] + x[40];
     R[44] = x[44];
     R[50] = x[50];
-    const T N_cno = K[K_b9]*x[46]/K[K_b12];
+    const T N_cno = nt_div<T>(K[K_b9]*x[46], K[K_b12]);
     const T N_dno = -N_cno + x[20];
     const bool sel_N_no2 = (N_dno) > (T(1e-30));
-    const T N_no2 = sel_N_no2 ? T(N_dno) : T(T(1e-30)*x[20]/(N_cno + T(1e-30)));
+    const T N_no2 = sel_N_no2 ? T(N_dno) : T(nt_div<T>(T(1e-30)*x[20], N_cno + T(1e-30)));
     R[48] = -N_no2 + x[48];
     const bool sel_N_clo = (x[22]) >= (T(0));
     const T N_clo = sel_N_clo ? T(x[22]) : T(T(0));
@@ -6969,10 +6969,10 @@ __device__ __forceinline__ void nt_residual_night_w4_3(const FF& F, PK K, PK tj,
     R[38] = -ck0[38] + x[38]*(F.dt*(K[K_e52]*x[42] + tj[J_h1211]) + T(1));
     R[45] = x[45];
     R[51] = x[51];
-    const T N_cno = K[K_b9]*x[46]/K[K_b12];
+    const T N_cno = nt_div<T>(K[K_b9]*x[46], K[K_b12]);
     const T N_dno = -N_cno + x[20];
     const bool sel_N_no3 = (N_dno) > (T(1e-30));
-    const T N_no3 = sel_N_no3 ? T(N_cno) : T(N_cno*x[20]/(N_cno + T(1e-30)));
+    const T N_no3 = sel_N_no3 ? T(N_cno) : T(nt_div<T>(N_cno*x[20], N_cno + T(1e-30)));
     R[54] = -N_no3 + x[54];
 }
 

@@ -97,6 +97,40 @@ __device__ __forceinline__ float nt_cvt<float>(double v) {
     return nt_f32_from_bits(f);
 }
 
+// Quotients of the generated equations. FP64 (the residual; the FP64
+// solver's Jacobian): the hardware's reciprocal estimate, one Newton-Raphson
+// step and Markstein's correction (P. Markstein, IBM J. Res. Dev. 34(1),
+// 1990) with no range test: five FP64 instructions against the IEEE
+// sequence's nine and its slow-path branch. For operands whose magnitudes
+// lie in 2^+-1000, as the chemistry's do, the quotient is the IEEE one but
+// for a / b within 2^-56 of a rounding boundary (one ulp there); a zero
+// divisor or an infinite dividend gives NaN where IEEE gives an infinity,
+// which fails the cell all the same. FP32 (the mixed solver's Jacobian, which
+// only steers the iteration): the fast division, within 2 ulp for divisors
+// below 2^126. The host build (CPU checks of the generated code) divides.
+template <typename T>
+__device__ __forceinline__ T nt_div(T a, T b);
+template <>
+__device__ __forceinline__ double nt_div<double>(double a, double b) {
+#ifdef __CUDA_ARCH__
+    double r;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(b));
+    r = fma(r, fma(-b, r, 1.0), r);
+    const double q = a * r;
+    return fma(r, fma(-b, q, a), q);
+#else
+    return a / b;
+#endif
+}
+template <>
+__device__ __forceinline__ float nt_div<float>(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fdividef(a, b);
+#else
+    return a / b;
+#endif
+}
+
 __device__ __forceinline__ double nt_widen(double z) { return z; }
 __device__ __forceinline__ double nt_widen(float z) {
     uint32_t f;
