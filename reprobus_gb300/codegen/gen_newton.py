@@ -893,7 +893,7 @@ def emit_factor(w, perm, rows, slot_a, slot_u, const_pos, n):
             for j in sorted(c for c in rows[k] if c > k):
                 w(f"        w{j} -= w{k} * J[{slot_u[(k, j)]}];")
         w(f"        T p = w{t}; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;")
-        w("        const T d = T(1) / p;")
+        w("        const T d = nt_rcp<T>(p);")
         w(f"        {Z(perm[t])} = zt * d;")
         for j in sorted(c for c in rows[t] if c > t):
             w(f"        J[{slot_u[(t, j)]}] = w{j} * d;")

@@ -7267,7 +7267,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w52 = J[10];
         T zt = z[6];
         T p = w0; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[6] = zt * d;
         J[0] = w2 * d;
         J[1] = w5 * d;
@@ -7293,7 +7293,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w52 = J[17];
         T zt = z[40];
         T p = w1; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[40] = zt * d;
         J[11] = w5 * d;
         J[12] = w12 * d;
@@ -7309,7 +7309,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w26 = J[19];
         T zt = z[32];
         T p = w2; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[32] = zt * d;
         J[18] = w26 * d;
     }
@@ -7323,7 +7323,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w55 = J[24];
         T zt = z[3];
         T p = w3; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[3] = zt * d;
         J[19] = w19 * d;
         J[20] = w20 * d;
@@ -7340,7 +7340,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w49 = J[29];
         T zt = z[17];
         T p = w4; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[17] = zt * d;
         J[24] = w18 * d;
         J[25] = w44 * d;
@@ -7353,7 +7353,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w26 = J[31];
         T zt = z[38];
         T p = w5; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[38] = zt * d;
         J[28] = w26 * d;
     }
@@ -7363,7 +7363,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w26 = J[33];
         T zt = z[33];
         T p = w6; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[33] = zt * d;
         J[29] = w26 * d;
     }
@@ -7372,7 +7372,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w7 = T(1.0);
         T zt = z[11];
         T p = w7; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[11] = zt * d;
     }
     NT_FENCE();
@@ -7383,7 +7383,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w53 = J[37];
         T zt = z[29];
         T p = w8; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[29] = zt * d;
         J[30] = w41 * d;
         J[31] = w52 * d;
@@ -7396,7 +7396,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w52 = J[40];
         T zt = z[36];
         T p = w9; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[36] = zt * d;
         J[33] = w26 * d;
         J[34] = w52 * d;
@@ -7407,7 +7407,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w26 = J[42];
         T zt = z[31];
         T p = w10; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[31] = zt * d;
         J[35] = w26 * d;
     }
@@ -7422,7 +7422,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w56 = J[49];
         T zt = z[26];
         T p = w11; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[26] = zt * d;
         J[36] = w21 * d;
         J[37] = w35 * d;
@@ -7437,7 +7437,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w26 = J[51];
         T zt = z[39];
         T p = w12; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[39] = zt * d;
         J[42] = w26 * d;
     }
@@ -7448,7 +7448,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w52 = J[54];
         T zt = z[37];
         T p = w13; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[37] = zt * d;
         J[43] = w26 * d;
         J[44] = w52 * d;
@@ -7462,7 +7462,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w50 = J[59];
         T zt = z[19];
         T p = w14; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[19] = zt * d;
         J[45] = w45 * d;
         J[46] = w46 * d;
@@ -7479,7 +7479,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w56 = J[65];
         T zt = z[15];
         T p = w15; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[15] = zt * d;
         J[49] = w22 * d;
         J[50] = w35 * d;
@@ -7493,7 +7493,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w52 = J[67];
         T zt = z[35];
         T p = w16; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[35] = zt * d;
         J[54] = w52 * d;
     }
@@ -7505,7 +7505,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w54 = J[70];
         T zt = z[54];
         T p = w17; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[54] = zt * d;
         J[55] = w43 * d;
         J[56] = w46 * d;
@@ -7526,7 +7526,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w46 -= w17 * J[56];
         w54 -= w17 * J[57];
         T p = w18; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[5] = zt * d;
         J[58] = w43 * d;
         J[59] = w44 * d;
@@ -7540,7 +7540,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w26 = J[77];
         T zt = z[0];
         T p = w19; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[0] = zt * d;
         J[63] = w26 * d;
     }
@@ -7550,7 +7550,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w55 = J[78];
         T zt = z[51];
         T p = w20; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[51] = zt * d;
         J[64] = w55 * d;
     }
@@ -7572,7 +7572,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w47 -= w14 * J[47];
         w50 -= w14 * J[48];
         T p = w21; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[25] = zt * d;
         J[65] = w37 * d;
         J[66] = w44 * d;
@@ -7592,7 +7592,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w56 = J[92];
         T zt = z[13];
         T p = w22; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[13] = zt * d;
         J[72] = w44 * d;
         J[73] = w45 * d;
@@ -7606,7 +7606,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w52 = J[94];
         T zt = z[34];
         T p = w23; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[34] = zt * d;
         J[77] = w52 * d;
     }
@@ -7616,7 +7616,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w26 = J[96];
         T zt = z[30];
         T p = w24; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[30] = zt * d;
         J[78] = w26 * d;
     }
@@ -7626,7 +7626,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w56 = J[98];
         T zt = z[24];
         T p = w25; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[24] = zt * d;
         J[79] = w56 * d;
     }
@@ -7636,7 +7636,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w54 = J[99];
         T zt = z[42];
         T p = w26; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[42] = zt * d;
         J[80] = w54 * d;
     }
@@ -7647,7 +7647,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w56 = J[102];
         T zt = z[9];
         T p = w27; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[9] = zt * d;
         J[81] = w50 * d;
         J[82] = w56 * d;
@@ -7695,7 +7695,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w47 -= w22 * J[75];
         w56 -= w22 * J[76];
         T p = w28; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[7] = zt * d;
         J[83] = w35 * d;
         J[84] = w37 * d;
@@ -7746,7 +7746,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w47 -= w22 * J[75];
         w56 -= w22 * J[76];
         T p = w29; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[4] = zt * d;
         J[97] = w43 * d;
         J[98] = w44 * d;
@@ -7764,7 +7764,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w52 = J[126];
         T zt = z[41];
         T p = w30; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[41] = zt * d;
         J[106] = w52 * d;
     }
@@ -7864,7 +7864,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w50 -= w27 * J[81];
         w56 -= w27 * J[82];
         T p = w31; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[22] = zt * d;
         J[107] = w33 * d;
         J[108] = w35 * d;
@@ -7890,7 +7890,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w53 = J[155];
         T zt = z[21];
         T p = w32; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[21] = zt * d;
         J[122] = w46 * d;
         J[123] = w52 * d;
@@ -7907,7 +7907,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         zt -= w26 * z[42];
         w54 -= w26 * J[80];
         T p = w33; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[1] = zt * d;
         J[125] = w49 * d;
         J[126] = w52 * d;
@@ -7923,7 +7923,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w52 = J[165];
         T zt = z[8];
         T p = w34; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[8] = zt * d;
         J[128] = w42 * d;
         J[129] = w47 * d;
@@ -7952,7 +7952,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w47 -= w22 * J[75];
         w56 -= w22 * J[76];
         T p = w35; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[14] = zt * d;
         J[133] = w37 * d;
         J[134] = w44 * d;
@@ -7981,7 +7981,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w52 -= w33 * J[126];
         w54 -= w33 * J[127];
         T p = w36; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[56] = zt * d;
         J[142] = w47 * d;
         J[143] = w49 * d;
@@ -8028,7 +8028,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w53 -= w35 * J[140];
         w56 -= w35 * J[141];
         T p = w37; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[18] = zt * d;
         J[146] = w42 * d;
         J[147] = w44 * d;
@@ -8050,7 +8050,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w53 = J[191];
         T zt = z[16];
         T p = w38; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[16] = zt * d;
         J[158] = w52 * d;
         J[159] = w53 * d;
@@ -8123,7 +8123,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w54 -= w37 * J[156];
         w56 -= w37 * J[157];
         T p = w39; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[23] = zt * d;
         J[160] = w42 * d;
         J[161] = w44 * d;
@@ -8157,7 +8157,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w51 -= w34 * J[131];
         w52 -= w34 * J[132];
         T p = w40; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[55] = zt * d;
         J[172] = w42 * d;
         J[173] = w47 * d;
@@ -8190,7 +8190,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w52 -= w36 * J[144];
         w54 -= w36 * J[145];
         T p = w41; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[28] = zt * d;
         J[179] = w47 * d;
         J[180] = w49 * d;
@@ -8241,7 +8241,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w55 -= w41 * J[184];
         w56 -= w41 * J[185];
         T p = w42; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[27] = zt * d;
         J[186] = w47 * d;
         J[187] = w49 * d;
@@ -8324,7 +8324,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w52 -= w32 * J[123];
         w53 -= w32 * J[124];
         T p = w43; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[20] = zt * d;
         J[194] = w44 * d;
         J[195] = w45 * d;
@@ -8430,7 +8430,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w55 -= w43 * J[203];
         w56 -= w43 * J[204];
         T p = w44; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[12] = zt * d;
         J[205] = w45 * d;
         J[206] = w46 * d;
@@ -8541,7 +8541,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w55 -= w44 * J[214];
         w56 -= w44 * J[215];
         T p = w45; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[2] = zt * d;
         J[216] = w46 * d;
         J[217] = w47 * d;
@@ -8615,7 +8615,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w55 -= w45 * J[224];
         w56 -= w45 * J[225];
         T p = w46; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[48] = zt * d;
         J[226] = w47 * d;
         J[227] = w49 * d;
@@ -8658,7 +8658,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w55 -= w42 * J[192];
         w56 -= w42 * J[193];
         T p = w47; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[45] = zt * d;
         J[235] = w49 * d;
         J[236] = w51 * d;
@@ -8673,7 +8673,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         T w48 = T(1.0);
         T zt = z[10];
         T p = w48; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[10] = zt * d;
     }
     NT_FENCE();
@@ -8782,7 +8782,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w55 -= w47 * J[240];
         w56 -= w47 * J[241];
         T p = w49; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[44] = zt * d;
         J[242] = w50 * d;
         J[243] = w51 * d;
@@ -8881,7 +8881,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w55 -= w49 * J[247];
         w56 -= w49 * J[248];
         T p = w50; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[53] = zt * d;
         J[249] = w51 * d;
         J[250] = w52 * d;
@@ -8947,7 +8947,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w55 -= w50 * J[253];
         w56 -= w50 * J[254];
         T p = w51; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[50] = zt * d;
         J[255] = w52 * d;
         J[256] = w53 * d;
@@ -9154,7 +9154,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w55 -= w51 * J[258];
         w56 -= w51 * J[259];
         T p = w52; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[43] = zt * d;
         J[260] = w53 * d;
         J[261] = w54 * d;
@@ -9238,7 +9238,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w55 -= w52 * J[262];
         w56 -= w52 * J[263];
         T p = w53; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[47] = zt * d;
         J[264] = w54 * d;
         J[265] = w55 * d;
@@ -9400,7 +9400,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w55 -= w53 * J[265];
         w56 -= w53 * J[266];
         T p = w54; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[46] = zt * d;
         J[267] = w55 * d;
         J[268] = w56 * d;
@@ -9479,7 +9479,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         w55 -= w54 * J[267];
         w56 -= w54 * J[268];
         T p = w55; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[49] = zt * d;
         J[269] = w56 * d;
     }
@@ -9654,7 +9654,7 @@ __device__ __forceinline__ void nt_factor_solve(PJ J, PZ z, T tiny) {
         zt -= w55 * z[49];
         w56 -= w55 * J[269];
         T p = w56; if (!(fabs(p) > tiny)) p = (p < T(0)) ? -tiny : tiny;
-        const T d = T(1) / p;
+        const T d = nt_rcp<T>(p);
         z[52] = zt * d;
     }
     NT_FENCE();

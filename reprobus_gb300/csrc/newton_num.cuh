@@ -131,6 +131,26 @@ __device__ __forceinline__ float nt_div<float>(float a, float b) {
 #endif
 }
 
+// Pivot reciprocals of the factorisation (|p| >= the pivot guard): FP64 as
+// nt_div(1, p); FP32 the hardware's approximate reciprocal (within 1 ulp,
+// no flush of a subnormal result).
+template <typename T>
+__device__ __forceinline__ T nt_rcp(T p);
+template <>
+__device__ __forceinline__ double nt_rcp<double>(double p) {
+    return nt_div<double>(1.0, p);
+}
+template <>
+__device__ __forceinline__ float nt_rcp<float>(float p) {
+#ifdef __CUDA_ARCH__
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(p));
+    return r;
+#else
+    return 1.0f / p;
+#endif
+}
+
 __device__ __forceinline__ double nt_widen(double z) { return z; }
 __device__ __forceinline__ double nt_widen(float z) {
     uint32_t f;
