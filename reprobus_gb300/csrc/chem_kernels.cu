@@ -371,8 +371,12 @@ __device__ __forceinline__ void cell_features(const Params& P, size_t g, double 
     f[63] = 0.f;
 }
 
+// Four 256-thread blocks per SM (64 registers, the cell's arrays on the
+// stack): the rate stage is FP64-pipe bound, and the extra warps keep that
+// pipe fed where two blocks at 128 registers left it idle a quarter of the
+// time.
 template <bool MIXED, int NTB = 128, bool LS = false>
-__global__ void __launch_bounds__(NTB) k_nt_setup(Params P) {
+__global__ void __launch_bounds__(NTB, 4) k_nt_setup(Params P) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const bool own = t < P.win_ncell;
     if (!LS && !own) return;
