@@ -39,10 +39,10 @@ BYTES_PER_CELL = 1008  # compulsory FP64 SoA traffic per cell-step: 63 reads + 6
 # (python -m oracle.count_ops --config cfg1 --rows 12).
 OPS_PER_CELL = 6793.08
 # DRAM bytes per cell-iteration of the mixed solve kernel, from one ncu capture
-# of the 394,560-cell grid (1.35 GB per launch at 3.79 iterations per cell):
+# of the 394,560-cell grid (1.35 GB per launch at 3.60 iterations per cell):
 # the cell records re-read from DRAM, proportional to the cell-iterations;
 # scaled to the benchmark launch
-SOLVE_DRAM_BYTES_PER_CELL_ITER = 899.0
+SOLVE_DRAM_BYTES_PER_CELL_ITER = 950.0
 # the accuracy leg: seeded columns of the grid (x 137 levels ~ 1.1e4 cells)
 # checked against the CPU FP64 oracle after the timed steps
 ACCURACY_COLUMNS = 80
@@ -582,7 +582,7 @@ def main():
             roof.update(kernel="k_nt_solve", kernel_ms=round(R["solve_ms"], 4), achieved=round(ach, 4),
                         frac=round(ach / peak64, 4), traffic=traffic,
                         traffic_ratio=(round(traffic / (BYTES_PER_CELL * ncell), 3) if traffic else None),
-                        traffic_note="DRAM bytes per launch: 899 B per cell-iteration from an ncu capture of the "
+                        traffic_note="DRAM bytes per launch: 950 B per cell-iteration from an ncu capture of the "
                                      "394,560-cell grid, times this launch's cell-iterations; ratio against the "
                                      "step's algorithmic 1,008 B per cell",
                         solver_ops={"fp64_ops_per_iteration": round(fp64_it, 1),
