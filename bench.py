@@ -52,8 +52,9 @@ STEP_TOL = 1e-4  # the Newton solvers' default step tolerance (both solvers alik
 
 def newton_ops():
     """Arithmetic operators (+ - * /) of one Newton iteration, counted in the
-    generated source (reprobus_gb300/csrc/newton_gen.cuh; an FMA counts 2):
-    residual (day, night), Jacobian (day, night), factorisation + solve."""
+    generated source (reprobus_gb300/csrc/newton_gen.cuh; an FMA counts 2, a
+    quotient nt_div or reciprocal nt_rcp one): residual (day, night), Jacobian
+    (day, night), factorisation + solve."""
     path = os.path.join(ROOT, "reprobus_gb300", "csrc", "newton_gen.cuh")
     src = open(path).read()
 
@@ -62,7 +63,7 @@ def newton_ops():
         j = src.index("\n}\n", i)
         lines = [ln.split("//")[0] for ln in src[i:j].splitlines()[1:]]
         text = "\n".join(lines)
-        return sum(text.count(op) for op in ("*", " + ", " - ", "/", "-=")) - text.count("J[") * 0
+        return sum(text.count(op) for op in ("*", " + ", " - ", "/", "-=", "nt_div<", "nt_rcp<"))
 
     return {"res_day": body("nt_residual_day"), "res_night": body("nt_residual_night"),
             "jac_day": body("nt_jacobian_day"), "jac_night": body("nt_jacobian_night"),
