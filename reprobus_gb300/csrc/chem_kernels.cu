@@ -371,12 +371,11 @@ __device__ __forceinline__ void cell_features(const Params& P, size_t g, double 
     f[63] = 0.f;
 }
 
-// Four 256-thread blocks per SM (64 registers, the cell's arrays on the
-// stack): the rate stage is FP64-pipe bound, and the extra warps keep that
-// pipe fed where two blocks at 128 registers left it idle a quarter of the
-// time.
+// 1024 threads per SM (64 registers, the cell's arrays on the stack): the
+// rate stage is FP64-pipe bound, and the extra warps keep that pipe fed where
+// two 256-thread blocks at 128 registers left it idle a quarter of the time.
 template <bool MIXED, int NTB = 128, bool LS = false>
-__global__ void __launch_bounds__(NTB, 4) k_nt_setup(Params P) {
+__global__ void __launch_bounds__(NTB, 1024 / NTB) k_nt_setup(Params P) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const bool own = t < P.win_ncell;
     if (!LS && !own) return;
@@ -1151,16 +1150,19 @@ static int ensure_newton(Handle* h) {
     return REPROBUS_OK;
 }
 
-// the rate-stage kernel of the Newton pipeline (and of REF5): blocks of 256
-// threads in lock-step (measured at cfg1: 36 -> 28 ms against 128-thread
-// blocks without barriers; 512 threads 30 ms)
+// blocks of the fused REF5 kernel k_chem (256 threads in lock-step)
 constexpr int SETUP_TB = 256;
+// the rate-stage kernel of the Newton pipeline (and of the split REF5): two
+// blocks of 512 threads per SM in lock-step. Measured at cfg1 (mixed step):
+// without the barriers 61.3 -> 64.7 ms; 128 / 256 / 512 / 1024 threads per
+// block at 64 registers: 63.1 / 61.3 / 60.4 / 63.9 ms
+constexpr int NT_SETUP_TB = 512;
 static void launch_setup(Handle* h, const Params& P, bool mixed) {
-    const unsigned nb = (unsigned)((P.win_ncell + SETUP_TB - 1) / SETUP_TB);
+    const unsigned nb = (unsigned)((P.win_ncell + NT_SETUP_TB - 1) / NT_SETUP_TB);
     if (mixed)
-        k_nt_setup<true, SETUP_TB, true><<<nb, SETUP_TB, 0, h->stream>>>(P);
+        k_nt_setup<true, NT_SETUP_TB, true><<<nb, NT_SETUP_TB, 0, h->stream>>>(P);
     else
-        k_nt_setup<false, SETUP_TB, true><<<nb, SETUP_TB, 0, h->stream>>>(P);
+        k_nt_setup<false, NT_SETUP_TB, true><<<nb, NT_SETUP_TB, 0, h->stream>>>(P);
 }
 
 // rate stage and plain start of the cells of P's row window; they join the
