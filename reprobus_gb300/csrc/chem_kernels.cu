@@ -512,12 +512,14 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
     static_assert(MODE == 0 || MODE == 3, "start modes");
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     int cell;
+    bool own = true;  // MODE 0: false for a thread past the window, which
+                      // passes the barriers on a valid cell and writes nothing
     if (MODE == 3) {
         if (t >= min(P.nt_head[3], P.mlp_cap)) return;
         cell = P.mlp_cells[t];
     } else {
-        if (t >= P.win_ncell) return;
-        cell = win_cell(P, t);
+        own = t < P.win_ncell;
+        cell = win_cell(P, own ? t : P.win_ncell - 1);
     }
     const double* r = P.nt_rec + (size_t)cell * NT_REC;
     const float* q = P.nt_rec32 + (size_t)cell * NT_REC32;
@@ -544,8 +546,14 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
 #pragma unroll
     for (int n = 0; n < NCM; n++) cc[n] = nt_cvt<float>(P.hc[g + pl * n] * hnm);
     const float dt = nt_cvt<float>(P.sc.dt);
+    // MODE 0: the block's warps run each pass between the same barriers, so
+    // that they fetch the same code at the same time
 #pragma unroll 1
-    for (int it = 0; it < P.npass_plain; it++) cell_pass(F, K, tj, het, ck0, dt, ck, cc);
+    for (int it = 0; it < P.npass_plain; it++) {
+        cell_pass(F, K, tj, het, ck0, dt, ck, cc);
+        if (MODE == 0) __syncthreads();
+    }
+    if (!own) return;
     bool finite = true;
 #pragma unroll
     for (int n = 0; n < NBCON - 1; n++) finite &= isfinite(ck[n]);

@@ -132,8 +132,9 @@ __device__ __forceinline__ float nt_div<float>(float a, float b) {
 }
 
 // Pivot reciprocals of the factorisation (|p| >= the pivot guard): FP64 as
-// nt_div(1, p); FP32 the hardware's approximate reciprocal (within 1 ulp,
-// no flush of a subnormal result).
+// nt_div(1, p); FP32 the hardware's approximate reciprocal, within 1 ulp
+// (a pivot beyond 2^126 would give 0 and fail its cell; the scaled pivots
+// are far below that).
 template <typename T>
 __device__ __forceinline__ T nt_rcp(T p);
 template <>
@@ -144,7 +145,7 @@ template <>
 __device__ __forceinline__ float nt_rcp<float>(float p) {
 #ifdef __CUDA_ARCH__
     float r;
-    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(p));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(p));
     return r;
 #else
     return 1.0f / p;
