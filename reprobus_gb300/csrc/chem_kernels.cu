@@ -512,14 +512,12 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
     static_assert(MODE == 0 || MODE == 3, "start modes");
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     int cell;
-    bool own = true;  // MODE 0: false for a thread past the window, which
-                      // passes the barriers on a valid cell and writes nothing
     if (MODE == 3) {
         if (t >= min(P.nt_head[3], P.mlp_cap)) return;
         cell = P.mlp_cells[t];
     } else {
-        own = t < P.win_ncell;
-        cell = win_cell(P, own ? t : P.win_ncell - 1);
+        if (t >= P.win_ncell) return;
+        cell = win_cell(P, t);
     }
     const double* r = P.nt_rec + (size_t)cell * NT_REC;
     const float* q = P.nt_rec32 + (size_t)cell * NT_REC32;
@@ -546,14 +544,8 @@ __global__ void __launch_bounds__(128) k_nt_start32(Params P) {
 #pragma unroll
     for (int n = 0; n < NCM; n++) cc[n] = nt_cvt<float>(P.hc[g + pl * n] * hnm);
     const float dt = nt_cvt<float>(P.sc.dt);
-    // MODE 0: the block's warps run each pass between the same barriers, so
-    // that they fetch the same code at the same time
 #pragma unroll 1
-    for (int it = 0; it < P.npass_plain; it++) {
-        cell_pass(F, K, tj, het, ck0, dt, ck, cc);
-        if (MODE == 0) __syncthreads();
-    }
-    if (!own) return;
+    for (int it = 0; it < P.npass_plain; it++) cell_pass(F, K, tj, het, ck0, dt, ck, cc);
     bool finite = true;
 #pragma unroll
     for (int n = 0; n < NBCON - 1; n++) finite &= isfinite(ck[n]);
@@ -628,8 +620,9 @@ __global__ void __launch_bounds__(128) k_nt_warm(Params P) {
 // arithmetic as k_chem, split so that each program is smaller for the
 // instruction cache
 __global__ void __launch_bounds__(128) k_ref_passes(Params P) {
-    const int cell = blockIdx.x * blockDim.x + threadIdx.x;
-    if (cell >= P.ncell) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool own = t < P.ncell;  // else: the passes on a valid cell, between the barriers, and no write
+    const int cell = own ? t : P.ncell - 1;
     const double* r = P.nt_rec + (size_t)cell * NT_REC;
     CellPro C;
     C.g = cell_global(P, cell);
@@ -651,8 +644,14 @@ __global__ void __launch_bounds__(128) k_ref_passes(Params P) {
     for (int n = 0; n < NBCON; n++) ck[n] = C.ck0[n] = r[NT_RCK0 + n];
 #pragma unroll
     for (int n = 0; n < NCM; n++) cc[n] = P.hc[C.g + pl * n] * F.hnm;
+    // the block's warps run each pass between the same barriers (REF5 at cfg1
+    // 40.5 -> 39.2 ms; the same in the Newton starts measured no gain)
 #pragma unroll 1
-    for (int it = 0; it < P.niter; it++) cell_pass(F, C.K, C.tj, C.A.het, C.ck0, P.sc.dt, ck, cc);
+    for (int it = 0; it < P.niter; it++) {
+        cell_pass(F, C.K, C.tj, C.A.het, C.ck0, P.sc.dt, ck, cc);
+        __syncthreads();
+    }
+    if (!own) return;
     cell_epilogue(P, C, ck, cc);
 }
 
