@@ -387,32 +387,38 @@ __global__ void __launch_bounds__(NTB, 1024 / NTB) k_nt_setup(Params P) {
     const double fx[14] = {F.o2, F.n2, F.h2, F.co2, F.hnm, F.parthno3, F.parth2o, F.parthcl, F.parthbr,
                            F.rain_hno3, F.rain_hcl, F.rain_hbr, F.rain_h2o2, P.sc.dt};
     double* r = P.nt_rec + (size_t)cell * NT_REC;
+    // MIXED: the FP32 copies beside the FP64 fields, each value read once
+    // from the cell's arrays; by integer operations (nt_cvt: truncated, below
+    // 2^-126 zero), not conversion instructions, which issue on the FP64 pipe
+    float* q = MIXED ? P.nt_rec32 + (size_t)cell * NT_REC32 : nullptr;
 #pragma unroll 4
-    for (int n = 0; n < NRATE; n++) r[NT_RK + n] = C.K[n];
+    for (int n = 0; n < NRATE; n++) {
+        const double v = C.K[n];
+        r[NT_RK + n] = v;
+        if (MIXED) q[NT_RK + n] = nt_cvt<float>(v);
+    }
 #pragma unroll 4
-    for (int n = 0; n < NPHOT; n++) r[NT_RJ + n] = C.tj[n];
+    for (int n = 0; n < NPHOT; n++) {
+        const double v = C.tj[n];
+        r[NT_RJ + n] = v;
+        if (MIXED) q[NT_RJ + n] = nt_cvt<float>(v);
+    }
 #pragma unroll
-    for (int n = 0; n < 9; n++) r[NT_RH + n] = C.A.het[n];
+    for (int n = 0; n < 9; n++) {
+        const double v = C.A.het[n];
+        r[NT_RH + n] = v;
+        if (MIXED) q[NT_RH + n] = nt_cvt<float>(v);
+    }
 #pragma unroll
-    for (int n = 0; n < 14; n++) r[NT_RF + n] = fx[n];
+    for (int n = 0; n < 14; n++) {
+        r[NT_RF + n] = fx[n];
+        if (MIXED) q[NT_RF + n] = nt_cvt<float>(fx[n]);
+    }
     r[NT_RSZA] = F.sza;
+    if (MIXED) q[NT_RSZA] = nt_cvt<float>(F.sza);
     r[NT_RSURF] = C.A.surf;
 #pragma unroll 4
     for (int n = 0; n < NBCON; n++) r[NT_RCK0 + n] = C.ck0[n];
-    if (MIXED) {
-        // FP32 copies by integer operations (nt_cvt: truncated, below 2^-126
-        // zero), not conversion instructions, which issue on the FP64 pipe
-        float* q = P.nt_rec32 + (size_t)cell * NT_REC32;
-#pragma unroll 4
-        for (int n = 0; n < NRATE; n++) q[NT_RK + n] = nt_cvt<float>(C.K[n]);
-#pragma unroll 4
-        for (int n = 0; n < NPHOT; n++) q[NT_RJ + n] = nt_cvt<float>(C.tj[n]);
-#pragma unroll
-        for (int n = 0; n < 9; n++) q[NT_RH + n] = nt_cvt<float>(C.A.het[n]);
-#pragma unroll
-        for (int n = 0; n < 14; n++) q[NT_RF + n] = nt_cvt<float>(fx[n]);
-        q[NT_RSZA] = nt_cvt<float>(F.sza);
-    }
 }
 
 // a cell into the work queue: day cells from the front of the list, night
