@@ -85,6 +85,16 @@ def test_generated_header_is_current(tmp_path):
     assert out.read_text() == open(GEN).read(), "rerun python -m reprobus_gb300.codegen.gen_newton"
 
 
+def test_generated_quotients_go_through_nt_div():
+    """Every quotient of the generated equations is an nt_div and every pivot
+    reciprocal an nt_rcp (newton_num.cuh): no IEEE division sequence is left
+    in the solve kernels' code."""
+    code = "\n".join(line.split("//")[0] for line in open(GEN).read().splitlines())
+    assert "/" not in code
+    assert code.count("nt_rcp<T>(p)") == 57 * code.count("void nt_factor_solve(")
+    assert code.count("nt_div<T>(") > 0
+
+
 def test_residual_vanishes_at_the_reference_fixed_point(host, data):
     c, dg, fp, stat, _ = data
     worst = 0.0
